@@ -1,0 +1,391 @@
+"""Ray-cast benchmark of the GB300 path: extend (closest-hit) + shadow (any-hit).
+
+Workload (the ray-cast kernel bench): seeded fBm terrain of 1024 x 1024 cells
+(2,097,152 FP32 triangles, 6 octaves, amplitude 0.1) plus 64 icospheres
+(subdivision 4, 5,120 triangles each) = 2,424,832 triangles, kd-trees built by
+the reference builder's algorithm; 16,777,216 closest-hit rays with origins
+uniform in the scene box and directions uniform on the sphere, and
+16,777,216 shadow rays with tmax = U[0,1] x |scene diagonal|.
+
+One step = one extend launch over the 16M rays + one shadow launch over the
+16M shadow rays.  metric = Mrays/s over both ray kinds.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+Under torchrun every rank runs the same workload on its own GPU (replicas,
+weak scaling, no data-path collective); value = all ranks' rays / max time.
+"""
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))  # the checker: CPU-baseline leg only
+
+METRIC = "Mrays/s (closest-hit + any-hit, ray-cast kernel bench)"
+UNIT = "Mrays/s"
+GRID, SPHERES, LEVEL = 1024, 64, 4
+N_RAYS = 16 * 1024 * 1024
+SEED = 1
+
+
+def parse():
+    p = argparse.ArgumentParser()
+    p.add_argument("--gpus", type=int, default=1)
+    p.add_argument("--steps", type=int, default=5)
+    p.add_argument("--warmup", type=int, default=3)
+    p.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    p.add_argument("--rays", type=int, default=N_RAYS)
+    p.add_argument("--grid", type=int, default=GRID)
+    p.add_argument("--no-cpu-baseline", action="store_true")
+    return p.parse_args()
+
+
+def dist_setup(args):
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    pg = None
+    if world > 1:
+        import torch.distributed as dist
+        backend = "nccl" if args.impl == "gb300" else "gloo"
+        dist.init_process_group(backend=backend)
+        pg = dist
+    return rank, world, local, pg
+
+
+def workload(grid):
+    from yar_gb300 import scenes
+    t0 = time.time()
+    s = scenes.raycast_scene(seed=SEED, grid=grid, spheres=SPHERES, level=LEVEL, build=False)
+    t1 = time.time()
+    s.build_kdtrees()
+    t2 = time.time()
+    return s, {"generate_s": round(t1 - t0, 3), "kdtree_build_s": round(t2 - t1, 3)}
+
+
+def rays_for(s, n):
+    from yar_gb300 import scenes
+    lo, hi = scenes.scene_box(s)
+    return scenes.random_rays(lo, hi, n, SEED + 100), scenes.random_shadow_rays(lo, hi, n, SEED + 200)
+
+
+# ------------------------------------------------------------------ clocks
+class ClockSampler:
+    """nvidia-smi sampling during the timed region (SM clock and throttle reasons)."""
+
+    FIELDS = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+              "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+              "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, device):
+        self.device = device
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.device), "--query-gpu=" + self.FIELDS,
+                                          "--format=csv,noheader,nounits", "-lms", "100"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(name)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ algorithmic bytes
+def algorithmic_bytes(s, rays, shadow, sample=65536):
+    """Per-ray bytes of the traversal in the reference's visit order, counted by
+    the oracle on a sample of the same batches:
+      closest: 32 (ray) + 20 (hit) + 8*nodes + 4*leaf index words + 48*triangles + 96*object visits
+      any:     32 (ray) + 1 (bit)  + the same traversal terms
+    (48 B per triangle = 12 B indices + 36 B vertices; 96 B per object record)."""
+    import oracle
+    idx = np.linspace(0, rays.shape[0] - 1, sample).astype(np.int64)
+    _, _, _, _, st = oracle.cast_closest(s, rays[idx], with_stats=True)
+    _, st2 = oracle.cast_any(s, shadow[idx], with_stats=True)
+    w = np.array([8, 4, 48, 96], np.float64)
+    closest = 52.0 + (st.astype(np.float64) @ w).mean()
+    anyhit = 33.0 + (st2.astype(np.float64) @ w).mean()
+    return closest, anyhit, st.mean(0).tolist(), st2.mean(0).tolist()
+
+
+def profile_traffic():
+    """DRAM bytes per extend launch from the committed ncu summary, if any."""
+    path = os.path.join(ROOT, "profiles", "extend_raycast_c2.md")
+    if not os.path.exists(path):
+        return None
+    for ln in open(path):
+        if ln.startswith("traffic_bytes_per_launch:"):
+            try:
+                return float(ln.split(":", 1)[1].strip())
+            except ValueError:
+                return None
+    return None
+
+
+# ------------------------------------------------------------------ CPU baselines
+def reference_cast_rate(s, rays, shadow, n_sample, threads):
+    """The reference's KdTree::intersect / intersect_any (oracle/_ref) on host cores."""
+    import oracle
+    idx = slice(0, n_sample)
+    (_, info_c) = oracle.ref_cast(s, rays[idx], threads=threads)
+    (_, info_a) = oracle.ref_cast(s, shadow[idx], any_hit=True, threads=threads)
+    seconds = info_c["seconds"] + info_a["seconds"]
+    return 2 * n_sample / seconds / 1e6, seconds
+
+
+def port_cast_rate(s, rays, shadow, n_sample):
+    import oracle
+    idx = slice(0, n_sample)
+    t0 = time.perf_counter()
+    oracle.cast_closest(s, rays[idx])
+    oracle.cast_any(s, shadow[idx])
+    seconds = time.perf_counter() - t0
+    return 2 * n_sample / seconds / 1e6, seconds
+
+
+def cpu_baseline(s, rays, shadow):
+    import oracle
+    threads = os.cpu_count() or 1
+    if oracle.have_reference():
+        n = min(rays.shape[0], 1 << 21)
+        rate, sec = reference_cast_rate(s, rays, shadow, n, threads)
+        return {"value": round(rate, 3), "unit": UNIT, "cores": threads, "kind": "reference",
+                "sample": "%d closest + %d any-hit rays of the same batches, reference KdTree::intersect/"
+                          "intersect_any on %d threads, %.2f s" % (n, n, threads, sec)}
+    n = min(rays.shape[0], 1 << 18)
+    rate, sec = port_cast_rate(s, rays, shadow, n)
+    return {"value": round(rate, 3), "unit": UNIT, "cores": 1, "kind": "port",
+            "sample": "%d closest + %d any-hit rays of the same batches, oracle C port, 1 thread, %.2f s"
+                      % (n, n, sec)}
+
+
+# ------------------------------------------------------------------ arms
+def run_reference(args, rank, world, pg):
+    if rank != 0:
+        return
+    s, setup = workload(args.grid)
+    rays, shadow = rays_for(s, args.rays)
+    import oracle
+    threads = os.cpu_count() or 1
+    have_ref = oracle.have_reference()
+    n = min(args.rays, (1 << 21) if have_ref else (1 << 18))
+    for _ in range(args.warmup):
+        if have_ref:
+            reference_cast_rate(s, rays, shadow, min(n, 1 << 16), threads)
+        else:
+            port_cast_rate(s, rays, shadow, min(n, 1 << 12))
+    rates, secs = [], []
+    for _ in range(args.steps):
+        if have_ref:
+            r, sec = reference_cast_rate(s, rays, shadow, n, threads)
+        else:
+            r, sec = port_cast_rate(s, rays, shadow, n)
+        rates.append(r)
+        secs.append(sec)
+    value = statistics.median(rates)
+    kind = "reference" if have_ref else "port"
+    cores = threads if have_ref else 1
+    line = {"metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": round(1000 * statistics.median(secs), 3),
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded fBm terrain + icospheres, seed %d)" % SEED,
+            "config": {"workload": "raycast C2: %d tris, %d closest + %d any-hit rays; each step a sample of %d+%d"
+                                   % (s.triangle_count, args.rays, args.rays, n, n),
+                       "triangles": s.triangle_count, "rays": args.rays},
+            "impl": "reference",
+            "cpu_baseline": {"value": round(value, 3), "unit": UNIT, "cores": cores, "kind": kind,
+                             "sample": "%d closest + %d any-hit rays per step on %d host threads" % (n, n, cores)},
+            "e2e": {"value": round(value, 3), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_gb300(args, rank, world, local, pg):
+    import torch
+    from yar_gb300 import native
+    torch.cuda.set_device(local)
+    s, setup = workload(args.grid)
+    rays, shadow = rays_for(s, args.rays)
+    n = args.rays
+    ctx = native.Context(local, max_batch_rays=n)
+    ctx.upload_scene(s)
+
+    dev = torch.device("cuda", local)
+    d_rays = torch.from_numpy(rays).to(dev)
+    d_shadow = torch.from_numpy(shadow).to(dev)
+    d_t = torch.empty(n, dtype=torch.float32, device=dev)
+    d_prim = torch.empty(n, dtype=torch.int32, device=dev)
+    d_obj = torch.empty(n, dtype=torch.int32, device=dev)
+    d_bary = torch.empty((n, 2), dtype=torch.float32, device=dev)
+    d_occ = torch.empty(n, dtype=torch.uint8, device=dev)
+    torch.cuda.synchronize()
+
+    def step(times=None):
+        ms1 = ctx.cast_closest_device(d_rays.data_ptr(), n, d_t.data_ptr(), d_prim.data_ptr(), d_obj.data_ptr(),
+                                      d_bary.data_ptr(), timed=True)
+        ms2 = ctx.cast_any_device(d_shadow.data_ptr(), n, d_occ.data_ptr(), timed=True)
+        if times is not None:
+            times.append((ms1, ms2))
+
+    def barrier():
+        if pg is not None:
+            pg.barrier()
+        torch.cuda.synchronize()
+
+    for _ in range(args.warmup):
+        step()
+    kernel_times = []
+    barrier()
+    with ClockSampler(local) as clocks:
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            step(kernel_times)
+        torch.cuda.synchronize()
+        elapsed = time.perf_counter() - t0
+    barrier()
+    if pg is not None:
+        tt = torch.tensor([elapsed], dtype=torch.float64, device=dev)
+        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
+        elapsed = float(tt.item())
+    ms_per_step = 1000 * elapsed / args.steps
+    value = world * 2 * n * args.steps / elapsed / 1e6
+
+    # end to end: the C ABI with pinned host buffers, copies inside the timed region
+    h_rays = torch.from_numpy(rays).pin_memory()
+    h_shadow = torch.from_numpy(shadow).pin_memory()
+    h_t = torch.empty(n, dtype=torch.float32).pin_memory()
+    h_prim = torch.empty(n, dtype=torch.int32).pin_memory()
+    h_obj = torch.empty(n, dtype=torch.int32).pin_memory()
+    h_bary = torch.empty((n, 2), dtype=torch.float32).pin_memory()
+    h_occ = torch.empty(n, dtype=torch.uint8).pin_memory()
+    hits = native.HitSoa(h_t.data_ptr(), h_prim.data_ptr(), h_obj.data_ptr(), h_bary.data_ptr())
+    import ctypes as C
+
+    def e2e_step():
+        rc = native.lib().yar_gpu_cast_closest(ctx._h, h_rays.data_ptr(), n, C.byref(hits), native.YAR_BUFFERS_HOST)
+        ctx._check(rc, "cast_closest")
+        rc = native.lib().yar_gpu_cast_any(ctx._h, h_shadow.data_ptr(), n, h_occ.data_ptr(), native.YAR_BUFFERS_HOST)
+        ctx._check(rc, "cast_any")
+
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        e2e_step()
+    torch.cuda.synchronize()
+    e2e_elapsed = time.perf_counter() - t0
+    barrier()
+    e2e_value = world * 2 * n * args.steps / e2e_elapsed / 1e6
+    h2d = 2 * n * 32
+    d2h = n * (4 + 4 + 4 + 8) + n
+
+    # correctness spot check of the timed outputs against the host-buffer path
+    same = bool(np.array_equal(d_prim[:4096].cpu().numpy().view(np.uint32), h_prim[:4096].numpy().view(np.uint32))
+                and np.array_equal(d_occ[:4096].cpu().numpy(), h_occ[:4096].numpy()))
+
+    if rank != 0:
+        return
+    ext_ms = statistics.median([a for a, b in kernel_times])
+    shd_ms = statistics.median([b for a, b in kernel_times])
+    bpr_closest, bpr_any, st_c, st_a = algorithmic_bytes(s, rays, shadow)
+    peaks = {}
+    try:
+        peaks = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json")))
+    except (OSError, ValueError):
+        pass
+    peak = peaks.get("hbm_gbs", 6800.0)
+    peak_src = "measured" if "hbm_gbs" in peaks else "fallback"
+    achieved = bpr_closest * n / (ext_ms * 1e-3) / 1e9
+    traffic = profile_traffic()
+    line = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": round(ms_per_step, 3), "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f32",
+        "data": "synthetic (seeded fBm terrain + icospheres, seed %d)" % SEED,
+        "config": {"workload": "raycast C2: %d tris (1024^2 fBm terrain + 64 icospheres L4), %d closest + %d "
+                               "any-hit rays per step" % (s.triangle_count, n, n),
+                   "triangles": s.triangle_count, "rays": n, "l2": "inputs larger than L2 (rays 512 MiB per kind)",
+                   "replicas": world},
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": 2 * args.steps,
+        "kernels": {"extend_ms": round(ext_ms, 3), "shadow_ms": round(shd_ms, 3),
+                    "extend_mrays_s": round(n / ext_ms / 1e3, 1), "shadow_mrays_s": round(n / shd_ms / 1e3, 1)},
+        "roofline": {"bound": "hbm", "achieved": round(achieved, 1), "peak": peak, "unit": "GB/s",
+                     "frac": round(achieved / peak, 4), "peak_source": peak_src,
+                     "traffic": traffic, "kernel": "extend",
+                     "algorithmic_bytes_per_ray": round(bpr_closest, 1),
+                     "any_hit_bytes_per_ray": round(bpr_any, 1),
+                     "mean_per_ray_closest": dict(zip(["nodes", "leaf_words", "triangles", "objects"],
+                                                      [round(x, 2) for x in st_c])),
+                     "mean_per_ray_any": dict(zip(["nodes", "leaf_words", "triangles", "objects"],
+                                                  [round(x, 2) for x in st_a]))},
+        "clocks": clocks.summary(),
+        "setup": setup,
+        "outputs_consistent": same,
+    }
+    if not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(s, rays, shadow)
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def main():
+    args = parse()
+    rank, world, local, pg = dist_setup(args)
+    try:
+        if args.impl == "reference":
+            run_reference(args, rank, world, pg)
+        else:
+            run_gb300(args, rank, world, local, pg)
+    finally:
+        if pg is not None:
+            pg.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

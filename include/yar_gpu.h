@@ -1,0 +1,274 @@
+/*
+ * yar_gpu.h - C ABI of the GB300 (sm_103a) path-tracing hot path.
+ *
+ * This is the drop-in boundary for the CPU reference renderer of
+ * kennyalive/YAR.  The reference has no C ABI: its seams are C++ functions,
+ * and every entry point below names the function it replaces:
+ *
+ *   yar_gpu_cast_closest  <- bool KdTree::intersect(const Ray&, Intersection&) const
+ *                            src/ref/kdtree.h:116, src/ref/kdtree.cpp:219-327
+ *   yar_gpu_cast_any      <- bool KdTree::intersect_any(const Ray&, float tmax) const
+ *                            src/ref/kdtree.h:117, src/ref/kdtree.cpp:329-439
+ *   yar_gpu_upload_scene  <- init_scene_context(Scene_Context&, const Scene&, ...)
+ *                            src/ref/reference_renderer.h:48-53 (the device-side part:
+ *                            kd-trees, meshes, objects, materials, lights, camera)
+ *   yar_gpu_render        <- Image render_scene(const Scene_Context&, double* variance,
+ *                            float* render_time)  src/ref/reference_renderer.h:55
+ *   yar_build_mesh_kdtree <- KdTree build_triangle_mesh_kdtree(const Triangle_Mesh_Geometry_Data*)
+ *                            src/ref/kdtree_builder.h:6, src/ref/kdtree_builder.cpp:425-441
+ *   yar_build_scene_kdtree<- KdTree build_scene_kdtree(const Scene_Geometry_Data*)
+ *                            src/ref/kdtree_builder.h:10, src/ref/kdtree_builder.cpp:443-463
+ *
+ * Conventions
+ *   - Plain pointers and sizes only.  Every function returns a status code
+ *     (YAR_OK == 0, negative on error) and never exits the process; the
+ *     reference calls exit(1) from error() (src/lib/common.cpp:10-28).
+ *   - Matrices are 3x4 row-major floats, the layout of Matrix3x4::a[3][4]
+ *     (src/lib/matrix.h:7-20).
+ *   - kd-tree nodes are the reference's 8-byte KdNode words (src/ref/kdtree.h:18-77),
+ *     bit for bit: interior word0 = axis | above_child << 2, word1 = split bits;
+ *     leaf word0 = 3 | count << 2, word1.. = sorted primitive indices.
+ *   - Enumerations reuse the reference's numeric values: Material_Type
+ *     (src/lib/material.h:6-21) and Light_Type (src/lib/light.h:7-17).
+ *   - A context owns one CUDA stream and its device memory.  A context is not
+ *     thread-safe; separate contexts are independent.
+ */
+#ifndef YAR_GPU_H
+#define YAR_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define YAR_GPU_ABI_VERSION 1
+
+/* status codes */
+#define YAR_OK                 0
+#define YAR_ERR_INVALID       -1  /* bad argument or malformed scene */
+#define YAR_ERR_NOMEM         -2  /* device or host allocation failed */
+#define YAR_ERR_CAPACITY      -3  /* a fixed capacity (stack depth, queue) was exceeded */
+#define YAR_ERR_TIMEOUT       -4  /* a bounded device wait gave up */
+#define YAR_ERR_CUDA          -5  /* CUDA runtime error (see yar_gpu_last_error) */
+#define YAR_ERR_UNSUPPORTED   -6  /* scene feature outside the implemented path */
+#define YAR_ERR_IO            -7  /* file read/write failure */
+#define YAR_ERR_NO_SCENE      -8  /* no scene uploaded */
+
+/* buffer residency flags for the ray-cast entry points */
+#define YAR_BUFFERS_HOST    0   /* pointers are host memory; copies happen inside the call */
+#define YAR_BUFFERS_DEVICE  1   /* pointers are device memory of the context's device */
+
+/* Material_Type values (src/lib/material.h:6-21) */
+#define YAR_MATERIAL_PERFECT_REFLECTOR 0
+#define YAR_MATERIAL_PERFECT_REFRACTOR 1
+#define YAR_MATERIAL_DIFFUSE           2
+#define YAR_MATERIAL_DIFFUSE_TRANSMISSION 3
+#define YAR_MATERIAL_METAL             4
+#define YAR_MATERIAL_PLASTIC           5
+#define YAR_MATERIAL_COATED_DIFFUSE    6
+#define YAR_MATERIAL_GLASS             7
+#define YAR_MATERIAL_NULL              0xffffffffu
+
+/* Light_Type values (src/lib/light.h:7-17) */
+#define YAR_LIGHT_DIFFUSE_RECTANGULAR  3
+#define YAR_LIGHT_NULL                 0xffffffffu
+
+/* Visibility (src/lib/triangle_mesh.h:7-11) */
+#define YAR_VISIBLE            0
+#define YAR_VISIBLE_NO_SHADOWS 1
+#define YAR_INVISIBLE          2
+
+typedef struct yar_gpu_ctx yar_gpu_ctx;
+
+/* KdNode, src/ref/kdtree.h:18-77 */
+typedef struct yar_kd_node {
+    uint32_t word0;
+    uint32_t word1;
+} yar_kd_node;
+
+/* KdTree::bounds + KdTree::nodes, src/ref/kdtree.h:119-126 */
+typedef struct yar_kdtree_view {
+    float bounds_min[3];
+    float bounds_max[3];
+    const yar_kd_node* nodes;
+    uint32_t node_count;
+} yar_kdtree_view;
+
+/* Triangle_Mesh, src/lib/triangle_mesh.h:13-131 */
+typedef struct yar_mesh_desc {
+    const float* vertices;      /* float3 x vertex_count */
+    const float* normals;       /* float3 x vertex_count, or NULL */
+    const float* uvs;           /* float2 x vertex_count, or NULL */
+    const int32_t* indices;     /* int3 x triangle_count */
+    uint32_t vertex_count;
+    uint32_t triangle_count;
+    int32_t reverse_geometric_normal_orientation;
+    int32_t visibility;         /* YAR_VISIBLE, ... */
+    yar_kdtree_view kdtree;     /* per-mesh tree (object space) */
+} yar_mesh_desc;
+
+/* Scene_Object, src/lib/scene_object.h:8-25 */
+typedef struct yar_object_desc {
+    int32_t mesh_index;
+    uint32_t material_type;     /* YAR_MATERIAL_* (YAR_MATERIAL_NULL for lights) */
+    int32_t material_index;     /* index into yar_flat_scene::materials */
+    uint32_t area_light_type;   /* YAR_LIGHT_* */
+    int32_t area_light_index;
+    float object_to_world[12];
+    float world_to_object[12];
+    float object_to_world_normal[12];
+} yar_object_desc;
+
+/* Constant-parameter materials (Diffuse/Metal/Glass_Material, src/lib/material.h:58-150).
+ * Textured parameters are outside the implemented path (YAR_ERR_UNSUPPORTED). */
+typedef struct yar_material_desc {
+    uint32_t type;              /* YAR_MATERIAL_DIFFUSE / METAL / GLASS */
+    float reflectance[3];       /* diffuse: reflectance; glass: reflectance (kr) */
+    float transmittance[3];     /* glass: transmittance (kt) */
+    float eta[3];               /* metal */
+    float k[3];                 /* metal */
+    float eta_i;                /* metal: IOR of the adjacent dielectric */
+    float u_roughness;          /* metal u roughness; glass roughness */
+    float v_roughness;          /* metal */
+    float index_of_refraction;  /* glass */
+    int32_t roughness_is_alpha;
+} yar_material_desc;
+
+/* Diffuse_Rectangular_Light, src/lib/light.h:66-73 */
+typedef struct yar_rect_light_desc {
+    float light_to_world[12];
+    float emitted_radiance[3];
+    float size[2];
+    int32_t sample_count;
+} yar_rect_light_desc;
+
+/* Camera, src/ref/camera.h:35-49 (fields as computed by Camera::Camera, camera.cpp:5-14) */
+typedef struct yar_camera_desc {
+    float camera_to_world[12];
+    float image_extent[2];
+    float horz_half_dist;
+    float vert_half_dist;
+    int32_t z_is_up;
+} yar_camera_desc;
+
+/* Raytracer_Config (src/lib/raytracer_config.h:5-49) plus the Scene_Context
+ * fields the render loop reads (render_region, rng_seed_offset, pbrt3_scene). */
+typedef struct yar_render_config {
+    int32_t render_region[4];       /* x0, y0, x1, y1 (x1/y1 exclusive) */
+    int32_t rendering_algorithm;    /* 0 direct lighting, 1 path tracer */
+    int32_t max_light_bounces;
+    float russian_roulette_threshold;
+    int32_t russian_roulette_bounce_count_threshold;
+    int32_t pixel_filter_type;      /* 0 box, 1 gaussian, 2 triangle */
+    float pixel_filter_radius;
+    float pixel_filter_alpha;
+    int32_t x_pixel_sample_count;
+    int32_t y_pixel_sample_count;
+    float film_radiance_scale;
+    float max_rgb_component_value_of_film_sample;
+    int32_t pbrt3_scene;            /* roughness remap: 1 pbrt3 polynomial, 0 alpha = r^2 */
+    int32_t rng_seed_offset;
+} yar_render_config;
+
+typedef struct yar_flat_scene {
+    uint32_t mesh_count;
+    const yar_mesh_desc* meshes;
+    uint32_t object_count;
+    const yar_object_desc* objects;
+    yar_kdtree_view scene_kdtree;   /* over objects (world space) */
+    uint32_t material_count;
+    const yar_material_desc* materials;
+    uint32_t rect_light_count;
+    const yar_rect_light_desc* rect_lights;
+    /* lights of other kinds (point, spot, directional, sphere, mesh, environment):
+       counted for total_light_count; rendering with any of them is unsupported */
+    uint32_t other_light_count;
+    yar_camera_desc camera;
+    yar_render_config config;
+} yar_flat_scene;
+
+/* One ray of a batch: 32 bytes, two float4.  tmax plays the role of the
+ * initial Intersection::t (src/ref/intersection.h:17-19) for closest hit and
+ * of ray_tmax for any hit. */
+typedef struct yar_ray {
+    float origin[3];
+    float tmax;
+    float direction[3];
+    float pad;
+} yar_ray;
+
+/* Closest-hit results, structure of arrays; any pointer may be NULL.
+ * t = Intersection::t (tmax when there is no hit), prim = triangle index
+ * within its mesh (0xffffffff when no hit), object = Scene_Object index,
+ * bary = barycentrics y,z (x = 1 - y - z is not stored). */
+typedef struct yar_hit_soa {
+    float* t;
+    uint32_t* prim;
+    uint32_t* object;
+    float* bary;        /* float2 per ray */
+} yar_hit_soa;
+
+typedef struct yar_gpu_options {
+    int32_t device;                 /* CUDA device ordinal */
+    uint32_t max_batch_rays;        /* capacity of the host-buffer staging area (0 = 16M) */
+} yar_gpu_options;
+
+typedef struct yar_render_stats {
+    double variance;            /* render_scene's variance_estimate */
+    float seconds;              /* render_scene's render_time */
+    uint64_t paths;             /* camera paths traced */
+    uint64_t rays_closest;      /* closest-hit rays (camera, continuation and MIS probe) */
+    uint64_t rays_any;          /* any-hit shadow rays */
+    uint32_t kernel_launches;
+} yar_render_stats;
+
+/* ---- context ---- */
+int yar_gpu_create(yar_gpu_ctx** out, const yar_gpu_options* options);
+void yar_gpu_destroy(yar_gpu_ctx* ctx);
+const char* yar_gpu_last_error(const yar_gpu_ctx* ctx);
+/* CUDA stream (cudaStream_t) the context launches on */
+void* yar_gpu_stream(yar_gpu_ctx* ctx);
+int yar_gpu_synchronize(yar_gpu_ctx* ctx);
+
+/* ---- scene ---- */
+int yar_gpu_upload_scene(yar_gpu_ctx* ctx, const yar_flat_scene* scene);
+
+/* ---- ray casts (KdTree::intersect / intersect_any over the scene tree) ---- */
+int yar_gpu_cast_closest(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t ray_count,
+                         const yar_hit_soa* hits, int32_t buffers);
+int yar_gpu_cast_any(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t ray_count,
+                     uint8_t* occluded, int32_t buffers);
+/* Same casts with per-kernel device time (CUDA events on the context stream,
+ * milliseconds) written to *kernel_ms; buffers must be device memory. */
+int yar_gpu_cast_closest_timed(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t ray_count,
+                               const yar_hit_soa* hits, float* kernel_ms);
+int yar_gpu_cast_any_timed(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t ray_count,
+                           uint8_t* occluded, float* kernel_ms);
+
+/* ---- render (render_scene) ----
+ * rgb_out: host float3 image of render_region size (FP32 film resolve).
+ * stats may be NULL. */
+int yar_gpu_render(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats);
+
+/* ---- host-side kd-tree builders (the reference's builder, same node stream) ----
+ * The returned node array is owned by the library; release it with yar_free_nodes. */
+int yar_build_mesh_kdtree(const float* vertices, uint32_t vertex_count,
+                          const int32_t* indices, uint32_t triangle_count,
+                          int32_t thread_count,
+                          float bounds_out[6], yar_kd_node** nodes_out, uint32_t* node_count_out);
+int yar_build_scene_kdtree(const float* object_bounds /* 6 floats per object, world space */,
+                           uint32_t object_count,
+                           float bounds_out[6], yar_kd_node** nodes_out, uint32_t* node_count_out);
+void yar_free_nodes(yar_kd_node* nodes);
+
+/* transform_bounding_box (src/lib/matrix.cpp:391-402) of a tree's bounds, for
+ * the scene-tree primitive bounds (src/ref/kdtree_builder.cpp:445-452) */
+void yar_transform_bounds(const float object_to_world[12], const float bounds_in[6], float bounds_out[6]);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* YAR_GPU_H */

@@ -1,0 +1,577 @@
+// ref_harness.cpp - test infrastructure: drives the reference renderer's own
+// code (compiled by oracle/build_ref.sh into oracle/_ref/libyarref.a) so the
+// oracle restatement and the GPU path can be pinned against it.
+//
+// It is also the reference-side adapter of the C ABI: flatten() converts a
+// reference Scene + Scene_Context into the flat scene (include/yar_gpu.h) that
+// yar_gpu_upload_scene consumes.
+//
+// commands
+//   flatten  <scene.pbrt> <out.yfs> [--spp=N] [--seedoffset=S]
+//       load_scene (src/lib/scene_loader.cpp:74-133) + init_scene_context
+//       (src/ref/reference_renderer.cpp:586-621, reference kd-tree builder)
+//       and write the flat scene.
+//   render   <scene.pbrt> <out.img> [--spp=N] [--seedoffset=S] [--threads=T]
+//       render_scene (src/ref/reference_renderer.cpp:479-584); writes
+//       u32 w, u32 h, f64 variance, f32 seconds, f32 rgb[w*h*3].
+//   build    <in.yfs> <out.yfs> [--threads=T]
+//       build_triangle_mesh_kdtree / build_scene_kdtree
+//       (src/ref/kdtree_builder.cpp:425-463) for the meshes and objects of a
+//       flat scene; prints the build time.
+//   cast     <in.yfs> <rays.bin> <out.bin> [--threads=T] [--any] [--repeat=R]
+//       KdTree::intersect / intersect_any (src/ref/kdtree.cpp:219-439) over
+//       the scene tree for a batch of yar_ray records; closest writes
+//       f32 t[n], u32 prim[n], u32 obj[n], f32 bary[2n]; any writes u8[n].
+//       Prints {"rays":..,"seconds":..,"threads":..} on stdout.
+#include "std.h"
+#include "lib/common.h"
+#include "lib/scene.h"
+#include "lib/scene_loader.h"
+#include "lib/scene_object.h"
+#include "lib/triangle_mesh.h"
+#include "ref/camera.h"
+#include "ref/intersection.h"
+#include "ref/kdtree.h"
+#include "ref/kdtree_builder.h"
+#include "ref/reference_renderer.h"
+#include "ref/sampling.h"
+#include "lib/math.h"
+#include "lib/random.h"
+#include "ref/scene_context.h"
+
+#include "yfs.hpp"
+
+#include <cstdio>
+#include <cstdlib>
+#include <cstring>
+#include <string>
+#include <thread>
+#include <vector>
+
+namespace {
+
+struct Args {
+    std::vector<std::string> pos;
+    int spp = 0;
+    int seed_offset = 0;
+    int threads = 0;
+    bool any = false;
+    int repeat = 1;
+};
+
+Args parse(int argc, char** argv) {
+    Args a;
+    for (int i = 2; i < argc; i++) {
+        std::string s = argv[i];
+        if (s.rfind("--spp=", 0) == 0) a.spp = atoi(s.c_str() + 6);
+        else if (s.rfind("--seedoffset=", 0) == 0) a.seed_offset = atoi(s.c_str() + 13);
+        else if (s.rfind("--threads=", 0) == 0) a.threads = atoi(s.c_str() + 10);
+        else if (s.rfind("--repeat=", 0) == 0) a.repeat = atoi(s.c_str() + 9);
+        else if (s == "--any") a.any = true;
+        else a.pos.push_back(s);
+    }
+    if (a.threads <= 0) a.threads = std::max(1u, std::thread::hardware_concurrency());
+    return a;
+}
+
+void matrix_to_floats(const Matrix3x4& m, float out[12]) {
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 4; c++) out[r * 4 + c] = m.a[r][c];
+}
+
+Matrix3x4 floats_to_matrix(const float in[12]) {
+    Matrix3x4 m;
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 4; c++) m.a[r][c] = in[r * 4 + c];
+    return m;
+}
+
+bool constant_rgb(const Parameter& p, float out[3]) {
+    if (p.eval_mode != EvaluationMode::value || !p.value.is_constant) return false;
+    out[0] = p.value.constant.r;
+    out[1] = p.value.constant.g;
+    out[2] = p.value.constant.b;
+    return true;
+}
+
+bool constant_float(const Parameter& p, float* out) {
+    float c[3];
+    if (!constant_rgb(p, c)) return false;
+    *out = c[0];
+    return true;
+}
+
+Scene load_with_overrides(const Args& a) {
+    Scene scene = load_scene(a.pos[0]);
+    if (a.spp > 0) {
+        int k = (int)std::ceil(std::sqrt(a.spp));  // src/ref/main.cpp:386-390
+        scene.raytracer_config.x_pixel_sample_count = k;
+        scene.raytracer_config.y_pixel_sample_count = k;
+    }
+    return scene;
+}
+
+void init_context(Scene_Context& ctx, const Scene& scene, const Args& a) {
+    // the kd-tree cache goes to a private directory, rebuilt every time
+    std::string data_dir = (fs::temp_directory_path() / ("yar_ref_data_" + std::to_string(getpid()))).string();
+    fs::create_directories(data_dir);
+    set_data_directory(data_dir);
+    Reference_Renderer_Config config;
+    config.thread_count = a.threads;
+    config.rebuild_kdtree_cache = true;
+    config.rng_seed_offset = a.seed_offset;
+    init_scene_context(ctx, scene, config);
+    std::error_code ec;
+    fs::remove_all(data_dir, ec);
+}
+
+// The C-ABI adapter: reference Scene/Scene_Context -> flat scene.
+yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
+    yfs::Scene out;
+    const auto& meshes = scene.geometries.triangle_meshes;
+    for (size_t i = 0; i < meshes.size(); i++) {
+        const Triangle_Mesh& m = meshes[i];
+        yfs::Mesh fm;
+        fm.vertices.resize(m.vertices.size() * 3);
+        memcpy(fm.vertices.data(), m.vertices.data(), fm.vertices.size() * 4);
+        fm.normals.resize(m.normals.size() * 3);
+        if (!m.normals.empty()) memcpy(fm.normals.data(), m.normals.data(), fm.normals.size() * 4);
+        fm.uvs.resize(m.uvs.size() * 2);
+        if (!m.uvs.empty()) memcpy(fm.uvs.data(), m.uvs.data(), fm.uvs.size() * 4);
+        fm.indices = m.indices;
+        fm.reverse_orientation = m.reverse_geometric_normal_orientation ? 1 : 0;
+        fm.visibility = (int32_t)m.visibility;
+        if (m.alpha_texture_index >= 0) fprintf(stderr, "warning: mesh %zu has an alpha texture (not flattened)\n", i);
+        const KdTree& t = ctx.kdtree_data.geometry_kdtrees[i];
+        memcpy(fm.bounds, &t.bounds.min_p.x, 12);
+        memcpy(fm.bounds + 3, &t.bounds.max_p.x, 12);
+        fm.nodes.resize(t.nodes.size());
+        memcpy(fm.nodes.data(), t.nodes.data(), t.nodes.size() * 8);
+        out.meshes.push_back(std::move(fm));
+    }
+    // materials: diffuse, metal, glass flattened in that order
+    std::vector<int> diffuse_index, metal_index, glass_index;
+    for (const Diffuse_Material& m : ctx.materials.diffuse) {
+        yar_material_desc d{};
+        d.type = YAR_MATERIAL_DIFFUSE;
+        if (!constant_rgb(m.reflectance, d.reflectance)) fprintf(stderr, "warning: textured diffuse reflectance\n");
+        diffuse_index.push_back((int)out.materials.size());
+        out.materials.push_back(d);
+    }
+    for (const Metal_Material& m : ctx.materials.metal) {
+        yar_material_desc d{};
+        d.type = YAR_MATERIAL_METAL;
+        constant_float(m.u_roughness, &d.u_roughness);
+        constant_float(m.v_roughness, &d.v_roughness);
+        constant_float(m.eta_i, &d.eta_i);
+        constant_rgb(m.eta, d.eta);
+        constant_rgb(m.k, d.k);
+        d.roughness_is_alpha = m.roughness_is_alpha ? 1 : 0;
+        metal_index.push_back((int)out.materials.size());
+        out.materials.push_back(d);
+    }
+    for (const Glass_Material& m : ctx.materials.glass) {
+        yar_material_desc d{};
+        d.type = YAR_MATERIAL_GLASS;
+        constant_rgb(m.reflectance, d.reflectance);
+        constant_rgb(m.transmittance, d.transmittance);
+        constant_float(m.index_of_refraction, &d.index_of_refraction);
+        constant_float(m.roughness, &d.u_roughness);
+        d.v_roughness = d.u_roughness;
+        d.roughness_is_alpha = m.roughness_is_alpha ? 1 : 0;
+        glass_index.push_back((int)out.materials.size());
+        out.materials.push_back(d);
+    }
+    for (const Scene_Object& o : scene.objects) {
+        yar_object_desc d{};
+        d.mesh_index = o.geometry.index;
+        d.material_type = (uint32_t)o.material.type;
+        d.material_index = -1;
+        if (o.material.type == Material_Type::diffuse) d.material_index = diffuse_index[o.material.index];
+        else if (o.material.type == Material_Type::metal) d.material_index = metal_index[o.material.index];
+        else if (o.material.type == Material_Type::glass) d.material_index = glass_index[o.material.index];
+        else if (o.material.type != Material_Type::null_material)
+            fprintf(stderr, "warning: material type %u not flattened\n", (unsigned)o.material.type);
+        d.area_light_type = (uint32_t)o.area_light.type;
+        d.area_light_index = o.area_light.index;
+        matrix_to_floats(o.object_to_world_transform, d.object_to_world);
+        matrix_to_floats(o.world_to_object_transform, d.world_to_object);
+        matrix_to_floats(o.object_to_world_normal_transform, d.object_to_world_normal);
+        out.objects.push_back(d);
+    }
+    const KdTree& st = ctx.kdtree_data.scene_kdtree;
+    memcpy(out.scene_bounds, &st.bounds.min_p.x, 12);
+    memcpy(out.scene_bounds + 3, &st.bounds.max_p.x, 12);
+    out.scene_nodes.resize(st.nodes.size());
+    memcpy(out.scene_nodes.data(), st.nodes.data(), st.nodes.size() * 8);
+
+    for (const Diffuse_Rectangular_Light& l : ctx.lights.diffuse_rectangular_lights) {
+        yar_rect_light_desc d{};
+        matrix_to_floats(l.light_to_world_transform, d.light_to_world);
+        d.emitted_radiance[0] = l.emitted_radiance.r;
+        d.emitted_radiance[1] = l.emitted_radiance.g;
+        d.emitted_radiance[2] = l.emitted_radiance.b;
+        d.size[0] = l.size.x;
+        d.size[1] = l.size.y;
+        d.sample_count = l.sample_count;
+        out.rect_lights.push_back(d);
+    }
+    out.other_light_count = (uint32_t)(ctx.lights.total_light_count - (int)ctx.lights.diffuse_rectangular_lights.size());
+
+    // Camera fields exactly as Camera::Camera computes them (src/ref/camera.cpp:5-14).
+    const Matrix3x4& pose = scene.view_points[0];
+    matrix_to_floats(pose, out.camera.camera_to_world);
+    Vector2 extent = Vector2(scene.film_resolution);
+    out.camera.image_extent[0] = extent.x;
+    out.camera.image_extent[1] = extent.y;
+    float tan_fovy_over_2 = std::tan(radians(scene.camera_fov_y / 2.f));
+    out.camera.vert_half_dist = tan_fovy_over_2;
+    out.camera.horz_half_dist = (extent.x / extent.y) * tan_fovy_over_2;
+    out.camera.z_is_up = scene.z_is_up ? 1 : 0;
+
+    const Raytracer_Config& rc = ctx.raytracer_config;
+    yar_render_config& c = out.config;
+    c.render_region[0] = ctx.render_region.p0.x;
+    c.render_region[1] = ctx.render_region.p0.y;
+    c.render_region[2] = ctx.render_region.p1.x;
+    c.render_region[3] = ctx.render_region.p1.y;
+    c.rendering_algorithm = (int32_t)rc.rendering_algorithm;
+    c.max_light_bounces = rc.max_light_bounces;
+    c.russian_roulette_threshold = rc.russian_roulette_threshold;
+    c.russian_roulette_bounce_count_threshold = rc.russian_roulette_bounce_count_threshold;
+    c.pixel_filter_type = (int32_t)rc.pixel_filter_type;
+    c.pixel_filter_radius = rc.pixel_filter_radius;
+    c.pixel_filter_alpha = rc.pixel_filter_alpha;
+    c.x_pixel_sample_count = rc.x_pixel_sample_count;
+    c.y_pixel_sample_count = rc.y_pixel_sample_count;
+    c.film_radiance_scale = rc.film_radiance_scale;
+    c.max_rgb_component_value_of_film_sample = rc.max_rgb_component_value_of_film_sample;
+    c.pbrt3_scene = ctx.pbrt3_scene ? 1 : 0;
+    c.rng_seed_offset = ctx.rng_seed_offset;
+    return out;
+}
+
+// Reference objects reconstructed from a flat scene (for build and cast).
+struct Ref_Scene {
+    std::vector<Triangle_Mesh> meshes;
+    std::vector<Triangle_Mesh_Geometry_Data> geometry_data;
+    std::vector<KdTree> kdtrees;
+    std::vector<Scene_Object> objects;
+    Scene_Geometry_Data scene_data;
+    KdTree scene_kdtree;
+};
+
+void load_ref_meshes(const yfs::Scene& fs_scene, Ref_Scene& rs) {
+    rs.meshes.resize(fs_scene.meshes.size());
+    for (size_t i = 0; i < fs_scene.meshes.size(); i++) {
+        const yfs::Mesh& fm = fs_scene.meshes[i];
+        Triangle_Mesh& m = rs.meshes[i];
+        m.vertices.resize(fm.vertices.size() / 3);
+        memcpy(m.vertices.data(), fm.vertices.data(), fm.vertices.size() * 4);
+        m.normals.resize(fm.normals.size() / 3);
+        if (!fm.normals.empty()) memcpy(m.normals.data(), fm.normals.data(), fm.normals.size() * 4);
+        m.uvs.resize(fm.uvs.size() / 2);
+        if (!fm.uvs.empty()) memcpy(m.uvs.data(), fm.uvs.data(), fm.uvs.size() * 4);
+        m.indices = fm.indices;
+        m.reverse_geometric_normal_orientation = fm.reverse_orientation != 0;
+        m.visibility = (Visibility)fm.visibility;
+    }
+    rs.geometry_data.resize(rs.meshes.size());
+    for (size_t i = 0; i < rs.meshes.size(); i++) {
+        rs.geometry_data[i].mesh = &rs.meshes[i];
+        if (rs.meshes[i].visibility == Visibility::invisible) {
+            rs.geometry_data[i].ignore_intersector = true;
+            rs.geometry_data[i].ignore_any_intersector = true;
+        } else if (rs.meshes[i].visibility == Visibility::visible_no_shadows) {
+            rs.geometry_data[i].ignore_any_intersector = true;
+        }
+    }
+    rs.objects.resize(fs_scene.objects.size());
+    for (size_t i = 0; i < fs_scene.objects.size(); i++) {
+        const yar_object_desc& d = fs_scene.objects[i];
+        Scene_Object& o = rs.objects[i];
+        o.geometry = {Geometry_Type::triangle_mesh, d.mesh_index};
+        o.material = {(Material_Type)d.material_type, d.material_index};
+        o.area_light = {(Light_Type)d.area_light_type, d.area_light_index};
+        o.object_to_world_transform = floats_to_matrix(d.object_to_world);
+        o.world_to_object_transform = floats_to_matrix(d.world_to_object);
+        o.object_to_world_normal_transform = floats_to_matrix(d.object_to_world_normal);
+    }
+}
+
+void attach_scene(Ref_Scene& rs) {
+    rs.scene_data.scene_objects = &rs.objects;
+    rs.scene_data.kdtrees = &rs.kdtrees;
+    rs.scene_data.geometry_type_offsets.fill(0);
+}
+
+int cmd_flatten(const Args& a) {
+    if (a.pos.size() < 2) return 2;
+    Scene scene = load_with_overrides(a);
+    Scene_Context ctx;
+    init_context(ctx, scene, a);
+    yfs::Scene out = flatten(scene, ctx);
+    if (!yfs::write(a.pos[1], out)) { fprintf(stderr, "write failed\n"); return 1; }
+    return 0;
+}
+
+int cmd_render(const Args& a) {
+    if (a.pos.size() < 2) return 2;
+    Scene scene = load_with_overrides(a);
+    Scene_Context ctx;
+    init_context(ctx, scene, a);
+    double variance = 0.0;
+    float seconds = 0.f;
+    Image image = render_scene(ctx, &variance, &seconds);
+    FILE* f = fopen(a.pos[1].c_str(), "wb");
+    if (!f) return 1;
+    uint32_t w = (uint32_t)image.width, h = (uint32_t)image.height;
+    fwrite(&w, 4, 1, f);
+    fwrite(&h, 4, 1, f);
+    fwrite(&variance, 8, 1, f);
+    fwrite(&seconds, 4, 1, f);
+    fwrite(image.data.data(), sizeof(ColorRGB), image.data.size(), f);
+    fclose(f);
+    printf("{\"render_seconds\": %.6f, \"variance\": %.9g, \"threads\": %d, \"spp\": %d, \"width\": %u, \"height\": %u}\n",
+           seconds, variance, a.threads, ctx.pixel_sampler_config.get_samples_per_pixel(), w, h);
+    return 0;
+}
+
+int cmd_build(const Args& a) {
+    if (a.pos.size() < 2) return 2;
+    yfs::Scene fs_scene;
+    std::string err;
+    if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
+    Ref_Scene rs;
+    load_ref_meshes(fs_scene, rs);
+    Timestamp t;
+    rs.kdtrees.resize(rs.meshes.size());
+    std::atomic_int counter{0};
+    auto worker = [&] {
+        int i = counter.fetch_add(1);
+        while (i < (int)rs.meshes.size()) {
+            rs.kdtrees[i] = build_triangle_mesh_kdtree(&rs.geometry_data[i]);
+            i = counter.fetch_add(1);
+        }
+    };
+    {
+        std::vector<std::jthread> threads;
+        for (int i = 1; i < std::min<int>(a.threads, (int)rs.meshes.size()); i++) threads.emplace_back(worker);
+        worker();
+    }
+    float mesh_seconds = elapsed_seconds(t);
+    attach_scene(rs);
+    Timestamp t2;
+    rs.scene_kdtree = build_scene_kdtree(&rs.scene_data);
+    float scene_seconds = elapsed_seconds(t2);
+    for (size_t i = 0; i < rs.meshes.size(); i++) {
+        yfs::Mesh& fm = fs_scene.meshes[i];
+        const KdTree& kt = rs.kdtrees[i];
+        memcpy(fm.bounds, &kt.bounds.min_p.x, 12);
+        memcpy(fm.bounds + 3, &kt.bounds.max_p.x, 12);
+        fm.nodes.resize(kt.nodes.size());
+        memcpy(fm.nodes.data(), kt.nodes.data(), kt.nodes.size() * 8);
+    }
+    memcpy(fs_scene.scene_bounds, &rs.scene_kdtree.bounds.min_p.x, 12);
+    memcpy(fs_scene.scene_bounds + 3, &rs.scene_kdtree.bounds.max_p.x, 12);
+    fs_scene.scene_nodes.resize(rs.scene_kdtree.nodes.size());
+    memcpy(fs_scene.scene_nodes.data(), rs.scene_kdtree.nodes.data(), rs.scene_kdtree.nodes.size() * 8);
+    if (!yfs::write(a.pos[1], fs_scene)) return 1;
+    printf("{\"mesh_build_seconds\": %.3f, \"scene_build_seconds\": %.3f, \"threads\": %d}\n",
+           mesh_seconds, scene_seconds, a.threads);
+    return 0;
+}
+
+int cmd_cast(const Args& a) {
+    if (a.pos.size() < 3) return 2;
+    yfs::Scene fs_scene;
+    std::string err;
+    if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
+    Ref_Scene rs;
+    load_ref_meshes(fs_scene, rs);
+    rs.kdtrees.resize(rs.meshes.size());
+    for (size_t i = 0; i < rs.meshes.size(); i++) {
+        KdTree& kt = rs.kdtrees[i];
+        const yfs::Mesh& fm = fs_scene.meshes[i];
+        kt.bounds = Bounding_Box(Vector3(fm.bounds), Vector3(fm.bounds + 3));
+        kt.nodes.resize(fm.nodes.size());
+        memcpy(kt.nodes.data(), fm.nodes.data(), fm.nodes.size() * 8);
+        kt.set_geometry_data(&rs.geometry_data[i]);
+    }
+    attach_scene(rs);
+    rs.scene_kdtree.bounds = Bounding_Box(Vector3(fs_scene.scene_bounds), Vector3(fs_scene.scene_bounds + 3));
+    rs.scene_kdtree.nodes.resize(fs_scene.scene_nodes.size());
+    memcpy(rs.scene_kdtree.nodes.data(), fs_scene.scene_nodes.data(), fs_scene.scene_nodes.size() * 8);
+    rs.scene_kdtree.set_geometry_data(&rs.scene_data);
+
+    std::vector<uint8_t> raw;
+    {
+        FILE* f = fopen(a.pos[1].c_str(), "rb");
+        if (!f) return 1;
+        fseek(f, 0, SEEK_END);
+        long size = ftell(f);
+        fseek(f, 0, SEEK_SET);
+        raw.resize((size_t)size);
+        if (fread(raw.data(), 1, raw.size(), f) != raw.size()) { fclose(f); return 1; }
+        fclose(f);
+    }
+    const size_t n = raw.size() / sizeof(yar_ray);
+    const yar_ray* rays = (const yar_ray*)raw.data();
+    std::vector<float> t(n), bary(2 * n);
+    std::vector<uint32_t> prim(n), obj(n);
+    std::vector<uint8_t> occluded(n);
+
+    std::atomic<size_t> next{0};
+    const size_t chunk = 4096;
+    auto worker = [&] {
+        initialize_fp_state();
+        for (;;) {
+            size_t begin = next.fetch_add(chunk);
+            if (begin >= n) break;
+            size_t end = std::min(n, begin + chunk);
+            for (size_t i = begin; i < end; i++) {
+                Ray ray{Vector3(rays[i].origin), Vector3(rays[i].direction)};
+                if (a.any) {
+                    occluded[i] = rs.scene_kdtree.intersect_any(ray, rays[i].tmax) ? 1 : 0;
+                } else {
+                    Intersection isect;
+                    isect.t = rays[i].tmax;
+                    if (rs.scene_kdtree.intersect(ray, isect)) {
+                        t[i] = isect.t;
+                        prim[i] = isect.triangle_intersection.triangle_index;
+                        obj[i] = (uint32_t)(isect.scene_object - rs.objects.data());
+                        bary[2 * i] = isect.triangle_intersection.barycentrics.y;
+                        bary[2 * i + 1] = isect.triangle_intersection.barycentrics.z;
+                    } else {
+                        t[i] = rays[i].tmax;
+                        prim[i] = 0xffffffffu;
+                        obj[i] = 0xffffffffu;
+                        bary[2 * i] = 0.f;
+                        bary[2 * i + 1] = 0.f;
+                    }
+                }
+            }
+        }
+    };
+    double best = 1e30;
+    for (int r = 0; r < std::max(1, a.repeat); r++) {
+        next = 0;
+        Timestamp ts;
+        {
+            std::vector<std::jthread> threads;
+            for (int i = 1; i < a.threads; i++) threads.emplace_back(worker);
+            worker();
+        }
+        best = std::min(best, (double)elapsed_nanoseconds(ts) / 1e9);
+    }
+    FILE* f = fopen(a.pos[2].c_str(), "wb");
+    if (!f) return 1;
+    if (a.any) {
+        fwrite(occluded.data(), 1, n, f);
+    } else {
+        fwrite(t.data(), 4, n, f);
+        fwrite(prim.data(), 4, n, f);
+        fwrite(obj.data(), 4, n, f);
+        fwrite(bary.data(), 4, 2 * n, f);
+    }
+    fclose(f);
+    printf("{\"rays\": %zu, \"seconds\": %.6f, \"threads\": %d, \"kind\": \"%s\"}\n", n, best, a.threads,
+           a.any ? "any" : "closest");
+    return 0;
+}
+
+// regress <mesh.yfs> <out.bin> <ray_count>
+// The ray stream of validate_triangle_mesh_kdtree (src/ref/test_kdtree.cpp:20-83,
+// :138-194) against a single-mesh flat scene: 25% of the rays restart from the
+// previous hit point, axis-aligned directions with probability 1/32 per axis.
+// Checks kd-tree t == brute-force t like the reference test and writes
+// f32 origin[3], f32 direction[3], f32 t, u32 prim per ray.
+int cmd_regress(const Args& a) {
+    if (a.pos.size() < 3) return 2;
+    yfs::Scene fs_scene;
+    std::string err;
+    if (!yfs::read(a.pos[0], fs_scene, &err) || fs_scene.meshes.empty()) return 1;
+    Ref_Scene rs;
+    load_ref_meshes(fs_scene, rs);
+    Triangle_Mesh_Geometry_Data& gd = rs.geometry_data[0];
+    KdTree kdtree = build_triangle_mesh_kdtree(&gd);
+    const int count = atoi(a.pos[2].c_str());
+
+    RNG rng;
+    Vector3 diagonal = kdtree.bounds.max_p - kdtree.bounds.min_p;
+    float delta = 2.0f * diagonal.length();
+    Bounding_Box ray_bounds(kdtree.bounds.min_p - Vector3(delta), kdtree.bounds.max_p + Vector3(delta));
+    Vector3 last_hit_position = (kdtree.bounds.min_p + kdtree.bounds.max_p) * 0.5f;
+    Vector3 last_hit_normal = Vector3(1, 0, 0);
+    FILE* f = fopen(a.pos[1].c_str(), "wb");
+    if (!f) return 1;
+    int mismatches = 0;
+    for (int i = 0; i < count; i++) {
+        Vector3 origin, direction;
+        if (rng.get_float() < 0.25f) {
+            origin = last_hit_position;
+            direction = sample_hemisphere_uniform(rng.get_vector2());
+            Vector3 axis_a, axis_b;
+            coordinate_system_from_vector(last_hit_normal, &axis_a, &axis_b);
+            Matrix3x4 m = Matrix3x4::identity;
+            m.set_column(0, axis_a);
+            m.set_column(1, axis_b);
+            m.set_column(2, last_hit_normal);
+            direction = transform_vector(m, direction);
+        } else {
+            auto range = [&rng](float lo, float hi) { return lo + (hi - lo) * rng.get_float(); };
+            origin.x = range(ray_bounds.min_p.x, ray_bounds.max_p.x);
+            origin.y = range(ray_bounds.min_p.y, ray_bounds.max_p.y);
+            origin.z = range(ray_bounds.min_p.z, ray_bounds.max_p.z);
+            direction = sample_sphere_uniform(rng.get_vector2());
+            if (rng.get_float() < 1.0f / 32.0f && direction.z != 0.0) direction.x = direction.y = 0.0;
+            else if (rng.get_float() < 1.0f / 32.0f && direction.y != 0.0) direction.x = direction.z = 0.0;
+            else if (rng.get_float() < 1.0f / 32.0f && direction.x != 0.0) direction.y = direction.z = 0.0;
+            direction = direction.normalized();
+        }
+        Ray ray{origin, direction};
+        Intersection isect;
+        kdtree.intersect(ray, isect);
+        Intersection brute;
+        const Triangle_Mesh& mesh = rs.meshes[0];
+        for (int k = 0; k < mesh.get_triangle_count(); k++) kdtree.intersector(ray, kdtree.geometry_data, k, brute);
+        if (isect.t != brute.t) mismatches++;
+        uint32_t prim = isect.t != Infinity ? isect.triangle_intersection.triangle_index : 0xffffffffu;
+        fwrite(&origin.x, 4, 3, f);
+        fwrite(&direction.x, 4, 3, f);
+        fwrite(&isect.t, 4, 1, f);
+        fwrite(&prim, 4, 1, f);
+        if (isect.t != Infinity) {
+            const Triangle_Intersection& ti = isect.triangle_intersection;
+            Vector3 hit_pos = ti.mesh->get_position(ti.triangle_index, ti.barycentrics);
+            Vector3 p[3];
+            ti.mesh->get_positions(ti.triangle_index, p);
+            Vector3 ng = cross(p[1] - p[0], p[2] - p[0]).normalized();
+            ng = dot(ng, -ray.direction) < 0 ? -ng : ng;
+            last_hit_position = offset_ray_origin(hit_pos, ng);
+            last_hit_normal = ng;
+        }
+    }
+    fclose(f);
+    printf("{\"rays\": %d, \"kdtree_vs_brute_force_mismatches\": %d}\n", count, mismatches);
+    return 0;
+}
+
+} // namespace
+
+int main(int argc, char** argv) {
+    if (argc < 2) {
+        fprintf(stderr, "usage: yar_ref flatten|render|build|cast ...\n");
+        return 2;
+    }
+    Args a = parse(argc, argv);
+    std::string cmd = argv[1];
+    int rc = 2;
+    if (cmd == "flatten") rc = cmd_flatten(a);
+    else if (cmd == "render") rc = cmd_render(a);
+    else if (cmd == "build") rc = cmd_build(a);
+    else if (cmd == "cast") rc = cmd_cast(a);
+    else if (cmd == "regress") rc = cmd_regress(a);
+    if (rc == 2) fprintf(stderr, "bad arguments for %s\n", cmd.c_str());
+    return rc;
+}

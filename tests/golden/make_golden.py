@@ -1,0 +1,136 @@
+"""Generates the golden fixtures in tests/golden/ by running the reference
+renderer itself (oracle/_ref/yar_ref, built from the reference sources by
+oracle/build_ref.sh).  Run from the repository root:
+
+    python tests/golden/make_golden.py
+
+Fixtures
+  raycast_small.yfs / .npz   small terrain + icosphere scene, kd-trees built by
+                             the reference builder; 4096 closest-hit rays with
+                             the reference's (t, prim, object, bary) and 4096
+                             shadow rays with its occlusion bits.
+  transform_small.yfs / .npz objects under rotation + non-uniform scale +
+                             translation (two-level transform path), same rays.
+  kdtree_regression.npz      the two hand-built meshes of the reference's
+                             kd-tree FP-regression test (src/ref/test_kdtree.cpp
+                             :196-246, parsed from that file), their reference
+                             kd-trees, and 4096 rays of the test's own ray
+                             stream (:20-83) with the reference's t and triangle.
+  cornell_c1_64.yfs / .npz   the Cornell box flattened by the reference loader
+                             and builder at 64x64, 16 spp, maxdepth 8, seed 1,
+                             and the reference's FP32 render of it.
+"""
+import os
+import re
+import sys
+import tempfile
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
+sys.path.insert(0, ROOT)
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+
+import oracle  # noqa: E402
+from yar_gb300 import scenes  # noqa: E402
+from yar_gb300.scene import FlatScene, Mesh, make_object  # noqa: E402
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REFERENCE = "/root/reference"
+
+
+def rays_and_results(flat, seed, n=4096):
+    lo, hi = scenes.scene_box(flat)
+    pad = 0.25 * (hi - lo)
+    rays = scenes.random_rays(lo - pad, hi + pad, n, seed)
+    # a slice of axis-aligned directions and rays starting on split planes
+    rays[: n // 16, 4:7] = 0.0
+    rays[: n // 16, 4 + (np.arange(n // 16) % 3)] = np.where(np.arange(n // 16) % 2 == 0, 1.0, -1.0)
+    shadow = scenes.random_shadow_rays(lo, hi, n, seed + 1)
+    (t, prim, obj, bary), _ = oracle.ref_cast(flat, rays)
+    occ, _ = oracle.ref_cast(flat, shadow, any_hit=True)
+    return dict(rays=rays, t=t, prim=prim, obj=obj, bary=bary, shadow_rays=shadow, occluded=occ)
+
+
+def raycast_small():
+    flat = scenes.raycast_scene(seed=3, grid=24, spheres=6, level=2, build=False)
+    flat, _ = oracle.ref_build(flat)
+    flat.write(os.path.join(HERE, "raycast_small.yfs"))
+    np.savez_compressed(os.path.join(HERE, "raycast_small.npz"), **rays_and_results(flat, 11))
+
+
+def transform_small():
+    rng = np.random.default_rng(5)
+    flat = FlatScene()
+    sv, si = scenes.icosphere(1.0, 2)
+    bv = np.array([[-1, -1, -1], [1, -1, -1], [1, 1, -1], [-1, 1, -1], [-1, -1, 1], [1, -1, 1], [1, 1, 1], [-1, 1, 1]],
+                  np.float32)
+    bi = np.array([[0, 1, 2], [2, 3, 0], [0, 1, 5], [5, 4, 0], [1, 2, 6], [6, 5, 1], [2, 3, 7], [7, 6, 2],
+                   [3, 0, 4], [4, 7, 3], [4, 5, 6], [6, 7, 4]], np.int32)
+    flat.meshes = [Mesh(sv, si), Mesh(bv, bi)]
+    objects = []
+    for k in range(12):
+        a, b = rng.uniform(0, 2 * np.pi, 2)
+        ca, sa, cb, sb = np.cos(a), np.sin(a), np.cos(b), np.sin(b)
+        rot = np.array([[ca, -sa, 0], [sa, ca, 0], [0, 0, 1]]) @ np.array([[1, 0, 0], [0, cb, -sb], [0, sb, cb]])
+        m = np.zeros((3, 4))
+        m[:, :3] = rot @ np.diag(rng.uniform(0.2, 0.7, 3))
+        m[:, 3] = rng.uniform(-2, 2, 3)
+        objects.append(make_object(k % 2, m.astype(np.float32).reshape(12)))
+    flat.objects = np.array(objects)
+    flat, _ = oracle.ref_build(flat)
+    flat.write(os.path.join(HERE, "transform_small.yfs"))
+    np.savez_compressed(os.path.join(HERE, "transform_small.npz"), **rays_and_results(flat, 21))
+
+
+def parse_regression_meshes():
+    text = open(os.path.join(REFERENCE, "src/ref/test_kdtree.cpp"), encoding="latin-1").read()
+    body = text[text.index("create_custom_meshes()"):]
+    meshes = []
+    for block in re.findall(r"mesh\.vertices = \{(.*?)\};\s*mesh\.indices = \{(.*?)\};", body, re.S)[:2]:
+        nums = [float(x.rstrip("f")) for x in re.findall(r"-?\d+\.\d+f?", block[0])]
+        idx = [int(x) for x in re.findall(r"\d+", block[1])]
+        meshes.append((np.array(nums, np.float32).reshape(-1, 3), np.array(idx, np.int32).reshape(-1, 3)))
+    return meshes
+
+
+def kdtree_regression(n=4096):
+    out = {}
+    for k, (v, i) in enumerate(parse_regression_meshes()):
+        flat = FlatScene()
+        flat.meshes = [Mesh(v, i)]
+        flat.objects = np.array([make_object(0)])
+        flat, _ = oracle.ref_build(flat)
+        with tempfile.TemporaryDirectory() as d:
+            s, o = os.path.join(d, "m.yfs"), os.path.join(d, "o.bin")
+            flat.write(s)
+            info = oracle._ref("regress", s, o, n)
+            raw = np.fromfile(o, np.uint8).reshape(n, 32)
+        assert info["kdtree_vs_brute_force_mismatches"] == 0, info
+        out["mesh%d_vertices" % k] = v
+        out["mesh%d_indices" % k] = i
+        out["mesh%d_bounds" % k] = flat.meshes[0].bounds
+        out["mesh%d_nodes" % k] = flat.meshes[0].nodes
+        out["mesh%d_rays" % k] = raw[:, :24].copy().view(np.float32)
+        out["mesh%d_t" % k] = raw[:, 24:28].copy().view(np.float32).reshape(n)
+        out["mesh%d_prim" % k] = raw[:, 28:32].copy().view(np.uint32).reshape(n)
+    np.savez_compressed(os.path.join(HERE, "kdtree_regression.npz"), **out)
+
+
+def cornell_c1_64():
+    with tempfile.TemporaryDirectory() as d:
+        pbrt = os.path.join(d, "cornell.pbrt")
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=1, width=64, height=64, spp=16, maxdepth=8))
+        yfs = os.path.join(HERE, "cornell_c1_64.yfs")
+        oracle.ref_flatten(pbrt, yfs, seed_offset=1)
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_c1_64.npz"), image=img, variance=np.float64(info["variance"]))
+
+
+if __name__ == "__main__":
+    if not oracle.have_reference():
+        sys.exit("oracle/_ref/yar_ref is not built (oracle/build_ref.sh)")
+    which = sys.argv[1:] or ["raycast_small", "transform_small", "kdtree_regression", "cornell_c1_64"]
+    for name in which:
+        globals()[name]()
+        print("wrote", name)

@@ -1,0 +1,48 @@
+"""The C-ABI library loads and exports every symbol include/yar_gpu.h declares
+(no compute calls: these run without a GPU)."""
+import ctypes
+import os
+import re
+
+from conftest import ROOT
+
+
+def declared_functions():
+    text = open(os.path.join(ROOT, "include", "yar_gpu.h")).read()
+    text = re.sub(r"/\*.*?\*/", "", text, flags=re.S)
+    return sorted(set(re.findall(r"^\s*(?:int|void|const char\*|void\*)\s+\**(yar_\w+)\s*\(", text, re.M)))
+
+
+def test_header_declares_the_reference_seams():
+    names = declared_functions()
+    for required in ["yar_gpu_create", "yar_gpu_destroy", "yar_gpu_last_error", "yar_gpu_upload_scene",
+                     "yar_gpu_cast_closest", "yar_gpu_cast_any", "yar_gpu_render", "yar_build_mesh_kdtree",
+                     "yar_build_scene_kdtree"]:
+        assert required in names
+
+
+def test_library_exports_every_declared_symbol():
+    from yar_gb300 import native
+    lib = ctypes.CDLL(native.LIB_PATH)
+    missing = [n for n in declared_functions() if not hasattr(lib, n)]
+    assert not missing, missing
+    # and the Python binding table covers all of them
+    assert set(declared_functions()) <= set(native.EXPORTS)
+
+
+def test_context_creation_fails_cleanly_without_a_device():
+    import pytest
+    from conftest import cuda_available
+    from yar_gb300 import native
+    if cuda_available():
+        pytest.skip("a device is present")
+    with pytest.raises(native.YarError):
+        native.Context(0)
+
+
+def test_struct_sizes_match_the_header():
+    from yar_gb300 import native
+    assert ctypes.sizeof(native.KdNode) == 8
+    assert ctypes.sizeof(native.ObjectDesc) == 164
+    assert ctypes.sizeof(native.MaterialDesc) == 72
+    assert ctypes.sizeof(native.RectLightDesc) == 72

@@ -1,0 +1,197 @@
+"""GPU parity of the extend (closest-hit) and shadow (any-hit) kernels through
+the C ABI: bit-exact hit triangle, object, t and barycentrics, and bit-exact
+occlusion, against the reference's golden outputs and the oracle."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden
+from yar_gb300 import native, scenes
+from yar_gb300.scene import FlatScene, Mesh, make_object
+
+pytestmark = pytest.mark.gpu
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+def assert_same_hits(got, want):
+    t, prim, obj, bary = got
+    wt, wprim, wobj, wbary = want
+    assert np.array_equal(prim, wprim), np.nonzero(prim != wprim)[0][:10]
+    assert np.array_equal(obj, wobj)
+    assert np.array_equal(bits(t), bits(wt))
+    assert np.array_equal(bits(bary), bits(wbary))
+
+
+@pytest.mark.parametrize("name", ["raycast_small", "transform_small", "cornell_c1_64"])
+def test_golden_scene_casts(gpu_ctx, name):
+    s = FlatScene.read(golden(name + ".yfs"))
+    gpu_ctx.upload_scene(s)
+    if name == "cornell_c1_64":
+        lo, hi = scenes.scene_box(s)
+        rays = scenes.random_rays(lo, hi, 8192, 5)
+        want = oracle.cast_closest(s, rays)
+        shadow = scenes.random_shadow_rays(lo, hi, 8192, 6)
+        want_occ = oracle.cast_any(s, shadow)
+    else:
+        g = np.load(golden(name + ".npz"))
+        rays, shadow = g["rays"], g["shadow_rays"]
+        want = (g["t"], g["prim"], g["obj"], g["bary"])
+        want_occ = g["occluded"]
+    assert_same_hits(gpu_ctx.cast_closest(rays), want)
+    assert np.array_equal(gpu_ctx.cast_any(shadow), want_occ)
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_kdtree_regression_meshes(gpu_ctx, k):
+    g = np.load(golden("kdtree_regression.npz"))
+    s = FlatScene()
+    s.meshes = [Mesh(g["mesh%d_vertices" % k], g["mesh%d_indices" % k], bounds=g["mesh%d_bounds" % k],
+                     nodes=g["mesh%d_nodes" % k])]
+    s.objects = np.array([make_object(0)])
+    s.build_scene_kdtree()
+    rays = np.zeros((g["mesh%d_rays" % k].shape[0], 8), np.float32)
+    rays[:, 0:3] = g["mesh%d_rays" % k][:, 0:3]
+    rays[:, 4:7] = g["mesh%d_rays" % k][:, 3:6]
+    rays[:, 3] = np.inf
+    gpu_ctx.upload_scene(s)
+    t, prim, obj, bary = gpu_ctx.cast_closest(rays)
+    assert np.array_equal(bits(t), bits(g["mesh%d_t" % k]))
+    assert np.array_equal(prim, g["mesh%d_prim" % k])
+
+
+@pytest.fixture(scope="module")
+def medium_scene():
+    return scenes.raycast_scene(seed=4, grid=256, spheres=64, level=4, build=True)
+
+
+def test_medium_scene_against_oracle(gpu_ctx, medium_scene):
+    s = medium_scene
+    gpu_ctx.upload_scene(s)
+    lo, hi = scenes.scene_box(s)
+    rays = scenes.random_rays(lo, hi, 300_000, 17)
+    assert_same_hits(gpu_ctx.cast_closest(rays), oracle.cast_closest(s, rays))
+    shadow = scenes.random_shadow_rays(lo, hi, 300_000, 18)
+    assert np.array_equal(gpu_ctx.cast_any(shadow), oracle.cast_any(s, shadow))
+
+
+def test_edge_case_rays(gpu_ctx, medium_scene):
+    """Axis-parallel directions (zero components, +-inf inverse), origins
+    exactly on split planes, zero tmax, rays starting outside and pointing
+    away, and empty batches."""
+    s = medium_scene
+    gpu_ctx.upload_scene(s)
+    lo, hi = scenes.scene_box(s)
+    rng = np.random.default_rng(1)
+    n = 60_000
+    rays = scenes.random_rays(lo, hi, n, 19)
+    axis = rng.integers(0, 3, n)
+    sign = np.where(rng.random(n) < 0.5, -1.0, 1.0).astype(np.float32)
+    rays[: n // 3, 4:7] = 0.0
+    rays[np.arange(n // 3), 4 + axis[: n // 3]] = sign[: n // 3]
+    # origins on split planes of the terrain tree
+    nodes = s.meshes[0].nodes
+    interior = nodes[(nodes[:, 0] & 3) != 3]
+    pick = rng.integers(0, interior.shape[0], n // 3)
+    planes = interior[pick, 1].view(np.float32)
+    ax = (interior[pick, 0] & 3).astype(np.int64)
+    sl = slice(n // 3, 2 * n // 3)
+    rays[sl][np.arange(n // 3), ax] = planes
+    rays[2 * n // 3: 2 * n // 3 + 1000, 3] = 0.0          # tmax = 0: nothing can hit
+    rays[-1000:, 0:3] = hi + 1.0                            # outside, pointing away
+    rays[-1000:, 4:7] = np.abs(rays[-1000:, 4:7])
+    assert_same_hits(gpu_ctx.cast_closest(rays), oracle.cast_closest(s, rays))
+    shadow = rays.copy()
+    shadow[:, 3] = np.where(np.isinf(shadow[:, 3]), 0.5, shadow[:, 3])
+    assert np.array_equal(gpu_ctx.cast_any(shadow), oracle.cast_any(s, shadow))
+    empty = np.zeros((0, 8), np.float32)
+    assert gpu_ctx.cast_closest(empty)[0].shape == (0,)
+    assert gpu_ctx.cast_any(empty).shape == (0,)
+
+
+def test_visibility_flags_and_degenerate_triangles(gpu_ctx):
+    """Invisible meshes are skipped by both casts, no-shadow meshes only by the
+    any-hit cast (src/ref/scene_context.cpp:98-106); degenerate triangles never
+    report a hit (src/ref/kdtree.cpp:27-29)."""
+    v = np.array([[-1, -1, 0], [1, -1, 0], [0, 1, 0], [0.5, 0.5, 0], [0.5, 0.5, 0]], np.float32)
+    tri = np.array([[0, 1, 2]], np.int32)
+    degenerate = np.array([[3, 4, 0], [0, 1, 2]], np.int32)
+    s = FlatScene()
+    s.meshes = [Mesh(v, tri, visibility=0), Mesh(v, tri, visibility=1), Mesh(v, tri, visibility=2),
+                Mesh(v, degenerate)]
+    m = lambda z: np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, z], np.float32)
+    s.objects = np.array([make_object(0, m(0.0)), make_object(1, m(-1.0)), make_object(2, m(-2.0)),
+                          make_object(3, m(-3.0))])
+    s.build_kdtrees(1)
+    gpu_ctx.upload_scene(s)
+    rays = np.zeros((4, 8), np.float32)
+    rays[:, 0:3] = [0.0, -0.2, 5.0]
+    rays[:, 4:7] = [0, 0, -1]
+    rays[:, 3] = [np.inf, 5.5, 6.5, 7.5]
+    t, prim, obj, _ = gpu_ctx.cast_closest(rays)
+    want = oracle.cast_closest(s, rays)
+    assert np.array_equal(obj, want[2]) and np.array_equal(prim, want[1])
+    assert obj[0] == 0
+    shadow = rays.copy()
+    shadow[0:3, 0:3] = [0.0, -0.2, -0.5]      # below object 0: only the no-shadow/invisible ones in range
+    occ = gpu_ctx.cast_any(shadow)
+    assert np.array_equal(occ, oracle.cast_any(s, shadow))
+
+
+def test_device_buffers_match_host_buffers(gpu_ctx, medium_scene):
+    torch = pytest.importorskip("torch")
+    s = medium_scene
+    gpu_ctx.upload_scene(s)
+    lo, hi = scenes.scene_box(s)
+    rays = scenes.random_rays(lo, hi, 100_000, 23)
+    host = gpu_ctx.cast_closest(rays)
+    d_rays = torch.from_numpy(rays).cuda()
+    n = rays.shape[0]
+    t = torch.empty(n, dtype=torch.float32, device="cuda")
+    prim = torch.empty(n, dtype=torch.int32, device="cuda")
+    obj = torch.empty(n, dtype=torch.int32, device="cuda")
+    bary = torch.empty((n, 2), dtype=torch.float32, device="cuda")
+    torch.cuda.synchronize()
+    ms = gpu_ctx.cast_closest_device(d_rays.data_ptr(), n, t.data_ptr(), prim.data_ptr(), obj.data_ptr(),
+                                     bary.data_ptr(), timed=True)
+    assert ms > 0
+    dev = (t.cpu().numpy(), prim.cpu().numpy().view(np.uint32), obj.cpu().numpy().view(np.uint32),
+           bary.cpu().numpy())
+    assert_same_hits(dev, host)
+    occ = torch.empty(n, dtype=torch.uint8, device="cuda")
+    gpu_ctx.cast_any_device(d_rays.data_ptr(), n, occ.data_ptr())
+    torch.cuda.synchronize()
+    assert np.array_equal(occ.cpu().numpy(), gpu_ctx.cast_any(rays))
+
+
+def test_malformed_scene_is_rejected_on_the_host(gpu_ctx):
+    s = FlatScene.read(golden("raycast_small.yfs"))
+    bad = FlatScene.read(golden("raycast_small.yfs"))
+    nodes = bad.meshes[0].nodes.copy()
+    interior = np.nonzero((nodes[:, 0] & 3) != 3)[0][0]
+    nodes[interior, 0] = (nodes[interior, 0] & 3) | (np.uint32(nodes.shape[0] + 5) << np.uint32(2))
+    bad.meshes[0].nodes = nodes
+    with pytest.raises(native.YarError) as e:
+        gpu_ctx.upload_scene(bad)
+    assert e.value.code == native.YAR_ERR_INVALID
+    with pytest.raises(native.YarError):
+        gpu_ctx.cast_closest(np.zeros((4, 8), np.float32))   # no scene after a failed upload
+    gpu_ctx.upload_scene(s)                                  # the context stays usable
+    g = np.load(golden("raycast_small.npz"))
+    assert np.array_equal(gpu_ctx.cast_closest(g["rays"])[1], g["prim"])
+
+
+def test_batch_capacity_error():
+    if not pytest.importorskip("torch").cuda.is_available():
+        pytest.skip("no CUDA device")
+    ctx = native.Context(0, max_batch_rays=1000)
+    try:
+        ctx.upload_scene(FlatScene.read(golden("raycast_small.yfs")))
+        with pytest.raises(native.YarError) as e:
+            ctx.cast_closest(np.zeros((1001, 8), np.float32))
+        assert e.value.code == native.YAR_ERR_CAPACITY
+        ctx.cast_closest(np.zeros((1000, 8), np.float32))
+    finally:
+        ctx.close()

@@ -1,0 +1,121 @@
+"""The oracle (C restatement) against the reference's own outputs: the
+golden fixtures are the reference renderer's results on the same inputs, and
+the live reference (oracle/_ref) when it is built here."""
+import numpy as np
+import pytest
+
+import oracle
+from conftest import golden
+from yar_gb300 import scenes
+from yar_gb300.scene import FlatScene, Mesh, make_object
+
+
+def bits(a):
+    return np.ascontiguousarray(a, np.float32).view(np.uint32)
+
+
+@pytest.mark.parametrize("name", ["raycast_small", "transform_small"])
+def test_oracle_closest_matches_reference(name):
+    s = FlatScene.read(golden(name + ".yfs"))
+    g = np.load(golden(name + ".npz"))
+    t, prim, obj, bary = oracle.cast_closest(s, g["rays"])
+    assert np.array_equal(prim, g["prim"])
+    assert np.array_equal(obj, g["obj"])
+    assert np.array_equal(bits(t), bits(g["t"]))
+    assert np.array_equal(bits(bary), bits(g["bary"]))
+    assert (prim != 0xFFFFFFFF).mean() > 0.1
+
+
+@pytest.mark.parametrize("name", ["raycast_small", "transform_small"])
+def test_oracle_any_matches_reference(name):
+    s = FlatScene.read(golden(name + ".yfs"))
+    g = np.load(golden(name + ".npz"))
+    occ = oracle.cast_any(s, g["shadow_rays"])
+    assert np.array_equal(occ, g["occluded"])
+    assert 0.05 < occ.mean() < 0.95
+
+
+def regression_scene(g, k):
+    s = FlatScene()
+    s.meshes = [Mesh(g["mesh%d_vertices" % k], g["mesh%d_indices" % k], bounds=g["mesh%d_bounds" % k],
+                     nodes=g["mesh%d_nodes" % k])]
+    s.objects = np.array([make_object(0)])
+    s.build_scene_kdtree()
+    rays = np.zeros((g["mesh%d_rays" % k].shape[0], 8), np.float32)
+    rays[:, 0:3] = g["mesh%d_rays" % k][:, 0:3]
+    rays[:, 4:7] = g["mesh%d_rays" % k][:, 3:6]
+    rays[:, 3] = np.inf
+    return s, rays
+
+
+@pytest.mark.parametrize("k", [0, 1])
+def test_oracle_kdtree_regression_meshes(k):
+    """src/ref/test_kdtree.cpp: kd-tree t equals the brute-force t on the
+    reference's FP-regression meshes and ray stream."""
+    g = np.load(golden("kdtree_regression.npz"))
+    s, rays = regression_scene(g, k)
+    t, prim, obj, bary = oracle.cast_closest(s, rays)
+    assert np.array_equal(bits(t), bits(g["mesh%d_t" % k]))
+    assert np.array_equal(prim, g["mesh%d_prim" % k])
+
+
+def test_watertight_known_answers():
+    """The watertight intersector on the known-answer layout of the reference's
+    SIMD test (src/ref/test_triangle_intersection.cpp:132-283): a ray from
+    (0,0,5) along -z hits a triangle in the z=0 plane at t=5, misses one offset
+    beyond its edge, and reports barycentrics that sum to 1."""
+    import ctypes
+    L = oracle.lib()
+    o = (ctypes.c_float * 3)(0, 0, 5)
+    d = (ctypes.c_float * 3)(0, 0, -1)
+    b = (ctypes.c_float * 3)()
+    hit = [(ctypes.c_float * 3)(*p) for p in ([-1, -1, 0], [1, -1, 0], [0, 1, 0])]
+    t = L.oracle_intersect_triangle_watertight(o, d, hit[0], hit[1], hit[2], b)
+    assert t == 5.0 and abs(sum(b) - 1) < 1e-6
+    for dz in (1.0, 2.0, 3.0):
+        shifted = [(ctypes.c_float * 3)(p[0], p[1], p[2] + dz) for p in hit]
+        assert L.oracle_intersect_triangle_watertight(o, d, *shifted, b) == 5.0 - dz
+    miss = [(ctypes.c_float * 3)(p[0] + 3, p[1], p[2]) for p in hit]
+    assert L.oracle_intersect_triangle_watertight(o, d, *miss, b) == float("inf")
+    # a shared edge is hit by exactly one of two triangles or both (never neither)
+    e = [(ctypes.c_float * 3)(*p) for p in ([0, -1, 0], [0, 1, 0], [-1, 0, 0], [1, 0, 0])]
+    t1 = L.oracle_intersect_triangle_watertight(o, d, e[0], e[1], e[2], b)
+    t2 = L.oracle_intersect_triangle_watertight(o, d, e[1], e[0], e[3], b)
+    assert min(t1, t2) == 5.0
+
+
+def test_pcg32_matches_reference_stream():
+    """pcg32_srandom_r(0, stream) then get_uint / get_float (src/lib/random.h)."""
+    import ctypes
+    L = oracle.lib()
+    rng = (ctypes.c_uint64 * 2)()
+    L.oracle_pcg32_seed(rng, 42, 54)
+    # the pcg-basic demo stream for initstate 42, initseq 54
+    expected = [0xa15c02b7, 0x7b47f409, 0xba1d3330, 0x83d2f293, 0xbfa4784b, 0xcbed606e]
+    assert [L.oracle_pcg32_next(rng) for _ in range(6)] == expected
+    L.oracle_pcg32_seed(rng, 0, 7)
+    f = [L.oracle_pcg32_float(rng) for _ in range(1000)]
+    assert min(f) >= 0.0 and max(f) < 1.0
+
+
+@pytest.mark.skipif(not oracle.have_reference(), reason="reference not built here")
+def test_oracle_against_live_reference_larger_batch():
+    s = scenes.raycast_scene(seed=9, grid=96, spheres=12, level=3, build=True, threads=4)
+    lo, hi = scenes.scene_box(s)
+    rays = scenes.random_rays(lo, hi, 50000, 3)
+    (rt, rp, ro, rb), _ = oracle.ref_cast(s, rays)
+    t, prim, obj, bary = oracle.cast_closest(s, rays)
+    assert np.array_equal(prim, rp) and np.array_equal(obj, ro) and np.array_equal(bits(t), bits(rt))
+    sr = scenes.random_shadow_rays(lo, hi, 50000, 4)
+    ra, _ = oracle.ref_cast(s, sr, any_hit=True)
+    assert np.array_equal(oracle.cast_any(s, sr), ra)
+
+
+@pytest.mark.skipif(not oracle.have_reference(), reason="reference not built here")
+def test_builder_against_live_reference_large_mesh():
+    from yar_gb300 import native
+    s = scenes.raycast_scene(seed=2, grid=160, spheres=2, level=3, build=False)
+    ref, _ = oracle.ref_build(s)
+    for m, r in zip(s.meshes, ref.meshes):
+        b, nodes = native.build_mesh_kdtree(m.vertices, m.indices, 8)
+        assert np.array_equal(nodes, r.nodes)

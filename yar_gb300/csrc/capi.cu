@@ -1,0 +1,385 @@
+// capi.cu - the C ABI of include/yar_gpu.h: contexts, scene upload and the
+// ray-cast entry points.  Scene upload validates every index the kernels will
+// follow (node links, leaf primitive indices, mesh and object references), so
+// a malformed scene is rejected on the host with YAR_ERR_INVALID instead of
+// reaching the device.
+#include "context.hpp"
+
+#include <cmath>
+#include <cstring>
+#include <new>
+#include <string>
+#include <vector>
+
+namespace yar {
+
+int fail(yar_gpu_ctx* ctx, int code, const std::string& message) {
+    if (ctx) ctx->last_error = message;
+    return code;
+}
+
+int cuda_fail(yar_gpu_ctx* ctx, cudaError_t e, const char* what) {
+    return fail(ctx, YAR_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+}
+
+int device_alloc(yar_gpu_ctx* ctx, Device_Buffer& b, size_t bytes) {
+    device_free(b);
+    if (bytes == 0) bytes = 16;
+    cudaError_t e = cudaMalloc(&b.ptr, bytes);
+    if (e != cudaSuccess) {
+        b.ptr = nullptr;
+        cudaGetLastError();
+        return fail(ctx, YAR_ERR_NOMEM, std::string("cudaMalloc(") + std::to_string(bytes) + "): " +
+                                            cudaGetErrorString(e));
+    }
+    b.bytes = bytes;
+    return YAR_OK;
+}
+
+void device_free(Device_Buffer& b) {
+    if (b.ptr) cudaFree(b.ptr);
+    b.ptr = nullptr;
+    b.bytes = 0;
+}
+
+namespace {
+
+int upload(yar_gpu_ctx* ctx, Device_Buffer& b, const void* src, size_t bytes) {
+    int rc = device_alloc(ctx, b, bytes);
+    if (rc != YAR_OK) return rc;
+    if (bytes) {
+        cudaError_t e = cudaMemcpyAsync(b.ptr, src, bytes, cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "scene upload");
+    }
+    return YAR_OK;
+}
+
+// Structural check of a KdNode array (src/ref/kdtree.h:18-77): every reachable
+// node index, leaf index-word range and primitive index stays inside bounds,
+// and no root-to-leaf path is deeper than the traversal stack.
+bool validate_tree(const yar_kdtree_view& t, uint32_t primitive_count, std::string& why) {
+    if (!t.nodes || t.node_count == 0) { why = "empty kd-tree"; return false; }
+    struct Item { uint32_t node; int depth; };
+    std::vector<Item> todo{{0u, 0}};
+    std::vector<uint8_t> seen(t.node_count, 0);
+    while (!todo.empty()) {
+        Item it = todo.back();
+        todo.pop_back();
+        if (it.node >= t.node_count) { why = "node index out of range"; return false; }
+        if (seen[it.node]) continue;  // DAG sharing would be unusual but harmless
+        seen[it.node] = 1;
+        if (it.depth > kMaxTraversalDepth) { why = "kd-tree deeper than the traversal stack"; return false; }
+        const yar_kd_node n = t.nodes[it.node];
+        if ((n.word0 & 3u) == 3u) {
+            const uint32_t count = n.word0 >> 2;
+            const uint64_t words_end = 2ull * it.node + 1 + count;  // word index one past the last index
+            if (count > 0 && words_end > 2ull * t.node_count) { why = "leaf index array out of range"; return false; }
+            const uint32_t* words = &t.nodes[it.node].word1;
+            for (uint32_t i = 0; i < count; i++)
+                if (words[i] >= primitive_count) { why = "leaf primitive index out of range"; return false; }
+        } else {
+            const uint32_t above = n.word0 >> 2;
+            if (it.node + 1 >= t.node_count || above >= t.node_count || above <= it.node) {
+                why = "interior child index out of range";
+                return false;
+            }
+            todo.push_back({it.node + 1, it.depth + 1});
+            todo.push_back({above, it.depth + 1});
+        }
+    }
+    return true;
+}
+
+} // namespace
+} // namespace yar
+
+using namespace yar;
+
+extern "C" int yar_gpu_create(yar_gpu_ctx** out, const yar_gpu_options* options) {
+    if (!out) return YAR_ERR_INVALID;
+    *out = nullptr;
+    yar_gpu_ctx* ctx = new (std::nothrow) yar_gpu_ctx();
+    if (!ctx) return YAR_ERR_NOMEM;
+    ctx->device = options ? options->device : 0;
+    ctx->staging_capacity = (options && options->max_batch_rays) ? options->max_batch_rays : (16u << 20);
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) {
+        cudaGetLastError();
+        delete ctx;
+        return YAR_ERR_CUDA;
+    }
+    if (ctx->device < 0 || ctx->device >= count) {
+        delete ctx;
+        return YAR_ERR_INVALID;
+    }
+    e = cudaSetDevice(ctx->device);
+    if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_error, sizeof(int));
+    if (e == cudaSuccess) e = cudaMemset(ctx->d_error, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_start);
+    if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_stop);
+    if (e != cudaSuccess) {
+        cudaGetLastError();
+        yar_gpu_destroy(ctx);
+        return YAR_ERR_CUDA;
+    }
+    *out = ctx;
+    return YAR_OK;
+}
+
+extern "C" void yar_gpu_destroy(yar_gpu_ctx* ctx) {
+    if (!ctx) return;
+    cudaSetDevice(ctx->device);
+    if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+    render_release(ctx);
+    for (Device_Buffer* b : {&ctx->scene_nodes, &ctx->mesh_nodes, &ctx->objects, &ctx->tris, &ctx->d_rays, &ctx->d_t,
+                             &ctx->d_prim, &ctx->d_obj, &ctx->d_bary, &ctx->d_occ})
+        device_free(*b);
+    if (ctx->d_error) cudaFree(ctx->d_error);
+    if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
+    if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
+    if (ctx->stream) cudaStreamDestroy(ctx->stream);
+    delete ctx;
+}
+
+extern "C" const char* yar_gpu_last_error(const yar_gpu_ctx* ctx) {
+    return ctx ? ctx->last_error.c_str() : "null context";
+}
+
+extern "C" void* yar_gpu_stream(yar_gpu_ctx* ctx) { return ctx ? (void*)ctx->stream : nullptr; }
+
+extern "C" int yar_gpu_synchronize(yar_gpu_ctx* ctx) {
+    if (!ctx) return YAR_ERR_INVALID;
+    cudaSetDevice(ctx->device);
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "synchronize");
+    return YAR_OK;
+}
+
+extern "C" int yar_gpu_upload_scene(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
+    if (!ctx) return YAR_ERR_INVALID;
+    if (!scene || scene->mesh_count == 0 || scene->object_count == 0 || !scene->meshes || !scene->objects)
+        return fail(ctx, YAR_ERR_INVALID, "scene has no meshes or objects");
+    cudaSetDevice(ctx->device);
+    ctx->has_scene = false;
+    std::string why;
+    // meshes: validate, gather triangles, concatenate node arrays
+    std::vector<uint32_t> node_offset(scene->mesh_count), tri_offset(scene->mesh_count);
+    uint64_t total_nodes = 0, total_tris = 0;
+    for (uint32_t m = 0; m < scene->mesh_count; m++) {
+        const yar_mesh_desc& mesh = scene->meshes[m];
+        if (!mesh.vertices || !mesh.indices || mesh.triangle_count == 0)
+            return fail(ctx, YAR_ERR_INVALID, "mesh " + std::to_string(m) + " has no triangles");
+        for (uint64_t i = 0; i < 3ull * mesh.triangle_count; i++)
+            if (mesh.indices[i] < 0 || (uint32_t)mesh.indices[i] >= mesh.vertex_count)
+                return fail(ctx, YAR_ERR_INVALID, "mesh " + std::to_string(m) + " index out of range");
+        if (!validate_tree(mesh.kdtree, mesh.triangle_count, why))
+            return fail(ctx, YAR_ERR_INVALID, "mesh " + std::to_string(m) + ": " + why);
+        node_offset[m] = (uint32_t)total_nodes;
+        tri_offset[m] = (uint32_t)total_tris;
+        total_nodes += mesh.kdtree.node_count;
+        total_tris += mesh.triangle_count;
+        if (total_nodes > 0xffffffffull || total_tris > 0x3fffffffull)
+            return fail(ctx, YAR_ERR_CAPACITY, "scene exceeds 2^32 nodes or 2^30 triangles");
+    }
+    if (!validate_tree(scene->scene_kdtree, scene->object_count, why))
+        return fail(ctx, YAR_ERR_INVALID, "scene tree: " + why);
+
+    std::vector<uint2> nodes;
+    std::vector<float4> tris;
+    std::vector<float4> objects;
+    try {
+        nodes.resize(total_nodes);
+        tris.resize(3 * total_tris);
+        objects.resize(6 * (size_t)scene->object_count);
+    } catch (const std::bad_alloc&) {
+        return fail(ctx, YAR_ERR_NOMEM, "host staging for scene upload");
+    }
+    for (uint32_t m = 0; m < scene->mesh_count; m++) {
+        const yar_mesh_desc& mesh = scene->meshes[m];
+        memcpy(&nodes[node_offset[m]], mesh.kdtree.nodes, mesh.kdtree.node_count * sizeof(uint2));
+        for (uint32_t t = 0; t < mesh.triangle_count; t++) {
+            const float* p[3];
+            for (int k = 0; k < 3; k++) p[k] = mesh.vertices + 3 * (size_t)mesh.indices[3 * (size_t)t + k];
+            // cross(p1 - p0, p2 - p0).length_squared() == 0, as src/ref/kdtree.cpp:27-29 evaluates it
+            const float a0 = p[1][0] - p[0][0], a1 = p[1][1] - p[0][1], a2 = p[1][2] - p[0][2];
+            const float c0 = p[2][0] - p[0][0], c1 = p[2][1] - p[0][1], c2 = p[2][2] - p[0][2];
+            const float x = a1 * c2 - a2 * c1, y = a2 * c0 - a0 * c2, z = a0 * c1 - a1 * c0;
+            const float len2 = x * x + y * y + z * z;
+            const float flag = (len2 == 0.f) ? 1.f : 0.f;
+            float4* dst = &tris[3 * ((size_t)tri_offset[m] + t)];
+            dst[0] = make_float4(p[0][0], p[0][1], p[0][2], flag);
+            dst[1] = make_float4(p[1][0], p[1][1], p[1][2], 0.f);
+            dst[2] = make_float4(p[2][0], p[2][1], p[2][2], 0.f);
+        }
+    }
+    for (uint32_t i = 0; i < scene->object_count; i++) {
+        const yar_object_desc& o = scene->objects[i];
+        if (o.mesh_index < 0 || (uint32_t)o.mesh_index >= scene->mesh_count)
+            return fail(ctx, YAR_ERR_INVALID, "object " + std::to_string(i) + " has an invalid mesh index");
+        const yar_mesh_desc& mesh = scene->meshes[o.mesh_index];
+        float4* r = &objects[6 * (size_t)i];
+        const float* w = o.world_to_object;
+        r[0] = make_float4(w[0], w[1], w[2], w[3]);
+        r[1] = make_float4(w[4], w[5], w[6], w[7]);
+        r[2] = make_float4(w[8], w[9], w[10], w[11]);
+        uint32_t no = node_offset[o.mesh_index], to = tri_offset[o.mesh_index];
+        float nof, tof;
+        memcpy(&nof, &no, 4);
+        memcpy(&tof, &to, 4);
+        r[3] = make_float4(mesh.kdtree.bounds_min[0], mesh.kdtree.bounds_min[1], mesh.kdtree.bounds_min[2], nof);
+        r[4] = make_float4(mesh.kdtree.bounds_max[0], mesh.kdtree.bounds_max[1], mesh.kdtree.bounds_max[2], tof);
+        int32_t info[4] = {o.mesh_index, mesh.visibility, 0, 0};
+        memcpy(&r[5], info, 16);
+    }
+    int rc;
+    if ((rc = upload(ctx, ctx->mesh_nodes, nodes.data(), nodes.size() * sizeof(uint2))) != YAR_OK) return rc;
+    if ((rc = upload(ctx, ctx->tris, tris.data(), tris.size() * sizeof(float4))) != YAR_OK) return rc;
+    if ((rc = upload(ctx, ctx->objects, objects.data(), objects.size() * sizeof(float4))) != YAR_OK) return rc;
+    if ((rc = upload(ctx, ctx->scene_nodes, scene->scene_kdtree.nodes,
+                     scene->scene_kdtree.node_count * sizeof(uint2))) != YAR_OK)
+        return rc;
+    cudaError_t e = cudaStreamSynchronize(ctx->stream);  // host staging vectors die at return
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "scene upload");
+
+    Device_Scene& ds = ctx->ds;
+    ds.scene_nodes = (const uint2*)ctx->scene_nodes.ptr;
+    ds.mesh_nodes = (const uint2*)ctx->mesh_nodes.ptr;
+    ds.objects = (const float4*)ctx->objects.ptr;
+    ds.tris = (const float4*)ctx->tris.ptr;
+    memcpy(ds.scene_bounds, scene->scene_kdtree.bounds_min, 12);
+    memcpy(ds.scene_bounds + 3, scene->scene_kdtree.bounds_max, 12);
+    ds.object_count = scene->object_count;
+
+    rc = render_upload(ctx, scene);
+    if (rc != YAR_OK) return rc;
+    ctx->has_scene = true;
+    return YAR_OK;
+}
+
+namespace {
+
+int ensure_staging(yar_gpu_ctx* ctx, uint32_t n, bool closest) {
+    if (n > ctx->staging_capacity)
+        return fail(ctx, YAR_ERR_CAPACITY, "batch of " + std::to_string(n) + " rays exceeds max_batch_rays");
+    int rc;
+    if (ctx->d_rays.bytes < (size_t)n * 32 && (rc = device_alloc(ctx, ctx->d_rays, (size_t)n * 32)) != YAR_OK) return rc;
+    if (closest) {
+        if (ctx->d_t.bytes < (size_t)n * 4 && (rc = device_alloc(ctx, ctx->d_t, (size_t)n * 4)) != YAR_OK) return rc;
+        if (ctx->d_prim.bytes < (size_t)n * 4 && (rc = device_alloc(ctx, ctx->d_prim, (size_t)n * 4)) != YAR_OK) return rc;
+        if (ctx->d_obj.bytes < (size_t)n * 4 && (rc = device_alloc(ctx, ctx->d_obj, (size_t)n * 4)) != YAR_OK) return rc;
+        if (ctx->d_bary.bytes < (size_t)n * 8 && (rc = device_alloc(ctx, ctx->d_bary, (size_t)n * 8)) != YAR_OK) return rc;
+    } else {
+        if (ctx->d_occ.bytes < (size_t)n && (rc = device_alloc(ctx, ctx->d_occ, (size_t)n)) != YAR_OK) return rc;
+    }
+    return YAR_OK;
+}
+
+int check_error_word(yar_gpu_ctx* ctx) {
+    int h = 0;
+    cudaError_t e = cudaMemcpyAsync(&h, ctx->d_error, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "kernel");
+    if (h) {
+        cudaMemsetAsync(ctx->d_error, 0, sizeof(int), ctx->stream);
+        return fail(ctx, YAR_ERR_CAPACITY, "kd-tree traversal stack overflow");
+    }
+    return YAR_OK;
+}
+
+int cast(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t n, const yar_hit_soa* hits, uint8_t* occluded,
+         int32_t buffers, float* kernel_ms) {
+    if (!ctx) return YAR_ERR_INVALID;
+    if (!ctx->has_scene) return fail(ctx, YAR_ERR_NO_SCENE, "no scene uploaded");
+    const bool closest = hits != nullptr;
+    if (n && !rays) return fail(ctx, YAR_ERR_INVALID, "null ray buffer");
+    if (!closest && n && !occluded) return fail(ctx, YAR_ERR_INVALID, "null output buffer");
+    if (buffers != YAR_BUFFERS_HOST && buffers != YAR_BUFFERS_DEVICE) return fail(ctx, YAR_ERR_INVALID, "buffers flag");
+    if (n == 0) return YAR_OK;
+    cudaSetDevice(ctx->device);
+    cudaError_t e;
+    const float4* d_rays;
+    float* d_t = nullptr;
+    uint32_t *d_prim = nullptr, *d_obj = nullptr;
+    float2* d_bary = nullptr;
+    uint8_t* d_occ = nullptr;
+    if (buffers == YAR_BUFFERS_HOST) {
+        int rc = ensure_staging(ctx, n, closest);
+        if (rc != YAR_OK) return rc;
+        e = cudaMemcpyAsync(ctx->d_rays.ptr, rays, (size_t)n * 32, cudaMemcpyHostToDevice, ctx->stream);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "ray upload");
+        d_rays = (const float4*)ctx->d_rays.ptr;
+        if (closest) {
+            d_t = hits->t ? (float*)ctx->d_t.ptr : nullptr;
+            d_prim = hits->prim ? (uint32_t*)ctx->d_prim.ptr : nullptr;
+            d_obj = hits->object ? (uint32_t*)ctx->d_obj.ptr : nullptr;
+            d_bary = hits->bary ? (float2*)ctx->d_bary.ptr : nullptr;
+        } else {
+            d_occ = (uint8_t*)ctx->d_occ.ptr;
+        }
+    } else {
+        if (((uintptr_t)rays & 15u) != 0) return fail(ctx, YAR_ERR_INVALID, "device ray buffer must be 16-byte aligned");
+        d_rays = (const float4*)rays;
+        if (closest) {
+            d_t = hits->t;
+            d_prim = hits->prim;
+            d_obj = hits->object;
+            d_bary = (float2*)hits->bary;
+            if (((uintptr_t)d_bary & 7u) != 0) return fail(ctx, YAR_ERR_INVALID, "bary buffer must be 8-byte aligned");
+        } else {
+            d_occ = occluded;
+        }
+    }
+    if (kernel_ms) cudaEventRecord(ctx->ev_start, ctx->stream);
+    e = closest ? launch_extend(ctx->ds, d_rays, n, d_t, d_prim, d_obj, d_bary, ctx->d_error, ctx->stream)
+                : launch_shadow(ctx->ds, d_rays, n, d_occ, ctx->d_error, ctx->stream);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, closest ? "extend launch" : "shadow launch");
+    if (kernel_ms) cudaEventRecord(ctx->ev_stop, ctx->stream);
+    if (buffers == YAR_BUFFERS_HOST) {
+        if (closest) {
+            if (hits->t) e = cudaMemcpyAsync(hits->t, d_t, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream);
+            if (e == cudaSuccess && hits->prim)
+                e = cudaMemcpyAsync(hits->prim, d_prim, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream);
+            if (e == cudaSuccess && hits->object)
+                e = cudaMemcpyAsync(hits->object, d_obj, (size_t)n * 4, cudaMemcpyDeviceToHost, ctx->stream);
+            if (e == cudaSuccess && hits->bary)
+                e = cudaMemcpyAsync(hits->bary, d_bary, (size_t)n * 8, cudaMemcpyDeviceToHost, ctx->stream);
+        } else {
+            e = cudaMemcpyAsync(occluded, d_occ, n, cudaMemcpyDeviceToHost, ctx->stream);
+        }
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "result download");
+    }
+    int rc = check_error_word(ctx);
+    if (rc != YAR_OK) return rc;
+    if (kernel_ms) {
+        e = cudaEventElapsedTime(kernel_ms, ctx->ev_start, ctx->ev_stop);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "event timing");
+    }
+    return YAR_OK;
+}
+
+} // namespace
+
+extern "C" int yar_gpu_cast_closest(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t n, const yar_hit_soa* hits,
+                                    int32_t buffers) {
+    if (!hits) return fail(ctx, YAR_ERR_INVALID, "null hit buffers");
+    return cast(ctx, rays, n, hits, nullptr, buffers, nullptr);
+}
+
+extern "C" int yar_gpu_cast_any(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t n, uint8_t* occluded,
+                                int32_t buffers) {
+    return cast(ctx, rays, n, nullptr, occluded, buffers, nullptr);
+}
+
+extern "C" int yar_gpu_cast_closest_timed(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t n,
+                                          const yar_hit_soa* hits, float* kernel_ms) {
+    if (!hits || !kernel_ms) return fail(ctx, YAR_ERR_INVALID, "null argument");
+    return cast(ctx, rays, n, hits, nullptr, YAR_BUFFERS_DEVICE, kernel_ms);
+}
+
+extern "C" int yar_gpu_cast_any_timed(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t n, uint8_t* occluded,
+                                      float* kernel_ms) {
+    if (!kernel_ms) return fail(ctx, YAR_ERR_INVALID, "null argument");
+    return cast(ctx, rays, n, nullptr, occluded, YAR_BUFFERS_DEVICE, kernel_ms);
+}

@@ -1,0 +1,264 @@
+// yfs.hpp - "flat scene" file: a serialised yar_flat_scene (include/yar_gpu.h).
+//
+// The file carries exactly what the device path consumes: meshes with their
+// kd-trees (node words bit for bit as KdTree::save writes them,
+// src/ref/kdtree.cpp:137-160), scene objects, the scene kd-tree, constant
+// materials, rectangular lights, camera and Raytracer_Config.  It is produced
+// by the host scene loader of this library and by the reference-side adapter
+// that flattens a reference Scene_Context, so both sides can be compared on
+// identical bytes.
+//
+// Layout: "YFS1" u32 version, then chunks {char tag[4]; u32 zero; u64 size;
+// payload}.  All scalar fields are 4-byte little-endian values.
+#pragma once
+
+#include "yar_gpu.h"
+
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+namespace yfs {
+
+struct Mesh {
+    std::vector<float> vertices;   // 3 per vertex
+    std::vector<float> normals;    // empty or 3 per vertex
+    std::vector<float> uvs;        // empty or 2 per vertex
+    std::vector<int32_t> indices;  // 3 per triangle
+    int32_t reverse_orientation = 0;
+    int32_t visibility = YAR_VISIBLE;
+    float bounds[6] = {0, 0, 0, 0, 0, 0};
+    std::vector<yar_kd_node> nodes;
+};
+
+struct Scene {
+    std::vector<Mesh> meshes;
+    std::vector<yar_object_desc> objects;
+    float scene_bounds[6] = {0, 0, 0, 0, 0, 0};
+    std::vector<yar_kd_node> scene_nodes;
+    std::vector<yar_material_desc> materials;
+    std::vector<yar_rect_light_desc> rect_lights;
+    uint32_t other_light_count = 0;
+    yar_camera_desc camera{};
+    yar_render_config config{};
+
+    // Views for the C ABI; valid while this object is alive and unmodified.
+    std::vector<yar_mesh_desc> mesh_views;
+    yar_flat_scene view() {
+        mesh_views.resize(meshes.size());
+        for (size_t i = 0; i < meshes.size(); i++) {
+            const Mesh& m = meshes[i];
+            yar_mesh_desc& d = mesh_views[i];
+            d.vertices = m.vertices.data();
+            d.normals = m.normals.empty() ? nullptr : m.normals.data();
+            d.uvs = m.uvs.empty() ? nullptr : m.uvs.data();
+            d.indices = m.indices.data();
+            d.vertex_count = (uint32_t)(m.vertices.size() / 3);
+            d.triangle_count = (uint32_t)(m.indices.size() / 3);
+            d.reverse_geometric_normal_orientation = m.reverse_orientation;
+            d.visibility = m.visibility;
+            memcpy(d.kdtree.bounds_min, m.bounds, 3 * sizeof(float));
+            memcpy(d.kdtree.bounds_max, m.bounds + 3, 3 * sizeof(float));
+            d.kdtree.nodes = m.nodes.data();
+            d.kdtree.node_count = (uint32_t)m.nodes.size();
+        }
+        yar_flat_scene s{};
+        s.mesh_count = (uint32_t)meshes.size();
+        s.meshes = mesh_views.data();
+        s.object_count = (uint32_t)objects.size();
+        s.objects = objects.data();
+        memcpy(s.scene_kdtree.bounds_min, scene_bounds, 3 * sizeof(float));
+        memcpy(s.scene_kdtree.bounds_max, scene_bounds + 3, 3 * sizeof(float));
+        s.scene_kdtree.nodes = scene_nodes.data();
+        s.scene_kdtree.node_count = (uint32_t)scene_nodes.size();
+        s.material_count = (uint32_t)materials.size();
+        s.materials = materials.data();
+        s.rect_light_count = (uint32_t)rect_lights.size();
+        s.rect_lights = rect_lights.data();
+        s.other_light_count = other_light_count;
+        s.camera = camera;
+        s.config = config;
+        return s;
+    }
+};
+
+namespace detail {
+struct Writer {
+    FILE* f;
+    bool ok = true;
+    void raw(const void* p, size_t n) { if (n && fwrite(p, 1, n, f) != n) ok = false; }
+    template <class T> void pod(const T& v) { raw(&v, sizeof(T)); }
+    void chunk(const char tag[4], const std::vector<uint8_t>& payload) {
+        raw(tag, 4);
+        uint32_t zero = 0;
+        pod(zero);
+        uint64_t size = payload.size();
+        pod(size);
+        raw(payload.data(), payload.size());
+    }
+};
+struct Buf {
+    std::vector<uint8_t> b;
+    void raw(const void* p, size_t n) {
+        const uint8_t* s = (const uint8_t*)p;
+        b.insert(b.end(), s, s + n);
+    }
+    template <class T> void pod(const T& v) { raw(&v, sizeof(T)); }
+};
+struct Reader {
+    const uint8_t* p;
+    const uint8_t* end;
+    bool ok = true;
+    void raw(void* dst, size_t n) {
+        if ((size_t)(end - p) < n) { ok = false; return; }
+        memcpy(dst, p, n);
+        p += n;
+    }
+    template <class T> T pod() { T v{}; raw(&v, sizeof(T)); return v; }
+};
+} // namespace detail
+
+inline bool write(const std::string& path, const Scene& s) {
+    FILE* f = fopen(path.c_str(), "wb");
+    if (!f) return false;
+    detail::Writer w{f};
+    w.raw("YFS1", 4);
+    uint32_t version = 1;
+    w.pod(version);
+    {
+        detail::Buf b;
+        b.pod(s.config);
+        b.pod(s.camera);
+        b.pod(s.other_light_count);
+        w.chunk("CONF", b.b);
+    }
+    for (const Mesh& m : s.meshes) {
+        detail::Buf b;
+        uint32_t vc = (uint32_t)(m.vertices.size() / 3), tc = (uint32_t)(m.indices.size() / 3);
+        uint32_t flags = (m.normals.empty() ? 0u : 1u) | (m.uvs.empty() ? 0u : 2u);
+        uint32_t nc = (uint32_t)m.nodes.size();
+        b.pod(vc); b.pod(tc); b.pod(flags); b.pod(m.reverse_orientation); b.pod(m.visibility); b.pod(nc);
+        b.raw(m.bounds, sizeof(m.bounds));
+        b.raw(m.vertices.data(), m.vertices.size() * 4);
+        b.raw(m.indices.data(), m.indices.size() * 4);
+        if (flags & 1) b.raw(m.normals.data(), m.normals.size() * 4);
+        if (flags & 2) b.raw(m.uvs.data(), m.uvs.size() * 4);
+        b.raw(m.nodes.data(), m.nodes.size() * sizeof(yar_kd_node));
+        w.chunk("MESH", b.b);
+    }
+    {
+        detail::Buf b;
+        uint32_t n = (uint32_t)s.objects.size();
+        b.pod(n);
+        b.raw(s.objects.data(), n * sizeof(yar_object_desc));
+        w.chunk("OBJS", b.b);
+    }
+    {
+        detail::Buf b;
+        uint32_t n = (uint32_t)s.scene_nodes.size();
+        b.raw(s.scene_bounds, sizeof(s.scene_bounds));
+        b.pod(n);
+        b.raw(s.scene_nodes.data(), n * sizeof(yar_kd_node));
+        w.chunk("SKDT", b.b);
+    }
+    {
+        detail::Buf b;
+        uint32_t n = (uint32_t)s.materials.size();
+        b.pod(n);
+        b.raw(s.materials.data(), n * sizeof(yar_material_desc));
+        w.chunk("MATS", b.b);
+    }
+    {
+        detail::Buf b;
+        uint32_t n = (uint32_t)s.rect_lights.size();
+        b.pod(n);
+        b.raw(s.rect_lights.data(), n * sizeof(yar_rect_light_desc));
+        w.chunk("RLIT", b.b);
+    }
+    bool ok = w.ok;
+    if (fclose(f) != 0) ok = false;
+    return ok;
+}
+
+inline bool read(const std::string& path, Scene& s, std::string* err = nullptr) {
+    auto fail = [&](const char* m) { if (err) *err = m; return false; };
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) return fail("cannot open file");
+    std::vector<uint8_t> data;
+    {
+        if (fseek(f, 0, SEEK_END) != 0) { fclose(f); return fail("seek failed"); }
+        long size = ftell(f);
+        if (size < 0) { fclose(f); return fail("tell failed"); }
+        fseek(f, 0, SEEK_SET);
+        data.resize((size_t)size);
+        size_t got = data.empty() ? 0 : fread(data.data(), 1, data.size(), f);
+        fclose(f);
+        if (got != data.size()) return fail("short read");
+    }
+    detail::Reader r{data.data(), data.data() + data.size()};
+    char magic[4];
+    r.raw(magic, 4);
+    uint32_t version = r.pod<uint32_t>();
+    if (!r.ok || memcmp(magic, "YFS1", 4) != 0 || version != 1) return fail("not a YFS1 file");
+    s = Scene{};
+    while (r.ok && r.p < r.end) {
+        char tag[4];
+        r.raw(tag, 4);
+        r.pod<uint32_t>();
+        uint64_t size = r.pod<uint64_t>();
+        if (!r.ok || (uint64_t)(r.end - r.p) < size) return fail("truncated chunk");
+        detail::Reader c{r.p, r.p + size};
+        r.p += size;
+        if (!memcmp(tag, "CONF", 4)) {
+            s.config = c.pod<yar_render_config>();
+            s.camera = c.pod<yar_camera_desc>();
+            s.other_light_count = c.pod<uint32_t>();
+        } else if (!memcmp(tag, "MESH", 4)) {
+            Mesh m;
+            uint32_t vc = c.pod<uint32_t>(), tc = c.pod<uint32_t>(), flags = c.pod<uint32_t>();
+            m.reverse_orientation = c.pod<int32_t>();
+            m.visibility = c.pod<int32_t>();
+            uint32_t nc = c.pod<uint32_t>();
+            c.raw(m.bounds, sizeof(m.bounds));
+            if (!c.ok || (uint64_t)vc * 12 + (uint64_t)tc * 12 + (uint64_t)nc * 8 > size) return fail("bad mesh chunk");
+            m.vertices.resize((size_t)vc * 3);
+            c.raw(m.vertices.data(), m.vertices.size() * 4);
+            m.indices.resize((size_t)tc * 3);
+            c.raw(m.indices.data(), m.indices.size() * 4);
+            if (flags & 1) { m.normals.resize((size_t)vc * 3); c.raw(m.normals.data(), m.normals.size() * 4); }
+            if (flags & 2) { m.uvs.resize((size_t)vc * 2); c.raw(m.uvs.data(), m.uvs.size() * 4); }
+            m.nodes.resize(nc);
+            c.raw(m.nodes.data(), nc * sizeof(yar_kd_node));
+            if (!c.ok) return fail("truncated mesh chunk");
+            s.meshes.push_back(std::move(m));
+        } else if (!memcmp(tag, "OBJS", 4)) {
+            uint32_t n = c.pod<uint32_t>();
+            if ((uint64_t)n * sizeof(yar_object_desc) > size) return fail("bad object chunk");
+            s.objects.resize(n);
+            c.raw(s.objects.data(), n * sizeof(yar_object_desc));
+        } else if (!memcmp(tag, "SKDT", 4)) {
+            c.raw(s.scene_bounds, sizeof(s.scene_bounds));
+            uint32_t n = c.pod<uint32_t>();
+            if ((uint64_t)n * 8 > size) return fail("bad scene tree chunk");
+            s.scene_nodes.resize(n);
+            c.raw(s.scene_nodes.data(), n * sizeof(yar_kd_node));
+        } else if (!memcmp(tag, "MATS", 4)) {
+            uint32_t n = c.pod<uint32_t>();
+            if ((uint64_t)n * sizeof(yar_material_desc) > size) return fail("bad material chunk");
+            s.materials.resize(n);
+            c.raw(s.materials.data(), n * sizeof(yar_material_desc));
+        } else if (!memcmp(tag, "RLIT", 4)) {
+            uint32_t n = c.pod<uint32_t>();
+            if ((uint64_t)n * sizeof(yar_rect_light_desc) > size) return fail("bad light chunk");
+            s.rect_lights.resize(n);
+            c.raw(s.rect_lights.data(), n * sizeof(yar_rect_light_desc));
+        }
+        if (!c.ok) return fail("truncated chunk payload");
+    }
+    if (!r.ok) return fail("truncated file");
+    return true;
+}
+
+} // namespace yfs

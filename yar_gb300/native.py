@@ -1,0 +1,281 @@
+"""ctypes bindings of include/yar_gpu.h (the product library libyar_gb300.so).
+
+The library is loaded from the package directory and nothing else: if it is
+missing the import fails loudly (there is no CPU fallback for the hot path).
+"""
+import ctypes as C
+import os
+
+import numpy as np
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "libyar_gb300.so")
+
+YAR_OK = 0
+YAR_ERR_INVALID = -1
+YAR_ERR_NOMEM = -2
+YAR_ERR_CAPACITY = -3
+YAR_ERR_TIMEOUT = -4
+YAR_ERR_CUDA = -5
+YAR_ERR_UNSUPPORTED = -6
+YAR_ERR_IO = -7
+YAR_ERR_NO_SCENE = -8
+
+YAR_BUFFERS_HOST = 0
+YAR_BUFFERS_DEVICE = 1
+
+MATERIAL_DIFFUSE = 2
+MATERIAL_METAL = 4
+MATERIAL_GLASS = 7
+MATERIAL_NULL = 0xFFFFFFFF
+LIGHT_RECT = 3
+LIGHT_NULL = 0xFFFFFFFF
+
+
+class KdNode(C.Structure):
+    _fields_ = [("word0", C.c_uint32), ("word1", C.c_uint32)]
+
+
+class KdTreeView(C.Structure):
+    _fields_ = [("bounds_min", C.c_float * 3), ("bounds_max", C.c_float * 3),
+                ("nodes", C.c_void_p), ("node_count", C.c_uint32)]
+
+
+class MeshDesc(C.Structure):
+    _fields_ = [("vertices", C.c_void_p), ("normals", C.c_void_p), ("uvs", C.c_void_p),
+                ("indices", C.c_void_p), ("vertex_count", C.c_uint32), ("triangle_count", C.c_uint32),
+                ("reverse_geometric_normal_orientation", C.c_int32), ("visibility", C.c_int32),
+                ("kdtree", KdTreeView)]
+
+
+class ObjectDesc(C.Structure):
+    _fields_ = [("mesh_index", C.c_int32), ("material_type", C.c_uint32), ("material_index", C.c_int32),
+                ("area_light_type", C.c_uint32), ("area_light_index", C.c_int32),
+                ("object_to_world", C.c_float * 12), ("world_to_object", C.c_float * 12),
+                ("object_to_world_normal", C.c_float * 12)]
+
+
+class MaterialDesc(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("reflectance", C.c_float * 3), ("transmittance", C.c_float * 3),
+                ("eta", C.c_float * 3), ("k", C.c_float * 3), ("eta_i", C.c_float),
+                ("u_roughness", C.c_float), ("v_roughness", C.c_float),
+                ("index_of_refraction", C.c_float), ("roughness_is_alpha", C.c_int32)]
+
+
+class RectLightDesc(C.Structure):
+    _fields_ = [("light_to_world", C.c_float * 12), ("emitted_radiance", C.c_float * 3),
+                ("size", C.c_float * 2), ("sample_count", C.c_int32)]
+
+
+class CameraDesc(C.Structure):
+    _fields_ = [("camera_to_world", C.c_float * 12), ("image_extent", C.c_float * 2),
+                ("horz_half_dist", C.c_float), ("vert_half_dist", C.c_float), ("z_is_up", C.c_int32)]
+
+
+class RenderConfig(C.Structure):
+    _fields_ = [("render_region", C.c_int32 * 4), ("rendering_algorithm", C.c_int32),
+                ("max_light_bounces", C.c_int32), ("russian_roulette_threshold", C.c_float),
+                ("russian_roulette_bounce_count_threshold", C.c_int32), ("pixel_filter_type", C.c_int32),
+                ("pixel_filter_radius", C.c_float), ("pixel_filter_alpha", C.c_float),
+                ("x_pixel_sample_count", C.c_int32), ("y_pixel_sample_count", C.c_int32),
+                ("film_radiance_scale", C.c_float), ("max_rgb_component_value_of_film_sample", C.c_float),
+                ("pbrt3_scene", C.c_int32), ("rng_seed_offset", C.c_int32)]
+
+
+class FlatSceneDesc(C.Structure):
+    _fields_ = [("mesh_count", C.c_uint32), ("meshes", C.POINTER(MeshDesc)),
+                ("object_count", C.c_uint32), ("objects", C.POINTER(ObjectDesc)),
+                ("scene_kdtree", KdTreeView),
+                ("material_count", C.c_uint32), ("materials", C.POINTER(MaterialDesc)),
+                ("rect_light_count", C.c_uint32), ("rect_lights", C.POINTER(RectLightDesc)),
+                ("other_light_count", C.c_uint32), ("camera", CameraDesc), ("config", RenderConfig)]
+
+
+class HitSoa(C.Structure):
+    _fields_ = [("t", C.c_void_p), ("prim", C.c_void_p), ("object", C.c_void_p), ("bary", C.c_void_p)]
+
+
+class GpuOptions(C.Structure):
+    _fields_ = [("device", C.c_int32), ("max_batch_rays", C.c_uint32)]
+
+
+class RenderStats(C.Structure):
+    _fields_ = [("variance", C.c_double), ("seconds", C.c_float), ("paths", C.c_uint64),
+                ("rays_closest", C.c_uint64), ("rays_any", C.c_uint64), ("kernel_launches", C.c_uint32)]
+
+
+# exported symbols and their prototypes: (restype, argtypes)
+EXPORTS = {
+    "yar_gpu_create": (C.c_int, [C.POINTER(C.c_void_p), C.POINTER(GpuOptions)]),
+    "yar_gpu_destroy": (None, [C.c_void_p]),
+    "yar_gpu_last_error": (C.c_char_p, [C.c_void_p]),
+    "yar_gpu_stream": (C.c_void_p, [C.c_void_p]),
+    "yar_gpu_synchronize": (C.c_int, [C.c_void_p]),
+    "yar_gpu_upload_scene": (C.c_int, [C.c_void_p, C.POINTER(FlatSceneDesc)]),
+    "yar_gpu_cast_closest": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(HitSoa), C.c_int32]),
+    "yar_gpu_cast_any": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.c_int32]),
+    "yar_gpu_cast_closest_timed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(HitSoa),
+                                             C.POINTER(C.c_float)]),
+    "yar_gpu_cast_any_timed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_float)]),
+    "yar_gpu_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
+    "yar_build_mesh_kdtree": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_int32,
+                                        C.POINTER(C.c_float), C.POINTER(C.c_void_p), C.POINTER(C.c_uint32)]),
+    "yar_build_scene_kdtree": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_void_p),
+                                         C.POINTER(C.c_uint32)]),
+    "yar_free_nodes": (None, [C.c_void_p]),
+    "yar_transform_bounds": (None, [C.c_void_p, C.c_void_p, C.c_void_p]),
+}
+
+_lib = None
+
+
+def lib():
+    """Load libyar_gb300.so (raises if it has not been built)."""
+    global _lib
+    if _lib is None:
+        if not os.path.exists(LIB_PATH):
+            raise ImportError("libyar_gb300.so is not built: run `python -c \"import __graft_entry__ as g; "
+                              "g.build()\"` (path %s)" % LIB_PATH)
+        L = C.CDLL(LIB_PATH)
+        for name, (res, args) in EXPORTS.items():
+            f = getattr(L, name)
+            f.restype = res
+            f.argtypes = args
+        _lib = L
+    return _lib
+
+
+class YarError(RuntimeError):
+    def __init__(self, code, message):
+        super().__init__("yar_gpu error %d: %s" % (code, message))
+        self.code = code
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data
+
+
+def build_mesh_kdtree(vertices, indices, threads=0):
+    """Reference kd-tree for a triangle mesh: returns (bounds[6] f32, nodes (N,2) u32)."""
+    v = np.ascontiguousarray(vertices, dtype=np.float32).reshape(-1, 3)
+    i = np.ascontiguousarray(indices, dtype=np.int32).reshape(-1, 3)
+    bounds = (C.c_float * 6)()
+    nodes = C.c_void_p()
+    count = C.c_uint32()
+    rc = lib().yar_build_mesh_kdtree(_ptr(v), v.shape[0], _ptr(i), i.shape[0], int(threads or os.cpu_count() or 1),
+                                     bounds, C.byref(nodes), C.byref(count))
+    if rc != YAR_OK:
+        raise YarError(rc, "yar_build_mesh_kdtree")
+    out = np.ctypeslib.as_array(C.cast(nodes, C.POINTER(C.c_uint32)), shape=(count.value * 2,)).copy()
+    lib().yar_free_nodes(nodes)
+    return np.array(bounds, dtype=np.float32), out.reshape(-1, 2)
+
+
+def build_scene_kdtree(object_bounds):
+    """Reference scene kd-tree over per-object world bounds (M,6)."""
+    b = np.ascontiguousarray(object_bounds, dtype=np.float32).reshape(-1, 6)
+    bounds = (C.c_float * 6)()
+    nodes = C.c_void_p()
+    count = C.c_uint32()
+    rc = lib().yar_build_scene_kdtree(_ptr(b), b.shape[0], bounds, C.byref(nodes), C.byref(count))
+    if rc != YAR_OK:
+        raise YarError(rc, "yar_build_scene_kdtree")
+    out = np.ctypeslib.as_array(C.cast(nodes, C.POINTER(C.c_uint32)), shape=(count.value * 2,)).copy()
+    lib().yar_free_nodes(nodes)
+    return np.array(bounds, dtype=np.float32), out.reshape(-1, 2)
+
+
+def transform_bounds(object_to_world, bounds):
+    m = np.ascontiguousarray(object_to_world, dtype=np.float32).reshape(12)
+    b = np.ascontiguousarray(bounds, dtype=np.float32).reshape(6)
+    out = np.zeros(6, dtype=np.float32)
+    lib().yar_transform_bounds(_ptr(m), _ptr(b), _ptr(out))
+    return out
+
+
+class Context:
+    """A yar_gpu_ctx: one CUDA device, one stream, one uploaded scene."""
+
+    def __init__(self, device=0, max_batch_rays=0):
+        L = lib()
+        h = C.c_void_p()
+        opts = GpuOptions(int(device), int(max_batch_rays))
+        rc = L.yar_gpu_create(C.byref(h), C.byref(opts))
+        if rc != YAR_OK:
+            raise YarError(rc, "yar_gpu_create (is a CUDA device visible?)")
+        self._h = h
+        self._scene_keepalive = None
+
+    def close(self):
+        if self._h:
+            lib().yar_gpu_destroy(self._h)
+            self._h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def _check(self, rc, what):
+        if rc != YAR_OK:
+            msg = lib().yar_gpu_last_error(self._h)
+            raise YarError(rc, "%s: %s" % (what, msg.decode() if msg else ""))
+
+    @property
+    def stream(self):
+        return lib().yar_gpu_stream(self._h)
+
+    def synchronize(self):
+        self._check(lib().yar_gpu_synchronize(self._h), "synchronize")
+
+    def upload_scene(self, flat):
+        desc, keep = flat.to_c()
+        self._check(lib().yar_gpu_upload_scene(self._h, C.byref(desc)), "upload_scene")
+        self._scene_keepalive = (desc, keep)
+
+    # host-buffer casts (copies inside the call)
+    def cast_closest(self, rays):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        t = np.empty(n, np.float32)
+        prim = np.empty(n, np.uint32)
+        obj = np.empty(n, np.uint32)
+        bary = np.empty((n, 2), np.float32)
+        hits = HitSoa(_ptr(t), _ptr(prim), _ptr(obj), _ptr(bary))
+        self._check(lib().yar_gpu_cast_closest(self._h, _ptr(rays), n, C.byref(hits), YAR_BUFFERS_HOST),
+                    "cast_closest")
+        return t, prim, obj, bary
+
+    def cast_any(self, rays):
+        rays = np.ascontiguousarray(rays, dtype=np.float32).reshape(-1, 8)
+        n = rays.shape[0]
+        occ = np.empty(n, np.uint8)
+        self._check(lib().yar_gpu_cast_any(self._h, _ptr(rays), n, _ptr(occ), YAR_BUFFERS_HOST), "cast_any")
+        return occ
+
+    # device-buffer casts: arguments are raw device pointers (e.g. torch data_ptr())
+    def cast_closest_device(self, rays_ptr, n, t_ptr, prim_ptr, obj_ptr, bary_ptr=None, timed=False):
+        hits = HitSoa(t_ptr, prim_ptr, obj_ptr, bary_ptr)
+        if timed:
+            ms = C.c_float()
+            self._check(lib().yar_gpu_cast_closest_timed(self._h, rays_ptr, n, C.byref(hits), C.byref(ms)),
+                        "cast_closest_timed")
+            return ms.value
+        self._check(lib().yar_gpu_cast_closest(self._h, rays_ptr, n, C.byref(hits), YAR_BUFFERS_DEVICE),
+                    "cast_closest")
+        return None
+
+    def cast_any_device(self, rays_ptr, n, occ_ptr, timed=False):
+        if timed:
+            ms = C.c_float()
+            self._check(lib().yar_gpu_cast_any_timed(self._h, rays_ptr, n, occ_ptr, C.byref(ms)), "cast_any_timed")
+            return ms.value
+        self._check(lib().yar_gpu_cast_any(self._h, rays_ptr, n, occ_ptr, YAR_BUFFERS_DEVICE), "cast_any")
+        return None
+
+    def render(self, width, height):
+        rgb = np.zeros((height, width, 3), np.float32)
+        stats = RenderStats()
+        self._check(lib().yar_gpu_render(self._h, _ptr(rgb), C.byref(stats)), "render")
+        return rgb, stats

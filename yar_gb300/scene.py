@@ -1,0 +1,273 @@
+"""Flat scenes: the host-side form of yar_flat_scene (include/yar_gpu.h).
+
+A FlatScene holds numpy arrays for meshes (with their kd-trees), scene
+objects, the scene kd-tree, constant materials, rectangular lights, the
+camera and the Raytracer_Config fields.  It reads and writes the flat scene
+file (yar_gb300/csrc/yfs.hpp) and builds the ctypes descriptor passed to
+yar_gpu_upload_scene.
+"""
+import ctypes as C
+import struct
+
+import numpy as np
+
+from . import native
+
+OBJECT_DTYPE = np.dtype([("mesh_index", "<i4"), ("material_type", "<u4"), ("material_index", "<i4"),
+                         ("area_light_type", "<u4"), ("area_light_index", "<i4"),
+                         ("object_to_world", "<f4", 12), ("world_to_object", "<f4", 12),
+                         ("object_to_world_normal", "<f4", 12)])
+MATERIAL_DTYPE = np.dtype([("type", "<u4"), ("reflectance", "<f4", 3), ("transmittance", "<f4", 3),
+                           ("eta", "<f4", 3), ("k", "<f4", 3), ("eta_i", "<f4"), ("u_roughness", "<f4"),
+                           ("v_roughness", "<f4"), ("index_of_refraction", "<f4"), ("roughness_is_alpha", "<i4")])
+LIGHT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("emitted_radiance", "<f4", 3), ("size", "<f4", 2),
+                        ("sample_count", "<i4")])
+CAMERA_DTYPE = np.dtype([("camera_to_world", "<f4", 12), ("image_extent", "<f4", 2), ("horz_half_dist", "<f4"),
+                         ("vert_half_dist", "<f4"), ("z_is_up", "<i4")])
+CONFIG_DTYPE = np.dtype([("render_region", "<i4", 4), ("rendering_algorithm", "<i4"), ("max_light_bounces", "<i4"),
+                         ("russian_roulette_threshold", "<f4"), ("russian_roulette_bounce_count_threshold", "<i4"),
+                         ("pixel_filter_type", "<i4"), ("pixel_filter_radius", "<f4"),
+                         ("pixel_filter_alpha", "<f4"), ("x_pixel_sample_count", "<i4"),
+                         ("y_pixel_sample_count", "<i4"), ("film_radiance_scale", "<f4"),
+                         ("max_rgb_component_value_of_film_sample", "<f4"), ("pbrt3_scene", "<i4"),
+                         ("rng_seed_offset", "<i4")])
+
+assert OBJECT_DTYPE.itemsize == C.sizeof(native.ObjectDesc)
+assert MATERIAL_DTYPE.itemsize == C.sizeof(native.MaterialDesc)
+assert LIGHT_DTYPE.itemsize == C.sizeof(native.RectLightDesc)
+assert CAMERA_DTYPE.itemsize == C.sizeof(native.CameraDesc)
+assert CONFIG_DTYPE.itemsize == C.sizeof(native.RenderConfig)
+
+IDENTITY = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32)
+
+
+class Mesh:
+    def __init__(self, vertices, indices, normals=None, uvs=None, reverse_orientation=0, visibility=0,
+                 bounds=None, nodes=None):
+        self.vertices = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
+        self.indices = np.ascontiguousarray(indices, np.int32).reshape(-1, 3)
+        self.normals = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
+        self.uvs = None if uvs is None else np.ascontiguousarray(uvs, np.float32).reshape(-1, 2)
+        self.reverse_orientation = int(reverse_orientation)
+        self.visibility = int(visibility)
+        self.bounds = np.zeros(6, np.float32) if bounds is None else np.asarray(bounds, np.float32)
+        self.nodes = np.zeros((0, 2), np.uint32) if nodes is None else np.ascontiguousarray(nodes, np.uint32)
+
+    @property
+    def triangle_count(self):
+        return self.indices.shape[0]
+
+
+def default_config(width=256, height=256, spp_x=1, spp_y=1, max_bounces=32, seed_offset=0):
+    c = np.zeros((), CONFIG_DTYPE)
+    c["render_region"] = (0, 0, width, height)
+    c["rendering_algorithm"] = 1
+    c["max_light_bounces"] = max_bounces
+    c["russian_roulette_threshold"] = 1.0
+    c["russian_roulette_bounce_count_threshold"] = 3
+    c["pixel_filter_type"] = 0
+    c["pixel_filter_radius"] = 0.5
+    c["pixel_filter_alpha"] = 2.0
+    c["x_pixel_sample_count"] = spp_x
+    c["y_pixel_sample_count"] = spp_y
+    c["film_radiance_scale"] = 1.0
+    c["max_rgb_component_value_of_film_sample"] = np.inf
+    c["pbrt3_scene"] = 1
+    c["rng_seed_offset"] = seed_offset
+    return c
+
+
+class FlatScene:
+    def __init__(self):
+        self.meshes = []
+        self.objects = np.zeros(0, OBJECT_DTYPE)
+        self.scene_bounds = np.zeros(6, np.float32)
+        self.scene_nodes = np.zeros((0, 2), np.uint32)
+        self.materials = np.zeros(0, MATERIAL_DTYPE)
+        self.rect_lights = np.zeros(0, LIGHT_DTYPE)
+        self.other_light_count = 0
+        self.camera = np.zeros((), CAMERA_DTYPE)
+        self.config = default_config()
+
+    @property
+    def triangle_count(self):
+        return sum(m.triangle_count for m in self.meshes)
+
+    # ---- kd-trees (the reference builder, run by the product library) ----
+    def build_kdtrees(self, threads=0):
+        """Per-mesh trees on a thread pool (the C builder releases the GIL),
+        largest meshes first, then the scene tree over the objects."""
+        import os
+        from concurrent.futures import ThreadPoolExecutor
+        threads = int(threads or os.cpu_count() or 1)
+        order = sorted(range(len(self.meshes)), key=lambda k: -self.meshes[k].triangle_count)
+
+        def one(k):
+            m = self.meshes[k]
+            m.bounds, m.nodes = native.build_mesh_kdtree(m.vertices, m.indices, threads)
+
+        with ThreadPoolExecutor(max_workers=threads) as ex:
+            list(ex.map(one, order))
+        self.build_scene_kdtree()
+        return self
+
+    def build_scene_kdtree(self):
+        ob = np.stack([native.transform_bounds(o["object_to_world"], self.meshes[o["mesh_index"]].bounds)
+                       for o in self.objects])
+        self.scene_bounds, self.scene_nodes = native.build_scene_kdtree(ob)
+        return self
+
+    # ---- ctypes descriptor ----
+    def to_c(self):
+        keep = []
+        meshes = (native.MeshDesc * len(self.meshes))()
+        for i, m in enumerate(self.meshes):
+            d = meshes[i]
+            d.vertices = m.vertices.ctypes.data
+            d.normals = m.normals.ctypes.data if m.normals is not None else None
+            d.uvs = m.uvs.ctypes.data if m.uvs is not None else None
+            d.indices = m.indices.ctypes.data
+            d.vertex_count = m.vertices.shape[0]
+            d.triangle_count = m.indices.shape[0]
+            d.reverse_geometric_normal_orientation = m.reverse_orientation
+            d.visibility = m.visibility
+            d.kdtree.bounds_min[:] = [float(x) for x in m.bounds[:3]]
+            d.kdtree.bounds_max[:] = [float(x) for x in m.bounds[3:]]
+            nodes = np.ascontiguousarray(m.nodes, np.uint32)
+            keep.append(nodes)
+            d.kdtree.nodes = nodes.ctypes.data if nodes.size else None
+            d.kdtree.node_count = nodes.shape[0]
+            keep.append(m)
+        objects = np.ascontiguousarray(self.objects)
+        materials = np.ascontiguousarray(self.materials)
+        lights = np.ascontiguousarray(self.rect_lights)
+        snodes = np.ascontiguousarray(self.scene_nodes, np.uint32)
+        keep += [objects, materials, lights, snodes, meshes]
+        s = native.FlatSceneDesc()
+        s.mesh_count = len(self.meshes)
+        s.meshes = meshes
+        s.object_count = objects.shape[0]
+        s.objects = C.cast(objects.ctypes.data, C.POINTER(native.ObjectDesc)) if objects.size else None
+        s.scene_kdtree.bounds_min[:] = [float(x) for x in self.scene_bounds[:3]]
+        s.scene_kdtree.bounds_max[:] = [float(x) for x in self.scene_bounds[3:]]
+        s.scene_kdtree.nodes = snodes.ctypes.data if snodes.size else None
+        s.scene_kdtree.node_count = snodes.shape[0]
+        s.material_count = materials.shape[0]
+        s.materials = C.cast(materials.ctypes.data, C.POINTER(native.MaterialDesc)) if materials.size else None
+        s.rect_light_count = lights.shape[0]
+        s.rect_lights = C.cast(lights.ctypes.data, C.POINTER(native.RectLightDesc)) if lights.size else None
+        s.other_light_count = int(self.other_light_count)
+        C.memmove(C.byref(s.camera), np.ascontiguousarray(self.camera).ctypes.data, CAMERA_DTYPE.itemsize)
+        C.memmove(C.byref(s.config), np.ascontiguousarray(self.config).ctypes.data, CONFIG_DTYPE.itemsize)
+        return s, keep
+
+    # ---- file I/O (yar_gb300/csrc/yfs.hpp) ----
+    def write(self, path):
+        def chunk(tag, payload):
+            return tag + struct.pack("<IQ", 0, len(payload)) + payload
+
+        parts = [b"YFS1", struct.pack("<I", 1)]
+        parts.append(chunk(b"CONF", self.config.tobytes() + self.camera.tobytes() +
+                           struct.pack("<I", int(self.other_light_count))))
+        for m in self.meshes:
+            flags = (1 if m.normals is not None else 0) | (2 if m.uvs is not None else 0)
+            p = struct.pack("<6I", m.vertices.shape[0], m.indices.shape[0], flags, m.reverse_orientation & 0xffffffff,
+                            m.visibility, m.nodes.shape[0])
+            p += m.bounds.astype(np.float32).tobytes() + m.vertices.tobytes() + m.indices.tobytes()
+            if m.normals is not None:
+                p += m.normals.tobytes()
+            if m.uvs is not None:
+                p += m.uvs.tobytes()
+            p += np.ascontiguousarray(m.nodes, np.uint32).tobytes()
+            parts.append(chunk(b"MESH", p))
+        parts.append(chunk(b"OBJS", struct.pack("<I", self.objects.shape[0]) + self.objects.tobytes()))
+        parts.append(chunk(b"SKDT", self.scene_bounds.astype(np.float32).tobytes() +
+                           struct.pack("<I", self.scene_nodes.shape[0]) +
+                           np.ascontiguousarray(self.scene_nodes, np.uint32).tobytes()))
+        parts.append(chunk(b"MATS", struct.pack("<I", self.materials.shape[0]) + self.materials.tobytes()))
+        parts.append(chunk(b"RLIT", struct.pack("<I", self.rect_lights.shape[0]) + self.rect_lights.tobytes()))
+        with open(path, "wb") as f:
+            f.write(b"".join(parts))
+
+    @staticmethod
+    def read(path):
+        data = open(path, "rb").read()
+        if data[:4] != b"YFS1" or struct.unpack_from("<I", data, 4)[0] != 1:
+            raise ValueError("%s is not a YFS1 file" % path)
+        s = FlatScene()
+        off = 8
+        while off < len(data):
+            tag = data[off:off + 4]
+            size = struct.unpack_from("<Q", data, off + 8)[0]
+            p = memoryview(data)[off + 16: off + 16 + size]
+            off += 16 + size
+            if tag == b"CONF":
+                s.config = np.frombuffer(p[:CONFIG_DTYPE.itemsize], CONFIG_DTYPE)[0].copy()
+                s.camera = np.frombuffer(p[CONFIG_DTYPE.itemsize:CONFIG_DTYPE.itemsize + CAMERA_DTYPE.itemsize],
+                                         CAMERA_DTYPE)[0].copy()
+                s.config = np.array(s.config, CONFIG_DTYPE)
+                s.camera = np.array(s.camera, CAMERA_DTYPE)
+                s.other_light_count = struct.unpack_from("<I", p, CONFIG_DTYPE.itemsize + CAMERA_DTYPE.itemsize)[0]
+            elif tag == b"MESH":
+                vc, tc, flags, rev, vis, nc = struct.unpack_from("<6I", p, 0)
+                q = 24
+                bounds = np.frombuffer(p[q:q + 24], np.float32).copy()
+                q += 24
+                v = np.frombuffer(p[q:q + 12 * vc], np.float32).reshape(-1, 3).copy()
+                q += 12 * vc
+                idx = np.frombuffer(p[q:q + 12 * tc], np.int32).reshape(-1, 3).copy()
+                q += 12 * tc
+                normals = uvs = None
+                if flags & 1:
+                    normals = np.frombuffer(p[q:q + 12 * vc], np.float32).reshape(-1, 3).copy()
+                    q += 12 * vc
+                if flags & 2:
+                    uvs = np.frombuffer(p[q:q + 8 * vc], np.float32).reshape(-1, 2).copy()
+                    q += 8 * vc
+                nodes = np.frombuffer(p[q:q + 8 * nc], np.uint32).reshape(-1, 2).copy()
+                s.meshes.append(Mesh(v, idx, normals, uvs, np.int32(np.uint32(rev)), vis, bounds, nodes))
+            elif tag == b"OBJS":
+                n = struct.unpack_from("<I", p, 0)[0]
+                s.objects = np.frombuffer(p[4:4 + n * OBJECT_DTYPE.itemsize], OBJECT_DTYPE).copy()
+            elif tag == b"SKDT":
+                s.scene_bounds = np.frombuffer(p[:24], np.float32).copy()
+                n = struct.unpack_from("<I", p, 24)[0]
+                s.scene_nodes = np.frombuffer(p[28:28 + 8 * n], np.uint32).reshape(-1, 2).copy()
+            elif tag == b"MATS":
+                n = struct.unpack_from("<I", p, 0)[0]
+                s.materials = np.frombuffer(p[4:4 + n * MATERIAL_DTYPE.itemsize], MATERIAL_DTYPE).copy()
+            elif tag == b"RLIT":
+                n = struct.unpack_from("<I", p, 0)[0]
+                s.rect_lights = np.frombuffer(p[4:4 + n * LIGHT_DTYPE.itemsize], LIGHT_DTYPE).copy()
+        return s
+
+
+def make_object(mesh_index, object_to_world=None, world_to_object=None, material_type=native.MATERIAL_DIFFUSE,
+                material_index=0, light_type=native.LIGHT_NULL, light_index=-1):
+    """A Scene_Object record; the inverse and normal transforms follow
+    src/lib/scene_loader.cpp:56-62 (normal transform = transpose of the 3x3
+    part of world_to_object)."""
+    o = np.zeros((), OBJECT_DTYPE)
+    m = IDENTITY.copy() if object_to_world is None else np.asarray(object_to_world, np.float32).reshape(12)
+    if world_to_object is None:
+        m44 = np.eye(4, dtype=np.float64)
+        m44[:3, :] = m.reshape(3, 4)
+        w = np.linalg.inv(m44)[:3, :].astype(np.float32).reshape(12)
+        if np.array_equal(m, IDENTITY):
+            w = IDENTITY.copy()
+    else:
+        w = np.asarray(world_to_object, np.float32).reshape(12)
+    n = np.zeros(12, np.float32)
+    w34 = w.reshape(3, 4)
+    for i in range(3):
+        for k in range(3):
+            n[4 * i + k] = w34[k, i]
+    o["mesh_index"] = mesh_index
+    o["material_type"] = material_type
+    o["material_index"] = material_index
+    o["area_light_type"] = light_type
+    o["area_light_index"] = light_index
+    o["object_to_world"] = m
+    o["world_to_object"] = w
+    o["object_to_world_normal"] = n
+    return o

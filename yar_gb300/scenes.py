@@ -1,0 +1,225 @@
+"""Seeded synthetic workloads (there are no published scenes for this path).
+
+cornell_pbrt      - procedural Cornell box as a pbrt-v3 file: 5 wall quads, two
+                    boxes rotated by seed-drawn angles in [0, 30] degrees
+                    (34 triangles), Lambertian albedos U[0.2, 0.8] per channel,
+                    one 0.25 x 0.25 quad light of radiance 17.
+raycast_scene     - seeded fBm terrain heightfield (grid x grid cells, 2
+                    triangles per cell, 6 octaves, amplitude 0.1) plus
+                    icospheres (subdivision 4, 5120 triangles each) at uniform
+                    random positions; one mesh per object, spheres placed by a
+                    translation so the two-level transform path is exercised.
+random_rays /
+random_shadow_rays - origins uniform in the scene box, directions uniform on
+                    the sphere; shadow rays have tmax = U[0,1] * |diagonal|.
+"""
+import math
+
+import numpy as np
+
+from . import native
+from .scene import FlatScene, Mesh, make_object
+
+
+# ---------------------------------------------------------------- icosphere
+def icosphere(radius=1.0, level=4):
+    """create_sphere_mesh (src/lib/tessellation.cpp:43-171): geodesic
+    subdivision of an icosahedron with shared, deduplicated vertices."""
+    f32 = np.float32
+    t = f32((f32(1.0) + np.sqrt(f32(5.0))) / f32(2.0))
+    s_inv = f32(f32(1.0) / np.sqrt(f32(1.0) + t * t))
+    verts = [(t, 1, 0), (-t, 1, 0), (t, -1, 0), (-t, -1, 0), (1, 0, t), (1, 0, -t), (-1, 0, t), (-1, 0, -t),
+             (0, t, 1), (0, -t, 1), (0, t, -1), (0, -t, -1)]
+    verts = [np.array(v, f32) * s_inv for v in verts]
+    idx = [0, 8, 4, 1, 10, 7, 2, 9, 11, 7, 3, 1, 0, 5, 10, 3, 9, 6, 3, 11, 9, 8, 6, 4, 2, 4, 9, 3, 7, 11,
+           4, 2, 0, 9, 4, 6, 2, 11, 5, 0, 10, 8, 5, 0, 2, 10, 5, 7, 1, 6, 8, 1, 8, 10, 6, 1, 3, 11, 7, 5]
+
+    def normalized(v):
+        length = np.sqrt(f32(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]))
+        return (v / length).astype(f32)
+
+    for _ in range(level):
+        new_verts, new_idx, lookup = [], [], {}
+
+        def add(v):
+            key = v.tobytes()
+            if key not in lookup:
+                lookup[key] = len(new_verts)
+                new_verts.append(v)
+            return lookup[key]
+
+        for k in range(0, len(idx), 3):
+            v0, v1, v2 = verts[idx[k]], verts[idx[k + 1]], verts[idx[k + 2]]
+            v01, v12, v02 = normalized(v0 + v1), normalized(v1 + v2), normalized(v0 + v2)
+            i0, i1, i2, i3, i4, i5 = add(v0), add(v1), add(v2), add(v01), add(v12), add(v02)
+            new_idx += [i0, i3, i5, i3, i1, i4, i5, i4, i2, i3, i4, i5]
+        verts, idx = new_verts, new_idx
+    v = np.stack(verts).astype(np.float32) * np.float32(radius)
+    return v.astype(np.float32), np.array(idx, np.int32).reshape(-1, 3)
+
+
+# ---------------------------------------------------------------- terrain
+def _value_noise(rng, freq, x, z):
+    lattice = rng.random((freq + 2, freq + 2))
+    fx, fz = x * freq, z * freq
+    ix, iz = np.floor(fx).astype(np.int64), np.floor(fz).astype(np.int64)
+    tx, tz = fx - ix, fz - iz
+    sx, sz = tx * tx * (3 - 2 * tx), tz * tz * (3 - 2 * tz)
+    a = lattice[ix, iz] * (1 - sx) + lattice[ix + 1, iz] * sx
+    b = lattice[ix, iz + 1] * (1 - sx) + lattice[ix + 1, iz + 1] * sx
+    return a * (1 - sz) + b * sz
+
+
+def fbm_terrain(seed, grid=1024, octaves=6, amplitude=0.1, base_freq=4):
+    rng = np.random.default_rng(seed)
+    lin = np.linspace(0.0, 1.0, grid + 1)
+    x, z = np.meshgrid(lin, lin, indexing="ij")
+    h = np.zeros_like(x)
+    norm = 0.0
+    for k in range(octaves):
+        w = 0.5 ** k
+        h += w * (_value_noise(rng, base_freq * 2 ** k, x, z) - 0.5)
+        norm += w
+    h = amplitude * h / norm
+    verts = np.stack([x, h, z], axis=-1).reshape(-1, 3).astype(np.float32)
+    n = grid + 1
+    i = np.arange(grid)
+    ii, jj = np.meshgrid(i, i, indexing="ij")
+    v00 = (ii * n + jj).reshape(-1)
+    v10 = ((ii + 1) * n + jj).reshape(-1)
+    v01 = (ii * n + jj + 1).reshape(-1)
+    v11 = ((ii + 1) * n + jj + 1).reshape(-1)
+    tris = np.empty((grid * grid * 2, 3), np.int32)
+    tris[0::2] = np.stack([v00, v10, v11], axis=1)
+    tris[1::2] = np.stack([v00, v11, v01], axis=1)
+    return verts, tris
+
+
+def raycast_scene(seed=1, grid=1024, spheres=64, level=4, build=True, threads=0):
+    """The ray-cast benchmark scene: ~2.42M triangles at grid=1024, 64 spheres."""
+    rng = np.random.default_rng(seed + 1000)
+    s = FlatScene()
+    tv, ti = fbm_terrain(seed, grid)
+    s.meshes.append(Mesh(tv, ti))
+    objects = [make_object(0)]
+    lo = tv.min(axis=0)
+    hi = tv.max(axis=0)
+    sv, si = icosphere(1.0, level)
+    for k in range(spheres):
+        r = np.float32(rng.uniform(0.01, 0.04))
+        c = rng.uniform([lo[0], lo[1], lo[2]], [hi[0], hi[1] + 0.1, hi[2]]).astype(np.float32)
+        s.meshes.append(Mesh(sv * r, si))
+        m = np.array([1, 0, 0, c[0], 0, 1, 0, c[1], 0, 0, 1, c[2]], np.float32)
+        w = np.array([1, 0, 0, -c[0], 0, 1, 0, -c[1], 0, 0, 1, -c[2]], np.float32)
+        objects.append(make_object(k + 1, m, w))
+    s.objects = np.array(objects)
+    if build:
+        s.build_kdtrees(threads)
+    return s
+
+
+def scene_box(s):
+    lo = s.scene_bounds[:3].astype(np.float64)
+    hi = s.scene_bounds[3:].astype(np.float64)
+    return lo, hi
+
+
+def _uniform_sphere(rng, n):
+    u0 = rng.random(n)
+    u1 = rng.random(n)
+    z = 1.0 - 2.0 * u0
+    r = np.sqrt(np.maximum(0.0, 1.0 - z * z))
+    phi = 2.0 * math.pi * u1
+    return np.stack([r * np.cos(phi), r * np.sin(phi), z], axis=1)
+
+
+def random_rays(lo, hi, n, seed, tmax=np.inf):
+    """(n, 8) float32 yar_ray records: origin, tmax, direction, pad."""
+    rng = np.random.default_rng(seed)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(lo, hi, size=(n, 3))
+    rays[:, 3] = tmax
+    rays[:, 4:7] = _uniform_sphere(rng, n)
+    return rays
+
+
+def random_shadow_rays(lo, hi, n, seed):
+    rng = np.random.default_rng(seed)
+    rays = np.zeros((n, 8), np.float32)
+    rays[:, 0:3] = rng.uniform(lo, hi, size=(n, 3))
+    rays[:, 4:7] = _uniform_sphere(rng, n)
+    diag = float(np.linalg.norm(np.asarray(hi) - np.asarray(lo)))
+    rays[:, 3] = rng.random(n) * diag
+    return rays
+
+
+# ---------------------------------------------------------------- Cornell box
+def _quad(p0, p1, p2, p3):
+    return np.array([p0, p1, p2, p3], np.float32), np.array([[0, 1, 2], [0, 2, 3]], np.int32)
+
+
+def _box(center, size, angle_deg):
+    cx, cz = center[0], center[2]
+    sx, sy, sz = size
+    a = math.radians(angle_deg)
+    ca, sa = math.cos(a), math.sin(a)
+    corners = []
+    for y in (0.0, sy):
+        for (dx, dz) in ((-1, -1), (1, -1), (1, 1), (-1, 1)):
+            x = dx * sx / 2
+            z = dz * sz / 2
+            corners.append((cx + ca * x + sa * z, y, cz - sa * x + ca * z))
+    v = np.array(corners, np.float32)
+    idx = np.array([[0, 2, 1], [0, 3, 2],        # bottom
+                    [4, 5, 6], [4, 6, 7],        # top
+                    [0, 1, 5], [0, 5, 4],
+                    [1, 2, 6], [1, 6, 5],
+                    [2, 3, 7], [2, 7, 6],
+                    [3, 0, 4], [3, 4, 7]], np.int32)
+    return v, idx
+
+
+def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0):
+    """pbrt-v3 text of the seeded Cornell box (34 triangles + a quad light)."""
+    rng = np.random.default_rng(seed)
+    k = int(math.ceil(math.sqrt(spp)))
+    shapes = []
+    walls = [
+        _quad((-1, 0, -1), (1, 0, -1), (1, 0, 1), (-1, 0, 1)),      # floor
+        _quad((-1, 2, -1), (-1, 2, 1), (1, 2, 1), (1, 2, -1)),      # ceiling
+        _quad((-1, 0, -1), (-1, 2, -1), (1, 2, -1), (1, 0, -1)),    # back
+        _quad((-1, 0, -1), (-1, 0, 1), (-1, 2, 1), (-1, 2, -1)),    # left
+        _quad((1, 0, -1), (1, 2, -1), (1, 2, 1), (1, 0, 1)),        # right
+    ]
+    for v, i in walls:
+        shapes.append((v, i, rng.uniform(0.2, 0.8, 3)))
+    a0, a1 = rng.uniform(0.0, 30.0, 2)
+    shapes.append(_box((0.35, 0, 0.3), (0.6, 0.6, 0.6), a0) + (rng.uniform(0.2, 0.8, 3),))
+    shapes.append(_box((-0.35, 0, -0.35), (0.6, 1.2, 0.6), a1) + (rng.uniform(0.2, 0.8, 3),))
+    h = 0.125
+    light = _quad((-h, 1.98, -h), (h, 1.98, -h), (h, 1.98, h), (-h, 1.98, h))
+
+    def fmt(a):
+        return " ".join("%.9g" % x for x in np.asarray(a).reshape(-1))
+
+    out = [
+        "LookAt 0 1 3.5  0 1 0  0 1 0",
+        'Camera "perspective" "float fov" [40]',
+        'Film "image" "integer xresolution" [%d] "integer yresolution" [%d] "string filename" "cornell.exr"'
+        % (width, height),
+        'Sampler "stratified" "integer xsamples" [%d] "integer ysamples" [%d]' % (k, k),
+        'Integrator "path" "integer maxdepth" [%d]' % maxdepth,
+        'PixelFilter "box"',
+        "WorldBegin",
+    ]
+    for v, i, albedo in shapes:
+        out += ["AttributeBegin",
+                '  Material "matte" "rgb Kd" [%s]' % fmt(albedo),
+                '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(i), fmt(v)),
+                "AttributeEnd"]
+    out += ["AttributeBegin",
+            '  AreaLightSource "diffuse" "rgb L" [%s]' % fmt([light_radiance] * 3),
+            '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(light[1]), fmt(light[0])),
+            "AttributeEnd",
+            "WorldEnd", ""]
+    return "\n".join(out)
