@@ -439,8 +439,923 @@ void oracle_pixel_samples(uint32_t stream_id, int nx, int ny, int n1d, int n2d, 
     free(tmp);
 }
 
-int oracle_render(const yar_flat_scene* scene, float* rgb, double* variance, int32_t row_begin, int32_t row_end,
+
+/* ======================================================================
+ * Render path: camera, shading context, BSDFs, MIS direct lighting from
+ * rectangular lights, the path loop and the film, restated from
+ * src/ref/{camera,shading_context,bsdf,scattering,sampling,direct_lighting,
+ * path_tracing,reference_renderer,film}.cpp and src/lib/math.cpp.
+ * ==================================================================== */
+#include <pthread.h>
+
+typedef struct v3 { float x, y, z; } v3;
+typedef struct col { float r, g, b; } col;
+
+static inline v3 mk3(float x, float y, float z) { v3 v = {x, y, z}; return v; }
+static inline v3 add3(v3 a, v3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+static inline v3 sub3(v3 a, v3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+static inline v3 mul3s(v3 v, float t) { return mk3(v.x * t, v.y * t, v.z * t); }   /* Vector3 * float */
+static inline v3 div3s(v3 v, float t) { return mk3(v.x / t, v.y / t, v.z / t); }   /* Vector3 / float */
+static inline v3 neg3(v3 v) { return mk3(-v.x, -v.y, -v.z); }
+static inline float dot3(v3 a, v3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+static inline v3 cross3(v3 a, v3 b) {
+    return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+static inline float len2_3(v3 v) { return v.x * v.x + v.y * v.y + v.z * v.z; }
+static inline float len3(v3 v) { return sqrtf(len2_3(v)); }
+static inline v3 norm3(v3 v) { return div3s(v, len3(v)); }
+static inline float get3(v3 v, int i) { return i == 0 ? v.x : (i == 1 ? v.y : v.z); }
+static inline v3 ld3(const float* p) { return mk3(p[0], p[1], p[2]); }
+
+static inline col mkc(float r, float g, float b) { col c = {r, g, b}; return c; }
+static inline col addc(col a, col b) { return mkc(a.r + b.r, a.g + b.g, a.b + b.b); }
+static inline col mulc(col a, col b) { return mkc(a.r * b.r, a.g * b.g, a.b * b.b); }
+static inline col mulcs(col c, float k) { return mkc(c.r * k, c.g * k, c.b * k); }   /* ColorRGB * float */
+static inline col divc(col a, col b) { return mkc(a.r / b.r, a.g / b.g, a.b / b.b); }
+static inline col subc(col a, col b) { return mkc(a.r - b.r, a.g - b.g, a.b - b.b); }
+static inline col sqrtc(col c) { return mkc(sqrtf(c.r), sqrtf(c.g), sqrtf(c.b)); }
+static inline int blackc(col c) { return c.r == 0 && c.g == 0 && c.b == 0; }
+static inline float fmaxf_std(float a, float b) { return (a < b) ? b : a; }       /* std::max */
+static inline float fminf_std(float a, float b) { return (b < a) ? b : a; }       /* std::min */
+static inline float maxcomp(col c) { return fmaxf_std(c.r, fmaxf_std(c.g, c.b)); }
+static inline col ldc(const float* p) { return mkc(p[0], p[1], p[2]); }
+
+#define PI_F 3.14159265f              /* src/lib/math.h:7 */
+static const float PI_INV_F = 1.f / PI_F;
+
+static v3 xform_point(const float m[12], v3 p) {
+    float in[3] = {p.x, p.y, p.z}, out[3];
+    transform_point(m, in, out);
+    return mk3(out[0], out[1], out[2]);
+}
+static v3 xform_vector(const float m[12], v3 v) {
+    float in[3] = {v.x, v.y, v.z}, out[3];
+    transform_vector(m, in, out);
+    return mk3(out[0], out[1], out[2]);
+}
+
+/* barycentric_interpolate, src/lib/math.h:146-153 */
+static v3 bary3(const v3 p[3], const float b[3]) {
+    return add3(add3(mul3s(p[0], b[0]), mul3s(p[1], b[1])), mul3s(p[2], b[2]));
+}
+
+/* coordinate_system_from_vector, src/lib/math.cpp:21-25 */
+static void coordinate_system(v3 v, v3* v1, v3* v2) {
+    *v1 = (fabsf(v.x) > fabsf(v.y)) ? mk3(-v.z, 0, v.x) : mk3(0, -v.z, v.y);
+    *v1 = div3s(*v1, len3(*v1));
+    *v2 = cross3(v, *v1);
+}
+
+/* project_vector_onto_plane_and_get_direction, src/lib/math.cpp:33-39 */
+static v3 project_direction(v3 v, v3 n) {
+    v3 t = cross3(v, n);
+    v3 d = cross3(n, t);
+    return norm3(d);
+}
+
+/* reflect / refract, src/lib/math.h:108-125 */
+static v3 reflect3(v3 w, v3 n) { return sub3(mul3s(n, 2.f * dot3(w, n)), w); }
+static int refract3(v3 wi, v3 n, float eta, v3* wt) {
+    float cos_i = dot3(wi, n);
+    float sin_t2 = eta * eta * fmaxf_std(0.f, 1.f - cos_i * cos_i);
+    if (sin_t2 >= 1.f) return 0;
+    float cos_t = sqrtf(1.f - sin_t2);
+    *wt = add3(mul3s(wi, -eta), mul3s(n, eta * cos_i - cos_t));
+    return 1;
+}
+
+static inline int f2i(float f) { int i; memcpy(&i, &f, 4); return i; }
+static inline float i2f(int i) { float f; memcpy(&f, &i, 4); return f; }
+
+/* offset_ray_origin_in_both_directions, src/lib/math.cpp:81-120 */
+static void offset_origins(v3 p, v3 n, v3* pos, v3* neg) {
+    const float int_scale = 256.f, origin = 1.0f / 32.0f, float_scale = 1.0f / 65536.0f;
+    const float pc[3] = {p.x, p.y, p.z}, nc[3] = {n.x, n.y, n.z};
+    float po[3], ne[3];
+    for (int k = 0; k < 3; k++) {
+        int di = (int)(int_scale * nc[k]);
+        int i1 = f2i(pc[k]) - di, i2 = f2i(pc[k]) + di;
+        po[k] = i2f(pc[k] < 0 ? i1 : i2);
+        ne[k] = i2f(pc[k] < 0 ? i2 : i1);
+        if (fabsf(pc[k]) < origin) {
+            float d = float_scale * nc[k];
+            po[k] = pc[k] + d;
+            ne[k] = pc[k] - d;
+        }
+    }
+    *pos = mk3(po[0], po[1], po[2]);
+    *neg = mk3(ne[0], ne[1], ne[2]);
+}
+
+typedef struct shading_ctx {
+    v3 wo, position, geometric_normal, normal, dpdu_shading;
+    v3 origin_pos, origin_neg;
+    int flipped;
+    uint32_t material_type;
+    int material_index;
+    uint32_t light_type;
+    int light_index;
+} shading_ctx;
+
+/* adjust_shading_normal, src/ref/shading_context.cpp:17-63 */
+static void adjust_shading_normal(v3 wo, v3 ng, v3* n) {
+    v3 R = reflect3(wo, *n);
+    float a = dot3(R, ng);
+    if (a >= 0.f) return;
+    const float cos_threshold = 0.0017453f;
+    if (dot3(wo, ng) < cos_threshold) { *n = ng; return; }
+    float b = dot3(*n, ng);
+    v3 tangent;
+    if (b > 1e-4f) {
+        float dist = fabsf(a) / b;
+        tangent = add3(R, mul3s(*n, dist));
+        tangent = div3s(tangent, len3(tangent));
+    } else {
+        tangent = *n;
+    }
+    tangent = add3(tangent, mul3s(ng, 1e-4f));
+    *n = norm3(add3(wo, tangent));
+}
+
+/* Shading_Context::initialize_local_geometry + init_from_triangle_mesh_intersection
+ * (src/ref/shading_context.cpp:65-172, :188-240) for constant-parameter
+ * materials (no bump, no differentials). */
+static void init_shading(const yar_flat_scene* s, v3 ray_d, uint32_t object_index, uint32_t tri, const float b[3],
+                         shading_ctx* sc) {
+    const yar_object_desc* obj = &s->objects[object_index];
+    const yar_mesh_desc* m = &s->meshes[obj->mesh_index];
+    memset(sc, 0, sizeof(*sc));
+    sc->wo = neg3(norm3(ray_d));
+    const int32_t* vi = m->indices + 3 * (size_t)tri;
+    v3 p[3] = {ld3(m->vertices + 3 * (size_t)vi[0]), ld3(m->vertices + 3 * (size_t)vi[1]),
+               ld3(m->vertices + 3 * (size_t)vi[2])};
+    v3 position = bary3(p, b);
+    v3 gn = norm3(cross3(sub3(p[1], p[0]), sub3(p[2], p[0])));
+    if (m->reverse_geometric_normal_orientation) gn = neg3(gn);
+    v3 normal = gn;
+    if (m->normals) {
+        v3 n[3] = {ld3(m->normals + 3 * (size_t)vi[0]), ld3(m->normals + 3 * (size_t)vi[1]),
+                   ld3(m->normals + 3 * (size_t)vi[2])};
+        v3 in = bary3(n, b);
+        if (len2_3(in) != 0) normal = norm3(in);
+    }
+    int has_uv = 0;
+    v3 dpdu = mk3(0, 0, 0);
+    if (m->uvs) {
+        has_uv = 1;
+        const float* u0 = m->uvs + 2 * (size_t)vi[0];
+        const float* u1 = m->uvs + 2 * (size_t)vi[1];
+        const float* u2 = m->uvs + 2 * (size_t)vi[2];
+        float a00 = u1[0] - u0[0], a01 = u1[1] - u0[1], a10 = u2[0] - u0[0], a11 = u2[1] - u0[1];
+        v3 bp0 = sub3(p[1], p[0]), bp1 = sub3(p[2], p[0]);
+        /* solve_linear_system_2x2 (src/lib/math.cpp:8-16) */
+        float det = a00 * a11 - a01 * a10;
+        if (det != 0.f) {
+            float inv_det = 1.f / det;
+            dpdu = mul3s(sub3(mul3s(bp0, a11), mul3s(bp1, a01)), inv_det);
+        }
+        if (fabsf(det) < 1e-9f) {
+            v3 dummy;
+            coordinate_system(gn, &dpdu, &dummy);
+        }
+    }
+    /* to world space */
+    position = xform_point(obj->object_to_world, position);
+    normal = xform_vector(obj->object_to_world_normal, normal);
+    normal = div3s(normal, len3(normal));
+    gn = xform_vector(obj->object_to_world_normal, gn);
+    gn = div3s(gn, len3(gn));
+    dpdu = xform_vector(obj->object_to_world, dpdu);
+    if (dot3(normal, gn) == 0.f) gn = normal;
+    if (dot3(gn, sc->wo) < 0) gn = neg3(gn);
+    if (dot3(normal, gn) < 0) { normal = neg3(normal); sc->flipped = 1; }
+    offset_origins(position, gn, &sc->origin_pos, &sc->origin_neg);
+    adjust_shading_normal(sc->wo, gn, &normal);
+    v3 dpdu_shading;
+    if (!has_uv) {
+        v3 dummy;
+        coordinate_system(normal, &dpdu_shading, &dummy);
+    } else if (fabsf(dot3(normal, gn) - 1.f) < 1e-6f) {
+        dpdu_shading = dpdu;
+    } else {
+        dpdu_shading = mul3s(project_direction(dpdu, normal), len3(dpdu));
+    }
+    sc->position = position;
+    sc->geometric_normal = gn;
+    sc->normal = normal;
+    sc->dpdu_shading = dpdu_shading;
+    sc->material_type = obj->material_type;
+    sc->material_index = obj->material_index;
+    sc->light_type = obj->area_light_type;
+    sc->light_index = obj->area_light_index;
+}
+
+/* get_ray_origin_using_control_direction / _point, src/ref/shading_context.cpp:405-417 */
+static v3 origin_for_direction(const shading_ctx* sc, v3 dir) {
+    return dot3(dir, sc->geometric_normal) > 0.f ? sc->origin_pos : sc->origin_neg;
+}
+static v3 origin_for_point(const shading_ctx* sc, v3 point) {
+    return origin_for_direction(sc, sub3(point, sc->position));
+}
+
+/* ---------------- BSDFs (src/ref/bsdf.cpp, src/ref/scattering.cpp, src/ref/sampling.cpp) */
+typedef struct bsdf_t {
+    uint32_t type;
+    v3 n, t, bt;  /* normal, tangent, bitangent */
+    int reflection, transmission;
+    col reflectance, transmittance;
+    float alpha_x, alpha_y, alpha;  /* metal: alpha_x/y; glass: alpha */
+    float eta_i_metal;
+    col eta_t, k_t;
+    float eta_o, eta_i;             /* glass */
+} bsdf_t;
+
+static float pbrt3_roughness_to_alpha(float roughness) {
+    /* src/ref/scattering.cpp:240-251 */
+    roughness = fmaxf_std(roughness, 1e-3f);
+    float x = logf(roughness);
+    return 1.621420000f + 0.819955000f * x + 0.173400000f * x * x + 0.017120100f * x * x * x +
+           0.000640711f * x * x * x * x;
+}
+static float roughness_to_alpha(const yar_flat_scene* s, float r, int no_remap) {
+    if (no_remap) return r;
+    if (s->config.pbrt3_scene) return pbrt3_roughness_to_alpha(r);
+    return r * r;
+}
+
+static v3 local_to_world(const bsdf_t* f, v3 l) {
+    return mk3(f->t.x * l.x + f->bt.x * l.y + f->n.x * l.z, f->t.y * l.x + f->bt.y * l.y + f->n.y * l.z,
+               f->t.z * l.x + f->bt.z * l.y + f->n.z * l.z);
+}
+static v3 world_to_local(const bsdf_t* f, v3 w) { return mk3(dot3(w, f->t), dot3(w, f->bt), dot3(w, f->n)); }
+
+static int make_bsdf(const yar_flat_scene* s, const shading_ctx* sc, bsdf_t* f) {
+    memset(f, 0, sizeof(*f));
+    f->n = sc->normal;
+    f->bt = norm3(cross3(sc->normal, sc->dpdu_shading));
+    f->t = cross3(f->bt, sc->normal);
+    const yar_material_desc* m = &s->materials[sc->material_index];
+    f->type = sc->material_type;
+    if (f->type == YAR_MATERIAL_DIFFUSE) {
+        f->reflection = 1;
+        f->reflectance = ldc(m->reflectance);
+    } else if (f->type == YAR_MATERIAL_METAL) {
+        f->reflection = 1;
+        f->alpha_x = roughness_to_alpha(s, m->u_roughness, m->roughness_is_alpha);
+        f->alpha_y = roughness_to_alpha(s, m->v_roughness, m->roughness_is_alpha);
+        f->eta_i_metal = m->eta_i;
+        f->eta_t = ldc(m->eta);
+        f->k_t = ldc(m->k);
+    } else if (f->type == YAR_MATERIAL_GLASS) {
+        f->reflection = f->transmission = 1;
+        f->reflectance = ldc(m->reflectance);
+        f->transmittance = ldc(m->transmittance);
+        f->alpha = roughness_to_alpha(s, m->u_roughness, m->roughness_is_alpha);
+        int enter = !sc->flipped;
+        f->eta_o = enter ? 1.f : m->index_of_refraction;
+        f->eta_i = enter ? m->index_of_refraction : 1.f;
+    } else {
+        return YAR_ERR_UNSUPPORTED;
+    }
+    return YAR_OK;
+}
+
+static v3 sample_hemisphere_cosine(float u0, float u1) {
+    float z = sqrtf(1.f - u0);
+    float r = sqrtf(u0);
+    float phi = 2.f * PI_F * u1;
+    return mk3(r * cosf(phi), r * sinf(phi), z);
+}
+
+static float dielectric_fresnel(float cos_i, float eta) {
+    cos_i = fminf_std(fabsf(cos_i), 1.f);
+    float sin_i = sqrtf(1.f - cos_i * cos_i);
+    float sin_t = (1.f / eta) * sin_i;
+    if (sin_t >= 1.f) return 1.f;
+    float cos_t = sqrtf(1.f - sin_t * sin_t);
+    float Rp = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
+    float Rs = (cos_i - eta * cos_t) / (cos_i + eta * cos_t);
+    return 0.5f * (Rp * Rp + Rs * Rs);
+}
+
+static col conductor_fresnel(float cos_i, float eta_i, col eta_t, col k_t) {
+    cos_i = fabsf(cos_i < -1.f ? -1.f : (cos_i > 1.f ? 1.f : cos_i));
+    float c2 = cos_i * cos_i;
+    float s2 = 1.f - c2;
+    col eta = mulcs(eta_t, 1.f / eta_i);           /* ColorRGB / float = c * (1/k) */
+    col k = mulcs(k_t, 1.f / eta_i);
+    col eta2 = mulc(eta, eta);
+    col k2 = mulc(k, k);
+    col t0 = subc(subc(eta2, k2), mkc(s2, s2, s2));
+    col a2b2 = sqrtc(addc(mulc(t0, t0), mulc(mulcs(eta2, 4.f), k2)));
+    col t1 = addc(a2b2, mkc(c2, c2, c2));
+    col a = sqrtc(mulcs(addc(a2b2, t0), 0.5f));
+    col t2 = mulcs(a, 2.f * cos_i);
+    col Rs = divc(subc(t1, t2), addc(t1, t2));
+    col t3 = addc(mulcs(a2b2, c2), mkc(s2 * s2, s2 * s2, s2 * s2));
+    col t4 = mulcs(t2, s2);
+    col Rp = divc(mulc(Rs, subc(t3, t4)), addc(t3, t4));
+    return mulcs(addc(Rp, Rs), 0.5f);
+}
+
+static float ggx_D(v3 wh, v3 n, float alpha) {
+    float c = dot3(wh, n);
+    if (c <= 0.f) return 0.f;
+    float c2 = c * c;
+    float a2 = alpha * alpha;
+    float k = c2 * (a2 - 1) + 1;
+    return a2 / (PI_F * k * k);
+}
+static float clamp1(float x) { return x < -1.f ? -1.f : (x > 1.f ? 1.f : x); }
+static float ggx_D_aniso(v3 wh, float ax, float ay) {
+    float c = clamp1(wh.z);
+    float c2 = c * c;
+    float s2 = 1.f - c2;
+    float s2inv = 1.f / s2;
+    float cos2_phi = (s2 == 0.f) ? 1.f : (wh.x * wh.x) * s2inv;
+    float sin2_phi = (s2 == 0.f) ? 0.f : (wh.y * wh.y) * s2inv;
+    float k = c2 + s2 * (cos2_phi / (ax * ax) + sin2_phi / (ay * ay));
+    return 1.f / (PI_F * ax * ay * k * k);
+}
+static float ggx_lambda(v3 v, v3 n, float alpha) {
+    float c = dot3(v, n);
+    float c2 = c * c;
+    float tan2 = fmaxf_std(0.f, (1.f - c2) / c2);
+    return 0.5f * (-1.f + sqrtf(1.f + alpha * alpha * tan2));
+}
+static float ggx_lambda_aniso(v3 v, float ax, float ay) {
+    float c = clamp1(v.z);
+    float c2 = c * c;
+    float s2 = 1.f - c2;
+    float tan2 = s2 / c2;
+    float s2inv = 1.f / s2;
+    float cos2_phi = (s2 == 0.f) ? 1.f : (v.x * v.x) * s2inv;
+    float sin2_phi = (s2 == 0.f) ? 0.f : (v.y * v.y) * s2inv;
+    float alpha2 = cos2_phi * ax * ax + sin2_phi * ay * ay;
+    return 0.5f * (-1.f + sqrtf(1.f + alpha2 * tan2));
+}
+static float ggx_G(v3 wi, v3 wo, v3 n, float a) { return 1.f / (1.f + ggx_lambda(wi, n, a) + ggx_lambda(wo, n, a)); }
+static float ggx_G1(v3 v, v3 n, float a) { return 1.f / (1.f + ggx_lambda(v, n, a)); }
+static float ggx_G_aniso(v3 wi, v3 wo, float ax, float ay) {
+    return 1.f / (1.f + ggx_lambda_aniso(wi, ax, ay) + ggx_lambda_aniso(wo, ax, ay));
+}
+static float ggx_G1_aniso(v3 v, float ax, float ay) { return 1.f / (1.f + ggx_lambda_aniso(v, ax, ay)); }
+
+/* GGX_sample_visible_microfacet_normal, src/ref/sampling.cpp:310-335 */
+static v3 ggx_sample_vndf(float u0, float u1, v3 wo, float ax, float ay) {
+    v3 N = norm3(mk3(ax * wo.x, ay * wo.y, wo.z));
+    float len_sq = N.x * N.x + N.y * N.y;
+    v3 T1 = len_sq > 0.f ? div3s(mk3(-N.y, N.x, 0), sqrtf(len_sq)) : mk3(1, 0, 0);
+    v3 T2 = cross3(N, T1);
+    float r = sqrtf(u0);
+    float phi = 2.f * PI_F * u1;
+    float t1 = r * cosf(phi);
+    float t2 = r * sinf(phi);
+    float s = 0.5f * (1.f + N.z);
+    t2 = (1.f - s) * sqrtf(1.f - t1 * t1) + s * t2;
+    v3 nh = add3(add3(mul3s(T1, t1), mul3s(T2, t2)), mul3s(N, sqrtf(fmaxf_std(0.f, 1.f - t1 * t1 - t2 * t2))));
+    return norm3(mk3(ax * nh.x, ay * nh.y, fmaxf_std(1e-6f, nh.z)));
+}
+static float vndf_pdf(v3 wo, v3 wh, v3 n, float alpha) {
+    float G1 = ggx_G1(wo, n, alpha);
+    float D = ggx_D(wh, n, alpha);
+    return G1 * D * fmaxf_std(0.f, dot3(wo, wh)) / dot3(wo, n);
+}
+static float vndf_pdf_aniso(v3 wo, v3 wh, float ax, float ay) {
+    float G1 = ggx_G1_aniso(wo, ax, ay);
+    float D = ggx_D_aniso(wh, ax, ay);
+    return G1 * D * fmaxf_std(0.f, dot3(wo, wh)) / wo.z;
+}
+static float refl_pdf(v3 wo, v3 wh, v3 n, float a) { return vndf_pdf(wo, wh, n, a) / (4 * dot3(wh, wo)); }
+static float refl_pdf_aniso(v3 wo, v3 wh, float ax, float ay) {
+    return vndf_pdf_aniso(wo, wh, ax, ay) / (4 * dot3(wh, wo));
+}
+static float trans_pdf(v3 wo, v3 wi, v3 wh, v3 n, float a, float eta_o, float eta_i) {
+    float wh_pdf = vndf_pdf(wo, wh, n, a);
+    float denom = eta_o * dot3(wo, wh) + eta_i * dot3(wi, wh);
+    float dwh = eta_i * eta_i * fabsf(dot3(wi, wh)) / (denom * denom);
+    return wh_pdf * dwh;
+}
+static v3 refraction_half(float eta_o, v3 wo, float eta_i, v3 wi, v3 n) {
+    v3 wh = neg3(norm3(add3(mul3s(wo, eta_o), mul3s(wi, eta_i))));
+    if (dot3(wh, n) < 0.f) wh = neg3(wh);
+    return wh;
+}
+
+static col bsdf_evaluate(const bsdf_t* f, v3 wo, v3 wi) {
+    if (f->type == YAR_MATERIAL_DIFFUSE) return mulcs(f->reflectance, PI_INV_F);
+    if (f->type == YAR_MATERIAL_METAL) {
+        v3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
+        v3 wh_l = norm3(add3(wo_l, wi_l));
+        float cos_i = dot3(wi_l, wh_l);
+        col F = conductor_fresnel(cos_i, f->eta_i_metal, f->eta_t, f->k_t);
+        float G = ggx_G_aniso(wi_l, wo_l, f->alpha_x, f->alpha_y);
+        float D = ggx_D_aniso(wh_l, f->alpha_x, f->alpha_y);
+        return mulcs(F, (G * D) / (4.f * wo_l.z * wi_l.z));
+    }
+    /* rough glass */
+    int same = dot3(wo, f->n) * dot3(wi, f->n) > 0.f;
+    if (same) {
+        v3 wh = norm3(add3(wo, wi));
+        float cos_i = dot3(wi, wh);
+        float F = dielectric_fresnel(cos_i, f->eta_i / f->eta_o);
+        float G = ggx_G(wi, wo, f->n, f->alpha);
+        float D = ggx_D(wh, f->n, f->alpha);
+        float base = (F * G * D) / (4.f * dot3(wo, f->n) * dot3(wi, f->n));
+        return mulcs(f->reflectance, base);
+    }
+    v3 wh = refraction_half(f->eta_o, wo, f->eta_i, wi, f->n);
+    float wo_wh = dot3(wo, wh), wi_wh = dot3(wi, wh);
+    if (wo_wh * wi_wh > 0.f) return mkc(0, 0, 0);
+    float cos_i = dot3(wi, wh);
+    float F = dielectric_fresnel(cos_i, f->eta_o / f->eta_i);
+    if (F == 1.f) return mkc(0, 0, 0);
+    float G = ggx_G(wi, wo, f->n, f->alpha);
+    float D = ggx_D(wh, f->n, f->alpha);
+    float wo_n = dot3(wo, f->n), wi_n = dot3(wi, f->n);
+    float k = fabsf((wo_wh * wi_wh) / (wo_n * wi_n));
+    float k2 = f->eta_o * wo_wh + f->eta_i * wi_wh;
+    float base = (f->eta_o * f->eta_o * k * G * D * (1.f - F)) / (k2 * k2);
+    return mulcs(f->transmittance, base);
+}
+
+static float glass_reflection_probability(const bsdf_t* f, float fresnel) {
+    float max_r = maxcomp(f->reflectance), max_t = maxcomp(f->transmittance);
+    float ratio = max_r / (max_r + max_t);
+    float r = fresnel * ratio;
+    float t = (1.f - fresnel) * (1 - ratio);
+    return ((r + t) == 0) ? 0.f : r / (r + t);
+}
+
+static float bsdf_pdf(const bsdf_t* f, v3 wo, v3 wi) {
+    if (f->type == YAR_MATERIAL_DIFFUSE) return dot3(f->n, wi) / PI_F;
+    if (f->type == YAR_MATERIAL_METAL) {
+        v3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
+        v3 wh_l = norm3(add3(wo_l, wi_l));
+        return refl_pdf_aniso(wo_l, wh_l, f->alpha_x, f->alpha_y);
+    }
+    int same = dot3(wo, f->n) * dot3(wi, f->n) > 0.f;
+    if (same) {
+        v3 wh = norm3(add3(wo, wi));
+        float rp = refl_pdf(wo, wh, f->n, f->alpha);
+        float cos_i = dot3(wi, wh);
+        float fr = dielectric_fresnel(cos_i, f->eta_i / f->eta_o);
+        return rp * glass_reflection_probability(f, fr);
+    }
+    v3 wh = refraction_half(f->eta_o, wo, f->eta_i, wi, f->n);
+    float wo_wh = dot3(wo, wh), wi_wh = dot3(wi, wh);
+    if (wo_wh * wi_wh > 0.f) return 0.f;
+    float cos_t = dot3(wo, wh);
+    float fr = dielectric_fresnel(cos_t, f->eta_i / f->eta_o);
+    float rprob = glass_reflection_probability(f, fr);
+    return trans_pdf(wo, wi, wh, f->n, f->alpha, f->eta_o, f->eta_i) * (1.f - rprob);
+}
+
+/* BSDF::sample for the three BSDFs; returns black when no direction is produced. */
+static col bsdf_sample(const bsdf_t* f, float u0, float u1, float u_scatter, v3 wo, v3* wi, float* pdf) {
+    if (f->type == YAR_MATERIAL_DIFFUSE) {
+        v3 l = sample_hemisphere_cosine(u0, u1);
+        *wi = local_to_world(f, l);
+        *pdf = bsdf_pdf(f, wo, *wi);
+        return bsdf_evaluate(f, wo, *wi);
+    }
+    if (f->type == YAR_MATERIAL_METAL) {
+        v3 wo_l = world_to_local(f, wo);
+        v3 wh_l = ggx_sample_vndf(u0, u1, wo_l, f->alpha_x, f->alpha_y);
+        v3 wi_l = reflect3(wo_l, wh_l);
+        if (wi_l.z <= 0.f) return mkc(0, 0, 0);
+        *wi = local_to_world(f, wi_l);
+        *pdf = refl_pdf_aniso(wo_l, wh_l, f->alpha_x, f->alpha_y);
+        return bsdf_evaluate(f, wo, *wi);
+    }
+    /* rough glass, src/ref/bsdf.cpp:336-370 */
+    v3 wo_l = world_to_local(f, wo);
+    v3 wh_l = ggx_sample_vndf(u0, u1, wo_l, f->alpha, f->alpha);
+    v3 wh = local_to_world(f, wh_l);
+    v3 rwi = reflect3(wo, wh);
+    if (dot3(rwi, f->n) <= 0.f) return mkc(0, 0, 0);
+    float cos_i = dot3(wo, wh);
+    float fresnel = dielectric_fresnel(cos_i, f->eta_i / f->eta_o);
+    float rprob = glass_reflection_probability(f, fresnel);
+    if (u_scatter < rprob) {
+        *wi = rwi;
+    } else {
+        if (!refract3(wo, wh, f->eta_o / f->eta_i, wi)) return mkc(0, 0, 0);
+        if (dot3(*wi, f->n) >= 0.f) return mkc(0, 0, 0);
+    }
+    *pdf = bsdf_pdf(f, wo, *wi);
+    if (*pdf == 0.f) return mkc(0, 0, 0);
+    return bsdf_evaluate(f, wo, *wi);
+}
+
+/* ---------------- ray queries on the flat scene */
+static int trace_closest(const yar_flat_scene* s, v3 o, v3 d, hit_state* hit) {
+    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    hit->t = INFINITY;
+    hit->prim = hit->object = 0xffffffffu;
+    return scene_closest(s, oo, dd, hit, NULL);
+}
+static int trace_any(const yar_flat_scene* s, v3 o, v3 d, float tmax) {
+    const float oo[3] = {o.x, o.y, o.z}, dd[3] = {d.x, d.y, d.z};
+    return scene_any(s, oo, dd, tmax, NULL);
+}
+
+/* mis_power_heuristic, src/ref/direct_lighting.cpp:18-24 */
+static float mis_power(float p1, float p2) {
+    if (p1 == INFINITY) return 1.f;
+    return p1 * p1 / (p1 * p1 + p2 * p2);
+}
+
+/* direct_lighting_from_rectangular_light, src/ref/direct_lighting.cpp:109-194 */
+static col direct_rect(const yar_flat_scene* s, const shading_ctx* sc, const bsdf_t* f, int light_index, float ul0,
+                       float ul1, float ub0, float ub1, float u_scatter) {
+    const yar_rect_light_desc* L = &s->rect_lights[light_index];
+    const float* m = L->light_to_world;
+    v3 light_n = mk3(m[2], m[6], m[10]);
+    col Le = ldc(L->emitted_radiance);
+    col out = mkc(0, 0, 0);
+    int have = 0;
+    {
+        v3 local = mk3(L->size[0] * (ul0 - 0.5f), L->size[1] * (ul1 - 0.5f), 0.0f);
+        v3 lp = xform_point(m, local);
+        v3 position = origin_for_point(sc, lp);
+        v3 lv = sub3(lp, position);
+        float dist = len3(lv);
+        v3 wi = div3s(lv, dist);
+        float lndw = dot3(light_n, neg3(wi));
+        if (lndw > 1e-4f) {
+            float ndw = dot3(sc->normal, wi);
+            int possible = (ndw > 0.f && f->reflection) || (ndw < 0.f && f->transmission);
+            if (possible) {
+                col fv = bsdf_evaluate(f, sc->wo, wi);
+                if (!blackc(fv)) {
+                    if (!trace_any(s, position, wi, dist * (1.f - 1e-5f))) {
+                        float light_pdf = (dist * dist) / (L->size[0] * L->size[1] * lndw);
+                        float bpdf = bsdf_pdf(f, sc->wo, wi);
+                        float w = mis_power(light_pdf, bpdf);
+                        col c = mulcs(mulc(Le, fv), w * fabsf(ndw) / light_pdf);
+                        out = have ? addc(out, c) : addc(mkc(0, 0, 0), c);
+                        have = 1;
+                    }
+                }
+            }
+        }
+    }
+    {
+        v3 wi;
+        float bpdf;
+        col fv = bsdf_sample(f, ub0, ub1, u_scatter, sc->wo, &wi, &bpdf);
+        if (!blackc(fv)) {
+            float lndw = dot3(light_n, neg3(wi));
+            if (lndw > 1e-4f) {
+                v3 position = origin_for_direction(sc, wi);
+                hit_state h;
+                if (trace_closest(s, position, wi, &h) > 0) {
+                    const yar_object_desc* o = &s->objects[h.object];
+                    if (o->area_light_type == YAR_LIGHT_DIFFUSE_RECTANGULAR && o->area_light_index == light_index) {
+                        const yar_mesh_desc* mm = &s->meshes[o->mesh_index];
+                        const int32_t* vi = mm->indices + 3 * (size_t)h.prim;
+                        v3 p[3] = {ld3(mm->vertices + 3 * (size_t)vi[0]), ld3(mm->vertices + 3 * (size_t)vi[1]),
+                                   ld3(mm->vertices + 3 * (size_t)vi[2])};
+                        v3 hp = bary3(p, h.b);
+                        float d = len3(sub3(hp, position));
+                        float light_pdf = (d * d) / (L->size[0] * L->size[1] * lndw);
+                        float w = mis_power(bpdf, light_pdf);
+                        float ndw = dot3(sc->normal, wi);
+                        col c = mulcs(mulc(Le, fv), w * fabsf(ndw) / bpdf);
+                        out = have ? addc(out, c) : addc(mkc(0, 0, 0), c);
+                        have = 1;
+                    }
+                }
+            }
+        }
+    }
+    return out;
+}
+
+typedef struct sampler_view {
+    const float* s1d;   /* this sample's 1d dims */
+    const float* s2d;   /* this sample's 2d dims (pairs) */
+    int n1d, n2d, i1d, i2d;
+    oracle_pcg32* rng;  /* the pixel rng for dims beyond the budget */
+} sampler_view;
+
+static float next1d(sampler_view* sv) {
+    if (sv->i1d < sv->n1d) return sv->s1d[sv->i1d++];
+    return oracle_pcg32_float(sv->rng);
+}
+static void next2d(sampler_view* sv, float* a, float* b) {
+    if (sv->i2d < sv->n2d) {
+        *a = sv->s2d[2 * sv->i2d];
+        *b = sv->s2d[2 * sv->i2d + 1];
+        sv->i2d++;
+        return;
+    }
+    *a = oracle_pcg32_float(sv->rng);
+    *b = oracle_pcg32_float(sv->rng);
+}
+
+/* Camera::generate_ray, src/ref/camera.cpp:16-31 */
+static void camera_ray(const yar_camera_desc* c, float fx, float fy, v3* o, v3* d) {
+    float u = 2.f * (fx / c->image_extent[0]) - 1.f;
+    float v = 2.f * (fy / c->image_extent[1]) - 1.f;
+    float right = u * c->horz_half_dist;
+    float up = -v * c->vert_half_dist;
+    v3 dir = mk3(right, c->z_is_up ? 1.f : up, c->z_is_up ? up : -1.f);
+    dir = div3s(dir, len3(dir));
+    *o = xform_point(c->camera_to_world, mk3(0, 0, 0));
+    *d = xform_vector(c->camera_to_world, dir);
+}
+
+/* trace_path, src/ref/path_tracing.cpp:11-133 (non-delta materials) */
+static int trace_path(const yar_flat_scene* s, v3 ro, v3 rd, sampler_view* sv, col* radiance) {
+    const yar_render_config* cfg = &s->config;
+    const int total_lights = (int)(s->rect_light_count + s->other_light_count);
+    col coeff = mkc(1, 1, 1), L = mkc(0, 0, 0);
+    int bounce = 0;
+    for (;;) {
+        hit_state h;
+        int hit = trace_closest(s, ro, rd, &h);
+        if (hit < 0) return YAR_ERR_CAPACITY;
+        shading_ctx sc;
+        if (hit) init_shading(s, rd, h.object, h.prim, h.b, &sc);
+        if (bounce == 0) {
+            if (hit && sc.light_type == YAR_LIGHT_DIFFUSE_RECTANGULAR)
+                L = addc(L, mulc(coeff, ldc(s->rect_lights[sc.light_index].emitted_radiance)));
+            if (cfg->max_light_bounces == 0) break;
+        }
+        if (!hit || sc.light_type != YAR_LIGHT_NULL) break;
+
+        float u_scatter = next1d(sv);
+        float u_light_index = next1d(sv);
+        float u_scatter_next = next1d(sv);
+        float ul0, ul1, ub0, ub1, un0, un1;
+        next2d(sv, &ul0, &ul1);
+        next2d(sv, &ub0, &ub1);
+        next2d(sv, &un0, &un1);
+
+        if (sc.material_type == YAR_MATERIAL_NULL) return YAR_ERR_UNSUPPORTED;
+        bsdf_t f;
+        int rc = make_bsdf(s, &sc, &f);
+        if (rc != YAR_OK) return rc;
+        /* estimate_direct_lighting_from_single_sample, src/ref/direct_lighting.cpp:522-578 */
+        int light_index = (int)(u_light_index * (float)total_lights);
+        col direct = mulcs(direct_rect(s, &sc, &f, light_index, ul0, ul1, ub0, ub1, u_scatter), (float)total_lights);
+        L = addc(L, mulc(coeff, direct));
+
+        bounce++;
+        if (bounce == cfg->max_light_bounces) break;
+        v3 wi;
+        float pdf;
+        col fv = bsdf_sample(&f, un0, un1, u_scatter_next, sc.wo, &wi, &pdf);
+        if (blackc(fv)) break;
+        coeff = mulc(coeff, mulcs(fv, fabsf(dot3(sc.normal, wi)) / (pdf * 1.f)));
+        ro = origin_for_direction(&sc, wi);
+        rd = wi;
+        if (bounce >= cfg->russian_roulette_bounce_count_threshold) {
+            float u_term = next1d(sv);
+            float max_coeff = fmaxf_std(coeff.r, fmaxf_std(coeff.g, coeff.b));
+            if (max_coeff < cfg->russian_roulette_threshold) {
+                float p_term = fmaxf_std(0.05f, 1.f - max_coeff);
+                if (u_term < p_term) break;
+                coeff = mulcs(coeff, 1.f / (1.f - p_term));
+            }
+        }
+    }
+    *radiance = L;
+    return YAR_OK;
+}
+
+/* ---------------- render_scene with the reference's tiles, merge order and variance */
+#define TILE 64 /* src/ref/film.cpp:5 */
+
+typedef struct film_px { float r, g, b, w; } film_px;
+
+typedef struct render_job {
+    const yar_flat_scene* s;
+    int x0, y0, x1, y1;         /* render region */
+    int sx0, sy0, sx1, sy1;     /* sample region */
+    int tiles_x, tiles_y;
+    int row_begin, row_end;     /* rows of the render region that must be exact */
+    film_px** tile_pixels;      /* per tile: pixel bounds size */
+    int* tile_bounds;           /* per tile: px0, py0, px1, py1 */
+    double* tile_variance;
+    int next_tile;
+    pthread_mutex_t lock;
+    int status;
+} render_job;
+
+static void tile_bounds(const render_job* J, int t, int* sb, int* pb) {
+    int tx = t % J->tiles_x, ty = t / J->tiles_x;
+    const float radius = J->s->config.pixel_filter_radius;
+    sb[0] = J->sx0 + tx * TILE;
+    sb[1] = J->sy0 + ty * TILE;
+    sb[2] = sb[0] + TILE < J->sx1 ? sb[0] + TILE : J->sx1;
+    sb[3] = sb[1] + TILE < J->sy1 ? sb[1] + TILE : J->sy1;
+    int a = (int)ceilf((float)sb[0] - radius - 0.5f), b = (int)ceilf((float)sb[1] - radius - 0.5f);
+    int c = (int)floorf((float)sb[2] + radius - 0.5f) + 1, d = (int)floorf((float)sb[3] + radius - 0.5f) + 1;
+    pb[0] = a > J->x0 ? a : J->x0;
+    pb[1] = b > J->y0 ? b : J->y0;
+    pb[2] = c < J->x1 ? c : J->x1;
+    pb[3] = d < J->y1 ? d : J->y1;
+}
+
+static int render_tile(render_job* J, int t) {
+    const yar_flat_scene* s = J->s;
+    const yar_render_config* cfg = &s->config;
+    int sb[4], pb[4];
+    tile_bounds(J, t, sb, pb);
+    memcpy(&J->tile_bounds[4 * t], pb, sizeof(pb));
+    const int pw = pb[2] - pb[0], ph = pb[3] - pb[1];
+    film_px* px = (film_px*)calloc((size_t)(pw > 0 ? pw : 1) * (ph > 0 ? ph : 1), sizeof(film_px));
+    if (!px) return YAR_ERR_NOMEM;
+    J->tile_pixels[t] = px;
+    const int nx = cfg->x_pixel_sample_count, ny = cfg->y_pixel_sample_count, spp = nx * ny;
+    const int maxb = cfg->max_light_bounces < 10 ? cfg->max_light_bounces : 10;
+    const int n1d = maxb * 4, n2d = maxb * 3; /* src/ref/reference_renderer.cpp:87-99 */
+    float* image = (float*)malloc(sizeof(float) * 2 * spp);
+    float* s1d = (float*)malloc(sizeof(float) * ((size_t)spp * n1d + 1));
+    float* s2d = (float*)malloc(sizeof(float) * (2 * (size_t)spp * n2d + 1));
+    const float radius = cfg->pixel_filter_radius;
+    double var_acc = 0.0;
+    int rc = YAR_OK;
+    for (int y = sb[1]; y < sb[3] && rc == YAR_OK; y++) {
+        if (y < J->row_begin - 1 || y > J->row_end) continue;  /* outside the rows requested (+1 row of filter support) */
+        for (int x = sb[0]; x < sb[2] && rc == YAR_OK; x++) {
+            uint32_t stream = ((uint32_t)x & 0xffffu) | ((uint32_t)y << 16);
+            stream += (uint32_t)cfg->rng_seed_offset;
+            oracle_pcg32 rng;
+            oracle_pcg32_seed(&rng, 0, stream);
+            /* next_pixel with the live rng so draws beyond the budget continue its stream */
+            {
+                const float dx = 1.f / (float)nx, dy = 1.f / (float)ny;
+                float* o = image;
+                for (int j = 0; j < ny; j++)
+                    for (int i = 0; i < nx; i++) {
+                        float a = ((float)i + oracle_pcg32_float(&rng)) * dx;
+                        *o++ = a < ONE_MINUS_EPSILON ? a : ONE_MINUS_EPSILON;
+                        float b = ((float)j + oracle_pcg32_float(&rng)) * dy;
+                        *o++ = b < ONE_MINUS_EPSILON ? b : ONE_MINUS_EPSILON;
+                    }
+                float tmp[2 * 4096];
+                if (spp > 4096) { rc = YAR_ERR_UNSUPPORTED; break; }
+                for (int i = 0; i < n1d; i++) {
+                    stratified_1d(&rng, spp, tmp);
+                    shuffle(tmp, spp, 1, &rng);
+                    for (int k = 0; k < spp; k++) s1d[k * n1d + i] = tmp[k];
+                }
+                for (int i = 0; i < n2d; i++) {
+                    stratified_2d(&rng, nx, ny, tmp);
+                    shuffle(tmp, spp, 2, &rng);
+                    for (int k = 0; k < spp; k++) {
+                        s2d[2 * (k * n2d + i)] = tmp[2 * k];
+                        s2d[2 * (k * n2d + i) + 1] = tmp[2 * k + 1];
+                    }
+                }
+            }
+            double lsum = 0.0, lsq = 0.0;
+            for (int k = 0; k < spp; k++) {
+                float fx = (float)x + image[2 * k], fy = (float)y + image[2 * k + 1];
+                v3 o, d;
+                camera_ray(&s->camera, fx, fy, &o, &d);
+                sampler_view sv = {s1d + (size_t)k * n1d, s2d + 2 * (size_t)k * n2d, n1d, n2d, 0, 0, &rng};
+                col radiance;
+                rc = trace_path(s, o, d, &sv, &radiance);
+                if (rc != YAR_OK) break;
+                float limit = cfg->max_rgb_component_value_of_film_sample;
+                float mc = fmaxf_std(radiance.r, fmaxf_std(radiance.g, radiance.b));
+                if (mc > limit) radiance = mulcs(radiance, limit / mc);
+                if (cfg->film_radiance_scale != 1.f) radiance = mulcs(radiance, cfg->film_radiance_scale);
+                /* Film_Tile::add_sample with the box filter, src/ref/film.cpp:27-50 */
+                int rx0 = (int)ceilf(fx - radius - 0.5f), ry0 = (int)ceilf(fy - radius - 0.5f);
+                int rx1 = (int)floorf(fx + radius - 0.5f) + 1, ry1 = (int)floorf(fy + radius - 0.5f) + 1;
+                if (rx0 < pb[0]) rx0 = pb[0];
+                if (ry0 < pb[1]) ry0 = pb[1];
+                if (rx1 > pb[2]) rx1 = pb[2];
+                if (ry1 > pb[3]) ry1 = pb[3];
+                for (int yy = ry0; yy < ry1; yy++)
+                    for (int xx = rx0; xx < rx1; xx++) {
+                        film_px* p = &px[(yy - pb[1]) * pw + (xx - pb[0])];
+                        p->r += 1.f * radiance.r;
+                        p->g += 1.f * radiance.g;
+                        p->b += 1.f * radiance.b;
+                        p->w += 1.f;
+                    }
+                float lum = 0.2126729f * radiance.r + 0.7151522f * radiance.g + 0.0721750f * radiance.b;
+                lsum += lum;
+                lsq += lum * lum;
+            }
+            if (spp > 1) {
+                double pv = (lsq - lsum * lsum / spp) / (spp * (spp - 1));
+                var_acc += pv > 0.0 ? pv : 0.0;
+            }
+        }
+    }
+    free(image);
+    free(s1d);
+    free(s2d);
+    J->tile_variance[t] = var_acc;
+    return rc;
+}
+
+static void* render_worker(void* arg) {
+    render_job* J = (render_job*)arg;
+    for (;;) {
+        pthread_mutex_lock(&J->lock);
+        int t = J->next_tile++;
+        int stop = J->status != YAR_OK;
+        pthread_mutex_unlock(&J->lock);
+        if (stop || t >= J->tiles_x * J->tiles_y) break;
+        int rc = render_tile(J, t);
+        if (rc != YAR_OK) {
+            pthread_mutex_lock(&J->lock);
+            J->status = rc;
+            pthread_mutex_unlock(&J->lock);
+        }
+    }
+    return NULL;
+}
+
+int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t row_begin, int32_t row_end,
                   int32_t thread_count) {
-    (void)scene; (void)rgb; (void)variance; (void)row_begin; (void)row_end; (void)thread_count;
-    return YAR_ERR_UNSUPPORTED;
+    const yar_render_config* cfg = &s->config;
+    if (cfg->rendering_algorithm != 1 || cfg->pixel_filter_type != 0) return YAR_ERR_UNSUPPORTED;
+    for (uint32_t i = 0; i < s->material_count; i++) {
+        uint32_t t = s->materials[i].type;
+        if (t != YAR_MATERIAL_DIFFUSE && t != YAR_MATERIAL_METAL && t != YAR_MATERIAL_GLASS) return YAR_ERR_UNSUPPORTED;
+        if (t == YAR_MATERIAL_GLASS && !(s->materials[i].u_roughness > 0.f)) return YAR_ERR_UNSUPPORTED;
+    }
+    if (s->other_light_count) return YAR_ERR_UNSUPPORTED;
+    render_job J;
+    memset(&J, 0, sizeof(J));
+    J.s = s;
+    J.x0 = cfg->render_region[0];
+    J.y0 = cfg->render_region[1];
+    J.x1 = cfg->render_region[2];
+    J.y1 = cfg->render_region[3];
+    const float radius = cfg->pixel_filter_radius;
+    J.sx0 = (int)floorf((float)J.x0 + 0.5f - radius);
+    J.sy0 = (int)floorf((float)J.y0 + 0.5f - radius);
+    J.sx1 = (int)ceilf((float)(J.x1 - 1) + 0.5f + radius);
+    J.sy1 = (int)ceilf((float)(J.y1 - 1) + 0.5f + radius);
+    J.tiles_x = (J.sx1 - J.sx0 + TILE - 1) / TILE;
+    J.tiles_y = (J.sy1 - J.sy0 + TILE - 1) / TILE;
+    J.row_begin = row_begin + J.y0;
+    J.row_end = row_end + J.y0;
+    const int nt = J.tiles_x * J.tiles_y;
+    J.tile_pixels = (film_px**)calloc(nt, sizeof(film_px*));
+    J.tile_bounds = (int*)calloc(4 * (size_t)nt, sizeof(int));
+    J.tile_variance = (double*)calloc(nt, sizeof(double));
+    pthread_mutex_init(&J.lock, NULL);
+    J.status = YAR_OK;
+    int nthreads = thread_count > 0 ? thread_count : 1;
+    pthread_t* th = (pthread_t*)malloc(sizeof(pthread_t) * nthreads);
+    for (int i = 0; i < nthreads; i++) pthread_create(&th[i], NULL, render_worker, &J);
+    for (int i = 0; i < nthreads; i++) pthread_join(th[i], NULL);
+    free(th);
+    int rc = J.status;
+    if (rc == YAR_OK) {
+        /* merge tiles in index order, then resolve (src/ref/film.cpp:88-120) */
+        const int W = J.x1 - J.x0, H = J.y1 - J.y0;
+        film_px* film = (film_px*)calloc((size_t)W * H, sizeof(film_px));
+        for (int t = 0; t < nt; t++) {
+            const int* pb = &J.tile_bounds[4 * t];
+            const int pw = pb[2] - pb[0];
+            for (int y = pb[1]; y < pb[3]; y++)
+                for (int x = pb[0]; x < pb[2]; x++) {
+                    film_px* f = &film[(y - J.y0) * W + (x - J.x0)];
+                    const film_px* p = &J.tile_pixels[t][(y - pb[1]) * pw + (x - pb[0])];
+                    f->r += p->r;
+                    f->g += p->g;
+                    f->b += p->b;
+                    f->w += p->w;
+                }
+        }
+        for (int i = 0; i < W * H; i++) {
+            col c = mkc(0, 0, 0);
+            if (film[i].w != 0.f) c = mulcs(mkc(film[i].r, film[i].g, film[i].b), 1.f / film[i].w);
+            rgb[3 * i + 0] = fmaxf_std(0.f, c.r);
+            rgb[3 * i + 1] = fmaxf_std(0.f, c.g);
+            rgb[3 * i + 2] = fmaxf_std(0.f, c.b);
+        }
+        free(film);
+        const int spp = cfg->x_pixel_sample_count * cfg->y_pixel_sample_count;
+        if (variance && spp > 1) {
+            double acc = 0.0;
+            int64_t count = 0;
+            for (int t = 0; t < nt; t++) {
+                int sb[4], pb[4];
+                acc += J.tile_variance[t];
+                tile_bounds(&J, t, sb, pb);
+                count += (int64_t)(sb[2] - sb[0]) * (sb[3] - sb[1]);
+            }
+            *variance = acc / (double)count;
+        }
+    }
+    for (int t = 0; t < nt; t++) free(J.tile_pixels[t]);
+    free(J.tile_pixels);
+    free(J.tile_bounds);
+    free(J.tile_variance);
+    pthread_mutex_destroy(&J.lock);
+    return rc;
 }

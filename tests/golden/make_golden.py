@@ -19,6 +19,7 @@ Fixtures
   cornell_c1_64.yfs / .npz   the Cornell box flattened by the reference loader
                              and builder at 64x64, 16 spp, maxdepth 8, seed 1,
                              and the reference's FP32 render of it.
+  cornell_ggx_64.yfs / .npz  the same with a GGX metal box and a rough-glass box.
 """
 import os
 import re
@@ -127,10 +128,23 @@ def cornell_c1_64():
     np.savez_compressed(os.path.join(HERE, "cornell_c1_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def cornell_ggx_64():
+    """The Cornell box with a GGX metal box and a rough-glass box."""
+    with tempfile.TemporaryDirectory() as d:
+        pbrt = os.path.join(d, "cornell_ggx.pbrt")
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=2, width=64, height=64, spp=16, maxdepth=8,
+                                                  box_materials=scenes.GGX_BOXES))
+        yfs = os.path.join(HERE, "cornell_ggx_64.yfs")
+        oracle.ref_flatten(pbrt, yfs, seed_offset=1)
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_ggx_64.npz"), image=img, variance=np.float64(info["variance"]))
+
+
 if __name__ == "__main__":
     if not oracle.have_reference():
         sys.exit("oracle/_ref/yar_ref is not built (oracle/build_ref.sh)")
-    which = sys.argv[1:] or ["raycast_small", "transform_small", "kdtree_regression", "cornell_c1_64"]
+    which = sys.argv[1:] or ["raycast_small", "transform_small", "kdtree_regression", "cornell_c1_64",
+                             "cornell_ggx_64"]
     for name in which:
         globals()[name]()
         print("wrote", name)

@@ -119,3 +119,29 @@ def test_builder_against_live_reference_large_mesh():
     for m, r in zip(s.meshes, ref.meshes):
         b, nodes = native.build_mesh_kdtree(m.vertices, m.indices, 8)
         assert np.array_equal(nodes, r.nodes)
+
+
+@pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64"])
+def test_oracle_render_matches_reference_golden(name):
+    """The oracle's path loop, sampler, shading, BSDFs, MIS and film reproduce
+    the reference's FP32 render and variance bit for bit."""
+    s = FlatScene.read(golden(name + ".yfs"))
+    g = np.load(golden(name + ".npz"))
+    img, var = oracle.render(s, threads=4)
+    assert np.array_equal(bits(img), bits(g["image"]))
+    assert var == float(g["variance"])
+
+
+@pytest.mark.skipif(not oracle.have_reference(), reason="reference not built here")
+def test_oracle_render_against_live_reference_past_the_sampler_budget(tmp_path):
+    """maxdepth 12 exceeds the sampler's 10-bounce dimension budget, so later
+    draws come from the pixel's raw pcg stream in path order; the oracle keeps
+    that order exactly (src/ref/pixel_sampling.cpp:159-173)."""
+    p = tmp_path / "c.pbrt"
+    p.write_text(scenes.cornell_pbrt(seed=4, width=32, height=32, spp=4, maxdepth=12, box_materials=scenes.GGX_BOXES))
+    y = tmp_path / "c.yfs"
+    oracle.ref_flatten(str(p), str(y), seed_offset=3)
+    ref_img, info = oracle.ref_render(str(p), seed_offset=3, threads=4)
+    img, var = oracle.render(FlatScene.read(str(y)), threads=4)
+    assert np.array_equal(bits(img), bits(ref_img))
+    assert var == info["variance"]

@@ -117,6 +117,7 @@ extern "C" int yar_gpu_create(yar_gpu_ctx** out, const yar_gpu_options* options)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_error, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_error, 0, sizeof(int));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_start);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_stop);
     if (e != cudaSuccess) {
@@ -137,6 +138,7 @@ extern "C" void yar_gpu_destroy(yar_gpu_ctx* ctx) {
                              &ctx->d_prim, &ctx->d_obj, &ctx->d_bary, &ctx->d_occ})
         device_free(*b);
     if (ctx->d_error) cudaFree(ctx->d_error);
+    if (ctx->d_counter) cudaFree(ctx->d_counter);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -332,8 +334,8 @@ int cast(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t n, const yar_hit_soa* h
         }
     }
     if (kernel_ms) cudaEventRecord(ctx->ev_start, ctx->stream);
-    e = closest ? launch_extend(ctx->ds, d_rays, n, d_t, d_prim, d_obj, d_bary, ctx->d_error, ctx->stream)
-                : launch_shadow(ctx->ds, d_rays, n, d_occ, ctx->d_error, ctx->stream);
+    e = closest ? launch_extend(ctx->ds, d_rays, n, d_t, d_prim, d_obj, d_bary, ctx->d_error, ctx->d_counter, ctx->stream)
+                : launch_shadow(ctx->ds, d_rays, n, d_occ, ctx->d_error, ctx->d_counter, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, closest ? "extend launch" : "shadow launch");
     if (kernel_ms) cudaEventRecord(ctx->ev_stop, ctx->stream);
     if (buffers == YAR_BUFFERS_HOST) {

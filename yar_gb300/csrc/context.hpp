@@ -55,6 +55,7 @@ struct yar_gpu_ctx {
     uint32_t staging_capacity = 0;
     yar::Device_Buffer d_rays, d_t, d_prim, d_obj, d_bary, d_occ;
     int* d_error = nullptr;  // device error word (stack overflow, bounded-wait expiry)
+    uint32_t* d_counter = nullptr;  // ray hand-out counter of the persistent cast kernels
 
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
 
@@ -70,10 +71,11 @@ int device_alloc(yar_gpu_ctx* ctx, Device_Buffer& b, size_t bytes);
 void device_free(Device_Buffer& b);
 
 // kernels (cast.cu)
+// `counter` is one device word the persistent kernels use to hand out rays.
 cudaError_t launch_extend(const Device_Scene& s, const float4* rays, uint32_t n, float* t, uint32_t* prim,
-                          uint32_t* obj, float2* bary, int* err, cudaStream_t stream);
+                          uint32_t* obj, float2* bary, int* err, uint32_t* counter, cudaStream_t stream);
 cudaError_t launch_shadow(const Device_Scene& s, const float4* rays, uint32_t n, uint8_t* occluded, int* err,
-                          cudaStream_t stream);
+                          uint32_t* counter, cudaStream_t stream);
 
 // render (render.cu)
 int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene);

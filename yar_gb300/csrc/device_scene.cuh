@@ -16,9 +16,22 @@
 //                          v0.w != 0 marks a degenerate triangle, which the
 //                          reference rejects after the test (kdtree.cpp:27-29)
 //
-// Arithmetic follows the reference operation by operation (the translation
-// unit is compiled with -fmad=false and IEEE division), so hit triangle ids,
-// t and barycentrics are bit-identical to KdTree::intersect.
+// Traversal structure (GB300-first): the reference recurses scene tree ->
+// object -> mesh tree with a separate loop per level.  On a SIMT machine that
+// nesting serialises a warp whose lanes sit at different levels, so here one
+// loop drives a small state machine per lane: DESCEND (fetch the current
+// level's node, descend through interior nodes), SCENE_LEAF (enter the next
+// object of a scene leaf: transform the ray, clip it to the mesh bounds),
+// MESH_LEAF (test the next triangle of a mesh leaf).  Scene and mesh levels
+// share the descend code and one traversal stack (mesh entries sit above the
+// scene entries).  Lanes reconverge at the top of every iteration.
+//
+// Visit order, termination tests and every float operation follow the
+// reference (src/ref/kdtree.cpp:12-109, :219-439) step by step: the
+// translation unit is compiled with -fmad=false and IEEE division, and small
+// per-axis values are selected with conditional moves rather than indexed
+// (indexing register arrays would put them in local memory).  Hit triangle
+// ids, t and barycentrics are therefore bit-identical to KdTree::intersect.
 #pragma once
 
 #include <cstdint>
@@ -44,48 +57,68 @@ struct Hit {
     float b0, b1, b2;
 };
 
-__device__ __forceinline__ float u2f(uint32_t u) { return __uint_as_float(u); }
+__device__ __forceinline__ float sel3(float x, float y, float z, int k) { return k == 0 ? x : (k == 1 ? y : z); }
 
 // Bounding_Box::intersect_by_ray_without_NaNs, src/lib/bounding_box.h:63-85
-__device__ __forceinline__ bool clip_ray(const float mn[3], const float mx[3], const float o[3], const float d[3],
-                                         float& t_min, float& t_max) {
-    float t0 = 0.f, t1 = __int_as_float(0x7f800000);
-#pragma unroll
-    for (int i = 0; i < 3; i++) {
-        if (d[i] != 0.f) {
-            const float inv = 1.f / d[i];
-            float s0 = (mn[i] - o[i]) * inv;
-            float s1 = (mx[i] - o[i]) * inv;
-            if (inv < 0.f) { const float tmp = s0; s0 = s1; s1 = tmp; }
-            t0 = s0 > t0 ? s0 : t0;
-            t1 = s1 < t1 ? s1 : t1;
-            if (t0 > t1) return false;
-        } else if (o[i] < mn[i] || o[i] > mx[i]) {
-            return false;
-        }
+__device__ __forceinline__ bool clip_axis(float mn, float mx, float o, float d, float& t0, float& t1) {
+    if (d != 0.f) {
+        const float inv = 1.f / d;
+        float s0 = (mn - o) * inv;
+        float s1 = (mx - o) * inv;
+        if (inv < 0.f) { const float tmp = s0; s0 = s1; s1 = tmp; }
+        t0 = s0 > t0 ? s0 : t0;
+        t1 = s1 < t1 ? s1 : t1;
+        return !(t0 > t1);
     }
+    return !(o < mn || o > mx);
+}
+
+__device__ __forceinline__ bool clip_ray(float3 mn, float3 mx, float3 o, float3 d, float& t_min, float& t_max) {
+    float t0 = 0.f, t1 = __int_as_float(0x7f800000);
+    if (!clip_axis(mn.x, mx.x, o.x, d.x, t0, t1)) return false;
+    if (!clip_axis(mn.y, mx.y, o.y, d.y, t0, t1)) return false;
+    if (!clip_axis(mn.z, mx.z, o.z, d.z, t0, t1)) return false;
     t_min = t0;
     t_max = t1;
     return true;
 }
 
-// intersect_triangle_watertight, src/ref/intersection.cpp:53-113.
+// Per-ray setup of the watertight test (src/ref/intersection.cpp:55-62).
+struct Watertight_Ray {
+    int kx, ky, kz;
+    float sx, sy, sz;
+};
+
+__device__ __forceinline__ Watertight_Ray watertight_setup(float3 d) {
+    Watertight_Ray w;
+    const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
+    w.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);  // Vector3::max_dimension
+    w.kx = (w.kz == 2 ? 0 : w.kz + 1);
+    w.ky = (w.kz == 0 ? 2 : w.kz - 1);
+    const float dx = sel3(d.x, d.y, d.z, w.kx), dy = sel3(d.x, d.y, d.z, w.ky), dz = sel3(d.x, d.y, d.z, w.kz);
+    w.sx = -dx / dz;
+    w.sy = -dy / dz;
+    w.sz = 1.f / dz;
+    return w;
+}
+
+// intersect_triangle_watertight, src/ref/intersection.cpp:64-113.
 // Returns +inf when there is no intersection.
-__device__ __forceinline__ float watertight(const float o[3], const float d[3], int kx, int ky, int kz, float sx,
-                                            float sy, float sz, const float4 v0, const float4 v1, const float4 v2,
+__device__ __forceinline__ float watertight(float3 o, const Watertight_Ray& w, float4 v0, float4 v1, float4 v2,
                                             float& b0, float& b1, float& b2) {
-    const float p0[3] = {v0.x, v0.y, v0.z};
-    const float p1[3] = {v1.x, v1.y, v1.z};
-    const float p2[3] = {v2.x, v2.y, v2.z};
-    const float p0x = p0[kx] - o[kx], p0y = p0[ky] - o[ky], p0z = p0[kz] - o[kz];
-    const float p1x = p1[kx] - o[kx], p1y = p1[ky] - o[ky], p1z = p1[kz] - o[kz];
-    const float p2x = p2[kx] - o[kx], p2y = p2[ky] - o[ky], p2z = p2[kz] - o[kz];
-    const float x0 = p0x + sx * p0z;
-    const float y0 = p0y + sy * p0z;
-    const float x1 = p1x + sx * p1z;
-    const float y1 = p1y + sy * p1z;
-    const float x2 = p2x + sx * p2z;
-    const float y2 = p2y + sy * p2z;
+    const float ox = sel3(o.x, o.y, o.z, w.kx), oy = sel3(o.x, o.y, o.z, w.ky), oz = sel3(o.x, o.y, o.z, w.kz);
+    const float p0x = sel3(v0.x, v0.y, v0.z, w.kx) - ox, p0y = sel3(v0.x, v0.y, v0.z, w.ky) - oy,
+                p0z = sel3(v0.x, v0.y, v0.z, w.kz) - oz;
+    const float p1x = sel3(v1.x, v1.y, v1.z, w.kx) - ox, p1y = sel3(v1.x, v1.y, v1.z, w.ky) - oy,
+                p1z = sel3(v1.x, v1.y, v1.z, w.kz) - oz;
+    const float p2x = sel3(v2.x, v2.y, v2.z, w.kx) - ox, p2y = sel3(v2.x, v2.y, v2.z, w.ky) - oy,
+                p2z = sel3(v2.x, v2.y, v2.z, w.kz) - oz;
+    const float x0 = p0x + w.sx * p0z;
+    const float y0 = p0y + w.sy * p0z;
+    const float x1 = p1x + w.sx * p1z;
+    const float y1 = p1y + w.sy * p1z;
+    const float x2 = p2x + w.sx * p2z;
+    const float y2 = p2y + w.sy * p2z;
     float e0 = x1 * y2 - y1 * x2;
     float e1 = x2 * y0 - y2 * x0;
     float e2 = x0 * y1 - y0 * x1;
@@ -98,9 +131,9 @@ __device__ __forceinline__ float watertight(const float o[3], const float d[3], 
     if ((e0 < 0.f || e1 < 0.f || e2 < 0.f) && (e0 > 0.f || e1 > 0.f || e2 > 0.f)) return inf;
     const float det = e0 + e1 + e2;
     if (det == 0.f) return inf;
-    const float z0 = sz * p0z;
-    const float z1 = sz * p1z;
-    const float z2 = sz * p2z;
+    const float z0 = w.sz * p0z;
+    const float z1 = w.sz * p1z;
+    const float z2 = w.sz * p2z;
     const float t_scaled = e0 * z0 + e1 * z1 + e2 * z2;
     if ((__float_as_uint(det) ^ __float_as_uint(t_scaled)) >> 31) return inf;
     const float inv_det = 1.f / det;
@@ -116,182 +149,234 @@ struct Stack_Entry {
     float t_max;
 };
 
-// One descent step, src/ref/kdtree.cpp:254-298 (closest) and :361-406 (any).
-// Returns false on stack overflow.
-__device__ __forceinline__ bool descend(uint2 n, uint32_t& node, const float o[3], const float d[3],
-                                        const float inv[3], float& t_min, float& t_max, Stack_Entry* stack,
-                                        int& sp) {
-    const int axis = (int)(n.x & 3u);
-    const float dist = u2f(n.y) - o[axis];
-    const uint32_t below_child = node + 1;
-    const uint32_t above_child = n.x >> 2;
-    if (dist != 0.f) {
-        const bool below_first = dist > 0.f;
-        const uint32_t first_child = below_first ? below_child : above_child;
-        const uint32_t second_child = below_first ? above_child : below_child;
-        const float t_split = dist * inv[axis];
-        if (t_split > t_max || t_split < 0.f) {
-            node = first_child;
-        } else if (t_split < t_min) {
-            node = second_child;
-        } else {
-            if (sp >= kMaxTraversalDepth) return false;
-            stack[sp].node = second_child;
-            stack[sp].t_max = t_max;
-            sp++;
-            node = first_child;
-            t_max = t_split;
-        }
-    } else {
-        node = (d[axis] > 0.f) ? above_child : below_child;
-    }
-    return true;
+// transform_ray, src/lib/matrix.cpp:368-389: ((a*x + b*y) + c*z) + w
+__device__ __forceinline__ void transform_ray(float4 r0, float4 r1, float4 r2, float3 o, float3 d, float3& oo,
+                                              float3& od) {
+    oo.x = r0.x * o.x + r0.y * o.y + r0.z * o.z + r0.w;
+    oo.y = r1.x * o.x + r1.y * o.y + r1.z * o.z + r1.w;
+    oo.z = r2.x * o.x + r2.y * o.y + r2.z * o.z + r2.w;
+    od.x = r0.x * d.x + r0.y * d.y + r0.z * d.z;
+    od.y = r1.x * d.x + r1.y * d.y + r1.z * d.z;
+    od.z = r2.x * d.x + r2.y * d.y + r2.z * d.z;
 }
 
-struct Object_Record {
-    float m[12];
-    float bmin[3];
-    float bmax[3];
-    uint32_t node_offset;
+enum : int { kDescend = 0, kSceneLeaf = 1, kMeshLeaf = 2, kDone = 3 };
+
+// Two-level closest-hit (ANY = false) or any-hit (ANY = true) traversal of one
+// ray as a resumable state machine: begin() sets up a ray, step() performs one
+// unit of work (a descent through interior nodes down to a leaf, one scene-leaf
+// object entry, or one triangle test) and returns false once the ray is
+// finished.  status afterwards: closest 1 = hit / 0 = miss; any 1 = occluded /
+// 0 = not; -1 = traversal-stack overflow.
+template <bool ANY>
+struct Traversal {
+    float3 o, d, inv;      // world ray
+    float ray_tmax;
+    float3 co, cd, cinv;   // ray of the current level
+    const uint2* nodes;
+    uint32_t node;
+    float t_min, t_max;
+    int sp, mesh_sp_base;
+    bool in_mesh;
+    uint32_t sl_node, sl_i, sl_count;
+    float scene_t_min, scene_t_max;
+    uint32_t cur_object;
+    float entry_t;
     uint32_t tri_offset;
-    int32_t visibility;
+    bool test_triangles;
+    Watertight_Ray wr;
+    uint32_t ml_node, ml_i, ml_count;
+    int mode;
+    int status;
+    Hit hit;
+
+    __device__ __forceinline__ void leave_mesh(const Device_Scene& s) {
+        if (!ANY && hit.t < entry_t) hit.object = cur_object;
+        in_mesh = false;
+        sp = mesh_sp_base;
+        co = o;
+        cd = d;
+        cinv = inv;
+        nodes = s.scene_nodes;
+        t_min = scene_t_min;
+        t_max = scene_t_max;
+        mode = kSceneLeaf;
+    }
+
+    __device__ __forceinline__ void finish(int st) {
+        mode = kDone;
+        status = st;
+    }
+
+    __device__ __forceinline__ void begin(const Device_Scene& s, float3 ro, float3 rd, float tmax) {
+        o = ro;
+        d = rd;
+        ray_tmax = tmax;
+        hit.t = tmax;
+        hit.prim = 0xffffffffu;
+        hit.object = 0xffffffffu;
+        hit.b0 = hit.b1 = hit.b2 = 0.f;
+        sp = 0;
+        mesh_sp_base = 0;
+        in_mesh = false;
+        node = 0;
+        nodes = s.scene_nodes;
+        status = 0;
+        if (!clip_ray(make_float3(s.scene_bounds[0], s.scene_bounds[1], s.scene_bounds[2]),
+                      make_float3(s.scene_bounds[3], s.scene_bounds[4], s.scene_bounds[5]), o, d, t_min, t_max)) {
+            mode = kDone;
+            return;
+        }
+        inv = make_float3(1.f / d.x, 1.f / d.y, 1.f / d.z);
+        co = o;
+        cd = d;
+        cinv = inv;
+        mode = kDescend;
+    }
+
+    // `stack` is the caller's array of 2 * kMaxTraversalDepth entries (kept out of
+    // this struct so the scalar state can live in registers).
+    __device__ __forceinline__ bool step(const Device_Scene& s, Stack_Entry* stack) {
+        if (mode == kDescend) {
+            for (;;) {  // while-while: descend through interior nodes of the current level
+                const float limit = ANY ? ray_tmax : hit.t;
+                if (!(limit > t_min)) {  // the level's loop condition failed
+                    if (in_mesh) {
+                        leave_mesh(s);
+                    } else {
+                        finish(ANY ? 0 : (hit.t < ray_tmax ? 1 : 0));
+                    }
+                    break;
+                }
+                const uint2 n = __ldg(nodes + node);
+                if ((n.x & 3u) == 3u) {
+                    const uint32_t count = n.x >> 2;
+                    if (in_mesh) {
+                        mode = kMeshLeaf;
+                        ml_node = node;
+                        ml_i = 0;
+                        ml_count = test_triangles ? count : 0u;
+                    } else {
+                        mode = kSceneLeaf;
+                        sl_node = node;
+                        sl_i = 0;
+                        sl_count = count;
+                    }
+                    break;
+                }
+                const int axis = (int)(n.x & 3u);
+                const float dist = __uint_as_float(n.y) - sel3(co.x, co.y, co.z, axis);
+                const uint32_t below_child = node + 1;
+                const uint32_t above_child = n.x >> 2;
+                if (dist != 0.f) {
+                    const bool below_first = dist > 0.f;
+                    const uint32_t first_child = below_first ? below_child : above_child;
+                    const uint32_t second_child = below_first ? above_child : below_child;
+                    const float t_split = dist * sel3(cinv.x, cinv.y, cinv.z, axis);
+                    if (t_split > t_max || t_split < 0.f) {
+                        node = first_child;
+                    } else if (t_split < t_min) {
+                        node = second_child;
+                    } else {
+                        if (sp >= 2 * kMaxTraversalDepth) {
+                            finish(-1);
+                            break;
+                        }
+                        stack[sp].node = second_child;
+                        stack[sp].t_max = t_max;
+                        sp++;
+                        node = first_child;
+                        t_max = t_split;
+                    }
+                } else {
+                    node = (sel3(cd.x, cd.y, cd.z, axis) > 0.f) ? above_child : below_child;
+                }
+            }
+        } else if (mode == kMeshLeaf) {
+            if (ml_i < ml_count) {
+                const uint32_t prim = (ml_i == 0) ? __ldg(&nodes[ml_node].y)
+                                                  : __ldg(reinterpret_cast<const uint32_t*>(nodes + ml_node) + 1 + ml_i);
+                ml_i++;
+                const float4* tp = s.tris + 3 * ((size_t)tri_offset + prim);
+                const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+                float b0, b1, b2;
+                const float t = watertight(co, wr, v0, v1, v2, b0, b1, b2);
+                if (ANY) {
+                    // `t >= ray_tmax` rejects; a NaN t does not (src/ref/kdtree.cpp:60-62)
+                    if (!(t >= ray_tmax) && v0.w == 0.f) finish(1);
+                } else if (t < hit.t && v0.w == 0.f) {
+                    hit.t = t;
+                    hit.prim = prim;
+                    hit.b0 = b0;
+                    hit.b1 = b1;
+                    hit.b2 = b2;
+                }
+            } else if (sp == mesh_sp_base) {  // mesh stack empty: the mesh is done
+                leave_mesh(s);
+            } else {
+                --sp;
+                node = stack[sp].node;
+                t_min = t_max;
+                t_max = stack[sp].t_max;
+                mode = kDescend;
+            }
+        } else if (mode == kSceneLeaf) {
+            if (sl_i < sl_count) {
+                const uint32_t obj = (sl_i == 0)
+                                         ? __ldg(&s.scene_nodes[sl_node].y)
+                                         : __ldg(reinterpret_cast<const uint32_t*>(s.scene_nodes + sl_node) + 1 + sl_i);
+                sl_i++;
+                const float4* p = s.objects + 6 * (size_t)obj;
+                const float4 r0 = __ldg(p + 0), r1 = __ldg(p + 1), r2 = __ldg(p + 2);
+                const float4 lo = __ldg(p + 3), hi = __ldg(p + 4), info = __ldg(p + 5);
+                float3 oo, od;
+                transform_ray(r0, r1, r2, o, d, oo, od);
+                float mt_min, mt_max;
+                if (clip_ray(make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z), oo, od, mt_min, mt_max)) {
+                    scene_t_min = t_min;
+                    scene_t_max = t_max;
+                    in_mesh = true;
+                    cur_object = obj;
+                    entry_t = hit.t;
+                    co = oo;
+                    cd = od;
+                    cinv = make_float3(1.f / od.x, 1.f / od.y, 1.f / od.z);
+                    nodes = s.mesh_nodes + __float_as_uint(lo.w);
+                    tri_offset = __float_as_uint(hi.w);
+                    const int visibility = __float_as_int(info.y);
+                    test_triangles = ANY ? (visibility == 0) : (visibility != 2);
+                    wr = watertight_setup(od);
+                    node = 0;
+                    t_min = mt_min;
+                    t_max = mt_max;
+                    mesh_sp_base = sp;
+                    mode = kDescend;
+                }
+            } else if (sp == 0) {
+                finish(ANY ? 0 : (hit.t < ray_tmax ? 1 : 0));
+            } else {
+                --sp;
+                node = stack[sp].node;
+                t_min = t_max;
+                t_max = stack[sp].t_max;
+                mode = kDescend;
+            }
+        }
+        return mode != kDone;
+    }
 };
 
-__device__ __forceinline__ Object_Record load_object(const float4* objects, uint32_t index) {
-    const float4* p = objects + 6 * (size_t)index;
-    const float4 r0 = __ldg(p + 0), r1 = __ldg(p + 1), r2 = __ldg(p + 2);
-    const float4 lo = __ldg(p + 3), hi = __ldg(p + 4), info = __ldg(p + 5);
-    Object_Record r;
-    r.m[0] = r0.x; r.m[1] = r0.y; r.m[2] = r0.z; r.m[3] = r0.w;
-    r.m[4] = r1.x; r.m[5] = r1.y; r.m[6] = r1.z; r.m[7] = r1.w;
-    r.m[8] = r2.x; r.m[9] = r2.y; r.m[10] = r2.z; r.m[11] = r2.w;
-    r.bmin[0] = lo.x; r.bmin[1] = lo.y; r.bmin[2] = lo.z;
-    r.bmax[0] = hi.x; r.bmax[1] = hi.y; r.bmax[2] = hi.z;
-    r.node_offset = __float_as_uint(lo.w);
-    r.tri_offset = __float_as_uint(hi.w);
-    r.visibility = __float_as_int(info.y);
-    return r;
-}
-
-// transform_ray, src/lib/matrix.cpp:368-389: ((a*x + b*y) + c*z) + w
-__device__ __forceinline__ void transform_ray(const float m[12], const float o[3], const float d[3], float oo[3],
-                                              float od[3]) {
-#pragma unroll
-    for (int r = 0; r < 3; r++) {
-        oo[r] = m[4 * r + 0] * o[0] + m[4 * r + 1] * o[1] + m[4 * r + 2] * o[2] + m[4 * r + 3];
-        od[r] = m[4 * r + 0] * d[0] + m[4 * r + 1] * d[1] + m[4 * r + 2] * d[2];
-    }
-}
-
-// KdTree::intersect (closest) or intersect_any (ANY) over one mesh tree with
-// the triangle leaf callbacks (src/ref/kdtree.cpp:12-79, :219-439).
-// Closest: updates hit, returns 1 if hit.t decreased, 0 otherwise.
-// Any: returns 1 when an occluder in [0, ray_tmax) was found.
-// Returns -1 on traversal-stack overflow.
+// One ray, start to finish (used by the render wavefront).  Returns the status.
 template <bool ANY>
-__device__ __forceinline__ int mesh_traverse(const Device_Scene& s, const Object_Record& obj, const float o[3],
-                                             const float d[3], float ray_tmax, Hit& hit) {
-    float t_min, t_max;
-    if (!clip_ray(obj.bmin, obj.bmax, o, d, t_min, t_max)) return 0;
-    const float inv[3] = {1.f / d[0], 1.f / d[1], 1.f / d[2]};
-    // watertight-test setup depends only on the ray (src/ref/intersection.cpp:55-62)
-    const float ax = fabsf(d[0]), ay = fabsf(d[1]), az = fabsf(d[2]);
-    const int kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);
-    const int kx = (kz == 2 ? 0 : kz + 1);
-    const int ky = (kz == 0 ? 2 : kz - 1);
-    const float sx = -d[kx] / d[kz];
-    const float sy = -d[ky] / d[kz];
-    const float sz = 1.f / d[kz];
-
-    const bool test_triangles = ANY ? (obj.visibility == 0) : (obj.visibility != 2);
-    const uint2* nodes = s.mesh_nodes + obj.node_offset;
-    Stack_Entry stack[kMaxTraversalDepth];
-    int sp = 0;
-    uint32_t node = 0;
-    const float entry_t = hit.t;
-    while ((ANY ? ray_tmax : hit.t) > t_min) {
-        const uint2 n = __ldg(nodes + node);
-        if ((n.x & 3u) != 3u) {
-            if (!descend(n, node, o, d, inv, t_min, t_max, stack, sp)) return -1;
-        } else {
-            const uint32_t count = n.x >> 2;
-            if (test_triangles && count) {
-                const uint32_t* idx = reinterpret_cast<const uint32_t*>(nodes + node) + 1;
-                for (uint32_t i = 0; i < count; i++) {
-                    const uint32_t prim = (i == 0) ? n.y : __ldg(idx + i);
-                    const float4* tp = s.tris + 3 * ((size_t)obj.tri_offset + prim);
-                    const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
-                    float b0, b1, b2;
-                    const float t = watertight(o, d, kx, ky, kz, sx, sy, sz, v0, v1, v2, b0, b1, b2);
-                    if (ANY) {
-                        // `t >= ray_tmax` rejects; a NaN t does not (src/ref/kdtree.cpp:60-62)
-                        if (!(t >= ray_tmax) && v0.w == 0.f) return 1;
-                    } else if (t < hit.t && v0.w == 0.f) {
-                        hit.t = t;
-                        hit.prim = prim;
-                        hit.b0 = b0;
-                        hit.b1 = b1;
-                        hit.b2 = b2;
-                    }
-                }
-            }
-            if (sp == 0) break;
-            --sp;
-            node = stack[sp].node;
-            t_min = t_max;
-            t_max = stack[sp].t_max;
-        }
+__device__ __forceinline__ int traverse(const Device_Scene& s, const float3 o, const float3 d, const float ray_tmax,
+                                        Hit& hit) {
+    Traversal<ANY> tr;
+    Stack_Entry stack[2 * kMaxTraversalDepth];
+    tr.begin(s, o, d, ray_tmax);
+    while (tr.step(s, stack)) {
     }
-    return ANY ? 0 : (hit.t < entry_t ? 1 : 0);
-}
-
-// Scene-level traversal with intersect_scene_geometry_data /
-// intersect_any_scene_geometry_data (src/ref/kdtree.cpp:81-109).
-// Closest: returns 1 on hit (hit filled), 0 on miss.  Any: 1 if occluded.
-// Returns -1 on stack overflow.
-template <bool ANY>
-__device__ __forceinline__ int scene_traverse(const Device_Scene& s, const float o[3], const float d[3],
-                                              float ray_tmax, Hit& hit) {
-    hit.t = ray_tmax;
-    hit.prim = 0xffffffffu;
-    hit.object = 0xffffffffu;
-    hit.b0 = hit.b1 = hit.b2 = 0.f;
-    float t_min, t_max;
-    const float mn[3] = {s.scene_bounds[0], s.scene_bounds[1], s.scene_bounds[2]};
-    const float mx[3] = {s.scene_bounds[3], s.scene_bounds[4], s.scene_bounds[5]};
-    if (!clip_ray(mn, mx, o, d, t_min, t_max)) return 0;
-    const float inv[3] = {1.f / d[0], 1.f / d[1], 1.f / d[2]};
-    Stack_Entry stack[kMaxTraversalDepth];
-    int sp = 0;
-    uint32_t node = 0;
-    while ((ANY ? ray_tmax : hit.t) > t_min) {
-        const uint2 n = __ldg(s.scene_nodes + node);
-        if ((n.x & 3u) != 3u) {
-            if (!descend(n, node, o, d, inv, t_min, t_max, stack, sp)) return -1;
-        } else {
-            const uint32_t count = n.x >> 2;
-            const uint32_t* idx = reinterpret_cast<const uint32_t*>(s.scene_nodes + node) + 1;
-            for (uint32_t i = 0; i < count; i++) {
-                const uint32_t object_index = (i == 0) ? n.y : __ldg(idx + i);
-                const Object_Record obj = load_object(s.objects, object_index);
-                float oo[3], od[3];
-                transform_ray(obj.m, o, d, oo, od);
-                const int r = mesh_traverse<ANY>(s, obj, oo, od, ray_tmax, hit);
-                if (r < 0) return -1;
-                if (ANY) {
-                    if (r) return 1;
-                } else if (r) {
-                    hit.object = object_index;
-                }
-            }
-            if (sp == 0) break;
-            --sp;
-            node = stack[sp].node;
-            t_min = t_max;
-            t_max = stack[sp].t_max;
-        }
-    }
-    return ANY ? 0 : (hit.t < ray_tmax ? 1 : 0);
+    hit = tr.hit;
+    return tr.status;
 }
 
 } // namespace yar

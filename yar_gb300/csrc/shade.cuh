@@ -1,0 +1,436 @@
+// shade.cuh - device restatement of the shading side of the reference path:
+// shading context (src/ref/shading_context.cpp), Diffuse/Metal/Rough_Glass
+// BSDFs (src/ref/bsdf.cpp), microfacet and Fresnel math (src/ref/scattering.cpp),
+// sampling (src/ref/sampling.cpp), ray-origin offsetting (src/lib/math.cpp).
+//
+// Every expression keeps the reference's operand order; the translation unit
+// is compiled with -fmad=false and IEEE division/sqrt, so all of it rounds
+// like the reference except sin/cos: those are evaluated in double precision
+// and rounded once to float, which gives the correctly rounded float result
+// (what glibc's sinf/cosf return for all but a vanishing fraction of inputs).
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace yar {
+
+struct V3 {
+    float x, y, z;
+};
+struct Col {
+    float r, g, b;
+};
+
+__device__ __forceinline__ V3 v3(float x, float y, float z) { return V3{x, y, z}; }
+__device__ __forceinline__ V3 operator+(V3 a, V3 b) { return v3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ V3 operator-(V3 a, V3 b) { return v3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ V3 operator-(V3 a) { return v3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ V3 mul(V3 v, float t) { return v3(v.x * t, v.y * t, v.z * t); }   // Vector3 * float
+__device__ __forceinline__ V3 divs(V3 v, float t) { return v3(v.x / t, v.y / t, v.z / t); }  // Vector3 / float
+__device__ __forceinline__ float dot(V3 a, V3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ V3 cross(V3 a, V3 b) {
+    return v3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float len2(V3 v) { return v.x * v.x + v.y * v.y + v.z * v.z; }
+__device__ __forceinline__ float len(V3 v) { return sqrtf(len2(v)); }
+__device__ __forceinline__ V3 normalized(V3 v) { return divs(v, len(v)); }
+
+__device__ __forceinline__ Col col(float r, float g, float b) { return Col{r, g, b}; }
+__device__ __forceinline__ Col operator+(Col a, Col b) { return col(a.r + b.r, a.g + b.g, a.b + b.b); }
+__device__ __forceinline__ Col operator-(Col a, Col b) { return col(a.r - b.r, a.g - b.g, a.b - b.b); }
+__device__ __forceinline__ Col operator*(Col a, Col b) { return col(a.r * b.r, a.g * b.g, a.b * b.b); }
+__device__ __forceinline__ Col operator/(Col a, Col b) { return col(a.r / b.r, a.g / b.g, a.b / b.b); }
+__device__ __forceinline__ Col mul(Col c, float k) { return col(c.r * k, c.g * k, c.b * k); }  // ColorRGB * float
+__device__ __forceinline__ Col csqrt(Col c) { return col(sqrtf(c.r), sqrtf(c.g), sqrtf(c.b)); }
+__device__ __forceinline__ bool black(Col c) { return c.r == 0.f && c.g == 0.f && c.b == 0.f; }
+__device__ __forceinline__ float max_std(float a, float b) { return (a < b) ? b : a; }  // std::max
+__device__ __forceinline__ float min_std(float a, float b) { return (b < a) ? b : a; }  // std::min
+__device__ __forceinline__ float max_component(Col c) { return max_std(c.r, max_std(c.g, c.b)); }
+__device__ __forceinline__ float clamp1(float x) { return x < -1.f ? -1.f : (x > 1.f ? 1.f : x); }
+
+__device__ __forceinline__ float sin_f(float x) { return (float)sin((double)x); }
+__device__ __forceinline__ float cos_f(float x) { return (float)cos((double)x); }
+
+constexpr float kPi = 3.14159265f;  // src/lib/math.h:7
+
+// transform_point / transform_vector (src/lib/matrix.cpp:368-382)
+__device__ __forceinline__ V3 xform_point(const float4& r0, const float4& r1, const float4& r2, V3 p) {
+    return v3(r0.x * p.x + r0.y * p.y + r0.z * p.z + r0.w, r1.x * p.x + r1.y * p.y + r1.z * p.z + r1.w,
+              r2.x * p.x + r2.y * p.y + r2.z * p.z + r2.w);
+}
+__device__ __forceinline__ V3 xform_vector(const float4& r0, const float4& r1, const float4& r2, V3 v) {
+    return v3(r0.x * v.x + r0.y * v.y + r0.z * v.z, r1.x * v.x + r1.y * v.y + r1.z * v.z,
+              r2.x * v.x + r2.y * v.y + r2.z * v.z);
+}
+
+// barycentric_interpolate (src/lib/math.h:146-153)
+__device__ __forceinline__ V3 bary(V3 p0, V3 p1, V3 p2, float b0, float b1, float b2) {
+    return (mul(p0, b0) + mul(p1, b1)) + mul(p2, b2);
+}
+
+// coordinate_system_from_vector (src/lib/math.cpp:21-25), first axis only
+__device__ __forceinline__ V3 coordinate_axis(V3 v) {
+    V3 v1 = (fabsf(v.x) > fabsf(v.y)) ? v3(-v.z, 0.f, v.x) : v3(0.f, -v.z, v.y);
+    return divs(v1, len(v1));
+}
+
+__device__ __forceinline__ V3 reflect(V3 w, V3 n) { return mul(n, 2.f * dot(w, n)) - w; }
+
+__device__ __forceinline__ bool refract(V3 wi, V3 n, float eta, V3& wt) {
+    const float cos_i = dot(wi, n);
+    const float sin_t2 = eta * eta * max_std(0.f, 1.f - cos_i * cos_i);
+    if (sin_t2 >= 1.f) return false;
+    const float cos_t = sqrtf(1.f - sin_t2);
+    wt = mul(wi, -eta) + mul(n, eta * cos_i - cos_t);
+    return true;
+}
+
+// offset_ray_origin_in_both_directions (src/lib/math.cpp:81-120)
+__device__ __forceinline__ void offset_axis(float p, float n, float& pos, float& neg) {
+    const int di = (int)(256.f * n);
+    const int i1 = __float_as_int(p) - di, i2 = __float_as_int(p) + di;
+    pos = __int_as_float(p < 0 ? i1 : i2);
+    neg = __int_as_float(p < 0 ? i2 : i1);
+    if (fabsf(p) < 1.0f / 32.0f) {
+        const float d = (1.0f / 65536.0f) * n;
+        pos = p + d;
+        neg = p - d;
+    }
+}
+
+struct Shading {
+    V3 wo, position, ng, n, dpdu_shading;
+    V3 origin_pos, origin_neg;
+    bool flipped;
+};
+
+__device__ __forceinline__ V3 origin_for_direction(const Shading& sc, V3 dir) {
+    return dot(dir, sc.ng) > 0.f ? sc.origin_pos : sc.origin_neg;
+}
+__device__ __forceinline__ V3 origin_for_point(const Shading& sc, V3 point) {
+    return origin_for_direction(sc, point - sc.position);
+}
+
+// adjust_shading_normal (src/ref/shading_context.cpp:17-63)
+__device__ __forceinline__ V3 adjust_shading_normal(V3 wo, V3 ng, V3 n) {
+    const V3 R = reflect(wo, n);
+    const float a = dot(R, ng);
+    if (a >= 0.f) return n;
+    if (dot(wo, ng) < 0.0017453f) return ng;
+    const float b = dot(n, ng);
+    V3 tangent;
+    if (b > 1e-4f) {
+        tangent = R + mul(n, fabsf(a) / b);
+        tangent = divs(tangent, len(tangent));
+    } else {
+        tangent = n;
+    }
+    tangent = tangent + mul(ng, 1e-4f);
+    return normalized(wo + tangent);
+}
+
+// ---------------------------------------------------------------- BSDFs
+enum : uint32_t { kDiffuse = 2, kMetal = 4, kGlass = 7 };
+
+// Material constants as the BSDF constructors evaluate them (src/ref/bsdf.cpp:60-66,
+// :146-158, :268-294); alpha values are computed on the host with the
+// reference's roughness remapping.
+struct Material_Dev {
+    uint32_t type;
+    float alpha_x, alpha_y, alpha;
+    Col reflectance, transmittance;
+    Col eta_t, k_t;
+    float eta_i_metal, ior;
+    float pad[2];
+};
+
+struct Bsdf {
+    uint32_t type;
+    V3 n, t, bt;
+    bool reflection, transmission;
+    Col reflectance, transmittance, eta_t, k_t;
+    float alpha_x, alpha_y, alpha, eta_i_metal, eta_o, eta_i;
+};
+
+__device__ __forceinline__ V3 local_to_world(const Bsdf& f, V3 l) {
+    return v3(f.t.x * l.x + f.bt.x * l.y + f.n.x * l.z, f.t.y * l.x + f.bt.y * l.y + f.n.y * l.z,
+              f.t.z * l.x + f.bt.z * l.y + f.n.z * l.z);
+}
+__device__ __forceinline__ V3 world_to_local(const Bsdf& f, V3 w) { return v3(dot(w, f.t), dot(w, f.bt), dot(w, f.n)); }
+
+__device__ __forceinline__ void make_bsdf(const Shading& sc, const Material_Dev& m, Bsdf& f) {
+    f.type = m.type;
+    f.n = sc.n;
+    f.bt = normalized(cross(sc.n, sc.dpdu_shading));
+    f.t = cross(f.bt, sc.n);
+    f.reflection = true;
+    f.transmission = m.type == kGlass;
+    f.reflectance = m.reflectance;
+    f.transmittance = m.transmittance;
+    f.eta_t = m.eta_t;
+    f.k_t = m.k_t;
+    f.alpha_x = m.alpha_x;
+    f.alpha_y = m.alpha_y;
+    f.alpha = m.alpha;
+    f.eta_i_metal = m.eta_i_metal;
+    const bool enter = !sc.flipped;
+    f.eta_o = enter ? 1.f : m.ior;
+    f.eta_i = enter ? m.ior : 1.f;
+}
+
+__device__ __forceinline__ V3 sample_hemisphere_cosine(float u0, float u1) {
+    const float z = sqrtf(1.f - u0);
+    const float r = sqrtf(u0);
+    const float phi = 2.f * kPi * u1;
+    return v3(r * cos_f(phi), r * sin_f(phi), z);
+}
+
+__device__ __forceinline__ float dielectric_fresnel(float cos_i, float eta) {
+    cos_i = min_std(fabsf(cos_i), 1.f);
+    const float sin_i = sqrtf(1.f - cos_i * cos_i);
+    const float sin_t = (1.f / eta) * sin_i;
+    if (sin_t >= 1.f) return 1.f;
+    const float cos_t = sqrtf(1.f - sin_t * sin_t);
+    const float Rp = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
+    const float Rs = (cos_i - eta * cos_t) / (cos_i + eta * cos_t);
+    return 0.5f * (Rp * Rp + Rs * Rs);
+}
+
+__device__ __forceinline__ Col conductor_fresnel(float cos_i, float eta_i, Col eta_t, Col k_t) {
+    cos_i = fabsf(clamp1(cos_i));
+    const float c2 = cos_i * cos_i;
+    const float s2 = 1.f - c2;
+    const Col eta = mul(eta_t, 1.f / eta_i);
+    const Col k = mul(k_t, 1.f / eta_i);
+    const Col eta2 = eta * eta;
+    const Col k2 = k * k;
+    const Col t0 = (eta2 - k2) - col(s2, s2, s2);
+    const Col a2b2 = csqrt(t0 * t0 + mul(eta2, 4.f) * k2);
+    const Col t1 = a2b2 + col(c2, c2, c2);
+    const Col a = csqrt(mul(a2b2 + t0, 0.5f));
+    const Col t2 = mul(a, 2.f * cos_i);
+    const Col Rs = (t1 - t2) / (t1 + t2);
+    const float s4 = s2 * s2;
+    const Col t3 = mul(a2b2, c2) + col(s4, s4, s4);
+    const Col t4 = mul(t2, s2);
+    const Col Rp = (Rs * (t3 - t4)) / (t3 + t4);
+    return mul(Rp + Rs, 0.5f);
+}
+
+__device__ __forceinline__ float ggx_D(V3 wh, V3 n, float alpha) {
+    const float c = dot(wh, n);
+    if (c <= 0.f) return 0.f;
+    const float c2 = c * c;
+    const float a2 = alpha * alpha;
+    const float k = c2 * (a2 - 1) + 1;
+    return a2 / (kPi * k * k);
+}
+__device__ __forceinline__ float ggx_D_aniso(V3 wh, float ax, float ay) {
+    const float c = clamp1(wh.z);
+    const float c2 = c * c;
+    const float s2 = 1.f - c2;
+    const float s2inv = 1.f / s2;
+    const float cos2_phi = (s2 == 0.f) ? 1.f : (wh.x * wh.x) * s2inv;
+    const float sin2_phi = (s2 == 0.f) ? 0.f : (wh.y * wh.y) * s2inv;
+    const float k = c2 + s2 * (cos2_phi / (ax * ax) + sin2_phi / (ay * ay));
+    return 1.f / (kPi * ax * ay * k * k);
+}
+__device__ __forceinline__ float ggx_lambda(V3 v, V3 n, float alpha) {
+    const float c = dot(v, n);
+    const float c2 = c * c;
+    const float tan2 = max_std(0.f, (1.f - c2) / c2);
+    return 0.5f * (-1.f + sqrtf(1.f + alpha * alpha * tan2));
+}
+__device__ __forceinline__ float ggx_lambda_aniso(V3 v, float ax, float ay) {
+    const float c = clamp1(v.z);
+    const float c2 = c * c;
+    const float s2 = 1.f - c2;
+    const float tan2 = s2 / c2;
+    const float s2inv = 1.f / s2;
+    const float cos2_phi = (s2 == 0.f) ? 1.f : (v.x * v.x) * s2inv;
+    const float sin2_phi = (s2 == 0.f) ? 0.f : (v.y * v.y) * s2inv;
+    const float alpha2 = cos2_phi * ax * ax + sin2_phi * ay * ay;
+    return 0.5f * (-1.f + sqrtf(1.f + alpha2 * tan2));
+}
+__device__ __forceinline__ float ggx_G(V3 wi, V3 wo, V3 n, float a) {
+    return 1.f / (1.f + ggx_lambda(wi, n, a) + ggx_lambda(wo, n, a));
+}
+__device__ __forceinline__ float ggx_G1(V3 v, V3 n, float a) { return 1.f / (1.f + ggx_lambda(v, n, a)); }
+__device__ __forceinline__ float ggx_G_aniso(V3 wi, V3 wo, float ax, float ay) {
+    return 1.f / (1.f + ggx_lambda_aniso(wi, ax, ay) + ggx_lambda_aniso(wo, ax, ay));
+}
+__device__ __forceinline__ float ggx_G1_aniso(V3 v, float ax, float ay) {
+    return 1.f / (1.f + ggx_lambda_aniso(v, ax, ay));
+}
+
+// GGX_sample_visible_microfacet_normal (src/ref/sampling.cpp:310-335)
+__device__ __forceinline__ V3 ggx_sample_vndf(float u0, float u1, V3 wo, float ax, float ay) {
+    const V3 N = normalized(v3(ax * wo.x, ay * wo.y, wo.z));
+    const float len_sq = N.x * N.x + N.y * N.y;
+    const V3 T1 = len_sq > 0.f ? divs(v3(-N.y, N.x, 0.f), sqrtf(len_sq)) : v3(1.f, 0.f, 0.f);
+    const V3 T2 = cross(N, T1);
+    const float r = sqrtf(u0);
+    const float phi = 2.f * kPi * u1;
+    const float t1 = r * cos_f(phi);
+    float t2 = r * sin_f(phi);
+    const float s = 0.5f * (1.f + N.z);
+    t2 = (1.f - s) * sqrtf(1.f - t1 * t1) + s * t2;
+    const V3 nh = (mul(T1, t1) + mul(T2, t2)) + mul(N, sqrtf(max_std(0.f, 1.f - t1 * t1 - t2 * t2)));
+    return normalized(v3(ax * nh.x, ay * nh.y, max_std(1e-6f, nh.z)));
+}
+__device__ __forceinline__ float vndf_pdf(V3 wo, V3 wh, V3 n, float alpha) {
+    const float G1 = ggx_G1(wo, n, alpha);
+    const float D = ggx_D(wh, n, alpha);
+    return G1 * D * max_std(0.f, dot(wo, wh)) / dot(wo, n);
+}
+__device__ __forceinline__ float vndf_pdf_aniso(V3 wo, V3 wh, float ax, float ay) {
+    const float G1 = ggx_G1_aniso(wo, ax, ay);
+    const float D = ggx_D_aniso(wh, ax, ay);
+    return G1 * D * max_std(0.f, dot(wo, wh)) / wo.z;
+}
+__device__ __forceinline__ V3 refraction_half(float eta_o, V3 wo, float eta_i, V3 wi, V3 n) {
+    V3 wh = -normalized(mul(wo, eta_o) + mul(wi, eta_i));
+    if (dot(wh, n) < 0.f) wh = -wh;
+    return wh;
+}
+__device__ __forceinline__ float glass_reflection_probability(const Bsdf& f, float fresnel) {
+    const float max_r = max_component(f.reflectance), max_t = max_component(f.transmittance);
+    const float ratio = max_r / (max_r + max_t);
+    const float r = fresnel * ratio;
+    const float t = (1.f - fresnel) * (1 - ratio);
+    return ((r + t) == 0) ? 0.f : r / (r + t);
+}
+
+__device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
+    if (f.type == kDiffuse) return mul(f.reflectance, 1.f / kPi);
+    if (f.type == kMetal) {
+        const V3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
+        const V3 wh_l = normalized(wo_l + wi_l);
+        const float cos_i = dot(wi_l, wh_l);
+        const Col F = conductor_fresnel(cos_i, f.eta_i_metal, f.eta_t, f.k_t);
+        const float G = ggx_G_aniso(wi_l, wo_l, f.alpha_x, f.alpha_y);
+        const float D = ggx_D_aniso(wh_l, f.alpha_x, f.alpha_y);
+        return mul(F, (G * D) / (4.f * wo_l.z * wi_l.z));
+    }
+    const bool same = dot(wo, f.n) * dot(wi, f.n) > 0.f;
+    if (same) {
+        const V3 wh = normalized(wo + wi);
+        const float cos_i = dot(wi, wh);
+        const float F = dielectric_fresnel(cos_i, f.eta_i / f.eta_o);
+        const float G = ggx_G(wi, wo, f.n, f.alpha);
+        const float D = ggx_D(wh, f.n, f.alpha);
+        const float base = (F * G * D) / (4.f * dot(wo, f.n) * dot(wi, f.n));
+        return mul(f.reflectance, base);
+    }
+    const V3 wh = refraction_half(f.eta_o, wo, f.eta_i, wi, f.n);
+    const float wo_wh = dot(wo, wh), wi_wh = dot(wi, wh);
+    if (wo_wh * wi_wh > 0.f) return col(0.f, 0.f, 0.f);
+    const float cos_i = dot(wi, wh);
+    const float F = dielectric_fresnel(cos_i, f.eta_o / f.eta_i);
+    if (F == 1.f) return col(0.f, 0.f, 0.f);
+    const float G = ggx_G(wi, wo, f.n, f.alpha);
+    const float D = ggx_D(wh, f.n, f.alpha);
+    const float wo_n = dot(wo, f.n), wi_n = dot(wi, f.n);
+    const float k = fabsf((wo_wh * wi_wh) / (wo_n * wi_n));
+    const float k2 = f.eta_o * wo_wh + f.eta_i * wi_wh;
+    const float base = (f.eta_o * f.eta_o * k * G * D * (1.f - F)) / (k2 * k2);
+    return mul(f.transmittance, base);
+}
+
+__device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
+    if (f.type == kDiffuse) return dot(f.n, wi) / kPi;
+    if (f.type == kMetal) {
+        const V3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
+        const V3 wh_l = normalized(wo_l + wi_l);
+        return vndf_pdf_aniso(wo_l, wh_l, f.alpha_x, f.alpha_y) / (4 * dot(wh_l, wo_l));
+    }
+    const bool same = dot(wo, f.n) * dot(wi, f.n) > 0.f;
+    if (same) {
+        const V3 wh = normalized(wo + wi);
+        const float rp = vndf_pdf(wo, wh, f.n, f.alpha) / (4 * dot(wh, wo));
+        const float cos_i = dot(wi, wh);
+        const float fr = dielectric_fresnel(cos_i, f.eta_i / f.eta_o);
+        return rp * glass_reflection_probability(f, fr);
+    }
+    const V3 wh = refraction_half(f.eta_o, wo, f.eta_i, wi, f.n);
+    const float wo_wh = dot(wo, wh), wi_wh = dot(wi, wh);
+    if (wo_wh * wi_wh > 0.f) return 0.f;
+    const float fr = dielectric_fresnel(dot(wo, wh), f.eta_i / f.eta_o);
+    const float rprob = glass_reflection_probability(f, fr);
+    const float wh_pdf = vndf_pdf(wo, wh, f.n, f.alpha);
+    const float denom = f.eta_o * dot(wo, wh) + f.eta_i * dot(wi, wh);
+    const float dwh = f.eta_i * f.eta_i * fabsf(dot(wi, wh)) / (denom * denom);
+    return (wh_pdf * dwh) * (1.f - rprob);
+}
+
+// BSDF::sample of the three BSDFs; black when no direction is produced.
+__device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
+                                           float& pdf) {
+    if (f.type == kDiffuse) {
+        wi = local_to_world(f, sample_hemisphere_cosine(u0, u1));
+        pdf = bsdf_pdf(f, wo, wi);
+        return bsdf_evaluate(f, wo, wi);
+    }
+    if (f.type == kMetal) {
+        const V3 wo_l = world_to_local(f, wo);
+        const V3 wh_l = ggx_sample_vndf(u0, u1, wo_l, f.alpha_x, f.alpha_y);
+        const V3 wi_l = reflect(wo_l, wh_l);
+        if (wi_l.z <= 0.f) return col(0.f, 0.f, 0.f);
+        wi = local_to_world(f, wi_l);
+        pdf = vndf_pdf_aniso(wo_l, wh_l, f.alpha_x, f.alpha_y) / (4 * dot(wh_l, wo_l));
+        return bsdf_evaluate(f, wo, wi);
+    }
+    const V3 wo_l = world_to_local(f, wo);
+    const V3 wh = local_to_world(f, ggx_sample_vndf(u0, u1, wo_l, f.alpha, f.alpha));
+    const V3 rwi = reflect(wo, wh);
+    if (dot(rwi, f.n) <= 0.f) return col(0.f, 0.f, 0.f);
+    const float fresnel = dielectric_fresnel(dot(wo, wh), f.eta_i / f.eta_o);
+    const float rprob = glass_reflection_probability(f, fresnel);
+    if (u_scatter < rprob) {
+        wi = rwi;
+    } else {
+        if (!refract(wo, wh, f.eta_o / f.eta_i, wi)) return col(0.f, 0.f, 0.f);
+        if (dot(wi, f.n) >= 0.f) return col(0.f, 0.f, 0.f);
+    }
+    pdf = bsdf_pdf(f, wo, wi);
+    if (pdf == 0.f) return col(0.f, 0.f, 0.f);
+    return bsdf_evaluate(f, wo, wi);
+}
+
+// mis_power_heuristic (src/ref/direct_lighting.cpp:18-24)
+__device__ __forceinline__ float mis_power(float p1, float p2) {
+    if (p1 == __int_as_float(0x7f800000)) return 1.f;
+    return p1 * p1 / (p1 * p1 + p2 * p2);
+}
+
+// ---------------------------------------------------------------- pcg32
+// pcg32 (third-party/pcg/pcg_basic.c:46-75) and RNG::get_float / bounded
+// draws (src/lib/random.h:17-72)
+struct Pcg {
+    uint64_t state, inc;
+};
+__device__ __forceinline__ uint32_t pcg_next(Pcg& r) {
+    const uint64_t old = r.state;
+    r.state = old * 6364136223846793005ULL + r.inc;
+    const uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
+    const uint32_t rot = (uint32_t)(old >> 59u);
+    return (xs >> rot) | (xs << ((-rot) & 31));
+}
+__device__ __forceinline__ Pcg pcg_seed(uint64_t initstate, uint64_t initseq) {
+    Pcg r;
+    r.state = 0u;
+    r.inc = (initseq << 1u) | 1u;
+    pcg_next(r);
+    r.state += initstate;
+    pcg_next(r);
+    return r;
+}
+__device__ __forceinline__ float pcg_float(Pcg& r) {
+    return __uint_as_float((pcg_next(r) >> 9) | 0x3f800000u) - 1.0f;
+}
+__device__ __forceinline__ uint32_t pcg_bounded_fast(Pcg& r, uint32_t bound) {
+    return (uint32_t)(((uint64_t)pcg_next(r) * bound) >> 32);
+}
+
+} // namespace yar

@@ -179,8 +179,11 @@ def _box(center, size, angle_deg):
     return v, idx
 
 
-def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0):
-    """pbrt-v3 text of the seeded Cornell box (34 triangles + a quad light)."""
+def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0, box_materials=None):
+    """pbrt-v3 text of the seeded Cornell box (34 triangles + a quad light).
+
+    box_materials: None for matte boxes, or two pbrt material statements for
+    the short and the tall box (e.g. metal and rough glass)."""
     rng = np.random.default_rng(seed)
     k = int(math.ceil(math.sqrt(spp)))
     shapes = []
@@ -212,9 +215,12 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
         'PixelFilter "box"',
         "WorldBegin",
     ]
-    for v, i, albedo in shapes:
+    for k, (v, i, albedo) in enumerate(shapes):
+        material = 'Material "matte" "rgb Kd" [%s]' % fmt(albedo)
+        if box_materials is not None and k >= 5:
+            material = box_materials[k - 5]
         out += ["AttributeBegin",
-                '  Material "matte" "rgb Kd" [%s]' % fmt(albedo),
+                '  ' + material,
                 '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(i), fmt(v)),
                 "AttributeEnd"]
     out += ["AttributeBegin",
@@ -223,3 +229,8 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
             "AttributeEnd",
             "WorldEnd", ""]
     return "\n".join(out)
+
+
+GGX_BOXES = ('Material "metal" "float roughness" [0.2] "rgb eta" [0.2 0.92 1.1] "rgb k" [3.9 2.45 2.14]',
+             'Material "glass" "float uroughness" [0.3] "float vroughness" [0.3] "float index" [1.5] '
+             '"rgb Kr" [1 1 1] "rgb Kt" [1 1 1]')
