@@ -252,6 +252,30 @@ int yar_gpu_cast_any_timed(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t ray_c
  * stats may be NULL. */
 int yar_gpu_render(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats);
 
+/* ---- render without allocation ----
+ * No counterpart in the reference.  yar_gpu_render allocates its working
+ * memory (path state, ray queues, per-sample film data) with cudaMalloc on
+ * every call.  Callers that must not allocate device memory at render time -
+ * an application running under a fixed, pre-reserved memory budget, a host
+ * that forbids allocation after start-up for latency reasons, or code whose
+ * device allocator is owned by someone else - use this entry point instead:
+ * it renders exactly like yar_gpu_render but takes all working memory from
+ * one static device array of YAR_GPU_STATIC_ARENA_BYTES (64 MiB) that is
+ * linked into the library (every GPU that loads the library keeps it until
+ * the process exits), and it calls no cudaMalloc, cudaFree or other
+ * allocating routine.
+ *   rgb_out_device: device memory of the context's device, float3 per pixel of
+ *                   the render region (the caller allocates it).
+ *   Renders whose film data and one chunk of paths do not fit in the array
+ *   are rejected with YAR_ERR_CAPACITY (a 256x256 image at 16 samples per
+ *   pixel fits).
+ * The first call on a device looks up the array's device address
+ * (cudaGetSymbolAddress); make that first call before any stream capture.
+ * All calls on a device share the one array and leave their data in it:
+ * calls that overlap on the GPU (from different streams or contexts) race. */
+#define YAR_GPU_STATIC_ARENA_BYTES (64u << 20)
+int yar_gpu_render_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats* stats);
+
 /* ---- host-side kd-tree builders (the reference's builder, same node stream) ----
  * The returned node array is owned by the library; release it with yar_free_nodes. */
 int yar_build_mesh_kdtree(const float* vertices, uint32_t vertex_count,

@@ -30,6 +30,7 @@
 #include <chrono>
 #include <cmath>
 #include <cstring>
+#include <mutex>
 
 namespace yar {
 
@@ -1014,7 +1015,240 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
     return YAR_OK;
 }
 
+// ---------------------------------------------------------------- render without allocation
+// yar_gpu_render_static: the same kernels as render_run, with every working
+// buffer carved out of one static device array instead of cudaMalloc'ed.
+// Rendering is chunked by the space left after the per-sample film data, so
+// the result is the same as render_run's (per-path results do not depend on
+// the chunking).
+namespace {
+
+__device__ __align__(256) unsigned char g_static_arena[YAR_GPU_STATIC_ARENA_BYTES];
+
+std::mutex g_arena_mutex;
+unsigned char* g_arena_address[64] = {};  // device address of g_static_arena per device ordinal
+
+// Sum of the tile variance accumulators in tile order, divided by the
+// sample-region area (render_scene, src/ref/reference_renderer.cpp:570-581).
+__global__ void variance_total_kernel(Render_Params p, const double* __restrict__ tile_variance,
+                                      double* __restrict__ out) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    double acc = 0.0;
+    int64_t count = 0;
+    for (int t = 0; t < p.tiles_x * p.tiles_y; t++) {
+        acc += tile_variance[t];
+        int x0, y0, x1, y1;
+        tile_sample_bounds(p, t, x0, y0, x1, y1);
+        count += (int64_t)(x1 - x0) * (y1 - y0);
+    }
+    *out = p.spp > 1 ? acc / (double)count : 0.0;
+}
+
+struct Arena {
+    unsigned char* base;
+    size_t size, used;
+    template <class T>
+    T* take(size_t count) {
+        used = (used + 255) & ~(size_t)255;
+        const size_t bytes = count * sizeof(T);
+        if (bytes > size || used > size - bytes) return nullptr;
+        T* p = reinterpret_cast<T*>(base + used);
+        used += bytes;
+        return p;
+    }
+};
+
+} // namespace
+
+int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats* stats) {
+    const Render_Scene& R = ctx->render;
+    const yar_render_config& c = R.config;
+    if (!rgb_out_device) return fail(ctx, YAR_ERR_INVALID, "null image buffer");
+    if (c.rendering_algorithm != 1) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the path tracer is implemented");
+    if (c.pixel_filter_type != 0) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the box filter is implemented");
+    if (R.other_light_count) return fail(ctx, YAR_ERR_UNSUPPORTED, "only rectangular area lights are implemented");
+    if (R.host_rect_lights.empty()) return fail(ctx, YAR_ERR_UNSUPPORTED, "scene has no light");
+    for (const yar_material_desc& m : R.host_materials) {
+        if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL && m.type != YAR_MATERIAL_GLASS)
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "material type " + std::to_string(m.type) + " is not implemented");
+        if (m.type == YAR_MATERIAL_GLASS && !(m.u_roughness > 0.f))
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "smooth (delta) glass is not implemented");
+    }
+    const size_t n_obj = R.host_object_info.size() / 4;
+    for (size_t i = 0; i < n_obj; i++) {
+        const int32_t* o = &R.host_object_info[4 * i];
+        const bool light = (uint32_t)o[2] != YAR_LIGHT_NULL;
+        if (light && ((uint32_t)o[2] != YAR_LIGHT_DIFFUSE_RECTANGULAR || o[3] < 0 ||
+                      (size_t)o[3] >= R.host_rect_lights.size()))
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "object " + std::to_string(i) + ": unsupported area light");
+        if (!light && (o[1] < 0 || (size_t)o[1] >= R.host_materials.size()))
+            return fail(ctx, YAR_ERR_INVALID, "object " + std::to_string(i) + " has no valid material");
+    }
+    const int nx = c.x_pixel_sample_count, ny = c.y_pixel_sample_count;
+    if (nx <= 0 || ny <= 0 || (int64_t)nx * ny > 4096)
+        return fail(ctx, YAR_ERR_INVALID, "pixel sample counts must be in 1..4096 samples per pixel");
+    if (c.max_light_bounces < 0 || c.max_light_bounces > 200) return fail(ctx, YAR_ERR_INVALID, "max_light_bounces");
+
+    Render_Params p{};
+    p.camera = R.camera;
+    p.rx0 = c.render_region[0];
+    p.ry0 = c.render_region[1];
+    p.rw = c.render_region[2] - c.render_region[0];
+    p.rh = c.render_region[3] - c.render_region[1];
+    if (p.rw <= 0 || p.rh <= 0 || c.render_region[2] > 0xffff + 1 || c.render_region[3] > 0xffff + 1)
+        return fail(ctx, YAR_ERR_INVALID, "render region");
+    const float radius = c.pixel_filter_radius;
+    p.sx0 = (int)std::floor((float)p.rx0 + 0.5f - radius);
+    p.sy0 = (int)std::floor((float)p.ry0 + 0.5f - radius);
+    p.sw = (int)std::ceil((float)(p.rx0 + p.rw - 1) + 0.5f + radius) - p.sx0;
+    p.sh = (int)std::ceil((float)(p.ry0 + p.rh - 1) + 0.5f + radius) - p.sy0;
+    p.tiles_x = (p.sw + kTile - 1) / kTile;
+    p.tiles_y = (p.sh + kTile - 1) / kTile;
+    p.nx = nx;
+    p.ny = ny;
+    p.spp = nx * ny;
+    const int maxb = std::min(10, c.max_light_bounces);
+    p.n1d = maxb * 4;
+    p.n2d = maxb * 3;
+    p.max_bounces = c.max_light_bounces;
+    p.rr_bounce_threshold = c.russian_roulette_bounce_count_threshold;
+    p.rr_threshold = c.russian_roulette_threshold;
+    p.filter_radius = radius;
+    p.film_scale = c.film_radiance_scale;
+    p.max_component = c.max_rgb_component_value_of_film_sample;
+    p.rect_lights = (int)R.host_rect_lights.size();
+    p.total_lights = p.rect_lights + (int)R.other_light_count;
+    p.seed_offset = (uint32_t)c.rng_seed_offset;
+
+    cudaSetDevice(ctx->device);
+    if (ctx->device < 0 || ctx->device >= 64) return fail(ctx, YAR_ERR_INVALID, "device ordinal above 63");
+    unsigned char* arena_base = nullptr;
+    {
+        std::lock_guard<std::mutex> lock(g_arena_mutex);
+        if (!g_arena_address[ctx->device]) {
+            void* addr = nullptr;
+            cudaError_t e = cudaGetSymbolAddress(&addr, g_static_arena);
+            if (e != cudaSuccess) return cuda_fail(ctx, e, "cudaGetSymbolAddress(static render arena)");
+            g_arena_address[ctx->device] = static_cast<unsigned char*>(addr);
+        }
+        arena_base = g_arena_address[ctx->device];
+    }
+    const auto t_start = std::chrono::steady_clock::now();
+    const uint64_t pixels = (uint64_t)p.sw * p.sh;
+    const uint64_t samples = pixels * p.spp;
+    const uint64_t tiles = (uint64_t)p.tiles_x * p.tiles_y;
+
+    // film data for the whole image first, then as many paths per chunk as fit
+    Arena A{arena_base, YAR_GPU_STATIC_ARENA_BYTES, 0};
+    float4* radiance = A.take<float4>(samples);
+    float2* image_samples = A.take<float2>(samples);
+    double* pixel_variance = A.take<double>(pixels);
+    double* tile_variance = A.take<double>(tiles);
+    double* variance_total = A.take<double>(1);
+    uint32_t* counters = A.take<uint32_t>(8);
+    const int kChunkBuffers = 24;
+    const size_t per_path = 4 * (size_t)std::max(1, p.n1d) + 8 * (size_t)std::max(1, p.n2d) + 157 + 168;
+    const size_t left = (radiance && image_samples && pixel_variance && tile_variance && variance_total && counters &&
+                         A.size > A.used + 256 * kChunkBuffers)
+                            ? A.size - A.used - 256 * kChunkBuffers
+                            : 0;
+    const uint64_t chunk_pixels = std::min<uint64_t>(pixels, left / per_path / p.spp);
+    if (chunk_pixels == 0)
+        return fail(ctx, YAR_ERR_CAPACITY,
+                    "render of " + std::to_string(samples) + " samples does not fit the " +
+                        std::to_string(YAR_GPU_STATIC_ARENA_BYTES >> 20) + " MiB static arena");
+    const uint64_t cap = chunk_pixels * p.spp;
+    float* s1d = A.take<float>(cap * std::max(1, p.n1d));
+    float2* s2d = A.take<float2>(cap * std::max(1, p.n2d));
+    Path_State ps{A.take<float4>(cap), A.take<float4>(cap), A.take<uint32_t>(cap), A.take<uint4>(cap),
+                  A.take<float4>(cap), A.take<float4>(cap), A.take<float4>(cap), A.take<float4>(cap),
+                  A.take<float4>(cap), A.take<uint8_t>(cap), A.take<float4>(cap), A.take<uint2>(cap)};
+    Queues q{};
+    q.ext_rays[0] = A.take<float4>(2 * cap);
+    q.ext_rays[1] = A.take<float4>(2 * cap);
+    q.ext_slot[0] = A.take<uint32_t>(cap);
+    q.ext_slot[1] = A.take<uint32_t>(cap);
+    q.ext_hit4 = A.take<float4>(cap);
+    q.ext_hit2 = A.take<uint2>(cap);
+    q.shd_rays = A.take<float4>(2 * cap);
+    q.shd_slot = A.take<uint32_t>(cap);
+    q.prb_rays = A.take<float4>(2 * cap);
+    q.prb_slot = A.take<uint32_t>(cap);
+    q.counters = counters;
+    if (!s1d || !s2d || !ps.probe_hit2 || !q.prb_slot)
+        return fail(ctx, YAR_ERR_CAPACITY, "static arena layout overflow");
+    Scene_Dev S{ctx->ds, dptr<float4>(ctx->render.shading), dptr<float4>(ctx->render.object_info),
+                dptr<Material_Dev>(ctx->render.materials), dptr<Rect_Light_Dev>(ctx->render.rect_lights)};
+
+    cudaStream_t st = ctx->stream;
+    cudaError_t e = cudaMemsetAsync(q.counters, 0, 8 * sizeof(uint32_t), st);  // the arena keeps the last call's data
+    uint64_t rays_closest = 0, rays_any = 0;
+    uint32_t launches = 0;
+    for (uint64_t first = 0; first < pixels && e == cudaSuccess; first += chunk_pixels) {
+        const uint32_t cp = (uint32_t)std::min<uint64_t>(chunk_pixels, pixels - first);
+        const uint32_t paths = cp * (uint32_t)p.spp;
+        generate_kernel<<<(cp + kBlock - 1) / kBlock, kBlock, 0, st>>>(p, (uint32_t)first, cp, s1d,
+                                                                       reinterpret_cast<float*>(s2d), image_samples,
+                                                                       ps, q);
+        launches++;
+        int cur = 0;
+        uint32_t count = paths;
+        for (int bounce = 0; count > 0 && bounce <= p.max_bounces + 1; bounce++) {
+            closest_queue_kernel<false><<<grid_for(count), kBlock, 0, st>>>(ctx->ds, q.ext_rays[cur], nullptr, nullptr,
+                                                                         count, q.ext_hit4, q.ext_hit2, q.counters + 3);
+            cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
+            shade_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, cur, count, s1d, s2d, ps, q);
+            shadow_queue_kernel<<<grid_for(count), kBlock, 0, st>>>(ctx->ds, q.shd_rays, q.shd_slot, q.counters + 1,
+                                                                    ps.occluded, q.counters + 3);
+            closest_queue_kernel<true><<<grid_for(count), kBlock, 0, st>>>(ctx->ds, q.prb_rays, q.prb_slot,
+                                                                        q.counters + 2, 0, ps.probe_hit4,
+                                                                        ps.probe_hit2, q.counters + 3);
+            connect_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, q.ext_slot[cur], count, ps);
+            launches += 5;
+            uint32_t h[4];
+            e = cudaMemcpyAsync(h, q.counters, sizeof(h), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) break;
+            if (h[3]) return fail(ctx, YAR_ERR_CAPACITY, "kd-tree traversal stack overflow");
+            rays_closest += count + h[2];
+            rays_any += h[1];
+            count = h[0];
+            cur ^= 1;
+        }
+        finish_chunk_kernel<<<grid_for(paths), kBlock, 0, st>>>(paths, first * p.spp, ps, radiance);
+        launches++;
+    }
+    double variance = 0.0;
+    if (e == cudaSuccess) {
+        samples_kernel<<<(uint32_t)((pixels + kBlock - 1) / kBlock), kBlock, 0, st>>>(p, radiance, pixel_variance);
+        tile_variance_kernel<<<(uint32_t)((tiles + 63) / 64), 64, 0, st>>>(p, pixel_variance, tile_variance);
+        variance_total_kernel<<<1, 1, 0, st>>>(p, tile_variance, variance_total);
+        film_kernel<<<(uint32_t)(((uint64_t)p.rw * p.rh + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+            p, radiance, image_samples, rgb_out_device);
+        launches += 4;
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&variance, variance_total, sizeof(double), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "static render");
+    if (stats) {
+        stats->variance = variance;
+        stats->seconds = (float)std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        stats->paths = samples;
+        stats->rays_closest = rays_closest;
+        stats->rays_any = rays_any;
+        stats->kernel_launches = launches;
+    }
+    return YAR_OK;
+}
+
 } // namespace yar
+
+extern "C" int yar_gpu_render_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats* stats) {
+    if (!ctx) return YAR_ERR_INVALID;
+    if (!ctx->has_scene) return yar::fail(ctx, YAR_ERR_NO_SCENE, "no scene uploaded");
+    return yar::render_run_static(ctx, rgb_out_device, stats);
+}
 
 extern "C" int yar_gpu_render(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
     if (!ctx) return YAR_ERR_INVALID;

@@ -118,6 +118,7 @@ EXPORTS = {
                                              C.POINTER(C.c_float)]),
     "yar_gpu_cast_any_timed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_float)]),
     "yar_gpu_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
+    "yar_gpu_render_static": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
     "yar_build_mesh_kdtree": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_int32,
                                         C.POINTER(C.c_float), C.POINTER(C.c_void_p), C.POINTER(C.c_uint32)]),
     "yar_build_scene_kdtree": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_void_p),
@@ -279,3 +280,11 @@ class Context:
         stats = RenderStats()
         self._check(lib().yar_gpu_render(self._h, _ptr(rgb), C.byref(stats)), "render")
         return rgb, stats
+
+    def render_static(self, rgb_device_ptr):
+        """yar_gpu_render_static: renders into caller-owned device memory
+        without allocating (working memory comes from the library's static
+        device arena)."""
+        stats = RenderStats()
+        self._check(lib().yar_gpu_render_static(self._h, rgb_device_ptr, C.byref(stats)), "render_static")
+        return stats
