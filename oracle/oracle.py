@@ -176,3 +176,20 @@ def ref_cast(flat, rays, any_hit=False, threads=0, repeat=1):
     obj = raw[8 * n:12 * n].view(np.uint32)
     bary = raw[12 * n:20 * n].view(np.float32).reshape(n, 2)
     return (t, prim, obj, bary), info
+
+
+def ref_render_flat(flat, spp=0, threads=0):
+    """The reference renderer on a flat scene (harness render-yfs)."""
+    with tempfile.TemporaryDirectory() as d:
+        s, out = os.path.join(d, "s.yfs"), os.path.join(d, "img.bin")
+        flat.write(s)
+        args = ["render-yfs", s, out, "--threads=%d" % (threads or os.cpu_count() or 1)]
+        if spp:
+            args.append("--spp=%d" % spp)
+        info = _ref(*args)
+        raw = open(out, "rb").read()
+    w, h = np.frombuffer(raw[:8], np.uint32)
+    variance = float(np.frombuffer(raw[8:16], np.float64)[0])
+    img = np.frombuffer(raw[20:], np.float32).reshape(int(h), int(w), 3).copy()
+    info.update(variance=variance)
+    return img, info

@@ -24,6 +24,11 @@
 //       f32 t[n], u32 prim[n], u32 obj[n], f32 bary[2n]; any writes u8[n].
 //       Prints {"rays":..,"seconds":..,"threads":..} on stdout.
 #include "std.h"
+// render-yfs sets the reference Camera's fields to the flat scene's exact
+// values; Camera keeps them private (src/ref/camera.h:41-48).
+#define private public
+#include "ref/camera.h"
+#undef private
 #include "lib/common.h"
 #include "lib/scene.h"
 #include "lib/scene_loader.h"
@@ -486,6 +491,132 @@ int cmd_cast(const Args& a) {
 // previous hit point, axis-aligned directions with probability 1/32 per axis.
 // Checks kd-tree t == brute-force t like the reference test and writes
 // f32 origin[3], f32 direction[3], f32 t, u32 prim per ray.
+// render-yfs <in.yfs> <out.img> [--threads=T] [--spp=N]
+// A flat scene (meshes, constant materials, rectangular lights, camera,
+// config) rebuilt as a reference Scene, initialised with init_scene_context
+// (reference kd-tree builder) and rendered with render_scene.  Used for
+// scenes generated without a pbrt file (the large wavefront workload).
+int cmd_render_yfs(const Args& a) {
+    if (a.pos.size() < 2) return 2;
+    yfs::Scene fs_scene;
+    std::string err;
+    if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
+    if (fs_scene.other_light_count) { fprintf(stderr, "only rectangular lights are supported\n"); return 1; }
+    Scene scene;
+    scene.type = fs_scene.config.pbrt3_scene ? Scene_Type::pbrt : Scene_Type::obj;
+    scene.path = a.pos[0];
+    for (const yfs::Mesh& fm : fs_scene.meshes) {
+        Triangle_Mesh m;
+        m.vertices.resize(fm.vertices.size() / 3);
+        memcpy(m.vertices.data(), fm.vertices.data(), fm.vertices.size() * 4);
+        m.normals.resize(fm.normals.size() / 3);
+        if (!fm.normals.empty()) memcpy(m.normals.data(), fm.normals.data(), fm.normals.size() * 4);
+        m.uvs.resize(fm.uvs.size() / 2);
+        if (!fm.uvs.empty()) memcpy(m.uvs.data(), fm.uvs.data(), fm.uvs.size() * 4);
+        m.indices = fm.indices;
+        m.reverse_geometric_normal_orientation = fm.reverse_orientation != 0;
+        m.visibility = (Visibility)fm.visibility;
+        scene.geometries.triangle_meshes.push_back(std::move(m));
+    }
+    std::vector<Material_Handle> handles;
+    for (const yar_material_desc& d : fs_scene.materials) {
+        if (d.type == YAR_MATERIAL_DIFFUSE) {
+            Diffuse_Material m;
+            set_constant_parameter(m.reflectance, ColorRGB(d.reflectance));
+            scene.materials.diffuse.push_back(m);
+            handles.push_back({Material_Type::diffuse, (int)scene.materials.diffuse.size() - 1});
+        } else if (d.type == YAR_MATERIAL_METAL) {
+            Metal_Material m;
+            set_constant_parameter(m.u_roughness, d.u_roughness);
+            set_constant_parameter(m.v_roughness, d.v_roughness);
+            m.roughness_is_alpha = d.roughness_is_alpha != 0;
+            set_constant_parameter(m.eta_i, d.eta_i);
+            set_constant_parameter(m.eta, ColorRGB(d.eta));
+            set_constant_parameter(m.k, ColorRGB(d.k));
+            scene.materials.metal.push_back(m);
+            handles.push_back({Material_Type::metal, (int)scene.materials.metal.size() - 1});
+        } else if (d.type == YAR_MATERIAL_GLASS) {
+            Glass_Material m;
+            set_constant_parameter(m.reflectance, ColorRGB(d.reflectance));
+            set_constant_parameter(m.transmittance, ColorRGB(d.transmittance));
+            set_constant_parameter(m.index_of_refraction, d.index_of_refraction);
+            set_constant_parameter(m.roughness, d.u_roughness);
+            m.roughness_is_alpha = d.roughness_is_alpha != 0;
+            scene.materials.glass.push_back(m);
+            handles.push_back({Material_Type::glass, (int)scene.materials.glass.size() - 1});
+        } else {
+            fprintf(stderr, "unsupported material type %u\n", d.type);
+            return 1;
+        }
+    }
+    for (const yar_rect_light_desc& d : fs_scene.rect_lights) {
+        Diffuse_Rectangular_Light l;
+        l.light_to_world_transform = floats_to_matrix(d.light_to_world);
+        l.emitted_radiance = ColorRGB(d.emitted_radiance);
+        l.size = Vector2(d.size[0], d.size[1]);
+        l.sample_count = d.sample_count;
+        scene.lights.diffuse_rectangular_lights.push_back(l);
+    }
+    scene.lights.update_total_light_count();
+    for (const yar_object_desc& d : fs_scene.objects) {
+        Scene_Object o;
+        o.geometry = {Geometry_Type::triangle_mesh, d.mesh_index};
+        o.material = d.material_index >= 0 ? handles[d.material_index] : Null_Material;
+        o.area_light = {(Light_Type)d.area_light_type, d.area_light_index};
+        o.object_to_world_transform = floats_to_matrix(d.object_to_world);
+        o.world_to_object_transform = floats_to_matrix(d.world_to_object);
+        o.object_to_world_normal_transform = floats_to_matrix(d.object_to_world_normal);
+        scene.objects.push_back(o);
+    }
+    const yar_render_config& c = fs_scene.config;
+    scene.film_resolution = Vector2i{(int)fs_scene.camera.image_extent[0], (int)fs_scene.camera.image_extent[1]};
+    scene.render_region = Bounds2i{{c.render_region[0], c.render_region[1]}, {c.render_region[2], c.render_region[3]}};
+    scene.camera_fov_y = 40.f;  // replaced by the flat scene's exact camera below
+    scene.z_is_up = fs_scene.camera.z_is_up != 0;
+    scene.view_points = {floats_to_matrix(fs_scene.camera.camera_to_world)};
+    Raytracer_Config& rc = scene.raytracer_config;
+    rc.rendering_algorithm = (Raytracer_Config::Rendering_Algorithm)c.rendering_algorithm;
+    rc.max_light_bounces = c.max_light_bounces;
+    rc.russian_roulette_threshold = c.russian_roulette_threshold;
+    rc.russian_roulette_bounce_count_threshold = c.russian_roulette_bounce_count_threshold;
+    rc.pixel_filter_type = (Raytracer_Config::Pixel_Filter_Type)c.pixel_filter_type;
+    rc.pixel_filter_radius = c.pixel_filter_radius;
+    rc.pixel_filter_alpha = c.pixel_filter_alpha;
+    rc.x_pixel_sample_count = c.x_pixel_sample_count;
+    rc.y_pixel_sample_count = c.y_pixel_sample_count;
+    if (a.spp > 0) {
+        int k = (int)std::ceil(std::sqrt(a.spp));
+        rc.x_pixel_sample_count = k;
+        rc.y_pixel_sample_count = k;
+    }
+    rc.film_radiance_scale = c.film_radiance_scale;
+    rc.max_rgb_component_value_of_film_sample = c.max_rgb_component_value_of_film_sample;
+    Args b = a;
+    b.seed_offset = c.rng_seed_offset;
+    Scene_Context ctx;
+    init_context(ctx, scene, b);
+    ctx.camera.camera_to_world = floats_to_matrix(fs_scene.camera.camera_to_world);
+    ctx.camera.image_extent = Vector2(fs_scene.camera.image_extent[0], fs_scene.camera.image_extent[1]);
+    ctx.camera.horz_half_dist = fs_scene.camera.horz_half_dist;
+    ctx.camera.vert_half_dist = fs_scene.camera.vert_half_dist;
+    ctx.camera.z_is_up = fs_scene.camera.z_is_up != 0;
+    double variance = 0.0;
+    float seconds = 0.f;
+    Image image = render_scene(ctx, &variance, &seconds);
+    FILE* f = fopen(a.pos[1].c_str(), "wb");
+    if (!f) return 1;
+    uint32_t w = (uint32_t)image.width, h = (uint32_t)image.height;
+    fwrite(&w, 4, 1, f);
+    fwrite(&h, 4, 1, f);
+    fwrite(&variance, 8, 1, f);
+    fwrite(&seconds, 4, 1, f);
+    fwrite(image.data.data(), sizeof(ColorRGB), image.data.size(), f);
+    fclose(f);
+    printf("{\"render_seconds\": %.6f, \"variance\": %.9g, \"threads\": %d, \"spp\": %d, \"width\": %u, \"height\": %u}\n",
+           seconds, variance, b.threads, ctx.pixel_sampler_config.get_samples_per_pixel(), w, h);
+    return 0;
+}
+
 int cmd_regress(const Args& a) {
     if (a.pos.size() < 3) return 2;
     yfs::Scene fs_scene;
@@ -572,6 +703,7 @@ int main(int argc, char** argv) {
     else if (cmd == "build") rc = cmd_build(a);
     else if (cmd == "cast") rc = cmd_cast(a);
     else if (cmd == "regress") rc = cmd_regress(a);
+    else if (cmd == "render-yfs") rc = cmd_render_yfs(a);
     if (rc == 2) fprintf(stderr, "bad arguments for %s\n", cmd.c_str());
     return rc;
 }

@@ -10,7 +10,7 @@
 // are written as structure of arrays at the ray's index.
 #include "context.hpp"
 
-
+#include <type_traits>
 
 namespace yar {
 
@@ -34,7 +34,7 @@ __device__ __forceinline__ void write_result(const Traversal<ANY>& tr, uint32_t 
     }
 }
 
-template <bool ANY, int MINB>
+template <bool ANY, int MINB, int MAXD, int SHORT>
 __global__ void __launch_bounds__(kCastBlock, MINB)
 cast_persistent(Device_Scene s, const float4* __restrict__ rays, uint32_t n, uint32_t* __restrict__ next_ray,
                 float* __restrict__ t_out, uint32_t* __restrict__ prim_out, uint32_t* __restrict__ obj_out,
@@ -43,7 +43,9 @@ cast_persistent(Device_Scene s, const float4* __restrict__ rays, uint32_t n, uin
     const int lane = threadIdx.x & 31;
     const unsigned lower = (1u << lane) - 1u;
     Traversal<ANY> tr;
-    Stack_Entry stack[2 * kMaxTraversalDepth];
+    __shared__ uint2 stack_smem[SHORT > 0 ? SHORT * kCastBlock : 1];
+    typename std::conditional<(SHORT > 0), Split_Stack<SHORT, kCastBlock>, Local_Stack>::type stack;
+    if constexpr (SHORT > 0) stack.smem = stack_smem + threadIdx.x;
     uint32_t ray = 0;
     bool have = false, alive = true;
     uint32_t batch_next = 0, batch_end = 0;  // warp-uniform
@@ -76,14 +78,14 @@ cast_persistent(Device_Scene s, const float4* __restrict__ rays, uint32_t n, uin
             want = __ballot_sync(full, !have && alive);
         }
         if (!__any_sync(full, have)) break;
-        if (have && !tr.step(s, stack)) {
+        if (have && !tr.template step<MAXD>(s, stack)) {
             write_result<ANY>(tr, ray, t_out, prim_out, obj_out, bary_out, occluded, err);
             have = false;
         }
     }
 }
 
-template <bool ANY, int MINB>
+template <bool ANY, int MINB, int MAXD, int SHORT>
 cudaError_t launch_persistent(const Device_Scene& s, const float4* rays, uint32_t n, uint32_t* counter, float* t,
                               uint32_t* prim, uint32_t* obj, float2* bary, uint8_t* occ, int* err,
                               cudaStream_t stream) {
@@ -92,24 +94,31 @@ cudaError_t launch_persistent(const Device_Scene& s, const float4* rays, uint32_
         int dev = 0, sms = 0, per_sm = 0;
         cudaGetDevice(&dev);
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cast_persistent<ANY, MINB>, kCastBlock, 0);
+        cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, cast_persistent<ANY, MINB, MAXD, SHORT>, kCastBlock, 0);
         grid = sms * (per_sm > 0 ? per_sm : 1);
     }
     cudaError_t e = cudaMemsetAsync(counter, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
-    cast_persistent<ANY, MINB><<<grid, kCastBlock, 0, stream>>>(s, rays, n, counter, t, prim, obj, bary, occ, err);
+    cast_persistent<ANY, MINB, MAXD, SHORT>
+        <<<grid, kCastBlock, 0, stream>>>(s, rays, n, counter, t, prim, obj, bary, occ, err);
     return cudaGetLastError();
 }
 
-// 8 resident blocks of 128 threads per SM (64 registers per thread): measured
-// on GB300 against 4 and 6 blocks per SM (102 and 80 registers), the highest
-// occupancy wins for this latency-bound traversal despite a few spills.
+// Launch shape, measured on GB300 with the 2.42M-triangle ray-cast workload
+// (16M + 16M incoherent rays): 8 resident blocks of 128 threads per SM
+// (64 registers) beat 4 and 6 blocks (102 and 80 registers); descending to a
+// leaf per step (while-while) beat one node per step and four nodes per step;
+// the local-memory stack beat an 8- or 16-entry shared-memory stack with
+// local overflow (770 vs 710 Mrays/s for the best shared variant).
 constexpr int kMinBlocksPerSm = 8;
+constexpr int kWhileWhile = 1 << 30;
+constexpr int kSharedStackEntries = 0;
 
 template <bool ANY>
 cudaError_t dispatch(const Device_Scene& s, const float4* rays, uint32_t n, uint32_t* counter, float* t,
                      uint32_t* prim, uint32_t* obj, float2* bary, uint8_t* occ, int* err, cudaStream_t stream) {
-    return launch_persistent<ANY, kMinBlocksPerSm>(s, rays, n, counter, t, prim, obj, bary, occ, err, stream);
+    return launch_persistent<ANY, kMinBlocksPerSm, kWhileWhile, kSharedStackEntries>(s, rays, n, counter, t, prim,
+                                                                                    obj, bary, occ, err, stream);
 }
 
 } // namespace

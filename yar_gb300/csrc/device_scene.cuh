@@ -234,11 +234,13 @@ struct Traversal {
         mode = kDescend;
     }
 
-    // `stack` is the caller's array of 2 * kMaxTraversalDepth entries (kept out of
-    // this struct so the scalar state can live in registers).
-    __device__ __forceinline__ bool step(const Device_Scene& s, Stack_Entry* stack) {
+    // `stack` holds up to 2 * kMaxTraversalDepth entries (Local_Stack or
+    // Split_Stack; kept out of this struct so the scalar state can live in
+    // registers).  A descent stops at a leaf or after MAXD interior nodes.
+    template <int MAXD, class STACK>
+    __device__ __forceinline__ bool step(const Device_Scene& s, STACK& stack) {
         if (mode == kDescend) {
-            for (;;) {  // while-while: descend through interior nodes of the current level
+            for (int steps = 0; steps < MAXD; steps++) {  // descend through interior nodes of the current level
                 const float limit = ANY ? ray_tmax : hit.t;
                 if (!(limit > t_min)) {  // the level's loop condition failed
                     if (in_mesh) {
@@ -282,8 +284,7 @@ struct Traversal {
                             finish(-1);
                             break;
                         }
-                        stack[sp].node = second_child;
-                        stack[sp].t_max = t_max;
+                        stack.push(sp, second_child, t_max);
                         sp++;
                         node = first_child;
                         t_max = t_split;
@@ -315,9 +316,10 @@ struct Traversal {
                 leave_mesh(s);
             } else {
                 --sp;
-                node = stack[sp].node;
+                const uint2 e = stack.pop(sp);
+                node = e.x;
                 t_min = t_max;
-                t_max = stack[sp].t_max;
+                t_max = __uint_as_float(e.y);
                 mode = kDescend;
             }
         } else if (mode == kSceneLeaf) {
@@ -356,9 +358,10 @@ struct Traversal {
                 finish(ANY ? 0 : (hit.t < ray_tmax ? 1 : 0));
             } else {
                 --sp;
-                node = stack[sp].node;
+                const uint2 e = stack.pop(sp);
+                node = e.x;
                 t_min = t_max;
-                t_max = stack[sp].t_max;
+                t_max = __uint_as_float(e.y);
                 mode = kDescend;
             }
         }
@@ -366,14 +369,38 @@ struct Traversal {
     }
 };
 
+// Traversal stack in local memory (L1-cached).
+struct Local_Stack {
+    uint2 e[2 * kMaxTraversalDepth];
+    __device__ __forceinline__ void push(int sp, uint32_t node, float t_max) {
+        e[sp] = make_uint2(node, __float_as_uint(t_max));
+    }
+    __device__ __forceinline__ uint2 pop(int sp) const { return e[sp]; }
+};
+
+// Traversal stack whose first SHORT entries live in shared memory, laid out
+// entry-major ([entry][thread], conflict-free for a warp), with the rarely
+// used deeper entries in local memory.
+template <int SHORT, int BLOCK>
+struct Split_Stack {
+    uint2* smem;  // this thread's column: base + threadIdx.x
+    uint2 deep[2 * kMaxTraversalDepth - SHORT];
+    __device__ __forceinline__ void push(int sp, uint32_t node, float t_max) {
+        const uint2 v = make_uint2(node, __float_as_uint(t_max));
+        if (sp < SHORT) smem[sp * BLOCK] = v;
+        else deep[sp - SHORT] = v;
+    }
+    __device__ __forceinline__ uint2 pop(int sp) const { return sp < SHORT ? smem[sp * BLOCK] : deep[sp - SHORT]; }
+};
+
 // One ray, start to finish (used by the render wavefront).  Returns the status.
 template <bool ANY>
 __device__ __forceinline__ int traverse(const Device_Scene& s, const float3 o, const float3 d, const float ray_tmax,
                                         Hit& hit) {
     Traversal<ANY> tr;
-    Stack_Entry stack[2 * kMaxTraversalDepth];
+    Local_Stack stack;
     tr.begin(s, o, d, ray_tmax);
-    while (tr.step(s, stack)) {
+    while (tr.step<1 << 30>(s, stack)) {
     }
     hit = tr.hit;
     return tr.status;

@@ -234,3 +234,109 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
 GGX_BOXES = ('Material "metal" "float roughness" [0.2] "rgb eta" [0.2 0.92 1.1] "rgb k" [3.9 2.45 2.14]',
              'Material "glass" "float uroughness" [0.3] "float vroughness" [0.3] "float index" [1.5] '
              '"rgb Kr" [1 1 1] "rgb Kt" [1 1 1]')
+
+
+# ---------------------------------------------------------------- large wavefront scene
+METALS = (((0.2, 0.92, 1.1), (3.9, 2.45, 2.14)),    # gold-like
+          ((0.27, 0.68, 1.32), (3.61, 2.63, 2.29)),  # copper-like
+          ((0.16, 0.14, 0.13), (4.0, 3.2, 2.5)))     # silver-like
+
+
+def _pbrt_quad_uvs():
+    # pbrt-v3 default uvs of a 4-vertex mesh (src/lib/pbrt_scene.cpp:305-315)
+    return np.array([[0, 0], [1, 0], [1, 1], [1, 0]], np.float32)
+
+
+def large_scene(seed=1, width=1920, height=1080, spp=64, maxdepth=16, meshes=200, level=5, lights=64, build=True,
+                threads=0):
+    """The plain-wavefront workload: the Cornell room and boxes plus `meshes`
+    icosphere copies (level 5: 20,480 triangles each, ~4.1M in total), half
+    Lambertian and half GGX (conductors and rough dielectrics, roughness
+    U[0.05, 0.5], IOR U[1.3, 1.7], pbrt-v3 roughness remapping), lit only by
+    `lights` 0.1 x 0.1 ceiling quads of radiance log-uniform in [1, 100].
+    Rendered at width x height, spp samples, maxdepth bounces, Russian roulette
+    from bounce 3 (the reference defaults)."""
+    from . import native as N
+    from .scene import LIGHT_DTYPE, MATERIAL_DTYPE, CAMERA_DTYPE, default_config
+    rng = np.random.default_rng(seed)
+    s = FlatScene()
+    objects, materials, rect_lights = [], [], []
+
+    def add_material(kind):
+        m = np.zeros((), MATERIAL_DTYPE)
+        if kind == "matte":
+            m["type"] = N.MATERIAL_DIFFUSE
+            m["reflectance"] = rng.uniform(0.2, 0.8, 3)
+        elif kind == "metal":
+            eta, k = METALS[int(rng.integers(0, len(METALS)))]
+            r = rng.uniform(0.05, 0.5)
+            m["type"] = N.MATERIAL_METAL
+            m["eta"], m["k"], m["eta_i"] = eta, k, 1.0
+            m["u_roughness"] = m["v_roughness"] = r
+        else:
+            r = rng.uniform(0.05, 0.5)
+            m["type"] = N.MATERIAL_GLASS
+            m["reflectance"] = m["transmittance"] = (1.0, 1.0, 1.0)
+            m["index_of_refraction"] = rng.uniform(1.3, 1.7)
+            m["u_roughness"] = m["v_roughness"] = r
+        materials.append(m)
+        return int(m["type"]), len(materials) - 1
+
+    walls = [
+        _quad((-1, 0, -1), (1, 0, -1), (1, 0, 1), (-1, 0, 1)),
+        _quad((-1, 2, -1), (-1, 2, 1), (1, 2, 1), (1, 2, -1)),
+        _quad((-1, 0, -1), (-1, 2, -1), (1, 2, -1), (1, 0, -1)),
+        _quad((-1, 0, -1), (-1, 0, 1), (-1, 2, 1), (-1, 2, -1)),
+        _quad((1, 0, -1), (1, 2, -1), (1, 2, 1), (1, 0, 1)),
+    ]
+    for v, i in walls:
+        s.meshes.append(Mesh(v, i, uvs=_pbrt_quad_uvs()))
+        t, k = add_material("matte")
+        objects.append(make_object(len(s.meshes) - 1, material_type=t, material_index=k))
+    for center, size in (((0.35, 0, 0.3), (0.6, 0.6, 0.6)), ((-0.35, 0, -0.35), (0.6, 1.2, 0.6))):
+        v, i = _box(center, size, rng.uniform(0.0, 30.0))
+        s.meshes.append(Mesh(v, i))
+        t, k = add_material("matte")
+        objects.append(make_object(len(s.meshes) - 1, material_type=t, material_index=k))
+    sv, si = icosphere(1.0, level)
+    for _ in range(meshes):
+        r = np.float32(rng.uniform(0.03, 0.12))
+        c = rng.uniform((-0.85, 0.1, -0.85), (0.85, 1.8, 0.85)).astype(np.float32)
+        s.meshes.append(Mesh(sv * r, si))
+        kind = "matte" if rng.random() < 0.5 else ("metal" if rng.random() < 0.5 else "glass")
+        t, k = add_material(kind)
+        m = np.array([1, 0, 0, c[0], 0, 1, 0, c[1], 0, 0, 1, c[2]], np.float32)
+        w = np.array([1, 0, 0, -c[0], 0, 1, 0, -c[1], 0, 0, 1, -c[2]], np.float32)
+        objects.append(make_object(len(s.meshes) - 1, m, w, material_type=t, material_index=k))
+    side = int(math.ceil(math.sqrt(lights)))
+    h = 0.05
+    for j in range(lights):
+        cx = -0.8 + 1.6 * ((j % side) + 0.5) / side
+        cz = -0.8 + 1.6 * ((j // side) + 0.5) / side
+        v, i = _quad((cx - h, 1.98, cz - h), (cx + h, 1.98, cz - h), (cx + h, 1.98, cz + h), (cx - h, 1.98, cz + h))
+        s.meshes.append(Mesh(v, i, uvs=_pbrt_quad_uvs()))
+        L = np.zeros((), LIGHT_DTYPE)
+        # rectangle frame: x along +x, y along +z, normal (x cross y) = -y (facing down)
+        L["light_to_world"] = (1, 0, 0, cx, 0, 0, -1, 1.98, 0, 1, 0, cz)
+        L["emitted_radiance"] = [float(np.exp(rng.uniform(np.log(1.0), np.log(100.0))))] * 3
+        L["size"] = (2 * h, 2 * h)
+        L["sample_count"] = 1
+        rect_lights.append(L)
+        objects.append(make_object(len(s.meshes) - 1, material_type=N.MATERIAL_NULL, material_index=-1,
+                                   light_type=N.LIGHT_RECT, light_index=len(rect_lights) - 1))
+    s.objects = np.array(objects)
+    s.materials = np.array(materials, MATERIAL_DTYPE)
+    s.rect_lights = np.array(rect_lights, LIGHT_DTYPE)
+    cam = np.zeros((), CAMERA_DTYPE)
+    cam["camera_to_world"] = (1, 0, 0, 0, 0, 1, 0, 1, 0, 0, 1, 3.5)
+    cam["image_extent"] = (width, height)
+    vert = np.float32(math.tan(math.radians(20.0)))
+    cam["vert_half_dist"] = vert
+    cam["horz_half_dist"] = np.float32(np.float32(width) / np.float32(height)) * vert
+    cam["z_is_up"] = 0
+    s.camera = cam
+    k = int(math.ceil(math.sqrt(spp)))
+    s.config = default_config(width, height, k, k, maxdepth)
+    if build:
+        s.build_kdtrees(threads)
+    return s
