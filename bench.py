@@ -47,6 +47,9 @@ def parse():
     p.add_argument("--rays", type=int, default=N_RAYS)
     p.add_argument("--grid", type=int, default=GRID)
     p.add_argument("--no-cpu-baseline", action="store_true")
+    p.add_argument("--no-render", action="store_true", help="skip the C1 render figures")
+    p.add_argument("--workload", default="raycast", choices=["raycast", "render-c1", "render-c3"],
+                   help="render-c1 / render-c3 print a separate line for the C1 or the large (C3) render")
     return p.parse_args()
 
 
@@ -370,15 +373,75 @@ def run_gb300(args, rank, world, local, pg):
     }
     if not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(s, rays, shadow)
-    print(json.dumps(line), flush=True)
     ctx.close()
+    if not args.no_render:
+        line["render_c1"] = render_bench("c1", with_cpu=not args.no_cpu_baseline)
+    print(json.dumps(line), flush=True)
+
+
+# ------------------------------------------------------------------ render path
+def c1_scene(width=256, height=256):
+    """The Cornell box (5 walls, 2 rotated boxes, a 0.25 x 0.25 light of
+    radiance 17) as the reference's loader and builder flattened it, at
+    width x height, 16 spp, maxdepth 8, pcg seed offset 1."""
+    from yar_gb300.scene import FlatScene
+    s = FlatScene.read(os.path.join(ROOT, "tests", "golden", "cornell_c1_64.yfs"))
+    s.config["render_region"] = (0, 0, width, height)
+    s.camera["image_extent"] = (width, height)
+    return s
+
+
+def render_bench(kind, with_cpu=True, reps=3):
+    """GPU render time (yar_gpu_render, best of `reps`) and, when the reference
+    is built here, the reference renderer's render_scene time on all host
+    threads (C3: at 1 spp, reported as paths/s)."""
+    import oracle
+    from yar_gb300 import native, scenes
+    if kind == "c1":
+        s = c1_scene()
+        desc = "C1 Cornell box 256x256, 16 spp, maxdepth 8 (diffuse, 1 quad light)"
+    else:
+        s = scenes.large_scene(seed=1)
+        desc = ("C3 %d triangles, 1920x1080, 64 spp, maxdepth 16, RR from bounce 3, 50%% Lambertian / 50%% GGX, "
+                "64 quad lights" % s.triangle_count)
+    w = int(s.config["render_region"][2])
+    h = int(s.config["render_region"][3])
+    ctx = native.Context(0)
+    ctx.upload_scene(s)
+    best = None
+    for _ in range(reps):
+        img, st = ctx.render(w, h)
+        if best is None or st.seconds < best.seconds:
+            best = st
+    ctx.close()
+    out = {"workload": desc, "gpu_seconds": round(best.seconds, 4), "paths": int(best.paths),
+           "gpu_paths_per_s": round(best.paths / best.seconds, 1),
+           "gpu_mrays_per_s": round((best.rays_closest + best.rays_any) / best.seconds / 1e6, 2),
+           "rays_closest": int(best.rays_closest), "rays_any": int(best.rays_any),
+           "kernel_launches": int(best.kernel_launches), "image_mean": float(img.mean())}
+    if with_cpu and oracle.have_reference():
+        spp = 1 if kind == "c3" else 0
+        _, info = oracle.ref_render_flat(s, spp=spp)
+        paths = w * h * (1 if spp else int(s.config["x_pixel_sample_count"] * s.config["y_pixel_sample_count"]))
+        out["cpu_reference"] = {"seconds": info["render_seconds"], "threads": info["threads"], "paths": paths,
+                                "paths_per_s": round(paths / info["render_seconds"], 1),
+                                "sample": "full image" if not spp else "full image at 1 spp"}
+        out["speedup_paths_per_s"] = round(out["gpu_paths_per_s"] / out["cpu_reference"]["paths_per_s"], 1)
+    return out
 
 
 def main():
     args = parse()
     rank, world, local, pg = dist_setup(args)
     try:
-        if args.impl == "reference":
+        if args.workload in ("render-c1", "render-c3"):
+            if rank == 0:
+                kind = args.workload[-2:]
+                r = render_bench(kind, with_cpu=not args.no_cpu_baseline, reps=1 if kind == "c3" else 3)
+                print(json.dumps({"metric": "paths/s (%s wavefront render)" % kind.upper(), "value": r["gpu_paths_per_s"],
+                                  "unit": "paths/s", "higher_is_better": True, "impl": args.impl, "render": r}),
+                      flush=True)
+        elif args.impl == "reference":
             run_reference(args, rank, world, pg)
         else:
             run_gb300(args, rank, world, local, pg)

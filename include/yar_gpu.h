@@ -213,7 +213,17 @@ typedef struct yar_hit_soa {
 typedef struct yar_gpu_options {
     int32_t device;                 /* CUDA device ordinal */
     uint32_t max_batch_rays;        /* capacity of the host-buffer staging area (0 = 16M) */
+    int32_t traversal_kernel;       /* YAR_TRAVERSAL_*: 0 = chosen per scene by timing */
 } yar_gpu_options;
+
+/* Traversal kernels (identical results, different speed): persistent warps
+ * with a 64- or 128-register cap, or one ray per thread.  With AUTO the first
+ * large enough batch of each ray kind (and the first render bounce) after a
+ * scene upload times all three and keeps the fastest. */
+#define YAR_TRAVERSAL_AUTO 0
+#define YAR_TRAVERSAL_PERSISTENT_64 1
+#define YAR_TRAVERSAL_PERSISTENT_128 2
+#define YAR_TRAVERSAL_PER_RAY 3
 
 typedef struct yar_render_stats {
     double variance;            /* render_scene's variance_estimate */

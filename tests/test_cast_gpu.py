@@ -195,3 +195,48 @@ def test_batch_capacity_error():
         ctx.cast_closest(np.zeros((1000, 8), np.float32))
     finally:
         ctx.close()
+
+
+@pytest.mark.parametrize("kernel", [native.TRAVERSAL_PERSISTENT_64, native.TRAVERSAL_PERSISTENT_128,
+                                    native.TRAVERSAL_PER_RAY])
+def test_every_traversal_kernel_matches_oracle(medium_scene, kernel):
+    if not pytest.importorskip("torch").cuda.is_available():
+        pytest.skip("no CUDA device")
+    s = medium_scene
+    ctx = native.Context(0, traversal_kernel=kernel)
+    try:
+        ctx.upload_scene(s)
+        lo, hi = scenes.scene_box(s)
+        rays = scenes.random_rays(lo, hi, 200_000, 31)
+        assert_same_hits(ctx.cast_closest(rays), oracle.cast_closest(s, rays))
+        shadow = scenes.random_shadow_rays(lo, hi, 200_000, 32)
+        assert np.array_equal(ctx.cast_any(shadow), oracle.cast_any(s, shadow))
+    finally:
+        ctx.close()
+
+
+def test_tuned_batch_matches_fixed_kernel(gpu_ctx, medium_scene):
+    """A batch large enough to trigger the per-scene kernel timing returns the
+    same results as a fixed kernel, on the timing call and after it."""
+    s = medium_scene
+    lo, hi = scenes.scene_box(s)
+    rays = scenes.random_rays(lo, hi, (1 << 20) + 3, 33)
+    shadow = scenes.random_shadow_rays(lo, hi, (1 << 20) + 3, 34)
+    fixed = native.Context(0, traversal_kernel=native.TRAVERSAL_PER_RAY)
+    try:
+        fixed.upload_scene(s)
+        want, want_occ = fixed.cast_closest(rays), fixed.cast_any(shadow)
+    finally:
+        fixed.close()
+    gpu_ctx.upload_scene(s)
+    for _ in range(2):
+        assert_same_hits(gpu_ctx.cast_closest(rays), want)
+        assert np.array_equal(gpu_ctx.cast_any(shadow), want_occ)
+
+
+def test_invalid_traversal_kernel_option():
+    if not pytest.importorskip("torch").cuda.is_available():
+        pytest.skip("no CUDA device")
+    with pytest.raises(native.YarError) as e:
+        native.Context(0, traversal_kernel=7)
+    assert e.value.code == native.YAR_ERR_INVALID

@@ -83,3 +83,29 @@ def test_render_unsupported_features_fail_cleanly(gpu_ctx):
     gpu_ctx.upload_scene(s)
     img, _ = gpu_ctx.render(64, 64)
     assert img.mean() > 0
+
+
+def test_render_identical_for_every_traversal_kernel():
+    """The traversal kernel choice (fixed, or timed per scene on the first
+    secondary bounce) changes no bit of the image or the variance."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    from yar_gb300 import native
+    s = FlatScene.read(golden("cornell_ggx_64.yfs"))
+    s.config["x_pixel_sample_count"], s.config["y_pixel_sample_count"] = 8, 8  # 262144 paths: tuning runs
+    results = []
+    for kernel in (native.TRAVERSAL_AUTO, native.TRAVERSAL_PERSISTENT_64, native.TRAVERSAL_PERSISTENT_128,
+                   native.TRAVERSAL_PER_RAY):
+        ctx = native.Context(0, traversal_kernel=kernel)
+        try:
+            ctx.upload_scene(s)
+            for _ in range(2 if kernel == native.TRAVERSAL_AUTO else 1):
+                img, stats = ctx.render(64, 64)
+                results.append((img, stats.variance))
+        finally:
+            ctx.close()
+    img0, var0 = results[0]
+    for img, var in results[1:]:
+        assert np.array_equal(img.view(np.uint32), img0.view(np.uint32))
+        assert var == var0

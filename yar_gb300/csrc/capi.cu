@@ -13,6 +13,12 @@
 
 namespace yar {
 
+namespace {
+// Casts of at least this many rays choose the traversal kernel by timing
+// (smaller batches use the persistent 64-register kernel until then).
+constexpr uint32_t kTuneMinRays = 1u << 20;
+}  // namespace
+
 int fail(yar_gpu_ctx* ctx, int code, const std::string& message) {
     if (ctx) ctx->last_error = message;
     return code;
@@ -102,6 +108,13 @@ extern "C" int yar_gpu_create(yar_gpu_ctx** out, const yar_gpu_options* options)
     if (!ctx) return YAR_ERR_NOMEM;
     ctx->device = options ? options->device : 0;
     ctx->staging_capacity = (options && options->max_batch_rays) ? options->max_batch_rays : (16u << 20);
+    if (options && options->traversal_kernel != YAR_TRAVERSAL_AUTO) {
+        if (options->traversal_kernel < YAR_TRAVERSAL_PERSISTENT_64 || options->traversal_kernel > YAR_TRAVERSAL_PER_RAY) {
+            delete ctx;
+            return YAR_ERR_INVALID;
+        }
+        ctx->forced_kernel = options->traversal_kernel - YAR_TRAVERSAL_PERSISTENT_64;
+    }
     int count = 0;
     cudaError_t e = cudaGetDeviceCount(&count);
     if (e != cudaSuccess || count == 0) {
@@ -256,6 +269,7 @@ extern "C" int yar_gpu_upload_scene(yar_gpu_ctx* ctx, const yar_flat_scene* scen
 
     rc = render_upload(ctx, scene);
     if (rc != YAR_OK) return rc;
+    for (int k = 0; k < 2; k++) ctx->cast_kernel[k] = ctx->render_kernel[k] = ctx->forced_kernel;
     ctx->has_scene = true;
     return YAR_OK;
 }
@@ -333,9 +347,24 @@ int cast(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t n, const yar_hit_soa* h
             d_occ = occluded;
         }
     }
+    Cast_Args a;
+    a.rays = d_rays;
+    a.n = n;
+    a.next_ray = ctx->d_counter;
+    a.err = ctx->d_error;
+    a.t = d_t;
+    a.prim = d_prim;
+    a.object = d_obj;
+    a.bary = d_bary;
+    a.occluded = d_occ;
+    int& kernel = ctx->cast_kernel[closest ? 0 : 1];
+    if (kernel < 0 && n >= kTuneMinRays) {
+        e = tune_cast(ctx->ds, a, !closest, ctx->stream, ctx->ev_start, ctx->ev_stop, &kernel);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "traversal kernel timing");
+    }
     if (kernel_ms) cudaEventRecord(ctx->ev_start, ctx->stream);
-    e = closest ? launch_extend(ctx->ds, d_rays, n, d_t, d_prim, d_obj, d_bary, ctx->d_error, ctx->d_counter, ctx->stream)
-                : launch_shadow(ctx->ds, d_rays, n, d_occ, ctx->d_error, ctx->d_counter, ctx->stream);
+    const int k = kernel < 0 ? kCastPersistent64 : kernel;
+    e = closest ? launch_extend(ctx->ds, a, k, ctx->stream) : launch_shadow(ctx->ds, a, k, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, closest ? "extend launch" : "shadow launch");
     if (kernel_ms) cudaEventRecord(ctx->ev_stop, ctx->stream);
     if (buffers == YAR_BUFFERS_HOST) {

@@ -56,6 +56,11 @@ struct yar_gpu_ctx {
     yar::Device_Buffer d_rays, d_t, d_prim, d_obj, d_bary, d_occ;
     int* d_error = nullptr;  // device error word (stack overflow, bounded-wait expiry)
     uint32_t* d_counter = nullptr;  // ray hand-out counter of the persistent cast kernels
+    // traversal kernel per ray kind (0 closest, 1 any) for C-ABI casts and for
+    // renders; -1 until tuned on the current scene (or fixed by the options)
+    int forced_kernel = -1;
+    int cast_kernel[2] = {-1, -1};
+    int render_kernel[2] = {-1, -1};
 
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
 
@@ -70,12 +75,37 @@ int cuda_fail(yar_gpu_ctx* ctx, cudaError_t e, const char* what);
 int device_alloc(yar_gpu_ctx* ctx, Device_Buffer& b, size_t bytes);
 void device_free(Device_Buffer& b);
 
-// kernels (cast.cu)
-// `counter` is one device word the persistent kernels use to hand out rays.
-cudaError_t launch_extend(const Device_Scene& s, const float4* rays, uint32_t n, float* t, uint32_t* prim,
-                          uint32_t* obj, float2* bary, int* err, uint32_t* counter, cudaStream_t stream);
-cudaError_t launch_shadow(const Device_Scene& s, const float4* rays, uint32_t n, uint8_t* occluded, int* err,
-                          uint32_t* counter, cudaStream_t stream);
+// Arguments of the persistent extend/shadow kernels (cast.cu).
+struct Cast_Args {
+    const float4* rays = nullptr;     // two float4 per ray
+    uint32_t n = 0;                   // ray count, unless `count` is set
+    const uint32_t* count = nullptr;  // device ray count (queues sized on the device)
+    uint32_t n_max = 0;               // upper bound of *count (grid of the one-ray-per-thread kernel)
+    const uint32_t* perm = nullptr;   // output index of each ray position (null: the position)
+    uint32_t* next_ray = nullptr;     // one device word used to hand out rays (zeroed per launch)
+    int* err = nullptr;               // error word (traversal-stack overflow)
+    // closest hit, C-ABI layout (any pointer may be null)
+    float* t = nullptr;
+    uint32_t* prim = nullptr;
+    uint32_t* object = nullptr;
+    float2* bary = nullptr;
+    // closest hit, render layout: {t, b0, b1, b2} and {prim, object}
+    float4* hit4 = nullptr;
+    uint2* hit2 = nullptr;
+    // any hit
+    uint8_t* occluded = nullptr;
+};
+// Traversal kernels: persistent warps capped at 64 registers (8 blocks per
+// SM), persistent warps capped at 128 registers (4 blocks per SM), one ray per
+// thread.  All give identical results; which is fastest depends on the scene
+// and the rays, so it is chosen per scene by timing (tune_cast).
+enum Cast_Kernel { kCastPersistent64 = 0, kCastPersistent128 = 1, kCastPerRay = 2, kCastKernelCount = 3 };
+cudaError_t launch_extend(const Device_Scene& s, const Cast_Args& a, int kernel, cudaStream_t stream);
+cudaError_t launch_shadow(const Device_Scene& s, const Cast_Args& a, int kernel, cudaStream_t stream);
+// Runs the batch once untimed and once with each kernel (event-timed on
+// `stream`), leaving the results of the last run in place; *best = fastest.
+cudaError_t tune_cast(const Device_Scene& s, const Cast_Args& a, bool any, cudaStream_t stream, cudaEvent_t ev0,
+                      cudaEvent_t ev1, int* best);
 
 // render (render.cu)
 int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene);

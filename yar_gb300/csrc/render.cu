@@ -116,123 +116,211 @@ __device__ __forceinline__ float one_minus_eps_min(float v) {
 }
 
 // ---------------------------------------------------------------- generate
-__global__ void __launch_bounds__(kBlock)
-generate_kernel(Render_Params p, uint32_t chunk_first, uint32_t chunk_pixels, float* __restrict__ s1d,
-                float* __restrict__ s2d, float2* __restrict__ image_samples, Path_State ps, Queues q) {
-    const uint32_t lp = blockIdx.x * blockDim.x + threadIdx.x;
-    if (lp >= chunk_pixels) return;
-    const uint32_t pix = chunk_first + lp;
-    const int x = p.sx0 + (int)(pix % (uint32_t)p.sw);
-    const int y = p.sy0 + (int)(pix / (uint32_t)p.sw);
+// Stratified_Pixel_Sampler::next_pixel (src/ref/sampling.cpp:98-133) draws,
+// from the pixel's pcg stream and in this order: the image samples (2 draws
+// per sample), then per 1D dimension spp stratified values and spp - 1
+// shuffle draws, then per 2D dimension 2 spp values and spp - 1 shuffle draws.
+// The bounded draw of the shuffle takes exactly one number
+// (RNG::get_bounded_uint_fast_and_biased, src/lib/random.h:58-62), so every
+// dimension starts at a fixed offset of the stream.  Each (pixel, dimension)
+// is built by its own thread from a jump-ahead of the stream to that offset
+// (Brown, "Random number generation with arbitrary strides", 1994: the LCG
+// s' = a s + c advanced n steps is A_n s + C_n c, both computable in
+// O(log n)), instead of one thread walking the pixel's stream sequentially.
+//
+// Sample tables, per pixel of the chunk, dimension-major:
+//   s1d[(lp * n1d + dim) * spp + sample],  s2d[(lp * n2d + dim) * spp + sample]
+// A thread's column is shuffled in shared memory ([sample][thread], so the
+// random indices of a warp's lanes never share a bank) and stored as a
+// contiguous row; the lanes of a warp own adjacent rows.
+
+// Advance the pcg stream by n draws.
+__device__ __forceinline__ void pcg_advance(Pcg& r, uint32_t n) {
+    uint64_t cur_mult = 6364136223846793005ULL, cur_plus = 1u;  // increment factored out
+    uint64_t acc_mult = 1u, acc_plus = 0u;
+    while (n) {
+        if (n & 1u) {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1u) * cur_plus;
+        cur_mult *= cur_mult;
+        n >>= 1;
+    }
+    r.state = acc_mult * r.state + acc_plus * r.inc;
+}
+
+__device__ __forceinline__ uint32_t pixel_stream(const Render_Params& p, uint32_t pix, int& x, int& y) {
+    x = p.sx0 + (int)(pix % (uint32_t)p.sw);
+    y = p.sy0 + (int)(pix / (uint32_t)p.sw);
     uint32_t stream = ((uint32_t)x & 0xffffu) | ((uint32_t)y << 16);
-    stream += p.seed_offset;
-    Pcg rng = pcg_seed(0, stream);
+    return stream + p.seed_offset;
+}
+
+// One thread per (pixel, table row): row 0 the image samples, rows
+// 1..n1d the 1D dimensions, then the 2D dimensions.  Shared memory: spp float2
+// per thread.  Stores are float4 when the row length allows.
+__global__ void sample_tables_kernel(Render_Params p, uint32_t chunk_first, uint32_t chunk_pixels,
+                                     float* __restrict__ s1d, float* __restrict__ s2d,
+                                     float2* __restrict__ image_samples) {
+    extern __shared__ float2 gen_smem[];
+    const uint32_t rows = 1u + (uint32_t)p.n1d + (uint32_t)p.n2d;
+    const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (uint64_t)chunk_pixels * rows) return;
+    const uint32_t lp = (uint32_t)(g / rows);
+    const uint32_t row = (uint32_t)(g % rows);
+    int x, y;
+    Pcg rng = pcg_seed(0, pixel_stream(p, chunk_first + lp, x, y));
     const int spp = p.spp;
-    float2* img = image_samples + (size_t)pix * spp;
-    {
-        const float dx = 1.f / (float)p.nx, dy = 1.f / (float)p.ny;
+    const uint32_t n1d = (uint32_t)p.n1d;
+    float2* sm = gen_smem + threadIdx.x;
+    const int stride = (int)blockDim.x;
+    const float dx = 1.f / (float)p.nx, dy = 1.f / (float)p.ny;
+    if (row == 0) {  // image samples: stratified, not shuffled
+        float2* img = image_samples + ((size_t)chunk_first + lp) * spp;
         for (int j = 0; j < p.ny; j++)
             for (int i = 0; i < p.nx; i++) {
-                float a = one_minus_eps_min(((float)i + pcg_float(rng)) * dx);
-                float b = one_minus_eps_min(((float)j + pcg_float(rng)) * dy);
+                const float a = one_minus_eps_min(((float)i + pcg_float(rng)) * dx);
+                const float b = one_minus_eps_min(((float)j + pcg_float(rng)) * dy);
                 img[j * p.nx + i] = make_float2(a, b);
             }
+        return;
     }
-    const size_t slot0 = (size_t)lp * spp;
-    {
+    if (row <= n1d) {
+        const uint32_t dim = row - 1u;
+        pcg_advance(rng, (uint32_t)(2 * spp) + dim * (uint32_t)(2 * spp - 1));
         const float d = 1.f / (float)spp;
-        for (int i = 0; i < p.n1d; i++) {
-            float* col0 = s1d + slot0 * p.n1d + i;
-            for (int k = 0; k < spp; k++) col0[(size_t)k * p.n1d] = one_minus_eps_min(((float)k + pcg_float(rng)) * d);
-            for (int m = spp; m > 1; m--) {  // shuffle, src/lib/math.h:138-145
-                const uint32_t r = pcg_bounded_fast(rng, (uint32_t)m);
-                const float t = col0[(size_t)(m - 1) * p.n1d];
-                col0[(size_t)(m - 1) * p.n1d] = col0[(size_t)r * p.n1d];
-                col0[(size_t)r * p.n1d] = t;
-            }
+        for (int k = 0; k < spp; k++) sm[k * stride].x = one_minus_eps_min(((float)k + pcg_float(rng)) * d);
+        for (int m = spp; m > 1; m--) {  // shuffle, src/lib/math.h:138-145
+            const uint32_t r = pcg_bounded_fast(rng, (uint32_t)m);
+            const float t = sm[(m - 1) * stride].x;
+            sm[(m - 1) * stride].x = sm[r * stride].x;
+            sm[r * stride].x = t;
         }
-    }
-    {
-        const float dx = 1.f / (float)p.nx, dy = 1.f / (float)p.ny;
-        for (int i = 0; i < p.n2d; i++) {
-            float2* col0 = reinterpret_cast<float2*>(s2d) + slot0 * p.n2d + i;
-            for (int j = 0; j < p.ny; j++)
-                for (int ii = 0; ii < p.nx; ii++) {
-                    float a = one_minus_eps_min(((float)ii + pcg_float(rng)) * dx);
-                    float b = one_minus_eps_min(((float)j + pcg_float(rng)) * dy);
-                    col0[(size_t)(j * p.nx + ii) * p.n2d] = make_float2(a, b);
-                }
-            for (int m = spp; m > 1; m--) {
-                const uint32_t r = pcg_bounded_fast(rng, (uint32_t)m);
-                const float2 t = col0[(size_t)(m - 1) * p.n2d];
-                col0[(size_t)(m - 1) * p.n2d] = col0[(size_t)r * p.n2d];
-                col0[(size_t)r * p.n2d] = t;
-            }
+        float* out = s1d + ((size_t)lp * n1d + dim) * spp;
+        if ((spp & 3) == 0) {
+            float4* o4 = reinterpret_cast<float4*>(out);
+            for (int k = 0; k < spp; k += 4)
+                o4[k >> 2] = make_float4(sm[k * stride].x, sm[(k + 1) * stride].x, sm[(k + 2) * stride].x,
+                                         sm[(k + 3) * stride].x);
+        } else {
+            for (int k = 0; k < spp; k++) out[k] = sm[k * stride].x;
         }
+        return;
     }
-    // camera rays (Camera::generate_ray) and path initialisation
+    const uint32_t dim = row - 1u - n1d;
+    pcg_advance(rng, (uint32_t)(2 * spp) + n1d * (uint32_t)(2 * spp - 1) + dim * (uint32_t)(3 * spp - 1));
+    for (int j = 0; j < p.ny; j++)
+        for (int i = 0; i < p.nx; i++) {
+            const float a = one_minus_eps_min(((float)i + pcg_float(rng)) * dx);
+            const float b = one_minus_eps_min(((float)j + pcg_float(rng)) * dy);
+            sm[(j * p.nx + i) * stride] = make_float2(a, b);
+        }
+    for (int m = spp; m > 1; m--) {
+        const uint32_t r = pcg_bounded_fast(rng, (uint32_t)m);
+        const float2 t = sm[(m - 1) * stride];
+        sm[(m - 1) * stride] = sm[r * stride];
+        sm[r * stride] = t;
+    }
+    float2* out = reinterpret_cast<float2*>(s2d) + ((size_t)lp * (uint32_t)p.n2d + dim) * spp;
+    if ((spp & 1) == 0) {
+        float4* o4 = reinterpret_cast<float4*>(out);
+        for (int k = 0; k < spp; k += 2) {
+            const float2 a = sm[k * stride], b = sm[(k + 1) * stride];
+            o4[k >> 1] = make_float4(a.x, a.y, b.x, b.y);
+        }
+    } else {
+        for (int k = 0; k < spp; k++) out[k] = sm[k * stride];
+    }
+}
+
+// One thread per path of the chunk: camera ray (Camera::generate_ray,
+// src/ref/camera.cpp) through the path's image sample, path initialisation.
+__global__ void __launch_bounds__(kBlock)
+camera_kernel(Render_Params p, uint32_t chunk_first, uint32_t chunk_paths, const float2* __restrict__ image_samples,
+              Path_State ps, Queues q) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= chunk_paths) return;
+    const int spp = p.spp;
+    const uint32_t lp = slot / (uint32_t)spp;
+    const uint32_t k = slot - lp * (uint32_t)spp;
+    int x, y;
+    const uint32_t stream = pixel_stream(p, chunk_first + lp, x, y);
+    const float2 s = image_samples[((size_t)chunk_first + lp) * spp + k];
     const yar_camera_desc& c = p.camera;
     const float4 m0 = make_float4(c.camera_to_world[0], c.camera_to_world[1], c.camera_to_world[2], c.camera_to_world[3]);
     const float4 m1 = make_float4(c.camera_to_world[4], c.camera_to_world[5], c.camera_to_world[6], c.camera_to_world[7]);
     const float4 m2 = make_float4(c.camera_to_world[8], c.camera_to_world[9], c.camera_to_world[10], c.camera_to_world[11]);
-    for (int k = 0; k < spp; k++) {
-        const float fx = (float)x + img[k].x;
-        const float fy = (float)y + img[k].y;
-        const float u = 2.f * (fx / c.image_extent[0]) - 1.f;
-        const float v = 2.f * (fy / c.image_extent[1]) - 1.f;
-        const float right = u * c.horz_half_dist;
-        const float up = -v * c.vert_half_dist;
-        V3 dir = v3(right, c.z_is_up ? 1.f : up, c.z_is_up ? up : -1.f);
-        dir = divs(dir, len(dir));
-        const V3 o = xform_point(m0, m1, m2, v3(0.f, 0.f, 0.f));
-        const V3 d = xform_vector(m0, m1, m2, dir);
-        const uint32_t slot = (uint32_t)(slot0 + k);
-        q.ext_rays[0][2 * (size_t)slot] = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
-        q.ext_rays[0][2 * (size_t)slot + 1] = make_float4(d.x, d.y, d.z, 0.f);
-        q.ext_slot[0][slot] = slot;
-        ps.coeff[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
-        ps.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
-        ps.info[slot] = 0u;
-        // dimensions beyond the sampler budget: an independent pcg stream per sample
-        const Pcg r2 = pcg_seed((uint64_t)k + 1u, ((uint64_t)stream << 20) ^ 0x2545F4914F6CDD1Dull);
-        ps.rng[slot] = make_uint4((uint32_t)r2.state, (uint32_t)(r2.state >> 32), (uint32_t)r2.inc,
-                                  (uint32_t)(r2.inc >> 32));
-    }
+    const float fx = (float)x + s.x;
+    const float fy = (float)y + s.y;
+    const float u = 2.f * (fx / c.image_extent[0]) - 1.f;
+    const float v = 2.f * (fy / c.image_extent[1]) - 1.f;
+    const float right = u * c.horz_half_dist;
+    const float up = -v * c.vert_half_dist;
+    V3 dir = v3(right, c.z_is_up ? 1.f : up, c.z_is_up ? up : -1.f);
+    dir = divs(dir, len(dir));
+    const V3 o = xform_point(m0, m1, m2, v3(0.f, 0.f, 0.f));
+    const V3 d = xform_vector(m0, m1, m2, dir);
+    q.ext_rays[0][2 * (size_t)slot] = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
+    q.ext_rays[0][2 * (size_t)slot + 1] = make_float4(d.x, d.y, d.z, 0.f);
+    q.ext_slot[0][slot] = slot;
+    ps.coeff[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
+    ps.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    ps.info[slot] = 0u;
+    // dimensions beyond the sampler budget: an independent pcg stream per sample
+    const Pcg r2 = pcg_seed((uint64_t)k + 1u, ((uint64_t)stream << 20) ^ 0x2545F4914F6CDD1Dull);
+    ps.rng[slot] = make_uint4((uint32_t)r2.state, (uint32_t)(r2.state >> 32), (uint32_t)r2.inc,
+                              (uint32_t)(r2.inc >> 32));
 }
 
 // ---------------------------------------------------------------- extend / probe / shadow
-template <bool BY_SLOT>
-__global__ void __launch_bounds__(kBlock)
-closest_queue_kernel(Device_Scene s, const float4* __restrict__ rays, const uint32_t* __restrict__ slots,
-                     const uint32_t* __restrict__ count_ptr, uint32_t count_host, float4* __restrict__ hit4,
-                     uint2* __restrict__ hit2, uint32_t* __restrict__ err) {
-    const uint32_t n = count_ptr ? *count_ptr : count_host;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 a = __ldg(rays + 2 * (size_t)i);
-        const float4 b = __ldg(rays + 2 * (size_t)i + 1);
-        Hit h;
-        const int r = traverse<false>(s, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), a.w, h);
-        if (r < 0) atomicOr(err, 1u);
-        if (r <= 0) { h.prim = h.object = 0xffffffffu; }
-        const uint32_t dst = BY_SLOT ? slots[i] : i;
-        hit4[dst] = make_float4(h.t, h.b0, h.b1, h.b2);
-        hit2[dst] = make_uint2(h.prim, h.object);
-    }
+// The three ray queues of a bounce are traced by the cast kernels (cast.cu).
+// Extend hits are written at the queue position (shade reads the queue in
+// order); shadow and probe results at the path slot.  Hand-out counters are
+// counters[4..6], the error word counters[3].  The traversal kernel of each
+// ray kind is chosen by timing on the first bounce after the camera bounce
+// with at least kRenderTuneMinRays paths (secondary rays are the incoherent
+// majority), unless the context fixes it.
+constexpr uint32_t kRenderTuneMinRays = 1u << 16;
+
+cudaError_t trace_extend(yar_gpu_ctx* ctx, const Queues& q, int cur, uint32_t count, bool tune, cudaStream_t st) {
+    Cast_Args a;
+    a.rays = q.ext_rays[cur];
+    a.n = count;
+    a.next_ray = q.counters + 4;
+    a.err = reinterpret_cast<int*>(q.counters + 3);
+    a.hit4 = q.ext_hit4;
+    a.hit2 = q.ext_hit2;
+    int& k = ctx->render_kernel[0];
+    if (tune && k < 0) return tune_cast(ctx->ds, a, false, st, ctx->ev_start, ctx->ev_stop, &k);
+    return launch_extend(ctx->ds, a, k < 0 ? kCastPersistent64 : k, st);
 }
 
-__global__ void __launch_bounds__(kBlock)
-shadow_queue_kernel(Device_Scene s, const float4* __restrict__ rays, const uint32_t* __restrict__ slots,
-                    const uint32_t* __restrict__ count_ptr, uint8_t* __restrict__ occluded,
-                    uint32_t* __restrict__ err) {
-    const uint32_t n = *count_ptr;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        const float4 a = __ldg(rays + 2 * (size_t)i);
-        const float4 b = __ldg(rays + 2 * (size_t)i + 1);
-        Hit h;
-        const int r = traverse<true>(s, make_float3(a.x, a.y, a.z), make_float3(b.x, b.y, b.z), a.w, h);
-        if (r < 0) atomicOr(err, 1u);
-        occluded[slots[i]] = (uint8_t)(r > 0 ? 1 : 0);
-    }
+cudaError_t trace_light_queues(yar_gpu_ctx* ctx, const Queues& q, const Path_State& ps, uint32_t count, bool tune,
+                               cudaStream_t st) {
+    Cast_Args sh;
+    sh.rays = q.shd_rays;
+    sh.count = q.counters + 1;
+    sh.n_max = count;
+    sh.perm = q.shd_slot;
+    sh.next_ray = q.counters + 5;
+    sh.err = reinterpret_cast<int*>(q.counters + 3);
+    sh.occluded = ps.occluded;
+    int& k = ctx->render_kernel[1];
+    cudaError_t e = (tune && k < 0) ? tune_cast(ctx->ds, sh, true, st, ctx->ev_start, ctx->ev_stop, &k)
+                                    : launch_shadow(ctx->ds, sh, k < 0 ? kCastPersistent64 : k, st);
+    if (e != cudaSuccess) return e;
+    Cast_Args pr;
+    pr.rays = q.prb_rays;
+    pr.count = q.counters + 2;
+    pr.n_max = count;
+    pr.perm = q.prb_slot;
+    pr.next_ray = q.counters + 6;
+    pr.err = reinterpret_cast<int*>(q.counters + 3);
+    pr.hit4 = ps.probe_hit4;
+    pr.hit2 = ps.probe_hit2;
+    const int kc = ctx->render_kernel[0];
+    return launch_extend(ctx->ds, pr, kc < 0 ? kCastPersistent64 : kc, st);
 }
 
 // ---------------------------------------------------------------- shading context
@@ -308,20 +396,22 @@ __device__ __forceinline__ void init_shading(const Scene_Dev& S, V3 ray_d, uint3
     sc.dpdu_shading = dpdu_shading;
 }
 
+// A path's view of its pixel's sample tables: dimension i of this sample is
+// s1d[i * spp] (s1d already offset to the sample).
 struct Dims {
     const float* s1d;
     const float2* s2d;
-    int n1d, n2d, i1d, i2d;
+    int n1d, n2d, i1d, i2d, spp;
     Pcg rng;
     bool rng_used;
 };
 __device__ __forceinline__ float next1d(Dims& d) {
-    if (d.i1d < d.n1d) return d.s1d[d.i1d++];
+    if (d.i1d < d.n1d) return d.s1d[(size_t)(d.i1d++) * d.spp];
     d.rng_used = true;
     return pcg_float(d.rng);
 }
 __device__ __forceinline__ float2 next2d(Dims& d) {
-    if (d.i2d < d.n2d) return d.s2d[d.i2d++];
+    if (d.i2d < d.n2d) return d.s2d[(size_t)(d.i2d++) * d.spp];
     d.rng_used = true;
     const float a = pcg_float(d.rng);
     const float b = pcg_float(d.rng);
@@ -364,8 +454,12 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
             if (!hit || is_light) done = true;
             if (!done) {
                 Dims dm;
-                dm.s1d = s1d + (size_t)slot * p.n1d;
-                dm.s2d = s2d + (size_t)slot * p.n2d;
+                {
+                    const uint32_t lp = slot / (uint32_t)p.spp, k = slot - lp * (uint32_t)p.spp;
+                    dm.s1d = s1d + (size_t)lp * p.n1d * p.spp + k;
+                    dm.s2d = s2d + (size_t)lp * p.n2d * p.spp + k;
+                    dm.spp = p.spp;
+                }
                 dm.n1d = p.n1d;
                 dm.n2d = p.n2d;
                 dm.i1d = (int)((info >> 8) & 0xffu);
@@ -605,16 +699,51 @@ __device__ __forceinline__ void tile_pixel_bounds(const Render_Params& p, int t,
 }
 
 // Tile variance accumulators in the reference's pixel order (render_tile loops).
-__global__ void tile_variance_kernel(Render_Params p, const double* __restrict__ pixel_variance,
-                                     double* __restrict__ tile_variance) {
-    const int t = blockIdx.x * blockDim.x + threadIdx.x;
-    if (t >= p.tiles_x * p.tiles_y) return;
+// One block per tile: the block stages the tile's pixel variances in shared
+// memory with coalesced loads, then one thread adds them in the reference's
+// sequential (y, x) order (double addition is not associative).
+constexpr int kTileVarThreads = 256;
+__global__ void __launch_bounds__(kTileVarThreads)
+tile_variance_kernel(Render_Params p, const double* __restrict__ pixel_variance, double* __restrict__ tile_variance) {
+    __shared__ double v[kTile * kTile];
+    const int t = blockIdx.x;
     int x0, y0, x1, y1;
     tile_sample_bounds(p, t, x0, y0, x1, y1);
-    double acc = 0.0;
-    for (int y = y0; y < y1; y++)
-        for (int x = x0; x < x1; x++) acc += pixel_variance[(size_t)(y - p.sy0) * p.sw + (x - p.sx0)];
-    tile_variance[t] = acc;
+    const int w = x1 - x0, h = y1 - y0;
+    for (int i = threadIdx.x; i < w * h; i += blockDim.x) {
+        const int y = i / w, x = i - y * w;
+        v[i] = pixel_variance[(size_t)(y0 + y - p.sy0) * p.sw + (x0 + x - p.sx0)];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double acc = 0.0;
+        for (int i = 0; i < w * h; i++) acc += v[i];
+        tile_variance[t] = acc;
+    }
+}
+
+// Sample tables and camera rays of a chunk.  The table kernel's block is
+// sized so that its spp float2 per thread fit in 96 KB of shared memory.
+cudaError_t launch_generate(const Render_Params& p, uint32_t first, uint32_t cp, float* s1d, float* s2d,
+                            float2* image_samples, const Path_State& ps, const Queues& q, cudaStream_t st) {
+    constexpr size_t kSmemLimit = 96 * 1024;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(sample_tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kSmemLimit);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    const size_t per_thread = (size_t)p.spp * sizeof(float2);
+    int threads = 128;
+    while (threads > 1 && (size_t)threads * per_thread > kSmemLimit) threads /= 2;
+    if ((size_t)threads * per_thread > kSmemLimit) return cudaErrorInvalidValue;
+    const uint64_t rows = (uint64_t)cp * (1u + (uint32_t)p.n1d + (uint32_t)p.n2d);
+    sample_tables_kernel<<<(uint32_t)((rows + threads - 1) / threads), threads, threads * per_thread, st>>>(
+        p, first, cp, s1d, s2d, image_samples);
+    const uint32_t paths = cp * (uint32_t)p.spp;
+    camera_kernel<<<(paths + kBlock - 1) / kBlock, kBlock, 0, st>>>(p, first, paths, image_samples, ps, q);
+    return cudaGetLastError();
 }
 
 // One film pixel: the tiles whose samples reach it are merged in tile order
@@ -948,22 +1077,19 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
     for (uint64_t first = 0; first < pixels && e == cudaSuccess; first += chunk_pixels) {
         const uint32_t cp = (uint32_t)std::min<uint64_t>(chunk_pixels, pixels - first);
         const uint32_t paths = cp * (uint32_t)p.spp;
-        generate_kernel<<<(cp + kBlock - 1) / kBlock, kBlock, 0, st>>>(p, (uint32_t)first, cp, dptr<float>(B[2]),
-                                                                       dptr<float>(B[3]), image_samples, ps, q);
+        launch_generate(p, (uint32_t)first, cp, dptr<float>(B[2]), dptr<float>(B[3]), image_samples, ps, q, st);
         launches++;
         int cur = 0;
         uint32_t count = paths;
         for (int bounce = 0; count > 0 && bounce <= p.max_bounces + 1; bounce++) {
-            closest_queue_kernel<false><<<grid_for(count), kBlock, 0, st>>>(ctx->ds, q.ext_rays[cur], nullptr, nullptr,
-                                                                         count, q.ext_hit4, q.ext_hit2, q.counters + 3);
+            const bool tune = bounce >= 1 && count >= kRenderTuneMinRays;
+            e = trace_extend(ctx, q, cur, count, tune, st);
+            if (e != cudaSuccess) break;
             cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
             shade_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, cur, count, dptr<float>(B[2]),
                                                              dptr<float2>(B[3]), ps, q);
-            shadow_queue_kernel<<<grid_for(count), kBlock, 0, st>>>(ctx->ds, q.shd_rays, q.shd_slot, q.counters + 1,
-                                                                    ps.occluded, q.counters + 3);
-            closest_queue_kernel<true><<<grid_for(count), kBlock, 0, st>>>(ctx->ds, q.prb_rays, q.prb_slot,
-                                                                        q.counters + 2, 0, ps.probe_hit4,
-                                                                        ps.probe_hit2, q.counters + 3);
+            e = trace_light_queues(ctx, q, ps, count, tune, st);
+            if (e != cudaSuccess) break;
             connect_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, q.ext_slot[cur], count, ps);
             launches += 5;
             uint32_t h[4];
@@ -981,8 +1107,8 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
     }
     if (e == cudaSuccess) {
         samples_kernel<<<(uint32_t)((pixels + kBlock - 1) / kBlock), kBlock, 0, st>>>(p, radiance, dptr<double>(B[27]));
-        tile_variance_kernel<<<(p.tiles_x * p.tiles_y + 63) / 64, 64, 0, st>>>(p, dptr<double>(B[27]),
-                                                                               dptr<double>(B[28]));
+        tile_variance_kernel<<<p.tiles_x * p.tiles_y, kTileVarThreads, 0, st>>>(p, dptr<double>(B[27]),
+                                                                                dptr<double>(B[28]));
         film_kernel<<<(uint32_t)(((uint64_t)p.rw * p.rh + kBlock - 1) / kBlock), kBlock, 0, st>>>(
             p, radiance, image_samples, dptr<float>(B[29]));
         launches += 3;
@@ -1187,22 +1313,18 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
     for (uint64_t first = 0; first < pixels && e == cudaSuccess; first += chunk_pixels) {
         const uint32_t cp = (uint32_t)std::min<uint64_t>(chunk_pixels, pixels - first);
         const uint32_t paths = cp * (uint32_t)p.spp;
-        generate_kernel<<<(cp + kBlock - 1) / kBlock, kBlock, 0, st>>>(p, (uint32_t)first, cp, s1d,
-                                                                       reinterpret_cast<float*>(s2d), image_samples,
-                                                                       ps, q);
+        launch_generate(p, (uint32_t)first, cp, s1d, reinterpret_cast<float*>(s2d), image_samples, ps, q, st);
         launches++;
         int cur = 0;
         uint32_t count = paths;
         for (int bounce = 0; count > 0 && bounce <= p.max_bounces + 1; bounce++) {
-            closest_queue_kernel<false><<<grid_for(count), kBlock, 0, st>>>(ctx->ds, q.ext_rays[cur], nullptr, nullptr,
-                                                                         count, q.ext_hit4, q.ext_hit2, q.counters + 3);
+            const bool tune = bounce >= 1 && count >= kRenderTuneMinRays;
+            e = trace_extend(ctx, q, cur, count, tune, st);
+            if (e != cudaSuccess) break;
             cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
             shade_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, cur, count, s1d, s2d, ps, q);
-            shadow_queue_kernel<<<grid_for(count), kBlock, 0, st>>>(ctx->ds, q.shd_rays, q.shd_slot, q.counters + 1,
-                                                                    ps.occluded, q.counters + 3);
-            closest_queue_kernel<true><<<grid_for(count), kBlock, 0, st>>>(ctx->ds, q.prb_rays, q.prb_slot,
-                                                                        q.counters + 2, 0, ps.probe_hit4,
-                                                                        ps.probe_hit2, q.counters + 3);
+            e = trace_light_queues(ctx, q, ps, count, tune, st);
+            if (e != cudaSuccess) break;
             connect_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, q.ext_slot[cur], count, ps);
             launches += 5;
             uint32_t h[4];
@@ -1221,7 +1343,7 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
     double variance = 0.0;
     if (e == cudaSuccess) {
         samples_kernel<<<(uint32_t)((pixels + kBlock - 1) / kBlock), kBlock, 0, st>>>(p, radiance, pixel_variance);
-        tile_variance_kernel<<<(uint32_t)((tiles + 63) / 64), 64, 0, st>>>(p, pixel_variance, tile_variance);
+        tile_variance_kernel<<<(uint32_t)tiles, kTileVarThreads, 0, st>>>(p, pixel_variance, tile_variance);
         variance_total_kernel<<<1, 1, 0, st>>>(p, tile_variance, variance_total);
         film_kernel<<<(uint32_t)(((uint64_t)p.rw * p.rh + kBlock - 1) / kBlock), kBlock, 0, st>>>(
             p, radiance, image_samples, rgb_out_device);

@@ -96,7 +96,10 @@ class HitSoa(C.Structure):
 
 
 class GpuOptions(C.Structure):
-    _fields_ = [("device", C.c_int32), ("max_batch_rays", C.c_uint32)]
+    _fields_ = [("device", C.c_int32), ("max_batch_rays", C.c_uint32), ("traversal_kernel", C.c_int32)]
+
+
+TRAVERSAL_AUTO, TRAVERSAL_PERSISTENT_64, TRAVERSAL_PERSISTENT_128, TRAVERSAL_PER_RAY = 0, 1, 2, 3
 
 
 class RenderStats(C.Structure):
@@ -197,10 +200,10 @@ def transform_bounds(object_to_world, bounds):
 class Context:
     """A yar_gpu_ctx: one CUDA device, one stream, one uploaded scene."""
 
-    def __init__(self, device=0, max_batch_rays=0):
+    def __init__(self, device=0, max_batch_rays=0, traversal_kernel=TRAVERSAL_AUTO):
         L = lib()
         h = C.c_void_p()
-        opts = GpuOptions(int(device), int(max_batch_rays))
+        opts = GpuOptions(int(device), int(max_batch_rays), int(traversal_kernel))
         rc = L.yar_gpu_create(C.byref(h), C.byref(opts))
         if rc != YAR_OK:
             raise YarError(rc, "yar_gpu_create (is a CUDA device visible?)")
