@@ -286,6 +286,34 @@ int yar_gpu_render(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats);
 #define YAR_GPU_STATIC_ARENA_BYTES (64u << 20)
 int yar_gpu_render_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats* stats);
 
+/* ---- learned directional proposal: the network ----
+ * No reference counterpart: the reference has no path guiding.  A BF16 MLP
+ * (FP32 accumulation on the tensor cores) maps a shading point to a mixture
+ * of 8 von Mises-Fisher lobes over world directions; the guided render
+ * trains it online and samples path continuations from it.  These calls
+ * expose the network itself (tests, custom training loops).
+ *   parameters: YAR_GUIDE_PARAMS floats, four row-major [out][in] matrices
+ *     W1 64x128, W2 64x64, W3 64x64, W4 64x64.  Input 127 and hidden unit 63
+ *     are the constant 1 (bias columns); outputs 0..39 are 8 x (mean xyz,
+ *     log kappa, logit).
+ *   box: scene bounds (min xyz, max xyz), positions are normalised by it.
+ *   queries (device, 16-byte aligned): 12 floats per row
+ *     {pos xyz, normal xyz, wo xyz, 0, 0, 0}
+ *   lobes (device): YAR_GUIDE_LOBE_FLOATS per row, 8 x {mean xyz, kappa, weight}
+ *   samples (device): 16 floats per row {pos, normal, wo, dir xyz, weight, 0, 0, 0};
+ *     loss = sum over rows of -(weight * weight_scale) * log q(dir) */
+#define YAR_GUIDE_PARAMS 20480
+#define YAR_GUIDE_LOBE_FLOATS 40
+int yar_guide_set_params(yar_gpu_ctx* ctx, const float* params);
+int yar_guide_get_params(yar_gpu_ctx* ctx, float* params);
+int yar_guide_infer(yar_gpu_ctx* ctx, const float* queries, uint32_t n, const float box[6], float* lobes);
+/* summed gradient of the loss (device, YAR_GUIDE_PARAMS floats); loss to the host */
+int yar_guide_gradient(yar_gpu_ctx* ctx, const float* samples, uint32_t n, const float box[6], float weight_scale,
+                       float* grad, float* loss);
+/* one Adam step (beta 0.9 / 0.99) on the loss */
+int yar_guide_train_step(yar_gpu_ctx* ctx, const float* samples, uint32_t n, const float box[6],
+                         float weight_scale, float learning_rate, float* loss);
+
 /* ---- host-side kd-tree builders (the reference's builder, same node stream) ----
  * The returned node array is owned by the library; release it with yar_free_nodes. */
 int yar_build_mesh_kdtree(const float* vertices, uint32_t vertex_count,

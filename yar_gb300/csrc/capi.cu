@@ -147,6 +147,7 @@ extern "C" void yar_gpu_destroy(yar_gpu_ctx* ctx) {
     cudaSetDevice(ctx->device);
     if (ctx->stream) cudaStreamSynchronize(ctx->stream);
     render_release(ctx);
+    guide_release(ctx);
     for (Device_Buffer* b : {&ctx->scene_nodes, &ctx->mesh_nodes, &ctx->objects, &ctx->tris, &ctx->d_rays, &ctx->d_t,
                              &ctx->d_prim, &ctx->d_obj, &ctx->d_bary, &ctx->d_occ})
         device_free(*b);

@@ -38,6 +38,17 @@ struct Render_Scene {
     uint32_t triangle_total = 0;
 };
 
+// The learned directional proposal's network (guide_mlp.cu): fp32 master
+// parameters with Adam moments, the bf16 operand images the tensor-core
+// kernels load, per-CTA partial gradients.
+constexpr int kGuideParams = 64 * 128 + 3 * 64 * 64;  // W1 (64x128), W2, W3, W4 (64x64), [out][in]
+constexpr int kGuideLobeFloats = 40;                   // 8 lobes x (mean xyz, kappa, weight)
+struct Guide {
+    Device_Buffer params, adam_m, adam_v, images, partials, scalars;
+    int step = 0;
+    float beta1 = 0.9f, beta2 = 0.99f, eps = 1e-8f;
+};
+
 } // namespace yar
 
 struct yar_gpu_ctx {
@@ -66,6 +77,9 @@ struct yar_gpu_ctx {
 
     // render scratch (path state, queues, per-pixel sample tables)
     std::vector<yar::Device_Buffer> render_scratch;
+
+    // learned proposal (allocated on first use)
+    yar::Guide guide;
 };
 
 namespace yar {
@@ -106,6 +120,22 @@ cudaError_t launch_shadow(const Device_Scene& s, const Cast_Args& a, int kernel,
 // `stream`), leaving the results of the last run in place; *best = fastest.
 cudaError_t tune_cast(const Device_Scene& s, const Cast_Args& a, bool any, cudaStream_t stream, cudaEvent_t ev0,
                       cudaEvent_t ev1, int* best);
+
+// guide network (guide_mlp.cu).  `box` = scene bounds (min xyz, max xyz)
+// for position normalisation.  Query rows: 3 float4 {pos, n.x | n.yz, wo.xy |
+// wo.z, -, -, -}; training rows add a 4th float4 and carry the sampled
+// direction in the 3rd: {.., wo.z, w.xyz | weight, -, -, -}.
+int guide_ensure(yar_gpu_ctx* ctx);
+int guide_reset(yar_gpu_ctx* ctx, uint64_t seed);
+int guide_set_params(yar_gpu_ctx* ctx, const float* host_params);
+void guide_release(yar_gpu_ctx* ctx);
+cudaError_t guide_infer(yar_gpu_ctx* ctx, const float4* queries, uint32_t n_max, const uint32_t* count,
+                        const float* box, float* lobes, cudaStream_t st);
+// One training step over the rows (Adam with learning rate `lr`), or, with
+// `grad_out`, only the summed gradient of the loss.  The loss sum is added to
+// ctx->guide.scalars[0].
+cudaError_t guide_train(yar_gpu_ctx* ctx, const float4* samples, uint32_t n_max, const uint32_t* count,
+                        const float* box, const float* w_scale_dev, float lr, float* grad_out, cudaStream_t st);
 
 // render (render.cu)
 int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene);

@@ -99,6 +99,9 @@ class GpuOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("max_batch_rays", C.c_uint32), ("traversal_kernel", C.c_int32)]
 
 
+GUIDE_PARAMS = 20480
+GUIDE_LOBE_FLOATS = 40
+
 TRAVERSAL_AUTO, TRAVERSAL_PERSISTENT_64, TRAVERSAL_PERSISTENT_128, TRAVERSAL_PER_RAY = 0, 1, 2, 3
 
 
@@ -122,6 +125,13 @@ EXPORTS = {
     "yar_gpu_cast_any_timed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_float)]),
     "yar_gpu_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
     "yar_gpu_render_static": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
+    "yar_guide_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "yar_guide_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
+    "yar_guide_infer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.c_void_p]),
+    "yar_guide_gradient": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.c_float,
+                                     C.c_void_p, C.POINTER(C.c_float)]),
+    "yar_guide_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.c_float,
+                                       C.c_float, C.POINTER(C.c_float)]),
     "yar_build_mesh_kdtree": (C.c_int, [C.c_void_p, C.c_uint32, C.c_void_p, C.c_uint32, C.c_int32,
                                         C.POINTER(C.c_float), C.POINTER(C.c_void_p), C.POINTER(C.c_uint32)]),
     "yar_build_scene_kdtree": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_void_p),
@@ -283,6 +293,35 @@ class Context:
         stats = RenderStats()
         self._check(lib().yar_gpu_render(self._h, _ptr(rgb), C.byref(stats)), "render")
         return rgb, stats
+
+    # ---- learned proposal network (device buffers are raw pointers)
+    def guide_set_params(self, params):
+        p = np.ascontiguousarray(params, np.float32)
+        assert p.size == GUIDE_PARAMS
+        self._check(lib().yar_guide_set_params(self._h, _ptr(p)), "guide_set_params")
+
+    def guide_get_params(self):
+        p = np.zeros(GUIDE_PARAMS, np.float32)
+        self._check(lib().yar_guide_get_params(self._h, _ptr(p)), "guide_get_params")
+        return p
+
+    def guide_infer(self, queries_ptr, n, box, lobes_ptr):
+        b = (C.c_float * 6)(*[float(x) for x in box])
+        self._check(lib().yar_guide_infer(self._h, queries_ptr, n, b, lobes_ptr), "guide_infer")
+
+    def guide_gradient(self, samples_ptr, n, box, weight_scale, grad_ptr):
+        b = (C.c_float * 6)(*[float(x) for x in box])
+        loss = C.c_float()
+        self._check(lib().yar_guide_gradient(self._h, samples_ptr, n, b, float(weight_scale), grad_ptr,
+                                             C.byref(loss)), "guide_gradient")
+        return loss.value
+
+    def guide_train_step(self, samples_ptr, n, box, weight_scale, learning_rate):
+        b = (C.c_float * 6)(*[float(x) for x in box])
+        loss = C.c_float()
+        self._check(lib().yar_guide_train_step(self._h, samples_ptr, n, b, float(weight_scale),
+                                               float(learning_rate), C.byref(loss)), "guide_train_step")
+        return loss.value
 
     def render_static(self, rgb_device_ptr):
         """yar_gpu_render_static: renders into caller-owned device memory
