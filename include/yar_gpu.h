@@ -286,6 +286,40 @@ int yar_gpu_render(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats);
 #define YAR_GPU_STATIC_ARENA_BYTES (64u << 20)
 int yar_gpu_render_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats* stats);
 
+/* ---- guided render (config: the uploaded scene's camera, region, depth, RR, film clamp) ----
+ * No reference counterpart.  Renders `passes` independent one-sample-per-
+ * pixel passes of the path tracer and returns the per-pixel FP64 sum of the
+ * sample radiance (clamped and scaled as the film does) and/or the mean.
+ * With guide_fraction > 0 the continuation of each path vertex is drawn
+ * from the learned proposal with that probability (one-sample MIS with the
+ * BSDF, so the estimate stays unbiased); the first train_passes passes also
+ * train the proposal online from their own path samples.  guide_fraction 0
+ * is the plain path tracer (the baseline).  Requires a box filter of radius
+ * <= 0.5 (each sample lands in its own pixel). */
+typedef struct yar_guided_params {
+    uint32_t passes;          /* samples per pixel, one independent pass each */
+    uint32_t train_passes;    /* guided: the first passes also train the proposal */
+    float guide_fraction;     /* probability of drawing a continuation from the proposal, [0, 1) */
+    float learning_rate;      /* Adam step size */
+    uint32_t train_steps;     /* optimizer steps (minibatches) per training pass */
+    uint32_t stream_offset;   /* distinct values give statistically independent renders (< 4096) */
+    float time_budget;        /* seconds; > 0 stops after the pass that reaches it */
+    uint32_t keep_guide;      /* 1: start from the current network instead of re-initialising it */
+} yar_guided_params;
+
+typedef struct yar_guided_stats {
+    uint32_t passes;          /* passes rendered */
+    float seconds;            /* wall time of the passes, training included */
+    float train_seconds;      /* of which record finalisation and optimizer steps */
+    uint64_t rays;            /* closest-hit + any-hit rays traced */
+    uint64_t train_samples;   /* training samples used */
+    float loss;               /* loss of the last minibatch (mean over its samples) */
+} yar_guided_stats;
+
+/* radiance_sum: host double[w * h * 3] or NULL; rgb_out: host float[w * h * 3] or NULL */
+int yar_gpu_guided_render(yar_gpu_ctx* ctx, const yar_guided_params* params, double* radiance_sum, float* rgb_out,
+                          yar_guided_stats* stats);
+
 /* ---- learned directional proposal: the network ----
  * No reference counterpart: the reference has no path guiding.  A BF16 MLP
  * (FP32 accumulation on the tensor cores) maps a shading point to a mixture

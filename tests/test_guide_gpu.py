@@ -70,7 +70,7 @@ def features(rows):
     p = (r[:, 0:3] - lo) / (hi - lo)
     cols = []
     for k in range(16):
-        s = 2.0 ** (0.5 * k)
+        s = float(np.exp2(np.float32(k) * np.float32(1.0 / 3.0)))
         for c in range(3):
             x = p[:, c].float().double() * s
             cols += [torch.sin(math.pi * x), torch.cos(math.pi * x)]

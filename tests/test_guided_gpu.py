@@ -1,0 +1,66 @@
+"""GPU tests of the guided render (yar_gpu_guided_render): its plain mode is
+the reference's path tracer in independent one-sample passes, and drawing
+continuations from the learned proposal changes the noise, not the
+expectation (one-sample MIS with the BSDF).
+
+Image means are compared, at sample counts where their Monte Carlo error is
+well under the stated bound: 3% between two estimators of the same image."""
+import numpy as np
+import pytest
+
+from conftest import golden
+from yar_gb300 import native, scenes
+from yar_gb300.scene import FlatScene
+
+pytestmark = pytest.mark.gpu
+
+MEAN_REL_TOL = 0.03
+
+
+@pytest.fixture(scope="module")
+def small_room():
+    s = scenes.hard_lighting_room(width=64, height=64, cells=100)
+    return s
+
+
+def test_plain_passes_match_the_reference_render(gpu_ctx):
+    s = FlatScene.read(golden("cornell_c1_64.yfs"))
+    g = np.load(golden("cornell_c1_64.npz"))
+    gpu_ctx.upload_scene(s)
+    img, sums, st = gpu_ctx.guided_render(64, 64, passes=64)
+    assert st.passes == 64 and st.train_samples == 0
+    assert np.allclose(sums / 64.0, img, rtol=1e-6, atol=1e-7)
+    ref = g["image"].astype(np.float64)
+    assert abs(img.mean() - ref.mean()) < MEAN_REL_TOL * ref.mean(), (img.mean(), ref.mean())
+    # independent pass streams: two offsets give different images with the same mean
+    img2, _, _ = gpu_ctx.guided_render(64, 64, passes=64, stream_offset=1)
+    assert not np.array_equal(img, img2)
+    assert abs(img2.mean() - img.mean()) < MEAN_REL_TOL * img.mean()
+
+
+def test_guided_is_unbiased_and_trains(gpu_ctx, small_room):
+    gpu_ctx.upload_scene(small_room)
+    plain, _, st_p = gpu_ctx.guided_render(64, 64, passes=512)
+    guided, _, st_g = gpu_ctx.guided_render(64, 64, passes=512, guide_fraction=0.5, train_passes=32,
+                                            stream_offset=2)
+    assert st_g.train_samples > 0 and np.isfinite(st_g.loss)
+    assert plain.mean() > 0
+    assert abs(guided.mean() - plain.mean()) < MEAN_REL_TOL * plain.mean(), (guided.mean(), plain.mean())
+    # the halves of the image agree too (the opening's light pool vs the rest)
+    for sl in (np.s_[:32], np.s_[32:]):
+        assert abs(guided[sl].mean() - plain[sl].mean()) < 2 * MEAN_REL_TOL * plain[sl].mean()
+
+
+def test_time_budget_stops_early(gpu_ctx, small_room):
+    gpu_ctx.upload_scene(small_room)
+    _, _, st = gpu_ctx.guided_render(64, 64, passes=100000, time_budget=0.5)
+    assert 1 <= st.passes < 100000
+    assert st.seconds >= 0.5
+
+
+def test_invalid_guided_params(gpu_ctx, small_room):
+    gpu_ctx.upload_scene(small_room)
+    for kw in ({"passes": 0}, {"passes": 4, "guide_fraction": 1.0}, {"passes": 4, "guide_fraction": -0.1}):
+        with pytest.raises(native.YarError) as e:
+            gpu_ctx.guided_render(64, 64, **kw)
+        assert e.value.code == native.YAR_ERR_INVALID

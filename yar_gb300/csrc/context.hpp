@@ -80,6 +80,7 @@ struct yar_gpu_ctx {
 
     // learned proposal (allocated on first use)
     yar::Guide guide;
+    float guided_weight_scale = 1.f;  // host source of an asynchronous copy during guided renders
 };
 
 namespace yar {
@@ -131,15 +132,19 @@ int guide_set_params(yar_gpu_ctx* ctx, const float* host_params);
 void guide_release(yar_gpu_ctx* ctx);
 cudaError_t guide_infer(yar_gpu_ctx* ctx, const float4* queries, uint32_t n_max, const uint32_t* count,
                         const float* box, float* lobes, cudaStream_t st);
-// One training step over the rows (Adam with learning rate `lr`), or, with
-// `grad_out`, only the summed gradient of the loss.  The loss sum is added to
-// ctx->guide.scalars[0].
+// One training step over rows offset, offset + stride, ... (n_max of them,
+// or as many as `count` holds rows when set): Adam with learning rate `lr`,
+// or, with `grad_out`, only the summed gradient of the loss.  The loss sum is
+// added to ctx->guide.scalars[0].
 cudaError_t guide_train(yar_gpu_ctx* ctx, const float4* samples, uint32_t n_max, const uint32_t* count,
-                        const float* box, const float* w_scale_dev, float lr, float* grad_out, cudaStream_t st);
+                        uint32_t stride, uint32_t offset, const float* box, const float* w_scale_dev, float lr,
+                        float* grad_out, cudaStream_t st);
 
 // render (render.cu)
 int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene);
 void render_release(yar_gpu_ctx* ctx);
 int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats);
+int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* params, double* sum_out, float* rgb_out,
+                  yar_guided_stats* stats);
 
 } // namespace yar

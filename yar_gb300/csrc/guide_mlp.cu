@@ -3,7 +3,7 @@
 // tensor memory), with hand-written inference and training kernels.
 //
 // Network: 128 inputs (16-frequency sin/cos encoding of the normalised
-// position = 96, shading normal 3, outgoing direction 3, zeros, input 127 =
+// position, frequencies pi 2^(k/3), k = 0..15: 96, shading normal 3, outgoing direction 3, zeros, input 127 =
 // constant 1) -> 3 hidden layers of 64 ReLU units (unit 63 of each is the
 // constant 1, so every bias is an ordinary weight column) -> 64 outputs, of
 // which 40 parameterise a mixture of 8 von Mises-Fisher lobes in world space:
@@ -76,6 +76,7 @@ struct Mlp_Args {
     const float4* rows;  // 3 float4 per query row, 4 per training row
     uint32_t n;
     const uint32_t* count;
+    uint32_t stride, offset;  // row r of this launch is input row offset + r * stride
     float3 lo, inv_ext;
     float* lobes;          // inference: kGuideLobeFloats per row
     float* partials;       // training: kGuideParams per CTA
@@ -89,13 +90,14 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-// Input feature j of a row (j < 96: sin/cos of pi 2^(k/2) p, k = j / 6).
+// Input feature j of a row (j < 96: sin/cos of pi 2^(k/3) p, k = j / 6:
+// 16 frequencies from 1 to 32 half-periods across the scene box).
 __device__ __forceinline__ float feature(int j, float3 p, float3 nrm, float3 wo, bool valid) {
     if (!valid) return 0.f;
     if (j < 96) {
         const int k = j / 6, m = j % 6;
         const float c = (m < 2) ? p.x : (m < 4 ? p.y : p.z);
-        const float x = c * exp2f(0.5f * (float)k);
+        const float x = c * exp2f((float)k * (1.f / 3.f));
         return (m & 1) ? cospif(x) : sinpif(x);
     }
     switch (j) {
@@ -228,7 +230,7 @@ __global__ void __launch_bounds__(kRows, 1) mlp_kernel(Mlp_Args a) {
     const uint32_t tmem = *tmem_slot;
     const uint32_t lane_addr = tmem + ((uint32_t)(warp * 32) << 16);
 
-    const uint32_t n = a.count ? *a.count : a.n;
+    const uint32_t n = a.count ? (*a.count > a.offset ? (*a.count - a.offset + a.stride - 1) / a.stride : 0u) : a.n;
     const uint32_t tiles = (n + kRows - 1) / kRows;
     const uint32_t r0 = base + (TRAIN ? kTrR0 : kInR0);
     uint8_t* R0 = sm + (TRAIN ? kTrR0 : kInR0);
@@ -251,7 +253,7 @@ __global__ void __launch_bounds__(kRows, 1) mlp_kernel(Mlp_Args a) {
         float3 p = make_float3(0.f, 0.f, 0.f), nrm = p, wo = p, wdir = p;
         float wt = 0.f;
         if (valid) {
-            const float4* q = a.rows + (size_t)row * (TRAIN ? 4 : 3);
+            const float4* q = a.rows + ((size_t)a.offset + (size_t)row * a.stride) * (TRAIN ? 4 : 3);
             const float4 q0 = __ldg(q), q1 = __ldg(q + 1), q2 = __ldg(q + 2);
             p = make_float3((q0.x - a.lo.x) * a.inv_ext.x, (q0.y - a.lo.y) * a.inv_ext.y,
                             (q0.z - a.lo.z) * a.inv_ext.z);
@@ -549,6 +551,8 @@ cudaError_t guide_infer(yar_gpu_ctx* ctx, const float4* queries, uint32_t n_max,
     a.rows = queries;
     a.n = n_max;
     a.count = count;
+    a.stride = 1;
+    a.offset = 0;
     a.lo = make_float3(box[0], box[1], box[2]);
     a.inv_ext = make_float3(1.f / std::max(box[3] - box[0], 1e-20f), 1.f / std::max(box[4] - box[1], 1e-20f),
                             1.f / std::max(box[5] - box[2], 1e-20f));
@@ -561,7 +565,8 @@ cudaError_t guide_infer(yar_gpu_ctx* ctx, const float4* queries, uint32_t n_max,
 }
 
 cudaError_t guide_train(yar_gpu_ctx* ctx, const float4* samples, uint32_t n_max, const uint32_t* count,
-                        const float* box, const float* w_scale_dev, float lr, float* grad_out, cudaStream_t st) {
+                        uint32_t stride, uint32_t offset, const float* box, const float* w_scale_dev, float lr,
+                        float* grad_out, cudaStream_t st) {
     Guide& g = ctx->guide;
     if (n_max == 0) return cudaSuccess;
     Mlp_Args a{};
@@ -569,6 +574,8 @@ cudaError_t guide_train(yar_gpu_ctx* ctx, const float4* samples, uint32_t n_max,
     a.rows = samples;
     a.n = n_max;
     a.count = count;
+    a.stride = stride;
+    a.offset = offset;
     a.lo = make_float3(box[0], box[1], box[2]);
     a.inv_ext = make_float3(1.f / std::max(box[3] - box[0], 1e-20f), 1.f / std::max(box[4] - box[1], 1e-20f),
                             1.f / std::max(box[5] - box[2], 1e-20f));
@@ -636,7 +643,7 @@ int guide_step(yar_gpu_ctx* ctx, const float* samples, uint32_t n, const float* 
     const float h[2] = {0.f, weight_scale};
     cudaError_t e = cudaMemcpyAsync(scal, h, sizeof(h), cudaMemcpyHostToDevice, ctx->stream);
     if (e == cudaSuccess)
-        e = guide_train(ctx, (const float4*)samples, n, nullptr, box, scal + 1, lr, grad, ctx->stream);
+        e = guide_train(ctx, (const float4*)samples, n, nullptr, 1, 0, box, scal + 1, lr, grad, ctx->stream);
     return guide_finish(ctx, e, "guide training step", loss);
 }
 

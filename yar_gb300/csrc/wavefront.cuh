@@ -1,0 +1,1020 @@
+// wavefront.cuh - the wavefront path tracer's kernels and their host-side
+// launch helpers, shared by the reference-order render (render.cu) and the
+// guided render (guided.cu).  Everything here has internal linkage: each
+// translation unit that includes it gets its own copies.
+//
+// Kernels, one wavefront step each:
+//   sample tables / camera   per (pixel, dimension) row and per path: the
+//              pixel's pcg stream, its stratified + shuffled sample tables
+//              (Stratified_Pixel_Sampler::next_pixel, src/ref/pixel_sampling.cpp:54-141)
+//              and one camera ray per sample (Camera::generate_ray, src/ref/camera.cpp:16-31)
+//   extend     closest hit for the path rays (shared traversal, cast.cu)
+//   shade      per path vertex: emission, shading context, BSDF, the light
+//              sample (shadow ray), the MIS BSDF sample (probe ray), the
+//              continuation ray and Russian roulette
+//              (trace_path, src/ref/path_tracing.cpp:11-133;
+//               direct_lighting_from_rectangular_light, direct_lighting.cpp:109-194)
+//   shadow     any hit for the shadow queue
+//   probe      closest hit for the MIS probe queue
+//   connect    adds the vertex's direct light in the reference's order
+//   film       clamp/scale, luminance variance, tile-ordered film merge and
+//              resolve (src/ref/film.cpp, reference_renderer.cpp:388-409, :565-581)
+//
+// Paths of a chunk of pixels live in structure-of-arrays state indexed by
+// slot = pixel_in_chunk * spp + sample.  Ray queues are compacted with one
+// warp-aggregated atomic per warp.  Queue order is not deterministic, the
+// results are: every path and every film pixel is computed in the
+// reference's order.
+#pragma once
+
+#include "context.hpp"
+#include "shade.cuh"
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstring>
+#include <string>
+
+namespace yar {
+
+namespace {
+
+constexpr int kBlock = 128;
+constexpr int kTile = 64;                           // src/ref/film.cpp:5
+constexpr uint64_t kChunkSampleBudget = 16u << 20;  // paths in flight per chunk
+
+enum : uint32_t { kPendShadow = 1u << 24, kPendProbe = 1u << 25, kPendDirect = 1u << 26 };
+
+struct Rect_Light_Dev {
+    float4 r0, r1, r2;  // light_to_world rows
+    float4 le;          // emitted radiance rgb, size.x
+    float4 sz;          // size.y, -, -, -
+};
+
+struct Render_Params {
+    yar_camera_desc camera;
+    int32_t sx0, sy0, sw, sh;    // sample region
+    int32_t rx0, ry0, rw, rh;    // render region
+    int32_t tiles_x, tiles_y;
+    int32_t nx, ny, spp, n1d, n2d;
+    int32_t max_bounces, rr_bounce_threshold;
+    float rr_threshold;
+    float filter_radius;
+    float film_scale, max_component;
+    int32_t total_lights, rect_lights;
+    uint32_t seed_offset;
+    uint32_t stream_hi;  // upper 32 bits of the pixel streams' sequence (0 = the reference's streams)
+};
+
+struct Path_State {
+    float4* coeff;
+    float4* L;
+    uint32_t* info;        // bounce | i1d << 8 | i2d << 16 | pending flags
+    uint4* rng;            // pcg state for dimensions beyond the sampler budget
+    float4* pend_light;    // unoccluded light-sample contribution
+    float4* pend_probe0;   // Le * f, bsdf pdf
+    float4* pend_probe1;   // probe origin, dot(light_n, -wi)
+    float4* pend_probe2;   // dot(n, wi), light index bits
+    float4* pend_coeff;    // path throughput at the vertex
+    uint8_t* occluded;
+    float4* probe_hit4;    // t, b0, b1, b2
+    uint2* probe_hit2;     // prim, object
+    uint32_t* rec;         // guided training: this bounce's record index (0xffffffff = none)
+};
+
+// Learned-proposal hooks of the shade kernel (guided render only).
+// Training records, kGuideRecordF4 float4 each:
+//   0 {pos, n.x}  1 {n.yz, wo.xy}  2 {wo.z, dir}  3 {f cos / p (luminance), slot bits, -, -}
+//   4 {path throughput after the continuation}  5 {path radiance after this vertex's direct light}
+constexpr int kGuideRecordF4 = 6;
+struct Guide_Shade {
+    const float* lobes = nullptr;    // per extend-queue position (null: BSDF continuation only)
+    const float4* queries = nullptr; // per extend-queue position: 3 float4 of the network input
+    float alpha = 0.f;               // probability of drawing the continuation from the mixture
+    float4* records = nullptr;       // null: no training records
+    uint32_t* record_count = nullptr;
+    uint32_t record_capacity = 0;
+};
+
+// Mixture of von Mises-Fisher lobes {mean xyz, kappa, weight} x 8.
+__device__ __forceinline__ float vmf_norm(float kappa) {
+    // kappa / (2 pi (1 - exp(-2 kappa)))
+    return kappa / (6.283185307f * -expm1f(-2.f * kappa));
+}
+__device__ __forceinline__ float mixture_pdf(const float* lob, V3 w) {
+    float q = 0.f;
+#pragma unroll
+    for (int k = 0; k < 8; k++) {
+        const float c = lob[5 * k] * w.x + lob[5 * k + 1] * w.y + lob[5 * k + 2] * w.z;
+        const float kap = lob[5 * k + 3];
+        q += lob[5 * k + 4] * vmf_norm(kap) * __expf(kap * (c - 1.f));
+    }
+    return q;
+}
+// Lobe by its weight (u0), then the vMF direction (u1, u2) by inversion of
+// its cosine distribution (Jakob, "Numerically stable sampling of the von
+// Mises-Fisher distribution on S^2", 2012).
+__device__ __forceinline__ V3 mixture_sample(const float* lob, float u0, float u1, float u2) {
+    int k = 0;
+    float acc = lob[4];
+    while (k < 7 && u0 >= acc) {
+        k++;
+        acc += lob[5 * k + 4];
+    }
+    const V3 mu = v3(lob[5 * k], lob[5 * k + 1], lob[5 * k + 2]);
+    const float kap = lob[5 * k + 3];
+    const float cz = fminf(1.f, fmaxf(-1.f, 1.f + log1pf(u1 * expm1f(-2.f * kap)) / kap));
+    const float s = sqrtf(fmaxf(0.f, 1.f - cz * cz));
+    float sp, cp;
+    sincospif(2.f * u2, &sp, &cp);
+    const V3 t = coordinate_axis(mu);
+    const V3 b = cross(mu, t);
+    return mul(t, s * cp) + mul(b, s * sp) + mul(mu, cz);
+}
+
+struct Queues {
+    float4* ext_rays[2];
+    uint32_t* ext_slot[2];
+    float4* ext_hit4;
+    uint2* ext_hit2;
+    float4* shd_rays;
+    uint32_t* shd_slot;
+    float4* prb_rays;
+    uint32_t* prb_slot;
+    uint32_t* counters;  // [0] next ext, [1] shadow, [2] probe, [3] error
+};
+
+struct Scene_Dev {
+    Device_Scene ds;
+    const float4* shading;        // 4 float4 per triangle
+    const float4* obj_render;     // 7 float4 per object
+    const Material_Dev* materials;
+    const Rect_Light_Dev* lights;
+};
+
+// Warp-aggregated queue append: one atomic per warp and predicate value.
+__device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
+    const unsigned active = __activemask();
+    const unsigned mask = __ballot_sync(active, pred);
+    if (!pred) return 0xffffffffu;
+    const int lane = threadIdx.x & 31;
+    const int leader = __ffs(mask) - 1;
+    uint32_t base = 0;
+    if (lane == leader) base = atomicAdd(counter, (uint32_t)__popc(mask));
+    base = __shfl_sync(mask, base, leader);
+    return base + (uint32_t)__popc(mask & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ float one_minus_eps_min(float v) {
+    const float ome = __uint_as_float(0x3f7fffffu);  // 0x1.fffffep-1, src/lib/math.h:14
+    return v < ome ? v : ome;
+}
+
+// ---------------------------------------------------------------- generate
+// Stratified_Pixel_Sampler::next_pixel (src/ref/sampling.cpp:98-133) draws,
+// from the pixel's pcg stream and in this order: the image samples (2 draws
+// per sample), then per 1D dimension spp stratified values and spp - 1
+// shuffle draws, then per 2D dimension 2 spp values and spp - 1 shuffle draws.
+// The bounded draw of the shuffle takes exactly one number
+// (RNG::get_bounded_uint_fast_and_biased, src/lib/random.h:58-62), so every
+// dimension starts at a fixed offset of the stream.  Each (pixel, dimension)
+// is built by its own thread from a jump-ahead of the stream to that offset
+// (Brown, "Random number generation with arbitrary strides", 1994: the LCG
+// s' = a s + c advanced n steps is A_n s + C_n c, both computable in
+// O(log n)), instead of one thread walking the pixel's stream sequentially.
+//
+// Sample tables, per pixel of the chunk, dimension-major:
+//   s1d[(lp * n1d + dim) * spp + sample],  s2d[(lp * n2d + dim) * spp + sample]
+// A thread's column is shuffled in shared memory ([sample][thread], so the
+// random indices of a warp's lanes never share a bank) and stored as a
+// contiguous row; the lanes of a warp own adjacent rows.
+
+// Advance the pcg stream by n draws.
+__device__ __forceinline__ void pcg_advance(Pcg& r, uint32_t n) {
+    uint64_t cur_mult = 6364136223846793005ULL, cur_plus = 1u;  // increment factored out
+    uint64_t acc_mult = 1u, acc_plus = 0u;
+    while (n) {
+        if (n & 1u) {
+            acc_mult *= cur_mult;
+            acc_plus = acc_plus * cur_mult + cur_plus;
+        }
+        cur_plus = (cur_mult + 1u) * cur_plus;
+        cur_mult *= cur_mult;
+        n >>= 1;
+    }
+    r.state = acc_mult * r.state + acc_plus * r.inc;
+}
+
+__device__ __forceinline__ uint32_t pixel_stream(const Render_Params& p, uint32_t pix, int& x, int& y) {
+    x = p.sx0 + (int)(pix % (uint32_t)p.sw);
+    y = p.sy0 + (int)(pix / (uint32_t)p.sw);
+    uint32_t stream = ((uint32_t)x & 0xffffu) | ((uint32_t)y << 16);
+    return stream + p.seed_offset;
+}
+
+// One thread per (pixel, table row): row 0 the image samples, rows
+// 1..n1d the 1D dimensions, then the 2D dimensions.  Shared memory: spp float2
+// per thread.  Stores are float4 when the row length allows.
+__global__ void sample_tables_kernel(Render_Params p, uint32_t chunk_first, uint32_t chunk_pixels,
+                                     float* __restrict__ s1d, float* __restrict__ s2d,
+                                     float2* __restrict__ image_samples) {
+    extern __shared__ float2 gen_smem[];
+    const uint32_t rows = 1u + (uint32_t)p.n1d + (uint32_t)p.n2d;
+    const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
+    if (g >= (uint64_t)chunk_pixels * rows) return;
+    const uint32_t lp = (uint32_t)(g / rows);
+    const uint32_t row = (uint32_t)(g % rows);
+    int x, y;
+    Pcg rng = pcg_seed(0, (uint64_t)pixel_stream(p, chunk_first + lp, x, y) | ((uint64_t)p.stream_hi << 32));
+    const int spp = p.spp;
+    const uint32_t n1d = (uint32_t)p.n1d;
+    float2* sm = gen_smem + threadIdx.x;
+    const int stride = (int)blockDim.x;
+    const float dx = 1.f / (float)p.nx, dy = 1.f / (float)p.ny;
+    if (row == 0) {  // image samples: stratified, not shuffled
+        float2* img = image_samples + ((size_t)chunk_first + lp) * spp;
+        for (int j = 0; j < p.ny; j++)
+            for (int i = 0; i < p.nx; i++) {
+                const float a = one_minus_eps_min(((float)i + pcg_float(rng)) * dx);
+                const float b = one_minus_eps_min(((float)j + pcg_float(rng)) * dy);
+                img[j * p.nx + i] = make_float2(a, b);
+            }
+        return;
+    }
+    if (row <= n1d) {
+        const uint32_t dim = row - 1u;
+        pcg_advance(rng, (uint32_t)(2 * spp) + dim * (uint32_t)(2 * spp - 1));
+        const float d = 1.f / (float)spp;
+        for (int k = 0; k < spp; k++) sm[k * stride].x = one_minus_eps_min(((float)k + pcg_float(rng)) * d);
+        for (int m = spp; m > 1; m--) {  // shuffle, src/lib/math.h:138-145
+            const uint32_t r = pcg_bounded_fast(rng, (uint32_t)m);
+            const float t = sm[(m - 1) * stride].x;
+            sm[(m - 1) * stride].x = sm[r * stride].x;
+            sm[r * stride].x = t;
+        }
+        float* out = s1d + ((size_t)lp * n1d + dim) * spp;
+        if ((spp & 3) == 0) {
+            float4* o4 = reinterpret_cast<float4*>(out);
+            for (int k = 0; k < spp; k += 4)
+                o4[k >> 2] = make_float4(sm[k * stride].x, sm[(k + 1) * stride].x, sm[(k + 2) * stride].x,
+                                         sm[(k + 3) * stride].x);
+        } else {
+            for (int k = 0; k < spp; k++) out[k] = sm[k * stride].x;
+        }
+        return;
+    }
+    const uint32_t dim = row - 1u - n1d;
+    pcg_advance(rng, (uint32_t)(2 * spp) + n1d * (uint32_t)(2 * spp - 1) + dim * (uint32_t)(3 * spp - 1));
+    for (int j = 0; j < p.ny; j++)
+        for (int i = 0; i < p.nx; i++) {
+            const float a = one_minus_eps_min(((float)i + pcg_float(rng)) * dx);
+            const float b = one_minus_eps_min(((float)j + pcg_float(rng)) * dy);
+            sm[(j * p.nx + i) * stride] = make_float2(a, b);
+        }
+    for (int m = spp; m > 1; m--) {
+        const uint32_t r = pcg_bounded_fast(rng, (uint32_t)m);
+        const float2 t = sm[(m - 1) * stride];
+        sm[(m - 1) * stride] = sm[r * stride];
+        sm[r * stride] = t;
+    }
+    float2* out = reinterpret_cast<float2*>(s2d) + ((size_t)lp * (uint32_t)p.n2d + dim) * spp;
+    if ((spp & 1) == 0) {
+        float4* o4 = reinterpret_cast<float4*>(out);
+        for (int k = 0; k < spp; k += 2) {
+            const float2 a = sm[k * stride], b = sm[(k + 1) * stride];
+            o4[k >> 1] = make_float4(a.x, a.y, b.x, b.y);
+        }
+    } else {
+        for (int k = 0; k < spp; k++) out[k] = sm[k * stride];
+    }
+}
+
+// One thread per path of the chunk: camera ray (Camera::generate_ray,
+// src/ref/camera.cpp) through the path's image sample, path initialisation.
+__global__ void __launch_bounds__(kBlock)
+camera_kernel(Render_Params p, uint32_t chunk_first, uint32_t chunk_paths, const float2* __restrict__ image_samples,
+              Path_State ps, Queues q) {
+    const uint32_t slot = blockIdx.x * blockDim.x + threadIdx.x;
+    if (slot >= chunk_paths) return;
+    const int spp = p.spp;
+    const uint32_t lp = slot / (uint32_t)spp;
+    const uint32_t k = slot - lp * (uint32_t)spp;
+    int x, y;
+    const uint32_t stream = pixel_stream(p, chunk_first + lp, x, y);
+    const float2 s = image_samples[((size_t)chunk_first + lp) * spp + k];
+    const yar_camera_desc& c = p.camera;
+    const float4 m0 = make_float4(c.camera_to_world[0], c.camera_to_world[1], c.camera_to_world[2], c.camera_to_world[3]);
+    const float4 m1 = make_float4(c.camera_to_world[4], c.camera_to_world[5], c.camera_to_world[6], c.camera_to_world[7]);
+    const float4 m2 = make_float4(c.camera_to_world[8], c.camera_to_world[9], c.camera_to_world[10], c.camera_to_world[11]);
+    const float fx = (float)x + s.x;
+    const float fy = (float)y + s.y;
+    const float u = 2.f * (fx / c.image_extent[0]) - 1.f;
+    const float v = 2.f * (fy / c.image_extent[1]) - 1.f;
+    const float right = u * c.horz_half_dist;
+    const float up = -v * c.vert_half_dist;
+    V3 dir = v3(right, c.z_is_up ? 1.f : up, c.z_is_up ? up : -1.f);
+    dir = divs(dir, len(dir));
+    const V3 o = xform_point(m0, m1, m2, v3(0.f, 0.f, 0.f));
+    const V3 d = xform_vector(m0, m1, m2, dir);
+    q.ext_rays[0][2 * (size_t)slot] = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
+    q.ext_rays[0][2 * (size_t)slot + 1] = make_float4(d.x, d.y, d.z, 0.f);
+    q.ext_slot[0][slot] = slot;
+    ps.coeff[slot] = make_float4(1.f, 1.f, 1.f, 0.f);
+    ps.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
+    ps.info[slot] = 0u;
+    // dimensions beyond the sampler budget: an independent pcg stream per sample
+    const Pcg r2 = pcg_seed((uint64_t)k + 1u, (((uint64_t)stream << 20) ^ 0x2545F4914F6CDD1Dull) +
+                                                  (uint64_t)p.stream_hi * 0x9E3779B97F4A7C15ull);
+    ps.rng[slot] = make_uint4((uint32_t)r2.state, (uint32_t)(r2.state >> 32), (uint32_t)r2.inc,
+                              (uint32_t)(r2.inc >> 32));
+}
+
+// ---------------------------------------------------------------- extend / probe / shadow
+// The three ray queues of a bounce are traced by the cast kernels (cast.cu).
+// Extend hits are written at the queue position (shade reads the queue in
+// order); shadow and probe results at the path slot.  Hand-out counters are
+// counters[4..6], the error word counters[3].  The traversal kernel of each
+// ray kind is chosen by timing on the first bounce after the camera bounce
+// with at least kRenderTuneMinRays paths (secondary rays are the incoherent
+// majority), unless the context fixes it.
+constexpr uint32_t kRenderTuneMinRays = 1u << 16;
+
+cudaError_t trace_extend(yar_gpu_ctx* ctx, const Queues& q, int cur, uint32_t count, bool tune, cudaStream_t st) {
+    Cast_Args a;
+    a.rays = q.ext_rays[cur];
+    a.n = count;
+    a.next_ray = q.counters + 4;
+    a.err = reinterpret_cast<int*>(q.counters + 3);
+    a.hit4 = q.ext_hit4;
+    a.hit2 = q.ext_hit2;
+    int& k = ctx->render_kernel[0];
+    if (tune && k < 0) return tune_cast(ctx->ds, a, false, st, ctx->ev_start, ctx->ev_stop, &k);
+    return launch_extend(ctx->ds, a, k < 0 ? kCastPersistent64 : k, st);
+}
+
+cudaError_t trace_light_queues(yar_gpu_ctx* ctx, const Queues& q, const Path_State& ps, uint32_t count, bool tune,
+                               cudaStream_t st) {
+    Cast_Args sh;
+    sh.rays = q.shd_rays;
+    sh.count = q.counters + 1;
+    sh.n_max = count;
+    sh.perm = q.shd_slot;
+    sh.next_ray = q.counters + 5;
+    sh.err = reinterpret_cast<int*>(q.counters + 3);
+    sh.occluded = ps.occluded;
+    int& k = ctx->render_kernel[1];
+    cudaError_t e = (tune && k < 0) ? tune_cast(ctx->ds, sh, true, st, ctx->ev_start, ctx->ev_stop, &k)
+                                    : launch_shadow(ctx->ds, sh, k < 0 ? kCastPersistent64 : k, st);
+    if (e != cudaSuccess) return e;
+    Cast_Args pr;
+    pr.rays = q.prb_rays;
+    pr.count = q.counters + 2;
+    pr.n_max = count;
+    pr.perm = q.prb_slot;
+    pr.next_ray = q.counters + 6;
+    pr.err = reinterpret_cast<int*>(q.counters + 3);
+    pr.hit4 = ps.probe_hit4;
+    pr.hit2 = ps.probe_hit2;
+    const int kc = ctx->render_kernel[0];
+    return launch_extend(ctx->ds, pr, kc < 0 ? kCastPersistent64 : kc, st);
+}
+
+// ---------------------------------------------------------------- shading context
+// Shading_Context::initialize_local_geometry + init_from_triangle_mesh_intersection
+// (src/ref/shading_context.cpp:65-172, :188-240), constant materials, no bump.
+__device__ __forceinline__ void init_shading(const Scene_Dev& S, V3 ray_d, uint32_t object, uint32_t prim, float b0,
+                                             float b1, float b2, Shading& sc, int4& info) {
+    const float4* orec = S.ds.objects + 6 * (size_t)object;
+    const uint32_t tri_offset = __float_as_uint(__ldg(orec + 4).w);
+    const float4* rrec = S.obj_render + 7 * (size_t)object;
+    const float4 w0 = __ldg(rrec + 0), w1 = __ldg(rrec + 1), w2 = __ldg(rrec + 2);
+    const float4 n0 = __ldg(rrec + 3), n1 = __ldg(rrec + 4), n2 = __ldg(rrec + 5);
+    const float4 inf4 = __ldg(rrec + 6);
+    info = make_int4(__float_as_int(inf4.x), __float_as_int(inf4.y), __float_as_int(inf4.z), __float_as_int(inf4.w));
+    const size_t g = (size_t)tri_offset + prim;
+    const float4 q0 = __ldg(S.ds.tris + 3 * g), q1 = __ldg(S.ds.tris + 3 * g + 1), q2 = __ldg(S.ds.tris + 3 * g + 2);
+    const V3 p0 = v3(q0.x, q0.y, q0.z), p1 = v3(q1.x, q1.y, q1.z), p2 = v3(q2.x, q2.y, q2.z);
+    const float4 h0 = __ldg(S.shading + 4 * g), h1 = __ldg(S.shading + 4 * g + 1);
+    const float4 h2 = __ldg(S.shading + 4 * g + 2), h3 = __ldg(S.shading + 4 * g + 3);
+    const uint32_t flags = __float_as_uint(h3.w);
+
+    sc.wo = -normalized(ray_d);
+    V3 position = bary(p0, p1, p2, b0, b1, b2);
+    V3 gn = normalized(cross(p1 - p0, p2 - p0));
+    if (flags & 4u) gn = -gn;
+    V3 normal = gn;
+    if (flags & 1u) {
+        const V3 in = bary(v3(h0.x, h0.y, h0.z), v3(h1.x, h1.y, h1.z), v3(h2.x, h2.y, h2.z), b0, b1, b2);
+        if (len2(in) != 0.f) normal = normalized(in);
+    }
+    const bool has_uv = (flags & 2u) != 0;
+    V3 dpdu = v3(0.f, 0.f, 0.f);
+    if (has_uv) {
+        // uvs: u0 = h0.w, v0 = h1.w, u1 = h2.w, v1 = h3.x, u2 = h3.y, v2 = h3.z
+        const float a00 = h2.w - h0.w, a01 = h3.x - h1.w, a10 = h3.y - h0.w, a11 = h3.z - h1.w;
+        const V3 bp0 = p1 - p0, bp1 = p2 - p0;
+        const float det = a00 * a11 - a01 * a10;  // solve_linear_system_2x2, src/lib/math.cpp:8-16
+        if (det != 0.f) {
+            const float inv_det = 1.f / det;
+            dpdu = mul(mul(bp0, a11) - mul(bp1, a01), inv_det);
+        }
+        if (fabsf(det) < 1e-9f) dpdu = coordinate_axis(gn);
+    }
+    position = xform_point(make_float4(w0.x, w0.y, w0.z, w0.w), w1, w2, position);
+    normal = xform_vector(n0, n1, n2, normal);
+    normal = divs(normal, len(normal));
+    gn = xform_vector(n0, n1, n2, gn);
+    gn = divs(gn, len(gn));
+    dpdu = xform_vector(w0, w1, w2, dpdu);
+    if (dot(normal, gn) == 0.f) gn = normal;
+    if (dot(gn, sc.wo) < 0) gn = -gn;
+    sc.flipped = false;
+    if (dot(normal, gn) < 0) {
+        normal = -normal;
+        sc.flipped = true;
+    }
+    offset_axis(position.x, gn.x, sc.origin_pos.x, sc.origin_neg.x);
+    offset_axis(position.y, gn.y, sc.origin_pos.y, sc.origin_neg.y);
+    offset_axis(position.z, gn.z, sc.origin_pos.z, sc.origin_neg.z);
+    normal = adjust_shading_normal(sc.wo, gn, normal);
+    V3 dpdu_shading;
+    if (!has_uv) {
+        dpdu_shading = coordinate_axis(normal);
+    } else if (fabsf(dot(normal, gn) - 1.f) < 1e-6f) {
+        dpdu_shading = dpdu;
+    } else {
+        const V3 t = cross(dpdu, normal);
+        dpdu_shading = mul(normalized(cross(normal, t)), len(dpdu));
+    }
+    sc.position = position;
+    sc.ng = gn;
+    sc.n = normal;
+    sc.dpdu_shading = dpdu_shading;
+}
+
+// A path's view of its pixel's sample tables: dimension i of this sample is
+// s1d[i * spp] (s1d already offset to the sample).
+struct Dims {
+    const float* s1d;
+    const float2* s2d;
+    int n1d, n2d, i1d, i2d, spp;
+    Pcg rng;
+    bool rng_used;
+};
+__device__ __forceinline__ float next1d(Dims& d) {
+    if (d.i1d < d.n1d) return d.s1d[(size_t)(d.i1d++) * d.spp];
+    d.rng_used = true;
+    return pcg_float(d.rng);
+}
+__device__ __forceinline__ float2 next2d(Dims& d) {
+    if (d.i2d < d.n2d) return d.s2d[(size_t)(d.i2d++) * d.spp];
+    d.rng_used = true;
+    const float a = pcg_float(d.rng);
+    const float b = pcg_float(d.rng);
+    return make_float2(a, b);
+}
+
+// ---------------------------------------------------------------- shade
+// GUIDED adds the learned proposal to the continuation: with probability
+// g.alpha the direction comes from the vertex's lobe mixture instead of the
+// BSDF, and the throughput divides by the one-sample mixture pdf
+// alpha q + (1 - alpha) p_bsdf, so the estimator stays unbiased; the light
+// sample and the MIS probe are unchanged.  With g.records set, every
+// continued vertex also leaves a training record.
+template <bool GUIDED>
+__global__ void __launch_bounds__(kBlock)
+shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float* __restrict__ s1d,
+             const float2* __restrict__ s2d, Path_State ps, Queues q, Guide_Shade g) {
+    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        bool want_shadow = false, want_probe = false, want_next = false;
+        float4 sh_a = make_float4(0, 0, 0, 0), sh_b = sh_a, pr_a = sh_a, pr_b = sh_a, nx_a = sh_a, nx_b = sh_a;
+        uint32_t slot = 0;
+        if (i < count) {
+            slot = q.ext_slot[cur][i];
+            const float4 rb = q.ext_rays[cur][2 * (size_t)i + 1];
+            const float4 h4 = q.ext_hit4[i];
+            const uint2 h2 = q.ext_hit2[i];
+            float4 coeff4 = ps.coeff[slot];
+            float4 L4 = ps.L[slot];
+            uint32_t info = ps.info[slot];
+            int bounce = (int)(info & 0xffu);
+            Col coeff = col(coeff4.x, coeff4.y, coeff4.z);
+            Col L = col(L4.x, L4.y, L4.z);
+            const bool hit = h2.y != 0xffffffffu;
+            Shading sc;
+            int4 oinfo = make_int4(-1, -1, -1, -1);
+            if (hit) init_shading(S, v3(rb.x, rb.y, rb.z), h2.y, h2.x, h4.y, h4.z, h4.w, sc, oinfo);
+            const bool is_light = hit && (uint32_t)oinfo.z != 0xffffffffu;
+            bool done = false;
+            if (bounce == 0) {
+                if (is_light && (uint32_t)oinfo.z == YAR_LIGHT_DIFFUSE_RECTANGULAR) {
+                    const float4 le = __ldg(&S.lights[oinfo.w].le);
+                    L = L + coeff * col(le.x, le.y, le.z);
+                }
+                if (p.max_bounces == 0) done = true;
+            }
+            if (!hit || is_light) done = true;
+            if (!done) {
+                Dims dm;
+                {
+                    const uint32_t lp = slot / (uint32_t)p.spp, k = slot - lp * (uint32_t)p.spp;
+                    dm.s1d = s1d + (size_t)lp * p.n1d * p.spp + k;
+                    dm.s2d = s2d + (size_t)lp * p.n2d * p.spp + k;
+                    dm.spp = p.spp;
+                }
+                dm.n1d = p.n1d;
+                dm.n2d = p.n2d;
+                dm.i1d = (int)((info >> 8) & 0xffu);
+                dm.i2d = (int)((info >> 16) & 0xffu);
+                const uint4 rs = ps.rng[slot];
+                dm.rng.state = (uint64_t)rs.x | ((uint64_t)rs.y << 32);
+                dm.rng.inc = (uint64_t)rs.z | ((uint64_t)rs.w << 32);
+                dm.rng_used = false;
+                const float u_scatter = next1d(dm);
+                const float u_light_index = next1d(dm);
+                const float u_scatter_next = next1d(dm);
+                const float2 ul = next2d(dm);
+                const float2 ub = next2d(dm);
+                const float2 un = next2d(dm);
+
+                const Material_Dev& mat = S.materials[oinfo.y];
+                Bsdf f;
+                make_bsdf(sc, mat, f);
+                // estimate_direct_lighting_from_single_sample (direct_lighting.cpp:522-578):
+                // a rectangular light chosen by int(u * total_light_count)
+                // (the reference asserts light_index < total; the clamp only guards memory)
+                const int light_index = min((int)(u_light_index * (float)p.total_lights), p.rect_lights - 1);
+                const Rect_Light_Dev& Ld = S.lights[light_index];
+                const float4 lr0 = __ldg(&Ld.r0), lr1 = __ldg(&Ld.r1), lr2 = __ldg(&Ld.r2);
+                const float4 lle = __ldg(&Ld.le), lsz = __ldg(&Ld.sz);
+                const V3 light_n = v3(lr0.z, lr1.z, lr2.z);
+                const Col Le = col(lle.x, lle.y, lle.z);
+                const float size_x = lle.w, size_y = lsz.x;
+                uint32_t pend = kPendDirect;
+                {   // light-sampling half of MIS
+                    const V3 local = v3(size_x * (ul.x - 0.5f), size_y * (ul.y - 0.5f), 0.0f);
+                    const V3 lp = xform_point(lr0, lr1, lr2, local);
+                    const V3 position = origin_for_point(sc, lp);
+                    const V3 lv = lp - position;
+                    const float dist = len(lv);
+                    const V3 wi = divs(lv, dist);
+                    const float lndw = dot(light_n, -wi);
+                    if (lndw > 1e-4f) {
+                        const float ndw = dot(sc.n, wi);
+                        const bool possible = (ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission);
+                        if (possible) {
+                            const Col fv = bsdf_evaluate(f, sc.wo, wi);
+                            if (!black(fv)) {
+                                const float light_pdf = (dist * dist) / (size_x * size_y * lndw);
+                                const float bpdf = bsdf_pdf(f, sc.wo, wi);
+                                const float w = mis_power(light_pdf, bpdf);
+                                const Col c = mul(Le * fv, w * fabsf(ndw) / light_pdf);
+                                ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
+                                want_shadow = true;
+                                sh_a = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
+                                sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                pend |= kPendShadow;
+                            }
+                        }
+                    }
+                }
+                {   // BSDF-sampling half of MIS: the probe ray must hit this light
+                    V3 wi;
+                    float bpdf = 0.f;
+                    const Col fv = bsdf_sample(f, ub.x, ub.y, u_scatter, sc.wo, wi, bpdf);
+                    if (!black(fv)) {
+                        const float lndw = dot(light_n, -wi);
+                        if (lndw > 1e-4f) {
+                            const V3 position = origin_for_direction(sc, wi);
+                            const Col lef = Le * fv;
+                            ps.pend_probe0[slot] = make_float4(lef.r, lef.g, lef.b, bpdf);
+                            ps.pend_probe1[slot] = make_float4(position.x, position.y, position.z, lndw);
+                            ps.pend_probe2[slot] = make_float4(dot(sc.n, wi), __int_as_float(light_index), 0.f, 0.f);
+                            want_probe = true;
+                            pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
+                            pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                            pend |= kPendProbe;
+                        }
+                    }
+                }
+                ps.pend_coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0.f);
+
+                bounce++;
+                bool cont = bounce != p.max_bounces;
+                float rec_value = 0.f;
+                V3 rec_dir = v3(0.f, 0.f, 0.f);
+                if (cont) {
+                    V3 wi;
+                    float pdf = 0.f;
+                    Col fv;
+                    if (GUIDED && g.lobes) {
+                        const float* lob = g.lobes + (size_t)i * kGuideLobeFloats;
+                        const float u_sel = pcg_float(dm.rng);
+                        dm.rng_used = true;
+                        float pdf_b = 0.f;
+                        if (u_sel < g.alpha) {
+                            const float u0 = pcg_float(dm.rng), u1 = pcg_float(dm.rng), u2 = pcg_float(dm.rng);
+                            wi = mixture_sample(lob, u0, u1, u2);
+                            const float ndw = dot(sc.n, wi);
+                            const bool possible = (ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission);
+                            fv = possible ? bsdf_evaluate(f, sc.wo, wi) : col(0.f, 0.f, 0.f);
+                            pdf_b = possible ? bsdf_pdf(f, sc.wo, wi) : 0.f;
+                        } else {
+                            fv = bsdf_sample(f, un.x, un.y, u_scatter_next, sc.wo, wi, pdf_b);
+                        }
+                        pdf = g.alpha * mixture_pdf(lob, wi) + (1.f - g.alpha) * pdf_b;
+                        if (!(pdf > 0.f)) fv = col(0.f, 0.f, 0.f);
+                    } else {
+                        fv = bsdf_sample(f, un.x, un.y, u_scatter_next, sc.wo, wi, pdf);
+                    }
+                    if (black(fv)) {
+                        cont = false;
+                    } else {
+                        if (GUIDED) {
+                            rec_value = (0.2126729f * fv.r + 0.7151522f * fv.g + 0.0721750f * fv.b) *
+                                        fabsf(dot(sc.n, wi)) / pdf;
+                            rec_dir = wi;
+                        }
+                        coeff = coeff * mul(fv, fabsf(dot(sc.n, wi)) / (pdf * 1.f));
+                        const V3 o = origin_for_direction(sc, wi);
+                        nx_a = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
+                        nx_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                        if (bounce >= p.rr_bounce_threshold) {  // Russian roulette
+                            const float u_term = next1d(dm);
+                            const float max_coeff = max_std(coeff.r, max_std(coeff.g, coeff.b));
+                            if (max_coeff < p.rr_threshold) {
+                                const float p_term = max_std(0.05f, 1.f - max_coeff);
+                                if (u_term < p_term) {
+                                    cont = false;
+                                } else {
+                                    coeff = mul(coeff, 1.f / (1.f - p_term));
+                                }
+                            }
+                        }
+                    }
+                }
+                want_next = cont;
+                if (GUIDED && g.records) {
+                    uint32_t r = 0xffffffffu;
+                    if (cont) {
+                        r = atomicAdd(g.record_count, 1u);
+                        if (r < g.record_capacity) {
+                            float4* rec = g.records + (size_t)r * kGuideRecordF4;
+                            const float4* qr = g.queries + 3 * (size_t)i;
+                            rec[0] = qr[0];
+                            rec[1] = qr[1];
+                            rec[2] = make_float4(qr[2].x, rec_dir.x, rec_dir.y, rec_dir.z);
+                            rec[3] = make_float4(rec_value, __uint_as_float(slot), 0.f, 0.f);
+                            rec[4] = make_float4(coeff.r, coeff.g, coeff.b, 0.f);
+                        } else {
+                            r = 0xffffffffu;
+                        }
+                    }
+                    ps.rec[slot] = r;
+                }
+                info = (uint32_t)bounce | ((uint32_t)dm.i1d << 8) | ((uint32_t)dm.i2d << 16) | pend;
+                if (dm.rng_used)
+                    ps.rng[slot] = make_uint4((uint32_t)dm.rng.state, (uint32_t)(dm.rng.state >> 32),
+                                              (uint32_t)dm.rng.inc, (uint32_t)(dm.rng.inc >> 32));
+            }
+            ps.coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0.f);
+            ps.L[slot] = make_float4(L.r, L.g, L.b, 0.f);
+            ps.info[slot] = info;
+        }
+        const uint32_t is = warp_append(&q.counters[1], want_shadow);
+        if (want_shadow) {
+            q.shd_rays[2 * (size_t)is] = sh_a;
+            q.shd_rays[2 * (size_t)is + 1] = sh_b;
+            q.shd_slot[is] = slot;
+        }
+        const uint32_t ip = warp_append(&q.counters[2], want_probe);
+        if (want_probe) {
+            q.prb_rays[2 * (size_t)ip] = pr_a;
+            q.prb_rays[2 * (size_t)ip + 1] = pr_b;
+            q.prb_slot[ip] = slot;
+        }
+        const uint32_t in = warp_append(&q.counters[0], want_next);
+        if (want_next) {
+            q.ext_rays[cur ^ 1][2 * (size_t)in] = nx_a;
+            q.ext_rays[cur ^ 1][2 * (size_t)in + 1] = nx_b;
+            q.ext_slot[cur ^ 1][in] = slot;
+        }
+    }
+}
+
+// ---------------------------------------------------------------- connect
+__global__ void __launch_bounds__(kBlock)
+connect_kernel(Render_Params p, Scene_Dev S, const uint32_t* __restrict__ slots, uint32_t count, Path_State ps,
+               float4* __restrict__ records) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t slot = slots[i];
+        const uint32_t info = ps.info[slot];
+        if (!(info & kPendDirect)) continue;
+        Col direct = col(0.f, 0.f, 0.f);
+        if ((info & kPendShadow) && !ps.occluded[slot]) {
+            const float4 c = ps.pend_light[slot];
+            direct = direct + col(c.x, c.y, c.z);
+        }
+        if (info & kPendProbe) {
+            const uint2 h2 = ps.probe_hit2[slot];
+            const float4 p2 = ps.pend_probe2[slot];
+            const int light_index = __float_as_int(p2.y);
+            if (h2.y != 0xffffffffu) {
+                const float4 inf4 = __ldg(S.obj_render + 7 * (size_t)h2.y + 6);
+                if ((uint32_t)__float_as_int(inf4.z) == YAR_LIGHT_DIFFUSE_RECTANGULAR &&
+                    __float_as_int(inf4.w) == light_index) {
+                    const float4 h4 = ps.probe_hit4[slot];
+                    const uint32_t tri_offset = __float_as_uint(__ldg(S.ds.objects + 6 * (size_t)h2.y + 4).w);
+                    const size_t g = (size_t)tri_offset + h2.x;
+                    const float4 q0 = __ldg(S.ds.tris + 3 * g), q1 = __ldg(S.ds.tris + 3 * g + 1),
+                                 q2 = __ldg(S.ds.tris + 3 * g + 2);
+                    // Triangle_Mesh::get_position: object-space barycentric interpolation
+                    const V3 hp = bary(v3(q0.x, q0.y, q0.z), v3(q1.x, q1.y, q1.z), v3(q2.x, q2.y, q2.z), h4.y, h4.z, h4.w);
+                    const float4 p0 = ps.pend_probe0[slot], p1 = ps.pend_probe1[slot];
+                    const float d = len(hp - v3(p1.x, p1.y, p1.z));
+                    const Rect_Light_Dev& Ld = S.lights[light_index];
+                    const float size_x = __ldg(&Ld.le).w, size_y = __ldg(&Ld.sz).x;
+                    const float light_pdf = (d * d) / (size_x * size_y * p1.w);
+                    const float w = mis_power(p0.w, light_pdf);
+                    const Col c = mul(col(p0.x, p0.y, p0.z), w * fabsf(p2.x) / p0.w);
+                    direct = direct + c;
+                }
+            }
+        }
+        const float4 cv = ps.pend_coeff[slot];
+        const Col scaled = mul(direct, (float)p.total_lights);
+        const float4 L4 = ps.L[slot];
+        const Col L = col(L4.x, L4.y, L4.z) + col(cv.x, cv.y, cv.z) * scaled;
+        ps.L[slot] = make_float4(L.r, L.g, L.b, 0.f);
+        ps.info[slot] = info & 0x00ffffffu;
+        if (records) {
+            const uint32_t r = ps.rec[slot];
+            if (r != 0xffffffffu) records[(size_t)r * kGuideRecordF4 + 5] = make_float4(L.r, L.g, L.b, 0.f);
+        }
+    }
+}
+
+__global__ void __launch_bounds__(kBlock)
+finish_chunk_kernel(uint32_t paths, uint64_t first_sample, const Path_State ps, float4* __restrict__ radiance) {
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < paths; i += gridDim.x * blockDim.x)
+        radiance[first_sample + i] = ps.L[i];
+}
+
+// ---------------------------------------------------------------- film
+// Per sample-region pixel: clamp/scale of each sample (reference_renderer.cpp:388-393)
+// and the luminance variance of the pixel (:397-409).
+__global__ void __launch_bounds__(kBlock)
+samples_kernel(Render_Params p, float4* __restrict__ radiance, double* __restrict__ pixel_variance) {
+    const uint32_t pix = blockIdx.x * blockDim.x + threadIdx.x;
+    if (pix >= (uint32_t)(p.sw * p.sh)) return;
+    double lsum = 0.0, lsq = 0.0;
+    for (int k = 0; k < p.spp; k++) {
+        float4 r = radiance[(size_t)pix * p.spp + k];
+        const float mc = max_std(r.x, max_std(r.y, r.z));
+        if (mc > p.max_component) {
+            const float s = p.max_component / mc;
+            r.x *= s; r.y *= s; r.z *= s;
+        }
+        if (p.film_scale != 1.f) {
+            r.x *= p.film_scale; r.y *= p.film_scale; r.z *= p.film_scale;
+        }
+        radiance[(size_t)pix * p.spp + k] = r;
+        const float lum = 0.2126729f * r.x + 0.7151522f * r.y + 0.0721750f * r.z;
+        lsum += lum;
+        lsq += lum * lum;
+    }
+    double v = 0.0;
+    if (p.spp > 1) {
+        const int n = p.spp;
+        v = (lsq - lsum * lsum / n) / (n * (n - 1));
+        v = v > 0.0 ? v : 0.0;
+    }
+    pixel_variance[pix] = v;
+}
+
+__device__ __forceinline__ void tile_sample_bounds(const Render_Params& p, int t, int& x0, int& y0, int& x1, int& y1) {
+    const int tx = t % p.tiles_x, ty = t / p.tiles_x;
+    x0 = p.sx0 + tx * kTile;
+    y0 = p.sy0 + ty * kTile;
+    x1 = min(x0 + kTile, p.sx0 + p.sw);
+    y1 = min(y0 + kTile, p.sy0 + p.sh);
+}
+
+__device__ __forceinline__ void tile_pixel_bounds(const Render_Params& p, int t, int& x0, int& y0, int& x1, int& y1) {
+    int sx0, sy0, sx1, sy1;
+    tile_sample_bounds(p, t, sx0, sy0, sx1, sy1);
+    const float r = p.filter_radius;
+    x0 = max((int)ceilf((float)sx0 - r - 0.5f), p.rx0);
+    y0 = max((int)ceilf((float)sy0 - r - 0.5f), p.ry0);
+    x1 = min((int)floorf((float)sx1 + r - 0.5f) + 1, p.rx0 + p.rw);
+    y1 = min((int)floorf((float)sy1 + r - 0.5f) + 1, p.ry0 + p.rh);
+}
+
+// Tile variance accumulators in the reference's pixel order (render_tile loops).
+// One block per tile: the block stages the tile's pixel variances in shared
+// memory with coalesced loads, then one thread adds them in the reference's
+// sequential (y, x) order (double addition is not associative).
+constexpr int kTileVarThreads = 256;
+__global__ void __launch_bounds__(kTileVarThreads)
+tile_variance_kernel(Render_Params p, const double* __restrict__ pixel_variance, double* __restrict__ tile_variance) {
+    __shared__ double v[kTile * kTile];
+    const int t = blockIdx.x;
+    int x0, y0, x1, y1;
+    tile_sample_bounds(p, t, x0, y0, x1, y1);
+    const int w = x1 - x0, h = y1 - y0;
+    for (int i = threadIdx.x; i < w * h; i += blockDim.x) {
+        const int y = i / w, x = i - y * w;
+        v[i] = pixel_variance[(size_t)(y0 + y - p.sy0) * p.sw + (x0 + x - p.sx0)];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        double acc = 0.0;
+        for (int i = 0; i < w * h; i++) acc += v[i];
+        tile_variance[t] = acc;
+    }
+}
+
+// Sample tables and camera rays of a chunk.  The table kernel's block is
+// sized so that its spp float2 per thread fit in 96 KB of shared memory.
+cudaError_t launch_generate(const Render_Params& p, uint32_t first, uint32_t cp, float* s1d, float* s2d,
+                            float2* image_samples, const Path_State& ps, const Queues& q, cudaStream_t st) {
+    constexpr size_t kSmemLimit = 96 * 1024;
+    static bool attr_set = false;
+    if (!attr_set) {
+        cudaError_t e = cudaFuncSetAttribute(sample_tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                             (int)kSmemLimit);
+        if (e != cudaSuccess) return e;
+        attr_set = true;
+    }
+    const size_t per_thread = (size_t)p.spp * sizeof(float2);
+    int threads = 128;
+    while (threads > 1 && (size_t)threads * per_thread > kSmemLimit) threads /= 2;
+    if ((size_t)threads * per_thread > kSmemLimit) return cudaErrorInvalidValue;
+    const uint64_t rows = (uint64_t)cp * (1u + (uint32_t)p.n1d + (uint32_t)p.n2d);
+    sample_tables_kernel<<<(uint32_t)((rows + threads - 1) / threads), threads, threads * per_thread, st>>>(
+        p, first, cp, s1d, s2d, image_samples);
+    const uint32_t paths = cp * (uint32_t)p.spp;
+    camera_kernel<<<(paths + kBlock - 1) / kBlock, kBlock, 0, st>>>(p, first, paths, image_samples, ps, q);
+    return cudaGetLastError();
+}
+
+// One film pixel: the tiles whose samples reach it are merged in tile order
+// (Film::merge_tile), each tile's sum accumulated in its own sample order
+// (Film_Tile::add_sample with the box filter), then resolved (Film::get_image).
+__global__ void __launch_bounds__(kBlock)
+film_kernel(Render_Params p, const float4* __restrict__ radiance, const float2* __restrict__ image_samples,
+            float* __restrict__ rgb) {
+    const uint32_t idx = blockIdx.x * blockDim.x + threadIdx.x;
+    if (idx >= (uint32_t)(p.rw * p.rh)) return;
+    const int px = p.rx0 + (int)(idx % (uint32_t)p.rw);
+    const int py = p.ry0 + (int)(idx / (uint32_t)p.rw);
+    const float r = p.filter_radius;
+    const int R = (int)ceilf(r) + 1;
+    // candidate sample pixels: [px - R, px + R] x [py - R, py + R] inside the sample region
+    const int qx0 = max(px - R, p.sx0), qx1 = min(px + R, p.sx0 + p.sw - 1);
+    const int qy0 = max(py - R, p.sy0), qy1 = min(py + R, p.sy0 + p.sh - 1);
+    const int tx0 = (qx0 - p.sx0) / kTile, tx1 = (qx1 - p.sx0) / kTile;
+    const int ty0 = (qy0 - p.sy0) / kTile, ty1 = (qy1 - p.sy0) / kTile;
+    float fr = 0.f, fg = 0.f, fb = 0.f, fw = 0.f;
+    for (int ty = ty0; ty <= ty1; ty++)
+        for (int tx = tx0; tx <= tx1; tx++) {
+            const int t = ty * p.tiles_x + tx;
+            int bx0, by0, bx1, by1;
+            tile_pixel_bounds(p, t, bx0, by0, bx1, by1);
+            if (px < bx0 || px >= bx1 || py < by0 || py >= by1) continue;
+            int sx0, sy0, sx1, sy1;
+            tile_sample_bounds(p, t, sx0, sy0, sx1, sy1);
+            float tr = 0.f, tg = 0.f, tb = 0.f, tw = 0.f;
+            for (int qy = max(qy0, sy0); qy <= min(qy1, sy1 - 1); qy++)
+                for (int qx = max(qx0, sx0); qx <= min(qx1, sx1 - 1); qx++) {
+                    const size_t pix = (size_t)(qy - p.sy0) * p.sw + (qx - p.sx0);
+                    for (int k = 0; k < p.spp; k++) {
+                        const float2 s = image_samples[pix * p.spp + k];
+                        const float fx = (float)qx + s.x, fy = (float)qy + s.y;
+                        int rx0 = (int)ceilf(fx - r - 0.5f), ry0 = (int)ceilf(fy - r - 0.5f);
+                        int rx1 = (int)floorf(fx + r - 0.5f) + 1, ry1 = (int)floorf(fy + r - 0.5f) + 1;
+                        rx0 = max(rx0, bx0); ry0 = max(ry0, by0);
+                        rx1 = min(rx1, bx1); ry1 = min(ry1, by1);
+                        if (px < rx0 || px >= rx1 || py < ry0 || py >= ry1) continue;
+                        const float4 c = radiance[pix * p.spp + k];
+                        tr += 1.f * c.x;
+                        tg += 1.f * c.y;
+                        tb += 1.f * c.z;
+                        tw += 1.f;
+                    }
+                }
+            fr += tr;
+            fg += tg;
+            fb += tb;
+            fw += tw;
+        }
+    float cr = 0.f, cg = 0.f, cb = 0.f;
+    if (fw != 0.f) {
+        const float inv = 1.f / fw;
+        cr = fr * inv;
+        cg = fg * inv;
+        cb = fb * inv;
+    }
+    rgb[3 * (size_t)idx + 0] = max_std(0.f, cr);
+    rgb[3 * (size_t)idx + 1] = max_std(0.f, cg);
+    rgb[3 * (size_t)idx + 2] = max_std(0.f, cb);
+}
+
+// ---------------------------------------------------------------- host helpers
+float pbrt3_roughness_to_alpha(float roughness) {
+    // src/ref/scattering.cpp:240-251 (host libm logf, as the reference evaluates it)
+    roughness = std::max(roughness, 1e-3f);
+    float x = std::log(roughness);
+    return 1.621420000f + 0.819955000f * x + 0.173400000f * x * x + 0.017120100f * x * x * x +
+           0.000640711f * x * x * x * x;
+}
+
+float roughness_to_alpha(const yar_render_config& c, float r, int no_remap) {
+    if (no_remap) return r;
+    if (c.pbrt3_scene) return pbrt3_roughness_to_alpha(r);
+    return r * r;
+}
+
+template <class T>
+T* dptr(Device_Buffer& b) {
+    return reinterpret_cast<T*>(b.ptr);
+}
+
+int grid_for(uint64_t n) {
+    uint64_t blocks = (n + kBlock - 1) / kBlock;
+    return (int)std::max<uint64_t>(1, std::min<uint64_t>(blocks, 152ull * 64));
+}
+
+// Checks the uploaded scene and configuration against what the path tracer
+// implements and derives the launch parameters: Film::Film's sample region
+// (src/ref/film.cpp:53-86) and the sampler's dimension budget
+// (src/ref/reference_renderer.cpp:87-99).
+int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
+    const Render_Scene& R = ctx->render;
+    const yar_render_config& c = R.config;
+    if (c.rendering_algorithm != 1) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the path tracer is implemented");
+    if (c.pixel_filter_type != 0) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the box filter is implemented");
+    if (R.other_light_count) return fail(ctx, YAR_ERR_UNSUPPORTED, "only rectangular area lights are implemented");
+    if (R.host_rect_lights.empty()) return fail(ctx, YAR_ERR_UNSUPPORTED, "scene has no light");
+    for (const yar_material_desc& m : R.host_materials) {
+        if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL && m.type != YAR_MATERIAL_GLASS)
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "material type " + std::to_string(m.type) + " is not implemented");
+        if (m.type == YAR_MATERIAL_GLASS && !(m.u_roughness > 0.f))
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "smooth (delta) glass is not implemented");
+    }
+    const size_t n_obj = R.host_object_info.size() / 4;
+    for (size_t i = 0; i < n_obj; i++) {
+        const int32_t* o = &R.host_object_info[4 * i];
+        const bool light = (uint32_t)o[2] != YAR_LIGHT_NULL;
+        if (light && ((uint32_t)o[2] != YAR_LIGHT_DIFFUSE_RECTANGULAR || o[3] < 0 ||
+                      (size_t)o[3] >= R.host_rect_lights.size()))
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "object " + std::to_string(i) + ": unsupported area light");
+        if (!light && (o[1] < 0 || (size_t)o[1] >= R.host_materials.size()))
+            return fail(ctx, YAR_ERR_INVALID, "object " + std::to_string(i) + " has no valid material");
+    }
+    const int nx = c.x_pixel_sample_count, ny = c.y_pixel_sample_count;
+    if (nx <= 0 || ny <= 0 || (int64_t)nx * ny > 4096)
+        return fail(ctx, YAR_ERR_INVALID, "pixel sample counts must be in 1..4096 samples per pixel");
+    if (c.max_light_bounces < 0 || c.max_light_bounces > 200) return fail(ctx, YAR_ERR_INVALID, "max_light_bounces");
+
+    p = Render_Params{};
+    p.camera = R.camera;
+    p.rx0 = c.render_region[0];
+    p.ry0 = c.render_region[1];
+    p.rw = c.render_region[2] - c.render_region[0];
+    p.rh = c.render_region[3] - c.render_region[1];
+    if (p.rw <= 0 || p.rh <= 0 || c.render_region[2] > 0xffff + 1 || c.render_region[3] > 0xffff + 1)
+        return fail(ctx, YAR_ERR_INVALID, "render region");
+    const float radius = c.pixel_filter_radius;
+    // Film::Film sample region (src/ref/film.cpp:53-86)
+    p.sx0 = (int)std::floor((float)p.rx0 + 0.5f - radius);
+    p.sy0 = (int)std::floor((float)p.ry0 + 0.5f - radius);
+    const int sx1 = (int)std::ceil((float)(p.rx0 + p.rw - 1) + 0.5f + radius);
+    const int sy1 = (int)std::ceil((float)(p.ry0 + p.rh - 1) + 0.5f + radius);
+    p.sw = sx1 - p.sx0;
+    p.sh = sy1 - p.sy0;
+    p.tiles_x = (p.sw + kTile - 1) / kTile;
+    p.tiles_y = (p.sh + kTile - 1) / kTile;
+    p.nx = nx;
+    p.ny = ny;
+    p.spp = nx * ny;
+    const int maxb = std::min(10, c.max_light_bounces);
+    p.n1d = maxb * 4;  // src/ref/reference_renderer.cpp:87-99
+    p.n2d = maxb * 3;
+    p.max_bounces = c.max_light_bounces;
+    p.rr_bounce_threshold = c.russian_roulette_bounce_count_threshold;
+    p.rr_threshold = c.russian_roulette_threshold;
+    p.filter_radius = radius;
+    p.film_scale = c.film_radiance_scale;
+    p.max_component = c.max_rgb_component_value_of_film_sample;
+    p.rect_lights = (int)R.host_rect_lights.size();
+    p.total_lights = p.rect_lights + (int)R.other_light_count;
+    p.seed_offset = (uint32_t)c.rng_seed_offset;
+    return YAR_OK;
+}
+
+} // namespace
+
+} // namespace yar

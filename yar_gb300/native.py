@@ -95,6 +95,17 @@ class HitSoa(C.Structure):
     _fields_ = [("t", C.c_void_p), ("prim", C.c_void_p), ("object", C.c_void_p), ("bary", C.c_void_p)]
 
 
+class GuidedParams(C.Structure):
+    _fields_ = [("passes", C.c_uint32), ("train_passes", C.c_uint32), ("guide_fraction", C.c_float),
+                ("learning_rate", C.c_float), ("train_steps", C.c_uint32), ("stream_offset", C.c_uint32),
+                ("time_budget", C.c_float), ("keep_guide", C.c_uint32)]
+
+
+class GuidedStats(C.Structure):
+    _fields_ = [("passes", C.c_uint32), ("seconds", C.c_float), ("train_seconds", C.c_float),
+                ("rays", C.c_uint64), ("train_samples", C.c_uint64), ("loss", C.c_float)]
+
+
 class GpuOptions(C.Structure):
     _fields_ = [("device", C.c_int32), ("max_batch_rays", C.c_uint32), ("traversal_kernel", C.c_int32)]
 
@@ -125,6 +136,8 @@ EXPORTS = {
     "yar_gpu_cast_any_timed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_float)]),
     "yar_gpu_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
     "yar_gpu_render_static": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
+    "yar_gpu_guided_render": (C.c_int, [C.c_void_p, C.POINTER(GuidedParams), C.c_void_p, C.c_void_p,
+                                        C.POINTER(GuidedStats)]),
     "yar_guide_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
     "yar_guide_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
     "yar_guide_infer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.c_void_p]),
@@ -293,6 +306,19 @@ class Context:
         stats = RenderStats()
         self._check(lib().yar_gpu_render(self._h, _ptr(rgb), C.byref(stats)), "render")
         return rgb, stats
+
+    def guided_render(self, width, height, passes, guide_fraction=0.0, train_passes=0, learning_rate=2e-3,
+                      train_steps=8, stream_offset=0, time_budget=0.0, keep_guide=False):
+        """yar_gpu_guided_render: returns (mean image, per-pixel FP64 radiance
+        sums, GuidedStats)."""
+        prm = GuidedParams(int(passes), int(train_passes), float(guide_fraction), float(learning_rate),
+                           int(train_steps), int(stream_offset), float(time_budget), int(bool(keep_guide)))
+        sums = np.zeros((height, width, 3), np.float64)
+        rgb = np.zeros((height, width, 3), np.float32)
+        st = GuidedStats()
+        self._check(lib().yar_gpu_guided_render(self._h, C.byref(prm), _ptr(sums), _ptr(rgb), C.byref(st)),
+                    "guided_render")
+        return rgb, sums, st
 
     # ---- learned proposal network (device buffers are raw pointers)
     def guide_set_params(self, params):

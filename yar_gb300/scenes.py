@@ -340,3 +340,95 @@ def large_scene(seed=1, width=1920, height=1080, spp=64, maxdepth=16, meshes=200
     if build:
         s.build_kdtrees(threads)
     return s
+
+
+# ---------------------------------------------------------------- hard-lighting room (learned proposal)
+def _grid(origin, du, dv, n, hole=None):
+    """n x n quads spanning origin + [0,1] du + [0,1] dv (two triangles each);
+    `hole` = (i0, i1, j0, j1) cell range left open."""
+    o, du, dv = (np.asarray(a, np.float64) for a in (origin, du, dv))
+    ii, jj = np.meshgrid(np.arange(n + 1), np.arange(n + 1), indexing="ij")
+    v = (o + ii[..., None] / n * du + jj[..., None] / n * dv).reshape(-1, 3).astype(np.float32)
+    ci, cj = np.meshgrid(np.arange(n), np.arange(n), indexing="ij")
+    ci, cj = ci.ravel(), cj.ravel()
+    if hole is not None:
+        i0, i1, j0, j1 = hole
+        keep = ~((ci >= i0) & (ci < i1) & (cj >= j0) & (cj < j1))
+        ci, cj = ci[keep], cj[keep]
+    a = ci * (n + 1) + cj
+    b, c, d = a + (n + 1), a + (n + 1) + 1, a + 1
+    idx = np.concatenate([np.stack([a, b, c], 1), np.stack([a, c, d], 1)]).astype(np.int32)
+    return v, idx
+
+
+def hard_lighting_room(seed=1, width=512, height=512, maxdepth=12, cells=200, light_size=0.1, build=True, threads=0):
+    """The learned-proposal workload: a closed 2 x 2 x 2 room whose six walls
+    are tessellated into `cells` x `cells` quads (200: 479,800 triangles, the
+    opening cut out) of
+    GGX metal (roughness U[0.1, 0.3] per wall, pbrt-v3 remapping), two
+    Lambertian boxes inside, and one light_size x light_size area light of
+    radiance 1000 0.3 above the ceiling, which reaches the room only through
+    a 0.1 x 0.1 opening in the ceiling's centre: the opening collimates it
+    into a small pool on the floor, and the rest of the room is lit by what
+    that pool and the glossy walls reflect.  512 x 512, maxdepth 12, Russian
+    roulette from bounce 3."""
+    from . import native as N
+    from .scene import LIGHT_DTYPE, MATERIAL_DTYPE, CAMERA_DTYPE, default_config
+    rng = np.random.default_rng(seed)
+    s = FlatScene()
+    objects, materials = [], []
+    h = int(round(0.025 * cells))                    # opening half-width in cells (0.05 of the 2-unit wall)
+    mid = cells // 2
+    walls = [
+        ((-1, 0, -1), (2, 0, 0), (0, 0, 2), None),                          # floor
+        ((-1, 2, -1), (2, 0, 0), (0, 0, 2), (mid - h, mid + h, mid - h, mid + h)),  # ceiling with the opening
+        ((-1, 0, -1), (2, 0, 0), (0, 2, 0), None),                          # back
+        ((-1, 0, 1), (2, 0, 0), (0, 2, 0), None),                           # front (behind the camera)
+        ((-1, 0, -1), (0, 0, 2), (0, 2, 0), None),                          # left
+        ((1, 0, -1), (0, 0, 2), (0, 2, 0), None),                           # right
+    ]
+    for origin, du, dv, hole in walls:
+        v, i = _grid(origin, du, dv, cells, hole)
+        s.meshes.append(Mesh(v, i))
+        m = np.zeros((), MATERIAL_DTYPE)
+        eta, k = METALS[2] if rng.random() < 0.5 else METALS[int(rng.integers(0, 2))]
+        m["type"] = N.MATERIAL_METAL
+        m["eta"], m["k"], m["eta_i"] = eta, k, 1.0
+        m["u_roughness"] = m["v_roughness"] = rng.uniform(0.1, 0.3)
+        materials.append(m)
+        objects.append(make_object(len(s.meshes) - 1, material_type=N.MATERIAL_METAL,
+                                   material_index=len(materials) - 1))
+    for center, size in (((0.4, 0, 0.2), (0.5, 0.5, 0.5)), ((-0.4, 0, -0.4), (0.5, 1.0, 0.5))):
+        v, i = _box(center, size, rng.uniform(0.0, 30.0))
+        s.meshes.append(Mesh(v, i))
+        m = np.zeros((), MATERIAL_DTYPE)
+        m["type"] = N.MATERIAL_DIFFUSE
+        m["reflectance"] = rng.uniform(0.4, 0.8, 3)
+        materials.append(m)
+        objects.append(make_object(len(s.meshes) - 1, material_type=N.MATERIAL_DIFFUSE,
+                                   material_index=len(materials) - 1))
+    lh, ly = 0.5 * light_size, 2.3
+    v, i = _quad((-lh, ly, -lh), (lh, ly, -lh), (lh, ly, lh), (-lh, ly, lh))
+    s.meshes.append(Mesh(v, i, uvs=_pbrt_quad_uvs()))
+    L = np.zeros((), LIGHT_DTYPE)
+    L["light_to_world"] = (1, 0, 0, 0, 0, 0, -1, ly, 0, 1, 0, 0)   # normal -y: facing the opening
+    L["emitted_radiance"] = (1000.0, 1000.0, 1000.0)
+    L["size"] = (2 * lh, 2 * lh)
+    L["sample_count"] = 1
+    objects.append(make_object(len(s.meshes) - 1, material_type=N.MATERIAL_NULL, material_index=-1,
+                               light_type=N.LIGHT_RECT, light_index=0))
+    s.objects = np.array(objects)
+    s.materials = np.array(materials, MATERIAL_DTYPE)
+    s.rect_lights = np.array([L], LIGHT_DTYPE)
+    cam = np.zeros((), CAMERA_DTYPE)
+    cam["camera_to_world"] = (1, 0, 0, 0, 0, 1, 0, 1.0, 0, 0, 1, 0.95)
+    cam["image_extent"] = (width, height)
+    vert = np.float32(math.tan(math.radians(35.0)))
+    cam["vert_half_dist"] = vert
+    cam["horz_half_dist"] = np.float32(np.float32(width) / np.float32(height)) * vert
+    cam["z_is_up"] = 0
+    s.camera = cam
+    s.config = default_config(width, height, 1, 1, maxdepth)
+    if build:
+        s.build_kdtrees(threads)
+    return s
