@@ -48,7 +48,8 @@ def parse():
     p.add_argument("--grid", type=int, default=GRID)
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-render", action="store_true", help="skip the C1 render figures")
-    p.add_argument("--workload", default="raycast", choices=["raycast", "render-c1", "render-c3"],
+    p.add_argument("--workload", default="raycast",
+                   choices=["raycast", "render-c1", "render-c3", "guided", "batch"],
                    help="render-c1 / render-c3 print a separate line for the C1 or the large (C3) render")
     return p.parse_args()
 
@@ -376,6 +377,9 @@ def run_gb300(args, rank, world, local, pg):
     ctx.close()
     if not args.no_render:
         line["render_c1"] = render_bench("c1", with_cpu=not args.no_cpu_baseline)
+        g = guided_bench()
+        if g is not None:
+            line["guided_c5"] = g
     print(json.dumps(line), flush=True)
 
 
@@ -430,11 +434,113 @@ def render_bench(kind, with_cpu=True, reps=3):
     return out
 
 
+GUIDE = dict(guide_fraction=0.7, train_passes=64, train_steps=32, learning_rate=5e-3)
+
+
+def guided_bench(plain_passes=1024):
+    """Equal-time RMSE of the guided render against the plain one on the
+    hard-lighting room, both against the committed FP64 plain-mode oracle
+    (tests/golden/room_oracle.npz, made by make_room_oracle.py).  The plain
+    render's time for `plain_passes` one-sample passes is the budget given to
+    the guided render (training included)."""
+    path = os.path.join(ROOT, "tests", "golden", "room_oracle.npz")
+    if not os.path.exists(path):
+        return None
+    from yar_gb300 import native, scenes
+    z = np.load(path)
+    oracle = z["image"].astype(np.float64)
+    s = scenes.hard_lighting_room()
+    w, h = int(s.config["render_region"][2]), int(s.config["render_region"][3])
+    ctx = native.Context(0)
+    ctx.upload_scene(s)
+    # warm-up: kernel loading and the per-scene traversal-kernel timing
+    ctx.guided_render(w, h, passes=4, stream_offset=4090)
+    ctx.guided_render(w, h, passes=4, train_passes=2, stream_offset=4091, **{k: v for k, v in GUIDE.items()
+                                                                           if k != "train_passes"})
+
+    def rmse(img):
+        return float(np.sqrt(((img.astype(np.float64) - oracle) ** 2).mean()))
+
+    img_p, _, st_p = ctx.guided_render(w, h, passes=plain_passes, stream_offset=1)
+    budget = st_p.seconds
+    img_g, _, st_g = ctx.guided_render(w, h, passes=1 << 24, stream_offset=2, time_budget=budget, **GUIDE)
+    ctx.close()
+    r_p, r_g = rmse(img_p), rmse(img_g)
+    return {
+        "workload": "hard-lighting room: %d triangles, 512x512, maxdepth 12, one 0.1x0.1 light of radiance 1000 "
+                    "behind a 0.1x0.1 ceiling opening, GGX metal walls (roughness 0.1-0.3)" % s.triangle_count,
+        "oracle": "plain mode, %d one-sample passes, FP64 accumulation" % int(z["passes"]),
+        "plain": {"passes": int(st_p.passes), "seconds": round(st_p.seconds, 3), "rmse": r_p,
+                  "mrays_per_s": round(st_p.rays / st_p.seconds / 1e6, 1)},
+        "guided": {"passes": int(st_g.passes), "seconds": round(st_g.seconds, 3), "rmse": r_g,
+                   "train_seconds": round(st_g.train_seconds, 3), "train_samples": int(st_g.train_samples),
+                   "mrays_per_s": round(st_g.rays / st_g.seconds / 1e6, 1), **GUIDE},
+        "rmse_ratio_equal_time": round(r_g / r_p, 4),
+        # RMSE falls as time^-1/2: time the guided render needs for the plain render's RMSE, relative
+        "time_ratio_equal_rmse": round((r_g / r_p) ** 2, 4),
+    }
+
+
+def batch_bench(count=64):
+    """The batched workload: `count` procedural scenes (scenes.batch_scenes)
+    in one yar_gpu_render_batch call; aggregate paths/s over the graph's GPU
+    makespan and per-scene completion percentiles."""
+    from yar_gb300 import native, scenes
+    t0 = time.time()
+    flats = scenes.batch_scenes(count=count)
+    gen = time.time() - t0
+    ctx = native.Context(0)
+    imgs, sst, st = ctx.render_batch(flats)
+    # the same scenes one after another through yar_gpu_render (host-driven
+    # bounces, one scene in flight), for the gain of batching
+    seq = 0.0
+    for f in flats:
+        ctx.upload_scene(f)
+        r = f.config["render_region"]
+        _, rs = ctx.render(int(r[2] - r[0]), int(r[3] - r[1]))
+        seq += rs.seconds
+    ctx.close()
+    comp = sorted(x.completion_seconds for x in sst)
+    pct = lambda q: comp[min(len(comp) - 1, int(round(q * (len(comp) - 1))))]
+    tris = sorted(f.triangle_count for f in flats)
+    return {
+        "workload": "%d scenes: triangles %d..%d (log-uniform 1K-200K), resolutions 128^2..1024^2, spp 4..256 "
+                    "(perfect squares), maxdepth 8, 50%% Lambertian / 50%% GGX, 4-16 quad lights"
+                    % (count, tris[0], tris[-1]),
+        "paths": int(st.paths),
+        "gpu_seconds": round(st.gpu_seconds, 4),
+        "paths_per_s": round(st.paths / st.gpu_seconds, 1),
+        "mrays_per_s": round((st.rays_closest + st.rays_any) / st.gpu_seconds / 1e6, 1),
+        "sequential_render_seconds": round(seq, 3),
+        "speedup_vs_sequential": round(seq / st.gpu_seconds, 2),
+        "completion_p50_s": round(pct(0.5), 4),
+        "completion_p99_s": round(pct(0.99), 4),
+        "autotuner": {"branches": int(st.branches), "chunk_paths": int(st.chunk_paths),
+                      "traversal_kernels": {k: sum(1 for x in sst if tuple(x.traversal_kernel) == v)
+                                            for k, v in (("p64/p64", (1, 1)), ("per_ray/per_ray", (3, 3)))}},
+        "host_seconds": {"generate_and_build": round(gen, 2), "upload": round(st.upload_seconds, 2),
+                         "tune": round(st.tune_seconds, 2), "capture": round(st.capture_seconds, 2)},
+        "image_mean": float(np.mean([i.mean() for i in imgs])),
+    }
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist_setup(args)
     try:
-        if args.workload in ("render-c1", "render-c3"):
+        if args.workload == "batch":
+            if rank == 0:
+                b = batch_bench()
+                print(json.dumps({"metric": "paths/s (batched render, one graph launch)", "impl": args.impl,
+                                  "value": b["paths_per_s"], "unit": "paths/s", "higher_is_better": True,
+                                  "batch": b}), flush=True)
+        elif args.workload == "guided":
+            if rank == 0:
+                g = guided_bench()
+                print(json.dumps({"metric": "equal-time RMSE vs FP64 oracle, guided / plain", "impl": args.impl,
+                                  "value": None if g is None else g["rmse_ratio_equal_time"],
+                                  "unit": "ratio", "higher_is_better": False, "guided": g}), flush=True)
+        elif args.workload in ("render-c1", "render-c3"):
             if rank == 0:
                 kind = args.workload[-2:]
                 r = render_bench(kind, with_cpu=not args.no_cpu_baseline, reps=2 if kind == "c3" else 3)

@@ -286,6 +286,36 @@ int yar_gpu_render(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats);
 #define YAR_GPU_STATIC_ARENA_BYTES (64u << 20)
 int yar_gpu_render_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats* stats);
 
+/* ---- batched render ----
+ * No reference counterpart.  Renders `count` scenes, each exactly as
+ * yar_gpu_render would (same per-pixel results), in one CUDA graph launch:
+ * each scene's chunks and bounces run device-driven (queue lengths stay on
+ * the device), the graph forks the scenes over concurrent streams, and an
+ * autotuner first picks each scene's traversal kernel (timed on random rays)
+ * and the stream count and paths in flight per stream (timed on the batch at
+ * one sample per pixel).  rgb_out[i]: host float[w_i * h_i * 3]. */
+typedef struct yar_batch_scene_stats {
+    double variance;              /* render_scene's variance_estimate */
+    float completion_seconds;     /* batch start to this scene's resolved film, GPU clock */
+    uint64_t paths;               /* camera paths */
+    uint32_t traversal_kernel[2]; /* YAR_TRAVERSAL_* used for closest-hit and any-hit rays */
+} yar_batch_scene_stats;
+
+typedef struct yar_batch_stats {
+    float gpu_seconds;            /* makespan of the batch graph, GPU clock */
+    uint64_t paths;               /* camera paths of all scenes */
+    uint64_t rays_closest;        /* camera, continuation and MIS probe rays */
+    uint64_t rays_any;            /* shadow rays */
+    uint32_t branches;            /* autotuner: concurrent streams */
+    uint32_t chunk_paths;         /* autotuner: paths in flight per stream */
+    float upload_seconds;         /* scene uploads (host) */
+    float tune_seconds;           /* autotuning (host wall time) */
+    float capture_seconds;        /* graph capture and instantiation (host wall time) */
+} yar_batch_stats;
+
+int yar_gpu_render_batch(yar_gpu_ctx* ctx, const yar_flat_scene* const* scenes, uint32_t count,
+                         float* const* rgb_out, yar_batch_scene_stats* scene_stats, yar_batch_stats* stats);
+
 /* ---- guided render (config: the uploaded scene's camera, region, depth, RR, film clamp) ----
  * No reference counterpart.  Renders `passes` independent one-sample-per-
  * pixel passes of the path tracer and returns the per-pixel FP64 sum of the

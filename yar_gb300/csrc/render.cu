@@ -268,22 +268,6 @@ __device__ __align__(256) unsigned char g_static_arena[YAR_GPU_STATIC_ARENA_BYTE
 std::mutex g_arena_mutex;
 unsigned char* g_arena_address[64] = {};  // device address of g_static_arena per device ordinal
 
-// Sum of the tile variance accumulators in tile order, divided by the
-// sample-region area (render_scene, src/ref/reference_renderer.cpp:570-581).
-__global__ void variance_total_kernel(Render_Params p, const double* __restrict__ tile_variance,
-                                      double* __restrict__ out) {
-    if (blockIdx.x != 0 || threadIdx.x != 0) return;
-    double acc = 0.0;
-    int64_t count = 0;
-    for (int t = 0; t < p.tiles_x * p.tiles_y; t++) {
-        acc += tile_variance[t];
-        int x0, y0, x1, y1;
-        tile_sample_bounds(p, t, x0, y0, x1, y1);
-        count += (int64_t)(x1 - x0) * (y1 - y0);
-    }
-    *out = p.spp > 1 ? acc / (double)count : 0.0;
-}
-
 struct Arena {
     unsigned char* base;
     size_t size, used;

@@ -142,7 +142,8 @@ struct Queues {
     uint32_t* shd_slot;
     float4* prb_rays;
     uint32_t* prb_slot;
-    uint32_t* counters;  // [0] next ext, [1] shadow, [2] probe, [3] error
+    uint32_t* counters;  // [0] next ext, [1] shadow, [2] probe, [3] error, [4..6] ray hand-out
+    const uint32_t* ext_count = nullptr;  // device count of the extend queue (graph-captured renders)
 };
 
 struct Scene_Dev {
@@ -486,6 +487,7 @@ template <bool GUIDED>
 __global__ void __launch_bounds__(kBlock)
 shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float* __restrict__ s1d,
              const float2* __restrict__ s2d, Path_State ps, Queues q, Guide_Shade g) {
+    if (q.ext_count) count = *q.ext_count;
     for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         bool want_shadow = false, want_probe = false, want_next = false;
@@ -707,7 +709,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
 // ---------------------------------------------------------------- connect
 __global__ void __launch_bounds__(kBlock)
 connect_kernel(Render_Params p, Scene_Dev S, const uint32_t* __restrict__ slots, uint32_t count, Path_State ps,
-               float4* __restrict__ records) {
+               float4* __restrict__ records, const uint32_t* __restrict__ count_dev = nullptr) {
+    if (count_dev) count = *count_dev;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
         const uint32_t slot = slots[i];
         const uint32_t info = ps.info[slot];
@@ -836,18 +839,45 @@ tile_variance_kernel(Render_Params p, const double* __restrict__ pixel_variance,
     }
 }
 
+// Mean pixel variance over the sample region (render_scene's
+// variance_estimate, reference_renderer.cpp:565-581), from the per-tile
+// sums, in tile order.
+__global__ void variance_total_kernel(Render_Params p, const double* __restrict__ tile_variance,
+                                      double* __restrict__ out) {
+    if (blockIdx.x != 0 || threadIdx.x != 0) return;
+    double acc = 0.0;
+    int64_t count = 0;
+    for (int t = 0; t < p.tiles_x * p.tiles_y; t++) {
+        acc += tile_variance[t];
+        int x0, y0, x1, y1;
+        tile_sample_bounds(p, t, x0, y0, x1, y1);
+        count += (int64_t)(x1 - x0) * (y1 - y0);
+    }
+    *out = p.spp > 1 ? acc / (double)count : 0.0;
+}
+
 // Sample tables and camera rays of a chunk.  The table kernel's block is
 // sized so that its spp float2 per thread fit in 96 KB of shared memory.
-cudaError_t launch_generate(const Render_Params& p, uint32_t first, uint32_t cp, float* s1d, float* s2d,
-                            float2* image_samples, const Path_State& ps, const Queues& q, cudaStream_t st) {
-    constexpr size_t kSmemLimit = 96 * 1024;
+constexpr size_t kTablesSmemLimit = 96 * 1024;
+
+// One-time kernel attribute (also called before a stream capture, so that
+// no attribute change happens inside one).
+cudaError_t generate_prepare() {
     static bool attr_set = false;
     if (!attr_set) {
         cudaError_t e = cudaFuncSetAttribute(sample_tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                             (int)kSmemLimit);
+                                             (int)kTablesSmemLimit);
         if (e != cudaSuccess) return e;
         attr_set = true;
     }
+    return cudaSuccess;
+}
+
+cudaError_t launch_generate(const Render_Params& p, uint32_t first, uint32_t cp, float* s1d, float* s2d,
+                            float2* image_samples, const Path_State& ps, const Queues& q, cudaStream_t st) {
+    constexpr size_t kSmemLimit = kTablesSmemLimit;
+    cudaError_t pe = generate_prepare();
+    if (pe != cudaSuccess) return pe;
     const size_t per_thread = (size_t)p.spp * sizeof(float2);
     int threads = 128;
     while (threads > 1 && (size_t)threads * per_thread > kSmemLimit) threads /= 2;

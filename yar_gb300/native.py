@@ -95,6 +95,17 @@ class HitSoa(C.Structure):
     _fields_ = [("t", C.c_void_p), ("prim", C.c_void_p), ("object", C.c_void_p), ("bary", C.c_void_p)]
 
 
+class BatchSceneStats(C.Structure):
+    _fields_ = [("variance", C.c_double), ("completion_seconds", C.c_float), ("paths", C.c_uint64),
+                ("traversal_kernel", C.c_uint32 * 2)]
+
+
+class BatchStats(C.Structure):
+    _fields_ = [("gpu_seconds", C.c_float), ("paths", C.c_uint64), ("rays_closest", C.c_uint64),
+                ("rays_any", C.c_uint64), ("branches", C.c_uint32), ("chunk_paths", C.c_uint32),
+                ("upload_seconds", C.c_float), ("tune_seconds", C.c_float), ("capture_seconds", C.c_float)]
+
+
 class GuidedParams(C.Structure):
     _fields_ = [("passes", C.c_uint32), ("train_passes", C.c_uint32), ("guide_fraction", C.c_float),
                 ("learning_rate", C.c_float), ("train_steps", C.c_uint32), ("stream_offset", C.c_uint32),
@@ -136,6 +147,8 @@ EXPORTS = {
     "yar_gpu_cast_any_timed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_float)]),
     "yar_gpu_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
     "yar_gpu_render_static": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
+    "yar_gpu_render_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
+                                       C.POINTER(BatchSceneStats), C.POINTER(BatchStats)]),
     "yar_gpu_guided_render": (C.c_int, [C.c_void_p, C.POINTER(GuidedParams), C.c_void_p, C.c_void_p,
                                         C.POINTER(GuidedStats)]),
     "yar_guide_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
@@ -306,6 +319,20 @@ class Context:
         stats = RenderStats()
         self._check(lib().yar_gpu_render(self._h, _ptr(rgb), C.byref(stats)), "render")
         return rgb, stats
+
+    def render_batch(self, flats):
+        """yar_gpu_render_batch: returns ([images], [BatchSceneStats], BatchStats)."""
+        descs = [f.to_c() for f in flats]
+        arr = (C.c_void_p * len(flats))(*[C.cast(C.byref(d), C.c_void_p) for d, _ in descs])
+        imgs = []
+        for f in flats:
+            r = f.config["render_region"]
+            imgs.append(np.zeros((int(r[3] - r[1]), int(r[2] - r[0]), 3), np.float32))
+        outs = (C.c_void_p * len(flats))(*[_ptr(i) for i in imgs])
+        sst = (BatchSceneStats * len(flats))()
+        st = BatchStats()
+        self._check(lib().yar_gpu_render_batch(self._h, arr, len(flats), outs, sst, C.byref(st)), "render_batch")
+        return imgs, list(sst), st
 
     def guided_render(self, width, height, passes, guide_fraction=0.0, train_passes=0, learning_rate=2e-3,
                       train_steps=8, stream_offset=0, time_budget=0.0, keep_guide=False):

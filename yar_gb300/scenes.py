@@ -432,3 +432,27 @@ def hard_lighting_room(seed=1, width=512, height=512, maxdepth=12, cells=200, li
     if build:
         s.build_kdtrees(threads)
     return s
+
+
+# ---------------------------------------------------------------- batched scenes
+def batch_scenes(seed=4, count=64, maxdepth=8, build=True, threads=0):
+    """The batched-render workload: `count` independent scenes built like the
+    large wavefront scene (Cornell room and boxes, icosphere copies, half
+    Lambertian and half GGX, quad ceiling lights) with triangle counts
+    log-uniform in [1K, 200K] (icosphere level 3, 4 or 5 by size),
+    resolutions uniform in {128^2, 256^2, 512^2, 1024^2}, samples per pixel
+    log-uniform in [4, 256] rounded to a perfect square (the stratified
+    sampler's k x k grid), 4-16 lights, maxdepth `maxdepth`."""
+    rng = np.random.default_rng(seed)
+    out = []
+    for i in range(count):
+        tris = float(np.exp(rng.uniform(np.log(1e3), np.log(2e5))))
+        res = int(rng.choice([128, 256, 512, 1024]))
+        spp = float(np.exp(rng.uniform(np.log(4.0), np.log(256.0))))
+        k = max(2, min(16, int(round(math.sqrt(spp)))))
+        level = 3 if tris < 20000 else (4 if tris < 80000 else 5)
+        meshes = max(1, int(round((tris - 36) / (20 * 4 ** level))))
+        lights = int(rng.integers(4, 17))
+        out.append(large_scene(seed=seed * 1000 + i, width=res, height=res, spp=k * k, maxdepth=maxdepth,
+                               meshes=meshes, level=level, lights=lights, build=build, threads=threads))
+    return out
