@@ -54,6 +54,16 @@ def parse():
     return p.parse_args()
 
 
+def max_over_ranks(pg, seconds, device):
+    """The slowest rank's time (the job's time) under torchrun; unchanged on one process."""
+    if pg is None:
+        return seconds
+    import torch
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
 def dist_setup(args):
     rank = int(os.environ.get("RANK", "0"))
     world = int(os.environ.get("WORLD_SIZE", "1"))
@@ -291,10 +301,7 @@ def run_gb300(args, rank, world, local, pg):
         torch.cuda.synchronize()
         elapsed = time.perf_counter() - t0
     barrier()
-    if pg is not None:
-        tt = torch.tensor([elapsed], dtype=torch.float64, device=dev)
-        pg.all_reduce(tt, op=pg.ReduceOp.MAX)
-        elapsed = float(tt.item())
+    elapsed = max_over_ranks(pg, elapsed, dev)
     ms_per_step = 1000 * elapsed / args.steps
     value = world * 2 * n * args.steps / elapsed / 1e6
 
@@ -324,6 +331,7 @@ def run_gb300(args, rank, world, local, pg):
     torch.cuda.synchronize()
     e2e_elapsed = time.perf_counter() - t0
     barrier()
+    e2e_elapsed = max_over_ranks(pg, e2e_elapsed, dev)
     e2e_value = world * 2 * n * args.steps / e2e_elapsed / 1e6
     h2d = 2 * n * 32
     d2h = n * (4 + 4 + 4 + 8) + n
