@@ -62,6 +62,9 @@ struct Args {
     int threads = 0;
     bool any = false;
     int repeat = 1;
+    bool compress = false;
+    float variance = 0.f;
+    std::string input_file;
 };
 
 Args parse(int argc, char** argv) {
@@ -73,6 +76,9 @@ Args parse(int argc, char** argv) {
         else if (s.rfind("--threads=", 0) == 0) a.threads = atoi(s.c_str() + 10);
         else if (s.rfind("--repeat=", 0) == 0) a.repeat = atoi(s.c_str() + 9);
         else if (s == "--any") a.any = true;
+        else if (s == "--compress") a.compress = true;
+        else if (s.rfind("--variance=", 0) == 0) a.variance = (float)atof(s.c_str() + 11);
+        else if (s.rfind("--input=", 0) == 0) a.input_file = s.substr(8);
         else a.pos.push_back(s);
     }
     if (a.threads <= 0) a.threads = std::max(1u, std::thread::hardware_concurrency());
@@ -688,6 +694,26 @@ int cmd_regress(const Args& a) {
     return 0;
 }
 
+// exr <image.f32> <width> <height> <out.exr> [--spp=N] [--variance=V] [--compress]
+// The reference's write_openexr_image (reference_renderer.cpp:673-705) on a
+// raw float RGB image: the golden files of the EXR writer's parity test.
+int cmd_exr(const Args& a) {
+    if (a.pos.size() < 4) return 2;
+    const int w = atoi(a.pos[1].c_str()), h = atoi(a.pos[2].c_str());
+    Image img(w, h);
+    FILE* f = fopen(a.pos[0].c_str(), "rb");
+    if (!f) return 1;
+    const size_t got = fread(&img.data[0].r, sizeof(float), (size_t)w * h * 3, f);
+    fclose(f);
+    if (got != (size_t)w * h * 3) return 1;
+    EXR_Write_Params params;
+    params.enable_compression = a.compress;
+    params.attributes.input_file = a.input_file;
+    params.attributes.spp = a.spp;
+    params.attributes.variance = a.variance;
+    return write_openexr_image(a.pos[3], img, params) ? 0 : 1;
+}
+
 } // namespace
 
 int main(int argc, char** argv) {
@@ -704,6 +730,7 @@ int main(int argc, char** argv) {
     else if (cmd == "cast") rc = cmd_cast(a);
     else if (cmd == "regress") rc = cmd_regress(a);
     else if (cmd == "render-yfs") rc = cmd_render_yfs(a);
+    else if (cmd == "exr") rc = cmd_exr(a);
     if (rc == 2) fprintf(stderr, "bad arguments for %s\n", cmd.c_str());
     return rc;
 }

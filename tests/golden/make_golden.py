@@ -140,11 +140,34 @@ def cornell_ggx_64():
     np.savez_compressed(os.path.join(HERE, "cornell_ggx_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def exr_files():
+    """The reference's EXR writer (write_openexr_image) on the C1 golden image
+    (uncompressed and ZIP) and on an image of special values (exact half
+    rounding ties, subnormals, overflow, signs)."""
+    img = np.load(os.path.join(HERE, "cornell_c1_64.npz"))["image"].astype(np.float32)
+    rng = np.random.default_rng(5)
+    n = 48 * 32 * 3
+    v = (rng.standard_normal(n) * 10 ** rng.uniform(-9, 5, n)).astype(np.float32)
+    base = rng.integers(0x0001, 0x7BFF, 400).astype(np.uint16).view(np.float16).astype(np.float32)
+    v[:400] = (base.view(np.uint32) + 0x1000).view(np.float32)     # exact ties between two halves
+    v[400:410] = [0.0, -0.0, 6.0e-8, 2.98e-8, 1e-30, 65504.0, 65519.99, 65520.0, 1e9, -1e9]
+    special = v.reshape(32, 48, 3)
+    np.save(os.path.join(HERE, "exr_special_input.npy"), special)
+    with tempfile.TemporaryDirectory() as d:
+        for name, im, extra in (("exr_cornell_none", img, []), ("exr_cornell_zip", img, ["--compress"]),
+                                ("exr_special_none", special, [])):
+            raw = os.path.join(d, "im.f32")
+            im.astype(np.float32).tofile(raw)
+            out = os.path.join(HERE, name + ".exr")
+            attrs = ["--spp=16", "--variance=0.25", "--input=cornell.pbrt"] if "cornell" in name else []
+            oracle._ref("exr", raw, im.shape[1], im.shape[0], out, *attrs, *extra)
+
+
 if __name__ == "__main__":
     if not oracle.have_reference():
         sys.exit("oracle/_ref/yar_ref is not built (oracle/build_ref.sh)")
     which = sys.argv[1:] or ["raycast_small", "transform_small", "kdtree_regression", "cornell_c1_64",
-                             "cornell_ggx_64"]
+                             "cornell_ggx_64", "exr_files"]
     for name in which:
         globals()[name]()
         print("wrote", name)

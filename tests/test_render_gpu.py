@@ -109,3 +109,28 @@ def test_render_identical_for_every_traversal_kernel():
     for img, var in results[1:]:
         assert np.array_equal(img.view(np.uint32), img0.view(np.uint32))
         assert var == var0
+
+
+def test_cli_render_writes_the_reference_exr(tmp_path):
+    """python -m yar_gb300 render: the EXR holds the render's pixels as the
+    reference's writer would store them, with yar_render_device = gpu."""
+    torch = pytest.importorskip("torch")
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    import os
+    from yar_gb300 import exr, native
+    from yar_gb300.__main__ import main
+    out = os.path.join(tmp_path, "c.exr")
+    assert main(["render", golden("cornell_c1_64.yfs"), "--out", out]) == 0
+    got, attrs = exr.read_exr(out)
+    s = FlatScene.read(golden("cornell_c1_64.yfs"))
+    ctx = native.Context(0)
+    try:
+        ctx.upload_scene(s)
+        img, st = ctx.render(64, 64)
+    finally:
+        ctx.close()
+    want = exr.to_half_bits(img).view(np.float16).astype(np.float32)
+    assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
+    assert attrs["yar_render_device"][1] == b"gpu"
+    assert attrs["yar_spp"][1] == (16).to_bytes(4, "little")
