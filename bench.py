@@ -425,12 +425,15 @@ def render_bench(kind, with_cpu=True, reps=3):
         img, st = ctx.render(w, h)
         if best is None or st.seconds < best.seconds:
             best = st
+    kernels = ctx.traversal_kernels()
     ctx.close()
     out = {"workload": desc, "gpu_seconds": round(best.seconds, 4), "paths": int(best.paths),
            "gpu_paths_per_s": round(best.paths / best.seconds, 1),
            "gpu_mrays_per_s": round((best.rays_closest + best.rays_any) / best.seconds / 1e6, 2),
            "rays_closest": int(best.rays_closest), "rays_any": int(best.rays_any),
-           "kernel_launches": int(best.kernel_launches), "image_mean": float(img.mean())}
+           "kernel_launches": int(best.kernel_launches), "image_mean": float(img.mean()),
+           "traversal_kernels": {k: [["-", "p64", "p128", "per_ray"][c] for c in v]
+                                 for k, v in kernels.items() if k != "cast"}}
     if with_cpu and oracle.have_reference():
         spp = 1 if kind == "c3" else 0
         _, info = oracle.ref_render_flat(s, spp=spp)

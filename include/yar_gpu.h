@@ -225,6 +225,14 @@ typedef struct yar_gpu_options {
 #define YAR_TRAVERSAL_PERSISTENT_128 2
 #define YAR_TRAVERSAL_PER_RAY 3
 
+/* The traversal kernels chosen so far on the uploaded scene (YAR_TRAVERSAL_*,
+ * 0 = not chosen yet): cast[0] closest-hit and cast[1] any-hit C-ABI casts;
+ * render_closest[b] / render_any[b] the render's extend and shadow queues of
+ * bounce b (the last entry covers deeper bounces). */
+#define YAR_TRAVERSAL_BOUNCE_BUCKETS 5
+int yar_gpu_traversal_kernels(yar_gpu_ctx* ctx, int32_t cast[2], int32_t render_closest[YAR_TRAVERSAL_BOUNCE_BUCKETS],
+                              int32_t render_any[YAR_TRAVERSAL_BOUNCE_BUCKETS]);
+
 typedef struct yar_render_stats {
     double variance;            /* render_scene's variance_estimate */
     float seconds;              /* render_scene's render_time */

@@ -347,8 +347,8 @@ int render_batch(yar_gpu_ctx* ctx, const yar_flat_scene* const* scenes, uint32_t
             a.hit4 = dp<float4>(hits);
             a.hit2 = reinterpret_cast<uint2*>(dp<float4>(hits) + n);
             for (int kind = 0; kind < 2 && e == cudaSuccess; kind++) {
-                if (s.sub->render_kernel[kind] >= 0) {
-                    s.kernel[kind] = s.sub->render_kernel[kind];
+                if (s.sub->forced_kernel >= 0) {
+                    s.kernel[kind] = s.sub->forced_kernel;
                     continue;
                 }
                 Cast_Args k = a;

@@ -101,6 +101,19 @@ bool validate_tree(const yar_kdtree_view& t, uint32_t primitive_count, std::stri
 
 using namespace yar;
 
+extern "C" int yar_gpu_traversal_kernels(yar_gpu_ctx* ctx, int32_t cast[2], int32_t render_closest[5],
+                                         int32_t render_any[5]) {
+    if (!ctx || !cast || !render_closest || !render_any) return YAR_ERR_INVALID;
+    static_assert(yar_gpu_ctx::kBounceBuckets == YAR_TRAVERSAL_BOUNCE_BUCKETS, "bucket count");
+    auto code = [](int k) { return k < 0 ? 0 : k + YAR_TRAVERSAL_PERSISTENT_64; };
+    for (int i = 0; i < 2; i++) cast[i] = code(ctx->cast_kernel[i]);
+    for (int b = 0; b < yar_gpu_ctx::kBounceBuckets; b++) {
+        render_closest[b] = code(ctx->render_kernel[0][b]);
+        render_any[b] = code(ctx->render_kernel[1][b]);
+    }
+    return YAR_OK;
+}
+
 extern "C" int yar_gpu_create(yar_gpu_ctx** out, const yar_gpu_options* options) {
     if (!out) return YAR_ERR_INVALID;
     *out = nullptr;
@@ -270,7 +283,10 @@ extern "C" int yar_gpu_upload_scene(yar_gpu_ctx* ctx, const yar_flat_scene* scen
 
     rc = render_upload(ctx, scene);
     if (rc != YAR_OK) return rc;
-    for (int k = 0; k < 2; k++) ctx->cast_kernel[k] = ctx->render_kernel[k] = ctx->forced_kernel;
+    for (int k = 0; k < 2; k++) {
+        ctx->cast_kernel[k] = ctx->forced_kernel;
+        for (int b = 0; b < yar_gpu_ctx::kBounceBuckets; b++) ctx->render_kernel[k][b] = ctx->forced_kernel;
+    }
     ctx->has_scene = true;
     return YAR_OK;
 }

@@ -23,18 +23,19 @@ constexpr uint32_t kBatch = 128;  // rays a warp takes per atomic
 
 template <bool ANY>
 __device__ __forceinline__ void write_result(const Traversal<ANY>& tr, uint32_t i, const Cast_Args& a) {
-    if (tr.status < 0) atomicOr(a.err, 1);
+    const int status = tr.status();
+    if (status < 0) atomicOr(a.err, 1);
     if (ANY) {
-        a.occluded[i] = (uint8_t)(tr.status > 0 ? 1 : 0);
+        a.occluded[i] = (uint8_t)(status > 0 ? 1 : 0);
         return;
     }
-    const bool hit = tr.status > 0;
+    const bool hit = status > 0;
     if (a.hit4) {  // render layout
         a.hit4[i] = make_float4(tr.hit.t, tr.hit.b0, tr.hit.b1, tr.hit.b2);
         a.hit2[i] = hit ? make_uint2(tr.hit.prim, tr.hit.object) : make_uint2(0xffffffffu, 0xffffffffu);
         return;
     }
-    if (a.t) a.t[i] = tr.status < 0 ? tr.ray_tmax : tr.hit.t;
+    if (a.t) a.t[i] = status < 0 ? tr.ray_tmax : tr.hit.t;
     if (a.prim) a.prim[i] = hit ? tr.hit.prim : 0xffffffffu;
     if (a.object) a.object[i] = hit ? tr.hit.object : 0xffffffffu;
     if (a.bary) a.bary[i] = hit ? make_float2(tr.hit.b1, tr.hit.b2) : make_float2(0.f, 0.f);
@@ -74,7 +75,7 @@ __global__ void __launch_bounds__(kCastBlock, MINB) cast_persistent(Device_Scene
                 ray = batch_next + rank;
                 const float4 r0 = __ldg(a.rays + 2 * (size_t)ray);
                 const float4 r1 = __ldg(a.rays + 2 * (size_t)ray + 1);
-                tr.begin(s, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z), r0.w);
+                tr.begin(s, ray, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z), r0.w);
                 have = true;
             }
             const uint32_t taken = (uint32_t)__popc(want) < avail ? (uint32_t)__popc(want) : avail;
@@ -82,7 +83,7 @@ __global__ void __launch_bounds__(kCastBlock, MINB) cast_persistent(Device_Scene
             want = __ballot_sync(full, !have && alive);
         }
         if (!__any_sync(full, have)) break;
-        if (have && !tr.template step<MAXD>(s, stack)) {
+        if (have && !tr.template step<MAXD>(s, a.rays, stack)) {
             write_result<ANY>(tr, a.perm ? __ldg(a.perm + ray) : ray, a);
             have = false;
         }
@@ -101,8 +102,8 @@ __global__ void __launch_bounds__(kCastBlock) cast_per_ray(Device_Scene s, Cast_
         const float4 r1 = __ldg(a.rays + 2 * (size_t)i + 1);
         Traversal<ANY> tr;
         Local_Stack stack;
-        tr.begin(s, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z), r0.w);
-        while (tr.template step<1 << 30>(s, stack)) {
+        tr.begin(s, i, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z), r0.w);
+        while (tr.template step<1 << 30>(s, a.rays, stack)) {
         }
         write_result<ANY>(tr, a.perm ? __ldg(a.perm + i) : i, a);
     }
@@ -163,12 +164,12 @@ cudaError_t launch_shadow(const Device_Scene& s, const Cast_Args& a, int kernel,
     return launch<true>(s, a, kernel, stream);
 }
 
-cudaError_t tune_cast(const Device_Scene& s, const Cast_Args& a, bool any, cudaStream_t stream, cudaEvent_t ev0,
-                      cudaEvent_t ev1, int* best) {
+namespace {
+
+cudaError_t time_cast_kernels(const Device_Scene& s, const Cast_Args& a, bool any, cudaStream_t stream,
+                              cudaEvent_t ev0, cudaEvent_t ev1, float* ms_acc) {
     auto run = [&](int k) { return any ? launch_shadow(s, a, k, stream) : launch_extend(s, a, k, stream); };
     cudaError_t e = run(kCastPersistent64);  // warms the caches for the timed runs
-    float best_ms = 0.f;
-    *best = kCastPersistent64;
     for (int k = 0; k < kCastKernelCount && e == cudaSuccess; k++) {
         e = cudaEventRecord(ev0, stream);
         if (e == cudaSuccess) e = run(k);
@@ -176,11 +177,25 @@ cudaError_t tune_cast(const Device_Scene& s, const Cast_Args& a, bool any, cudaS
         if (e == cudaSuccess) e = cudaEventSynchronize(ev1);
         float ms = 0.f;
         if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev0, ev1);
-        if (e == cudaSuccess && (k == 0 || ms < best_ms)) {
-            best_ms = ms;
-            *best = k;
-        }
+        ms_acc[k] += ms;
     }
+    return e;
+}
+
+int fastest_cast_kernel(const float* ms) {
+    int best = 0;
+    for (int k = 1; k < kCastKernelCount; k++)
+        if (ms[k] < ms[best]) best = k;
+    return best;
+}
+
+} // namespace
+
+cudaError_t tune_cast(const Device_Scene& s, const Cast_Args& a, bool any, cudaStream_t stream, cudaEvent_t ev0,
+                      cudaEvent_t ev1, int* best) {
+    float ms[kCastKernelCount] = {};
+    cudaError_t e = time_cast_kernels(s, a, any, stream, ev0, ev1, ms);
+    *best = e == cudaSuccess ? fastest_cast_kernel(ms) : kCastPersistent64;
     return e;
 }
 

@@ -71,7 +71,9 @@ struct yar_gpu_ctx {
     // renders; -1 until tuned on the current scene (or fixed by the options)
     int forced_kernel = -1;
     int cast_kernel[2] = {-1, -1};
-    int render_kernel[2] = {-1, -1};
+    // renders: per ray kind and bounce (bounces past the last share its entry)
+    static constexpr int kBounceBuckets = 5;
+    int render_kernel[2][kBounceBuckets] = {{-1, -1, -1, -1, -1}, {-1, -1, -1, -1, -1}};
 
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
 

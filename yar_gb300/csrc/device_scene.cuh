@@ -144,11 +144,6 @@ __device__ __forceinline__ float watertight(float3 o, const Watertight_Ray& w, f
     return t;
 }
 
-struct Stack_Entry {
-    uint32_t node;
-    float t_max;
-};
-
 // transform_ray, src/lib/matrix.cpp:368-389: ((a*x + b*y) + c*z) + w
 __device__ __forceinline__ void transform_ray(float4 r0, float4 r1, float4 r2, float3 o, float3 d, float3& oo,
                                               float3& od) {
@@ -162,55 +157,67 @@ __device__ __forceinline__ void transform_ray(float4 r0, float4 r1, float4 r2, f
 
 enum : int { kDescend = 0, kSceneLeaf = 1, kMeshLeaf = 2, kDone = 3 };
 
+// Traversal stack: 2 * kMaxTraversalDepth node entries (scene level below,
+// mesh level above) plus the two entries that save the scene level while a
+// mesh is traversed.
+constexpr int kStackEntries = 2 * kMaxTraversalDepth + 2;
+
 // Two-level closest-hit (ANY = false) or any-hit (ANY = true) traversal of one
 // ray as a resumable state machine: begin() sets up a ray, step() performs one
 // unit of work (a descent through interior nodes down to a leaf, one scene-leaf
 // object entry, or one triangle test) and returns false once the ray is
-// finished.  status afterwards: closest 1 = hit / 0 = miss; any 1 = occluded /
-// 0 = not; -1 = traversal-stack overflow.
+// finished.  status() afterwards: closest 1 = hit / 0 = miss; any 1 =
+// occluded / 0 = not; -1 = traversal-stack overflow.
+//
+// The state is kept small so that it stays in registers: the world ray is not
+// held while a mesh is traversed (it is reloaded from the ray record when the
+// mesh is left, and 1/d recomputed with the same IEEE division); the scene
+// level's interval and leaf cursor go onto the traversal stack when an object
+// is entered; mode, level, the triangle-test flag, the watertight axis
+// permutation and the status share one word; a leaf's primitive count is
+// re-read from its node (an L1 hit) instead of being held.
 template <bool ANY>
 struct Traversal {
-    float3 o, d, inv;      // world ray
+    float3 co, cd, cinv;   // ray of the current level (the world ray at scene level)
     float ray_tmax;
-    float3 co, cd, cinv;   // ray of the current level
-    const uint2* nodes;
-    uint32_t node;
+    uint32_t ray;          // index of the ray record
+    uint32_t node;         // current node; while a leaf is processed, the leaf
     float t_min, t_max;
     int sp, mesh_sp_base;
-    bool in_mesh;
-    uint32_t sl_node, sl_i, sl_count;
-    float scene_t_min, scene_t_max;
+    uint32_t mesh_offset;  // node offset of the current mesh in mesh_nodes
+    uint32_t tri_offset;   // triangle offset of the current mesh
+    uint32_t leaf_i;       // next primitive of the current leaf
     uint32_t cur_object;
-    float entry_t;
-    uint32_t tri_offset;
-    bool test_triangles;
-    Watertight_Ray wr;
-    uint32_t ml_node, ml_i, ml_count;
-    int mode;
-    int status;
+    uint32_t flags;        // bits 0-1 mode, 2 in mesh, 3 test triangles, 4-9 kx ky kz, 10-11 status + 1
+    float sx, sy, sz;      // watertight setup of the mesh ray (src/ref/intersection.cpp:55-62)
     Hit hit;
 
-    __device__ __forceinline__ void leave_mesh(const Device_Scene& s) {
-        if (!ANY && hit.t < entry_t) hit.object = cur_object;
-        in_mesh = false;
+    __device__ __forceinline__ int mode() const { return (int)(flags & 3u); }
+    __device__ __forceinline__ void set_mode(int m) { flags = (flags & ~3u) | (uint32_t)m; }
+    __device__ __forceinline__ bool in_mesh() const { return (flags >> 2) & 1u; }
+    __device__ __forceinline__ int status() const { return (int)((flags >> 10) & 3u) - 1; }
+
+    __device__ __forceinline__ void finish(int st) { flags = (flags & ~(3u | (3u << 10))) | (uint32_t)kDone | ((uint32_t)(st + 1) << 10); }
+
+    template <class STACK>
+    __device__ __forceinline__ void leave_mesh(const Device_Scene& s, const float4* rays, STACK& stack) {
         sp = mesh_sp_base;
-        co = o;
-        cd = d;
-        cinv = inv;
-        nodes = s.scene_nodes;
-        t_min = scene_t_min;
-        t_max = scene_t_max;
-        mode = kSceneLeaf;
+        const uint2 cursor = stack.pop(sp - 1);
+        const uint2 interval = stack.pop(sp - 2);
+        sp -= 2;
+        node = cursor.x;
+        leaf_i = cursor.y;
+        t_min = __uint_as_float(interval.x);
+        t_max = __uint_as_float(interval.y);
+        const float4 r0 = __ldg(rays + 2 * (size_t)ray), r1 = __ldg(rays + 2 * (size_t)ray + 1);
+        co = make_float3(r0.x, r0.y, r0.z);
+        cd = make_float3(r1.x, r1.y, r1.z);
+        cinv = make_float3(1.f / cd.x, 1.f / cd.y, 1.f / cd.z);
+        flags = (flags & ~(3u | 4u)) | (uint32_t)kSceneLeaf;
     }
 
-    __device__ __forceinline__ void finish(int st) {
-        mode = kDone;
-        status = st;
-    }
-
-    __device__ __forceinline__ void begin(const Device_Scene& s, float3 ro, float3 rd, float tmax) {
-        o = ro;
-        d = rd;
+    __device__ __forceinline__ void begin(const Device_Scene& s, uint32_t ray_index, float3 ro, float3 rd, float tmax) {
+        ray = ray_index;
         ray_tmax = tmax;
         hit.t = tmax;
         hit.prim = 0xffffffffu;
@@ -218,33 +225,31 @@ struct Traversal {
         hit.b0 = hit.b1 = hit.b2 = 0.f;
         sp = 0;
         mesh_sp_base = 0;
-        in_mesh = false;
         node = 0;
-        nodes = s.scene_nodes;
-        status = 0;
+        flags = (uint32_t)kDescend | (1u << 10);  // status 0
         if (!clip_ray(make_float3(s.scene_bounds[0], s.scene_bounds[1], s.scene_bounds[2]),
-                      make_float3(s.scene_bounds[3], s.scene_bounds[4], s.scene_bounds[5]), o, d, t_min, t_max)) {
-            mode = kDone;
+                      make_float3(s.scene_bounds[3], s.scene_bounds[4], s.scene_bounds[5]), ro, rd, t_min, t_max)) {
+            finish(0);
             return;
         }
-        inv = make_float3(1.f / d.x, 1.f / d.y, 1.f / d.z);
-        co = o;
-        cd = d;
-        cinv = inv;
-        mode = kDescend;
+        co = ro;
+        cd = rd;
+        cinv = make_float3(1.f / rd.x, 1.f / rd.y, 1.f / rd.z);
     }
 
-    // `stack` holds up to 2 * kMaxTraversalDepth entries (Local_Stack or
-    // Split_Stack; kept out of this struct so the scalar state can live in
-    // registers).  A descent stops at a leaf or after MAXD interior nodes.
+    // `stack` holds kStackEntries entries (Local_Stack or Split_Stack; kept out
+    // of this struct so the scalar state can live in registers).  A descent
+    // stops at a leaf or after MAXD interior nodes.
     template <int MAXD, class STACK>
-    __device__ __forceinline__ bool step(const Device_Scene& s, STACK& stack) {
-        if (mode == kDescend) {
+    __device__ __forceinline__ bool step(const Device_Scene& s, const float4* rays, STACK& stack) {
+        const int m = mode();
+        if (m == kDescend) {
+            const uint2* nodes = in_mesh() ? s.mesh_nodes + mesh_offset : s.scene_nodes;
             for (int steps = 0; steps < MAXD; steps++) {  // descend through interior nodes of the current level
                 const float limit = ANY ? ray_tmax : hit.t;
                 if (!(limit > t_min)) {  // the level's loop condition failed
-                    if (in_mesh) {
-                        leave_mesh(s);
+                    if (in_mesh()) {
+                        leave_mesh(s, rays, stack);
                     } else {
                         finish(ANY ? 0 : (hit.t < ray_tmax ? 1 : 0));
                     }
@@ -252,18 +257,8 @@ struct Traversal {
                 }
                 const uint2 n = __ldg(nodes + node);
                 if ((n.x & 3u) == 3u) {
-                    const uint32_t count = n.x >> 2;
-                    if (in_mesh) {
-                        mode = kMeshLeaf;
-                        ml_node = node;
-                        ml_i = 0;
-                        ml_count = test_triangles ? count : 0u;
-                    } else {
-                        mode = kSceneLeaf;
-                        sl_node = node;
-                        sl_i = 0;
-                        sl_count = count;
-                    }
+                    leaf_i = 0;
+                    set_mode(in_mesh() ? kMeshLeaf : kSceneLeaf);
                     break;
                 }
                 const int axis = (int)(n.x & 3u);
@@ -280,7 +275,7 @@ struct Traversal {
                     } else if (t_split < t_min) {
                         node = second_child;
                     } else {
-                        if (sp >= 2 * kMaxTraversalDepth) {
+                        if (sp >= kStackEntries) {
                             finish(-1);
                             break;
                         }
@@ -293,66 +288,87 @@ struct Traversal {
                     node = (sel3(cd.x, cd.y, cd.z, axis) > 0.f) ? above_child : below_child;
                 }
             }
-        } else if (mode == kMeshLeaf) {
-            if (ml_i < ml_count) {
-                const uint32_t prim = (ml_i == 0) ? __ldg(&nodes[ml_node].y)
-                                                  : __ldg(reinterpret_cast<const uint32_t*>(nodes + ml_node) + 1 + ml_i);
-                ml_i++;
+        } else if (m == kMeshLeaf) {
+            const uint2* nodes = s.mesh_nodes + mesh_offset;
+            const uint2 leaf = __ldg(nodes + node);
+            const uint32_t count = ((flags >> 3) & 1u) ? (leaf.x >> 2) : 0u;
+            if (leaf_i < count) {
+                const uint32_t prim =
+                    (leaf_i == 0) ? leaf.y : __ldg(reinterpret_cast<const uint32_t*>(nodes + node) + 1 + leaf_i);
+                leaf_i++;
                 const float4* tp = s.tris + 3 * ((size_t)tri_offset + prim);
                 const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+                Watertight_Ray wr;
+                wr.kx = (int)((flags >> 4) & 3u);
+                wr.ky = (int)((flags >> 6) & 3u);
+                wr.kz = (int)((flags >> 8) & 3u);
+                wr.sx = sx;
+                wr.sy = sy;
+                wr.sz = sz;
                 float b0, b1, b2;
                 const float t = watertight(co, wr, v0, v1, v2, b0, b1, b2);
                 if (ANY) {
                     // `t >= ray_tmax` rejects; a NaN t does not (src/ref/kdtree.cpp:60-62)
                     if (!(t >= ray_tmax) && v0.w == 0.f) finish(1);
                 } else if (t < hit.t && v0.w == 0.f) {
+                    // the object of the closest hit is the one whose mesh produced it
+                    // (src/ref/kdtree.cpp:81-95 sets it after the mesh improved the hit)
                     hit.t = t;
                     hit.prim = prim;
+                    hit.object = cur_object;
                     hit.b0 = b0;
                     hit.b1 = b1;
                     hit.b2 = b2;
                 }
             } else if (sp == mesh_sp_base) {  // mesh stack empty: the mesh is done
-                leave_mesh(s);
+                leave_mesh(s, rays, stack);
             } else {
                 --sp;
                 const uint2 e = stack.pop(sp);
                 node = e.x;
                 t_min = t_max;
                 t_max = __uint_as_float(e.y);
-                mode = kDescend;
+                set_mode(kDescend);
             }
-        } else if (mode == kSceneLeaf) {
-            if (sl_i < sl_count) {
-                const uint32_t obj = (sl_i == 0)
-                                         ? __ldg(&s.scene_nodes[sl_node].y)
-                                         : __ldg(reinterpret_cast<const uint32_t*>(s.scene_nodes + sl_node) + 1 + sl_i);
-                sl_i++;
+        } else if (m == kSceneLeaf) {
+            const uint2 leaf = __ldg(s.scene_nodes + node);
+            const uint32_t count = leaf.x >> 2;
+            if (leaf_i < count) {
+                const uint32_t obj =
+                    (leaf_i == 0) ? leaf.y : __ldg(reinterpret_cast<const uint32_t*>(s.scene_nodes + node) + 1 + leaf_i);
+                leaf_i++;
                 const float4* p = s.objects + 6 * (size_t)obj;
                 const float4 r0 = __ldg(p + 0), r1 = __ldg(p + 1), r2 = __ldg(p + 2);
                 const float4 lo = __ldg(p + 3), hi = __ldg(p + 4), info = __ldg(p + 5);
                 float3 oo, od;
-                transform_ray(r0, r1, r2, o, d, oo, od);
+                transform_ray(r0, r1, r2, co, cd, oo, od);
                 float mt_min, mt_max;
                 if (clip_ray(make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z), oo, od, mt_min, mt_max)) {
-                    scene_t_min = t_min;
-                    scene_t_max = t_max;
-                    in_mesh = true;
+                    if (sp + 2 > kStackEntries) {
+                        finish(-1);
+                        return false;
+                    }
+                    stack.push(sp, __float_as_uint(t_min), t_max);  // the scene level's interval
+                    stack.push(sp + 1, node, __uint_as_float(leaf_i));  // and its leaf cursor
+                    sp += 2;
+                    mesh_sp_base = sp;
                     cur_object = obj;
-                    entry_t = hit.t;
                     co = oo;
                     cd = od;
                     cinv = make_float3(1.f / od.x, 1.f / od.y, 1.f / od.z);
-                    nodes = s.mesh_nodes + __float_as_uint(lo.w);
+                    mesh_offset = __float_as_uint(lo.w);
                     tri_offset = __float_as_uint(hi.w);
                     const int visibility = __float_as_int(info.y);
-                    test_triangles = ANY ? (visibility == 0) : (visibility != 2);
-                    wr = watertight_setup(od);
+                    const bool test_triangles = ANY ? (visibility == 0) : (visibility != 2);
+                    const Watertight_Ray wr = watertight_setup(od);
+                    sx = wr.sx;
+                    sy = wr.sy;
+                    sz = wr.sz;
+                    flags = (flags & (3u << 10)) | (uint32_t)kDescend | 4u | (test_triangles ? 8u : 0u) |
+                            ((uint32_t)wr.kx << 4) | ((uint32_t)wr.ky << 6) | ((uint32_t)wr.kz << 8);
                     node = 0;
                     t_min = mt_min;
                     t_max = mt_max;
-                    mesh_sp_base = sp;
-                    mode = kDescend;
                 }
             } else if (sp == 0) {
                 finish(ANY ? 0 : (hit.t < ray_tmax ? 1 : 0));
@@ -362,16 +378,16 @@ struct Traversal {
                 node = e.x;
                 t_min = t_max;
                 t_max = __uint_as_float(e.y);
-                mode = kDescend;
+                set_mode(kDescend);
             }
         }
-        return mode != kDone;
+        return mode() != kDone;
     }
 };
 
 // Traversal stack in local memory (L1-cached).
 struct Local_Stack {
-    uint2 e[2 * kMaxTraversalDepth];
+    uint2 e[kStackEntries];
     __device__ __forceinline__ void push(int sp, uint32_t node, float t_max) {
         e[sp] = make_uint2(node, __float_as_uint(t_max));
     }
@@ -384,7 +400,7 @@ struct Local_Stack {
 template <int SHORT, int BLOCK>
 struct Split_Stack {
     uint2* smem;  // this thread's column: base + threadIdx.x
-    uint2 deep[2 * kMaxTraversalDepth - SHORT];
+    uint2 deep[kStackEntries - SHORT];
     __device__ __forceinline__ void push(int sp, uint32_t node, float t_max) {
         const uint2 v = make_uint2(node, __float_as_uint(t_max));
         if (sp < SHORT) smem[sp * BLOCK] = v;
@@ -392,18 +408,5 @@ struct Split_Stack {
     }
     __device__ __forceinline__ uint2 pop(int sp) const { return sp < SHORT ? smem[sp * BLOCK] : deep[sp - SHORT]; }
 };
-
-// One ray, start to finish (used by the render wavefront).  Returns the status.
-template <bool ANY>
-__device__ __forceinline__ int traverse(const Device_Scene& s, const float3 o, const float3 d, const float ray_tmax,
-                                        Hit& hit) {
-    Traversal<ANY> tr;
-    Local_Stack stack;
-    tr.begin(s, o, d, ray_tmax);
-    while (tr.step<1 << 30>(s, stack)) {
-    }
-    hit = tr.hit;
-    return tr.status;
-}
 
 } // namespace yar

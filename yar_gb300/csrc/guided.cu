@@ -236,8 +236,7 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
         int cur = 0;
         uint32_t count = paths;
         for (int bounce = 0; count > 0 && bounce <= p.max_bounces + 1 && e == cudaSuccess; bounce++) {
-            const bool tune = bounce >= 1 && count >= kRenderTuneMinRays;
-            e = trace_extend(ctx, q, cur, count, tune, st);
+            e = trace_extend(ctx, q, cur, count, bounce, st);
             if (e != cudaSuccess) break;
             if (g.queries && (g.lobes || g.records)) {
                 guide_query_kernel<<<grid_for(count), kBlock, 0, st>>>(S, q.ext_rays[cur], q.ext_hit4, q.ext_hit2, count,
@@ -248,7 +247,7 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
             cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
             shade_kernel<true><<<grid_for(count), kBlock, 0, st>>>(p, S, cur, count, dp<float>(B[2]),
                                                                    dp<float2>(B[3]), ps, q, g);
-            e = trace_light_queues(ctx, q, ps, count, tune, st);
+            e = trace_light_queues(ctx, q, ps, count, bounce, st);
             if (e != cudaSuccess) break;
             connect_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, q.ext_slot[cur], count, ps, g.records);
             uint32_t h[4];

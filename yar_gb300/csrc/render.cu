@@ -196,13 +196,12 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
         int cur = 0;
         uint32_t count = paths;
         for (int bounce = 0; count > 0 && bounce <= p.max_bounces + 1; bounce++) {
-            const bool tune = bounce >= 1 && count >= kRenderTuneMinRays;
-            e = trace_extend(ctx, q, cur, count, tune, st);
+            e = trace_extend(ctx, q, cur, count, bounce, st);
             if (e != cudaSuccess) break;
             cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
             shade_kernel<false><<<grid_for(count), kBlock, 0, st>>>(p, S, cur, count, dptr<float>(B[2]),
                                                              dptr<float2>(B[3]), ps, q, Guide_Shade{});
-            e = trace_light_queues(ctx, q, ps, count, tune, st);
+            e = trace_light_queues(ctx, q, ps, count, bounce, st);
             if (e != cudaSuccess) break;
             connect_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, q.ext_slot[cur], count, ps, nullptr);
             launches += 5;
@@ -361,12 +360,11 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
         int cur = 0;
         uint32_t count = paths;
         for (int bounce = 0; count > 0 && bounce <= p.max_bounces + 1; bounce++) {
-            const bool tune = bounce >= 1 && count >= kRenderTuneMinRays;
-            e = trace_extend(ctx, q, cur, count, tune, st);
+            e = trace_extend(ctx, q, cur, count, bounce, st);
             if (e != cudaSuccess) break;
             cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
             shade_kernel<false><<<grid_for(count), kBlock, 0, st>>>(p, S, cur, count, s1d, s2d, ps, q, Guide_Shade{});
-            e = trace_light_queues(ctx, q, ps, count, tune, st);
+            e = trace_light_queues(ctx, q, ps, count, bounce, st);
             if (e != cudaSuccess) break;
             connect_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, q.ext_slot[cur], count, ps, nullptr);
             launches += 5;

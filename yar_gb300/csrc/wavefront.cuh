@@ -335,13 +335,28 @@ camera_kernel(Render_Params p, uint32_t chunk_first, uint32_t chunk_paths, const
 // The three ray queues of a bounce are traced by the cast kernels (cast.cu).
 // Extend hits are written at the queue position (shade reads the queue in
 // order); shadow and probe results at the path slot.  Hand-out counters are
-// counters[4..6], the error word counters[3].  The traversal kernel of each
-// ray kind is chosen by timing on the first bounce after the camera bounce
-// with at least kRenderTuneMinRays paths (secondary rays are the incoherent
-// majority), unless the context fixes it.
+// counters[4..6], the error word counters[3].
+//
+// The traversal kernel is chosen per ray kind and per bounce (camera rays,
+// the first bounces and the deep, sparse, incoherent ones favour different
+// kernels): the first queue of at least kRenderTuneMinRays rays of a bounce
+// after a scene upload is traced by all three kernels, timed, and the fastest
+// kept (the queue's results are the same whichever ran last); the MIS probe
+// queue uses the extend queue's choice.  A context option can fix the kernel.
 constexpr uint32_t kRenderTuneMinRays = 1u << 16;
 
-cudaError_t trace_extend(yar_gpu_ctx* ctx, const Queues& q, int cur, uint32_t count, bool tune, cudaStream_t st) {
+inline int bounce_bucket(int bounce) { return bounce < yar_gpu_ctx::kBounceBuckets ? bounce : yar_gpu_ctx::kBounceBuckets - 1; }
+
+// The kernel a bounce runs with: its own choice, else the choice of the
+// nearest earlier bounce (queues too short to time follow the bounce before
+// them), else the persistent 64-register kernel.
+inline int render_choice(const yar_gpu_ctx* ctx, int kind, int bounce) {
+    for (int b = bounce_bucket(bounce); b >= 0; b--)
+        if (ctx->render_kernel[kind][b] >= 0) return ctx->render_kernel[kind][b];
+    return kCastPersistent64;
+}
+
+cudaError_t trace_extend(yar_gpu_ctx* ctx, const Queues& q, int cur, uint32_t count, int bounce, cudaStream_t st) {
     Cast_Args a;
     a.rays = q.ext_rays[cur];
     a.n = count;
@@ -349,12 +364,12 @@ cudaError_t trace_extend(yar_gpu_ctx* ctx, const Queues& q, int cur, uint32_t co
     a.err = reinterpret_cast<int*>(q.counters + 3);
     a.hit4 = q.ext_hit4;
     a.hit2 = q.ext_hit2;
-    int& k = ctx->render_kernel[0];
-    if (tune && k < 0) return tune_cast(ctx->ds, a, false, st, ctx->ev_start, ctx->ev_stop, &k);
-    return launch_extend(ctx->ds, a, k < 0 ? kCastPersistent64 : k, st);
+    int& k = ctx->render_kernel[0][bounce_bucket(bounce)];
+    if (k < 0 && count >= kRenderTuneMinRays) return tune_cast(ctx->ds, a, false, st, ctx->ev_start, ctx->ev_stop, &k);
+    return launch_extend(ctx->ds, a, render_choice(ctx, 0, bounce), st);
 }
 
-cudaError_t trace_light_queues(yar_gpu_ctx* ctx, const Queues& q, const Path_State& ps, uint32_t count, bool tune,
+cudaError_t trace_light_queues(yar_gpu_ctx* ctx, const Queues& q, const Path_State& ps, uint32_t count, int bounce,
                                cudaStream_t st) {
     Cast_Args sh;
     sh.rays = q.shd_rays;
@@ -364,9 +379,10 @@ cudaError_t trace_light_queues(yar_gpu_ctx* ctx, const Queues& q, const Path_Sta
     sh.next_ray = q.counters + 5;
     sh.err = reinterpret_cast<int*>(q.counters + 3);
     sh.occluded = ps.occluded;
-    int& k = ctx->render_kernel[1];
-    cudaError_t e = (tune && k < 0) ? tune_cast(ctx->ds, sh, true, st, ctx->ev_start, ctx->ev_stop, &k)
-                                    : launch_shadow(ctx->ds, sh, k < 0 ? kCastPersistent64 : k, st);
+    int& k = ctx->render_kernel[1][bounce_bucket(bounce)];
+    cudaError_t e = (k < 0 && count >= kRenderTuneMinRays)
+                        ? tune_cast(ctx->ds, sh, true, st, ctx->ev_start, ctx->ev_stop, &k)
+                        : launch_shadow(ctx->ds, sh, render_choice(ctx, 1, bounce), st);
     if (e != cudaSuccess) return e;
     Cast_Args pr;
     pr.rays = q.prb_rays;
@@ -377,8 +393,7 @@ cudaError_t trace_light_queues(yar_gpu_ctx* ctx, const Queues& q, const Path_Sta
     pr.err = reinterpret_cast<int*>(q.counters + 3);
     pr.hit4 = ps.probe_hit4;
     pr.hit2 = ps.probe_hit2;
-    const int kc = ctx->render_kernel[0];
-    return launch_extend(ctx->ds, pr, kc < 0 ? kCastPersistent64 : kc, st);
+    return launch_extend(ctx->ds, pr, render_choice(ctx, 0, bounce), st);
 }
 
 // ---------------------------------------------------------------- shading context

@@ -147,6 +147,8 @@ EXPORTS = {
     "yar_gpu_cast_any_timed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_float)]),
     "yar_gpu_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
     "yar_gpu_render_static": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
+    "yar_gpu_traversal_kernels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
+                                            C.POINTER(C.c_int32)]),
     "yar_gpu_render_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
                                        C.POINTER(BatchSceneStats), C.POINTER(BatchStats)]),
     "yar_gpu_guided_render": (C.c_int, [C.c_void_p, C.POINTER(GuidedParams), C.c_void_p, C.c_void_p,
@@ -319,6 +321,13 @@ class Context:
         stats = RenderStats()
         self._check(lib().yar_gpu_render(self._h, _ptr(rgb), C.byref(stats)), "render")
         return rgb, stats
+
+    def traversal_kernels(self):
+        """The traversal kernels chosen so far: {"cast": [closest, any], "render_closest": [per bounce],
+        "render_any": [per bounce]} as TRAVERSAL_* codes (0 = not chosen yet)."""
+        c, rc, ra = (C.c_int32 * 2)(), (C.c_int32 * 5)(), (C.c_int32 * 5)()
+        self._check(lib().yar_gpu_traversal_kernels(self._h, c, rc, ra), "traversal_kernels")
+        return {"cast": list(c), "render_closest": list(rc), "render_any": list(ra)}
 
     def render_batch(self, flats):
         """yar_gpu_render_batch: returns ([images], [BatchSceneStats], BatchStats)."""
