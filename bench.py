@@ -49,7 +49,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-render", action="store_true", help="skip the C1 render figures")
     p.add_argument("--workload", default="raycast",
-                   choices=["raycast", "render-c1", "render-c3", "guided", "batch"],
+                   choices=["raycast", "render-c1", "render-c3", "guided", "batch", "guide-mlp"],
                    help="render-c1 / render-c3 print a separate line for the C1 or the large (C3) render")
     return p.parse_args()
 
@@ -535,11 +535,73 @@ def batch_bench(count=64):
     }
 
 
+def guide_mlp_bench(n_infer=1 << 20, n_train=1 << 18, reps=20):
+    """The learned proposal's tensor-core kernels alone: inference of n_infer
+    rows and one Adam step over n_train rows through the C ABI (each call
+    synchronises; host-timed over `reps` calls, so launch and synchronisation
+    overhead is included), against the measured dense bf16 peak."""
+    import torch
+    from yar_gb300 import native
+    box = (-1.0, 0.0, -1.0, 1.0, 2.0, 1.0)
+    g = torch.Generator(device="cuda").manual_seed(5)
+
+    def rows(n, width):
+        r = torch.zeros((n, width), device="cuda")
+        r[:, 0:3] = torch.rand((n, 3), device="cuda", generator=g) * torch.tensor([2.0, 2.0, 2.0], device="cuda") + \
+            torch.tensor(box[:3], device="cuda")
+        for c in (3, 6) + ((9,) if width == 16 else ()):
+            v = torch.randn((n, 3), device="cuda", generator=g)
+            r[:, c:c + 3] = v / v.norm(dim=1, keepdim=True)
+        if width == 16:
+            r[:, 12] = torch.rand(n, device="cuda", generator=g)
+        return r
+
+    ctx = native.Context(0)
+    q, s = rows(n_infer, 12), rows(n_train, 16)
+    lobes = torch.empty((n_infer, 40), device="cuda")
+    torch.cuda.synchronize()
+    for _ in range(3):
+        ctx.guide_infer(q.data_ptr(), n_infer, box, lobes.data_ptr())
+        ctx.guide_train_step(s.data_ptr(), n_train, box, 1.0 / n_train, 1e-4)
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ctx.guide_infer(q.data_ptr(), n_infer, box, lobes.data_ptr())
+    t_inf = (time.perf_counter() - t0) / reps
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        ctx.guide_train_step(s.data_ptr(), n_train, box, 1.0 / n_train, 1e-4)
+    t_tr = (time.perf_counter() - t0) / reps
+    ctx.close()
+    try:
+        peak = json.load(open(os.path.join(ROOT, "MEASURED_PEAKS.json"))).get("bf16_tflops", 1900.0)
+        src = "measured"
+    except (OSError, ValueError):
+        peak, src = 1900.0, "fallback"
+    f_inf = 2 * (64 * 128 + 3 * 64 * 64)             # MMA flops per row: 4 layers
+    f_tr = f_inf + 2 * 3 * 64 * 64 + f_inf           # + input gradients of layers 4..2 + weight gradients
+    return {
+        "inference": {"rows": n_infer, "ms": round(1e3 * t_inf, 3), "rows_per_s": round(n_infer / t_inf, 1),
+                      "tflops": round(f_inf * n_infer / t_inf / 1e12, 2),
+                      "frac_of_peak": round(f_inf * n_infer / t_inf / 1e12 / peak, 4)},
+        "train_step": {"rows": n_train, "ms": round(1e3 * t_tr, 3), "rows_per_s": round(n_train / t_tr, 1),
+                       "tflops": round(f_tr * n_train / t_tr / 1e12, 2),
+                       "frac_of_peak": round(f_tr * n_train / t_tr / 1e12 / peak, 4)},
+        "peak_bf16_tflops": peak, "peak_source": src,
+        "flops_per_row": {"inference": f_inf, "train": f_tr},
+    }
+
+
 def main():
     args = parse()
     rank, world, local, pg = dist_setup(args)
     try:
-        if args.workload == "batch":
+        if args.workload == "guide-mlp":
+            if rank == 0:
+                m = guide_mlp_bench()
+                print(json.dumps({"metric": "guide network rows/s (tcgen05 BF16 MLP inference)", "impl": args.impl,
+                                  "value": m["inference"]["rows_per_s"], "unit": "rows/s", "higher_is_better": True,
+                                  "guide_mlp": m}), flush=True)
+        elif args.workload == "batch":
             if rank == 0:
                 b = batch_bench()
                 print(json.dumps({"metric": "paths/s (batched render, one graph launch)", "impl": args.impl,
