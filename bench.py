@@ -445,7 +445,7 @@ def render_bench(kind, with_cpu=True, reps=3):
     return out
 
 
-GUIDE = dict(guide_fraction=0.7, train_passes=64, train_steps=32, learning_rate=5e-3)
+GUIDE = dict(guide_fraction=0.7, train_passes=32, train_steps=32, learning_rate=5e-3)
 
 
 def guided_bench(plain_passes=1024):
@@ -478,8 +478,8 @@ def guided_bench(plain_passes=1024):
     ctx.close()
     r_p, r_g = rmse(img_p), rmse(img_g)
     return {
-        "workload": "hard-lighting room: %d triangles, 512x512, maxdepth 12, one 0.1x0.1 light of radiance 1000 "
-                    "behind a 0.1x0.1 ceiling opening, GGX metal walls (roughness 0.1-0.3)" % s.triangle_count,
+        "workload": "hard-lighting room: %d triangles, 512x512, maxdepth 12, one 0.1x0.1 light of radiance 1000 0.6 "
+                    "above a 0.1x0.1 ceiling opening, GGX metal walls (roughness 0.1-0.3), boxes outside the beam" % s.triangle_count,
         "oracle": "plain mode, %d one-sample passes, FP64 accumulation" % int(z["passes"]),
         "plain": {"passes": int(st_p.passes), "seconds": round(st_p.seconds, 3), "rmse": r_p,
                   "mrays_per_s": round(st_p.rays / st_p.seconds / 1e6, 1)},

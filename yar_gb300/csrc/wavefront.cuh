@@ -207,6 +207,24 @@ __device__ __forceinline__ void pcg_advance(Pcg& r, uint32_t n) {
     r.state = acc_mult * r.state + acc_plus * r.inc;
 }
 
+// SplitMix64's output function (Steele, Lea, Flood, "Fast splittable
+// pseudorandom number generators", 2014): a bijective 64-bit mix.
+__device__ __forceinline__ uint64_t mix64(uint64_t z) {
+    z = (z ^ (z >> 30)) * 0xBF58476D1CE4E5B9ull;
+    z = (z ^ (z >> 27)) * 0x94D049BB133111EBull;
+    return z ^ (z >> 31);
+}
+
+// The pcg stream of a pixel: the reference's (initstate 0, sequence = the
+// pixel's stream id) when stream_hi is 0; otherwise (independent passes of
+// the guided render) sequence and initial state are mixed from the stream id
+// and the pass, so that passes share no low-order state bits.
+__device__ __forceinline__ Pcg pixel_pcg(const Render_Params& p, uint32_t stream) {
+    if (p.stream_hi == 0) return pcg_seed(0, stream);
+    const uint64_t key = (uint64_t)stream | ((uint64_t)p.stream_hi << 32);
+    return pcg_seed(mix64(key ^ 0x6A09E667F3BCC909ull), mix64(key));
+}
+
 __device__ __forceinline__ uint32_t pixel_stream(const Render_Params& p, uint32_t pix, int& x, int& y) {
     x = p.sx0 + (int)(pix % (uint32_t)p.sw);
     y = p.sy0 + (int)(pix / (uint32_t)p.sw);
@@ -227,7 +245,7 @@ __global__ void sample_tables_kernel(Render_Params p, uint32_t chunk_first, uint
     const uint32_t lp = (uint32_t)(g / rows);
     const uint32_t row = (uint32_t)(g % rows);
     int x, y;
-    Pcg rng = pcg_seed(0, (uint64_t)pixel_stream(p, chunk_first + lp, x, y) | ((uint64_t)p.stream_hi << 32));
+    Pcg rng = pixel_pcg(p, pixel_stream(p, chunk_first + lp, x, y));
     const int spp = p.spp;
     const uint32_t n1d = (uint32_t)p.n1d;
     float2* sm = gen_smem + threadIdx.x;
@@ -325,8 +343,9 @@ camera_kernel(Render_Params p, uint32_t chunk_first, uint32_t chunk_paths, const
     ps.L[slot] = make_float4(0.f, 0.f, 0.f, 0.f);
     ps.info[slot] = 0u;
     // dimensions beyond the sampler budget: an independent pcg stream per sample
-    const Pcg r2 = pcg_seed((uint64_t)k + 1u, (((uint64_t)stream << 20) ^ 0x2545F4914F6CDD1Dull) +
-                                                  (uint64_t)p.stream_hi * 0x9E3779B97F4A7C15ull);
+    const uint64_t seq2 = ((uint64_t)stream << 20) ^ 0x2545F4914F6CDD1Dull;
+    const Pcg r2 = pcg_seed((uint64_t)k + 1u,
+                            p.stream_hi ? mix64(seq2 + (uint64_t)p.stream_hi * 0x9E3779B97F4A7C15ull) : seq2);
     ps.rng[slot] = make_uint4((uint32_t)r2.state, (uint32_t)(r2.state >> 32), (uint32_t)r2.inc,
                               (uint32_t)(r2.inc >> 32));
 }

@@ -361,17 +361,19 @@ def _grid(origin, du, dv, n, hole=None):
     return v, idx
 
 
-def hard_lighting_room(seed=1, width=512, height=512, maxdepth=12, cells=200, light_size=0.1, build=True, threads=0):
+def hard_lighting_room(seed=1, width=512, height=512, maxdepth=12, cells=200, light_size=0.1, light_height=0.6,
+                       build=True, threads=0):
     """The learned-proposal workload: a closed 2 x 2 x 2 room whose six walls
     are tessellated into `cells` x `cells` quads (200: 479,800 triangles, the
     opening cut out) of
     GGX metal (roughness U[0.1, 0.3] per wall, pbrt-v3 remapping), two
     Lambertian boxes inside, and one light_size x light_size area light of
-    radiance 1000 0.3 above the ceiling, which reaches the room only through
-    a 0.1 x 0.1 opening in the ceiling's centre: the opening collimates it
-    into a small pool on the floor, and the rest of the room is lit by what
-    that pool and the glossy walls reflect.  512 x 512, maxdepth 12, Russian
-    roulette from bounce 3."""
+    radiance 1000 light_height above the ceiling, which reaches the room
+    only through a 0.1 x 0.1 opening in the ceiling's centre: the opening
+    collimates it into a pool on the floor (about 0.75 wide, all penumbra),
+    and the rest of the room, the boxes (placed outside the beam) and
+    everything the camera sees, is lit only by what that pool and the glossy
+    walls reflect.  512 x 512, maxdepth 12, Russian roulette from bounce 3."""
     from . import native as N
     from .scene import LIGHT_DTYPE, MATERIAL_DTYPE, CAMERA_DTYPE, default_config
     rng = np.random.default_rng(seed)
@@ -398,7 +400,7 @@ def hard_lighting_room(seed=1, width=512, height=512, maxdepth=12, cells=200, li
         materials.append(m)
         objects.append(make_object(len(s.meshes) - 1, material_type=N.MATERIAL_METAL,
                                    material_index=len(materials) - 1))
-    for center, size in (((0.4, 0, 0.2), (0.5, 0.5, 0.5)), ((-0.4, 0, -0.4), (0.5, 1.0, 0.5))):
+    for center, size in (((0.62, 0, 0.4), (0.45, 0.5, 0.45)), ((-0.62, 0, -0.55), (0.45, 1.0, 0.45))):
         v, i = _box(center, size, rng.uniform(0.0, 30.0))
         s.meshes.append(Mesh(v, i))
         m = np.zeros((), MATERIAL_DTYPE)
@@ -407,7 +409,7 @@ def hard_lighting_room(seed=1, width=512, height=512, maxdepth=12, cells=200, li
         materials.append(m)
         objects.append(make_object(len(s.meshes) - 1, material_type=N.MATERIAL_DIFFUSE,
                                    material_index=len(materials) - 1))
-    lh, ly = 0.5 * light_size, 2.3
+    lh, ly = 0.5 * light_size, 2.0 + light_height
     v, i = _quad((-lh, ly, -lh), (lh, ly, -lh), (lh, ly, lh), (-lh, ly, lh))
     s.meshes.append(Mesh(v, i, uvs=_pbrt_quad_uvs()))
     L = np.zeros((), LIGHT_DTYPE)
