@@ -217,9 +217,12 @@ typedef struct yar_gpu_options {
 } yar_gpu_options;
 
 /* Traversal kernels (identical results, different speed): persistent warps
- * with a 64- or 128-register cap, or one ray per thread.  With AUTO the first
- * large enough batch of each ray kind (and the first render bounce) after a
- * scene upload times all three and keeps the fastest. */
+ * at high occupancy (PERSISTENT_64: a register cap for 8 blocks of 128
+ * threads per SM, 64 registers, for closest-hit rays and for 12 blocks, 40
+ * registers, for any-hit rays), persistent warps with up to 128 registers
+ * (PERSISTENT_128), or one ray per thread.  With AUTO the first large enough
+ * batch of each ray kind (and each render bounce) after a scene upload times
+ * all three and keeps the fastest. */
 #define YAR_TRAVERSAL_AUTO 0
 #define YAR_TRAVERSAL_PERSISTENT_64 1
 #define YAR_TRAVERSAL_PERSISTENT_128 2

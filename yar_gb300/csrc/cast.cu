@@ -110,13 +110,18 @@ __global__ void __launch_bounds__(kCastBlock) cast_per_ray(Device_Scene s, Cast_
 }
 
 // Persistent launch shape, measured on GB300 with the 2.42M-triangle ray-cast
-// workload (16M + 16M incoherent rays): 8 resident blocks of 128 threads per
-// SM (64 registers) beat 4 and 6 blocks (102 and 80 registers); descending to
-// a leaf per step (while-while) beat one node per step and four nodes per
-// step; the local-memory stack beat an 8- or 16-entry shared-memory stack
-// with local overflow (770 vs 710 Mrays/s for the best shared variant).
+// workload (16M + 16M incoherent rays).  High-occupancy variant: closest hit
+// at 8 resident blocks of 128 threads per SM (64 registers: 25.3 ms, against
+// 25.2 ms at 10 blocks, 26.4 ms at 12, 31.1 ms at 16), any hit at 12 blocks
+// (40 registers: 12.6 ms, against 14.3 ms at 8, 13.3 ms at 10, 14.1 ms at
+// 16).  Descending to a leaf per step (while-while) beat one node per step
+// and four nodes per step; testing all of a leaf's triangles in one step was
+// slower (27.0 against 25.3 ms); the local-memory stack beat an 8- or
+// 16-entry shared-memory stack with local overflow.
 constexpr int kWhileWhile = 1 << 30;
 constexpr int kSharedStackEntries = 0;
+template <bool ANY>
+constexpr int kHighOccupancyBlocks = ANY ? 12 : 8;
 
 template <class Kernel>
 int resident_grid(Kernel kernel, int& cache) {
@@ -146,7 +151,7 @@ cudaError_t launch(const Device_Scene& s, const Cast_Args& a, int kernel, cudaSt
         k<<<resident_grid(k, grid), kCastBlock, 0, stream>>>(s, a);
     } else {
         static int grid = 0;
-        auto k = cast_persistent<ANY, 8, kWhileWhile, kSharedStackEntries>;
+        auto k = cast_persistent<ANY, kHighOccupancyBlocks<ANY>, kWhileWhile, kSharedStackEntries>;
         k<<<resident_grid(k, grid), kCastBlock, 0, stream>>>(s, a);
     }
     return cudaGetLastError();

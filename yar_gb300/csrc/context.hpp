@@ -112,10 +112,11 @@ struct Cast_Args {
     // any hit
     uint8_t* occluded = nullptr;
 };
-// Traversal kernels: persistent warps capped at 64 registers (8 blocks per
-// SM), persistent warps capped at 128 registers (4 blocks per SM), one ray per
-// thread.  All give identical results; which is fastest depends on the scene
-// and the rays, so it is chosen per scene by timing (tune_cast).
+// Traversal kernels: persistent warps at high occupancy (closest hit 8
+// blocks per SM / 64 registers, any hit 12 blocks / 40 registers), persistent
+// warps capped at 128 registers (4 blocks per SM), one ray per thread.  All
+// give identical results; which is fastest depends on the scene and the rays,
+// so it is chosen per scene by timing (tune_cast).
 enum Cast_Kernel { kCastPersistent64 = 0, kCastPersistent128 = 1, kCastPerRay = 2, kCastKernelCount = 3 };
 cudaError_t launch_extend(const Device_Scene& s, const Cast_Args& a, int kernel, cudaStream_t stream);
 cudaError_t launch_shadow(const Device_Scene& s, const Cast_Args& a, int kernel, cudaStream_t stream);
