@@ -3,8 +3,8 @@
 // tensor memory), with hand-written inference and training kernels.
 //
 // Network: 128 inputs (16-frequency sin/cos encoding of the normalised
-// position, frequencies pi 2^(k/3), k = 0..15: 96, shading normal 3, outgoing direction 3, zeros, input 127 =
-// constant 1) -> 3 hidden layers of 64 ReLU units (unit 63 of each is the
+// position, frequencies pi 2^(k/3), k = 0..15: 96; shading normal 3,
+// outgoing direction 3, zeros, input 127 = constant 1) -> 3 hidden layers of 64 ReLU units (unit 63 of each is the
 // constant 1, so every bias is an ordinary weight column) -> 64 outputs, of
 // which 40 parameterise a mixture of 8 von Mises-Fisher lobes in world space:
 // per lobe an unnormalised mean direction m (3), log-concentration r and a
@@ -90,26 +90,42 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-// Input feature j of a row (j < 96: sin/cos of pi 2^(k/3) p, k = j / 6:
-// 16 frequencies from 1 to 32 half-periods across the scene box).
-__device__ __forceinline__ float feature(int j, float3 p, float3 nrm, float3 wo, bool valid) {
-    if (!valid) return 0.f;
+// Encoding frequencies 2^(k/3), k = 0..15 (1 to 32 half-periods across the
+// scene box), as float32 values of exp2(k * (1/3)).
+__constant__ float kFreq[16] = {1.000000000e+00f, 1.259921074e+00f, 1.587401032e+00f, 2.000000000e+00f,
+                                2.519842148e+00f, 3.174802303e+00f, 4.000000000e+00f, 5.039684772e+00f,
+                                6.349604607e+00f, 8.000000000e+00f, 1.007936954e+01f, 1.269920921e+01f,
+                                1.600000000e+01f, 2.015873909e+01f, 2.539842224e+01f, 3.200000000e+01f};
+
+// Input features j and j + 1 (j even).  j < 96: sin and cos of
+// pi 2^(k/3) p_axis, k = j / 6, axis = (j % 6) / 2 (one sincospif per pair);
+// then the normal, wo, zeros and the constant 1 at 127.
+__device__ __forceinline__ void feature_pair(int j, float3 p, float3 nrm, float3 wo, bool valid, float& f0,
+                                             float& f1) {
+    if (!valid) {
+        f0 = f1 = 0.f;
+        return;
+    }
     if (j < 96) {
         const int k = j / 6, m = j % 6;
         const float c = (m < 2) ? p.x : (m < 4 ? p.y : p.z);
-        const float x = c * exp2f((float)k * (1.f / 3.f));
-        return (m & 1) ? cospif(x) : sinpif(x);
+        sincospif(c * kFreq[k], &f0, &f1);
+        return;
     }
-    switch (j) {
-        case 96: return nrm.x;
-        case 97: return nrm.y;
-        case 98: return nrm.z;
-        case 99: return wo.x;
-        case 100: return wo.y;
-        case 101: return wo.z;
-        case 127: return 1.f;
-        default: return 0.f;
-    }
+    auto fixed = [&](int i) -> float {
+        switch (i) {
+            case 96: return nrm.x;
+            case 97: return nrm.y;
+            case 98: return nrm.z;
+            case 99: return wo.x;
+            case 100: return wo.y;
+            case 101: return wo.z;
+            case 127: return 1.f;
+            default: return 0.f;
+        }
+    };
+    f0 = fixed(j);
+    f1 = fixed(j + 1);
 }
 
 // Transposed tile write: element (feature f, batch row r) of a tile with
@@ -269,7 +285,7 @@ __global__ void __launch_bounds__(kRows, 1) mlp_kernel(Mlp_Args a) {
         for (int c = 0; c < 16; c++) {
             float v[8];
 #pragma unroll
-            for (int i = 0; i < 8; i++) v[i] = feature(8 * c + i, p, nrm, wo, valid);
+            for (int i = 0; i < 8; i += 2) feature_pair(8 * c + i, p, nrm, wo, valid, v[i], v[i + 1]);
             store_row8(R0, tid, 8 * c, kIn, v);
             if (TRAIN) {
 #pragma unroll
@@ -559,7 +575,7 @@ cudaError_t guide_infer(yar_gpu_ctx* ctx, const float4* queries, uint32_t n_max,
     a.lobes = lobes;
     a.err = ctx->d_error;
     const uint32_t tiles = (n_max + kRows - 1) / kRows;
-    const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sm_count() * 2u);
+    const uint32_t grid = std::min<uint32_t>(tiles, (uint32_t)sm_count() * 3u);  // 3 CTAs fit per SM
     mlp_kernel<false><<<grid, kRows, kInMisc + 64, st>>>(a);
     return cudaGetLastError();
 }

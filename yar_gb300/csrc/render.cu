@@ -262,7 +262,7 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
 // the chunking).
 namespace {
 
-__device__ __align__(256) unsigned char g_static_arena[YAR_GPU_STATIC_ARENA_BYTES];
+static __device__ __align__(256) unsigned char g_static_arena[YAR_GPU_STATIC_ARENA_BYTES];
 
 std::mutex g_arena_mutex;
 unsigned char* g_arena_address[64] = {};  // device address of g_static_arena per device ordinal
