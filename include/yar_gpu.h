@@ -400,6 +400,16 @@ int yar_build_scene_kdtree(const float* object_bounds /* 6 floats per object, wo
                            float bounds_out[6], yar_kd_node** nodes_out, uint32_t* node_count_out);
 void yar_free_nodes(yar_kd_node* nodes);
 
+/* kd-tree cache files in the reference's format (KdTree::save / KdTree::load,
+ * src/ref/kdtree.cpp:111-160): bounds, 64-bit geometry hash, node count,
+ * nodes.  A file the reference wrote loads here and vice versa, so trees
+ * built once (by either builder) need not be rebuilt.  The read node array
+ * is released with yar_free_nodes; trailing bytes are an error. */
+int yar_read_kdtree_cache(const char* path, float bounds_out[6], uint64_t* hash_out,
+                          yar_kd_node** nodes_out, uint32_t* node_count_out);
+int yar_write_kdtree_cache(const char* path, const float bounds[6], uint64_t hash,
+                           const yar_kd_node* nodes, uint32_t node_count);
+
 /* transform_bounding_box (src/lib/matrix.cpp:391-402) of a tree's bounds, for
  * the scene-tree primitive bounds (src/ref/kdtree_builder.cpp:445-452) */
 void yar_transform_bounds(const float object_to_world[12], const float bounds_in[6], float bounds_out[6]);

@@ -65,6 +65,7 @@ struct Args {
     bool compress = false;
     float variance = 0.f;
     std::string input_file;
+    std::string cache_dir;
 };
 
 Args parse(int argc, char** argv) {
@@ -79,6 +80,7 @@ Args parse(int argc, char** argv) {
         else if (s == "--compress") a.compress = true;
         else if (s.rfind("--variance=", 0) == 0) a.variance = (float)atof(s.c_str() + 11);
         else if (s.rfind("--input=", 0) == 0) a.input_file = s.substr(8);
+        else if (s.rfind("--cache-dir=", 0) == 0) a.cache_dir = s.substr(12);
         else a.pos.push_back(s);
     }
     if (a.threads <= 0) a.threads = std::max(1u, std::thread::hardware_concurrency());
@@ -388,6 +390,11 @@ int cmd_build(const Args& a) {
     fs_scene.scene_nodes.resize(rs.scene_kdtree.nodes.size());
     memcpy(fs_scene.scene_nodes.data(), rs.scene_kdtree.nodes.data(), rs.scene_kdtree.nodes.size() * 8);
     if (!yfs::write(a.pos[1], fs_scene)) return 1;
+    if (!a.cache_dir.empty()) {  // the reference's own cache files (KdTree::save)
+        for (size_t i = 0; i < rs.kdtrees.size(); i++)
+            rs.kdtrees[i].save(a.cache_dir + "/mesh_" + std::to_string(i) + ".kdtree");
+        rs.scene_kdtree.save(a.cache_dir + "/scene.kdtree");
+    }
     printf("{\"mesh_build_seconds\": %.3f, \"scene_build_seconds\": %.3f, \"threads\": %d}\n",
            mesh_seconds, scene_seconds, a.threads);
     return 0;

@@ -140,6 +140,21 @@ def cornell_ggx_64():
     np.savez_compressed(os.path.join(HERE, "cornell_ggx_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def kdtree_cache_files():
+    """The reference's kd-tree cache files (KdTree::save) of the raycast_small
+    scene's first two meshes and of its scene tree."""
+    flat = FlatScene.read(os.path.join(HERE, "raycast_small.yfs"))
+    out_dir = os.path.join(HERE, "kdtree_cache")
+    os.makedirs(out_dir, exist_ok=True)
+    with tempfile.TemporaryDirectory() as d:
+        a, b = os.path.join(d, "in.yfs"), os.path.join(d, "out.yfs")
+        flat.write(a)
+        oracle._ref("build", a, b, "--threads=2", "--cache-dir=" + d)
+        for name in ("mesh_0.kdtree", "mesh_1.kdtree", "scene.kdtree"):
+            with open(os.path.join(d, name), "rb") as src, open(os.path.join(out_dir, name), "wb") as dst:
+                dst.write(src.read())
+
+
 def exr_files():
     """The reference's EXR writer (write_openexr_image) on the C1 golden image
     (uncompressed and ZIP) and on an image of special values (exact half
@@ -167,7 +182,7 @@ if __name__ == "__main__":
     if not oracle.have_reference():
         sys.exit("oracle/_ref/yar_ref is not built (oracle/build_ref.sh)")
     which = sys.argv[1:] or ["raycast_small", "transform_small", "kdtree_regression", "cornell_c1_64",
-                             "cornell_ggx_64", "exr_files"]
+                             "cornell_ggx_64", "exr_files", "kdtree_cache_files"]
     for name in which:
         globals()[name]()
         print("wrote", name)

@@ -69,3 +69,35 @@ def test_leaf_layout():
         else:
             i += 1
     assert seen_multi
+
+
+def test_kdtree_cache_files_match_the_reference(tmp_path):
+    """Cache files the reference wrote (KdTree::save) read back as the nodes
+    and bounds of the reference-built scene, and writing those nodes gives
+    byte-identical files."""
+    import os
+    from yar_gb300 import native
+    s = FlatScene.read(golden("raycast_small.yfs"))
+    cache = golden("kdtree_cache")
+    for name, bounds, nodes in (("mesh_0.kdtree", s.meshes[0].bounds, s.meshes[0].nodes),
+                                ("mesh_1.kdtree", s.meshes[1].bounds, s.meshes[1].nodes),
+                                ("scene.kdtree", s.scene_bounds, s.scene_nodes)):
+        b, n, h = native.read_kdtree_cache(os.path.join(cache, name))
+        assert h == 0
+        assert np.array_equal(b.view(np.uint32), np.asarray(bounds, np.float32).view(np.uint32))
+        assert np.array_equal(n, nodes)
+        out = os.path.join(tmp_path, name)
+        native.write_kdtree_cache(out, b, n)
+        assert open(out, "rb").read() == open(os.path.join(cache, name), "rb").read()
+    # a whole scene round trip through the cache directory
+    s.write_kdtree_caches(str(tmp_path / "all"))
+    t = FlatScene.read(golden("raycast_small.yfs")).read_kdtree_caches(str(tmp_path / "all"))
+    for m, mm in zip(s.meshes, t.meshes):
+        assert np.array_equal(m.nodes, mm.nodes)
+    # truncated and missing files are refused
+    bad = os.path.join(tmp_path, "bad.kdtree")
+    open(bad, "wb").write(open(os.path.join(cache, "mesh_0.kdtree"), "rb").read()[:-3])
+    with pytest.raises(native.YarError):
+        native.read_kdtree_cache(bad)
+    with pytest.raises(native.YarError):
+        native.read_kdtree_cache(os.path.join(tmp_path, "missing.kdtree"))

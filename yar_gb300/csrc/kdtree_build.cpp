@@ -21,6 +21,7 @@
 #include <atomic>
 #include <cmath>
 #include <cstdint>
+#include <cstdio>
 #include <cstdlib>
 #include <cstring>
 #include <future>
@@ -417,4 +418,54 @@ extern "C" void yar_transform_bounds(const float m[12], const float in[6], float
     }
     memcpy(out, b.mn, 12);
     memcpy(out + 3, b.mx, 12);
+}
+
+// ---------------------------------------------------------------- cache files
+// The reference's kd-tree cache file (KdTree::save / KdTree::load,
+// src/ref/kdtree.cpp:111-160): bounds (min xyz, max xyz as 6 float32),
+// the 64-bit geometry hash, the 32-bit node count, then the 8-byte nodes,
+// all little-endian.  The reference writes hash 0 (its hash functions are
+// stubs returning 0, src/ref/kdtree.cpp:205-215); `hash_out` returns what the
+// file holds and the writer takes the value to store.
+extern "C" int yar_read_kdtree_cache(const char* path, float bounds_out[6], uint64_t* hash_out,
+                                     yar_kd_node** nodes_out, uint32_t* node_count_out) {
+    if (!path || !bounds_out || !nodes_out || !node_count_out) return YAR_ERR_INVALID;
+    *nodes_out = nullptr;
+    *node_count_out = 0;
+    FILE* f = fopen(path, "rb");
+    if (!f) return YAR_ERR_IO;
+    float bounds[6];
+    uint64_t hash = 0;
+    uint32_t count = 0;
+    int rc = YAR_OK;
+    if (fread(bounds, 4, 6, f) != 6 || fread(&hash, 8, 1, f) != 1 || fread(&count, 4, 1, f) != 1) rc = YAR_ERR_IO;
+    if (rc == YAR_OK && (count == 0 || count > (1u << 31) / sizeof(yar_kd_node))) rc = YAR_ERR_INVALID;
+    yar_kd_node* nodes = nullptr;
+    if (rc == YAR_OK) {
+        nodes = static_cast<yar_kd_node*>(malloc((size_t)count * sizeof(yar_kd_node)));
+        if (!nodes) rc = YAR_ERR_NOMEM;
+    }
+    if (rc == YAR_OK && fread(nodes, sizeof(yar_kd_node), count, f) != count) rc = YAR_ERR_IO;
+    if (rc == YAR_OK && fgetc(f) != EOF) rc = YAR_ERR_INVALID;  // trailing bytes: not a cache file
+    fclose(f);
+    if (rc != YAR_OK) {
+        free(nodes);
+        return rc;
+    }
+    memcpy(bounds_out, bounds, sizeof(bounds));
+    if (hash_out) *hash_out = hash;
+    *nodes_out = nodes;
+    *node_count_out = count;
+    return YAR_OK;
+}
+
+extern "C" int yar_write_kdtree_cache(const char* path, const float bounds[6], uint64_t hash,
+                                      const yar_kd_node* nodes, uint32_t node_count) {
+    if (!path || !bounds || !nodes || node_count == 0) return YAR_ERR_INVALID;
+    FILE* f = fopen(path, "wb");
+    if (!f) return YAR_ERR_IO;
+    bool ok = fwrite(bounds, 4, 6, f) == 6 && fwrite(&hash, 8, 1, f) == 1 && fwrite(&node_count, 4, 1, f) == 1 &&
+              fwrite(nodes, sizeof(yar_kd_node), node_count, f) == node_count;
+    ok = (fclose(f) == 0) && ok;
+    return ok ? YAR_OK : YAR_ERR_IO;
 }

@@ -165,6 +165,9 @@ EXPORTS = {
     "yar_build_scene_kdtree": (C.c_int, [C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.POINTER(C.c_void_p),
                                          C.POINTER(C.c_uint32)]),
     "yar_free_nodes": (None, [C.c_void_p]),
+    "yar_read_kdtree_cache": (C.c_int, [C.c_char_p, C.POINTER(C.c_float), C.POINTER(C.c_uint64),
+                                        C.POINTER(C.c_void_p), C.POINTER(C.c_uint32)]),
+    "yar_write_kdtree_cache": (C.c_int, [C.c_char_p, C.POINTER(C.c_float), C.c_uint64, C.c_void_p, C.c_uint32]),
     "yar_transform_bounds": (None, [C.c_void_p, C.c_void_p, C.c_void_p]),
 }
 
@@ -225,6 +228,28 @@ def build_scene_kdtree(object_bounds):
     out = np.ctypeslib.as_array(C.cast(nodes, C.POINTER(C.c_uint32)), shape=(count.value * 2,)).copy()
     lib().yar_free_nodes(nodes)
     return np.array(bounds, dtype=np.float32), out.reshape(-1, 2)
+
+
+def read_kdtree_cache(path):
+    """A kd-tree cache file in the reference's format: (bounds (6,), nodes (N, 2) uint32, hash)."""
+    bounds = (C.c_float * 6)()
+    h = C.c_uint64()
+    nodes = C.c_void_p()
+    count = C.c_uint32()
+    rc = lib().yar_read_kdtree_cache(os.fsencode(path), bounds, C.byref(h), C.byref(nodes), C.byref(count))
+    if rc != YAR_OK:
+        raise YarError(rc, "yar_read_kdtree_cache(%s)" % path)
+    out = np.ctypeslib.as_array(C.cast(nodes, C.POINTER(C.c_uint32)), shape=(count.value * 2,)).copy()
+    lib().yar_free_nodes(nodes)
+    return np.array(bounds, dtype=np.float32), out.reshape(-1, 2), int(h.value)
+
+
+def write_kdtree_cache(path, bounds, nodes, hash_value=0):
+    b = (C.c_float * 6)(*[float(x) for x in np.asarray(bounds, np.float32).reshape(6)])
+    n = np.ascontiguousarray(nodes, dtype=np.uint32).reshape(-1, 2)
+    rc = lib().yar_write_kdtree_cache(os.fsencode(path), b, int(hash_value), _ptr(n), n.shape[0])
+    if rc != YAR_OK:
+        raise YarError(rc, "yar_write_kdtree_cache(%s)" % path)
 
 
 def transform_bounds(object_to_world, bounds):

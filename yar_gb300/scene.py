@@ -111,6 +111,25 @@ class FlatScene:
         self.build_scene_kdtree()
         return self
 
+    # ---- kd-tree cache files (the reference's KdTree::save format) ----
+    def write_kdtree_caches(self, directory):
+        """mesh_<i>.kdtree per mesh and scene.kdtree, loadable by the reference."""
+        import os
+        os.makedirs(directory, exist_ok=True)
+        for i, m in enumerate(self.meshes):
+            native.write_kdtree_cache(os.path.join(directory, "mesh_%d.kdtree" % i), m.bounds, m.nodes)
+        native.write_kdtree_cache(os.path.join(directory, "scene.kdtree"), self.scene_bounds, self.scene_nodes)
+
+    def read_kdtree_caches(self, directory):
+        """Trees from cache files (written by write_kdtree_caches or by the
+        reference) instead of building them.  The reference's files carry no
+        real geometry hash, so a cache must belong to the same meshes."""
+        import os
+        for i, m in enumerate(self.meshes):
+            m.bounds, m.nodes, _ = native.read_kdtree_cache(os.path.join(directory, "mesh_%d.kdtree" % i))
+        self.scene_bounds, self.scene_nodes, _ = native.read_kdtree_cache(os.path.join(directory, "scene.kdtree"))
+        return self
+
     def build_scene_kdtree(self):
         ob = np.stack([native.transform_bounds(o["object_to_world"], self.meshes[o["mesh_index"]].bounds)
                        for o in self.objects])
