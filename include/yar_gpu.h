@@ -121,18 +121,20 @@ typedef struct yar_object_desc {
     float object_to_world_normal[12];
 } yar_object_desc;
 
-/* Constant-parameter materials (Diffuse/Metal/Glass_Material, src/lib/material.h:58-150).
- * Textured parameters are outside the implemented path (YAR_ERR_UNSUPPORTED). */
+/* Constant-parameter materials (Perfect_Reflector/Perfect_Refractor/Diffuse/Metal/
+ * Glass_Material, src/lib/material.h:48-150).  Glass with roughness 0 scatters as
+ * the reference's smooth (delta) glass.  Textured parameters and bump maps are
+ * outside the implemented path (YAR_ERR_UNSUPPORTED). */
 typedef struct yar_material_desc {
-    uint32_t type;              /* YAR_MATERIAL_DIFFUSE / METAL / GLASS */
-    float reflectance[3];       /* diffuse: reflectance; glass: reflectance (kr) */
+    uint32_t type;              /* YAR_MATERIAL_PERFECT_REFLECTOR / PERFECT_REFRACTOR / DIFFUSE / METAL / GLASS */
+    float reflectance[3];       /* perfect reflector, diffuse: reflectance; glass: reflectance (kr) */
     float transmittance[3];     /* glass: transmittance (kt) */
     float eta[3];               /* metal */
     float k[3];                 /* metal */
     float eta_i;                /* metal: IOR of the adjacent dielectric */
     float u_roughness;          /* metal u roughness; glass roughness */
     float v_roughness;          /* metal */
-    float index_of_refraction;  /* glass */
+    float index_of_refraction;  /* glass, perfect refractor */
     int32_t roughness_is_alpha;
 } yar_material_desc;
 

@@ -162,7 +162,7 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         memcpy(fm.nodes.data(), t.nodes.data(), t.nodes.size() * 8);
         out.meshes.push_back(std::move(fm));
     }
-    // materials: diffuse, metal, glass flattened in that order
+    // materials: diffuse, metal, glass, perfect reflector, perfect refractor flattened in that order
     std::vector<int> diffuse_index, metal_index, glass_index;
     for (const Diffuse_Material& m : ctx.materials.diffuse) {
         yar_material_desc d{};
@@ -195,6 +195,21 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         glass_index.push_back((int)out.materials.size());
         out.materials.push_back(d);
     }
+    std::vector<int> reflector_index, refractor_index;
+    for (const Perfect_Reflector_Material& m : ctx.materials.perfect_reflector) {
+        yar_material_desc d{};
+        d.type = YAR_MATERIAL_PERFECT_REFLECTOR;
+        constant_rgb(m.reflectance, d.reflectance);
+        reflector_index.push_back((int)out.materials.size());
+        out.materials.push_back(d);
+    }
+    for (const Perfect_Refractor_Material& m : ctx.materials.perfect_refractor) {
+        yar_material_desc d{};
+        d.type = YAR_MATERIAL_PERFECT_REFRACTOR;
+        constant_float(m.index_of_refraction, &d.index_of_refraction);
+        refractor_index.push_back((int)out.materials.size());
+        out.materials.push_back(d);
+    }
     for (const Scene_Object& o : scene.objects) {
         yar_object_desc d{};
         d.mesh_index = o.geometry.index;
@@ -203,6 +218,10 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         if (o.material.type == Material_Type::diffuse) d.material_index = diffuse_index[o.material.index];
         else if (o.material.type == Material_Type::metal) d.material_index = metal_index[o.material.index];
         else if (o.material.type == Material_Type::glass) d.material_index = glass_index[o.material.index];
+        else if (o.material.type == Material_Type::perfect_reflector)
+            d.material_index = reflector_index[o.material.index];
+        else if (o.material.type == Material_Type::perfect_refractor)
+            d.material_index = refractor_index[o.material.index];
         else if (o.material.type != Material_Type::null_material)
             fprintf(stderr, "warning: material type %u not flattened\n", (unsigned)o.material.type);
         d.area_light_type = (uint32_t)o.area_light.type;
@@ -557,6 +576,16 @@ int cmd_render_yfs(const Args& a) {
             m.roughness_is_alpha = d.roughness_is_alpha != 0;
             scene.materials.glass.push_back(m);
             handles.push_back({Material_Type::glass, (int)scene.materials.glass.size() - 1});
+        } else if (d.type == YAR_MATERIAL_PERFECT_REFLECTOR) {
+            Perfect_Reflector_Material m;
+            set_constant_parameter(m.reflectance, ColorRGB(d.reflectance));
+            scene.materials.perfect_reflector.push_back(m);
+            handles.push_back({Material_Type::perfect_reflector, (int)scene.materials.perfect_reflector.size() - 1});
+        } else if (d.type == YAR_MATERIAL_PERFECT_REFRACTOR) {
+            Perfect_Refractor_Material m;
+            set_constant_parameter(m.index_of_refraction, d.index_of_refraction);
+            scene.materials.perfect_refractor.push_back(m);
+            handles.push_back({Material_Type::perfect_refractor, (int)scene.materials.perfect_refractor.size() - 1});
         } else {
             fprintf(stderr, "unsupported material type %u\n", d.type);
             return 1;

@@ -1067,24 +1067,71 @@ static void camera_ray(const yar_camera_desc* c, float fx, float fy, v3* o, v3* 
     *d = xform_vector(c->camera_to_world, dir);
 }
 
-/* trace_path, src/ref/path_tracing.cpp:11-133 (non-delta materials) */
+/* check_for_delta_scattering_event / get_*_info, src/ref/delta_scattering.cpp:27-97, :252-324
+ * (perfect reflector, perfect refractor, smooth glass; no nested dielectrics,
+ * no bump maps).  Returns 1 and the delta direction and attenuation for a delta
+ * material, 2 for a delta material without a direction, 0 otherwise. */
+static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, float u, v3* dir, col* atten) {
+    if (sc->material_type != YAR_MATERIAL_PERFECT_REFLECTOR && sc->material_type != YAR_MATERIAL_PERFECT_REFRACTOR &&
+        sc->material_type != YAR_MATERIAL_GLASS)
+        return 0;
+    const yar_material_desc* m = &s->materials[sc->material_index];
+    if (sc->material_type == YAR_MATERIAL_GLASS && m->u_roughness > 0.f) return 0;
+    *atten = mkc(1, 1, 1);
+    if (sc->material_type == YAR_MATERIAL_PERFECT_REFLECTOR) {
+        *dir = reflect3(sc->wo, sc->normal);
+        *atten = ldc(m->reflectance);
+        return 1;
+    }
+    const int enter = !sc->flipped;
+    if (sc->material_type == YAR_MATERIAL_PERFECT_REFRACTOR) {
+        const float eta = enter ? 1.f / m->index_of_refraction : m->index_of_refraction;
+        /* Total internal reflection leaves the reference's direction at its
+         * zero default (an ASSERT in debug builds); the zero-length ray finds
+         * nothing and the path ends.  Reported here as 2: no delta ray. */
+        if (!refract3(sc->wo, sc->normal, eta, dir)) {
+            *dir = mk3(0, 0, 0);
+            return 2;
+        }
+        return 1;
+    }
+    const float eta_t_over_i = enter ? m->index_of_refraction : 1.f / m->index_of_refraction;
+    const float cos_i = dot3(sc->normal, sc->wo);
+    const float fresnel = dielectric_fresnel(cos_i, eta_t_over_i);
+    if (u < fresnel) {
+        *dir = reflect3(sc->wo, sc->normal);
+        *atten = ldc(m->reflectance);
+    } else {
+        const float eta = 1.f / eta_t_over_i;
+        *atten = mulcs(ldc(m->transmittance), eta * eta);
+        refract3(sc->wo, sc->normal, eta, dir);
+    }
+    return 1;
+}
+
+/* trace_path, src/ref/path_tracing.cpp:11-133 */
 static int trace_path(const yar_flat_scene* s, v3 ro, v3 rd, sampler_view* sv, col* radiance) {
     const yar_render_config* cfg = &s->config;
     const int total_lights = (int)(s->rect_light_count + s->other_light_count);
     col coeff = mkc(1, 1, 1), L = mkc(0, 0, 0);
     int bounce = 0;
+    int traced_by_delta_bounce = 0;
+    hit_state h;
+    shading_ctx sc;
+    int hit = 0;
     for (;;) {
-        hit_state h;
-        int hit = trace_closest(s, ro, rd, &h);
-        if (hit < 0) return YAR_ERR_CAPACITY;
-        shading_ctx sc;
-        if (hit) init_shading(s, rd, h.object, h.prim, h.b, &sc);
-        if (bounce == 0) {
-            if (hit && sc.light_type == YAR_LIGHT_DIFFUSE_RECTANGULAR)
-                L = addc(L, mulc(coeff, ldc(s->rect_lights[sc.light_index].emitted_radiance)));
-            if (cfg->max_light_bounces == 0) break;
+        if (!traced_by_delta_bounce) {
+            hit = trace_closest(s, ro, rd, &h);
+            if (hit < 0) return YAR_ERR_CAPACITY;
+            if (hit) init_shading(s, rd, h.object, h.prim, h.b, &sc);
+            if (bounce == 0) {
+                if (hit && sc.light_type == YAR_LIGHT_DIFFUSE_RECTANGULAR)
+                    L = addc(L, mulc(coeff, ldc(s->rect_lights[sc.light_index].emitted_radiance)));
+                if (cfg->max_light_bounces == 0) break;
+            }
+            if (!hit || sc.light_type != YAR_LIGHT_NULL) break;
         }
-        if (!hit || sc.light_type != YAR_LIGHT_NULL) break;
+        traced_by_delta_bounce = 0;
 
         float u_scatter = next1d(sv);
         float u_light_index = next1d(sv);
@@ -1095,23 +1142,43 @@ static int trace_path(const yar_flat_scene* s, v3 ro, v3 rd, sampler_view* sv, c
         next2d(sv, &un0, &un1);
 
         if (sc.material_type == YAR_MATERIAL_NULL) return YAR_ERR_UNSUPPORTED;
-        bsdf_t f;
-        int rc = make_bsdf(s, &sc, &f);
-        if (rc != YAR_OK) return rc;
-        /* estimate_direct_lighting_from_single_sample, src/ref/direct_lighting.cpp:522-578 */
-        int light_index = (int)(u_light_index * (float)total_lights);
-        col direct = mulcs(direct_rect(s, &sc, &f, light_index, ul0, ul1, ub0, ub1, u_scatter), (float)total_lights);
-        L = addc(L, mulc(coeff, direct));
+        v3 ddir;
+        col datten;
+        const int delta = delta_scattering(s, &sc, u_scatter, &ddir, &datten);
+        if (delta == 2) break; /* perfect refractor at total internal reflection */
+        if (!delta) {
+            bsdf_t f;
+            int rc = make_bsdf(s, &sc, &f);
+            if (rc != YAR_OK) return rc;
+            /* estimate_direct_lighting_from_single_sample, src/ref/direct_lighting.cpp:522-578 */
+            int light_index = (int)(u_light_index * (float)total_lights);
+            col direct = mulcs(direct_rect(s, &sc, &f, light_index, ul0, ul1, ub0, ub1, u_scatter), (float)total_lights);
+            L = addc(L, mulc(coeff, direct));
 
-        bounce++;
-        if (bounce == cfg->max_light_bounces) break;
-        v3 wi;
-        float pdf;
-        col fv = bsdf_sample(&f, un0, un1, u_scatter_next, sc.wo, &wi, &pdf);
-        if (blackc(fv)) break;
-        coeff = mulc(coeff, mulcs(fv, fabsf(dot3(sc.normal, wi)) / (pdf * 1.f)));
-        ro = origin_for_direction(&sc, wi);
-        rd = wi;
+            bounce++;
+            if (bounce == cfg->max_light_bounces) break;
+            v3 wi;
+            float pdf;
+            col fv = bsdf_sample(&f, un0, un1, u_scatter_next, sc.wo, &wi, &pdf);
+            if (blackc(fv)) break;
+            coeff = mulc(coeff, mulcs(fv, fabsf(dot3(sc.normal, wi)) / (pdf * 1.f)));
+            ro = origin_for_direction(&sc, wi);
+            rd = wi;
+        } else {
+            /* the delta ray is traced at once; light it reaches counts (path_tracing.cpp:76-107) */
+            ro = origin_for_direction(&sc, ddir);
+            rd = ddir;
+            hit = trace_closest(s, ro, rd, &h);
+            if (hit < 0) return YAR_ERR_CAPACITY;
+            if (hit) init_shading(s, rd, h.object, h.prim, h.b, &sc);
+            coeff = mulc(coeff, datten);
+            if (hit && sc.light_type == YAR_LIGHT_DIFFUSE_RECTANGULAR)
+                L = addc(L, mulc(coeff, ldc(s->rect_lights[sc.light_index].emitted_radiance)));
+            bounce++;
+            if (bounce == cfg->max_light_bounces) break;
+            if (!hit || sc.light_type != YAR_LIGHT_NULL) break;
+            traced_by_delta_bounce = 1;
+        }
         if (bounce >= cfg->russian_roulette_bounce_count_threshold) {
             float u_term = next1d(sv);
             float max_coeff = fmaxf_std(coeff.r, fmaxf_std(coeff.g, coeff.b));
@@ -1282,8 +1349,9 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
     if (cfg->rendering_algorithm != 1 || cfg->pixel_filter_type != 0) return YAR_ERR_UNSUPPORTED;
     for (uint32_t i = 0; i < s->material_count; i++) {
         uint32_t t = s->materials[i].type;
-        if (t != YAR_MATERIAL_DIFFUSE && t != YAR_MATERIAL_METAL && t != YAR_MATERIAL_GLASS) return YAR_ERR_UNSUPPORTED;
-        if (t == YAR_MATERIAL_GLASS && !(s->materials[i].u_roughness > 0.f)) return YAR_ERR_UNSUPPORTED;
+        if (t != YAR_MATERIAL_DIFFUSE && t != YAR_MATERIAL_METAL && t != YAR_MATERIAL_GLASS &&
+            t != YAR_MATERIAL_PERFECT_REFLECTOR && t != YAR_MATERIAL_PERFECT_REFRACTOR)
+            return YAR_ERR_UNSUPPORTED;
     }
     if (s->other_light_count) return YAR_ERR_UNSUPPORTED;
     render_job J;

@@ -2,8 +2,9 @@
  * yar_oracle.h - TEST INFRASTRUCTURE ONLY.
  *
  * A plain-C CPU restatement of the reference renderer's hot path (kd-tree
- * traversal, watertight intersection, sampler, shading, BSDFs, MIS direct
- * lighting and the path loop of kennyalive/YAR src/ref/*), used by tests/,
+ * traversal, watertight intersection, sampler, shading, BSDFs, delta
+ * scattering, MIS direct lighting and the path loop of kennyalive/YAR
+ * src/ref), used by tests/,
  * __graft_entry__.smoke() and the cpu_baseline leg of bench.py as the checker
  * of the CUDA path.  The product never links or calls it.
  *

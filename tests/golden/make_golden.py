@@ -20,6 +20,15 @@ Fixtures
                              and builder at 64x64, 16 spp, maxdepth 8, seed 1,
                              and the reference's FP32 render of it.
   cornell_ggx_64.yfs / .npz  the same with a GGX metal box and a rough-glass box.
+  cornell_delta_64.yfs / .npz the same with a mirror box and a smooth-glass box
+                             (delta scattering) and a second light above the
+                             ceiling, seed 5.
+  cornell_refractor_64.yfs / .npz  cornell_delta_64 with the ceiling turned
+                             into a perfect refractor (IOR 1/1.5 on its
+                             upward-facing normal: no total internal
+                             reflection from the room) that lets the upper
+                             light in, rendered by the reference from the flat
+                             scene (pbrt has no perfect refractor).
 """
 import os
 import re
@@ -140,6 +149,30 @@ def cornell_ggx_64():
     np.savez_compressed(os.path.join(HERE, "cornell_ggx_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def cornell_delta_64():
+    """The Cornell box with a mirror box, a smooth-glass box and a light above
+    the ceiling."""
+    with tempfile.TemporaryDirectory() as d:
+        pbrt = os.path.join(d, "cornell_delta.pbrt")
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=5, width=64, height=64, spp=16, maxdepth=8,
+                                                  box_materials=scenes.DELTA_BOXES,
+                                                  upper_light=scenes.UPPER_LIGHT))
+        yfs = os.path.join(HERE, "cornell_delta_64.yfs")
+        oracle.ref_flatten(pbrt, yfs, seed_offset=1)
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_delta_64.npz"), image=img, variance=np.float64(info["variance"]))
+
+
+def cornell_refractor_64():
+    """cornell_delta_64 with a perfect-refractor ceiling (object 1)."""
+    s = FlatScene.read(os.path.join(HERE, "cornell_delta_64.yfs"))
+    scenes.make_ceiling_refractor(s)
+    s.write(os.path.join(HERE, "cornell_refractor_64.yfs"))
+    img, info = oracle.ref_render_flat(s, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_refractor_64.npz"), image=img,
+                        variance=np.float64(info["variance"]))
+
+
 def kdtree_cache_files():
     """The reference's kd-tree cache files (KdTree::save) of the raycast_small
     scene's first two meshes and of its scene tree."""
@@ -182,7 +215,8 @@ if __name__ == "__main__":
     if not oracle.have_reference():
         sys.exit("oracle/_ref/yar_ref is not built (oracle/build_ref.sh)")
     which = sys.argv[1:] or ["raycast_small", "transform_small", "kdtree_regression", "cornell_c1_64",
-                             "cornell_ggx_64", "exr_files", "kdtree_cache_files"]
+                             "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "exr_files",
+                             "kdtree_cache_files"]
     for name in which:
         globals()[name]()
         print("wrote", name)

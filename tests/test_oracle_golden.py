@@ -121,10 +121,11 @@ def test_builder_against_live_reference_large_mesh():
         assert np.array_equal(nodes, r.nodes)
 
 
-@pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64"])
+@pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64"])
 def test_oracle_render_matches_reference_golden(name):
-    """The oracle's path loop, sampler, shading, BSDFs, MIS and film reproduce
-    the reference's FP32 render and variance bit for bit."""
+    """The oracle's path loop, sampler, shading, BSDFs, delta scattering (mirror,
+    smooth glass, perfect refractor), MIS and film reproduce the reference's
+    FP32 render and variance bit for bit."""
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
     img, var = oracle.render(s, threads=4)
@@ -143,5 +144,21 @@ def test_oracle_render_against_live_reference_past_the_sampler_budget(tmp_path):
     oracle.ref_flatten(str(p), str(y), seed_offset=3)
     ref_img, info = oracle.ref_render(str(p), seed_offset=3, threads=4)
     img, var = oracle.render(FlatScene.read(str(y)), threads=4)
+    assert np.array_equal(bits(img), bits(ref_img))
+    assert var == info["variance"]
+
+
+@pytest.mark.skipif(not oracle.have_reference(), reason="reference not built here")
+@pytest.mark.parametrize("maxb,rr", [(1, 3), (2, 1), (12, 1)])
+def test_oracle_delta_paths_against_live_reference(maxb, rr):
+    """Delta vertices at the last bounce (the delta ray still adds the light it
+    reaches), Russian roulette right after a delta bounce, and paths past the
+    sampler's dimension budget, on the perfect-refractor scene."""
+    s = scenes.make_ceiling_refractor(FlatScene.read(golden("cornell_delta_64.yfs")))
+    s.config["x_pixel_sample_count"] = s.config["y_pixel_sample_count"] = 2
+    s.config["max_light_bounces"] = maxb
+    s.config["russian_roulette_bounce_count_threshold"] = rr
+    ref_img, info = oracle.ref_render_flat(s, threads=8)
+    img, var = oracle.render(s, threads=8)
     assert np.array_equal(bits(img), bits(ref_img))
     assert var == info["variance"]

@@ -17,6 +17,7 @@ import pytest
 
 import oracle
 from conftest import golden
+from yar_gb300 import scenes
 from yar_gb300.scene import FlatScene
 
 pytestmark = pytest.mark.gpu
@@ -32,7 +33,7 @@ def compare(img, ref):
     return same, rel
 
 
-@pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64"])
+@pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64"])
 def test_render_matches_reference_golden(gpu_ctx, name):
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
@@ -69,6 +70,24 @@ def test_render_matches_oracle_other_configs(gpu_ctx, seed_offset, spp_xy, maxb)
             assert abs(stats.variance - ref_var) <= VARIANCE_REL_TOL * ref_var
     else:
         assert abs(img.mean() - ref.mean()) < 0.02 * ref.mean()
+
+
+@pytest.mark.parametrize("maxb,rr,seed_offset", [(1, 3, 0), (2, 1, 5), (3, 2, 9), (8, 1, 2)])
+def test_render_delta_paths_match_oracle(gpu_ctx, maxb, rr, seed_offset):
+    """Mirror, smooth glass and a perfect-refractor ceiling: delta vertices at
+    the last bounce, Russian roulette right after a delta bounce, light reached
+    only through the refractor."""
+    s = scenes.make_ceiling_refractor(FlatScene.read(golden("cornell_delta_64.yfs")))
+    s.config["max_light_bounces"] = maxb
+    s.config["russian_roulette_bounce_count_threshold"] = rr
+    s.config["rng_seed_offset"] = seed_offset
+    ref, ref_var = oracle.render(s, threads=8)
+    gpu_ctx.upload_scene(s)
+    img, stats = gpu_ctx.render(64, 64)
+    same, rel = compare(img, ref)
+    assert same >= BIT_EQUAL_MIN, (same, rel)
+    assert rel < MEAN_REL_TOL, (same, rel)
+    assert abs(stats.variance - ref_var) <= VARIANCE_REL_TOL * ref_var
 
 
 def test_render_unsupported_features_fail_cleanly(gpu_ctx):

@@ -66,6 +66,10 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
         d.alpha_x = roughness_to_alpha(scene->config, m.u_roughness, m.roughness_is_alpha);
         d.alpha_y = roughness_to_alpha(scene->config, m.v_roughness, m.roughness_is_alpha);
         d.alpha = d.alpha_x;
+        d.delta = m.type == YAR_MATERIAL_PERFECT_REFLECTOR   ? kDeltaReflector
+                  : m.type == YAR_MATERIAL_PERFECT_REFRACTOR ? kDeltaRefractor
+                  : m.type == YAR_MATERIAL_GLASS && !(m.u_roughness > 0.f) ? kDeltaGlass
+                                                                            : kDeltaNone;
     }
     std::vector<Rect_Light_Dev> lights(std::max<uint32_t>(1, scene->rect_light_count));
     for (uint32_t i = 0; i < scene->rect_light_count; i++) {

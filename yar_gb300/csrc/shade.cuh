@@ -131,7 +131,11 @@ __device__ __forceinline__ V3 adjust_shading_normal(V3 wo, V3 ng, V3 n) {
 }
 
 // ---------------------------------------------------------------- BSDFs
-enum : uint32_t { kDiffuse = 2, kMetal = 4, kGlass = 7 };
+enum : uint32_t { kPerfectReflector = 0, kPerfectRefractor = 1, kDiffuse = 2, kMetal = 4, kGlass = 7 };
+
+// How a material scatters without a BSDF: not at all (kDeltaNone), as a
+// mirror, a perfect refractor, or smooth glass (glass of roughness 0).
+enum : uint32_t { kDeltaNone = 0, kDeltaReflector = 1, kDeltaRefractor = 2, kDeltaGlass = 3 };
 
 // Material constants as the BSDF constructors evaluate them (src/ref/bsdf.cpp:60-66,
 // :146-158, :268-294); alpha values are computed on the host with the
@@ -142,7 +146,8 @@ struct Material_Dev {
     Col reflectance, transmittance;
     Col eta_t, k_t;
     float eta_i_metal, ior;
-    float pad[2];
+    uint32_t delta;  // kDelta*
+    float pad;
 };
 
 struct Bsdf {
@@ -195,6 +200,32 @@ __device__ __forceinline__ float dielectric_fresnel(float cos_i, float eta) {
     const float Rp = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
     const float Rs = (cos_i - eta * cos_t) / (cos_i + eta * cos_t);
     return 0.5f * (Rp * Rp + Rs * Rs);
+}
+
+// check_for_delta_scattering_event with get_perfect_reflector_info,
+// get_perfect_refractor_info and get_glass_info (src/ref/delta_scattering.cpp:27-97,
+// :252-324), constant parameters, no bump map, no nested dielectrics.  Returns
+// false for a perfect refractor at total internal reflection: the reference
+// has no direction there (an assertion), and the path ends.
+__device__ __forceinline__ bool delta_scattering(const Shading& sc, const Material_Dev& m, float u, V3& dir, Col& atten) {
+    atten = col(1.f, 1.f, 1.f);
+    if (m.delta == kDeltaReflector) {
+        dir = reflect(sc.wo, sc.n);
+        atten = m.reflectance;
+        return true;
+    }
+    const bool enter = !sc.flipped;
+    if (m.delta == kDeltaRefractor) return refract(sc.wo, sc.n, enter ? 1.f / m.ior : m.ior, dir);
+    const float eta_t_over_i = enter ? m.ior : 1.f / m.ior;
+    const float fresnel = dielectric_fresnel(dot(sc.n, sc.wo), eta_t_over_i);
+    if (u < fresnel) {
+        dir = reflect(sc.wo, sc.n);
+        atten = m.reflectance;
+        return true;
+    }
+    const float eta = 1.f / eta_t_over_i;
+    atten = mul(m.transmittance, eta * eta);
+    return refract(sc.wo, sc.n, eta, dir);
 }
 
 __device__ __forceinline__ Col conductor_fresnel(float cos_i, float eta_i, Col eta_t, Col k_t) {

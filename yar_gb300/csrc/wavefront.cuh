@@ -44,7 +44,17 @@ constexpr int kBlock = 128;
 constexpr int kTile = 64;                           // src/ref/film.cpp:5
 constexpr uint64_t kChunkSampleBudget = 16u << 20;  // paths in flight per chunk
 
-enum : uint32_t { kPendShadow = 1u << 24, kPendProbe = 1u << 25, kPendDirect = 1u << 26 };
+// Path flags above the bounce and dimension counters of Path_State::info.
+// kDeltaArrival: the path's extend ray left a delta vertex (mirror, perfect
+// refractor, smooth glass) and its hit is shaded as the reference's delta
+// branch does; kDeltaFinal: that delta vertex used the last bounce.
+enum : uint32_t {
+    kPendShadow = 1u << 24,
+    kPendProbe = 1u << 25,
+    kPendDirect = 1u << 26,
+    kDeltaArrival = 1u << 27,
+    kDeltaFinal = 1u << 28
+};
 
 struct Rect_Light_Dev {
     float4 r0, r1, r2;  // light_to_world rows
@@ -539,6 +549,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
             float4 L4 = ps.L[slot];
             uint32_t info = ps.info[slot];
             int bounce = (int)(info & 0xffu);
+            const bool arrival = (info & kDeltaArrival) != 0;
             Col coeff = col(coeff4.x, coeff4.y, coeff4.z);
             Col L = col(L4.x, L4.y, L4.z);
             const bool hit = h2.y != 0xffffffffu;
@@ -547,16 +558,18 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
             if (hit) init_shading(S, v3(rb.x, rb.y, rb.z), h2.y, h2.x, h4.y, h4.z, h4.w, sc, oinfo);
             const bool is_light = hit && (uint32_t)oinfo.z != 0xffffffffu;
             bool done = false;
-            if (bounce == 0) {
+            // Emission seen by a camera ray or by a delta ray (the delta vertex
+            // already applied its attenuation and counted the bounce).
+            if (bounce == 0 || arrival) {
                 if (is_light && (uint32_t)oinfo.z == YAR_LIGHT_DIFFUSE_RECTANGULAR) {
                     const float4 le = __ldg(&S.lights[oinfo.w].le);
                     L = L + coeff * col(le.x, le.y, le.z);
                 }
-                if (p.max_bounces == 0) done = true;
+                if (arrival ? (info & kDeltaFinal) != 0 : p.max_bounces == 0) done = true;
             }
             if (!hit || is_light) done = true;
+            Dims dm;
             if (!done) {
-                Dims dm;
                 {
                     const uint32_t lp = slot / (uint32_t)p.spp, k = slot - lp * (uint32_t)p.spp;
                     dm.s1d = s1d + (size_t)lp * p.n1d * p.spp + k;
@@ -571,6 +584,21 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 dm.rng.state = (uint64_t)rs.x | ((uint64_t)rs.y << 32);
                 dm.rng.inc = (uint64_t)rs.z | ((uint64_t)rs.w << 32);
                 dm.rng_used = false;
+                // The Russian roulette that ends the reference's delta iteration
+                // (path_tracing.cpp:114-131) takes its draw before this vertex's.
+                if (arrival && bounce >= p.rr_bounce_threshold) {
+                    const float u_term = next1d(dm);
+                    const float max_coeff = max_std(coeff.r, max_std(coeff.g, coeff.b));
+                    if (max_coeff < p.rr_threshold) {
+                        const float p_term = max_std(0.05f, 1.f - max_coeff);
+                        if (u_term < p_term)
+                            done = true;
+                        else
+                            coeff = mul(coeff, 1.f / (1.f - p_term));
+                    }
+                }
+            }
+            if (!done) {
                 const float u_scatter = next1d(dm);
                 const float u_light_index = next1d(dm);
                 const float u_scatter_next = next1d(dm);
@@ -579,141 +607,161 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 const float2 un = next2d(dm);
 
                 const Material_Dev& mat = S.materials[oinfo.y];
-                Bsdf f;
-                make_bsdf(sc, mat, f);
-                // estimate_direct_lighting_from_single_sample (direct_lighting.cpp:522-578):
-                // a rectangular light chosen by int(u * total_light_count)
-                // (the reference asserts light_index < total; the clamp only guards memory)
-                const int light_index = min((int)(u_light_index * (float)p.total_lights), p.rect_lights - 1);
-                const Rect_Light_Dev& Ld = S.lights[light_index];
-                const float4 lr0 = __ldg(&Ld.r0), lr1 = __ldg(&Ld.r1), lr2 = __ldg(&Ld.r2);
-                const float4 lle = __ldg(&Ld.le), lsz = __ldg(&Ld.sz);
-                const V3 light_n = v3(lr0.z, lr1.z, lr2.z);
-                const Col Le = col(lle.x, lle.y, lle.z);
-                const float size_x = lle.w, size_y = lsz.x;
-                uint32_t pend = kPendDirect;
-                {   // light-sampling half of MIS
-                    const V3 local = v3(size_x * (ul.x - 0.5f), size_y * (ul.y - 0.5f), 0.0f);
-                    const V3 lp = xform_point(lr0, lr1, lr2, local);
-                    const V3 position = origin_for_point(sc, lp);
-                    const V3 lv = lp - position;
-                    const float dist = len(lv);
-                    const V3 wi = divs(lv, dist);
-                    const float lndw = dot(light_n, -wi);
-                    if (lndw > 1e-4f) {
-                        const float ndw = dot(sc.n, wi);
-                        const bool possible = (ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission);
-                        if (possible) {
-                            const Col fv = bsdf_evaluate(f, sc.wo, wi);
-                            if (!black(fv)) {
-                                const float light_pdf = (dist * dist) / (size_x * size_y * lndw);
-                                const float bpdf = bsdf_pdf(f, sc.wo, wi);
-                                const float w = mis_power(light_pdf, bpdf);
-                                const Col c = mul(Le * fv, w * fabsf(ndw) / light_pdf);
-                                ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
-                                want_shadow = true;
-                                sh_a = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
-                                sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
-                                pend |= kPendShadow;
-                            }
-                        }
-                    }
-                }
-                {   // BSDF-sampling half of MIS: the probe ray must hit this light
+                if (mat.delta != kDeltaNone) {
+                    // The delta branch of trace_path (path_tracing.cpp:76-112): no
+                    // light sample; the delta ray is the next extend ray, whose hit
+                    // adds the light it reaches.  A perfect refractor at total
+                    // internal reflection ends the path.
                     V3 wi;
-                    float bpdf = 0.f;
-                    const Col fv = bsdf_sample(f, ub.x, ub.y, u_scatter, sc.wo, wi, bpdf);
-                    if (!black(fv)) {
-                        const float lndw = dot(light_n, -wi);
-                        if (lndw > 1e-4f) {
-                            const V3 position = origin_for_direction(sc, wi);
-                            const Col lef = Le * fv;
-                            ps.pend_probe0[slot] = make_float4(lef.r, lef.g, lef.b, bpdf);
-                            ps.pend_probe1[slot] = make_float4(position.x, position.y, position.z, lndw);
-                            ps.pend_probe2[slot] = make_float4(dot(sc.n, wi), __int_as_float(light_index), 0.f, 0.f);
-                            want_probe = true;
-                            pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
-                            pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
-                            pend |= kPendProbe;
-                        }
-                    }
-                }
-                ps.pend_coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0.f);
-
-                bounce++;
-                bool cont = bounce != p.max_bounces;
-                float rec_value = 0.f;
-                V3 rec_dir = v3(0.f, 0.f, 0.f);
-                if (cont) {
-                    V3 wi;
-                    float pdf = 0.f;
-                    Col fv;
-                    if (GUIDED && g.lobes) {
-                        const float* lob = g.lobes + (size_t)i * kGuideLobeFloats;
-                        const float u_sel = pcg_float(dm.rng);
-                        dm.rng_used = true;
-                        float pdf_b = 0.f;
-                        if (u_sel < g.alpha) {
-                            const float u0 = pcg_float(dm.rng), u1 = pcg_float(dm.rng), u2 = pcg_float(dm.rng);
-                            wi = mixture_sample(lob, u0, u1, u2);
-                            const float ndw = dot(sc.n, wi);
-                            const bool possible = (ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission);
-                            fv = possible ? bsdf_evaluate(f, sc.wo, wi) : col(0.f, 0.f, 0.f);
-                            pdf_b = possible ? bsdf_pdf(f, sc.wo, wi) : 0.f;
-                        } else {
-                            fv = bsdf_sample(f, un.x, un.y, u_scatter_next, sc.wo, wi, pdf_b);
-                        }
-                        pdf = g.alpha * mixture_pdf(lob, wi) + (1.f - g.alpha) * pdf_b;
-                        if (!(pdf > 0.f)) fv = col(0.f, 0.f, 0.f);
-                    } else {
-                        fv = bsdf_sample(f, un.x, un.y, u_scatter_next, sc.wo, wi, pdf);
-                    }
-                    if (black(fv)) {
-                        cont = false;
-                    } else {
-                        if (GUIDED) {
-                            rec_value = (0.2126729f * fv.r + 0.7151522f * fv.g + 0.0721750f * fv.b) *
-                                        fabsf(dot(sc.n, wi)) / pdf;
-                            rec_dir = wi;
-                        }
-                        coeff = coeff * mul(fv, fabsf(dot(sc.n, wi)) / (pdf * 1.f));
+                    Col atten;
+                    bounce++;
+                    if (delta_scattering(sc, mat, u_scatter, wi, atten)) {
+                        coeff = coeff * atten;
                         const V3 o = origin_for_direction(sc, wi);
                         nx_a = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
                         nx_b = make_float4(wi.x, wi.y, wi.z, 0.f);
-                        if (bounce >= p.rr_bounce_threshold) {  // Russian roulette
-                            const float u_term = next1d(dm);
-                            const float max_coeff = max_std(coeff.r, max_std(coeff.g, coeff.b));
-                            if (max_coeff < p.rr_threshold) {
-                                const float p_term = max_std(0.05f, 1.f - max_coeff);
-                                if (u_term < p_term) {
-                                    cont = false;
-                                } else {
-                                    coeff = mul(coeff, 1.f / (1.f - p_term));
+                        want_next = true;
+                    }
+                    if (GUIDED && g.records) ps.rec[slot] = 0xffffffffu;
+                    info = (uint32_t)bounce | ((uint32_t)dm.i1d << 8) | ((uint32_t)dm.i2d << 16) | kDeltaArrival |
+                           (bounce == p.max_bounces ? kDeltaFinal : 0u);
+                } else {
+                    Bsdf f;
+                    make_bsdf(sc, mat, f);
+                    // estimate_direct_lighting_from_single_sample (direct_lighting.cpp:522-578):
+                    // a rectangular light chosen by int(u * total_light_count)
+                    // (the reference asserts light_index < total; the clamp only guards memory)
+                    const int light_index = min((int)(u_light_index * (float)p.total_lights), p.rect_lights - 1);
+                    const Rect_Light_Dev& Ld = S.lights[light_index];
+                    const float4 lr0 = __ldg(&Ld.r0), lr1 = __ldg(&Ld.r1), lr2 = __ldg(&Ld.r2);
+                    const float4 lle = __ldg(&Ld.le), lsz = __ldg(&Ld.sz);
+                    const V3 light_n = v3(lr0.z, lr1.z, lr2.z);
+                    const Col Le = col(lle.x, lle.y, lle.z);
+                    const float size_x = lle.w, size_y = lsz.x;
+                    uint32_t pend = kPendDirect;
+                    {   // light-sampling half of MIS
+                        const V3 local = v3(size_x * (ul.x - 0.5f), size_y * (ul.y - 0.5f), 0.0f);
+                        const V3 lp = xform_point(lr0, lr1, lr2, local);
+                        const V3 position = origin_for_point(sc, lp);
+                        const V3 lv = lp - position;
+                        const float dist = len(lv);
+                        const V3 wi = divs(lv, dist);
+                        const float lndw = dot(light_n, -wi);
+                        if (lndw > 1e-4f) {
+                            const float ndw = dot(sc.n, wi);
+                            const bool possible = (ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission);
+                            if (possible) {
+                                const Col fv = bsdf_evaluate(f, sc.wo, wi);
+                                if (!black(fv)) {
+                                    const float light_pdf = (dist * dist) / (size_x * size_y * lndw);
+                                    const float bpdf = bsdf_pdf(f, sc.wo, wi);
+                                    const float w = mis_power(light_pdf, bpdf);
+                                    const Col c = mul(Le * fv, w * fabsf(ndw) / light_pdf);
+                                    ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
+                                    want_shadow = true;
+                                    sh_a = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
+                                    sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                    pend |= kPendShadow;
                                 }
                             }
                         }
                     }
-                }
-                want_next = cont;
-                if (GUIDED && g.records) {
-                    uint32_t r = 0xffffffffu;
-                    if (cont) {
-                        r = atomicAdd(g.record_count, 1u);
-                        if (r < g.record_capacity) {
-                            float4* rec = g.records + (size_t)r * kGuideRecordF4;
-                            const float4* qr = g.queries + 3 * (size_t)i;
-                            rec[0] = qr[0];
-                            rec[1] = qr[1];
-                            rec[2] = make_float4(qr[2].x, rec_dir.x, rec_dir.y, rec_dir.z);
-                            rec[3] = make_float4(rec_value, __uint_as_float(slot), 0.f, 0.f);
-                            rec[4] = make_float4(coeff.r, coeff.g, coeff.b, 0.f);
-                        } else {
-                            r = 0xffffffffu;
+                    {   // BSDF-sampling half of MIS: the probe ray must hit this light
+                        V3 wi;
+                        float bpdf = 0.f;
+                        const Col fv = bsdf_sample(f, ub.x, ub.y, u_scatter, sc.wo, wi, bpdf);
+                        if (!black(fv)) {
+                            const float lndw = dot(light_n, -wi);
+                            if (lndw > 1e-4f) {
+                                const V3 position = origin_for_direction(sc, wi);
+                                const Col lef = Le * fv;
+                                ps.pend_probe0[slot] = make_float4(lef.r, lef.g, lef.b, bpdf);
+                                ps.pend_probe1[slot] = make_float4(position.x, position.y, position.z, lndw);
+                                ps.pend_probe2[slot] = make_float4(dot(sc.n, wi), __int_as_float(light_index), 0.f, 0.f);
+                                want_probe = true;
+                                pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
+                                pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                pend |= kPendProbe;
+                            }
                         }
                     }
-                    ps.rec[slot] = r;
+                    ps.pend_coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0.f);
+
+                    bounce++;
+                    bool cont = bounce != p.max_bounces;
+                    float rec_value = 0.f;
+                    V3 rec_dir = v3(0.f, 0.f, 0.f);
+                    if (cont) {
+                        V3 wi;
+                        float pdf = 0.f;
+                        Col fv;
+                        if (GUIDED && g.lobes) {
+                            const float* lob = g.lobes + (size_t)i * kGuideLobeFloats;
+                            const float u_sel = pcg_float(dm.rng);
+                            dm.rng_used = true;
+                            float pdf_b = 0.f;
+                            if (u_sel < g.alpha) {
+                                const float u0 = pcg_float(dm.rng), u1 = pcg_float(dm.rng), u2 = pcg_float(dm.rng);
+                                wi = mixture_sample(lob, u0, u1, u2);
+                                const float ndw = dot(sc.n, wi);
+                                const bool possible = (ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission);
+                                fv = possible ? bsdf_evaluate(f, sc.wo, wi) : col(0.f, 0.f, 0.f);
+                                pdf_b = possible ? bsdf_pdf(f, sc.wo, wi) : 0.f;
+                            } else {
+                                fv = bsdf_sample(f, un.x, un.y, u_scatter_next, sc.wo, wi, pdf_b);
+                            }
+                            pdf = g.alpha * mixture_pdf(lob, wi) + (1.f - g.alpha) * pdf_b;
+                            if (!(pdf > 0.f)) fv = col(0.f, 0.f, 0.f);
+                        } else {
+                            fv = bsdf_sample(f, un.x, un.y, u_scatter_next, sc.wo, wi, pdf);
+                        }
+                        if (black(fv)) {
+                            cont = false;
+                        } else {
+                            if (GUIDED) {
+                                rec_value = (0.2126729f * fv.r + 0.7151522f * fv.g + 0.0721750f * fv.b) *
+                                            fabsf(dot(sc.n, wi)) / pdf;
+                                rec_dir = wi;
+                            }
+                            coeff = coeff * mul(fv, fabsf(dot(sc.n, wi)) / (pdf * 1.f));
+                            const V3 o = origin_for_direction(sc, wi);
+                            nx_a = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
+                            nx_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                            if (bounce >= p.rr_bounce_threshold) {  // Russian roulette
+                                const float u_term = next1d(dm);
+                                const float max_coeff = max_std(coeff.r, max_std(coeff.g, coeff.b));
+                                if (max_coeff < p.rr_threshold) {
+                                    const float p_term = max_std(0.05f, 1.f - max_coeff);
+                                    if (u_term < p_term) {
+                                        cont = false;
+                                    } else {
+                                        coeff = mul(coeff, 1.f / (1.f - p_term));
+                                    }
+                                }
+                            }
+                        }
+                    }
+                    want_next = cont;
+                    if (GUIDED && g.records) {
+                        uint32_t r = 0xffffffffu;
+                        if (cont) {
+                            r = atomicAdd(g.record_count, 1u);
+                            if (r < g.record_capacity) {
+                                float4* rec = g.records + (size_t)r * kGuideRecordF4;
+                                const float4* qr = g.queries + 3 * (size_t)i;
+                                rec[0] = qr[0];
+                                rec[1] = qr[1];
+                                rec[2] = make_float4(qr[2].x, rec_dir.x, rec_dir.y, rec_dir.z);
+                                rec[3] = make_float4(rec_value, __uint_as_float(slot), 0.f, 0.f);
+                                rec[4] = make_float4(coeff.r, coeff.g, coeff.b, 0.f);
+                            } else {
+                                r = 0xffffffffu;
+                            }
+                        }
+                        ps.rec[slot] = r;
+                    }
+                    info = (uint32_t)bounce | ((uint32_t)dm.i1d << 8) | ((uint32_t)dm.i2d << 16) | pend;
                 }
-                info = (uint32_t)bounce | ((uint32_t)dm.i1d << 8) | ((uint32_t)dm.i2d << 16) | pend;
                 if (dm.rng_used)
                     ps.rng[slot] = make_uint4((uint32_t)dm.rng.state, (uint32_t)(dm.rng.state >> 32),
                                               (uint32_t)dm.rng.inc, (uint32_t)(dm.rng.inc >> 32));
@@ -1026,10 +1074,9 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     if (R.other_light_count) return fail(ctx, YAR_ERR_UNSUPPORTED, "only rectangular area lights are implemented");
     if (R.host_rect_lights.empty()) return fail(ctx, YAR_ERR_UNSUPPORTED, "scene has no light");
     for (const yar_material_desc& m : R.host_materials) {
-        if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL && m.type != YAR_MATERIAL_GLASS)
+        if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL && m.type != YAR_MATERIAL_GLASS &&
+            m.type != YAR_MATERIAL_PERFECT_REFLECTOR && m.type != YAR_MATERIAL_PERFECT_REFRACTOR)
             return fail(ctx, YAR_ERR_UNSUPPORTED, "material type " + std::to_string(m.type) + " is not implemented");
-        if (m.type == YAR_MATERIAL_GLASS && !(m.u_roughness > 0.f))
-            return fail(ctx, YAR_ERR_UNSUPPORTED, "smooth (delta) glass is not implemented");
     }
     const size_t n_obj = R.host_object_info.size() / 4;
     for (size_t i = 0; i < n_obj; i++) {

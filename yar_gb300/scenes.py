@@ -179,11 +179,15 @@ def _box(center, size, angle_deg):
     return v, idx
 
 
-def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0, box_materials=None):
+def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0, box_materials=None,
+                 upper_light=None):
     """pbrt-v3 text of the seeded Cornell box (34 triangles + a quad light).
 
     box_materials: None for matte boxes, or two pbrt material statements for
-    the short and the tall box (e.g. metal and rough glass)."""
+    the short and the tall box (e.g. metal and rough glass).
+    upper_light: None, or (half size, height, radiance) of a second quad light
+    above the ceiling, facing down; it reaches the room only through a ceiling
+    that transmits (a perfect refractor set on the flattened scene)."""
     rng = np.random.default_rng(seed)
     k = int(math.ceil(math.sqrt(spp)))
     shapes = []
@@ -226,9 +230,39 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
     out += ["AttributeBegin",
             '  AreaLightSource "diffuse" "rgb L" [%s]' % fmt([light_radiance] * 3),
             '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(light[1]), fmt(light[0])),
-            "AttributeEnd",
-            "WorldEnd", ""]
+            "AttributeEnd"]
+    if upper_light is not None:
+        uh, uy, ul = upper_light
+        v, i = _quad((-uh, uy, -uh), (uh, uy, -uh), (uh, uy, uh), (-uh, uy, uh))
+        out += ["AttributeBegin",
+                '  AreaLightSource "diffuse" "rgb L" [%s]' % fmt([ul] * 3),
+                '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(i), fmt(v)),
+                "AttributeEnd"]
+    out += ["WorldEnd", ""]
     return "\n".join(out)
+
+
+DELTA_BOXES = ('Material "mirror" "rgb Kr" [0.9 0.85 0.8]',
+               'Material "glass" "float index" [1.5] "rgb Kr" [0.95 0.95 0.95] "rgb Kt" [0.9 0.95 1]')
+
+UPPER_LIGHT = (0.8, 2.3, 4.0)  # half size, height, radiance
+
+
+def make_ceiling_refractor(flat, ior=1.0 / 1.5):
+    """Turns the ceiling (object 1 of cornell_pbrt's flattened scene) into a
+    perfect refractor.  Its normal faces up, so rays from the room leave the
+    medium with eta = ior < 1 and never meet total internal reflection (the
+    reference asserts there); nothing above the ceiling but the upper light
+    sends rays back."""
+    m = flat.materials.copy()
+    o = flat.objects.copy()
+    k = int(o[1]["material_index"])
+    m[k]["type"] = 1  # YAR_MATERIAL_PERFECT_REFRACTOR
+    m[k]["index_of_refraction"] = np.float32(ior)
+    o[1]["material_type"] = 1
+    flat.materials = m
+    flat.objects = o
+    return flat
 
 
 GGX_BOXES = ('Material "metal" "float roughness" [0.2] "rgb eta" [0.2 0.92 1.1] "rgb k" [3.9 2.45 2.14]',
