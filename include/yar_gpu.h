@@ -122,18 +122,23 @@ typedef struct yar_object_desc {
 } yar_object_desc;
 
 /* Constant-parameter materials (Perfect_Reflector/Perfect_Refractor/Diffuse/Metal/
- * Glass_Material, src/lib/material.h:48-150).  Glass with roughness 0 scatters as
- * the reference's smooth (delta) glass.  Textured parameters and bump maps are
- * outside the implemented path (YAR_ERR_UNSUPPORTED). */
+ * Plastic/Coated_Diffuse/Glass_Material, src/lib/material.h:48-150).  Glass with
+ * roughness 0 scatters as the reference's smooth (delta) glass; plastic in a scene
+ * with pbrt3_scene set is shaded as pbrt-v3's plastic, as the reference does.
+ * Textured parameters and bump maps are outside the implemented path
+ * (YAR_ERR_UNSUPPORTED). */
 typedef struct yar_material_desc {
-    uint32_t type;              /* YAR_MATERIAL_PERFECT_REFLECTOR / PERFECT_REFRACTOR / DIFFUSE / METAL / GLASS */
-    float reflectance[3];       /* perfect reflector, diffuse: reflectance; glass: reflectance (kr) */
-    float transmittance[3];     /* glass: transmittance (kt) */
+    uint32_t type;              /* YAR_MATERIAL_PERFECT_REFLECTOR / PERFECT_REFRACTOR / DIFFUSE / METAL /
+                                   PLASTIC / COATED_DIFFUSE / GLASS */
+    float reflectance[3];       /* perfect reflector: reflectance; diffuse, plastic, coated diffuse:
+                                   diffuse reflectance; glass: reflectance (kr) */
+    float transmittance[3];     /* glass: transmittance (kt); plastic, coated diffuse: specular r0
+                                   (plastic: all three equal) */
     float eta[3];               /* metal */
     float k[3];                 /* metal */
     float eta_i;                /* metal: IOR of the adjacent dielectric */
-    float u_roughness;          /* metal u roughness; glass roughness */
-    float v_roughness;          /* metal */
+    float u_roughness;          /* metal, coated diffuse: u roughness; glass, plastic: roughness */
+    float v_roughness;          /* metal, coated diffuse (plastic: = u_roughness) */
     float index_of_refraction;  /* glass, perfect refractor */
     int32_t roughness_is_alpha;
 } yar_material_desc;

@@ -162,7 +162,8 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         memcpy(fm.nodes.data(), t.nodes.data(), t.nodes.size() * 8);
         out.meshes.push_back(std::move(fm));
     }
-    // materials: diffuse, metal, glass, perfect reflector, perfect refractor flattened in that order
+    // materials: diffuse, metal, glass, plastic, coated diffuse, perfect reflector, perfect refractor
+    // flattened in that order
     std::vector<int> diffuse_index, metal_index, glass_index;
     for (const Diffuse_Material& m : ctx.materials.diffuse) {
         yar_material_desc d{};
@@ -195,6 +196,32 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         glass_index.push_back((int)out.materials.size());
         out.materials.push_back(d);
     }
+    // plastic and coated diffuse: reflectance = diffuse reflectance, transmittance = r0
+    std::vector<int> plastic_index, coated_index;
+    for (const Plastic_Material& m : ctx.materials.plastic) {
+        yar_material_desc d{};
+        d.type = YAR_MATERIAL_PLASTIC;
+        constant_rgb(m.diffuse_reflectance, d.reflectance);
+        float r0 = 0.f;
+        constant_float(m.r0, &r0);
+        d.transmittance[0] = d.transmittance[1] = d.transmittance[2] = r0;
+        constant_float(m.roughness, &d.u_roughness);
+        d.v_roughness = d.u_roughness;
+        d.roughness_is_alpha = m.roughness_is_alpha ? 1 : 0;
+        plastic_index.push_back((int)out.materials.size());
+        out.materials.push_back(d);
+    }
+    for (const Coated_Diffuse_Material& m : ctx.materials.coated_diffuse) {
+        yar_material_desc d{};
+        d.type = YAR_MATERIAL_COATED_DIFFUSE;
+        constant_rgb(m.diffuse_reflectance, d.reflectance);
+        constant_rgb(m.r0, d.transmittance);
+        constant_float(m.u_roughness, &d.u_roughness);
+        constant_float(m.v_roughness, &d.v_roughness);
+        d.roughness_is_alpha = m.roughness_is_alpha ? 1 : 0;
+        coated_index.push_back((int)out.materials.size());
+        out.materials.push_back(d);
+    }
     std::vector<int> reflector_index, refractor_index;
     for (const Perfect_Reflector_Material& m : ctx.materials.perfect_reflector) {
         yar_material_desc d{};
@@ -218,6 +245,8 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         if (o.material.type == Material_Type::diffuse) d.material_index = diffuse_index[o.material.index];
         else if (o.material.type == Material_Type::metal) d.material_index = metal_index[o.material.index];
         else if (o.material.type == Material_Type::glass) d.material_index = glass_index[o.material.index];
+        else if (o.material.type == Material_Type::plastic) d.material_index = plastic_index[o.material.index];
+        else if (o.material.type == Material_Type::coated_diffuse) d.material_index = coated_index[o.material.index];
         else if (o.material.type == Material_Type::perfect_reflector)
             d.material_index = reflector_index[o.material.index];
         else if (o.material.type == Material_Type::perfect_refractor)
@@ -576,6 +605,23 @@ int cmd_render_yfs(const Args& a) {
             m.roughness_is_alpha = d.roughness_is_alpha != 0;
             scene.materials.glass.push_back(m);
             handles.push_back({Material_Type::glass, (int)scene.materials.glass.size() - 1});
+        } else if (d.type == YAR_MATERIAL_PLASTIC) {
+            Plastic_Material m;
+            set_constant_parameter(m.roughness, d.u_roughness);
+            m.roughness_is_alpha = d.roughness_is_alpha != 0;
+            set_constant_parameter(m.r0, d.transmittance[0]);
+            set_constant_parameter(m.diffuse_reflectance, ColorRGB(d.reflectance));
+            scene.materials.plastic.push_back(m);
+            handles.push_back({Material_Type::plastic, (int)scene.materials.plastic.size() - 1});
+        } else if (d.type == YAR_MATERIAL_COATED_DIFFUSE) {
+            Coated_Diffuse_Material m;
+            set_constant_parameter(m.u_roughness, d.u_roughness);
+            set_constant_parameter(m.v_roughness, d.v_roughness);
+            m.roughness_is_alpha = d.roughness_is_alpha != 0;
+            set_constant_parameter(m.r0, ColorRGB(d.transmittance));
+            set_constant_parameter(m.diffuse_reflectance, ColorRGB(d.reflectance));
+            scene.materials.coated_diffuse.push_back(m);
+            handles.push_back({Material_Type::coated_diffuse, (int)scene.materials.coated_diffuse.size() - 1});
         } else if (d.type == YAR_MATERIAL_PERFECT_REFLECTOR) {
             Perfect_Reflector_Material m;
             set_constant_parameter(m.reflectance, ColorRGB(d.reflectance));

@@ -663,11 +663,12 @@ typedef struct bsdf_t {
     uint32_t type;
     v3 n, t, bt;  /* normal, tangent, bitangent */
     int reflection, transmission;
-    col reflectance, transmittance;
-    float alpha_x, alpha_y, alpha;  /* metal: alpha_x/y; glass: alpha */
+    col reflectance, transmittance; /* plastic, coated diffuse: diffuse reflectance and r0 */
+    float alpha_x, alpha_y, alpha;  /* metal, coated diffuse: alpha_x/y; glass, plastic: alpha */
     float eta_i_metal;
     col eta_t, k_t;
     float eta_o, eta_i;             /* glass */
+    int pbrt3_plastic, flipped;     /* plastic: Pbrt3_Plastic_BRDF, original shading normal flipped */
 } bsdf_t;
 
 static float pbrt3_roughness_to_alpha(float roughness) {
@@ -714,6 +715,17 @@ static int make_bsdf(const yar_flat_scene* s, const shading_ctx* sc, bsdf_t* f) 
         int enter = !sc->flipped;
         f->eta_o = enter ? 1.f : m->index_of_refraction;
         f->eta_i = enter ? m->index_of_refraction : 1.f;
+    } else if (f->type == YAR_MATERIAL_PLASTIC || f->type == YAR_MATERIAL_COATED_DIFFUSE) {
+        /* Plastic_BRDF / Pbrt3_Plastic_BRDF / Ashikhmin_Shirley_Phong_BRDF constructors,
+         * src/ref/bsdf.cpp:205-213, :427-438, src/ref/bsdf_pbrt.cpp:258-262 */
+        f->reflection = 1;
+        f->reflectance = ldc(m->reflectance);
+        f->transmittance = ldc(m->transmittance);
+        f->alpha_x = roughness_to_alpha(s, m->u_roughness, m->roughness_is_alpha);
+        f->alpha_y = roughness_to_alpha(s, m->v_roughness, m->roughness_is_alpha);
+        f->alpha = f->alpha_x;
+        f->pbrt3_plastic = f->type == YAR_MATERIAL_PLASTIC && s->config.pbrt3_scene;
+        f->flipped = sc->flipped;
     } else {
         return YAR_ERR_UNSUPPORTED;
     }
@@ -736,6 +748,13 @@ static float dielectric_fresnel(float cos_i, float eta) {
     float Rp = (eta * cos_i - cos_t) / (eta * cos_i + cos_t);
     float Rs = (cos_i - eta * cos_t) / (cos_i + eta * cos_t);
     return 0.5f * (Rp * Rp + Rs * Rs);
+}
+
+/* schlick_fresnel, src/ref/scattering.cpp:10-15 */
+static col schlick_fresnel(col r0, float cos_i) {
+    float k = 1.f - fabsf(cos_i);
+    float k5 = (k * k) * (k * k) * k;
+    return addc(r0, mulcs(subc(mkc(1, 1, 1), r0), k5));
 }
 
 static col conductor_fresnel(float cos_i, float eta_i, col eta_t, col k_t) {
@@ -842,8 +861,44 @@ static v3 refraction_half(float eta_o, v3 wo, float eta_i, v3 wi, v3 n) {
     return wh;
 }
 
+static float pow5(float v) { return (v * v) * (v * v) * v; }
+
 static col bsdf_evaluate(const bsdf_t* f, v3 wo, v3 wi) {
     if (f->type == YAR_MATERIAL_DIFFUSE) return mulcs(f->reflectance, PI_INV_F);
+    if (f->type == YAR_MATERIAL_PLASTIC) {
+        /* Plastic_BRDF::evaluate, src/ref/bsdf.cpp:215-234; Pbrt3_Plastic_BRDF::evaluate,
+         * src/ref/bsdf_pbrt.cpp:264-290 (pbrt3's swapped 1.0/1.5 IOR pair) */
+        v3 wh = norm3(add3(wo, wi));
+        float cos_i = dot3(wi, wh);
+        col F;
+        if (f->pbrt3_plastic) {
+            v3 original_n = f->flipped ? neg3(f->n) : f->n;
+            float relative_ior = dot3(original_n, wi) < 0.f ? 1.5f / 1.f : 1.f / 1.5f;
+            float fr = dielectric_fresnel(cos_i, relative_ior);
+            F = mkc(fr, fr, fr);
+        } else {
+            F = schlick_fresnel(mkc(0.04f, 0.04f, 0.04f), cos_i);
+        }
+        float G = ggx_G(wi, wo, f->n, f->alpha);
+        float D = ggx_D(wh, f->n, f->alpha);
+        float wo_n = dot3(wo, f->n), wi_n = dot3(wi, f->n);
+        col base = mulcs(F, (G * D) / (4.f * wo_n * wi_n));
+        col specular = mulcs(base, f->transmittance.r);
+        return addc(mulcs(f->reflectance, PI_INV_F), specular);
+    }
+    if (f->type == YAR_MATERIAL_COATED_DIFFUSE) {
+        /* Ashikhmin_Shirley_Phong_BRDF::evaluate, src/ref/bsdf.cpp:440-460 */
+        v3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
+        v3 wh_l = norm3(add3(wo_l, wi_l));
+        float cos_i = dot3(wi_l, wh_l);
+        col F = schlick_fresnel(f->transmittance, cos_i);
+        float D = ggx_D_aniso(wh_l, f->alpha_x, f->alpha_y);
+        col specular = mulcs(F, D / (4.f * cos_i * fmaxf_std(wo_l.z, wi_l.z)));
+        col diffuse = mulcs(mulc(f->reflectance, subc(mkc(1, 1, 1), f->transmittance)),
+                            28.f / (23.f * PI_F) * (1.f - pow5(1.f - 0.5f * wi_l.z)) *
+                                (1.f - pow5(1.f - 0.5f * wo_l.z)));
+        return addc(diffuse, specular);
+    }
     if (f->type == YAR_MATERIAL_METAL) {
         v3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
         v3 wh_l = norm3(add3(wo_l, wi_l));
@@ -889,6 +944,19 @@ static float glass_reflection_probability(const bsdf_t* f, float fresnel) {
 
 static float bsdf_pdf(const bsdf_t* f, v3 wo, v3 wi) {
     if (f->type == YAR_MATERIAL_DIFFUSE) return dot3(f->n, wi) / PI_F;
+    if (f->type == YAR_MATERIAL_PLASTIC) {
+        /* Plastic_BRDF::pdf, src/ref/bsdf.cpp:253-263 */
+        float diffuse_pdf = dot3(f->n, wi) / PI_F;
+        float spec_pdf = refl_pdf(wo, norm3(add3(wo, wi)), f->n, f->alpha);
+        return 0.5f * (diffuse_pdf + spec_pdf);
+    }
+    if (f->type == YAR_MATERIAL_COATED_DIFFUSE) {
+        /* Ashikhmin_Shirley_Phong_BRDF::pdf, src/ref/bsdf.cpp:480-492 */
+        float diffuse_pdf = dot3(f->n, wi) / PI_F;
+        v3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
+        float spec_pdf = refl_pdf_aniso(wo_l, norm3(add3(wo_l, wi_l)), f->alpha_x, f->alpha_y);
+        return 0.5f * (diffuse_pdf + spec_pdf);
+    }
     if (f->type == YAR_MATERIAL_METAL) {
         v3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
         v3 wh_l = norm3(add3(wo_l, wi_l));
@@ -911,11 +979,30 @@ static float bsdf_pdf(const bsdf_t* f, v3 wo, v3 wi) {
     return trans_pdf(wo, wi, wh, f->n, f->alpha, f->eta_o, f->eta_i) * (1.f - rprob);
 }
 
-/* BSDF::sample for the three BSDFs; returns black when no direction is produced. */
+/* BSDF::sample; returns black when no direction is produced. */
 static col bsdf_sample(const bsdf_t* f, float u0, float u1, float u_scatter, v3 wo, v3* wi, float* pdf) {
     if (f->type == YAR_MATERIAL_DIFFUSE) {
         v3 l = sample_hemisphere_cosine(u0, u1);
         *wi = local_to_world(f, l);
+        *pdf = bsdf_pdf(f, wo, *wi);
+        return bsdf_evaluate(f, wo, *wi);
+    }
+    if (f->type == YAR_MATERIAL_PLASTIC || f->type == YAR_MATERIAL_COATED_DIFFUSE) {
+        /* Plastic_BRDF::sample, src/ref/bsdf.cpp:236-251; Ashikhmin_Shirley_Phong_BRDF::sample,
+         * :462-478: the first 1D sample picks the diffuse or the specular lobe */
+        if (u_scatter < 0.5f) {
+            *wi = local_to_world(f, sample_hemisphere_cosine(u0, u1));
+        } else {
+            v3 wo_l = world_to_local(f, wo);
+            if (f->type == YAR_MATERIAL_PLASTIC) {
+                v3 wh = local_to_world(f, ggx_sample_vndf(u0, u1, wo_l, f->alpha, f->alpha));
+                *wi = reflect3(wo, wh);
+            } else {
+                v3 wh_l = ggx_sample_vndf(u0, u1, wo_l, f->alpha_x, f->alpha_y);
+                *wi = local_to_world(f, reflect3(wo_l, wh_l));
+            }
+        }
+        if (dot3(f->n, *wi) <= 0.f) return mkc(0, 0, 0);
         *pdf = bsdf_pdf(f, wo, *wi);
         return bsdf_evaluate(f, wo, *wi);
     }
@@ -1350,7 +1437,8 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
     for (uint32_t i = 0; i < s->material_count; i++) {
         uint32_t t = s->materials[i].type;
         if (t != YAR_MATERIAL_DIFFUSE && t != YAR_MATERIAL_METAL && t != YAR_MATERIAL_GLASS &&
-            t != YAR_MATERIAL_PERFECT_REFLECTOR && t != YAR_MATERIAL_PERFECT_REFRACTOR)
+            t != YAR_MATERIAL_PLASTIC && t != YAR_MATERIAL_COATED_DIFFUSE && t != YAR_MATERIAL_PERFECT_REFLECTOR &&
+            t != YAR_MATERIAL_PERFECT_REFRACTOR)
             return YAR_ERR_UNSUPPORTED;
     }
     if (s->other_light_count) return YAR_ERR_UNSUPPORTED;

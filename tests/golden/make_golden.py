@@ -29,6 +29,12 @@ Fixtures
                              reflection from the room) that lets the upper
                              light in, rendered by the reference from the flat
                              scene (pbrt has no perfect refractor).
+  cornell_layered_64.yfs / .npz  the same with a pbrt "plastic" box
+                             (Pbrt3_Plastic_BRDF) and a pbrt "substrate" box
+                             (Ashikhmin-Shirley coated diffuse), seed 6.
+  cornell_layered_yar_64.yfs / .npz  cornell_layered_64 as a non-pbrt scene
+                             (YAR's Plastic_BRDF, alpha = roughness^2),
+                             rendered by the reference from the flat scene.
 """
 import os
 import re
@@ -173,6 +179,29 @@ def cornell_refractor_64():
                         variance=np.float64(info["variance"]))
 
 
+def cornell_layered_64():
+    """The Cornell box with a plastic box and a coated-diffuse (substrate) box."""
+    with tempfile.TemporaryDirectory() as d:
+        pbrt = os.path.join(d, "cornell_layered.pbrt")
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=6, width=64, height=64, spp=16, maxdepth=8,
+                                                  box_materials=scenes.LAYERED_BOXES))
+        yfs = os.path.join(HERE, "cornell_layered_64.yfs")
+        oracle.ref_flatten(pbrt, yfs, seed_offset=1)
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_layered_64.npz"), image=img,
+                        variance=np.float64(info["variance"]))
+
+
+def cornell_layered_yar_64():
+    """cornell_layered_64 rendered as a non-pbrt scene."""
+    s = FlatScene.read(os.path.join(HERE, "cornell_layered_64.yfs"))
+    s.config["pbrt3_scene"] = 0
+    s.write(os.path.join(HERE, "cornell_layered_yar_64.yfs"))
+    img, info = oracle.ref_render_flat(s, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_layered_yar_64.npz"), image=img,
+                        variance=np.float64(info["variance"]))
+
+
 def kdtree_cache_files():
     """The reference's kd-tree cache files (KdTree::save) of the raycast_small
     scene's first two meshes and of its scene tree."""
@@ -215,7 +244,8 @@ if __name__ == "__main__":
     if not oracle.have_reference():
         sys.exit("oracle/_ref/yar_ref is not built (oracle/build_ref.sh)")
     which = sys.argv[1:] or ["raycast_small", "transform_small", "kdtree_regression", "cornell_c1_64",
-                             "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "exr_files",
+                             "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "cornell_layered_64",
+                             "cornell_layered_yar_64", "exr_files",
                              "kdtree_cache_files"]
     for name in which:
         globals()[name]()

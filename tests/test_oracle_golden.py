@@ -121,11 +121,13 @@ def test_builder_against_live_reference_large_mesh():
         assert np.array_equal(nodes, r.nodes)
 
 
-@pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64"])
+@pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64",
+                                  "cornell_layered_64", "cornell_layered_yar_64"])
 def test_oracle_render_matches_reference_golden(name):
-    """The oracle's path loop, sampler, shading, BSDFs, delta scattering (mirror,
-    smooth glass, perfect refractor), MIS and film reproduce the reference's
-    FP32 render and variance bit for bit."""
+    """The oracle's path loop, sampler, shading, BSDFs (diffuse, GGX metal, rough
+    glass, plastic in both of the reference's forms, coated diffuse), delta
+    scattering (mirror, smooth glass, perfect refractor), MIS and film
+    reproduce the reference's FP32 render and variance bit for bit."""
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
     img, var = oracle.render(s, threads=4)

@@ -33,7 +33,8 @@ def compare(img, ref):
     return same, rel
 
 
-@pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64"])
+@pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64",
+                                  "cornell_layered_64", "cornell_layered_yar_64"])
 def test_render_matches_reference_golden(gpu_ctx, name):
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
@@ -81,6 +82,23 @@ def test_render_delta_paths_match_oracle(gpu_ctx, maxb, rr, seed_offset):
     s.config["max_light_bounces"] = maxb
     s.config["russian_roulette_bounce_count_threshold"] = rr
     s.config["rng_seed_offset"] = seed_offset
+    ref, ref_var = oracle.render(s, threads=8)
+    gpu_ctx.upload_scene(s)
+    img, stats = gpu_ctx.render(64, 64)
+    same, rel = compare(img, ref)
+    assert same >= BIT_EQUAL_MIN, (same, rel)
+    assert rel < MEAN_REL_TOL, (same, rel)
+    assert abs(stats.variance - ref_var) <= VARIANCE_REL_TOL * ref_var
+
+
+@pytest.mark.parametrize("pbrt3,seed_offset,maxb", [(1, 4, 3), (0, 8, 5)])
+def test_render_layered_materials_match_oracle(gpu_ctx, pbrt3, seed_offset, maxb):
+    """Plastic (pbrt-v3's and YAR's forms) and coated diffuse at other seeds
+    and depths."""
+    s = FlatScene.read(golden("cornell_layered_64.yfs"))
+    s.config["pbrt3_scene"] = pbrt3
+    s.config["rng_seed_offset"] = seed_offset
+    s.config["max_light_bounces"] = maxb
     ref, ref_var = oracle.render(s, threads=8)
     gpu_ctx.upload_scene(s)
     img, stats = gpu_ctx.render(64, 64)

@@ -56,7 +56,7 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
         const yar_material_desc& m = scene->materials[i];
         Material_Dev& d = mats[i];
         memset(&d, 0, sizeof(d));
-        d.type = m.type;
+        d.type = m.type == YAR_MATERIAL_PLASTIC && scene->config.pbrt3_scene ? kPbrt3Plastic : m.type;
         d.reflectance = Col{m.reflectance[0], m.reflectance[1], m.reflectance[2]};
         d.transmittance = Col{m.transmittance[0], m.transmittance[1], m.transmittance[2]};
         d.eta_t = Col{m.eta[0], m.eta[1], m.eta[2]};

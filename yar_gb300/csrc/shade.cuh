@@ -131,15 +131,27 @@ __device__ __forceinline__ V3 adjust_shading_normal(V3 wo, V3 ng, V3 n) {
 }
 
 // ---------------------------------------------------------------- BSDFs
-enum : uint32_t { kPerfectReflector = 0, kPerfectRefractor = 1, kDiffuse = 2, kMetal = 4, kGlass = 7 };
+// The reference's Material_Type values, and kPbrt3Plastic: plastic in a pbrt-v3
+// scene, which the reference shades with Pbrt3_Plastic_BRDF (src/ref/bsdf.cpp:656-667).
+enum : uint32_t {
+    kPerfectReflector = 0,
+    kPerfectRefractor = 1,
+    kDiffuse = 2,
+    kMetal = 4,
+    kPlastic = 5,
+    kCoatedDiffuse = 6,
+    kGlass = 7,
+    kPbrt3Plastic = 0x105
+};
 
 // How a material scatters without a BSDF: not at all (kDeltaNone), as a
 // mirror, a perfect refractor, or smooth glass (glass of roughness 0).
 enum : uint32_t { kDeltaNone = 0, kDeltaReflector = 1, kDeltaRefractor = 2, kDeltaGlass = 3 };
 
 // Material constants as the BSDF constructors evaluate them (src/ref/bsdf.cpp:60-66,
-// :146-158, :268-294); alpha values are computed on the host with the
-// reference's roughness remapping.
+// :146-158, :205-213, :268-294, :427-438); alpha values are computed on the host
+// with the reference's roughness remapping.  Plastic and coated diffuse keep
+// their diffuse reflectance in `reflectance` and their r0 in `transmittance`.
 struct Material_Dev {
     uint32_t type;
     float alpha_x, alpha_y, alpha;
@@ -154,6 +166,7 @@ struct Bsdf {
     uint32_t type;
     V3 n, t, bt;
     bool reflection, transmission;
+    bool flipped;  // the shading normal was flipped towards wo (Pbrt3_Plastic_BRDF's IOR choice)
     Col reflectance, transmittance, eta_t, k_t;
     float alpha_x, alpha_y, alpha, eta_i_metal, eta_o, eta_i;
 };
@@ -171,6 +184,7 @@ __device__ __forceinline__ void make_bsdf(const Shading& sc, const Material_Dev&
     f.t = cross(f.bt, sc.n);
     f.reflection = true;
     f.transmission = m.type == kGlass;
+    f.flipped = sc.flipped;
     f.reflectance = m.reflectance;
     f.transmittance = m.transmittance;
     f.eta_t = m.eta_t;
@@ -226,6 +240,13 @@ __device__ __forceinline__ bool delta_scattering(const Shading& sc, const Materi
     const float eta = 1.f / eta_t_over_i;
     atten = mul(m.transmittance, eta * eta);
     return refract(sc.wo, sc.n, eta, dir);
+}
+
+// schlick_fresnel (src/ref/scattering.cpp:10-15)
+__device__ __forceinline__ Col schlick_fresnel(Col r0, float cos_i) {
+    const float k = 1.f - fabsf(cos_i);
+    const float k5 = (k * k) * (k * k) * k;
+    return r0 + mul(col(1.f, 1.f, 1.f) - r0, k5);
 }
 
 __device__ __forceinline__ Col conductor_fresnel(float cos_i, float eta_i, Col eta_t, Col k_t) {
@@ -333,8 +354,41 @@ __device__ __forceinline__ float glass_reflection_probability(const Bsdf& f, flo
     return ((r + t) == 0) ? 0.f : r / (r + t);
 }
 
+__device__ __forceinline__ float pow5(float v) { return (v * v) * (v * v) * v; }
+
 __device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
     if (f.type == kDiffuse) return mul(f.reflectance, 1.f / kPi);
+    if (f.type == kPlastic || f.type == kPbrt3Plastic) {
+        // Plastic_BRDF::evaluate (src/ref/bsdf.cpp:215-234); Pbrt3_Plastic_BRDF::evaluate
+        // (src/ref/bsdf_pbrt.cpp:264-290) with pbrt-v3's swapped 1.0 / 1.5 IOR pair
+        const V3 wh = normalized(wo + wi);
+        const float cos_i = dot(wi, wh);
+        Col F;
+        if (f.type == kPbrt3Plastic) {
+            const V3 original_n = f.flipped ? -f.n : f.n;
+            const float fr = dielectric_fresnel(cos_i, dot(original_n, wi) < 0.f ? 1.5f / 1.f : 1.f / 1.5f);
+            F = col(fr, fr, fr);
+        } else {
+            F = schlick_fresnel(col(0.04f, 0.04f, 0.04f), cos_i);
+        }
+        const float G = ggx_G(wi, wo, f.n, f.alpha);
+        const float D = ggx_D(wh, f.n, f.alpha);
+        const Col base = mul(F, (G * D) / (4.f * dot(wo, f.n) * dot(wi, f.n)));
+        return mul(f.reflectance, 1.f / kPi) + mul(base, f.transmittance.r);
+    }
+    if (f.type == kCoatedDiffuse) {
+        // Ashikhmin_Shirley_Phong_BRDF::evaluate (src/ref/bsdf.cpp:440-460)
+        const V3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
+        const V3 wh_l = normalized(wo_l + wi_l);
+        const float cos_i = dot(wi_l, wh_l);
+        const Col F = schlick_fresnel(f.transmittance, cos_i);
+        const float D = ggx_D_aniso(wh_l, f.alpha_x, f.alpha_y);
+        const Col specular = mul(F, D / (4.f * cos_i * max_std(wo_l.z, wi_l.z)));
+        const Col diffuse = mul(f.reflectance * (col(1.f, 1.f, 1.f) - f.transmittance),
+                                28.f / (23.f * kPi) * (1.f - pow5(1.f - 0.5f * wi_l.z)) *
+                                    (1.f - pow5(1.f - 0.5f * wo_l.z)));
+        return diffuse + specular;
+    }
     if (f.type == kMetal) {
         const V3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
         const V3 wh_l = normalized(wo_l + wi_l);
@@ -371,6 +425,19 @@ __device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
 
 __device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
     if (f.type == kDiffuse) return dot(f.n, wi) / kPi;
+    if (f.type == kPlastic || f.type == kPbrt3Plastic) {  // Plastic_BRDF::pdf (src/ref/bsdf.cpp:253-263)
+        const float diffuse_pdf = dot(f.n, wi) / kPi;
+        const V3 wh = normalized(wo + wi);
+        const float spec_pdf = vndf_pdf(wo, wh, f.n, f.alpha) / (4 * dot(wh, wo));
+        return 0.5f * (diffuse_pdf + spec_pdf);
+    }
+    if (f.type == kCoatedDiffuse) {  // Ashikhmin_Shirley_Phong_BRDF::pdf (src/ref/bsdf.cpp:480-492)
+        const float diffuse_pdf = dot(f.n, wi) / kPi;
+        const V3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
+        const V3 wh_l = normalized(wo_l + wi_l);
+        const float spec_pdf = vndf_pdf_aniso(wo_l, wh_l, f.alpha_x, f.alpha_y) / (4 * dot(wh_l, wo_l));
+        return 0.5f * (diffuse_pdf + spec_pdf);
+    }
     if (f.type == kMetal) {
         const V3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
         const V3 wh_l = normalized(wo_l + wi_l);
@@ -395,9 +462,28 @@ __device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
     return (wh_pdf * dwh) * (1.f - rprob);
 }
 
-// BSDF::sample of the three BSDFs; black when no direction is produced.
+// BSDF::sample; black when no direction is produced.
 __device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
                                            float& pdf) {
+    if (f.type == kPlastic || f.type == kPbrt3Plastic || f.type == kCoatedDiffuse) {
+        // Plastic_BRDF::sample (src/ref/bsdf.cpp:236-251), Ashikhmin_Shirley_Phong_BRDF::sample
+        // (:462-478): the first 1D sample picks the diffuse or the specular lobe
+        if (u_scatter < 0.5f) {
+            wi = local_to_world(f, sample_hemisphere_cosine(u0, u1));
+        } else {
+            const V3 wo_l = world_to_local(f, wo);
+            if (f.type == kCoatedDiffuse) {
+                const V3 wh_l = ggx_sample_vndf(u0, u1, wo_l, f.alpha_x, f.alpha_y);
+                wi = local_to_world(f, reflect(wo_l, wh_l));
+            } else {
+                const V3 wh = local_to_world(f, ggx_sample_vndf(u0, u1, wo_l, f.alpha, f.alpha));
+                wi = reflect(wo, wh);
+            }
+        }
+        if (dot(f.n, wi) <= 0.f) return col(0.f, 0.f, 0.f);
+        pdf = bsdf_pdf(f, wo, wi);
+        return bsdf_evaluate(f, wo, wi);
+    }
     if (f.type == kDiffuse) {
         wi = local_to_world(f, sample_hemisphere_cosine(u0, u1));
         pdf = bsdf_pdf(f, wo, wi);

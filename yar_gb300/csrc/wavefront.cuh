@@ -1075,6 +1075,7 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     if (R.host_rect_lights.empty()) return fail(ctx, YAR_ERR_UNSUPPORTED, "scene has no light");
     for (const yar_material_desc& m : R.host_materials) {
         if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL && m.type != YAR_MATERIAL_GLASS &&
+            m.type != YAR_MATERIAL_PLASTIC && m.type != YAR_MATERIAL_COATED_DIFFUSE &&
             m.type != YAR_MATERIAL_PERFECT_REFLECTOR && m.type != YAR_MATERIAL_PERFECT_REFRACTOR)
             return fail(ctx, YAR_ERR_UNSUPPORTED, "material type " + std::to_string(m.type) + " is not implemented");
     }

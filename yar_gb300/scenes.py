@@ -245,6 +245,10 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
 DELTA_BOXES = ('Material "mirror" "rgb Kr" [0.9 0.85 0.8]',
                'Material "glass" "float index" [1.5] "rgb Kr" [0.95 0.95 0.95] "rgb Kt" [0.9 0.95 1]')
 
+LAYERED_BOXES = ('Material "plastic" "rgb Kd" [0.6 0.25 0.1] "rgb Ks" [0.4 0.4 0.4] "float roughness" [0.15]',
+                 'Material "substrate" "rgb Kd" [0.2 0.4 0.6] "rgb Ks" [0.06 0.05 0.04] '
+                 '"float uroughness" [0.1] "float vroughness" [0.3]')
+
 UPPER_LIGHT = (0.8, 2.3, 4.0)  # half size, height, radiance
 
 
