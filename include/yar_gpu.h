@@ -72,6 +72,9 @@ extern "C" {
 #define YAR_MATERIAL_NULL              0xffffffffu
 
 /* Light_Type values (src/lib/light.h:7-17) */
+#define YAR_LIGHT_POINT                0
+#define YAR_LIGHT_SPOT                 1
+#define YAR_LIGHT_DIRECTIONAL          2
 #define YAR_LIGHT_DIFFUSE_RECTANGULAR  3
 #define YAR_LIGHT_NULL                 0xffffffffu
 
@@ -151,6 +154,19 @@ typedef struct yar_rect_light_desc {
     int32_t sample_count;
 } yar_rect_light_desc;
 
+/* Point_Light, Spot_Light and Directional_Light (src/lib/light.h:35-64) in one
+ * record: the lights without geometry, which are sampled but never hit.  A scene
+ * lists them in the reference's selection order (src/ref/direct_lighting.cpp:
+ * 522-547): all point lights, then all spot lights, then all directional lights. */
+typedef struct yar_delta_light_desc {
+    uint32_t type;              /* YAR_LIGHT_POINT / SPOT / DIRECTIONAL */
+    float position[3];          /* point, spot */
+    float direction[3];         /* spot: the cone axis; directional: towards the light */
+    float intensity[3];         /* point, spot: intensity; directional: irradiance */
+    float cone_angle;           /* spot, radians */
+    float penumbra_angle;       /* spot, radians */
+} yar_delta_light_desc;
+
 /* Camera, src/ref/camera.h:35-49 (fields as computed by Camera::Camera, camera.cpp:5-14) */
 typedef struct yar_camera_desc {
     float camera_to_world[12];
@@ -189,11 +205,13 @@ typedef struct yar_flat_scene {
     const yar_material_desc* materials;
     uint32_t rect_light_count;
     const yar_rect_light_desc* rect_lights;
-    /* lights of other kinds (point, spot, directional, sphere, mesh, environment):
-       counted for total_light_count; rendering with any of them is unsupported */
+    /* lights of other kinds (sphere, mesh, environment): counted for
+       total_light_count; rendering with any of them is unsupported */
     uint32_t other_light_count;
     yar_camera_desc camera;
     yar_render_config config;
+    uint32_t delta_light_count;     /* point, spot and directional lights */
+    const yar_delta_light_desc* delta_lights;
 } yar_flat_scene;
 
 /* One ray of a batch: 32 bytes, two float4.  tmax plays the role of the

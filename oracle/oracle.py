@@ -48,6 +48,9 @@ def lib():
                                            C.c_void_p]
         L.oracle_render.restype = C.c_int
         L.oracle_render.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32]
+        L.oracle_render_trig.restype = C.c_int
+        L.oracle_render_trig.argtypes = [C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_int32, C.c_int32,
+                                         C.c_int32]
         _lib = L
     return _lib
 
@@ -86,15 +89,18 @@ def cast_any(flat, rays, with_stats=False):
     return occ
 
 
-def render(flat, threads=0, rows=None):
+def render(flat, threads=0, rows=None, correctly_rounded_trig=False):
+    """The reference's render.  correctly_rounded_trig: sines and cosines of
+    sampled angles correctly rounded (as the CUDA path computes them) instead
+    of the C library's sinf/cosf (as the reference computes them)."""
     w = int(flat.config["render_region"][2] - flat.config["render_region"][0])
     h = int(flat.config["render_region"][3] - flat.config["render_region"][1])
     rgb = np.zeros((h, w, 3), np.float32)
     var = C.c_double(0.0)
     desc, keep = flat.to_c()
     r0, r1 = (0, h) if rows is None else rows
-    rc = lib().oracle_render(C.addressof(desc), rgb.ctypes.data, C.addressof(var), r0, r1,
-                             int(threads or os.cpu_count() or 1))
+    rc = lib().oracle_render_trig(C.addressof(desc), rgb.ctypes.data, C.addressof(var), r0, r1,
+                                  int(threads or os.cpu_count() or 1), int(bool(correctly_rounded_trig)))
     if rc != 0:
         raise RuntimeError("oracle_render failed: %d" % rc)
     return rgb, var.value

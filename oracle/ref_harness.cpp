@@ -277,7 +277,33 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         d.sample_count = l.sample_count;
         out.rect_lights.push_back(d);
     }
-    out.other_light_count = (uint32_t)(ctx.lights.total_light_count - (int)ctx.lights.diffuse_rectangular_lights.size());
+    // point, spot, directional lights in the reference's selection order
+    for (const Point_Light& l : ctx.lights.point_lights) {
+        yar_delta_light_desc d{};
+        d.type = YAR_LIGHT_POINT;
+        memcpy(d.position, &l.position.x, 12);
+        memcpy(d.intensity, &l.intensity.r, 12);
+        out.delta_lights.push_back(d);
+    }
+    for (const Spot_Light& l : ctx.lights.spot_lights) {
+        yar_delta_light_desc d{};
+        d.type = YAR_LIGHT_SPOT;
+        memcpy(d.position, &l.position.x, 12);
+        memcpy(d.direction, &l.direction.x, 12);
+        memcpy(d.intensity, &l.intensity.r, 12);
+        d.cone_angle = l.cone_angle;
+        d.penumbra_angle = l.penumbra_angle;
+        out.delta_lights.push_back(d);
+    }
+    for (const Directional_Light& l : ctx.lights.directional_lights) {
+        yar_delta_light_desc d{};
+        d.type = YAR_LIGHT_DIRECTIONAL;
+        memcpy(d.direction, &l.direction.x, 12);
+        memcpy(d.intensity, &l.irradiance.r, 12);
+        out.delta_lights.push_back(d);
+    }
+    out.other_light_count = (uint32_t)(ctx.lights.total_light_count - (int)ctx.lights.diffuse_rectangular_lights.size() -
+                                       (int)out.delta_lights.size());
 
     // Camera fields exactly as Camera::Camera computes them (src/ref/camera.cpp:5-14).
     const Matrix3x4& pose = scene.view_points[0];
@@ -562,7 +588,10 @@ int cmd_render_yfs(const Args& a) {
     yfs::Scene fs_scene;
     std::string err;
     if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
-    if (fs_scene.other_light_count) { fprintf(stderr, "only rectangular lights are supported\n"); return 1; }
+    if (fs_scene.other_light_count) {
+        fprintf(stderr, "only rectangular, point, spot and directional lights are supported\n");
+        return 1;
+    }
     Scene scene;
     scene.type = fs_scene.config.pbrt3_scene ? Scene_Type::pbrt : Scene_Type::obj;
     scene.path = a.pos[0];
@@ -644,6 +673,30 @@ int cmd_render_yfs(const Args& a) {
         l.size = Vector2(d.size[0], d.size[1]);
         l.sample_count = d.sample_count;
         scene.lights.diffuse_rectangular_lights.push_back(l);
+    }
+    for (const yar_delta_light_desc& d : fs_scene.delta_lights) {
+        if (d.type == YAR_LIGHT_POINT) {
+            Point_Light l;
+            l.position = Vector3(d.position);
+            l.intensity = ColorRGB(d.intensity);
+            scene.lights.point_lights.push_back(l);
+        } else if (d.type == YAR_LIGHT_SPOT) {
+            Spot_Light l;
+            l.position = Vector3(d.position);
+            l.direction = Vector3(d.direction);
+            l.intensity = ColorRGB(d.intensity);
+            l.cone_angle = d.cone_angle;
+            l.penumbra_angle = d.penumbra_angle;
+            scene.lights.spot_lights.push_back(l);
+        } else if (d.type == YAR_LIGHT_DIRECTIONAL) {
+            Directional_Light l;
+            l.direction = Vector3(d.direction);
+            l.irradiance = ColorRGB(d.intensity);
+            scene.lights.directional_lights.push_back(l);
+        } else {
+            fprintf(stderr, "unsupported light type %u\n", d.type);
+            return 1;
+        }
     }
     scene.lights.update_total_light_count();
     for (const yar_object_desc& d : fs_scene.objects) {

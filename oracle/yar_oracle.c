@@ -732,11 +732,20 @@ static int make_bsdf(const yar_flat_scene* s, const shading_ctx* sc, bsdf_t* f) 
     return YAR_OK;
 }
 
+/* The sine and cosine of sampled angles.  The reference calls the C library's
+ * sinf/cosf (std::sin/std::cos on floats), which is what this oracle does by
+ * default.  oracle_render_trig can switch to the correctly rounded values
+ * (double evaluation rounded to float), which is what the CUDA path computes:
+ * with it, the two must agree bit for bit.  Set per render, not reentrant. */
+static int g_correctly_rounded_trig = 0;
+static float sin_sample(float x) { return g_correctly_rounded_trig ? (float)sin((double)x) : sinf(x); }
+static float cos_sample(float x) { return g_correctly_rounded_trig ? (float)cos((double)x) : cosf(x); }
+
 static v3 sample_hemisphere_cosine(float u0, float u1) {
     float z = sqrtf(1.f - u0);
     float r = sqrtf(u0);
     float phi = 2.f * PI_F * u1;
-    return mk3(r * cosf(phi), r * sinf(phi), z);
+    return mk3(r * cos_sample(phi), r * sin_sample(phi), z);
 }
 
 static float dielectric_fresnel(float cos_i, float eta) {
@@ -828,8 +837,8 @@ static v3 ggx_sample_vndf(float u0, float u1, v3 wo, float ax, float ay) {
     v3 T2 = cross3(N, T1);
     float r = sqrtf(u0);
     float phi = 2.f * PI_F * u1;
-    float t1 = r * cosf(phi);
-    float t2 = r * sinf(phi);
+    float t1 = r * cos_sample(phi);
+    float t2 = r * sin_sample(phi);
     float s = 0.5f * (1.f + N.z);
     t2 = (1.f - s) * sqrtf(1.f - t1 * t1) + s * t2;
     v3 nh = add3(add3(mul3s(T1, t1), mul3s(T2, t2)), mul3s(N, sqrtf(fmaxf_std(0.f, 1.f - t1 * t1 - t2 * t2))));
@@ -1120,6 +1129,48 @@ static col direct_rect(const yar_flat_scene* s, const shading_ctx* sc, const bsd
     return out;
 }
 
+/* direct_lighting_from_point_light / _spot_light / _directional_light,
+ * src/ref/direct_lighting.cpp:26-107: one shadow ray, no MIS. */
+static col direct_delta(const yar_flat_scene* s, const shading_ctx* sc, const bsdf_t* f, const yar_delta_light_desc* L) {
+    const col black = mkc(0, 0, 0);
+    const col I = ldc(L->intensity);
+    const v3 ldir = ld3(L->direction);
+    if (L->type == YAR_LIGHT_DIRECTIONAL) {
+        float n_dot_l = dot3(sc->normal, ldir);
+        if (n_dot_l <= 0.f) return black;
+        v3 position = origin_for_direction(sc, ldir);
+        if (trace_any(s, position, ldir, INFINITY)) return black;
+        return mulcs(mulc(I, bsdf_evaluate(f, sc->wo, ldir)), n_dot_l);
+    }
+    const v3 lpos = ld3(L->position);
+    v3 position = origin_for_point(sc, lpos);
+    v3 lv = sub3(lpos, position);
+    float dist = len3(lv);
+    v3 wi = div3s(lv, dist);
+    if (L->type == YAR_LIGHT_POINT) {
+        float n_dot_l = dot3(sc->normal, wi);
+        if (n_dot_l <= 0.f) return black;
+        if (trace_any(s, position, wi, dist * (1.f - 1e-5f))) return black;
+        return mulcs(mulc(I, bsdf_evaluate(f, sc->wo, wi)), n_dot_l / (dist * dist));
+    }
+    float cone_cos = cosf(L->cone_angle);
+    float wi_cos = dot3(neg3(wi), ldir);
+    if (wi_cos < cone_cos) return black;
+    float penumbra_attenuation = 1.f;
+    float penumbra_cos = cosf(fmaxf_std(0.f, L->cone_angle - L->penumbra_angle));
+    if (wi_cos < penumbra_cos) {
+        float k = (wi_cos - cone_cos) / (penumbra_cos - cone_cos);
+        penumbra_attenuation = (k * k) * (k * k);
+    }
+    float n_dot_wi = dot3(sc->normal, wi);
+    int possible = (n_dot_wi > 0.f && f->reflection) || (n_dot_wi < 0.f && f->transmission);
+    if (!possible) return black;
+    col fv = bsdf_evaluate(f, sc->wo, wi);
+    if (blackc(fv)) return black;
+    if (trace_any(s, position, wi, dist * (1.f - 1e-5f))) return black;
+    return mulcs(mulc(I, fv), penumbra_attenuation * fabsf(n_dot_wi) / (dist * dist));
+}
+
 typedef struct sampler_view {
     const float* s1d;   /* this sample's 1d dims */
     const float* s2d;   /* this sample's 2d dims (pairs) */
@@ -1199,7 +1250,7 @@ static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, floa
 /* trace_path, src/ref/path_tracing.cpp:11-133 */
 static int trace_path(const yar_flat_scene* s, v3 ro, v3 rd, sampler_view* sv, col* radiance) {
     const yar_render_config* cfg = &s->config;
-    const int total_lights = (int)(s->rect_light_count + s->other_light_count);
+    const int total_lights = (int)(s->delta_light_count + s->rect_light_count + s->other_light_count);
     col coeff = mkc(1, 1, 1), L = mkc(0, 0, 0);
     int bounce = 0;
     int traced_by_delta_bounce = 0;
@@ -1239,7 +1290,11 @@ static int trace_path(const yar_flat_scene* s, v3 ro, v3 rd, sampler_view* sv, c
             if (rc != YAR_OK) return rc;
             /* estimate_direct_lighting_from_single_sample, src/ref/direct_lighting.cpp:522-578 */
             int light_index = (int)(u_light_index * (float)total_lights);
-            col direct = mulcs(direct_rect(s, &sc, &f, light_index, ul0, ul1, ub0, ub1, u_scatter), (float)total_lights);
+            col one = light_index < (int)s->delta_light_count
+                          ? direct_delta(s, &sc, &f, &s->delta_lights[light_index])
+                          : direct_rect(s, &sc, &f, light_index - (int)s->delta_light_count, ul0, ul1, ub0, ub1,
+                                        u_scatter);
+            col direct = mulcs(one, (float)total_lights);
             L = addc(L, mulc(coeff, direct));
 
             bounce++;
@@ -1430,6 +1485,12 @@ static void* render_worker(void* arg) {
     return NULL;
 }
 
+int oracle_render_trig(const yar_flat_scene* s, float* rgb, double* variance, int32_t row_begin, int32_t row_end,
+                       int32_t thread_count, int32_t correctly_rounded_trig) {
+    g_correctly_rounded_trig = correctly_rounded_trig != 0;
+    return oracle_render(s, rgb, variance, row_begin, row_end, thread_count);
+}
+
 int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t row_begin, int32_t row_end,
                   int32_t thread_count) {
     const yar_render_config* cfg = &s->config;
@@ -1442,6 +1503,10 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
             return YAR_ERR_UNSUPPORTED;
     }
     if (s->other_light_count) return YAR_ERR_UNSUPPORTED;
+    for (uint32_t i = 0; i < s->delta_light_count; i++) {
+        uint32_t t = s->delta_lights[i].type;
+        if (t > YAR_LIGHT_DIRECTIONAL || (i > 0 && t < s->delta_lights[i - 1].type)) return YAR_ERR_INVALID;
+    }
     render_job J;
     memset(&J, 0, sizeof(J));
     J.s = s;

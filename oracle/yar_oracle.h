@@ -62,6 +62,13 @@ void oracle_pixel_samples(uint32_t stream_id, int nx, int ny, int n1d, int n2d,
 int oracle_render(const yar_flat_scene* scene, float* rgb, double* variance,
                   int32_t row_begin, int32_t row_end, int32_t thread_count);
 
+/* oracle_render with the sines and cosines of sampled angles either from the C
+ * library (0, as the reference computes them) or correctly rounded (1, as the
+ * CUDA path computes them).  The choice stays for later oracle_render calls. */
+int oracle_render_trig(const yar_flat_scene* scene, float* rgb, double* variance,
+                       int32_t row_begin, int32_t row_end, int32_t thread_count,
+                       int32_t correctly_rounded_trig);
+
 #ifdef __cplusplus
 }
 #endif

@@ -122,7 +122,7 @@ def test_builder_against_live_reference_large_mesh():
 
 
 @pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64",
-                                  "cornell_layered_64", "cornell_layered_yar_64"])
+                                  "cornell_layered_64", "cornell_layered_yar_64", "cornell_lights_64"])
 def test_oracle_render_matches_reference_golden(name):
     """The oracle's path loop, sampler, shading, BSDFs (diffuse, GGX metal, rough
     glass, plastic in both of the reference's forms, coated diffuse), delta
@@ -164,3 +164,17 @@ def test_oracle_delta_paths_against_live_reference(maxb, rr):
     img, var = oracle.render(s, threads=8)
     assert np.array_equal(bits(img), bits(ref_img))
     assert var == info["variance"]
+
+
+def test_oracle_correctly_rounded_trig_changes_only_the_trig():
+    """The oracle's correctly-rounded-trig switch (the CUDA path's sines and
+    cosines) moves only a few percent of the pixels, and switching back
+    restores the reference's image bit for bit."""
+    s = FlatScene.read(golden("cornell_ggx_64.yfs"))
+    g = np.load(golden("cornell_ggx_64.npz"))
+    img_cr, _ = oracle.render(s, threads=4, correctly_rounded_trig=True)
+    same = np.all(bits(img_cr) == bits(g["image"]), axis=2).mean()
+    assert 0.9 <= same < 1.0
+    img, var = oracle.render(s, threads=4)
+    assert np.array_equal(bits(img), bits(g["image"]))
+    assert var == float(g["variance"])

@@ -25,6 +25,13 @@ pytestmark = pytest.mark.gpu
 MEAN_REL_TOL = 1e-4
 BIT_EQUAL_MIN = 0.90
 VARIANCE_REL_TOL = 1e-5
+# Scenes with point, spot and directional lights: the few samples whose paths
+# diverge from the reference's (sin/cos rounding) can pick up a point light's
+# 1/d^2 peak near a wall.  The share of bit-identical pixels is unchanged
+# (97-98% measured), but those samples move the mean relative error and the
+# image variance by up to ~2e-4 and ~1e-4.
+LIGHTS_MEAN_REL_TOL = 3e-4
+LIGHTS_VARIANCE_REL_TOL = 1e-4
 
 
 def compare(img, ref):
@@ -34,7 +41,7 @@ def compare(img, ref):
 
 
 @pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64",
-                                  "cornell_layered_64", "cornell_layered_yar_64"])
+                                  "cornell_layered_64", "cornell_layered_yar_64", "cornell_lights_64"])
 def test_render_matches_reference_golden(gpu_ctx, name):
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
@@ -43,11 +50,34 @@ def test_render_matches_reference_golden(gpu_ctx, name):
     h = int(s.config["render_region"][3] - s.config["render_region"][1])
     img, stats = gpu_ctx.render(w, h)
     same, rel = compare(img, g["image"])
+    lights = s.delta_lights.shape[0] > 0
     assert same >= BIT_EQUAL_MIN, (same, rel)
-    assert rel < MEAN_REL_TOL, (same, rel)
-    assert abs(stats.variance - float(g["variance"])) <= VARIANCE_REL_TOL * float(g["variance"])
+    assert rel < (LIGHTS_MEAN_REL_TOL if lights else MEAN_REL_TOL), (same, rel)
+    vtol = LIGHTS_VARIANCE_REL_TOL if lights else VARIANCE_REL_TOL
+    assert abs(stats.variance - float(g["variance"])) <= vtol * float(g["variance"])
     assert stats.paths == w * h * 16
     assert stats.rays_closest >= stats.paths
+
+
+RENDER_GOLDENS = ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "cornell_layered_64",
+                  "cornell_layered_yar_64", "cornell_lights_64"]
+
+
+@pytest.mark.parametrize("name", RENDER_GOLDENS)
+@pytest.mark.parametrize("seed_offset,maxb", [(1, 8), (5, 3)])
+def test_render_bit_identical_to_oracle_with_correctly_rounded_trig(gpu_ctx, name, seed_offset, maxb):
+    """The only arithmetic the CUDA path does not share with the reference is
+    the sine and cosine of sampled angles: the device rounds them correctly,
+    the reference takes the C library's sinf/cosf.  With the oracle switched to
+    correctly rounded values, every pixel and the variance are bit-identical."""
+    s = FlatScene.read(golden(name + ".yfs"))
+    s.config["rng_seed_offset"] = seed_offset
+    s.config["max_light_bounces"] = maxb
+    ref, ref_var = oracle.render(s, threads=8, correctly_rounded_trig=True)
+    gpu_ctx.upload_scene(s)
+    img, stats = gpu_ctx.render(64, 64)
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    assert stats.variance == ref_var
 
 
 @pytest.mark.parametrize("seed_offset,spp_xy,maxb", [(7, (2, 3), 5), (0, (1, 1), 1), (3, (4, 4), 12)])
@@ -106,6 +136,36 @@ def test_render_layered_materials_match_oracle(gpu_ctx, pbrt3, seed_offset, maxb
     assert same >= BIT_EQUAL_MIN, (same, rel)
     assert rel < MEAN_REL_TOL, (same, rel)
     assert abs(stats.variance - ref_var) <= VARIANCE_REL_TOL * ref_var
+
+
+@pytest.mark.parametrize("seed_offset,maxb", [(2, 1), (9, 4)])
+def test_render_point_spot_directional_lights_match_oracle(gpu_ctx, seed_offset, maxb):
+    """Point, spot and directional lights beside the quad light, at other seeds
+    and depths (maxdepth 1: direct light only): bit-identical to the oracle
+    with correctly rounded sines and cosines, and within the lights bars of
+    the oracle as the reference computes it."""
+    s = FlatScene.read(golden("cornell_lights_64.yfs"))
+    s.config["rng_seed_offset"] = seed_offset
+    s.config["max_light_bounces"] = maxb
+    gpu_ctx.upload_scene(s)
+    img, stats = gpu_ctx.render(64, 64)
+    exact, exact_var = oracle.render(s, threads=8, correctly_rounded_trig=True)
+    assert np.array_equal(img.view(np.uint32), exact.view(np.uint32))
+    assert stats.variance == exact_var
+    ref, ref_var = oracle.render(s, threads=8)
+    same, rel = compare(img, ref)
+    assert same >= BIT_EQUAL_MIN, (same, rel)
+    assert rel < LIGHTS_MEAN_REL_TOL, (same, rel)
+
+
+def test_render_rejects_delta_lights_out_of_order(gpu_ctx):
+    from yar_gb300 import native
+    s = FlatScene.read(golden("cornell_lights_64.yfs"))
+    s.delta_lights = s.delta_lights[::-1].copy()
+    gpu_ctx.upload_scene(s)
+    with pytest.raises(native.YarError) as e:
+        gpu_ctx.render(64, 64)
+    assert e.value.code == native.YAR_ERR_INVALID
 
 
 def test_render_unsupported_features_fail_cleanly(gpu_ctx):

@@ -81,6 +81,17 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
         lights[i].le = make_float4(l.emitted_radiance[0], l.emitted_radiance[1], l.emitted_radiance[2], l.size[0]);
         lights[i].sz = make_float4(l.size[1], 0.f, 0.f, 0.f);
     }
+    std::vector<Delta_Light_Dev> dlights(std::max<uint32_t>(1, scene->delta_light_count));
+    for (uint32_t i = 0; i < scene->delta_light_count; i++) {
+        const yar_delta_light_desc& l = scene->delta_lights[i];
+        float type_bits;
+        memcpy(&type_bits, &l.type, 4);
+        dlights[i].a = make_float4(l.position[0], l.position[1], l.position[2], type_bits);
+        dlights[i].b = make_float4(l.direction[0], l.direction[1], l.direction[2], std::cos(l.cone_angle));
+        dlights[i].c = make_float4(l.intensity[0], l.intensity[1], l.intensity[2],
+                                   std::cos(std::max(0.f, l.cone_angle - l.penumbra_angle)));
+    }
+    R.host_delta_lights.assign(scene->delta_lights, scene->delta_lights + scene->delta_light_count);
     R.host_materials.assign(scene->materials, scene->materials + scene->material_count);
     R.host_rect_lights.assign(scene->rect_lights, scene->rect_lights + scene->rect_light_count);
     R.host_object_info.resize(4 * (size_t)scene->object_count);
@@ -102,6 +113,7 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
     if ((rc = up(R.object_info, obj.data(), obj.size() * sizeof(float4))) != YAR_OK) return rc;
     if ((rc = up(R.materials, mats.data(), mats.size() * sizeof(Material_Dev))) != YAR_OK) return rc;
     if ((rc = up(R.rect_lights, lights.data(), lights.size() * sizeof(Rect_Light_Dev))) != YAR_OK) return rc;
+    if ((rc = up(R.delta_lights, dlights.data(), dlights.size() * sizeof(Delta_Light_Dev))) != YAR_OK) return rc;
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render upload");
     return YAR_OK;
@@ -109,8 +121,8 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
 
 void render_release(yar_gpu_ctx* ctx) {
     Render_Scene& R = ctx->render;
-    for (Device_Buffer* b : {&R.shading, &R.materials, &R.rect_lights, &R.object_info, &R.object_to_world,
-                             &R.object_to_world_normal})
+    for (Device_Buffer* b : {&R.shading, &R.materials, &R.rect_lights, &R.delta_lights, &R.object_info,
+                             &R.object_to_world, &R.object_to_world_normal})
         device_free(*b);
     for (Device_Buffer& b : ctx->render_scratch) device_free(b);
     ctx->render_scratch.clear();
@@ -184,7 +196,8 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
     q.prb_slot = dptr<uint32_t>(B[25]);
     q.counters = dptr<uint32_t>(B[26]);
     Scene_Dev S{ctx->ds, dptr<float4>(ctx->render.shading), dptr<float4>(ctx->render.object_info),
-                dptr<Material_Dev>(ctx->render.materials), dptr<Rect_Light_Dev>(ctx->render.rect_lights)};
+                dptr<Material_Dev>(ctx->render.materials), dptr<Rect_Light_Dev>(ctx->render.rect_lights),
+                dptr<Delta_Light_Dev>(ctx->render.delta_lights)};
     float4* radiance = dptr<float4>(B[0]);
     float2* image_samples = dptr<float2>(B[1]);
 
@@ -350,7 +363,8 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
     if (!s1d || !s2d || !ps.probe_hit2 || !q.prb_slot)
         return fail(ctx, YAR_ERR_CAPACITY, "static arena layout overflow");
     Scene_Dev S{ctx->ds, dptr<float4>(ctx->render.shading), dptr<float4>(ctx->render.object_info),
-                dptr<Material_Dev>(ctx->render.materials), dptr<Rect_Light_Dev>(ctx->render.rect_lights)};
+                dptr<Material_Dev>(ctx->render.materials), dptr<Rect_Light_Dev>(ctx->render.rect_lights),
+                dptr<Delta_Light_Dev>(ctx->render.delta_lights)};
 
     cudaStream_t st = ctx->stream;
     cudaError_t e = cudaMemsetAsync(q.counters, 0, 8 * sizeof(uint32_t), st);  // the arena keeps the last call's data

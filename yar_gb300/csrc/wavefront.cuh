@@ -62,6 +62,14 @@ struct Rect_Light_Dev {
     float4 sz;          // size.y, -, -, -
 };
 
+// Point, spot and directional lights (direct_lighting.cpp:26-107):
+//   a = position xyz, type bits | b = direction xyz, cos(cone angle)
+//   c = intensity (irradiance) rgb, cos(max(0, cone angle - penumbra angle))
+// The cosines are computed on the host, as the reference computes them per use.
+struct Delta_Light_Dev {
+    float4 a, b, c;
+};
+
 struct Render_Params {
     yar_camera_desc camera;
     int32_t sx0, sy0, sw, sh;    // sample region
@@ -72,7 +80,7 @@ struct Render_Params {
     float rr_threshold;
     float filter_radius;
     float film_scale, max_component;
-    int32_t total_lights, rect_lights;
+    int32_t total_lights, delta_lights, rect_lights;  // delta lights come first in the selection order
     uint32_t seed_offset;
     uint32_t stream_hi;  // upper 32 bits of the pixel streams' sequence (0 = the reference's streams)
 };
@@ -162,6 +170,7 @@ struct Scene_Dev {
     const float4* obj_render;     // 7 float4 per object
     const Material_Dev* materials;
     const Rect_Light_Dev* lights;
+    const Delta_Light_Dev* delta_lights;
 };
 
 // Warp-aggregated queue append: one atomic per warp and predicate value.
@@ -629,59 +638,116 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                     Bsdf f;
                     make_bsdf(sc, mat, f);
                     // estimate_direct_lighting_from_single_sample (direct_lighting.cpp:522-578):
-                    // a rectangular light chosen by int(u * total_light_count)
-                    // (the reference asserts light_index < total; the clamp only guards memory)
-                    const int light_index = min((int)(u_light_index * (float)p.total_lights), p.rect_lights - 1);
-                    const Rect_Light_Dev& Ld = S.lights[light_index];
-                    const float4 lr0 = __ldg(&Ld.r0), lr1 = __ldg(&Ld.r1), lr2 = __ldg(&Ld.r2);
-                    const float4 lle = __ldg(&Ld.le), lsz = __ldg(&Ld.sz);
-                    const V3 light_n = v3(lr0.z, lr1.z, lr2.z);
-                    const Col Le = col(lle.x, lle.y, lle.z);
-                    const float size_x = lle.w, size_y = lsz.x;
+                    // the light int(u * total_light_count), point, spot and directional lights
+                    // first, then the rectangular lights (the reference asserts the index is
+                    // below the total; the clamp only guards memory)
+                    const int selected = min((int)(u_light_index * (float)p.total_lights), p.total_lights - 1);
                     uint32_t pend = kPendDirect;
-                    {   // light-sampling half of MIS
-                        const V3 local = v3(size_x * (ul.x - 0.5f), size_y * (ul.y - 0.5f), 0.0f);
-                        const V3 lp = xform_point(lr0, lr1, lr2, local);
-                        const V3 position = origin_for_point(sc, lp);
-                        const V3 lv = lp - position;
-                        const float dist = len(lv);
-                        const V3 wi = divs(lv, dist);
-                        const float lndw = dot(light_n, -wi);
-                        if (lndw > 1e-4f) {
-                            const float ndw = dot(sc.n, wi);
-                            const bool possible = (ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission);
-                            if (possible) {
-                                const Col fv = bsdf_evaluate(f, sc.wo, wi);
-                                if (!black(fv)) {
-                                    const float light_pdf = (dist * dist) / (size_x * size_y * lndw);
-                                    const float bpdf = bsdf_pdf(f, sc.wo, wi);
-                                    const float w = mis_power(light_pdf, bpdf);
-                                    const Col c = mul(Le * fv, w * fabsf(ndw) / light_pdf);
-                                    ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
-                                    want_shadow = true;
-                                    sh_a = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
-                                    sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
-                                    pend |= kPendShadow;
+                    if (selected < p.delta_lights) {
+                        // direct_lighting_from_point/spot/directional_light (direct_lighting.cpp:26-107):
+                        // one shadow ray, no MIS
+                        const Delta_Light_Dev& D = S.delta_lights[selected];
+                        const float4 da = __ldg(&D.a), db = __ldg(&D.b), dc = __ldg(&D.c);
+                        const uint32_t kind = __float_as_uint(da.w);
+                        const V3 ldir = v3(db.x, db.y, db.z);
+                        V3 wi, position;
+                        float tmax = __int_as_float(0x7f800000), scale = 0.f;
+                        bool lit = false;
+                        if (kind == YAR_LIGHT_DIRECTIONAL) {
+                            wi = ldir;
+                            const float n_dot_l = dot(sc.n, wi);
+                            position = origin_for_direction(sc, wi);
+                            lit = n_dot_l > 0.f;
+                            scale = n_dot_l;
+                        } else {
+                            const V3 lp = v3(da.x, da.y, da.z);
+                            position = origin_for_point(sc, lp);
+                            const V3 lv = lp - position;
+                            const float dist = len(lv);
+                            wi = divs(lv, dist);
+                            tmax = dist * (1.f - 1e-5f);
+                            if (kind == YAR_LIGHT_POINT) {
+                                const float n_dot_l = dot(sc.n, wi);
+                                lit = n_dot_l > 0.f;
+                                scale = n_dot_l / (dist * dist);
+                            } else {
+                                const float cone_cos = db.w, penumbra_cos = dc.w;
+                                const float wi_cos = dot(-wi, ldir);
+                                if (!(wi_cos < cone_cos)) {
+                                    float attenuation = 1.f;
+                                    if (wi_cos < penumbra_cos) {
+                                        const float k = (wi_cos - cone_cos) / (penumbra_cos - cone_cos);
+                                        attenuation = (k * k) * (k * k);
+                                    }
+                                    const float ndw = dot(sc.n, wi);
+                                    lit = (ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission);
+                                    scale = attenuation * fabsf(ndw) / (dist * dist);
                                 }
                             }
                         }
-                    }
-                    {   // BSDF-sampling half of MIS: the probe ray must hit this light
-                        V3 wi;
-                        float bpdf = 0.f;
-                        const Col fv = bsdf_sample(f, ub.x, ub.y, u_scatter, sc.wo, wi, bpdf);
-                        if (!black(fv)) {
+                        if (lit) {
+                            const Col fv = bsdf_evaluate(f, sc.wo, wi);
+                            if (kind != YAR_LIGHT_SPOT || !black(fv)) {  // only the spot light skips a black BSDF
+                                const Col c = mul(col(dc.x, dc.y, dc.z) * fv, scale);
+                                ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
+                                want_shadow = true;
+                                sh_a = make_float4(position.x, position.y, position.z, tmax);
+                                sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                pend |= kPendShadow;
+                            }
+                        }
+                    } else {
+                        const int light_index = selected - p.delta_lights;
+                        const Rect_Light_Dev& Ld = S.lights[light_index];
+                        const float4 lr0 = __ldg(&Ld.r0), lr1 = __ldg(&Ld.r1), lr2 = __ldg(&Ld.r2);
+                        const float4 lle = __ldg(&Ld.le), lsz = __ldg(&Ld.sz);
+                        const V3 light_n = v3(lr0.z, lr1.z, lr2.z);
+                        const Col Le = col(lle.x, lle.y, lle.z);
+                        const float size_x = lle.w, size_y = lsz.x;
+                        {   // light-sampling half of MIS
+                            const V3 local = v3(size_x * (ul.x - 0.5f), size_y * (ul.y - 0.5f), 0.0f);
+                            const V3 lp = xform_point(lr0, lr1, lr2, local);
+                            const V3 position = origin_for_point(sc, lp);
+                            const V3 lv = lp - position;
+                            const float dist = len(lv);
+                            const V3 wi = divs(lv, dist);
                             const float lndw = dot(light_n, -wi);
                             if (lndw > 1e-4f) {
-                                const V3 position = origin_for_direction(sc, wi);
-                                const Col lef = Le * fv;
-                                ps.pend_probe0[slot] = make_float4(lef.r, lef.g, lef.b, bpdf);
-                                ps.pend_probe1[slot] = make_float4(position.x, position.y, position.z, lndw);
-                                ps.pend_probe2[slot] = make_float4(dot(sc.n, wi), __int_as_float(light_index), 0.f, 0.f);
-                                want_probe = true;
-                                pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
-                                pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
-                                pend |= kPendProbe;
+                                const float ndw = dot(sc.n, wi);
+                                const bool possible = (ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission);
+                                if (possible) {
+                                    const Col fv = bsdf_evaluate(f, sc.wo, wi);
+                                    if (!black(fv)) {
+                                        const float light_pdf = (dist * dist) / (size_x * size_y * lndw);
+                                        const float bpdf = bsdf_pdf(f, sc.wo, wi);
+                                        const float w = mis_power(light_pdf, bpdf);
+                                        const Col c = mul(Le * fv, w * fabsf(ndw) / light_pdf);
+                                        ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
+                                        want_shadow = true;
+                                        sh_a = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
+                                        sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                        pend |= kPendShadow;
+                                    }
+                                }
+                            }
+                        }
+                        {   // BSDF-sampling half of MIS: the probe ray must hit this light
+                            V3 wi;
+                            float bpdf = 0.f;
+                            const Col fv = bsdf_sample(f, ub.x, ub.y, u_scatter, sc.wo, wi, bpdf);
+                            if (!black(fv)) {
+                                const float lndw = dot(light_n, -wi);
+                                if (lndw > 1e-4f) {
+                                    const V3 position = origin_for_direction(sc, wi);
+                                    const Col lef = Le * fv;
+                                    ps.pend_probe0[slot] = make_float4(lef.r, lef.g, lef.b, bpdf);
+                                    ps.pend_probe1[slot] = make_float4(position.x, position.y, position.z, lndw);
+                                    ps.pend_probe2[slot] = make_float4(dot(sc.n, wi), __int_as_float(light_index), 0.f, 0.f);
+                                    want_probe = true;
+                                    pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
+                                    pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                    pend |= kPendProbe;
+                                }
                             }
                         }
                     }
@@ -1071,8 +1137,15 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     const yar_render_config& c = R.config;
     if (c.rendering_algorithm != 1) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the path tracer is implemented");
     if (c.pixel_filter_type != 0) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the box filter is implemented");
-    if (R.other_light_count) return fail(ctx, YAR_ERR_UNSUPPORTED, "only rectangular area lights are implemented");
-    if (R.host_rect_lights.empty()) return fail(ctx, YAR_ERR_UNSUPPORTED, "scene has no light");
+    if (R.other_light_count)
+        return fail(ctx, YAR_ERR_UNSUPPORTED, "only rectangular, point, spot and directional lights are implemented");
+    if (R.host_rect_lights.empty() && R.host_delta_lights.empty())
+        return fail(ctx, YAR_ERR_UNSUPPORTED, "scene has no light");
+    for (size_t i = 0; i < R.host_delta_lights.size(); i++) {
+        const uint32_t t = R.host_delta_lights[i].type;
+        if (t > YAR_LIGHT_DIRECTIONAL || (i > 0 && t < R.host_delta_lights[i - 1].type))
+            return fail(ctx, YAR_ERR_INVALID, "point, spot and directional lights must be listed in that order");
+    }
     for (const yar_material_desc& m : R.host_materials) {
         if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL && m.type != YAR_MATERIAL_GLASS &&
             m.type != YAR_MATERIAL_PLASTIC && m.type != YAR_MATERIAL_COATED_DIFFUSE &&
@@ -1125,7 +1198,8 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     p.film_scale = c.film_radiance_scale;
     p.max_component = c.max_rgb_component_value_of_film_sample;
     p.rect_lights = (int)R.host_rect_lights.size();
-    p.total_lights = p.rect_lights + (int)R.other_light_count;
+    p.delta_lights = (int)R.host_delta_lights.size();
+    p.total_lights = p.delta_lights + p.rect_lights + (int)R.other_light_count;
     p.seed_offset = (uint32_t)c.rng_seed_offset;
     return YAR_OK;
 }

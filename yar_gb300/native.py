@@ -82,13 +82,19 @@ class RenderConfig(C.Structure):
                 ("pbrt3_scene", C.c_int32), ("rng_seed_offset", C.c_int32)]
 
 
+class DeltaLightDesc(C.Structure):
+    _fields_ = [("type", C.c_uint32), ("position", C.c_float * 3), ("direction", C.c_float * 3),
+                ("intensity", C.c_float * 3), ("cone_angle", C.c_float), ("penumbra_angle", C.c_float)]
+
+
 class FlatSceneDesc(C.Structure):
     _fields_ = [("mesh_count", C.c_uint32), ("meshes", C.POINTER(MeshDesc)),
                 ("object_count", C.c_uint32), ("objects", C.POINTER(ObjectDesc)),
                 ("scene_kdtree", KdTreeView),
                 ("material_count", C.c_uint32), ("materials", C.POINTER(MaterialDesc)),
                 ("rect_light_count", C.c_uint32), ("rect_lights", C.POINTER(RectLightDesc)),
-                ("other_light_count", C.c_uint32), ("camera", CameraDesc), ("config", RenderConfig)]
+                ("other_light_count", C.c_uint32), ("camera", CameraDesc), ("config", RenderConfig),
+                ("delta_light_count", C.c_uint32), ("delta_lights", C.POINTER(DeltaLightDesc))]
 
 
 class HitSoa(C.Structure):

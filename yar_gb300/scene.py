@@ -22,6 +22,8 @@ MATERIAL_DTYPE = np.dtype([("type", "<u4"), ("reflectance", "<f4", 3), ("transmi
                            ("v_roughness", "<f4"), ("index_of_refraction", "<f4"), ("roughness_is_alpha", "<i4")])
 LIGHT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("emitted_radiance", "<f4", 3), ("size", "<f4", 2),
                         ("sample_count", "<i4")])
+DELTA_LIGHT_DTYPE = np.dtype([("type", "<u4"), ("position", "<f4", 3), ("direction", "<f4", 3),
+                              ("intensity", "<f4", 3), ("cone_angle", "<f4"), ("penumbra_angle", "<f4")])
 CAMERA_DTYPE = np.dtype([("camera_to_world", "<f4", 12), ("image_extent", "<f4", 2), ("horz_half_dist", "<f4"),
                          ("vert_half_dist", "<f4"), ("z_is_up", "<i4")])
 CONFIG_DTYPE = np.dtype([("render_region", "<i4", 4), ("rendering_algorithm", "<i4"), ("max_light_bounces", "<i4"),
@@ -35,6 +37,7 @@ CONFIG_DTYPE = np.dtype([("render_region", "<i4", 4), ("rendering_algorithm", "<
 assert OBJECT_DTYPE.itemsize == C.sizeof(native.ObjectDesc)
 assert MATERIAL_DTYPE.itemsize == C.sizeof(native.MaterialDesc)
 assert LIGHT_DTYPE.itemsize == C.sizeof(native.RectLightDesc)
+assert DELTA_LIGHT_DTYPE.itemsize == C.sizeof(native.DeltaLightDesc)
 assert CAMERA_DTYPE.itemsize == C.sizeof(native.CameraDesc)
 assert CONFIG_DTYPE.itemsize == C.sizeof(native.RenderConfig)
 
@@ -85,6 +88,8 @@ class FlatScene:
         self.scene_nodes = np.zeros((0, 2), np.uint32)
         self.materials = np.zeros(0, MATERIAL_DTYPE)
         self.rect_lights = np.zeros(0, LIGHT_DTYPE)
+        # point, spot and directional lights, in that order
+        self.delta_lights = np.zeros(0, DELTA_LIGHT_DTYPE)
         self.other_light_count = 0
         self.camera = np.zeros((), CAMERA_DTYPE)
         self.config = default_config()
@@ -160,8 +165,9 @@ class FlatScene:
         objects = np.ascontiguousarray(self.objects)
         materials = np.ascontiguousarray(self.materials)
         lights = np.ascontiguousarray(self.rect_lights)
+        dlights = np.ascontiguousarray(self.delta_lights)
         snodes = np.ascontiguousarray(self.scene_nodes, np.uint32)
-        keep += [objects, materials, lights, snodes, meshes]
+        keep += [objects, materials, lights, dlights, snodes, meshes]
         s = native.FlatSceneDesc()
         s.mesh_count = len(self.meshes)
         s.meshes = meshes
@@ -176,6 +182,8 @@ class FlatScene:
         s.rect_light_count = lights.shape[0]
         s.rect_lights = C.cast(lights.ctypes.data, C.POINTER(native.RectLightDesc)) if lights.size else None
         s.other_light_count = int(self.other_light_count)
+        s.delta_light_count = dlights.shape[0]
+        s.delta_lights = C.cast(dlights.ctypes.data, C.POINTER(native.DeltaLightDesc)) if dlights.size else None
         C.memmove(C.byref(s.camera), np.ascontiguousarray(self.camera).ctypes.data, CAMERA_DTYPE.itemsize)
         C.memmove(C.byref(s.config), np.ascontiguousarray(self.config).ctypes.data, CONFIG_DTYPE.itemsize)
         return s, keep
@@ -205,6 +213,8 @@ class FlatScene:
                            np.ascontiguousarray(self.scene_nodes, np.uint32).tobytes()))
         parts.append(chunk(b"MATS", struct.pack("<I", self.materials.shape[0]) + self.materials.tobytes()))
         parts.append(chunk(b"RLIT", struct.pack("<I", self.rect_lights.shape[0]) + self.rect_lights.tobytes()))
+        if self.delta_lights.shape[0]:
+            parts.append(chunk(b"DLIT", struct.pack("<I", self.delta_lights.shape[0]) + self.delta_lights.tobytes()))
         with open(path, "wb") as f:
             f.write(b"".join(parts))
 
@@ -258,6 +268,9 @@ class FlatScene:
             elif tag == b"RLIT":
                 n = struct.unpack_from("<I", p, 0)[0]
                 s.rect_lights = np.frombuffer(p[4:4 + n * LIGHT_DTYPE.itemsize], LIGHT_DTYPE).copy()
+            elif tag == b"DLIT":
+                n = struct.unpack_from("<I", p, 0)[0]
+                s.delta_lights = np.frombuffer(p[4:4 + n * DELTA_LIGHT_DTYPE.itemsize], DELTA_LIGHT_DTYPE).copy()
         return s
 
 

@@ -180,14 +180,16 @@ def _box(center, size, angle_deg):
 
 
 def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0, box_materials=None,
-                 upper_light=None):
+                 upper_light=None, light_sources=()):
     """pbrt-v3 text of the seeded Cornell box (34 triangles + a quad light).
 
     box_materials: None for matte boxes, or two pbrt material statements for
     the short and the tall box (e.g. metal and rough glass).
     upper_light: None, or (half size, height, radiance) of a second quad light
     above the ceiling, facing down; it reaches the room only through a ceiling
-    that transmits (a perfect refractor set on the flattened scene)."""
+    that transmits (a perfect refractor set on the flattened scene).
+    light_sources: pbrt LightSource statements added to the world (point,
+    spot, distant)."""
     rng = np.random.default_rng(seed)
     k = int(math.ceil(math.sqrt(spp)))
     shapes = []
@@ -218,7 +220,7 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
         'Integrator "path" "integer maxdepth" [%d]' % maxdepth,
         'PixelFilter "box"',
         "WorldBegin",
-    ]
+    ] + list(light_sources)
     for k, (v, i, albedo) in enumerate(shapes):
         material = 'Material "matte" "rgb Kd" [%s]' % fmt(albedo)
         if box_materials is not None and k >= 5:
@@ -249,7 +251,14 @@ LAYERED_BOXES = ('Material "plastic" "rgb Kd" [0.6 0.25 0.1] "rgb Ks" [0.4 0.4 0
                  'Material "substrate" "rgb Kd" [0.2 0.4 0.6] "rgb Ks" [0.06 0.05 0.04] '
                  '"float uroughness" [0.1] "float vroughness" [0.3]')
 
-UPPER_LIGHT = (0.8, 2.3, 4.0)  # half size, height, radiance
+UPPER_LIGHT = (0.8, 2.3, 4.0)
+
+# A point light low in the room, a spot light from the ceiling onto the boxes
+# with a penumbra, and a distant light through the open front.
+DELTA_LIGHTS = ('LightSource "point" "point from" [-0.6 0.4 0.6] "rgb I" [0.8 0.6 0.4]',
+                'LightSource "spot" "point from" [0.3 1.9 0.2] "point to" [0.2 0 0.1] "float coneangle" [25] '
+                '"float conedeltaangle" [8] "rgb I" [3 3 3.5]',
+                'LightSource "distant" "point from" [0.4 0.9 2.5] "point to" [0 0 0] "rgb L" [0.6 0.65 0.7]')  # half size, height, radiance
 
 
 def make_ceiling_refractor(flat, ior=1.0 / 1.5):
