@@ -198,8 +198,8 @@ cudaError_t enqueue_scene(Batch& bt, int si, bool one_spp, unsigned long long* s
             a.hit2 = q.ext_hit2;
             e = launch_extend(sub->ds, a, sc.kernel[0], st);
             if (e != cudaSuccess) break;
-            shade_kernel<false><<<kFixedGrid, kBlock, 0, st>>>(p, S, cur, paths, dp<float>(br.B[2]),
-                                                               dp<float2>(br.B[3]), ps, q, Guide_Shade{});
+            launch_shade<false>(p, kFixedGrid, st, S, cur, paths, dp<float>(br.B[2]), dp<float2>(br.B[3]), ps, q,
+                                Guide_Shade{});
             Cast_Args sh;
             sh.rays = q.shd_rays;
             sh.count = ctr + 1;

@@ -246,8 +246,7 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
                 if (e != cudaSuccess) break;
             }
             cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
-            shade_kernel<true><<<grid_for(count), kBlock, 0, st>>>(p, S, cur, count, dp<float>(B[2]),
-                                                                   dp<float2>(B[3]), ps, q, g);
+            launch_shade<true>(p, grid_for(count), st, S, cur, count, dp<float>(B[2]), dp<float2>(B[3]), ps, q, g);
             e = trace_light_queues(ctx, q, ps, count, bounce, st);
             if (e != cudaSuccess) break;
             connect_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, q.ext_slot[cur], count, ps, g.records);

@@ -216,8 +216,8 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
             e = trace_extend(ctx, q, cur, count, bounce, st);
             if (e != cudaSuccess) break;
             cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
-            shade_kernel<false><<<grid_for(count), kBlock, 0, st>>>(p, S, cur, count, dptr<float>(B[2]),
-                                                             dptr<float2>(B[3]), ps, q, Guide_Shade{});
+            launch_shade<false>(p, grid_for(count), st, S, cur, count, dptr<float>(B[2]), dptr<float2>(B[3]), ps, q,
+                                Guide_Shade{});
             e = trace_light_queues(ctx, q, ps, count, bounce, st);
             if (e != cudaSuccess) break;
             connect_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, q.ext_slot[cur], count, ps, nullptr);
@@ -381,7 +381,7 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
             e = trace_extend(ctx, q, cur, count, bounce, st);
             if (e != cudaSuccess) break;
             cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
-            shade_kernel<false><<<grid_for(count), kBlock, 0, st>>>(p, S, cur, count, s1d, s2d, ps, q, Guide_Shade{});
+            launch_shade<false>(p, grid_for(count), st, S, cur, count, s1d, s2d, ps, q, Guide_Shade{});
             e = trace_light_queues(ctx, q, ps, count, bounce, st);
             if (e != cudaSuccess) break;
             connect_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, q.ext_slot[cur], count, ps, nullptr);

@@ -356,9 +356,12 @@ __device__ __forceinline__ float glass_reflection_probability(const Bsdf& f, flo
 
 __device__ __forceinline__ float pow5(float v) { return (v * v) * (v * v) * v; }
 
+// FULL = false compiles out the plastic and coated-diffuse branches, for
+// scenes that only use the diffuse, metal and rough-glass BSDFs.
+template <bool FULL = true>
 __device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
     if (f.type == kDiffuse) return mul(f.reflectance, 1.f / kPi);
-    if (f.type == kPlastic || f.type == kPbrt3Plastic) {
+    if (FULL && (f.type == kPlastic || f.type == kPbrt3Plastic)) {
         // Plastic_BRDF::evaluate (src/ref/bsdf.cpp:215-234); Pbrt3_Plastic_BRDF::evaluate
         // (src/ref/bsdf_pbrt.cpp:264-290) with pbrt-v3's swapped 1.0 / 1.5 IOR pair
         const V3 wh = normalized(wo + wi);
@@ -376,7 +379,7 @@ __device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
         const Col base = mul(F, (G * D) / (4.f * dot(wo, f.n) * dot(wi, f.n)));
         return mul(f.reflectance, 1.f / kPi) + mul(base, f.transmittance.r);
     }
-    if (f.type == kCoatedDiffuse) {
+    if (FULL && f.type == kCoatedDiffuse) {
         // Ashikhmin_Shirley_Phong_BRDF::evaluate (src/ref/bsdf.cpp:440-460)
         const V3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
         const V3 wh_l = normalized(wo_l + wi_l);
@@ -423,15 +426,16 @@ __device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
     return mul(f.transmittance, base);
 }
 
+template <bool FULL = true>
 __device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
     if (f.type == kDiffuse) return dot(f.n, wi) / kPi;
-    if (f.type == kPlastic || f.type == kPbrt3Plastic) {  // Plastic_BRDF::pdf (src/ref/bsdf.cpp:253-263)
+    if (FULL && (f.type == kPlastic || f.type == kPbrt3Plastic)) {  // Plastic_BRDF::pdf (src/ref/bsdf.cpp:253-263)
         const float diffuse_pdf = dot(f.n, wi) / kPi;
         const V3 wh = normalized(wo + wi);
         const float spec_pdf = vndf_pdf(wo, wh, f.n, f.alpha) / (4 * dot(wh, wo));
         return 0.5f * (diffuse_pdf + spec_pdf);
     }
-    if (f.type == kCoatedDiffuse) {  // Ashikhmin_Shirley_Phong_BRDF::pdf (src/ref/bsdf.cpp:480-492)
+    if (FULL && f.type == kCoatedDiffuse) {  // Ashikhmin_Shirley_Phong_BRDF::pdf (src/ref/bsdf.cpp:480-492)
         const float diffuse_pdf = dot(f.n, wi) / kPi;
         const V3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
         const V3 wh_l = normalized(wo_l + wi_l);
@@ -463,9 +467,10 @@ __device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
 }
 
 // BSDF::sample; black when no direction is produced.
+template <bool FULL = true>
 __device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
                                            float& pdf) {
-    if (f.type == kPlastic || f.type == kPbrt3Plastic || f.type == kCoatedDiffuse) {
+    if (FULL && (f.type == kPlastic || f.type == kPbrt3Plastic || f.type == kCoatedDiffuse)) {
         // Plastic_BRDF::sample (src/ref/bsdf.cpp:236-251), Ashikhmin_Shirley_Phong_BRDF::sample
         // (:462-478): the first 1D sample picks the diffuse or the specular lobe
         if (u_scatter < 0.5f) {
@@ -481,13 +486,13 @@ __device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, fl
             }
         }
         if (dot(f.n, wi) <= 0.f) return col(0.f, 0.f, 0.f);
-        pdf = bsdf_pdf(f, wo, wi);
-        return bsdf_evaluate(f, wo, wi);
+        pdf = bsdf_pdf<FULL>(f, wo, wi);
+        return bsdf_evaluate<FULL>(f, wo, wi);
     }
     if (f.type == kDiffuse) {
         wi = local_to_world(f, sample_hemisphere_cosine(u0, u1));
-        pdf = bsdf_pdf(f, wo, wi);
-        return bsdf_evaluate(f, wo, wi);
+        pdf = bsdf_pdf<FULL>(f, wo, wi);
+        return bsdf_evaluate<FULL>(f, wo, wi);
     }
     if (f.type == kMetal) {
         const V3 wo_l = world_to_local(f, wo);
@@ -496,7 +501,7 @@ __device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, fl
         if (wi_l.z <= 0.f) return col(0.f, 0.f, 0.f);
         wi = local_to_world(f, wi_l);
         pdf = vndf_pdf_aniso(wo_l, wh_l, f.alpha_x, f.alpha_y) / (4 * dot(wh_l, wo_l));
-        return bsdf_evaluate(f, wo, wi);
+        return bsdf_evaluate<FULL>(f, wo, wi);
     }
     const V3 wo_l = world_to_local(f, wo);
     const V3 wh = local_to_world(f, ggx_sample_vndf(u0, u1, wo_l, f.alpha, f.alpha));
@@ -510,9 +515,9 @@ __device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, fl
         if (!refract(wo, wh, f.eta_o / f.eta_i, wi)) return col(0.f, 0.f, 0.f);
         if (dot(wi, f.n) >= 0.f) return col(0.f, 0.f, 0.f);
     }
-    pdf = bsdf_pdf(f, wo, wi);
+    pdf = bsdf_pdf<FULL>(f, wo, wi);
     if (pdf == 0.f) return col(0.f, 0.f, 0.f);
-    return bsdf_evaluate(f, wo, wi);
+    return bsdf_evaluate<FULL>(f, wo, wi);
 }
 
 // mis_power_heuristic (src/ref/direct_lighting.cpp:18-24)

@@ -81,6 +81,7 @@ struct Render_Params {
     float filter_radius;
     float film_scale, max_component;
     int32_t total_lights, delta_lights, rect_lights;  // delta lights come first in the selection order
+    int32_t full_shading;  // the scene needs shade_kernel<*, true>
     uint32_t seed_offset;
     uint32_t stream_hi;  // upper 32 bits of the pixel streams' sequence (0 = the reference's streams)
 };
@@ -536,10 +537,13 @@ __device__ __forceinline__ float2 next2d(Dims& d) {
 // alpha q + (1 - alpha) p_bsdf, so the estimator stays unbiased; the light
 // sample and the MIS probe are unchanged.  With g.records set, every
 // continued vertex also leaves a training record.
+// FULL: delta materials, delta-light sampling, plastic and coated diffuse.  A
+// scene without them runs the FULL = false instantiation, which has none of
+// that code (launch_shade picks it from Render_Params::full_shading).
 // Launch bounds: at least 5 blocks of 128 threads per SM (96 registers).
 // Measured on GB300 (C3 render): 1.726 s against 1.732 s at 4 blocks
 // (128 registers) and 1.764 s without a bound (160 registers, 3 blocks).
-template <bool GUIDED>
+template <bool GUIDED, bool FULL>
 __global__ void __launch_bounds__(kBlock, 5)
 shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float* __restrict__ s1d,
              const float2* __restrict__ s2d, Path_State ps, Queues q, Guide_Shade g) {
@@ -558,7 +562,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
             float4 L4 = ps.L[slot];
             uint32_t info = ps.info[slot];
             int bounce = (int)(info & 0xffu);
-            const bool arrival = (info & kDeltaArrival) != 0;
+            const bool arrival = FULL && (info & kDeltaArrival) != 0;
             Col coeff = col(coeff4.x, coeff4.y, coeff4.z);
             Col L = col(L4.x, L4.y, L4.z);
             const bool hit = h2.y != 0xffffffffu;
@@ -616,7 +620,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 const float2 un = next2d(dm);
 
                 const Material_Dev& mat = S.materials[oinfo.y];
-                if (mat.delta != kDeltaNone) {
+                if (FULL && mat.delta != kDeltaNone) {
                     // The delta branch of trace_path (path_tracing.cpp:76-112): no
                     // light sample; the delta ray is the next extend ray, whose hit
                     // adds the light it reaches.  A perfect refractor at total
@@ -643,7 +647,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                     // below the total; the clamp only guards memory)
                     const int selected = min((int)(u_light_index * (float)p.total_lights), p.total_lights - 1);
                     uint32_t pend = kPendDirect;
-                    if (selected < p.delta_lights) {
+                    if (FULL && selected < p.delta_lights) {
                         // direct_lighting_from_point/spot/directional_light (direct_lighting.cpp:26-107):
                         // one shadow ray, no MIS
                         const Delta_Light_Dev& D = S.delta_lights[selected];
@@ -686,7 +690,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                             }
                         }
                         if (lit) {
-                            const Col fv = bsdf_evaluate(f, sc.wo, wi);
+                            const Col fv = bsdf_evaluate<FULL>(f, sc.wo, wi);
                             if (kind != YAR_LIGHT_SPOT || !black(fv)) {  // only the spot light skips a black BSDF
                                 const Col c = mul(col(dc.x, dc.y, dc.z) * fv, scale);
                                 ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
@@ -716,10 +720,10 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                 const float ndw = dot(sc.n, wi);
                                 const bool possible = (ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission);
                                 if (possible) {
-                                    const Col fv = bsdf_evaluate(f, sc.wo, wi);
+                                    const Col fv = bsdf_evaluate<FULL>(f, sc.wo, wi);
                                     if (!black(fv)) {
                                         const float light_pdf = (dist * dist) / (size_x * size_y * lndw);
-                                        const float bpdf = bsdf_pdf(f, sc.wo, wi);
+                                        const float bpdf = bsdf_pdf<FULL>(f, sc.wo, wi);
                                         const float w = mis_power(light_pdf, bpdf);
                                         const Col c = mul(Le * fv, w * fabsf(ndw) / light_pdf);
                                         ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
@@ -734,7 +738,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                         {   // BSDF-sampling half of MIS: the probe ray must hit this light
                             V3 wi;
                             float bpdf = 0.f;
-                            const Col fv = bsdf_sample(f, ub.x, ub.y, u_scatter, sc.wo, wi, bpdf);
+                            const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_scatter, sc.wo, wi, bpdf);
                             if (!black(fv)) {
                                 const float lndw = dot(light_n, -wi);
                                 if (lndw > 1e-4f) {
@@ -771,15 +775,15 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                 wi = mixture_sample(lob, u0, u1, u2);
                                 const float ndw = dot(sc.n, wi);
                                 const bool possible = (ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission);
-                                fv = possible ? bsdf_evaluate(f, sc.wo, wi) : col(0.f, 0.f, 0.f);
-                                pdf_b = possible ? bsdf_pdf(f, sc.wo, wi) : 0.f;
+                                fv = possible ? bsdf_evaluate<FULL>(f, sc.wo, wi) : col(0.f, 0.f, 0.f);
+                                pdf_b = possible ? bsdf_pdf<FULL>(f, sc.wo, wi) : 0.f;
                             } else {
-                                fv = bsdf_sample(f, un.x, un.y, u_scatter_next, sc.wo, wi, pdf_b);
+                                fv = bsdf_sample<FULL>(f, un.x, un.y, u_scatter_next, sc.wo, wi, pdf_b);
                             }
                             pdf = g.alpha * mixture_pdf(lob, wi) + (1.f - g.alpha) * pdf_b;
                             if (!(pdf > 0.f)) fv = col(0.f, 0.f, 0.f);
                         } else {
-                            fv = bsdf_sample(f, un.x, un.y, u_scatter_next, sc.wo, wi, pdf);
+                            fv = bsdf_sample<FULL>(f, un.x, un.y, u_scatter_next, sc.wo, wi, pdf);
                         }
                         if (black(fv)) {
                             cont = false;
@@ -855,6 +859,15 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
             q.ext_slot[cur ^ 1][in] = slot;
         }
     }
+}
+
+template <bool GUIDED>
+void launch_shade(const Render_Params& p, unsigned grid, cudaStream_t st, const Scene_Dev& S, int cur, uint32_t count,
+                  const float* s1d, const float2* s2d, const Path_State& ps, const Queues& q, const Guide_Shade& g) {
+    if (p.full_shading)
+        shade_kernel<GUIDED, true><<<grid, kBlock, 0, st>>>(p, S, cur, count, s1d, s2d, ps, q, g);
+    else
+        shade_kernel<GUIDED, false><<<grid, kBlock, 0, st>>>(p, S, cur, count, s1d, s2d, ps, q, g);
 }
 
 // ---------------------------------------------------------------- connect
@@ -1200,6 +1213,11 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     p.rect_lights = (int)R.host_rect_lights.size();
     p.delta_lights = (int)R.host_delta_lights.size();
     p.total_lights = p.delta_lights + p.rect_lights + (int)R.other_light_count;
+    p.full_shading = p.delta_lights > 0;
+    for (const yar_material_desc& m : R.host_materials)
+        if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL &&
+            !(m.type == YAR_MATERIAL_GLASS && m.u_roughness > 0.f))
+            p.full_shading = 1;
     p.seed_offset = (uint32_t)c.rng_seed_offset;
     return YAR_OK;
 }
