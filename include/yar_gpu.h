@@ -76,6 +76,8 @@ extern "C" {
 #define YAR_LIGHT_SPOT                 1
 #define YAR_LIGHT_DIRECTIONAL          2
 #define YAR_LIGHT_DIFFUSE_RECTANGULAR  3
+#define YAR_LIGHT_DIFFUSE_SPHERE       4
+#define YAR_LIGHT_DIFFUSE_TRIANGLE_MESH 5
 #define YAR_LIGHT_NULL                 0xffffffffu
 
 /* Visibility (src/lib/triangle_mesh.h:7-11) */
@@ -167,6 +169,17 @@ typedef struct yar_delta_light_desc {
     float penumbra_angle;       /* spot, radians */
 } yar_delta_light_desc;
 
+/* Diffuse_Triangle_Mesh_Light, src/lib/light.h:82-86: a one-sided emitting
+ * mesh.  It is sampled in proportion to triangle area over the mesh's own
+ * vertices (Diffuse_Triangle_Mesh_Light_Sampler, src/ref/light_sampling.cpp:
+ * 126-184), and the scene object that shows it carries
+ * YAR_LIGHT_DIFFUSE_TRIANGLE_MESH with this light's index. */
+typedef struct yar_mesh_light_desc {
+    float light_to_world[12];
+    float emitted_radiance[3];
+    uint32_t triangle_mesh_index;  /* into yar_flat_scene::meshes */
+} yar_mesh_light_desc;
+
 /* Camera, src/ref/camera.h:35-49 (fields as computed by Camera::Camera, camera.cpp:5-14) */
 typedef struct yar_camera_desc {
     float camera_to_world[12];
@@ -205,13 +218,15 @@ typedef struct yar_flat_scene {
     const yar_material_desc* materials;
     uint32_t rect_light_count;
     const yar_rect_light_desc* rect_lights;
-    /* lights of other kinds (sphere, mesh, environment): counted for
+    /* lights of other kinds (sphere, environment): counted for
        total_light_count; rendering with any of them is unsupported */
     uint32_t other_light_count;
     yar_camera_desc camera;
     yar_render_config config;
     uint32_t delta_light_count;     /* point, spot and directional lights */
     const yar_delta_light_desc* delta_lights;
+    uint32_t mesh_light_count;      /* triangle-mesh lights */
+    const yar_mesh_light_desc* mesh_lights;
 } yar_flat_scene;
 
 /* One ray of a batch: 32 bytes, two float4.  tmax plays the role of the

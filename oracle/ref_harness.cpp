@@ -302,8 +302,15 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         memcpy(d.intensity, &l.irradiance.r, 12);
         out.delta_lights.push_back(d);
     }
+    for (const Diffuse_Triangle_Mesh_Light& l : ctx.lights.diffuse_triangle_mesh_lights) {
+        yar_mesh_light_desc d{};
+        matrix_to_floats(l.light_to_world_transform, d.light_to_world);
+        memcpy(d.emitted_radiance, &l.emitted_radiance.r, 12);
+        d.triangle_mesh_index = l.triangle_mesh_index;
+        out.mesh_lights.push_back(d);
+    }
     out.other_light_count = (uint32_t)(ctx.lights.total_light_count - (int)ctx.lights.diffuse_rectangular_lights.size() -
-                                       (int)out.delta_lights.size());
+                                       (int)out.delta_lights.size() - (int)out.mesh_lights.size());
 
     // Camera fields exactly as Camera::Camera computes them (src/ref/camera.cpp:5-14).
     const Matrix3x4& pose = scene.view_points[0];
@@ -589,7 +596,7 @@ int cmd_render_yfs(const Args& a) {
     std::string err;
     if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
     if (fs_scene.other_light_count) {
-        fprintf(stderr, "only rectangular, point, spot and directional lights are supported\n");
+        fprintf(stderr, "only rectangular, point, spot, directional and triangle-mesh lights are supported\n");
         return 1;
     }
     Scene scene;
@@ -697,6 +704,13 @@ int cmd_render_yfs(const Args& a) {
             fprintf(stderr, "unsupported light type %u\n", d.type);
             return 1;
         }
+    }
+    for (const yar_mesh_light_desc& d : fs_scene.mesh_lights) {
+        Diffuse_Triangle_Mesh_Light l;
+        l.light_to_world_transform = floats_to_matrix(d.light_to_world);
+        l.emitted_radiance = ColorRGB(d.emitted_radiance);
+        l.triangle_mesh_index = d.triangle_mesh_index;
+        scene.lights.diffuse_triangle_mesh_lights.push_back(l);
     }
     scene.lights.update_total_light_count();
     for (const yar_object_desc& d : fs_scene.objects) {

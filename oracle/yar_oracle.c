@@ -1171,6 +1171,160 @@ static col direct_delta(const yar_flat_scene* s, const shading_ctx* sc, const bs
     return mulcs(mulc(I, fv), penumbra_attenuation * fabsf(n_dot_wi) / (dist * dist));
 }
 
+/* Diffuse_Triangle_Mesh_Light_Sampler with its Distribution_1D over triangle
+ * areas, built as init_triangle_mesh_light_samplers does
+ * (src/ref/reference_renderer.cpp:131-151). */
+typedef struct mesh_light_sampler {
+    const yar_mesh_desc* mesh;
+    float mesh_area;
+    float interval_length;
+    float* cdf; /* triangle_count entries */
+} mesh_light_sampler;
+
+static v3 mesh_vertex(const yar_mesh_desc* m, uint32_t tri, int k) {
+    return ld3(m->vertices + 3 * (size_t)m->indices[3 * (size_t)tri + k]);
+}
+/* Triangle_Mesh::get_triangle_area, src/lib/triangle_mesh.h:103-109 */
+static float triangle_area(const yar_mesh_desc* m, uint32_t tri) {
+    v3 p0 = mesh_vertex(m, tri, 0), p1 = mesh_vertex(m, tri, 1), p2 = mesh_vertex(m, tri, 2);
+    return len3(cross3(sub3(p1, p0), sub3(p2, p0))) * 0.5f;
+}
+static void free_mesh_samplers(mesh_light_sampler* ms, uint32_t n) {
+    if (!ms) return;
+    for (uint32_t i = 0; i < n; i++) free(ms[i].cdf);
+    free(ms);
+}
+/* Triangle_Mesh::get_area (:111-118) and Distribution_1D::initialize (src/ref/sampling.cpp:149-166) */
+static int build_mesh_samplers(const yar_flat_scene* s, mesh_light_sampler** out) {
+    *out = NULL;
+    if (!s->mesh_light_count) return YAR_OK;
+    mesh_light_sampler* ms = (mesh_light_sampler*)calloc(s->mesh_light_count, sizeof(mesh_light_sampler));
+    if (!ms) return YAR_ERR_CAPACITY;
+    for (uint32_t i = 0; i < s->mesh_light_count; i++) {
+        const uint32_t mi = s->mesh_lights[i].triangle_mesh_index;
+        if (mi >= s->mesh_count || s->meshes[mi].triangle_count == 0) {
+            free_mesh_samplers(ms, s->mesh_light_count);
+            return YAR_ERR_INVALID;
+        }
+        const yar_mesh_desc* m = &s->meshes[mi];
+        const uint32_t n = m->triangle_count;
+        ms[i].mesh = m;
+        ms[i].cdf = (float*)malloc(sizeof(float) * n);
+        if (!ms[i].cdf) {
+            free_mesh_samplers(ms, s->mesh_light_count);
+            return YAR_ERR_CAPACITY;
+        }
+        float area = 0.f;
+        for (uint32_t t = 0; t < n; t++) area += triangle_area(m, t);
+        ms[i].mesh_area = area;
+        ms[i].interval_length = 1.f / (float)n;
+        float total = 0.f, sum = 0.f;
+        for (uint32_t t = 0; t < n; t++) total += triangle_area(m, t);
+        for (uint32_t t = 0; t < n; t++) {
+            sum += triangle_area(m, t);
+            ms[i].cdf[t] = sum / total;
+        }
+    }
+    *out = ms;
+    return YAR_OK;
+}
+
+/* The light's normal at a point of triangle tri: the interpolated vertex normal
+ * (not normalised) or the geometric normal (Triangle_Mesh::get_normal /
+ * get_geometric_normal, src/lib/triangle_mesh.h:61-77). */
+static v3 mesh_light_normal(const yar_mesh_desc* m, uint32_t tri, const float b[3]) {
+    if (m->normals) {
+        const int32_t* vi = m->indices + 3 * (size_t)tri;
+        v3 n[3] = {ld3(m->normals + 3 * (size_t)vi[0]), ld3(m->normals + 3 * (size_t)vi[1]),
+                   ld3(m->normals + 3 * (size_t)vi[2])};
+        return bary3(n, b);
+    }
+    v3 p0 = mesh_vertex(m, tri, 0), p1 = mesh_vertex(m, tri, 1), p2 = mesh_vertex(m, tri, 2);
+    v3 gn = norm3(cross3(sub3(p1, p0), sub3(p2, p0)));
+    return m->reverse_geometric_normal_orientation ? neg3(gn) : gn;
+}
+
+/* Diffuse_Triangle_Mesh_Light_Sampler::sample (src/ref/light_sampling.cpp:126-161) with
+ * sample_from_CDF (src/ref/sampling.cpp:98-147) and uniform_sample_triangle_baricentrics (:69-77) */
+static v3 mesh_light_sample(const mesh_light_sampler* ms, float u0, float u1, v3 shading_pos, float* pdf) {
+    const uint32_t n = ms->mesh->triangle_count;
+    uint32_t k = 0;
+    while (k < n - 1 && ms->cdf[k] < u0) k++; /* std::lower_bound */
+    const float cdf_a = k == 0 ? 0.f : ms->cdf[k - 1], cdf_b = ms->cdf[k];
+    const float fraction = (u0 - cdf_a) / (cdf_b - cdf_a);
+    float x = ((float)k + fraction) * ms->interval_length;
+    x = x < ONE_MINUS_EPSILON ? x : ONE_MINUS_EPSILON;
+    const float remapped = fraction < ONE_MINUS_EPSILON ? fraction : ONE_MINUS_EPSILON;
+    uint32_t tri = (uint32_t)(x * (float)n);
+    if (tri > n - 1) tri = n - 1;
+    const float a = sqrtf(remapped);
+    float b[3];
+    b[0] = 1 - a;
+    b[1] = u1 * a;
+    b[2] = 1.f - b[0] - b[1];
+    v3 p[3] = {mesh_vertex(ms->mesh, tri, 0), mesh_vertex(ms->mesh, tri, 1), mesh_vertex(ms->mesh, tri, 2)};
+    v3 light_p = bary3(p, b);
+    v3 light_n = mesh_light_normal(ms->mesh, tri, b);
+    v3 lv = sub3(light_p, shading_pos);
+    float d2 = len2_3(lv);
+    v3 wi = div3s(lv, sqrtf(d2));
+    float lndw = dot3(light_n, neg3(wi));
+    *pdf = lndw <= 0.f ? 0.f : d2 / (lndw * ms->mesh_area);
+    return light_p;
+}
+
+/* direct_lighting_from_triangle_mesh_light, src/ref/direct_lighting.cpp:262-322 */
+static col direct_mesh(const yar_flat_scene* s, const shading_ctx* sc, const bsdf_t* f, const mesh_light_sampler* ms,
+                       int light_index, float ul0, float ul1, float ub0, float ub1, float u_scatter) {
+    const col Le = ldc(s->mesh_lights[light_index].emitted_radiance);
+    col out = mkc(0, 0, 0);
+    int have = 0;
+    {
+        float light_pdf;
+        v3 lp = mesh_light_sample(ms, ul0, ul1, sc->position, &light_pdf);
+        if (light_pdf != 0.f) {
+            v3 position = origin_for_point(sc, lp);
+            v3 lv = sub3(lp, position);
+            float dist = len3(lv);
+            v3 wi = div3s(lv, dist);
+            float ndw = dot3(sc->normal, wi);
+            int possible = (ndw > 0.f && f->reflection) || (ndw < 0.f && f->transmission);
+            if (possible) {
+                col fv = bsdf_evaluate(f, sc->wo, wi);
+                if (!blackc(fv) && !trace_any(s, position, wi, dist * (1.f - 1e-5f))) {
+                    float bpdf = bsdf_pdf(f, sc->wo, wi);
+                    float w = mis_power(light_pdf, bpdf);
+                    out = addc(out, mulcs(mulc(Le, fv), w * fabsf(ndw) / light_pdf));
+                    have = 1;
+                }
+            }
+        }
+    }
+    {
+        v3 wi;
+        float bpdf;
+        col fv = bsdf_sample(f, ub0, ub1, u_scatter, sc->wo, &wi, &bpdf);
+        if (!blackc(fv)) {
+            v3 position = origin_for_direction(sc, wi);
+            hit_state h;
+            if (trace_closest(s, position, wi, &h) > 0) {
+                const yar_object_desc* o = &s->objects[h.object];
+                if (o->area_light_type == YAR_LIGHT_DIFFUSE_TRIANGLE_MESH && o->area_light_index == light_index) {
+                    /* Diffuse_Triangle_Mesh_Light_Sampler::pdf (light_sampling.cpp:163-184) */
+                    v3 light_n = mesh_light_normal(ms->mesh, h.prim, h.b);
+                    float lndw = dot3(light_n, neg3(wi));
+                    float light_pdf = lndw <= 0.f ? 0.f : (h.t * h.t) / (lndw * ms->mesh_area);
+                    float w = mis_power(bpdf, light_pdf);
+                    col c = mulcs(mulc(Le, fv), w * fabsf(dot3(sc->normal, wi)) / bpdf);
+                    out = have ? addc(out, c) : addc(mkc(0, 0, 0), c);
+                    have = 1;
+                }
+            }
+        }
+    }
+    return out;
+}
+
 typedef struct sampler_view {
     const float* s1d;   /* this sample's 1d dims */
     const float* s2d;   /* this sample's 2d dims (pairs) */
@@ -1247,10 +1401,27 @@ static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, floa
     return 1;
 }
 
+/* get_emitted_radiance, src/ref/direct_lighting.cpp:386-413: rectangular lights
+ * emit on both sides, triangle-mesh lights only on the side their normal faces. */
+static int emitted_radiance(const yar_flat_scene* s, const shading_ctx* sc, col* le) {
+    if (sc->light_type == YAR_LIGHT_DIFFUSE_RECTANGULAR) {
+        *le = ldc(s->rect_lights[sc->light_index].emitted_radiance);
+        return 1;
+    }
+    if (sc->light_type == YAR_LIGHT_DIFFUSE_TRIANGLE_MESH && !sc->flipped) {
+        *le = ldc(s->mesh_lights[sc->light_index].emitted_radiance);
+        return 1;
+    }
+    return 0;
+}
+
 /* trace_path, src/ref/path_tracing.cpp:11-133 */
-static int trace_path(const yar_flat_scene* s, v3 ro, v3 rd, sampler_view* sv, col* radiance) {
+static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_samplers, v3 ro, v3 rd,
+                      sampler_view* sv, col* radiance) {
     const yar_render_config* cfg = &s->config;
-    const int total_lights = (int)(s->delta_light_count + s->rect_light_count + s->other_light_count);
+    const int total_lights =
+        (int)(s->delta_light_count + s->rect_light_count + s->mesh_light_count + s->other_light_count);
+    col le;
     col coeff = mkc(1, 1, 1), L = mkc(0, 0, 0);
     int bounce = 0;
     int traced_by_delta_bounce = 0;
@@ -1263,8 +1434,7 @@ static int trace_path(const yar_flat_scene* s, v3 ro, v3 rd, sampler_view* sv, c
             if (hit < 0) return YAR_ERR_CAPACITY;
             if (hit) init_shading(s, rd, h.object, h.prim, h.b, &sc);
             if (bounce == 0) {
-                if (hit && sc.light_type == YAR_LIGHT_DIFFUSE_RECTANGULAR)
-                    L = addc(L, mulc(coeff, ldc(s->rect_lights[sc.light_index].emitted_radiance)));
+                if (hit && emitted_radiance(s, &sc, &le)) L = addc(L, mulc(coeff, le));
                 if (cfg->max_light_bounces == 0) break;
             }
             if (!hit || sc.light_type != YAR_LIGHT_NULL) break;
@@ -1290,10 +1460,13 @@ static int trace_path(const yar_flat_scene* s, v3 ro, v3 rd, sampler_view* sv, c
             if (rc != YAR_OK) return rc;
             /* estimate_direct_lighting_from_single_sample, src/ref/direct_lighting.cpp:522-578 */
             int light_index = (int)(u_light_index * (float)total_lights);
-            col one = light_index < (int)s->delta_light_count
-                          ? direct_delta(s, &sc, &f, &s->delta_lights[light_index])
-                          : direct_rect(s, &sc, &f, light_index - (int)s->delta_light_count, ul0, ul1, ub0, ub1,
-                                        u_scatter);
+            /* point, spot, directional, rectangular, then triangle-mesh lights */
+            const int rect_first = (int)s->delta_light_count, mesh_first = rect_first + (int)s->rect_light_count;
+            col one = light_index < rect_first ? direct_delta(s, &sc, &f, &s->delta_lights[light_index])
+                      : light_index < mesh_first
+                          ? direct_rect(s, &sc, &f, light_index - rect_first, ul0, ul1, ub0, ub1, u_scatter)
+                          : direct_mesh(s, &sc, &f, &mesh_samplers[light_index - mesh_first], light_index - mesh_first,
+                                        ul0, ul1, ub0, ub1, u_scatter);
             col direct = mulcs(one, (float)total_lights);
             L = addc(L, mulc(coeff, direct));
 
@@ -1314,8 +1487,7 @@ static int trace_path(const yar_flat_scene* s, v3 ro, v3 rd, sampler_view* sv, c
             if (hit < 0) return YAR_ERR_CAPACITY;
             if (hit) init_shading(s, rd, h.object, h.prim, h.b, &sc);
             coeff = mulc(coeff, datten);
-            if (hit && sc.light_type == YAR_LIGHT_DIFFUSE_RECTANGULAR)
-                L = addc(L, mulc(coeff, ldc(s->rect_lights[sc.light_index].emitted_radiance)));
+            if (hit && emitted_radiance(s, &sc, &le)) L = addc(L, mulc(coeff, le));
             bounce++;
             if (bounce == cfg->max_light_bounces) break;
             if (!hit || sc.light_type != YAR_LIGHT_NULL) break;
@@ -1350,6 +1522,7 @@ typedef struct render_job {
     int* tile_bounds;           /* per tile: px0, py0, px1, py1 */
     double* tile_variance;
     int next_tile;
+    mesh_light_sampler* mesh_samplers;
     pthread_mutex_t lock;
     int status;
 } render_job;
@@ -1429,7 +1602,7 @@ static int render_tile(render_job* J, int t) {
                 camera_ray(&s->camera, fx, fy, &o, &d);
                 sampler_view sv = {s1d + (size_t)k * n1d, s2d + 2 * (size_t)k * n2d, n1d, n2d, 0, 0, &rng};
                 col radiance;
-                rc = trace_path(s, o, d, &sv, &radiance);
+                rc = trace_path(s, J->mesh_samplers, o, d, &sv, &radiance);
                 if (rc != YAR_OK) break;
                 float limit = cfg->max_rgb_component_value_of_film_sample;
                 float mc = fmaxf_std(radiance.r, fmaxf_std(radiance.g, radiance.b));
@@ -1527,6 +1700,13 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
     J.tile_pixels = (film_px**)calloc(nt, sizeof(film_px*));
     J.tile_bounds = (int*)calloc(4 * (size_t)nt, sizeof(int));
     J.tile_variance = (double*)calloc(nt, sizeof(double));
+    int ms_rc = build_mesh_samplers(s, &J.mesh_samplers);
+    if (ms_rc != YAR_OK) {
+        free(J.tile_pixels);
+        free(J.tile_bounds);
+        free(J.tile_variance);
+        return ms_rc;
+    }
     pthread_mutex_init(&J.lock, NULL);
     J.status = YAR_OK;
     int nthreads = thread_count > 0 ? thread_count : 1;
@@ -1577,6 +1757,7 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
     free(J.tile_pixels);
     free(J.tile_bounds);
     free(J.tile_variance);
+    free_mesh_samplers(J.mesh_samplers, s->mesh_light_count);
     pthread_mutex_destroy(&J.lock);
     return rc;
 }

@@ -37,6 +37,11 @@ Fixtures
                              rendered by the reference from the flat scene.
   cornell_lights_64.yfs / .npz  the GGX Cornell box lit also by a point, a
                              spot (with penumbra) and a distant light, seed 7.
+  cornell_meshlight_64.yfs / .npz  the GGX Cornell box with two hexagonal
+                             emitting meshes (triangle-mesh lights: one with
+                             geometric normals on the ceiling, one with vertex
+                             normals on the left wall) besides the quad light,
+                             seed 8.
 """
 import os
 import re
@@ -217,6 +222,19 @@ def cornell_lights_64():
                         variance=np.float64(info["variance"]))
 
 
+def cornell_meshlight_64():
+    """The GGX Cornell box with two triangle-mesh lights besides the quad light."""
+    with tempfile.TemporaryDirectory() as d:
+        pbrt = os.path.join(d, "cornell_meshlight.pbrt")
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=8, width=64, height=64, spp=16, maxdepth=8,
+                                                  box_materials=scenes.GGX_BOXES, mesh_lights=scenes.MESH_LIGHTS))
+        yfs = os.path.join(HERE, "cornell_meshlight_64.yfs")
+        oracle.ref_flatten(pbrt, yfs, seed_offset=1)
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_meshlight_64.npz"), image=img,
+                        variance=np.float64(info["variance"]))
+
+
 def kdtree_cache_files():
     """The reference's kd-tree cache files (KdTree::save) of the raycast_small
     scene's first two meshes and of its scene tree."""
@@ -260,7 +278,8 @@ if __name__ == "__main__":
         sys.exit("oracle/_ref/yar_ref is not built (oracle/build_ref.sh)")
     which = sys.argv[1:] or ["raycast_small", "transform_small", "kdtree_regression", "cornell_c1_64",
                              "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "cornell_layered_64",
-                             "cornell_layered_yar_64", "cornell_lights_64", "exr_files",
+                             "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64",
+                             "exr_files",
                              "kdtree_cache_files"]
     for name in which:
         globals()[name]()

@@ -92,6 +92,41 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
                                    std::cos(std::max(0.f, l.cone_angle - l.penumbra_angle)));
     }
     R.host_delta_lights.assign(scene->delta_lights, scene->delta_lights + scene->delta_light_count);
+    // Triangle-mesh lights: init_triangle_mesh_light_samplers (src/ref/reference_renderer.cpp:131-151)
+    // with Triangle_Mesh::get_area / get_triangle_area and Distribution_1D::initialize
+    // (src/ref/sampling.cpp:149-166), in the reference's float order.
+    std::vector<uint32_t> mesh_first(scene->mesh_count + 1, 0);
+    for (uint32_t m = 0; m < scene->mesh_count; m++) mesh_first[m + 1] = mesh_first[m] + scene->meshes[m].triangle_count;
+    std::vector<Mesh_Light_Dev> mlights(std::max<uint32_t>(1, scene->mesh_light_count));
+    std::vector<float> cdf;
+    for (uint32_t i = 0; i < scene->mesh_light_count; i++) {
+        const yar_mesh_light_desc& l = scene->mesh_lights[i];
+        if (l.triangle_mesh_index >= scene->mesh_count || scene->meshes[l.triangle_mesh_index].triangle_count == 0)
+            return fail(ctx, YAR_ERR_INVALID, "triangle-mesh light " + std::to_string(i) + " has no valid mesh");
+        const yar_mesh_desc& mesh = scene->meshes[l.triangle_mesh_index];
+        auto area = [&](uint32_t t) {
+            float p[3][3];
+            for (int k = 0; k < 3; k++) memcpy(p[k], mesh.vertices + 3 * (size_t)mesh.indices[3 * (size_t)t + k], 12);
+            const float e1[3] = {p[1][0] - p[0][0], p[1][1] - p[0][1], p[1][2] - p[0][2]};
+            const float e2[3] = {p[2][0] - p[0][0], p[2][1] - p[0][1], p[2][2] - p[0][2]};
+            const float c[3] = {e1[1] * e2[2] - e1[2] * e2[1], e1[2] * e2[0] - e1[0] * e2[2],
+                                e1[0] * e2[1] - e1[1] * e2[0]};
+            return std::sqrt(c[0] * c[0] + c[1] * c[1] + c[2] * c[2]) * 0.5f;
+        };
+        float mesh_area = 0.f;
+        for (uint32_t t = 0; t < mesh.triangle_count; t++) mesh_area += area(t);
+        const uint32_t offset = (uint32_t)cdf.size();
+        float total = 0.f, sum = 0.f;
+        for (uint32_t t = 0; t < mesh.triangle_count; t++) total += area(t);
+        for (uint32_t t = 0; t < mesh.triangle_count; t++) {
+            sum += area(t);
+            cdf.push_back(sum / total);
+        }
+        mlights[i].le = make_float4(l.emitted_radiance[0], l.emitted_radiance[1], l.emitted_radiance[2], mesh_area);
+        mlights[i].info = make_uint4(mesh_first[l.triangle_mesh_index], mesh.triangle_count, offset, 0u);
+    }
+    if (cdf.empty()) cdf.push_back(1.f);
+    R.mesh_light_count = scene->mesh_light_count;
     R.host_materials.assign(scene->materials, scene->materials + scene->material_count);
     R.host_rect_lights.assign(scene->rect_lights, scene->rect_lights + scene->rect_light_count);
     R.host_object_info.resize(4 * (size_t)scene->object_count);
@@ -114,6 +149,8 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
     if ((rc = up(R.materials, mats.data(), mats.size() * sizeof(Material_Dev))) != YAR_OK) return rc;
     if ((rc = up(R.rect_lights, lights.data(), lights.size() * sizeof(Rect_Light_Dev))) != YAR_OK) return rc;
     if ((rc = up(R.delta_lights, dlights.data(), dlights.size() * sizeof(Delta_Light_Dev))) != YAR_OK) return rc;
+    if ((rc = up(R.mesh_lights, mlights.data(), mlights.size() * sizeof(Mesh_Light_Dev))) != YAR_OK) return rc;
+    if ((rc = up(R.mesh_cdf, cdf.data(), cdf.size() * sizeof(float))) != YAR_OK) return rc;
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render upload");
     return YAR_OK;
@@ -121,8 +158,8 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
 
 void render_release(yar_gpu_ctx* ctx) {
     Render_Scene& R = ctx->render;
-    for (Device_Buffer* b : {&R.shading, &R.materials, &R.rect_lights, &R.delta_lights, &R.object_info,
-                             &R.object_to_world, &R.object_to_world_normal})
+    for (Device_Buffer* b : {&R.shading, &R.materials, &R.rect_lights, &R.delta_lights, &R.mesh_lights, &R.mesh_cdf,
+                             &R.object_info, &R.object_to_world, &R.object_to_world_normal})
         device_free(*b);
     for (Device_Buffer& b : ctx->render_scratch) device_free(b);
     ctx->render_scratch.clear();
@@ -197,7 +234,8 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
     q.counters = dptr<uint32_t>(B[26]);
     Scene_Dev S{ctx->ds, dptr<float4>(ctx->render.shading), dptr<float4>(ctx->render.object_info),
                 dptr<Material_Dev>(ctx->render.materials), dptr<Rect_Light_Dev>(ctx->render.rect_lights),
-                dptr<Delta_Light_Dev>(ctx->render.delta_lights)};
+                dptr<Delta_Light_Dev>(ctx->render.delta_lights),
+                dptr<Mesh_Light_Dev>(ctx->render.mesh_lights), dptr<float>(ctx->render.mesh_cdf)};
     float4* radiance = dptr<float4>(B[0]);
     float2* image_samples = dptr<float2>(B[1]);
 
@@ -364,7 +402,8 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
         return fail(ctx, YAR_ERR_CAPACITY, "static arena layout overflow");
     Scene_Dev S{ctx->ds, dptr<float4>(ctx->render.shading), dptr<float4>(ctx->render.object_info),
                 dptr<Material_Dev>(ctx->render.materials), dptr<Rect_Light_Dev>(ctx->render.rect_lights),
-                dptr<Delta_Light_Dev>(ctx->render.delta_lights)};
+                dptr<Delta_Light_Dev>(ctx->render.delta_lights),
+                dptr<Mesh_Light_Dev>(ctx->render.mesh_lights), dptr<float>(ctx->render.mesh_cdf)};
 
     cudaStream_t st = ctx->stream;
     cudaError_t e = cudaMemsetAsync(q.counters, 0, 8 * sizeof(uint32_t), st);  // the arena keeps the last call's data

@@ -48,6 +48,9 @@ constexpr uint64_t kChunkSampleBudget = 16u << 20;  // paths in flight per chunk
 // kDeltaArrival: the path's extend ray left a delta vertex (mirror, perfect
 // refractor, smooth glass) and its hit is shaded as the reference's delta
 // branch does; kDeltaFinal: that delta vertex used the last bounce.
+// What the MIS probe of a vertex must hit: pend_probe2.z
+enum : uint32_t { kProbeRectLight = 0, kProbeMeshLight = 1 };
+
 enum : uint32_t {
     kPendShadow = 1u << 24,
     kPendProbe = 1u << 25,
@@ -70,6 +73,15 @@ struct Delta_Light_Dev {
     float4 a, b, c;
 };
 
+// Triangle-mesh lights (Diffuse_Triangle_Mesh_Light_Sampler, light_sampling.cpp:126-184):
+//   le = emitted radiance rgb, mesh area
+//   info = first triangle of the mesh in the scene's triangle arrays, triangle
+//          count, offset of its CDF in Scene_Dev::mesh_cdf, -
+struct Mesh_Light_Dev {
+    float4 le;
+    uint4 info;
+};
+
 struct Render_Params {
     yar_camera_desc camera;
     int32_t sx0, sy0, sw, sh;    // sample region
@@ -80,7 +92,7 @@ struct Render_Params {
     float rr_threshold;
     float filter_radius;
     float film_scale, max_component;
-    int32_t total_lights, delta_lights, rect_lights;  // delta lights come first in the selection order
+    int32_t total_lights, delta_lights, rect_lights, mesh_lights;  // selection order: delta, rect, mesh
     int32_t full_shading;  // the scene needs shade_kernel<*, true>
     uint32_t seed_offset;
     uint32_t stream_hi;  // upper 32 bits of the pixel streams' sequence (0 = the reference's streams)
@@ -172,6 +184,8 @@ struct Scene_Dev {
     const Material_Dev* materials;
     const Rect_Light_Dev* lights;
     const Delta_Light_Dev* delta_lights;
+    const Mesh_Light_Dev* mesh_lights;
+    const float* mesh_cdf;
 };
 
 // Warp-aggregated queue append: one atomic per warp and predicate value.
@@ -530,6 +544,58 @@ __device__ __forceinline__ float2 next2d(Dims& d) {
     return make_float2(a, b);
 }
 
+// ---------------------------------------------------------------- triangle-mesh lights
+// The light's normal at barycentrics b of global triangle g: the interpolated
+// vertex normal (not normalised) or the geometric normal
+// (Triangle_Mesh::get_normal / get_geometric_normal, src/lib/triangle_mesh.h:61-77).
+__device__ __forceinline__ V3 mesh_light_normal(const Scene_Dev& S, size_t g, float b0, float b1, float b2) {
+    const float4 h0 = __ldg(S.shading + 4 * g), h1 = __ldg(S.shading + 4 * g + 1);
+    const float4 h2 = __ldg(S.shading + 4 * g + 2), h3 = __ldg(S.shading + 4 * g + 3);
+    const uint32_t flags = __float_as_uint(h3.w);
+    if (flags & 1u) return bary(v3(h0.x, h0.y, h0.z), v3(h1.x, h1.y, h1.z), v3(h2.x, h2.y, h2.z), b0, b1, b2);
+    const float4 q0 = __ldg(S.ds.tris + 3 * g), q1 = __ldg(S.ds.tris + 3 * g + 1), q2 = __ldg(S.ds.tris + 3 * g + 2);
+    const V3 p0 = v3(q0.x, q0.y, q0.z);
+    const V3 gn = normalized(cross(v3(q1.x, q1.y, q1.z) - p0, v3(q2.x, q2.y, q2.z) - p0));
+    return (flags & 4u) ? -gn : gn;
+}
+
+// Diffuse_Triangle_Mesh_Light_Sampler::sample (light_sampling.cpp:126-161): a
+// triangle by sample_from_CDF over the area CDF (sampling.cpp:98-147), the
+// remapped first sample and the second one give uniform barycentrics
+// (uniform_sample_triangle_baricentrics, sampling.cpp:69-77).  pdf is per solid
+// angle from shading_pos, 0 on the light's back side.
+__device__ __forceinline__ V3 mesh_light_sample(const Scene_Dev& S, uint4 info, float mesh_area, float u0, float u1,
+                                                V3 shading_pos, float& pdf) {
+    const float* cdf = S.mesh_cdf + info.z;
+    const uint32_t n = info.y;
+    uint32_t lo = 0, hi = n;  // std::lower_bound
+    while (lo < hi) {
+        const uint32_t mid = (lo + hi) >> 1;
+        if (__ldg(cdf + mid) < u0) lo = mid + 1;
+        else hi = mid;
+    }
+    const uint32_t k = lo < n ? lo : n - 1;
+    const float cdf_a = k == 0 ? 0.f : __ldg(cdf + k - 1), cdf_b = __ldg(cdf + k);
+    const float fraction = (u0 - cdf_a) / (cdf_b - cdf_a);
+    const float x = one_minus_eps_min(((float)k + fraction) * (1.f / (float)n));
+    const float remapped = one_minus_eps_min(fraction);
+    uint32_t tri = (uint32_t)(x * (float)n);
+    if (tri > n - 1) tri = n - 1;
+    const float a = sqrtf(remapped);
+    const float b0 = 1 - a, b1 = u1 * a;
+    const float b2 = 1.f - b0 - b1;
+    const size_t g = (size_t)info.x + tri;
+    const float4 q0 = __ldg(S.ds.tris + 3 * g), q1 = __ldg(S.ds.tris + 3 * g + 1), q2 = __ldg(S.ds.tris + 3 * g + 2);
+    const V3 light_p = bary(v3(q0.x, q0.y, q0.z), v3(q1.x, q1.y, q1.z), v3(q2.x, q2.y, q2.z), b0, b1, b2);
+    const V3 light_n = mesh_light_normal(S, g, b0, b1, b2);
+    const V3 lv = light_p - shading_pos;
+    const float d2 = len2(lv);
+    const V3 wi = divs(lv, sqrtf(d2));
+    const float lndw = dot(light_n, -wi);
+    pdf = lndw <= 0.f ? 0.f : d2 / (lndw * mesh_area);
+    return light_p;
+}
+
 // ---------------------------------------------------------------- shade
 // GUIDED adds the learned proposal to the continuation: with probability
 // g.alpha the direction comes from the vertex's lobe mixture instead of the
@@ -574,8 +640,13 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
             // Emission seen by a camera ray or by a delta ray (the delta vertex
             // already applied its attenuation and counted the bounce).
             if (bounce == 0 || arrival) {
+                // get_emitted_radiance (direct_lighting.cpp:386-413): triangle-mesh
+                // lights emit only on the side their normal faces
                 if (is_light && (uint32_t)oinfo.z == YAR_LIGHT_DIFFUSE_RECTANGULAR) {
                     const float4 le = __ldg(&S.lights[oinfo.w].le);
+                    L = L + coeff * col(le.x, le.y, le.z);
+                } else if (FULL && is_light && (uint32_t)oinfo.z == YAR_LIGHT_DIFFUSE_TRIANGLE_MESH && !sc.flipped) {
+                    const float4 le = __ldg(&S.mesh_lights[oinfo.w].le);
                     L = L + coeff * col(le.x, le.y, le.z);
                 }
                 if (arrival ? (info & kDeltaFinal) != 0 : p.max_bounces == 0) done = true;
@@ -698,6 +769,54 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                 sh_a = make_float4(position.x, position.y, position.z, tmax);
                                 sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
                                 pend |= kPendShadow;
+                            }
+                        }
+                    } else if (FULL && selected >= p.delta_lights + p.rect_lights) {
+                        // direct_lighting_from_triangle_mesh_light (direct_lighting.cpp:262-322)
+                        const int light_index = selected - p.delta_lights - p.rect_lights;
+                        const Mesh_Light_Dev& M = S.mesh_lights[light_index];
+                        const float4 mle = __ldg(&M.le);
+                        const uint4 minfo = __ldg(&M.info);
+                        const Col Le = col(mle.x, mle.y, mle.z);
+                        {   // light-sampling half of MIS
+                            float light_pdf;
+                            const V3 lp = mesh_light_sample(S, minfo, mle.w, ul.x, ul.y, sc.position, light_pdf);
+                            if (light_pdf != 0.f) {
+                                const V3 position = origin_for_point(sc, lp);
+                                const V3 lv = lp - position;
+                                const float dist = len(lv);
+                                const V3 wi = divs(lv, dist);
+                                const float ndw = dot(sc.n, wi);
+                                if ((ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission)) {
+                                    const Col fv = bsdf_evaluate<FULL>(f, sc.wo, wi);
+                                    if (!black(fv)) {
+                                        const float bpdf = bsdf_pdf<FULL>(f, sc.wo, wi);
+                                        const float w = mis_power(light_pdf, bpdf);
+                                        const Col c = mul(Le * fv, w * fabsf(ndw) / light_pdf);
+                                        ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
+                                        want_shadow = true;
+                                        sh_a = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
+                                        sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                        pend |= kPendShadow;
+                                    }
+                                }
+                            }
+                        }
+                        {   // BSDF-sampling half of MIS: the probe ray must hit this light
+                            V3 wi;
+                            float bpdf = 0.f;
+                            const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_scatter, sc.wo, wi, bpdf);
+                            if (!black(fv)) {
+                                const V3 position = origin_for_direction(sc, wi);
+                                const Col lef = Le * fv;
+                                ps.pend_probe0[slot] = make_float4(lef.r, lef.g, lef.b, bpdf);
+                                ps.pend_probe1[slot] = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                ps.pend_probe2[slot] = make_float4(dot(sc.n, wi), __int_as_float(light_index),
+                                                                   __uint_as_float(kProbeMeshLight), 0.f);
+                                want_probe = true;
+                                pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
+                                pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                pend |= kPendProbe;
                             }
                         }
                     } else {
@@ -888,10 +1007,24 @@ connect_kernel(Render_Params p, Scene_Dev S, const uint32_t* __restrict__ slots,
             const uint2 h2 = ps.probe_hit2[slot];
             const float4 p2 = ps.pend_probe2[slot];
             const int light_index = __float_as_int(p2.y);
+            const uint32_t kind = __float_as_uint(p2.z);
             if (h2.y != 0xffffffffu) {
                 const float4 inf4 = __ldg(S.obj_render + 7 * (size_t)h2.y + 6);
-                if ((uint32_t)__float_as_int(inf4.z) == YAR_LIGHT_DIFFUSE_RECTANGULAR &&
+                const uint32_t hit_light = (uint32_t)__float_as_int(inf4.z);
+                if (kind == kProbeMeshLight && hit_light == YAR_LIGHT_DIFFUSE_TRIANGLE_MESH &&
                     __float_as_int(inf4.w) == light_index) {
+                    // Diffuse_Triangle_Mesh_Light_Sampler::pdf (light_sampling.cpp:163-184)
+                    const float4 h4 = ps.probe_hit4[slot];
+                    const Mesh_Light_Dev& M = S.mesh_lights[light_index];
+                    const size_t g = (size_t)__ldg(&M.info).x + h2.x;
+                    const float4 p0 = ps.pend_probe0[slot], p1 = ps.pend_probe1[slot];
+                    const V3 light_n = mesh_light_normal(S, g, h4.y, h4.z, h4.w);
+                    const float lndw = dot(light_n, -v3(p1.x, p1.y, p1.z));
+                    const float light_pdf = lndw <= 0.f ? 0.f : (h4.x * h4.x) / (lndw * __ldg(&M.le).w);
+                    const float w = mis_power(p0.w, light_pdf);
+                    direct = direct + mul(col(p0.x, p0.y, p0.z), w * fabsf(p2.x) / p0.w);
+                } else if (kind == kProbeRectLight && hit_light == YAR_LIGHT_DIFFUSE_RECTANGULAR &&
+                           __float_as_int(inf4.w) == light_index) {
                     const float4 h4 = ps.probe_hit4[slot];
                     const uint32_t tri_offset = __float_as_uint(__ldg(S.ds.objects + 6 * (size_t)h2.y + 4).w);
                     const size_t g = (size_t)tri_offset + h2.x;
@@ -1151,8 +1284,9 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     if (c.rendering_algorithm != 1) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the path tracer is implemented");
     if (c.pixel_filter_type != 0) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the box filter is implemented");
     if (R.other_light_count)
-        return fail(ctx, YAR_ERR_UNSUPPORTED, "only rectangular, point, spot and directional lights are implemented");
-    if (R.host_rect_lights.empty() && R.host_delta_lights.empty())
+        return fail(ctx, YAR_ERR_UNSUPPORTED,
+                    "only rectangular, point, spot, directional and triangle-mesh lights are implemented");
+    if (R.host_rect_lights.empty() && R.host_delta_lights.empty() && R.mesh_light_count == 0)
         return fail(ctx, YAR_ERR_UNSUPPORTED, "scene has no light");
     for (size_t i = 0; i < R.host_delta_lights.size(); i++) {
         const uint32_t t = R.host_delta_lights[i].type;
@@ -1169,8 +1303,11 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     for (size_t i = 0; i < n_obj; i++) {
         const int32_t* o = &R.host_object_info[4 * i];
         const bool light = (uint32_t)o[2] != YAR_LIGHT_NULL;
-        if (light && ((uint32_t)o[2] != YAR_LIGHT_DIFFUSE_RECTANGULAR || o[3] < 0 ||
-                      (size_t)o[3] >= R.host_rect_lights.size()))
+        const bool rect_ok = (uint32_t)o[2] == YAR_LIGHT_DIFFUSE_RECTANGULAR && o[3] >= 0 &&
+                             (size_t)o[3] < R.host_rect_lights.size();
+        const bool mesh_ok = (uint32_t)o[2] == YAR_LIGHT_DIFFUSE_TRIANGLE_MESH && o[3] >= 0 &&
+                             (uint32_t)o[3] < R.mesh_light_count;
+        if (light && !rect_ok && !mesh_ok)
             return fail(ctx, YAR_ERR_UNSUPPORTED, "object " + std::to_string(i) + ": unsupported area light");
         if (!light && (o[1] < 0 || (size_t)o[1] >= R.host_materials.size()))
             return fail(ctx, YAR_ERR_INVALID, "object " + std::to_string(i) + " has no valid material");
@@ -1212,8 +1349,9 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     p.max_component = c.max_rgb_component_value_of_film_sample;
     p.rect_lights = (int)R.host_rect_lights.size();
     p.delta_lights = (int)R.host_delta_lights.size();
-    p.total_lights = p.delta_lights + p.rect_lights + (int)R.other_light_count;
-    p.full_shading = p.delta_lights > 0;
+    p.mesh_lights = (int)R.mesh_light_count;
+    p.total_lights = p.delta_lights + p.rect_lights + p.mesh_lights + (int)R.other_light_count;
+    p.full_shading = p.delta_lights > 0 || p.mesh_lights > 0;
     for (const yar_material_desc& m : R.host_materials)
         if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL &&
             !(m.type == YAR_MATERIAL_GLASS && m.u_roughness > 0.f))

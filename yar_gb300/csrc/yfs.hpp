@@ -3,8 +3,8 @@
 // The file carries exactly what the device path consumes: meshes with their
 // kd-trees (node words bit for bit as KdTree::save writes them,
 // src/ref/kdtree.cpp:137-160), scene objects, the scene kd-tree, constant
-// materials, rectangular lights, point/spot/directional lights (an optional
-// chunk), camera and Raytracer_Config.  It is produced
+// materials, rectangular lights, point/spot/directional and triangle-mesh
+// lights (optional chunks), camera and Raytracer_Config.  It is produced
 // by the host scene loader of this library and by the reference-side adapter
 // that flattens a reference Scene_Context, so both sides can be compared on
 // identical bytes.
@@ -42,6 +42,7 @@ struct Scene {
     std::vector<yar_material_desc> materials;
     std::vector<yar_rect_light_desc> rect_lights;
     std::vector<yar_delta_light_desc> delta_lights;
+    std::vector<yar_mesh_light_desc> mesh_lights;
     uint32_t other_light_count = 0;
     yar_camera_desc camera{};
     yar_render_config config{};
@@ -84,6 +85,8 @@ struct Scene {
         s.config = config;
         s.delta_light_count = (uint32_t)delta_lights.size();
         s.delta_lights = delta_lights.empty() ? nullptr : delta_lights.data();
+        s.mesh_light_count = (uint32_t)mesh_lights.size();
+        s.mesh_lights = mesh_lights.empty() ? nullptr : mesh_lights.data();
         return s;
     }
 };
@@ -188,6 +191,13 @@ inline bool write(const std::string& path, const Scene& s) {
         b.raw(s.delta_lights.data(), n * sizeof(yar_delta_light_desc));
         w.chunk("DLIT", b.b);
     }
+    if (!s.mesh_lights.empty()) {
+        detail::Buf b;
+        uint32_t n = (uint32_t)s.mesh_lights.size();
+        b.pod(n);
+        b.raw(s.mesh_lights.data(), n * sizeof(yar_mesh_light_desc));
+        w.chunk("MLIT", b.b);
+    }
     bool ok = w.ok;
     if (fclose(f) != 0) ok = false;
     return ok;
@@ -270,6 +280,11 @@ inline bool read(const std::string& path, Scene& s, std::string* err = nullptr) 
             if ((uint64_t)n * sizeof(yar_delta_light_desc) > size) return fail("bad delta light chunk");
             s.delta_lights.resize(n);
             c.raw(s.delta_lights.data(), n * sizeof(yar_delta_light_desc));
+        } else if (!memcmp(tag, "MLIT", 4)) {
+            uint32_t n = c.pod<uint32_t>();
+            if ((uint64_t)n * sizeof(yar_mesh_light_desc) > size) return fail("bad mesh light chunk");
+            s.mesh_lights.resize(n);
+            c.raw(s.mesh_lights.data(), n * sizeof(yar_mesh_light_desc));
         }
         if (!c.ok) return fail("truncated chunk payload");
     }

@@ -87,6 +87,11 @@ class DeltaLightDesc(C.Structure):
                 ("intensity", C.c_float * 3), ("cone_angle", C.c_float), ("penumbra_angle", C.c_float)]
 
 
+class MeshLightDesc(C.Structure):
+    _fields_ = [("light_to_world", C.c_float * 12), ("emitted_radiance", C.c_float * 3),
+                ("triangle_mesh_index", C.c_uint32)]
+
+
 class FlatSceneDesc(C.Structure):
     _fields_ = [("mesh_count", C.c_uint32), ("meshes", C.POINTER(MeshDesc)),
                 ("object_count", C.c_uint32), ("objects", C.POINTER(ObjectDesc)),
@@ -94,7 +99,8 @@ class FlatSceneDesc(C.Structure):
                 ("material_count", C.c_uint32), ("materials", C.POINTER(MaterialDesc)),
                 ("rect_light_count", C.c_uint32), ("rect_lights", C.POINTER(RectLightDesc)),
                 ("other_light_count", C.c_uint32), ("camera", CameraDesc), ("config", RenderConfig),
-                ("delta_light_count", C.c_uint32), ("delta_lights", C.POINTER(DeltaLightDesc))]
+                ("delta_light_count", C.c_uint32), ("delta_lights", C.POINTER(DeltaLightDesc)),
+                ("mesh_light_count", C.c_uint32), ("mesh_lights", C.POINTER(MeshLightDesc))]
 
 
 class HitSoa(C.Structure):

@@ -24,6 +24,8 @@ LIGHT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("emitted_radiance", "<f4
                         ("sample_count", "<i4")])
 DELTA_LIGHT_DTYPE = np.dtype([("type", "<u4"), ("position", "<f4", 3), ("direction", "<f4", 3),
                               ("intensity", "<f4", 3), ("cone_angle", "<f4"), ("penumbra_angle", "<f4")])
+MESH_LIGHT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("emitted_radiance", "<f4", 3),
+                             ("triangle_mesh_index", "<u4")])
 CAMERA_DTYPE = np.dtype([("camera_to_world", "<f4", 12), ("image_extent", "<f4", 2), ("horz_half_dist", "<f4"),
                          ("vert_half_dist", "<f4"), ("z_is_up", "<i4")])
 CONFIG_DTYPE = np.dtype([("render_region", "<i4", 4), ("rendering_algorithm", "<i4"), ("max_light_bounces", "<i4"),
@@ -38,6 +40,7 @@ assert OBJECT_DTYPE.itemsize == C.sizeof(native.ObjectDesc)
 assert MATERIAL_DTYPE.itemsize == C.sizeof(native.MaterialDesc)
 assert LIGHT_DTYPE.itemsize == C.sizeof(native.RectLightDesc)
 assert DELTA_LIGHT_DTYPE.itemsize == C.sizeof(native.DeltaLightDesc)
+assert MESH_LIGHT_DTYPE.itemsize == C.sizeof(native.MeshLightDesc)
 assert CAMERA_DTYPE.itemsize == C.sizeof(native.CameraDesc)
 assert CONFIG_DTYPE.itemsize == C.sizeof(native.RenderConfig)
 
@@ -90,6 +93,7 @@ class FlatScene:
         self.rect_lights = np.zeros(0, LIGHT_DTYPE)
         # point, spot and directional lights, in that order
         self.delta_lights = np.zeros(0, DELTA_LIGHT_DTYPE)
+        self.mesh_lights = np.zeros(0, MESH_LIGHT_DTYPE)  # triangle-mesh lights
         self.other_light_count = 0
         self.camera = np.zeros((), CAMERA_DTYPE)
         self.config = default_config()
@@ -166,8 +170,9 @@ class FlatScene:
         materials = np.ascontiguousarray(self.materials)
         lights = np.ascontiguousarray(self.rect_lights)
         dlights = np.ascontiguousarray(self.delta_lights)
+        mlights = np.ascontiguousarray(self.mesh_lights)
         snodes = np.ascontiguousarray(self.scene_nodes, np.uint32)
-        keep += [objects, materials, lights, dlights, snodes, meshes]
+        keep += [objects, materials, lights, dlights, mlights, snodes, meshes]
         s = native.FlatSceneDesc()
         s.mesh_count = len(self.meshes)
         s.meshes = meshes
@@ -184,6 +189,8 @@ class FlatScene:
         s.other_light_count = int(self.other_light_count)
         s.delta_light_count = dlights.shape[0]
         s.delta_lights = C.cast(dlights.ctypes.data, C.POINTER(native.DeltaLightDesc)) if dlights.size else None
+        s.mesh_light_count = mlights.shape[0]
+        s.mesh_lights = C.cast(mlights.ctypes.data, C.POINTER(native.MeshLightDesc)) if mlights.size else None
         C.memmove(C.byref(s.camera), np.ascontiguousarray(self.camera).ctypes.data, CAMERA_DTYPE.itemsize)
         C.memmove(C.byref(s.config), np.ascontiguousarray(self.config).ctypes.data, CONFIG_DTYPE.itemsize)
         return s, keep
@@ -215,6 +222,8 @@ class FlatScene:
         parts.append(chunk(b"RLIT", struct.pack("<I", self.rect_lights.shape[0]) + self.rect_lights.tobytes()))
         if self.delta_lights.shape[0]:
             parts.append(chunk(b"DLIT", struct.pack("<I", self.delta_lights.shape[0]) + self.delta_lights.tobytes()))
+        if self.mesh_lights.shape[0]:
+            parts.append(chunk(b"MLIT", struct.pack("<I", self.mesh_lights.shape[0]) + self.mesh_lights.tobytes()))
         with open(path, "wb") as f:
             f.write(b"".join(parts))
 
@@ -271,6 +280,9 @@ class FlatScene:
             elif tag == b"DLIT":
                 n = struct.unpack_from("<I", p, 0)[0]
                 s.delta_lights = np.frombuffer(p[4:4 + n * DELTA_LIGHT_DTYPE.itemsize], DELTA_LIGHT_DTYPE).copy()
+            elif tag == b"MLIT":
+                n = struct.unpack_from("<I", p, 0)[0]
+                s.mesh_lights = np.frombuffer(p[4:4 + n * MESH_LIGHT_DTYPE.itemsize], MESH_LIGHT_DTYPE).copy()
         return s
 
 

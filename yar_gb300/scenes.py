@@ -180,7 +180,7 @@ def _box(center, size, angle_deg):
 
 
 def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0, box_materials=None,
-                 upper_light=None, light_sources=()):
+                 upper_light=None, light_sources=(), mesh_lights=()):
     """pbrt-v3 text of the seeded Cornell box (34 triangles + a quad light).
 
     box_materials: None for matte boxes, or two pbrt material statements for
@@ -189,7 +189,10 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
     above the ceiling, facing down; it reaches the room only through a ceiling
     that transmits (a perfect refractor set on the flattened scene).
     light_sources: pbrt LightSource statements added to the world (point,
-    spot, distant)."""
+    spot, distant).
+    mesh_lights: (vertices, indices, normals or None, radiance) emitting
+    triangle meshes that are not rectangles (the reference makes them
+    triangle-mesh lights)."""
     rng = np.random.default_rng(seed)
     k = int(math.ceil(math.sqrt(spp)))
     shapes = []
@@ -233,6 +236,14 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
             '  AreaLightSource "diffuse" "rgb L" [%s]' % fmt([light_radiance] * 3),
             '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(light[1]), fmt(light[0])),
             "AttributeEnd"]
+    for v, i, n, radiance in mesh_lights:
+        shape = '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(i), fmt(v))
+        if n is not None:
+            shape += ' "normal N" [%s]' % fmt(n)
+        out += ["AttributeBegin",
+                '  AreaLightSource "diffuse" "rgb L" [%s]' % fmt(radiance),
+                shape,
+                "AttributeEnd"]
     if upper_light is not None:
         uh, uy, ul = upper_light
         v, i = _quad((-uh, uy, -uh), (uh, uy, -uh), (uh, uy, uh), (-uh, uy, uh))
@@ -252,6 +263,38 @@ LAYERED_BOXES = ('Material "plastic" "rgb Kd" [0.6 0.25 0.1] "rgb Ks" [0.4 0.4 0
                  '"float uroughness" [0.1] "float vroughness" [0.3]')
 
 UPPER_LIGHT = (0.8, 2.3, 4.0)
+
+
+def hexagon(center, radius, axis, facing):
+    """A 6-triangle fan in the plane normal to `axis` (0 x, 1 y, 2 z), wound
+    so that its geometric normal points along `facing` (+1 or -1)."""
+    c = np.asarray(center, np.float32)
+    u, w = [(1, 2), (2, 0), (0, 1)][axis]
+    ring = []
+    for k in range(6):
+        t = 2 * math.pi * k / 6
+        p = c.copy()
+        p[u] += radius * math.cos(t)
+        p[w] += radius * math.sin(t)
+        ring.append(p)
+    v = np.array([c] + ring, np.float32)
+    idx = [[0, 1 + k, 1 + (k + 1) % 6] for k in range(6)]
+    e1, e2 = v[1] - v[0], v[2] - v[0]
+    if np.cross(e1, e2)[axis] * facing < 0:
+        idx = [[a, b2, b1] for a, b1, b2 in idx]
+    return v, np.array(idx, np.int32)
+
+
+def _mesh_lights():
+    ceiling_v, ceiling_i = hexagon((0.45, 1.97, 0.35), 0.12, 1, -1)
+    wall_v, wall_i = hexagon((-0.98, 1.2, -0.3), 0.15, 0, +1)
+    wall_n = np.tile(np.array([[1.0, 0.0, 0.0]], np.float32), (wall_v.shape[0], 1))
+    return ((ceiling_v, ceiling_i, None, (6.0, 5.5, 5.0)), (wall_v, wall_i, wall_n, (1.5, 2.0, 3.0)))
+
+
+# A hexagonal light on the ceiling (geometric normal) and one on the left wall
+# (vertex normals), both triangle-mesh lights.
+MESH_LIGHTS = _mesh_lights()
 
 # A point light low in the room, a spot light from the ceiling onto the boxes
 # with a penumbra, and a distant light through the open front.
