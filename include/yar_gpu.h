@@ -169,6 +169,17 @@ typedef struct yar_delta_light_desc {
     float penumbra_angle;       /* spot, radians */
 } yar_delta_light_desc;
 
+/* Diffuse_Sphere_Light, src/lib/light.h:75-80: sampled over the cone it
+ * subtends (Diffuse_Sphere_Light_Sampler, src/ref/light_sampling.cpp:76-123);
+ * the scene object that shows it (a tessellated sphere) carries
+ * YAR_LIGHT_DIFFUSE_SPHERE with this light's index. */
+typedef struct yar_sphere_light_desc {
+    float position[3];
+    float emitted_radiance[3];
+    float radius;
+    int32_t sample_count;
+} yar_sphere_light_desc;
+
 /* Diffuse_Triangle_Mesh_Light, src/lib/light.h:82-86: a one-sided emitting
  * mesh.  It is sampled in proportion to triangle area over the mesh's own
  * vertices (Diffuse_Triangle_Mesh_Light_Sampler, src/ref/light_sampling.cpp:
@@ -218,8 +229,8 @@ typedef struct yar_flat_scene {
     const yar_material_desc* materials;
     uint32_t rect_light_count;
     const yar_rect_light_desc* rect_lights;
-    /* lights of other kinds (sphere, environment): counted for
-       total_light_count; rendering with any of them is unsupported */
+    /* lights of other kinds (environment): counted for total_light_count;
+       rendering with any of them is unsupported */
     uint32_t other_light_count;
     yar_camera_desc camera;
     yar_render_config config;
@@ -227,6 +238,8 @@ typedef struct yar_flat_scene {
     const yar_delta_light_desc* delta_lights;
     uint32_t mesh_light_count;      /* triangle-mesh lights */
     const yar_mesh_light_desc* mesh_lights;
+    uint32_t sphere_light_count;    /* sphere lights */
+    const yar_sphere_light_desc* sphere_lights;
 } yar_flat_scene;
 
 /* One ray of a batch: 32 bytes, two float4.  tmax plays the role of the

@@ -309,8 +309,17 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         d.triangle_mesh_index = l.triangle_mesh_index;
         out.mesh_lights.push_back(d);
     }
+    for (const Diffuse_Sphere_Light& l : ctx.lights.diffuse_sphere_lights) {
+        yar_sphere_light_desc d{};
+        memcpy(d.position, &l.position.x, 12);
+        memcpy(d.emitted_radiance, &l.emitted_radiance.r, 12);
+        d.radius = l.radius;
+        d.sample_count = l.sample_count;
+        out.sphere_lights.push_back(d);
+    }
     out.other_light_count = (uint32_t)(ctx.lights.total_light_count - (int)ctx.lights.diffuse_rectangular_lights.size() -
-                                       (int)out.delta_lights.size() - (int)out.mesh_lights.size());
+                                       (int)out.delta_lights.size() - (int)out.mesh_lights.size() -
+                                       (int)out.sphere_lights.size());
 
     // Camera fields exactly as Camera::Camera computes them (src/ref/camera.cpp:5-14).
     const Matrix3x4& pose = scene.view_points[0];
@@ -596,7 +605,7 @@ int cmd_render_yfs(const Args& a) {
     std::string err;
     if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
     if (fs_scene.other_light_count) {
-        fprintf(stderr, "only rectangular, point, spot, directional and triangle-mesh lights are supported\n");
+        fprintf(stderr, "only rectangular, point, spot, directional, triangle-mesh and sphere lights are supported\n");
         return 1;
     }
     Scene scene;
@@ -704,6 +713,14 @@ int cmd_render_yfs(const Args& a) {
             fprintf(stderr, "unsupported light type %u\n", d.type);
             return 1;
         }
+    }
+    for (const yar_sphere_light_desc& d : fs_scene.sphere_lights) {
+        Diffuse_Sphere_Light l;
+        l.position = Vector3(d.position);
+        l.emitted_radiance = ColorRGB(d.emitted_radiance);
+        l.radius = d.radius;
+        l.sample_count = d.sample_count;
+        scene.lights.diffuse_sphere_lights.push_back(l);
     }
     for (const yar_mesh_light_desc& d : fs_scene.mesh_lights) {
         Diffuse_Triangle_Mesh_Light l;

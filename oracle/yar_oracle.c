@@ -1325,6 +1325,91 @@ static col direct_mesh(const yar_flat_scene* s, const shading_ctx* sc, const bsd
     return out;
 }
 
+/* Diffuse_Sphere_Light_Sampler (src/ref/light_sampling.cpp:76-123), built per
+ * shading point, and direct_lighting_from_sphere_light (direct_lighting.cpp:196-260). */
+typedef struct sphere_sampler {
+    v3 center, axes[3];
+    float radius, d_center, cos_theta_max, cone_pdf;
+} sphere_sampler;
+
+static void sphere_sampler_init(sphere_sampler* ss, const yar_sphere_light_desc* L, v3 shading_pos) {
+    ss->center = ld3(L->position);
+    ss->radius = L->radius;
+    v3 a2 = sub3(shading_pos, ss->center);
+    ss->d_center = len3(a2);
+    a2 = div3s(a2, ss->d_center);
+    /* coordinate_system_from_vector, src/lib/math.cpp:21-25 */
+    v3 a0 = fabsf(a2.x) > fabsf(a2.y) ? mk3(-a2.z, 0, a2.x) : mk3(0, -a2.z, a2.y);
+    a0 = div3s(a0, len3(a0));
+    ss->axes[0] = a0;
+    ss->axes[1] = cross3(a2, a0);
+    ss->axes[2] = a2;
+    float sin_theta_max = ss->radius / ss->d_center;
+    ss->cos_theta_max = sqrtf(fmaxf_std(0.f, 1.f - sin_theta_max * sin_theta_max));
+    ss->cone_pdf = 1.f / (2.f * PI_F * (1.f - ss->cos_theta_max));
+}
+
+static v3 sphere_sampler_sample(const sphere_sampler* ss, float u0, float u1) {
+    float radius2 = ss->radius * ss->radius;
+    float d_center2 = ss->d_center * ss->d_center;
+    float cos_theta = (1.f - u0) + u0 * ss->cos_theta_max;
+    float phi = 2.f * PI_F * u1;
+    float sin_theta2 = fmaxf_std(0.f, 1.f - cos_theta * cos_theta);
+    float d_sample = ss->d_center * cos_theta - sqrtf(fmaxf_std(0.f, radius2 - d_center2 * sin_theta2));
+    float cos_alpha = (d_center2 + radius2 - d_sample * d_sample) / (2.f * ss->d_center * ss->radius);
+    float sin_alpha = sqrtf(fmaxf_std(0.f, 1.f - cos_alpha * cos_alpha));
+    v3 dir = add3(add3(mul3s(ss->axes[0], sin_alpha * cos_sample(phi)), mul3s(ss->axes[1], sin_alpha * sin_sample(phi))),
+                  mul3s(ss->axes[2], cos_alpha));
+    return add3(mul3s(dir, ss->radius), ss->center);
+}
+
+static col direct_sphere(const yar_flat_scene* s, const shading_ctx* sc, const bsdf_t* f, int light_index, float ul0,
+                         float ul1, float ub0, float ub1, float u_scatter) {
+    const yar_sphere_light_desc* L = &s->sphere_lights[light_index];
+    const col Le = ldc(L->emitted_radiance);
+    sphere_sampler ss;
+    sphere_sampler_init(&ss, L, sc->position);
+    col out = mkc(0, 0, 0);
+    int have = 0;
+    {
+        v3 lp = sphere_sampler_sample(&ss, ul0, ul1);
+        v3 position = origin_for_point(sc, lp);
+        v3 lv = sub3(lp, position);
+        float dist = len3(lv);
+        v3 wi = div3s(lv, dist);
+        float ndw = dot3(sc->normal, wi);
+        int possible = (ndw > 0.f && f->reflection) || (ndw < 0.f && f->transmission);
+        if (possible) {
+            col fv = bsdf_evaluate(f, sc->wo, wi);
+            if (!blackc(fv) && !trace_any(s, position, wi, dist * (1.f - 1e-5f))) {
+                float bpdf = bsdf_pdf(f, sc->wo, wi);
+                float w = mis_power(ss.cone_pdf, bpdf);
+                out = addc(out, mulcs(mulc(Le, fv), w * fabsf(ndw) / ss.cone_pdf));
+                have = 1;
+            }
+        }
+    }
+    {
+        v3 wi;
+        float bpdf;
+        col fv = bsdf_sample(f, ub0, ub1, u_scatter, sc->wo, &wi, &bpdf);
+        if (!blackc(fv) && dot3(neg3(ss.axes[2]), wi) >= ss.cos_theta_max) {
+            v3 position = origin_for_direction(sc, wi);
+            hit_state h;
+            if (trace_closest(s, position, wi, &h) > 0) {
+                const yar_object_desc* o = &s->objects[h.object];
+                if (o->area_light_type == YAR_LIGHT_DIFFUSE_SPHERE && o->area_light_index == light_index) {
+                    float w = mis_power(bpdf, ss.cone_pdf);
+                    col c = mulcs(mulc(Le, fv), w * fabsf(dot3(sc->normal, wi)) / bpdf);
+                    out = have ? addc(out, c) : addc(mkc(0, 0, 0), c);
+                    have = 1;
+                }
+            }
+        }
+    }
+    return out;
+}
+
 typedef struct sampler_view {
     const float* s1d;   /* this sample's 1d dims */
     const float* s2d;   /* this sample's 2d dims (pairs) */
@@ -1408,6 +1493,10 @@ static int emitted_radiance(const yar_flat_scene* s, const shading_ctx* sc, col*
         *le = ldc(s->rect_lights[sc->light_index].emitted_radiance);
         return 1;
     }
+    if (sc->light_type == YAR_LIGHT_DIFFUSE_SPHERE) {
+        *le = ldc(s->sphere_lights[sc->light_index].emitted_radiance);
+        return 1;
+    }
     if (sc->light_type == YAR_LIGHT_DIFFUSE_TRIANGLE_MESH && !sc->flipped) {
         *le = ldc(s->mesh_lights[sc->light_index].emitted_radiance);
         return 1;
@@ -1419,8 +1508,8 @@ static int emitted_radiance(const yar_flat_scene* s, const shading_ctx* sc, col*
 static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_samplers, v3 ro, v3 rd,
                       sampler_view* sv, col* radiance) {
     const yar_render_config* cfg = &s->config;
-    const int total_lights =
-        (int)(s->delta_light_count + s->rect_light_count + s->mesh_light_count + s->other_light_count);
+    const int total_lights = (int)(s->delta_light_count + s->rect_light_count + s->sphere_light_count +
+                                   s->mesh_light_count + s->other_light_count);
     col le;
     col coeff = mkc(1, 1, 1), L = mkc(0, 0, 0);
     int bounce = 0;
@@ -1460,11 +1549,14 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
             if (rc != YAR_OK) return rc;
             /* estimate_direct_lighting_from_single_sample, src/ref/direct_lighting.cpp:522-578 */
             int light_index = (int)(u_light_index * (float)total_lights);
-            /* point, spot, directional, rectangular, then triangle-mesh lights */
-            const int rect_first = (int)s->delta_light_count, mesh_first = rect_first + (int)s->rect_light_count;
+            /* point, spot, directional, rectangular, sphere, then triangle-mesh lights */
+            const int rect_first = (int)s->delta_light_count, sphere_first = rect_first + (int)s->rect_light_count;
+            const int mesh_first = sphere_first + (int)s->sphere_light_count;
             col one = light_index < rect_first ? direct_delta(s, &sc, &f, &s->delta_lights[light_index])
-                      : light_index < mesh_first
+                      : light_index < sphere_first
                           ? direct_rect(s, &sc, &f, light_index - rect_first, ul0, ul1, ub0, ub1, u_scatter)
+                      : light_index < mesh_first
+                          ? direct_sphere(s, &sc, &f, light_index - sphere_first, ul0, ul1, ub0, ub1, u_scatter)
                           : direct_mesh(s, &sc, &f, &mesh_samplers[light_index - mesh_first], light_index - mesh_first,
                                         ul0, ul1, ub0, ub1, u_scatter);
             col direct = mulcs(one, (float)total_lights);

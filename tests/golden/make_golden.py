@@ -42,6 +42,10 @@ Fixtures
                              geometric normals on the ceiling, one with vertex
                              normals on the left wall) besides the quad light,
                              seed 8.
+  cornell_spherelight_64.yfs / .npz  cornell_ggx_64 with two emitting spheres
+                             (sphere lights shown by level-2 icospheres, added
+                             on the flat scene), rendered by the reference from
+                             the flat scene.
 """
 import os
 import re
@@ -235,6 +239,16 @@ def cornell_meshlight_64():
                         variance=np.float64(info["variance"]))
 
 
+def cornell_spherelight_64():
+    """cornell_ggx_64 with two sphere lights."""
+    s = FlatScene.read(os.path.join(HERE, "cornell_ggx_64.yfs"))
+    scenes.add_sphere_lights(s)
+    s.write(os.path.join(HERE, "cornell_spherelight_64.yfs"))
+    img, info = oracle.ref_render_flat(s, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_spherelight_64.npz"), image=img,
+                        variance=np.float64(info["variance"]))
+
+
 def kdtree_cache_files():
     """The reference's kd-tree cache files (KdTree::save) of the raycast_small
     scene's first two meshes and of its scene tree."""
@@ -279,6 +293,7 @@ if __name__ == "__main__":
     which = sys.argv[1:] or ["raycast_small", "transform_small", "kdtree_regression", "cornell_c1_64",
                              "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "cornell_layered_64",
                              "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64",
+                             "cornell_spherelight_64",
                              "exr_files",
                              "kdtree_cache_files"]
     for name in which:

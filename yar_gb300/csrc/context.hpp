@@ -29,6 +29,7 @@ struct Render_Scene {
     Device_Buffer delta_lights; // point, spot and directional lights (Delta_Light_Dev[])
     Device_Buffer mesh_lights;  // triangle-mesh lights (Mesh_Light_Dev[])
     Device_Buffer mesh_cdf;     // their triangle-area CDFs, concatenated
+    Device_Buffer sphere_lights; // Sphere_Light_Dev[]
     Device_Buffer object_info;  // int4 per object: material type, material index, light type, light index
     Device_Buffer object_to_world;         // float[12] per object
     Device_Buffer object_to_world_normal;  // float[12] per object
@@ -36,6 +37,7 @@ struct Render_Scene {
     std::vector<yar_rect_light_desc> host_rect_lights;
     std::vector<yar_delta_light_desc> host_delta_lights;
     uint32_t mesh_light_count = 0;
+    uint32_t sphere_light_count = 0;
     std::vector<int32_t> host_object_info;
     yar_camera_desc camera{};
     yar_render_config config{};

@@ -127,6 +127,13 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
     }
     if (cdf.empty()) cdf.push_back(1.f);
     R.mesh_light_count = scene->mesh_light_count;
+    std::vector<Sphere_Light_Dev> slights(std::max<uint32_t>(1, scene->sphere_light_count));
+    for (uint32_t i = 0; i < scene->sphere_light_count; i++) {
+        const yar_sphere_light_desc& l = scene->sphere_lights[i];
+        slights[i].a = make_float4(l.position[0], l.position[1], l.position[2], l.radius);
+        slights[i].le = make_float4(l.emitted_radiance[0], l.emitted_radiance[1], l.emitted_radiance[2], 0.f);
+    }
+    R.sphere_light_count = scene->sphere_light_count;
     R.host_materials.assign(scene->materials, scene->materials + scene->material_count);
     R.host_rect_lights.assign(scene->rect_lights, scene->rect_lights + scene->rect_light_count);
     R.host_object_info.resize(4 * (size_t)scene->object_count);
@@ -151,6 +158,7 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
     if ((rc = up(R.delta_lights, dlights.data(), dlights.size() * sizeof(Delta_Light_Dev))) != YAR_OK) return rc;
     if ((rc = up(R.mesh_lights, mlights.data(), mlights.size() * sizeof(Mesh_Light_Dev))) != YAR_OK) return rc;
     if ((rc = up(R.mesh_cdf, cdf.data(), cdf.size() * sizeof(float))) != YAR_OK) return rc;
+    if ((rc = up(R.sphere_lights, slights.data(), slights.size() * sizeof(Sphere_Light_Dev))) != YAR_OK) return rc;
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render upload");
     return YAR_OK;
@@ -159,7 +167,7 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
 void render_release(yar_gpu_ctx* ctx) {
     Render_Scene& R = ctx->render;
     for (Device_Buffer* b : {&R.shading, &R.materials, &R.rect_lights, &R.delta_lights, &R.mesh_lights, &R.mesh_cdf,
-                             &R.object_info, &R.object_to_world, &R.object_to_world_normal})
+                             &R.sphere_lights, &R.object_info, &R.object_to_world, &R.object_to_world_normal})
         device_free(*b);
     for (Device_Buffer& b : ctx->render_scratch) device_free(b);
     ctx->render_scratch.clear();
@@ -235,7 +243,8 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
     Scene_Dev S{ctx->ds, dptr<float4>(ctx->render.shading), dptr<float4>(ctx->render.object_info),
                 dptr<Material_Dev>(ctx->render.materials), dptr<Rect_Light_Dev>(ctx->render.rect_lights),
                 dptr<Delta_Light_Dev>(ctx->render.delta_lights),
-                dptr<Mesh_Light_Dev>(ctx->render.mesh_lights), dptr<float>(ctx->render.mesh_cdf)};
+                dptr<Mesh_Light_Dev>(ctx->render.mesh_lights), dptr<float>(ctx->render.mesh_cdf),
+                dptr<Sphere_Light_Dev>(ctx->render.sphere_lights)};
     float4* radiance = dptr<float4>(B[0]);
     float2* image_samples = dptr<float2>(B[1]);
 
@@ -403,7 +412,8 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
     Scene_Dev S{ctx->ds, dptr<float4>(ctx->render.shading), dptr<float4>(ctx->render.object_info),
                 dptr<Material_Dev>(ctx->render.materials), dptr<Rect_Light_Dev>(ctx->render.rect_lights),
                 dptr<Delta_Light_Dev>(ctx->render.delta_lights),
-                dptr<Mesh_Light_Dev>(ctx->render.mesh_lights), dptr<float>(ctx->render.mesh_cdf)};
+                dptr<Mesh_Light_Dev>(ctx->render.mesh_lights), dptr<float>(ctx->render.mesh_cdf),
+                dptr<Sphere_Light_Dev>(ctx->render.sphere_lights)};
 
     cudaStream_t st = ctx->stream;
     cudaError_t e = cudaMemsetAsync(q.counters, 0, 8 * sizeof(uint32_t), st);  // the arena keeps the last call's data

@@ -49,7 +49,7 @@ constexpr uint64_t kChunkSampleBudget = 16u << 20;  // paths in flight per chunk
 // refractor, smooth glass) and its hit is shaded as the reference's delta
 // branch does; kDeltaFinal: that delta vertex used the last bounce.
 // What the MIS probe of a vertex must hit: pend_probe2.z
-enum : uint32_t { kProbeRectLight = 0, kProbeMeshLight = 1 };
+enum : uint32_t { kProbeRectLight = 0, kProbeMeshLight = 1, kProbeSphereLight = 2 };
 
 enum : uint32_t {
     kPendShadow = 1u << 24,
@@ -82,6 +82,11 @@ struct Mesh_Light_Dev {
     uint4 info;
 };
 
+// Sphere lights (Diffuse_Sphere_Light): a = center xyz, radius; le = emitted rgb.
+struct Sphere_Light_Dev {
+    float4 a, le;
+};
+
 struct Render_Params {
     yar_camera_desc camera;
     int32_t sx0, sy0, sw, sh;    // sample region
@@ -92,7 +97,7 @@ struct Render_Params {
     float rr_threshold;
     float filter_radius;
     float film_scale, max_component;
-    int32_t total_lights, delta_lights, rect_lights, mesh_lights;  // selection order: delta, rect, mesh
+    int32_t total_lights, delta_lights, rect_lights, sphere_lights, mesh_lights;  // in the selection order
     int32_t full_shading;  // the scene needs shade_kernel<*, true>
     uint32_t seed_offset;
     uint32_t stream_hi;  // upper 32 bits of the pixel streams' sequence (0 = the reference's streams)
@@ -186,6 +191,7 @@ struct Scene_Dev {
     const Delta_Light_Dev* delta_lights;
     const Mesh_Light_Dev* mesh_lights;
     const float* mesh_cdf;
+    const Sphere_Light_Dev* sphere_lights;
 };
 
 // Warp-aggregated queue append: one atomic per warp and predicate value.
@@ -596,6 +602,40 @@ __device__ __forceinline__ V3 mesh_light_sample(const Scene_Dev& S, uint4 info, 
     return light_p;
 }
 
+// ---------------------------------------------------------------- sphere lights
+// Diffuse_Sphere_Light_Sampler (light_sampling.cpp:76-123): the cone the
+// sphere subtends from the shading point, sampled uniformly in solid angle.
+struct Sphere_Sampler {
+    V3 center, axes[3];
+    float radius, d_center, cos_theta_max, cone_pdf;
+};
+__device__ __forceinline__ void sphere_sampler_init(Sphere_Sampler& ss, V3 center, float radius, V3 shading_pos) {
+    ss.center = center;
+    ss.radius = radius;
+    V3 a2 = shading_pos - center;
+    ss.d_center = len(a2);
+    a2 = divs(a2, ss.d_center);
+    ss.axes[0] = coordinate_axis(a2);  // coordinate_system_from_vector, src/lib/math.cpp:21-25
+    ss.axes[1] = cross(a2, ss.axes[0]);
+    ss.axes[2] = a2;
+    const float sin_theta_max = radius / ss.d_center;
+    ss.cos_theta_max = sqrtf(max_std(0.f, 1.f - sin_theta_max * sin_theta_max));
+    ss.cone_pdf = 1.f / (2.f * kPi * (1.f - ss.cos_theta_max));
+}
+__device__ __forceinline__ V3 sphere_sampler_sample(const Sphere_Sampler& ss, float u0, float u1) {
+    const float radius2 = ss.radius * ss.radius;
+    const float d_center2 = ss.d_center * ss.d_center;
+    const float cos_theta = (1.f - u0) + u0 * ss.cos_theta_max;
+    const float phi = 2.f * kPi * u1;
+    const float sin_theta2 = max_std(0.f, 1.f - cos_theta * cos_theta);
+    const float d_sample = ss.d_center * cos_theta - sqrtf(max_std(0.f, radius2 - d_center2 * sin_theta2));
+    const float cos_alpha = (d_center2 + radius2 - d_sample * d_sample) / (2.f * ss.d_center * ss.radius);
+    const float sin_alpha = sqrtf(max_std(0.f, 1.f - cos_alpha * cos_alpha));
+    const V3 dir = (mul(ss.axes[0], sin_alpha * cos_f(phi)) + mul(ss.axes[1], sin_alpha * sin_f(phi))) +
+                   mul(ss.axes[2], cos_alpha);
+    return mul(dir, ss.radius) + ss.center;
+}
+
 // ---------------------------------------------------------------- shade
 // GUIDED adds the learned proposal to the continuation: with probability
 // g.alpha the direction comes from the vertex's lobe mixture instead of the
@@ -647,6 +687,9 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                     L = L + coeff * col(le.x, le.y, le.z);
                 } else if (FULL && is_light && (uint32_t)oinfo.z == YAR_LIGHT_DIFFUSE_TRIANGLE_MESH && !sc.flipped) {
                     const float4 le = __ldg(&S.mesh_lights[oinfo.w].le);
+                    L = L + coeff * col(le.x, le.y, le.z);
+                } else if (FULL && is_light && (uint32_t)oinfo.z == YAR_LIGHT_DIFFUSE_SPHERE) {
+                    const float4 le = __ldg(&S.sphere_lights[oinfo.w].le);
                     L = L + coeff * col(le.x, le.y, le.z);
                 }
                 if (arrival ? (info & kDeltaFinal) != 0 : p.max_bounces == 0) done = true;
@@ -771,9 +814,56 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                 pend |= kPendShadow;
                             }
                         }
-                    } else if (FULL && selected >= p.delta_lights + p.rect_lights) {
-                        // direct_lighting_from_triangle_mesh_light (direct_lighting.cpp:262-322)
+                    } else if (FULL && selected >= p.delta_lights + p.rect_lights &&
+                               selected < p.delta_lights + p.rect_lights + p.sphere_lights) {
+                        // direct_lighting_from_sphere_light (direct_lighting.cpp:196-260)
                         const int light_index = selected - p.delta_lights - p.rect_lights;
+                        const Sphere_Light_Dev& SL = S.sphere_lights[light_index];
+                        const float4 sa = __ldg(&SL.a), sle = __ldg(&SL.le);
+                        const Col Le = col(sle.x, sle.y, sle.z);
+                        Sphere_Sampler ss;
+                        sphere_sampler_init(ss, v3(sa.x, sa.y, sa.z), sa.w, sc.position);
+                        {   // light-sampling half of MIS
+                            const V3 lp = sphere_sampler_sample(ss, ul.x, ul.y);
+                            const V3 position = origin_for_point(sc, lp);
+                            const V3 lv = lp - position;
+                            const float dist = len(lv);
+                            const V3 wi = divs(lv, dist);
+                            const float ndw = dot(sc.n, wi);
+                            if ((ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission)) {
+                                const Col fv = bsdf_evaluate<FULL>(f, sc.wo, wi);
+                                if (!black(fv)) {
+                                    const float bpdf = bsdf_pdf<FULL>(f, sc.wo, wi);
+                                    const float w = mis_power(ss.cone_pdf, bpdf);
+                                    const Col c = mul(Le * fv, w * fabsf(ndw) / ss.cone_pdf);
+                                    ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
+                                    want_shadow = true;
+                                    sh_a = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
+                                    sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                    pend |= kPendShadow;
+                                }
+                            }
+                        }
+                        {   // BSDF-sampling half of MIS: inside the light's cone, the probe must hit it
+                            V3 wi;
+                            float bpdf = 0.f;
+                            const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_scatter, sc.wo, wi, bpdf);
+                            if (!black(fv) && dot(-ss.axes[2], wi) >= ss.cos_theta_max) {
+                                const V3 position = origin_for_direction(sc, wi);
+                                const Col lef = Le * fv;
+                                ps.pend_probe0[slot] = make_float4(lef.r, lef.g, lef.b, bpdf);
+                                ps.pend_probe1[slot] = make_float4(wi.x, wi.y, wi.z, ss.cone_pdf);
+                                ps.pend_probe2[slot] = make_float4(dot(sc.n, wi), __int_as_float(light_index),
+                                                                   __uint_as_float(kProbeSphereLight), 0.f);
+                                want_probe = true;
+                                pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
+                                pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                pend |= kPendProbe;
+                            }
+                        }
+                    } else if (FULL && selected >= p.delta_lights + p.rect_lights + p.sphere_lights) {
+                        // direct_lighting_from_triangle_mesh_light (direct_lighting.cpp:262-322)
+                        const int light_index = selected - p.delta_lights - p.rect_lights - p.sphere_lights;
                         const Mesh_Light_Dev& M = S.mesh_lights[light_index];
                         const float4 mle = __ldg(&M.le);
                         const uint4 minfo = __ldg(&M.info);
@@ -1011,7 +1101,12 @@ connect_kernel(Render_Params p, Scene_Dev S, const uint32_t* __restrict__ slots,
             if (h2.y != 0xffffffffu) {
                 const float4 inf4 = __ldg(S.obj_render + 7 * (size_t)h2.y + 6);
                 const uint32_t hit_light = (uint32_t)__float_as_int(inf4.z);
-                if (kind == kProbeMeshLight && hit_light == YAR_LIGHT_DIFFUSE_TRIANGLE_MESH &&
+                if (kind == kProbeSphereLight && hit_light == YAR_LIGHT_DIFFUSE_SPHERE &&
+                    __float_as_int(inf4.w) == light_index) {
+                    const float4 p0 = ps.pend_probe0[slot], p1 = ps.pend_probe1[slot];
+                    const float w = mis_power(p0.w, p1.w);
+                    direct = direct + mul(col(p0.x, p0.y, p0.z), w * fabsf(p2.x) / p0.w);
+                } else if (kind == kProbeMeshLight && hit_light == YAR_LIGHT_DIFFUSE_TRIANGLE_MESH &&
                     __float_as_int(inf4.w) == light_index) {
                     // Diffuse_Triangle_Mesh_Light_Sampler::pdf (light_sampling.cpp:163-184)
                     const float4 h4 = ps.probe_hit4[slot];
@@ -1284,9 +1379,9 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     if (c.rendering_algorithm != 1) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the path tracer is implemented");
     if (c.pixel_filter_type != 0) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the box filter is implemented");
     if (R.other_light_count)
-        return fail(ctx, YAR_ERR_UNSUPPORTED,
-                    "only rectangular, point, spot, directional and triangle-mesh lights are implemented");
-    if (R.host_rect_lights.empty() && R.host_delta_lights.empty() && R.mesh_light_count == 0)
+        return fail(ctx, YAR_ERR_UNSUPPORTED, "environment lights are not implemented");
+    if (R.host_rect_lights.empty() && R.host_delta_lights.empty() && R.mesh_light_count == 0 &&
+        R.sphere_light_count == 0)
         return fail(ctx, YAR_ERR_UNSUPPORTED, "scene has no light");
     for (size_t i = 0; i < R.host_delta_lights.size(); i++) {
         const uint32_t t = R.host_delta_lights[i].type;
@@ -1307,7 +1402,9 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
                              (size_t)o[3] < R.host_rect_lights.size();
         const bool mesh_ok = (uint32_t)o[2] == YAR_LIGHT_DIFFUSE_TRIANGLE_MESH && o[3] >= 0 &&
                              (uint32_t)o[3] < R.mesh_light_count;
-        if (light && !rect_ok && !mesh_ok)
+        const bool sphere_ok = (uint32_t)o[2] == YAR_LIGHT_DIFFUSE_SPHERE && o[3] >= 0 &&
+                               (uint32_t)o[3] < R.sphere_light_count;
+        if (light && !rect_ok && !mesh_ok && !sphere_ok)
             return fail(ctx, YAR_ERR_UNSUPPORTED, "object " + std::to_string(i) + ": unsupported area light");
         if (!light && (o[1] < 0 || (size_t)o[1] >= R.host_materials.size()))
             return fail(ctx, YAR_ERR_INVALID, "object " + std::to_string(i) + " has no valid material");
@@ -1350,8 +1447,9 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     p.rect_lights = (int)R.host_rect_lights.size();
     p.delta_lights = (int)R.host_delta_lights.size();
     p.mesh_lights = (int)R.mesh_light_count;
-    p.total_lights = p.delta_lights + p.rect_lights + p.mesh_lights + (int)R.other_light_count;
-    p.full_shading = p.delta_lights > 0 || p.mesh_lights > 0;
+    p.sphere_lights = (int)R.sphere_light_count;
+    p.total_lights = p.delta_lights + p.rect_lights + p.sphere_lights + p.mesh_lights + (int)R.other_light_count;
+    p.full_shading = p.delta_lights > 0 || p.mesh_lights > 0 || p.sphere_lights > 0;
     for (const yar_material_desc& m : R.host_materials)
         if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL &&
             !(m.type == YAR_MATERIAL_GLASS && m.u_roughness > 0.f))

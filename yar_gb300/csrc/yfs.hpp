@@ -3,8 +3,8 @@
 // The file carries exactly what the device path consumes: meshes with their
 // kd-trees (node words bit for bit as KdTree::save writes them,
 // src/ref/kdtree.cpp:137-160), scene objects, the scene kd-tree, constant
-// materials, rectangular lights, point/spot/directional and triangle-mesh
-// lights (optional chunks), camera and Raytracer_Config.  It is produced
+// materials, rectangular lights, point/spot/directional, triangle-mesh and
+// sphere lights (optional chunks), camera and Raytracer_Config.  It is produced
 // by the host scene loader of this library and by the reference-side adapter
 // that flattens a reference Scene_Context, so both sides can be compared on
 // identical bytes.
@@ -43,6 +43,7 @@ struct Scene {
     std::vector<yar_rect_light_desc> rect_lights;
     std::vector<yar_delta_light_desc> delta_lights;
     std::vector<yar_mesh_light_desc> mesh_lights;
+    std::vector<yar_sphere_light_desc> sphere_lights;
     uint32_t other_light_count = 0;
     yar_camera_desc camera{};
     yar_render_config config{};
@@ -87,6 +88,8 @@ struct Scene {
         s.delta_lights = delta_lights.empty() ? nullptr : delta_lights.data();
         s.mesh_light_count = (uint32_t)mesh_lights.size();
         s.mesh_lights = mesh_lights.empty() ? nullptr : mesh_lights.data();
+        s.sphere_light_count = (uint32_t)sphere_lights.size();
+        s.sphere_lights = sphere_lights.empty() ? nullptr : sphere_lights.data();
         return s;
     }
 };
@@ -198,6 +201,13 @@ inline bool write(const std::string& path, const Scene& s) {
         b.raw(s.mesh_lights.data(), n * sizeof(yar_mesh_light_desc));
         w.chunk("MLIT", b.b);
     }
+    if (!s.sphere_lights.empty()) {
+        detail::Buf b;
+        uint32_t n = (uint32_t)s.sphere_lights.size();
+        b.pod(n);
+        b.raw(s.sphere_lights.data(), n * sizeof(yar_sphere_light_desc));
+        w.chunk("SPHL", b.b);
+    }
     bool ok = w.ok;
     if (fclose(f) != 0) ok = false;
     return ok;
@@ -285,6 +295,11 @@ inline bool read(const std::string& path, Scene& s, std::string* err = nullptr) 
             if ((uint64_t)n * sizeof(yar_mesh_light_desc) > size) return fail("bad mesh light chunk");
             s.mesh_lights.resize(n);
             c.raw(s.mesh_lights.data(), n * sizeof(yar_mesh_light_desc));
+        } else if (!memcmp(tag, "SPHL", 4)) {
+            uint32_t n = c.pod<uint32_t>();
+            if ((uint64_t)n * sizeof(yar_sphere_light_desc) > size) return fail("bad sphere light chunk");
+            s.sphere_lights.resize(n);
+            c.raw(s.sphere_lights.data(), n * sizeof(yar_sphere_light_desc));
         }
         if (!c.ok) return fail("truncated chunk payload");
     }

@@ -24,11 +24,20 @@ YAR_ERR_NO_SCENE = -8
 YAR_BUFFERS_HOST = 0
 YAR_BUFFERS_DEVICE = 1
 
+MATERIAL_PERFECT_REFLECTOR = 0
+MATERIAL_PERFECT_REFRACTOR = 1
 MATERIAL_DIFFUSE = 2
 MATERIAL_METAL = 4
+MATERIAL_PLASTIC = 5
+MATERIAL_COATED_DIFFUSE = 6
 MATERIAL_GLASS = 7
 MATERIAL_NULL = 0xFFFFFFFF
+LIGHT_POINT = 0
+LIGHT_SPOT = 1
+LIGHT_DIRECTIONAL = 2
 LIGHT_RECT = 3
+LIGHT_SPHERE = 4
+LIGHT_TRIANGLE_MESH = 5
 LIGHT_NULL = 0xFFFFFFFF
 
 
@@ -92,6 +101,11 @@ class MeshLightDesc(C.Structure):
                 ("triangle_mesh_index", C.c_uint32)]
 
 
+class SphereLightDesc(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("emitted_radiance", C.c_float * 3), ("radius", C.c_float),
+                ("sample_count", C.c_int32)]
+
+
 class FlatSceneDesc(C.Structure):
     _fields_ = [("mesh_count", C.c_uint32), ("meshes", C.POINTER(MeshDesc)),
                 ("object_count", C.c_uint32), ("objects", C.POINTER(ObjectDesc)),
@@ -100,7 +114,8 @@ class FlatSceneDesc(C.Structure):
                 ("rect_light_count", C.c_uint32), ("rect_lights", C.POINTER(RectLightDesc)),
                 ("other_light_count", C.c_uint32), ("camera", CameraDesc), ("config", RenderConfig),
                 ("delta_light_count", C.c_uint32), ("delta_lights", C.POINTER(DeltaLightDesc)),
-                ("mesh_light_count", C.c_uint32), ("mesh_lights", C.POINTER(MeshLightDesc))]
+                ("mesh_light_count", C.c_uint32), ("mesh_lights", C.POINTER(MeshLightDesc)),
+                ("sphere_light_count", C.c_uint32), ("sphere_lights", C.POINTER(SphereLightDesc))]
 
 
 class HitSoa(C.Structure):

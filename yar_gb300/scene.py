@@ -26,6 +26,8 @@ DELTA_LIGHT_DTYPE = np.dtype([("type", "<u4"), ("position", "<f4", 3), ("directi
                               ("intensity", "<f4", 3), ("cone_angle", "<f4"), ("penumbra_angle", "<f4")])
 MESH_LIGHT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("emitted_radiance", "<f4", 3),
                              ("triangle_mesh_index", "<u4")])
+SPHERE_LIGHT_DTYPE = np.dtype([("position", "<f4", 3), ("emitted_radiance", "<f4", 3), ("radius", "<f4"),
+                               ("sample_count", "<i4")])
 CAMERA_DTYPE = np.dtype([("camera_to_world", "<f4", 12), ("image_extent", "<f4", 2), ("horz_half_dist", "<f4"),
                          ("vert_half_dist", "<f4"), ("z_is_up", "<i4")])
 CONFIG_DTYPE = np.dtype([("render_region", "<i4", 4), ("rendering_algorithm", "<i4"), ("max_light_bounces", "<i4"),
@@ -41,6 +43,7 @@ assert MATERIAL_DTYPE.itemsize == C.sizeof(native.MaterialDesc)
 assert LIGHT_DTYPE.itemsize == C.sizeof(native.RectLightDesc)
 assert DELTA_LIGHT_DTYPE.itemsize == C.sizeof(native.DeltaLightDesc)
 assert MESH_LIGHT_DTYPE.itemsize == C.sizeof(native.MeshLightDesc)
+assert SPHERE_LIGHT_DTYPE.itemsize == C.sizeof(native.SphereLightDesc)
 assert CAMERA_DTYPE.itemsize == C.sizeof(native.CameraDesc)
 assert CONFIG_DTYPE.itemsize == C.sizeof(native.RenderConfig)
 
@@ -94,6 +97,7 @@ class FlatScene:
         # point, spot and directional lights, in that order
         self.delta_lights = np.zeros(0, DELTA_LIGHT_DTYPE)
         self.mesh_lights = np.zeros(0, MESH_LIGHT_DTYPE)  # triangle-mesh lights
+        self.sphere_lights = np.zeros(0, SPHERE_LIGHT_DTYPE)
         self.other_light_count = 0
         self.camera = np.zeros((), CAMERA_DTYPE)
         self.config = default_config()
@@ -171,8 +175,9 @@ class FlatScene:
         lights = np.ascontiguousarray(self.rect_lights)
         dlights = np.ascontiguousarray(self.delta_lights)
         mlights = np.ascontiguousarray(self.mesh_lights)
+        slights = np.ascontiguousarray(self.sphere_lights)
         snodes = np.ascontiguousarray(self.scene_nodes, np.uint32)
-        keep += [objects, materials, lights, dlights, mlights, snodes, meshes]
+        keep += [objects, materials, lights, dlights, mlights, slights, snodes, meshes]
         s = native.FlatSceneDesc()
         s.mesh_count = len(self.meshes)
         s.meshes = meshes
@@ -191,6 +196,8 @@ class FlatScene:
         s.delta_lights = C.cast(dlights.ctypes.data, C.POINTER(native.DeltaLightDesc)) if dlights.size else None
         s.mesh_light_count = mlights.shape[0]
         s.mesh_lights = C.cast(mlights.ctypes.data, C.POINTER(native.MeshLightDesc)) if mlights.size else None
+        s.sphere_light_count = slights.shape[0]
+        s.sphere_lights = C.cast(slights.ctypes.data, C.POINTER(native.SphereLightDesc)) if slights.size else None
         C.memmove(C.byref(s.camera), np.ascontiguousarray(self.camera).ctypes.data, CAMERA_DTYPE.itemsize)
         C.memmove(C.byref(s.config), np.ascontiguousarray(self.config).ctypes.data, CONFIG_DTYPE.itemsize)
         return s, keep
@@ -224,6 +231,8 @@ class FlatScene:
             parts.append(chunk(b"DLIT", struct.pack("<I", self.delta_lights.shape[0]) + self.delta_lights.tobytes()))
         if self.mesh_lights.shape[0]:
             parts.append(chunk(b"MLIT", struct.pack("<I", self.mesh_lights.shape[0]) + self.mesh_lights.tobytes()))
+        if self.sphere_lights.shape[0]:
+            parts.append(chunk(b"SPHL", struct.pack("<I", self.sphere_lights.shape[0]) + self.sphere_lights.tobytes()))
         with open(path, "wb") as f:
             f.write(b"".join(parts))
 
@@ -283,6 +292,9 @@ class FlatScene:
             elif tag == b"MLIT":
                 n = struct.unpack_from("<I", p, 0)[0]
                 s.mesh_lights = np.frombuffer(p[4:4 + n * MESH_LIGHT_DTYPE.itemsize], MESH_LIGHT_DTYPE).copy()
+            elif tag == b"SPHL":
+                n = struct.unpack_from("<I", p, 0)[0]
+                s.sphere_lights = np.frombuffer(p[4:4 + n * SPHERE_LIGHT_DTYPE.itemsize], SPHERE_LIGHT_DTYPE).copy()
         return s
 
 

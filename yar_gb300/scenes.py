@@ -180,7 +180,7 @@ def _box(center, size, angle_deg):
 
 
 def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0, box_materials=None,
-                 upper_light=None, light_sources=(), mesh_lights=()):
+                 upper_light=None, light_sources=(), mesh_lights=(), sphere_lights=()):
     """pbrt-v3 text of the seeded Cornell box (34 triangles + a quad light).
 
     box_materials: None for matte boxes, or two pbrt material statements for
@@ -192,7 +192,9 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
     spot, distant).
     mesh_lights: (vertices, indices, normals or None, radiance) emitting
     triangle meshes that are not rectangles (the reference makes them
-    triangle-mesh lights)."""
+    triangle-mesh lights).
+    sphere_lights: (center, radius, radiance) emitting pbrt spheres (sphere
+    lights, shown by the reference's tessellated sphere)."""
     rng = np.random.default_rng(seed)
     k = int(math.ceil(math.sqrt(spp)))
     shapes = []
@@ -236,6 +238,12 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
             '  AreaLightSource "diffuse" "rgb L" [%s]' % fmt([light_radiance] * 3),
             '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(light[1]), fmt(light[0])),
             "AttributeEnd"]
+    for center, radius, radiance in sphere_lights:
+        out += ["AttributeBegin",
+                "  Translate %s" % fmt(center),
+                '  AreaLightSource "diffuse" "rgb L" [%s]' % fmt(radiance),
+                '  Shape "sphere" "float radius" [%s]' % fmt([radius]),
+                "AttributeEnd"]
     for v, i, n, radiance in mesh_lights:
         shape = '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(i), fmt(v))
         if n is not None:
@@ -290,6 +298,37 @@ def _mesh_lights():
     wall_v, wall_i = hexagon((-0.98, 1.2, -0.3), 0.15, 0, +1)
     wall_n = np.tile(np.array([[1.0, 0.0, 0.0]], np.float32), (wall_v.shape[0], 1))
     return ((ceiling_v, ceiling_i, None, (6.0, 5.5, 5.0)), (wall_v, wall_i, wall_n, (1.5, 2.0, 3.0)))
+
+
+# Two small emitting spheres: one in the open, one close to the tall box.
+SPHERE_LIGHTS = (((0.55, 1.35, 0.55), 0.08, (5.0, 4.5, 4.0)), ((-0.2, 0.5, 0.2), 0.05, (2.0, 3.0, 4.0)))
+
+def add_sphere_lights(flat, lights=SPHERE_LIGHTS, level=2, threads=0):
+    """Adds emitting spheres to a flat scene: per light an icosphere mesh of
+    the light's radius (the reference tessellates pbrt spheres the same way,
+    here at a lower level), an object translated to the center that carries
+    the sphere light, and the Diffuse_Sphere_Light record; the kd-trees are
+    rebuilt with the reference builder."""
+    from .scene import Mesh, SPHERE_LIGHT_DTYPE, make_object
+    records = np.zeros(len(lights), SPHERE_LIGHT_DTYPE)
+    objects = list(flat.objects)
+    first = flat.sphere_lights.shape[0]
+    for k, (center, radius, radiance) in enumerate(lights):
+        v, idx = icosphere(radius, level)
+        m = Mesh(v, idx)
+        m.bounds, m.nodes = native.build_mesh_kdtree(m.vertices, m.indices, threads)
+        flat.meshes.append(m)
+        xf = np.array([1, 0, 0, center[0], 0, 1, 0, center[1], 0, 0, 1, center[2]], np.float32)
+        objects.append(make_object(len(flat.meshes) - 1, xf, material_type=native.MATERIAL_NULL, material_index=-1,
+                                   light_type=native.LIGHT_SPHERE, light_index=first + k))
+        records[k]["position"] = center
+        records[k]["emitted_radiance"] = radiance
+        records[k]["radius"] = radius
+        records[k]["sample_count"] = 1
+    flat.objects = np.array(objects, flat.objects.dtype)
+    flat.sphere_lights = np.concatenate([flat.sphere_lights, records])
+    flat.build_scene_kdtree()
+    return flat
 
 
 # A hexagonal light on the ceiling (geometric normal) and one on the left wall
