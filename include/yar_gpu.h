@@ -69,6 +69,10 @@ extern "C" {
 #define YAR_MATERIAL_PLASTIC           5
 #define YAR_MATERIAL_COATED_DIFFUSE    6
 #define YAR_MATERIAL_GLASS             7
+#define YAR_MATERIAL_MIX               8
+#define YAR_MATERIAL_PBRT3_UBER        9
+#define YAR_MATERIAL_PBRT3_TRANSLUCENT 10
+#define YAR_MATERIAL_PBRT3_FOURIER     11
 #define YAR_MATERIAL_NULL              0xffffffffu
 
 /* Light_Type values (src/lib/light.h:7-17) */
@@ -144,9 +148,25 @@ typedef struct yar_material_desc {
     float eta_i;                /* metal: IOR of the adjacent dielectric */
     float u_roughness;          /* metal, coated diffuse: u roughness; glass, plastic: roughness */
     float v_roughness;          /* metal, coated diffuse (plastic: = u_roughness) */
-    float index_of_refraction;  /* glass, perfect refractor */
+    float index_of_refraction;  /* glass, perfect refractor, pbrt3 uber */
     int32_t roughness_is_alpha;
+    /* Fields of the layered and mixed materials (zero for the other kinds). */
+    float specular[3];          /* pbrt3 uber, pbrt3 translucent: Ks */
+    float diffuse[3];           /* pbrt3 translucent: Kd; diffuse transmission: scale */
+    float delta_reflectance[3]; /* pbrt3 uber: Kr */
+    float opacity[3];           /* pbrt3 uber */
+    uint32_t component_count;   /* pbrt3 uber: its layers (YAR_UBER_*) in the reference's order */
+    uint32_t components[5];
+    int32_t mix_materials[2];   /* mix: the two materials, indices into yar_flat_scene::materials */
+    float mix_amount[3];        /* mix */
 } yar_material_desc;
+
+/* Pbrt3_Uber_Material component kinds (src/lib/material_pbrt.h) */
+#define YAR_UBER_DIFFUSE            0
+#define YAR_UBER_SPECULAR           1
+#define YAR_UBER_DELTA_REFLECTION   2
+#define YAR_UBER_DELTA_TRANSMISSION 3
+#define YAR_UBER_OPACITY            4
 
 /* Diffuse_Rectangular_Light, src/lib/light.h:66-73 */
 typedef struct yar_rect_light_desc {

@@ -162,8 +162,8 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         memcpy(fm.nodes.data(), t.nodes.data(), t.nodes.size() * 8);
         out.meshes.push_back(std::move(fm));
     }
-    // materials: diffuse, metal, glass, plastic, coated diffuse, perfect reflector, perfect refractor
-    // flattened in that order
+    // materials: diffuse, metal, glass, plastic, coated diffuse, perfect reflector, perfect refractor,
+    // diffuse transmission, pbrt3 translucent, pbrt3 uber, mix flattened in that order
     std::vector<int> diffuse_index, metal_index, glass_index;
     for (const Diffuse_Material& m : ctx.materials.diffuse) {
         yar_material_desc d{};
@@ -237,21 +237,80 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         refractor_index.push_back((int)out.materials.size());
         out.materials.push_back(d);
     }
+    // diffuse transmission: reflectance, transmittance, diffuse = scale
+    std::vector<int> transmission_index, translucent_index, uber_index, mix_index;
+    for (const Diffuse_Transmission_Material& m : ctx.materials.diffuse_transmission) {
+        yar_material_desc d{};
+        d.type = YAR_MATERIAL_DIFFUSE_TRANSMISSION;
+        constant_rgb(m.reflectance, d.reflectance);
+        constant_rgb(m.transmittance, d.transmittance);
+        constant_rgb(m.scale, d.diffuse);
+        transmission_index.push_back((int)out.materials.size());
+        out.materials.push_back(d);
+    }
+    for (const Pbrt3_Translucent_Material& m : ctx.materials.pbrt3_translucent) {
+        yar_material_desc d{};
+        d.type = YAR_MATERIAL_PBRT3_TRANSLUCENT;
+        constant_rgb(m.reflectance, d.reflectance);
+        constant_rgb(m.transmittance, d.transmittance);
+        constant_rgb(m.diffuse, d.diffuse);
+        constant_rgb(m.specular, d.specular);
+        constant_float(m.roughness, &d.u_roughness);
+        d.v_roughness = d.u_roughness;
+        translucent_index.push_back((int)out.materials.size());
+        out.materials.push_back(d);
+    }
+    // pbrt3 uber: reflectance = Kd, transmittance = Kt
+    for (const Pbrt3_Uber_Material& m : ctx.materials.pbrt3_uber) {
+        yar_material_desc d{};
+        d.type = YAR_MATERIAL_PBRT3_UBER;
+        constant_rgb(m.diffuse_reflectance, d.reflectance);
+        constant_rgb(m.specular_reflectance, d.specular);
+        constant_rgb(m.delta_reflectance, d.delta_reflectance);
+        constant_rgb(m.delta_transmission, d.transmittance);
+        constant_rgb(m.opacity, d.opacity);
+        constant_float(m.u_roughness, &d.u_roughness);
+        constant_float(m.v_roughness, &d.v_roughness);
+        constant_float(m.index_of_refraction, &d.index_of_refraction);
+        d.component_count = m.component_count;
+        for (int k = 0; k < m.component_count; k++) d.components[k] = (uint32_t)m.components[k];
+        uber_index.push_back((int)out.materials.size());
+        out.materials.push_back(d);
+    }
+    for (size_t i = 0; i < ctx.materials.mix.size(); i++) {
+        mix_index.push_back((int)out.materials.size() + (int)i);
+    }
+    auto flat_index = [&](Material_Handle h) -> int {
+        switch (h.type) {
+        case Material_Type::diffuse: return diffuse_index[h.index];
+        case Material_Type::metal: return metal_index[h.index];
+        case Material_Type::glass: return glass_index[h.index];
+        case Material_Type::plastic: return plastic_index[h.index];
+        case Material_Type::coated_diffuse: return coated_index[h.index];
+        case Material_Type::perfect_reflector: return reflector_index[h.index];
+        case Material_Type::perfect_refractor: return refractor_index[h.index];
+        case Material_Type::diffuse_transmission: return transmission_index[h.index];
+        case Material_Type::pbrt3_translucent: return translucent_index[h.index];
+        case Material_Type::pbrt3_uber: return uber_index[h.index];
+        case Material_Type::mix: return mix_index[h.index];
+        default: return -1;
+        }
+    };
+    // mix: the two materials by flat index, mix_amount
+    for (const Mix_Material& m : ctx.materials.mix) {
+        yar_material_desc d{};
+        d.type = YAR_MATERIAL_MIX;
+        d.mix_materials[0] = flat_index(m.material1);
+        d.mix_materials[1] = flat_index(m.material2);
+        constant_rgb(m.mix_amount, d.mix_amount);
+        out.materials.push_back(d);
+    }
     for (const Scene_Object& o : scene.objects) {
         yar_object_desc d{};
         d.mesh_index = o.geometry.index;
         d.material_type = (uint32_t)o.material.type;
-        d.material_index = -1;
-        if (o.material.type == Material_Type::diffuse) d.material_index = diffuse_index[o.material.index];
-        else if (o.material.type == Material_Type::metal) d.material_index = metal_index[o.material.index];
-        else if (o.material.type == Material_Type::glass) d.material_index = glass_index[o.material.index];
-        else if (o.material.type == Material_Type::plastic) d.material_index = plastic_index[o.material.index];
-        else if (o.material.type == Material_Type::coated_diffuse) d.material_index = coated_index[o.material.index];
-        else if (o.material.type == Material_Type::perfect_reflector)
-            d.material_index = reflector_index[o.material.index];
-        else if (o.material.type == Material_Type::perfect_refractor)
-            d.material_index = refractor_index[o.material.index];
-        else if (o.material.type != Material_Type::null_material)
+        d.material_index = o.material.type == Material_Type::null_material ? -1 : flat_index(o.material);
+        if (o.material.type != Material_Type::null_material && d.material_index < 0)
             fprintf(stderr, "warning: material type %u not flattened\n", (unsigned)o.material.type);
         d.area_light_type = (uint32_t)o.area_light.type;
         d.area_light_index = o.area_light.index;
@@ -677,10 +736,58 @@ int cmd_render_yfs(const Args& a) {
             set_constant_parameter(m.index_of_refraction, d.index_of_refraction);
             scene.materials.perfect_refractor.push_back(m);
             handles.push_back({Material_Type::perfect_refractor, (int)scene.materials.perfect_refractor.size() - 1});
+        } else if (d.type == YAR_MATERIAL_DIFFUSE_TRANSMISSION) {
+            Diffuse_Transmission_Material m;
+            set_constant_parameter(m.reflectance, ColorRGB(d.reflectance));
+            set_constant_parameter(m.transmittance, ColorRGB(d.transmittance));
+            set_constant_parameter(m.scale, ColorRGB(d.diffuse));
+            scene.materials.diffuse_transmission.push_back(m);
+            handles.push_back({Material_Type::diffuse_transmission,
+                               (int)scene.materials.diffuse_transmission.size() - 1});
+        } else if (d.type == YAR_MATERIAL_PBRT3_TRANSLUCENT) {
+            Pbrt3_Translucent_Material m;
+            set_constant_parameter(m.reflectance, ColorRGB(d.reflectance));
+            set_constant_parameter(m.transmittance, ColorRGB(d.transmittance));
+            set_constant_parameter(m.diffuse, ColorRGB(d.diffuse));
+            set_constant_parameter(m.specular, ColorRGB(d.specular));
+            set_constant_parameter(m.roughness, d.u_roughness);
+            scene.materials.pbrt3_translucent.push_back(m);
+            handles.push_back({Material_Type::pbrt3_translucent, (int)scene.materials.pbrt3_translucent.size() - 1});
+        } else if (d.type == YAR_MATERIAL_PBRT3_UBER) {
+            Pbrt3_Uber_Material m;
+            set_constant_parameter(m.diffuse_reflectance, ColorRGB(d.reflectance));
+            set_constant_parameter(m.specular_reflectance, ColorRGB(d.specular));
+            set_constant_parameter(m.delta_reflectance, ColorRGB(d.delta_reflectance));
+            set_constant_parameter(m.delta_transmission, ColorRGB(d.transmittance));
+            set_constant_parameter(m.opacity, ColorRGB(d.opacity));
+            set_constant_parameter(m.u_roughness, d.u_roughness);
+            set_constant_parameter(m.v_roughness, d.v_roughness);
+            set_constant_parameter(m.index_of_refraction, d.index_of_refraction);
+            m.component_count = (uint8_t)d.component_count;
+            for (uint32_t k = 0; k < d.component_count && k < 5; k++)
+                m.components[k] = (Pbrt3_Uber_Material::Component_Type)d.components[k];
+            scene.materials.pbrt3_uber.push_back(m);
+            handles.push_back({Material_Type::pbrt3_uber, (int)scene.materials.pbrt3_uber.size() - 1});
+        } else if (d.type == YAR_MATERIAL_MIX) {
+            scene.materials.mix.push_back(Mix_Material{});  // sub-materials below, once every handle exists
+            handles.push_back({Material_Type::mix, (int)scene.materials.mix.size() - 1});
         } else {
             fprintf(stderr, "unsupported material type %u\n", d.type);
             return 1;
         }
+    }
+    for (size_t i = 0; i < fs_scene.materials.size(); i++) {
+        const yar_material_desc& d = fs_scene.materials[i];
+        if (d.type != YAR_MATERIAL_MIX) continue;
+        for (int k = 0; k < 2; k++)
+            if (d.mix_materials[k] < 0 || (size_t)d.mix_materials[k] >= handles.size()) {
+                fprintf(stderr, "mix material %zu: bad sub-material\n", i);
+                return 1;
+            }
+        Mix_Material& m = scene.materials.mix[handles[i].index];
+        m.material1 = handles[d.mix_materials[0]];
+        m.material2 = handles[d.mix_materials[1]];
+        set_constant_parameter(m.mix_amount, ColorRGB(d.mix_amount));
     }
     for (const yar_rect_light_desc& d : fs_scene.rect_lights) {
         Diffuse_Rectangular_Light l;

@@ -669,7 +669,15 @@ typedef struct bsdf_t {
     col eta_t, k_t;
     float eta_o, eta_i;             /* glass */
     int pbrt3_plastic, flipped;     /* plastic: Pbrt3_Plastic_BRDF, original shading normal flipped */
+    col diffuse_coeff, specular_coeff; /* pbrt3 translucent: Kd, Ks */
 } bsdf_t;
+
+static col clamp_unit(col c) { /* ColorRGB::clamp_to_unit_range, src/lib/color.h:83-88 */
+    c.r = c.r < 0.f ? 0.f : (1.f < c.r ? 1.f : c.r);
+    c.g = c.g < 0.f ? 0.f : (1.f < c.g ? 1.f : c.g);
+    c.b = c.b < 0.f ? 0.f : (1.f < c.b ? 1.f : c.b);
+    return c;
+}
 
 static float pbrt3_roughness_to_alpha(float roughness) {
     /* src/ref/scattering.cpp:240-251 */
@@ -726,6 +734,32 @@ static int make_bsdf(const yar_flat_scene* s, const shading_ctx* sc, bsdf_t* f) 
         f->alpha = f->alpha_x;
         f->pbrt3_plastic = f->type == YAR_MATERIAL_PLASTIC && s->config.pbrt3_scene;
         f->flipped = sc->flipped;
+    } else if (f->type == YAR_MATERIAL_PBRT3_UBER) {
+        /* Pbrt3_Uber_BRDF, src/ref/bsdf_pbrt.cpp:14-32: Kd, Ks, opacity; roughness always remapped */
+        f->reflection = 1;
+        f->reflectance = ldc(m->reflectance);
+        f->specular_coeff = ldc(m->specular);
+        f->diffuse_coeff = ldc(m->opacity);
+        f->alpha_x = roughness_to_alpha(s, m->u_roughness, 0);
+        f->alpha_y = roughness_to_alpha(s, m->v_roughness, 0);
+        f->eta_i = !sc->flipped ? m->index_of_refraction : 1.f / m->index_of_refraction;
+    } else if (f->type == YAR_MATERIAL_DIFFUSE_TRANSMISSION) {
+        /* Diffuse_Transmission_BSDF, src/ref/bsdf.cpp:89-103 */
+        f->reflection = f->transmission = 1;
+        f->reflectance = clamp_unit(mulc(ldc(m->diffuse), ldc(m->reflectance)));
+        f->transmittance = clamp_unit(mulc(ldc(m->diffuse), ldc(m->transmittance)));
+    } else if (f->type == YAR_MATERIAL_PBRT3_TRANSLUCENT) {
+        /* Pbrt3_Translucent_BSDF, src/ref/bsdf_pbrt.cpp:94-115 */
+        f->reflectance = ldc(m->reflectance);
+        f->transmittance = ldc(m->transmittance);
+        f->diffuse_coeff = ldc(m->diffuse);
+        f->specular_coeff = ldc(m->specular);
+        f->alpha = roughness_to_alpha(s, m->u_roughness, 0);
+        int enter = !sc->flipped;
+        f->eta_o = enter ? 1.f : 1.5f;
+        f->eta_i = enter ? 1.5f : 1.f;
+        f->reflection = !blackc(f->reflectance);
+        f->transmission = !blackc(f->transmittance);
     } else {
         return YAR_ERR_UNSUPPORTED;
     }
@@ -874,6 +908,49 @@ static float pow5(float v) { return (v * v) * (v * v) * v; }
 
 static col bsdf_evaluate(const bsdf_t* f, v3 wo, v3 wi) {
     if (f->type == YAR_MATERIAL_DIFFUSE) return mulcs(f->reflectance, PI_INV_F);
+    if (f->type == YAR_MATERIAL_PBRT3_UBER) { /* src/ref/bsdf_pbrt.cpp:34-52; diffuse_coeff holds the opacity */
+        col diffuse = mulc(mulcs(f->reflectance, PI_INV_F), f->diffuse_coeff);
+        v3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
+        v3 wh_l = norm3(add3(wo_l, wi_l));
+        float F = dielectric_fresnel(dot3(wi_l, wh_l), f->eta_i);
+        float G = ggx_G_aniso(wi_l, wo_l, f->alpha_x, f->alpha_y);
+        float D = ggx_D_aniso(wh_l, f->alpha_x, f->alpha_y);
+        float mf = (F * G * D) / (4.f * wo_l.z * wi_l.z);
+        return addc(diffuse, mulcs(mulc(f->specular_coeff, f->diffuse_coeff), mf));
+    }
+    if (f->type == YAR_MATERIAL_DIFFUSE_TRANSMISSION) { /* src/ref/bsdf.cpp:105-112 */
+        int same = dot3(wo, f->n) * dot3(wi, f->n) > 0.f;
+        return mulcs(same ? f->reflectance : f->transmittance, PI_INV_F);
+    }
+    if (f->type == YAR_MATERIAL_PBRT3_TRANSLUCENT) { /* src/ref/bsdf_pbrt.cpp:117-158 */
+        int same = dot3(wo, f->n) * dot3(wi, f->n) > 0.f;
+        if (same) {
+            col diffuse = mulc(mulcs(f->diffuse_coeff, PI_INV_F), f->reflectance);
+            v3 wh = norm3(add3(wo, wi));
+            float F = dielectric_fresnel(dot3(wi, wh), f->eta_i / f->eta_o);
+            float G = ggx_G(wi, wo, f->n, f->alpha);
+            float D = ggx_D(wh, f->n, f->alpha);
+            float base = (F * G * D) / (4.f * dot3(wo, f->n) * dot3(wi, f->n));
+            return addc(diffuse, mulcs(mulc(f->specular_coeff, f->reflectance), base));
+        }
+        col diffuse = mulc(mulcs(f->diffuse_coeff, PI_INV_F), f->transmittance);
+        col specular = mkc(0, 0, 0);
+        v3 wh = refraction_half(f->eta_o, wo, f->eta_i, wi, f->n);
+        float wo_wh = dot3(wo, wh), wi_wh = dot3(wi, wh);
+        if (wo_wh * wi_wh <= 0.f) {
+            float F = dielectric_fresnel(wi_wh, f->eta_o / f->eta_i);
+            if (F < 1.f) {
+                float G = ggx_G(wi, wo, f->n, f->alpha);
+                float D = ggx_D(wh, f->n, f->alpha);
+                float wo_n = dot3(wo, f->n), wi_n = dot3(wi, f->n);
+                float k = fabsf((wo_wh * wi_wh) / (wo_n * wi_n));
+                float k2 = f->eta_o * wo_wh + f->eta_i * wi_wh;
+                float base = (f->eta_o * f->eta_o * k * G * D * (1.f - F)) / (k2 * k2);
+                specular = mulcs(mulc(f->specular_coeff, f->transmittance), base);
+            }
+        }
+        return addc(diffuse, specular);
+    }
     if (f->type == YAR_MATERIAL_PLASTIC) {
         /* Plastic_BRDF::evaluate, src/ref/bsdf.cpp:215-234; Pbrt3_Plastic_BRDF::evaluate,
          * src/ref/bsdf_pbrt.cpp:264-290 (pbrt3's swapped 1.0/1.5 IOR pair) */
@@ -953,6 +1030,33 @@ static float glass_reflection_probability(const bsdf_t* f, float fresnel) {
 
 static float bsdf_pdf(const bsdf_t* f, v3 wo, v3 wi) {
     if (f->type == YAR_MATERIAL_DIFFUSE) return dot3(f->n, wi) / PI_F;
+    if (f->type == YAR_MATERIAL_PBRT3_UBER) { /* src/ref/bsdf_pbrt.cpp:74-87 */
+        float diffuse_pdf = dot3(f->n, wi) / PI_F;
+        v3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
+        float spec_pdf = refl_pdf_aniso(wo_l, norm3(add3(wo_l, wi_l)), f->alpha_x, f->alpha_y);
+        return 0.5f * (diffuse_pdf + spec_pdf);
+    }
+    if (f->type == YAR_MATERIAL_DIFFUSE_TRANSMISSION) { /* src/ref/bsdf.cpp:128-141 */
+        float max_r = maxcomp(f->reflectance), max_t = maxcomp(f->transmittance);
+        float pdf = fabsf(dot3(f->n, wi)) * PI_INV_F;
+        int same = dot3(wo, f->n) * dot3(wi, f->n) > 0.f;
+        return same ? (max_r / (max_r + max_t)) * pdf : (max_t / (max_r + max_t)) * pdf;
+    }
+    if (f->type == YAR_MATERIAL_PBRT3_TRANSLUCENT) { /* src/ref/bsdf_pbrt.cpp:211-250 */
+        float max_r = maxcomp(f->reflectance), max_t = maxcomp(f->transmittance);
+        float rp = max_r / (max_r + max_t);
+        int same = dot3(wo, f->n) * dot3(wi, f->n) > 0.f;
+        if (same) {
+            float diffuse_pdf = dot3(wi, f->n) * PI_INV_F;
+            float spec_pdf = refl_pdf(wo, norm3(add3(wo, wi)), f->n, f->alpha);
+            return rp * 0.5f * (diffuse_pdf + spec_pdf);
+        }
+        float diffuse_pdf = -dot3(wi, f->n) * PI_INV_F;
+        float spec_pdf = 0.f;
+        v3 wh = refraction_half(f->eta_o, wo, f->eta_i, wi, f->n);
+        if (dot3(wo, wh) * dot3(wi, wh) <= 0.f) spec_pdf = trans_pdf(wo, wi, wh, f->n, f->alpha, f->eta_o, f->eta_i);
+        return (1.f - rp) * 0.5f * (diffuse_pdf + spec_pdf);
+    }
     if (f->type == YAR_MATERIAL_PLASTIC) {
         /* Plastic_BRDF::pdf, src/ref/bsdf.cpp:253-263 */
         float diffuse_pdf = dot3(f->n, wi) / PI_F;
@@ -990,14 +1094,55 @@ static float bsdf_pdf(const bsdf_t* f, v3 wo, v3 wi) {
 
 /* BSDF::sample; returns black when no direction is produced. */
 static col bsdf_sample(const bsdf_t* f, float u0, float u1, float u_scatter, v3 wo, v3* wi, float* pdf) {
+    if (f->type == YAR_MATERIAL_DIFFUSE_TRANSMISSION) { /* src/ref/bsdf.cpp:114-126 */
+        float max_r = maxcomp(f->reflectance), max_t = maxcomp(f->transmittance);
+        float sign = u_scatter < max_r / (max_r + max_t) ? 1.f : -1.f;
+        *wi = local_to_world(f, mul3s(sample_hemisphere_cosine(u0, u1), sign));
+        *pdf = bsdf_pdf(f, wo, *wi);
+        return bsdf_evaluate(f, wo, *wi);
+    }
+    if (f->type == YAR_MATERIAL_PBRT3_TRANSLUCENT) { /* src/ref/bsdf_pbrt.cpp:160-209 */
+        float max_r = maxcomp(f->reflectance), max_t = maxcomp(f->transmittance);
+        float rp = max_r / (max_r + max_t);
+        if (u_scatter < rp) {
+            float u = u_scatter / rp;
+            u = u < ONE_MINUS_EPSILON ? u : ONE_MINUS_EPSILON;
+            if (u < 0.5f) {
+                *wi = local_to_world(f, sample_hemisphere_cosine(u0, u1));
+            } else {
+                v3 wh = local_to_world(f, ggx_sample_vndf(u0, u1, world_to_local(f, wo), f->alpha, f->alpha));
+                v3 c = reflect3(wo, wh);
+                if (dot3(c, f->n) <= 0.f) return mkc(0, 0, 0);
+                *wi = c;
+            }
+        } else {
+            float u = (u_scatter - rp) / (1.f - rp);
+            u = u < ONE_MINUS_EPSILON ? u : ONE_MINUS_EPSILON;
+            if (u < 0.5f) {
+                *wi = local_to_world(f, neg3(sample_hemisphere_cosine(u0, u1)));
+            } else {
+                v3 wh = local_to_world(f, ggx_sample_vndf(u0, u1, world_to_local(f, wo), f->alpha, f->alpha));
+                if (dot3(wh, wo) < 0.f) return mkc(0, 0, 0);
+                v3 c;
+                if (!refract3(wo, wh, f->eta_o / f->eta_i, &c)) return mkc(0, 0, 0);
+                if (dot3(c, f->n) >= 0.f) return mkc(0, 0, 0);
+                *wi = c;
+            }
+        }
+        *pdf = bsdf_pdf(f, wo, *wi);
+        if (*pdf == 0.f) return mkc(0, 0, 0);
+        return bsdf_evaluate(f, wo, *wi);
+    }
     if (f->type == YAR_MATERIAL_DIFFUSE) {
         v3 l = sample_hemisphere_cosine(u0, u1);
         *wi = local_to_world(f, l);
         *pdf = bsdf_pdf(f, wo, *wi);
         return bsdf_evaluate(f, wo, *wi);
     }
-    if (f->type == YAR_MATERIAL_PLASTIC || f->type == YAR_MATERIAL_COATED_DIFFUSE) {
-        /* Plastic_BRDF::sample, src/ref/bsdf.cpp:236-251; Ashikhmin_Shirley_Phong_BRDF::sample,
+    if (f->type == YAR_MATERIAL_PLASTIC || f->type == YAR_MATERIAL_COATED_DIFFUSE ||
+        f->type == YAR_MATERIAL_PBRT3_UBER) {
+        /* Pbrt3_Uber_BRDF::sample (src/ref/bsdf_pbrt.cpp:54-72) has the same shape.
+         * Plastic_BRDF::sample, src/ref/bsdf.cpp:236-251; Ashikhmin_Shirley_Phong_BRDF::sample,
          * :462-478: the first 1D sample picks the diffuse or the specular lobe */
         if (u_scatter < 0.5f) {
             *wi = local_to_world(f, sample_hemisphere_cosine(u0, u1));
@@ -1448,13 +1593,42 @@ static void camera_ray(const yar_camera_desc* c, float fx, float fy, v3* o, v3* 
  * (perfect reflector, perfect refractor, smooth glass; no nested dielectrics,
  * no bump maps).  Returns 1 and the delta direction and attenuation for a delta
  * material, 2 for a delta material without a direction, 0 otherwise. */
-static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, float u, v3* dir, col* atten) {
+static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, float* u_ptr, v3* dir, col* atten,
+                            float* bsdf_prob) {
+    const yar_material_desc* m = &s->materials[sc->material_index];
+    *atten = mkc(1, 1, 1);
+    if (sc->material_type == YAR_MATERIAL_PBRT3_UBER) {
+        /* get_pbrt_uber_info, src/ref/delta_scattering.cpp:102-150 */
+        const float fp = *u_ptr * (float)m->component_count;
+        const int k = (int)fp;
+        const uint32_t kind = m->components[k];
+        const float r = fp - (float)k;
+        *u_ptr = r < 0.f ? 0.f : (ONE_MINUS_EPSILON < r ? ONE_MINUS_EPSILON : r);
+        float delta_terms = 0.f;
+        for (uint32_t c = 0; c < m->component_count; c++)
+            if (m->components[c] >= YAR_UBER_DELTA_REFLECTION) delta_terms += 1.f;
+        *bsdf_prob = 1.f - delta_terms / (float)m->component_count;
+        if (kind == YAR_UBER_DELTA_REFLECTION) {
+            const int enter = !sc->flipped;
+            float fresnel = dielectric_fresnel(dot3(sc->normal, sc->wo),
+                                               enter ? m->index_of_refraction : 1.f / m->index_of_refraction);
+            *atten = mulcs(ldc(m->delta_reflectance), (float)m->component_count * fresnel);
+            *dir = reflect3(sc->wo, sc->normal);
+            return 1;
+        }
+        if (kind == YAR_UBER_OPACITY) {
+            *atten = mulcs(subc(mkc(1, 1, 1), ldc(m->opacity)), (float)m->component_count);
+            *dir = neg3(sc->wo);
+            return 1;
+        }
+        return 0;
+    }
+    const float u = *u_ptr;
     if (sc->material_type != YAR_MATERIAL_PERFECT_REFLECTOR && sc->material_type != YAR_MATERIAL_PERFECT_REFRACTOR &&
         sc->material_type != YAR_MATERIAL_GLASS)
         return 0;
-    const yar_material_desc* m = &s->materials[sc->material_index];
     if (sc->material_type == YAR_MATERIAL_GLASS && m->u_roughness > 0.f) return 0;
-    *atten = mkc(1, 1, 1);
+    *bsdf_prob = 0.f;
     if (sc->material_type == YAR_MATERIAL_PERFECT_REFLECTOR) {
         *dir = reflect3(sc->wo, sc->normal);
         *atten = ldc(m->reflectance);
@@ -1539,12 +1713,14 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
         next2d(sv, &un0, &un1);
 
         if (sc.material_type == YAR_MATERIAL_NULL) return YAR_ERR_UNSUPPORTED;
+        /* Shading_Context::initialize_scattering (src/ref/shading_context.cpp:174-186) */
         v3 ddir;
         col datten;
-        const int delta = delta_scattering(s, &sc, u_scatter, &ddir, &datten);
+        float bsdf_prob = 1.f; /* 1 - delta_layer_selection_probability */
+        const int delta = delta_scattering(s, &sc, &u_scatter, &ddir, &datten, &bsdf_prob);
         if (delta == 2) break; /* perfect refractor at total internal reflection */
-        if (!delta) {
-            bsdf_t f;
+        bsdf_t f;
+        if (!delta || bsdf_prob != 0.f) {
             int rc = make_bsdf(s, &sc, &f);
             if (rc != YAR_OK) return rc;
             /* estimate_direct_lighting_from_single_sample, src/ref/direct_lighting.cpp:522-578 */
@@ -1561,14 +1737,15 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
                                         ul0, ul1, ub0, ub1, u_scatter);
             col direct = mulcs(one, (float)total_lights);
             L = addc(L, mulc(coeff, direct));
-
+        }
+        if (!delta) {
             bounce++;
             if (bounce == cfg->max_light_bounces) break;
             v3 wi;
             float pdf;
             col fv = bsdf_sample(&f, un0, un1, u_scatter_next, sc.wo, &wi, &pdf);
             if (blackc(fv)) break;
-            coeff = mulc(coeff, mulcs(fv, fabsf(dot3(sc.normal, wi)) / (pdf * 1.f)));
+            coeff = mulc(coeff, mulcs(fv, fabsf(dot3(sc.normal, wi)) / (pdf * bsdf_prob)));
             ro = origin_for_direction(&sc, wi);
             rd = wi;
         } else {
@@ -1764,10 +1941,19 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
         uint32_t t = s->materials[i].type;
         if (t != YAR_MATERIAL_DIFFUSE && t != YAR_MATERIAL_METAL && t != YAR_MATERIAL_GLASS &&
             t != YAR_MATERIAL_PLASTIC && t != YAR_MATERIAL_COATED_DIFFUSE && t != YAR_MATERIAL_PERFECT_REFLECTOR &&
-            t != YAR_MATERIAL_PERFECT_REFRACTOR)
+            t != YAR_MATERIAL_PERFECT_REFRACTOR && t != YAR_MATERIAL_DIFFUSE_TRANSMISSION &&
+            t != YAR_MATERIAL_PBRT3_TRANSLUCENT && t != YAR_MATERIAL_PBRT3_UBER)
             return YAR_ERR_UNSUPPORTED;
     }
     if (s->other_light_count) return YAR_ERR_UNSUPPORTED;
+    for (uint32_t i = 0; i < s->material_count; i++) {
+        const yar_material_desc* m = &s->materials[i];
+        if (m->type != YAR_MATERIAL_PBRT3_UBER) continue;
+        if (m->component_count < 1 || m->component_count > 5) return YAR_ERR_UNSUPPORTED;
+        for (uint32_t k = 0; k < m->component_count; k++)
+            if (m->components[k] > YAR_UBER_OPACITY || m->components[k] == YAR_UBER_DELTA_TRANSMISSION)
+                return YAR_ERR_UNSUPPORTED;
+    }
     for (uint32_t i = 0; i < s->delta_light_count; i++) {
         uint32_t t = s->delta_lights[i].type;
         if (t > YAR_LIGHT_DIRECTIONAL || (i > 0 && t < s->delta_lights[i - 1].type)) return YAR_ERR_INVALID;

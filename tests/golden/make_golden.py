@@ -46,6 +46,12 @@ Fixtures
                              (sphere lights shown by level-2 icospheres, added
                              on the flat scene), rendered by the reference from
                              the flat scene.
+  cornell_translucent_64.yfs / .npz  a pbrt "translucent" tall box, seed 9.
+  cornell_transmission_64.yfs / .npz  cornell_translucent_64 with the short box
+                             turned into YAR's diffuse-transmission material,
+                             rendered by the reference from the flat scene.
+  cornell_uber_64.yfs / .npz  pbrt "uber" boxes: one with a delta-reflection
+                             layer, one with opacity (passthrough), seed 10.
 """
 import os
 import re
@@ -249,6 +255,31 @@ def cornell_spherelight_64():
                         variance=np.float64(info["variance"]))
 
 
+def _pbrt_golden(name, seed, **kw):
+    with tempfile.TemporaryDirectory() as d:
+        pbrt = os.path.join(d, name + ".pbrt")
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=seed, width=64, height=64, spp=16, maxdepth=8, **kw))
+        oracle.ref_flatten(pbrt, os.path.join(HERE, name + ".yfs"), seed_offset=1)
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), image=img, variance=np.float64(info["variance"]))
+
+
+def cornell_translucent_64():
+    _pbrt_golden("cornell_translucent_64", 9, box_materials=scenes.TRANSLUCENT_BOXES)
+
+
+def cornell_transmission_64():
+    s = scenes.make_diffuse_transmission(FlatScene.read(os.path.join(HERE, "cornell_translucent_64.yfs")))
+    s.write(os.path.join(HERE, "cornell_transmission_64.yfs"))
+    img, info = oracle.ref_render_flat(s, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_transmission_64.npz"), image=img,
+                        variance=np.float64(info["variance"]))
+
+
+def cornell_uber_64():
+    _pbrt_golden("cornell_uber_64", 10, box_materials=scenes.UBER_BOXES)
+
+
 def kdtree_cache_files():
     """The reference's kd-tree cache files (KdTree::save) of the raycast_small
     scene's first two meshes and of its scene tree."""
@@ -293,7 +324,8 @@ if __name__ == "__main__":
     which = sys.argv[1:] or ["raycast_small", "transform_small", "kdtree_regression", "cornell_c1_64",
                              "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "cornell_layered_64",
                              "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64",
-                             "cornell_spherelight_64",
+                             "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64",
+                             "cornell_uber_64",
                              "exr_files",
                              "kdtree_cache_files"]
     for name in which:

@@ -4,6 +4,8 @@ import ctypes
 import os
 import re
 
+import pytest
+
 from conftest import ROOT
 
 
@@ -44,5 +46,36 @@ def test_struct_sizes_match_the_header():
     from yar_gb300 import native
     assert ctypes.sizeof(native.KdNode) == 8
     assert ctypes.sizeof(native.ObjectDesc) == 164
-    assert ctypes.sizeof(native.MaterialDesc) == 72
+    assert ctypes.sizeof(native.MaterialDesc) == 164
     assert ctypes.sizeof(native.RectLightDesc) == 72
+
+
+def test_struct_layouts_match_the_c_compiler(tmp_path):
+    """Every ctypes mirror has the size and field offsets the C compiler gives
+    the header's structs."""
+    import shutil
+    import subprocess
+    from yar_gb300 import native
+    if shutil.which("gcc") is None:
+        pytest.skip("no C compiler")
+    mirrors = {"yar_material_desc": native.MaterialDesc, "yar_object_desc": native.ObjectDesc,
+               "yar_rect_light_desc": native.RectLightDesc, "yar_delta_light_desc": native.DeltaLightDesc,
+               "yar_mesh_light_desc": native.MeshLightDesc, "yar_sphere_light_desc": native.SphereLightDesc,
+               "yar_camera_desc": native.CameraDesc, "yar_render_config": native.RenderConfig,
+               "yar_flat_scene": native.FlatSceneDesc}
+    lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "yar_gpu.h"', "int main(void) {"]
+    for name, cls in mirrors.items():
+        lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (name, name))
+        for field, _ in cls._fields_:
+            lines.append('  printf("%s.%s %%zu\\n", offsetof(%s, %s));' % (name, field, name, field))
+    lines.append("  return 0;\n}")
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I" + os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    out = dict(l.rsplit(" ", 1) for l in subprocess.run([str(exe)], capture_output=True, text=True,
+                                                        check=True).stdout.split("\n") if l)
+    for name, cls in mirrors.items():
+        assert int(out[name]) == ctypes.sizeof(cls), name
+        for field, _ in cls._fields_:
+            assert int(out[name + "." + field]) == getattr(cls, field).offset, (name, field)

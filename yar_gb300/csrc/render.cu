@@ -70,6 +70,30 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
                   : m.type == YAR_MATERIAL_PERFECT_REFRACTOR ? kDeltaRefractor
                   : m.type == YAR_MATERIAL_GLASS && !(m.u_roughness > 0.f) ? kDeltaGlass
                                                                             : kDeltaNone;
+        auto rgb = [](const float* v) { return Col{v[0], v[1], v[2]}; };
+        auto clamp_unit = [](Col c) {  // ColorRGB::clamp_to_unit_range
+            auto c1 = [](float v) { return v < 0.f ? 0.f : (1.f < v ? 1.f : v); };
+            return Col{c1(c.r), c1(c.g), c1(c.b)};
+        };
+        if (m.type == YAR_MATERIAL_DIFFUSE_TRANSMISSION) {  // Diffuse_Transmission_BSDF (bsdf.cpp:89-103)
+            d.reflectance = clamp_unit(Col{m.diffuse[0] * m.reflectance[0], m.diffuse[1] * m.reflectance[1],
+                                           m.diffuse[2] * m.reflectance[2]});
+            d.transmittance = clamp_unit(Col{m.diffuse[0] * m.transmittance[0], m.diffuse[1] * m.transmittance[1],
+                                             m.diffuse[2] * m.transmittance[2]});
+        } else if (m.type == YAR_MATERIAL_PBRT3_TRANSLUCENT) {  // roughness always remapped
+            d.extra = rgb(m.diffuse);
+            d.specular = rgb(m.specular);
+            d.alpha = roughness_to_alpha(scene->config, m.u_roughness, 0);
+        } else if (m.type == YAR_MATERIAL_PBRT3_UBER) {  // roughness always remapped
+            d.specular = rgb(m.specular);
+            d.extra = rgb(m.opacity);
+            d.delta_reflectance = rgb(m.delta_reflectance);
+            d.alpha_x = roughness_to_alpha(scene->config, m.u_roughness, 0);
+            d.alpha_y = roughness_to_alpha(scene->config, m.v_roughness, 0);
+            d.uber_components = std::min<uint32_t>(m.component_count, 5) << 24;
+            for (uint32_t k = 0; k < m.component_count && k < 5; k++) d.uber_components |= (m.components[k] & 7u) << (3 * k);
+            d.delta = kDeltaUber;  // every sample picks a layer
+        }
     }
     std::vector<Rect_Light_Dev> lights(std::max<uint32_t>(1, scene->rect_light_count));
     for (uint32_t i = 0; i < scene->rect_light_count; i++) {

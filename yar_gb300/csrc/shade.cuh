@@ -138,15 +138,18 @@ enum : uint32_t {
     kPerfectRefractor = 1,
     kDiffuse = 2,
     kMetal = 4,
+    kDiffuseTransmission = 3,
     kPlastic = 5,
     kCoatedDiffuse = 6,
     kGlass = 7,
+    kUber = 9,
+    kTranslucent = 10,
     kPbrt3Plastic = 0x105
 };
 
 // How a material scatters without a BSDF: not at all (kDeltaNone), as a
 // mirror, a perfect refractor, or smooth glass (glass of roughness 0).
-enum : uint32_t { kDeltaNone = 0, kDeltaReflector = 1, kDeltaRefractor = 2, kDeltaGlass = 3 };
+enum : uint32_t { kDeltaNone = 0, kDeltaReflector = 1, kDeltaRefractor = 2, kDeltaGlass = 3, kDeltaUber = 4 };
 
 // Material constants as the BSDF constructors evaluate them (src/ref/bsdf.cpp:60-66,
 // :146-158, :205-213, :268-294, :427-438); alpha values are computed on the host
@@ -159,7 +162,10 @@ struct Material_Dev {
     Col eta_t, k_t;
     float eta_i_metal, ior;
     uint32_t delta;  // kDelta*
-    float pad;
+    uint32_t uber_components;  // pbrt3 uber: component kinds, 3 bits each, count in bits 24..27
+    Col specular;     // pbrt3 uber, pbrt3 translucent: Ks
+    Col extra;        // pbrt3 uber: opacity; pbrt3 translucent: Kd
+    Col delta_reflectance;  // pbrt3 uber: Kr
 };
 
 struct Bsdf {
@@ -168,6 +174,7 @@ struct Bsdf {
     bool reflection, transmission;
     bool flipped;  // the shading normal was flipped towards wo (Pbrt3_Plastic_BRDF's IOR choice)
     Col reflectance, transmittance, eta_t, k_t;
+    Col specular, extra;  // pbrt3 uber: Ks, opacity; pbrt3 translucent: Ks, Kd
     float alpha_x, alpha_y, alpha, eta_i_metal, eta_o, eta_i;
 };
 
@@ -182,9 +189,12 @@ __device__ __forceinline__ void make_bsdf(const Shading& sc, const Material_Dev&
     f.n = sc.n;
     f.bt = normalized(cross(sc.n, sc.dpdu_shading));
     f.t = cross(f.bt, sc.n);
-    f.reflection = true;
-    f.transmission = m.type == kGlass;
+    f.reflection = m.type != kTranslucent || !black(m.reflectance);
+    f.transmission = m.type == kGlass || m.type == kDiffuseTransmission ||
+                     (m.type == kTranslucent && !black(m.transmittance));
     f.flipped = sc.flipped;
+    f.specular = m.specular;
+    f.extra = m.extra;
     f.reflectance = m.reflectance;
     f.transmittance = m.transmittance;
     f.eta_t = m.eta_t;
@@ -196,6 +206,12 @@ __device__ __forceinline__ void make_bsdf(const Shading& sc, const Material_Dev&
     const bool enter = !sc.flipped;
     f.eta_o = enter ? 1.f : m.ior;
     f.eta_i = enter ? m.ior : 1.f;
+    if (m.type == kTranslucent) {  // Pbrt3_Translucent_BSDF: the fixed 1.0 / 1.5 pair
+        f.eta_o = enter ? 1.f : 1.5f;
+        f.eta_i = enter ? 1.5f : 1.f;
+    } else if (m.type == kUber) {  // Pbrt3_Uber_BRDF's relative IOR (bsdf_pbrt.cpp:14-32)
+        f.eta_i = enter ? m.ior : 1.f / m.ior;
+    }
 }
 
 __device__ __forceinline__ V3 sample_hemisphere_cosine(float u0, float u1) {
@@ -218,28 +234,63 @@ __device__ __forceinline__ float dielectric_fresnel(float cos_i, float eta) {
 
 // check_for_delta_scattering_event with get_perfect_reflector_info,
 // get_perfect_refractor_info and get_glass_info (src/ref/delta_scattering.cpp:27-97,
-// :252-324), constant parameters, no bump map, no nested dielectrics.  Returns
-// false for a perfect refractor at total internal reflection: the reference
-// has no direction there (an assertion), and the path ends.
-__device__ __forceinline__ bool delta_scattering(const Shading& sc, const Material_Dev& m, float u, V3& dir, Col& atten) {
+// :252-324) and get_pbrt_uber_info (:102-150), constant parameters, no bump
+// map, no nested dielectrics.  Returns 0 (no delta event), 1 (dir and atten
+// set) or 2: a perfect refractor at total internal reflection, where the
+// reference has no direction (an assertion) and the path ends.  bsdf_prob is
+// 1 - the delta layers' selection probability.
+__device__ __forceinline__ int delta_scattering(const Shading& sc, const Material_Dev& m, float& u, V3& dir,
+                                                Col& atten, float& bsdf_prob) {
     atten = col(1.f, 1.f, 1.f);
+    const bool enter = !sc.flipped;
+    if (m.delta == kDeltaUber) {
+        // get_pbrt_uber_info (delta_scattering.cpp:102-150): u picks a layer and is
+        // re-normalised for the BSDF; delta reflection and opacity are delta events
+        const uint32_t count = (m.uber_components >> 24) & 0xfu;
+        const float fp = u * (float)count;
+        const int k = (int)fp;
+        const uint32_t kind = (m.uber_components >> (3 * k)) & 7u;
+        const float r = fp - (float)k;
+        u = r < 0.f ? 0.f : (__uint_as_float(0x3f7fffffu) < r ? __uint_as_float(0x3f7fffffu) : r);
+        float delta_terms = 0.f;
+        for (uint32_t c = 0; c < count; c++)
+            if (((m.uber_components >> (3 * c)) & 7u) >= YAR_UBER_DELTA_REFLECTION) delta_terms += 1.f;
+        bsdf_prob = 1.f - delta_terms / (float)count;
+        if (kind == YAR_UBER_DELTA_REFLECTION) {
+            const float fresnel = dielectric_fresnel(dot(sc.n, sc.wo), enter ? m.ior : 1.f / m.ior);
+            atten = mul(m.delta_reflectance, (float)count * fresnel);
+            dir = reflect(sc.wo, sc.n);
+            return 1;
+        }
+        if (kind == YAR_UBER_OPACITY) {
+            atten = mul(col(1.f, 1.f, 1.f) - m.extra, (float)count);
+            dir = -sc.wo;
+            return 1;
+        }
+        return 0;
+    }
+    bsdf_prob = 0.f;
     if (m.delta == kDeltaReflector) {
         dir = reflect(sc.wo, sc.n);
         atten = m.reflectance;
-        return true;
+        return 1;
     }
-    const bool enter = !sc.flipped;
-    if (m.delta == kDeltaRefractor) return refract(sc.wo, sc.n, enter ? 1.f / m.ior : m.ior, dir);
+    if (m.delta == kDeltaRefractor) return refract(sc.wo, sc.n, enter ? 1.f / m.ior : m.ior, dir) ? 1 : 2;
     const float eta_t_over_i = enter ? m.ior : 1.f / m.ior;
     const float fresnel = dielectric_fresnel(dot(sc.n, sc.wo), eta_t_over_i);
     if (u < fresnel) {
         dir = reflect(sc.wo, sc.n);
         atten = m.reflectance;
-        return true;
+        return 1;
     }
     const float eta = 1.f / eta_t_over_i;
     atten = mul(m.transmittance, eta * eta);
-    return refract(sc.wo, sc.n, eta, dir);
+    return refract(sc.wo, sc.n, eta, dir) ? 1 : 2;
+}
+
+__device__ __forceinline__ float one_minus_eps_min_s(float v) {  // std::min(v, One_Minus_Epsilon)
+    const float ome = __uint_as_float(0x3f7fffffu);
+    return v < ome ? v : ome;
 }
 
 // schlick_fresnel (src/ref/scattering.cpp:10-15)
@@ -379,6 +430,48 @@ __device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
         const Col base = mul(F, (G * D) / (4.f * dot(wo, f.n) * dot(wi, f.n)));
         return mul(f.reflectance, 1.f / kPi) + mul(base, f.transmittance.r);
     }
+    if (FULL && f.type == kDiffuseTransmission) {  // Diffuse_Transmission_BSDF::evaluate (bsdf.cpp:105-112)
+        const bool same = dot(wo, f.n) * dot(wi, f.n) > 0.f;
+        return mul(same ? f.reflectance : f.transmittance, 1.f / kPi);
+    }
+    if (FULL && f.type == kUber) {  // Pbrt3_Uber_BRDF::evaluate (bsdf_pbrt.cpp:34-52)
+        const Col diffuse = mul(f.reflectance, 1.f / kPi) * f.extra;
+        const V3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
+        const V3 wh_l = normalized(wo_l + wi_l);
+        const float F = dielectric_fresnel(dot(wi_l, wh_l), f.eta_i);
+        const float G = ggx_G_aniso(wi_l, wo_l, f.alpha_x, f.alpha_y);
+        const float D = ggx_D_aniso(wh_l, f.alpha_x, f.alpha_y);
+        const float m = (F * G * D) / (4.f * wo_l.z * wi_l.z);
+        return diffuse + mul(f.specular * f.extra, m);
+    }
+    if (FULL && f.type == kTranslucent) {  // Pbrt3_Translucent_BSDF::evaluate (bsdf_pbrt.cpp:117-158)
+        if (dot(wo, f.n) * dot(wi, f.n) > 0.f) {
+            const Col diffuse = mul(f.extra, 1.f / kPi) * f.reflectance;
+            const V3 wh = normalized(wo + wi);
+            const float F = dielectric_fresnel(dot(wi, wh), f.eta_i / f.eta_o);
+            const float G = ggx_G(wi, wo, f.n, f.alpha);
+            const float D = ggx_D(wh, f.n, f.alpha);
+            const float base = (F * G * D) / (4.f * dot(wo, f.n) * dot(wi, f.n));
+            return diffuse + mul(f.specular * f.reflectance, base);
+        }
+        const Col diffuse = mul(f.extra, 1.f / kPi) * f.transmittance;
+        Col specular = col(0.f, 0.f, 0.f);
+        const V3 wh = refraction_half(f.eta_o, wo, f.eta_i, wi, f.n);
+        const float wo_wh = dot(wo, wh), wi_wh = dot(wi, wh);
+        if (wo_wh * wi_wh <= 0.f) {
+            const float F = dielectric_fresnel(wi_wh, f.eta_o / f.eta_i);
+            if (F < 1.f) {
+                const float G = ggx_G(wi, wo, f.n, f.alpha);
+                const float D = ggx_D(wh, f.n, f.alpha);
+                const float wo_n = dot(wo, f.n), wi_n = dot(wi, f.n);
+                const float k = fabsf((wo_wh * wi_wh) / (wo_n * wi_n));
+                const float k2 = f.eta_o * wo_wh + f.eta_i * wi_wh;
+                const float base = (f.eta_o * f.eta_o * k * G * D * (1.f - F)) / (k2 * k2);
+                specular = mul(f.specular * f.transmittance, base);
+            }
+        }
+        return diffuse + specular;
+    }
     if (FULL && f.type == kCoatedDiffuse) {
         // Ashikhmin_Shirley_Phong_BRDF::evaluate (src/ref/bsdf.cpp:440-460)
         const V3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
@@ -435,6 +528,38 @@ __device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
         const float spec_pdf = vndf_pdf(wo, wh, f.n, f.alpha) / (4 * dot(wh, wo));
         return 0.5f * (diffuse_pdf + spec_pdf);
     }
+    if (FULL && f.type == kDiffuseTransmission) {  // Diffuse_Transmission_BSDF::pdf (bsdf.cpp:128-141)
+        const float max_r = max_component(f.reflectance), max_t = max_component(f.transmittance);
+        const float pdf = fabsf(dot(f.n, wi)) * (1.f / kPi);
+        return dot(wo, f.n) * dot(wi, f.n) > 0.f ? (max_r / (max_r + max_t)) * pdf : (max_t / (max_r + max_t)) * pdf;
+    }
+    if (FULL && f.type == kUber) {  // Pbrt3_Uber_BRDF::pdf (bsdf_pbrt.cpp:74-87)
+        const float diffuse_pdf = dot(f.n, wi) / kPi;
+        const V3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
+        const V3 wh_l = normalized(wo_l + wi_l);
+        const float spec_pdf = vndf_pdf_aniso(wo_l, wh_l, f.alpha_x, f.alpha_y) / (4 * dot(wh_l, wo_l));
+        return 0.5f * (diffuse_pdf + spec_pdf);
+    }
+    if (FULL && f.type == kTranslucent) {  // Pbrt3_Translucent_BSDF::pdf (bsdf_pbrt.cpp:211-250)
+        const float max_r = max_component(f.reflectance), max_t = max_component(f.transmittance);
+        const float rp = max_r / (max_r + max_t);
+        if (dot(wo, f.n) * dot(wi, f.n) > 0.f) {
+            const float diffuse_pdf = dot(wi, f.n) * (1.f / kPi);
+            const V3 wh = normalized(wo + wi);
+            const float spec_pdf = vndf_pdf(wo, wh, f.n, f.alpha) / (4 * dot(wh, wo));
+            return rp * 0.5f * (diffuse_pdf + spec_pdf);
+        }
+        const float diffuse_pdf = -dot(wi, f.n) * (1.f / kPi);
+        float spec_pdf = 0.f;
+        const V3 wh = refraction_half(f.eta_o, wo, f.eta_i, wi, f.n);
+        if (dot(wo, wh) * dot(wi, wh) <= 0.f) {
+            const float wh_pdf = vndf_pdf(wo, wh, f.n, f.alpha);
+            const float denom = f.eta_o * dot(wo, wh) + f.eta_i * dot(wi, wh);
+            const float dwh = f.eta_i * f.eta_i * fabsf(dot(wi, wh)) / (denom * denom);
+            spec_pdf = wh_pdf * dwh;
+        }
+        return (1.f - rp) * 0.5f * (diffuse_pdf + spec_pdf);
+    }
     if (FULL && f.type == kCoatedDiffuse) {  // Ashikhmin_Shirley_Phong_BRDF::pdf (src/ref/bsdf.cpp:480-492)
         const float diffuse_pdf = dot(f.n, wi) / kPi;
         const V3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
@@ -470,14 +595,47 @@ __device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
 template <bool FULL = true>
 __device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
                                            float& pdf) {
-    if (FULL && (f.type == kPlastic || f.type == kPbrt3Plastic || f.type == kCoatedDiffuse)) {
+    if (FULL && f.type == kDiffuseTransmission) {  // Diffuse_Transmission_BSDF::sample (bsdf.cpp:114-126)
+        const float max_r = max_component(f.reflectance), max_t = max_component(f.transmittance);
+        const float sign = u_scatter < max_r / (max_r + max_t) ? 1.f : -1.f;
+        wi = local_to_world(f, mul(sample_hemisphere_cosine(u0, u1), sign));
+        pdf = bsdf_pdf<FULL>(f, wo, wi);
+        return bsdf_evaluate<FULL>(f, wo, wi);
+    }
+    if (FULL && f.type == kTranslucent) {  // Pbrt3_Translucent_BSDF::sample (bsdf_pbrt.cpp:160-209)
+        const float max_r = max_component(f.reflectance), max_t = max_component(f.transmittance);
+        const float rp = max_r / (max_r + max_t);
+        const bool reflect_side = u_scatter < rp;
+        const float u = one_minus_eps_min_s(reflect_side ? u_scatter / rp : (u_scatter - rp) / (1.f - rp));
+        if (u < 0.5f) {
+            const V3 l = sample_hemisphere_cosine(u0, u1);
+            wi = local_to_world(f, reflect_side ? l : -l);
+        } else {
+            const V3 wh = local_to_world(f, ggx_sample_vndf(u0, u1, world_to_local(f, wo), f.alpha, f.alpha));
+            if (reflect_side) {
+                const V3 c = reflect(wo, wh);
+                if (dot(c, f.n) <= 0.f) return col(0.f, 0.f, 0.f);
+                wi = c;
+            } else {
+                if (dot(wh, wo) < 0.f) return col(0.f, 0.f, 0.f);
+                V3 c;
+                if (!refract(wo, wh, f.eta_o / f.eta_i, c)) return col(0.f, 0.f, 0.f);
+                if (dot(c, f.n) >= 0.f) return col(0.f, 0.f, 0.f);
+                wi = c;
+            }
+        }
+        pdf = bsdf_pdf<FULL>(f, wo, wi);
+        if (pdf == 0.f) return col(0.f, 0.f, 0.f);
+        return bsdf_evaluate<FULL>(f, wo, wi);
+    }
+    if (FULL && (f.type == kPlastic || f.type == kPbrt3Plastic || f.type == kCoatedDiffuse || f.type == kUber)) {
         // Plastic_BRDF::sample (src/ref/bsdf.cpp:236-251), Ashikhmin_Shirley_Phong_BRDF::sample
         // (:462-478): the first 1D sample picks the diffuse or the specular lobe
         if (u_scatter < 0.5f) {
             wi = local_to_world(f, sample_hemisphere_cosine(u0, u1));
         } else {
             const V3 wo_l = world_to_local(f, wo);
-            if (f.type == kCoatedDiffuse) {
+            if (f.type == kCoatedDiffuse || f.type == kUber) {
                 const V3 wh_l = ggx_sample_vndf(u0, u1, wo_l, f.alpha_x, f.alpha_y);
                 wi = local_to_world(f, reflect(wo_l, wh_l));
             } else {

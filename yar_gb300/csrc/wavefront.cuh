@@ -734,33 +734,26 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 const float2 un = next2d(dm);
 
                 const Material_Dev& mat = S.materials[oinfo.y];
-                if (FULL && mat.delta != kDeltaNone) {
-                    // The delta branch of trace_path (path_tracing.cpp:76-112): no
-                    // light sample; the delta ray is the next extend ray, whose hit
-                    // adds the light it reaches.  A perfect refractor at total
-                    // internal reflection ends the path.
-                    V3 wi;
-                    Col atten;
-                    bounce++;
-                    if (delta_scattering(sc, mat, u_scatter, wi, atten)) {
-                        coeff = coeff * atten;
-                        const V3 o = origin_for_direction(sc, wi);
-                        nx_a = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
-                        nx_b = make_float4(wi.x, wi.y, wi.z, 0.f);
-                        want_next = true;
-                    }
-                    if (GUIDED && g.records) ps.rec[slot] = 0xffffffffu;
-                    info = (uint32_t)bounce | ((uint32_t)dm.i1d << 8) | ((uint32_t)dm.i2d << 16) | kDeltaArrival |
-                           (bounce == p.max_bounces ? kDeltaFinal : 0u);
-                } else {
-                    Bsdf f;
+                // Shading_Context::initialize_scattering (shading_context.cpp:174-186): a
+                // delta event may be chosen (for the pbrt3 uber material per sample,
+                // which remaps u_scatter); the BSDF exists unless every layer is delta.
+                float u_sc = u_scatter;
+                float bsdf_prob = 1.f;  // 1 - delta_layer_selection_probability
+                V3 delta_wi = v3(0.f, 0.f, 0.f);
+                Col delta_atten = col(1.f, 1.f, 1.f);
+                int delta = 0;
+                if (FULL && mat.delta != kDeltaNone)
+                    delta = delta_scattering(sc, mat, u_sc, delta_wi, delta_atten, bsdf_prob);
+                Bsdf f;
+                uint32_t pend = 0;
+                if (delta == 0 || bsdf_prob != 0.f) {
                     make_bsdf(sc, mat, f);
                     // estimate_direct_lighting_from_single_sample (direct_lighting.cpp:522-578):
                     // the light int(u * total_light_count), point, spot and directional lights
                     // first, then the rectangular lights (the reference asserts the index is
                     // below the total; the clamp only guards memory)
                     const int selected = min((int)(u_light_index * (float)p.total_lights), p.total_lights - 1);
-                    uint32_t pend = kPendDirect;
+                    pend = kPendDirect;
                     if (FULL && selected < p.delta_lights) {
                         // direct_lighting_from_point/spot/directional_light (direct_lighting.cpp:26-107):
                         // one shadow ray, no MIS
@@ -847,7 +840,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                         {   // BSDF-sampling half of MIS: inside the light's cone, the probe must hit it
                             V3 wi;
                             float bpdf = 0.f;
-                            const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_scatter, sc.wo, wi, bpdf);
+                            const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_sc, sc.wo, wi, bpdf);
                             if (!black(fv) && dot(-ss.axes[2], wi) >= ss.cos_theta_max) {
                                 const V3 position = origin_for_direction(sc, wi);
                                 const Col lef = Le * fv;
@@ -895,7 +888,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                         {   // BSDF-sampling half of MIS: the probe ray must hit this light
                             V3 wi;
                             float bpdf = 0.f;
-                            const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_scatter, sc.wo, wi, bpdf);
+                            const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_sc, sc.wo, wi, bpdf);
                             if (!black(fv)) {
                                 const V3 position = origin_for_direction(sc, wi);
                                 const Col lef = Le * fv;
@@ -947,7 +940,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                         {   // BSDF-sampling half of MIS: the probe ray must hit this light
                             V3 wi;
                             float bpdf = 0.f;
-                            const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_scatter, sc.wo, wi, bpdf);
+                            const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_sc, sc.wo, wi, bpdf);
                             if (!black(fv)) {
                                 const float lndw = dot(light_n, -wi);
                                 if (lndw > 1e-4f) {
@@ -965,7 +958,23 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                         }
                     }
                     ps.pend_coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0.f);
-
+                }
+                if (delta != 0) {
+                    // The delta branch of trace_path (path_tracing.cpp:76-112): the delta
+                    // ray is the next extend ray, whose hit adds the light it reaches.
+                    // A perfect refractor at total internal reflection ends the path.
+                    bounce++;
+                    if (delta == 1) {
+                        coeff = coeff * delta_atten;
+                        const V3 o = origin_for_direction(sc, delta_wi);
+                        nx_a = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
+                        nx_b = make_float4(delta_wi.x, delta_wi.y, delta_wi.z, 0.f);
+                        want_next = true;
+                    }
+                    if (GUIDED && g.records) ps.rec[slot] = 0xffffffffu;
+                    info = (uint32_t)bounce | ((uint32_t)dm.i1d << 8) | ((uint32_t)dm.i2d << 16) | kDeltaArrival |
+                           (bounce == p.max_bounces ? kDeltaFinal : 0u) | pend;
+                } else {
                     bounce++;
                     bool cont = bounce != p.max_bounces;
                     float rec_value = 0.f;
@@ -1002,7 +1011,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                             fabsf(dot(sc.n, wi)) / pdf;
                                 rec_dir = wi;
                             }
-                            coeff = coeff * mul(fv, fabsf(dot(sc.n, wi)) / (pdf * 1.f));
+                            coeff = coeff * mul(fv, fabsf(dot(sc.n, wi)) / (pdf * bsdf_prob));
                             const V3 o = origin_for_direction(sc, wi);
                             nx_a = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
                             nx_b = make_float4(wi.x, wi.y, wi.z, 0.f);
@@ -1143,7 +1152,7 @@ connect_kernel(Render_Params p, Scene_Dev S, const uint32_t* __restrict__ slots,
         const float4 L4 = ps.L[slot];
         const Col L = col(L4.x, L4.y, L4.z) + col(cv.x, cv.y, cv.z) * scaled;
         ps.L[slot] = make_float4(L.r, L.g, L.b, 0.f);
-        ps.info[slot] = info & 0x00ffffffu;
+        ps.info[slot] = info & ~(kPendShadow | kPendProbe | kPendDirect);
         if (records) {
             const uint32_t r = ps.rec[slot];
             if (r != 0xffffffffu) records[(size_t)r * kGuideRecordF4 + 5] = make_float4(L.r, L.g, L.b, 0.f);
@@ -1391,8 +1400,17 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     for (const yar_material_desc& m : R.host_materials) {
         if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL && m.type != YAR_MATERIAL_GLASS &&
             m.type != YAR_MATERIAL_PLASTIC && m.type != YAR_MATERIAL_COATED_DIFFUSE &&
-            m.type != YAR_MATERIAL_PERFECT_REFLECTOR && m.type != YAR_MATERIAL_PERFECT_REFRACTOR)
+            m.type != YAR_MATERIAL_PERFECT_REFLECTOR && m.type != YAR_MATERIAL_PERFECT_REFRACTOR &&
+            m.type != YAR_MATERIAL_DIFFUSE_TRANSMISSION && m.type != YAR_MATERIAL_PBRT3_TRANSLUCENT &&
+            m.type != YAR_MATERIAL_PBRT3_UBER)
             return fail(ctx, YAR_ERR_UNSUPPORTED, "material type " + std::to_string(m.type) + " is not implemented");
+        if (m.type == YAR_MATERIAL_PBRT3_UBER) {
+            // the reference asserts on an empty component list and has no delta transmission
+            bool ok = m.component_count >= 1 && m.component_count <= 5;
+            for (uint32_t k = 0; ok && k < m.component_count; k++)
+                ok = m.components[k] <= YAR_UBER_OPACITY && m.components[k] != YAR_UBER_DELTA_TRANSMISSION;
+            if (!ok) return fail(ctx, YAR_ERR_UNSUPPORTED, "pbrt3 uber: empty component list or delta transmission");
+        }
     }
     const size_t n_obj = R.host_object_info.size() / 4;
     for (size_t i = 0; i < n_obj; i++) {

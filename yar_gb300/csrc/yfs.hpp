@@ -23,6 +23,8 @@
 
 namespace yfs {
 
+constexpr uint32_t kMaterialRecordV1 = 72;  // yar_material_desc up to roughness_is_alpha
+
 struct Mesh {
     std::vector<float> vertices;   // 3 per vertex
     std::vector<float> normals;    // empty or 3 per vertex
@@ -173,12 +175,13 @@ inline bool write(const std::string& path, const Scene& s) {
         b.raw(s.scene_nodes.data(), n * sizeof(yar_kd_node));
         w.chunk("SKDT", b.b);
     }
-    {
+    {   // MAT2: record size first, so the records can grow
         detail::Buf b;
-        uint32_t n = (uint32_t)s.materials.size();
+        uint32_t n = (uint32_t)s.materials.size(), record = (uint32_t)sizeof(yar_material_desc);
         b.pod(n);
+        b.pod(record);
         b.raw(s.materials.data(), n * sizeof(yar_material_desc));
-        w.chunk("MATS", b.b);
+        w.chunk("MAT2", b.b);
     }
     {
         detail::Buf b;
@@ -275,11 +278,17 @@ inline bool read(const std::string& path, Scene& s, std::string* err = nullptr) 
             if ((uint64_t)n * 8 > size) return fail("bad scene tree chunk");
             s.scene_nodes.resize(n);
             c.raw(s.scene_nodes.data(), n * sizeof(yar_kd_node));
-        } else if (!memcmp(tag, "MATS", 4)) {
+        } else if (!memcmp(tag, "MATS", 4) || !memcmp(tag, "MAT2", 4)) {
+            // MATS: the first records, without the layered-material fields (72 bytes)
             uint32_t n = c.pod<uint32_t>();
-            if ((uint64_t)n * sizeof(yar_material_desc) > size) return fail("bad material chunk");
-            s.materials.resize(n);
-            c.raw(s.materials.data(), n * sizeof(yar_material_desc));
+            const uint32_t record = !memcmp(tag, "MATS", 4) ? kMaterialRecordV1 : c.pod<uint32_t>();
+            if (record < kMaterialRecordV1 || (uint64_t)n * record > size) return fail("bad material chunk");
+            s.materials.assign(n, yar_material_desc{});
+            for (uint32_t i = 0; i < n && c.ok; i++) {
+                const size_t keep = record < sizeof(yar_material_desc) ? record : sizeof(yar_material_desc);
+                c.raw(&s.materials[i], keep);
+                if (record > keep) c.p += record - keep;
+            }
         } else if (!memcmp(tag, "RLIT", 4)) {
             uint32_t n = c.pod<uint32_t>();
             if ((uint64_t)n * sizeof(yar_rect_light_desc) > size) return fail("bad light chunk");

@@ -31,6 +31,9 @@ MATERIAL_METAL = 4
 MATERIAL_PLASTIC = 5
 MATERIAL_COATED_DIFFUSE = 6
 MATERIAL_GLASS = 7
+MATERIAL_MIX = 8
+MATERIAL_PBRT3_UBER = 9
+MATERIAL_PBRT3_TRANSLUCENT = 10
 MATERIAL_NULL = 0xFFFFFFFF
 LIGHT_POINT = 0
 LIGHT_SPOT = 1
@@ -68,7 +71,10 @@ class MaterialDesc(C.Structure):
     _fields_ = [("type", C.c_uint32), ("reflectance", C.c_float * 3), ("transmittance", C.c_float * 3),
                 ("eta", C.c_float * 3), ("k", C.c_float * 3), ("eta_i", C.c_float),
                 ("u_roughness", C.c_float), ("v_roughness", C.c_float),
-                ("index_of_refraction", C.c_float), ("roughness_is_alpha", C.c_int32)]
+                ("index_of_refraction", C.c_float), ("roughness_is_alpha", C.c_int32),
+                ("specular", C.c_float * 3), ("diffuse", C.c_float * 3), ("delta_reflectance", C.c_float * 3),
+                ("opacity", C.c_float * 3), ("component_count", C.c_uint32), ("components", C.c_uint32 * 5),
+                ("mix_materials", C.c_int32 * 2), ("mix_amount", C.c_float * 3)]
 
 
 class RectLightDesc(C.Structure):

@@ -19,7 +19,11 @@ OBJECT_DTYPE = np.dtype([("mesh_index", "<i4"), ("material_type", "<u4"), ("mate
                          ("object_to_world_normal", "<f4", 12)])
 MATERIAL_DTYPE = np.dtype([("type", "<u4"), ("reflectance", "<f4", 3), ("transmittance", "<f4", 3),
                            ("eta", "<f4", 3), ("k", "<f4", 3), ("eta_i", "<f4"), ("u_roughness", "<f4"),
-                           ("v_roughness", "<f4"), ("index_of_refraction", "<f4"), ("roughness_is_alpha", "<i4")])
+                           ("v_roughness", "<f4"), ("index_of_refraction", "<f4"), ("roughness_is_alpha", "<i4"),
+                           ("specular", "<f4", 3), ("diffuse", "<f4", 3), ("delta_reflectance", "<f4", 3),
+                           ("opacity", "<f4", 3), ("component_count", "<u4"), ("components", "<u4", 5),
+                           ("mix_materials", "<i4", 2), ("mix_amount", "<f4", 3)])
+MATERIAL_RECORD_V1 = 72  # the MATS chunk's records: the fields up to roughness_is_alpha
 LIGHT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("emitted_radiance", "<f4", 3), ("size", "<f4", 2),
                         ("sample_count", "<i4")])
 DELTA_LIGHT_DTYPE = np.dtype([("type", "<u4"), ("position", "<f4", 3), ("direction", "<f4", 3),
@@ -225,7 +229,8 @@ class FlatScene:
         parts.append(chunk(b"SKDT", self.scene_bounds.astype(np.float32).tobytes() +
                            struct.pack("<I", self.scene_nodes.shape[0]) +
                            np.ascontiguousarray(self.scene_nodes, np.uint32).tobytes()))
-        parts.append(chunk(b"MATS", struct.pack("<I", self.materials.shape[0]) + self.materials.tobytes()))
+        parts.append(chunk(b"MAT2", struct.pack("<II", self.materials.shape[0], MATERIAL_DTYPE.itemsize) +
+                           np.ascontiguousarray(self.materials, MATERIAL_DTYPE).tobytes()))
         parts.append(chunk(b"RLIT", struct.pack("<I", self.rect_lights.shape[0]) + self.rect_lights.tobytes()))
         if self.delta_lights.shape[0]:
             parts.append(chunk(b"DLIT", struct.pack("<I", self.delta_lights.shape[0]) + self.delta_lights.tobytes()))
@@ -280,9 +285,14 @@ class FlatScene:
                 s.scene_bounds = np.frombuffer(p[:24], np.float32).copy()
                 n = struct.unpack_from("<I", p, 24)[0]
                 s.scene_nodes = np.frombuffer(p[28:28 + 8 * n], np.uint32).reshape(-1, 2).copy()
-            elif tag == b"MATS":
+            elif tag in (b"MATS", b"MAT2"):
                 n = struct.unpack_from("<I", p, 0)[0]
-                s.materials = np.frombuffer(p[4:4 + n * MATERIAL_DTYPE.itemsize], MATERIAL_DTYPE).copy()
+                record, q = (MATERIAL_RECORD_V1, 4) if tag == b"MATS" else (struct.unpack_from("<I", p, 4)[0], 8)
+                raw = np.frombuffer(p[q:q + n * record], np.uint8).reshape(n, record)
+                keep = min(record, MATERIAL_DTYPE.itemsize)
+                buf = np.zeros((n, MATERIAL_DTYPE.itemsize), np.uint8)
+                buf[:, :keep] = raw[:, :keep]
+                s.materials = buf.view(MATERIAL_DTYPE).reshape(n).copy()
             elif tag == b"RLIT":
                 n = struct.unpack_from("<I", p, 0)[0]
                 s.rect_lights = np.frombuffer(p[4:4 + n * LIGHT_DTYPE.itemsize], LIGHT_DTYPE).copy()

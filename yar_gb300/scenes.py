@@ -270,6 +270,35 @@ LAYERED_BOXES = ('Material "plastic" "rgb Kd" [0.6 0.25 0.1] "rgb Ks" [0.4 0.4 0
                  'Material "substrate" "rgb Kd" [0.2 0.4 0.6] "rgb Ks" [0.06 0.05 0.04] '
                  '"float uroughness" [0.1] "float vroughness" [0.3]')
 
+TRANSLUCENT_BOXES = ('Material "matte" "rgb Kd" [0.5 0.5 0.5]',
+                     'Material "translucent" "rgb Kd" [0.3 0.35 0.4] "rgb Ks" [0.6 0.6 0.6] '
+                     '"rgb reflect" [0.5 0.5 0.5] "rgb transmit" [0.5 0.45 0.4] "float roughness" [0.1]')
+
+
+UBER_BOXES = ('Material "uber" "rgb Kd" [0.5 0.3 0.2] "rgb Ks" [0.3 0.3 0.3] "rgb Kr" [0.4 0.4 0.4] '
+              '"float roughness" [0.15] "float index" [1.5]',
+              'Material "uber" "rgb Kd" [0.2 0.4 0.5] "rgb Ks" [0.2 0.2 0.2] "rgb opacity" [0.6 0.7 0.8] '
+              '"float uroughness" [0.1] "float vroughness" [0.3] "float index" [1.4]')
+
+
+def make_diffuse_transmission(flat, obj=5, reflectance=(0.6, 0.5, 0.4), transmittance=(0.3, 0.4, 0.5),
+                              scale=(1.2, 1.0, 0.9)):
+    """Turns object `obj`'s material (object 5 is cornell_pbrt's short box)
+    into a diffuse-transmission material (a YAR material pbrt has no name for)."""
+    m = flat.materials.copy()
+    o = flat.objects.copy()
+    k = int(o[obj]["material_index"])
+    m[k] = np.zeros((), m.dtype)
+    m[k]["type"] = 3  # YAR_MATERIAL_DIFFUSE_TRANSMISSION
+    m[k]["reflectance"] = reflectance
+    m[k]["transmittance"] = transmittance
+    m[k]["diffuse"] = scale
+    o[obj]["material_type"] = 3
+    flat.materials = m
+    flat.objects = o
+    return flat
+
+
 UPPER_LIGHT = (0.8, 2.3, 4.0)
 
 
