@@ -670,7 +670,18 @@ typedef struct bsdf_t {
     float eta_o, eta_i;             /* glass */
     int pbrt3_plastic, flipped;     /* plastic: Pbrt3_Plastic_BRDF, original shading normal flipped */
     col diffuse_coeff, specular_coeff; /* pbrt3 translucent: Kd, Ks */
+    const struct bsdf_t* sub[2];    /* mix: the two BSDFs; scaled: sub[0] */
+    col mix_coeff;                  /* mix: White - amount */
+    float p_coeff, scale;           /* mix: 1 - luminance(mix_coeff); scaled: the factor */
 } bsdf_t;
+
+#define ORACLE_BSDF_SCALED 0x100u   /* Scaled_BSDF: a mix whose other material is pure delta */
+
+/* ColorRGB::luminance, src/lib/color.h:74-76 with sRGB_to_XYZ (src/lib/color.cpp:18-24) */
+static float luminance(col c) { return 0.2126729f * c.r + 0.7151522f * c.g + 0.0721750f * c.b; }
+static int is_pure_delta(uint32_t type) { /* !material_has_bsdf, src/lib/material.h:27-30 */
+    return type == YAR_MATERIAL_PERFECT_REFLECTOR || type == YAR_MATERIAL_PERFECT_REFRACTOR;
+}
 
 static col clamp_unit(col c) { /* ColorRGB::clamp_to_unit_range, src/lib/color.h:83-88 */
     c.r = c.r < 0.f ? 0.f : (1.f < c.r ? 1.f : c.r);
@@ -698,13 +709,13 @@ static v3 local_to_world(const bsdf_t* f, v3 l) {
 }
 static v3 world_to_local(const bsdf_t* f, v3 w) { return mk3(dot3(w, f->t), dot3(w, f->bt), dot3(w, f->n)); }
 
-static int make_bsdf(const yar_flat_scene* s, const shading_ctx* sc, bsdf_t* f) {
+static int make_leaf_bsdf(const yar_flat_scene* s, const shading_ctx* sc, uint32_t type, const yar_material_desc* m,
+                          bsdf_t* f) {
     memset(f, 0, sizeof(*f));
     f->n = sc->normal;
     f->bt = norm3(cross3(sc->normal, sc->dpdu_shading));
     f->t = cross3(f->bt, sc->normal);
-    const yar_material_desc* m = &s->materials[sc->material_index];
-    f->type = sc->material_type;
+    f->type = type;
     if (f->type == YAR_MATERIAL_DIFFUSE) {
         f->reflection = 1;
         f->reflectance = ldc(m->reflectance);
@@ -764,6 +775,39 @@ static int make_bsdf(const yar_flat_scene* s, const shading_ctx* sc, bsdf_t* f) 
         return YAR_ERR_UNSUPPORTED;
     }
     return YAR_OK;
+}
+
+/* create_bsdf (src/ref/bsdf.cpp:631-714) with create_mix_bsdf (:599-629): a mix of
+ * two BSDF materials is a Mix_BSDF, a mix with a pure delta material the Scaled_BSDF
+ * of the other one.  sub holds the mix's leaf BSDFs. */
+static int make_bsdf(const yar_flat_scene* s, const shading_ctx* sc, bsdf_t* f, bsdf_t sub[2]) {
+    const yar_material_desc* m = &s->materials[sc->material_index];
+    if (sc->material_type != YAR_MATERIAL_MIX) return make_leaf_bsdf(s, sc, sc->material_type, m, f);
+    const yar_material_desc* m1 = &s->materials[m->mix_materials[0]];
+    const yar_material_desc* m2 = &s->materials[m->mix_materials[1]];
+    const int has1 = !is_pure_delta(m1->type), has2 = !is_pure_delta(m2->type);
+    if (!has1 && !has2) return YAR_ERR_UNSUPPORTED;
+    const float amount = luminance(ldc(m->mix_amount));
+    int rc = make_leaf_bsdf(s, sc, YAR_MATERIAL_DIFFUSE, m, f); /* the frame */
+    if (rc != YAR_OK) return rc;
+    f->sub[0] = &sub[0];
+    if (!has1 || !has2) {
+        rc = make_leaf_bsdf(s, sc, has1 ? m1->type : m2->type, has1 ? m1 : m2, &sub[0]);
+        f->type = ORACLE_BSDF_SCALED;
+        f->scale = has1 ? amount : 1.f - amount;
+        f->reflection = sub[0].reflection;
+        f->transmission = sub[0].transmission;
+        return rc;
+    }
+    rc = make_leaf_bsdf(s, sc, m1->type, m1, &sub[0]);
+    if (rc == YAR_OK) rc = make_leaf_bsdf(s, sc, m2->type, m2, &sub[1]);
+    f->sub[1] = &sub[1];
+    f->type = YAR_MATERIAL_MIX;
+    f->mix_coeff = subc(mkc(1, 1, 1), ldc(m->mix_amount));
+    f->p_coeff = 1.f - luminance(f->mix_coeff);
+    f->reflection = sub[0].reflection || sub[1].reflection;
+    f->transmission = sub[0].transmission || sub[1].transmission;
+    return rc;
 }
 
 /* The sine and cosine of sampled angles.  The reference calls the C library's
@@ -906,7 +950,7 @@ static v3 refraction_half(float eta_o, v3 wo, float eta_i, v3 wi, v3 n) {
 
 static float pow5(float v) { return (v * v) * (v * v) * v; }
 
-static col bsdf_evaluate(const bsdf_t* f, v3 wo, v3 wi) {
+static col leaf_evaluate(const bsdf_t* f, v3 wo, v3 wi) {
     if (f->type == YAR_MATERIAL_DIFFUSE) return mulcs(f->reflectance, PI_INV_F);
     if (f->type == YAR_MATERIAL_PBRT3_UBER) { /* src/ref/bsdf_pbrt.cpp:34-52; diffuse_coeff holds the opacity */
         col diffuse = mulc(mulcs(f->reflectance, PI_INV_F), f->diffuse_coeff);
@@ -1028,7 +1072,7 @@ static float glass_reflection_probability(const bsdf_t* f, float fresnel) {
     return ((r + t) == 0) ? 0.f : r / (r + t);
 }
 
-static float bsdf_pdf(const bsdf_t* f, v3 wo, v3 wi) {
+static float leaf_pdf(const bsdf_t* f, v3 wo, v3 wi) {
     if (f->type == YAR_MATERIAL_DIFFUSE) return dot3(f->n, wi) / PI_F;
     if (f->type == YAR_MATERIAL_PBRT3_UBER) { /* src/ref/bsdf_pbrt.cpp:74-87 */
         float diffuse_pdf = dot3(f->n, wi) / PI_F;
@@ -1093,13 +1137,13 @@ static float bsdf_pdf(const bsdf_t* f, v3 wo, v3 wi) {
 }
 
 /* BSDF::sample; returns black when no direction is produced. */
-static col bsdf_sample(const bsdf_t* f, float u0, float u1, float u_scatter, v3 wo, v3* wi, float* pdf) {
+static col leaf_sample(const bsdf_t* f, float u0, float u1, float u_scatter, v3 wo, v3* wi, float* pdf) {
     if (f->type == YAR_MATERIAL_DIFFUSE_TRANSMISSION) { /* src/ref/bsdf.cpp:114-126 */
         float max_r = maxcomp(f->reflectance), max_t = maxcomp(f->transmittance);
         float sign = u_scatter < max_r / (max_r + max_t) ? 1.f : -1.f;
         *wi = local_to_world(f, mul3s(sample_hemisphere_cosine(u0, u1), sign));
-        *pdf = bsdf_pdf(f, wo, *wi);
-        return bsdf_evaluate(f, wo, *wi);
+        *pdf = leaf_pdf(f, wo, *wi);
+        return leaf_evaluate(f, wo, *wi);
     }
     if (f->type == YAR_MATERIAL_PBRT3_TRANSLUCENT) { /* src/ref/bsdf_pbrt.cpp:160-209 */
         float max_r = maxcomp(f->reflectance), max_t = maxcomp(f->transmittance);
@@ -1129,15 +1173,15 @@ static col bsdf_sample(const bsdf_t* f, float u0, float u1, float u_scatter, v3 
                 *wi = c;
             }
         }
-        *pdf = bsdf_pdf(f, wo, *wi);
+        *pdf = leaf_pdf(f, wo, *wi);
         if (*pdf == 0.f) return mkc(0, 0, 0);
-        return bsdf_evaluate(f, wo, *wi);
+        return leaf_evaluate(f, wo, *wi);
     }
     if (f->type == YAR_MATERIAL_DIFFUSE) {
         v3 l = sample_hemisphere_cosine(u0, u1);
         *wi = local_to_world(f, l);
-        *pdf = bsdf_pdf(f, wo, *wi);
-        return bsdf_evaluate(f, wo, *wi);
+        *pdf = leaf_pdf(f, wo, *wi);
+        return leaf_evaluate(f, wo, *wi);
     }
     if (f->type == YAR_MATERIAL_PLASTIC || f->type == YAR_MATERIAL_COATED_DIFFUSE ||
         f->type == YAR_MATERIAL_PBRT3_UBER) {
@@ -1157,8 +1201,8 @@ static col bsdf_sample(const bsdf_t* f, float u0, float u1, float u_scatter, v3 
             }
         }
         if (dot3(f->n, *wi) <= 0.f) return mkc(0, 0, 0);
-        *pdf = bsdf_pdf(f, wo, *wi);
-        return bsdf_evaluate(f, wo, *wi);
+        *pdf = leaf_pdf(f, wo, *wi);
+        return leaf_evaluate(f, wo, *wi);
     }
     if (f->type == YAR_MATERIAL_METAL) {
         v3 wo_l = world_to_local(f, wo);
@@ -1167,7 +1211,7 @@ static col bsdf_sample(const bsdf_t* f, float u0, float u1, float u_scatter, v3 
         if (wi_l.z <= 0.f) return mkc(0, 0, 0);
         *wi = local_to_world(f, wi_l);
         *pdf = refl_pdf_aniso(wo_l, wh_l, f->alpha_x, f->alpha_y);
-        return bsdf_evaluate(f, wo, *wi);
+        return leaf_evaluate(f, wo, *wi);
     }
     /* rough glass, src/ref/bsdf.cpp:336-370 */
     v3 wo_l = world_to_local(f, wo);
@@ -1184,9 +1228,56 @@ static col bsdf_sample(const bsdf_t* f, float u0, float u1, float u_scatter, v3 
         if (!refract3(wo, wh, f->eta_o / f->eta_i, wi)) return mkc(0, 0, 0);
         if (dot3(*wi, f->n) >= 0.f) return mkc(0, 0, 0);
     }
-    *pdf = bsdf_pdf(f, wo, *wi);
+    *pdf = leaf_pdf(f, wo, *wi);
     if (*pdf == 0.f) return mkc(0, 0, 0);
-    return bsdf_evaluate(f, wo, *wi);
+    return leaf_evaluate(f, wo, *wi);
+}
+
+/* Mix_BSDF (src/ref/bsdf.cpp:497-567) and Scaled_BSDF (:572-592) over leaf
+ * BSDFs; every other BSDF forwards to its own functions. */
+static int possible_for(const bsdf_t* f, float n_dot_wi) {
+    return (n_dot_wi > 0 && f->reflection) || (n_dot_wi < 0 && f->transmission);
+}
+static col bsdf_evaluate(const bsdf_t* f, v3 wo, v3 wi) {
+    if (f->type == ORACLE_BSDF_SCALED) return mulcs(leaf_evaluate(f->sub[0], wo, wi), f->scale);
+    if (f->type != YAR_MATERIAL_MIX) return leaf_evaluate(f, wo, wi);
+    col f1 = mkc(0, 0, 0), f2 = mkc(0, 0, 0);
+    float n_dot_wi = dot3(f->n, wi);
+    if (possible_for(f->sub[0], n_dot_wi)) f1 = leaf_evaluate(f->sub[0], wo, wi);
+    if (possible_for(f->sub[1], n_dot_wi)) f2 = leaf_evaluate(f->sub[1], wo, wi);
+    return addc(mulc(subc(mkc(1, 1, 1), f->mix_coeff), f1), mulc(f->mix_coeff, f2));
+}
+static float bsdf_pdf(const bsdf_t* f, v3 wo, v3 wi) {
+    if (f->type == ORACLE_BSDF_SCALED) return leaf_pdf(f->sub[0], wo, wi);
+    if (f->type != YAR_MATERIAL_MIX) return leaf_pdf(f, wo, wi);
+    float n_dot_wi = dot3(f->n, wi);
+    float pdf1 = 0.f, pdf2 = 0.f;
+    if (possible_for(f->sub[0], n_dot_wi)) pdf1 = leaf_pdf(f->sub[0], wo, wi);
+    if (possible_for(f->sub[1], n_dot_wi)) pdf2 = leaf_pdf(f->sub[1], wo, wi);
+    return (1.f - f->p_coeff) * pdf1 + f->p_coeff * pdf2;
+}
+static col bsdf_sample(const bsdf_t* f, float u0, float u1, float u_scatter, v3 wo, v3* wi, float* pdf) {
+    if (f->type == ORACLE_BSDF_SCALED) return mulcs(leaf_sample(f->sub[0], u0, u1, u_scatter, wo, wi, pdf), f->scale);
+    if (f->type != YAR_MATERIAL_MIX) return leaf_sample(f, u0, u1, u_scatter, wo, wi, pdf);
+    col f1 = mkc(0, 0, 0), f2 = mkc(0, 0, 0);
+    float pdf1 = 0.f, pdf2 = 0.f;
+    if (u_scatter < f->p_coeff) {
+        f2 = leaf_sample(f->sub[1], u0, u1, u_scatter / f->p_coeff, wo, wi, &pdf2);
+        float n_dot_wi = dot3(f->n, *wi);
+        if (possible_for(f->sub[0], n_dot_wi)) {
+            pdf1 = leaf_pdf(f->sub[0], wo, *wi);
+            f1 = leaf_evaluate(f->sub[0], wo, *wi);
+        }
+    } else {
+        f1 = leaf_sample(f->sub[0], u0, u1, (u_scatter - f->p_coeff) / (1.f - f->p_coeff), wo, wi, &pdf1);
+        float n_dot_wi = dot3(f->n, *wi);
+        if (possible_for(f->sub[1], n_dot_wi)) {
+            pdf2 = leaf_pdf(f->sub[1], wo, *wi);
+            f2 = leaf_evaluate(f->sub[1], wo, *wi);
+        }
+    }
+    *pdf = (1.f - f->p_coeff) * pdf1 + f->p_coeff * pdf2;
+    return addc(mulc(subc(mkc(1, 1, 1), f->mix_coeff), f1), mulc(f->mix_coeff, f2));
 }
 
 /* ---------------- ray queries on the flat scene */
@@ -1243,7 +1334,7 @@ static col direct_rect(const yar_flat_scene* s, const shading_ctx* sc, const bsd
         }
     }
     {
-        v3 wi;
+        v3 wi = mk3(0, 0, 0); /* Vector3 default: a BSDF sample may leave it unset */
         float bpdf;
         col fv = bsdf_sample(f, ub0, ub1, u_scatter, sc->wo, &wi, &bpdf);
         if (!blackc(fv)) {
@@ -1446,7 +1537,7 @@ static col direct_mesh(const yar_flat_scene* s, const shading_ctx* sc, const bsd
         }
     }
     {
-        v3 wi;
+        v3 wi = mk3(0, 0, 0);
         float bpdf;
         col fv = bsdf_sample(f, ub0, ub1, u_scatter, sc->wo, &wi, &bpdf);
         if (!blackc(fv)) {
@@ -1535,7 +1626,7 @@ static col direct_sphere(const yar_flat_scene* s, const shading_ctx* sc, const b
         }
     }
     {
-        v3 wi;
+        v3 wi = mk3(0, 0, 0);
         float bpdf;
         col fv = bsdf_sample(f, ub0, ub1, u_scatter, sc->wo, &wi, &bpdf);
         if (!blackc(fv) && dot3(neg3(ss.axes[2]), wi) >= ss.cos_theta_max) {
@@ -1622,6 +1713,38 @@ static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, floa
             return 1;
         }
         return 0;
+    }
+    if (sc->material_type == YAR_MATERIAL_MIX) {
+        /* get_mix_info, src/ref/delta_scattering.cpp:154-189, with sub-materials that are
+         * pure delta or have no delta event */
+        const yar_material_desc* m1 = &s->materials[m->mix_materials[0]];
+        const yar_material_desc* m2 = &s->materials[m->mix_materials[1]];
+        const float amount = fminf_std(luminance(ldc(m->mix_amount)), 1.f);
+        const int has1 = !is_pure_delta(m1->type), has2 = !is_pure_delta(m2->type);
+        const yar_material_desc* pick;
+        if (*u_ptr < amount) {
+            *u_ptr /= amount;
+            pick = m1;
+        } else {
+            *u_ptr = (*u_ptr - amount) / (1.f - amount);
+            pick = m2;
+        }
+        int event = 0;
+        float prob = 0.f;
+        if (pick->type == YAR_MATERIAL_PERFECT_REFLECTOR) {
+            *dir = reflect3(sc->wo, sc->normal);
+            *atten = ldc(pick->reflectance);
+            event = 1;
+            prob = 1.f;
+        } else if (pick->type == YAR_MATERIAL_PERFECT_REFRACTOR) {
+            const float eta = !sc->flipped ? 1.f / pick->index_of_refraction : pick->index_of_refraction;
+            event = refract3(sc->wo, sc->normal, eta, dir) ? 1 : 2;
+            prob = 1.f;
+        }
+        if (has1 && has2) prob *= pick == m1 ? amount : 1.f - amount;
+        else prob = has1 ? 1.f - amount : amount;
+        *bsdf_prob = 1.f - prob;
+        return event;
     }
     const float u = *u_ptr;
     if (sc->material_type != YAR_MATERIAL_PERFECT_REFLECTOR && sc->material_type != YAR_MATERIAL_PERFECT_REFRACTOR &&
@@ -1719,9 +1842,9 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
         float bsdf_prob = 1.f; /* 1 - delta_layer_selection_probability */
         const int delta = delta_scattering(s, &sc, &u_scatter, &ddir, &datten, &bsdf_prob);
         if (delta == 2) break; /* perfect refractor at total internal reflection */
-        bsdf_t f;
+        bsdf_t f, f_sub[2];
         if (!delta || bsdf_prob != 0.f) {
-            int rc = make_bsdf(s, &sc, &f);
+            int rc = make_bsdf(s, &sc, &f, f_sub);
             if (rc != YAR_OK) return rc;
             /* estimate_direct_lighting_from_single_sample, src/ref/direct_lighting.cpp:522-578 */
             int light_index = (int)(u_light_index * (float)total_lights);
@@ -1741,7 +1864,7 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
         if (!delta) {
             bounce++;
             if (bounce == cfg->max_light_bounces) break;
-            v3 wi;
+            v3 wi = mk3(0, 0, 0);
             float pdf;
             col fv = bsdf_sample(&f, un0, un1, u_scatter_next, sc.wo, &wi, &pdf);
             if (blackc(fv)) break;
@@ -1942,12 +2065,27 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
         if (t != YAR_MATERIAL_DIFFUSE && t != YAR_MATERIAL_METAL && t != YAR_MATERIAL_GLASS &&
             t != YAR_MATERIAL_PLASTIC && t != YAR_MATERIAL_COATED_DIFFUSE && t != YAR_MATERIAL_PERFECT_REFLECTOR &&
             t != YAR_MATERIAL_PERFECT_REFRACTOR && t != YAR_MATERIAL_DIFFUSE_TRANSMISSION &&
-            t != YAR_MATERIAL_PBRT3_TRANSLUCENT && t != YAR_MATERIAL_PBRT3_UBER)
+            t != YAR_MATERIAL_PBRT3_TRANSLUCENT && t != YAR_MATERIAL_PBRT3_UBER && t != YAR_MATERIAL_MIX)
             return YAR_ERR_UNSUPPORTED;
     }
     if (s->other_light_count) return YAR_ERR_UNSUPPORTED;
     for (uint32_t i = 0; i < s->material_count; i++) {
         const yar_material_desc* m = &s->materials[i];
+        if (m->type == YAR_MATERIAL_MIX) {
+            /* sub-materials: pure delta, or BSDF materials without a delta event; not both delta */
+            int delta_subs = 0;
+            for (int k = 0; k < 2; k++) {
+                const int32_t si = m->mix_materials[k];
+                if (si < 0 || (uint32_t)si >= s->material_count) return YAR_ERR_INVALID;
+                const yar_material_desc* sm = &s->materials[si];
+                if (sm->type == YAR_MATERIAL_MIX || sm->type == YAR_MATERIAL_PBRT3_UBER ||
+                    (sm->type == YAR_MATERIAL_GLASS && !(sm->u_roughness > 0.f)))
+                    return YAR_ERR_UNSUPPORTED;
+                delta_subs += is_pure_delta(sm->type);
+            }
+            if (delta_subs == 2) return YAR_ERR_UNSUPPORTED;
+            continue;
+        }
         if (m->type != YAR_MATERIAL_PBRT3_UBER) continue;
         if (m->component_count < 1 || m->component_count > 5) return YAR_ERR_UNSUPPORTED;
         for (uint32_t k = 0; k < m->component_count; k++)

@@ -52,6 +52,9 @@ Fixtures
                              rendered by the reference from the flat scene.
   cornell_uber_64.yfs / .npz  pbrt "uber" boxes: one with a delta-reflection
                              layer, one with opacity (passthrough), seed 10.
+  cornell_mix_64.yfs / .npz  pbrt "mix" boxes: matte with metal (Mix_BSDF) and
+                             mirror with plastic (a delta layer and a scaled
+                             BSDF), seed 11.
 """
 import os
 import re
@@ -280,6 +283,10 @@ def cornell_uber_64():
     _pbrt_golden("cornell_uber_64", 10, box_materials=scenes.UBER_BOXES)
 
 
+def cornell_mix_64():
+    _pbrt_golden("cornell_mix_64", 11, box_materials=scenes.MIX_BOXES, named_materials=scenes.MIX_NAMED)
+
+
 def kdtree_cache_files():
     """The reference's kd-tree cache files (KdTree::save) of the raycast_small
     scene's first two meshes and of its scene tree."""
@@ -325,7 +332,7 @@ if __name__ == "__main__":
                              "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "cornell_layered_64",
                              "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64",
                              "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64",
-                             "cornell_uber_64",
+                             "cornell_uber_64", "cornell_mix_64",
                              "exr_files",
                              "kdtree_cache_files"]
     for name in which:

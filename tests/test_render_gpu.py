@@ -42,7 +42,7 @@ def compare(img, ref):
 
 @pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64",
                                   "cornell_layered_64", "cornell_layered_yar_64", "cornell_lights_64",
-                                  "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64"])
+                                  "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64"])
 def test_render_matches_reference_golden(gpu_ctx, name):
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
@@ -62,7 +62,7 @@ def test_render_matches_reference_golden(gpu_ctx, name):
 
 RENDER_GOLDENS = ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "cornell_layered_64",
                   "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64", "cornell_spherelight_64",
-                  "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64"]
+                  "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64"]
 
 
 @pytest.mark.parametrize("name", RENDER_GOLDENS)

@@ -95,6 +95,39 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
             d.delta = kDeltaUber;  // every sample picks a layer
         }
     }
+    // BSDF::reflection_scattering / transmission_scattering of each material, then the
+    // mixes (Mix_BSDF, Scaled_BSDF and get_mix_info's constants, bsdf.cpp:497-629)
+    auto luminance = [](const float* c) { return 0.2126729f * c[0] + 0.7151522f * c[1] + 0.0721750f * c[2]; };
+    for (uint32_t i = 0; i < scene->material_count; i++) {
+        const yar_material_desc& m = scene->materials[i];
+        const bool black_r = !(m.reflectance[0] != 0.f || m.reflectance[1] != 0.f || m.reflectance[2] != 0.f);
+        const bool black_t = !(m.transmittance[0] != 0.f || m.transmittance[1] != 0.f || m.transmittance[2] != 0.f);
+        uint32_t sc = 1u;
+        if (m.type == YAR_MATERIAL_GLASS || m.type == YAR_MATERIAL_DIFFUSE_TRANSMISSION) sc = 3u;
+        if (m.type == YAR_MATERIAL_PBRT3_TRANSLUCENT) sc = (black_r ? 0u : 1u) | (black_t ? 0u : 2u);
+        if (m.type == YAR_MATERIAL_PERFECT_REFLECTOR || m.type == YAR_MATERIAL_PERFECT_REFRACTOR) sc = 0u;
+        mats[i].scattering = sc;
+    }
+    for (uint32_t i = 0; i < scene->material_count; i++) {
+        const yar_material_desc& m = scene->materials[i];
+        if (m.type != YAR_MATERIAL_MIX) continue;
+        Material_Dev& d = mats[i];
+        const int32_t a = m.mix_materials[0], b = m.mix_materials[1];
+        if (a < 0 || b < 0 || (uint32_t)a >= scene->material_count || (uint32_t)b >= scene->material_count)
+            return fail(ctx, YAR_ERR_INVALID, "mix material " + std::to_string(i) + " has no valid sub-materials");
+        d.mix_sub[0] = a;
+        d.mix_sub[1] = b;
+        const float lum = luminance(m.mix_amount);
+        d.mix_lum = lum;
+        d.mix_amount = 1.f < lum ? 1.f : lum;
+        d.mix_coeff = Col{1.f - m.mix_amount[0], 1.f - m.mix_amount[1], 1.f - m.mix_amount[2]};
+        const float coeff[3] = {d.mix_coeff.r, d.mix_coeff.g, d.mix_coeff.b};
+        d.mix_p = 1.f - luminance(coeff);
+        const bool has_a = mats[a].type != kPerfectReflector && mats[a].type != kPerfectRefractor;
+        const bool has_b = mats[b].type != kPerfectReflector && mats[b].type != kPerfectRefractor;
+        d.scattering = (has_a ? mats[a].scattering : 0u) | (has_b ? mats[b].scattering : 0u);
+        d.delta = kDeltaMix;
+    }
     std::vector<Rect_Light_Dev> lights(std::max<uint32_t>(1, scene->rect_light_count));
     for (uint32_t i = 0; i < scene->rect_light_count; i++) {
         const yar_rect_light_desc& l = scene->rect_lights[i];

@@ -142,14 +142,16 @@ enum : uint32_t {
     kPlastic = 5,
     kCoatedDiffuse = 6,
     kGlass = 7,
+    kMix = 8,
     kUber = 9,
     kTranslucent = 10,
-    kPbrt3Plastic = 0x105
+    kPbrt3Plastic = 0x105,
+    kScaled = 0x108  // a mix with a pure delta material: the other one's BSDF, scaled
 };
 
 // How a material scatters without a BSDF: not at all (kDeltaNone), as a
 // mirror, a perfect refractor, or smooth glass (glass of roughness 0).
-enum : uint32_t { kDeltaNone = 0, kDeltaReflector = 1, kDeltaRefractor = 2, kDeltaGlass = 3, kDeltaUber = 4 };
+enum : uint32_t { kDeltaNone = 0, kDeltaReflector = 1, kDeltaRefractor = 2, kDeltaGlass = 3, kDeltaUber = 4, kDeltaMix = 5 };
 
 // Material constants as the BSDF constructors evaluate them (src/ref/bsdf.cpp:60-66,
 // :146-158, :205-213, :268-294, :427-438); alpha values are computed on the host
@@ -166,6 +168,12 @@ struct Material_Dev {
     Col specular;     // pbrt3 uber, pbrt3 translucent: Ks
     Col extra;        // pbrt3 uber: opacity; pbrt3 translucent: Kd
     Col delta_reflectance;  // pbrt3 uber: Kr
+    uint32_t scattering;    // bit 0 reflection, bit 1 transmission (BSDF::reflection/transmission_scattering)
+    int32_t mix_sub[2];     // mix: the two materials
+    float mix_amount;       // mix: min(luminance(amount), 1), the layer choice
+    float mix_p;            // mix: 1 - luminance(White - amount) (Mix_BSDF::p_coeff)
+    float mix_lum;          // mix: luminance(amount), unclamped (the Scaled_BSDF factor)
+    Col mix_coeff;          // mix: White - amount
 };
 
 struct Bsdf {
@@ -175,6 +183,9 @@ struct Bsdf {
     bool flipped;  // the shading normal was flipped towards wo (Pbrt3_Plastic_BRDF's IOR choice)
     Col reflectance, transmittance, eta_t, k_t;
     Col specular, extra;  // pbrt3 uber: Ks, opacity; pbrt3 translucent: Ks, Kd
+    const Material_Dev* sub[2];  // mix: the two materials; scaled: sub[0]
+    Col mix_coeff;
+    float mix_p;
     float alpha_x, alpha_y, alpha, eta_i_metal, eta_o, eta_i;
 };
 
@@ -184,15 +195,12 @@ __device__ __forceinline__ V3 local_to_world(const Bsdf& f, V3 l) {
 }
 __device__ __forceinline__ V3 world_to_local(const Bsdf& f, V3 w) { return v3(dot(w, f.t), dot(w, f.bt), dot(w, f.n)); }
 
-__device__ __forceinline__ void make_bsdf(const Shading& sc, const Material_Dev& m, Bsdf& f) {
+// The material part of a BSDF (its frame and flip stay): the constructors of
+// src/ref/bsdf.cpp and bsdf_pbrt.cpp with constant parameters.
+__device__ __forceinline__ void set_material(Bsdf& f, const Material_Dev& m) {
     f.type = m.type;
-    f.n = sc.n;
-    f.bt = normalized(cross(sc.n, sc.dpdu_shading));
-    f.t = cross(f.bt, sc.n);
-    f.reflection = m.type != kTranslucent || !black(m.reflectance);
-    f.transmission = m.type == kGlass || m.type == kDiffuseTransmission ||
-                     (m.type == kTranslucent && !black(m.transmittance));
-    f.flipped = sc.flipped;
+    f.reflection = (m.scattering & 1u) != 0;
+    f.transmission = (m.scattering & 2u) != 0;
     f.specular = m.specular;
     f.extra = m.extra;
     f.reflectance = m.reflectance;
@@ -203,7 +211,7 @@ __device__ __forceinline__ void make_bsdf(const Shading& sc, const Material_Dev&
     f.alpha_y = m.alpha_y;
     f.alpha = m.alpha;
     f.eta_i_metal = m.eta_i_metal;
-    const bool enter = !sc.flipped;
+    const bool enter = !f.flipped;
     f.eta_o = enter ? 1.f : m.ior;
     f.eta_i = enter ? m.ior : 1.f;
     if (m.type == kTranslucent) {  // Pbrt3_Translucent_BSDF: the fixed 1.0 / 1.5 pair
@@ -211,6 +219,31 @@ __device__ __forceinline__ void make_bsdf(const Shading& sc, const Material_Dev&
         f.eta_i = enter ? 1.5f : 1.f;
     } else if (m.type == kUber) {  // Pbrt3_Uber_BRDF's relative IOR (bsdf_pbrt.cpp:14-32)
         f.eta_i = enter ? m.ior : 1.f / m.ior;
+    }
+}
+
+// create_bsdf (src/ref/bsdf.cpp:631-714): the frame from the shading normal and
+// dpdu, then the material.  A mix (create_mix_bsdf, :599-629) keeps its two
+// materials and builds their BSDFs when it is evaluated or sampled.
+__device__ __forceinline__ void make_bsdf(const Shading& sc, const Material_Dev& m, const Material_Dev* materials,
+                                          Bsdf& f) {
+    f.n = sc.n;
+    f.bt = normalized(cross(sc.n, sc.dpdu_shading));
+    f.t = cross(f.bt, sc.n);
+    f.flipped = sc.flipped;
+    set_material(f, m);
+    if (m.type == kMix) {
+        const Material_Dev& m1 = materials[m.mix_sub[0]];
+        const Material_Dev& m2 = materials[m.mix_sub[1]];
+        const bool has1 = m1.type != kPerfectReflector && m1.type != kPerfectRefractor;
+        const bool has2 = m2.type != kPerfectReflector && m2.type != kPerfectRefractor;
+        f.type = has1 && has2 ? kMix : kScaled;
+        f.sub[0] = has1 ? &m1 : &m2;
+        f.sub[1] = &m2;
+        f.mix_coeff = m.mix_coeff;
+        f.mix_p = has1 && has2 ? m.mix_p : (has1 ? m.mix_lum : 1.f - m.mix_lum);
+        f.reflection = (m.scattering & 1u) != 0;
+        f.transmission = (m.scattering & 2u) != 0;
     }
 }
 
@@ -239,10 +272,37 @@ __device__ __forceinline__ float dielectric_fresnel(float cos_i, float eta) {
 // set) or 2: a perfect refractor at total internal reflection, where the
 // reference has no direction (an assertion) and the path ends.  bsdf_prob is
 // 1 - the delta layers' selection probability.
-__device__ __forceinline__ int delta_scattering(const Shading& sc, const Material_Dev& m, float& u, V3& dir,
-                                                Col& atten, float& bsdf_prob) {
+__device__ __forceinline__ int delta_scattering(const Shading& sc, const Material_Dev& m,
+                                                const Material_Dev* materials, float& u, V3& dir, Col& atten,
+                                                float& bsdf_prob) {
     atten = col(1.f, 1.f, 1.f);
     const bool enter = !sc.flipped;
+    if (m.delta == kDeltaMix) {
+        // get_mix_info (delta_scattering.cpp:154-189) for sub-materials that are pure
+        // delta or have no delta event
+        const Material_Dev& m1 = materials[m.mix_sub[0]];
+        const Material_Dev& m2 = materials[m.mix_sub[1]];
+        const bool has1 = m1.type != kPerfectReflector && m1.type != kPerfectRefractor;
+        const bool has2 = m2.type != kPerfectReflector && m2.type != kPerfectRefractor;
+        const bool first = u < m.mix_amount;
+        u = first ? u / m.mix_amount : (u - m.mix_amount) / (1.f - m.mix_amount);
+        const Material_Dev& pick = first ? m1 : m2;
+        int event = 0;
+        float prob = 0.f;
+        if (pick.type == kPerfectReflector) {
+            dir = reflect(sc.wo, sc.n);
+            atten = pick.reflectance;
+            event = 1;
+            prob = 1.f;
+        } else if (pick.type == kPerfectRefractor) {
+            event = refract(sc.wo, sc.n, enter ? 1.f / pick.ior : pick.ior, dir) ? 1 : 2;
+            prob = 1.f;
+        }
+        if (has1 && has2) prob *= first ? m.mix_amount : 1.f - m.mix_amount;
+        else prob = has1 ? 1.f - m.mix_amount : m.mix_amount;
+        bsdf_prob = 1.f - prob;
+        return event;
+    }
     if (m.delta == kDeltaUber) {
         // get_pbrt_uber_info (delta_scattering.cpp:102-150): u picks a layer and is
         // re-normalised for the BSDF; delta reflection and opacity are delta events
@@ -410,7 +470,7 @@ __device__ __forceinline__ float pow5(float v) { return (v * v) * (v * v) * v; }
 // FULL = false compiles out the plastic and coated-diffuse branches, for
 // scenes that only use the diffuse, metal and rough-glass BSDFs.
 template <bool FULL = true>
-__device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
+__device__ __forceinline__ Col leaf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
     if (f.type == kDiffuse) return mul(f.reflectance, 1.f / kPi);
     if (FULL && (f.type == kPlastic || f.type == kPbrt3Plastic)) {
         // Plastic_BRDF::evaluate (src/ref/bsdf.cpp:215-234); Pbrt3_Plastic_BRDF::evaluate
@@ -520,7 +580,7 @@ __device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
 }
 
 template <bool FULL = true>
-__device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
+__device__ __forceinline__ float leaf_pdf(const Bsdf& f, V3 wo, V3 wi) {
     if (f.type == kDiffuse) return dot(f.n, wi) / kPi;
     if (FULL && (f.type == kPlastic || f.type == kPbrt3Plastic)) {  // Plastic_BRDF::pdf (src/ref/bsdf.cpp:253-263)
         const float diffuse_pdf = dot(f.n, wi) / kPi;
@@ -593,14 +653,14 @@ __device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
 
 // BSDF::sample; black when no direction is produced.
 template <bool FULL = true>
-__device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
+__device__ __forceinline__ Col leaf_sample(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
                                            float& pdf) {
     if (FULL && f.type == kDiffuseTransmission) {  // Diffuse_Transmission_BSDF::sample (bsdf.cpp:114-126)
         const float max_r = max_component(f.reflectance), max_t = max_component(f.transmittance);
         const float sign = u_scatter < max_r / (max_r + max_t) ? 1.f : -1.f;
         wi = local_to_world(f, mul(sample_hemisphere_cosine(u0, u1), sign));
-        pdf = bsdf_pdf<FULL>(f, wo, wi);
-        return bsdf_evaluate<FULL>(f, wo, wi);
+        pdf = leaf_pdf<FULL>(f, wo, wi);
+        return leaf_evaluate<FULL>(f, wo, wi);
     }
     if (FULL && f.type == kTranslucent) {  // Pbrt3_Translucent_BSDF::sample (bsdf_pbrt.cpp:160-209)
         const float max_r = max_component(f.reflectance), max_t = max_component(f.transmittance);
@@ -624,9 +684,9 @@ __device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, fl
                 wi = c;
             }
         }
-        pdf = bsdf_pdf<FULL>(f, wo, wi);
+        pdf = leaf_pdf<FULL>(f, wo, wi);
         if (pdf == 0.f) return col(0.f, 0.f, 0.f);
-        return bsdf_evaluate<FULL>(f, wo, wi);
+        return leaf_evaluate<FULL>(f, wo, wi);
     }
     if (FULL && (f.type == kPlastic || f.type == kPbrt3Plastic || f.type == kCoatedDiffuse || f.type == kUber)) {
         // Plastic_BRDF::sample (src/ref/bsdf.cpp:236-251), Ashikhmin_Shirley_Phong_BRDF::sample
@@ -644,13 +704,13 @@ __device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, fl
             }
         }
         if (dot(f.n, wi) <= 0.f) return col(0.f, 0.f, 0.f);
-        pdf = bsdf_pdf<FULL>(f, wo, wi);
-        return bsdf_evaluate<FULL>(f, wo, wi);
+        pdf = leaf_pdf<FULL>(f, wo, wi);
+        return leaf_evaluate<FULL>(f, wo, wi);
     }
     if (f.type == kDiffuse) {
         wi = local_to_world(f, sample_hemisphere_cosine(u0, u1));
-        pdf = bsdf_pdf<FULL>(f, wo, wi);
-        return bsdf_evaluate<FULL>(f, wo, wi);
+        pdf = leaf_pdf<FULL>(f, wo, wi);
+        return leaf_evaluate<FULL>(f, wo, wi);
     }
     if (f.type == kMetal) {
         const V3 wo_l = world_to_local(f, wo);
@@ -659,7 +719,7 @@ __device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, fl
         if (wi_l.z <= 0.f) return col(0.f, 0.f, 0.f);
         wi = local_to_world(f, wi_l);
         pdf = vndf_pdf_aniso(wo_l, wh_l, f.alpha_x, f.alpha_y) / (4 * dot(wh_l, wo_l));
-        return bsdf_evaluate<FULL>(f, wo, wi);
+        return leaf_evaluate<FULL>(f, wo, wi);
     }
     const V3 wo_l = world_to_local(f, wo);
     const V3 wh = local_to_world(f, ggx_sample_vndf(u0, u1, wo_l, f.alpha, f.alpha));
@@ -673,9 +733,87 @@ __device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, fl
         if (!refract(wo, wh, f.eta_o / f.eta_i, wi)) return col(0.f, 0.f, 0.f);
         if (dot(wi, f.n) >= 0.f) return col(0.f, 0.f, 0.f);
     }
-    pdf = bsdf_pdf<FULL>(f, wo, wi);
+    pdf = leaf_pdf<FULL>(f, wo, wi);
     if (pdf == 0.f) return col(0.f, 0.f, 0.f);
-    return bsdf_evaluate<FULL>(f, wo, wi);
+    return leaf_evaluate<FULL>(f, wo, wi);
+}
+
+// Mix_BSDF (src/ref/bsdf.cpp:497-567) and Scaled_BSDF (:572-592) over leaf BSDFs;
+// every other BSDF forwards.  FULL = false compiles the mix out.
+__device__ __forceinline__ bool possible_for(const Bsdf& f, float n_dot_wi) {
+    return (n_dot_wi > 0.f && f.reflection) || (n_dot_wi < 0.f && f.transmission);
+}
+template <bool FULL = true>
+__device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
+    if (FULL && f.type == kScaled) {
+        Bsdf a = f;
+        set_material(a, *f.sub[0]);
+        return mul(leaf_evaluate<true>(a, wo, wi), f.mix_p);
+    }
+    if (FULL && f.type == kMix) {
+        Bsdf a = f, b = f;
+        set_material(a, *f.sub[0]);
+        set_material(b, *f.sub[1]);
+        Col f1 = col(0.f, 0.f, 0.f), f2 = col(0.f, 0.f, 0.f);
+        const float n_dot_wi = dot(f.n, wi);
+        if (possible_for(a, n_dot_wi)) f1 = leaf_evaluate<true>(a, wo, wi);
+        if (possible_for(b, n_dot_wi)) f2 = leaf_evaluate<true>(b, wo, wi);
+        return (col(1.f, 1.f, 1.f) - f.mix_coeff) * f1 + f.mix_coeff * f2;
+    }
+    return leaf_evaluate<FULL>(f, wo, wi);
+}
+template <bool FULL = true>
+__device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
+    if (FULL && f.type == kScaled) {
+        Bsdf a = f;
+        set_material(a, *f.sub[0]);
+        return leaf_pdf<true>(a, wo, wi);
+    }
+    if (FULL && f.type == kMix) {
+        Bsdf a = f, b = f;
+        set_material(a, *f.sub[0]);
+        set_material(b, *f.sub[1]);
+        float pdf1 = 0.f, pdf2 = 0.f;
+        const float n_dot_wi = dot(f.n, wi);
+        if (possible_for(a, n_dot_wi)) pdf1 = leaf_pdf<true>(a, wo, wi);
+        if (possible_for(b, n_dot_wi)) pdf2 = leaf_pdf<true>(b, wo, wi);
+        return (1.f - f.mix_p) * pdf1 + f.mix_p * pdf2;
+    }
+    return leaf_pdf<FULL>(f, wo, wi);
+}
+// wi must come in as the zero vector: the reference's default-constructed
+// direction, which a leaf sample that gives up early leaves as it is.
+template <bool FULL = true>
+__device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
+                                           float& pdf) {
+    if (FULL && f.type == kScaled) {
+        Bsdf a = f;
+        set_material(a, *f.sub[0]);
+        return mul(leaf_sample<true>(a, u0, u1, u_scatter, wo, wi, pdf), f.mix_p);
+    }
+    if (FULL && f.type == kMix) {
+        Bsdf a = f, b = f;
+        set_material(a, *f.sub[0]);
+        set_material(b, *f.sub[1]);
+        Col f1 = col(0.f, 0.f, 0.f), f2 = col(0.f, 0.f, 0.f);
+        float pdf1 = 0.f, pdf2 = 0.f;
+        if (u_scatter < f.mix_p) {
+            f2 = leaf_sample<true>(b, u0, u1, u_scatter / f.mix_p, wo, wi, pdf2);
+            if (possible_for(a, dot(f.n, wi))) {
+                pdf1 = leaf_pdf<true>(a, wo, wi);
+                f1 = leaf_evaluate<true>(a, wo, wi);
+            }
+        } else {
+            f1 = leaf_sample<true>(a, u0, u1, (u_scatter - f.mix_p) / (1.f - f.mix_p), wo, wi, pdf1);
+            if (possible_for(b, dot(f.n, wi))) {
+                pdf2 = leaf_pdf<true>(b, wo, wi);
+                f2 = leaf_evaluate<true>(b, wo, wi);
+            }
+        }
+        pdf = (1.f - f.mix_p) * pdf1 + f.mix_p * pdf2;
+        return (col(1.f, 1.f, 1.f) - f.mix_coeff) * f1 + f.mix_coeff * f2;
+    }
+    return leaf_sample<FULL>(f, u0, u1, u_scatter, wo, wi, pdf);
 }
 
 // mis_power_heuristic (src/ref/direct_lighting.cpp:18-24)

@@ -643,14 +643,17 @@ __device__ __forceinline__ V3 sphere_sampler_sample(const Sphere_Sampler& ss, fl
 // alpha q + (1 - alpha) p_bsdf, so the estimator stays unbiased; the light
 // sample and the MIS probe are unchanged.  With g.records set, every
 // continued vertex also leaves a training record.
-// FULL: delta materials, delta-light sampling, plastic and coated diffuse.  A
-// scene without them runs the FULL = false instantiation, which has none of
-// that code (launch_shade picks it from Render_Params::full_shading).
-// Launch bounds: at least 5 blocks of 128 threads per SM (96 registers).
-// Measured on GB300 (C3 render): 1.726 s against 1.732 s at 4 blocks
-// (128 registers) and 1.764 s without a bound (160 registers, 3 blocks).
+// FULL: delta materials, the layered, translucent and mixed BSDFs, and every
+// light kind but the quad light.  A scene without them runs the FULL = false
+// instantiation, which has none of that code (launch_shade picks it from
+// Render_Params::full_shading).
+// Launch bounds, FULL = false: at least 5 blocks of 128 threads per SM (96
+// registers).  Measured on GB300 (C3 render): 1.726 s against 1.732 s at 4
+// blocks (128 registers) and 1.764 s without a bound (160 registers, 3
+// blocks).  FULL = true: 3 blocks (168 registers); at 5 blocks its larger
+// state spilled about 2 KB per thread.
 template <bool GUIDED, bool FULL>
-__global__ void __launch_bounds__(kBlock, 5)
+__global__ void __launch_bounds__(kBlock, FULL ? 3 : 5)
 shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float* __restrict__ s1d,
              const float2* __restrict__ s2d, Path_State ps, Queues q, Guide_Shade g) {
     if (q.ext_count) count = *q.ext_count;
@@ -743,11 +746,11 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 Col delta_atten = col(1.f, 1.f, 1.f);
                 int delta = 0;
                 if (FULL && mat.delta != kDeltaNone)
-                    delta = delta_scattering(sc, mat, u_sc, delta_wi, delta_atten, bsdf_prob);
+                    delta = delta_scattering(sc, mat, S.materials, u_sc, delta_wi, delta_atten, bsdf_prob);
                 Bsdf f;
                 uint32_t pend = 0;
                 if (delta == 0 || bsdf_prob != 0.f) {
-                    make_bsdf(sc, mat, f);
+                    make_bsdf(sc, mat, S.materials, f);
                     // estimate_direct_lighting_from_single_sample (direct_lighting.cpp:522-578):
                     // the light int(u * total_light_count), point, spot and directional lights
                     // first, then the rectangular lights (the reference asserts the index is
@@ -838,7 +841,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                             }
                         }
                         {   // BSDF-sampling half of MIS: inside the light's cone, the probe must hit it
-                            V3 wi;
+                            V3 wi = v3(0.f, 0.f, 0.f);
                             float bpdf = 0.f;
                             const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_sc, sc.wo, wi, bpdf);
                             if (!black(fv) && dot(-ss.axes[2], wi) >= ss.cos_theta_max) {
@@ -886,7 +889,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                             }
                         }
                         {   // BSDF-sampling half of MIS: the probe ray must hit this light
-                            V3 wi;
+                            V3 wi = v3(0.f, 0.f, 0.f);
                             float bpdf = 0.f;
                             const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_sc, sc.wo, wi, bpdf);
                             if (!black(fv)) {
@@ -938,7 +941,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                             }
                         }
                         {   // BSDF-sampling half of MIS: the probe ray must hit this light
-                            V3 wi;
+                            V3 wi = v3(0.f, 0.f, 0.f);
                             float bpdf = 0.f;
                             const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_sc, sc.wo, wi, bpdf);
                             if (!black(fv)) {
@@ -980,7 +983,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                     float rec_value = 0.f;
                     V3 rec_dir = v3(0.f, 0.f, 0.f);
                     if (cont) {
-                        V3 wi;
+                        V3 wi = v3(0.f, 0.f, 0.f);
                         float pdf = 0.f;
                         Col fv;
                         if (GUIDED && g.lobes) {
@@ -1402,8 +1405,23 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
             m.type != YAR_MATERIAL_PLASTIC && m.type != YAR_MATERIAL_COATED_DIFFUSE &&
             m.type != YAR_MATERIAL_PERFECT_REFLECTOR && m.type != YAR_MATERIAL_PERFECT_REFRACTOR &&
             m.type != YAR_MATERIAL_DIFFUSE_TRANSMISSION && m.type != YAR_MATERIAL_PBRT3_TRANSLUCENT &&
-            m.type != YAR_MATERIAL_PBRT3_UBER)
+            m.type != YAR_MATERIAL_PBRT3_UBER && m.type != YAR_MATERIAL_MIX)
             return fail(ctx, YAR_ERR_UNSUPPORTED, "material type " + std::to_string(m.type) + " is not implemented");
+        if (m.type == YAR_MATERIAL_MIX) {
+            // one level: sub-materials that are pure delta or have no delta event, not both delta
+            int delta_subs = 0;
+            for (int k = 0; k < 2; k++) {
+                const int32_t si = m.mix_materials[k];
+                if (si < 0 || (size_t)si >= R.host_materials.size())
+                    return fail(ctx, YAR_ERR_INVALID, "mix material with an invalid sub-material");
+                const yar_material_desc& sm = R.host_materials[si];
+                if (sm.type == YAR_MATERIAL_MIX || sm.type == YAR_MATERIAL_PBRT3_UBER ||
+                    (sm.type == YAR_MATERIAL_GLASS && !(sm.u_roughness > 0.f)))
+                    return fail(ctx, YAR_ERR_UNSUPPORTED, "mix of a mix, an uber or a smooth glass material");
+                delta_subs += sm.type == YAR_MATERIAL_PERFECT_REFLECTOR || sm.type == YAR_MATERIAL_PERFECT_REFRACTOR;
+            }
+            if (delta_subs == 2) return fail(ctx, YAR_ERR_UNSUPPORTED, "mix of two pure delta materials");
+        }
         if (m.type == YAR_MATERIAL_PBRT3_UBER) {
             // the reference asserts on an empty component list and has no delta transmission
             bool ok = m.component_count >= 1 && m.component_count <= 5;

@@ -180,7 +180,7 @@ def _box(center, size, angle_deg):
 
 
 def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0, box_materials=None,
-                 upper_light=None, light_sources=(), mesh_lights=(), sphere_lights=()):
+                 upper_light=None, light_sources=(), mesh_lights=(), sphere_lights=(), named_materials=()):
     """pbrt-v3 text of the seeded Cornell box (34 triangles + a quad light).
 
     box_materials: None for matte boxes, or two pbrt material statements for
@@ -194,7 +194,8 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
     triangle meshes that are not rectangles (the reference makes them
     triangle-mesh lights).
     sphere_lights: (center, radius, radiance) emitting pbrt spheres (sphere
-    lights, shown by the reference's tessellated sphere)."""
+    lights, shown by the reference's tessellated sphere).
+    named_materials: pbrt MakeNamedMaterial statements (for "mix")."""
     rng = np.random.default_rng(seed)
     k = int(math.ceil(math.sqrt(spp)))
     shapes = []
@@ -225,7 +226,7 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
         'Integrator "path" "integer maxdepth" [%d]' % maxdepth,
         'PixelFilter "box"',
         "WorldBegin",
-    ] + list(light_sources)
+    ] + list(named_materials) + list(light_sources)
     for k, (v, i, albedo) in enumerate(shapes):
         material = 'Material "matte" "rgb Kd" [%s]' % fmt(albedo)
         if box_materials is not None and k >= 5:
@@ -279,6 +280,16 @@ UBER_BOXES = ('Material "uber" "rgb Kd" [0.5 0.3 0.2] "rgb Ks" [0.3 0.3 0.3] "rg
               '"float roughness" [0.15] "float index" [1.5]',
               'Material "uber" "rgb Kd" [0.2 0.4 0.5] "rgb Ks" [0.2 0.2 0.2] "rgb opacity" [0.6 0.7 0.8] '
               '"float uroughness" [0.1] "float vroughness" [0.3] "float index" [1.4]')
+
+
+MIX_NAMED = ('MakeNamedMaterial "red" "string type" "matte" "rgb Kd" [0.7 0.2 0.15]',
+             'MakeNamedMaterial "gold" "string type" "metal" "float roughness" [0.15] "rgb eta" [0.2 0.92 1.1] '
+             '"rgb k" [3.9 2.45 2.14]',
+             'MakeNamedMaterial "mirror" "string type" "mirror" "rgb Kr" [0.85 0.85 0.9]',
+             'MakeNamedMaterial "plastic" "string type" "plastic" "rgb Kd" [0.2 0.5 0.3] "rgb Ks" [0.3 0.3 0.3] '
+             '"float roughness" [0.1]')
+MIX_BOXES = ('Material "mix" "string namedmaterial1" "red" "string namedmaterial2" "gold" "rgb amount" [0.3 0.4 0.5]',
+             'Material "mix" "string namedmaterial1" "mirror" "string namedmaterial2" "plastic" "rgb amount" [0.4 0.4 0.4]')
 
 
 def make_diffuse_transmission(flat, obj=5, reflectance=(0.6, 0.5, 0.4), transmittance=(0.3, 0.4, 0.5),
