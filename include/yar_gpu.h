@@ -82,6 +82,7 @@ extern "C" {
 #define YAR_LIGHT_DIFFUSE_RECTANGULAR  3
 #define YAR_LIGHT_DIFFUSE_SPHERE       4
 #define YAR_LIGHT_DIFFUSE_TRIANGLE_MESH 5
+#define YAR_LIGHT_ENVIRONMENT_MAP      6
 #define YAR_LIGHT_NULL                 0xffffffffu
 
 /* Visibility (src/lib/triangle_mesh.h:7-11) */
@@ -211,6 +212,18 @@ typedef struct yar_mesh_light_desc {
     uint32_t triangle_mesh_index;  /* into yar_flat_scene::meshes */
 } yar_mesh_light_desc;
 
+/* Environment_Light (src/lib/light.h:88-94) with its latitude-longitude map as
+ * the reference sees it: the texture's mip 0 (a constant light is a 1 x 1 map).
+ * Sampled by Environment_Light_Sampler (src/ref/light_sampling.cpp:29-71). */
+typedef struct yar_environment_desc {
+    float light_to_world[12];
+    float world_to_light[12];
+    float scale[3];
+    int32_t sample_count;
+    uint32_t width, height;
+    const float* radiance;      /* width * height RGB triples, row 0 first */
+} yar_environment_desc;
+
 /* Camera, src/ref/camera.h:35-49 (fields as computed by Camera::Camera, camera.cpp:5-14) */
 typedef struct yar_camera_desc {
     float camera_to_world[12];
@@ -249,7 +262,7 @@ typedef struct yar_flat_scene {
     const yar_material_desc* materials;
     uint32_t rect_light_count;
     const yar_rect_light_desc* rect_lights;
-    /* lights of other kinds (environment): counted for total_light_count;
+    /* lights the library does not carry: counted for total_light_count;
        rendering with any of them is unsupported */
     uint32_t other_light_count;
     yar_camera_desc camera;
@@ -260,6 +273,7 @@ typedef struct yar_flat_scene {
     const yar_mesh_light_desc* mesh_lights;
     uint32_t sphere_light_count;    /* sphere lights */
     const yar_sphere_light_desc* sphere_lights;
+    const yar_environment_desc* environment;  /* NULL: no environment light */
 } yar_flat_scene;
 
 /* One ray of a batch: 32 bytes, two float4.  tmax plays the role of the

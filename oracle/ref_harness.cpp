@@ -376,9 +376,22 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         d.sample_count = l.sample_count;
         out.sphere_lights.push_back(d);
     }
+    if (ctx.lights.has_environment_light) {
+        const Environment_Light& l = ctx.lights.environment_light;
+        const Image& map = ctx.textures[l.environment_map_index].get_mips()[0];
+        out.has_environment = true;
+        matrix_to_floats(l.light_to_world, out.environment.light_to_world);
+        matrix_to_floats(l.world_to_light, out.environment.world_to_light);
+        memcpy(out.environment.scale, &l.scale.r, 12);
+        out.environment.sample_count = l.sample_count;
+        out.environment.width = (uint32_t)map.width;
+        out.environment.height = (uint32_t)map.height;
+        out.environment_radiance.resize(3 * map.data.size());
+        memcpy(out.environment_radiance.data(), map.data.data(), out.environment_radiance.size() * sizeof(float));
+    }
     out.other_light_count = (uint32_t)(ctx.lights.total_light_count - (int)ctx.lights.diffuse_rectangular_lights.size() -
                                        (int)out.delta_lights.size() - (int)out.mesh_lights.size() -
-                                       (int)out.sphere_lights.size());
+                                       (int)out.sphere_lights.size() - (out.has_environment ? 1 : 0));
 
     // Camera fields exactly as Camera::Camera computes them (src/ref/camera.cpp:5-14).
     const Matrix3x4& pose = scene.view_points[0];
@@ -663,6 +676,10 @@ int cmd_render_yfs(const Args& a) {
     yfs::Scene fs_scene;
     std::string err;
     if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
+    if (fs_scene.has_environment) {
+        fprintf(stderr, "render-yfs: environment lights are rendered from their pbrt scene only\n");
+        return 1;
+    }
     if (fs_scene.other_light_count) {
         fprintf(stderr, "only rectangular, point, spot, directional, triangle-mesh and sphere lights are supported\n");
         return 1;

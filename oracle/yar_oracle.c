@@ -818,6 +818,10 @@ static int make_bsdf(const yar_flat_scene* s, const shading_ctx* sc, bsdf_t* f, 
 static int g_correctly_rounded_trig = 0;
 static float sin_sample(float x) { return g_correctly_rounded_trig ? (float)sin((double)x) : sinf(x); }
 static float cos_sample(float x) { return g_correctly_rounded_trig ? (float)cos((double)x) : cosf(x); }
+static float atan2_sample(float y, float x) {
+    return g_correctly_rounded_trig ? (float)atan2((double)y, (double)x) : atan2f(y, x);
+}
+static float acos_sample(float x) { return g_correctly_rounded_trig ? (float)acos((double)x) : acosf(x); }
 
 static v3 sample_hemisphere_cosine(float u0, float u1) {
     float z = sqrtf(1.f - u0);
@@ -1646,6 +1650,200 @@ static col direct_sphere(const yar_flat_scene* s, const shading_ctx* sc, const b
     return out;
 }
 
+/* Environment_Light_Sampler (src/ref/light_sampling.cpp:11-71) over the map's
+ * mip 0, with Distribution_2D (src/ref/sampling.cpp:185-276) built by
+ * initialize_from_latitude_longitude_radiance_map (:236-259). */
+#define PI2_F 6.2831853f /* src/lib/math.h:10 */
+typedef struct env_sampler {
+    const yar_environment_desc* e;
+    int nx, ny;
+    float x_interval, y_interval;
+    float* marginal; /* ny */
+    float* cdfs;     /* nx * ny */
+} env_sampler;
+
+static col env_texel(const yar_environment_desc* e, int x, int y) { /* get_texel_clamp, image_texture.cpp:417-421 */
+    x = x < 0 ? 0 : ((int)e->width - 1 < x ? (int)e->width - 1 : x);
+    y = y < 0 ? 0 : ((int)e->height - 1 < y ? (int)e->height - 1 : y);
+    return ldc(e->radiance + 3 * ((size_t)y * e->width + x));
+}
+static col env_nearest(const yar_environment_desc* e, float u, float v) { /* sample_nearest, :423-439 */
+    return env_texel(e, (int)(u * (float)e->width), (int)(v * (float)e->height));
+}
+static col env_bilinear(const yar_environment_desc* e, float u, float v) { /* sample_bilinear, :441-480 */
+    float x = u * (float)e->width - 0.5f, y = v * (float)e->height - 0.5f;
+    float x_floor = floorf(x), y_floor = floorf(y);
+    float wx = x - x_floor, wy = y - y_floor;
+    int x0 = (int)x_floor, y0 = (int)y_floor, x1 = x0 + 1, y1 = y0 + 1;
+    col c = addc(addc(addc(mulcs(env_texel(e, x0, y0), (1 - wy) * (1 - wx)), mulcs(env_texel(e, x1, y0), (1 - wy) * wx)),
+                      mulcs(env_texel(e, x0, y1), wy * (1 - wx))),
+                 mulcs(env_texel(e, x1, y1), wy * wx));
+    return c;
+}
+static v3 xform_vec(const float m[12], v3 v) { /* transform_vector, src/lib/matrix.cpp:376-382 */
+    return mk3(m[0] * v.x + m[1] * v.y + m[2] * v.z, m[4] * v.x + m[5] * v.y + m[6] * v.z,
+               m[8] * v.x + m[9] * v.y + m[10] * v.z);
+}
+static void env_uv(v3 d, float* u, float* v) { /* get_uv_from_direction, light_sampling.cpp:15-25 */
+    float phi = atan2_sample(d.y, d.x);
+    phi = phi < 0 ? phi + PI2_F : phi;
+    float z = d.z < -1.f ? -1.f : (1.f < d.z ? 1.f : d.z);
+    float theta = acos_sample(z);
+    float a = phi * (1.f / PI2_F);
+    *u = a < 0.f ? 0.f : (ONE_MINUS_EPSILON < a ? ONE_MINUS_EPSILON : a);
+    float b = theta * PI_INV_F;
+    *v = b < ONE_MINUS_EPSILON ? b : ONE_MINUS_EPSILON;
+}
+static void free_env_sampler(env_sampler* es) {
+    free(es->marginal);
+    free(es->cdfs);
+}
+static int build_env_sampler(const yar_flat_scene* s, env_sampler* es) {
+    memset(es, 0, sizeof(*es));
+    const yar_environment_desc* e = s->environment;
+    if (!e) return YAR_OK;
+    if (!e->radiance || e->width == 0 || e->height == 0) return YAR_ERR_INVALID;
+    const int nx = (int)e->width, ny = (int)e->height;
+    es->e = e;
+    es->nx = nx;
+    es->ny = ny;
+    es->x_interval = 1.f / (float)nx;
+    es->y_interval = 1.f / (float)ny;
+    float* values = (float*)malloc(sizeof(float) * (size_t)nx * ny);
+    float* row_sums = (float*)malloc(sizeof(float) * (size_t)ny);
+    es->marginal = (float*)malloc(sizeof(float) * (size_t)ny);
+    es->cdfs = (float*)calloc((size_t)nx * ny, sizeof(float));
+    if (!values || !row_sums || !es->marginal || !es->cdfs) {
+        free(values);
+        free(row_sums);
+        free_env_sampler(es);
+        return YAR_ERR_CAPACITY;
+    }
+    for (int y = 0; y < ny; y++) {
+        float sin_theta = sinf((y + 0.5f) / (float)ny * PI_F);
+        float v = (y + 0.5f) / (float)ny;
+        for (int x = 0; x < nx; x++) {
+            float u = (x + 0.5f) / (float)nx;
+            values[(size_t)y * nx + x] = luminance(env_nearest(e, u, v)) * sin_theta;
+        }
+    }
+    float total = 0.f;
+    int last_nonzero = -1;
+    for (int y = 0; y < ny; y++) {
+        float row = 0.f;
+        for (int x = 0; x < nx; x++) row += values[(size_t)y * nx + x];
+        row_sums[y] = row;
+        total += row;
+        if (row != 0.f) last_nonzero = y;
+    }
+    int rc = YAR_OK;
+    if (last_nonzero < 0) {
+        rc = YAR_ERR_UNSUPPORTED; /* the reference asserts on an all-black map */
+    } else {
+        for (int y = 0; y < last_nonzero; y++) es->marginal[y] = (y == 0 ? 0.f : es->marginal[y - 1]) + row_sums[y] / total;
+        for (int y = last_nonzero; y < ny; y++) es->marginal[y] = 1.f;
+        for (int y = 0; y < ny; y++) {
+            float* cdf = es->cdfs + (size_t)y * nx;
+            if (row_sums[y] == 0.f) continue;
+            for (int x = 0; x < nx - 1; x++) cdf[x] = (x == 0 ? 0.f : cdf[x - 1]) + values[(size_t)y * nx + x] / row_sums[y];
+            cdf[nx - 1] = 1.f;
+        }
+    }
+    free(values);
+    free(row_sums);
+    if (rc != YAR_OK) free_env_sampler(es);
+    return rc;
+}
+/* sample_from_CDF (src/ref/sampling.cpp:98-147) returning the interval too */
+static float cdf_sample(const float* cdf, int n, float interval, float u, float* pdf, int* index) {
+    int k = 0;
+    while (k < n - 1 && cdf[k] < u) k++;
+    float a = k == 0 ? 0.f : cdf[k - 1], b = cdf[k];
+    float fraction = (u - a) / (b - a);
+    float x = ((float)k + fraction) * interval;
+    *pdf = (b - a) * (float)n;
+    *index = k;
+    return x < ONE_MINUS_EPSILON ? x : ONE_MINUS_EPSILON;
+}
+static float env_pdf_uv(const env_sampler* es, float u, float v) { /* Distribution_2D::pdf_uv, :278-291 */
+    int x = (int)(u * (float)es->nx), y = (int)(v * (float)es->ny);
+    float pdf_y = (es->marginal[y] - (y == 0 ? 0.f : es->marginal[y - 1])) * (float)es->ny;
+    const float* c = es->cdfs + (size_t)y * es->nx;
+    float pdf_x = (c[x] - (x == 0 ? 0.f : c[x - 1])) * (float)es->nx;
+    return pdf_y * pdf_x;
+}
+static col env_radiance(const env_sampler* es, v3 world_dir, int filtered) {
+    float u, v;
+    env_uv(xform_vec(es->e->world_to_light, world_dir), &u, &v);
+    col c = filtered ? env_bilinear(es->e, u, v) : env_nearest(es->e, u, v);
+    return mulc(c, ldc(es->e->scale));
+}
+static float env_light_pdf(const env_sampler* es, v3 world_dir) { /* Environment_Light_Sampler::pdf, :61-71 */
+    v3 d = xform_vec(es->e->world_to_light, world_dir);
+    float u, v;
+    env_uv(d, &u, &v);
+    float pdf_uv = env_pdf_uv(es, u, v);
+    float sin_theta = sqrtf(fmaxf_std(0.f, 1.f - d.z * d.z));
+    return pdf_uv / (2 * PI_F * PI_F * sin_theta);
+}
+static col env_light_sample(const env_sampler* es, float u0, float u1, v3* wi, float* pdf) { /* :29-49 */
+    float pdf_y, pdf_x;
+    int y, x;
+    float ky = cdf_sample(es->marginal, es->ny, es->y_interval, u0, &pdf_y, &y);
+    float kx = cdf_sample(es->cdfs + (size_t)y * es->nx, es->nx, es->x_interval, u1, &pdf_x, &x);
+    float pdf_uv = pdf_y * pdf_x;
+    float phi = kx * PI2_F, theta = ky * PI_F;
+    float sin_theta = sin_sample(theta);
+    *pdf = pdf_uv / (2 * PI_F * PI_F * sin_theta);
+    *wi = xform_vec(es->e->light_to_world, mk3(sin_theta * cos_sample(phi), sin_theta * sin_sample(phi), cos_sample(theta)));
+    return mulc(env_nearest(es->e, kx, ky), ldc(es->e->scale));
+}
+
+/* direct_lighting_from_environment_light, src/ref/direct_lighting.cpp:324-384 */
+static col direct_env(const yar_flat_scene* s, const shading_ctx* sc, const bsdf_t* f, const env_sampler* es,
+                      float ul0, float ul1, float ub0, float ub1, float u_scatter) {
+    col out = mkc(0, 0, 0);
+    int have = 0;
+    {
+        v3 wi;
+        float light_pdf;
+        col Le = env_light_sample(es, ul0, ul1, &wi, &light_pdf);
+        float ndw = dot3(sc->normal, wi);
+        int possible = (ndw > 0.f && f->reflection) || (ndw < 0.f && f->transmission);
+        if (possible) {
+            col fv = bsdf_evaluate(f, sc->wo, wi);
+            if (!blackc(fv)) {
+                v3 position = origin_for_direction(sc, wi);
+                if (!trace_any(s, position, wi, INFINITY)) {
+                    float bpdf = bsdf_pdf(f, sc->wo, wi);
+                    float w = mis_power(light_pdf, bpdf);
+                    out = addc(out, mulcs(mulc(Le, fv), w * fabsf(ndw) / light_pdf));
+                    have = 1;
+                }
+            }
+        }
+    }
+    {
+        v3 wi = mk3(0, 0, 0);
+        float bpdf;
+        col fv = bsdf_sample(f, ub0, ub1, u_scatter, sc->wo, &wi, &bpdf);
+        if (!blackc(fv)) {
+            col Le = env_radiance(es, wi, 0);
+            if (!blackc(Le)) {
+                v3 position = origin_for_direction(sc, wi);
+                if (!trace_any(s, position, wi, INFINITY)) {
+                    float light_pdf = env_light_pdf(es, wi);
+                    float w = mis_power(bpdf, light_pdf);
+                    col c = mulcs(mulc(Le, fv), w * fabsf(dot3(sc->normal, wi)) / bpdf);
+                    out = have ? addc(out, c) : addc(mkc(0, 0, 0), c);
+                    have = 1;
+                }
+            }
+        }
+    }
+    return out;
+}
+
 typedef struct sampler_view {
     const float* s1d;   /* this sample's 1d dims */
     const float* s2d;   /* this sample's 2d dims (pairs) */
@@ -1802,11 +2000,11 @@ static int emitted_radiance(const yar_flat_scene* s, const shading_ctx* sc, col*
 }
 
 /* trace_path, src/ref/path_tracing.cpp:11-133 */
-static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_samplers, v3 ro, v3 rd,
-                      sampler_view* sv, col* radiance) {
+static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_samplers, const env_sampler* env,
+                      v3 ro, v3 rd, sampler_view* sv, col* radiance) {
     const yar_render_config* cfg = &s->config;
     const int total_lights = (int)(s->delta_light_count + s->rect_light_count + s->sphere_light_count +
-                                   s->mesh_light_count + s->other_light_count);
+                                   s->mesh_light_count + (env->e ? 1 : 0) + s->other_light_count);
     col le;
     col coeff = mkc(1, 1, 1), L = mkc(0, 0, 0);
     int bounce = 0;
@@ -1821,6 +2019,7 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
             if (hit) init_shading(s, rd, h.object, h.prim, h.b, &sc);
             if (bounce == 0) {
                 if (hit && emitted_radiance(s, &sc, &le)) L = addc(L, mulc(coeff, le));
+                else if (!hit && env->e) L = addc(L, mulc(coeff, env_radiance(env, rd, 1)));
                 if (cfg->max_light_bounces == 0) break;
             }
             if (!hit || sc.light_type != YAR_LIGHT_NULL) break;
@@ -1848,16 +2047,19 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
             if (rc != YAR_OK) return rc;
             /* estimate_direct_lighting_from_single_sample, src/ref/direct_lighting.cpp:522-578 */
             int light_index = (int)(u_light_index * (float)total_lights);
-            /* point, spot, directional, rectangular, sphere, then triangle-mesh lights */
+            /* point, spot, directional, rectangular, sphere, triangle-mesh, then the environment light */
             const int rect_first = (int)s->delta_light_count, sphere_first = rect_first + (int)s->rect_light_count;
             const int mesh_first = sphere_first + (int)s->sphere_light_count;
+            const int env_first = mesh_first + (int)s->mesh_light_count;
             col one = light_index < rect_first ? direct_delta(s, &sc, &f, &s->delta_lights[light_index])
                       : light_index < sphere_first
                           ? direct_rect(s, &sc, &f, light_index - rect_first, ul0, ul1, ub0, ub1, u_scatter)
                       : light_index < mesh_first
                           ? direct_sphere(s, &sc, &f, light_index - sphere_first, ul0, ul1, ub0, ub1, u_scatter)
-                          : direct_mesh(s, &sc, &f, &mesh_samplers[light_index - mesh_first], light_index - mesh_first,
-                                        ul0, ul1, ub0, ub1, u_scatter);
+                      : light_index < env_first
+                          ? direct_mesh(s, &sc, &f, &mesh_samplers[light_index - mesh_first], light_index - mesh_first,
+                                        ul0, ul1, ub0, ub1, u_scatter)
+                          : direct_env(s, &sc, &f, env, ul0, ul1, ub0, ub1, u_scatter);
             col direct = mulcs(one, (float)total_lights);
             L = addc(L, mulc(coeff, direct));
         }
@@ -1880,6 +2082,7 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
             if (hit) init_shading(s, rd, h.object, h.prim, h.b, &sc);
             coeff = mulc(coeff, datten);
             if (hit && emitted_radiance(s, &sc, &le)) L = addc(L, mulc(coeff, le));
+            else if (!hit && env->e) L = addc(L, mulc(coeff, env_radiance(env, rd, 1)));
             bounce++;
             if (bounce == cfg->max_light_bounces) break;
             if (!hit || sc.light_type != YAR_LIGHT_NULL) break;
@@ -1915,6 +2118,7 @@ typedef struct render_job {
     double* tile_variance;
     int next_tile;
     mesh_light_sampler* mesh_samplers;
+    env_sampler env;
     pthread_mutex_t lock;
     int status;
 } render_job;
@@ -1994,7 +2198,7 @@ static int render_tile(render_job* J, int t) {
                 camera_ray(&s->camera, fx, fy, &o, &d);
                 sampler_view sv = {s1d + (size_t)k * n1d, s2d + 2 * (size_t)k * n2d, n1d, n2d, 0, 0, &rng};
                 col radiance;
-                rc = trace_path(s, J->mesh_samplers, o, d, &sv, &radiance);
+                rc = trace_path(s, J->mesh_samplers, &J->env, o, d, &sv, &radiance);
                 if (rc != YAR_OK) break;
                 float limit = cfg->max_rgb_component_value_of_film_sample;
                 float mc = fmaxf_std(radiance.r, fmaxf_std(radiance.g, radiance.b));
@@ -2117,6 +2321,10 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
     J.tile_bounds = (int*)calloc(4 * (size_t)nt, sizeof(int));
     J.tile_variance = (double*)calloc(nt, sizeof(double));
     int ms_rc = build_mesh_samplers(s, &J.mesh_samplers);
+    if (ms_rc == YAR_OK) {
+        ms_rc = build_env_sampler(s, &J.env);
+        if (ms_rc != YAR_OK) free_mesh_samplers(J.mesh_samplers, s->mesh_light_count);
+    }
     if (ms_rc != YAR_OK) {
         free(J.tile_pixels);
         free(J.tile_bounds);
@@ -2174,6 +2382,7 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
     free(J.tile_bounds);
     free(J.tile_variance);
     free_mesh_samplers(J.mesh_samplers, s->mesh_light_count);
+    free_env_sampler(&J.env);
     pthread_mutex_destroy(&J.lock);
     return rc;
 }

@@ -55,6 +55,11 @@ Fixtures
   cornell_mix_64.yfs / .npz  pbrt "mix" boxes: matte with metal (Mix_BSDF) and
                              mirror with plastic (a delta layer and a scaled
                              BSDF), seed 11.
+  cornell_envconst_64.yfs / .npz  the GGX Cornell box lit also by a constant
+                             pbrt "infinite" light through its open side, seed 12.
+  cornell_envmap_64.yfs / .npz  the delta-box Cornell box with an "infinite"
+                             light of a 64 x 32 sky map with a sun (written by
+                             yar_gb300.exr), seed 13.
 """
 import os
 import re
@@ -287,6 +292,24 @@ def cornell_mix_64():
     _pbrt_golden("cornell_mix_64", 11, box_materials=scenes.MIX_BOXES, named_materials=scenes.MIX_NAMED)
 
 
+def cornell_envconst_64():
+    _pbrt_golden("cornell_envconst_64", 12, box_materials=scenes.GGX_BOXES,
+                 light_sources=scenes.ENVIRONMENT_CONSTANT)
+
+
+def cornell_envmap_64():
+    from yar_gb300 import exr
+    with tempfile.TemporaryDirectory() as d:
+        exr.write_exr(os.path.join(d, "sky.exr"), scenes.environment_map(), False, {})
+        pbrt = os.path.join(d, "cornell_envmap.pbrt")
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=13, width=64, height=64, spp=16, maxdepth=8,
+                                                  box_materials=scenes.DELTA_BOXES,
+                                                  light_sources=scenes.environment_statements("sky.exr")))
+        oracle.ref_flatten(pbrt, os.path.join(HERE, "cornell_envmap_64.yfs"), seed_offset=1)
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_envmap_64.npz"), image=img, variance=np.float64(info["variance"]))
+
+
 def kdtree_cache_files():
     """The reference's kd-tree cache files (KdTree::save) of the raycast_small
     scene's first two meshes and of its scene tree."""
@@ -332,7 +355,7 @@ if __name__ == "__main__":
                              "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "cornell_layered_64",
                              "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64",
                              "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64",
-                             "cornell_uber_64", "cornell_mix_64",
+                             "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64",
                              "exr_files",
                              "kdtree_cache_files"]
     for name in which:

@@ -32,6 +32,11 @@ VARIANCE_REL_TOL = 1e-5
 # image variance by up to ~2e-4 and ~1e-4.
 LIGHTS_MEAN_REL_TOL = 3e-4
 LIGHTS_VARIANCE_REL_TOL = 1e-4
+# Environment maps: every lookup takes an atan2 and an acos, and glibc's
+# atan2f/acosf round differently from the correctly rounded value more often
+# than sinf/cosf do (89.3% bit-identical pixels on cornell_envmap_64; an oracle
+# run with correctly rounded trigonometry gives the same figure).
+ENV_BIT_EQUAL_MIN = 0.85
 
 
 def compare(img, ref):
@@ -42,7 +47,8 @@ def compare(img, ref):
 
 @pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64",
                                   "cornell_layered_64", "cornell_layered_yar_64", "cornell_lights_64",
-                                  "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64"])
+                                  "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
+                  "cornell_envmap_64"])
 def test_render_matches_reference_golden(gpu_ctx, name):
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
@@ -51,8 +57,8 @@ def test_render_matches_reference_golden(gpu_ctx, name):
     h = int(s.config["render_region"][3] - s.config["render_region"][1])
     img, stats = gpu_ctx.render(w, h)
     same, rel = compare(img, g["image"])
-    lights = s.delta_lights.shape[0] > 0
-    assert same >= BIT_EQUAL_MIN, (same, rel)
+    lights = s.delta_lights.shape[0] > 0 or s.environment is not None
+    assert same >= (ENV_BIT_EQUAL_MIN if s.environment is not None else BIT_EQUAL_MIN), (same, rel)
     assert rel < (LIGHTS_MEAN_REL_TOL if lights else MEAN_REL_TOL), (same, rel)
     vtol = LIGHTS_VARIANCE_REL_TOL if lights else VARIANCE_REL_TOL
     assert abs(stats.variance - float(g["variance"])) <= vtol * float(g["variance"])
@@ -62,7 +68,8 @@ def test_render_matches_reference_golden(gpu_ctx, name):
 
 RENDER_GOLDENS = ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "cornell_layered_64",
                   "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64", "cornell_spherelight_64",
-                  "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64"]
+                  "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
+                  "cornell_envmap_64"]
 
 
 @pytest.mark.parametrize("name", RENDER_GOLDENS)

@@ -170,11 +170,7 @@ cudaError_t enqueue_scene(Batch& bt, int si, bool one_spp, unsigned long long* s
     Render_Params p = sc.p;
     if (one_spp) p.nx = p.ny = p.spp = 1;
     yar_gpu_ctx* sub = sc.sub;
-    Scene_Dev S{sub->ds, dp<float4>(sub->render.shading), dp<float4>(sub->render.object_info),
-                dp<Material_Dev>(sub->render.materials), dp<Rect_Light_Dev>(sub->render.rect_lights),
-                dp<Delta_Light_Dev>(sub->render.delta_lights),
-                dp<Mesh_Light_Dev>(sub->render.mesh_lights), dp<float>(sub->render.mesh_cdf),
-                dp<Sphere_Light_Dev>(sub->render.sphere_lights)};
+    Scene_Dev S = scene_dev(sub->ds, sub->render);
     const uint64_t chunk_pixels = std::max<uint64_t>(1, std::min<uint64_t>(sc.pixels, br.cap / p.spp));
     Queues q = br.q;
     Path_State ps = br.ps;

@@ -30,6 +30,9 @@ struct Render_Scene {
     Device_Buffer mesh_lights;  // triangle-mesh lights (Mesh_Light_Dev[])
     Device_Buffer mesh_cdf;     // their triangle-area CDFs, concatenated
     Device_Buffer sphere_lights; // Sphere_Light_Dev[]
+    Device_Buffer env_map;       // environment map texels (float4 rgb), row 0 first
+    Device_Buffer env_marginal;  // its Distribution_2D: marginal CDF over rows
+    Device_Buffer env_cdfs;      // and the conditional CDFs, one row each
     Device_Buffer object_info;  // int4 per object: material type, material index, light type, light index
     Device_Buffer object_to_world;         // float[12] per object
     Device_Buffer object_to_world_normal;  // float[12] per object
@@ -38,6 +41,9 @@ struct Render_Scene {
     std::vector<yar_delta_light_desc> host_delta_lights;
     uint32_t mesh_light_count = 0;
     uint32_t sphere_light_count = 0;
+    bool has_environment = false;
+    yar_environment_desc environment{};  // radiance is not kept
+    bool has_no_shadow_meshes = false;
     std::vector<int32_t> host_object_info;
     yar_camera_desc camera{};
     yar_render_config config{};

@@ -204,11 +204,7 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
     q.prb_rays = dp<float4>(B[24]);
     q.prb_slot = dp<uint32_t>(B[25]);
     q.counters = dp<uint32_t>(B[26]);
-    Scene_Dev S{ctx->ds, dp<float4>(ctx->render.shading), dp<float4>(ctx->render.object_info),
-                dp<Material_Dev>(ctx->render.materials), dp<Rect_Light_Dev>(ctx->render.rect_lights),
-                dp<Delta_Light_Dev>(ctx->render.delta_lights),
-                dp<Mesh_Light_Dev>(ctx->render.mesh_lights), dp<float>(ctx->render.mesh_cdf),
-                dp<Sphere_Light_Dev>(ctx->render.sphere_lights)};
+    Scene_Dev S = scene_dev(ctx->ds, ctx->render);
     const float box[6] = {ctx->ds.scene_bounds[0], ctx->ds.scene_bounds[1], ctx->ds.scene_bounds[2],
                           ctx->ds.scene_bounds[3], ctx->ds.scene_bounds[4], ctx->ds.scene_bounds[5]};
 

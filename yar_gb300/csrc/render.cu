@@ -191,6 +191,57 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
         slights[i].le = make_float4(l.emitted_radiance[0], l.emitted_radiance[1], l.emitted_radiance[2], 0.f);
     }
     R.sphere_light_count = scene->sphere_light_count;
+    // Environment light: the map as float4 texels and its Distribution_2D, built as
+    // initialize_from_latitude_longitude_radiance_map does (src/ref/sampling.cpp:185-259).
+    R.has_environment = scene->environment != nullptr;
+    R.has_no_shadow_meshes = false;
+    for (uint32_t m = 0; m < scene->mesh_count; m++)
+        if (scene->meshes[m].visibility == YAR_VISIBLE_NO_SHADOWS) R.has_no_shadow_meshes = true;
+    std::vector<float4> env_map(1, make_float4(0.f, 0.f, 0.f, 0.f));
+    std::vector<float> env_marginal(1, 1.f), env_cdfs(1, 1.f);
+    if (R.has_environment) {
+        const yar_environment_desc& e = *scene->environment;
+        if (!e.radiance || e.width == 0 || e.height == 0)
+            return fail(ctx, YAR_ERR_INVALID, "environment light without a map");
+        R.environment = e;
+        R.environment.radiance = nullptr;
+        const int nx = (int)e.width, ny = (int)e.height;
+        env_map.assign((size_t)nx * ny, make_float4(0.f, 0.f, 0.f, 0.f));
+        for (size_t i = 0; i < env_map.size(); i++)
+            env_map[i] = make_float4(e.radiance[3 * i], e.radiance[3 * i + 1], e.radiance[3 * i + 2], 0.f);
+        auto nearest_lum = [&](float u, float v) {
+            int x = (int)(u * (float)nx), y = (int)(v * (float)ny);
+            x = x < 0 ? 0 : (nx - 1 < x ? nx - 1 : x);
+            y = y < 0 ? 0 : (ny - 1 < y ? ny - 1 : y);
+            const float4 t = env_map[(size_t)y * nx + x];
+            return 0.2126729f * t.x + 0.7151522f * t.y + 0.0721750f * t.z;
+        };
+        std::vector<float> values((size_t)nx * ny), row_sums(ny);
+        for (int y = 0; y < ny; y++) {
+            const float sin_theta = std::sin((y + 0.5f) / (float)ny * 3.14159265f);
+            const float v = (y + 0.5f) / (float)ny;
+            for (int x = 0; x < nx; x++) values[(size_t)y * nx + x] = nearest_lum((x + 0.5f) / (float)nx, v) * sin_theta;
+        }
+        float total = 0.f;
+        int last_nonzero = -1;
+        for (int y = 0; y < ny; y++) {
+            float row = 0.f;
+            for (int x = 0; x < nx; x++) row += values[(size_t)y * nx + x];
+            row_sums[y] = row;
+            total += row;
+            if (row != 0.f) last_nonzero = y;
+        }
+        if (last_nonzero < 0) return fail(ctx, YAR_ERR_UNSUPPORTED, "environment map is black");
+        env_marginal.assign(ny, 1.f);
+        for (int y = 0; y < last_nonzero; y++) env_marginal[y] = (y == 0 ? 0.f : env_marginal[y - 1]) + row_sums[y] / total;
+        env_cdfs.assign((size_t)nx * ny, 0.f);
+        for (int y = 0; y < ny; y++) {
+            float* cdf = env_cdfs.data() + (size_t)y * nx;
+            if (row_sums[y] == 0.f) continue;
+            for (int x = 0; x < nx - 1; x++) cdf[x] = (x == 0 ? 0.f : cdf[x - 1]) + values[(size_t)y * nx + x] / row_sums[y];
+            cdf[nx - 1] = 1.f;
+        }
+    }
     R.host_materials.assign(scene->materials, scene->materials + scene->material_count);
     R.host_rect_lights.assign(scene->rect_lights, scene->rect_lights + scene->rect_light_count);
     R.host_object_info.resize(4 * (size_t)scene->object_count);
@@ -216,6 +267,9 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
     if ((rc = up(R.mesh_lights, mlights.data(), mlights.size() * sizeof(Mesh_Light_Dev))) != YAR_OK) return rc;
     if ((rc = up(R.mesh_cdf, cdf.data(), cdf.size() * sizeof(float))) != YAR_OK) return rc;
     if ((rc = up(R.sphere_lights, slights.data(), slights.size() * sizeof(Sphere_Light_Dev))) != YAR_OK) return rc;
+    if ((rc = up(R.env_map, env_map.data(), env_map.size() * sizeof(float4))) != YAR_OK) return rc;
+    if ((rc = up(R.env_marginal, env_marginal.data(), env_marginal.size() * sizeof(float))) != YAR_OK) return rc;
+    if ((rc = up(R.env_cdfs, env_cdfs.data(), env_cdfs.size() * sizeof(float))) != YAR_OK) return rc;
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render upload");
     return YAR_OK;
@@ -224,7 +278,8 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
 void render_release(yar_gpu_ctx* ctx) {
     Render_Scene& R = ctx->render;
     for (Device_Buffer* b : {&R.shading, &R.materials, &R.rect_lights, &R.delta_lights, &R.mesh_lights, &R.mesh_cdf,
-                             &R.sphere_lights, &R.object_info, &R.object_to_world, &R.object_to_world_normal})
+                             &R.sphere_lights, &R.env_map, &R.env_marginal, &R.env_cdfs, &R.object_info,
+                             &R.object_to_world, &R.object_to_world_normal})
         device_free(*b);
     for (Device_Buffer& b : ctx->render_scratch) device_free(b);
     ctx->render_scratch.clear();
@@ -297,11 +352,7 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
     q.prb_rays = dptr<float4>(B[24]);
     q.prb_slot = dptr<uint32_t>(B[25]);
     q.counters = dptr<uint32_t>(B[26]);
-    Scene_Dev S{ctx->ds, dptr<float4>(ctx->render.shading), dptr<float4>(ctx->render.object_info),
-                dptr<Material_Dev>(ctx->render.materials), dptr<Rect_Light_Dev>(ctx->render.rect_lights),
-                dptr<Delta_Light_Dev>(ctx->render.delta_lights),
-                dptr<Mesh_Light_Dev>(ctx->render.mesh_lights), dptr<float>(ctx->render.mesh_cdf),
-                dptr<Sphere_Light_Dev>(ctx->render.sphere_lights)};
+    Scene_Dev S = scene_dev(ctx->ds, ctx->render);
     float4* radiance = dptr<float4>(B[0]);
     float2* image_samples = dptr<float2>(B[1]);
 
@@ -466,11 +517,7 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
     q.counters = counters;
     if (!s1d || !s2d || !ps.probe_hit2 || !q.prb_slot)
         return fail(ctx, YAR_ERR_CAPACITY, "static arena layout overflow");
-    Scene_Dev S{ctx->ds, dptr<float4>(ctx->render.shading), dptr<float4>(ctx->render.object_info),
-                dptr<Material_Dev>(ctx->render.materials), dptr<Rect_Light_Dev>(ctx->render.rect_lights),
-                dptr<Delta_Light_Dev>(ctx->render.delta_lights),
-                dptr<Mesh_Light_Dev>(ctx->render.mesh_lights), dptr<float>(ctx->render.mesh_cdf),
-                dptr<Sphere_Light_Dev>(ctx->render.sphere_lights)};
+    Scene_Dev S = scene_dev(ctx->ds, ctx->render);
 
     cudaStream_t st = ctx->stream;
     cudaError_t e = cudaMemsetAsync(q.counters, 0, 8 * sizeof(uint32_t), st);  // the arena keeps the last call's data

@@ -49,7 +49,7 @@ constexpr uint64_t kChunkSampleBudget = 16u << 20;  // paths in flight per chunk
 // refractor, smooth glass) and its hit is shaded as the reference's delta
 // branch does; kDeltaFinal: that delta vertex used the last bounce.
 // What the MIS probe of a vertex must hit: pend_probe2.z
-enum : uint32_t { kProbeRectLight = 0, kProbeMeshLight = 1, kProbeSphereLight = 2 };
+enum : uint32_t { kProbeRectLight = 0, kProbeMeshLight = 1, kProbeSphereLight = 2, kProbeEnvLight = 3 };
 
 enum : uint32_t {
     kPendShadow = 1u << 24,
@@ -97,7 +97,7 @@ struct Render_Params {
     float rr_threshold;
     float filter_radius;
     float film_scale, max_component;
-    int32_t total_lights, delta_lights, rect_lights, sphere_lights, mesh_lights;  // in the selection order
+    int32_t total_lights, delta_lights, rect_lights, sphere_lights, mesh_lights, env_lights;  // selection order
     int32_t full_shading;  // the scene needs shade_kernel<*, true>
     uint32_t seed_offset;
     uint32_t stream_hi;  // upper 32 bits of the pixel streams' sequence (0 = the reference's streams)
@@ -192,7 +192,42 @@ struct Scene_Dev {
     const Mesh_Light_Dev* mesh_lights;
     const float* mesh_cdf;
     const Sphere_Light_Dev* sphere_lights;
+    // environment light (env_map null: none)
+    const float4* env_map;
+    const float* env_marginal;
+    const float* env_cdfs;
+    float4 env_l2w[3], env_w2l[3];
+    float4 env_scale;  // rgb, -
+    int32_t env_nx, env_ny;
 };
+
+// The device view of an uploaded scene.
+inline Scene_Dev scene_dev(const Device_Scene& ds, const Render_Scene& R) {
+    Scene_Dev S{};
+    S.ds = ds;
+    S.shading = reinterpret_cast<const float4*>(R.shading.ptr);
+    S.obj_render = reinterpret_cast<const float4*>(R.object_info.ptr);
+    S.materials = reinterpret_cast<const Material_Dev*>(R.materials.ptr);
+    S.lights = reinterpret_cast<const Rect_Light_Dev*>(R.rect_lights.ptr);
+    S.delta_lights = reinterpret_cast<const Delta_Light_Dev*>(R.delta_lights.ptr);
+    S.mesh_lights = reinterpret_cast<const Mesh_Light_Dev*>(R.mesh_lights.ptr);
+    S.mesh_cdf = reinterpret_cast<const float*>(R.mesh_cdf.ptr);
+    S.sphere_lights = reinterpret_cast<const Sphere_Light_Dev*>(R.sphere_lights.ptr);
+    S.env_map = R.has_environment ? reinterpret_cast<const float4*>(R.env_map.ptr) : nullptr;
+    S.env_marginal = reinterpret_cast<const float*>(R.env_marginal.ptr);
+    S.env_cdfs = reinterpret_cast<const float*>(R.env_cdfs.ptr);
+    const yar_environment_desc& e = R.environment;
+    for (int r = 0; r < 3; r++) {
+        S.env_l2w[r] = make_float4(e.light_to_world[4 * r], e.light_to_world[4 * r + 1], e.light_to_world[4 * r + 2],
+                                   e.light_to_world[4 * r + 3]);
+        S.env_w2l[r] = make_float4(e.world_to_light[4 * r], e.world_to_light[4 * r + 1], e.world_to_light[4 * r + 2],
+                                   e.world_to_light[4 * r + 3]);
+    }
+    S.env_scale = make_float4(e.scale[0], e.scale[1], e.scale[2], 0.f);
+    S.env_nx = (int32_t)e.width;
+    S.env_ny = (int32_t)e.height;
+    return S;
+}
 
 // Warp-aggregated queue append: one atomic per warp and predicate value.
 __device__ __forceinline__ uint32_t warp_append(uint32_t* counter, bool pred) {
@@ -602,6 +637,83 @@ __device__ __forceinline__ V3 mesh_light_sample(const Scene_Dev& S, uint4 info, 
     return light_p;
 }
 
+// ---------------------------------------------------------------- environment light
+// Environment_Light_Sampler (light_sampling.cpp:11-71) and Distribution_2D
+// (sampling.cpp:185-291) over the map's mip 0.  atan2 and acos are rounded
+// correctly (evaluated in double), like the sines and cosines.
+__device__ __forceinline__ Col env_texel(const Scene_Dev& S, int x, int y) {  // get_texel_clamp
+    x = x < 0 ? 0 : (S.env_nx - 1 < x ? S.env_nx - 1 : x);
+    y = y < 0 ? 0 : (S.env_ny - 1 < y ? S.env_ny - 1 : y);
+    const float4 t = __ldg(S.env_map + (size_t)y * S.env_nx + x);
+    return col(t.x, t.y, t.z);
+}
+__device__ __forceinline__ Col env_nearest(const Scene_Dev& S, float u, float v) {
+    return env_texel(S, (int)(u * (float)S.env_nx), (int)(v * (float)S.env_ny));
+}
+__device__ __forceinline__ Col env_bilinear(const Scene_Dev& S, float u, float v) {
+    const float x = u * (float)S.env_nx - 0.5f, y = v * (float)S.env_ny - 0.5f;
+    const float x_floor = floorf(x), y_floor = floorf(y);
+    const float wx = x - x_floor, wy = y - y_floor;
+    const int x0 = (int)x_floor, y0 = (int)y_floor, x1 = x0 + 1, y1 = y0 + 1;
+    return ((mul(env_texel(S, x0, y0), (1 - wy) * (1 - wx)) + mul(env_texel(S, x1, y0), (1 - wy) * wx)) +
+            mul(env_texel(S, x0, y1), wy * (1 - wx))) +
+           mul(env_texel(S, x1, y1), wy * wx);
+}
+__device__ __forceinline__ void env_uv(V3 d, float& u, float& v) {  // get_uv_from_direction
+    const float pi2 = 6.2831853f;  // src/lib/math.h:10
+    float phi = (float)atan2((double)d.y, (double)d.x);
+    phi = phi < 0 ? phi + pi2 : phi;
+    const float z = d.z < -1.f ? -1.f : (1.f < d.z ? 1.f : d.z);
+    const float theta = (float)acos((double)z);
+    const float a = phi * (1.f / pi2);
+    u = a < 0.f ? 0.f : one_minus_eps_min(a);
+    v = one_minus_eps_min(theta * (1.f / kPi));
+}
+__device__ __forceinline__ Col env_radiance(const Scene_Dev& S, V3 world_dir, bool filtered) {
+    float u, v;
+    env_uv(xform_vector(S.env_w2l[0], S.env_w2l[1], S.env_w2l[2], world_dir), u, v);
+    const Col c = filtered ? env_bilinear(S, u, v) : env_nearest(S, u, v);
+    return c * col(S.env_scale.x, S.env_scale.y, S.env_scale.z);
+}
+__device__ __forceinline__ float env_light_pdf(const Scene_Dev& S, V3 world_dir) {
+    const V3 d = xform_vector(S.env_w2l[0], S.env_w2l[1], S.env_w2l[2], world_dir);
+    float u, v;
+    env_uv(d, u, v);
+    const int x = (int)(u * (float)S.env_nx), y = (int)(v * (float)S.env_ny);
+    const float pdf_y = (__ldg(S.env_marginal + y) - (y == 0 ? 0.f : __ldg(S.env_marginal + y - 1))) * (float)S.env_ny;
+    const float* c = S.env_cdfs + (size_t)y * S.env_nx;
+    const float pdf_x = (__ldg(c + x) - (x == 0 ? 0.f : __ldg(c + x - 1))) * (float)S.env_nx;
+    const float sin_theta = sqrtf(max_std(0.f, 1.f - d.z * d.z));
+    return (pdf_y * pdf_x) / (2 * kPi * kPi * sin_theta);
+}
+// sample_from_CDF (sampling.cpp:98-147): the sample, its pdf and interval
+__device__ __forceinline__ float cdf_sample(const float* cdf, int n, float u, float& pdf, int& index) {
+    int lo = 0, hi = n;  // std::lower_bound
+    while (lo < hi) {
+        const int mid = (lo + hi) >> 1;
+        if (__ldg(cdf + mid) < u) lo = mid + 1;
+        else hi = mid;
+    }
+    const int k = lo < n ? lo : n - 1;
+    const float a = k == 0 ? 0.f : __ldg(cdf + k - 1), b = __ldg(cdf + k);
+    const float fraction = (u - a) / (b - a);
+    pdf = (b - a) * (float)n;
+    index = k;
+    return one_minus_eps_min(((float)k + fraction) * (1.f / (float)n));
+}
+__device__ __forceinline__ Col env_light_sample(const Scene_Dev& S, float u0, float u1, V3& wi, float& pdf) {
+    float pdf_y, pdf_x;
+    int y, x;
+    const float ky = cdf_sample(S.env_marginal, S.env_ny, u0, pdf_y, y);
+    const float kx = cdf_sample(S.env_cdfs + (size_t)y * S.env_nx, S.env_nx, u1, pdf_x, x);
+    const float phi = kx * 6.2831853f, theta = ky * kPi;
+    const float sin_theta = sin_f(theta);
+    pdf = (pdf_y * pdf_x) / (2 * kPi * kPi * sin_theta);
+    wi = xform_vector(S.env_l2w[0], S.env_l2w[1], S.env_l2w[2],
+                      v3(sin_theta * cos_f(phi), sin_theta * sin_f(phi), cos_f(theta)));
+    return env_nearest(S, kx, ky) * col(S.env_scale.x, S.env_scale.y, S.env_scale.z);
+}
+
 // ---------------------------------------------------------------- sphere lights
 // Diffuse_Sphere_Light_Sampler (light_sampling.cpp:76-123): the cone the
 // sphere subtends from the shading point, sampled uniformly in solid angle.
@@ -694,6 +806,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 } else if (FULL && is_light && (uint32_t)oinfo.z == YAR_LIGHT_DIFFUSE_SPHERE) {
                     const float4 le = __ldg(&S.sphere_lights[oinfo.w].le);
                     L = L + coeff * col(le.x, le.y, le.z);
+                } else if (FULL && !hit && S.env_map) {  // a miss sees the environment, filtered
+                    L = L + coeff * env_radiance(S, v3(rb.x, rb.y, rb.z), true);
                 }
                 if (arrival ? (info & kDeltaFinal) != 0 : p.max_bounces == 0) done = true;
             }
@@ -855,6 +969,49 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                 pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
                                 pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
                                 pend |= kPendProbe;
+                            }
+                        }
+                    } else if (FULL && selected >= p.total_lights - p.env_lights) {
+                        // direct_lighting_from_environment_light (direct_lighting.cpp:324-384): the
+                        // light sample is a shadow ray to infinity, the BSDF sample's probe must miss
+                        {
+                            V3 wi;
+                            float light_pdf;
+                            const Col Le = env_light_sample(S, ul.x, ul.y, wi, light_pdf);
+                            const float ndw = dot(sc.n, wi);
+                            if ((ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission)) {
+                                const Col fv = bsdf_evaluate<FULL>(f, sc.wo, wi);
+                                if (!black(fv)) {
+                                    const V3 position = origin_for_direction(sc, wi);
+                                    const float bpdf = bsdf_pdf<FULL>(f, sc.wo, wi);
+                                    const float w = mis_power(light_pdf, bpdf);
+                                    const Col c = mul(Le * fv, w * fabsf(ndw) / light_pdf);
+                                    ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
+                                    want_shadow = true;
+                                    sh_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
+                                    sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                    pend |= kPendShadow;
+                                }
+                            }
+                        }
+                        {
+                            V3 wi = v3(0.f, 0.f, 0.f);
+                            float bpdf = 0.f;
+                            const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_sc, sc.wo, wi, bpdf);
+                            if (!black(fv)) {
+                                const Col Le = env_radiance(S, wi, false);
+                                if (!black(Le)) {
+                                    const V3 position = origin_for_direction(sc, wi);
+                                    const Col lef = Le * fv;
+                                    ps.pend_probe0[slot] = make_float4(lef.r, lef.g, lef.b, bpdf);
+                                    ps.pend_probe1[slot] = make_float4(wi.x, wi.y, wi.z, env_light_pdf(S, wi));
+                                    ps.pend_probe2[slot] = make_float4(dot(sc.n, wi), 0.f,
+                                                                       __uint_as_float(kProbeEnvLight), 0.f);
+                                    want_probe = true;
+                                    pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
+                                    pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                    pend |= kPendProbe;
+                                }
                             }
                         }
                     } else if (FULL && selected >= p.delta_lights + p.rect_lights + p.sphere_lights) {
@@ -1110,7 +1267,12 @@ connect_kernel(Render_Params p, Scene_Dev S, const uint32_t* __restrict__ slots,
             const float4 p2 = ps.pend_probe2[slot];
             const int light_index = __float_as_int(p2.y);
             const uint32_t kind = __float_as_uint(p2.z);
-            if (h2.y != 0xffffffffu) {
+            if (kind == kProbeEnvLight && h2.y == 0xffffffffu) {
+                const float4 p0 = ps.pend_probe0[slot], p1 = ps.pend_probe1[slot];
+                const float w = mis_power(p0.w, p1.w);
+                direct = direct + mul(col(p0.x, p0.y, p0.z), w * fabsf(p2.x) / p0.w);
+            }
+            if (kind != kProbeEnvLight && h2.y != 0xffffffffu) {
                 const float4 inf4 = __ldg(S.obj_render + 7 * (size_t)h2.y + 6);
                 const uint32_t hit_light = (uint32_t)__float_as_int(inf4.z);
                 if (kind == kProbeSphereLight && hit_light == YAR_LIGHT_DIFFUSE_SPHERE &&
@@ -1391,9 +1553,11 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     if (c.rendering_algorithm != 1) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the path tracer is implemented");
     if (c.pixel_filter_type != 0) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the box filter is implemented");
     if (R.other_light_count)
-        return fail(ctx, YAR_ERR_UNSUPPORTED, "environment lights are not implemented");
+        return fail(ctx, YAR_ERR_UNSUPPORTED, "the scene has lights of a kind that is not implemented");
+    if (R.has_environment && R.has_no_shadow_meshes)
+        return fail(ctx, YAR_ERR_UNSUPPORTED, "environment light with meshes that cast no shadows");
     if (R.host_rect_lights.empty() && R.host_delta_lights.empty() && R.mesh_light_count == 0 &&
-        R.sphere_light_count == 0)
+        R.sphere_light_count == 0 && !R.has_environment)
         return fail(ctx, YAR_ERR_UNSUPPORTED, "scene has no light");
     for (size_t i = 0; i < R.host_delta_lights.size(); i++) {
         const uint32_t t = R.host_delta_lights[i].type;
@@ -1484,8 +1648,10 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     p.delta_lights = (int)R.host_delta_lights.size();
     p.mesh_lights = (int)R.mesh_light_count;
     p.sphere_lights = (int)R.sphere_light_count;
-    p.total_lights = p.delta_lights + p.rect_lights + p.sphere_lights + p.mesh_lights + (int)R.other_light_count;
-    p.full_shading = p.delta_lights > 0 || p.mesh_lights > 0 || p.sphere_lights > 0;
+    p.env_lights = R.has_environment ? 1 : 0;
+    p.total_lights = p.delta_lights + p.rect_lights + p.sphere_lights + p.mesh_lights + p.env_lights +
+                     (int)R.other_light_count;
+    p.full_shading = p.delta_lights > 0 || p.mesh_lights > 0 || p.sphere_lights > 0 || p.env_lights > 0;
     for (const yar_material_desc& m : R.host_materials)
         if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL &&
             !(m.type == YAR_MATERIAL_GLASS && m.u_roughness > 0.f))

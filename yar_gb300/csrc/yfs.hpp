@@ -3,8 +3,8 @@
 // The file carries exactly what the device path consumes: meshes with their
 // kd-trees (node words bit for bit as KdTree::save writes them,
 // src/ref/kdtree.cpp:137-160), scene objects, the scene kd-tree, constant
-// materials, rectangular lights, point/spot/directional, triangle-mesh and
-// sphere lights (optional chunks), camera and Raytracer_Config.  It is produced
+// materials, rectangular lights, point/spot/directional, triangle-mesh,
+// sphere and environment lights (optional chunks), camera and Raytracer_Config.  It is produced
 // by the host scene loader of this library and by the reference-side adapter
 // that flattens a reference Scene_Context, so both sides can be compared on
 // identical bytes.
@@ -46,6 +46,9 @@ struct Scene {
     std::vector<yar_delta_light_desc> delta_lights;
     std::vector<yar_mesh_light_desc> mesh_lights;
     std::vector<yar_sphere_light_desc> sphere_lights;
+    bool has_environment = false;
+    yar_environment_desc environment{};   // radiance points into environment_radiance
+    std::vector<float> environment_radiance;
     uint32_t other_light_count = 0;
     yar_camera_desc camera{};
     yar_render_config config{};
@@ -92,6 +95,8 @@ struct Scene {
         s.mesh_lights = mesh_lights.empty() ? nullptr : mesh_lights.data();
         s.sphere_light_count = (uint32_t)sphere_lights.size();
         s.sphere_lights = sphere_lights.empty() ? nullptr : sphere_lights.data();
+        environment.radiance = environment_radiance.data();
+        s.environment = has_environment ? &environment : nullptr;
         return s;
     }
 };
@@ -211,6 +216,14 @@ inline bool write(const std::string& path, const Scene& s) {
         b.raw(s.sphere_lights.data(), n * sizeof(yar_sphere_light_desc));
         w.chunk("SPHL", b.b);
     }
+    if (s.has_environment) {
+        detail::Buf b;
+        yar_environment_desc e = s.environment;
+        e.radiance = nullptr;
+        b.pod(e);
+        b.raw(s.environment_radiance.data(), s.environment_radiance.size() * sizeof(float));
+        w.chunk("ENVM", b.b);
+    }
     bool ok = w.ok;
     if (fclose(f) != 0) ok = false;
     return ok;
@@ -309,6 +322,14 @@ inline bool read(const std::string& path, Scene& s, std::string* err = nullptr) 
             if ((uint64_t)n * sizeof(yar_sphere_light_desc) > size) return fail("bad sphere light chunk");
             s.sphere_lights.resize(n);
             c.raw(s.sphere_lights.data(), n * sizeof(yar_sphere_light_desc));
+        } else if (!memcmp(tag, "ENVM", 4)) {
+            s.environment = c.pod<yar_environment_desc>();
+            const uint64_t count = 3ull * s.environment.width * s.environment.height;
+            if (!c.ok || count * sizeof(float) > size) return fail("bad environment chunk");
+            s.environment_radiance.resize(count);
+            c.raw(s.environment_radiance.data(), count * sizeof(float));
+            s.environment.radiance = nullptr;
+            s.has_environment = true;
         }
         if (!c.ok) return fail("truncated chunk payload");
     }

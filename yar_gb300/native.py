@@ -112,6 +112,12 @@ class SphereLightDesc(C.Structure):
                 ("sample_count", C.c_int32)]
 
 
+class EnvironmentDesc(C.Structure):
+    _fields_ = [("light_to_world", C.c_float * 12), ("world_to_light", C.c_float * 12), ("scale", C.c_float * 3),
+                ("sample_count", C.c_int32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("radiance", C.c_void_p)]
+
+
 class FlatSceneDesc(C.Structure):
     _fields_ = [("mesh_count", C.c_uint32), ("meshes", C.POINTER(MeshDesc)),
                 ("object_count", C.c_uint32), ("objects", C.POINTER(ObjectDesc)),
@@ -121,7 +127,8 @@ class FlatSceneDesc(C.Structure):
                 ("other_light_count", C.c_uint32), ("camera", CameraDesc), ("config", RenderConfig),
                 ("delta_light_count", C.c_uint32), ("delta_lights", C.POINTER(DeltaLightDesc)),
                 ("mesh_light_count", C.c_uint32), ("mesh_lights", C.POINTER(MeshLightDesc)),
-                ("sphere_light_count", C.c_uint32), ("sphere_lights", C.POINTER(SphereLightDesc))]
+                ("sphere_light_count", C.c_uint32), ("sphere_lights", C.POINTER(SphereLightDesc)),
+                ("environment", C.POINTER(EnvironmentDesc))]
 
 
 class HitSoa(C.Structure):

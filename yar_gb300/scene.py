@@ -32,6 +32,8 @@ MESH_LIGHT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("emitted_radiance",
                              ("triangle_mesh_index", "<u4")])
 SPHERE_LIGHT_DTYPE = np.dtype([("position", "<f4", 3), ("emitted_radiance", "<f4", 3), ("radius", "<f4"),
                                ("sample_count", "<i4")])
+ENVIRONMENT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("world_to_light", "<f4", 12), ("scale", "<f4", 3),
+                              ("sample_count", "<i4"), ("width", "<u4"), ("height", "<u4"), ("radiance", "<u8")])
 CAMERA_DTYPE = np.dtype([("camera_to_world", "<f4", 12), ("image_extent", "<f4", 2), ("horz_half_dist", "<f4"),
                          ("vert_half_dist", "<f4"), ("z_is_up", "<i4")])
 CONFIG_DTYPE = np.dtype([("render_region", "<i4", 4), ("rendering_algorithm", "<i4"), ("max_light_bounces", "<i4"),
@@ -47,6 +49,7 @@ assert MATERIAL_DTYPE.itemsize == C.sizeof(native.MaterialDesc)
 assert LIGHT_DTYPE.itemsize == C.sizeof(native.RectLightDesc)
 assert DELTA_LIGHT_DTYPE.itemsize == C.sizeof(native.DeltaLightDesc)
 assert MESH_LIGHT_DTYPE.itemsize == C.sizeof(native.MeshLightDesc)
+assert ENVIRONMENT_DTYPE.itemsize == C.sizeof(native.EnvironmentDesc)
 assert SPHERE_LIGHT_DTYPE.itemsize == C.sizeof(native.SphereLightDesc)
 assert CAMERA_DTYPE.itemsize == C.sizeof(native.CameraDesc)
 assert CONFIG_DTYPE.itemsize == C.sizeof(native.RenderConfig)
@@ -102,6 +105,8 @@ class FlatScene:
         self.delta_lights = np.zeros(0, DELTA_LIGHT_DTYPE)
         self.mesh_lights = np.zeros(0, MESH_LIGHT_DTYPE)  # triangle-mesh lights
         self.sphere_lights = np.zeros(0, SPHERE_LIGHT_DTYPE)
+        # environment light: None, or (ENVIRONMENT_DTYPE record, (height, width, 3) float32 map)
+        self.environment = None
         self.other_light_count = 0
         self.camera = np.zeros((), CAMERA_DTYPE)
         self.config = default_config()
@@ -202,6 +207,18 @@ class FlatScene:
         s.mesh_lights = C.cast(mlights.ctypes.data, C.POINTER(native.MeshLightDesc)) if mlights.size else None
         s.sphere_light_count = slights.shape[0]
         s.sphere_lights = C.cast(slights.ctypes.data, C.POINTER(native.SphereLightDesc)) if slights.size else None
+        if self.environment is not None:
+            rec, img = self.environment
+            img = np.ascontiguousarray(img, np.float32)
+            env = native.EnvironmentDesc()
+            env.light_to_world[:] = [float(x) for x in rec["light_to_world"]]
+            env.world_to_light[:] = [float(x) for x in rec["world_to_light"]]
+            env.scale[:] = [float(x) for x in rec["scale"]]
+            env.sample_count = int(rec["sample_count"])
+            env.height, env.width = img.shape[0], img.shape[1]
+            env.radiance = img.ctypes.data
+            keep += [img, env]
+            s.environment = C.pointer(env)
         C.memmove(C.byref(s.camera), np.ascontiguousarray(self.camera).ctypes.data, CAMERA_DTYPE.itemsize)
         C.memmove(C.byref(s.config), np.ascontiguousarray(self.config).ctypes.data, CONFIG_DTYPE.itemsize)
         return s, keep
@@ -238,6 +255,12 @@ class FlatScene:
             parts.append(chunk(b"MLIT", struct.pack("<I", self.mesh_lights.shape[0]) + self.mesh_lights.tobytes()))
         if self.sphere_lights.shape[0]:
             parts.append(chunk(b"SPHL", struct.pack("<I", self.sphere_lights.shape[0]) + self.sphere_lights.tobytes()))
+        if self.environment is not None:
+            rec, img = self.environment
+            r = np.array(rec, ENVIRONMENT_DTYPE).copy()
+            r["height"], r["width"] = img.shape[0], img.shape[1]
+            r["radiance"] = 0
+            parts.append(chunk(b"ENVM", r.tobytes() + np.ascontiguousarray(img, np.float32).tobytes()))
         with open(path, "wb") as f:
             f.write(b"".join(parts))
 
@@ -302,6 +325,12 @@ class FlatScene:
             elif tag == b"MLIT":
                 n = struct.unpack_from("<I", p, 0)[0]
                 s.mesh_lights = np.frombuffer(p[4:4 + n * MESH_LIGHT_DTYPE.itemsize], MESH_LIGHT_DTYPE).copy()
+            elif tag == b"ENVM":
+                rec = np.frombuffer(p[:ENVIRONMENT_DTYPE.itemsize], ENVIRONMENT_DTYPE)[0].copy()
+                w, h = int(rec["width"]), int(rec["height"])
+                img = np.frombuffer(p[ENVIRONMENT_DTYPE.itemsize:ENVIRONMENT_DTYPE.itemsize + 12 * w * h],
+                                    np.float32).reshape(h, w, 3).copy()
+                s.environment = (np.array(rec, ENVIRONMENT_DTYPE), img)
             elif tag == b"SPHL":
                 n = struct.unpack_from("<I", p, 0)[0]
                 s.sphere_lights = np.frombuffer(p[4:4 + n * SPHERE_LIGHT_DTYPE.itemsize], SPHERE_LIGHT_DTYPE).copy()

@@ -292,6 +292,32 @@ MIX_BOXES = ('Material "mix" "string namedmaterial1" "red" "string namedmaterial
              'Material "mix" "string namedmaterial1" "mirror" "string namedmaterial2" "plastic" "rgb amount" [0.4 0.4 0.4]')
 
 
+ENVIRONMENT_CONSTANT = ('LightSource "infinite" "rgb L" [0.5 0.55 0.6]',)
+
+
+def environment_map(width=64, height=32, seed=1):
+    """A latitude-longitude sky: a vertical gradient, seeded noise and a small
+    bright sun, as float32 (height, width, 3)."""
+    rng = np.random.default_rng(seed)
+    v = (np.arange(height, dtype=np.float32) + 0.5) / height
+    u = (np.arange(width, dtype=np.float32) + 0.5) / width
+    sky = np.stack([0.3 + 0.5 * (1 - v), 0.4 + 0.5 * (1 - v), 0.6 + 0.6 * (1 - v)], axis=-1)[:, None, :]
+    img = np.broadcast_to(sky, (height, width, 3)).copy()
+    img *= (0.8 + 0.4 * rng.random((height, width, 1))).astype(np.float32)
+    du = np.minimum(np.abs(u[None, :] - 0.3), 1 - np.abs(u[None, :] - 0.3))
+    sun = np.exp(-((du / 0.03) ** 2 + ((v[:, None] - 0.35) / 0.05) ** 2))
+    img += (40.0 * sun)[..., None] * np.array([1.0, 0.9, 0.7], np.float32)
+    return img.astype(np.float32)
+
+
+def environment_statements(mapname, scale=(1, 1, 1)):
+    """pbrt statements of an infinite light with the given map, turned so that
+    the map's pole points along +y."""
+    return ("AttributeBegin", "  Rotate -90 1 0 0",
+            '  LightSource "infinite" "string mapname" "%s" "rgb L" [%g %g %g]' % ((mapname,) + tuple(scale)),
+            "AttributeEnd")
+
+
 def make_diffuse_transmission(flat, obj=5, reflectance=(0.6, 0.5, 0.4), transmittance=(0.3, 0.4, 0.5),
                               scale=(1.2, 1.0, 0.9)):
     """Turns object `obj`'s material (object 5 is cornell_pbrt's short box)
