@@ -360,6 +360,19 @@ int yar_gpu_cast_any_timed(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t ray_c
  * stats may be NULL. */
 int yar_gpu_render(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats);
 
+/* render_scene with Scene_Context::checkpoint_directory set
+ * (src/ref/reference_renderer.cpp:180-324, :446-584): the directory holds the
+ * reference's checkpoint files, so a render may be resumed by either renderer.
+ * An empty or missing directory starts a checkpoint; otherwise its metadata
+ * must name the same input_filename (the reference stores Scene::path), tile
+ * count and samples per pixel, and its finished tiles are loaded instead of
+ * rendered.  The others are rendered one row of tiles at a time, each tile
+ * written (temporary file, then rename) as its row completes.  stats->seconds
+ * includes the time of earlier sessions.  YAR_ERR_IO for a checkpoint that
+ * does not match or a file that cannot be read or written. */
+int yar_gpu_render_checkpoint(yar_gpu_ctx* ctx, const char* checkpoint_directory, const char* input_filename,
+                              float* rgb_out, yar_render_stats* stats);
+
 /* ---- render without allocation ----
  * No counterpart in the reference.  yar_gpu_render allocates its working
  * memory (path state, ray queues, per-sample film data) with cudaMalloc on

@@ -136,7 +136,7 @@ def ref_flatten(pbrt_path, yfs_path, spp=0, seed_offset=0):
     return _ref(*args)
 
 
-def ref_render(pbrt_path, spp=0, seed_offset=0, threads=0):
+def ref_render(pbrt_path, spp=0, seed_offset=0, threads=0, checkpoint_dir=None):
     with tempfile.TemporaryDirectory() as d:
         out = os.path.join(d, "img.bin")
         args = ["render", pbrt_path, out, "--threads=%d" % (threads or os.cpu_count() or 1)]
@@ -144,6 +144,8 @@ def ref_render(pbrt_path, spp=0, seed_offset=0, threads=0):
             args.append("--spp=%d" % spp)
         if seed_offset:
             args.append("--seedoffset=%d" % seed_offset)
+        if checkpoint_dir:
+            args.append("--checkpoint-dir=%s" % checkpoint_dir)
         info = _ref(*args)
         raw = open(out, "rb").read()
     w, h = np.frombuffer(raw[:8], np.uint32)

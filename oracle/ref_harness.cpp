@@ -66,6 +66,7 @@ struct Args {
     float variance = 0.f;
     std::string input_file;
     std::string cache_dir;
+    std::string checkpoint_dir;
 };
 
 Args parse(int argc, char** argv) {
@@ -77,6 +78,7 @@ Args parse(int argc, char** argv) {
         else if (s.rfind("--threads=", 0) == 0) a.threads = atoi(s.c_str() + 10);
         else if (s.rfind("--repeat=", 0) == 0) a.repeat = atoi(s.c_str() + 9);
         else if (s == "--any") a.any = true;
+        else if (s.rfind("--checkpoint-dir=", 0) == 0) a.checkpoint_dir = s.substr(17);
         else if (s == "--compress") a.compress = true;
         else if (s.rfind("--variance=", 0) == 0) a.variance = (float)atof(s.c_str() + 11);
         else if (s.rfind("--input=", 0) == 0) a.input_file = s.substr(8);
@@ -133,6 +135,7 @@ void init_context(Scene_Context& ctx, const Scene& scene, const Args& a) {
     config.thread_count = a.threads;
     config.rebuild_kdtree_cache = true;
     config.rng_seed_offset = a.seed_offset;
+    config.checkpoint_directory = a.checkpoint_dir;
     init_scene_context(ctx, scene, config);
     std::error_code ec;
     fs::remove_all(data_dir, ec);

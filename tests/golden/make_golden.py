@@ -60,6 +60,11 @@ Fixtures
   cornell_envmap_64.yfs / .npz  the delta-box Cornell box with an "infinite"
                              light of a 64 x 32 sky map with a sun (written by
                              yar_gb300.exr), seed 13.
+  checkpoint_c1/             the reference's checkpoint directory (metadata and
+                             four tile files) of a 72 x 72, 4 spp Cornell box
+                             render (seed 14) with input file name
+                             "cornell_checkpoint.pbrt"; checkpoint_c1.yfs / .npz
+                             are that scene and the reference's image.
 """
 import os
 import re
@@ -310,6 +315,27 @@ def cornell_envmap_64():
     np.savez_compressed(os.path.join(HERE, "cornell_envmap_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def checkpoint_c1():
+    """The reference's own checkpoint files: render_scene with a checkpoint directory."""
+    import shutil
+    import subprocess
+    out_dir = os.path.join(HERE, "checkpoint_c1")
+    shutil.rmtree(out_dir, ignore_errors=True)
+    with tempfile.TemporaryDirectory() as d:
+        name = "cornell_checkpoint.pbrt"
+        open(os.path.join(d, name), "w").write(scenes.cornell_pbrt(seed=14, width=72, height=72, spp=4, maxdepth=6))
+        oracle.ref_flatten(os.path.join(d, name), os.path.join(HERE, "checkpoint_c1.yfs"), seed_offset=1)
+        raw = os.path.join(d, "img.bin")
+        subprocess.run([oracle.REF_BIN, "render", name, raw, "--threads=4", "--seedoffset=1", "--checkpoint-dir=ckpt"],
+                       cwd=d, check=True, stdout=subprocess.DEVNULL)
+        shutil.copytree(os.path.join(d, "ckpt"), out_dir)
+        data = open(raw, "rb").read()
+    w, h = np.frombuffer(data[:8], np.uint32)
+    variance = float(np.frombuffer(data[8:16], np.float64)[0])
+    img = np.frombuffer(data[20:], np.float32).reshape(int(h), int(w), 3).copy()
+    np.savez_compressed(os.path.join(HERE, "checkpoint_c1.npz"), image=img, variance=np.float64(variance))
+
+
 def kdtree_cache_files():
     """The reference's kd-tree cache files (KdTree::save) of the raycast_small
     scene's first two meshes and of its scene tree."""
@@ -356,6 +382,7 @@ if __name__ == "__main__":
                              "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64",
                              "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64",
                              "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64",
+                             "checkpoint_c1",
                              "exr_files",
                              "kdtree_cache_files"]
     for name in which:

@@ -3,6 +3,9 @@
 // yar_gpu_render_static; the kernels are in wavefront.cuh.
 #include "wavefront.cuh"
 
+#include <filesystem>
+#include <fstream>
+#include <map>
 #include <mutex>
 
 namespace yar {
@@ -285,11 +288,28 @@ void render_release(yar_gpu_ctx* ctx) {
     ctx->render_scratch.clear();
 }
 
+// Per-tile film data of a render (checkpoint bands): each tile's variance
+// accumulator and its Film_Pixel array (color sum, weight) over its pixel bounds.
+struct Tile_Output {
+    std::vector<double> tile_variance;
+    std::vector<uint32_t> offset;  // per tile, into pixels
+    std::vector<float4> pixels;
+};
+
+int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p, float* rgb_out, yar_render_stats* stats,
+                      Tile_Output* tiles_out);
+
 int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
     if (!rgb_out) return fail(ctx, YAR_ERR_INVALID, "null image buffer");
     Render_Params p;
     if (int rc0 = prepare_render_params(ctx, p)) return rc0;
+    return render_run_params(ctx, p, rgb_out, stats, nullptr);
+}
 
+// The render of render_run over the sample region of p.  With tiles_out, the
+// image is not resolved: the tiles' film data come back instead.
+int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p, float* rgb_out, yar_render_stats* stats,
+                      Tile_Output* tiles_out) {
     cudaSetDevice(ctx->device);
     const auto t_start = std::chrono::steady_clock::now();
     const uint64_t pixels = (uint64_t)p.sw * p.sh;
@@ -394,18 +414,58 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
         samples_kernel<<<(uint32_t)((pixels + kBlock - 1) / kBlock), kBlock, 0, st>>>(p, radiance, dptr<double>(B[27]));
         tile_variance_kernel<<<p.tiles_x * p.tiles_y, kTileVarThreads, 0, st>>>(p, dptr<double>(B[27]),
                                                                                 dptr<double>(B[28]));
-        film_kernel<<<(uint32_t)(((uint64_t)p.rw * p.rh + kBlock - 1) / kBlock), kBlock, 0, st>>>(
-            p, radiance, image_samples, dptr<float>(B[29]));
-        launches += 3;
+        launches += 2;
+        if (!tiles_out) {
+            film_kernel<<<(uint32_t)(((uint64_t)p.rw * p.rh + kBlock - 1) / kBlock), kBlock, 0, st>>>(
+                p, radiance, image_samples, dptr<float>(B[29]));
+            launches++;
+        }
         e = cudaGetLastError();
     }
     std::vector<double> tile_var((size_t)p.tiles_x * p.tiles_y);
-    if (e == cudaSuccess)
+    if (e == cudaSuccess && tiles_out) {
+        // per-tile Film_Pixel arrays: offsets from the tiles' pixel bounds (Film::get_tile_bounds)
+        const int n_tiles = p.tiles_x * p.tiles_y;
+        tiles_out->offset.assign(n_tiles + 1, 0);
+        uint32_t max_area = 0;
+        for (int t = 0; t < n_tiles; t++) {
+            int b[4];
+            host_tile_pixel_bounds(p, t, b);
+            const uint32_t area = (uint32_t)std::max(0, b[2] - b[0]) * (uint32_t)std::max(0, b[3] - b[1]);
+            tiles_out->offset[t + 1] = tiles_out->offset[t] + area;
+            max_area = std::max(max_area, area);
+        }
+        Device_Buffer offs, pix;
+        int rc2 = device_alloc(ctx, offs, tiles_out->offset.size() * sizeof(uint32_t));
+        if (rc2 == YAR_OK) rc2 = device_alloc(ctx, pix, std::max<size_t>(1, tiles_out->offset[n_tiles]) * sizeof(float4));
+        if (rc2 != YAR_OK) {
+            device_free(offs);
+            device_free(pix);
+            return rc2;
+        }
+        tiles_out->pixels.resize(tiles_out->offset[n_tiles]);
+        e = cudaMemcpyAsync(offs.ptr, tiles_out->offset.data(), tiles_out->offset.size() * sizeof(uint32_t),
+                            cudaMemcpyHostToDevice, st);
+        if (e == cudaSuccess && max_area > 0) {
+            tile_film_kernel<<<dim3((max_area + kBlock - 1) / kBlock, (unsigned)n_tiles), kBlock, 0, st>>>(
+                p, radiance, image_samples, dptr<uint32_t>(offs), dptr<float4>(pix));
+            launches++;
+            e = cudaGetLastError();
+        }
+        if (e == cudaSuccess && !tiles_out->pixels.empty())
+            e = cudaMemcpyAsync(tiles_out->pixels.data(), pix.ptr, tiles_out->pixels.size() * sizeof(float4),
+                                cudaMemcpyDeviceToHost, st);
+        if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+        device_free(offs);
+        device_free(pix);
+    }
+    if (e == cudaSuccess && !tiles_out)
         e = cudaMemcpyAsync(rgb_out, B[29].ptr, (size_t)p.rw * p.rh * 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(tile_var.data(), B[28].ptr, tile_var.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render");
+    if (tiles_out) tiles_out->tile_variance = tile_var;
     const double seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     if (stats) {
         double acc = 0.0;
@@ -576,7 +636,211 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
     return YAR_OK;
 }
 
+// ---------------------------------------------------------------- checkpointed render
+// render_scene with a checkpoint directory (src/ref/reference_renderer.cpp:180-324,
+// :446-476, :479-584), in the reference's file format: a "checkpoint" metadata
+// file (input file name, tile count, samples per pixel) and one "tile_NNNN" file
+// per finished tile: render time (float), variance accumulator (double), pixel
+// bounds (4 x int32), Film_Pixel[area] (color sum rgb, weight sum).  Tiles
+// already in the directory are loaded; the others are rendered one row of tiles
+// at a time and written as soon as their row is done (a temporary file renamed
+// into place); the image merges all tiles in index order, as Film::merge_tile
+// and Film::get_image do.
+namespace {
+namespace fs = std::filesystem;
+
+std::string format_tile_index(int tile_index) {  // reference_renderer.cpp:153-158
+    std::string s = std::to_string(tile_index);
+    s.insert(0, s.length() <= 4 ? 4 - s.length() : 0, '0');
+    return s;
+}
+
+struct Checkpoint_Tile {
+    bool present = false;
+    double variance = 0.0;
+    int bounds[4] = {0, 0, 0, 0};
+    std::vector<float4> pixels;  // color sum rgb, weight sum
+};
+
+bool write_tile_file(const fs::path& dir, int tile_index, float time, const Checkpoint_Tile& t, std::string& err) {
+    const fs::path temp = dir / ("temp_tile_" + format_tile_index(tile_index));
+    const fs::path final_path = dir / ("tile_" + format_tile_index(tile_index));
+    {
+        std::ofstream f(temp, std::ofstream::out | std::ofstream::binary);
+        if (!f) {
+            err = "failed to create file: " + temp.string();
+            return false;
+        }
+        f.write(reinterpret_cast<const char*>(&time), sizeof(float));
+        f.write(reinterpret_cast<const char*>(&t.variance), sizeof(double));
+        f.write(reinterpret_cast<const char*>(t.bounds), 4 * sizeof(int32_t));
+        f.write(reinterpret_cast<const char*>(t.pixels.data()), (std::streamsize)(t.pixels.size() * sizeof(float4)));
+        if (!f) {
+            err = "failed to write to file: " + temp.string();
+            return false;
+        }
+    }
+    std::error_code ec;
+    if (fs::exists(final_path, ec)) {
+        err = "tile file already exists: " + final_path.string();
+        return false;
+    }
+    fs::rename(temp, final_path, ec);
+    if (ec) {
+        err = "failed to rename temp file to: " + final_path.string();
+        return false;
+    }
+    return true;
+}
+
+// start_or_resume_checkpoint: creates the directory and its metadata, or checks
+// the metadata and loads the finished tiles.  Returns an empty string or the error.
+std::string start_or_resume(const fs::path& dir, const std::string& input_filename, int tile_count, int spp,
+                            std::vector<Checkpoint_Tile>& tiles, float* previous_time) {
+    std::error_code ec;
+    const fs::path meta = dir / "checkpoint";
+    *previous_time = 0.f;
+    if (!fs::exists(dir, ec) && !fs::create_directories(dir, ec))
+        return "failed to create checkpoint directory: " + dir.string();
+    if (fs::is_empty(dir, ec)) {
+        std::ofstream f(meta, std::ofstream::out);
+        if (!f) return "failed to create checkpoint file: " + meta.string();
+        f << "input_filename " << input_filename << "\n";
+        f << "total_tile_count " << tile_count << "\n";
+        f << "samples_per_pixer " << spp << "\n";  // the reference's spelling
+        return "";
+    }
+    if (!fs::exists(meta, ec)) return dir.string() + " is not a checkpoint directory: 'checkpoint' file is missing";
+    std::ifstream f(meta);
+    std::string tag, stored_name, stored_tiles, stored_spp;
+    f >> tag >> stored_name >> tag >> stored_tiles >> tag >> stored_spp;
+    if (!f) return "failed to read all the required fields from the metadata file: " + meta.string();
+    if (stored_name != input_filename) return "can not resume rendering because input_filename is changed";
+    if (stored_tiles != std::to_string(tile_count))
+        return "can not resume rendering because total_tile_count is changed";
+    if (stored_spp != std::to_string(spp)) return "can not resume rendering because samples_per_pixer is changed";
+    for (const fs::directory_entry& entry : fs::directory_iterator(dir, ec)) {
+        const std::string name = entry.path().stem().string();
+        if (name.rfind("tile_", 0) != 0) continue;
+        char* end = nullptr;
+        const long index = std::strtol(name.c_str() + 5, &end, 10);
+        if (!end || *end != '\0' || index < 0 || index >= tile_count) return "unexpected tile file: " + name;
+        std::ifstream tf(entry.path(), std::ifstream::in | std::ifstream::binary);
+        std::vector<char> content((std::istreambuf_iterator<char>(tf)), std::istreambuf_iterator<char>());
+        Checkpoint_Tile& t = tiles[index];
+        float time = 0.f;
+        if (content.size() < 28) return "truncated tile file: " + name;
+        memcpy(&time, content.data(), 4);
+        memcpy(&t.variance, content.data() + 4, 8);
+        memcpy(t.bounds, content.data() + 12, 16);
+        const int64_t area = (int64_t)std::max(0, t.bounds[2] - t.bounds[0]) * std::max(0, t.bounds[3] - t.bounds[1]);
+        if ((int64_t)content.size() != 28 + 16 * area) return "tile file of the wrong size: " + name;
+        t.pixels.resize((size_t)area);
+        memcpy(t.pixels.data(), content.data() + 28, (size_t)area * 16);
+        t.present = true;
+        *previous_time = std::max(*previous_time, time);
+    }
+    return "";
+}
+
+} // namespace
+
+int render_checkpoint(yar_gpu_ctx* ctx, const char* directory, const char* input_filename, float* rgb_out,
+                      yar_render_stats* stats) {
+    if (!rgb_out || !directory || !input_filename) return fail(ctx, YAR_ERR_INVALID, "null argument");
+    Render_Params p;
+    if (int rc0 = prepare_render_params(ctx, p)) return rc0;
+    const auto t_start = std::chrono::steady_clock::now();
+    const int tile_count = p.tiles_x * p.tiles_y;
+    std::vector<Checkpoint_Tile> tiles(tile_count);
+    float previous_time = 0.f;
+    const std::string err = start_or_resume(fs::path(directory), input_filename, tile_count, p.spp, tiles,
+                                            &previous_time);
+    if (!err.empty()) return fail(ctx, YAR_ERR_IO, "checkpoint: " + err);
+    yar_render_stats total{};
+    for (int ty = 0; ty < p.tiles_y; ty++) {
+        bool needed = false;
+        for (int tx = 0; tx < p.tiles_x; tx++) needed = needed || !tiles[ty * p.tiles_x + tx].present;
+        if (!needed) continue;
+        // one row of tiles: the render over its sample rows
+        Render_Params band = p;
+        band.sy0 = p.sy0 + ty * kTile;
+        band.sh = std::min(kTile, p.sh - ty * kTile);
+        band.tiles_y = 1;
+        Tile_Output out;
+        yar_render_stats bs{};
+        int rc = render_run_params(ctx, band, nullptr, &bs, &out);
+        if (rc != YAR_OK) return rc;
+        total.paths += bs.paths;
+        total.rays_closest += bs.rays_closest;
+        total.rays_any += bs.rays_any;
+        total.kernel_launches += bs.kernel_launches;
+        const float now = previous_time +
+                          (float)std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+        for (int tx = 0; tx < p.tiles_x; tx++) {
+            Checkpoint_Tile& t = tiles[ty * p.tiles_x + tx];
+            if (t.present) continue;
+            host_tile_pixel_bounds(p, ty * p.tiles_x + tx, t.bounds);
+            t.variance = out.tile_variance[tx];
+            t.pixels.assign(out.pixels.begin() + out.offset[tx], out.pixels.begin() + out.offset[tx + 1]);
+            t.present = true;
+            std::string werr;
+            if (!write_tile_file(fs::path(directory), ty * p.tiles_x + tx, now, t, werr))
+                return fail(ctx, YAR_ERR_IO, "checkpoint: " + werr);
+        }
+    }
+    // Film::merge_tile in tile order, then Film::get_image (box filter)
+    std::vector<float4> film((size_t)p.rw * p.rh, make_float4(0.f, 0.f, 0.f, 0.f));
+    for (int t = 0; t < tile_count; t++) {
+        const Checkpoint_Tile& tile = tiles[t];
+        const int w = tile.bounds[2] - tile.bounds[0];
+        for (int y = tile.bounds[1]; y < tile.bounds[3]; y++)
+            for (int x = tile.bounds[0]; x < tile.bounds[2]; x++) {
+                const float4 c = tile.pixels[(size_t)(y - tile.bounds[1]) * w + (x - tile.bounds[0])];
+                float4& f = film[(size_t)(y - p.ry0) * p.rw + (x - p.rx0)];
+                f.x += c.x;
+                f.y += c.y;
+                f.z += c.z;
+                f.w += c.w;
+            }
+    }
+    for (size_t i = 0; i < film.size(); i++) {
+        const float4 f = film[i];
+        float cr = 0.f, cg = 0.f, cb = 0.f;
+        if (f.w != 0.f) {
+            const float inv = 1.f / f.w;
+            cr = f.x * inv;
+            cg = f.y * inv;
+            cb = f.z * inv;
+        }
+        rgb_out[3 * i + 0] = std::max(0.f, cr);
+        rgb_out[3 * i + 1] = std::max(0.f, cg);
+        rgb_out[3 * i + 2] = std::max(0.f, cb);
+    }
+    if (stats) {
+        double acc = 0.0;
+        int64_t count = 0;
+        for (int t = 0; t < tile_count; t++) {
+            acc += tiles[t].variance;
+            const int tx = t % p.tiles_x, ty = t / p.tiles_x;
+            count += (int64_t)std::min(kTile, p.sw - tx * kTile) * std::min(kTile, p.sh - ty * kTile);
+        }
+        *stats = total;
+        stats->variance = p.spp > 1 ? acc / (double)count : 0.0;
+        stats->seconds = previous_time +
+                         (float)std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
+    }
+    return YAR_OK;
+}
+
 } // namespace yar
+
+extern "C" int yar_gpu_render_checkpoint(yar_gpu_ctx* ctx, const char* checkpoint_directory,
+                                         const char* input_filename, float* rgb_out, yar_render_stats* stats) {
+    if (!ctx) return YAR_ERR_INVALID;
+    if (!ctx->has_scene) return yar::fail(ctx, YAR_ERR_NO_SCENE, "no scene uploaded");
+    return yar::render_checkpoint(ctx, checkpoint_directory, input_filename, rgb_out, stats);
+}
 
 extern "C" int yar_gpu_render_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats* stats) {
     if (!ctx) return YAR_ERR_INVALID;

@@ -1456,6 +1456,41 @@ cudaError_t launch_generate(const Render_Params& p, uint32_t first, uint32_t cp,
     return cudaGetLastError();
 }
 
+// Film_Tile t's sum for film pixel (px, py): the samples of the tile's sample
+// region whose box-filter footprint covers the pixel, in the tile's own sample
+// order (Film_Tile::add_sample, src/ref/film.cpp:27-50), as (color sum, weight).
+__device__ __forceinline__ float4 tile_pixel_sum(const Render_Params& p, const float4* __restrict__ radiance,
+                                                 const float2* __restrict__ image_samples, int t, int px, int py) {
+    const float r = p.filter_radius;
+    const int R = (int)ceilf(r) + 1;
+    const int qx0 = max(px - R, p.sx0), qx1 = min(px + R, p.sx0 + p.sw - 1);
+    const int qy0 = max(py - R, p.sy0), qy1 = min(py + R, p.sy0 + p.sh - 1);
+    int bx0, by0, bx1, by1;
+    tile_pixel_bounds(p, t, bx0, by0, bx1, by1);
+    int sx0, sy0, sx1, sy1;
+    tile_sample_bounds(p, t, sx0, sy0, sx1, sy1);
+    float tr = 0.f, tg = 0.f, tb = 0.f, tw = 0.f;
+    for (int qy = max(qy0, sy0); qy <= min(qy1, sy1 - 1); qy++)
+        for (int qx = max(qx0, sx0); qx <= min(qx1, sx1 - 1); qx++) {
+            const size_t pix = (size_t)(qy - p.sy0) * p.sw + (qx - p.sx0);
+            for (int k = 0; k < p.spp; k++) {
+                const float2 s = image_samples[pix * p.spp + k];
+                const float fx = (float)qx + s.x, fy = (float)qy + s.y;
+                int rx0 = (int)ceilf(fx - r - 0.5f), ry0 = (int)ceilf(fy - r - 0.5f);
+                int rx1 = (int)floorf(fx + r - 0.5f) + 1, ry1 = (int)floorf(fy + r - 0.5f) + 1;
+                rx0 = max(rx0, bx0); ry0 = max(ry0, by0);
+                rx1 = min(rx1, bx1); ry1 = min(ry1, by1);
+                if (px < rx0 || px >= rx1 || py < ry0 || py >= ry1) continue;
+                const float4 c = radiance[pix * p.spp + k];
+                tr += 1.f * c.x;
+                tg += 1.f * c.y;
+                tb += 1.f * c.z;
+                tw += 1.f;
+            }
+        }
+    return make_float4(tr, tg, tb, tw);
+}
+
 // One film pixel: the tiles whose samples reach it are merged in tile order
 // (Film::merge_tile), each tile's sum accumulated in its own sample order
 // (Film_Tile::add_sample with the box filter), then resolved (Film::get_image).
@@ -1480,31 +1515,11 @@ film_kernel(Render_Params p, const float4* __restrict__ radiance, const float2* 
             int bx0, by0, bx1, by1;
             tile_pixel_bounds(p, t, bx0, by0, bx1, by1);
             if (px < bx0 || px >= bx1 || py < by0 || py >= by1) continue;
-            int sx0, sy0, sx1, sy1;
-            tile_sample_bounds(p, t, sx0, sy0, sx1, sy1);
-            float tr = 0.f, tg = 0.f, tb = 0.f, tw = 0.f;
-            for (int qy = max(qy0, sy0); qy <= min(qy1, sy1 - 1); qy++)
-                for (int qx = max(qx0, sx0); qx <= min(qx1, sx1 - 1); qx++) {
-                    const size_t pix = (size_t)(qy - p.sy0) * p.sw + (qx - p.sx0);
-                    for (int k = 0; k < p.spp; k++) {
-                        const float2 s = image_samples[pix * p.spp + k];
-                        const float fx = (float)qx + s.x, fy = (float)qy + s.y;
-                        int rx0 = (int)ceilf(fx - r - 0.5f), ry0 = (int)ceilf(fy - r - 0.5f);
-                        int rx1 = (int)floorf(fx + r - 0.5f) + 1, ry1 = (int)floorf(fy + r - 0.5f) + 1;
-                        rx0 = max(rx0, bx0); ry0 = max(ry0, by0);
-                        rx1 = min(rx1, bx1); ry1 = min(ry1, by1);
-                        if (px < rx0 || px >= rx1 || py < ry0 || py >= ry1) continue;
-                        const float4 c = radiance[pix * p.spp + k];
-                        tr += 1.f * c.x;
-                        tg += 1.f * c.y;
-                        tb += 1.f * c.z;
-                        tw += 1.f;
-                    }
-                }
-            fr += tr;
-            fg += tg;
-            fb += tb;
-            fw += tw;
+            const float4 c = tile_pixel_sum(p, radiance, image_samples, t, px, py);
+            fr += c.x;
+            fg += c.y;
+            fb += c.z;
+            fw += c.w;
         }
     float cr = 0.f, cg = 0.f, cb = 0.f;
     if (fw != 0.f) {
@@ -1518,7 +1533,33 @@ film_kernel(Render_Params p, const float4* __restrict__ radiance, const float2* 
     rgb[3 * (size_t)idx + 2] = max_std(0.f, cb);
 }
 
+// Every tile's Film_Pixel array (color sum, weight) over its pixel bounds, tile
+// t at out + offset[t], row-major: one block row per tile (blockIdx.y).
+__global__ void __launch_bounds__(kBlock)
+tile_film_kernel(Render_Params p, const float4* __restrict__ radiance, const float2* __restrict__ image_samples,
+                 const uint32_t* __restrict__ offset, float4* __restrict__ out) {
+    const int t = blockIdx.y;
+    int bx0, by0, bx1, by1;
+    tile_pixel_bounds(p, t, bx0, by0, bx1, by1);
+    const int w = bx1 - bx0, h = by1 - by0;
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (w <= 0 || h <= 0 || i >= (uint32_t)(w * h)) return;
+    const int px = bx0 + (int)(i % (uint32_t)w), py = by0 + (int)(i / (uint32_t)w);
+    out[offset[t] + i] = tile_pixel_sum(p, radiance, image_samples, t, px, py);
+}
+
 // ---------------------------------------------------------------- host helpers
+// Film::get_tile_bounds' pixel bounds of tile t (x0, y0, x1, y1), on the host.
+inline void host_tile_pixel_bounds(const Render_Params& p, int t, int b[4]) {
+    const int tx = t % p.tiles_x, ty = t / p.tiles_x;
+    const int sx0 = p.sx0 + tx * kTile, sy0 = p.sy0 + ty * kTile;
+    const int sx1 = std::min(sx0 + kTile, p.sx0 + p.sw), sy1 = std::min(sy0 + kTile, p.sy0 + p.sh);
+    const float r = p.filter_radius;
+    b[0] = std::max((int)std::ceil((float)sx0 - r - 0.5f), p.rx0);
+    b[1] = std::max((int)std::ceil((float)sy0 - r - 0.5f), p.ry0);
+    b[2] = std::min((int)std::floor((float)sx1 + r - 0.5f) + 1, p.rx0 + p.rw);
+    b[3] = std::min((int)std::floor((float)sy1 + r - 0.5f) + 1, p.ry0 + p.rh);
+}
 float pbrt3_roughness_to_alpha(float roughness) {
     // src/ref/scattering.cpp:240-251 (host libm logf, as the reference evaluates it)
     roughness = std::max(roughness, 1e-3f);

@@ -187,6 +187,7 @@ EXPORTS = {
     "yar_gpu_cast_any_timed": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p, C.POINTER(C.c_float)]),
     "yar_gpu_render": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
     "yar_gpu_render_static": (C.c_int, [C.c_void_p, C.c_void_p, C.POINTER(RenderStats)]),
+    "yar_gpu_render_checkpoint": (C.c_int, [C.c_void_p, C.c_char_p, C.c_char_p, C.c_void_p, C.POINTER(RenderStats)]),
     "yar_gpu_traversal_kernels": (C.c_int, [C.c_void_p, C.POINTER(C.c_int32), C.POINTER(C.c_int32),
                                             C.POINTER(C.c_int32)]),
     "yar_gpu_render_batch": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.c_void_p,
@@ -385,6 +386,15 @@ class Context:
         rgb = np.zeros((height, width, 3), np.float32)
         stats = RenderStats()
         self._check(lib().yar_gpu_render(self._h, _ptr(rgb), C.byref(stats)), "render")
+        return rgb, stats
+
+    def render_checkpoint(self, width, height, directory, input_filename):
+        """yar_gpu_render_checkpoint: render_scene with a checkpoint directory in the
+        reference's format (resumes from the tiles already there)."""
+        rgb = np.zeros((height, width, 3), np.float32)
+        stats = RenderStats()
+        self._check(lib().yar_gpu_render_checkpoint(self._h, str(directory).encode(), str(input_filename).encode(),
+                                                     _ptr(rgb), C.byref(stats)), "render_checkpoint")
         return rgb, stats
 
     def traversal_kernels(self):
