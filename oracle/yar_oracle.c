@@ -2107,6 +2107,92 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
 
 typedef struct film_px { float r, g, b, w; } film_px;
 
+/* The direct-lighting algorithm's sample arrays of one pixel sample: per
+ * rectangular light, then per sphere light, k x k 2D light samples, k x k 2D
+ * BSDF samples and k x k 1D scattering samples
+ * (src/ref/reference_renderer.cpp:101-128). */
+typedef struct direct_arrays {
+    const float* light2d[2];  /* [0] rectangular lights, [1] sphere lights: per light, k*k float2 */
+    const float* bsdf2d[2];
+    const float* scatter1d[2];
+    const int* k[2];          /* array side per light */
+    const size_t* offset[2];  /* per light, its first element in the arrays above */
+} direct_arrays;
+
+/* estimate_direct_lighting, src/ref/direct_lighting.cpp:415-520 */
+static int trace_direct(const yar_flat_scene* s, const env_sampler* env, v3 ro, v3 rd, const direct_arrays* da,
+                        oracle_pcg32* rng, col* radiance) {
+    hit_state h;
+    int hit = trace_closest(s, ro, rd, &h);
+    if (hit < 0) return YAR_ERR_CAPACITY;
+    if (!hit) {
+        *radiance = env->e ? env_radiance(env, rd, 1) : mkc(0, 0, 0);
+        return YAR_OK;
+    }
+    shading_ctx sc;
+    init_shading(s, rd, h.object, h.prim, h.b, &sc);
+    float u_scatter = oracle_pcg32_float(rng); /* past the (empty) 1D budget */
+    col L = mkc(0, 0, 0), le;
+    v3 ddir;
+    col datten;
+    float bsdf_prob = 1.f;
+    int delta = 0;
+    if (sc.material_type != YAR_MATERIAL_NULL) delta = delta_scattering(s, &sc, &u_scatter, &ddir, &datten, &bsdf_prob);
+    if (sc.light_type != YAR_LIGHT_NULL) {
+        if (emitted_radiance(s, &sc, &le)) L = le;
+    } else if (sc.material_type != YAR_MATERIAL_NULL && (!delta || bsdf_prob != 0.f)) {
+        bsdf_t f, f_sub[2];
+        int rc = make_bsdf(s, &sc, &f, f_sub);
+        if (rc != YAR_OK) return rc;
+        for (uint32_t i = 0; i < s->delta_light_count; i++) /* point lights */
+            if (s->delta_lights[i].type == YAR_LIGHT_POINT) L = addc(L, direct_delta(s, &sc, &f, &s->delta_lights[i]));
+        for (uint32_t i = 0; i < s->delta_light_count; i++) /* directional lights */
+            if (s->delta_lights[i].type == YAR_LIGHT_DIRECTIONAL)
+                L = addc(L, direct_delta(s, &sc, &f, &s->delta_lights[i]));
+        for (int kind = 0; kind < 2; kind++) {
+            const uint32_t n = kind == 0 ? s->rect_light_count : s->sphere_light_count;
+            for (uint32_t i = 0; i < n; i++) {
+                const int k = da->k[kind][i], count = k * k;
+                const size_t o = da->offset[kind][i];
+                col L2 = mkc(0, 0, 0);
+                for (int j = 0; j < count; j++) {
+                    const float* ul = da->light2d[kind] + 2 * (o + j);
+                    const float* ub = da->bsdf2d[kind] + 2 * (o + j);
+                    const float us = da->scatter1d[kind][o + j];
+                    L2 = addc(L2, kind == 0 ? direct_rect(s, &sc, &f, (int)i, ul[0], ul[1], ub[0], ub[1], us)
+                                            : direct_sphere(s, &sc, &f, (int)i, ul[0], ul[1], ub[0], ub[1], us));
+                }
+                L = addc(L, mulcs(L2, 1.f / (float)count)); /* ColorRGB::operator/= multiplies by 1/v */
+            }
+        }
+        if (env->e) {
+            col L2 = mkc(0, 0, 0);
+            for (int j = 0; j < env->e->sample_count; j++) {
+                float ul0 = oracle_pcg32_float(rng), ul1 = oracle_pcg32_float(rng);
+                float ub0 = oracle_pcg32_float(rng), ub1 = oracle_pcg32_float(rng);
+                float us = oracle_pcg32_float(rng);
+                L2 = addc(L2, direct_env(s, &sc, &f, env, ul0, ul1, ub0, ub1, us));
+            }
+            L = addc(L, mulcs(L2, 1.f / (float)env->e->sample_count));
+        }
+    }
+    if (delta == 1) {
+        v3 o = origin_for_direction(&sc, ddir);
+        hit = trace_closest(s, o, ddir, &h);
+        if (hit < 0) return YAR_ERR_CAPACITY;
+        col emitted = mkc(0, 0, 0);
+        if (hit) {
+            init_shading(s, ddir, h.object, h.prim, h.b, &sc);
+            if (emitted_radiance(s, &sc, &le)) emitted = le;
+        } else if (env->e) {
+            emitted = env_radiance(env, ddir, 1);
+        }
+        L = addc(L, mulc(datten, emitted));
+    }
+    *radiance = L;
+    return YAR_OK;
+}
+
 typedef struct render_job {
     const yar_flat_scene* s;
     int x0, y0, x1, y1;         /* render region */
@@ -2149,8 +2235,29 @@ static int render_tile(render_job* J, int t) {
     if (!px) return YAR_ERR_NOMEM;
     J->tile_pixels[t] = px;
     const int nx = cfg->x_pixel_sample_count, ny = cfg->y_pixel_sample_count, spp = nx * ny;
+    const int direct = cfg->rendering_algorithm == 0;
     const int maxb = cfg->max_light_bounces < 10 ? cfg->max_light_bounces : 10;
-    const int n1d = maxb * 4, n2d = maxb * 3; /* src/ref/reference_renderer.cpp:87-99 */
+    const int n1d = direct ? 0 : maxb * 4, n2d = direct ? 0 : maxb * 3; /* src/ref/reference_renderer.cpp:87-99 */
+    /* direct lighting: k x k sample arrays per rectangular and per sphere light */
+    int* dk[2] = {NULL, NULL};
+    size_t* doff[2] = {NULL, NULL};
+    size_t dper[2] = {0, 0}; /* array elements per pixel sample */
+    float* dbuf[2][3] = {{NULL, NULL, NULL}, {NULL, NULL, NULL}};
+    if (direct) {
+        for (int kind = 0; kind < 2; kind++) {
+            const uint32_t n = kind == 0 ? s->rect_light_count : s->sphere_light_count;
+            dk[kind] = (int*)calloc(n + 1, sizeof(int));
+            doff[kind] = (size_t*)calloc(n + 1, sizeof(size_t));
+            for (uint32_t i = 0; i < n; i++) {
+                const int sc = kind == 0 ? s->rect_lights[i].sample_count : s->sphere_lights[i].sample_count;
+                dk[kind][i] = (int)ceil(sqrt((double)sc));
+                doff[kind][i] = dper[kind];
+                dper[kind] += (size_t)dk[kind][i] * dk[kind][i];
+            }
+            for (int b = 0; b < 3; b++)
+                dbuf[kind][b] = (float*)malloc(sizeof(float) * (b < 2 ? 2 : 1) * (dper[kind] * spp + 1));
+        }
+    }
     float* image = (float*)malloc(sizeof(float) * 2 * spp);
     float* s1d = (float*)malloc(sizeof(float) * ((size_t)spp * n1d + 1));
     float* s2d = (float*)malloc(sizeof(float) * (2 * (size_t)spp * n2d + 1));
@@ -2190,6 +2297,42 @@ static int render_tile(render_job* J, int t) {
                         s2d[2 * (k * n2d + i) + 1] = tmp[2 * k + 1];
                     }
                 }
+                /* Stratified_Pixel_Sampler::next_pixel's array samples (src/ref/pixel_sampling.cpp:88-141):
+                 * the 2D arrays in registration order (per light: light, BSDF), then the 1D arrays */
+                for (int pass = 0; pass < 2 && direct && rc == YAR_OK; pass++) {
+                    for (int kind = 0; kind < 2; kind++) {
+                        const uint32_t n = kind == 0 ? s->rect_light_count : s->sphere_light_count;
+                        for (uint32_t li = 0; li < n; li++) {
+                            const int k = dk[kind][li], count = k * k;
+                            float* grids = (float*)malloc(sizeof(float) * 2 * (size_t)count * spp);
+                            for (int which = 0; which < (pass == 0 ? 2 : 1); which++) {
+                                for (int g = 0; g < count; g++) {
+                                    float* grid = grids + (pass == 0 ? 2 : 1) * (size_t)g * spp;
+                                    if (pass == 0) stratified_2d(&rng, nx, ny, grid);
+                                    else stratified_1d(&rng, spp, grid);
+                                    shuffle(grid, spp, pass == 0 ? 2 : 1, &rng);
+                                }
+                                float* out = dbuf[kind][pass == 0 ? which : 2];
+                                const float dxa = pass == 0 ? 1.f / (float)k : 1.f / (float)count;
+                                for (int i = 0; i < spp; i++)
+                                    for (int g = 0; g < count; g++) {
+                                        const size_t e = (size_t)i * dper[kind] + doff[kind][li] + g;
+                                        if (pass == 0) {
+                                            const float* u = grids + 2 * ((size_t)g * spp + i);
+                                            const int gx = g % k, gy = g / k;
+                                            float sx = ((float)gx + u[0]) * dxa, sy = ((float)gy + u[1]) * dxa;
+                                            out[2 * e] = sx < ONE_MINUS_EPSILON ? sx : ONE_MINUS_EPSILON;
+                                            out[2 * e + 1] = sy < ONE_MINUS_EPSILON ? sy : ONE_MINUS_EPSILON;
+                                        } else {
+                                            float v = ((float)g + grids[(size_t)g * spp + i]) * dxa;
+                                            out[e] = v < ONE_MINUS_EPSILON ? v : ONE_MINUS_EPSILON;
+                                        }
+                                    }
+                            }
+                            free(grids);
+                        }
+                    }
+                }
             }
             double lsum = 0.0, lsq = 0.0;
             for (int k = 0; k < spp; k++) {
@@ -2198,7 +2341,19 @@ static int render_tile(render_job* J, int t) {
                 camera_ray(&s->camera, fx, fy, &o, &d);
                 sampler_view sv = {s1d + (size_t)k * n1d, s2d + 2 * (size_t)k * n2d, n1d, n2d, 0, 0, &rng};
                 col radiance;
-                rc = trace_path(s, J->mesh_samplers, &J->env, o, d, &sv, &radiance);
+                if (direct) {
+                    direct_arrays da;
+                    for (int kind = 0; kind < 2; kind++) {
+                        da.light2d[kind] = dbuf[kind][0] + 2 * (size_t)k * dper[kind];
+                        da.bsdf2d[kind] = dbuf[kind][1] + 2 * (size_t)k * dper[kind];
+                        da.scatter1d[kind] = dbuf[kind][2] + (size_t)k * dper[kind];
+                        da.k[kind] = dk[kind];
+                        da.offset[kind] = doff[kind];
+                    }
+                    rc = trace_direct(s, &J->env, o, d, &da, &rng, &radiance);
+                } else {
+                    rc = trace_path(s, J->mesh_samplers, &J->env, o, d, &sv, &radiance);
+                }
                 if (rc != YAR_OK) break;
                 float limit = cfg->max_rgb_component_value_of_film_sample;
                 float mc = fmaxf_std(radiance.r, fmaxf_std(radiance.g, radiance.b));
@@ -2232,6 +2387,11 @@ static int render_tile(render_job* J, int t) {
     free(image);
     free(s1d);
     free(s2d);
+    for (int kind = 0; kind < 2; kind++) {
+        free(dk[kind]);
+        free(doff[kind]);
+        for (int b = 0; b < 3; b++) free(dbuf[kind][b]);
+    }
     J->tile_variance[t] = var_acc;
     return rc;
 }
@@ -2263,7 +2423,8 @@ int oracle_render_trig(const yar_flat_scene* s, float* rgb, double* variance, in
 int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t row_begin, int32_t row_end,
                   int32_t thread_count) {
     const yar_render_config* cfg = &s->config;
-    if (cfg->rendering_algorithm != 1 || cfg->pixel_filter_type != 0) return YAR_ERR_UNSUPPORTED;
+    if ((cfg->rendering_algorithm != 0 && cfg->rendering_algorithm != 1) || cfg->pixel_filter_type != 0)
+        return YAR_ERR_UNSUPPORTED;
     for (uint32_t i = 0; i < s->material_count; i++) {
         uint32_t t = s->materials[i].type;
         if (t != YAR_MATERIAL_DIFFUSE && t != YAR_MATERIAL_METAL && t != YAR_MATERIAL_GLASS &&

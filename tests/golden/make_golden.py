@@ -60,6 +60,13 @@ Fixtures
   cornell_envmap_64.yfs / .npz  the delta-box Cornell box with an "infinite"
                              light of a 64 x 32 sky map with a sun (written by
                              yar_gb300.exr), seed 13.
+  cornell_direct_64.yfs / .npz  the reference's direct-lighting algorithm
+                             (pbrt "directlighting"): GGX boxes, the quad light
+                             with 4 samples (2 x 2 arrays), point, spot and
+                             distant lights, seed 15.
+  cornell_direct_env_64.yfs / .npz  direct lighting with delta boxes, the quad
+                             light with 3 samples and a sky map with 2 samples,
+                             seed 16.
   checkpoint_c1/             the reference's checkpoint directory (metadata and
                              four tile files) of a 72 x 72, 4 spp Cornell box
                              render (seed 14) with input file name
@@ -315,6 +322,26 @@ def cornell_envmap_64():
     np.savez_compressed(os.path.join(HERE, "cornell_envmap_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def cornell_direct_64():
+    _pbrt_golden("cornell_direct_64", 15, box_materials=scenes.GGX_BOXES, light_sources=scenes.DELTA_LIGHTS,
+                 light_samples=4, integrator="directlighting")
+
+
+def cornell_direct_env_64():
+    from yar_gb300 import exr
+    with tempfile.TemporaryDirectory() as d:
+        exr.write_exr(os.path.join(d, "sky.exr"), scenes.environment_map(), False, {})
+        pbrt = os.path.join(d, "cornell_direct_env.pbrt")
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=16, width=64, height=64, spp=16, maxdepth=8,
+                                                  box_materials=scenes.DELTA_BOXES, light_samples=3,
+                                                  light_sources=scenes.environment_statements("sky.exr", samples=2),
+                                                  integrator="directlighting"))
+        oracle.ref_flatten(pbrt, os.path.join(HERE, "cornell_direct_env_64.yfs"), seed_offset=1)
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_direct_env_64.npz"), image=img,
+                        variance=np.float64(info["variance"]))
+
+
 def checkpoint_c1():
     """The reference's own checkpoint files: render_scene with a checkpoint directory."""
     import shutil
@@ -382,7 +409,7 @@ if __name__ == "__main__":
                              "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64",
                              "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64",
                              "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64",
-                             "checkpoint_c1",
+                             "cornell_direct_64", "cornell_direct_env_64", "checkpoint_c1",
                              "exr_files",
                              "kdtree_cache_files"]
     for name in which:

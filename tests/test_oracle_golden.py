@@ -124,7 +124,7 @@ def test_builder_against_live_reference_large_mesh():
 @pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64",
                                   "cornell_layered_64", "cornell_layered_yar_64", "cornell_lights_64",
                                   "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64",
-                                  "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64"])
+                                  "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64"])
 def test_oracle_render_matches_reference_golden(name):
     """The oracle's path loop, sampler, shading, BSDFs (diffuse, GGX metal, rough
     glass, plastic in both of the reference's forms, coated diffuse), delta

@@ -180,7 +180,8 @@ def _box(center, size, angle_deg):
 
 
 def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0, box_materials=None,
-                 upper_light=None, light_sources=(), mesh_lights=(), sphere_lights=(), named_materials=()):
+                 upper_light=None, light_sources=(), mesh_lights=(), sphere_lights=(), named_materials=(),
+                 integrator="path", light_samples=1):
     """pbrt-v3 text of the seeded Cornell box (34 triangles + a quad light).
 
     box_materials: None for matte boxes, or two pbrt material statements for
@@ -195,7 +196,9 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
     triangle-mesh lights).
     sphere_lights: (center, radius, radiance) emitting pbrt spheres (sphere
     lights, shown by the reference's tessellated sphere).
-    named_materials: pbrt MakeNamedMaterial statements (for "mix")."""
+    named_materials: pbrt MakeNamedMaterial statements (for "mix").
+    integrator: "path" or "directlighting" (the reference's direct-lighting
+    algorithm); light_samples: the quad light's "integer samples"."""
     rng = np.random.default_rng(seed)
     k = int(math.ceil(math.sqrt(spp)))
     shapes = []
@@ -223,7 +226,7 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
         'Film "image" "integer xresolution" [%d] "integer yresolution" [%d] "string filename" "cornell.exr"'
         % (width, height),
         'Sampler "stratified" "integer xsamples" [%d] "integer ysamples" [%d]' % (k, k),
-        'Integrator "path" "integer maxdepth" [%d]' % maxdepth,
+        'Integrator "%s" "integer maxdepth" [%d]' % (integrator, maxdepth),
         'PixelFilter "box"',
         "WorldBegin",
     ] + list(named_materials) + list(light_sources)
@@ -236,7 +239,8 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
                 '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(i), fmt(v)),
                 "AttributeEnd"]
     out += ["AttributeBegin",
-            '  AreaLightSource "diffuse" "rgb L" [%s]' % fmt([light_radiance] * 3),
+            '  AreaLightSource "diffuse" "rgb L" [%s] "integer nsamples" [%d]' % (fmt([light_radiance] * 3),
+                                                                              light_samples),
             '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(light[1]), fmt(light[0])),
             "AttributeEnd"]
     for center, radius, radiance in sphere_lights:
@@ -310,11 +314,12 @@ def environment_map(width=64, height=32, seed=1):
     return img.astype(np.float32)
 
 
-def environment_statements(mapname, scale=(1, 1, 1)):
+def environment_statements(mapname, scale=(1, 1, 1), samples=1):
     """pbrt statements of an infinite light with the given map, turned so that
     the map's pole points along +y."""
     return ("AttributeBegin", "  Rotate -90 1 0 0",
-            '  LightSource "infinite" "string mapname" "%s" "rgb L" [%g %g %g]' % ((mapname,) + tuple(scale)),
+            '  LightSource "infinite" "string mapname" "%s" "integer nsamples" [%d] "rgb L" [%g %g %g]'
+            % ((mapname, samples) + tuple(scale)),
             "AttributeEnd")
 
 
