@@ -48,7 +48,7 @@ def compare(img, ref):
 @pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64",
                                   "cornell_layered_64", "cornell_layered_yar_64", "cornell_lights_64",
                                   "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
-                  "cornell_envmap_64"])
+                  "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64"])
 def test_render_matches_reference_golden(gpu_ctx, name):
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
@@ -69,7 +69,7 @@ def test_render_matches_reference_golden(gpu_ctx, name):
 RENDER_GOLDENS = ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "cornell_layered_64",
                   "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64", "cornell_spherelight_64",
                   "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
-                  "cornell_envmap_64"]
+                  "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64"]
 
 
 @pytest.mark.parametrize("name", RENDER_GOLDENS)
@@ -175,6 +175,26 @@ def test_render_rejects_delta_lights_out_of_order(gpu_ctx):
     with pytest.raises(native.YarError) as e:
         gpu_ctx.render(64, 64)
     assert e.value.code == native.YAR_ERR_INVALID
+
+
+@pytest.mark.parametrize("samples", [(4, 2), (1, 9)])
+def test_render_direct_lighting_sphere_lights_bit_identical(gpu_ctx, samples):
+    """The direct-lighting algorithm over sphere lights' k x k sample arrays
+    (and the quad light's), against the oracle with correctly rounded
+    trigonometry."""
+    s = FlatScene.read(golden("cornell_spherelight_64.yfs"))
+    s.config["rendering_algorithm"] = 0
+    sl = s.sphere_lights.copy()
+    sl["sample_count"] = samples
+    s.sphere_lights = sl
+    rl = s.rect_lights.copy()
+    rl["sample_count"] = 2
+    s.rect_lights = rl
+    ref, ref_var = oracle.render(s, threads=8, correctly_rounded_trig=True)
+    gpu_ctx.upload_scene(s)
+    img, stats = gpu_ctx.render(64, 64)
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    assert stats.variance == ref_var
 
 
 def test_render_unsupported_features_fail_cleanly(gpu_ctx):

@@ -32,7 +32,7 @@ NVCC_FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-fmad=false", "--expt-relaxed-c
 CXX_FLAGS = ["-O2", "-std=c++17", "-fPIC", "-ffp-contract=off", "-pthread",
              "-I" + os.path.join(ROOT, "include"), "-I" + CSRC]
 
-CU_SOURCES = ["capi.cu", "cast.cu", "render.cu", "guide_mlp.cu", "guided.cu", "batch.cu"]
+CU_SOURCES = ["capi.cu", "cast.cu", "render.cu", "guide_mlp.cu", "guided.cu", "batch.cu", "direct.cu"]
 CXX_SOURCES = ["kdtree_build.cpp"]
 
 

@@ -41,6 +41,7 @@ struct Render_Scene {
     std::vector<yar_delta_light_desc> host_delta_lights;
     uint32_t mesh_light_count = 0;
     uint32_t sphere_light_count = 0;
+    std::vector<yar_sphere_light_desc> host_sphere_lights;
     bool has_environment = false;
     yar_environment_desc environment{};  // radiance is not kept
     bool has_no_shadow_meshes = false;
@@ -160,6 +161,8 @@ cudaError_t guide_train(yar_gpu_ctx* ctx, const float4* samples, uint32_t n_max,
 int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene);
 void render_release(yar_gpu_ctx* ctx);
 int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats);
+// The direct-lighting algorithm (Raytracer_Config::rendering_algorithm 0), direct.cu.
+int render_direct(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats);
 int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* params, double* sum_out, float* rgb_out,
                   yar_guided_stats* stats);
 

@@ -131,6 +131,14 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
         d.scattering = (has_a ? mats[a].scattering : 0u) | (has_b ? mats[b].scattering : 0u);
         d.delta = kDeltaMix;
     }
+    // whether Shading_Context::initialize_scattering creates a BSDF (some layer is not delta)
+    for (uint32_t i = 0; i < scene->material_count; i++) {
+        const yar_material_desc& m = scene->materials[i];
+        bool has = mats[i].delta == kDeltaNone || mats[i].delta == kDeltaMix;
+        if (m.type == YAR_MATERIAL_PBRT3_UBER)
+            for (uint32_t k = 0; k < m.component_count && k < 5; k++) has = has || m.components[k] < YAR_UBER_DELTA_REFLECTION;
+        mats[i].has_bsdf = has ? 1u : 0u;
+    }
     std::vector<Rect_Light_Dev> lights(std::max<uint32_t>(1, scene->rect_light_count));
     for (uint32_t i = 0; i < scene->rect_light_count; i++) {
         const yar_rect_light_desc& l = scene->rect_lights[i];
@@ -194,6 +202,7 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
         slights[i].le = make_float4(l.emitted_radiance[0], l.emitted_radiance[1], l.emitted_radiance[2], 0.f);
     }
     R.sphere_light_count = scene->sphere_light_count;
+    R.host_sphere_lights.assign(scene->sphere_lights, scene->sphere_lights + scene->sphere_light_count);
     // Environment light: the map as float4 texels and its Distribution_2D, built as
     // initialize_from_latitude_longitude_radiance_map does (src/ref/sampling.cpp:185-259).
     R.has_environment = scene->environment != nullptr;
@@ -301,6 +310,7 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p, float* rgb_out, 
 
 int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
     if (!rgb_out) return fail(ctx, YAR_ERR_INVALID, "null image buffer");
+    if (ctx->render.config.rendering_algorithm == 0) return render_direct(ctx, rgb_out, stats);
     Render_Params p;
     if (int rc0 = prepare_render_params(ctx, p)) return rc0;
     return render_run_params(ctx, p, rgb_out, stats, nullptr);

@@ -174,6 +174,7 @@ struct Material_Dev {
     float mix_p;            // mix: 1 - luminance(White - amount) (Mix_BSDF::p_coeff)
     float mix_lum;          // mix: luminance(amount), unclamped (the Scaled_BSDF factor)
     Col mix_coeff;          // mix: White - amount
+    uint32_t has_bsdf;      // initialize_scattering creates a BSDF: some layer is not delta
 };
 
 struct Bsdf {

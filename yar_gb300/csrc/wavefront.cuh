@@ -99,6 +99,7 @@ struct Render_Params {
     float film_scale, max_component;
     int32_t total_lights, delta_lights, rect_lights, sphere_lights, mesh_lights, env_lights;  // selection order
     int32_t full_shading;  // the scene needs shade_kernel<*, true>
+    int32_t arrays_2d_first;  // direct lighting: the 2D rows (array grids) come before the 1D rows in the stream
     uint32_t seed_offset;
     uint32_t stream_hi;  // upper 32 bits of the pixel streams' sequence (0 = the reference's streams)
 };
@@ -338,7 +339,8 @@ __global__ void sample_tables_kernel(Render_Params p, uint32_t chunk_first, uint
     }
     if (row <= n1d) {
         const uint32_t dim = row - 1u;
-        pcg_advance(rng, (uint32_t)(2 * spp) + dim * (uint32_t)(2 * spp - 1));
+        pcg_advance(rng, (uint32_t)(2 * spp) + (p.arrays_2d_first ? (uint32_t)p.n2d * (uint32_t)(3 * spp - 1) : 0u) +
+                             dim * (uint32_t)(2 * spp - 1));
         const float d = 1.f / (float)spp;
         for (int k = 0; k < spp; k++) sm[k * stride].x = one_minus_eps_min(((float)k + pcg_float(rng)) * d);
         for (int m = spp; m > 1; m--) {  // shuffle, src/lib/math.h:138-145
@@ -359,7 +361,8 @@ __global__ void sample_tables_kernel(Render_Params p, uint32_t chunk_first, uint
         return;
     }
     const uint32_t dim = row - 1u - n1d;
-    pcg_advance(rng, (uint32_t)(2 * spp) + n1d * (uint32_t)(2 * spp - 1) + dim * (uint32_t)(3 * spp - 1));
+    pcg_advance(rng, (uint32_t)(2 * spp) + (p.arrays_2d_first ? 0u : n1d * (uint32_t)(2 * spp - 1)) +
+                         dim * (uint32_t)(3 * spp - 1));
     for (int j = 0; j < p.ny; j++)
         for (int i = 0; i < p.nx; i++) {
             const float a = one_minus_eps_min(((float)i + pcg_float(rng)) * dx);
@@ -1591,7 +1594,8 @@ int grid_for(uint64_t n) {
 int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     const Render_Scene& R = ctx->render;
     const yar_render_config& c = R.config;
-    if (c.rendering_algorithm != 1) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the path tracer is implemented");
+    if (c.rendering_algorithm != 0 && c.rendering_algorithm != 1)
+        return fail(ctx, YAR_ERR_UNSUPPORTED, "unknown rendering algorithm");
     if (c.pixel_filter_type != 0) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the box filter is implemented");
     if (R.other_light_count)
         return fail(ctx, YAR_ERR_UNSUPPORTED, "the scene has lights of a kind that is not implemented");
@@ -1679,6 +1683,22 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     const int maxb = std::min(10, c.max_light_bounces);
     p.n1d = maxb * 4;  // src/ref/reference_renderer.cpp:87-99
     p.n2d = maxb * 3;
+    p.arrays_2d_first = 0;
+    if (c.rendering_algorithm == 0) {
+        // direct lighting: no sample vectors, k x k arrays per rectangular and sphere
+        // light (reference_renderer.cpp:101-128): 2 two-dimensional, 1 one-dimensional
+        int grids_2d = 0, grids_1d = 0;
+        auto add = [&](int sample_count) {
+            const int k = (int)std::ceil(std::sqrt((double)sample_count));
+            grids_2d += 2 * k * k;
+            grids_1d += k * k;
+        };
+        for (const yar_rect_light_desc& l : R.host_rect_lights) add(l.sample_count);
+        for (const yar_sphere_light_desc& l : R.host_sphere_lights) add(l.sample_count);
+        p.n1d = grids_1d;
+        p.n2d = grids_2d;
+        p.arrays_2d_first = 1;
+    }
     p.max_bounces = c.max_light_bounces;
     p.rr_bounce_threshold = c.russian_roulette_bounce_count_threshold;
     p.rr_threshold = c.russian_roulette_threshold;
