@@ -318,9 +318,15 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
 
 // The render of render_run over the sample region of p.  With tiles_out, the
 // image is not resolved: the tiles' film data come back instead.
-int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p, float* rgb_out, yar_render_stats* stats,
+int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_out, yar_render_stats* stats,
                       Tile_Output* tiles_out) {
     cudaSetDevice(ctx->device);
+    // Draws past the sampler budget follow the reference's per-pixel stream
+    // (exact tail) for the reference's own streams.
+    Render_Params p = p_in;
+    p.exact_tail = (p.stream_hi == 0 && p.n1d > 0) ? 1 : 0;
+    Render_Params p_wave = p;
+    p_wave.exact_tail = 2;
     const auto t_start = std::chrono::steady_clock::now();
     const uint64_t pixels = (uint64_t)p.sw * p.sh;
     const uint64_t samples = pixels * p.spp;
@@ -330,7 +336,7 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p, float* rgb_out, 
     // scratch: everything sized by the largest chunk, allocated per call
     std::vector<Device_Buffer>& B = ctx->render_scratch;
     for (Device_Buffer& b : B) device_free(b);
-    B.assign(32, Device_Buffer{});
+    B.assign(36, Device_Buffer{});
     int rc = YAR_OK;
     auto alloc = [&](int i, size_t bytes) {
         if (rc == YAR_OK) rc = device_alloc(ctx, B[i], bytes);
@@ -365,11 +371,21 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p, float* rgb_out, 
     alloc(27, pixels * sizeof(double));                    // pixel variance
     alloc(28, (size_t)p.tiles_x * p.tiles_y * sizeof(double));
     alloc(29, (size_t)p.rw * p.rh * 3 * sizeof(float));    // rgb
+    if (p.exact_tail) {
+        alloc(30, cap * sizeof(uint32_t));                 // rng draws past the budget
+        alloc(31, cap * 2 * sizeof(float4));               // deferred extend rays
+        alloc(32, cap * sizeof(uint32_t));                 // deferred slots per pixel, in sample order
+        alloc(33, chunk_pixels * sizeof(uint32_t));        // deferred count per pixel
+        alloc(34, chunk_pixels * sizeof(uint32_t));        // stream position per pixel
+        alloc(35, 2 * sizeof(uint32_t));                   // largest count, stray-draw flag
+    }
     if (rc != YAR_OK) return rc;
 
     Path_State ps{dptr<float4>(B[4]), dptr<float4>(B[5]), dptr<uint32_t>(B[6]), dptr<uint4>(B[7]),
                   dptr<float4>(B[8]), dptr<float4>(B[9]), dptr<float4>(B[10]), dptr<float4>(B[11]),
                   dptr<float4>(B[12]), dptr<uint8_t>(B[13]), dptr<float4>(B[14]), dptr<uint2>(B[15])};
+    ps.rng_draws = dptr<uint32_t>(B[30]);
+    ps.deferred = dptr<float4>(B[31]);
     Queues q{};
     q.ext_rays[0] = dptr<float4>(B[16]);
     q.ext_rays[1] = dptr<float4>(B[17]);
@@ -390,22 +406,20 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p, float* rgb_out, 
     cudaError_t e = cudaMemsetAsync(q.counters, 0, 8 * sizeof(uint32_t), st);
     uint64_t rays_closest = 0, rays_any = 0;
     uint32_t launches = 0;
-    for (uint64_t first = 0; first < pixels && e == cudaSuccess; first += chunk_pixels) {
-        const uint32_t cp = (uint32_t)std::min<uint64_t>(chunk_pixels, pixels - first);
-        const uint32_t paths = cp * (uint32_t)p.spp;
-        launch_generate(p, (uint32_t)first, cp, dptr<float>(B[2]), dptr<float>(B[3]), image_samples, ps, q, st);
-        launches++;
+    // The bounce loop over extend queue 0 of `count` paths; bounce0 picks the
+    // traversal kernels.  Sets e; returns a YAR_ERR_* for a traversal overflow.
+    auto run_bounces = [&](const Render_Params& pp, uint32_t count, int bounce0) -> int {
         int cur = 0;
-        uint32_t count = paths;
-        for (int bounce = 0; count > 0 && bounce <= p.max_bounces + 1; bounce++) {
+        for (int it = 0; count > 0 && it <= p.max_bounces + 1; it++) {
+            const int bounce = bounce0 + it;
             e = trace_extend(ctx, q, cur, count, bounce, st);
             if (e != cudaSuccess) break;
             cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
-            launch_shade<false>(p, grid_for(count), st, S, cur, count, dptr<float>(B[2]), dptr<float2>(B[3]), ps, q,
+            launch_shade<false>(pp, grid_for(count), st, S, cur, count, dptr<float>(B[2]), dptr<float2>(B[3]), ps, q,
                                 Guide_Shade{});
             e = trace_light_queues(ctx, q, ps, count, bounce, st);
             if (e != cudaSuccess) break;
-            connect_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, q.ext_slot[cur], count, ps, nullptr);
+            connect_kernel<<<grid_for(count), kBlock, 0, st>>>(pp, S, q.ext_slot[cur], count, ps, nullptr);
             launches += 5;
             uint32_t h[4];
             e = cudaMemcpyAsync(h, q.counters, sizeof(h), cudaMemcpyDeviceToHost, st);
@@ -416,6 +430,41 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p, float* rgb_out, 
             rays_any += h[1];
             count = h[0];
             cur ^= 1;
+        }
+        return YAR_OK;
+    };
+    for (uint64_t first = 0; first < pixels && e == cudaSuccess; first += chunk_pixels) {
+        const uint32_t cp = (uint32_t)std::min<uint64_t>(chunk_pixels, pixels - first);
+        const uint32_t paths = cp * (uint32_t)p.spp;
+        launch_generate(p, (uint32_t)first, cp, dptr<float>(B[2]), dptr<float>(B[3]), image_samples, ps, q, st);
+        launches++;
+        if (int rc1 = run_bounces(p, paths, 0)) return rc1;
+        if (e != cudaSuccess) break;
+        if (p.exact_tail) {
+            uint32_t* list = dptr<uint32_t>(B[32]);
+            uint32_t* deferred_count = dptr<uint32_t>(B[33]);
+            uint32_t* stream_pos = dptr<uint32_t>(B[34]);
+            uint32_t* tail = dptr<uint32_t>(B[35]);
+            cudaMemsetAsync(tail, 0, 2 * sizeof(uint32_t), st);
+            tail_rank_kernel<<<grid_for(cp), kBlock, 0, st>>>(p, cp, ps, list, deferred_count, stream_pos, tail);
+            launches++;
+            uint32_t ht[2];
+            e = cudaMemcpyAsync(ht, tail, sizeof(ht), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) break;
+            if (ht[1]) return fail(ctx, YAR_ERR_INVALID, "a path drew past the sampler budget before its deferral");
+            for (uint32_t wave = 0; wave < ht[0] && e == cudaSuccess; wave++) {
+                cudaMemsetAsync(q.counters, 0, sizeof(uint32_t), st);
+                tail_wave_kernel<<<grid_for(cp), kBlock, 0, st>>>(p_wave, (uint32_t)first, cp, wave, ps, q, list,
+                                                                  deferred_count, stream_pos);
+                launches++;
+                uint32_t n = 0;
+                e = cudaMemcpyAsync(&n, q.counters, sizeof(n), cudaMemcpyDeviceToHost, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+                if (e != cudaSuccess) break;
+                if (int rc1 = run_bounces(p_wave, n, yar_gpu_ctx::kBounceBuckets - 1)) return rc1;
+            }
+            if (e != cudaSuccess) break;
         }
         finish_chunk_kernel<<<grid_for(paths), kBlock, 0, st>>>(paths, first * p.spp, ps, radiance);
         launches++;

@@ -56,7 +56,8 @@ enum : uint32_t {
     kPendProbe = 1u << 25,
     kPendDirect = 1u << 26,
     kDeltaArrival = 1u << 27,
-    kDeltaFinal = 1u << 28
+    kDeltaFinal = 1u << 28,
+    kDeferred = 1u << 29  // exact tail: the path's next extend ray waits in Path_State::deferred
 };
 
 struct Rect_Light_Dev {
@@ -102,6 +103,10 @@ struct Render_Params {
     int32_t arrays_2d_first;  // direct lighting: the 2D rows (array grids) come before the 1D rows in the stream
     uint32_t seed_offset;
     uint32_t stream_hi;  // upper 32 bits of the pixel streams' sequence (0 = the reference's streams)
+    // Draws past the sampler budget: 0 = one pcg stream per sample; 1 = exact
+    // tail, first phase (a path that might draw past the budget at its next
+    // vertex is deferred); 2 = exact tail, waves (draws are counted per path).
+    int32_t exact_tail;
 };
 
 struct Path_State {
@@ -118,6 +123,8 @@ struct Path_State {
     float4* probe_hit4;    // t, b0, b1, b2
     uint2* probe_hit2;     // prim, object
     uint32_t* rec;         // guided training: this bounce's record index (0xffffffff = none)
+    uint32_t* rng_draws;   // exact tail: pcg draws this path took past the budget
+    float4* deferred;      // exact tail: the deferred extend ray, 2 float4 per slot
 };
 
 // Learned-proposal hooks of the shade kernel (guided render only).
@@ -426,6 +433,7 @@ camera_kernel(Render_Params p, uint32_t chunk_first, uint32_t chunk_paths, const
                             p.stream_hi ? mix64(seq2 + (uint64_t)p.stream_hi * 0x9E3779B97F4A7C15ull) : seq2);
     ps.rng[slot] = make_uint4((uint32_t)r2.state, (uint32_t)(r2.state >> 32), (uint32_t)r2.inc,
                               (uint32_t)(r2.inc >> 32));
+    if (p.exact_tail) ps.rng_draws[slot] = 0u;
 }
 
 // ---------------------------------------------------------------- extend / probe / shadow
@@ -574,18 +582,33 @@ struct Dims {
     int n1d, n2d, i1d, i2d, spp;
     Pcg rng;
     bool rng_used;
+    uint32_t draws;  // pcg draws past the budget
 };
 __device__ __forceinline__ float next1d(Dims& d) {
     if (d.i1d < d.n1d) return d.s1d[(size_t)(d.i1d++) * d.spp];
     d.rng_used = true;
+    d.draws += 1u;
     return pcg_float(d.rng);
 }
 __device__ __forceinline__ float2 next2d(Dims& d) {
     if (d.i2d < d.n2d) return d.s2d[(size_t)(d.i2d++) * d.spp];
     d.rng_used = true;
+    d.draws += 2u;
     const float a = pcg_float(d.rng);
     const float b = pcg_float(d.rng);
     return make_float2(a, b);
+}
+
+// Whether the vertex a path reaches next may take a draw past the sampler
+// budget: a vertex takes 3 1D and 3 2D dimensions, one more 1D for the
+// Russian roulette after a delta arrival and one for the roulette after the
+// continuation.
+__device__ __forceinline__ bool tail_may_draw_past_budget(const Render_Params& p, uint32_t info) {
+    const int bounce = (int)(info & 0xffu);
+    const int i1d = (int)((info >> 8) & 0xffu), i2d = (int)((info >> 16) & 0xffu);
+    const int n1 = 3 + ((info & kDeltaArrival) && bounce >= p.rr_bounce_threshold ? 1 : 0) +
+                   (bounce + 1 >= p.rr_bounce_threshold ? 1 : 0);
+    return i1d + n1 > p.n1d || i2d + 3 > p.n2d;
 }
 
 // ---------------------------------------------------------------- triangle-mesh lights
@@ -816,6 +839,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
             }
             if (!hit || is_light) done = true;
             Dims dm;
+            dm.rng_used = false;
+            dm.draws = 0u;
             if (!done) {
                 {
                     const uint32_t lp = slot / (uint32_t)p.spp, k = slot - lp * (uint32_t)p.spp;
@@ -830,7 +855,6 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 const uint4 rs = ps.rng[slot];
                 dm.rng.state = (uint64_t)rs.x | ((uint64_t)rs.y << 32);
                 dm.rng.inc = (uint64_t)rs.z | ((uint64_t)rs.w << 32);
-                dm.rng_used = false;
                 // The Russian roulette that ends the reference's delta iteration
                 // (path_tracing.cpp:114-131) takes its draw before this vertex's.
                 if (arrival && bounce >= p.rr_bounce_threshold) {
@@ -1213,9 +1237,18 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                     }
                     info = (uint32_t)bounce | ((uint32_t)dm.i1d << 8) | ((uint32_t)dm.i2d << 16) | pend;
                 }
-                if (dm.rng_used)
-                    ps.rng[slot] = make_uint4((uint32_t)dm.rng.state, (uint32_t)(dm.rng.state >> 32),
-                                              (uint32_t)dm.rng.inc, (uint32_t)(dm.rng.inc >> 32));
+            }
+            // Saved also when the Russian roulette of a delta arrival ended the path.
+            if (dm.rng_used) {
+                ps.rng[slot] = make_uint4((uint32_t)dm.rng.state, (uint32_t)(dm.rng.state >> 32),
+                                          (uint32_t)dm.rng.inc, (uint32_t)(dm.rng.inc >> 32));
+                if (p.exact_tail) ps.rng_draws[slot] += dm.draws;
+            }
+            if (p.exact_tail == 1 && want_next && tail_may_draw_past_budget(p, info)) {
+                ps.deferred[2 * (size_t)slot] = nx_a;
+                ps.deferred[2 * (size_t)slot + 1] = nx_b;
+                info |= kDeferred;
+                want_next = false;
             }
             ps.coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0.f);
             ps.L[slot] = make_float4(L.r, L.g, L.b, 0.f);
@@ -1332,6 +1365,78 @@ __global__ void __launch_bounds__(kBlock)
 finish_chunk_kernel(uint32_t paths, uint64_t first_sample, const Path_State ps, float4* __restrict__ radiance) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < paths; i += gridDim.x * blockDim.x)
         radiance[first_sample + i] = ps.L[i];
+}
+
+// ---------------------------------------------------------------- exact tail
+// The reference draws the dimensions past the sampler budget from the pixel's
+// pcg stream, after the sample tables, in sample order: sample k starts where
+// sample k-1 stopped (Stratified_Pixel_Sampler::get_next_1d/2d_sample,
+// src/ref/pixel_sampling.cpp:159-173).  A path that may take such a draw at its next
+// vertex is deferred (kDeferred, its extend ray kept per slot), and the
+// deferred paths are finished in waves: wave j takes each pixel's j-th
+// deferred sample, whose stream is the pixel's advanced by the table draws
+// plus the draws of the pixel's earlier deferred samples.
+
+// Per chunk pixel: the deferred samples' slots in sample order (list, spp
+// entries per pixel), their count, and the stream position of the first.
+// tail[0] = the largest count, tail[1] != 0 if a path drew past the budget
+// before it was deferred.
+__global__ void __launch_bounds__(kBlock)
+tail_rank_kernel(Render_Params p, uint32_t chunk_pixels, Path_State ps, uint32_t* __restrict__ list,
+                 uint32_t* __restrict__ deferred_count, uint32_t* __restrict__ stream_pos, uint32_t* __restrict__ tail) {
+    const uint32_t spp = (uint32_t)p.spp;
+    const uint32_t table_draws = 2u * spp + (uint32_t)p.n1d * (2u * spp - 1u) + (uint32_t)p.n2d * (3u * spp - 1u);
+    for (uint32_t lp = blockIdx.x * blockDim.x + threadIdx.x; lp < chunk_pixels; lp += gridDim.x * blockDim.x) {
+        uint32_t n = 0, stray = 0;
+        for (uint32_t k = 0; k < spp; k++) {
+            const uint32_t slot = lp * spp + k;
+            if (ps.info[slot] & kDeferred) list[slot - k + n++] = slot;
+            stray |= ps.rng_draws[slot];
+        }
+        deferred_count[lp] = n;
+        stream_pos[lp] = table_draws;
+        if (n) atomicMax(&tail[0], n);
+        if (stray) atomicOr(&tail[1], 1u);
+    }
+}
+
+// Wave `wave`: advances each pixel's stream position past its previous
+// wave's draws and queues its next deferred sample as extend queue 0
+// (count in counters[0]) with the pcg state at that position.
+__global__ void __launch_bounds__(kBlock)
+tail_wave_kernel(Render_Params p, uint32_t chunk_first, uint32_t chunk_pixels, uint32_t wave, Path_State ps, Queues q,
+                 const uint32_t* __restrict__ list, const uint32_t* __restrict__ deferred_count,
+                 uint32_t* __restrict__ stream_pos) {
+    for (uint32_t base = blockIdx.x * blockDim.x; base < chunk_pixels; base += gridDim.x * blockDim.x) {
+        const uint32_t lp = base + threadIdx.x;
+        bool take = false;
+        uint32_t slot = 0;
+        if (lp < chunk_pixels) {
+            const uint32_t n = deferred_count[lp];
+            const size_t row = (size_t)lp * (uint32_t)p.spp;
+            uint32_t pos = stream_pos[lp];
+            if (wave > 0 && wave <= n) {
+                pos += ps.rng_draws[list[row + wave - 1]];
+                stream_pos[lp] = pos;
+            }
+            if (wave < n) {
+                take = true;
+                slot = list[row + wave];
+                int x, y;
+                Pcg r = pixel_pcg(p, pixel_stream(p, chunk_first + lp, x, y));
+                pcg_advance(r, pos);
+                ps.rng[slot] = make_uint4((uint32_t)r.state, (uint32_t)(r.state >> 32), (uint32_t)r.inc,
+                                          (uint32_t)(r.inc >> 32));
+                ps.rng_draws[slot] = 0u;
+            }
+        }
+        const uint32_t at = warp_append(&q.counters[0], take);
+        if (take) {
+            q.ext_rays[0][2 * (size_t)at] = ps.deferred[2 * (size_t)slot];
+            q.ext_rays[0][2 * (size_t)at + 1] = ps.deferred[2 * (size_t)slot + 1];
+            q.ext_slot[0][at] = slot;
+        }
+    }
 }
 
 // ---------------------------------------------------------------- film
