@@ -160,7 +160,27 @@ typedef struct yar_material_desc {
     uint32_t components[5];
     int32_t mix_materials[2];   /* mix: the two materials, indices into yar_flat_scene::materials */
     float mix_amount[3];        /* mix */
+    /* Image textures (RGB_Parameter in value mode with a texture leaf,
+       src/lib/material_parameter.h): the texture of `reflectance` and its uv
+       scale.  0: the constant above; k > 0: yar_flat_scene::textures[k - 1]. */
+    uint32_t reflectance_texture;
+    float reflectance_uv_scale[2];
+    uint32_t other_textured_parameters;  /* parameters given by textures the library does not evaluate */
 } yar_material_desc;
+
+/* Image_Texture (src/ref/image_texture.h) as the reference builds it from the
+ * file: the base level (scaled, decoded from sRGB, upsampled to powers of two)
+ * and its mip chain.  Mips are listed level 0 first in
+ * yar_flat_scene::texture_mips; texels are RGB float triples, row 0 first. */
+typedef struct yar_texture_desc {
+    uint32_t first_mip;   /* index into texture_mips */
+    uint32_t mip_count;
+} yar_texture_desc;
+
+typedef struct yar_texture_mip_desc {
+    uint32_t width, height;   /* powers of two */
+    uint64_t texel_offset;    /* into yar_flat_scene::texels, in texels (3 floats each) */
+} yar_texture_mip_desc;
 
 /* Pbrt3_Uber_Material component kinds (src/lib/material_pbrt.h) */
 #define YAR_UBER_DIFFUSE            0
@@ -274,6 +294,11 @@ typedef struct yar_flat_scene {
     uint32_t sphere_light_count;    /* sphere lights */
     const yar_sphere_light_desc* sphere_lights;
     const yar_environment_desc* environment;  /* NULL: no environment light */
+    uint32_t texture_count;         /* image textures */
+    const yar_texture_desc* textures;
+    uint32_t texture_mip_count;
+    const yar_texture_mip_desc* texture_mips;
+    const float* texels;            /* RGB triples of every mip */
 } yar_flat_scene;
 
 /* One ray of a batch: 32 bytes, two float4.  tmax plays the role of the

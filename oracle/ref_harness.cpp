@@ -101,8 +101,15 @@ Matrix3x4 floats_to_matrix(const float in[12]) {
     return m;
 }
 
+// Parameters of the material being flattened that a texture gives and the
+// library does not evaluate (counted into yar_material_desc::other_textured_parameters).
+static uint32_t g_textured_parameters = 0;
+
 bool constant_rgb(const Parameter& p, float out[3]) {
-    if (p.eval_mode != EvaluationMode::value || !p.value.is_constant) return false;
+    if (p.eval_mode != EvaluationMode::value || !p.value.is_constant) {
+        if (p.eval_mode != EvaluationMode::none) g_textured_parameters++;
+        return false;
+    }
     out[0] = p.value.constant.r;
     out[1] = p.value.constant.g;
     out[2] = p.value.constant.b;
@@ -114,6 +121,16 @@ bool constant_float(const Parameter& p, float* out) {
     if (!constant_rgb(p, c)) return false;
     *out = c[0];
     return true;
+}
+
+void note_bump(const Parameter& bump_map) {
+    if (bump_map.eval_mode != EvaluationMode::none) g_textured_parameters++;
+}
+
+void push_material(yfs::Scene& out, yar_material_desc d) {
+    d.other_textured_parameters = g_textured_parameters;
+    g_textured_parameters = 0;
+    out.materials.push_back(d);
 }
 
 Scene load_with_overrides(const Args& a) {
@@ -170,13 +187,21 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
     std::vector<int> diffuse_index, metal_index, glass_index;
     for (const Diffuse_Material& m : ctx.materials.diffuse) {
         yar_material_desc d{};
+        note_bump(m.bump_map);
         d.type = YAR_MATERIAL_DIFFUSE;
-        if (!constant_rgb(m.reflectance, d.reflectance)) fprintf(stderr, "warning: textured diffuse reflectance\n");
+        if (m.reflectance.eval_mode == EvaluationMode::value && !m.reflectance.value.is_constant) {
+            d.reflectance_texture = (uint32_t)m.reflectance.value.texture.texture_index + 1u;
+            d.reflectance_uv_scale[0] = m.reflectance.value.texture.u_scale;
+            d.reflectance_uv_scale[1] = m.reflectance.value.texture.v_scale;
+        } else {
+            constant_rgb(m.reflectance, d.reflectance);
+        }
         diffuse_index.push_back((int)out.materials.size());
-        out.materials.push_back(d);
+        push_material(out, d);
     }
     for (const Metal_Material& m : ctx.materials.metal) {
         yar_material_desc d{};
+        note_bump(m.bump_map);
         d.type = YAR_MATERIAL_METAL;
         constant_float(m.u_roughness, &d.u_roughness);
         constant_float(m.v_roughness, &d.v_roughness);
@@ -185,10 +210,11 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         constant_rgb(m.k, d.k);
         d.roughness_is_alpha = m.roughness_is_alpha ? 1 : 0;
         metal_index.push_back((int)out.materials.size());
-        out.materials.push_back(d);
+        push_material(out, d);
     }
     for (const Glass_Material& m : ctx.materials.glass) {
         yar_material_desc d{};
+        note_bump(m.bump_map);
         d.type = YAR_MATERIAL_GLASS;
         constant_rgb(m.reflectance, d.reflectance);
         constant_rgb(m.transmittance, d.transmittance);
@@ -197,12 +223,13 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         d.v_roughness = d.u_roughness;
         d.roughness_is_alpha = m.roughness_is_alpha ? 1 : 0;
         glass_index.push_back((int)out.materials.size());
-        out.materials.push_back(d);
+        push_material(out, d);
     }
     // plastic and coated diffuse: reflectance = diffuse reflectance, transmittance = r0
     std::vector<int> plastic_index, coated_index;
     for (const Plastic_Material& m : ctx.materials.plastic) {
         yar_material_desc d{};
+        note_bump(m.bump_map);
         d.type = YAR_MATERIAL_PLASTIC;
         constant_rgb(m.diffuse_reflectance, d.reflectance);
         float r0 = 0.f;
@@ -212,10 +239,11 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         d.v_roughness = d.u_roughness;
         d.roughness_is_alpha = m.roughness_is_alpha ? 1 : 0;
         plastic_index.push_back((int)out.materials.size());
-        out.materials.push_back(d);
+        push_material(out, d);
     }
     for (const Coated_Diffuse_Material& m : ctx.materials.coated_diffuse) {
         yar_material_desc d{};
+        note_bump(m.bump_map);
         d.type = YAR_MATERIAL_COATED_DIFFUSE;
         constant_rgb(m.diffuse_reflectance, d.reflectance);
         constant_rgb(m.r0, d.transmittance);
@@ -223,36 +251,40 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         constant_float(m.v_roughness, &d.v_roughness);
         d.roughness_is_alpha = m.roughness_is_alpha ? 1 : 0;
         coated_index.push_back((int)out.materials.size());
-        out.materials.push_back(d);
+        push_material(out, d);
     }
     std::vector<int> reflector_index, refractor_index;
     for (const Perfect_Reflector_Material& m : ctx.materials.perfect_reflector) {
         yar_material_desc d{};
+        note_bump(m.bump_map);
         d.type = YAR_MATERIAL_PERFECT_REFLECTOR;
         constant_rgb(m.reflectance, d.reflectance);
         reflector_index.push_back((int)out.materials.size());
-        out.materials.push_back(d);
+        push_material(out, d);
     }
     for (const Perfect_Refractor_Material& m : ctx.materials.perfect_refractor) {
         yar_material_desc d{};
+        note_bump(m.bump_map);
         d.type = YAR_MATERIAL_PERFECT_REFRACTOR;
         constant_float(m.index_of_refraction, &d.index_of_refraction);
         refractor_index.push_back((int)out.materials.size());
-        out.materials.push_back(d);
+        push_material(out, d);
     }
     // diffuse transmission: reflectance, transmittance, diffuse = scale
     std::vector<int> transmission_index, translucent_index, uber_index, mix_index;
     for (const Diffuse_Transmission_Material& m : ctx.materials.diffuse_transmission) {
         yar_material_desc d{};
+        note_bump(m.bump_map);
         d.type = YAR_MATERIAL_DIFFUSE_TRANSMISSION;
         constant_rgb(m.reflectance, d.reflectance);
         constant_rgb(m.transmittance, d.transmittance);
         constant_rgb(m.scale, d.diffuse);
         transmission_index.push_back((int)out.materials.size());
-        out.materials.push_back(d);
+        push_material(out, d);
     }
     for (const Pbrt3_Translucent_Material& m : ctx.materials.pbrt3_translucent) {
         yar_material_desc d{};
+        note_bump(m.bump_map);
         d.type = YAR_MATERIAL_PBRT3_TRANSLUCENT;
         constant_rgb(m.reflectance, d.reflectance);
         constant_rgb(m.transmittance, d.transmittance);
@@ -261,11 +293,12 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         constant_float(m.roughness, &d.u_roughness);
         d.v_roughness = d.u_roughness;
         translucent_index.push_back((int)out.materials.size());
-        out.materials.push_back(d);
+        push_material(out, d);
     }
     // pbrt3 uber: reflectance = Kd, transmittance = Kt
     for (const Pbrt3_Uber_Material& m : ctx.materials.pbrt3_uber) {
         yar_material_desc d{};
+        note_bump(m.bump_map);
         d.type = YAR_MATERIAL_PBRT3_UBER;
         constant_rgb(m.diffuse_reflectance, d.reflectance);
         constant_rgb(m.specular_reflectance, d.specular);
@@ -278,7 +311,7 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         d.component_count = m.component_count;
         for (int k = 0; k < m.component_count; k++) d.components[k] = (uint32_t)m.components[k];
         uber_index.push_back((int)out.materials.size());
-        out.materials.push_back(d);
+        push_material(out, d);
     }
     for (size_t i = 0; i < ctx.materials.mix.size(); i++) {
         mix_index.push_back((int)out.materials.size() + (int)i);
@@ -306,7 +339,7 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         d.mix_materials[0] = flat_index(m.material1);
         d.mix_materials[1] = flat_index(m.material2);
         constant_rgb(m.mix_amount, d.mix_amount);
-        out.materials.push_back(d);
+        push_material(out, d);
     }
     for (const Scene_Object& o : scene.objects) {
         yar_object_desc d{};
@@ -391,6 +424,27 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         out.environment.height = (uint32_t)map.height;
         out.environment_radiance.resize(3 * map.data.size());
         memcpy(out.environment_radiance.data(), map.data.data(), out.environment_radiance.size() * sizeof(float));
+    }
+    // image textures, when a flattened material reads one: every texture of the
+    // scene context (indices stay the reference's), each with its mip chain
+    bool textured = false;
+    for (const yar_material_desc& d : out.materials) textured = textured || d.reflectance_texture != 0;
+    for (size_t ti = 0; textured && ti < ctx.textures.size(); ti++) {
+        const std::vector<Image>& mips = ctx.textures[ti].get_mips();
+        yar_texture_desc td{};
+        td.first_mip = (uint32_t)out.texture_mips.size();
+        td.mip_count = (uint32_t)mips.size();
+        for (const Image& im : mips) {
+            yar_texture_mip_desc md{};
+            md.width = (uint32_t)im.width;
+            md.height = (uint32_t)im.height;
+            md.texel_offset = out.texels.size() / 3;
+            out.texture_mips.push_back(md);
+            const size_t at = out.texels.size();
+            out.texels.resize(at + 3 * im.data.size());
+            memcpy(out.texels.data() + at, im.data.data(), 3 * im.data.size() * sizeof(float));
+        }
+        out.textures.push_back(td);
     }
     out.other_light_count = (uint32_t)(ctx.lights.total_light_count - (int)ctx.lights.diffuse_rectangular_lights.size() -
                                        (int)out.delta_lights.size() - (int)out.mesh_lights.size() -
@@ -681,6 +735,10 @@ int cmd_render_yfs(const Args& a) {
     if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
     if (fs_scene.has_environment) {
         fprintf(stderr, "render-yfs: environment lights are rendered from their pbrt scene only\n");
+        return 1;
+    }
+    if (!fs_scene.textures.empty()) {
+        fprintf(stderr, "render-yfs: textured scenes are rendered from their pbrt scene only\n");
         return 1;
     }
     if (fs_scene.other_light_count) {

@@ -555,6 +555,11 @@ typedef struct shading_ctx {
     int material_index;
     uint32_t light_type;
     int light_index;
+    /* uv parameterization and its screen-space derivatives (zero without differential rays) */
+    int has_uv;
+    float uv[2];
+    v3 dpdu, dpdv;              /* world space */
+    float dudx, dvdx, dudy, dvdy;
 } shading_ctx;
 
 /* adjust_shading_normal, src/ref/shading_context.cpp:17-63 */
@@ -600,12 +605,15 @@ static void init_shading(const yar_flat_scene* s, v3 ray_d, uint32_t object_inde
         if (len2_3(in) != 0) normal = norm3(in);
     }
     int has_uv = 0;
-    v3 dpdu = mk3(0, 0, 0);
+    v3 dpdu = mk3(0, 0, 0), dpdv = mk3(0, 0, 0);
     if (m->uvs) {
         has_uv = 1;
         const float* u0 = m->uvs + 2 * (size_t)vi[0];
         const float* u1 = m->uvs + 2 * (size_t)vi[1];
         const float* u2 = m->uvs + 2 * (size_t)vi[2];
+        /* barycentric_interpolate (src/lib/math.h:146-153) of the vertex uvs */
+        sc->uv[0] = u0[0] * b[0] + u1[0] * b[1] + u2[0] * b[2];
+        sc->uv[1] = u0[1] * b[0] + u1[1] * b[1] + u2[1] * b[2];
         float a00 = u1[0] - u0[0], a01 = u1[1] - u0[1], a10 = u2[0] - u0[0], a11 = u2[1] - u0[1];
         v3 bp0 = sub3(p[1], p[0]), bp1 = sub3(p[2], p[0]);
         /* solve_linear_system_2x2 (src/lib/math.cpp:8-16) */
@@ -613,11 +621,9 @@ static void init_shading(const yar_flat_scene* s, v3 ray_d, uint32_t object_inde
         if (det != 0.f) {
             float inv_det = 1.f / det;
             dpdu = mul3s(sub3(mul3s(bp0, a11), mul3s(bp1, a01)), inv_det);
+            dpdv = mul3s(add3(mul3s(bp0, -a10), mul3s(bp1, a00)), inv_det);
         }
-        if (fabsf(det) < 1e-9f) {
-            v3 dummy;
-            coordinate_system(gn, &dpdu, &dummy);
-        }
+        if (fabsf(det) < 1e-9f) coordinate_system(gn, &dpdu, &dpdv);
     }
     /* to world space */
     position = xform_point(obj->object_to_world, position);
@@ -626,6 +632,10 @@ static void init_shading(const yar_flat_scene* s, v3 ray_d, uint32_t object_inde
     gn = xform_vector(obj->object_to_world_normal, gn);
     gn = div3s(gn, len3(gn));
     dpdu = xform_vector(obj->object_to_world, dpdu);
+    dpdv = xform_vector(obj->object_to_world, dpdv);
+    sc->has_uv = has_uv;
+    sc->dpdu = dpdu;
+    sc->dpdv = dpdv;
     if (dot3(normal, gn) == 0.f) gn = normal;
     if (dot3(gn, sc->wo) < 0) gn = neg3(gn);
     if (dot3(normal, gn) < 0) { normal = neg3(normal); sc->flipped = 1; }
@@ -709,6 +719,8 @@ static v3 local_to_world(const bsdf_t* f, v3 l) {
 }
 static v3 world_to_local(const bsdf_t* f, v3 w) { return mk3(dot3(w, f->t), dot3(w, f->bt), dot3(w, f->n)); }
 
+static col texture_reflectance(const yar_flat_scene* s, const shading_ctx* sc, const yar_material_desc* m);
+
 static int make_leaf_bsdf(const yar_flat_scene* s, const shading_ctx* sc, uint32_t type, const yar_material_desc* m,
                           bsdf_t* f) {
     memset(f, 0, sizeof(*f));
@@ -718,7 +730,7 @@ static int make_leaf_bsdf(const yar_flat_scene* s, const shading_ctx* sc, uint32
     f->type = type;
     if (f->type == YAR_MATERIAL_DIFFUSE) {
         f->reflection = 1;
-        f->reflectance = ldc(m->reflectance);
+        f->reflectance = m->reflectance_texture ? texture_reflectance(s, sc, m) : ldc(m->reflectance);
     } else if (f->type == YAR_MATERIAL_METAL) {
         f->reflection = 1;
         f->alpha_x = roughness_to_alpha(s, m->u_roughness, m->roughness_is_alpha);
@@ -822,6 +834,164 @@ static float atan2_sample(float y, float x) {
     return g_correctly_rounded_trig ? (float)atan2((double)y, (double)x) : atan2f(y, x);
 }
 static float acos_sample(float x) { return g_correctly_rounded_trig ? (float)acos((double)x) : acosf(x); }
+/* log2 of the EWA footprint: the C library's log2f, or correctly rounded like the device */
+static float log2_lod(float x) { return g_correctly_rounded_trig ? (float)log2((double)x) : log2f(x); }
+
+/* ---------------- image textures (src/ref/image_texture.cpp, src/ref/parameter_evaluation.cpp:10-31) */
+
+/* do_EWA's filter weights (src/ref/image_texture.cpp:503-512), exp(-2 x) over
+ * 256 steps, with the C library's expf [0] or correctly rounded [1] */
+static float g_ewa_weights[2][256];
+static void init_ewa_weights(void) {
+    for (int i = 0; i < 256; i++) {
+        const float x = (float)i / (float)(256 - 1);
+        g_ewa_weights[0][i] = expf(-2.f * x);
+        g_ewa_weights[1][i] = (float)exp((double)(-2.f * x));
+    }
+}
+
+/* get_texel_repeat (image_texture.cpp:386-410): power-of-two mips */
+static col texel_repeat(const yar_flat_scene* s, const yar_texture_mip_desc* mip, int x, int y) {
+    const int w = (int)mip->width, h = (int)mip->height;
+    if (x >= 0) x &= w - 1;
+    else { x %= w; x += (x >> 31) & w; }
+    if (y >= 0) y &= h - 1;
+    else { y %= h; y += (y >> 31) & h; }
+    const float* t = s->texels + 3 * (mip->texel_offset + (uint64_t)y * (uint64_t)w + (uint64_t)x);
+    return mkc(t[0], t[1], t[2]);
+}
+
+/* Image_Texture::sample_bilinear with Wrap_Mode::repeat (image_texture.cpp:436-477) */
+static col texture_bilinear(const yar_flat_scene* s, const yar_texture_mip_desc* mip, float u, float v) {
+    const float x = u * (float)mip->width - 0.5f, y = v * (float)mip->height - 0.5f;
+    const float x_floor = floorf(x), y_floor = floorf(y);
+    const float wx = x - x_floor, wy = y - y_floor;
+    const int x0 = (int)x_floor, y0 = (int)y_floor, x1 = x0 + 1, y1 = y0 + 1;
+    col c = mulcs(texel_repeat(s, mip, x0, y0), (1 - wy) * (1 - wx));
+    c = addc(c, mulcs(texel_repeat(s, mip, x1, y0), (1 - wy) * wx));
+    c = addc(c, mulcs(texel_repeat(s, mip, x0, y1), wy * (1 - wx)));
+    return addc(c, mulcs(texel_repeat(s, mip, x1, y1), wy * wx));
+}
+
+/* do_EWA (image_texture.cpp:501-578): the elliptical Gaussian footprint on one mip */
+static col texture_ewa_level(const yar_flat_scene* s, const yar_texture_mip_desc* mip, float u, float v,
+                             const float a1[2], const float a2[2]) {
+    const float* weights = g_ewa_weights[g_correctly_rounded_trig ? 1 : 0];
+    const float w = (float)mip->width, h = (float)mip->height;
+    u = u * w - 0.5f;
+    v = v * h - 0.5f;
+    const float a1x = a1[0] * w, a1y = a1[1] * h, a2x = a2[0] * w, a2y = a2[1] * h;
+    float A = a1y * a1y + a2y * a2y + 1;
+    float B = -2 * (a1x * a1y + a2x * a2y);
+    float C = a1x * a1x + a2x * a2x + 1;
+    const float F = A * C - 0.25f * B * B;
+    const float inv_F = 1.f / F;
+    A *= inv_F;
+    B *= inv_F;
+    C *= inv_F;
+    const float inv_det = 0.25f * F;
+    const float u_delta = 2 * sqrtf(C * inv_det);
+    const float x0 = ceilf(u - u_delta), x1 = floorf(u + u_delta);
+    const float v_delta = 2 * sqrtf(A * inv_det);
+    const float y0 = ceilf(v - v_delta), y1 = floorf(v + v_delta);
+    col sum = mkc(0, 0, 0);
+    float weight_sum = 0.f;
+    for (float y = y0; y <= y1; y++) {
+        const float yy = y - v;
+        for (float x = x0; x <= x1; x++) {
+            const float xx = x - u;
+            const float r2 = A * xx * xx + B * xx * yy + C * yy * yy;
+            if (r2 < 1.f) {
+                const float wt = weights[(int)(r2 * 256)];
+                sum = addc(sum, mulcs(texel_repeat(s, mip, (int)x, (int)y), wt));
+                weight_sum += wt;
+            }
+        }
+    }
+    return mulcs(sum, 1.f / weight_sum);
+}
+
+/* Image_Texture::sample_EWA (image_texture.cpp:580-615), max anisotropy 32 */
+static col texture_ewa(const yar_flat_scene* s, const yar_texture_desc* t, float u, float v, float a1[2], float a2[2]) {
+    const yar_texture_mip_desc* mips = s->texture_mips + t->first_mip;
+    float l1 = a1[0] * a1[0] + a1[1] * a1[1], l2 = a2[0] * a2[0] + a2[1] * a2[1];
+    if (l1 < l2) {
+        float tmp[2] = {a1[0], a1[1]};
+        a1[0] = a2[0]; a1[1] = a2[1];
+        a2[0] = tmp[0]; a2[1] = tmp[1];
+        const float tl = l1; l1 = l2; l2 = tl;
+    }
+    const float major_length = sqrtf(l1);
+    float minor_length = sqrtf(l2);
+    if (minor_length < 1e-6f) return texture_bilinear(s, &mips[0], u, v);
+    if (minor_length * 32.f < major_length) {
+        const float scale = major_length / (minor_length * 32.f);
+        minor_length *= scale;
+        a2[0] *= scale;
+        a2[1] *= scale;
+    }
+    const float lod = fmaxf_std(0.f, (float)((int)t->mip_count - 1) + log2_lod(minor_length));
+    float lod_floor;
+    const float frac = modff(lod, &lod_floor);
+    const int level0 = (int)lod_floor;
+    if (level0 >= (int)t->mip_count - 1) {
+        const float* c = s->texels + 3 * mips[t->mip_count - 1].texel_offset;
+        return mkc(c[0], c[1], c[2]);
+    }
+    const col c0 = texture_ewa_level(s, &mips[level0], u, v, a1, a2);
+    const col c1 = texture_ewa_level(s, &mips[level0 + 1], u, v, a1, a2);
+    return addc(mulcs(c0, 1.f - frac), mulcs(c1, frac));  /* lerp, src/lib/math.h:82-85 */
+}
+
+/* evaluate_texture_parameter (parameter_evaluation.cpp:10-31): uv and its
+ * derivatives scaled, then EWA with repeat wrapping */
+static col texture_reflectance(const yar_flat_scene* s, const shading_ctx* sc, const yar_material_desc* m) {
+    const yar_texture_desc* t = &s->textures[m->reflectance_texture - 1];
+    const float su = m->reflectance_uv_scale[0], sv = m->reflectance_uv_scale[1];
+    float a1[2] = {sc->dudx * su, sc->dvdx * sv}, a2[2] = {sc->dudy * su, sc->dvdy * sv};
+    return texture_ewa(s, t, sc->uv[0] * su, sc->uv[1] * sv, a1, a2);
+}
+
+/* ray_plane_intersection, src/lib/math.cpp:27-31 */
+static float ray_plane_t(v3 o, v3 d, v3 n, float plane_d) {
+    const float k = -dot3(o, n) - plane_d;
+    if (k == 0) return 0.f;
+    return k / dot3(d, n);
+}
+
+/* Shading_Context::calculate_dxdy_derivatives + calculate_uv_derivates
+ * (src/ref/shading_context.cpp:242-333) for differential rays from origin o */
+static void uv_derivatives(shading_ctx* sc, v3 o, v3 dx_dir, v3 dy_dir) {
+    if (!sc->has_uv) return;
+    const v3 gn = sc->geometric_normal;
+    const float plane_d = -dot3(gn, sc->position);
+    v3 dpdx = mk3(0, 0, 0), dpdy = mk3(0, 0, 0);
+    const float tx = ray_plane_t(o, dx_dir, gn, plane_d);
+    if (fabsf(tx) != INFINITY) dpdx = sub3(add3(o, mul3s(dx_dir, tx)), sc->position);
+    const float ty = ray_plane_t(o, dy_dir, gn, plane_d);
+    if (fabsf(ty) != INFINITY) dpdy = sub3(add3(o, mul3s(dy_dir, ty)), sc->position);
+    int dim0, dim1;
+    {
+        const float ax = fabsf(gn.x), ay = fabsf(gn.y), az = fabsf(gn.z);
+        if (ax > ay && ax > az) { dim0 = 1; dim1 = 2; }
+        else if (ay > az) { dim0 = 0; dim1 = 2; }
+        else { dim0 = 0; dim1 = 1; }
+    }
+    const float pu[3] = {sc->dpdu.x, sc->dpdu.y, sc->dpdu.z}, pv[3] = {sc->dpdv.x, sc->dpdv.y, sc->dpdv.z};
+    const float px[3] = {dpdx.x, dpdx.y, dpdx.z}, py[3] = {dpdy.x, dpdy.y, dpdy.z};
+    const float a00 = pu[dim0], a01 = pv[dim0], a10 = pu[dim1], a11 = pv[dim1];
+    const float det = a00 * a11 - a01 * a10;  /* solve_linear_system_2x2, src/lib/math.cpp:8-16 */
+    sc->dudx = sc->dvdx = sc->dudy = sc->dvdy = 0.f;
+    if (det != 0.f) {
+        const float inv_det = 1.f / det;
+        sc->dudx = (a11 * px[dim0] - a01 * px[dim1]) * inv_det;
+        sc->dvdx = (-a10 * px[dim0] + a00 * px[dim1]) * inv_det;
+        sc->dudy = (a11 * py[dim0] - a01 * py[dim1]) * inv_det;
+        sc->dvdy = (-a10 * py[dim0] + a00 * py[dim1]) * inv_det;
+    }
+    if (fabsf(sc->dudx) > 1e9f || fabsf(sc->dvdx) > 1e9f || fabsf(sc->dudy) > 1e9f || fabsf(sc->dvdy) > 1e9f)
+        sc->dudx = sc->dvdx = sc->dudy = sc->dvdy = 0.f;
+}
 
 static v3 sample_hemisphere_cosine(float u0, float u1) {
     float z = sqrtf(1.f - u0);
@@ -2001,7 +2171,7 @@ static int emitted_radiance(const yar_flat_scene* s, const shading_ctx* sc, col*
 
 /* trace_path, src/ref/path_tracing.cpp:11-133 */
 static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_samplers, const env_sampler* env,
-                      v3 ro, v3 rd, sampler_view* sv, col* radiance) {
+                      v3 ro, v3 rd, const v3 differential_dirs[2], sampler_view* sv, col* radiance) {
     const yar_render_config* cfg = &s->config;
     const int total_lights = (int)(s->delta_light_count + s->rect_light_count + s->sphere_light_count +
                                    s->mesh_light_count + (env->e ? 1 : 0) + s->other_light_count);
@@ -2017,6 +2187,8 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
             hit = trace_closest(s, ro, rd, &h);
             if (hit < 0) return YAR_ERR_CAPACITY;
             if (hit) init_shading(s, rd, h.object, h.prim, h.b, &sc);
+            /* the camera ray's differential rays (trace_ray at bounce 0, path_tracing.cpp:25) */
+            if (hit && bounce == 0) uv_derivatives(&sc, ro, differential_dirs[0], differential_dirs[1]);
             if (bounce == 0) {
                 if (hit && emitted_radiance(s, &sc, &le)) L = addc(L, mulc(coeff, le));
                 else if (!hit && env->e) L = addc(L, mulc(coeff, env_radiance(env, rd, 1)));
@@ -2352,7 +2524,17 @@ static int render_tile(render_job* J, int t) {
                     }
                     rc = trace_direct(s, &J->env, o, d, &da, &rng, &radiance);
                 } else {
-                    rc = trace_path(s, J->mesh_samplers, &J->env, o, d, &sv, &radiance);
+                    /* differential rays one pixel over, scaled to the sample's footprint
+                     * (src/ref/reference_renderer.cpp:367-378) */
+                    v3 dd[2], ox;
+                    camera_ray(&s->camera, fx + 1.f, fy, &ox, &dd[0]);
+                    camera_ray(&s->camera, fx, fy + 1.f, &ox, &dd[1]);
+                    const float dscale = 1.f / sqrtf((float)spp);
+                    for (int q = 0; q < 2; q++) {
+                        dd[q] = add3(d, mul3s(sub3(dd[q], d), dscale));
+                        dd[q] = div3s(dd[q], len3(dd[q]));
+                    }
+                    rc = trace_path(s, J->mesh_samplers, &J->env, o, d, dd, &sv, &radiance);
                 }
                 if (rc != YAR_OK) break;
                 float limit = cfg->max_rgb_component_value_of_film_sample;
@@ -2434,6 +2616,24 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
             return YAR_ERR_UNSUPPORTED;
     }
     if (s->other_light_count) return YAR_ERR_UNSUPPORTED;
+    /* image textures: a diffuse reflectance with camera-ray differentials in the
+     * path tracer; no delta materials (their differential rays are not restated) */
+    int textured = 0, delta_materials = 0;
+    for (uint32_t i = 0; i < s->material_count; i++) {
+        const yar_material_desc* m = &s->materials[i];
+        if (m->other_textured_parameters) return YAR_ERR_UNSUPPORTED;
+        if (m->reflectance_texture) {
+            if (m->type != YAR_MATERIAL_DIFFUSE || m->reflectance_texture > s->texture_count) return YAR_ERR_UNSUPPORTED;
+            const yar_texture_desc* t = &s->textures[m->reflectance_texture - 1];
+            if (t->mip_count == 0 || t->first_mip + t->mip_count > s->texture_mip_count) return YAR_ERR_INVALID;
+            textured = 1;
+        }
+        delta_materials |= m->type == YAR_MATERIAL_PERFECT_REFLECTOR || m->type == YAR_MATERIAL_PERFECT_REFRACTOR ||
+                           (m->type == YAR_MATERIAL_GLASS && !(m->u_roughness > 0.f)) ||
+                           m->type == YAR_MATERIAL_PBRT3_UBER || m->type == YAR_MATERIAL_MIX;
+    }
+    if (textured && (cfg->rendering_algorithm == 0 || delta_materials)) return YAR_ERR_UNSUPPORTED;
+    init_ewa_weights();
     for (uint32_t i = 0; i < s->material_count; i++) {
         const yar_material_desc* m = &s->materials[i];
         if (m->type == YAR_MATERIAL_MIX) {

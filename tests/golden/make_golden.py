@@ -60,6 +60,10 @@ Fixtures
   cornell_envmap_64.yfs / .npz  the delta-box Cornell box with an "infinite"
                              light of a 64 x 32 sky map with a sun (written by
                              yar_gb300.exr), seed 13.
+  cornell_texture_64.yfs / .npz  GGX boxes, the back wall, the left wall and
+                             the floor lit with pbrt "imagemap" textures of a
+                             48 x 40 checker image (uv scale 1 and 2 x 3;
+                             EWA filtering with camera-ray differentials), seed 17.
   cornell_direct_64.yfs / .npz  the reference's direct-lighting algorithm
                              (pbrt "directlighting"): GGX boxes, the quad light
                              with 4 samples (2 x 2 arrays), point, spot and
@@ -322,6 +326,20 @@ def cornell_envmap_64():
     np.savez_compressed(os.path.join(HERE, "cornell_envmap_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def cornell_texture_64():
+    from yar_gb300 import exr
+    with tempfile.TemporaryDirectory() as d:
+        exr.write_exr(os.path.join(d, "checks.exr"), scenes.texture_image(), False, {})
+        pbrt = os.path.join(d, "cornell_texture.pbrt")
+        texs = scenes.texture_statements("checks.exr") + scenes.texture_statements("checks.exr", "fine", 2.0, 3.0)
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=17, width=64, height=64, spp=16, maxdepth=8,
+                                                  box_materials=scenes.GGX_BOXES, textures=texs,
+                                                  wall_textures={2: "checks", 3: "fine", 0: "fine"}))
+        oracle.ref_flatten(pbrt, os.path.join(HERE, "cornell_texture_64.yfs"), seed_offset=1)
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_texture_64.npz"), image=img, variance=np.float64(info["variance"]))
+
+
 def cornell_direct_64():
     _pbrt_golden("cornell_direct_64", 15, box_materials=scenes.GGX_BOXES, light_sources=scenes.DELTA_LIGHTS,
                  light_samples=4, integrator="directlighting")
@@ -409,7 +427,7 @@ if __name__ == "__main__":
                              "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64",
                              "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64",
                              "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64",
-                             "cornell_direct_64", "cornell_direct_env_64", "checkpoint_c1",
+                             "cornell_direct_64", "cornell_direct_env_64", "cornell_texture_64", "checkpoint_c1",
                              "exr_files",
                              "kdtree_cache_files"]
     for name in which:

@@ -46,7 +46,7 @@ def test_struct_sizes_match_the_header():
     from yar_gb300 import native
     assert ctypes.sizeof(native.KdNode) == 8
     assert ctypes.sizeof(native.ObjectDesc) == 164
-    assert ctypes.sizeof(native.MaterialDesc) == 164
+    assert ctypes.sizeof(native.MaterialDesc) == 180
     assert ctypes.sizeof(native.RectLightDesc) == 72
 
 
@@ -62,7 +62,8 @@ def test_struct_layouts_match_the_c_compiler(tmp_path):
                "yar_rect_light_desc": native.RectLightDesc, "yar_delta_light_desc": native.DeltaLightDesc,
                "yar_mesh_light_desc": native.MeshLightDesc, "yar_sphere_light_desc": native.SphereLightDesc,
                "yar_camera_desc": native.CameraDesc, "yar_render_config": native.RenderConfig,
-               "yar_flat_scene": native.FlatSceneDesc}
+               "yar_flat_scene": native.FlatSceneDesc, "yar_texture_desc": native.TextureDesc,
+               "yar_texture_mip_desc": native.TextureMipDesc}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "yar_gpu.h"', "int main(void) {"]
     for name, cls in mirrors.items():
         lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (name, name))

@@ -124,7 +124,8 @@ def test_builder_against_live_reference_large_mesh():
 @pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64",
                                   "cornell_layered_64", "cornell_layered_yar_64", "cornell_lights_64",
                                   "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64",
-                                  "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64"])
+                                  "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64",
+                                  "cornell_texture_64"])
 def test_oracle_render_matches_reference_golden(name):
     """The oracle's path loop, sampler, shading, BSDFs (diffuse, GGX metal, rough
     glass, plastic in both of the reference's forms, coated diffuse), delta
@@ -180,3 +181,33 @@ def test_oracle_correctly_rounded_trig_changes_only_the_trig():
     img, var = oracle.render(s, threads=4)
     assert np.array_equal(bits(img), bits(g["image"]))
     assert var == float(g["variance"])
+
+
+def test_texture_scene_file_round_trip(tmp_path):
+    """The TEXS chunk (texture records, mip records, texels) and the material
+    records' texture fields survive a write and a read."""
+    s = FlatScene.read(golden("cornell_texture_64.yfs"))
+    assert s.textures.shape[0] == 1 and s.texture_mips.shape[0] == 7
+    assert int(s.texture_mips["width"][0]) == 64 and int(s.texture_mips["texel_offset"][-1]) == 5460
+    p = tmp_path / "t.yfs"
+    s.write(str(p))
+    t = FlatScene.read(str(p))
+    assert np.array_equal(t.textures, s.textures) and np.array_equal(t.texture_mips, s.texture_mips)
+    assert np.array_equal(t.texels, s.texels) and np.array_equal(t.materials, s.materials)
+    assert sorted(int(x) for x in s.materials["reflectance_texture"]) == [0, 0, 0, 0, 1, 1]
+
+
+def test_textured_scenes_outside_the_restated_part_are_refused():
+    """Image textures are restated for diffuse reflectance in the path tracer
+    with camera-ray differentials; with the direct-lighting algorithm, next to
+    delta materials, or on other parameters the oracle refuses the scene."""
+    for change in ("direct", "mirror", "other"):
+        s = FlatScene.read(golden("cornell_texture_64.yfs"))
+        if change == "direct":
+            s.config["rendering_algorithm"] = 0
+        elif change == "mirror":
+            s.materials["type"][-1] = 0  # perfect reflector
+        else:
+            s.materials["other_textured_parameters"][-1] = 1
+        with pytest.raises(Exception):
+            oracle.render(s, threads=2)

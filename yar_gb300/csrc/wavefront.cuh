@@ -1715,6 +1715,8 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
             return fail(ctx, YAR_ERR_INVALID, "point, spot and directional lights must be listed in that order");
     }
     for (const yar_material_desc& m : R.host_materials) {
+        if (m.reflectance_texture || m.other_textured_parameters)
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "image textures are not implemented on the device");
         if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL && m.type != YAR_MATERIAL_GLASS &&
             m.type != YAR_MATERIAL_PLASTIC && m.type != YAR_MATERIAL_COATED_DIFFUSE &&
             m.type != YAR_MATERIAL_PERFECT_REFLECTOR && m.type != YAR_MATERIAL_PERFECT_REFRACTOR &&

@@ -4,7 +4,8 @@
 // kd-trees (node words bit for bit as KdTree::save writes them,
 // src/ref/kdtree.cpp:137-160), scene objects, the scene kd-tree, constant
 // materials, rectangular lights, point/spot/directional, triangle-mesh,
-// sphere and environment lights (optional chunks), camera and Raytracer_Config.  It is produced
+// sphere and environment lights and image textures (optional chunks), camera
+// and Raytracer_Config.  It is produced
 // by the host scene loader of this library and by the reference-side adapter
 // that flattens a reference Scene_Context, so both sides can be compared on
 // identical bytes.
@@ -49,6 +50,9 @@ struct Scene {
     bool has_environment = false;
     yar_environment_desc environment{};   // radiance points into environment_radiance
     std::vector<float> environment_radiance;
+    std::vector<yar_texture_desc> textures;
+    std::vector<yar_texture_mip_desc> texture_mips;
+    std::vector<float> texels;           // RGB triples
     uint32_t other_light_count = 0;
     yar_camera_desc camera{};
     yar_render_config config{};
@@ -97,6 +101,11 @@ struct Scene {
         s.sphere_lights = sphere_lights.empty() ? nullptr : sphere_lights.data();
         environment.radiance = environment_radiance.data();
         s.environment = has_environment ? &environment : nullptr;
+        s.texture_count = (uint32_t)textures.size();
+        s.textures = textures.empty() ? nullptr : textures.data();
+        s.texture_mip_count = (uint32_t)texture_mips.size();
+        s.texture_mips = texture_mips.empty() ? nullptr : texture_mips.data();
+        s.texels = texels.empty() ? nullptr : texels.data();
         return s;
     }
 };
@@ -224,6 +233,18 @@ inline bool write(const std::string& path, const Scene& s) {
         b.raw(s.environment_radiance.data(), s.environment_radiance.size() * sizeof(float));
         w.chunk("ENVM", b.b);
     }
+    if (!s.textures.empty()) {  // TEXS: counts, texture records, mip records, texels
+        detail::Buf b;
+        const uint32_t nt = (uint32_t)s.textures.size(), nm = (uint32_t)s.texture_mips.size();
+        const uint64_t nx = s.texels.size() / 3;
+        b.pod(nt);
+        b.pod(nm);
+        b.pod(nx);
+        b.raw(s.textures.data(), nt * sizeof(yar_texture_desc));
+        b.raw(s.texture_mips.data(), nm * sizeof(yar_texture_mip_desc));
+        b.raw(s.texels.data(), s.texels.size() * sizeof(float));
+        w.chunk("TEXS", b.b);
+    }
     bool ok = w.ok;
     if (fclose(f) != 0) ok = false;
     return ok;
@@ -322,6 +343,18 @@ inline bool read(const std::string& path, Scene& s, std::string* err = nullptr) 
             if ((uint64_t)n * sizeof(yar_sphere_light_desc) > size) return fail("bad sphere light chunk");
             s.sphere_lights.resize(n);
             c.raw(s.sphere_lights.data(), n * sizeof(yar_sphere_light_desc));
+        } else if (!memcmp(tag, "TEXS", 4)) {
+            const uint32_t nt = c.pod<uint32_t>(), nm = c.pod<uint32_t>();
+            const uint64_t nx = c.pod<uint64_t>();
+            if (!c.ok || (uint64_t)nt * sizeof(yar_texture_desc) + (uint64_t)nm * sizeof(yar_texture_mip_desc) +
+                                 nx * 12 > size)
+                return fail("bad texture chunk");
+            s.textures.resize(nt);
+            c.raw(s.textures.data(), nt * sizeof(yar_texture_desc));
+            s.texture_mips.resize(nm);
+            c.raw(s.texture_mips.data(), nm * sizeof(yar_texture_mip_desc));
+            s.texels.resize(nx * 3);
+            c.raw(s.texels.data(), s.texels.size() * sizeof(float));
         } else if (!memcmp(tag, "ENVM", 4)) {
             s.environment = c.pod<yar_environment_desc>();
             const uint64_t count = 3ull * s.environment.width * s.environment.height;

@@ -74,7 +74,9 @@ class MaterialDesc(C.Structure):
                 ("index_of_refraction", C.c_float), ("roughness_is_alpha", C.c_int32),
                 ("specular", C.c_float * 3), ("diffuse", C.c_float * 3), ("delta_reflectance", C.c_float * 3),
                 ("opacity", C.c_float * 3), ("component_count", C.c_uint32), ("components", C.c_uint32 * 5),
-                ("mix_materials", C.c_int32 * 2), ("mix_amount", C.c_float * 3)]
+                ("mix_materials", C.c_int32 * 2), ("mix_amount", C.c_float * 3),
+                ("reflectance_texture", C.c_uint32), ("reflectance_uv_scale", C.c_float * 2),
+                ("other_textured_parameters", C.c_uint32)]
 
 
 class RectLightDesc(C.Structure):
@@ -118,6 +120,14 @@ class EnvironmentDesc(C.Structure):
                 ("radiance", C.c_void_p)]
 
 
+class TextureDesc(C.Structure):
+    _fields_ = [("first_mip", C.c_uint32), ("mip_count", C.c_uint32)]
+
+
+class TextureMipDesc(C.Structure):
+    _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("texel_offset", C.c_uint64)]
+
+
 class FlatSceneDesc(C.Structure):
     _fields_ = [("mesh_count", C.c_uint32), ("meshes", C.POINTER(MeshDesc)),
                 ("object_count", C.c_uint32), ("objects", C.POINTER(ObjectDesc)),
@@ -128,7 +138,10 @@ class FlatSceneDesc(C.Structure):
                 ("delta_light_count", C.c_uint32), ("delta_lights", C.POINTER(DeltaLightDesc)),
                 ("mesh_light_count", C.c_uint32), ("mesh_lights", C.POINTER(MeshLightDesc)),
                 ("sphere_light_count", C.c_uint32), ("sphere_lights", C.POINTER(SphereLightDesc)),
-                ("environment", C.POINTER(EnvironmentDesc))]
+                ("environment", C.POINTER(EnvironmentDesc)),
+                ("texture_count", C.c_uint32), ("textures", C.POINTER(TextureDesc)),
+                ("texture_mip_count", C.c_uint32), ("texture_mips", C.POINTER(TextureMipDesc)),
+                ("texels", C.c_void_p)]
 
 
 class HitSoa(C.Structure):

@@ -22,7 +22,9 @@ MATERIAL_DTYPE = np.dtype([("type", "<u4"), ("reflectance", "<f4", 3), ("transmi
                            ("v_roughness", "<f4"), ("index_of_refraction", "<f4"), ("roughness_is_alpha", "<i4"),
                            ("specular", "<f4", 3), ("diffuse", "<f4", 3), ("delta_reflectance", "<f4", 3),
                            ("opacity", "<f4", 3), ("component_count", "<u4"), ("components", "<u4", 5),
-                           ("mix_materials", "<i4", 2), ("mix_amount", "<f4", 3)])
+                           ("mix_materials", "<i4", 2), ("mix_amount", "<f4", 3),
+                           ("reflectance_texture", "<u4"), ("reflectance_uv_scale", "<f4", 2),
+                           ("other_textured_parameters", "<u4")])
 MATERIAL_RECORD_V1 = 72  # the MATS chunk's records: the fields up to roughness_is_alpha
 LIGHT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("emitted_radiance", "<f4", 3), ("size", "<f4", 2),
                         ("sample_count", "<i4")])
@@ -34,6 +36,8 @@ SPHERE_LIGHT_DTYPE = np.dtype([("position", "<f4", 3), ("emitted_radiance", "<f4
                                ("sample_count", "<i4")])
 ENVIRONMENT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("world_to_light", "<f4", 12), ("scale", "<f4", 3),
                               ("sample_count", "<i4"), ("width", "<u4"), ("height", "<u4"), ("radiance", "<u8")])
+TEXTURE_DTYPE = np.dtype([("first_mip", "<u4"), ("mip_count", "<u4")])
+TEXTURE_MIP_DTYPE = np.dtype([("width", "<u4"), ("height", "<u4"), ("texel_offset", "<u8")])
 CAMERA_DTYPE = np.dtype([("camera_to_world", "<f4", 12), ("image_extent", "<f4", 2), ("horz_half_dist", "<f4"),
                          ("vert_half_dist", "<f4"), ("z_is_up", "<i4")])
 CONFIG_DTYPE = np.dtype([("render_region", "<i4", 4), ("rendering_algorithm", "<i4"), ("max_light_bounces", "<i4"),
@@ -52,6 +56,8 @@ assert MESH_LIGHT_DTYPE.itemsize == C.sizeof(native.MeshLightDesc)
 assert ENVIRONMENT_DTYPE.itemsize == C.sizeof(native.EnvironmentDesc)
 assert SPHERE_LIGHT_DTYPE.itemsize == C.sizeof(native.SphereLightDesc)
 assert CAMERA_DTYPE.itemsize == C.sizeof(native.CameraDesc)
+assert TEXTURE_DTYPE.itemsize == C.sizeof(native.TextureDesc)
+assert TEXTURE_MIP_DTYPE.itemsize == C.sizeof(native.TextureMipDesc)
 assert CONFIG_DTYPE.itemsize == C.sizeof(native.RenderConfig)
 
 IDENTITY = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32)
@@ -107,6 +113,10 @@ class FlatScene:
         self.sphere_lights = np.zeros(0, SPHERE_LIGHT_DTYPE)
         # environment light: None, or (ENVIRONMENT_DTYPE record, (height, width, 3) float32 map)
         self.environment = None
+        # image textures: records, their mips (level 0 first) and every mip's RGB texels
+        self.textures = np.zeros(0, TEXTURE_DTYPE)
+        self.texture_mips = np.zeros(0, TEXTURE_MIP_DTYPE)
+        self.texels = np.zeros((0, 3), np.float32)
         self.other_light_count = 0
         self.camera = np.zeros((), CAMERA_DTYPE)
         self.config = default_config()
@@ -219,6 +229,16 @@ class FlatScene:
             env.radiance = img.ctypes.data
             keep += [img, env]
             s.environment = C.pointer(env)
+        if self.textures.shape[0]:
+            tex = np.ascontiguousarray(self.textures, TEXTURE_DTYPE)
+            mips = np.ascontiguousarray(self.texture_mips, TEXTURE_MIP_DTYPE)
+            texels = np.ascontiguousarray(self.texels, np.float32)
+            keep += [tex, mips, texels]
+            s.texture_count = tex.shape[0]
+            s.textures = C.cast(tex.ctypes.data, C.POINTER(native.TextureDesc))
+            s.texture_mip_count = mips.shape[0]
+            s.texture_mips = C.cast(mips.ctypes.data, C.POINTER(native.TextureMipDesc))
+            s.texels = texels.ctypes.data
         C.memmove(C.byref(s.camera), np.ascontiguousarray(self.camera).ctypes.data, CAMERA_DTYPE.itemsize)
         C.memmove(C.byref(s.config), np.ascontiguousarray(self.config).ctypes.data, CONFIG_DTYPE.itemsize)
         return s, keep
@@ -261,6 +281,12 @@ class FlatScene:
             r["height"], r["width"] = img.shape[0], img.shape[1]
             r["radiance"] = 0
             parts.append(chunk(b"ENVM", r.tobytes() + np.ascontiguousarray(img, np.float32).tobytes()))
+        if self.textures.shape[0]:
+            parts.append(chunk(b"TEXS", struct.pack("<IIQ", self.textures.shape[0], self.texture_mips.shape[0],
+                                                    self.texels.shape[0]) +
+                               np.ascontiguousarray(self.textures, TEXTURE_DTYPE).tobytes() +
+                               np.ascontiguousarray(self.texture_mips, TEXTURE_MIP_DTYPE).tobytes() +
+                               np.ascontiguousarray(self.texels, np.float32).tobytes()))
         with open(path, "wb") as f:
             f.write(b"".join(parts))
 
@@ -331,6 +357,14 @@ class FlatScene:
                 img = np.frombuffer(p[ENVIRONMENT_DTYPE.itemsize:ENVIRONMENT_DTYPE.itemsize + 12 * w * h],
                                     np.float32).reshape(h, w, 3).copy()
                 s.environment = (np.array(rec, ENVIRONMENT_DTYPE), img)
+            elif tag == b"TEXS":
+                nt, nm, nx = struct.unpack_from("<IIQ", p, 0)
+                q = 16
+                s.textures = np.frombuffer(p[q:q + nt * TEXTURE_DTYPE.itemsize], TEXTURE_DTYPE).copy()
+                q += nt * TEXTURE_DTYPE.itemsize
+                s.texture_mips = np.frombuffer(p[q:q + nm * TEXTURE_MIP_DTYPE.itemsize], TEXTURE_MIP_DTYPE).copy()
+                q += nm * TEXTURE_MIP_DTYPE.itemsize
+                s.texels = np.frombuffer(p[q:q + 12 * nx], np.float32).reshape(-1, 3).copy()
             elif tag == b"SPHL":
                 n = struct.unpack_from("<I", p, 0)[0]
                 s.sphere_lights = np.frombuffer(p[4:4 + n * SPHERE_LIGHT_DTYPE.itemsize], SPHERE_LIGHT_DTYPE).copy()

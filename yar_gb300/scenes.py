@@ -181,7 +181,7 @@ def _box(center, size, angle_deg):
 
 def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0, box_materials=None,
                  upper_light=None, light_sources=(), mesh_lights=(), sphere_lights=(), named_materials=(),
-                 integrator="path", light_samples=1):
+                 integrator="path", light_samples=1, textures=(), wall_textures=None):
     """pbrt-v3 text of the seeded Cornell box (34 triangles + a quad light).
 
     box_materials: None for matte boxes, or two pbrt material statements for
@@ -198,7 +198,10 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
     lights, shown by the reference's tessellated sphere).
     named_materials: pbrt MakeNamedMaterial statements (for "mix").
     integrator: "path" or "directlighting" (the reference's direct-lighting
-    algorithm); light_samples: the quad light's "integer samples"."""
+    algorithm); light_samples: the quad light's "integer samples".
+    textures: pbrt Texture statements; wall_textures: {wall index (0 floor,
+    1 ceiling, 2 back, 3 left, 4 right): texture name} walls whose matte Kd is
+    that texture, given uvs (0,0), (1,0), (1,1), (0,1) at their corners."""
     rng = np.random.default_rng(seed)
     k = int(math.ceil(math.sqrt(spp)))
     shapes = []
@@ -229,14 +232,19 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
         'Integrator "%s" "integer maxdepth" [%d]' % (integrator, maxdepth),
         'PixelFilter "box"',
         "WorldBegin",
-    ] + list(named_materials) + list(light_sources)
+    ] + list(textures) + list(named_materials) + list(light_sources)
+    wall_textures = wall_textures or {}
     for k, (v, i, albedo) in enumerate(shapes):
         material = 'Material "matte" "rgb Kd" [%s]' % fmt(albedo)
+        shape = '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(i), fmt(v))
         if box_materials is not None and k >= 5:
             material = box_materials[k - 5]
+        if k in wall_textures:
+            material = 'Material "matte" "texture Kd" "%s"' % wall_textures[k]
+            shape += ' "float uv" [0 0 1 0 1 1 0 1]'
         out += ["AttributeBegin",
                 '  ' + material,
-                '  Shape "trianglemesh" "integer indices" [%s] "point P" [%s]' % (fmt(i), fmt(v)),
+                shape,
                 "AttributeEnd"]
     out += ["AttributeBegin",
             '  AreaLightSource "diffuse" "rgb L" [%s] "integer nsamples" [%d]' % (fmt([light_radiance] * 3),
@@ -312,6 +320,23 @@ def environment_map(width=64, height=32, seed=1):
     sun = np.exp(-((du / 0.03) ** 2 + ((v[:, None] - 0.35) / 0.05) ** 2))
     img += (40.0 * sun)[..., None] * np.array([1.0, 0.9, 0.7], np.float32)
     return img.astype(np.float32)
+
+
+def texture_image(width=48, height=40, seed=3):
+    """A linear RGB test texture of a size that is not a power of two (the
+    reference upsamples it): 8 x 8 checks with seeded per-texel noise, as
+    float32 (height, width, 3)."""
+    rng = np.random.default_rng(seed)
+    y, x = np.mgrid[0:height, 0:width]
+    checks = (((x * 8) // width + (y * 8) // height) % 2).astype(np.float32)
+    base = np.stack([0.15 + 0.7 * checks, 0.6 - 0.4 * checks, 0.3 + 0.2 * (x / width)], axis=-1)
+    return (base * (0.85 + 0.3 * rng.random((height, width, 1)))).astype(np.float32)
+
+
+def texture_statements(filename, name="checks", uscale=1.0, vscale=1.0):
+    """A pbrt "imagemap" spectrum texture of a linear image file."""
+    return ('Texture "%s" "spectrum" "imagemap" "string filename" "%s" "float uscale" [%g] "float vscale" [%g]'
+            % (name, filename, uscale, vscale),)
 
 
 def environment_statements(mapname, scale=(1, 1, 1), samples=1):
