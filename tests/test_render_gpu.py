@@ -48,7 +48,8 @@ def compare(img, ref):
 @pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64",
                                   "cornell_layered_64", "cornell_layered_yar_64", "cornell_lights_64",
                                   "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
-                  "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64"])
+                  "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64",
+                                  "cornell_texture_64"])
 def test_render_matches_reference_golden(gpu_ctx, name):
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
@@ -69,7 +70,7 @@ def test_render_matches_reference_golden(gpu_ctx, name):
 RENDER_GOLDENS = ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "cornell_layered_64",
                   "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64", "cornell_spherelight_64",
                   "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
-                  "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64"]
+                  "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64", "cornell_texture_64"]
 
 
 @pytest.mark.parametrize("name", RENDER_GOLDENS)
@@ -281,3 +282,33 @@ def test_cli_render_writes_the_reference_exr(tmp_path):
     assert np.array_equal(got.view(np.uint32), want.view(np.uint32))
     assert attrs["yar_render_device"][1] == b"gpu"
     assert attrs["yar_spp"][1] == (16).to_bytes(4, "little")
+
+
+@pytest.mark.parametrize("seed_offset,spp_xy", [(2, (4, 4)), (6, (3, 2))])
+def test_textured_render_bit_identical_to_oracle(gpu_ctx, seed_offset, spp_xy):
+    """Image-textured diffuse walls (EWA over the reference's mip chain, the
+    camera ray's differentials scaled to the sample footprint, bilinear mip 0
+    at later vertices, uv scale 2 x 3): bit-identical to the oracle with
+    correctly rounded trigonometry, log2 and filter weights."""
+    s = FlatScene.read(golden("cornell_texture_64.yfs"))
+    s.config["rng_seed_offset"] = seed_offset
+    s.config["x_pixel_sample_count"], s.config["y_pixel_sample_count"] = spp_xy
+    ref, ref_var = oracle.render(s, threads=8, correctly_rounded_trig=True)
+    gpu_ctx.upload_scene(s)
+    img, stats = gpu_ctx.render(64, 64)
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    assert stats.variance == ref_var
+
+
+def test_textured_scene_refused_where_textures_are_not_evaluated(gpu_ctx):
+    """The static and batched renders and scenes with delta materials refuse
+    image textures instead of rendering them as constants."""
+    from yar_gb300 import native
+    s = FlatScene.read(golden("cornell_texture_64.yfs"))
+    gpu_ctx.upload_scene(s)
+    with pytest.raises(native.YarError):
+        gpu_ctx.render_batch([s])
+    s.materials["type"][-1] = native.MATERIAL_PERFECT_REFLECTOR
+    gpu_ctx.upload_scene(s)
+    with pytest.raises(native.YarError):
+        gpu_ctx.render(64, 64)

@@ -309,6 +309,8 @@ int render_batch(yar_gpu_ctx* ctx, const yar_flat_scene* const* scenes, uint32_t
             return fail(ctx, rc, "scene " + std::to_string(i) + ": " + yar_gpu_last_error(s.sub));
         if ((rc = prepare_render_params(s.sub, s.p)) != YAR_OK)
             return fail(ctx, rc, "scene " + std::to_string(i) + ": " + yar_gpu_last_error(s.sub));
+        if (s.p.textured)
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "scene " + std::to_string(i) + ": batched renders do not evaluate image textures");
         s.pixels = (uint64_t)s.p.sw * s.p.sh;
         s.samples = s.pixels * s.p.spp;
         if (s.samples > 0xffffffffull) return fail(ctx, YAR_ERR_CAPACITY, "render batch: too many samples in a scene");

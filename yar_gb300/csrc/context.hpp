@@ -33,6 +33,10 @@ struct Render_Scene {
     Device_Buffer env_map;       // environment map texels (float4 rgb), row 0 first
     Device_Buffer env_marginal;  // its Distribution_2D: marginal CDF over rows
     Device_Buffer env_cdfs;      // and the conditional CDFs, one row each
+    Device_Buffer texels;        // image textures: every mip's texels (float4 rgb), mip after mip
+    Device_Buffer texture_mips;  // uint4 per mip: width, height, texel offset, -
+    Device_Buffer textures;      // uint2 per texture: first mip, mip count
+    Device_Buffer ewa_weights;   // the EWA filter's 256 weights
     Device_Buffer object_info;  // int4 per object: material type, material index, light type, light index
     Device_Buffer object_to_world;         // float[12] per object
     Device_Buffer object_to_world_normal;  // float[12] per object
@@ -43,6 +47,7 @@ struct Render_Scene {
     uint32_t sphere_light_count = 0;
     std::vector<yar_sphere_light_desc> host_sphere_lights;
     bool has_environment = false;
+    uint32_t texture_count = 0;
     yar_environment_desc environment{};  // radiance is not kept
     bool has_no_shadow_meshes = false;
     std::vector<int32_t> host_object_info;

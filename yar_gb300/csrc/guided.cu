@@ -127,6 +127,7 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
         return fail(ctx, YAR_ERR_INVALID, "guide fraction must be in [0, 1)");
     Render_Params p;
     if (int rc0 = prepare_render_params(ctx, p)) return rc0;
+    if (p.textured) return fail(ctx, YAR_ERR_UNSUPPORTED, "the guided render does not evaluate image textures");
     if (p.filter_radius > 0.5f)
         return fail(ctx, YAR_ERR_UNSUPPORTED, "guided render: box filter of radius <= 0.5 only (one pixel per sample)");
     p.nx = p.ny = p.spp = 1;

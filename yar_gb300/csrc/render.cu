@@ -61,6 +61,8 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
         memset(&d, 0, sizeof(d));
         d.type = m.type == YAR_MATERIAL_PLASTIC && scene->config.pbrt3_scene ? kPbrt3Plastic : m.type;
         d.reflectance = Col{m.reflectance[0], m.reflectance[1], m.reflectance[2]};
+        d.texture = m.reflectance_texture;
+        d.texture_scale = make_float2(m.reflectance_uv_scale[0], m.reflectance_uv_scale[1]);
         d.transmittance = Col{m.transmittance[0], m.transmittance[1], m.transmittance[2]};
         d.eta_t = Col{m.eta[0], m.eta[1], m.eta[2]};
         d.k_t = Col{m.k[0], m.k[1], m.k[2]};
@@ -206,6 +208,7 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
     // Environment light: the map as float4 texels and its Distribution_2D, built as
     // initialize_from_latitude_longitude_radiance_map does (src/ref/sampling.cpp:185-259).
     R.has_environment = scene->environment != nullptr;
+    R.texture_count = scene->texture_count;
     R.has_no_shadow_meshes = false;
     for (uint32_t m = 0; m < scene->mesh_count; m++)
         if (scene->meshes[m].visibility == YAR_VISIBLE_NO_SHADOWS) R.has_no_shadow_meshes = true;
@@ -282,6 +285,44 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
     if ((rc = up(R.env_map, env_map.data(), env_map.size() * sizeof(float4))) != YAR_OK) return rc;
     if ((rc = up(R.env_marginal, env_marginal.data(), env_marginal.size() * sizeof(float))) != YAR_OK) return rc;
     if ((rc = up(R.env_cdfs, env_cdfs.data(), env_cdfs.size() * sizeof(float))) != YAR_OK) return rc;
+    {   // image textures: texels as float4, per-mip and per-texture records, EWA weights
+        std::vector<float4> texels(1, make_float4(0.f, 0.f, 0.f, 0.f));
+        std::vector<uint4> mips(1, make_uint4(1, 1, 0, 0));
+        std::vector<uint2> texs(1, make_uint2(0, 1));
+        if (scene->texture_count) {
+            uint64_t total = 0;
+            for (uint32_t i = 0; i < scene->texture_mip_count; i++) {
+                const yar_texture_mip_desc& m = scene->texture_mips[i];
+                if (m.width == 0 || m.height == 0 || (m.width & (m.width - 1)) || (m.height & (m.height - 1)))
+                    return fail(ctx, YAR_ERR_INVALID, "texture mips must have power-of-two sizes");
+                total = std::max<uint64_t>(total, m.texel_offset + (uint64_t)m.width * m.height);
+            }
+            if (total >= (1ull << 32)) return fail(ctx, YAR_ERR_CAPACITY, "more than 2^32 texels");
+            if (!scene->texels) return fail(ctx, YAR_ERR_INVALID, "textures without texels");
+            texels.assign(total, make_float4(0.f, 0.f, 0.f, 0.f));
+            for (uint64_t i = 0; i < total; i++)
+                texels[i] = make_float4(scene->texels[3 * i], scene->texels[3 * i + 1], scene->texels[3 * i + 2], 0.f);
+            mips.resize(scene->texture_mip_count);
+            for (uint32_t i = 0; i < scene->texture_mip_count; i++) {
+                const yar_texture_mip_desc& m = scene->texture_mips[i];
+                mips[i] = make_uint4(m.width, m.height, (uint32_t)m.texel_offset, 0u);
+            }
+            texs.resize(scene->texture_count);
+            for (uint32_t i = 0; i < scene->texture_count; i++) {
+                const yar_texture_desc& t = scene->textures[i];
+                if (t.mip_count == 0 || (uint64_t)t.first_mip + t.mip_count > scene->texture_mip_count)
+                    return fail(ctx, YAR_ERR_INVALID, "texture with invalid mips");
+                texs[i] = make_uint2(t.first_mip, t.mip_count);
+            }
+        }
+        // do_EWA's weights exp(-2 x), x = i / 255 (src/ref/image_texture.cpp:503-512), correctly rounded
+        std::vector<float> w(256);
+        for (int i = 0; i < 256; i++) w[i] = (float)std::exp((double)(-2.f * ((float)i / (float)(256 - 1))));
+        if ((rc = up(R.texels, texels.data(), texels.size() * sizeof(float4))) != YAR_OK) return rc;
+        if ((rc = up(R.texture_mips, mips.data(), mips.size() * sizeof(uint4))) != YAR_OK) return rc;
+        if ((rc = up(R.textures, texs.data(), texs.size() * sizeof(uint2))) != YAR_OK) return rc;
+        if ((rc = up(R.ewa_weights, w.data(), w.size() * sizeof(float))) != YAR_OK) return rc;
+    }
     cudaError_t e = cudaStreamSynchronize(ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render upload");
     return YAR_OK;
@@ -290,7 +331,8 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
 void render_release(yar_gpu_ctx* ctx) {
     Render_Scene& R = ctx->render;
     for (Device_Buffer* b : {&R.shading, &R.materials, &R.rect_lights, &R.delta_lights, &R.mesh_lights, &R.mesh_cdf,
-                             &R.sphere_lights, &R.env_map, &R.env_marginal, &R.env_cdfs, &R.object_info,
+                             &R.sphere_lights, &R.env_map, &R.env_marginal, &R.env_cdfs, &R.texels,
+                             &R.texture_mips, &R.textures, &R.ewa_weights, &R.object_info,
                              &R.object_to_world, &R.object_to_world_normal})
         device_free(*b);
     for (Device_Buffer& b : ctx->render_scratch) device_free(b);
@@ -386,6 +428,7 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
                   dptr<float4>(B[12]), dptr<uint8_t>(B[13]), dptr<float4>(B[14]), dptr<uint2>(B[15])};
     ps.rng_draws = dptr<uint32_t>(B[30]);
     ps.deferred = dptr<float4>(B[31]);
+    ps.image_samples = dptr<float2>(B[1]);
     Queues q{};
     q.ext_rays[0] = dptr<float4>(B[16]);
     q.ext_rays[1] = dptr<float4>(B[17]);
@@ -436,6 +479,7 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
     for (uint64_t first = 0; first < pixels && e == cudaSuccess; first += chunk_pixels) {
         const uint32_t cp = (uint32_t)std::min<uint64_t>(chunk_pixels, pixels - first);
         const uint32_t paths = cp * (uint32_t)p.spp;
+        ps.chunk_first = (uint32_t)first;
         launch_generate(p, (uint32_t)first, cp, dptr<float>(B[2]), dptr<float>(B[3]), image_samples, ps, q, st);
         launches++;
         if (int rc1 = run_bounces(p, paths, 0)) return rc1;
@@ -578,6 +622,7 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
     if (!rgb_out_device) return fail(ctx, YAR_ERR_INVALID, "null image buffer");
     Render_Params p;
     if (int rc0 = prepare_render_params(ctx, p)) return rc0;
+    if (p.textured) return fail(ctx, YAR_ERR_UNSUPPORTED, "the static render does not evaluate image textures");
 
     cudaSetDevice(ctx->device);
     if (ctx->device < 0 || ctx->device >= 64) return fail(ctx, YAR_ERR_INVALID, "device ordinal above 63");

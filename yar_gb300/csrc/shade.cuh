@@ -175,6 +175,8 @@ struct Material_Dev {
     float mix_lum;          // mix: luminance(amount), unclamped (the Scaled_BSDF factor)
     Col mix_coeff;          // mix: White - amount
     uint32_t has_bsdf;      // initialize_scattering creates a BSDF: some layer is not delta
+    uint32_t texture;       // diffuse: 1 + the reflectance's texture (0: the constant)
+    float2 texture_scale;   // its uv scale
 };
 
 struct Bsdf {

@@ -107,6 +107,7 @@ struct Render_Params {
     // tail, first phase (a path that might draw past the budget at its next
     // vertex is deferred); 2 = exact tail, waves (draws are counted per path).
     int32_t exact_tail;
+    int32_t textured;  // some diffuse reflectance is an image texture
 };
 
 struct Path_State {
@@ -125,6 +126,8 @@ struct Path_State {
     uint32_t* rec;         // guided training: this bounce's record index (0xffffffff = none)
     uint32_t* rng_draws;   // exact tail: pcg draws this path took past the budget
     float4* deferred;      // exact tail: the deferred extend ray, 2 float4 per slot
+    const float2* image_samples;  // image-plane samples of the render (textured scenes' ray differentials)
+    uint32_t chunk_first;         // the chunk's first pixel
 };
 
 // Learned-proposal hooks of the shade kernel (guided render only).
@@ -207,6 +210,10 @@ struct Scene_Dev {
     float4 env_l2w[3], env_w2l[3];
     float4 env_scale;  // rgb, -
     int32_t env_nx, env_ny;
+    const float4* texels;        // image textures (rgb)
+    const uint4* texture_mips;   // width, height, texel offset
+    const uint2* textures;       // first mip, mip count
+    const float* ewa_weights;    // 256
 };
 
 // The device view of an uploaded scene.
@@ -234,6 +241,10 @@ inline Scene_Dev scene_dev(const Device_Scene& ds, const Render_Scene& R) {
     S.env_scale = make_float4(e.scale[0], e.scale[1], e.scale[2], 0.f);
     S.env_nx = (int32_t)e.width;
     S.env_ny = (int32_t)e.height;
+    S.texels = reinterpret_cast<const float4*>(R.texels.ptr);
+    S.texture_mips = reinterpret_cast<const uint4*>(R.texture_mips.ptr);
+    S.textures = reinterpret_cast<const uint2*>(R.textures.ptr);
+    S.ewa_weights = reinterpret_cast<const float*>(R.ewa_weights.ptr);
     return S;
 }
 
@@ -394,6 +405,21 @@ __global__ void sample_tables_kernel(Render_Params p, uint32_t chunk_first, uint
     }
 }
 
+// Camera::generate_ray (src/ref/camera.cpp:16-31) through film position (fx, fy).
+__device__ __forceinline__ void camera_ray(const yar_camera_desc& c, float fx, float fy, V3& o, V3& d) {
+    const float4 m0 = make_float4(c.camera_to_world[0], c.camera_to_world[1], c.camera_to_world[2], c.camera_to_world[3]);
+    const float4 m1 = make_float4(c.camera_to_world[4], c.camera_to_world[5], c.camera_to_world[6], c.camera_to_world[7]);
+    const float4 m2 = make_float4(c.camera_to_world[8], c.camera_to_world[9], c.camera_to_world[10], c.camera_to_world[11]);
+    const float u = 2.f * (fx / c.image_extent[0]) - 1.f;
+    const float v = 2.f * (fy / c.image_extent[1]) - 1.f;
+    const float right = u * c.horz_half_dist;
+    const float up = -v * c.vert_half_dist;
+    V3 dir = v3(right, c.z_is_up ? 1.f : up, c.z_is_up ? up : -1.f);
+    dir = divs(dir, len(dir));
+    o = xform_point(m0, m1, m2, v3(0.f, 0.f, 0.f));
+    d = xform_vector(m0, m1, m2, dir);
+}
+
 // One thread per path of the chunk: camera ray (Camera::generate_ray,
 // src/ref/camera.cpp) through the path's image sample, path initialisation.
 __global__ void __launch_bounds__(kBlock)
@@ -407,20 +433,8 @@ camera_kernel(Render_Params p, uint32_t chunk_first, uint32_t chunk_paths, const
     int x, y;
     const uint32_t stream = pixel_stream(p, chunk_first + lp, x, y);
     const float2 s = image_samples[((size_t)chunk_first + lp) * spp + k];
-    const yar_camera_desc& c = p.camera;
-    const float4 m0 = make_float4(c.camera_to_world[0], c.camera_to_world[1], c.camera_to_world[2], c.camera_to_world[3]);
-    const float4 m1 = make_float4(c.camera_to_world[4], c.camera_to_world[5], c.camera_to_world[6], c.camera_to_world[7]);
-    const float4 m2 = make_float4(c.camera_to_world[8], c.camera_to_world[9], c.camera_to_world[10], c.camera_to_world[11]);
-    const float fx = (float)x + s.x;
-    const float fy = (float)y + s.y;
-    const float u = 2.f * (fx / c.image_extent[0]) - 1.f;
-    const float v = 2.f * (fy / c.image_extent[1]) - 1.f;
-    const float right = u * c.horz_half_dist;
-    const float up = -v * c.vert_half_dist;
-    V3 dir = v3(right, c.z_is_up ? 1.f : up, c.z_is_up ? up : -1.f);
-    dir = divs(dir, len(dir));
-    const V3 o = xform_point(m0, m1, m2, v3(0.f, 0.f, 0.f));
-    const V3 d = xform_vector(m0, m1, m2, dir);
+    V3 o, d;
+    camera_ray(p.camera, (float)x + s.x, (float)y + s.y, o, d);
     q.ext_rays[0][2 * (size_t)slot] = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
     q.ext_rays[0][2 * (size_t)slot + 1] = make_float4(d.x, d.y, d.z, 0.f);
     q.ext_slot[0][slot] = slot;
@@ -740,6 +754,204 @@ __device__ __forceinline__ Col env_light_sample(const Scene_Dev& S, float u0, fl
     return env_nearest(S, kx, ky) * col(S.env_scale.x, S.env_scale.y, S.env_scale.z);
 }
 
+// ---------------------------------------------------------------- image textures
+// Image_Texture (src/ref/image_texture.cpp) over the reference's mip chain
+// and evaluate_texture_parameter (src/ref/parameter_evaluation.cpp:10-31):
+// EWA filtering with repeat wrapping.  log2 of the footprint and the filter
+// weights are rounded correctly (double evaluation), like the sines and cosines.
+__device__ __forceinline__ Col texel_repeat(const Scene_Dev& S, uint4 mip, int x, int y) {  // get_texel_repeat
+    const int w = (int)mip.x, h = (int)mip.y;
+    if (x >= 0) x &= w - 1;
+    else { x %= w; x += (x >> 31) & w; }
+    if (y >= 0) y &= h - 1;
+    else { y %= h; y += (y >> 31) & h; }
+    const float4 t = __ldg(S.texels + mip.z + (size_t)y * (size_t)w + (size_t)x);
+    return col(t.x, t.y, t.z);
+}
+__device__ __forceinline__ Col texture_bilinear(const Scene_Dev& S, uint4 mip, float u, float v) {
+    const float x = u * (float)mip.x - 0.5f, y = v * (float)mip.y - 0.5f;
+    const float x_floor = floorf(x), y_floor = floorf(y);
+    const float wx = x - x_floor, wy = y - y_floor;
+    const int x0 = (int)x_floor, y0 = (int)y_floor, x1 = x0 + 1, y1 = y0 + 1;
+    return ((mul(texel_repeat(S, mip, x0, y0), (1 - wy) * (1 - wx)) +
+             mul(texel_repeat(S, mip, x1, y0), (1 - wy) * wx)) +
+            mul(texel_repeat(S, mip, x0, y1), wy * (1 - wx))) +
+           mul(texel_repeat(S, mip, x1, y1), wy * wx);
+}
+// do_EWA (image_texture.cpp:501-578) on one mip
+__device__ __noinline__ Col texture_ewa_level(const Scene_Dev& S, uint4 mip, float u, float v, float2 a1, float2 a2) {
+    const float w = (float)mip.x, h = (float)mip.y;
+    u = u * w - 0.5f;
+    v = v * h - 0.5f;
+    const float a1x = a1.x * w, a1y = a1.y * h, a2x = a2.x * w, a2y = a2.y * h;
+    float A = a1y * a1y + a2y * a2y + 1;
+    float B = -2 * (a1x * a1y + a2x * a2y);
+    float C = a1x * a1x + a2x * a2x + 1;
+    const float F = A * C - 0.25f * B * B;
+    const float inv_F = 1.f / F;
+    A *= inv_F;
+    B *= inv_F;
+    C *= inv_F;
+    const float inv_det = 0.25f * F;
+    const float u_delta = 2 * sqrtf(C * inv_det);
+    const float x0 = ceilf(u - u_delta), x1 = floorf(u + u_delta);
+    const float v_delta = 2 * sqrtf(A * inv_det);
+    const float y0 = ceilf(v - v_delta), y1 = floorf(v + v_delta);
+    Col sum = col(0.f, 0.f, 0.f);
+    float weight_sum = 0.f;
+    for (float y = y0; y <= y1; y++) {
+        const float yy = y - v;
+        for (float x = x0; x <= x1; x++) {
+            const float xx = x - u;
+            const float r2 = A * xx * xx + B * xx * yy + C * yy * yy;
+            if (r2 < 1.f) {
+                const float wt = __ldg(S.ewa_weights + (int)(r2 * 256));
+                sum = sum + mul(texel_repeat(S, mip, (int)x, (int)y), wt);
+                weight_sum += wt;
+            }
+        }
+    }
+    return mul(sum, 1.f / weight_sum);
+}
+// Image_Texture::sample_EWA (image_texture.cpp:580-615), max anisotropy 32
+__device__ Col texture_ewa(const Scene_Dev& S, uint2 tex, float u, float v, float2 a1, float2 a2) {
+    float l1 = a1.x * a1.x + a1.y * a1.y, l2 = a2.x * a2.x + a2.y * a2.y;
+    if (l1 < l2) {
+        const float2 t = a1;
+        a1 = a2;
+        a2 = t;
+        const float tl = l1;
+        l1 = l2;
+        l2 = tl;
+    }
+    const float major_length = sqrtf(l1);
+    float minor_length = sqrtf(l2);
+    if (minor_length < 1e-6f) return texture_bilinear(S, __ldg(S.texture_mips + tex.x), u, v);
+    if (minor_length * 32.f < major_length) {
+        const float scale = major_length / (minor_length * 32.f);
+        minor_length *= scale;
+        a2.x *= scale;
+        a2.y *= scale;
+    }
+    const float lod = max_std(0.f, (float)((int)tex.y - 1) + (float)log2((double)minor_length));
+    const float lod_floor = truncf(lod);  // std::modf of a non-negative value
+    const float frac = lod - lod_floor;
+    const int level0 = (int)lod_floor;
+    if (level0 >= (int)tex.y - 1) {
+        const float4 c = __ldg(S.texels + __ldg(S.texture_mips + tex.x + tex.y - 1).z);
+        return col(c.x, c.y, c.z);
+    }
+    const Col c0 = texture_ewa_level(S, __ldg(S.texture_mips + tex.x + level0), u, v, a1, a2);
+    const Col c1 = texture_ewa_level(S, __ldg(S.texture_mips + tex.x + level0 + 1), u, v, a1, a2);
+    return mul(c0, 1.f - frac) + mul(c1, frac);  // lerp, src/lib/math.h:82-85
+}
+
+// The hit's uv and world-space dpdu/dpdv (init_from_triangle_mesh_intersection,
+// src/ref/shading_context.cpp:209-223); false without uvs.
+__device__ bool texture_geometry(const Scene_Dev& S, uint32_t object, uint32_t prim, float b0, float b1, float b2,
+                                 float2& uv, V3& dpdu, V3& dpdv) {
+    const float4* orec = S.ds.objects + 6 * (size_t)object;
+    const uint32_t tri_offset = __float_as_uint(__ldg(orec + 4).w);
+    const size_t g = (size_t)tri_offset + prim;
+    const float4 h0 = __ldg(S.shading + 4 * g), h1 = __ldg(S.shading + 4 * g + 1);
+    const float4 h2 = __ldg(S.shading + 4 * g + 2), h3 = __ldg(S.shading + 4 * g + 3);
+    const uint32_t flags = __float_as_uint(h3.w);
+    if (!(flags & 2u)) return false;
+    const float4 q0 = __ldg(S.ds.tris + 3 * g), q1 = __ldg(S.ds.tris + 3 * g + 1), q2 = __ldg(S.ds.tris + 3 * g + 2);
+    const V3 p0 = v3(q0.x, q0.y, q0.z), p1 = v3(q1.x, q1.y, q1.z), p2 = v3(q2.x, q2.y, q2.z);
+    V3 gn = normalized(cross(p1 - p0, p2 - p0));
+    if (flags & 4u) gn = -gn;
+    // uvs: u0 = h0.w, v0 = h1.w, u1 = h2.w, v1 = h3.x, u2 = h3.y, v2 = h3.z
+    uv = make_float2(h0.w * b0 + h2.w * b1 + h3.y * b2, h1.w * b0 + h3.x * b1 + h3.z * b2);
+    const float a00 = h2.w - h0.w, a01 = h3.x - h1.w, a10 = h3.y - h0.w, a11 = h3.z - h1.w;
+    const V3 bp0 = p1 - p0, bp1 = p2 - p0;
+    const float det = a00 * a11 - a01 * a10;
+    dpdu = v3(0.f, 0.f, 0.f);
+    dpdv = v3(0.f, 0.f, 0.f);
+    if (det != 0.f) {
+        const float inv_det = 1.f / det;
+        dpdu = mul(mul(bp0, a11) - mul(bp1, a01), inv_det);
+        dpdv = mul(mul(bp0, -a10) + mul(bp1, a00), inv_det);
+    }
+    if (fabsf(det) < 1e-9f) {
+        dpdu = coordinate_axis(gn);
+        dpdv = cross(gn, dpdu);
+    }
+    const float4* rrec = S.obj_render + 7 * (size_t)object;
+    const float4 w0 = __ldg(rrec + 0), w1 = __ldg(rrec + 1), w2 = __ldg(rrec + 2);
+    dpdu = xform_vector(w0, w1, w2, dpdu);
+    dpdv = xform_vector(w0, w1, w2, dpdv);
+    return true;
+}
+
+// Shading_Context::calculate_dxdy_derivatives + calculate_uv_derivates
+// (shading_context.cpp:242-333): the uv derivatives along the differential
+// rays (origin o, directions dx, dy) through the hit plane.
+__device__ void uv_derivatives(const Shading& sc, V3 o, V3 dx, V3 dy, V3 dpdu, V3 dpdv, float2& duvdx,
+                               float2& duvdy) {
+    const V3 gn = sc.ng;
+    const float plane_d = -dot(gn, sc.position);
+    V3 dpdx = v3(0.f, 0.f, 0.f), dpdy = v3(0.f, 0.f, 0.f);
+    auto plane_t = [&](V3 d) {  // ray_plane_intersection, src/lib/math.cpp:27-31
+        const float k = -dot(o, gn) - plane_d;
+        return k == 0 ? 0.f : k / dot(d, gn);
+    };
+    const float tx = plane_t(dx);
+    if (fabsf(tx) != __int_as_float(0x7f800000)) dpdx = (o + mul(dx, tx)) - sc.position;
+    const float ty = plane_t(dy);
+    if (fabsf(ty) != __int_as_float(0x7f800000)) dpdy = (o + mul(dy, ty)) - sc.position;
+    const float ax = fabsf(gn.x), ay = fabsf(gn.y), az = fabsf(gn.z);
+    const int dim0 = (ax > ay && ax > az) ? 1 : 0;
+    const int dim1 = (ax > ay && ax > az) ? 2 : (ay > az ? 2 : 1);
+    auto comp = [](V3 a, int k) { return k == 0 ? a.x : (k == 1 ? a.y : a.z); };
+    const float a00 = comp(dpdu, dim0), a01 = comp(dpdv, dim0), a10 = comp(dpdu, dim1), a11 = comp(dpdv, dim1);
+    const float det = a00 * a11 - a01 * a10;  // solve_linear_system_2x2, src/lib/math.cpp:8-16
+    duvdx = make_float2(0.f, 0.f);
+    duvdy = make_float2(0.f, 0.f);
+    if (det != 0.f) {
+        const float inv_det = 1.f / det;
+        duvdx = make_float2((a11 * comp(dpdx, dim0) - a01 * comp(dpdx, dim1)) * inv_det,
+                            (-a10 * comp(dpdx, dim0) + a00 * comp(dpdx, dim1)) * inv_det);
+        duvdy = make_float2((a11 * comp(dpdy, dim0) - a01 * comp(dpdy, dim1)) * inv_det,
+                            (-a10 * comp(dpdy, dim0) + a00 * comp(dpdy, dim1)) * inv_det);
+    }
+    if (fabsf(duvdx.x) > 1e9f || fabsf(duvdx.y) > 1e9f || fabsf(duvdy.x) > 1e9f || fabsf(duvdy.y) > 1e9f) {
+        duvdx = make_float2(0.f, 0.f);
+        duvdy = make_float2(0.f, 0.f);
+    }
+}
+
+// A textured diffuse reflectance at a hit (evaluate_rgb_parameter with the
+// shading context's uv and derivatives, parameter_evaluation.cpp:84-89): the
+// camera ray's differential rays, one pixel over and scaled to the sample's
+// footprint (src/ref/reference_renderer.cpp:367-378), give the derivatives at
+// bounce 0; later vertices have none.
+__device__ __forceinline__ Col textured_reflectance(const Render_Params& p, const Scene_Dev& S, const Path_State& ps, uint32_t slot,
+                                    int bounce, const Shading& sc, const Material_Dev& mat, float4 h4, uint2 h2) {
+    float2 uv = make_float2(0.f, 0.f), duvdx = make_float2(0.f, 0.f), duvdy = make_float2(0.f, 0.f);
+    V3 dpdu, dpdv;
+    if (texture_geometry(S, h2.y, h2.x, h4.y, h4.z, h4.w, uv, dpdu, dpdv) && bounce == 0) {
+        const uint32_t lp = slot / (uint32_t)p.spp, k = slot - lp * (uint32_t)p.spp;
+        int x, y;
+        pixel_stream(p, ps.chunk_first + lp, x, y);
+        const float2 fs = ps.image_samples[((size_t)ps.chunk_first + lp) * (uint32_t)p.spp + k];
+        const float fx = (float)x + fs.x, fy = (float)y + fs.y;
+        V3 o, d, o1, dx, dy;
+        camera_ray(p.camera, fx, fy, o, d);
+        camera_ray(p.camera, fx + 1.f, fy, o1, dx);
+        camera_ray(p.camera, fx, fy + 1.f, o1, dy);
+        const float scale = 1.f / sqrtf((float)p.spp);
+        dx = d + mul(dx - d, scale);
+        dx = divs(dx, len(dx));
+        dy = d + mul(dy - d, scale);
+        dy = divs(dy, len(dy));
+        uv_derivatives(sc, o, dx, dy, dpdu, dpdv, duvdx, duvdy);
+    }
+    const float su = mat.texture_scale.x, sv = mat.texture_scale.y;
+    return texture_ewa(S, __ldg(S.textures + mat.texture - 1), uv.x * su, uv.y * sv,
+                       make_float2(duvdx.x * su, duvdx.y * sv), make_float2(duvdy.x * su, duvdy.y * sv));
+}
+
 // ---------------------------------------------------------------- sphere lights
 // Diffuse_Sphere_Light_Sampler (light_sampling.cpp:76-123): the cone the
 // sphere subtends from the shading point, sampled uniformly in solid angle.
@@ -892,6 +1104,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 uint32_t pend = 0;
                 if (delta == 0 || bsdf_prob != 0.f) {
                     make_bsdf(sc, mat, S.materials, f);
+                    if (FULL && !GUIDED && mat.texture)
+                        f.reflectance = textured_reflectance(p, S, ps, slot, bounce, sc, mat, h4, h2);
                     // estimate_direct_lighting_from_single_sample (direct_lighting.cpp:522-578):
                     // the light int(u * total_light_count), point, spot and directional lights
                     // first, then the rectangular lights (the reference asserts the index is
@@ -1715,8 +1929,10 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
             return fail(ctx, YAR_ERR_INVALID, "point, spot and directional lights must be listed in that order");
     }
     for (const yar_material_desc& m : R.host_materials) {
-        if (m.reflectance_texture || m.other_textured_parameters)
-            return fail(ctx, YAR_ERR_UNSUPPORTED, "image textures are not implemented on the device");
+        if (m.other_textured_parameters)
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "a material parameter other than a diffuse reflectance is a texture");
+        if (m.reflectance_texture && (m.type != YAR_MATERIAL_DIFFUSE || m.reflectance_texture > R.texture_count))
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "image textures are implemented for diffuse reflectance only");
         if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL && m.type != YAR_MATERIAL_GLASS &&
             m.type != YAR_MATERIAL_PLASTIC && m.type != YAR_MATERIAL_COATED_DIFFUSE &&
             m.type != YAR_MATERIAL_PERFECT_REFLECTOR && m.type != YAR_MATERIAL_PERFECT_REFRACTOR &&
@@ -1824,6 +2040,19 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
         if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL &&
             !(m.type == YAR_MATERIAL_GLASS && m.u_roughness > 0.f))
             p.full_shading = 1;
+    // Image textures (diffuse reflectance): FULL shading; the differential rays
+    // of delta bounces and of the direct-lighting algorithm are not restated.
+    bool delta_materials = false;
+    for (const yar_material_desc& m : R.host_materials) {
+        if (m.reflectance_texture) p.textured = 1;
+        delta_materials = delta_materials || m.type == YAR_MATERIAL_PERFECT_REFLECTOR ||
+                          m.type == YAR_MATERIAL_PERFECT_REFRACTOR ||
+                          (m.type == YAR_MATERIAL_GLASS && !(m.u_roughness > 0.f)) ||
+                          m.type == YAR_MATERIAL_PBRT3_UBER || m.type == YAR_MATERIAL_MIX;
+    }
+    if (p.textured && (c.rendering_algorithm == 0 || delta_materials))
+        return fail(ctx, YAR_ERR_UNSUPPORTED, "image textures with delta materials or the direct-lighting algorithm");
+    if (p.textured) p.full_shading = 1;
     p.seed_offset = (uint32_t)c.rng_seed_offset;
     return YAR_OK;
 }
