@@ -299,6 +299,7 @@ typedef struct yar_flat_scene {
     uint32_t texture_mip_count;
     const yar_texture_mip_desc* texture_mips;
     const float* texels;            /* RGB triples of every mip */
+    uint64_t texel_count;           /* texels (RGB triples) behind `texels`; every mip must lie inside */
 } yar_flat_scene;
 
 /* One ray of a batch: 32 bytes, two float4.  tmax plays the role of the
@@ -405,7 +406,10 @@ int yar_gpu_render_checkpoint(yar_gpu_ctx* ctx, const char* checkpoint_directory
  * an application running under a fixed, pre-reserved memory budget, a host
  * that forbids allocation after start-up for latency reasons, or code whose
  * device allocator is owned by someone else - use this entry point instead:
- * it renders exactly like yar_gpu_render but takes all working memory from
+ * it renders the path tracer (rendering_algorithm 1; direct-lighting scenes
+ * and image textures are refused with YAR_ERR_UNSUPPORTED) exactly like
+ * yar_gpu_render, draws past the sampler's dimension budget included, but
+ * takes all working memory from
  * one static device array of YAR_GPU_STATIC_ARENA_BYTES (64 MiB) that is
  * linked into the library (every GPU that loads the library keeps it until
  * the process exits), and it calls no cudaMalloc, cudaFree or other

@@ -312,3 +312,22 @@ def test_textured_scene_refused_where_textures_are_not_evaluated(gpu_ctx):
     gpu_ctx.upload_scene(s)
     with pytest.raises(native.YarError):
         gpu_ctx.render(64, 64)
+
+
+def test_direct_lighting_scene_refused_by_path_tracer_only_entry_points(gpu_ctx, tmp_path):
+    """The batched, guided and checkpointed renders run the path tracer only:
+    a direct-lighting scene (rendering_algorithm 0) is refused by each instead
+    of coming back path traced."""
+    from yar_gb300 import native
+    s = FlatScene.read(golden("cornell_direct_64.yfs"))
+    assert int(s.config["rendering_algorithm"]) == 0
+    with pytest.raises(native.YarError) as e:
+        gpu_ctx.render_batch([s])
+    assert e.value.code == native.YAR_ERR_UNSUPPORTED
+    gpu_ctx.upload_scene(s)
+    with pytest.raises(native.YarError) as e:
+        gpu_ctx.guided_render(64, 64, passes=1)
+    assert e.value.code == native.YAR_ERR_UNSUPPORTED
+    with pytest.raises(native.YarError) as e:
+        gpu_ctx.render_checkpoint(64, 64, tmp_path, "scene.pbrt")
+    assert e.value.code == native.YAR_ERR_UNSUPPORTED

@@ -7,9 +7,11 @@ image in device memory.
 
 Checked here through the C ABI: two calls in a row give the same image and
 variance as yar_gpu_render (within the render tolerance of the other render
-tests - in practice bit for bit), the second call changes no device memory
-usage, and a render that does not fit the static array is refused with
-YAR_ERR_CAPACITY.  This file is collected last so that a failure here comes
+tests - in practice bit for bit, and at maxdepth 12, past the sampler's
+dimension budget, too), the second call changes no device memory usage, a
+render that does not fit the static array is refused with YAR_ERR_CAPACITY,
+and a direct-lighting scene (which this entry point does not render) is
+refused with YAR_ERR_UNSUPPORTED.  This file is collected last so that a failure here comes
 after every other test has run."""
 import numpy as np
 import pytest
@@ -39,10 +41,13 @@ def torch_cuda():
     return torch
 
 
-@pytest.mark.parametrize("name", ["cornell_c1_64", "cornell_ggx_64"])
-def test_static_render_matches_render_twice(torch_cuda, name):
+@pytest.mark.parametrize("name,maxdepth", [("cornell_c1_64", None), ("cornell_ggx_64", None),
+                                           ("cornell_ggx_64", 12)])
+def test_static_render_matches_render_twice(torch_cuda, name, maxdepth):
     torch = torch_cuda
     s = FlatScene.read(golden(name + ".yfs"))
+    if maxdepth is not None:
+        s.config["max_light_bounces"] = maxdepth
     ctx = native.Context(0)
     try:
         ctx.upload_scene(s)
@@ -79,5 +84,20 @@ def test_static_render_refuses_renders_beyond_the_arena(torch_cuda):
             ctx.render_static(out.data_ptr())
         assert e.value.code == native.YAR_ERR_CAPACITY
         assert "static arena" in str(e.value)
+    finally:
+        ctx.close()
+
+
+def test_static_render_refuses_direct_lighting(torch_cuda):
+    torch = torch_cuda
+    s = FlatScene.read(golden("cornell_direct_64.yfs"))
+    assert int(s.config["rendering_algorithm"]) == 0
+    ctx = native.Context(0)
+    try:
+        ctx.upload_scene(s)
+        out = torch.zeros((64, 64, 3), dtype=torch.float32, device="cuda")
+        with pytest.raises(native.YarError) as e:
+            ctx.render_static(out.data_ptr())
+        assert e.value.code == native.YAR_ERR_UNSUPPORTED
     finally:
         ctx.close()

@@ -311,6 +311,9 @@ int render_batch(yar_gpu_ctx* ctx, const yar_flat_scene* const* scenes, uint32_t
             return fail(ctx, rc, "scene " + std::to_string(i) + ": " + yar_gpu_last_error(s.sub));
         if (s.p.textured)
             return fail(ctx, YAR_ERR_UNSUPPORTED, "scene " + std::to_string(i) + ": batched renders do not evaluate image textures");
+        if (s.sub->render.config.rendering_algorithm == 0)
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "scene " + std::to_string(i) +
+                                                      ": batched renders run the path tracer only (rendering_algorithm 1)");
         s.pixels = (uint64_t)s.p.sw * s.p.sh;
         s.samples = s.pixels * s.p.spp;
         if (s.samples > 0xffffffffull) return fail(ctx, YAR_ERR_CAPACITY, "render batch: too many samples in a scene");

@@ -125,6 +125,8 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
     if (!gp || gp->passes == 0) return fail(ctx, YAR_ERR_INVALID, "guided render: no passes");
     if (!(gp->guide_fraction >= 0.f && gp->guide_fraction < 1.f))
         return fail(ctx, YAR_ERR_INVALID, "guide fraction must be in [0, 1)");
+    if (ctx->render.config.rendering_algorithm == 0)
+        return fail(ctx, YAR_ERR_UNSUPPORTED, "the guided render runs the path tracer only (rendering_algorithm 1)");
     Render_Params p;
     if (int rc0 = prepare_render_params(ctx, p)) return rc0;
     if (p.textured) return fail(ctx, YAR_ERR_UNSUPPORTED, "the guided render does not evaluate image textures");

@@ -295,6 +295,9 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
                 const yar_texture_mip_desc& m = scene->texture_mips[i];
                 if (m.width == 0 || m.height == 0 || (m.width & (m.width - 1)) || (m.height & (m.height - 1)))
                     return fail(ctx, YAR_ERR_INVALID, "texture mips must have power-of-two sizes");
+                if (m.texel_offset > scene->texel_count ||
+                    (uint64_t)m.width * m.height > scene->texel_count - m.texel_offset)
+                    return fail(ctx, YAR_ERR_INVALID, "texture mip outside the texel array");
                 total = std::max<uint64_t>(total, m.texel_offset + (uint64_t)m.width * m.height);
             }
             if (total >= (1ull << 32)) return fail(ctx, YAR_ERR_CAPACITY, "more than 2^32 texels");
@@ -313,6 +316,26 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
                 if (t.mip_count == 0 || (uint64_t)t.first_mip + t.mip_count > scene->texture_mip_count)
                     return fail(ctx, YAR_ERR_INVALID, "texture with invalid mips");
                 texs[i] = make_uint2(t.first_mip, t.mip_count);
+            }
+            // The EWA footprint walks integer texel coordinates held in floats:
+            // refuse uv ranges whose texel coordinates reach 2^22.
+            for (uint32_t o = 0; o < scene->object_count; o++) {
+                const yar_object_desc& ob = scene->objects[o];
+                if (ob.material_index < 0 || (uint32_t)ob.material_index >= scene->material_count) continue;
+                const yar_material_desc& md = scene->materials[ob.material_index];
+                if (!md.reflectance_texture || md.reflectance_texture > scene->texture_count) continue;
+                const yar_texture_desc& t = scene->textures[md.reflectance_texture - 1];
+                const yar_texture_mip_desc& top = scene->texture_mips[t.first_mip];
+                const yar_mesh_desc& mesh = scene->meshes[ob.mesh_index];
+                if (!mesh.uvs) continue;
+                float uv_max = 0.f;
+                for (uint64_t k = 0; k < 2ull * mesh.vertex_count; k++) uv_max = std::max(uv_max, std::fabs(mesh.uvs[k]));
+                const double reach = (double)uv_max *
+                                     std::max(std::fabs(md.reflectance_uv_scale[0]), std::fabs(md.reflectance_uv_scale[1])) *
+                                     std::max(top.width, top.height);
+                if (!(reach < (double)(1 << 22)))
+                    return fail(ctx, YAR_ERR_UNSUPPORTED, "texture coordinates of object " + std::to_string(o) +
+                                                              " reach 2^22 texels");
             }
         }
         // do_EWA's weights exp(-2 x), x = i / 255 (src/ref/image_texture.cpp:503-512), correctly rounded
@@ -620,8 +643,14 @@ struct Arena {
 
 int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats* stats) {
     if (!rgb_out_device) return fail(ctx, YAR_ERR_INVALID, "null image buffer");
+    if (ctx->render.config.rendering_algorithm == 0)
+        return fail(ctx, YAR_ERR_UNSUPPORTED, "the static render runs the path tracer only (rendering_algorithm 1)");
     Render_Params p;
     if (int rc0 = prepare_render_params(ctx, p)) return rc0;
+    // draws past the sampler budget from the pixel's own stream, as render_run_params
+    p.exact_tail = (p.stream_hi == 0 && p.n1d > 0) ? 1 : 0;
+    Render_Params p_wave = p;
+    p_wave.exact_tail = 2;
     if (p.textured) return fail(ctx, YAR_ERR_UNSUPPORTED, "the static render does not evaluate image textures");
 
     cudaSetDevice(ctx->device);
@@ -650,10 +679,15 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
     double* tile_variance = A.take<double>(tiles);
     double* variance_total = A.take<double>(1);
     uint32_t* counters = A.take<uint32_t>(8);
-    const int kChunkBuffers = 24;
-    const size_t per_path = 4 * (size_t)std::max(1, p.n1d) + 8 * (size_t)std::max(1, p.n2d) + 157 + 168;
+    uint32_t* tail = A.take<uint32_t>(2);
+    const int kChunkBuffers = 29;
+    // per path: sample tables, path state (157 B), queues (168 B) and, for the
+    // exact tail, the draw count, the deferred ray and the per-pixel list (40 B)
+    // plus two words per pixel
+    const size_t per_path = 4 * (size_t)std::max(1, p.n1d) + 8 * (size_t)std::max(1, p.n2d) + 157 + 168 +
+                            (p.exact_tail ? 40 + (8 + p.spp - 1) / p.spp : 0);
     const size_t left = (radiance && image_samples && pixel_variance && tile_variance && variance_total && counters &&
-                         A.size > A.used + 256 * kChunkBuffers)
+                         tail && A.size > A.used + 256 * kChunkBuffers)
                             ? A.size - A.used - 256 * kChunkBuffers
                             : 0;
     const uint64_t chunk_pixels = std::min<uint64_t>(pixels, left / per_path / p.spp);
@@ -679,6 +713,17 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
     q.prb_rays = A.take<float4>(2 * cap);
     q.prb_slot = A.take<uint32_t>(cap);
     q.counters = counters;
+    uint32_t *list = nullptr, *deferred_count = nullptr, *stream_pos = nullptr;
+    if (p.exact_tail) {
+        ps.rng_draws = A.take<uint32_t>(cap);
+        ps.deferred = A.take<float4>(2 * cap);
+        list = A.take<uint32_t>(cap);
+        deferred_count = A.take<uint32_t>(chunk_pixels);
+        stream_pos = A.take<uint32_t>(chunk_pixels);
+        if (!ps.rng_draws || !ps.deferred || !list || !deferred_count || !stream_pos)
+            return fail(ctx, YAR_ERR_CAPACITY, "static arena layout overflow");
+    }
+    ps.image_samples = image_samples;
     if (!s1d || !s2d || !ps.probe_hit2 || !q.prb_slot)
         return fail(ctx, YAR_ERR_CAPACITY, "static arena layout overflow");
     Scene_Dev S = scene_dev(ctx->ds, ctx->render);
@@ -687,21 +732,17 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
     cudaError_t e = cudaMemsetAsync(q.counters, 0, 8 * sizeof(uint32_t), st);  // the arena keeps the last call's data
     uint64_t rays_closest = 0, rays_any = 0;
     uint32_t launches = 0;
-    for (uint64_t first = 0; first < pixels && e == cudaSuccess; first += chunk_pixels) {
-        const uint32_t cp = (uint32_t)std::min<uint64_t>(chunk_pixels, pixels - first);
-        const uint32_t paths = cp * (uint32_t)p.spp;
-        launch_generate(p, (uint32_t)first, cp, s1d, reinterpret_cast<float*>(s2d), image_samples, ps, q, st);
-        launches++;
+    auto run_bounces = [&](const Render_Params& pp, uint32_t count, int bounce0) -> int {
         int cur = 0;
-        uint32_t count = paths;
-        for (int bounce = 0; count > 0 && bounce <= p.max_bounces + 1; bounce++) {
+        for (int it = 0; count > 0 && it <= p.max_bounces + 1; it++) {
+            const int bounce = bounce0 + it;
             e = trace_extend(ctx, q, cur, count, bounce, st);
             if (e != cudaSuccess) break;
             cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
-            launch_shade<false>(p, grid_for(count), st, S, cur, count, s1d, s2d, ps, q, Guide_Shade{});
+            launch_shade<false>(pp, grid_for(count), st, S, cur, count, s1d, s2d, ps, q, Guide_Shade{});
             e = trace_light_queues(ctx, q, ps, count, bounce, st);
             if (e != cudaSuccess) break;
-            connect_kernel<<<grid_for(count), kBlock, 0, st>>>(p, S, q.ext_slot[cur], count, ps, nullptr);
+            connect_kernel<<<grid_for(count), kBlock, 0, st>>>(pp, S, q.ext_slot[cur], count, ps, nullptr);
             launches += 5;
             uint32_t h[4];
             e = cudaMemcpyAsync(h, q.counters, sizeof(h), cudaMemcpyDeviceToHost, st);
@@ -712,6 +753,38 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
             rays_any += h[1];
             count = h[0];
             cur ^= 1;
+        }
+        return YAR_OK;
+    };
+    for (uint64_t first = 0; first < pixels && e == cudaSuccess; first += chunk_pixels) {
+        const uint32_t cp = (uint32_t)std::min<uint64_t>(chunk_pixels, pixels - first);
+        const uint32_t paths = cp * (uint32_t)p.spp;
+        ps.chunk_first = (uint32_t)first;
+        launch_generate(p, (uint32_t)first, cp, s1d, reinterpret_cast<float*>(s2d), image_samples, ps, q, st);
+        launches++;
+        if (int rc1 = run_bounces(p, paths, 0)) return rc1;
+        if (e != cudaSuccess) break;
+        if (p.exact_tail) {  // the waves of deferred samples, as render_run_params runs them
+            cudaMemsetAsync(tail, 0, 2 * sizeof(uint32_t), st);
+            tail_rank_kernel<<<grid_for(cp), kBlock, 0, st>>>(p, cp, ps, list, deferred_count, stream_pos, tail);
+            launches++;
+            uint32_t ht[2];
+            e = cudaMemcpyAsync(ht, tail, sizeof(ht), cudaMemcpyDeviceToHost, st);
+            if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+            if (e != cudaSuccess) break;
+            if (ht[1]) return fail(ctx, YAR_ERR_INVALID, "a path drew past the sampler budget before its deferral");
+            for (uint32_t wave = 0; wave < ht[0] && e == cudaSuccess; wave++) {
+                cudaMemsetAsync(q.counters, 0, sizeof(uint32_t), st);
+                tail_wave_kernel<<<grid_for(cp), kBlock, 0, st>>>(p_wave, (uint32_t)first, cp, wave, ps, q, list,
+                                                                  deferred_count, stream_pos);
+                launches++;
+                uint32_t n = 0;
+                e = cudaMemcpyAsync(&n, q.counters, sizeof(n), cudaMemcpyDeviceToHost, st);
+                if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+                if (e != cudaSuccess) break;
+                if (int rc1 = run_bounces(p_wave, n, yar_gpu_ctx::kBounceBuckets - 1)) return rc1;
+            }
+            if (e != cudaSuccess) break;
         }
         finish_chunk_kernel<<<grid_for(paths), kBlock, 0, st>>>(paths, first * p.spp, ps, radiance);
         launches++;
@@ -852,6 +925,8 @@ std::string start_or_resume(const fs::path& dir, const std::string& input_filena
 int render_checkpoint(yar_gpu_ctx* ctx, const char* directory, const char* input_filename, float* rgb_out,
                       yar_render_stats* stats) {
     if (!rgb_out || !directory || !input_filename) return fail(ctx, YAR_ERR_INVALID, "null argument");
+    if (ctx->render.config.rendering_algorithm == 0)
+        return fail(ctx, YAR_ERR_UNSUPPORTED, "checkpointed renders run the path tracer only (rendering_algorithm 1)");
     Render_Params p;
     if (int rc0 = prepare_render_params(ctx, p)) return rc0;
     const auto t_start = std::chrono::steady_clock::now();

@@ -470,10 +470,42 @@ __device__ __forceinline__ float glass_reflection_probability(const Bsdf& f, flo
 
 __device__ __forceinline__ float pow5(float v) { return (v * v) * (v * v) * v; }
 
-// FULL = false compiles out the plastic and coated-diffuse branches, for
-// scenes that only use the diffuse, metal and rough-glass BSDFs.
+// The FULL forms (every material, mixes included) are called out of line:
+// inlined at each of the shade kernels' call sites they multiplied the
+// kernels' code and took the device compiler minutes per kernel.  The
+// FULL = false forms (diffuse, metal, rough glass) stay inlined.
+template <bool FULL> __device__ __forceinline__ Col leaf_evaluate_body(const Bsdf& f, V3 wo, V3 wi);
+template <bool FULL> __device__ __forceinline__ float leaf_pdf_body(const Bsdf& f, V3 wo, V3 wi);
+template <bool FULL>
+__device__ __forceinline__ Col leaf_sample_body(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
+                                                float& pdf);
+static __device__ __noinline__ Col leaf_evaluate_full(const Bsdf& f, V3 wo, V3 wi) { return leaf_evaluate_body<true>(f, wo, wi); }
+static __device__ __noinline__ float leaf_pdf_full(const Bsdf& f, V3 wo, V3 wi) { return leaf_pdf_body<true>(f, wo, wi); }
+static __device__ __noinline__ Col leaf_sample_full(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
+                                             float& pdf) {
+    return leaf_sample_body<true>(f, u0, u1, u_scatter, wo, wi, pdf);
+}
 template <bool FULL = true>
 __device__ __forceinline__ Col leaf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
+    if constexpr (FULL) return leaf_evaluate_full(f, wo, wi);
+    else return leaf_evaluate_body<false>(f, wo, wi);
+}
+template <bool FULL = true>
+__device__ __forceinline__ float leaf_pdf(const Bsdf& f, V3 wo, V3 wi) {
+    if constexpr (FULL) return leaf_pdf_full(f, wo, wi);
+    else return leaf_pdf_body<false>(f, wo, wi);
+}
+template <bool FULL = true>
+__device__ __forceinline__ Col leaf_sample(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
+                                           float& pdf) {
+    if constexpr (FULL) return leaf_sample_full(f, u0, u1, u_scatter, wo, wi, pdf);
+    else return leaf_sample_body<false>(f, u0, u1, u_scatter, wo, wi, pdf);
+}
+
+// FULL = false compiles out the plastic and coated-diffuse branches, for
+// scenes that only use the diffuse, metal and rough-glass BSDFs.
+template <bool FULL>
+__device__ __forceinline__ Col leaf_evaluate_body(const Bsdf& f, V3 wo, V3 wi) {
     if (f.type == kDiffuse) return mul(f.reflectance, 1.f / kPi);
     if (FULL && (f.type == kPlastic || f.type == kPbrt3Plastic)) {
         // Plastic_BRDF::evaluate (src/ref/bsdf.cpp:215-234); Pbrt3_Plastic_BRDF::evaluate
@@ -582,8 +614,8 @@ __device__ __forceinline__ Col leaf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
     return mul(f.transmittance, base);
 }
 
-template <bool FULL = true>
-__device__ __forceinline__ float leaf_pdf(const Bsdf& f, V3 wo, V3 wi) {
+template <bool FULL>
+__device__ __forceinline__ float leaf_pdf_body(const Bsdf& f, V3 wo, V3 wi) {
     if (f.type == kDiffuse) return dot(f.n, wi) / kPi;
     if (FULL && (f.type == kPlastic || f.type == kPbrt3Plastic)) {  // Plastic_BRDF::pdf (src/ref/bsdf.cpp:253-263)
         const float diffuse_pdf = dot(f.n, wi) / kPi;
@@ -655,9 +687,9 @@ __device__ __forceinline__ float leaf_pdf(const Bsdf& f, V3 wo, V3 wi) {
 }
 
 // BSDF::sample; black when no direction is produced.
-template <bool FULL = true>
-__device__ __forceinline__ Col leaf_sample(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
-                                           float& pdf) {
+template <bool FULL>
+__device__ __forceinline__ Col leaf_sample_body(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
+                                                float& pdf) {
     if (FULL && f.type == kDiffuseTransmission) {  // Diffuse_Transmission_BSDF::sample (bsdf.cpp:114-126)
         const float max_r = max_component(f.reflectance), max_t = max_component(f.transmittance);
         const float sign = u_scatter < max_r / (max_r + max_t) ? 1.f : -1.f;
@@ -746,8 +778,8 @@ __device__ __forceinline__ Col leaf_sample(const Bsdf& f, float u0, float u1, fl
 __device__ __forceinline__ bool possible_for(const Bsdf& f, float n_dot_wi) {
     return (n_dot_wi > 0.f && f.reflection) || (n_dot_wi < 0.f && f.transmission);
 }
-template <bool FULL = true>
-__device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
+template <bool FULL>
+__device__ __forceinline__ Col bsdf_evaluate_body(const Bsdf& f, V3 wo, V3 wi) {
     if (FULL && f.type == kScaled) {
         Bsdf a = f;
         set_material(a, *f.sub[0]);
@@ -765,8 +797,8 @@ __device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
     }
     return leaf_evaluate<FULL>(f, wo, wi);
 }
-template <bool FULL = true>
-__device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
+template <bool FULL>
+__device__ __forceinline__ float bsdf_pdf_body(const Bsdf& f, V3 wo, V3 wi) {
     if (FULL && f.type == kScaled) {
         Bsdf a = f;
         set_material(a, *f.sub[0]);
@@ -786,9 +818,9 @@ __device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
 }
 // wi must come in as the zero vector: the reference's default-constructed
 // direction, which a leaf sample that gives up early leaves as it is.
-template <bool FULL = true>
-__device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
-                                           float& pdf) {
+template <bool FULL>
+__device__ __forceinline__ Col bsdf_sample_body(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
+                                                float& pdf) {
     if (FULL && f.type == kScaled) {
         Bsdf a = f;
         set_material(a, *f.sub[0]);
@@ -817,6 +849,29 @@ __device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, fl
         return (col(1.f, 1.f, 1.f) - f.mix_coeff) * f1 + f.mix_coeff * f2;
     }
     return leaf_sample<FULL>(f, u0, u1, u_scatter, wo, wi, pdf);
+}
+
+static __device__ __noinline__ Col bsdf_evaluate_full(const Bsdf& f, V3 wo, V3 wi) { return bsdf_evaluate_body<true>(f, wo, wi); }
+static __device__ __noinline__ float bsdf_pdf_full(const Bsdf& f, V3 wo, V3 wi) { return bsdf_pdf_body<true>(f, wo, wi); }
+static __device__ __noinline__ Col bsdf_sample_full(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
+                                             float& pdf) {
+    return bsdf_sample_body<true>(f, u0, u1, u_scatter, wo, wi, pdf);
+}
+template <bool FULL = true>
+__device__ __forceinline__ Col bsdf_evaluate(const Bsdf& f, V3 wo, V3 wi) {
+    if constexpr (FULL) return bsdf_evaluate_full(f, wo, wi);
+    else return bsdf_evaluate_body<false>(f, wo, wi);
+}
+template <bool FULL = true>
+__device__ __forceinline__ float bsdf_pdf(const Bsdf& f, V3 wo, V3 wi) {
+    if constexpr (FULL) return bsdf_pdf_full(f, wo, wi);
+    else return bsdf_pdf_body<false>(f, wo, wi);
+}
+template <bool FULL = true>
+__device__ __forceinline__ Col bsdf_sample(const Bsdf& f, float u0, float u1, float u_scatter, V3 wo, V3& wi,
+                                           float& pdf) {
+    if constexpr (FULL) return bsdf_sample_full(f, u0, u1, u_scatter, wo, wi, pdf);
+    else return bsdf_sample_body<false>(f, u0, u1, u_scatter, wo, wi, pdf);
 }
 
 // mis_power_heuristic (src/ref/direct_lighting.cpp:18-24)

@@ -778,6 +778,11 @@ __device__ __forceinline__ Col texture_bilinear(const Scene_Dev& S, uint4 mip, f
             mul(texel_repeat(S, mip, x0, y1), wy * (1 - wx))) +
            mul(texel_repeat(S, mip, x1, y1), wy * wx);
 }
+// Texels from lo to lo + span (span = hi - lo of integer-valued floats): 0 for
+// an empty or NaN span, at most 513.
+__device__ __forceinline__ int ewa_trip_count(float span) {
+    return span >= 0.f ? (span < 512.f ? (int)span + 1 : 513) : 0;
+}
 // do_EWA (image_texture.cpp:501-578) on one mip
 __device__ __noinline__ Col texture_ewa_level(const Scene_Dev& S, uint4 mip, float u, float v, float2 a1, float2 a2) {
     const float w = (float)mip.x, h = (float)mip.y;
@@ -799,9 +804,17 @@ __device__ __noinline__ Col texture_ewa_level(const Scene_Dev& S, uint4 mip, flo
     const float y0 = ceilf(v - v_delta), y1 = floorf(v + v_delta);
     Col sum = col(0.f, 0.f, 0.f);
     float weight_sum = 0.f;
-    for (float y = y0; y <= y1; y++) {
+    // The reference steps float counters (y++) over the footprint and asserts
+    // u_delta, v_delta < 256.  Integer trip counts visit the same integer-valued
+    // x and y (exact below 2^24) and end even outside that domain, where a
+    // float counter stops advancing; they are capped at the 513 texels per axis
+    // that the assertion allows (upload also refuses uv ranges that reach 2^22).
+    const int nx = ewa_trip_count(x1 - x0), ny = ewa_trip_count(y1 - y0);
+    for (int iy = 0; iy < ny; iy++) {
+        const float y = y0 + (float)iy;
         const float yy = y - v;
-        for (float x = x0; x <= x1; x++) {
+        for (int ix = 0; ix < nx; ix++) {
+            const float x = x0 + (float)ix;
             const float xx = x - u;
             const float r2 = A * xx * xx + B * xx * yy + C * yy * yy;
             if (r2 < 1.f) {

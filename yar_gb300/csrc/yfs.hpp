@@ -106,6 +106,7 @@ struct Scene {
         s.texture_mip_count = (uint32_t)texture_mips.size();
         s.texture_mips = texture_mips.empty() ? nullptr : texture_mips.data();
         s.texels = texels.empty() ? nullptr : texels.data();
+        s.texel_count = texels.size() / 3;
         return s;
     }
 };
@@ -346,8 +347,10 @@ inline bool read(const std::string& path, Scene& s, std::string* err = nullptr) 
         } else if (!memcmp(tag, "TEXS", 4)) {
             const uint32_t nt = c.pod<uint32_t>(), nm = c.pod<uint32_t>();
             const uint64_t nx = c.pod<uint64_t>();
-            if (!c.ok || (uint64_t)nt * sizeof(yar_texture_desc) + (uint64_t)nm * sizeof(yar_texture_mip_desc) +
-                                 nx * 12 > size)
+            // each count is checked against the chunk size before it is multiplied
+            if (!c.ok || nt > size / sizeof(yar_texture_desc) || nm > size / sizeof(yar_texture_mip_desc) ||
+                nx > size / 12 ||
+                (uint64_t)nt * sizeof(yar_texture_desc) + (uint64_t)nm * sizeof(yar_texture_mip_desc) + nx * 12 > size)
                 return fail("bad texture chunk");
             s.textures.resize(nt);
             c.raw(s.textures.data(), nt * sizeof(yar_texture_desc));

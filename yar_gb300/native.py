@@ -141,7 +141,7 @@ class FlatSceneDesc(C.Structure):
                 ("environment", C.POINTER(EnvironmentDesc)),
                 ("texture_count", C.c_uint32), ("textures", C.POINTER(TextureDesc)),
                 ("texture_mip_count", C.c_uint32), ("texture_mips", C.POINTER(TextureMipDesc)),
-                ("texels", C.c_void_p)]
+                ("texels", C.c_void_p), ("texel_count", C.c_uint64)]
 
 
 class HitSoa(C.Structure):

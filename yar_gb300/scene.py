@@ -239,6 +239,7 @@ class FlatScene:
             s.texture_mip_count = mips.shape[0]
             s.texture_mips = C.cast(mips.ctypes.data, C.POINTER(native.TextureMipDesc))
             s.texels = texels.ctypes.data
+            s.texel_count = texels.shape[0]
         C.memmove(C.byref(s.camera), np.ascontiguousarray(self.camera).ctypes.data, CAMERA_DTYPE.itemsize)
         C.memmove(C.byref(s.config), np.ascontiguousarray(self.config).ctypes.data, CONFIG_DTYPE.itemsize)
         return s, keep
