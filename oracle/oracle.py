@@ -186,6 +186,25 @@ def ref_cast(flat, rays, any_hit=False, threads=0, repeat=1):
     return (t, prim, obj, bary), info
 
 
+def ref_bench_cast(flat, rays, shadow, warmup=0, steps=1, threads=0, build=False):
+    """The ray-cast benchmark through the reference (harness bench-cast): W
+    untimed and K timed steps of one KdTree::intersect batch over `rays` and one
+    KdTree::intersect_any batch over `shadow` on all host threads.  build: the
+    kd-trees come from the reference builder instead of the flat scene."""
+    rays = np.ascontiguousarray(rays, np.float32).reshape(-1, 8)
+    shadow = np.ascontiguousarray(shadow, np.float32).reshape(-1, 8)
+    with tempfile.TemporaryDirectory() as d:
+        s, r, a = os.path.join(d, "s.yfs"), os.path.join(d, "r.bin"), os.path.join(d, "a.bin")
+        flat.write(s)
+        rays.tofile(r)
+        shadow.tofile(a)
+        args = ["bench-cast", s, r, a, "--threads=%d" % (threads or os.cpu_count() or 1), "--warmup=%d" % warmup,
+                "--steps=%d" % steps]
+        if build:
+            args.append("--build")
+        return _ref(*args)
+
+
 def ref_render_flat(flat, spp=0, threads=0):
     """The reference renderer on a flat scene (harness render-yfs)."""
     with tempfile.TemporaryDirectory() as d:

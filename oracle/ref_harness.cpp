@@ -23,6 +23,9 @@
 //       the scene tree for a batch of yar_ray records; closest writes
 //       f32 t[n], u32 prim[n], u32 obj[n], f32 bary[2n]; any writes u8[n].
 //       Prints {"rays":..,"seconds":..,"threads":..} on stdout.
+//   bench-cast <in.yfs> <rays.bin> <shadow_rays.bin> [--build] [--threads=T] [--warmup=W] [--steps=K]
+//       the ray-cast benchmark: reference kd-tree build (--build), then timed
+//       steps of one closest-hit and one any-hit batch.
 #include "std.h"
 // render-yfs sets the reference Camera's fields to the flat scene's exact
 // values; Camera keeps them private (src/ref/camera.h:41-48).
@@ -62,6 +65,9 @@ struct Args {
     int threads = 0;
     bool any = false;
     int repeat = 1;
+    int steps = 1;
+    int warmup = 0;
+    bool build = false;
     bool compress = false;
     float variance = 0.f;
     std::string input_file;
@@ -77,6 +83,9 @@ Args parse(int argc, char** argv) {
         else if (s.rfind("--seedoffset=", 0) == 0) a.seed_offset = atoi(s.c_str() + 13);
         else if (s.rfind("--threads=", 0) == 0) a.threads = atoi(s.c_str() + 10);
         else if (s.rfind("--repeat=", 0) == 0) a.repeat = atoi(s.c_str() + 9);
+        else if (s.rfind("--steps=", 0) == 0) a.steps = atoi(s.c_str() + 8);
+        else if (s.rfind("--warmup=", 0) == 0) a.warmup = atoi(s.c_str() + 9);
+        else if (s == "--build") a.build = true;
         else if (s == "--any") a.any = true;
         else if (s.rfind("--checkpoint-dir=", 0) == 0) a.checkpoint_dir = s.substr(17);
         else if (s == "--compress") a.compress = true;
@@ -569,13 +578,11 @@ int cmd_render(const Args& a) {
     return 0;
 }
 
-int cmd_build(const Args& a) {
-    if (a.pos.size() < 2) return 2;
-    yfs::Scene fs_scene;
-    std::string err;
-    if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
-    Ref_Scene rs;
-    load_ref_meshes(fs_scene, rs);
+// build_triangle_mesh_kdtree for every mesh (meshes on `threads` threads) and
+// build_scene_kdtree (src/ref/kdtree_builder.cpp:425-463); the trees are also
+// copied into the flat scene.
+void build_ref_trees(yfs::Scene& fs_scene, Ref_Scene& rs, int thread_count, float* mesh_seconds_out,
+                     float* scene_seconds_out) {
     Timestamp t;
     rs.kdtrees.resize(rs.meshes.size());
     std::atomic_int counter{0};
@@ -588,7 +595,7 @@ int cmd_build(const Args& a) {
     };
     {
         std::vector<std::jthread> threads;
-        for (int i = 1; i < std::min<int>(a.threads, (int)rs.meshes.size()); i++) threads.emplace_back(worker);
+        for (int i = 1; i < std::min<int>(thread_count, (int)rs.meshes.size()); i++) threads.emplace_back(worker);
         worker();
     }
     float mesh_seconds = elapsed_seconds(t);
@@ -608,6 +615,21 @@ int cmd_build(const Args& a) {
     memcpy(fs_scene.scene_bounds + 3, &rs.scene_kdtree.bounds.max_p.x, 12);
     fs_scene.scene_nodes.resize(rs.scene_kdtree.nodes.size());
     memcpy(fs_scene.scene_nodes.data(), rs.scene_kdtree.nodes.data(), rs.scene_kdtree.nodes.size() * 8);
+    for (size_t i = 0; i < rs.meshes.size(); i++) rs.kdtrees[i].set_geometry_data(&rs.geometry_data[i]);
+    rs.scene_kdtree.set_geometry_data(&rs.scene_data);
+    *mesh_seconds_out = mesh_seconds;
+    *scene_seconds_out = scene_seconds;
+}
+
+int cmd_build(const Args& a) {
+    if (a.pos.size() < 2) return 2;
+    yfs::Scene fs_scene;
+    std::string err;
+    if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
+    Ref_Scene rs;
+    load_ref_meshes(fs_scene, rs);
+    float mesh_seconds = 0.f, scene_seconds = 0.f;
+    build_ref_trees(fs_scene, rs, a.threads, &mesh_seconds, &scene_seconds);
     if (!yfs::write(a.pos[1], fs_scene)) return 1;
     if (!a.cache_dir.empty()) {  // the reference's own cache files (KdTree::save)
         for (size_t i = 0; i < rs.kdtrees.size(); i++)
@@ -619,13 +641,8 @@ int cmd_build(const Args& a) {
     return 0;
 }
 
-int cmd_cast(const Args& a) {
-    if (a.pos.size() < 3) return 2;
-    yfs::Scene fs_scene;
-    std::string err;
-    if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
-    Ref_Scene rs;
-    load_ref_meshes(fs_scene, rs);
+// The kd-trees stored in a flat scene, as reference KdTree objects.
+void load_ref_trees(const yfs::Scene& fs_scene, Ref_Scene& rs) {
     rs.kdtrees.resize(rs.meshes.size());
     for (size_t i = 0; i < rs.meshes.size(); i++) {
         KdTree& kt = rs.kdtrees[i];
@@ -640,24 +657,42 @@ int cmd_cast(const Args& a) {
     rs.scene_kdtree.nodes.resize(fs_scene.scene_nodes.size());
     memcpy(rs.scene_kdtree.nodes.data(), fs_scene.scene_nodes.data(), fs_scene.scene_nodes.size() * 8);
     rs.scene_kdtree.set_geometry_data(&rs.scene_data);
+}
 
-    std::vector<uint8_t> raw;
-    {
-        FILE* f = fopen(a.pos[1].c_str(), "rb");
-        if (!f) return 1;
-        fseek(f, 0, SEEK_END);
-        long size = ftell(f);
-        fseek(f, 0, SEEK_SET);
-        raw.resize((size_t)size);
-        if (fread(raw.data(), 1, raw.size(), f) != raw.size()) { fclose(f); return 1; }
-        fclose(f);
+bool read_file(const std::string& path, std::vector<uint8_t>& raw) {
+    FILE* f = fopen(path.c_str(), "rb");
+    if (!f) return false;
+    fseek(f, 0, SEEK_END);
+    long size = ftell(f);
+    fseek(f, 0, SEEK_SET);
+    raw.resize((size_t)size);
+    const bool ok = fread(raw.data(), 1, raw.size(), f) == raw.size();
+    fclose(f);
+    return ok;
+}
+
+// Casts a batch of yar_ray records through the scene tree on `thread_count`
+// threads (chunks of 4096 rays taken from a shared counter); returns seconds.
+struct Cast_Out {
+    std::vector<float> t, bary;
+    std::vector<uint32_t> prim, obj;
+    std::vector<uint8_t> occluded;
+};
+
+double cast_rays(const Ref_Scene& rs, const yar_ray* rays, size_t n, bool any, int thread_count, Cast_Out& o) {
+    if (any) {
+        o.occluded.resize(n);
+    } else {
+        o.t.resize(n);
+        o.bary.resize(2 * n);
+        o.prim.resize(n);
+        o.obj.resize(n);
     }
-    const size_t n = raw.size() / sizeof(yar_ray);
-    const yar_ray* rays = (const yar_ray*)raw.data();
-    std::vector<float> t(n), bary(2 * n);
-    std::vector<uint32_t> prim(n), obj(n);
-    std::vector<uint8_t> occluded(n);
-
+    std::vector<float>& t = o.t;
+    std::vector<float>& bary = o.bary;
+    std::vector<uint32_t>& prim = o.prim;
+    std::vector<uint32_t>& obj = o.obj;
+    std::vector<uint8_t>& occluded = o.occluded;
     std::atomic<size_t> next{0};
     const size_t chunk = 4096;
     auto worker = [&] {
@@ -668,7 +703,7 @@ int cmd_cast(const Args& a) {
             size_t end = std::min(n, begin + chunk);
             for (size_t i = begin; i < end; i++) {
                 Ray ray{Vector3(rays[i].origin), Vector3(rays[i].direction)};
-                if (a.any) {
+                if (any) {
                     occluded[i] = rs.scene_kdtree.intersect_any(ray, rays[i].tmax) ? 1 : 0;
                 } else {
                     Intersection isect;
@@ -690,30 +725,81 @@ int cmd_cast(const Args& a) {
             }
         }
     };
-    double best = 1e30;
-    for (int r = 0; r < std::max(1, a.repeat); r++) {
-        next = 0;
-        Timestamp ts;
-        {
-            std::vector<std::jthread> threads;
-            for (int i = 1; i < a.threads; i++) threads.emplace_back(worker);
-            worker();
-        }
-        best = std::min(best, (double)elapsed_nanoseconds(ts) / 1e9);
+    Timestamp ts;
+    {
+        std::vector<std::jthread> threads;
+        for (int i = 1; i < thread_count; i++) threads.emplace_back(worker);
+        worker();
     }
+    return (double)elapsed_nanoseconds(ts) / 1e9;
+}
+
+int cmd_cast(const Args& a) {
+    if (a.pos.size() < 3) return 2;
+    yfs::Scene fs_scene;
+    std::string err;
+    if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
+    Ref_Scene rs;
+    load_ref_meshes(fs_scene, rs);
+    load_ref_trees(fs_scene, rs);
+    std::vector<uint8_t> raw;
+    if (!read_file(a.pos[1], raw)) return 1;
+    const size_t n = raw.size() / sizeof(yar_ray);
+    const yar_ray* rays = (const yar_ray*)raw.data();
+    Cast_Out o;
+    double best = 1e30;
+    for (int r = 0; r < std::max(1, a.repeat); r++) best = std::min(best, cast_rays(rs, rays, n, a.any, a.threads, o));
     FILE* f = fopen(a.pos[2].c_str(), "wb");
     if (!f) return 1;
     if (a.any) {
-        fwrite(occluded.data(), 1, n, f);
+        fwrite(o.occluded.data(), 1, n, f);
     } else {
-        fwrite(t.data(), 4, n, f);
-        fwrite(prim.data(), 4, n, f);
-        fwrite(obj.data(), 4, n, f);
-        fwrite(bary.data(), 4, 2 * n, f);
+        fwrite(o.t.data(), 4, n, f);
+        fwrite(o.prim.data(), 4, n, f);
+        fwrite(o.obj.data(), 4, n, f);
+        fwrite(o.bary.data(), 4, 2 * n, f);
     }
     fclose(f);
     printf("{\"rays\": %zu, \"seconds\": %.6f, \"threads\": %d, \"kind\": \"%s\"}\n", n, best, a.threads,
            a.any ? "any" : "closest");
+    return 0;
+}
+
+// bench-cast <in.yfs> <rays.bin> <shadow_rays.bin> [--build] [--threads=T] [--warmup=W] [--steps=K]
+// The reference's ray-cast path end to end for the ray-cast benchmark: with
+// --build the kd-trees come from the reference's own builder (else from the
+// flat scene), then W untimed and K timed steps, each one closest-hit batch
+// (KdTree::intersect) and one any-hit batch (KdTree::intersect_any) over all
+// rays on T threads.  Prints the build and per-step times.
+int cmd_bench_cast(const Args& a) {
+    if (a.pos.size() < 3) return 2;
+    yfs::Scene fs_scene;
+    std::string err;
+    if (!yfs::read(a.pos[0], fs_scene, &err)) { fprintf(stderr, "read: %s\n", err.c_str()); return 1; }
+    Ref_Scene rs;
+    load_ref_meshes(fs_scene, rs);
+    float mesh_seconds = 0.f, scene_seconds = 0.f;
+    if (a.build) build_ref_trees(fs_scene, rs, a.threads, &mesh_seconds, &scene_seconds);
+    else load_ref_trees(fs_scene, rs);
+    std::vector<uint8_t> raw_c, raw_a;
+    if (!read_file(a.pos[1], raw_c) || !read_file(a.pos[2], raw_a)) return 1;
+    const size_t nc = raw_c.size() / sizeof(yar_ray), na = raw_a.size() / sizeof(yar_ray);
+    Cast_Out oc, oa;
+    for (int w = 0; w < a.warmup; w++) {
+        cast_rays(rs, (const yar_ray*)raw_c.data(), nc, false, a.threads, oc);
+        cast_rays(rs, (const yar_ray*)raw_a.data(), na, true, a.threads, oa);
+    }
+    std::string steps;
+    for (int s = 0; s < std::max(1, a.steps); s++) {
+        const double c = cast_rays(rs, (const yar_ray*)raw_c.data(), nc, false, a.threads, oc);
+        const double y = cast_rays(rs, (const yar_ray*)raw_a.data(), na, true, a.threads, oa);
+        char buf[96];
+        snprintf(buf, sizeof(buf), "%s[%.6f, %.6f]", s ? ", " : "", c, y);
+        steps += buf;
+    }
+    printf("{\"closest_rays\": %zu, \"any_rays\": %zu, \"threads\": %d, \"built\": %s, "
+           "\"mesh_build_seconds\": %.3f, \"scene_build_seconds\": %.3f, \"steps\": [%s]}\n",
+           nc, na, a.threads, a.build ? "true" : "false", mesh_seconds, scene_seconds, steps.c_str());
     return 0;
 }
 
@@ -1079,6 +1165,7 @@ int main(int argc, char** argv) {
     else if (cmd == "render") rc = cmd_render(a);
     else if (cmd == "build") rc = cmd_build(a);
     else if (cmd == "cast") rc = cmd_cast(a);
+    else if (cmd == "bench-cast") rc = cmd_bench_cast(a);
     else if (cmd == "regress") rc = cmd_regress(a);
     else if (cmd == "render-yfs") rc = cmd_render_yfs(a);
     else if (cmd == "exr") rc = cmd_exr(a);
