@@ -511,6 +511,13 @@ int yar_gpu_guided_render(yar_gpu_ctx* ctx, const yar_guided_params* params, dou
 int yar_guide_set_params(yar_gpu_ctx* ctx, const float* params);
 int yar_guide_get_params(yar_gpu_ctx* ctx, float* params);
 int yar_guide_infer(yar_gpu_ctx* ctx, const float* queries, uint32_t n, const float box[6], float* lobes);
+
+/* Diagnostic, no counterpart in the reference: runs the tensor-core kernels'
+ * bounded mbarrier wait (`limit` polls, 1..2^24) on a barrier that nothing
+ * arrives at.  Returns YAR_ERR_TIMEOUT once the wait gives up - the status the
+ * network kernels report when a tensor-core wait runs out - and leaves the
+ * context usable. */
+int yar_gpu_wait_selftest(yar_gpu_ctx* ctx, uint32_t limit);
 /* summed gradient of the loss (device, YAR_GUIDE_PARAMS floats); loss to the host */
 int yar_guide_gradient(yar_gpu_ctx* ctx, const float* samples, uint32_t n, const float box[6], float weight_scale,
                        float* grad, float* loss);

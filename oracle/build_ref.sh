@@ -13,11 +13,12 @@
 # oracle/_ref/src (git-ignored) so it can be rebuilt on an aarch64 host that
 # has no access to the reference tree.
 #
-# usage: oracle/build_ref.sh [REFERENCE_ROOT]   (default: /root/reference)
+# usage: oracle/build_ref.sh [REFERENCE_ROOT]
+#   (default: $YAR_REFERENCE_ROOT, else a `reference` folder beside the repository)
 set -euo pipefail
 HERE="$(cd "$(dirname "${BASH_SOURCE[0]}")" && pwd)"
 OUT="$HERE/_ref"
-REF="${1:-/root/reference}"
+REF="${1:-${YAR_REFERENCE_ROOT:-$(cd "$HERE/../.." && pwd)/reference}}"
 SRC="$OUT/src"
 
 if [ -d "$REF/src/ref" ]; then

@@ -93,7 +93,9 @@ from yar_gb300 import scenes  # noqa: E402
 from yar_gb300.scene import FlatScene, Mesh, make_object  # noqa: E402
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REFERENCE = "/root/reference"
+from yar_gb300.build import reference_root  # noqa: E402
+
+REFERENCE = reference_root()  # $YAR_REFERENCE_ROOT, else a `reference` folder beside the repository
 
 
 def rays_and_results(flat, seed, n=4096):

@@ -192,3 +192,20 @@ def test_training_concentrates_the_mixture(gpu_ctx):
     c = (mu * torch.as_tensor(target, dtype=torch.float32)).sum(2)
     dens = (pi * kappa / (2 * math.pi * (1 - torch.exp(-2 * kappa))) * torch.exp(kappa * (c - 1))).sum(1)
     assert float(dens.median()) > 10.0 / (4 * math.pi), float(dens.median())
+
+
+def test_bounded_wait_gives_up_and_the_context_stays_usable(gpu_ctx):
+    """The tensor-core kernels wait on mbarriers with an iteration limit.  A
+    wait on a barrier that nothing arrives at (a 1000-poll test limit) must
+    come back as YAR_ERR_TIMEOUT, and the next network call must work."""
+    with pytest.raises(native.YarError) as e:
+        gpu_ctx.wait_selftest(1000)
+    assert e.value.code == native.YAR_ERR_TIMEOUT
+    params = random_params(5)
+    gpu_ctx.guide_set_params(params)
+    n = 256
+    q = device(random_rows(n, 77))
+    lobes = torch.zeros((n, 40), dtype=torch.float32, device="cuda")
+    gpu_ctx.guide_infer(q.data_ptr(), n, BOX, lobes.data_ptr())
+    got = lobes.cpu().numpy().reshape(n, 8, 5)
+    assert np.allclose(got[:, :, 4].sum(1), 1.0, atol=1e-5)

@@ -7,7 +7,7 @@
 SCENE is a .yfs flat scene (the reference's pbrt-v3 loader and kd-tree
 builder flattened by the reference harness: `yar_ref flatten scene.pbrt
 scene.yfs`, or FlatScene.write from the generators) or a built-in generator:
-cornell, large, room.  Options mirror the reference's RAY (--spp rounds up
+large, room.  Options mirror the reference's RAY (--spp rounds up
 to a perfect square as RAY does; --seedoffset offsets the pixel streams).
 The EXR carries YAR's attributes with yar_render_device = gpu.
 """
@@ -20,21 +20,11 @@ from .scene import FlatScene
 
 
 def load(name):
-    if name == "cornell":
-        return _cornell()
     if name == "large":
         return scenes.large_scene()
     if name == "room":
         return scenes.hard_lighting_room()
     return FlatScene.read(name)
-
-
-def _cornell():
-    """The C1 Cornell box as the reference flattened it (64 x 64, 16 spp)."""
-    import os
-    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "tests", "golden",
-                        "cornell_c1_64.yfs")
-    return FlatScene.read(path)
 
 
 def main(argv=None):

@@ -100,10 +100,18 @@ def build_oracle():
     return ORACLE_LIB
 
 
+def reference_root():
+    """The reference checkout: $YAR_REFERENCE_ROOT, else a `reference` folder
+    beside this repository."""
+    return os.environ.get("YAR_REFERENCE_ROOT") or os.path.join(os.path.dirname(ROOT), "reference")
+
+
 def build_reference():
     """Build oracle/_ref from the reference sources when they are present."""
     script = os.path.join(ORACLE_DIR, "build_ref.sh")
-    have_src = os.path.isdir("/root/reference/src/ref") or os.path.isdir(os.path.join(ORACLE_DIR, "_ref", "src", "src", "ref"))
+    ref = reference_root()
+    have_src = os.path.isdir(os.path.join(ref, "src", "ref")) or \
+        os.path.isdir(os.path.join(ORACLE_DIR, "_ref", "src", "src", "ref"))
     if not have_src:
         return None
     binary = os.path.join(ORACLE_DIR, "_ref", "yar_ref")
@@ -115,7 +123,7 @@ def build_reference():
             return binary
         except OSError:
             pass
-    _run(["bash", script])
+    _run(["bash", script, ref])
     return binary
 
 

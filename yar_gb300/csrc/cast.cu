@@ -12,6 +12,7 @@
 // the ray's index) and the render wavefront (hit records at the path slot).
 #include "context.hpp"
 
+#include <atomic>
 #include <type_traits>
 
 namespace yar {
@@ -76,14 +77,33 @@ __global__ void __launch_bounds__(kCastBlock, MINB) cast_persistent(Device_Scene
                 const float4 r0 = __ldg(a.rays + 2 * (size_t)ray);
                 const float4 r1 = __ldg(a.rays + 2 * (size_t)ray + 1);
                 tr.begin(s, ray, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z), r0.w);
-                have = true;
+                if (tr.mode() == kDone)  // missed the scene box: done, take another
+                    write_result<ANY>(tr, a.perm ? __ldg(a.perm + ray) : ray, a);
+                else
+                    have = true;
             }
             const uint32_t taken = (uint32_t)__popc(want) < avail ? (uint32_t)__popc(want) : avail;
             batch_next += taken;
             want = __ballot_sync(full, !have && alive);
         }
-        if (!__any_sync(full, have)) break;
-        if (have && !tr.template step<MAXD>(s, a.rays, stack)) {
+        // Run one mode for the whole warp: the mode most lanes are in
+        // (descents win ties).  Lanes in other modes wait, so the lanes that
+        // run share one code path instead of the warp running every mode's
+        // code with a few lanes each.
+        const int m = have ? tr.mode() : -1;  // every lane with a ray is in one of the three modes
+        const unsigned md = __ballot_sync(full, m == kDescend);
+        const unsigned mm = __ballot_sync(full, m == kMeshLeaf);
+        const unsigned ms = __ballot_sync(full, m == kSceneLeaf);
+        if (!(md | mm | ms)) break;
+        const int nd = __popc(md), nm = __popc(mm), ns = __popc(ms);
+        if (nd >= nm && nd >= ns) {
+            if (m == kDescend) tr.template step_descend<MAXD>(s, a.rays, stack);
+        } else if (nm >= ns) {
+            if (m == kMeshLeaf) tr.step_mesh_leaf(s, a.rays, stack);
+        } else {
+            if (m == kSceneLeaf) tr.step_scene_leaf(s, a.rays, stack);
+        }
+        if (have && tr.mode() == kDone) {
             write_result<ANY>(tr, a.perm ? __ldg(a.perm + ray) : ray, a);
             have = false;
         }
@@ -110,29 +130,47 @@ __global__ void __launch_bounds__(kCastBlock) cast_per_ray(Device_Scene s, Cast_
 }
 
 // Persistent launch shape, measured on GB300 with the 2.42M-triangle ray-cast
-// workload (16M + 16M incoherent rays).  High-occupancy variant: closest hit
-// at 8 resident blocks of 128 threads per SM (64 registers: 25.3 ms, against
-// 25.2 ms at 10 blocks, 26.4 ms at 12, 31.1 ms at 16), any hit at 12 blocks
-// (40 registers: 12.6 ms, against 14.3 ms at 8, 13.3 ms at 10, 14.1 ms at
-// 16).  Descending to a leaf per step (while-while) beat one node per step
-// and four nodes per step; testing all of a leaf's triangles in one step was
-// slower (27.0 against 25.3 ms); the local-memory stack beat an 8- or
-// 16-entry shared-memory stack with local overflow.
-constexpr int kWhileWhile = 1 << 30;
+// workload (16M + 16M incoherent rays).  With one mode per warp iteration,
+// one node fetch per descent step: closest hit 19.8 ms against 21.3 ms at two
+// nodes per step, 21.6 ms at four and 25.7 ms descending to a leaf (the
+// per-lane schedule, every mode's code each iteration, took 25.4 ms).  High-
+// occupancy variant: closest hit at 10 resident blocks of 128 threads per SM
+// (19.0 ms, against 19.8 ms at 8 and 21.0 ms at 6), any hit at 12 blocks
+// (11.2 ms, against 11.6 ms at 10 and 12.7 ms at 8).  Earlier, with the
+// per-lane schedule: testing all of a leaf's triangles in one step was slower,
+// and the local-memory stack beat an 8- or 16-entry shared-memory stack with
+// local overflow.
+#ifndef YAR_CAST_NODES_PER_STEP
+#define YAR_CAST_NODES_PER_STEP 1
+#endif
+constexpr int kWhileWhile = YAR_CAST_NODES_PER_STEP;
 constexpr int kSharedStackEntries = 0;
+#ifndef YAR_CAST_BLOCKS_CLOSEST
+#define YAR_CAST_BLOCKS_CLOSEST 10
+#endif
+#ifndef YAR_CAST_BLOCKS_ANY
+#define YAR_CAST_BLOCKS_ANY 12
+#endif
 template <bool ANY>
-constexpr int kHighOccupancyBlocks = ANY ? 12 : 8;
+constexpr int kHighOccupancyBlocks = ANY ? YAR_CAST_BLOCKS_ANY : YAR_CAST_BLOCKS_CLOSEST;
 
+// Resident blocks of a persistent kernel on the current device: SM count x
+// blocks per SM, looked up once per device (devices may differ in SM count).
+constexpr int kMaxDevices = 64;
 template <class Kernel>
-int resident_grid(Kernel kernel, int& cache) {
-    if (cache == 0) {
-        int dev = 0, sms = 0, per_sm = 0;
-        cudaGetDevice(&dev);
+int resident_grid(Kernel kernel, std::atomic<int>* cache) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    std::atomic<int>& slot = cache[(unsigned)dev < (unsigned)kMaxDevices ? dev : 0];
+    int g = slot.load(std::memory_order_relaxed);
+    if (g == 0) {
+        int sms = 0, per_sm = 0;
         cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
         cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kernel, kCastBlock, 0);
-        cache = sms * (per_sm > 0 ? per_sm : 1);
+        g = sms * (per_sm > 0 ? per_sm : 1);
+        if ((unsigned)dev < (unsigned)kMaxDevices) slot.store(g, std::memory_order_relaxed);
     }
-    return cache;
+    return g;
 }
 
 template <bool ANY>
@@ -146,11 +184,11 @@ cudaError_t launch(const Device_Scene& s, const Cast_Args& a, int kernel, cudaSt
     cudaError_t e = cudaMemsetAsync(a.next_ray, 0, sizeof(uint32_t), stream);
     if (e != cudaSuccess) return e;
     if (kernel == kCastPersistent128) {
-        static int grid = 0;
+        static std::atomic<int> grid[kMaxDevices];
         auto k = cast_persistent<ANY, 4, kWhileWhile, kSharedStackEntries>;
         k<<<resident_grid(k, grid), kCastBlock, 0, stream>>>(s, a);
     } else {
-        static int grid = 0;
+        static std::atomic<int> grid[kMaxDevices];
         auto k = cast_persistent<ANY, kHighOccupancyBlocks<ANY>, kWhileWhile, kSharedStackEntries>;
         k<<<resident_grid(k, grid), kCastBlock, 0, stream>>>(s, a);
     }

@@ -237,150 +237,189 @@ struct Traversal {
         cinv = make_float3(1.f / rd.x, 1.f / rd.y, 1.f / rd.z);
     }
 
-    // `stack` holds kStackEntries entries (Local_Stack or Split_Stack; kept out
-    // of this struct so the scalar state can live in registers).  A descent
-    // stops at a leaf or after MAXD interior nodes.
+    // The current level's leaf is done: pop the level's next node, or end the
+    // level (leave the mesh; finish the ray at the scene level).
+    template <class STACK>
+    __device__ __forceinline__ void leaf_done(const Device_Scene& s, const float4* rays, STACK& stack) {
+        if (in_mesh()) {
+            if (sp == mesh_sp_base) {
+                leave_mesh(s, rays, stack);
+                return;
+            }
+        } else if (sp == 0) {
+            finish(ANY ? 0 : (hit.t < ray_tmax ? 1 : 0));
+            return;
+        }
+        --sp;
+        const uint2 e = stack.pop(sp);
+        node = e.x;
+        t_min = t_max;
+        t_max = __uint_as_float(e.y);
+        set_mode(kDescend);
+    }
+
+    // DESCEND: up to MAXD node fetches of the current level.  A leaf with
+    // primitives to process switches the mode; an empty leaf (or a mesh leaf
+    // whose triangles this ray kind skips) is done at once, as the reference's
+    // leaf callback returns without work, and the descent goes on from the
+    // popped node.  `stack` holds kStackEntries entries (Local_Stack or
+    // Split_Stack; kept out of this struct so the scalar state can live in
+    // registers).
+    template <int MAXD, class STACK>
+    __device__ __forceinline__ void step_descend(const Device_Scene& s, const float4* rays, STACK& stack) {
+        for (int steps = 0; steps < MAXD; steps++) {
+            const uint2* nodes = in_mesh() ? s.mesh_nodes + mesh_offset : s.scene_nodes;
+            const float limit = ANY ? ray_tmax : hit.t;
+            if (!(limit > t_min)) {  // the level's loop condition failed
+                if (in_mesh()) {
+                    leave_mesh(s, rays, stack);
+                } else {
+                    finish(ANY ? 0 : (hit.t < ray_tmax ? 1 : 0));
+                }
+                return;
+            }
+            const uint2 n = __ldg(nodes + node);
+            if ((n.x & 3u) == 3u) {
+                const bool skip = in_mesh() && !((flags >> 3) & 1u);
+                if ((n.x >> 2) == 0u || skip) {
+                    leaf_done(s, rays, stack);
+                    if (mode() != kDescend) return;
+                    continue;
+                }
+                leaf_i = 0;
+                set_mode(in_mesh() ? kMeshLeaf : kSceneLeaf);
+                return;
+            }
+            const int axis = (int)(n.x & 3u);
+            const float dist = __uint_as_float(n.y) - sel3(co.x, co.y, co.z, axis);
+            const uint32_t below_child = node + 1;
+            const uint32_t above_child = n.x >> 2;
+            if (dist != 0.f) {
+                const bool below_first = dist > 0.f;
+                const uint32_t first_child = below_first ? below_child : above_child;
+                const uint32_t second_child = below_first ? above_child : below_child;
+                const float t_split = dist * sel3(cinv.x, cinv.y, cinv.z, axis);
+                if (t_split > t_max || t_split < 0.f) {
+                    node = first_child;
+                } else if (t_split < t_min) {
+                    node = second_child;
+                } else {
+                    if (sp >= kStackEntries) {
+                        finish(-1);
+                        return;
+                    }
+                    stack.push(sp, second_child, t_max);
+                    sp++;
+                    node = first_child;
+                    t_max = t_split;
+                }
+            } else {
+                node = (sel3(cd.x, cd.y, cd.z, axis) > 0.f) ? above_child : below_child;
+            }
+        }
+    }
+
+    // MESH_LEAF: one triangle test of the current mesh leaf; after the leaf's
+    // last triangle the leaf is done in the same step.
+    template <class STACK>
+    __device__ __forceinline__ void step_mesh_leaf(const Device_Scene& s, const float4* rays, STACK& stack) {
+        const uint2* nodes = s.mesh_nodes + mesh_offset;
+        const uint2 leaf = __ldg(nodes + node);
+        const uint32_t count = leaf.x >> 2;
+        if (leaf_i < count) {
+            const uint32_t prim =
+                (leaf_i == 0) ? leaf.y : __ldg(reinterpret_cast<const uint32_t*>(nodes + node) + 1 + leaf_i);
+            leaf_i++;
+            const float4* tp = s.tris + 3 * ((size_t)tri_offset + prim);
+            const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
+            Watertight_Ray wr;
+            wr.kx = (int)((flags >> 4) & 3u);
+            wr.ky = (int)((flags >> 6) & 3u);
+            wr.kz = (int)((flags >> 8) & 3u);
+            wr.sx = sx;
+            wr.sy = sy;
+            wr.sz = sz;
+            float b0, b1, b2;
+            const float t = watertight(co, wr, v0, v1, v2, b0, b1, b2);
+            if (ANY) {
+                // `t >= ray_tmax` rejects; a NaN t does not (src/ref/kdtree.cpp:60-62)
+                if (!(t >= ray_tmax) && v0.w == 0.f) {
+                    finish(1);
+                    return;
+                }
+            } else if (t < hit.t && v0.w == 0.f) {
+                // the object of the closest hit is the one whose mesh produced it
+                // (src/ref/kdtree.cpp:81-95 sets it after the mesh improved the hit)
+                hit.t = t;
+                hit.prim = prim;
+                hit.object = cur_object;
+                hit.b0 = b0;
+                hit.b1 = b1;
+                hit.b2 = b2;
+            }
+            if (leaf_i < count) return;
+        }
+        leaf_done(s, rays, stack);
+    }
+
+    // SCENE_LEAF: one object of the current scene leaf (transform the ray into
+    // the object's space and clip it to the mesh bounds; when it overlaps,
+    // save the scene level on the stack and descend the mesh tree), or, with
+    // every object done, the end of the leaf.
+    template <class STACK>
+    __device__ __forceinline__ void step_scene_leaf(const Device_Scene& s, const float4* rays, STACK& stack) {
+        const uint2 leaf = __ldg(s.scene_nodes + node);
+        const uint32_t count = leaf.x >> 2;
+        if (leaf_i < count) {
+            const uint32_t obj =
+                (leaf_i == 0) ? leaf.y : __ldg(reinterpret_cast<const uint32_t*>(s.scene_nodes + node) + 1 + leaf_i);
+            leaf_i++;
+            const float4* p = s.objects + 6 * (size_t)obj;
+            const float4 r0 = __ldg(p + 0), r1 = __ldg(p + 1), r2 = __ldg(p + 2);
+            const float4 lo = __ldg(p + 3), hi = __ldg(p + 4), info = __ldg(p + 5);
+            float3 oo, od;
+            transform_ray(r0, r1, r2, co, cd, oo, od);
+            float mt_min, mt_max;
+            if (clip_ray(make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z), oo, od, mt_min, mt_max)) {
+                if (sp + 2 > kStackEntries) {
+                    finish(-1);
+                    return;
+                }
+                stack.push(sp, __float_as_uint(t_min), t_max);  // the scene level's interval
+                stack.push(sp + 1, node, __uint_as_float(leaf_i));  // and its leaf cursor
+                sp += 2;
+                mesh_sp_base = sp;
+                cur_object = obj;
+                co = oo;
+                cd = od;
+                cinv = make_float3(1.f / od.x, 1.f / od.y, 1.f / od.z);
+                mesh_offset = __float_as_uint(lo.w);
+                tri_offset = __float_as_uint(hi.w);
+                const int visibility = __float_as_int(info.y);
+                const bool test_triangles = ANY ? (visibility == 0) : (visibility != 2);
+                const Watertight_Ray wr = watertight_setup(od);
+                sx = wr.sx;
+                sy = wr.sy;
+                sz = wr.sz;
+                flags = (flags & (3u << 10)) | (uint32_t)kDescend | 4u | (test_triangles ? 8u : 0u) |
+                        ((uint32_t)wr.kx << 4) | ((uint32_t)wr.ky << 6) | ((uint32_t)wr.kz << 8);
+                node = 0;
+                t_min = mt_min;
+                t_max = mt_max;
+            }
+            return;
+        }
+        leaf_done(s, rays, stack);
+    }
+
+    // One unit of work in the current mode; false once the ray is finished.
+    // A descent stops at a leaf or after MAXD node fetches.
     template <int MAXD, class STACK>
     __device__ __forceinline__ bool step(const Device_Scene& s, const float4* rays, STACK& stack) {
         const int m = mode();
-        if (m == kDescend) {
-            const uint2* nodes = in_mesh() ? s.mesh_nodes + mesh_offset : s.scene_nodes;
-            for (int steps = 0; steps < MAXD; steps++) {  // descend through interior nodes of the current level
-                const float limit = ANY ? ray_tmax : hit.t;
-                if (!(limit > t_min)) {  // the level's loop condition failed
-                    if (in_mesh()) {
-                        leave_mesh(s, rays, stack);
-                    } else {
-                        finish(ANY ? 0 : (hit.t < ray_tmax ? 1 : 0));
-                    }
-                    break;
-                }
-                const uint2 n = __ldg(nodes + node);
-                if ((n.x & 3u) == 3u) {
-                    leaf_i = 0;
-                    set_mode(in_mesh() ? kMeshLeaf : kSceneLeaf);
-                    break;
-                }
-                const int axis = (int)(n.x & 3u);
-                const float dist = __uint_as_float(n.y) - sel3(co.x, co.y, co.z, axis);
-                const uint32_t below_child = node + 1;
-                const uint32_t above_child = n.x >> 2;
-                if (dist != 0.f) {
-                    const bool below_first = dist > 0.f;
-                    const uint32_t first_child = below_first ? below_child : above_child;
-                    const uint32_t second_child = below_first ? above_child : below_child;
-                    const float t_split = dist * sel3(cinv.x, cinv.y, cinv.z, axis);
-                    if (t_split > t_max || t_split < 0.f) {
-                        node = first_child;
-                    } else if (t_split < t_min) {
-                        node = second_child;
-                    } else {
-                        if (sp >= kStackEntries) {
-                            finish(-1);
-                            break;
-                        }
-                        stack.push(sp, second_child, t_max);
-                        sp++;
-                        node = first_child;
-                        t_max = t_split;
-                    }
-                } else {
-                    node = (sel3(cd.x, cd.y, cd.z, axis) > 0.f) ? above_child : below_child;
-                }
-            }
-        } else if (m == kMeshLeaf) {
-            const uint2* nodes = s.mesh_nodes + mesh_offset;
-            const uint2 leaf = __ldg(nodes + node);
-            const uint32_t count = ((flags >> 3) & 1u) ? (leaf.x >> 2) : 0u;
-            if (leaf_i < count) {
-                const uint32_t prim =
-                    (leaf_i == 0) ? leaf.y : __ldg(reinterpret_cast<const uint32_t*>(nodes + node) + 1 + leaf_i);
-                leaf_i++;
-                const float4* tp = s.tris + 3 * ((size_t)tri_offset + prim);
-                const float4 v0 = __ldg(tp), v1 = __ldg(tp + 1), v2 = __ldg(tp + 2);
-                Watertight_Ray wr;
-                wr.kx = (int)((flags >> 4) & 3u);
-                wr.ky = (int)((flags >> 6) & 3u);
-                wr.kz = (int)((flags >> 8) & 3u);
-                wr.sx = sx;
-                wr.sy = sy;
-                wr.sz = sz;
-                float b0, b1, b2;
-                const float t = watertight(co, wr, v0, v1, v2, b0, b1, b2);
-                if (ANY) {
-                    // `t >= ray_tmax` rejects; a NaN t does not (src/ref/kdtree.cpp:60-62)
-                    if (!(t >= ray_tmax) && v0.w == 0.f) finish(1);
-                } else if (t < hit.t && v0.w == 0.f) {
-                    // the object of the closest hit is the one whose mesh produced it
-                    // (src/ref/kdtree.cpp:81-95 sets it after the mesh improved the hit)
-                    hit.t = t;
-                    hit.prim = prim;
-                    hit.object = cur_object;
-                    hit.b0 = b0;
-                    hit.b1 = b1;
-                    hit.b2 = b2;
-                }
-            } else if (sp == mesh_sp_base) {  // mesh stack empty: the mesh is done
-                leave_mesh(s, rays, stack);
-            } else {
-                --sp;
-                const uint2 e = stack.pop(sp);
-                node = e.x;
-                t_min = t_max;
-                t_max = __uint_as_float(e.y);
-                set_mode(kDescend);
-            }
-        } else if (m == kSceneLeaf) {
-            const uint2 leaf = __ldg(s.scene_nodes + node);
-            const uint32_t count = leaf.x >> 2;
-            if (leaf_i < count) {
-                const uint32_t obj =
-                    (leaf_i == 0) ? leaf.y : __ldg(reinterpret_cast<const uint32_t*>(s.scene_nodes + node) + 1 + leaf_i);
-                leaf_i++;
-                const float4* p = s.objects + 6 * (size_t)obj;
-                const float4 r0 = __ldg(p + 0), r1 = __ldg(p + 1), r2 = __ldg(p + 2);
-                const float4 lo = __ldg(p + 3), hi = __ldg(p + 4), info = __ldg(p + 5);
-                float3 oo, od;
-                transform_ray(r0, r1, r2, co, cd, oo, od);
-                float mt_min, mt_max;
-                if (clip_ray(make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z), oo, od, mt_min, mt_max)) {
-                    if (sp + 2 > kStackEntries) {
-                        finish(-1);
-                        return false;
-                    }
-                    stack.push(sp, __float_as_uint(t_min), t_max);  // the scene level's interval
-                    stack.push(sp + 1, node, __uint_as_float(leaf_i));  // and its leaf cursor
-                    sp += 2;
-                    mesh_sp_base = sp;
-                    cur_object = obj;
-                    co = oo;
-                    cd = od;
-                    cinv = make_float3(1.f / od.x, 1.f / od.y, 1.f / od.z);
-                    mesh_offset = __float_as_uint(lo.w);
-                    tri_offset = __float_as_uint(hi.w);
-                    const int visibility = __float_as_int(info.y);
-                    const bool test_triangles = ANY ? (visibility == 0) : (visibility != 2);
-                    const Watertight_Ray wr = watertight_setup(od);
-                    sx = wr.sx;
-                    sy = wr.sy;
-                    sz = wr.sz;
-                    flags = (flags & (3u << 10)) | (uint32_t)kDescend | 4u | (test_triangles ? 8u : 0u) |
-                            ((uint32_t)wr.kx << 4) | ((uint32_t)wr.ky << 6) | ((uint32_t)wr.kz << 8);
-                    node = 0;
-                    t_min = mt_min;
-                    t_max = mt_max;
-                }
-            } else if (sp == 0) {
-                finish(ANY ? 0 : (hit.t < ray_tmax ? 1 : 0));
-            } else {
-                --sp;
-                const uint2 e = stack.pop(sp);
-                node = e.x;
-                t_min = t_max;
-                t_max = __uint_as_float(e.y);
-                set_mode(kDescend);
-            }
-        }
+        if (m == kDescend) step_descend<MAXD>(s, rays, stack);
+        else if (m == kMeshLeaf) step_mesh_leaf(s, rays, stack);
+        else if (m == kSceneLeaf) step_scene_leaf(s, rays, stack);
         return mode() != kDone;
     }
 };

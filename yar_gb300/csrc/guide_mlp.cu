@@ -446,6 +446,18 @@ __global__ void __launch_bounds__(kRows, 1) mlp_kernel(Mlp_Args a) {
     if (warp == 0) tc::tmem_dealloc(tmem, kCols);
 }
 
+// The MLP kernels' bounded mbarrier wait on a barrier that nothing arrives
+// at: the limit runs out, the error word is set and the kernel returns, with
+// no copy or MMA in flight.  Exercises the expiry path of the wait.
+__global__ void wait_selftest_kernel(uint32_t limit, int* err) {
+    __shared__ __align__(8) uint64_t mbar;
+    if (threadIdx.x == 0) {
+        const uint32_t a = (uint32_t)__cvta_generic_to_shared(&mbar);
+        tc::mbar_init(a, 1);
+        if (!tc::mbar_wait(a, 0, limit)) atomicExch(err, 1);
+    }
+}
+
 // fp32 parameters -> bf16 operand images (forward and transposed).
 __global__ void images_kernel(const float* __restrict__ params, uint8_t* __restrict__ img) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -679,6 +691,14 @@ extern "C" int yar_guide_get_params(yar_gpu_ctx* ctx, float* params) {
     cudaError_t e = cudaMemcpyAsync(params, ctx->guide.params.ptr, kGuideParams * sizeof(float),
                                     cudaMemcpyDeviceToHost, ctx->stream);
     return guide_finish(ctx, e, "guide parameters", nullptr);
+}
+
+extern "C" int yar_gpu_wait_selftest(yar_gpu_ctx* ctx, uint32_t limit) {
+    if (!ctx) return YAR_ERR_INVALID;
+    if (limit == 0 || limit > (1u << 24)) return fail(ctx, YAR_ERR_INVALID, "wait self-test: limit in [1, 2^24]");
+    cudaSetDevice(ctx->device);
+    wait_selftest_kernel<<<1, 32, 0, ctx->stream>>>(limit, ctx->d_error);
+    return guide_finish(ctx, cudaGetLastError(), "wait self-test", nullptr);
 }
 
 extern "C" int yar_guide_infer(yar_gpu_ctx* ctx, const float* queries, uint32_t n, const float* box, float* lobes) {

@@ -210,6 +210,7 @@ EXPORTS = {
     "yar_guide_set_params": (C.c_int, [C.c_void_p, C.c_void_p]),
     "yar_guide_get_params": (C.c_int, [C.c_void_p, C.c_void_p]),
     "yar_guide_infer": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.c_void_p]),
+    "yar_gpu_wait_selftest": (C.c_int, [C.c_void_p, C.c_uint32]),
     "yar_guide_gradient": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.c_float,
                                      C.c_void_p, C.POINTER(C.c_float)]),
     "yar_guide_train_step": (C.c_int, [C.c_void_p, C.c_void_p, C.c_uint32, C.POINTER(C.c_float), C.c_float,
@@ -454,6 +455,11 @@ class Context:
         p = np.zeros(GUIDE_PARAMS, np.float32)
         self._check(lib().yar_guide_get_params(self._h, _ptr(p)), "guide_get_params")
         return p
+
+    def wait_selftest(self, limit):
+        """yar_gpu_wait_selftest: the tensor-core kernels' bounded mbarrier wait
+        on a barrier nothing arrives at; raises YarError(YAR_ERR_TIMEOUT)."""
+        self._check(lib().yar_gpu_wait_selftest(self._h, int(limit)), "wait_selftest")
 
     def guide_infer(self, queries_ptr, n, box, lobes_ptr):
         b = (C.c_float * 6)(*[float(x) for x in box])
