@@ -589,9 +589,11 @@ def guided_bench(plain_spp_side=32, offsets=(2, 3, 4), with_cpu=True):
         plain_spp_side^2 samples per pixel (1024);
       - plain passes: yar_gpu_guided_render at guide fraction 0, 1024 one-sample
         passes;
-      - guided: for each stream offset, the guided render's time budget
-        (training included) is raised until its RMSE is at or below the better
-        plain form's; the time it took is the measured time to that RMSE.
+      - guided (stratified form of yar_gpu_guided_render: the training passes,
+        then the pixel sampler at k x k samples per pixel with continuations
+        from the trained proposal): for each stream offset, k is raised until
+        the RMSE is at or below the better plain form's; the wall time of that
+        render (training included) is the measured time to that RMSE.
     oracle_vs_reference: the oracle's 64 x 64 tile means against the reference
     CPU renderer's at 16 spp (z-scores from the noise of two reference renders
     with different seed offsets)."""
@@ -623,17 +625,21 @@ def guided_bench(plain_spp_side=32, offsets=(2, 3, 4), with_cpu=True):
     img_p, _, st_p = ctx.guided_render(w, h, passes=plain_spp_side ** 2, stream_offset=1)
     r_r, r_p = rmse(img_r), rmse(img_p)
     target, t_target = min((r_r, st_r.seconds), (r_p, st_p.seconds))
+    ctx.guided_render(w, h, samples_per_pixel=16, stream_offset=4092, **GUIDE)  # warm-up of the stratified form
     runs = []
     for off in offsets:
-        budget = 0.5 * t_target
+        side = 16
+        img_g, _, st_g = ctx.guided_render(w, h, samples_per_pixel=side * side, stream_offset=off, **GUIDE)
+        r_g = rmse(img_g)
+        side = max(1, int(np.ceil(side * r_g / target)))  # RMSE ~ 1 / sqrt(spp)
         for _ in range(8):
-            img_g, _, st_g = ctx.guided_render(w, h, passes=1 << 24, stream_offset=off, time_budget=budget, **GUIDE)
+            img_g, _, st_g = ctx.guided_render(w, h, samples_per_pixel=side * side, stream_offset=off, **GUIDE)
             r_g = rmse(img_g)
             if r_g <= target:
                 break
-            budget = budget * max(1.02, (r_g / target) ** 2 * 1.02)
-        runs.append({"stream_offset": off, "seconds": round(st_g.seconds, 3), "rmse": r_g,
-                     "reached": bool(r_g <= target), "passes": int(st_g.passes),
+            side += 1
+        runs.append({"stream_offset": off, "spp": side * side, "seconds": round(st_g.seconds, 3), "rmse": r_g,
+                     "reached": bool(r_g <= target), "train_passes": int(st_g.passes),
                      "train_seconds": round(st_g.train_seconds, 3)})
     ctx.close()
     times = [r["seconds"] for r in runs if r["reached"]]

@@ -117,6 +117,11 @@ typedef struct yar_mesh_desc {
     int32_t reverse_geometric_normal_orientation;
     int32_t visibility;         /* YAR_VISIBLE, ... */
     yar_kdtree_view kdtree;     /* per-mesh tree (object space) */
+    /* Alpha test (src/ref/kdtree.cpp:31-38, :69-77): 0 none, else 1 + an index
+     * into yar_flat_scene::textures.  A triangle hit whose texture value at
+     * the hit's uv (mip 0, bilinear, repeat) has red 0 is skipped by both
+     * casts.  Needs uvs. */
+    uint32_t alpha_texture;
 } yar_mesh_desc;
 
 /* Scene_Object, src/lib/scene_object.h:8-25 */
@@ -475,6 +480,13 @@ typedef struct yar_guided_params {
     uint32_t stream_offset;   /* distinct values give statistically independent renders (< 4096) */
     float time_budget;        /* seconds; > 0 stops after the pass that reaches it */
     uint32_t keep_guide;      /* 1: start from the current network instead of re-initialising it */
+    /* 0: the image is the mean of `passes` one-sample passes.  > 0: the
+     * stratified form - the train_passes training passes (guided only), then
+     * the image rendered with the scene's stratified pixel sampler at this
+     * many samples per pixel (rounded up to a perfect square, as RAY's --spp),
+     * continuations drawn from the trained proposal; `passes` and
+     * `time_budget` are not used, radiance_sum receives image x spp. */
+    uint32_t samples_per_pixel;
 } yar_guided_params;
 
 typedef struct yar_guided_stats {

@@ -81,3 +81,11 @@ rm -f "$OUT/libyarref.a"
 ar rcs "$OUT/libyarref.a" "$OUT"/obj/*.o
 $CXX $CXXFLAGS -I"$HERE" -I"$HERE/../include" -I"$HERE/../yar_gb300/csrc" "$HERE/ref_harness.cpp" "$OUT/libyarref.a" -o "$OUT/yar_ref" -pthread
 echo "built $OUT/yar_ref"
+# the drop-in render_scene_gpu: the reference's loader and builder, the product library's render
+PRODUCT="$HERE/../yar_gb300/libyar_gb300.so"
+if [ -f "$PRODUCT" ]; then
+    $CXX $CXXFLAGS -I"$HERE" -I"$HERE/../include" -I"$HERE/../yar_gb300/csrc" "$HERE/render_scene_gpu.cpp" \
+        "$OUT/libyarref.a" -L"$HERE/../yar_gb300" -lyar_gb300 -Wl,-rpath,'$ORIGIN/../../yar_gb300' \
+        -o "$OUT/yar_ref_gpu" -pthread
+    echo "built $OUT/yar_ref_gpu"
+fi

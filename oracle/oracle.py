@@ -16,6 +16,7 @@ import numpy as np
 HERE = os.path.dirname(os.path.abspath(__file__))
 ORACLE_LIB = os.path.join(HERE, "liboracle.so")
 REF_BIN = os.path.join(HERE, "_ref", "yar_ref")
+REF_GPU_BIN = os.path.join(HERE, "_ref", "yar_ref_gpu")
 
 
 class RayStats(C.Structure):
@@ -154,6 +155,26 @@ def ref_render(pbrt_path, spp=0, seed_offset=0, threads=0, checkpoint_dir=None):
     img = np.frombuffer(raw[20:], np.float32).reshape(int(h), int(w), 3).copy()
     info.update(variance=variance, seconds=seconds)
     return img, info
+
+
+def ref_render_gpu(pbrt_path, spp=0, seed_offset=0):
+    """The drop-in render_scene_gpu (oracle/render_scene_gpu.cpp): the
+    reference's pbrt loader and kd-tree builder, rendered through the C ABI."""
+    with tempfile.TemporaryDirectory() as d:
+        out = os.path.join(d, "img.bin")
+        args = [pbrt_path, out]
+        if spp:
+            args.append("--spp=%d" % spp)
+        if seed_offset:
+            args.append("--seedoffset=%d" % seed_offset)
+        r = subprocess.run([REF_GPU_BIN] + args, stdout=subprocess.PIPE, stderr=subprocess.PIPE, text=True, timeout=600)
+        if r.returncode != 0:
+            raise RuntimeError("yar_ref_gpu failed (%d): %s %s" % (r.returncode, r.stdout[-2000:], r.stderr[-2000:]))
+        raw = open(out, "rb").read()
+    w, h = np.frombuffer(raw[:8], np.uint32)
+    variance = float(np.frombuffer(raw[8:16], np.float64)[0])
+    img = np.frombuffer(raw[20:], np.float32).reshape(int(h), int(w), 3).copy()
+    return img, variance
 
 
 def ref_build(flat, threads=0):

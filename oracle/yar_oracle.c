@@ -154,10 +154,42 @@ static inline uint32_t descend(const yar_kd_node* nodes, uint32_t node, const fl
     return (d[axis] > 0.0) ? above_child : below_child;
 }
 
+/* The alpha test of both leaf callbacks (src/ref/kdtree.cpp:31-38, :69-77):
+ * Triangle_Mesh::get_uv (barycentric_interpolate, src/lib/math.h:146-153),
+ * then Image_Texture::sample_bilinear of mip 0 with repeat wrapping
+ * (image_texture.cpp:441-476); 1 when the red channel is 0 (skip). */
+static float alpha_texel_r(const yar_flat_scene* s, const yar_texture_mip_desc* mip, int x, int y) {
+    const int w = (int)mip->width, h = (int)mip->height;
+    if (x >= 0) x &= w - 1;
+    else { x %= w; x += (x >> 31) & w; }
+    if (y >= 0) y &= h - 1;
+    else { y %= h; y += (y >> 31) & h; }
+    return s->texels[3 * (mip->texel_offset + (uint64_t)y * (uint64_t)w + (uint64_t)x)];
+}
+static int alpha_rejects(const yar_flat_scene* s, const yar_mesh_desc* m, uint32_t prim, const float b[3]) {
+    if (!s || !m->alpha_texture) return 0;
+    const int32_t* vi = &m->indices[3 * (size_t)prim];
+    const float* uv0 = &m->uvs[2 * (size_t)vi[0]];
+    const float* uv1 = &m->uvs[2 * (size_t)vi[1]];
+    const float* uv2 = &m->uvs[2 * (size_t)vi[2]];
+    const float u = b[0] * uv0[0] + b[1] * uv1[0] + b[2] * uv2[0];
+    const float v = b[0] * uv0[1] + b[1] * uv1[1] + b[2] * uv2[1];
+    const yar_texture_mip_desc* mip = &s->texture_mips[s->textures[m->alpha_texture - 1].first_mip];
+    const float x = u * (float)mip->width - 0.5f, y = v * (float)mip->height - 0.5f;
+    const float x_floor = floorf(x), y_floor = floorf(y);
+    const float wx = x - x_floor, wy = y - y_floor;
+    const int x0 = (int)x_floor, y0 = (int)y_floor, x1 = x0 + 1, y1 = y0 + 1;
+    float r = alpha_texel_r(s, mip, x0, y0) * ((1 - wy) * (1 - wx));
+    r = r + alpha_texel_r(s, mip, x1, y0) * ((1 - wy) * wx);
+    r = r + alpha_texel_r(s, mip, x0, y1) * (wy * (1 - wx));
+    r = r + alpha_texel_r(s, mip, x1, y1) * (wy * wx);
+    return r == 0.f;
+}
+
 /* KdTree::intersect for a triangle-mesh tree with the leaf callback
  * intersect_triangle_mesh_geometry_data (src/ref/kdtree.cpp:12-45, :219-327). */
-static int mesh_closest(const yar_mesh_desc* m, const float o[3], const float d[3], hit_state* hit,
-                        oracle_ray_stats* st) {
+static int mesh_closest(const yar_flat_scene* s, const yar_mesh_desc* m, const float o[3], const float d[3],
+                        hit_state* hit, oracle_ray_stats* st) {
     float t_min, t_max;
     if (!clip_ray(m->kdtree.bounds_min, m->kdtree.bounds_max, o, d, &t_min, &t_max)) return 0;
     const float inv[3] = {1.f / d[0], 1.f / d[1], 1.f / d[2]};
@@ -184,6 +216,7 @@ static int mesh_closest(const yar_mesh_desc* m, const float o[3], const float d[
                     const float t = oracle_intersect_triangle_watertight(o, d, p0, p1, p2, b);
                     if (t < hit->t) {
                         if (degenerate(p0, p1, p2)) continue;
+                        if (alpha_rejects(s, m, idx[i], b)) continue;
                         hit->t = t;
                         hit->prim = idx[i];
                         hit->b[0] = b[0];
@@ -204,8 +237,8 @@ static int mesh_closest(const yar_mesh_desc* m, const float o[3], const float d[
 
 /* KdTree::intersect_any with intersect_any_triangle_mesh_geometry_data
  * (src/ref/kdtree.cpp:47-79, :329-439). */
-static int mesh_any(const yar_mesh_desc* m, const float o[3], const float d[3], float ray_tmax,
-                    oracle_ray_stats* st) {
+static int mesh_any(const yar_flat_scene* s, const yar_mesh_desc* m, const float o[3], const float d[3],
+                    float ray_tmax, oracle_ray_stats* st) {
     float t_min, t_max;
     if (!clip_ray(m->kdtree.bounds_min, m->kdtree.bounds_max, o, d, &t_min, &t_max)) return 0;
     const float inv[3] = {1.f / d[0], 1.f / d[1], 1.f / d[2]};
@@ -231,6 +264,7 @@ static int mesh_any(const yar_mesh_desc* m, const float o[3], const float d[3], 
                     const float t = oracle_intersect_triangle_watertight(o, d, p0, p1, p2, b);
                     if (t >= ray_tmax) continue;
                     if (degenerate(p0, p1, p2)) continue;
+                    if (alpha_rejects(s, m, idx[i], b)) continue;
                     return 1;
                 }
             }
@@ -271,7 +305,7 @@ static int scene_closest(const yar_flat_scene* s, const float o[3], const float 
                 transform_point(obj->world_to_object, o, oo);
                 transform_vector(obj->world_to_object, d, od);
                 if (st) st->object_visits++;
-                int r = mesh_closest(&s->meshes[obj->mesh_index], oo, od, hit, st);
+                int r = mesh_closest(s, &s->meshes[obj->mesh_index], oo, od, hit, st);
                 if (r < 0) return -1;
                 if (r) hit->object = idx[i];
             }
@@ -309,7 +343,7 @@ static int scene_any(const yar_flat_scene* s, const float o[3], const float d[3]
                 transform_point(obj->world_to_object, o, oo);
                 transform_vector(obj->world_to_object, d, od);
                 if (st) st->object_visits++;
-                int r = mesh_any(&s->meshes[obj->mesh_index], oo, od, ray_tmax, st);
+                int r = mesh_any(s, &s->meshes[obj->mesh_index], oo, od, ray_tmax, st);
                 if (r != 0) return r;
             }
             if (sp == 0) break;
@@ -835,6 +869,24 @@ static float atan2_sample(float y, float x) {
 }
 static float acos_sample(float x) { return g_correctly_rounded_trig ? (float)acos((double)x) : acosf(x); }
 /* log2 of the EWA footprint: the C library's log2f, or correctly rounded like the device */
+/* The film filters (src/ref/film.cpp:123-142) at offset (x, y) from the pixel
+ * center: box 1; gaussian max(0, exp(-alpha |p|^2) - exp(-alpha r^2)), the
+ * zero level from expf as the reference's constructor computes it; triangle
+ * max(0, r - |x|) max(0, r - |y|). */
+static float film_filter_weight(const yar_render_config* c, float x, float y) {
+    if (c->pixel_filter_type == 1) {
+        const float zero_level = expf(-c->pixel_filter_alpha * c->pixel_filter_radius * c->pixel_filter_radius);
+        const float a = -c->pixel_filter_alpha * (x * x + y * y);
+        const float e = g_correctly_rounded_trig ? (float)exp((double)a) : expf(a);
+        const float v = e - zero_level;
+        return 0.f < v ? v : 0.f;
+    }
+    if (c->pixel_filter_type == 2) {
+        const float ax = c->pixel_filter_radius - fabsf(x), ay = c->pixel_filter_radius - fabsf(y);
+        return (0.f < ax ? ax : 0.f) * (0.f < ay ? ay : 0.f);
+    }
+    return 1.f;
+}
 static float log2_lod(float x) { return g_correctly_rounded_trig ? (float)log2((double)x) : log2f(x); }
 
 /* ---------------- image textures (src/ref/image_texture.cpp, src/ref/parameter_evaluation.cpp:10-31) */
@@ -2434,10 +2486,11 @@ static int render_tile(render_job* J, int t) {
     float* s1d = (float*)malloc(sizeof(float) * ((size_t)spp * n1d + 1));
     float* s2d = (float*)malloc(sizeof(float) * (2 * (size_t)spp * n2d + 1));
     const float radius = cfg->pixel_filter_radius;
+    const int support = (int)ceilf(radius + 0.5f);  /* sample rows that reach a requested row */
     double var_acc = 0.0;
     int rc = YAR_OK;
     for (int y = sb[1]; y < sb[3] && rc == YAR_OK; y++) {
-        if (y < J->row_begin - 1 || y > J->row_end) continue;  /* outside the rows requested (+1 row of filter support) */
+        if (y < J->row_begin - support || y >= J->row_end + support) continue;  /* outside the rows requested */
         for (int x = sb[0]; x < sb[2] && rc == YAR_OK; x++) {
             uint32_t stream = ((uint32_t)x & 0xffffu) | ((uint32_t)y << 16);
             stream += (uint32_t)cfg->rng_seed_offset;
@@ -2541,7 +2594,7 @@ static int render_tile(render_job* J, int t) {
                 float mc = fmaxf_std(radiance.r, fmaxf_std(radiance.g, radiance.b));
                 if (mc > limit) radiance = mulcs(radiance, limit / mc);
                 if (cfg->film_radiance_scale != 1.f) radiance = mulcs(radiance, cfg->film_radiance_scale);
-                /* Film_Tile::add_sample with the box filter, src/ref/film.cpp:27-50 */
+                /* Film_Tile::add_sample, src/ref/film.cpp:27-50 */
                 int rx0 = (int)ceilf(fx - radius - 0.5f), ry0 = (int)ceilf(fy - radius - 0.5f);
                 int rx1 = (int)floorf(fx + radius - 0.5f) + 1, ry1 = (int)floorf(fy + radius - 0.5f) + 1;
                 if (rx0 < pb[0]) rx0 = pb[0];
@@ -2551,10 +2604,11 @@ static int render_tile(render_job* J, int t) {
                 for (int yy = ry0; yy < ry1; yy++)
                     for (int xx = rx0; xx < rx1; xx++) {
                         film_px* p = &px[(yy - pb[1]) * pw + (xx - pb[0])];
-                        p->r += 1.f * radiance.r;
-                        p->g += 1.f * radiance.g;
-                        p->b += 1.f * radiance.b;
-                        p->w += 1.f;
+                        const float w = film_filter_weight(cfg, fx - ((float)xx + 0.5f), fy - ((float)yy + 0.5f));
+                        p->r += w * radiance.r;
+                        p->g += w * radiance.g;
+                        p->b += w * radiance.b;
+                        p->w += w;
                     }
                 float lum = 0.2126729f * radiance.r + 0.7151522f * radiance.g + 0.0721750f * radiance.b;
                 lsum += lum;
@@ -2605,7 +2659,8 @@ int oracle_render_trig(const yar_flat_scene* s, float* rgb, double* variance, in
 int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t row_begin, int32_t row_end,
                   int32_t thread_count) {
     const yar_render_config* cfg = &s->config;
-    if ((cfg->rendering_algorithm != 0 && cfg->rendering_algorithm != 1) || cfg->pixel_filter_type != 0)
+    if ((cfg->rendering_algorithm != 0 && cfg->rendering_algorithm != 1) || cfg->pixel_filter_type < 0 ||
+        cfg->pixel_filter_type > 2)
         return YAR_ERR_UNSUPPORTED;
     for (uint32_t i = 0; i < s->material_count; i++) {
         uint32_t t = s->materials[i].type;

@@ -212,6 +212,38 @@ def cornell_delta_64():
     np.savez_compressed(os.path.join(HERE, "cornell_delta_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def _filter_golden(name, pixel_filter, seed):
+    with tempfile.TemporaryDirectory() as d:
+        pbrt = os.path.join(d, name + ".pbrt")
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=seed, width=64, height=64, spp=16, maxdepth=8,
+                                                  box_materials=scenes.GGX_BOXES, pixel_filter=pixel_filter))
+        yfs = os.path.join(HERE, name + ".yfs")
+        oracle.ref_flatten(pbrt, yfs, seed_offset=1)
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), image=img, variance=np.float64(info["variance"]))
+
+
+def cornell_gaussian_64():
+    """The GGX Cornell box through a Gaussian pixel filter of radius 1.5, alpha 2."""
+    _filter_golden("cornell_gaussian_64", '"gaussian" "float xwidth" [1.5] "float ywidth" [1.5] "float alpha" [2]', 6)
+
+
+def cornell_triangle_64():
+    """The GGX Cornell box through a triangle pixel filter of radius 2."""
+    _filter_golden("cornell_triangle_64", '"triangle" "float xwidth" [2] "float ywidth" [2]', 7)
+
+
+def cornell_c1_256():
+    """The C1 configuration itself: the Cornell box at 256 x 256, 16 spp,
+    maxdepth 8, seed offset 1 (the image and variance only; the scene is
+    cornell_c1_64.yfs at 256 x 256)."""
+    with tempfile.TemporaryDirectory() as d:
+        pbrt = os.path.join(d, "cornell.pbrt")
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8))
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_c1_256.npz"), image=img, variance=np.float64(info["variance"]))
+
+
 def cornell_refractor_64():
     """cornell_delta_64 with a perfect-refractor ceiling (object 1)."""
     s = FlatScene.read(os.path.join(HERE, "cornell_delta_64.yfs"))
@@ -342,6 +374,22 @@ def cornell_texture_64():
     np.savez_compressed(os.path.join(HERE, "cornell_texture_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def cornell_alpha_64():
+    """The GGX Cornell box with an alpha-textured fence across the room: the
+    alpha test cuts the fence's camera, bounce, probe and shadow hits."""
+    from yar_gb300 import exr
+    with tempfile.TemporaryDirectory() as d:
+        exr.write_exr(os.path.join(d, "cutout.exr"), scenes.cutout_image(), False, {})
+        pbrt = os.path.join(d, "cornell_alpha.pbrt")
+        tex = ('Texture "cutout" "float" "imagemap" "string filename" "cutout.exr"',)
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=19, width=64, height=64, spp=16, maxdepth=8,
+                                                  box_materials=scenes.GGX_BOXES, textures=tex,
+                                                  extra_shapes=scenes.cutout_fence()))
+        oracle.ref_flatten(pbrt, os.path.join(HERE, "cornell_alpha_64.yfs"), seed_offset=1)
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_alpha_64.npz"), image=img, variance=np.float64(info["variance"]))
+
+
 def cornell_direct_64():
     _pbrt_golden("cornell_direct_64", 15, box_materials=scenes.GGX_BOXES, light_sources=scenes.DELTA_LIGHTS,
                  light_samples=4, integrator="directlighting")
@@ -430,6 +478,7 @@ if __name__ == "__main__":
                              "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64",
                              "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64",
                              "cornell_direct_64", "cornell_direct_env_64", "cornell_texture_64", "checkpoint_c1",
+                             "cornell_gaussian_64", "cornell_triangle_64", "cornell_c1_256", "cornell_alpha_64",
                              "exr_files",
                              "kdtree_cache_files"]
     for name in which:

@@ -240,3 +240,32 @@ def test_invalid_traversal_kernel_option():
     with pytest.raises(native.YarError) as e:
         native.Context(0, traversal_kernel=7)
     assert e.value.code == native.YAR_ERR_INVALID
+
+
+@pytest.mark.parametrize("kernel", [native.TRAVERSAL_PERSISTENT_64, native.TRAVERSAL_PER_RAY])
+def test_alpha_test_matches_oracle(kernel):
+    """Both casts skip triangle hits whose alpha texture reads red 0 at the hit's
+    uv (src/ref/kdtree.cpp:31-38, :69-77): bit-identical to the oracle on rays
+    through the cut-out fence of cornell_alpha_64, and different from the same
+    scene without its alpha texture."""
+    s = FlatScene.read(golden("cornell_alpha_64.yfs"))
+    fence = [i for i, m in enumerate(s.meshes) if m.alpha_texture]
+    assert fence
+    ctx = native.Context(0, traversal_kernel=kernel)
+    try:
+        ctx.upload_scene(s)
+        lo, hi = scenes.scene_box(s)
+        rays = scenes.random_rays(lo, hi, 200_000, 23)
+        got = ctx.cast_closest(rays)
+        assert_same_hits(got, oracle.cast_closest(s, rays))
+        shadow = scenes.random_shadow_rays(lo, hi, 200_000, 24)
+        occ = ctx.cast_any(shadow)
+        assert np.array_equal(occ, oracle.cast_any(s, shadow))
+        fence_objects = [k for k, o in enumerate(s.objects) if o["mesh_index"] in fence]
+        assert np.isin(got[2], fence_objects).sum() > 1000  # the fence's kept parts are hit
+        for i in fence:
+            s.meshes[i].alpha_texture = 0
+        ctx.upload_scene(s)
+        assert not np.array_equal(ctx.cast_any(shadow), occ)
+    finally:
+        ctx.close()

@@ -64,3 +64,32 @@ def test_invalid_guided_params(gpu_ctx, small_room):
         with pytest.raises(native.YarError) as e:
             gpu_ctx.guided_render(64, 64, **kw)
         assert e.value.code == native.YAR_ERR_INVALID
+
+
+def test_stratified_guided_is_unbiased(gpu_ctx, small_room):
+    """The stratified form: the training passes, then the pixel sampler with
+    continuations from the trained proposal.  Its image mean matches the plain
+    render's (yar_gpu_render at the same sample count), and with guide
+    fraction 0 it is the plain render on other pixel streams (checked on the
+    Cornell box, whose light is not behind an opening: its image mean is
+    steady at this sample count)."""
+    s = small_room
+    s.config["x_pixel_sample_count"] = 16
+    s.config["y_pixel_sample_count"] = 16
+    gpu_ctx.upload_scene(s)
+    plain, _ = gpu_ctx.render(64, 64)
+    guided, sums, st = gpu_ctx.guided_render(64, 64, samples_per_pixel=256, guide_fraction=0.5, train_passes=32,
+                                             stream_offset=3)
+    assert st.passes == 32 and st.train_samples > 0
+    assert np.allclose(sums / 256.0, guided, rtol=1e-6, atol=1e-7)
+    assert abs(guided.mean() - plain.mean()) < MEAN_REL_TOL * plain.mean(), (guided.mean(), plain.mean())
+    for sl in (np.s_[:32], np.s_[32:]):
+        assert abs(guided[sl].mean() - plain[sl].mean()) < 2 * MEAN_REL_TOL * plain[sl].mean()
+    c = FlatScene.read(golden("cornell_c1_64.yfs"))
+    c.config["x_pixel_sample_count"] = c.config["y_pixel_sample_count"] = 15
+    gpu_ctx.upload_scene(c)
+    plain, _ = gpu_ctx.render(64, 64)
+    unguided, _, st0 = gpu_ctx.guided_render(64, 64, samples_per_pixel=200, stream_offset=4)  # rounds up to 15 x 15
+    assert st0.passes == 0
+    assert not np.array_equal(unguided, plain)
+    assert abs(unguided.mean() - plain.mean()) < 0.01 * plain.mean(), (unguided.mean(), plain.mean())

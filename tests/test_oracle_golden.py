@@ -125,7 +125,8 @@ def test_builder_against_live_reference_large_mesh():
                                   "cornell_layered_64", "cornell_layered_yar_64", "cornell_lights_64",
                                   "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64",
                                   "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64",
-                                  "cornell_texture_64"])
+                                  "cornell_texture_64", "cornell_gaussian_64", "cornell_triangle_64",
+                                  "cornell_alpha_64"])
 def test_oracle_render_matches_reference_golden(name):
     """The oracle's path loop, sampler, shading, BSDFs (diffuse, GGX metal, rough
     glass, plastic in both of the reference's forms, coated diffuse), delta
@@ -197,6 +198,19 @@ def test_texture_scene_file_round_trip(tmp_path):
     assert sorted(int(x) for x in s.materials["reflectance_texture"]) == [0, 0, 0, 0, 1, 1]
 
 
+def test_alpha_texture_file_round_trip(tmp_path):
+    """A mesh's alpha texture (MESH chunk flag 4) survives a write and a read,
+    in the Python and the C++ readers (the reference harness reads the file
+    to render it)."""
+    s = FlatScene.read(golden("cornell_alpha_64.yfs"))
+    assert [m.alpha_texture for m in s.meshes].count(1) == 1
+    p = tmp_path / "a.yfs"
+    s.write(str(p))
+    t = FlatScene.read(str(p))
+    assert [m.alpha_texture for m in t.meshes] == [m.alpha_texture for m in s.meshes]
+    assert open(str(p), "rb").read() == open(golden("cornell_alpha_64.yfs"), "rb").read()
+
+
 def test_textured_scenes_outside_the_restated_part_are_refused():
     """Image textures are restated for diffuse reflectance in the path tracer
     with camera-ray differentials; with the direct-lighting algorithm, next to
@@ -211,3 +225,15 @@ def test_textured_scenes_outside_the_restated_part_are_refused():
             s.materials["other_textured_parameters"][-1] = 1
         with pytest.raises(Exception):
             oracle.render(s, threads=2)
+
+
+def test_oracle_c1_configuration_matches_reference_golden():
+    """The C1 configuration (256 x 256 from the flattened Cornell box) against
+    the reference's render of its pbrt scene, bit for bit."""
+    s = FlatScene.read(golden("cornell_c1_64.yfs"))
+    s.config["render_region"] = (0, 0, 256, 256)
+    s.camera["image_extent"] = (256, 256)
+    g = np.load(golden("cornell_c1_256.npz"))
+    img, var = oracle.render(s, threads=8)
+    assert np.array_equal(bits(img), bits(g["image"]))
+    assert var == float(g["variance"])

@@ -37,6 +37,21 @@ LIGHTS_VARIANCE_REL_TOL = 1e-4
 # than sinf/cosf do (89.3% bit-identical pixels on cornell_envmap_64; an oracle
 # run with correctly rounded trigonometry gives the same figure).
 ENV_BIT_EQUAL_MIN = 0.85
+# Wide pixel filters (gaussian of radius 1.5, triangle of radius 2): a sample
+# whose path diverges through sin/cos rounding reaches up to 16 pixels with
+# its weight, so the mean relative error of the same divergences is larger
+# (1.1e-4 measured on cornell_gaussian_64 at 91.5% bit-identical pixels).
+FILTER_MEAN_REL_TOL = 3e-4
+
+
+def sample_region_pixels(s):
+    """Pixels of the film's sample region (Film::Film, src/ref/film.cpp:53-86)."""
+    import math
+    r = float(s.config["pixel_filter_radius"])
+    x0, y0, x1, y1 = (int(v) for v in s.config["render_region"])
+    w = math.ceil(x1 - 1 + 0.5 + r) - math.floor(x0 + 0.5 - r)
+    h = math.ceil(y1 - 1 + 0.5 + r) - math.floor(y0 + 0.5 - r)
+    return w * h
 
 
 def compare(img, ref):
@@ -49,7 +64,8 @@ def compare(img, ref):
                                   "cornell_layered_64", "cornell_layered_yar_64", "cornell_lights_64",
                                   "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
                   "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64",
-                                  "cornell_texture_64"])
+                                  "cornell_texture_64", "cornell_gaussian_64", "cornell_triangle_64",
+                                  "cornell_alpha_64"])
 def test_render_matches_reference_golden(gpu_ctx, name):
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
@@ -59,18 +75,20 @@ def test_render_matches_reference_golden(gpu_ctx, name):
     img, stats = gpu_ctx.render(w, h)
     same, rel = compare(img, g["image"])
     lights = s.delta_lights.shape[0] > 0 or s.environment is not None
+    wide = int(s.config["pixel_filter_type"]) != 0 or float(s.config["pixel_filter_radius"]) > 0.5
     assert same >= (ENV_BIT_EQUAL_MIN if s.environment is not None else BIT_EQUAL_MIN), (same, rel)
-    assert rel < (LIGHTS_MEAN_REL_TOL if lights else MEAN_REL_TOL), (same, rel)
+    assert rel < (LIGHTS_MEAN_REL_TOL if lights else FILTER_MEAN_REL_TOL if wide else MEAN_REL_TOL), (same, rel)
     vtol = LIGHTS_VARIANCE_REL_TOL if lights else VARIANCE_REL_TOL
     assert abs(stats.variance - float(g["variance"])) <= vtol * float(g["variance"])
-    assert stats.paths == w * h * 16
+    assert stats.paths == sample_region_pixels(s) * 16
     assert stats.rays_closest >= stats.paths
 
 
 RENDER_GOLDENS = ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornell_refractor_64", "cornell_layered_64",
                   "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64", "cornell_spherelight_64",
                   "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
-                  "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64", "cornell_texture_64"]
+                  "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64", "cornell_texture_64",
+                  "cornell_gaussian_64", "cornell_triangle_64", "cornell_alpha_64"]
 
 
 @pytest.mark.parametrize("name", RENDER_GOLDENS)
@@ -222,7 +240,7 @@ def test_render_direct_lighting_sphere_lights_bit_identical(gpu_ctx, samples):
 def test_render_unsupported_features_fail_cleanly(gpu_ctx):
     from yar_gb300 import native
     s = FlatScene.read(golden("cornell_c1_64.yfs"))
-    s.config["pixel_filter_type"] = 1  # gaussian
+    s.config["pixel_filter_type"] = 3  # no such filter
     gpu_ctx.upload_scene(s)
     with pytest.raises(native.YarError) as e:
         gpu_ctx.render(64, 64)
@@ -331,3 +349,18 @@ def test_direct_lighting_scene_refused_by_path_tracer_only_entry_points(gpu_ctx,
     with pytest.raises(native.YarError) as e:
         gpu_ctx.render_checkpoint(64, 64, tmp_path, "scene.pbrt")
     assert e.value.code == native.YAR_ERR_UNSUPPORTED
+
+
+def test_render_c1_configuration_matches_the_reference(gpu_ctx):
+    """The C1 configuration itself (256 x 256, 16 spp, maxdepth 8, seed offset
+    1) against the reference's own render of it, under the render bars."""
+    s = FlatScene.read(golden("cornell_c1_64.yfs"))
+    s.config["render_region"] = (0, 0, 256, 256)
+    s.camera["image_extent"] = (256, 256)
+    g = np.load(golden("cornell_c1_256.npz"))
+    gpu_ctx.upload_scene(s)
+    img, stats = gpu_ctx.render(256, 256)
+    same, rel = compare(img, g["image"])
+    assert same >= BIT_EQUAL_MIN and rel < MEAN_REL_TOL, (same, rel)
+    assert abs(stats.variance - float(g["variance"])) <= VARIANCE_REL_TOL * float(g["variance"])
+    assert stats.paths == 256 * 256 * 16

@@ -1,7 +1,7 @@
 """Command line: render a flat scene on the GPU and write the reference's EXR.
 
-    python -m yar_gb300 render SCENE --out image.exr [--spp N] [--seedoffset K] [--compress]
-    python -m yar_gb300 guided SCENE --out image.exr --passes N [--guide-fraction A] [--train-passes T]
+    python -m yar_gb300 render SCENE --out image.exr [--spp N] [--seedoffset K] [--compress] [--resolution WxH]
+    python -m yar_gb300 guided SCENE --out image.exr --passes N [--guide-fraction A] [--train-passes T] [--spp N]
     python -m yar_gb300 info SCENE
 
 SCENE is a .yfs flat scene (the reference's pbrt-v3 loader and kd-tree
@@ -38,6 +38,7 @@ def main(argv=None):
         q.add_argument("--out", required=True)
         q.add_argument("--compress", action="store_true", help="ZIP-compressed EXR")
         q.add_argument("--device", type=int, default=0)
+        q.add_argument("--resolution", default=None, help="WxH: render the whole image at this size")
         if name == "render":
             q.add_argument("--spp", type=int, default=0, help="samples per pixel (rounded up to k*k)")
             q.add_argument("--seedoffset", type=int, default=None)
@@ -47,8 +48,14 @@ def main(argv=None):
             q.add_argument("--guide-fraction", type=float, default=0.7)
             q.add_argument("--train-passes", type=int, default=64)
             q.add_argument("--time-budget", type=float, default=0.0)
+            q.add_argument("--spp", type=int, default=0,
+                           help="stratified form: after the training passes, this many samples per pixel")
     a = p.parse_args(argv)
     s = load(a.scene)
+    if getattr(a, "resolution", None):
+        rw, rh = (int(v) for v in a.resolution.lower().split("x"))
+        s.config["render_region"] = (0, 0, rw, rh)
+        s.camera["image_extent"] = (rw, rh)
     region = s.config["render_region"]
     w, h = int(region[2] - region[0]), int(region[3] - region[1])
     if a.cmd == "info":
@@ -74,10 +81,13 @@ def main(argv=None):
     else:
         ctx.upload_scene(s)
         img, _, st = ctx.guided_render(w, h, passes=a.passes, guide_fraction=a.guide_fraction,
-                                       train_passes=a.train_passes, time_budget=a.time_budget)
-        attrs = exr.yar_attributes(spp=st.passes, input_file=a.scene, device="gpu")
-        print("rendered %dx%d, %d guided passes in %.3f s (training %.3f s)" % (w, h, st.passes, st.seconds,
-                                                                              st.train_seconds))
+                                       train_passes=a.train_passes, time_budget=a.time_budget,
+                                       samples_per_pixel=a.spp)
+        spp = int(math.ceil(math.sqrt(a.spp))) ** 2 if a.spp else st.passes
+        attrs = exr.yar_attributes(spp=spp, input_file=a.scene, device="gpu")
+        print("rendered %dx%d, %s in %.3f s (training %.3f s)" % (
+            w, h, ("%d guided samples per pixel after %d training passes" % (spp, st.passes)) if a.spp
+            else "%d guided passes" % st.passes, st.seconds, st.train_seconds))
     exr.write_exr(a.out, img, a.compress, attrs)
     ctx.close()
     print("wrote", a.out)

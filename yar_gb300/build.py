@@ -115,8 +115,9 @@ def build_reference():
     if not have_src:
         return None
     binary = os.path.join(ORACLE_DIR, "_ref", "yar_ref")
-    deps = [os.path.join(ORACLE_DIR, "ref_harness.cpp"), script, os.path.join(ROOT, "include", "yar_gpu.h"),
-            os.path.join(CSRC, "yfs.hpp")]
+    deps = [os.path.join(ORACLE_DIR, "ref_harness.cpp"), os.path.join(ORACLE_DIR, "ref_flatten.hpp"),
+            os.path.join(ORACLE_DIR, "render_scene_gpu.cpp"), script, os.path.join(ROOT, "include", "yar_gpu.h"),
+            os.path.join(CSRC, "yfs.hpp"), LIB]
     if os.path.exists(binary) and not _stale(binary, deps):
         try:  # an x86 binary copied to an aarch64 host does not run: rebuild
             subprocess.run([binary], stdout=subprocess.DEVNULL, stderr=subprocess.DEVNULL, timeout=30)

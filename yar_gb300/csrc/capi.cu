@@ -259,7 +259,18 @@ extern "C" int yar_gpu_upload_scene(yar_gpu_ctx* ctx, const yar_flat_scene* scen
         memcpy(&tof, &to, 4);
         r[3] = make_float4(mesh.kdtree.bounds_min[0], mesh.kdtree.bounds_min[1], mesh.kdtree.bounds_min[2], nof);
         r[4] = make_float4(mesh.kdtree.bounds_max[0], mesh.kdtree.bounds_max[1], mesh.kdtree.bounds_max[2], tof);
-        int32_t info[4] = {o.mesh_index, mesh.visibility, 0, 0};
+        // info.z: the first mip of the mesh's alpha texture, -1 without one
+        int32_t alpha_mip = -1;
+        if (mesh.alpha_texture) {
+            if (mesh.alpha_texture > scene->texture_count || !mesh.uvs || !scene->texture_mips)
+                return fail(ctx, YAR_ERR_INVALID, "mesh " + std::to_string(o.mesh_index) +
+                                                      ": alpha texture without uvs or out of range");
+            const uint32_t first = scene->textures[mesh.alpha_texture - 1].first_mip;
+            if (first >= scene->texture_mip_count)
+                return fail(ctx, YAR_ERR_INVALID, "alpha texture with an invalid mip");
+            alpha_mip = (int32_t)first;
+        }
+        int32_t info[4] = {o.mesh_index, mesh.visibility, alpha_mip, 0};
         memcpy(&r[5], info, 16);
     }
     int rc;
@@ -283,6 +294,10 @@ extern "C" int yar_gpu_upload_scene(yar_gpu_ctx* ctx, const yar_flat_scene* scen
 
     rc = render_upload(ctx, scene);
     if (rc != YAR_OK) return rc;
+    // the alpha test reads the triangles' uvs and the textures' texels
+    ds.shading = (const float4*)ctx->render.shading.ptr;
+    ds.texels = (const float4*)ctx->render.texels.ptr;
+    ds.texture_mips = (const uint4*)ctx->render.texture_mips.ptr;
     for (int k = 0; k < 2; k++) {
         ctx->cast_kernel[k] = ctx->forced_kernel;
         for (int b = 0; b < yar_gpu_ctx::kBounceBuckets; b++) ctx->render_kernel[k][b] = ctx->forced_kernel;

@@ -36,7 +36,7 @@ __device__ __forceinline__ void write_result(const Traversal<ANY>& tr, uint32_t 
         a.hit2[i] = hit ? make_uint2(tr.hit.prim, tr.hit.object) : make_uint2(0xffffffffu, 0xffffffffu);
         return;
     }
-    if (a.t) a.t[i] = status < 0 ? tr.ray_tmax : tr.hit.t;
+    if (a.t) a.t[i] = status < 0 ? __ldg(a.rays + 2 * (size_t)tr.ray).w : tr.hit.t;
     if (a.prim) a.prim[i] = hit ? tr.hit.prim : 0xffffffffu;
     if (a.object) a.object[i] = hit ? tr.hit.object : 0xffffffffu;
     if (a.bary) a.bary[i] = hit ? make_float2(tr.hit.b1, tr.hit.b2) : make_float2(0.f, 0.f);
@@ -52,7 +52,6 @@ __global__ void __launch_bounds__(kCastBlock, MINB) cast_persistent(Device_Scene
     __shared__ uint2 stack_smem[SHORT > 0 ? SHORT * kCastBlock : 1];
     typename std::conditional<(SHORT > 0), Split_Stack<SHORT, kCastBlock>, Local_Stack>::type stack;
     if constexpr (SHORT > 0) stack.smem = stack_smem + threadIdx.x;
-    uint32_t ray = 0;
     bool have = false, alive = true;
     uint32_t batch_next = 0, batch_end = 0;  // warp-uniform
     for (;;) {
@@ -73,7 +72,7 @@ __global__ void __launch_bounds__(kCastBlock, MINB) cast_persistent(Device_Scene
             const uint32_t avail = batch_end - batch_next;
             const uint32_t rank = (uint32_t)__popc(want & lower);
             if (((want >> lane) & 1u) && rank < avail) {
-                ray = batch_next + rank;
+                const uint32_t ray = batch_next + rank;
                 const float4 r0 = __ldg(a.rays + 2 * (size_t)ray);
                 const float4 r1 = __ldg(a.rays + 2 * (size_t)ray + 1);
                 tr.begin(s, ray, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z), r0.w);
@@ -104,7 +103,7 @@ __global__ void __launch_bounds__(kCastBlock, MINB) cast_persistent(Device_Scene
             if (m == kSceneLeaf) tr.step_scene_leaf(s, a.rays, stack);
         }
         if (have && tr.mode() == kDone) {
-            write_result<ANY>(tr, a.perm ? __ldg(a.perm + ray) : ray, a);
+            write_result<ANY>(tr, a.perm ? __ldg(a.perm + tr.ray) : tr.ray, a);
             have = false;
         }
     }
@@ -133,18 +132,23 @@ __global__ void __launch_bounds__(kCastBlock) cast_per_ray(Device_Scene s, Cast_
 // workload (16M + 16M incoherent rays).  With one mode per warp iteration,
 // one node fetch per descent step: closest hit 19.8 ms against 21.3 ms at two
 // nodes per step, 21.6 ms at four and 25.7 ms descending to a leaf (the
-// per-lane schedule, every mode's code each iteration, took 25.4 ms).  High-
-// occupancy variant: closest hit at 10 resident blocks of 128 threads per SM
-// (19.0 ms, against 19.8 ms at 8 and 21.0 ms at 6), any hit at 12 blocks
-// (11.2 ms, against 11.6 ms at 10 and 12.7 ms at 8).  Earlier, with the
-// per-lane schedule: testing all of a leaf's triangles in one step was slower,
-// and the local-memory stack beat an 8- or 16-entry shared-memory stack with
-// local overflow.
+// per-lane schedule, every mode's code each iteration, took 25.4 ms); a loop
+// of node fetches while half the lanes descend (one vote per node) was no
+// faster (19.3 against 19.1 ms).  High-occupancy variant: closest hit at 10
+// resident blocks of 128 threads per SM (19.0 ms, against 19.7 ms at 8, 19.4
+// ms at 12 and 21.0 ms at 6), any hit at 12 blocks (11.2 ms, against 11.6 ms
+// at 10, 11.9 ms at 16 and 12.7 ms at 8).  With the traversal state trimmed
+// (direction signs in the flags word, 1/d shared by clipping and the
+// watertight setup): 18.5 and 10.7 ms; a 4-, 8- or 16-entry shared-memory
+// stack with local overflow was slower (18.6-19.2 and 11.4-13.6 ms).
 #ifndef YAR_CAST_NODES_PER_STEP
 #define YAR_CAST_NODES_PER_STEP 1
 #endif
 constexpr int kWhileWhile = YAR_CAST_NODES_PER_STEP;
-constexpr int kSharedStackEntries = 0;
+#ifndef YAR_CAST_SHARED_STACK
+#define YAR_CAST_SHARED_STACK 0
+#endif
+constexpr int kSharedStackEntries = YAR_CAST_SHARED_STACK;
 #ifndef YAR_CAST_BLOCKS_CLOSEST
 #define YAR_CAST_BLOCKS_CLOSEST 10
 #endif

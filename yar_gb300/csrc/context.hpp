@@ -131,8 +131,8 @@ struct Cast_Args {
     // any hit
     uint8_t* occluded = nullptr;
 };
-// Traversal kernels: persistent warps at high occupancy (closest hit 8
-// blocks per SM / 64 registers, any hit 12 blocks / 40 registers), persistent
+// Traversal kernels: persistent warps at high occupancy (closest hit 10
+// blocks per SM, any hit 12 blocks), persistent
 // warps capped at 128 registers (4 blocks per SM), one ray per thread.  All
 // give identical results; which is fastest depends on the scene and the rays,
 // so it is chosen per scene by timing (tune_cast).
@@ -170,5 +170,25 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats);
 int render_direct(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats);
 int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* params, double* sum_out, float* rgb_out,
                   yar_guided_stats* stats);
+
+// The learned proposal inside the stratified render (guided.cu -> render.cu):
+// before each shade launch `before_shade` computes the network inputs of the
+// extend queue's hits into `queries` and their lobe mixtures into `lobes`
+// (both per queue position, sized for `chunk_paths`); the shade kernel then
+// draws continuations from the mixture with probability `alpha`.
+struct Guide_Render_Hook {
+    const float* lobes = nullptr;
+    const float4* queries = nullptr;
+    float alpha = 0.f;
+    uint64_t chunk_paths = 0;  // paths in flight per chunk
+    cudaError_t (*before_shade)(void* user, const float4* rays, const float4* hit4, const uint2* hit2,
+                                uint32_t count, cudaStream_t st) = nullptr;
+    void* user = nullptr;
+};
+// The path tracer with the scene's pixel sampler at spp_side x spp_side
+// samples per pixel, pixel streams offset by stream_hi (non-zero: streams
+// independent of the reference's), continuations guided through `hook`.
+int render_guided_stratified(yar_gpu_ctx* ctx, int spp_side, uint32_t stream_hi, const Guide_Render_Hook& hook,
+                             float* rgb_out, yar_render_stats* stats);
 
 } // namespace yar

@@ -46,6 +46,11 @@ struct Device_Scene {
     const uint2* mesh_nodes = nullptr;
     const float4* objects = nullptr;
     const float4* tris = nullptr;
+    // alpha test: per-triangle shading records (uvs in the .w / last lanes),
+    // texels and mip records of the scene's image textures
+    const float4* shading = nullptr;
+    const float4* texels = nullptr;
+    const uint4* texture_mips = nullptr;
     float scene_bounds[6] = {0, 0, 0, 0, 0, 0};
     uint32_t object_count = 0;
 };
@@ -73,6 +78,30 @@ __device__ __forceinline__ bool clip_axis(float mn, float mx, float o, float d, 
     return !(o < mn || o > mx);
 }
 
+// The same with 1/d already computed (the value clip_axis divides out).
+__device__ __forceinline__ bool clip_axis_inv(float mn, float mx, float o, float d, float inv, float& t0, float& t1) {
+    if (d != 0.f) {
+        float s0 = (mn - o) * inv;
+        float s1 = (mx - o) * inv;
+        if (inv < 0.f) { const float tmp = s0; s0 = s1; s1 = tmp; }
+        t0 = s0 > t0 ? s0 : t0;
+        t1 = s1 < t1 ? s1 : t1;
+        return !(t0 > t1);
+    }
+    return !(o < mn || o > mx);
+}
+
+__device__ __forceinline__ bool clip_ray_inv(float3 mn, float3 mx, float3 o, float3 d, float3 inv, float& t_min,
+                                             float& t_max) {
+    float t0 = 0.f, t1 = __int_as_float(0x7f800000);
+    if (!clip_axis_inv(mn.x, mx.x, o.x, d.x, inv.x, t0, t1)) return false;
+    if (!clip_axis_inv(mn.y, mx.y, o.y, d.y, inv.y, t0, t1)) return false;
+    if (!clip_axis_inv(mn.z, mx.z, o.z, d.z, inv.z, t0, t1)) return false;
+    t_min = t0;
+    t_max = t1;
+    return true;
+}
+
 __device__ __forceinline__ bool clip_ray(float3 mn, float3 mx, float3 o, float3 d, float& t_min, float& t_max) {
     float t0 = 0.f, t1 = __int_as_float(0x7f800000);
     if (!clip_axis(mn.x, mx.x, o.x, d.x, t0, t1)) return false;
@@ -89,7 +118,8 @@ struct Watertight_Ray {
     float sx, sy, sz;
 };
 
-__device__ __forceinline__ Watertight_Ray watertight_setup(float3 d) {
+// inv = 1/d per axis (the same IEEE division the setup's 1/dz is).
+__device__ __forceinline__ Watertight_Ray watertight_setup(float3 d, float3 inv) {
     Watertight_Ray w;
     const float ax = fabsf(d.x), ay = fabsf(d.y), az = fabsf(d.z);
     w.kz = (ax > ay) ? (ax > az ? 0 : 2) : (ay > az ? 1 : 2);  // Vector3::max_dimension
@@ -98,7 +128,7 @@ __device__ __forceinline__ Watertight_Ray watertight_setup(float3 d) {
     const float dx = sel3(d.x, d.y, d.z, w.kx), dy = sel3(d.x, d.y, d.z, w.ky), dz = sel3(d.x, d.y, d.z, w.kz);
     w.sx = -dx / dz;
     w.sy = -dy / dz;
-    w.sz = 1.f / dz;
+    w.sz = sel3(inv.x, inv.y, inv.z, w.kz);
     return w;
 }
 
@@ -144,6 +174,38 @@ __device__ __forceinline__ float watertight(float3 o, const Watertight_Ray& w, f
     return t;
 }
 
+// The alpha test of both leaf callbacks (src/ref/kdtree.cpp:31-38, :69-77):
+// the hit's uv, Triangle_Mesh::get_uv (barycentric_interpolate, src/lib/math.h:
+// 146-153: b.x uv0 + b.y uv1 + b.z uv2), the alpha texture's mip 0 sampled by
+// Image_Texture::sample_bilinear with repeat wrapping (image_texture.cpp:441-476);
+// true when its red channel is 0 (the triangle is skipped).
+__device__ __forceinline__ float alpha_texel_r(const Device_Scene& s, uint4 mip, int x, int y) {  // get_texel_repeat
+    const int w = (int)mip.x, h = (int)mip.y;
+    if (x >= 0) x &= w - 1;
+    else { x %= w; x += (x >> 31) & w; }
+    if (y >= 0) y &= h - 1;
+    else { y %= h; y += (y >> 31) & h; }
+    return __ldg(&s.texels[mip.z + (size_t)y * (size_t)w + (size_t)x].x);
+}
+static __device__ __noinline__ bool alpha_rejects(const Device_Scene& s, uint32_t object, uint32_t global_tri, float b0, float b1,
+                                           float b2) {
+    const uint32_t mip_index = __float_as_uint(__ldg(s.objects + 6 * (size_t)object + 5).z);
+    const float4* sh = s.shading + 4 * (size_t)global_tri;
+    const float4 s0 = __ldg(sh), s1 = __ldg(sh + 1), s2 = __ldg(sh + 2), s3 = __ldg(sh + 3);
+    const float u = b0 * s0.w + b1 * s2.w + b2 * s3.y;
+    const float v = b0 * s1.w + b1 * s3.x + b2 * s3.z;
+    const uint4 mip = __ldg(s.texture_mips + mip_index);
+    const float x = u * (float)mip.x - 0.5f, y = v * (float)mip.y - 0.5f;
+    const float x_floor = floorf(x), y_floor = floorf(y);
+    const float wx = x - x_floor, wy = y - y_floor;
+    const int x0 = (int)x_floor, y0 = (int)y_floor, x1 = x0 + 1, y1 = y0 + 1;
+    const float r = ((alpha_texel_r(s, mip, x0, y0) * ((1 - wy) * (1 - wx)) +
+                      alpha_texel_r(s, mip, x1, y0) * ((1 - wy) * wx)) +
+                     alpha_texel_r(s, mip, x0, y1) * (wy * (1 - wx))) +
+                    alpha_texel_r(s, mip, x1, y1) * (wy * wx);
+    return r == 0.f;
+}
+
 // transform_ray, src/lib/matrix.cpp:368-389: ((a*x + b*y) + c*z) + w
 __device__ __forceinline__ void transform_ray(float4 r0, float4 r1, float4 r2, float3 o, float3 d, float3& oo,
                                               float3& od) {
@@ -178,8 +240,8 @@ constexpr int kStackEntries = 2 * kMaxTraversalDepth + 2;
 // re-read from its node (an L1 hit) instead of being held.
 template <bool ANY>
 struct Traversal {
-    float3 co, cd, cinv;   // ray of the current level (the world ray at scene level)
-    float ray_tmax;
+    float3 co, cinv;       // ray origin and 1/direction of the current level (world ray at scene level)
+    float ray_tmax;        // (read by any hit only)
     uint32_t ray;          // index of the ray record
     uint32_t node;         // current node; while a leaf is processed, the leaf
     float t_min, t_max;
@@ -188,7 +250,9 @@ struct Traversal {
     uint32_t tri_offset;   // triangle offset of the current mesh
     uint32_t leaf_i;       // next primitive of the current leaf
     uint32_t cur_object;
-    uint32_t flags;        // bits 0-1 mode, 2 in mesh, 3 test triangles, 4-9 kx ky kz, 10-11 status + 1
+    uint32_t flags;        // bits 0-1 mode, 2 in mesh, 3 test triangles, 4-9 kx ky kz, 10-11 status + 1,
+                           // 12-14 direction component > 0 (x, y, z) of the current level's ray,
+                           // 15 the current mesh has an alpha texture
     float sx, sy, sz;      // watertight setup of the mesh ray (src/ref/intersection.cpp:55-62)
     Hit hit;
 
@@ -196,6 +260,15 @@ struct Traversal {
     __device__ __forceinline__ void set_mode(int m) { flags = (flags & ~3u) | (uint32_t)m; }
     __device__ __forceinline__ bool in_mesh() const { return (flags >> 2) & 1u; }
     __device__ __forceinline__ int status() const { return (int)((flags >> 10) & 3u) - 1; }
+
+    // the direction itself is not held: its per-axis signs steer descents
+    // through split planes the origin lies on, and the world direction is
+    // reloaded from the ray record where an object is entered
+    static __device__ __forceinline__ uint32_t positive_bits(float x, float y, float z) {
+        return (x > 0.f ? 1u << 12 : 0u) | (y > 0.f ? 1u << 13 : 0u) | (z > 0.f ? 1u << 14 : 0u);
+    }
+    static constexpr uint32_t kSignBits = 7u << 12;
+    __device__ __forceinline__ int closest_status() const { return hit.prim != 0xffffffffu ? 1 : 0; }
 
     __device__ __forceinline__ void finish(int st) { flags = (flags & ~(3u | (3u << 10))) | (uint32_t)kDone | ((uint32_t)(st + 1) << 10); }
 
@@ -211,9 +284,8 @@ struct Traversal {
         t_max = __uint_as_float(interval.y);
         const float4 r0 = __ldg(rays + 2 * (size_t)ray), r1 = __ldg(rays + 2 * (size_t)ray + 1);
         co = make_float3(r0.x, r0.y, r0.z);
-        cd = make_float3(r1.x, r1.y, r1.z);
-        cinv = make_float3(1.f / cd.x, 1.f / cd.y, 1.f / cd.z);
-        flags = (flags & ~(3u | 4u)) | (uint32_t)kSceneLeaf;
+        cinv = make_float3(1.f / r1.x, 1.f / r1.y, 1.f / r1.z);
+        flags = (flags & ~(3u | 4u | kSignBits)) | (uint32_t)kSceneLeaf | positive_bits(r1.x, r1.y, r1.z);
     }
 
     __device__ __forceinline__ void begin(const Device_Scene& s, uint32_t ray_index, float3 ro, float3 rd, float tmax) {
@@ -227,14 +299,16 @@ struct Traversal {
         mesh_sp_base = 0;
         node = 0;
         flags = (uint32_t)kDescend | (1u << 10);  // status 0
-        if (!clip_ray(make_float3(s.scene_bounds[0], s.scene_bounds[1], s.scene_bounds[2]),
-                      make_float3(s.scene_bounds[3], s.scene_bounds[4], s.scene_bounds[5]), ro, rd, t_min, t_max)) {
+        const float3 inv = make_float3(1.f / rd.x, 1.f / rd.y, 1.f / rd.z);
+        if (!clip_ray_inv(make_float3(s.scene_bounds[0], s.scene_bounds[1], s.scene_bounds[2]),
+                          make_float3(s.scene_bounds[3], s.scene_bounds[4], s.scene_bounds[5]), ro, rd, inv, t_min,
+                          t_max)) {
             finish(0);
             return;
         }
         co = ro;
-        cd = rd;
-        cinv = make_float3(1.f / rd.x, 1.f / rd.y, 1.f / rd.z);
+        cinv = inv;
+        flags |= positive_bits(rd.x, rd.y, rd.z);
     }
 
     // The current level's leaf is done: pop the level's next node, or end the
@@ -247,7 +321,7 @@ struct Traversal {
                 return;
             }
         } else if (sp == 0) {
-            finish(ANY ? 0 : (hit.t < ray_tmax ? 1 : 0));
+            finish(ANY ? 0 : closest_status());
             return;
         }
         --sp;
@@ -274,7 +348,7 @@ struct Traversal {
                 if (in_mesh()) {
                     leave_mesh(s, rays, stack);
                 } else {
-                    finish(ANY ? 0 : (hit.t < ray_tmax ? 1 : 0));
+                    finish(ANY ? 0 : closest_status());
                 }
                 return;
             }
@@ -314,7 +388,7 @@ struct Traversal {
                     t_max = t_split;
                 }
             } else {
-                node = (sel3(cd.x, cd.y, cd.z, axis) > 0.f) ? above_child : below_child;
+                node = ((flags >> (12 + axis)) & 1u) ? above_child : below_child;
             }
         }
     }
@@ -343,11 +417,13 @@ struct Traversal {
             const float t = watertight(co, wr, v0, v1, v2, b0, b1, b2);
             if (ANY) {
                 // `t >= ray_tmax` rejects; a NaN t does not (src/ref/kdtree.cpp:60-62)
-                if (!(t >= ray_tmax) && v0.w == 0.f) {
+                if (!(t >= ray_tmax) && v0.w == 0.f &&
+                    !(((flags >> 15) & 1u) && alpha_rejects(s, cur_object, tri_offset + prim, b0, b1, b2))) {
                     finish(1);
                     return;
                 }
-            } else if (t < hit.t && v0.w == 0.f) {
+            } else if (t < hit.t && v0.w == 0.f &&
+                       !(((flags >> 15) & 1u) && alpha_rejects(s, cur_object, tri_offset + prim, b0, b1, b2))) {
                 // the object of the closest hit is the one whose mesh produced it
                 // (src/ref/kdtree.cpp:81-95 sets it after the mesh improved the hit)
                 hit.t = t;
@@ -377,10 +453,12 @@ struct Traversal {
             const float4* p = s.objects + 6 * (size_t)obj;
             const float4 r0 = __ldg(p + 0), r1 = __ldg(p + 1), r2 = __ldg(p + 2);
             const float4 lo = __ldg(p + 3), hi = __ldg(p + 4), info = __ldg(p + 5);
+            const float4 wd = __ldg(rays + 2 * (size_t)ray + 1);  // the world direction
             float3 oo, od;
-            transform_ray(r0, r1, r2, co, cd, oo, od);
+            transform_ray(r0, r1, r2, co, make_float3(wd.x, wd.y, wd.z), oo, od);
             float mt_min, mt_max;
-            if (clip_ray(make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z), oo, od, mt_min, mt_max)) {
+            const float3 oinv = make_float3(1.f / od.x, 1.f / od.y, 1.f / od.z);
+            if (clip_ray_inv(make_float3(lo.x, lo.y, lo.z), make_float3(hi.x, hi.y, hi.z), oo, od, oinv, mt_min, mt_max)) {
                 if (sp + 2 > kStackEntries) {
                     finish(-1);
                     return;
@@ -391,18 +469,18 @@ struct Traversal {
                 mesh_sp_base = sp;
                 cur_object = obj;
                 co = oo;
-                cd = od;
-                cinv = make_float3(1.f / od.x, 1.f / od.y, 1.f / od.z);
+                cinv = oinv;
                 mesh_offset = __float_as_uint(lo.w);
                 tri_offset = __float_as_uint(hi.w);
                 const int visibility = __float_as_int(info.y);
                 const bool test_triangles = ANY ? (visibility == 0) : (visibility != 2);
-                const Watertight_Ray wr = watertight_setup(od);
+                const Watertight_Ray wr = watertight_setup(od, oinv);
                 sx = wr.sx;
                 sy = wr.sy;
                 sz = wr.sz;
                 flags = (flags & (3u << 10)) | (uint32_t)kDescend | 4u | (test_triangles ? 8u : 0u) |
-                        ((uint32_t)wr.kx << 4) | ((uint32_t)wr.ky << 6) | ((uint32_t)wr.kz << 8);
+                        ((uint32_t)wr.kx << 4) | ((uint32_t)wr.ky << 6) | ((uint32_t)wr.kz << 8) |
+                        positive_bits(od.x, od.y, od.z) | (__float_as_int(info.z) >= 0 ? 1u << 15 : 0u);
                 node = 0;
                 t_min = mt_min;
                 t_max = mt_max;

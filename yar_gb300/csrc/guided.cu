@@ -118,11 +118,37 @@ T* dp(Device_Buffer& b) {
     return reinterpret_cast<T*>(b.ptr);
 }
 
+// The guide hook of the stratified render: network inputs of the extend
+// queue's hits, then tensor-core inference of their lobe mixtures.
+struct Guide_Hook_State {
+    yar_gpu_ctx* ctx;
+    Scene_Dev S;
+    float4* queries;
+    float* lobes;
+    float box[6];
+};
+
+cudaError_t guided_before_shade(void* user, const float4* rays, const float4* hit4, const uint2* hit2, uint32_t count,
+                                cudaStream_t st) {
+    Guide_Hook_State* h = static_cast<Guide_Hook_State*>(user);
+    guide_query_kernel<<<grid_for(count), kBlock, 0, st>>>(h->S, rays, hit4, hit2, count, h->queries);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) return e;
+    return guide_infer(h->ctx, h->queries, count, nullptr, h->box, h->lobes, st);
+}
+
+constexpr uint64_t kGuidedChunkPaths = 8u << 20;  // stratified phase: paths in flight (lobes 160 B each)
+
 } // namespace
 
 int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out, float* rgb_out,
                   yar_guided_stats* stats) {
-    if (!gp || gp->passes == 0) return fail(ctx, YAR_ERR_INVALID, "guided render: no passes");
+    if (!gp || (gp->passes == 0 && gp->samples_per_pixel == 0))
+        return fail(ctx, YAR_ERR_INVALID, "guided render: no passes");
+    // stratified: the training passes, then one render with the pixel sampler
+    const int spp_side = gp->samples_per_pixel ? (int)std::ceil(std::sqrt((double)gp->samples_per_pixel)) : 0;
+    if (spp_side > 256) return fail(ctx, YAR_ERR_INVALID, "guided render: at most 65536 samples per pixel");
+    const uint32_t pass_count = spp_side ? (gp->guide_fraction > 0.f ? gp->train_passes : 0u) : gp->passes;
     if (!(gp->guide_fraction >= 0.f && gp->guide_fraction < 1.f))
         return fail(ctx, YAR_ERR_INVALID, "guide fraction must be in [0, 1)");
     if (ctx->render.config.rendering_algorithm == 0)
@@ -130,8 +156,8 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
     Render_Params p;
     if (int rc0 = prepare_render_params(ctx, p)) return rc0;
     if (p.textured) return fail(ctx, YAR_ERR_UNSUPPORTED, "the guided render does not evaluate image textures");
-    if (p.filter_radius > 0.5f)
-        return fail(ctx, YAR_ERR_UNSUPPORTED, "guided render: box filter of radius <= 0.5 only (one pixel per sample)");
+    if (!spp_side && (p.filter_radius > 0.5f || p.filter_type != 0))
+        return fail(ctx, YAR_ERR_UNSUPPORTED, "guided passes: box filter of radius <= 0.5 only (one pixel per sample)");
     p.nx = p.ny = p.spp = 1;
     const uint32_t paths = (uint32_t)((uint64_t)p.sw * p.sh);
     if ((uint64_t)p.sw * p.sh > kChunkSampleBudget) return fail(ctx, YAR_ERR_CAPACITY, "guided render: image too large");
@@ -219,9 +245,9 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
     float last_loss = 0.f;
     uint32_t done = 0;
     const auto t0 = std::chrono::steady_clock::now();
-    for (uint32_t pass = 0; pass < gp->passes && e == cudaSuccess; pass++) {
+    for (uint32_t pass = 0; pass < pass_count && e == cudaSuccess; pass++) {
         p.stream_hi = (gp->stream_offset << 20) + pass + 1u;
-        const bool training = guided && pass < gp->train_passes;
+        const bool training = guided && pass < gp->train_passes;  // (every pass, stratified)
         Guide_Shade g;
         if (guided) {
             g.queries = dp<float4>(B[30]);
@@ -299,7 +325,61 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
         if (e == cudaSuccess) e = cudaStreamSynchronize(st);
         done = pass + 1;
         const double elapsed = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        if (gp->time_budget > 0.f && elapsed >= gp->time_budget) break;
+        if (!spp_side && gp->time_budget > 0.f && elapsed >= gp->time_budget) break;
+    }
+    if (spp_side && e == cudaSuccess) {
+        // the image: the scene's pixel sampler at spp_side^2 samples per pixel,
+        // continuations from the trained proposal
+        for (Device_Buffer& b : B) device_free(b);  // the stratified render allocates its own working set
+        Device_Buffer qbuf, lbuf;
+        Guide_Hook_State hs{ctx, S, nullptr, nullptr, {box[0], box[1], box[2], box[3], box[4], box[5]}};
+        Guide_Render_Hook hook;
+        hook.alpha = guided ? gp->guide_fraction : 0.f;
+        hook.chunk_paths = std::max<uint64_t>(kGuidedChunkPaths, (uint64_t)spp_side * spp_side);
+        if (guided) {
+            rc = device_alloc(ctx, qbuf, hook.chunk_paths * 3 * sizeof(float4));
+            if (rc == YAR_OK) rc = device_alloc(ctx, lbuf, hook.chunk_paths * kGuideLobeFloats * sizeof(float));
+            if (rc != YAR_OK) {
+                device_free(qbuf);
+                device_free(lbuf);
+                return rc;
+            }
+            hs.queries = dp<float4>(qbuf);
+            hs.lobes = dp<float>(lbuf);
+            hook.queries = hs.queries;
+            hook.lobes = hs.lobes;
+            hook.before_shade = guided_before_shade;
+            hook.user = &hs;
+        }
+        std::vector<float> img((size_t)p.rw * p.rh * 3);
+        yar_render_stats rs{};
+        if (!guided) hook.chunk_paths = std::max<uint64_t>(kChunkSampleBudget, (uint64_t)spp_side * spp_side);
+        rc = render_guided_stratified(ctx, spp_side, (gp->stream_offset << 20) | 0xfffffu, hook, img.data(), &rs);
+        device_free(qbuf);
+        device_free(lbuf);
+        if (rc != YAR_OK) return rc;
+        int h_err = 0;
+        e = cudaMemcpy(&h_err, ctx->d_error, sizeof(int), cudaMemcpyDeviceToHost);
+        if (e != cudaSuccess) return cuda_fail(ctx, e, "guided render");
+        if (h_err) {
+            cudaMemset(ctx->d_error, 0, sizeof(int));
+            return fail(ctx, YAR_ERR_TIMEOUT, "tensor-core wait gave up");
+        }
+        const double seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
+        const double n = (double)spp_side * spp_side;
+        for (size_t k = 0; k < img.size(); k++) {
+            if (rgb_out) rgb_out[k] = img[k];
+            if (sum_out) sum_out[k] = (double)img[k] * n;
+        }
+        if (stats) {
+            stats->passes = done;
+            stats->seconds = (float)seconds;
+            stats->train_seconds = (float)train_seconds;
+            stats->rays = rays + rs.rays_closest + rs.rays_any;
+            stats->train_samples = train_samples;
+            stats->loss = last_loss;
+        }
+        return YAR_OK;
     }
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     const double seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();

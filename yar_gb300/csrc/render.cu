@@ -371,7 +371,7 @@ struct Tile_Output {
 };
 
 int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p, float* rgb_out, yar_render_stats* stats,
-                      Tile_Output* tiles_out);
+                      Tile_Output* tiles_out, const Guide_Render_Hook* guide = nullptr);
 
 int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
     if (!rgb_out) return fail(ctx, YAR_ERR_INVALID, "null image buffer");
@@ -384,7 +384,7 @@ int render_run(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
 // The render of render_run over the sample region of p.  With tiles_out, the
 // image is not resolved: the tiles' film data come back instead.
 int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_out, yar_render_stats* stats,
-                      Tile_Output* tiles_out) {
+                      Tile_Output* tiles_out, const Guide_Render_Hook* guide) {
     cudaSetDevice(ctx->device);
     // Draws past the sampler budget follow the reference's per-pixel stream
     // (exact tail) for the reference's own streams.
@@ -395,7 +395,8 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
     const auto t_start = std::chrono::steady_clock::now();
     const uint64_t pixels = (uint64_t)p.sw * p.sh;
     const uint64_t samples = pixels * p.spp;
-    const uint64_t chunk_pixels = std::max<uint64_t>(1, std::min<uint64_t>(pixels, kChunkSampleBudget / p.spp));
+    const uint64_t budget = guide && guide->chunk_paths ? guide->chunk_paths : kChunkSampleBudget;
+    const uint64_t chunk_pixels = std::max<uint64_t>(1, std::min<uint64_t>(pixels, budget / p.spp));
     const uint64_t cap = chunk_pixels * p.spp;  // paths per chunk
 
     // scratch: everything sized by the largest chunk, allocated per call
@@ -481,8 +482,20 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
             e = trace_extend(ctx, q, cur, count, bounce, st);
             if (e != cudaSuccess) break;
             cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
-            launch_shade<false>(pp, grid_for(count), st, S, cur, count, dptr<float>(B[2]), dptr<float2>(B[3]), ps, q,
-                                Guide_Shade{});
+            if (guide && guide->before_shade) {
+                e = guide->before_shade(guide->user, q.ext_rays[cur], q.ext_hit4, q.ext_hit2, count, st);
+                if (e != cudaSuccess) break;
+                Guide_Shade gs;
+                gs.lobes = guide->lobes;
+                gs.queries = guide->queries;
+                gs.alpha = guide->alpha;
+                launch_shade<true>(pp, grid_for(count), st, S, cur, count, dptr<float>(B[2]), dptr<float2>(B[3]), ps,
+                                   q, gs);
+                launches += 2;
+            } else {
+                launch_shade<false>(pp, grid_for(count), st, S, cur, count, dptr<float>(B[2]), dptr<float2>(B[3]), ps,
+                                    q, Guide_Shade{});
+            }
             e = trace_light_queues(ctx, q, ps, count, bounce, st);
             if (e != cudaSuccess) break;
             connect_kernel<<<grid_for(count), kBlock, 0, st>>>(pp, S, q.ext_slot[cur], count, ps, nullptr);
@@ -610,6 +623,19 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
         stats->kernel_launches = launches;
     }
     return YAR_OK;
+}
+
+int render_guided_stratified(yar_gpu_ctx* ctx, int spp_side, uint32_t stream_hi, const Guide_Render_Hook& hook,
+                             float* rgb_out, yar_render_stats* stats) {
+    if (!rgb_out || spp_side < 1 || spp_side > 256 || stream_hi == 0)
+        return fail(ctx, YAR_ERR_INVALID, "guided stratified render: arguments");
+    Render_Params p;
+    if (int rc0 = prepare_render_params(ctx, p)) return rc0;
+    p.nx = p.ny = spp_side;
+    p.spp = spp_side * spp_side;
+    p.stream_hi = stream_hi;  // own pixel streams: draws past the budget from one pcg stream per sample
+    if (hook.chunk_paths < (uint64_t)p.spp) return fail(ctx, YAR_ERR_CAPACITY, "guided stratified render: chunk");
+    return render_run_params(ctx, p, rgb_out, stats, nullptr, &hook);
 }
 
 // ---------------------------------------------------------------- render without allocation

@@ -97,6 +97,9 @@ struct Render_Params {
     int32_t max_bounces, rr_bounce_threshold;
     float rr_threshold;
     float filter_radius;
+    int32_t filter_type;    // Raytracer_Config::Pixel_Filter_Type: 0 box, 1 gaussian, 2 triangle
+    float filter_alpha;     // gaussian falloff
+    float filter_zero;      // gaussian: exp(-alpha r^2), the weight at the radius (computed on the host)
     float film_scale, max_component;
     int32_t total_lights, delta_lights, rect_lights, sphere_lights, mesh_lights, env_lights;  // selection order
     int32_t full_shading;  // the scene needs shade_kernel<*, true>
@@ -1791,8 +1794,20 @@ cudaError_t launch_generate(const Render_Params& p, uint32_t first, uint32_t cp,
     return cudaGetLastError();
 }
 
+// The film filter's weight at offset (x, y) = film position - pixel center
+// (src/ref/film.cpp:123-142): box 1; gaussian max(0, exp(-alpha |p|^2) - exp(-alpha
+// r^2)) with the exponential correctly rounded; triangle max(0, r - |x|) max(0, r - |y|).
+__device__ __forceinline__ float film_filter_weight(const Render_Params& p, float x, float y) {
+    if (p.filter_type == 1) {
+        const float e = (float)exp((double)(-p.filter_alpha * (x * x + y * y)));
+        return max_std(0.f, e - p.filter_zero);
+    }
+    if (p.filter_type == 2) return max_std(0.f, p.filter_radius - fabsf(x)) * max_std(0.f, p.filter_radius - fabsf(y));
+    return 1.f;
+}
+
 // Film_Tile t's sum for film pixel (px, py): the samples of the tile's sample
-// region whose box-filter footprint covers the pixel, in the tile's own sample
+// region whose filter footprint covers the pixel, in the tile's own sample
 // order (Film_Tile::add_sample, src/ref/film.cpp:27-50), as (color sum, weight).
 __device__ __forceinline__ float4 tile_pixel_sum(const Render_Params& p, const float4* __restrict__ radiance,
                                                  const float2* __restrict__ image_samples, int t, int px, int py) {
@@ -1817,10 +1832,11 @@ __device__ __forceinline__ float4 tile_pixel_sum(const Render_Params& p, const f
                 rx1 = min(rx1, bx1); ry1 = min(ry1, by1);
                 if (px < rx0 || px >= rx1 || py < ry0 || py >= ry1) continue;
                 const float4 c = radiance[pix * p.spp + k];
-                tr += 1.f * c.x;
-                tg += 1.f * c.y;
-                tb += 1.f * c.z;
-                tw += 1.f;
+                const float w = film_filter_weight(p, fx - ((float)px + 0.5f), fy - ((float)py + 0.5f));
+                tr += w * c.x;
+                tg += w * c.y;
+                tb += w * c.z;
+                tw += w;
             }
         }
     return make_float4(tr, tg, tb, tw);
@@ -1928,7 +1944,7 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     const yar_render_config& c = R.config;
     if (c.rendering_algorithm != 0 && c.rendering_algorithm != 1)
         return fail(ctx, YAR_ERR_UNSUPPORTED, "unknown rendering algorithm");
-    if (c.pixel_filter_type != 0) return fail(ctx, YAR_ERR_UNSUPPORTED, "only the box filter is implemented");
+    if (c.pixel_filter_type < 0 || c.pixel_filter_type > 2) return fail(ctx, YAR_ERR_UNSUPPORTED, "unknown pixel filter");
     if (R.other_light_count)
         return fail(ctx, YAR_ERR_UNSUPPORTED, "the scene has lights of a kind that is not implemented");
     if (R.has_environment && R.has_no_shadow_meshes)
@@ -2039,6 +2055,10 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     p.rr_bounce_threshold = c.russian_roulette_bounce_count_threshold;
     p.rr_threshold = c.russian_roulette_threshold;
     p.filter_radius = radius;
+    p.filter_type = c.pixel_filter_type;
+    p.filter_alpha = c.pixel_filter_alpha;
+    // get_gaussian_filter (src/ref/film.cpp:128-135) evaluates the zero level once, in float
+    p.filter_zero = c.pixel_filter_type == 1 ? std::exp(-c.pixel_filter_alpha * radius * radius) : 0.f;
     p.film_scale = c.film_radiance_scale;
     p.max_component = c.max_rgb_component_value_of_film_sample;
     p.rect_lights = (int)R.host_rect_lights.size();

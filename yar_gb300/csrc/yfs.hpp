@@ -35,6 +35,7 @@ struct Mesh {
     int32_t visibility = YAR_VISIBLE;
     float bounds[6] = {0, 0, 0, 0, 0, 0};
     std::vector<yar_kd_node> nodes;
+    uint32_t alpha_texture = 0;  // 0 none, else 1 + texture index
 };
 
 struct Scene {
@@ -76,6 +77,7 @@ struct Scene {
             memcpy(d.kdtree.bounds_max, m.bounds + 3, 3 * sizeof(float));
             d.kdtree.nodes = m.nodes.data();
             d.kdtree.node_count = (uint32_t)m.nodes.size();
+            d.alpha_texture = m.alpha_texture;
         }
         yar_flat_scene s{};
         s.mesh_count = (uint32_t)meshes.size();
@@ -164,7 +166,7 @@ inline bool write(const std::string& path, const Scene& s) {
     for (const Mesh& m : s.meshes) {
         detail::Buf b;
         uint32_t vc = (uint32_t)(m.vertices.size() / 3), tc = (uint32_t)(m.indices.size() / 3);
-        uint32_t flags = (m.normals.empty() ? 0u : 1u) | (m.uvs.empty() ? 0u : 2u);
+        uint32_t flags = (m.normals.empty() ? 0u : 1u) | (m.uvs.empty() ? 0u : 2u) | (m.alpha_texture ? 4u : 0u);
         uint32_t nc = (uint32_t)m.nodes.size();
         b.pod(vc); b.pod(tc); b.pod(flags); b.pod(m.reverse_orientation); b.pod(m.visibility); b.pod(nc);
         b.raw(m.bounds, sizeof(m.bounds));
@@ -173,6 +175,7 @@ inline bool write(const std::string& path, const Scene& s) {
         if (flags & 1) b.raw(m.normals.data(), m.normals.size() * 4);
         if (flags & 2) b.raw(m.uvs.data(), m.uvs.size() * 4);
         b.raw(m.nodes.data(), m.nodes.size() * sizeof(yar_kd_node));
+        if (flags & 4) b.pod(m.alpha_texture);
         w.chunk("MESH", b.b);
     }
     {
@@ -300,6 +303,7 @@ inline bool read(const std::string& path, Scene& s, std::string* err = nullptr) 
             if (flags & 2) { m.uvs.resize((size_t)vc * 2); c.raw(m.uvs.data(), m.uvs.size() * 4); }
             m.nodes.resize(nc);
             c.raw(m.nodes.data(), nc * sizeof(yar_kd_node));
+            if (flags & 4) m.alpha_texture = c.pod<uint32_t>();
             if (!c.ok) return fail("truncated mesh chunk");
             s.meshes.push_back(std::move(m));
         } else if (!memcmp(tag, "OBJS", 4)) {

@@ -57,7 +57,7 @@ class MeshDesc(C.Structure):
     _fields_ = [("vertices", C.c_void_p), ("normals", C.c_void_p), ("uvs", C.c_void_p),
                 ("indices", C.c_void_p), ("vertex_count", C.c_uint32), ("triangle_count", C.c_uint32),
                 ("reverse_geometric_normal_orientation", C.c_int32), ("visibility", C.c_int32),
-                ("kdtree", KdTreeView)]
+                ("kdtree", KdTreeView), ("alpha_texture", C.c_uint32)]
 
 
 class ObjectDesc(C.Structure):
@@ -162,7 +162,7 @@ class BatchStats(C.Structure):
 class GuidedParams(C.Structure):
     _fields_ = [("passes", C.c_uint32), ("train_passes", C.c_uint32), ("guide_fraction", C.c_float),
                 ("learning_rate", C.c_float), ("train_steps", C.c_uint32), ("stream_offset", C.c_uint32),
-                ("time_budget", C.c_float), ("keep_guide", C.c_uint32)]
+                ("time_budget", C.c_float), ("keep_guide", C.c_uint32), ("samples_per_pixel", C.c_uint32)]
 
 
 class GuidedStats(C.Structure):
@@ -432,12 +432,14 @@ class Context:
         self._check(lib().yar_gpu_render_batch(self._h, arr, len(flats), outs, sst, C.byref(st)), "render_batch")
         return imgs, list(sst), st
 
-    def guided_render(self, width, height, passes, guide_fraction=0.0, train_passes=0, learning_rate=2e-3,
-                      train_steps=8, stream_offset=0, time_budget=0.0, keep_guide=False):
+    def guided_render(self, width, height, passes=0, guide_fraction=0.0, train_passes=0, learning_rate=2e-3,
+                      train_steps=8, stream_offset=0, time_budget=0.0, keep_guide=False, samples_per_pixel=0):
         """yar_gpu_guided_render: returns (mean image, per-pixel FP64 radiance
-        sums, GuidedStats)."""
+        sums, GuidedStats).  samples_per_pixel > 0: the stratified form (the
+        training passes, then the pixel sampler at that many samples)."""
         prm = GuidedParams(int(passes), int(train_passes), float(guide_fraction), float(learning_rate),
-                           int(train_steps), int(stream_offset), float(time_budget), int(bool(keep_guide)))
+                           int(train_steps), int(stream_offset), float(time_budget), int(bool(keep_guide)),
+                           int(samples_per_pixel))
         sums = np.zeros((height, width, 3), np.float64)
         rgb = np.zeros((height, width, 3), np.float32)
         st = GuidedStats()

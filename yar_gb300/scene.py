@@ -65,7 +65,7 @@ IDENTITY = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32)
 
 class Mesh:
     def __init__(self, vertices, indices, normals=None, uvs=None, reverse_orientation=0, visibility=0,
-                 bounds=None, nodes=None):
+                 bounds=None, nodes=None, alpha_texture=0):
         self.vertices = np.ascontiguousarray(vertices, np.float32).reshape(-1, 3)
         self.indices = np.ascontiguousarray(indices, np.int32).reshape(-1, 3)
         self.normals = None if normals is None else np.ascontiguousarray(normals, np.float32).reshape(-1, 3)
@@ -74,6 +74,7 @@ class Mesh:
         self.visibility = int(visibility)
         self.bounds = np.zeros(6, np.float32) if bounds is None else np.asarray(bounds, np.float32)
         self.nodes = np.zeros((0, 2), np.uint32) if nodes is None else np.ascontiguousarray(nodes, np.uint32)
+        self.alpha_texture = int(alpha_texture)  # 0 none, else 1 + texture index (alpha test)
 
     @property
     def triangle_count(self):
@@ -188,6 +189,7 @@ class FlatScene:
             keep.append(nodes)
             d.kdtree.nodes = nodes.ctypes.data if nodes.size else None
             d.kdtree.node_count = nodes.shape[0]
+            d.alpha_texture = m.alpha_texture
             keep.append(m)
         objects = np.ascontiguousarray(self.objects)
         materials = np.ascontiguousarray(self.materials)
@@ -253,7 +255,7 @@ class FlatScene:
         parts.append(chunk(b"CONF", self.config.tobytes() + self.camera.tobytes() +
                            struct.pack("<I", int(self.other_light_count))))
         for m in self.meshes:
-            flags = (1 if m.normals is not None else 0) | (2 if m.uvs is not None else 0)
+            flags = (1 if m.normals is not None else 0) | (2 if m.uvs is not None else 0) | (4 if m.alpha_texture else 0)
             p = struct.pack("<6I", m.vertices.shape[0], m.indices.shape[0], flags, m.reverse_orientation & 0xffffffff,
                             m.visibility, m.nodes.shape[0])
             p += m.bounds.astype(np.float32).tobytes() + m.vertices.tobytes() + m.indices.tobytes()
@@ -262,6 +264,8 @@ class FlatScene:
             if m.uvs is not None:
                 p += m.uvs.tobytes()
             p += np.ascontiguousarray(m.nodes, np.uint32).tobytes()
+            if m.alpha_texture:
+                p += struct.pack("<I", m.alpha_texture)
             parts.append(chunk(b"MESH", p))
         parts.append(chunk(b"OBJS", struct.pack("<I", self.objects.shape[0]) + self.objects.tobytes()))
         parts.append(chunk(b"SKDT", self.scene_bounds.astype(np.float32).tobytes() +
@@ -327,7 +331,9 @@ class FlatScene:
                     uvs = np.frombuffer(p[q:q + 8 * vc], np.float32).reshape(-1, 2).copy()
                     q += 8 * vc
                 nodes = np.frombuffer(p[q:q + 8 * nc], np.uint32).reshape(-1, 2).copy()
-                s.meshes.append(Mesh(v, idx, normals, uvs, np.int32(np.uint32(rev)), vis, bounds, nodes))
+                q += 8 * nc
+                alpha = struct.unpack_from("<I", p, q)[0] if flags & 4 else 0
+                s.meshes.append(Mesh(v, idx, normals, uvs, np.int32(np.uint32(rev)), vis, bounds, nodes, alpha))
             elif tag == b"OBJS":
                 n = struct.unpack_from("<I", p, 0)[0]
                 s.objects = np.frombuffer(p[4:4 + n * OBJECT_DTYPE.itemsize], OBJECT_DTYPE).copy()

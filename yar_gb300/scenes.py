@@ -181,7 +181,8 @@ def _box(center, size, angle_deg):
 
 def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0, box_materials=None,
                  upper_light=None, light_sources=(), mesh_lights=(), sphere_lights=(), named_materials=(),
-                 integrator="path", light_samples=1, textures=(), wall_textures=None):
+                 integrator="path", light_samples=1, textures=(), wall_textures=None, pixel_filter='"box"',
+                 extra_shapes=()):
     """pbrt-v3 text of the seeded Cornell box (34 triangles + a quad light).
 
     box_materials: None for matte boxes, or two pbrt material statements for
@@ -230,7 +231,7 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
         % (width, height),
         'Sampler "stratified" "integer xsamples" [%d] "integer ysamples" [%d]' % (k, k),
         'Integrator "%s" "integer maxdepth" [%d]' % (integrator, maxdepth),
-        'PixelFilter "box"',
+        'PixelFilter %s' % pixel_filter,
         "WorldBegin",
     ] + list(textures) + list(named_materials) + list(light_sources)
     wall_textures = wall_textures or {}
@@ -265,6 +266,7 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
                 '  AreaLightSource "diffuse" "rgb L" [%s]' % fmt(radiance),
                 shape,
                 "AttributeEnd"]
+    out += list(extra_shapes)
     if upper_light is not None:
         uh, uy, ul = upper_light
         v, i = _quad((-uh, uy, -uh), (uh, uy, -uh), (uh, uy, uh), (-uh, uy, uh))
@@ -331,6 +333,24 @@ def texture_image(width=48, height=40, seed=3):
     checks = (((x * 8) // width + (y * 8) // height) % 2).astype(np.float32)
     base = np.stack([0.15 + 0.7 * checks, 0.6 - 0.4 * checks, 0.3 + 0.2 * (x / width)], axis=-1)
     return (base * (0.85 + 0.3 * rng.random((height, width, 1)))).astype(np.float32)
+
+
+def cutout_image(size=16, cells=4):
+    """An alpha texture for the alpha test: cells x cells checks of 0 and 1
+    (all three channels), size x size texels."""
+    y, x = np.mgrid[0:size, 0:size]
+    on = (((x * cells) // size + (y * cells) // size) % 2).astype(np.float32)
+    return np.repeat(on[:, :, None], 3, axis=2)
+
+
+def cutout_fence(texture="cutout", material='Material "matte" "rgb Kd" [0.8 0.7 0.3]'):
+    """pbrt statements of a vertical quad across the room, between the camera
+    and the boxes, cut out by an alpha texture (uvs repeat it twice)."""
+    v = [-0.8, 0.05, 0.3, 0.8, 0.05, 0.3, 0.8, 1.5, 0.3, -0.8, 1.5, 0.3]
+    return ("AttributeBegin", "  " + material,
+            '  Shape "trianglemesh" "integer indices" [0 1 2 0 2 3] "point P" [%s] "float uv" [0 0 2 0 2 2 0 2] '
+            '"texture alpha" "%s"' % (" ".join("%g" % a for a in v), texture),
+            "AttributeEnd")
 
 
 def texture_statements(filename, name="checks", uscale=1.0, vscale=1.0):
