@@ -544,7 +544,7 @@ def render_bench(kind, with_cpu=True, reps=3):
            "gpu_mrays_per_s": round((best.rays_closest + best.rays_any) / best.seconds / 1e6, 2),
            "rays_closest": int(best.rays_closest), "rays_any": int(best.rays_any),
            "kernel_launches": int(best.kernel_launches), "image_mean": float(img.mean()),
-           "traversal_kernels": {k: [["-", "p64", "p128", "per_ray"][c] for c in v]
+           "traversal_kernels": {k: [["-", "p64", "p128", "per_ray", "per_ray_vote"][c] for c in v]
                                  for k, v in kernels.items() if k != "cast"}}
     if not with_cpu:
         return out
@@ -578,7 +578,10 @@ def render_bench(kind, with_cpu=True, reps=3):
     return out
 
 
-GUIDE = dict(guide_fraction=0.7, train_passes=32, train_steps=32, learning_rate=5e-3)
+GUIDE = dict(guide_fraction=0.7, train_passes=32, train_steps=32, learning_rate=5e-3)  # one-sample passes
+# stratified form: settings from a sweep on the room (guide fraction 0.5-0.8, guided bounces 1-3 or all,
+# 4-16 training passes, 32-128 Adam steps, learning rate 3e-3-1e-2)
+GUIDE_STRATIFIED = dict(guide_fraction=0.6, train_passes=8, train_steps=64, learning_rate=5e-3, guide_bounces=2)
 
 
 def guided_bench(plain_spp_side=32, offsets=(2, 3, 4), with_cpu=True):
@@ -625,15 +628,16 @@ def guided_bench(plain_spp_side=32, offsets=(2, 3, 4), with_cpu=True):
     img_p, _, st_p = ctx.guided_render(w, h, passes=plain_spp_side ** 2, stream_offset=1)
     r_r, r_p = rmse(img_r), rmse(img_p)
     target, t_target = min((r_r, st_r.seconds), (r_p, st_p.seconds))
-    ctx.guided_render(w, h, samples_per_pixel=16, stream_offset=4092, **GUIDE)  # warm-up of the stratified form
+    ctx.guided_render(w, h, samples_per_pixel=16, stream_offset=4092, **GUIDE_STRATIFIED)  # warm-up of the stratified form
     runs = []
     for off in offsets:
         side = 16
-        img_g, _, st_g = ctx.guided_render(w, h, samples_per_pixel=side * side, stream_offset=off, **GUIDE)
+        img_g, _, st_g = ctx.guided_render(w, h, samples_per_pixel=side * side, stream_offset=off, **GUIDE_STRATIFIED)
         r_g = rmse(img_g)
         side = max(1, int(np.ceil(side * r_g / target)))  # RMSE ~ 1 / sqrt(spp)
         for _ in range(8):
-            img_g, _, st_g = ctx.guided_render(w, h, samples_per_pixel=side * side, stream_offset=off, **GUIDE)
+            img_g, _, st_g = ctx.guided_render(w, h, samples_per_pixel=side * side, stream_offset=off,
+                                               **GUIDE_STRATIFIED)
             r_g = rmse(img_g)
             if r_g <= target:
                 break
@@ -656,7 +660,7 @@ def guided_bench(plain_spp_side=32, offsets=(2, 3, 4), with_cpu=True):
                          "mrays_per_s": round(st_p.rays / st_p.seconds / 1e6, 1)},
         "target": {"rmse": target, "seconds": round(t_target, 3),
                    "form": "plain_render" if r_r <= r_p else "plain_passes"},
-        "guided": {"runs": runs, **GUIDE},
+        "guided": {"runs": runs, **GUIDE_STRATIFIED},
         "time_to_plain_rmse": round(statistics.median(times) / t_target, 4) if len(times) == len(runs) else None,
     }
     if with_cpu:
@@ -744,7 +748,8 @@ def batch_bench(count=64, sequential=True):
         "completion_p99_s": round(pct(0.99), 4),
         "autotuner": {"branches": int(st.branches), "chunk_paths": int(st.chunk_paths),
                       "traversal_kernels": {k: sum(1 for x in sst if tuple(x.traversal_kernel) == v)
-                                            for k, v in (("p64/p64", (1, 1)), ("per_ray/per_ray", (3, 3)))}},
+                                            for k, v in (("p64/p64", (1, 1)), ("per_ray/per_ray", (3, 3)),
+                                                         ("per_ray_vote/per_ray_vote", (4, 4)))}},
         "host_seconds": {"generate_and_build": round(gen, 2), "upload": round(st.upload_seconds, 2),
                          "tune": round(st.tune_seconds, 2), "capture": round(st.capture_seconds, 2)},
         "image_mean": float(np.mean([i.mean() for i in imgs])),

@@ -345,6 +345,7 @@ typedef struct yar_gpu_options {
 #define YAR_TRAVERSAL_PERSISTENT_64 1
 #define YAR_TRAVERSAL_PERSISTENT_128 2
 #define YAR_TRAVERSAL_PER_RAY 3
+#define YAR_TRAVERSAL_PER_RAY_VOTE 4  /* one ray per thread, the warp runs one traversal mode per iteration */
 
 /* The traversal kernels chosen so far on the uploaded scene (YAR_TRAVERSAL_*,
  * 0 = not chosen yet): cast[0] closest-hit and cast[1] any-hit C-ABI casts;
@@ -487,6 +488,10 @@ typedef struct yar_guided_params {
      * continuations drawn from the trained proposal; `passes` and
      * `time_budget` are not used, radiance_sum receives image x spp. */
     uint32_t samples_per_pixel;
+    /* stratified form: the proposal guides the continuations of the first
+     * guide_bounces vertices of each path (0: every vertex); deeper vertices
+     * sample the BSDF alone */
+    uint32_t guide_bounces;
 } yar_guided_params;
 
 typedef struct yar_guided_stats {

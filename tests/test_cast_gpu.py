@@ -198,7 +198,7 @@ def test_batch_capacity_error():
 
 
 @pytest.mark.parametrize("kernel", [native.TRAVERSAL_PERSISTENT_64, native.TRAVERSAL_PERSISTENT_128,
-                                    native.TRAVERSAL_PER_RAY])
+                                    native.TRAVERSAL_PER_RAY, native.TRAVERSAL_PER_RAY_VOTE])
 def test_every_traversal_kernel_matches_oracle(medium_scene, kernel):
     if not pytest.importorskip("torch").cuda.is_available():
         pytest.skip("no CUDA device")

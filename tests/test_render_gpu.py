@@ -262,7 +262,7 @@ def test_render_identical_for_every_traversal_kernel():
     s.config["x_pixel_sample_count"], s.config["y_pixel_sample_count"] = 8, 8  # 262144 paths: tuning runs
     results = []
     for kernel in (native.TRAVERSAL_AUTO, native.TRAVERSAL_PERSISTENT_64, native.TRAVERSAL_PERSISTENT_128,
-                   native.TRAVERSAL_PER_RAY):
+                   native.TRAVERSAL_PER_RAY, native.TRAVERSAL_PER_RAY_VOTE):
         ctx = native.Context(0, traversal_kernel=kernel)
         try:
             ctx.upload_scene(s)

@@ -42,7 +42,7 @@ def main(argv=None):
         if name == "render":
             q.add_argument("--spp", type=int, default=0, help="samples per pixel (rounded up to k*k)")
             q.add_argument("--seedoffset", type=int, default=None)
-            q.add_argument("--traversal", choices=["auto", "p64", "p128", "per-ray"], default="auto")
+            q.add_argument("--traversal", choices=["auto", "p64", "p128", "per-ray", "per-ray-vote"], default="auto")
         else:
             q.add_argument("--passes", type=int, default=256)
             q.add_argument("--guide-fraction", type=float, default=0.7)
@@ -64,7 +64,8 @@ def main(argv=None):
             s.config["y_pixel_sample_count"], s.config["max_light_bounces"]))
         return 0
     kernels = {"auto": native.TRAVERSAL_AUTO, "p64": native.TRAVERSAL_PERSISTENT_64,
-               "p128": native.TRAVERSAL_PERSISTENT_128, "per-ray": native.TRAVERSAL_PER_RAY}
+               "p128": native.TRAVERSAL_PERSISTENT_128, "per-ray": native.TRAVERSAL_PER_RAY,
+               "per-ray-vote": native.TRAVERSAL_PER_RAY_VOTE}
     ctx = native.Context(a.device, traversal_kernel=kernels[getattr(a, "traversal", "auto")])
     if a.cmd == "render":
         if a.spp:

@@ -14,7 +14,7 @@
 // film is resolved: per-scene completion times come from the device.
 //
 // Autotuner: before capture, (1) each scene's traversal kernel is chosen by
-// timing the three kernels on 2^16 random rays in its box (tune_cast), and
+// timing the traversal kernels on 2^16 random rays in its box (tune_cast), and
 // (2) the branch count and the chunk capacity (paths in flight per branch)
 // are chosen by capturing and timing the whole batch at one sample per pixel
 // for each candidate; the full-sample graph is then captured with the winner.

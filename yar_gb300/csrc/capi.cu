@@ -122,7 +122,8 @@ extern "C" int yar_gpu_create(yar_gpu_ctx** out, const yar_gpu_options* options)
     ctx->device = options ? options->device : 0;
     ctx->staging_capacity = (options && options->max_batch_rays) ? options->max_batch_rays : (16u << 20);
     if (options && options->traversal_kernel != YAR_TRAVERSAL_AUTO) {
-        if (options->traversal_kernel < YAR_TRAVERSAL_PERSISTENT_64 || options->traversal_kernel > YAR_TRAVERSAL_PER_RAY) {
+        if (options->traversal_kernel < YAR_TRAVERSAL_PERSISTENT_64 ||
+            options->traversal_kernel > YAR_TRAVERSAL_PER_RAY_VOTE) {
             delete ctx;
             return YAR_ERR_INVALID;
         }

@@ -19,6 +19,9 @@ namespace yar {
 
 namespace {
 
+#ifndef YAR_CAST_NODES_PER_STEP
+#define YAR_CAST_NODES_PER_STEP 1
+#endif
 constexpr int kCastBlock = 128;
 constexpr uint32_t kBatch = 128;  // rays a warp takes per atomic
 
@@ -128,6 +131,52 @@ __global__ void __launch_bounds__(kCastBlock) cast_per_ray(Device_Scene s, Cast_
     }
 }
 
+// One ray per thread as cast_per_ray, but the warp votes each iteration and
+// runs one mode for all its lanes, as the persistent kernel does (no hand-out
+// of new rays: a lane whose ray is done waits for its warp).  Warps iterate
+// together (the grid-stride base is a multiple of 32), so every vote sees
+// all 32 lanes.
+template <bool ANY>
+__global__ void __launch_bounds__(kCastBlock) cast_per_ray_vote(Device_Scene s, Cast_Args a) {
+    const unsigned full = 0xffffffffu;
+    const uint32_t n = a.count ? *a.count : a.n;
+    const uint32_t lane = threadIdx.x & 31u;
+    for (uint32_t base = (blockIdx.x * blockDim.x + threadIdx.x) - lane; base < n; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + lane;
+        Traversal<ANY> tr;
+        Local_Stack stack;
+        bool have = false;
+        if (i < n) {
+            const float4 r0 = __ldg(a.rays + 2 * (size_t)i);
+            const float4 r1 = __ldg(a.rays + 2 * (size_t)i + 1);
+            tr.begin(s, i, make_float3(r0.x, r0.y, r0.z), make_float3(r1.x, r1.y, r1.z), r0.w);
+            if (tr.mode() == kDone)
+                write_result<ANY>(tr, a.perm ? __ldg(a.perm + i) : i, a);
+            else
+                have = true;
+        }
+        for (;;) {
+            const int m = have ? tr.mode() : -1;
+            const unsigned md = __ballot_sync(full, m == kDescend);
+            const unsigned mm = __ballot_sync(full, m == kMeshLeaf);
+            const unsigned ms = __ballot_sync(full, m == kSceneLeaf);
+            if (!(md | mm | ms)) break;
+            const int nd = __popc(md), nm = __popc(mm), ns = __popc(ms);
+            if (nd >= nm && nd >= ns) {
+                if (m == kDescend) tr.template step_descend<YAR_CAST_NODES_PER_STEP>(s, a.rays, stack);
+            } else if (nm >= ns) {
+                if (m == kMeshLeaf) tr.step_mesh_leaf(s, a.rays, stack);
+            } else {
+                if (m == kSceneLeaf) tr.step_scene_leaf(s, a.rays, stack);
+            }
+            if (have && tr.mode() == kDone) {
+                write_result<ANY>(tr, a.perm ? __ldg(a.perm + i) : i, a);
+                have = false;
+            }
+        }
+    }
+}
+
 // Persistent launch shape, measured on GB300 with the 2.42M-triangle ray-cast
 // workload (16M + 16M incoherent rays).  With one mode per warp iteration,
 // one node fetch per descent step: closest hit 19.8 ms against 21.3 ms at two
@@ -141,9 +190,6 @@ __global__ void __launch_bounds__(kCastBlock) cast_per_ray(Device_Scene s, Cast_
 // (direction signs in the flags word, 1/d shared by clipping and the
 // watertight setup): 18.5 and 10.7 ms; a 4-, 8- or 16-entry shared-memory
 // stack with local overflow was slower (18.6-19.2 and 11.4-13.6 ms).
-#ifndef YAR_CAST_NODES_PER_STEP
-#define YAR_CAST_NODES_PER_STEP 1
-#endif
 constexpr int kWhileWhile = YAR_CAST_NODES_PER_STEP;
 #ifndef YAR_CAST_SHARED_STACK
 #define YAR_CAST_SHARED_STACK 0
@@ -179,10 +225,13 @@ int resident_grid(Kernel kernel, std::atomic<int>* cache) {
 
 template <bool ANY>
 cudaError_t launch(const Device_Scene& s, const Cast_Args& a, int kernel, cudaStream_t stream) {
-    if (kernel == kCastPerRay) {
+    if (kernel == kCastPerRay || kernel == kCastPerRayVote) {
         const uint32_t bound = a.count ? a.n_max : a.n;
         if (bound == 0) return cudaSuccess;
-        cast_per_ray<ANY><<<(bound + kCastBlock - 1) / kCastBlock, kCastBlock, 0, stream>>>(s, a);
+        if (kernel == kCastPerRay)
+            cast_per_ray<ANY><<<(bound + kCastBlock - 1) / kCastBlock, kCastBlock, 0, stream>>>(s, a);
+        else
+            cast_per_ray_vote<ANY><<<(bound + kCastBlock - 1) / kCastBlock, kCastBlock, 0, stream>>>(s, a);
         return cudaGetLastError();
     }
     cudaError_t e = cudaMemsetAsync(a.next_ray, 0, sizeof(uint32_t), stream);

@@ -136,7 +136,13 @@ struct Cast_Args {
 // warps capped at 128 registers (4 blocks per SM), one ray per thread.  All
 // give identical results; which is fastest depends on the scene and the rays,
 // so it is chosen per scene by timing (tune_cast).
-enum Cast_Kernel { kCastPersistent64 = 0, kCastPersistent128 = 1, kCastPerRay = 2, kCastKernelCount = 3 };
+enum Cast_Kernel {
+    kCastPersistent64 = 0,
+    kCastPersistent128 = 1,
+    kCastPerRay = 2,
+    kCastPerRayVote = 3,  // one ray per thread, one mode per warp iteration
+    kCastKernelCount = 4
+};
 cudaError_t launch_extend(const Device_Scene& s, const Cast_Args& a, int kernel, cudaStream_t stream);
 cudaError_t launch_shadow(const Device_Scene& s, const Cast_Args& a, int kernel, cudaStream_t stream);
 // Runs the batch once untimed and once with each kernel (event-timed on
@@ -180,6 +186,7 @@ struct Guide_Render_Hook {
     const float* lobes = nullptr;
     const float4* queries = nullptr;
     float alpha = 0.f;
+    int max_bounce = 0;        // guide the continuations of bounces below this one (0: every bounce)
     uint64_t chunk_paths = 0;  // paths in flight per chunk
     cudaError_t (*before_shade)(void* user, const float4* rays, const float4* hit4, const uint2* hit2,
                                 uint32_t count, cudaStream_t st) = nullptr;

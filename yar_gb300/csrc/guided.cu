@@ -335,6 +335,7 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
         Guide_Hook_State hs{ctx, S, nullptr, nullptr, {box[0], box[1], box[2], box[3], box[4], box[5]}};
         Guide_Render_Hook hook;
         hook.alpha = guided ? gp->guide_fraction : 0.f;
+        hook.max_bounce = (int)std::min<uint32_t>(gp->guide_bounces, 1u << 20);
         hook.chunk_paths = std::max<uint64_t>(kGuidedChunkPaths, (uint64_t)spp_side * spp_side);
         if (guided) {
             rc = device_alloc(ctx, qbuf, hook.chunk_paths * 3 * sizeof(float4));

@@ -482,7 +482,7 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
             e = trace_extend(ctx, q, cur, count, bounce, st);
             if (e != cudaSuccess) break;
             cudaMemsetAsync(q.counters, 0, 3 * sizeof(uint32_t), st);
-            if (guide && guide->before_shade) {
+            if (guide && guide->before_shade && (guide->max_bounce <= 0 || bounce < guide->max_bounce)) {
                 e = guide->before_shade(guide->user, q.ext_rays[cur], q.ext_hit4, q.ext_hit2, count, st);
                 if (e != cudaSuccess) break;
                 Guide_Shade gs;

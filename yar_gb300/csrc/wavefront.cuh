@@ -1406,8 +1406,10 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                             dm.rng_used = true;
                             float pdf_b = 0.f;
                             if (u_sel < g.alpha) {
-                                const float u0 = pcg_float(dm.rng), u1 = pcg_float(dm.rng), u2 = pcg_float(dm.rng);
-                                wi = mixture_sample(lob, u0, u1, u2);
+                                // the continuation's own stratified sample dimensions (the ones
+                                // the BSDF branch takes): guided directions stay stratified
+                                // over a pixel's samples
+                                wi = mixture_sample(lob, u_scatter_next, un.x, un.y);
                                 const float ndw = dot(sc.n, wi);
                                 const bool possible = (ndw > 0.f && f.reflection) || (ndw < 0.f && f.transmission);
                                 fv = possible ? bsdf_evaluate<FULL>(f, sc.wo, wi) : col(0.f, 0.f, 0.f);
