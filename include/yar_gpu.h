@@ -167,10 +167,24 @@ typedef struct yar_material_desc {
     float mix_amount[3];        /* mix */
     /* Image textures (RGB_Parameter in value mode with a texture leaf,
        src/lib/material_parameter.h): the texture of `reflectance` and its uv
-       scale.  0: the constant above; k > 0: yar_flat_scene::textures[k - 1]. */
+       scale.  0: the constant above; k > 0: yar_flat_scene::textures[k - 1].
+       `reflectance` is the diffuse reflectance of diffuse, plastic and coated
+       diffuse materials, Kr of glass, the reflectance of diffuse transmission. */
     uint32_t reflectance_texture;
     float reflectance_uv_scale[2];
     uint32_t other_textured_parameters;  /* parameters given by textures the library does not evaluate */
+    /* the texture of `transmittance` (Kt of glass, the transmittance of
+       diffuse transmission), as reflectance_texture */
+    uint32_t transmittance_texture;
+    float transmittance_uv_scale[2];
+    /* Bump map (Float_Parameter, applied by Shading_Context::apply_bump_map,
+       src/ref/shading_context.cpp:419-462): 0 none, 1 the constant height
+       bump_height, 2 the luminance of texture bump_texture (1 + index) at uv x
+       bump_uv_scale. */
+    uint32_t bump;
+    float bump_height;
+    uint32_t bump_texture;
+    float bump_uv_scale[2];
 } yar_material_desc;
 
 /* Image_Texture (src/ref/image_texture.h) as the reference builds it from the

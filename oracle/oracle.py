@@ -226,14 +226,18 @@ def ref_bench_cast(flat, rays, shadow, warmup=0, steps=1, threads=0, build=False
         return _ref(*args)
 
 
-def ref_render_flat(flat, spp=0, threads=0):
-    """The reference renderer on a flat scene (harness render-yfs)."""
+def ref_render_flat(flat, spp=0, threads=0, textures_from=None):
+    """The reference renderer on a flat scene (harness render-yfs).  A textured
+    flat scene names the pbrt scene it was flattened from (`textures_from`),
+    whose texture files the reference loads."""
     with tempfile.TemporaryDirectory() as d:
         s, out = os.path.join(d, "s.yfs"), os.path.join(d, "img.bin")
         flat.write(s)
         args = ["render-yfs", s, out, "--threads=%d" % (threads or os.cpu_count() or 1)]
         if spp:
             args.append("--spp=%d" % spp)
+        if textures_from:
+            args.append("--textures-from=%s" % textures_from)
         info = _ref(*args)
         raw = open(out, "rb").read()
     w, h = np.frombuffer(raw[:8], np.uint32)

@@ -51,8 +51,35 @@ bool constant_float(const Parameter& p, float* out) {
     return true;
 }
 
-void note_bump(const Parameter& bump_map) {
-    if (bump_map.eval_mode != EvaluationMode::none) g_textured_parameters++;
+// An RGB parameter: its constant, or (value mode, texture leaf) its texture
+// and uv scale; any other form is counted as not evaluated.
+void constant_or_texture(const RGB_Parameter& p, float out[3], uint32_t* texture, float uv_scale[2]) {
+    if (p.eval_mode == EvaluationMode::value && !p.value.is_constant) {
+        *texture = (uint32_t)p.value.texture.texture_index + 1u;
+        uv_scale[0] = p.value.texture.u_scale;
+        uv_scale[1] = p.value.texture.v_scale;
+        return;
+    }
+    constant_rgb(p, out);
+}
+
+// The bump map of a material (Shading_Context::apply_bump_map runs in create_bsdf
+// and, for the delta-capable materials, in check_for_delta_scattering_event).
+void flatten_bump(const Float_Parameter& bump_map, yar_material_desc& d) {
+    if (bump_map.eval_mode == EvaluationMode::none) return;
+    if (bump_map.eval_mode == EvaluationMode::value) {
+        if (bump_map.value.is_constant) {
+            d.bump = 1;
+            d.bump_height = bump_map.value.constant.r;
+        } else {
+            d.bump = 2;
+            d.bump_texture = (uint32_t)bump_map.value.texture.texture_index + 1u;
+            d.bump_uv_scale[0] = bump_map.value.texture.u_scale;
+            d.bump_uv_scale[1] = bump_map.value.texture.v_scale;
+        }
+        return;
+    }
+    g_textured_parameters++;
 }
 
 void push_material(yfs::Scene& out, yar_material_desc d) {
@@ -90,21 +117,15 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
     std::vector<int> diffuse_index, metal_index, glass_index;
     for (const Diffuse_Material& m : ctx.materials.diffuse) {
         yar_material_desc d{};
-        note_bump(m.bump_map);
+        flatten_bump(m.bump_map, d);
         d.type = YAR_MATERIAL_DIFFUSE;
-        if (m.reflectance.eval_mode == EvaluationMode::value && !m.reflectance.value.is_constant) {
-            d.reflectance_texture = (uint32_t)m.reflectance.value.texture.texture_index + 1u;
-            d.reflectance_uv_scale[0] = m.reflectance.value.texture.u_scale;
-            d.reflectance_uv_scale[1] = m.reflectance.value.texture.v_scale;
-        } else {
-            constant_rgb(m.reflectance, d.reflectance);
-        }
+        constant_or_texture(m.reflectance, d.reflectance, &d.reflectance_texture, d.reflectance_uv_scale);
         diffuse_index.push_back((int)out.materials.size());
         push_material(out, d);
     }
     for (const Metal_Material& m : ctx.materials.metal) {
         yar_material_desc d{};
-        note_bump(m.bump_map);
+        flatten_bump(m.bump_map, d);
         d.type = YAR_MATERIAL_METAL;
         constant_float(m.u_roughness, &d.u_roughness);
         constant_float(m.v_roughness, &d.v_roughness);
@@ -117,10 +138,10 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
     }
     for (const Glass_Material& m : ctx.materials.glass) {
         yar_material_desc d{};
-        note_bump(m.bump_map);
+        flatten_bump(m.bump_map, d);
         d.type = YAR_MATERIAL_GLASS;
-        constant_rgb(m.reflectance, d.reflectance);
-        constant_rgb(m.transmittance, d.transmittance);
+        constant_or_texture(m.reflectance, d.reflectance, &d.reflectance_texture, d.reflectance_uv_scale);
+        constant_or_texture(m.transmittance, d.transmittance, &d.transmittance_texture, d.transmittance_uv_scale);
         constant_float(m.index_of_refraction, &d.index_of_refraction);
         constant_float(m.roughness, &d.u_roughness);
         d.v_roughness = d.u_roughness;
@@ -132,9 +153,9 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
     std::vector<int> plastic_index, coated_index;
     for (const Plastic_Material& m : ctx.materials.plastic) {
         yar_material_desc d{};
-        note_bump(m.bump_map);
+        flatten_bump(m.bump_map, d);
         d.type = YAR_MATERIAL_PLASTIC;
-        constant_rgb(m.diffuse_reflectance, d.reflectance);
+        constant_or_texture(m.diffuse_reflectance, d.reflectance, &d.reflectance_texture, d.reflectance_uv_scale);
         float r0 = 0.f;
         constant_float(m.r0, &r0);
         d.transmittance[0] = d.transmittance[1] = d.transmittance[2] = r0;
@@ -146,9 +167,9 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
     }
     for (const Coated_Diffuse_Material& m : ctx.materials.coated_diffuse) {
         yar_material_desc d{};
-        note_bump(m.bump_map);
+        flatten_bump(m.bump_map, d);
         d.type = YAR_MATERIAL_COATED_DIFFUSE;
-        constant_rgb(m.diffuse_reflectance, d.reflectance);
+        constant_or_texture(m.diffuse_reflectance, d.reflectance, &d.reflectance_texture, d.reflectance_uv_scale);
         constant_rgb(m.r0, d.transmittance);
         constant_float(m.u_roughness, &d.u_roughness);
         constant_float(m.v_roughness, &d.v_roughness);
@@ -159,7 +180,7 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
     std::vector<int> reflector_index, refractor_index;
     for (const Perfect_Reflector_Material& m : ctx.materials.perfect_reflector) {
         yar_material_desc d{};
-        note_bump(m.bump_map);
+        flatten_bump(m.bump_map, d);  // applied in check_for_delta_scattering_event
         d.type = YAR_MATERIAL_PERFECT_REFLECTOR;
         constant_rgb(m.reflectance, d.reflectance);
         reflector_index.push_back((int)out.materials.size());
@@ -167,7 +188,7 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
     }
     for (const Perfect_Refractor_Material& m : ctx.materials.perfect_refractor) {
         yar_material_desc d{};
-        note_bump(m.bump_map);
+        flatten_bump(m.bump_map, d);  // applied in check_for_delta_scattering_event
         d.type = YAR_MATERIAL_PERFECT_REFRACTOR;
         constant_float(m.index_of_refraction, &d.index_of_refraction);
         refractor_index.push_back((int)out.materials.size());
@@ -177,17 +198,17 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
     std::vector<int> transmission_index, translucent_index, uber_index, mix_index;
     for (const Diffuse_Transmission_Material& m : ctx.materials.diffuse_transmission) {
         yar_material_desc d{};
-        note_bump(m.bump_map);
+        flatten_bump(m.bump_map, d);
         d.type = YAR_MATERIAL_DIFFUSE_TRANSMISSION;
-        constant_rgb(m.reflectance, d.reflectance);
-        constant_rgb(m.transmittance, d.transmittance);
+        constant_or_texture(m.reflectance, d.reflectance, &d.reflectance_texture, d.reflectance_uv_scale);
+        constant_or_texture(m.transmittance, d.transmittance, &d.transmittance_texture, d.transmittance_uv_scale);
         constant_rgb(m.scale, d.diffuse);
         transmission_index.push_back((int)out.materials.size());
         push_material(out, d);
     }
     for (const Pbrt3_Translucent_Material& m : ctx.materials.pbrt3_translucent) {
         yar_material_desc d{};
-        note_bump(m.bump_map);
+        flatten_bump(m.bump_map, d);
         d.type = YAR_MATERIAL_PBRT3_TRANSLUCENT;
         constant_rgb(m.reflectance, d.reflectance);
         constant_rgb(m.transmittance, d.transmittance);
@@ -201,7 +222,7 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
     // pbrt3 uber: reflectance = Kd, transmittance = Kt
     for (const Pbrt3_Uber_Material& m : ctx.materials.pbrt3_uber) {
         yar_material_desc d{};
-        note_bump(m.bump_map);
+        flatten_bump(m.bump_map, d);
         d.type = YAR_MATERIAL_PBRT3_UBER;
         constant_rgb(m.diffuse_reflectance, d.reflectance);
         constant_rgb(m.specular_reflectance, d.specular);
@@ -332,7 +353,8 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
     // one: every texture of the scene context (indices stay the reference's),
     // each with its mip chain
     bool textured = false;
-    for (const yar_material_desc& d : out.materials) textured = textured || d.reflectance_texture != 0;
+    for (const yar_material_desc& d : out.materials)
+        textured = textured || d.reflectance_texture != 0 || d.transmittance_texture != 0 || d.bump_texture != 0;
     for (const yfs::Mesh& fm : out.meshes) textured = textured || fm.alpha_texture != 0;
     for (size_t ti = 0; textured && ti < ctx.textures.size(); ti++) {
         const std::vector<Image>& mips = ctx.textures[ti].get_mips();

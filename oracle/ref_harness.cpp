@@ -74,6 +74,7 @@ struct Args {
     std::string input_file;
     std::string cache_dir;
     std::string checkpoint_dir;
+    std::string textures_from;
 };
 
 Args parse(int argc, char** argv) {
@@ -93,6 +94,7 @@ Args parse(int argc, char** argv) {
         else if (s.rfind("--variance=", 0) == 0) a.variance = (float)atof(s.c_str() + 11);
         else if (s.rfind("--input=", 0) == 0) a.input_file = s.substr(8);
         else if (s.rfind("--cache-dir=", 0) == 0) a.cache_dir = s.substr(12);
+        else if (s.rfind("--textures-from=", 0) == 0) a.textures_from = s.substr(16);
         else a.pos.push_back(s);
     }
     if (a.threads <= 0) a.threads = std::max(1u, std::thread::hardware_concurrency());
@@ -441,11 +443,41 @@ int cmd_bench_cast(const Args& a) {
 // previous hit point, axis-aligned directions with probability 1/32 per axis.
 // Checks kd-tree t == brute-force t like the reference test and writes
 // f32 origin[3], f32 direction[3], f32 t, u32 prim per ray.
-// render-yfs <in.yfs> <out.img> [--threads=T] [--spp=N]
-// A flat scene (meshes, constant materials, rectangular lights, camera,
-// config) rebuilt as a reference Scene, initialised with init_scene_context
-// (reference kd-tree builder) and rendered with render_scene.  Used for
-// scenes generated without a pbrt file (the large wavefront workload).
+// An RGB material parameter of a flat material: its texture slot (1-based,
+// with the uv scale) or its constant.
+static RGB_Parameter flat_rgb(const float c[3], uint32_t texture, const float uv_scale[2]) {
+    RGB_Parameter p;
+    if (texture) {
+        set_texture_parameter(p, (int)texture - 1);
+        p.value.texture.u_scale = uv_scale[0];
+        p.value.texture.v_scale = uv_scale[1];
+    } else {
+        set_constant_parameter(p, ColorRGB(c));
+    }
+    return p;
+}
+
+// The bump map of a flat material: none, a constant height or a texture.
+static Float_Parameter flat_bump(const yar_material_desc& d) {
+    Float_Parameter p;
+    if (d.bump == 1) {
+        set_constant_parameter(p, d.bump_height);
+    } else if (d.bump == 2) {
+        set_texture_parameter(p, (int)d.bump_texture - 1);
+        p.value.texture.u_scale = d.bump_uv_scale[0];
+        p.value.texture.v_scale = d.bump_uv_scale[1];
+    }
+    return p;
+}
+
+// render-yfs <in.yfs> <out.img> [--threads=T] [--spp=N] [--textures-from=<scene.pbrt>]
+// A flat scene (meshes, materials, lights, camera, config) rebuilt as a
+// reference Scene, initialised with init_scene_context (reference kd-tree
+// builder) and rendered with render_scene.  Used for scenes generated
+// without a pbrt file (the large wavefront workload) and for flat scenes
+// edited after flattening a pbrt scene: a textured one names that pbrt scene,
+// whose texture files the reference loads (its texture indices are the flat
+// scene's, as flattening keeps them).
 int cmd_render_yfs(const Args& a) {
     if (a.pos.size() < 2) return 2;
     yfs::Scene fs_scene;
@@ -455,9 +487,18 @@ int cmd_render_yfs(const Args& a) {
         fprintf(stderr, "render-yfs: environment lights are rendered from their pbrt scene only\n");
         return 1;
     }
+    Scene texture_source;
     if (!fs_scene.textures.empty()) {
-        fprintf(stderr, "render-yfs: textured scenes are rendered from their pbrt scene only\n");
-        return 1;
+        if (a.textures_from.empty()) {
+            fprintf(stderr, "render-yfs: a textured scene needs --textures-from=<the pbrt scene it came from>\n");
+            return 1;
+        }
+        texture_source = load_scene(a.textures_from);
+        if (texture_source.texture_descriptors.size() != fs_scene.textures.size()) {
+            fprintf(stderr, "render-yfs: %zu textures in the pbrt scene, %zu in the flat scene\n",
+                    texture_source.texture_descriptors.size(), fs_scene.textures.size());
+            return 1;
+        }
     }
     if (fs_scene.other_light_count) {
         fprintf(stderr, "only rectangular, point, spot, directional, triangle-mesh and sphere lights are supported\n");
@@ -466,6 +507,10 @@ int cmd_render_yfs(const Args& a) {
     Scene scene;
     scene.type = fs_scene.config.pbrt3_scene ? Scene_Type::pbrt : Scene_Type::obj;
     scene.path = a.pos[0];
+    if (!fs_scene.textures.empty()) {
+        scene.path = a.textures_from;  // texture file names are relative to it
+        scene.texture_descriptors = texture_source.texture_descriptors;
+    }
     for (const yfs::Mesh& fm : fs_scene.meshes) {
         Triangle_Mesh m;
         m.vertices.resize(fm.vertices.size() / 3);
@@ -477,13 +522,15 @@ int cmd_render_yfs(const Args& a) {
         m.indices = fm.indices;
         m.reverse_geometric_normal_orientation = fm.reverse_orientation != 0;
         m.visibility = (Visibility)fm.visibility;
+        m.alpha_texture_index = fm.alpha_texture ? (int)fm.alpha_texture - 1 : -1;
         scene.geometries.triangle_meshes.push_back(std::move(m));
     }
     std::vector<Material_Handle> handles;
     for (const yar_material_desc& d : fs_scene.materials) {
         if (d.type == YAR_MATERIAL_DIFFUSE) {
             Diffuse_Material m;
-            set_constant_parameter(m.reflectance, ColorRGB(d.reflectance));
+            m.reflectance = flat_rgb(d.reflectance, d.reflectance_texture, d.reflectance_uv_scale);
+            m.bump_map = flat_bump(d);
             scene.materials.diffuse.push_back(m);
             handles.push_back({Material_Type::diffuse, (int)scene.materials.diffuse.size() - 1});
         } else if (d.type == YAR_MATERIAL_METAL) {
@@ -494,15 +541,17 @@ int cmd_render_yfs(const Args& a) {
             set_constant_parameter(m.eta_i, d.eta_i);
             set_constant_parameter(m.eta, ColorRGB(d.eta));
             set_constant_parameter(m.k, ColorRGB(d.k));
+            m.bump_map = flat_bump(d);
             scene.materials.metal.push_back(m);
             handles.push_back({Material_Type::metal, (int)scene.materials.metal.size() - 1});
         } else if (d.type == YAR_MATERIAL_GLASS) {
             Glass_Material m;
-            set_constant_parameter(m.reflectance, ColorRGB(d.reflectance));
-            set_constant_parameter(m.transmittance, ColorRGB(d.transmittance));
+            m.reflectance = flat_rgb(d.reflectance, d.reflectance_texture, d.reflectance_uv_scale);
+            m.transmittance = flat_rgb(d.transmittance, d.transmittance_texture, d.transmittance_uv_scale);
             set_constant_parameter(m.index_of_refraction, d.index_of_refraction);
             set_constant_parameter(m.roughness, d.u_roughness);
             m.roughness_is_alpha = d.roughness_is_alpha != 0;
+            m.bump_map = flat_bump(d);
             scene.materials.glass.push_back(m);
             handles.push_back({Material_Type::glass, (int)scene.materials.glass.size() - 1});
         } else if (d.type == YAR_MATERIAL_PLASTIC) {
@@ -510,7 +559,8 @@ int cmd_render_yfs(const Args& a) {
             set_constant_parameter(m.roughness, d.u_roughness);
             m.roughness_is_alpha = d.roughness_is_alpha != 0;
             set_constant_parameter(m.r0, d.transmittance[0]);
-            set_constant_parameter(m.diffuse_reflectance, ColorRGB(d.reflectance));
+            m.diffuse_reflectance = flat_rgb(d.reflectance, d.reflectance_texture, d.reflectance_uv_scale);
+            m.bump_map = flat_bump(d);
             scene.materials.plastic.push_back(m);
             handles.push_back({Material_Type::plastic, (int)scene.materials.plastic.size() - 1});
         } else if (d.type == YAR_MATERIAL_COATED_DIFFUSE) {
@@ -519,24 +569,28 @@ int cmd_render_yfs(const Args& a) {
             set_constant_parameter(m.v_roughness, d.v_roughness);
             m.roughness_is_alpha = d.roughness_is_alpha != 0;
             set_constant_parameter(m.r0, ColorRGB(d.transmittance));
-            set_constant_parameter(m.diffuse_reflectance, ColorRGB(d.reflectance));
+            m.diffuse_reflectance = flat_rgb(d.reflectance, d.reflectance_texture, d.reflectance_uv_scale);
+            m.bump_map = flat_bump(d);
             scene.materials.coated_diffuse.push_back(m);
             handles.push_back({Material_Type::coated_diffuse, (int)scene.materials.coated_diffuse.size() - 1});
         } else if (d.type == YAR_MATERIAL_PERFECT_REFLECTOR) {
             Perfect_Reflector_Material m;
             set_constant_parameter(m.reflectance, ColorRGB(d.reflectance));
+            m.bump_map = flat_bump(d);
             scene.materials.perfect_reflector.push_back(m);
             handles.push_back({Material_Type::perfect_reflector, (int)scene.materials.perfect_reflector.size() - 1});
         } else if (d.type == YAR_MATERIAL_PERFECT_REFRACTOR) {
             Perfect_Refractor_Material m;
             set_constant_parameter(m.index_of_refraction, d.index_of_refraction);
+            m.bump_map = flat_bump(d);
             scene.materials.perfect_refractor.push_back(m);
             handles.push_back({Material_Type::perfect_refractor, (int)scene.materials.perfect_refractor.size() - 1});
         } else if (d.type == YAR_MATERIAL_DIFFUSE_TRANSMISSION) {
             Diffuse_Transmission_Material m;
-            set_constant_parameter(m.reflectance, ColorRGB(d.reflectance));
-            set_constant_parameter(m.transmittance, ColorRGB(d.transmittance));
+            m.reflectance = flat_rgb(d.reflectance, d.reflectance_texture, d.reflectance_uv_scale);
+            m.transmittance = flat_rgb(d.transmittance, d.transmittance_texture, d.transmittance_uv_scale);
             set_constant_parameter(m.scale, ColorRGB(d.diffuse));
+            m.bump_map = flat_bump(d);
             scene.materials.diffuse_transmission.push_back(m);
             handles.push_back({Material_Type::diffuse_transmission,
                                (int)scene.materials.diffuse_transmission.size() - 1});
@@ -547,6 +601,7 @@ int cmd_render_yfs(const Args& a) {
             set_constant_parameter(m.diffuse, ColorRGB(d.diffuse));
             set_constant_parameter(m.specular, ColorRGB(d.specular));
             set_constant_parameter(m.roughness, d.u_roughness);
+            m.bump_map = flat_bump(d);
             scene.materials.pbrt3_translucent.push_back(m);
             handles.push_back({Material_Type::pbrt3_translucent, (int)scene.materials.pbrt3_translucent.size() - 1});
         } else if (d.type == YAR_MATERIAL_PBRT3_UBER) {
@@ -559,6 +614,7 @@ int cmd_render_yfs(const Args& a) {
             set_constant_parameter(m.u_roughness, d.u_roughness);
             set_constant_parameter(m.v_roughness, d.v_roughness);
             set_constant_parameter(m.index_of_refraction, d.index_of_refraction);
+            m.bump_map = flat_bump(d);
             m.component_count = (uint8_t)d.component_count;
             for (uint32_t k = 0; k < d.component_count && k < 5; k++)
                 m.components[k] = (Pbrt3_Uber_Material::Component_Type)d.components[k];

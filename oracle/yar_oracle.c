@@ -594,6 +594,9 @@ typedef struct shading_ctx {
     float uv[2];
     v3 dpdu, dpdv;              /* world space */
     float dudx, dvdx, dudy, dvdy;
+    /* for bump mapping: the normal's uv derivatives (world space, flipped
+     * with the normal) and the shading frame's second tangent */
+    v3 dndu, dndv, dpdv_shading;
 } shading_ctx;
 
 /* adjust_shading_normal, src/ref/shading_context.cpp:17-63 */
@@ -639,7 +642,7 @@ static void init_shading(const yar_flat_scene* s, v3 ray_d, uint32_t object_inde
         if (len2_3(in) != 0) normal = norm3(in);
     }
     int has_uv = 0;
-    v3 dpdu = mk3(0, 0, 0), dpdv = mk3(0, 0, 0);
+    v3 dpdu = mk3(0, 0, 0), dpdv = mk3(0, 0, 0), dndu = mk3(0, 0, 0), dndv = mk3(0, 0, 0);
     if (m->uvs) {
         has_uv = 1;
         const float* u0 = m->uvs + 2 * (size_t)vi[0];
@@ -658,32 +661,66 @@ static void init_shading(const yar_flat_scene* s, v3 ray_d, uint32_t object_inde
             dpdv = mul3s(add3(mul3s(bp0, -a10), mul3s(bp1, a00)), inv_det);
         }
         if (fabsf(det) < 1e-9f) coordinate_system(gn, &dpdu, &dpdv);
+        /* the normals' derivatives (zero vertex normals without them) */
+        v3 n[3] = {mk3(0, 0, 0), mk3(0, 0, 0), mk3(0, 0, 0)};
+        if (m->normals)
+            for (int k = 0; k < 3; k++) n[k] = ld3(m->normals + 3 * (size_t)vi[k]);
+        v3 bn0 = sub3(n[1], n[0]), bn1 = sub3(n[2], n[0]);
+        if (det != 0.f) {
+            float inv_det = 1.f / det;
+            dndu = mul3s(sub3(mul3s(bn0, a11), mul3s(bn1, a01)), inv_det);
+            dndv = mul3s(add3(mul3s(bn0, -a10), mul3s(bn1, a00)), inv_det);
+        }
+        if (fabsf(det) < 1e-9f) {  /* pbrt's approximation */
+            v3 dn = cross3(bn1, bn0);
+            if (len2_3(dn) == 0.f) {
+                dndu = mk3(0, 0, 0);
+                dndv = mk3(0, 0, 0);
+            } else {
+                coordinate_system(dn, &dndu, &dndv);
+            }
+        }
     }
     /* to world space */
     position = xform_point(obj->object_to_world, position);
     normal = xform_vector(obj->object_to_world_normal, normal);
-    normal = div3s(normal, len3(normal));
+    const float length_of_scaled_normal = len3(normal);
+    normal = div3s(normal, length_of_scaled_normal);
     gn = xform_vector(obj->object_to_world_normal, gn);
     gn = div3s(gn, len3(gn));
     dpdu = xform_vector(obj->object_to_world, dpdu);
     dpdv = xform_vector(obj->object_to_world, dpdv);
+    {
+        const float inv_length = 1 / length_of_scaled_normal;
+        dndu = mul3s(xform_vector(obj->object_to_world_normal, dndu), inv_length);
+        dndv = mul3s(xform_vector(obj->object_to_world_normal, dndv), inv_length);
+    }
     sc->has_uv = has_uv;
     sc->dpdu = dpdu;
     sc->dpdv = dpdv;
     if (dot3(normal, gn) == 0.f) gn = normal;
     if (dot3(gn, sc->wo) < 0) gn = neg3(gn);
-    if (dot3(normal, gn) < 0) { normal = neg3(normal); sc->flipped = 1; }
+    if (dot3(normal, gn) < 0) {
+        normal = neg3(normal);
+        dndu = neg3(dndu);
+        dndv = neg3(dndv);
+        sc->flipped = 1;
+    }
     offset_origins(position, gn, &sc->origin_pos, &sc->origin_neg);
     adjust_shading_normal(sc->wo, gn, &normal);
-    v3 dpdu_shading;
+    v3 dpdu_shading, dpdv_shading;
     if (!has_uv) {
-        v3 dummy;
-        coordinate_system(normal, &dpdu_shading, &dummy);
+        coordinate_system(normal, &dpdu_shading, &dpdv_shading);
     } else if (fabsf(dot3(normal, gn) - 1.f) < 1e-6f) {
         dpdu_shading = dpdu;
+        dpdv_shading = dpdv;
     } else {
         dpdu_shading = mul3s(project_direction(dpdu, normal), len3(dpdu));
+        dpdv_shading = mul3s(project_direction(dpdv, normal), len3(dpdv));
     }
+    sc->dndu = dndu;
+    sc->dndv = dndv;
+    sc->dpdv_shading = dpdv_shading;
     sc->position = position;
     sc->geometric_normal = gn;
     sc->normal = normal;
@@ -754,6 +791,7 @@ static v3 local_to_world(const bsdf_t* f, v3 l) {
 static v3 world_to_local(const bsdf_t* f, v3 w) { return mk3(dot3(w, f->t), dot3(w, f->bt), dot3(w, f->n)); }
 
 static col texture_reflectance(const yar_flat_scene* s, const shading_ctx* sc, const yar_material_desc* m);
+static col texture_transmittance(const yar_flat_scene* s, const shading_ctx* sc, const yar_material_desc* m);
 
 static int make_leaf_bsdf(const yar_flat_scene* s, const shading_ctx* sc, uint32_t type, const yar_material_desc* m,
                           bsdf_t* f) {
@@ -774,8 +812,8 @@ static int make_leaf_bsdf(const yar_flat_scene* s, const shading_ctx* sc, uint32
         f->k_t = ldc(m->k);
     } else if (f->type == YAR_MATERIAL_GLASS) {
         f->reflection = f->transmission = 1;
-        f->reflectance = ldc(m->reflectance);
-        f->transmittance = ldc(m->transmittance);
+        f->reflectance = m->reflectance_texture ? texture_reflectance(s, sc, m) : ldc(m->reflectance);
+        f->transmittance = m->transmittance_texture ? texture_transmittance(s, sc, m) : ldc(m->transmittance);
         f->alpha = roughness_to_alpha(s, m->u_roughness, m->roughness_is_alpha);
         int enter = !sc->flipped;
         f->eta_o = enter ? 1.f : m->index_of_refraction;
@@ -784,7 +822,7 @@ static int make_leaf_bsdf(const yar_flat_scene* s, const shading_ctx* sc, uint32
         /* Plastic_BRDF / Pbrt3_Plastic_BRDF / Ashikhmin_Shirley_Phong_BRDF constructors,
          * src/ref/bsdf.cpp:205-213, :427-438, src/ref/bsdf_pbrt.cpp:258-262 */
         f->reflection = 1;
-        f->reflectance = ldc(m->reflectance);
+        f->reflectance = m->reflectance_texture ? texture_reflectance(s, sc, m) : ldc(m->reflectance);
         f->transmittance = ldc(m->transmittance);
         f->alpha_x = roughness_to_alpha(s, m->u_roughness, m->roughness_is_alpha);
         f->alpha_y = roughness_to_alpha(s, m->v_roughness, m->roughness_is_alpha);
@@ -803,8 +841,10 @@ static int make_leaf_bsdf(const yar_flat_scene* s, const shading_ctx* sc, uint32
     } else if (f->type == YAR_MATERIAL_DIFFUSE_TRANSMISSION) {
         /* Diffuse_Transmission_BSDF, src/ref/bsdf.cpp:89-103 */
         f->reflection = f->transmission = 1;
-        f->reflectance = clamp_unit(mulc(ldc(m->diffuse), ldc(m->reflectance)));
-        f->transmittance = clamp_unit(mulc(ldc(m->diffuse), ldc(m->transmittance)));
+        const col r = m->reflectance_texture ? texture_reflectance(s, sc, m) : ldc(m->reflectance);
+        const col t = m->transmittance_texture ? texture_transmittance(s, sc, m) : ldc(m->transmittance);
+        f->reflectance = clamp_unit(mulc(ldc(m->diffuse), r));
+        f->transmittance = clamp_unit(mulc(ldc(m->diffuse), t));
     } else if (f->type == YAR_MATERIAL_PBRT3_TRANSLUCENT) {
         /* Pbrt3_Translucent_BSDF, src/ref/bsdf_pbrt.cpp:94-115 */
         f->reflectance = ldc(m->reflectance);
@@ -997,11 +1037,57 @@ static col texture_ewa(const yar_flat_scene* s, const yar_texture_desc* t, float
 
 /* evaluate_texture_parameter (parameter_evaluation.cpp:10-31): uv and its
  * derivatives scaled, then EWA with repeat wrapping */
-static col texture_reflectance(const yar_flat_scene* s, const shading_ctx* sc, const yar_material_desc* m) {
-    const yar_texture_desc* t = &s->textures[m->reflectance_texture - 1];
-    const float su = m->reflectance_uv_scale[0], sv = m->reflectance_uv_scale[1];
+static col texture_parameter(const yar_flat_scene* s, uint32_t texture, const float uv_scale[2], float u, float v,
+                             const shading_ctx* sc) {
+    const yar_texture_desc* t = &s->textures[texture - 1];
+    const float su = uv_scale[0], sv = uv_scale[1];
     float a1[2] = {sc->dudx * su, sc->dvdx * sv}, a2[2] = {sc->dudy * su, sc->dvdy * sv};
-    return texture_ewa(s, t, sc->uv[0] * su, sc->uv[1] * sv, a1, a2);
+    return texture_ewa(s, t, u * su, v * sv, a1, a2);
+}
+static col texture_reflectance(const yar_flat_scene* s, const shading_ctx* sc, const yar_material_desc* m) {
+    return texture_parameter(s, m->reflectance_texture, m->reflectance_uv_scale, sc->uv[0], sc->uv[1], sc);
+}
+static col texture_transmittance(const yar_flat_scene* s, const shading_ctx* sc, const yar_material_desc* m) {
+    return texture_parameter(s, m->transmittance_texture, m->transmittance_uv_scale, sc->uv[0], sc->uv[1], sc);
+}
+
+/* evaluate_float_parameter of a bump map at (u, v): the constant, or the
+ * luminance of the texture (parameter_evaluation.cpp:46-55) */
+static float bump_height_at(const yar_flat_scene* s, const yar_material_desc* m, float u, float v,
+                            const shading_ctx* sc) {
+    if (m->bump == 1) return m->bump_height;
+    return luminance(texture_parameter(s, m->bump_texture, m->bump_uv_scale, u, v, sc));
+}
+
+/* Shading_Context::apply_bump_map (src/ref/shading_context.cpp:419-462): the
+ * height and its finite differences along u and v perturb the shading
+ * tangents; the shading normal is rebuilt from them, turned into the
+ * geometric normal's hemisphere and adjusted. */
+static void apply_bump_map(const yar_flat_scene* s, const yar_material_desc* m, shading_ctx* sc) {
+    if (!m->bump) return;
+    const float height = bump_height_at(s, m, sc->uv[0], sc->uv[1], sc);
+    float du = 0.5f * (fabsf(sc->dudx) + fabsf(sc->dudy));
+    if (du == 0.f) du = 0.0005f;
+    const float height_du = bump_height_at(s, m, sc->uv[0] + du, sc->uv[1] + 0.f, sc);
+    float dv = 0.5f * (fabsf(sc->dvdx) + fabsf(sc->dvdy));
+    if (dv == 0.f) dv = 0.0005f;
+    const float height_dv = bump_height_at(s, m, sc->uv[0] + 0.f, sc->uv[1] + dv, sc);
+    const v3 original_shading_normal = sc->flipped ? neg3(sc->normal) : sc->normal;
+    float du_scale = 1.f, dv_scale = 1.f;
+    if (m->bump == 2) {
+        du_scale = m->bump_uv_scale[0];
+        dv_scale = m->bump_uv_scale[1];
+    }
+    const v3 dpdu_shading = add3(add3(sc->dpdu_shading, mul3s(original_shading_normal, (height_du - height) / (du * du_scale))),
+                                 mul3s(mul3s(sc->dndu, du_scale), height));
+    const v3 dpdv_shading = add3(add3(sc->dpdv_shading, mul3s(original_shading_normal, (height_dv - height) / (dv * dv_scale))),
+                                 mul3s(mul3s(sc->dndv, dv_scale), height));
+    v3 normal = norm3(cross3(dpdu_shading, dpdv_shading));
+    if (dot3(normal, sc->geometric_normal) < 0) normal = neg3(normal);
+    adjust_shading_normal(sc->wo, sc->geometric_normal, &normal);
+    sc->normal = normal;
+    sc->dpdu_shading = dpdu_shading;
+    sc->dpdv_shading = dpdv_shading;
 }
 
 /* ray_plane_intersection, src/lib/math.cpp:27-31 */
@@ -2100,9 +2186,18 @@ static void camera_ray(const yar_camera_desc* c, float fx, float fy, v3* o, v3* 
     *d = xform_vector(c->camera_to_world, dir);
 }
 
+/* The material's bump map, applied once per hit before the delta check and
+ * the BSDF: check_for_delta_scattering_event (src/ref/delta_scattering.cpp:252-257)
+ * applies it for the delta-capable materials and create_bsdf (src/ref/bsdf.cpp:631-714)
+ * for the others; applying it twice gives the same shading frame.  Mix
+ * materials have none (their sub-materials' bump maps are refused). */
+static void apply_material_bump(const yar_flat_scene* s, shading_ctx* sc) {
+    if (sc->material_type == YAR_MATERIAL_NULL || sc->material_type == YAR_MATERIAL_MIX) return;
+    apply_bump_map(s, &s->materials[sc->material_index], sc);
+}
+
 /* check_for_delta_scattering_event / get_*_info, src/ref/delta_scattering.cpp:27-97, :252-324
- * (perfect reflector, perfect refractor, smooth glass; no nested dielectrics,
- * no bump maps).  Returns 1 and the delta direction and attenuation for a delta
+ * (perfect reflector, perfect refractor, smooth glass; no nested dielectrics).  Returns 1 and the delta direction and attenuation for a delta
  * material, 2 for a delta material without a direction, 0 otherwise. */
 static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, float* u_ptr, v3* dir, col* atten,
                             float* bsdf_prob) {
@@ -2194,10 +2289,10 @@ static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, floa
     const float fresnel = dielectric_fresnel(cos_i, eta_t_over_i);
     if (u < fresnel) {
         *dir = reflect3(sc->wo, sc->normal);
-        *atten = ldc(m->reflectance);
+        *atten = m->reflectance_texture ? texture_reflectance(s, sc, m) : ldc(m->reflectance);
     } else {
         const float eta = 1.f / eta_t_over_i;
-        *atten = mulcs(ldc(m->transmittance), eta * eta);
+        *atten = mulcs(m->transmittance_texture ? texture_transmittance(s, sc, m) : ldc(m->transmittance), eta * eta);
         refract3(sc->wo, sc->normal, eta, dir);
     }
     return 1;
@@ -2263,6 +2358,7 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
         v3 ddir;
         col datten;
         float bsdf_prob = 1.f; /* 1 - delta_layer_selection_probability */
+        apply_material_bump(s, &sc);
         const int delta = delta_scattering(s, &sc, &u_scatter, &ddir, &datten, &bsdf_prob);
         if (delta == 2) break; /* perfect refractor at total internal reflection */
         bsdf_t f, f_sub[2];
@@ -2361,6 +2457,7 @@ static int trace_direct(const yar_flat_scene* s, const env_sampler* env, v3 ro, 
     col datten;
     float bsdf_prob = 1.f;
     int delta = 0;
+    if (sc.light_type == YAR_LIGHT_NULL) apply_material_bump(s, &sc);
     if (sc.material_type != YAR_MATERIAL_NULL) delta = delta_scattering(s, &sc, &u_scatter, &ddir, &datten, &bsdf_prob);
     if (sc.light_type != YAR_LIGHT_NULL) {
         if (emitted_radiance(s, &sc, &le)) L = le;
@@ -2671,18 +2768,31 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
             return YAR_ERR_UNSUPPORTED;
     }
     if (s->other_light_count) return YAR_ERR_UNSUPPORTED;
-    /* image textures: a diffuse reflectance with camera-ray differentials in the
-     * path tracer; no delta materials (their differential rays are not restated) */
+    /* image textures: the reflectance of diffuse, plastic, coated diffuse, glass
+     * and diffuse transmission, the transmittance of glass and diffuse
+     * transmission, and bump maps, with camera-ray differentials in the path
+     * tracer; no delta materials in a textured scene (their differential rays
+     * are not restated).  A constant bump height needs no differentials. */
     int textured = 0, delta_materials = 0;
     for (uint32_t i = 0; i < s->material_count; i++) {
         const yar_material_desc* m = &s->materials[i];
         if (m->other_textured_parameters) return YAR_ERR_UNSUPPORTED;
-        if (m->reflectance_texture) {
-            if (m->type != YAR_MATERIAL_DIFFUSE || m->reflectance_texture > s->texture_count) return YAR_ERR_UNSUPPORTED;
-            const yar_texture_desc* t = &s->textures[m->reflectance_texture - 1];
+        const int reflectance_slot = m->type == YAR_MATERIAL_DIFFUSE || m->type == YAR_MATERIAL_PLASTIC ||
+                                     m->type == YAR_MATERIAL_COATED_DIFFUSE || m->type == YAR_MATERIAL_GLASS ||
+                                     m->type == YAR_MATERIAL_DIFFUSE_TRANSMISSION;
+        const int transmittance_slot = m->type == YAR_MATERIAL_GLASS || m->type == YAR_MATERIAL_DIFFUSE_TRANSMISSION;
+        if ((m->reflectance_texture && !reflectance_slot) || (m->transmittance_texture && !transmittance_slot) ||
+            m->bump > 2 || (m->bump && m->type == YAR_MATERIAL_MIX))
+            return YAR_ERR_UNSUPPORTED;
+        const uint32_t used[3] = {m->reflectance_texture, m->transmittance_texture, m->bump == 2 ? m->bump_texture : 0u};
+        for (int k = 0; k < 3; k++) {
+            if (!used[k]) continue;
+            if (used[k] > s->texture_count) return YAR_ERR_INVALID;
+            const yar_texture_desc* t = &s->textures[used[k] - 1];
             if (t->mip_count == 0 || t->first_mip + t->mip_count > s->texture_mip_count) return YAR_ERR_INVALID;
             textured = 1;
         }
+        if (m->bump == 2 && !used[2]) return YAR_ERR_INVALID;
         delta_materials |= m->type == YAR_MATERIAL_PERFECT_REFLECTOR || m->type == YAR_MATERIAL_PERFECT_REFRACTOR ||
                            (m->type == YAR_MATERIAL_GLASS && !(m->u_roughness > 0.f)) ||
                            m->type == YAR_MATERIAL_PBRT3_UBER || m->type == YAR_MATERIAL_MIX;
@@ -2699,7 +2809,7 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
                 if (si < 0 || (uint32_t)si >= s->material_count) return YAR_ERR_INVALID;
                 const yar_material_desc* sm = &s->materials[si];
                 if (sm->type == YAR_MATERIAL_MIX || sm->type == YAR_MATERIAL_PBRT3_UBER ||
-                    (sm->type == YAR_MATERIAL_GLASS && !(sm->u_roughness > 0.f)))
+                    (sm->type == YAR_MATERIAL_GLASS && !(sm->u_roughness > 0.f)) || sm->bump)
                     return YAR_ERR_UNSUPPORTED;
                 delta_subs += is_pure_delta(sm->type);
             }

@@ -64,6 +64,18 @@ Fixtures
                              the floor lit with pbrt "imagemap" textures of a
                              48 x 40 checker image (uv scale 1 and 2 x 3;
                              EWA filtering with camera-ray differentials), seed 17.
+  cornell_bump_64.yfs / .npz  bump maps and textures on every texture slot:
+                             the back wall matte (checker Kd, image bump map),
+                             the left wall plastic (checker Kd 2 x 3, bump
+                             map 2 x 2), the floor matte with splayed vertex
+                             normals and a constant bump height, the right
+                             wall translucent (image bump map), a rough glass
+                             panel with splayed normals (bump map 2 x 2;
+                             checker Kr and Kt set on the flattened scene),
+                             the ceiling made diffuse transmission with
+                             checker reflectance and transmittance, GGX boxes;
+                             rendered by the reference from the edited flat
+                             scene, seed 21.
   cornell_direct_64.yfs / .npz  the reference's direct-lighting algorithm
                              (pbrt "directlighting"): GGX boxes, the quad light
                              with 4 samples (2 x 2 arrays), point, spot and
@@ -390,6 +402,61 @@ def cornell_alpha_64():
     np.savez_compressed(os.path.join(HERE, "cornell_alpha_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def cornell_bump_64():
+    from yar_gb300 import exr
+    with tempfile.TemporaryDirectory() as d:
+        exr.write_exr(os.path.join(d, "checks.exr"), scenes.texture_image(), False, {})
+        exr.write_exr(os.path.join(d, "bumps.exr"), scenes.bump_image(), False, {})
+        pbrt = os.path.join(d, "cornell_bump.pbrt")
+        texs = (scenes.texture_statements("checks.exr") + scenes.texture_statements("checks.exr", "fine", 2.0, 3.0) +
+                ('Texture "bumps" "float" "imagemap" "string filename" "bumps.exr"',
+                 'Texture "bumps2" "float" "imagemap" "string filename" "bumps.exr" "float uscale" [2] '
+                 '"float vscale" [2]',
+                 'Texture "lift" "float" "constant" "float value" [0.02]'))
+        floor_normals = ' "normal N" [-0.1 1 -0.1 0.1 1 -0.1 0.1 1 0.1 -0.1 1 0.1]'
+        walls = {
+            0: ('Material "matte" "rgb Kd" [0.6 0.55 0.5] "texture bumpmap" "lift"', floor_normals),
+            1: ('Material "matte" "rgb Kd" [0.7 0.7 0.7]', ""),
+            2: ('Material "matte" "texture Kd" "checks" "texture bumpmap" "bumps"', ""),
+            3: ('Material "plastic" "texture Kd" "fine" "rgb Ks" [0.3 0.3 0.3] "float roughness" [0.1] '
+                '"texture bumpmap" "bumps2"', ""),
+            4: ('Material "translucent" "rgb Kd" [0.5 0.4 0.3] "rgb Ks" [0.2 0.2 0.2] "rgb reflect" [0.6 0.6 0.6] '
+                '"rgb transmit" [0.3 0.3 0.3] "float roughness" [0.2] "texture bumpmap" "bumps"', ""),
+        }
+        panel = scenes.bump_panel('Material "glass" "float uroughness" [0.25] "float vroughness" [0.25] '
+                                  '"float index" [1.5] "rgb Kr" [1 1 1] "rgb Kt" [1 1 1] "texture bumpmap" "bumps2"')
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=21, width=64, height=64, spp=16, maxdepth=8,
+                                                  box_materials=scenes.GGX_BOXES, textures=texs,
+                                                  wall_materials=walls, extra_shapes=panel))
+        yfs = os.path.join(d, "cornell_bump.yfs")
+        oracle.ref_flatten(pbrt, yfs, seed_offset=1)
+        s = FlatScene.read(yfs)
+        mats = s.materials
+        checks = int(mats["reflectance_texture"][s.objects["material_index"][2]])
+        assert checks > 0 and int(mats["bump_texture"][s.objects["material_index"][2]]) > 0
+        # the panel: textured Kr (2 x 3) and Kt
+        g = int(s.objects["material_index"][-1])
+        assert int(mats["type"][g]) == 7 and int(mats["bump"][g]) == 2  # glass
+        mats["reflectance_texture"][g] = checks
+        mats["reflectance_uv_scale"][g] = (2.0, 3.0)
+        mats["transmittance_texture"][g] = checks
+        mats["transmittance_uv_scale"][g] = (1.0, 1.0)
+        # the ceiling: diffuse transmission with textured reflectance and transmittance
+        c = int(s.objects["material_index"][1])
+        mats["type"][c] = 3  # diffuse transmission
+        s.objects["material_type"][s.objects["material_index"] == c] = 3
+        mats["reflectance"][c] = (0.5, 0.5, 0.5)
+        mats["reflectance_texture"][c] = checks
+        mats["reflectance_uv_scale"][c] = (1.0, 1.0)
+        mats["transmittance"][c] = (0.4, 0.4, 0.4)
+        mats["transmittance_texture"][c] = checks
+        mats["transmittance_uv_scale"][c] = (3.0, 2.0)
+        mats["diffuse"][c] = (0.9, 0.8, 0.7)
+        s.write(os.path.join(HERE, "cornell_bump_64.yfs"))
+        img, info = oracle.ref_render_flat(s, threads=8, textures_from=pbrt)
+    np.savez_compressed(os.path.join(HERE, "cornell_bump_64.npz"), image=img, variance=np.float64(info["variance"]))
+
+
 def cornell_direct_64():
     _pbrt_golden("cornell_direct_64", 15, box_materials=scenes.GGX_BOXES, light_sources=scenes.DELTA_LIGHTS,
                  light_samples=4, integrator="directlighting")
@@ -479,6 +546,7 @@ if __name__ == "__main__":
                              "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64",
                              "cornell_direct_64", "cornell_direct_env_64", "cornell_texture_64", "checkpoint_c1",
                              "cornell_gaussian_64", "cornell_triangle_64", "cornell_c1_256", "cornell_alpha_64",
+                             "cornell_bump_64",
                              "exr_files",
                              "kdtree_cache_files"]
     for name in which:

@@ -126,7 +126,7 @@ def test_builder_against_live_reference_large_mesh():
                                   "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64",
                                   "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64",
                                   "cornell_texture_64", "cornell_gaussian_64", "cornell_triangle_64",
-                                  "cornell_alpha_64"])
+                                  "cornell_alpha_64", "cornell_bump_64"])
 def test_oracle_render_matches_reference_golden(name):
     """The oracle's path loop, sampler, shading, BSDFs (diffuse, GGX metal, rough
     glass, plastic in both of the reference's forms, coated diffuse), delta
@@ -208,21 +208,33 @@ def test_alpha_texture_file_round_trip(tmp_path):
     s.write(str(p))
     t = FlatScene.read(str(p))
     assert [m.alpha_texture for m in t.meshes] == [m.alpha_texture for m in s.meshes]
-    assert open(str(p), "rb").read() == open(golden("cornell_alpha_64.yfs"), "rb").read()
+    assert np.array_equal(t.materials, s.materials) and np.array_equal(t.texels, s.texels)
+    q = tmp_path / "b.yfs"
+    t.write(str(q))
+    assert open(str(p), "rb").read() == open(str(q), "rb").read()
 
 
 def test_textured_scenes_outside_the_restated_part_are_refused():
-    """Image textures are restated for diffuse reflectance in the path tracer
-    with camera-ray differentials; with the direct-lighting algorithm, next to
-    delta materials, or on other parameters the oracle refuses the scene."""
-    for change in ("direct", "mirror", "other"):
+    """Image textures are restated for the reflectance and transmittance slots
+    and bump maps in the path tracer with camera-ray differentials; with the
+    direct-lighting algorithm, next to delta materials, on other parameters,
+    in a slot the material does not read, or as the bump map of a mix's
+    sub-material the oracle refuses the scene."""
+    for change in ("direct", "mirror", "other", "slot", "mix_bump"):
         s = FlatScene.read(golden("cornell_texture_64.yfs"))
         if change == "direct":
             s.config["rendering_algorithm"] = 0
         elif change == "mirror":
             s.materials["type"][-1] = 0  # perfect reflector
-        else:
+        elif change == "other":
             s.materials["other_textured_parameters"][-1] = 1
+        elif change == "slot":
+            k = int(np.nonzero(s.materials["reflectance_texture"])[0][0])
+            s.materials["transmittance_texture"][k] = s.materials["reflectance_texture"][k]  # diffuse: no such slot
+        else:
+            s = FlatScene.read(golden("cornell_mix_64.yfs"))
+            mix = int(np.nonzero(s.materials["type"] == 8)[0][0])
+            s.materials["bump"][int(s.materials["mix_materials"][mix][0])] = 1
         with pytest.raises(Exception):
             oracle.render(s, threads=2)
 

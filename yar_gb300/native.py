@@ -76,7 +76,10 @@ class MaterialDesc(C.Structure):
                 ("opacity", C.c_float * 3), ("component_count", C.c_uint32), ("components", C.c_uint32 * 5),
                 ("mix_materials", C.c_int32 * 2), ("mix_amount", C.c_float * 3),
                 ("reflectance_texture", C.c_uint32), ("reflectance_uv_scale", C.c_float * 2),
-                ("other_textured_parameters", C.c_uint32)]
+                ("other_textured_parameters", C.c_uint32),
+                ("transmittance_texture", C.c_uint32), ("transmittance_uv_scale", C.c_float * 2),
+                ("bump", C.c_uint32), ("bump_height", C.c_float), ("bump_texture", C.c_uint32),
+                ("bump_uv_scale", C.c_float * 2)]
 
 
 class RectLightDesc(C.Structure):

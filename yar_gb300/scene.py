@@ -24,7 +24,10 @@ MATERIAL_DTYPE = np.dtype([("type", "<u4"), ("reflectance", "<f4", 3), ("transmi
                            ("opacity", "<f4", 3), ("component_count", "<u4"), ("components", "<u4", 5),
                            ("mix_materials", "<i4", 2), ("mix_amount", "<f4", 3),
                            ("reflectance_texture", "<u4"), ("reflectance_uv_scale", "<f4", 2),
-                           ("other_textured_parameters", "<u4")])
+                           ("other_textured_parameters", "<u4"),
+                           ("transmittance_texture", "<u4"), ("transmittance_uv_scale", "<f4", 2),
+                           ("bump", "<u4"), ("bump_height", "<f4"), ("bump_texture", "<u4"),
+                           ("bump_uv_scale", "<f4", 2)])
 MATERIAL_RECORD_V1 = 72  # the MATS chunk's records: the fields up to roughness_is_alpha
 LIGHT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("emitted_radiance", "<f4", 3), ("size", "<f4", 2),
                         ("sample_count", "<i4")])

@@ -182,7 +182,7 @@ def _box(center, size, angle_deg):
 def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radiance=17.0, box_materials=None,
                  upper_light=None, light_sources=(), mesh_lights=(), sphere_lights=(), named_materials=(),
                  integrator="path", light_samples=1, textures=(), wall_textures=None, pixel_filter='"box"',
-                 extra_shapes=()):
+                 extra_shapes=(), wall_materials=None):
     """pbrt-v3 text of the seeded Cornell box (34 triangles + a quad light).
 
     box_materials: None for matte boxes, or two pbrt material statements for
@@ -202,7 +202,11 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
     algorithm); light_samples: the quad light's "integer samples".
     textures: pbrt Texture statements; wall_textures: {wall index (0 floor,
     1 ceiling, 2 back, 3 left, 4 right): texture name} walls whose matte Kd is
-    that texture, given uvs (0,0), (1,0), (1,1), (0,1) at their corners."""
+    that texture, given uvs (0,0), (1,0), (1,1), (0,1) at their corners.
+    wall_materials: {wall index: (material statement, extra shape parameters)}
+    walls with that material, the same uvs and the extra parameters (e.g.
+    per-vertex normals).
+    extra_shapes: pbrt statements added after the room."""
     rng = np.random.default_rng(seed)
     k = int(math.ceil(math.sqrt(spp)))
     shapes = []
@@ -243,6 +247,9 @@ def cornell_pbrt(seed=1, width=256, height=256, spp=16, maxdepth=8, light_radian
         if k in wall_textures:
             material = 'Material "matte" "texture Kd" "%s"' % wall_textures[k]
             shape += ' "float uv" [0 0 1 0 1 1 0 1]'
+        if k in (wall_materials or {}):
+            material, extra = wall_materials[k]
+            shape += ' "float uv" [0 0 1 0 1 1 0 1]' + extra
         out += ["AttributeBegin",
                 '  ' + material,
                 shape,
@@ -341,6 +348,30 @@ def cutout_image(size=16, cells=4):
     y, x = np.mgrid[0:size, 0:size]
     on = (((x * cells) // size + (y * cells) // size) % 2).astype(np.float32)
     return np.repeat(on[:, :, None], 3, axis=2)
+
+
+def bump_image(size=32, seed=5):
+    """A height map for bump mapping: concentric ripples plus seeded noise,
+    heights in [0, 0.05] in all three channels, size x size texels."""
+    rng = np.random.default_rng(seed)
+    y, x = (np.mgrid[0:size, 0:size] + 0.5) / size
+    r = np.hypot(x - 0.5, y - 0.5)
+    h = 0.5 + 0.35 * np.sin(2 * math.pi * 5 * r) + 0.15 * rng.random((size, size))
+    h = 0.05 * np.clip(h, 0.0, 1.0)
+    return np.repeat(h[:, :, None], 3, axis=2).astype(np.float32)
+
+
+def bump_panel(material, normals=True):
+    """pbrt statements of a vertical quad across the front of the room (uvs
+    repeat twice), with slightly splayed per-vertex normals when `normals`,
+    so that the normal's uv derivatives take part in the bump."""
+    v = [-0.7, 0.05, 0.5, 0.7, 0.05, 0.5, 0.7, 1.3, 0.5, -0.7, 1.3, 0.5]
+    n = [-0.15, -0.1, 1, 0.15, -0.1, 1, 0.15, 0.1, 1, -0.15, 0.1, 1]
+    shape = ('  Shape "trianglemesh" "integer indices" [0 1 2 0 2 3] "point P" [%s] "float uv" [0 0 2 0 2 2 0 2]'
+             % " ".join("%g" % a for a in v))
+    if normals:
+        shape += ' "normal N" [%s]' % " ".join("%g" % a for a in n)
+    return ("AttributeBegin", "  " + material, shape, "AttributeEnd")
 
 
 def cutout_fence(texture="cutout", material='Material "matte" "rgb Kd" [0.8 0.7 0.3]'):
