@@ -46,7 +46,7 @@ def test_struct_sizes_match_the_header():
     from yar_gb300 import native
     assert ctypes.sizeof(native.KdNode) == 8
     assert ctypes.sizeof(native.ObjectDesc) == 164
-    assert ctypes.sizeof(native.MaterialDesc) == 180
+    assert ctypes.sizeof(native.MaterialDesc) == 212
     assert ctypes.sizeof(native.RectLightDesc) == 72
 
 

@@ -5,7 +5,7 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import golden
+from conftest import constant_bumps_with_delta_materials, golden
 from yar_gb300 import scenes
 from yar_gb300.scene import FlatScene, Mesh, make_object
 
@@ -237,6 +237,20 @@ def test_textured_scenes_outside_the_restated_part_are_refused():
             s.materials["bump"][int(s.materials["mix_materials"][mix][0])] = 1
         with pytest.raises(Exception):
             oracle.render(s, threads=2)
+
+
+@pytest.mark.skipif(not oracle.have_reference(), reason="reference not built here")
+def test_oracle_constant_bump_on_delta_materials_against_live_reference():
+    """A constant bump height on a mirror and on smooth glass (the bump comes
+    before the delta check, src/ref/delta_scattering.cpp:252-257) and on a floor
+    with splayed vertex normals: the oracle against the reference's render of
+    the same flat scene, bit for bit."""
+    s = constant_bumps_with_delta_materials()
+    s.config["max_light_bounces"] = 5
+    ref, info = oracle.ref_render_flat(s, threads=8)
+    img, var = oracle.render(s, threads=8)
+    assert np.array_equal(bits(img), bits(ref))
+    assert var == info["variance"]
 
 
 def test_oracle_c1_configuration_matches_reference_golden():

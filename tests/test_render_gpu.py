@@ -16,7 +16,7 @@ import numpy as np
 import pytest
 
 import oracle
-from conftest import golden
+from conftest import constant_bumps_with_delta_materials, golden
 from yar_gb300 import scenes
 from yar_gb300.scene import FlatScene
 
@@ -65,7 +65,7 @@ def compare(img, ref):
                                   "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
                   "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64",
                                   "cornell_texture_64", "cornell_gaussian_64", "cornell_triangle_64",
-                                  "cornell_alpha_64"])
+                                  "cornell_alpha_64", "cornell_bump_64"])
 def test_render_matches_reference_golden(gpu_ctx, name):
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
@@ -88,7 +88,7 @@ RENDER_GOLDENS = ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornel
                   "cornell_layered_yar_64", "cornell_lights_64", "cornell_meshlight_64", "cornell_spherelight_64",
                   "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
                   "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64", "cornell_texture_64",
-                  "cornell_gaussian_64", "cornell_triangle_64", "cornell_alpha_64"]
+                  "cornell_gaussian_64", "cornell_triangle_64", "cornell_alpha_64", "cornell_bump_64"]
 
 
 @pytest.mark.parametrize("name", RENDER_GOLDENS)
@@ -316,6 +316,65 @@ def test_textured_render_bit_identical_to_oracle(gpu_ctx, seed_offset, spp_xy):
     img, stats = gpu_ctx.render(64, 64)
     assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
     assert stats.variance == ref_var
+
+
+@pytest.mark.parametrize("seed_offset,spp_xy", [(3, (4, 4)), (7, (2, 3))])
+def test_bump_mapped_render_bit_identical_to_oracle(gpu_ctx, seed_offset, spp_xy):
+    """Bump maps (image and constant heights, uv scales, splayed vertex normals
+    whose uv derivatives take part) on matte, plastic, translucent and rough
+    glass, with textured reflectance and transmittance on glass and diffuse
+    transmission: bit-identical to the oracle with correctly rounded
+    trigonometry."""
+    s = FlatScene.read(golden("cornell_bump_64.yfs"))
+    s.config["rng_seed_offset"] = seed_offset
+    s.config["x_pixel_sample_count"], s.config["y_pixel_sample_count"] = spp_xy
+    ref, ref_var = oracle.render(s, threads=8, correctly_rounded_trig=True)
+    gpu_ctx.upload_scene(s)
+    img, stats = gpu_ctx.render(64, 64)
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    assert stats.variance == ref_var
+
+
+def test_constant_bump_with_delta_materials_bit_identical_to_oracle(gpu_ctx):
+    """A constant bump height reads no ray differentials, so it may sit on
+    delta materials: the mirror and the smooth glass reflect and refract about
+    the bumped normal, bit-identical to the oracle."""
+    s = constant_bumps_with_delta_materials()
+    ref, ref_var = oracle.render(s, threads=8, correctly_rounded_trig=True)
+    gpu_ctx.upload_scene(s)
+    img, stats = gpu_ctx.render(64, 64)
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    assert stats.variance == ref_var
+
+
+def test_bump_maps_refused_where_they_are_not_evaluated(gpu_ctx):
+    """The static, batched and guided renders and the direct-lighting algorithm
+    refuse bump maps; a mix's sub-material may not have one; a texture in a
+    slot the material does not read is refused."""
+    from yar_gb300 import native
+    s = constant_bumps_with_delta_materials()
+    gpu_ctx.upload_scene(s)
+    with pytest.raises(native.YarError):
+        gpu_ctx.render_batch([s])
+    with pytest.raises(native.YarError):
+        gpu_ctx.guided_render(64, 64, passes=1)
+    d = constant_bumps_with_delta_materials()
+    d.config["rendering_algorithm"] = 0
+    gpu_ctx.upload_scene(d)
+    with pytest.raises(native.YarError):
+        gpu_ctx.render(64, 64)
+    t = FlatScene.read(golden("cornell_texture_64.yfs"))
+    k = int(np.nonzero(t.materials["reflectance_texture"])[0][0])
+    t.materials["transmittance_texture"][k] = t.materials["reflectance_texture"][k]  # diffuse has no such slot
+    gpu_ctx.upload_scene(t)
+    with pytest.raises(native.YarError):
+        gpu_ctx.render(64, 64)
+    x = FlatScene.read(golden("cornell_mix_64.yfs"))
+    mix = int(np.nonzero(x.materials["type"] == native.MATERIAL_MIX)[0][0])
+    x.materials["bump"][int(x.materials["mix_materials"][mix][0])] = 1
+    gpu_ctx.upload_scene(x)
+    with pytest.raises(native.YarError):
+        gpu_ctx.render(64, 64)
 
 
 def test_textured_scene_refused_where_textures_are_not_evaluated(gpu_ctx):

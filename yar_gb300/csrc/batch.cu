@@ -310,7 +310,7 @@ int render_batch(yar_gpu_ctx* ctx, const yar_flat_scene* const* scenes, uint32_t
         if ((rc = prepare_render_params(s.sub, s.p)) != YAR_OK)
             return fail(ctx, rc, "scene " + std::to_string(i) + ": " + yar_gpu_last_error(s.sub));
         if (s.p.textured)
-            return fail(ctx, YAR_ERR_UNSUPPORTED, "scene " + std::to_string(i) + ": batched renders do not evaluate image textures");
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "scene " + std::to_string(i) + ": batched renders do not evaluate image textures or bump maps");
         if (s.sub->render.config.rendering_algorithm == 0)
             return fail(ctx, YAR_ERR_UNSUPPORTED, "scene " + std::to_string(i) +
                                                       ": batched renders run the path tracer only (rendering_algorithm 1)");

@@ -155,7 +155,7 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
         return fail(ctx, YAR_ERR_UNSUPPORTED, "the guided render runs the path tracer only (rendering_algorithm 1)");
     Render_Params p;
     if (int rc0 = prepare_render_params(ctx, p)) return rc0;
-    if (p.textured) return fail(ctx, YAR_ERR_UNSUPPORTED, "the guided render does not evaluate image textures");
+    if (p.textured) return fail(ctx, YAR_ERR_UNSUPPORTED, "the guided render does not evaluate image textures or bump maps");
     if (!spp_side && (p.filter_radius > 0.5f || p.filter_type != 0))
         return fail(ctx, YAR_ERR_UNSUPPORTED, "guided passes: box filter of radius <= 0.5 only (one pixel per sample)");
     p.nx = p.ny = p.spp = 1;

@@ -63,6 +63,12 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
         d.reflectance = Col{m.reflectance[0], m.reflectance[1], m.reflectance[2]};
         d.texture = m.reflectance_texture;
         d.texture_scale = make_float2(m.reflectance_uv_scale[0], m.reflectance_uv_scale[1]);
+        d.texture2 = m.transmittance_texture;
+        d.texture2_scale = make_float2(m.transmittance_uv_scale[0], m.transmittance_uv_scale[1]);
+        d.bump = m.bump;
+        d.bump_height = m.bump_height;
+        d.bump_texture = m.bump == 2 ? m.bump_texture : 0u;
+        d.bump_scale = make_float2(m.bump_uv_scale[0], m.bump_uv_scale[1]);
         d.transmittance = Col{m.transmittance[0], m.transmittance[1], m.transmittance[2]};
         d.eta_t = Col{m.eta[0], m.eta[1], m.eta[2]};
         d.k_t = Col{m.k[0], m.k[1], m.k[2]};
@@ -85,6 +91,7 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
                                            m.diffuse[2] * m.reflectance[2]});
             d.transmittance = clamp_unit(Col{m.diffuse[0] * m.transmittance[0], m.diffuse[1] * m.transmittance[1],
                                              m.diffuse[2] * m.transmittance[2]});
+            d.extra = rgb(m.diffuse);  // the scale, for textured reflectance and transmittance
         } else if (m.type == YAR_MATERIAL_PBRT3_TRANSLUCENT) {  // roughness always remapped
             d.extra = rgb(m.diffuse);
             d.specular = rgb(m.specular);
@@ -318,24 +325,36 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
                 texs[i] = make_uint2(t.first_mip, t.mip_count);
             }
             // The EWA footprint walks integer texel coordinates held in floats:
-            // refuse uv ranges whose texel coordinates reach 2^22.
+            // refuse uv ranges whose texel coordinates reach 2^22 (a bump map's
+            // finite-difference lookups step past the uv by the footprint, which
+            // only grazing hits make large; there the reference's own float
+            // counters stop advancing, and the device's loops stay bounded).
             for (uint32_t o = 0; o < scene->object_count; o++) {
                 const yar_object_desc& ob = scene->objects[o];
                 if (ob.material_index < 0 || (uint32_t)ob.material_index >= scene->material_count) continue;
                 const yar_material_desc& md = scene->materials[ob.material_index];
-                if (!md.reflectance_texture || md.reflectance_texture > scene->texture_count) continue;
-                const yar_texture_desc& t = scene->textures[md.reflectance_texture - 1];
-                const yar_texture_mip_desc& top = scene->texture_mips[t.first_mip];
                 const yar_mesh_desc& mesh = scene->meshes[ob.mesh_index];
                 if (!mesh.uvs) continue;
-                float uv_max = 0.f;
-                for (uint64_t k = 0; k < 2ull * mesh.vertex_count; k++) uv_max = std::max(uv_max, std::fabs(mesh.uvs[k]));
-                const double reach = (double)uv_max *
-                                     std::max(std::fabs(md.reflectance_uv_scale[0]), std::fabs(md.reflectance_uv_scale[1])) *
-                                     std::max(top.width, top.height);
-                if (!(reach < (double)(1 << 22)))
-                    return fail(ctx, YAR_ERR_UNSUPPORTED, "texture coordinates of object " + std::to_string(o) +
-                                                              " reach 2^22 texels");
+                const uint32_t slot_texture[3] = {md.reflectance_texture, md.transmittance_texture,
+                                                  md.bump == 2 ? md.bump_texture : 0u};
+                const float* slot_scale[3] = {md.reflectance_uv_scale, md.transmittance_uv_scale, md.bump_uv_scale};
+                float uv_max = -1.f;
+                for (int k = 0; k < 3; k++) {
+                    if (!slot_texture[k] || slot_texture[k] > scene->texture_count) continue;
+                    if (uv_max < 0.f) {
+                        uv_max = 0.f;
+                        for (uint64_t j = 0; j < 2ull * mesh.vertex_count; j++)
+                            uv_max = std::max(uv_max, std::fabs(mesh.uvs[j]));
+                    }
+                    const yar_texture_desc& t = scene->textures[slot_texture[k] - 1];
+                    const yar_texture_mip_desc& top = scene->texture_mips[t.first_mip];
+                    const double reach = (double)uv_max *
+                                         std::max(std::fabs(slot_scale[k][0]), std::fabs(slot_scale[k][1])) *
+                                         std::max(top.width, top.height);
+                    if (!(reach < (double)(1 << 22)))
+                        return fail(ctx, YAR_ERR_UNSUPPORTED, "texture coordinates of object " + std::to_string(o) +
+                                                                  " reach 2^22 texels");
+                }
             }
         }
         // do_EWA's weights exp(-2 x), x = i / 255 (src/ref/image_texture.cpp:503-512), correctly rounded
@@ -677,7 +696,7 @@ int render_run_static(yar_gpu_ctx* ctx, float* rgb_out_device, yar_render_stats*
     p.exact_tail = (p.stream_hi == 0 && p.n1d > 0) ? 1 : 0;
     Render_Params p_wave = p;
     p_wave.exact_tail = 2;
-    if (p.textured) return fail(ctx, YAR_ERR_UNSUPPORTED, "the static render does not evaluate image textures");
+    if (p.textured) return fail(ctx, YAR_ERR_UNSUPPORTED, "the static render does not evaluate image textures or bump maps");
 
     cudaSetDevice(ctx->device);
     if (ctx->device < 0 || ctx->device >= 64) return fail(ctx, YAR_ERR_INVALID, "device ordinal above 63");

@@ -156,7 +156,8 @@ enum : uint32_t { kDeltaNone = 0, kDeltaReflector = 1, kDeltaRefractor = 2, kDel
 // Material constants as the BSDF constructors evaluate them (src/ref/bsdf.cpp:60-66,
 // :146-158, :205-213, :268-294, :427-438); alpha values are computed on the host
 // with the reference's roughness remapping.  Plastic and coated diffuse keep
-// their diffuse reflectance in `reflectance` and their r0 in `transmittance`.
+// their diffuse reflectance in `reflectance` and their r0 in `transmittance`;
+// diffuse transmission keeps its scale in `extra` (for textured slots).
 struct Material_Dev {
     uint32_t type;
     float alpha_x, alpha_y, alpha;
@@ -175,8 +176,15 @@ struct Material_Dev {
     float mix_lum;          // mix: luminance(amount), unclamped (the Scaled_BSDF factor)
     Col mix_coeff;          // mix: White - amount
     uint32_t has_bsdf;      // initialize_scattering creates a BSDF: some layer is not delta
-    uint32_t texture;       // diffuse: 1 + the reflectance's texture (0: the constant)
+    uint32_t texture;       // 1 + the reflectance's texture (0: the constant); diffuse, plastic,
+                            // coated diffuse, glass, diffuse transmission
     float2 texture_scale;   // its uv scale
+    uint32_t texture2;      // 1 + the transmittance's texture; glass, diffuse transmission
+    float2 texture2_scale;
+    uint32_t bump;          // bump map: 0 none, 1 constant height, 2 texture (its luminance)
+    float bump_height;      // bump 1: the height
+    uint32_t bump_texture;  // bump 2: 1 + the texture
+    float2 bump_scale;      // bump 2: its uv scale
 };
 
 struct Bsdf {

@@ -110,7 +110,7 @@ struct Render_Params {
     // tail, first phase (a path that might draw past the budget at its next
     // vertex is deferred); 2 = exact tail, waves (draws are counted per path).
     int32_t exact_tail;
-    int32_t textured;  // some diffuse reflectance is an image texture
+    int32_t textured;  // some material has an image texture or a bump map
 };
 
 struct Path_State {
@@ -937,16 +937,25 @@ __device__ void uv_derivatives(const Shading& sc, V3 o, V3 dx, V3 dy, V3 dpdu, V
     }
 }
 
-// A textured diffuse reflectance at a hit (evaluate_rgb_parameter with the
-// shading context's uv and derivatives, parameter_evaluation.cpp:84-89): the
-// camera ray's differential rays, one pixel over and scaled to the sample's
-// footprint (src/ref/reference_renderer.cpp:367-378), give the derivatives at
-// bounce 0; later vertices have none.
-__device__ __forceinline__ Col textured_reflectance(const Render_Params& p, const Scene_Dev& S, const Path_State& ps, uint32_t slot,
-                                    int bounce, const Shading& sc, const Material_Dev& mat, float4 h4, uint2 h2) {
-    float2 uv = make_float2(0.f, 0.f), duvdx = make_float2(0.f, 0.f), duvdy = make_float2(0.f, 0.f);
+// Where a hit looks its textures up: the shading context's uv, world-space
+// dpdu/dpdv and uv derivatives (zero without uvs).
+struct Tex_Site {
+    float2 uv, duvdx, duvdy;
     V3 dpdu, dpdv;
-    if (texture_geometry(S, h2.y, h2.x, h4.y, h4.z, h4.w, uv, dpdu, dpdv) && bounce == 0) {
+    bool has_uv;
+};
+
+// The texture site of a hit (init_from_triangle_mesh_intersection and
+// calculate_dxdy_derivatives): the camera ray's differential rays, one pixel
+// over and scaled to the sample's footprint (src/ref/reference_renderer.cpp:367-378),
+// give the derivatives at bounce 0; later vertices have none.
+__device__ __noinline__ void texture_site(const Render_Params& p, const Scene_Dev& S, const Path_State& ps,
+                                          uint32_t slot, int bounce, const Shading& sc, float4 h4, uint2 h2,
+                                          Tex_Site& t) {
+    float2 uv = make_float2(0.f, 0.f), duvdx = make_float2(0.f, 0.f), duvdy = make_float2(0.f, 0.f);
+    V3 dpdu = v3(0.f, 0.f, 0.f), dpdv = v3(0.f, 0.f, 0.f);
+    t.has_uv = texture_geometry(S, h2.y, h2.x, h4.y, h4.z, h4.w, uv, dpdu, dpdv);
+    if (t.has_uv && bounce == 0) {
         const uint32_t lp = slot / (uint32_t)p.spp, k = slot - lp * (uint32_t)p.spp;
         int x, y;
         pixel_stream(p, ps.chunk_first + lp, x, y);
@@ -963,9 +972,136 @@ __device__ __forceinline__ Col textured_reflectance(const Render_Params& p, cons
         dy = divs(dy, len(dy));
         uv_derivatives(sc, o, dx, dy, dpdu, dpdv, duvdx, duvdy);
     }
-    const float su = mat.texture_scale.x, sv = mat.texture_scale.y;
-    return texture_ewa(S, __ldg(S.textures + mat.texture - 1), uv.x * su, uv.y * sv,
-                       make_float2(duvdx.x * su, duvdx.y * sv), make_float2(duvdy.x * su, duvdy.y * sv));
+    t.uv = uv;
+    t.duvdx = duvdx;
+    t.duvdy = duvdy;
+    t.dpdu = dpdu;
+    t.dpdv = dpdv;
+}
+
+// evaluate_texture_parameter (parameter_evaluation.cpp:10-31): the uv and its
+// derivatives scaled, then EWA with repeat wrapping.
+__device__ __forceinline__ Col texture_lookup(const Scene_Dev& S, const Tex_Site& t, uint32_t texture, float2 scale,
+                                              float u, float v) {
+    return texture_ewa(S, __ldg(S.textures + texture - 1), u * scale.x, v * scale.y,
+                       make_float2(t.duvdx.x * scale.x, t.duvdx.y * scale.y),
+                       make_float2(t.duvdy.x * scale.x, t.duvdy.y * scale.y));
+}
+
+// The bump map's height at (u, v): the constant, or the luminance of the
+// texture (evaluate_leaf_parameter_float, parameter_evaluation.cpp:46-55;
+// ColorRGB::luminance, src/lib/color.h:74-76).
+__device__ __forceinline__ float bump_height_at(const Scene_Dev& S, const Tex_Site& t, const Material_Dev& m, float u,
+                                                float v) {
+    if (m.bump == 1) return m.bump_height;
+    const Col c = texture_lookup(S, t, m.bump_texture, m.bump_scale, u, v);
+    return 0.2126729f * c.r + 0.7151522f * c.g + 0.0721750f * c.b;
+}
+
+// Shading_Context::apply_bump_map (src/ref/shading_context.cpp:419-462) with the
+// geometry it reads: the normal's uv derivatives (init_from_triangle_mesh_intersection,
+// :225-238; to world space and flipped with the normal, :102-109, :128-133) and
+// the shading frame's second tangent (:150-167).  Heights at the uv and one
+// footprint step along u and v perturb the tangents; the normal is rebuilt
+// from them, turned into the geometric normal's hemisphere and adjusted.
+__device__ __noinline__ void apply_bump(const Scene_Dev& S, const Material_Dev& m, const Tex_Site& t,
+                                        uint32_t object, uint32_t prim, float b0, float b1, float b2, Shading& sc) {
+    const float4* orec = S.ds.objects + 6 * (size_t)object;
+    const uint32_t tri_offset = __float_as_uint(__ldg(orec + 4).w);
+    const size_t g = (size_t)tri_offset + prim;
+    const float4 h0 = __ldg(S.shading + 4 * g), h1 = __ldg(S.shading + 4 * g + 1);
+    const float4 h2 = __ldg(S.shading + 4 * g + 2), h3 = __ldg(S.shading + 4 * g + 3);
+    const uint32_t flags = __float_as_uint(h3.w);
+    const float4 q0 = __ldg(S.ds.tris + 3 * g), q1 = __ldg(S.ds.tris + 3 * g + 1), q2 = __ldg(S.ds.tris + 3 * g + 2);
+    const V3 p0 = v3(q0.x, q0.y, q0.z), p1 = v3(q1.x, q1.y, q1.z), p2 = v3(q2.x, q2.y, q2.z);
+    // the object-space normal as init_shading interpolates it, for its length after the transform
+    V3 normal = normalized(cross(p1 - p0, p2 - p0));
+    if (flags & 4u) normal = -normal;
+    const V3 vn0 = (flags & 1u) ? v3(h0.x, h0.y, h0.z) : v3(0.f, 0.f, 0.f);
+    const V3 vn1 = (flags & 1u) ? v3(h1.x, h1.y, h1.z) : v3(0.f, 0.f, 0.f);
+    const V3 vn2 = (flags & 1u) ? v3(h2.x, h2.y, h2.z) : v3(0.f, 0.f, 0.f);
+    if (flags & 1u) {
+        const V3 in = bary(vn0, vn1, vn2, b0, b1, b2);
+        if (len2(in) != 0.f) normal = normalized(in);
+    }
+    V3 dndu = v3(0.f, 0.f, 0.f), dndv = v3(0.f, 0.f, 0.f);
+    if (t.has_uv) {
+        // uvs: u0 = h0.w, v0 = h1.w, u1 = h2.w, v1 = h3.x, u2 = h3.y, v2 = h3.z
+        const float a00 = h2.w - h0.w, a01 = h3.x - h1.w, a10 = h3.y - h0.w, a11 = h3.z - h1.w;
+        const V3 bn0 = vn1 - vn0, bn1 = vn2 - vn0;
+        const float det = a00 * a11 - a01 * a10;  // solve_linear_system_2x2, src/lib/math.cpp:8-16
+        if (det != 0.f) {
+            const float inv_det = 1.f / det;
+            dndu = mul(mul(bn0, a11) - mul(bn1, a01), inv_det);
+            dndv = mul(mul(bn0, -a10) + mul(bn1, a00), inv_det);
+        }
+        if (fabsf(det) < 1e-9f) {  // pbrt's approximation
+            const V3 dn = cross(bn1, bn0);
+            if (len2(dn) == 0.f) {
+                dndu = v3(0.f, 0.f, 0.f);
+                dndv = v3(0.f, 0.f, 0.f);
+            } else {
+                dndu = coordinate_axis(dn);
+                dndv = cross(dn, dndu);
+            }
+        }
+    }
+    const float4* rrec = S.obj_render + 7 * (size_t)object;
+    const float4 n0 = __ldg(rrec + 3), n1 = __ldg(rrec + 4), n2 = __ldg(rrec + 5);
+    const float inv_length = 1 / len(xform_vector(n0, n1, n2, normal));
+    dndu = mul(xform_vector(n0, n1, n2, dndu), inv_length);
+    dndv = mul(xform_vector(n0, n1, n2, dndv), inv_length);
+    if (sc.flipped) {
+        dndu = -dndu;
+        dndv = -dndv;
+    }
+    // the shading frame's second tangent before the bump
+    V3 dpdv_shading;
+    if (!t.has_uv) {
+        dpdv_shading = cross(sc.n, sc.dpdu_shading);
+    } else if (fabsf(dot(sc.n, sc.ng) - 1.f) < 1e-6f) {
+        dpdv_shading = t.dpdv;
+    } else {
+        const V3 tv = cross(t.dpdv, sc.n);
+        dpdv_shading = mul(normalized(cross(sc.n, tv)), len(t.dpdv));
+    }
+    const float height = bump_height_at(S, t, m, t.uv.x, t.uv.y);
+    float du = 0.5f * (fabsf(t.duvdx.x) + fabsf(t.duvdy.x));
+    if (du == 0.f) du = 0.0005f;
+    const float height_du = bump_height_at(S, t, m, t.uv.x + du, t.uv.y + 0.f);
+    float dv = 0.5f * (fabsf(t.duvdx.y) + fabsf(t.duvdy.y));
+    if (dv == 0.f) dv = 0.0005f;
+    const float height_dv = bump_height_at(S, t, m, t.uv.x + 0.f, t.uv.y + dv);
+    const V3 original_shading_normal = sc.flipped ? -sc.n : sc.n;
+    const float du_scale = m.bump == 2 ? m.bump_scale.x : 1.f;
+    const float dv_scale = m.bump == 2 ? m.bump_scale.y : 1.f;
+    const V3 dpdu_b = (sc.dpdu_shading + mul(original_shading_normal, (height_du - height) / (du * du_scale))) +
+                      mul(mul(dndu, du_scale), height);
+    const V3 dpdv_b = (dpdv_shading + mul(original_shading_normal, (height_dv - height) / (dv * dv_scale))) +
+                      mul(mul(dndv, dv_scale), height);
+    V3 n = normalized(cross(dpdu_b, dpdv_b));
+    if (dot(n, sc.ng) < 0) n = -n;
+    sc.n = adjust_shading_normal(sc.wo, sc.ng, n);
+    sc.dpdu_shading = dpdu_b;
+}
+
+// The textured reflectance and transmittance of a BSDF (the constructors'
+// evaluate_rgb_parameter calls, src/ref/bsdf.cpp:89-103, :205-213, :268-276,
+// :427-438): diffuse transmission scales and clamps them.
+__device__ __noinline__ void textured_bsdf_params(const Scene_Dev& S, const Tex_Site& t, const Material_Dev& m,
+                                                  Bsdf& f) {
+    auto clamp_unit = [](Col c) {
+        auto c1 = [](float v) { return v < 0.f ? 0.f : (1.f < v ? 1.f : v); };
+        return col(c1(c.r), c1(c.g), c1(c.b));
+    };
+    if (m.texture) {
+        const Col r = texture_lookup(S, t, m.texture, m.texture_scale, t.uv.x, t.uv.y);
+        f.reflectance = m.type == YAR_MATERIAL_DIFFUSE_TRANSMISSION ? clamp_unit(m.extra * r) : r;
+    }
+    if (m.texture2) {
+        const Col r = texture_lookup(S, t, m.texture2, m.texture2_scale, t.uv.x, t.uv.y);
+        f.transmittance = m.type == YAR_MATERIAL_DIFFUSE_TRANSMISSION ? clamp_unit(m.extra * r) : r;
+    }
 }
 
 // ---------------------------------------------------------------- sphere lights
@@ -1106,6 +1242,17 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 const float2 un = next2d(dm);
 
                 const Material_Dev& mat = S.materials[oinfo.y];
+                // Image textures and bump maps read the hit's texture site; the bump
+                // map changes the shading frame before the delta check and the BSDF
+                // (check_for_delta_scattering_event applies it first,
+                // src/ref/delta_scattering.cpp:252-257; create_bsdf again, which
+                // gives the same frame).
+                Tex_Site site;
+                const bool textured = FULL && !GUIDED && (mat.texture | mat.texture2 | mat.bump) != 0u;
+                if (textured) {
+                    texture_site(p, S, ps, slot, bounce, sc, h4, h2, site);
+                    if (mat.bump) apply_bump(S, mat, site, h2.y, h2.x, h4.y, h4.z, h4.w, sc);
+                }
                 // Shading_Context::initialize_scattering (shading_context.cpp:174-186): a
                 // delta event may be chosen (for the pbrt3 uber material per sample,
                 // which remaps u_scatter); the BSDF exists unless every layer is delta.
@@ -1120,8 +1267,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 uint32_t pend = 0;
                 if (delta == 0 || bsdf_prob != 0.f) {
                     make_bsdf(sc, mat, S.materials, f);
-                    if (FULL && !GUIDED && mat.texture)
-                        f.reflectance = textured_reflectance(p, S, ps, slot, bounce, sc, mat, h4, h2);
+                    if (textured && (mat.texture | mat.texture2) != 0u) textured_bsdf_params(S, site, mat, f);
                     // estimate_direct_lighting_from_single_sample (direct_lighting.cpp:522-578):
                     // the light int(u * total_light_count), point, spot and directional lights
                     // first, then the rectangular lights (the reference asserts the index is
@@ -1961,9 +2107,20 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
     }
     for (const yar_material_desc& m : R.host_materials) {
         if (m.other_textured_parameters)
-            return fail(ctx, YAR_ERR_UNSUPPORTED, "a material parameter other than a diffuse reflectance is a texture");
-        if (m.reflectance_texture && (m.type != YAR_MATERIAL_DIFFUSE || m.reflectance_texture > R.texture_count))
-            return fail(ctx, YAR_ERR_UNSUPPORTED, "image textures are implemented for diffuse reflectance only");
+            return fail(ctx, YAR_ERR_UNSUPPORTED,
+                        "a material parameter other than a reflectance, a transmittance or a bump map is a texture");
+        const bool reflectance_slot = m.type == YAR_MATERIAL_DIFFUSE || m.type == YAR_MATERIAL_PLASTIC ||
+                                      m.type == YAR_MATERIAL_COATED_DIFFUSE || m.type == YAR_MATERIAL_GLASS ||
+                                      m.type == YAR_MATERIAL_DIFFUSE_TRANSMISSION;
+        const bool transmittance_slot = m.type == YAR_MATERIAL_GLASS || m.type == YAR_MATERIAL_DIFFUSE_TRANSMISSION;
+        if ((m.reflectance_texture && !reflectance_slot) || (m.transmittance_texture && !transmittance_slot))
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "an image texture in a slot the material does not read");
+        if (m.reflectance_texture > R.texture_count || m.transmittance_texture > R.texture_count ||
+            (m.bump == 2 && (m.bump_texture == 0 || m.bump_texture > R.texture_count)))
+            return fail(ctx, YAR_ERR_INVALID, "a material names a texture the scene does not have");
+        if (m.bump > 2) return fail(ctx, YAR_ERR_INVALID, "bump map kind " + std::to_string(m.bump));
+        if (m.bump && m.type == YAR_MATERIAL_MIX)
+            return fail(ctx, YAR_ERR_UNSUPPORTED, "a mix material has no bump map");
         if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL && m.type != YAR_MATERIAL_GLASS &&
             m.type != YAR_MATERIAL_PLASTIC && m.type != YAR_MATERIAL_COATED_DIFFUSE &&
             m.type != YAR_MATERIAL_PERFECT_REFLECTOR && m.type != YAR_MATERIAL_PERFECT_REFRACTOR &&
@@ -1981,6 +2138,8 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
                 if (sm.type == YAR_MATERIAL_MIX || sm.type == YAR_MATERIAL_PBRT3_UBER ||
                     (sm.type == YAR_MATERIAL_GLASS && !(sm.u_roughness > 0.f)))
                     return fail(ctx, YAR_ERR_UNSUPPORTED, "mix of a mix, an uber or a smooth glass material");
+                if (sm.bump)
+                    return fail(ctx, YAR_ERR_UNSUPPORTED, "a mix of a bump-mapped material");
                 delta_subs += sm.type == YAR_MATERIAL_PERFECT_REFLECTOR || sm.type == YAR_MATERIAL_PERFECT_REFRACTOR;
             }
             if (delta_subs == 2) return fail(ctx, YAR_ERR_UNSUPPORTED, "mix of two pure delta materials");
@@ -2075,18 +2234,22 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
         if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL &&
             !(m.type == YAR_MATERIAL_GLASS && m.u_roughness > 0.f))
             p.full_shading = 1;
-    // Image textures (diffuse reflectance): FULL shading; the differential rays
-    // of delta bounces and of the direct-lighting algorithm are not restated.
-    bool delta_materials = false;
+    // Image textures and bump maps: FULL shading.  The differential rays of
+    // delta bounces are not restated, so image textures (which read them) and
+    // delta materials are not mixed; a constant bump height reads none.  The
+    // direct-lighting algorithm evaluates neither.
+    bool delta_materials = false, image_textures = false;
     for (const yar_material_desc& m : R.host_materials) {
-        if (m.reflectance_texture) p.textured = 1;
+        if (m.reflectance_texture || m.transmittance_texture || m.bump == 2) image_textures = true;
+        if (m.reflectance_texture || m.transmittance_texture || m.bump) p.textured = 1;
         delta_materials = delta_materials || m.type == YAR_MATERIAL_PERFECT_REFLECTOR ||
                           m.type == YAR_MATERIAL_PERFECT_REFRACTOR ||
                           (m.type == YAR_MATERIAL_GLASS && !(m.u_roughness > 0.f)) ||
                           m.type == YAR_MATERIAL_PBRT3_UBER || m.type == YAR_MATERIAL_MIX;
     }
-    if (p.textured && (c.rendering_algorithm == 0 || delta_materials))
-        return fail(ctx, YAR_ERR_UNSUPPORTED, "image textures with delta materials or the direct-lighting algorithm");
+    if ((image_textures && delta_materials) || (p.textured && c.rendering_algorithm == 0))
+        return fail(ctx, YAR_ERR_UNSUPPORTED,
+                    "image textures with delta materials, or textures or bump maps with the direct-lighting algorithm");
     if (p.textured) p.full_shading = 1;
     p.seed_offset = (uint32_t)c.rng_seed_offset;
     return YAR_OK;
