@@ -152,6 +152,24 @@ def test_render_past_the_dimension_budget_bit_identical(gpu_ctx, name, maxb, rr,
     assert stats.variance == ref_var
 
 
+@pytest.mark.parametrize("name,maxb,past_budget", [("cornell_c1_64", 8, False), ("cornell_bump_64", 8, False),
+                                                  ("cornell_delta_64", 16, True), ("cornell_envmap_64", 13, True)])
+def test_device_driven_bounces_match_host_driven(gpu_ctx, name, maxb, past_budget):
+    """The first render of a scene reads each bounce's queue lengths on the host
+    (and tunes the traversal kernels); later renders drive the bounces, and the
+    exact tail's waves, from the device.  Both give the same image, variance and
+    ray counts, bit for bit."""
+    s = _past_budget_scene(name) if past_budget else FlatScene.read(golden(name + ".yfs"))
+    s.config["max_light_bounces"] = maxb
+    gpu_ctx.upload_scene(s)
+    img1, st1 = gpu_ctx.render(64, 64)
+    img2, st2 = gpu_ctx.render(64, 64)
+    assert np.array_equal(img1.view(np.uint32), img2.view(np.uint32))
+    assert st1.variance == st2.variance
+    assert (st1.rays_closest, st1.rays_any, st1.paths) == (st2.rays_closest, st2.rays_any, st2.paths)
+    assert st1.kernel_launches != st2.kernel_launches  # the second render ran the other loop
+
+
 @pytest.mark.parametrize("maxb,rr,seed_offset", [(1, 3, 0), (2, 1, 5), (3, 2, 9), (8, 1, 2)])
 def test_render_delta_paths_match_oracle(gpu_ctx, maxb, rr, seed_offset):
     """Mirror, smooth glass and a perfect-refractor ceiling: delta vertices at

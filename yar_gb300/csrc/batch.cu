@@ -26,16 +26,6 @@ namespace yar {
 
 namespace {
 
-// counters of a branch: [0] next ext, [1] shadow, [2] probe, [3] error,
-// [4..6] ray hand-out, [7] this bounce's extend count; rays: [0] closest, [1] any
-__global__ void bounce_begin_kernel(uint32_t* counters, uint32_t first_paths, unsigned long long* rays) {
-    const uint32_t prev_ext = counters[7], prev_shadow = counters[1], prev_probe = counters[2];
-    rays[0] += prev_ext + prev_probe;
-    rays[1] += prev_shadow;
-    counters[7] = first_paths ? first_paths : counters[0];
-    counters[0] = counters[1] = counters[2] = 0;
-}
-
 __global__ void stamp_kernel(unsigned long long* out) {
     unsigned long long t;
     asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));

@@ -303,6 +303,7 @@ extern "C" int yar_gpu_upload_scene(yar_gpu_ctx* ctx, const yar_flat_scene* scen
         ctx->cast_kernel[k] = ctx->forced_kernel;
         for (int b = 0; b < yar_gpu_ctx::kBounceBuckets; b++) ctx->render_kernel[k][b] = ctx->forced_kernel;
     }
+    ctx->render_tuned = ctx->forced_kernel >= 0;
     ctx->has_scene = true;
     return YAR_OK;
 }

@@ -93,6 +93,9 @@ struct yar_gpu_ctx {
     // renders: per ray kind and bounce (bounces past the last share its entry)
     static constexpr int kBounceBuckets = 5;
     int render_kernel[2][kBounceBuckets] = {{-1, -1, -1, -1, -1}, {-1, -1, -1, -1, -1}};
+    // a render of the current scene has run with host-read queue lengths (and
+    // tuned the buckets it filled): later renders drive their bounces on the device
+    bool render_tuned = false;
 
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
 

@@ -418,13 +418,16 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
     const uint64_t chunk_pixels = std::max<uint64_t>(1, std::min<uint64_t>(pixels, budget / p.spp));
     const uint64_t cap = chunk_pixels * p.spp;  // paths per chunk
 
-    // scratch: everything sized by the largest chunk, allocated per call
+    // scratch: everything sized by the largest chunk; a buffer of the last
+    // call is kept when it is large enough (cudaMalloc and cudaFree synchronise)
     std::vector<Device_Buffer>& B = ctx->render_scratch;
-    for (Device_Buffer& b : B) device_free(b);
-    B.assign(36, Device_Buffer{});
+    if (B.size() != 37) {
+        for (Device_Buffer& b : B) device_free(b);
+        B.assign(37, Device_Buffer{});
+    }
     int rc = YAR_OK;
     auto alloc = [&](int i, size_t bytes) {
-        if (rc == YAR_OK) rc = device_alloc(ctx, B[i], bytes);
+        if (rc == YAR_OK && !(B[i].ptr && B[i].bytes >= bytes)) rc = device_alloc(ctx, B[i], bytes);
     };
     alloc(0, samples * sizeof(float4));                    // radiance
     alloc(1, samples * sizeof(float2));                    // image-plane samples
@@ -464,6 +467,7 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
         alloc(34, chunk_pixels * sizeof(uint32_t));        // stream position per pixel
         alloc(35, 2 * sizeof(uint32_t));                   // largest count, stray-draw flag
     }
+    alloc(36, 2 * sizeof(unsigned long long));             // closest and any rays (device-driven bounces)
     if (rc != YAR_OK) return rc;
 
     Path_State ps{dptr<float4>(B[4]), dptr<float4>(B[5]), dptr<uint32_t>(B[6]), dptr<uint4>(B[7]),
@@ -492,6 +496,13 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
     cudaError_t e = cudaMemsetAsync(q.counters, 0, 8 * sizeof(uint32_t), st);
     uint64_t rays_closest = 0, rays_any = 0;
     uint32_t launches = 0;
+    // Bounces are driven from the device once a render of this scene has tuned
+    // the traversal kernels with host-read queue lengths (the guided render's
+    // hook reads them too): no host round trip until the render ends, or per
+    // chunk with the exact tail (its wave count).
+    const bool device_driven = !guide && ctx->render_tuned;
+    unsigned long long* rays_dev = dptr<unsigned long long>(B[36]);
+    if (device_driven && e == cudaSuccess) e = cudaMemsetAsync(rays_dev, 0, 2 * sizeof(unsigned long long), st);
     // The bounce loop over extend queue 0 of `count` paths; bounce0 picks the
     // traversal kernels.  Sets e; returns a YAR_ERR_* for a traversal overflow.
     auto run_bounces = [&](const Render_Params& pp, uint32_t count, int bounce0) -> int {
@@ -531,13 +542,69 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
         }
         return YAR_OK;
     };
+    // The same bounces with the queue lengths on the device: every iteration
+    // runs (the kernels exit on an empty queue); first_paths = 0 takes the
+    // first count from counters[0] (a tail wave's queue).
+    auto run_bounces_device = [&](const Render_Params& pp, uint32_t first_paths, uint32_t max_paths, int bounce0) {
+        Queues qd = q;
+        qd.ext_count = q.counters + 7;
+        const int grid = grid_for(max_paths);
+        int cur = 0;
+        for (int it = 0; it <= p.max_bounces + 1 && e == cudaSuccess; it++) {
+            const int bounce = bounce0 + it;
+            bounce_begin_kernel<<<1, 1, 0, st>>>(q.counters, it == 0 ? first_paths : 0u, rays_dev);
+            Cast_Args a;
+            a.rays = q.ext_rays[cur];
+            a.count = q.counters + 7;
+            a.n_max = max_paths;
+            a.next_ray = q.counters + 4;
+            a.err = reinterpret_cast<int*>(q.counters + 3);
+            a.hit4 = q.ext_hit4;
+            a.hit2 = q.ext_hit2;
+            e = launch_extend(ctx->ds, a, render_choice(ctx, 0, bounce), st);
+            if (e != cudaSuccess) break;
+            launch_shade<false>(pp, grid, st, S, cur, max_paths, dptr<float>(B[2]), dptr<float2>(B[3]), ps, qd,
+                                Guide_Shade{});
+            Cast_Args sh;
+            sh.rays = q.shd_rays;
+            sh.count = q.counters + 1;
+            sh.n_max = max_paths;
+            sh.perm = q.shd_slot;
+            sh.next_ray = q.counters + 5;
+            sh.err = reinterpret_cast<int*>(q.counters + 3);
+            sh.occluded = ps.occluded;
+            e = launch_shadow(ctx->ds, sh, render_choice(ctx, 1, bounce), st);
+            if (e != cudaSuccess) break;
+            Cast_Args pr;
+            pr.rays = q.prb_rays;
+            pr.count = q.counters + 2;
+            pr.n_max = max_paths;
+            pr.perm = q.prb_slot;
+            pr.next_ray = q.counters + 6;
+            pr.err = reinterpret_cast<int*>(q.counters + 3);
+            pr.hit4 = ps.probe_hit4;
+            pr.hit2 = ps.probe_hit2;
+            e = launch_extend(ctx->ds, pr, render_choice(ctx, 0, bounce), st);
+            if (e != cudaSuccess) break;
+            connect_kernel<<<grid, kBlock, 0, st>>>(pp, S, q.ext_slot[cur], max_paths, ps, nullptr, q.counters + 7);
+            launches += 6;
+            cur ^= 1;
+        }
+        bounce_begin_kernel<<<1, 1, 0, st>>>(q.counters, 0u, rays_dev);  // adds the last bounce's rays
+        launches++;
+        if (e == cudaSuccess) e = cudaGetLastError();
+    };
     for (uint64_t first = 0; first < pixels && e == cudaSuccess; first += chunk_pixels) {
         const uint32_t cp = (uint32_t)std::min<uint64_t>(chunk_pixels, pixels - first);
         const uint32_t paths = cp * (uint32_t)p.spp;
         ps.chunk_first = (uint32_t)first;
         launch_generate(p, (uint32_t)first, cp, dptr<float>(B[2]), dptr<float>(B[3]), image_samples, ps, q, st);
         launches++;
-        if (int rc1 = run_bounces(p, paths, 0)) return rc1;
+        if (device_driven) {
+            run_bounces_device(p, paths, paths, 0);
+        } else if (int rc1 = run_bounces(p, paths, 0)) {
+            return rc1;
+        }
         if (e != cudaSuccess) break;
         if (p.exact_tail) {
             uint32_t* list = dptr<uint32_t>(B[32]);
@@ -557,6 +624,10 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
                 tail_wave_kernel<<<grid_for(cp), kBlock, 0, st>>>(p_wave, (uint32_t)first, cp, wave, ps, q, list,
                                                                   deferred_count, stream_pos);
                 launches++;
+                if (device_driven) {  // at most one deferred sample per pixel and wave
+                    run_bounces_device(p_wave, 0u, cp, yar_gpu_ctx::kBounceBuckets - 1);
+                    continue;
+                }
                 uint32_t n = 0;
                 e = cudaMemcpyAsync(&n, q.counters, sizeof(n), cudaMemcpyDeviceToHost, st);
                 if (e == cudaSuccess) e = cudaStreamSynchronize(st);
@@ -621,8 +692,20 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
         e = cudaMemcpyAsync(rgb_out, B[29].ptr, (size_t)p.rw * p.rh * 3 * sizeof(float), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess)
         e = cudaMemcpyAsync(tile_var.data(), B[28].ptr, tile_var.size() * sizeof(double), cudaMemcpyDeviceToHost, st);
+    uint32_t err_word = 0;
+    unsigned long long rays_h[2] = {0, 0};
+    if (device_driven && e == cudaSuccess)
+        e = cudaMemcpyAsync(&err_word, q.counters + 3, sizeof(err_word), cudaMemcpyDeviceToHost, st);
+    if (device_driven && e == cudaSuccess) e = cudaMemcpyAsync(rays_h, rays_dev, sizeof(rays_h), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "render");
+    if (err_word) return fail(ctx, YAR_ERR_CAPACITY, "kd-tree traversal stack overflow");
+    if (device_driven) {
+        rays_closest = rays_h[0];
+        rays_any = rays_h[1];
+    } else if (!guide) {
+        ctx->render_tuned = true;
+    }
     if (tiles_out) tiles_out->tile_variance = tile_var;
     const double seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t_start).count();
     if (stats) {

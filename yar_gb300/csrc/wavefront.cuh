@@ -1739,6 +1739,19 @@ connect_kernel(Render_Params p, Scene_Dev S, const uint32_t* __restrict__ slots,
     }
 }
 
+// Device-driven bounces.  Queue counters: [0] next extend, [1] shadow, [2]
+// probe, [3] error, [4..6] ray hand-out, [7] this bounce's extend count; rays:
+// [0] closest, [1] any.  Turns the last bounce's appends into this bounce's
+// extend count (first_paths for a chunk's first bounce) and adds the last
+// bounce's rays.
+__global__ void bounce_begin_kernel(uint32_t* counters, uint32_t first_paths, unsigned long long* rays) {
+    const uint32_t prev_ext = counters[7], prev_shadow = counters[1], prev_probe = counters[2];
+    rays[0] += prev_ext + prev_probe;
+    rays[1] += prev_shadow;
+    counters[7] = first_paths ? first_paths : counters[0];
+    counters[0] = counters[1] = counters[2] = 0;
+}
+
 __global__ void __launch_bounds__(kBlock)
 finish_chunk_kernel(uint32_t paths, uint64_t first_sample, const Path_State ps, float4* __restrict__ radiance) {
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < paths; i += gridDim.x * blockDim.x)
