@@ -346,6 +346,9 @@ typedef struct yar_gpu_options {
     int32_t device;                 /* CUDA device ordinal */
     uint32_t max_batch_rays;        /* capacity of the host-buffer staging area (0 = 16M) */
     int32_t traversal_kernel;       /* YAR_TRAVERSAL_*: 0 = chosen per scene by timing */
+    uint32_t pipeline_chunk_rays;   /* host-buffer casts of two or more chunks of this many rays (0 = 4M,
+                                       at most 32 chunks) overlap their copies with the traversal once
+                                       the traversal kernel is chosen; UINT32_MAX: never */
 } yar_gpu_options;
 
 /* Traversal kernels (identical results, different speed): persistent warps

@@ -63,7 +63,8 @@ def test_struct_layouts_match_the_c_compiler(tmp_path):
                "yar_mesh_light_desc": native.MeshLightDesc, "yar_sphere_light_desc": native.SphereLightDesc,
                "yar_camera_desc": native.CameraDesc, "yar_render_config": native.RenderConfig,
                "yar_flat_scene": native.FlatSceneDesc, "yar_texture_desc": native.TextureDesc,
-               "yar_texture_mip_desc": native.TextureMipDesc}
+               "yar_texture_mip_desc": native.TextureMipDesc, "yar_gpu_options": native.GpuOptions,
+               "yar_hit_soa": native.HitSoa}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "yar_gpu.h"', "int main(void) {"]
     for name, cls in mirrors.items():
         lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (name, name))

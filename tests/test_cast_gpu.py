@@ -166,6 +166,53 @@ def test_device_buffers_match_host_buffers(gpu_ctx, medium_scene):
     assert np.array_equal(occ.cpu().numpy(), gpu_ctx.cast_any(rays))
 
 
+def test_pipelined_host_casts_match_device_casts(medium_scene):
+    """Host-buffer batches of two or more pipeline chunks overlap their copies
+    with the traversal (the first call of a scene tunes the kernel and runs
+    unpipelined): a ragged 3,145,745-ray batch in 1M-ray chunks gives the
+    device-buffer results bit for bit, without the output it leaves out (bary)."""
+    torch = pytest.importorskip("torch")
+    from yar_gb300 import native
+    import ctypes as C
+    from conftest import cuda_available
+    if not cuda_available():
+        pytest.skip("no CUDA device")
+    s = medium_scene
+    gpu_ctx = native.Context(0, pipeline_chunk_rays=1 << 20)
+    gpu_ctx.upload_scene(s)
+    lo, hi = scenes.scene_box(s)
+    n = 3 * (1 << 20) + 17
+    rays = scenes.random_rays(lo, hi, n, 31)
+    shadow = scenes.random_shadow_rays(lo, hi, n, 32)
+    first = gpu_ctx.cast_closest(rays)  # tunes
+    gpu_ctx.cast_any(shadow)
+    t = np.empty(n, np.float32)
+    prim = np.empty(n, np.uint32)
+    obj = np.empty(n, np.uint32)
+    hits = native.HitSoa(t.ctypes.data, prim.ctypes.data, obj.ctypes.data, None)
+    assert native.lib().yar_gpu_cast_closest(gpu_ctx._h, rays.ctypes.data, n, C.byref(hits),
+                                             native.YAR_BUFFERS_HOST) == 0
+    host_occ = gpu_ctx.cast_any(shadow)
+    d_rays = torch.from_numpy(rays).cuda()
+    d_shadow = torch.from_numpy(shadow).cuda()
+    dt = torch.empty(n, dtype=torch.float32, device="cuda")
+    dprim = torch.empty(n, dtype=torch.int32, device="cuda")
+    dobj = torch.empty(n, dtype=torch.int32, device="cuda")
+    dbary = torch.empty((n, 2), dtype=torch.float32, device="cuda")
+    docc = torch.empty(n, dtype=torch.uint8, device="cuda")
+    torch.cuda.synchronize()
+    gpu_ctx.cast_closest_device(d_rays.data_ptr(), n, dt.data_ptr(), dprim.data_ptr(), dobj.data_ptr(),
+                                dbary.data_ptr())
+    gpu_ctx.cast_any_device(d_shadow.data_ptr(), n, docc.data_ptr())
+    torch.cuda.synchronize()
+    dev = (dt.cpu().numpy(), dprim.cpu().numpy().view(np.uint32), dobj.cpu().numpy().view(np.uint32),
+           dbary.cpu().numpy())
+    assert np.array_equal(bits(t), bits(dev[0])) and np.array_equal(prim, dev[1]) and np.array_equal(obj, dev[2])
+    assert_same_hits(first, dev)
+    assert np.array_equal(host_occ, docc.cpu().numpy())
+    gpu_ctx.close()
+
+
 def test_malformed_scene_is_rejected_on_the_host(gpu_ctx):
     s = FlatScene.read(golden("raycast_small.yfs"))
     bad = FlatScene.read(golden("raycast_small.yfs"))

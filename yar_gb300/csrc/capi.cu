@@ -121,6 +121,7 @@ extern "C" int yar_gpu_create(yar_gpu_ctx** out, const yar_gpu_options* options)
     if (!ctx) return YAR_ERR_NOMEM;
     ctx->device = options ? options->device : 0;
     ctx->staging_capacity = (options && options->max_batch_rays) ? options->max_batch_rays : (16u << 20);
+    if (options && options->pipeline_chunk_rays) ctx->pipe_chunk = options->pipeline_chunk_rays;
     if (options && options->traversal_kernel != YAR_TRAVERSAL_AUTO) {
         if (options->traversal_kernel < YAR_TRAVERSAL_PERSISTENT_64 ||
             options->traversal_kernel > YAR_TRAVERSAL_PER_RAY_VOTE) {
@@ -144,7 +145,7 @@ extern "C" int yar_gpu_create(yar_gpu_ctx** out, const yar_gpu_options* options)
     if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
     if (e == cudaSuccess) e = cudaMalloc(&ctx->d_error, sizeof(int));
     if (e == cudaSuccess) e = cudaMemset(ctx->d_error, 0, sizeof(int));
-    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, sizeof(uint32_t));
+    if (e == cudaSuccess) e = cudaMalloc(&ctx->d_counter, yar_gpu_ctx::kPipeChunks * sizeof(uint32_t));
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_start);
     if (e == cudaSuccess) e = cudaEventCreate(&ctx->ev_stop);
     if (e != cudaSuccess) {
@@ -169,6 +170,13 @@ extern "C" void yar_gpu_destroy(yar_gpu_ctx* ctx) {
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
+    for (cudaStream_t s : {ctx->pipe_in, ctx->pipe_compute, ctx->pipe_out})
+        if (s) cudaStreamDestroy(s);
+    if (ctx->pipe_start) cudaEventDestroy(ctx->pipe_start);
+    for (int c = 0; c < yar_gpu_ctx::kPipeChunks; c++) {
+        if (ctx->pipe_in_done[c]) cudaEventDestroy(ctx->pipe_in_done[c]);
+        if (ctx->pipe_cast_done[c]) cudaEventDestroy(ctx->pipe_cast_done[c]);
+    }
     if (ctx->stream) cudaStreamDestroy(ctx->stream);
     delete ctx;
 }
@@ -304,6 +312,8 @@ extern "C" int yar_gpu_upload_scene(yar_gpu_ctx* ctx, const yar_flat_scene* scen
         for (int b = 0; b < yar_gpu_ctx::kBounceBuckets; b++) ctx->render_kernel[k][b] = ctx->forced_kernel;
     }
     ctx->render_tuned = ctx->forced_kernel >= 0;
+    memset(ctx->render_tune_ms, 0, sizeof(ctx->render_tune_ms));
+    memset(ctx->render_tune_queues, 0, sizeof(ctx->render_tune_queues));
     ctx->has_scene = true;
     return YAR_OK;
 }
@@ -338,6 +348,92 @@ int check_error_word(yar_gpu_ctx* ctx) {
     return YAR_OK;
 }
 
+// Host-buffer casts of at least two pipeline chunks: chunk c's rays go up on
+// pipe_in, its traversal runs on the context's stream or pipe_compute
+// (alternating, so one chunk's tail overlaps the next chunk's start), its
+// results come down on pipe_out.  Every chunk keeps its own offsets in the
+// staging buffers and its own hand-out counter.
+uint32_t pipeline_chunks(const yar_gpu_ctx* ctx, uint32_t n) {
+    if (ctx->pipe_chunk == 0xffffffffu) return 1;
+    const uint64_t c = ((uint64_t)n + ctx->pipe_chunk - 1) / ctx->pipe_chunk;
+    return (uint32_t)std::min<uint64_t>(c, yar_gpu_ctx::kPipeChunks);
+}
+
+int ensure_pipeline(yar_gpu_ctx* ctx) {
+    cudaError_t e = cudaSuccess;
+    for (cudaStream_t* s : {&ctx->pipe_in, &ctx->pipe_compute, &ctx->pipe_out})
+        if (!*s && e == cudaSuccess) e = cudaStreamCreateWithFlags(s, cudaStreamNonBlocking);
+    if (!ctx->pipe_start && e == cudaSuccess) e = cudaEventCreateWithFlags(&ctx->pipe_start, cudaEventDisableTiming);
+    for (int c = 0; c < yar_gpu_ctx::kPipeChunks && e == cudaSuccess; c++) {
+        if (!ctx->pipe_in_done[c]) e = cudaEventCreateWithFlags(&ctx->pipe_in_done[c], cudaEventDisableTiming);
+        if (!ctx->pipe_cast_done[c] && e == cudaSuccess)
+            e = cudaEventCreateWithFlags(&ctx->pipe_cast_done[c], cudaEventDisableTiming);
+    }
+    return e == cudaSuccess ? YAR_OK : cuda_fail(ctx, e, "cast pipeline streams");
+}
+
+int cast_pipelined(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t n, const yar_hit_soa* hits, uint8_t* occluded,
+                   int kernel) {
+    const bool closest = hits != nullptr;
+    int rc = ensure_pipeline(ctx);
+    if (rc != YAR_OK) return rc;
+    const uint32_t chunks = pipeline_chunks(ctx, n);
+    const uint32_t per = (uint32_t)((((uint64_t)n + chunks - 1) / chunks + 31u) & ~31ull);
+    cudaStream_t compute[2] = {ctx->stream, ctx->pipe_compute};
+    cudaError_t e = cudaEventRecord(ctx->pipe_start, ctx->stream);  // after the context's earlier work
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->pipe_in, ctx->pipe_start, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->pipe_compute, ctx->pipe_start, 0);
+    if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->pipe_out, ctx->pipe_start, 0);
+    float4* d_rays = (float4*)ctx->d_rays.ptr;
+    for (uint32_t c = 0; c < chunks && e == cudaSuccess; c++) {
+        const uint32_t first = c * per;
+        if (first >= n) break;
+        const uint32_t m = std::min(per, n - first);
+        e = cudaMemcpyAsync(d_rays + 2 * (size_t)first, rays + first, (size_t)m * 32, cudaMemcpyHostToDevice,
+                            ctx->pipe_in);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->pipe_in_done[c], ctx->pipe_in);
+        cudaStream_t ks = compute[c & 1];
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ks, ctx->pipe_in_done[c], 0);
+        if (e != cudaSuccess) break;
+        Cast_Args a;
+        a.rays = d_rays + 2 * (size_t)first;
+        a.n = m;
+        a.next_ray = ctx->d_counter + c;
+        a.err = ctx->d_error;
+        if (closest) {
+            a.t = hits->t ? (float*)ctx->d_t.ptr + first : nullptr;
+            a.prim = hits->prim ? (uint32_t*)ctx->d_prim.ptr + first : nullptr;
+            a.object = hits->object ? (uint32_t*)ctx->d_obj.ptr + first : nullptr;
+            a.bary = hits->bary ? (float2*)ctx->d_bary.ptr + first : nullptr;
+        } else {
+            a.occluded = (uint8_t*)ctx->d_occ.ptr + first;
+        }
+        e = closest ? launch_extend(ctx->ds, a, kernel, ks) : launch_shadow(ctx->ds, a, kernel, ks);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->pipe_cast_done[c], ks);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->pipe_out, ctx->pipe_cast_done[c], 0);
+        cudaStream_t os = ctx->pipe_out;
+        if (closest) {
+            if (e == cudaSuccess && hits->t)
+                e = cudaMemcpyAsync(hits->t + first, a.t, (size_t)m * 4, cudaMemcpyDeviceToHost, os);
+            if (e == cudaSuccess && hits->prim)
+                e = cudaMemcpyAsync(hits->prim + first, a.prim, (size_t)m * 4, cudaMemcpyDeviceToHost, os);
+            if (e == cudaSuccess && hits->object)
+                e = cudaMemcpyAsync(hits->object + first, a.object, (size_t)m * 4, cudaMemcpyDeviceToHost, os);
+            if (e == cudaSuccess && hits->bary)
+                e = cudaMemcpyAsync(hits->bary + 2 * (size_t)first, a.bary, (size_t)m * 8, cudaMemcpyDeviceToHost, os);
+        } else if (e == cudaSuccess) {
+            e = cudaMemcpyAsync(occluded + first, a.occluded, m, cudaMemcpyDeviceToHost, os);
+        }
+    }
+    // every stream finishes before the call returns; the context's stream last
+    for (cudaStream_t s : {ctx->pipe_in, ctx->pipe_compute, ctx->pipe_out}) {
+        const cudaError_t e2 = cudaStreamSynchronize(s);
+        if (e == cudaSuccess) e = e2;
+    }
+    if (e != cudaSuccess) return cuda_fail(ctx, e, "pipelined cast");
+    return check_error_word(ctx);
+}
+
 int cast(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t n, const yar_hit_soa* hits, uint8_t* occluded,
          int32_t buffers, float* kernel_ms) {
     if (!ctx) return YAR_ERR_INVALID;
@@ -357,6 +453,10 @@ int cast(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t n, const yar_hit_soa* h
     if (buffers == YAR_BUFFERS_HOST) {
         int rc = ensure_staging(ctx, n, closest);
         if (rc != YAR_OK) return rc;
+        // a tuned (or fixed) traversal kernel and at least two chunks: overlap copies and traversal
+        const int tuned = ctx->cast_kernel[closest ? 0 : 1];
+        if (!kernel_ms && pipeline_chunks(ctx, n) >= 2 && (tuned >= 0 || n < kTuneMinRays))
+            return cast_pipelined(ctx, rays, n, hits, occluded, tuned < 0 ? kCastPersistent64 : tuned);
         e = cudaMemcpyAsync(ctx->d_rays.ptr, rays, (size_t)n * 32, cudaMemcpyHostToDevice, ctx->stream);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "ray upload");
         d_rays = (const float4*)ctx->d_rays.ptr;

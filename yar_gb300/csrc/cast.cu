@@ -262,21 +262,9 @@ cudaError_t launch_shadow(const Device_Scene& s, const Cast_Args& a, int kernel,
 
 namespace {
 
-cudaError_t time_cast_kernels(const Device_Scene& s, const Cast_Args& a, bool any, cudaStream_t stream,
-                              cudaEvent_t ev0, cudaEvent_t ev1, float* ms_acc) {
-    auto run = [&](int k) { return any ? launch_shadow(s, a, k, stream) : launch_extend(s, a, k, stream); };
-    cudaError_t e = run(kCastPersistent64);  // warms the caches for the timed runs
-    for (int k = 0; k < kCastKernelCount && e == cudaSuccess; k++) {
-        e = cudaEventRecord(ev0, stream);
-        if (e == cudaSuccess) e = run(k);
-        if (e == cudaSuccess) e = cudaEventRecord(ev1, stream);
-        if (e == cudaSuccess) e = cudaEventSynchronize(ev1);
-        float ms = 0.f;
-        if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev0, ev1);
-        ms_acc[k] += ms;
-    }
-    return e;
-}
+// C-ABI casts take each kernel's best of kTuneRounds timed runs on their
+// first large batch (rounds interleave the kernels).
+constexpr int kTuneRounds = 3;
 
 int fastest_cast_kernel(const float* ms) {
     int best = 0;
@@ -287,10 +275,29 @@ int fastest_cast_kernel(const float* ms) {
 
 } // namespace
 
+cudaError_t time_cast_kernels(const Device_Scene& s, const Cast_Args& a, bool any, cudaStream_t stream,
+                              cudaEvent_t ev0, cudaEvent_t ev1, int rounds, bool warm, float* ms_best) {
+    auto run = [&](int k) { return any ? launch_shadow(s, a, k, stream) : launch_extend(s, a, k, stream); };
+    cudaError_t e = warm ? run(kCastPersistent64) : cudaSuccess;  // warms the caches for the timed runs
+    for (int k = 0; k < kCastKernelCount; k++) ms_best[k] = 3.0e38f;
+    for (int r = 0; r < rounds; r++) {
+        for (int k = 0; k < kCastKernelCount && e == cudaSuccess; k++) {
+            e = cudaEventRecord(ev0, stream);
+            if (e == cudaSuccess) e = run(k);
+            if (e == cudaSuccess) e = cudaEventRecord(ev1, stream);
+            if (e == cudaSuccess) e = cudaEventSynchronize(ev1);
+            float ms = 0.f;
+            if (e == cudaSuccess) e = cudaEventElapsedTime(&ms, ev0, ev1);
+            ms_best[k] = ms < ms_best[k] ? ms : ms_best[k];
+        }
+    }
+    return e;
+}
+
 cudaError_t tune_cast(const Device_Scene& s, const Cast_Args& a, bool any, cudaStream_t stream, cudaEvent_t ev0,
                       cudaEvent_t ev1, int* best) {
     float ms[kCastKernelCount] = {};
-    cudaError_t e = time_cast_kernels(s, a, any, stream, ev0, ev1, ms);
+    cudaError_t e = time_cast_kernels(s, a, any, stream, ev0, ev1, kTuneRounds, true, ms);
     *best = e == cudaSuccess ? fastest_cast_kernel(ms) : kCastPersistent64;
     return e;
 }

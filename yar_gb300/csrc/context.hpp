@@ -85,7 +85,16 @@ struct yar_gpu_ctx {
     uint32_t staging_capacity = 0;
     yar::Device_Buffer d_rays, d_t, d_prim, d_obj, d_bary, d_occ;
     int* d_error = nullptr;  // device error word (stack overflow, bounded-wait expiry)
-    uint32_t* d_counter = nullptr;  // ray hand-out counter of the persistent cast kernels
+    uint32_t* d_counter = nullptr;  // ray hand-out counters of the persistent cast kernels, one per pipeline chunk
+    // host-buffer casts in chunks: copies in, the traversal on two compute
+    // streams (the context's and pipe_compute) and copies out overlap
+    static constexpr int kPipeChunks = 32;
+    // rays per chunk: on GB300 (C2, 16M rays per call) 4M overlapped best (33.8 ms
+    // per closest + any step against 36.8 ms unpipelined; 35.7 at 2M, 46.5 at 1M,
+    // where the persistent traversal's tail per launch outweighs the overlap)
+    uint32_t pipe_chunk = 4u << 20;
+    cudaStream_t pipe_in = nullptr, pipe_compute = nullptr, pipe_out = nullptr;
+    cudaEvent_t pipe_start = nullptr, pipe_in_done[kPipeChunks] = {}, pipe_cast_done[kPipeChunks] = {};
     // traversal kernel per ray kind (0 closest, 1 any) for C-ABI casts and for
     // renders; -1 until tuned on the current scene (or fixed by the options)
     int forced_kernel = -1;
@@ -93,6 +102,10 @@ struct yar_gpu_ctx {
     // renders: per ray kind and bounce (bounces past the last share its entry)
     static constexpr int kBounceBuckets = 5;
     int render_kernel[2][kBounceBuckets] = {{-1, -1, -1, -1, -1}, {-1, -1, -1, -1, -1}};
+    // while a bucket is being chosen: per kernel the summed times of its timed
+    // queues, and how many queues were timed
+    float render_tune_ms[2][kBounceBuckets][4] = {};
+    int render_tune_queues[2][kBounceBuckets] = {};
     // a render of the current scene has run with host-read queue lengths (and
     // tuned the buckets it filled): later renders drive their bounces on the device
     bool render_tuned = false;
@@ -148,10 +161,15 @@ enum Cast_Kernel {
 };
 cudaError_t launch_extend(const Device_Scene& s, const Cast_Args& a, int kernel, cudaStream_t stream);
 cudaError_t launch_shadow(const Device_Scene& s, const Cast_Args& a, int kernel, cudaStream_t stream);
-// Runs the batch once untimed and once with each kernel (event-timed on
-// `stream`), leaving the results of the last run in place; *best = fastest.
+// Runs the batch once untimed and three times with each kernel (event-timed
+// on `stream`), leaving the results of the last run in place; *best = the
+// kernel of the shortest run.
 cudaError_t tune_cast(const Device_Scene& s, const Cast_Args& a, bool any, cudaStream_t stream, cudaEvent_t ev0,
                       cudaEvent_t ev1, int* best);
+// ms[k] = kernel k's shortest of `rounds` timed runs (after one untimed run
+// when `warm`); the results of the last run stay in place.
+cudaError_t time_cast_kernels(const Device_Scene& s, const Cast_Args& a, bool any, cudaStream_t stream,
+                              cudaEvent_t ev0, cudaEvent_t ev1, int rounds, bool warm, float* ms);
 
 // guide network (guide_mlp.cu).  `box` = scene bounds (min xyz, max xyz)
 // for position normalisation.  Query rows: 3 float4 {pos, n.x | n.yz, wo.xy |

@@ -704,6 +704,7 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
         rays_closest = rays_h[0];
         rays_any = rays_h[1];
     } else if (!guide) {
+        finish_render_tuning(ctx);
         ctx->render_tuned = true;
     }
     if (tiles_out) tiles_out->tile_variance = tile_var;

@@ -461,11 +461,44 @@ camera_kernel(Render_Params p, uint32_t chunk_first, uint32_t chunk_paths, const
 //
 // The traversal kernel is chosen per ray kind and per bounce (camera rays,
 // the first bounces and the deep, sparse, incoherent ones favour different
-// kernels): the first queue of at least kRenderTuneMinRays rays of a bounce
-// after a scene upload is traced by all three kernels, timed, and the fastest
-// kept (the queue's results are the same whichever ran last); the MIS probe
-// queue uses the extend queue's choice.  A context option can fix the kernel.
+// kernels): the first kRenderTuneQueues queues of at least kRenderTuneMinRays
+// rays of a bounce bucket after a scene upload are traced by every kernel and
+// timed, and the kernel of the least summed time is kept (a queue's results
+// are the same whichever ran last).  A bucket timed on fewer queues by the
+// end of the first render takes its best so far.  The deep bucket covers
+// bounces 4 and later, whose queues shrink: one queue alone picked a kernel
+// that was 8% slower on C3 in one of four scene uploads.  The MIS probe queue
+// uses the extend queue's choice.  A context option can fix the kernel.
 constexpr uint32_t kRenderTuneMinRays = 1u << 16;
+constexpr int kRenderTuneQueues = 3;
+
+inline void fix_render_bucket(yar_gpu_ctx* ctx, int kind, int bucket) {
+    const float* ms = ctx->render_tune_ms[kind][bucket];
+    int best = 0;
+    for (int k = 1; k < kCastKernelCount; k++)
+        if (ms[k] < ms[best]) best = k;
+    ctx->render_kernel[kind][bucket] = best;
+}
+
+// Times every kernel on this queue (its results stay in place) and adds the
+// times to the bucket's sums; fixes the bucket after kRenderTuneQueues queues.
+inline cudaError_t tune_render_bucket(yar_gpu_ctx* ctx, const Cast_Args& a, int kind, int bucket, cudaStream_t st) {
+    static_assert(kCastKernelCount == 4, "tuning sums per kernel");
+    float ms[kCastKernelCount];
+    const bool first = ctx->render_tune_queues[kind][bucket] == 0;
+    cudaError_t e = time_cast_kernels(ctx->ds, a, kind == 1, st, ctx->ev_start, ctx->ev_stop, 1, first, ms);
+    if (e != cudaSuccess) return e;
+    for (int k = 0; k < kCastKernelCount; k++) ctx->render_tune_ms[kind][bucket][k] += ms[k];
+    if (++ctx->render_tune_queues[kind][bucket] >= kRenderTuneQueues) fix_render_bucket(ctx, kind, bucket);
+    return cudaSuccess;
+}
+
+// After the first render: buckets timed on fewer queues take their best so far.
+inline void finish_render_tuning(yar_gpu_ctx* ctx) {
+    for (int kind = 0; kind < 2; kind++)
+        for (int b = 0; b < yar_gpu_ctx::kBounceBuckets; b++)
+            if (ctx->render_kernel[kind][b] < 0 && ctx->render_tune_queues[kind][b] > 0) fix_render_bucket(ctx, kind, b);
+}
 
 inline int bounce_bucket(int bounce) { return bounce < yar_gpu_ctx::kBounceBuckets ? bounce : yar_gpu_ctx::kBounceBuckets - 1; }
 
@@ -486,8 +519,8 @@ cudaError_t trace_extend(yar_gpu_ctx* ctx, const Queues& q, int cur, uint32_t co
     a.err = reinterpret_cast<int*>(q.counters + 3);
     a.hit4 = q.ext_hit4;
     a.hit2 = q.ext_hit2;
-    int& k = ctx->render_kernel[0][bounce_bucket(bounce)];
-    if (k < 0 && count >= kRenderTuneMinRays) return tune_cast(ctx->ds, a, false, st, ctx->ev_start, ctx->ev_stop, &k);
+    const int b = bounce_bucket(bounce);
+    if (ctx->render_kernel[0][b] < 0 && count >= kRenderTuneMinRays) return tune_render_bucket(ctx, a, 0, b, st);
     return launch_extend(ctx->ds, a, render_choice(ctx, 0, bounce), st);
 }
 
@@ -501,9 +534,9 @@ cudaError_t trace_light_queues(yar_gpu_ctx* ctx, const Queues& q, const Path_Sta
     sh.next_ray = q.counters + 5;
     sh.err = reinterpret_cast<int*>(q.counters + 3);
     sh.occluded = ps.occluded;
-    int& k = ctx->render_kernel[1][bounce_bucket(bounce)];
-    cudaError_t e = (k < 0 && count >= kRenderTuneMinRays)
-                        ? tune_cast(ctx->ds, sh, true, st, ctx->ev_start, ctx->ev_stop, &k)
+    const int b = bounce_bucket(bounce);
+    cudaError_t e = (ctx->render_kernel[1][b] < 0 && count >= kRenderTuneMinRays)
+                        ? tune_render_bucket(ctx, sh, 1, b, st)
                         : launch_shadow(ctx->ds, sh, render_choice(ctx, 1, bounce), st);
     if (e != cudaSuccess) return e;
     Cast_Args pr;
@@ -1149,20 +1182,26 @@ __device__ __forceinline__ V3 sphere_sampler_sample(const Sphere_Sampler& ss, fl
 // light kind but the quad light.  A scene without them runs the FULL = false
 // instantiation, which has none of that code (launch_shade picks it from
 // Render_Params::full_shading).
-// Launch bounds, FULL = false: at least 5 blocks of 128 threads per SM (96
-// registers).  Measured on GB300 (C3 render): 1.726 s against 1.732 s at 4
-// blocks (128 registers) and 1.764 s without a bound (160 registers, 3
-// blocks).  FULL = true: 3 blocks (168 registers); at 5 blocks its larger
-// state spilled about 2 KB per thread.
+// Launch bounds: 4 blocks of 128 threads per SM (128 registers), where the
+// plain and the FULL instantiations spill nothing: the shadow, probe and next
+// extend rays wait for the warp's appends in shared memory, and the path's
+// radiance is read and written only where emission adds to it.  The guided
+// FULL instantiation keeps 3 blocks (164 registers, no spills); the guided
+// plain one spills 10 B at 4.  Before those changes the plain kernel ran at 5
+// blocks (96 registers, 202 B of spill stores), which measured 1.726 s on the
+// C3 render against 1.732 s at 4 blocks and 1.764 s at 3.
 template <bool GUIDED, bool FULL>
-__global__ void __launch_bounds__(kBlock, FULL ? 3 : 5)
+__global__ void __launch_bounds__(kBlock, GUIDED && FULL ? 3 : 4)
 shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float* __restrict__ s1d,
              const float2* __restrict__ s2d, Path_State ps, Queues q, Guide_Shade g) {
+    // this thread's shadow, probe and next extend rays (origin + tmax,
+    // direction) from where they are made until the warp's appends: in shared
+    // memory, not in 24 registers live across the whole shading
+    __shared__ float4 stash[6][kBlock];
     if (q.ext_count) count = *q.ext_count;
     for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
         const uint32_t i = base + threadIdx.x;
         bool want_shadow = false, want_probe = false, want_next = false;
-        float4 sh_a = make_float4(0, 0, 0, 0), sh_b = sh_a, pr_a = sh_a, pr_b = sh_a, nx_a = sh_a, nx_b = sh_a;
         uint32_t slot = 0;
         if (i < count) {
             slot = q.ext_slot[cur][i];
@@ -1170,12 +1209,10 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
             const float4 h4 = q.ext_hit4[i];
             const uint2 h2 = q.ext_hit2[i];
             float4 coeff4 = ps.coeff[slot];
-            float4 L4 = ps.L[slot];
             uint32_t info = ps.info[slot];
             int bounce = (int)(info & 0xffu);
             const bool arrival = FULL && (info & kDeltaArrival) != 0;
             Col coeff = col(coeff4.x, coeff4.y, coeff4.z);
-            Col L = col(L4.x, L4.y, L4.z);
             const bool hit = h2.y != 0xffffffffu;
             Shading sc;
             int4 oinfo = make_int4(-1, -1, -1, -1);
@@ -1184,20 +1221,33 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
             bool done = false;
             // Emission seen by a camera ray or by a delta ray (the delta vertex
             // already applied its attenuation and counted the bounce).
+            // The path's radiance changes only here in this kernel (direct light
+            // is added by the connect kernel): read and written back only then.
             if (bounce == 0 || arrival) {
                 // get_emitted_radiance (direct_lighting.cpp:386-413): triangle-mesh
                 // lights emit only on the side their normal faces
+                bool emits = false;
+                Col le = col(0.f, 0.f, 0.f);
                 if (is_light && (uint32_t)oinfo.z == YAR_LIGHT_DIFFUSE_RECTANGULAR) {
-                    const float4 le = __ldg(&S.lights[oinfo.w].le);
-                    L = L + coeff * col(le.x, le.y, le.z);
+                    const float4 e4 = __ldg(&S.lights[oinfo.w].le);
+                    le = col(e4.x, e4.y, e4.z);
+                    emits = true;
                 } else if (FULL && is_light && (uint32_t)oinfo.z == YAR_LIGHT_DIFFUSE_TRIANGLE_MESH && !sc.flipped) {
-                    const float4 le = __ldg(&S.mesh_lights[oinfo.w].le);
-                    L = L + coeff * col(le.x, le.y, le.z);
+                    const float4 e4 = __ldg(&S.mesh_lights[oinfo.w].le);
+                    le = col(e4.x, e4.y, e4.z);
+                    emits = true;
                 } else if (FULL && is_light && (uint32_t)oinfo.z == YAR_LIGHT_DIFFUSE_SPHERE) {
-                    const float4 le = __ldg(&S.sphere_lights[oinfo.w].le);
-                    L = L + coeff * col(le.x, le.y, le.z);
+                    const float4 e4 = __ldg(&S.sphere_lights[oinfo.w].le);
+                    le = col(e4.x, e4.y, e4.z);
+                    emits = true;
                 } else if (FULL && !hit && S.env_map) {  // a miss sees the environment, filtered
-                    L = L + coeff * env_radiance(S, v3(rb.x, rb.y, rb.z), true);
+                    le = env_radiance(S, v3(rb.x, rb.y, rb.z), true);
+                    emits = true;
+                }
+                if (emits) {
+                    const float4 L4 = ps.L[slot];
+                    const Col L = col(L4.x, L4.y, L4.z) + coeff * le;
+                    ps.L[slot] = make_float4(L.r, L.g, L.b, 0.f);
                 }
                 if (arrival ? (info & kDeltaFinal) != 0 : p.max_bounces == 0) done = true;
             }
@@ -1322,8 +1372,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                 const Col c = mul(col(dc.x, dc.y, dc.z) * fv, scale);
                                 ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
                                 want_shadow = true;
-                                sh_a = make_float4(position.x, position.y, position.z, tmax);
-                                sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                stash[0][threadIdx.x] = make_float4(position.x, position.y, position.z, tmax);
+                                stash[1][threadIdx.x] = make_float4(wi.x, wi.y, wi.z, 0.f);
                                 pend |= kPendShadow;
                             }
                         }
@@ -1351,8 +1401,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                     const Col c = mul(Le * fv, w * fabsf(ndw) / ss.cone_pdf);
                                     ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
                                     want_shadow = true;
-                                    sh_a = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
-                                    sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                    stash[0][threadIdx.x] = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
+                                    stash[1][threadIdx.x] = make_float4(wi.x, wi.y, wi.z, 0.f);
                                     pend |= kPendShadow;
                                 }
                             }
@@ -1369,8 +1419,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                 ps.pend_probe2[slot] = make_float4(dot(sc.n, wi), __int_as_float(light_index),
                                                                    __uint_as_float(kProbeSphereLight), 0.f);
                                 want_probe = true;
-                                pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
-                                pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                stash[2][threadIdx.x] = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
+                                stash[3][threadIdx.x] = make_float4(wi.x, wi.y, wi.z, 0.f);
                                 pend |= kPendProbe;
                             }
                         }
@@ -1391,8 +1441,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                     const Col c = mul(Le * fv, w * fabsf(ndw) / light_pdf);
                                     ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
                                     want_shadow = true;
-                                    sh_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
-                                    sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                    stash[0][threadIdx.x] = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
+                                    stash[1][threadIdx.x] = make_float4(wi.x, wi.y, wi.z, 0.f);
                                     pend |= kPendShadow;
                                 }
                             }
@@ -1411,8 +1461,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                     ps.pend_probe2[slot] = make_float4(dot(sc.n, wi), 0.f,
                                                                        __uint_as_float(kProbeEnvLight), 0.f);
                                     want_probe = true;
-                                    pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
-                                    pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                    stash[2][threadIdx.x] = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
+                                    stash[3][threadIdx.x] = make_float4(wi.x, wi.y, wi.z, 0.f);
                                     pend |= kPendProbe;
                                 }
                             }
@@ -1441,8 +1491,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                         const Col c = mul(Le * fv, w * fabsf(ndw) / light_pdf);
                                         ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
                                         want_shadow = true;
-                                        sh_a = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
-                                        sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                        stash[0][threadIdx.x] = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
+                                        stash[1][threadIdx.x] = make_float4(wi.x, wi.y, wi.z, 0.f);
                                         pend |= kPendShadow;
                                     }
                                 }
@@ -1460,8 +1510,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                 ps.pend_probe2[slot] = make_float4(dot(sc.n, wi), __int_as_float(light_index),
                                                                    __uint_as_float(kProbeMeshLight), 0.f);
                                 want_probe = true;
-                                pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
-                                pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                stash[2][threadIdx.x] = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
+                                stash[3][threadIdx.x] = make_float4(wi.x, wi.y, wi.z, 0.f);
                                 pend |= kPendProbe;
                             }
                         }
@@ -1493,8 +1543,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                         const Col c = mul(Le * fv, w * fabsf(ndw) / light_pdf);
                                         ps.pend_light[slot] = make_float4(c.r, c.g, c.b, 0.f);
                                         want_shadow = true;
-                                        sh_a = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
-                                        sh_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                        stash[0][threadIdx.x] = make_float4(position.x, position.y, position.z, dist * (1.f - 1e-5f));
+                                        stash[1][threadIdx.x] = make_float4(wi.x, wi.y, wi.z, 0.f);
                                         pend |= kPendShadow;
                                     }
                                 }
@@ -1513,8 +1563,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                                     ps.pend_probe1[slot] = make_float4(position.x, position.y, position.z, lndw);
                                     ps.pend_probe2[slot] = make_float4(dot(sc.n, wi), __int_as_float(light_index), 0.f, 0.f);
                                     want_probe = true;
-                                    pr_a = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
-                                    pr_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                                    stash[2][threadIdx.x] = make_float4(position.x, position.y, position.z, __int_as_float(0x7f800000));
+                                    stash[3][threadIdx.x] = make_float4(wi.x, wi.y, wi.z, 0.f);
                                     pend |= kPendProbe;
                                 }
                             }
@@ -1530,8 +1580,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                     if (delta == 1) {
                         coeff = coeff * delta_atten;
                         const V3 o = origin_for_direction(sc, delta_wi);
-                        nx_a = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
-                        nx_b = make_float4(delta_wi.x, delta_wi.y, delta_wi.z, 0.f);
+                        stash[4][threadIdx.x] = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
+                        stash[5][threadIdx.x] = make_float4(delta_wi.x, delta_wi.y, delta_wi.z, 0.f);
                         want_next = true;
                     }
                     if (GUIDED && g.records) ps.rec[slot] = 0xffffffffu;
@@ -1578,8 +1628,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                             }
                             coeff = coeff * mul(fv, fabsf(dot(sc.n, wi)) / (pdf * bsdf_prob));
                             const V3 o = origin_for_direction(sc, wi);
-                            nx_a = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
-                            nx_b = make_float4(wi.x, wi.y, wi.z, 0.f);
+                            stash[4][threadIdx.x] = make_float4(o.x, o.y, o.z, __int_as_float(0x7f800000));
+                            stash[5][threadIdx.x] = make_float4(wi.x, wi.y, wi.z, 0.f);
                             if (bounce >= p.rr_bounce_threshold) {  // Russian roulette
                                 const float u_term = next1d(dm);
                                 const float max_coeff = max_std(coeff.r, max_std(coeff.g, coeff.b));
@@ -1623,31 +1673,30 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 if (p.exact_tail) ps.rng_draws[slot] += dm.draws;
             }
             if (p.exact_tail == 1 && want_next && tail_may_draw_past_budget(p, info)) {
-                ps.deferred[2 * (size_t)slot] = nx_a;
-                ps.deferred[2 * (size_t)slot + 1] = nx_b;
+                ps.deferred[2 * (size_t)slot] = stash[4][threadIdx.x];
+                ps.deferred[2 * (size_t)slot + 1] = stash[5][threadIdx.x];
                 info |= kDeferred;
                 want_next = false;
             }
             ps.coeff[slot] = make_float4(coeff.r, coeff.g, coeff.b, 0.f);
-            ps.L[slot] = make_float4(L.r, L.g, L.b, 0.f);
             ps.info[slot] = info;
         }
         const uint32_t is = warp_append(&q.counters[1], want_shadow);
         if (want_shadow) {
-            q.shd_rays[2 * (size_t)is] = sh_a;
-            q.shd_rays[2 * (size_t)is + 1] = sh_b;
+            q.shd_rays[2 * (size_t)is] = stash[0][threadIdx.x];
+            q.shd_rays[2 * (size_t)is + 1] = stash[1][threadIdx.x];
             q.shd_slot[is] = slot;
         }
         const uint32_t ip = warp_append(&q.counters[2], want_probe);
         if (want_probe) {
-            q.prb_rays[2 * (size_t)ip] = pr_a;
-            q.prb_rays[2 * (size_t)ip + 1] = pr_b;
+            q.prb_rays[2 * (size_t)ip] = stash[2][threadIdx.x];
+            q.prb_rays[2 * (size_t)ip + 1] = stash[3][threadIdx.x];
             q.prb_slot[ip] = slot;
         }
         const uint32_t in = warp_append(&q.counters[0], want_next);
         if (want_next) {
-            q.ext_rays[cur ^ 1][2 * (size_t)in] = nx_a;
-            q.ext_rays[cur ^ 1][2 * (size_t)in + 1] = nx_b;
+            q.ext_rays[cur ^ 1][2 * (size_t)in] = stash[4][threadIdx.x];
+            q.ext_rays[cur ^ 1][2 * (size_t)in + 1] = stash[5][threadIdx.x];
             q.ext_slot[cur ^ 1][in] = slot;
         }
     }

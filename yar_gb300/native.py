@@ -175,7 +175,8 @@ class GuidedStats(C.Structure):
 
 
 class GpuOptions(C.Structure):
-    _fields_ = [("device", C.c_int32), ("max_batch_rays", C.c_uint32), ("traversal_kernel", C.c_int32)]
+    _fields_ = [("device", C.c_int32), ("max_batch_rays", C.c_uint32), ("traversal_kernel", C.c_int32),
+                ("pipeline_chunk_rays", C.c_uint32)]
 
 
 GUIDE_PARAMS = 20480
@@ -323,10 +324,10 @@ def transform_bounds(object_to_world, bounds):
 class Context:
     """A yar_gpu_ctx: one CUDA device, one stream, one uploaded scene."""
 
-    def __init__(self, device=0, max_batch_rays=0, traversal_kernel=TRAVERSAL_AUTO):
+    def __init__(self, device=0, max_batch_rays=0, traversal_kernel=TRAVERSAL_AUTO, pipeline_chunk_rays=0):
         L = lib()
         h = C.c_void_p()
-        opts = GpuOptions(int(device), int(max_batch_rays), int(traversal_kernel))
+        opts = GpuOptions(int(device), int(max_batch_rays), int(traversal_kernel), int(pipeline_chunk_rays))
         rc = L.yar_gpu_create(C.byref(h), C.byref(opts))
         if rc != YAR_OK:
             raise YarError(rc, "yar_gpu_create (is a CUDA device visible?)")
