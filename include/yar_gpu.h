@@ -185,6 +185,8 @@ typedef struct yar_material_desc {
     float bump_height;
     uint32_t bump_texture;
     float bump_uv_scale[2];
+    /* pbrt3 fourier: 1 + the index of its table in yar_flat_scene::fourier_tables */
+    uint32_t fourier_table;
 } yar_material_desc;
 
 /* Image_Texture (src/ref/image_texture.h) as the reference builds it from the
@@ -263,6 +265,23 @@ typedef struct yar_environment_desc {
     const float* radiance;      /* width * height RGB triples, row 0 first */
 } yar_environment_desc;
 
+/* A pbrt3 fourier BSDF table (Pbrt3_Fourier_Material, src/lib/material_pbrt.h:4-38,
+ * as Pbrt3_Fourier_Material::load_bsdf_file reads a layerlab file): the
+ * zenith-angle cosines, increasing, the last at least 1; per pair of nodes
+ * (outgoing-major) the offset and length of its Fourier series; the
+ * coefficients, channel-major within a series (Y, then R and B for three
+ * channels).  Offsets index the flat scene's fourier_floats / fourier_uints. */
+typedef struct yar_fourier_desc {
+    uint32_t node_count;
+    uint32_t channel_count;     /* 1 or 3 */
+    uint32_t max_order;
+    float eta;                  /* relative IOR; the reference evaluates reflection only (eta 1) */
+    uint64_t nodes;             /* fourier_floats offset of node_count cosines */
+    uint64_t coeffs;            /* fourier_floats offset of the coefficients */
+    uint64_t coeff_count;       /* coefficients of this table */
+    uint64_t series;            /* fourier_uints offset of node_count^2 (offset into coeffs, length) pairs */
+} yar_fourier_desc;
+
 /* Camera, src/ref/camera.h:35-49 (fields as computed by Camera::Camera, camera.cpp:5-14) */
 typedef struct yar_camera_desc {
     float camera_to_world[12];
@@ -319,6 +338,12 @@ typedef struct yar_flat_scene {
     const yar_texture_mip_desc* texture_mips;
     const float* texels;            /* RGB triples of every mip */
     uint64_t texel_count;           /* texels (RGB triples) behind `texels`; every mip must lie inside */
+    uint32_t fourier_count;         /* pbrt3 fourier BSDF tables */
+    const yar_fourier_desc* fourier_tables;
+    uint64_t fourier_float_count;
+    const float* fourier_floats;
+    uint64_t fourier_uint_count;
+    const uint32_t* fourier_uints;
 } yar_flat_scene;
 
 /* One ray of a batch: 32 bytes, two float4.  tmax plays the role of the

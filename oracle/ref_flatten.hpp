@@ -113,7 +113,7 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         out.meshes.push_back(std::move(fm));
     }
     // materials: diffuse, metal, glass, plastic, coated diffuse, perfect reflector, perfect refractor,
-    // diffuse transmission, pbrt3 translucent, pbrt3 uber, mix flattened in that order
+    // diffuse transmission, pbrt3 translucent, pbrt3 uber, pbrt3 fourier, mix flattened in that order
     std::vector<int> diffuse_index, metal_index, glass_index;
     for (const Diffuse_Material& m : ctx.materials.diffuse) {
         yar_material_desc d{};
@@ -237,6 +237,32 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         uber_index.push_back((int)out.materials.size());
         push_material(out, d);
     }
+    // pbrt3 fourier: the table as Pbrt3_Fourier_Material::load_bsdf_file read it
+    std::vector<int> fourier_index;
+    for (const Pbrt3_Fourier_Material& m : ctx.materials.pbrt3_fourier) {
+        yar_material_desc d{};
+        d.type = YAR_MATERIAL_PBRT3_FOURIER;
+        yar_fourier_desc t{};
+        t.node_count = (uint32_t)m.zenith_angle_discretization.size();
+        t.channel_count = m.channel_count;
+        t.max_order = m.max_order;
+        t.eta = m.eta;
+        t.nodes = out.fourier_floats.size();
+        out.fourier_floats.insert(out.fourier_floats.end(), m.zenith_angle_discretization.begin(),
+                                  m.zenith_angle_discretization.end());
+        t.coeffs = out.fourier_floats.size();
+        t.coeff_count = m.coeffs.size();
+        out.fourier_floats.insert(out.fourier_floats.end(), m.coeffs.begin(), m.coeffs.end());
+        t.series = out.fourier_uints.size();
+        for (size_t k = 0; k < m.coeff_offset.size(); k++) {
+            out.fourier_uints.push_back(m.coeff_offset[k]);
+            out.fourier_uints.push_back(m.coeff_count[k]);
+        }
+        out.fourier_tables.push_back(t);
+        d.fourier_table = (uint32_t)out.fourier_tables.size();
+        fourier_index.push_back((int)out.materials.size());
+        push_material(out, d);
+    }
     for (size_t i = 0; i < ctx.materials.mix.size(); i++) {
         mix_index.push_back((int)out.materials.size() + (int)i);
     }
@@ -252,6 +278,7 @@ yfs::Scene flatten(const Scene& scene, const Scene_Context& ctx) {
         case Material_Type::diffuse_transmission: return transmission_index[h.index];
         case Material_Type::pbrt3_translucent: return translucent_index[h.index];
         case Material_Type::pbrt3_uber: return uber_index[h.index];
+        case Material_Type::pbrt3_fourier: return fourier_index[h.index];
         case Material_Type::mix: return mix_index[h.index];
         default: return -1;
         }

@@ -620,6 +620,37 @@ int cmd_render_yfs(const Args& a) {
                 m.components[k] = (Pbrt3_Uber_Material::Component_Type)d.components[k];
             scene.materials.pbrt3_uber.push_back(m);
             handles.push_back({Material_Type::pbrt3_uber, (int)scene.materials.pbrt3_uber.size() - 1});
+        } else if (d.type == YAR_MATERIAL_PBRT3_FOURIER) {
+            // the table as load_bsdf_file leaves it (src/lib/material_pbrt.cpp:24-102)
+            if (d.fourier_table == 0 || d.fourier_table > fs_scene.fourier_tables.size()) {
+                fprintf(stderr, "fourier material without a table\n");
+                return 1;
+            }
+            const yar_fourier_desc& t = fs_scene.fourier_tables[d.fourier_table - 1];
+            const uint64_t pairs = (uint64_t)t.node_count * t.node_count;
+            if (t.nodes + t.node_count > fs_scene.fourier_floats.size() ||
+                t.coeffs + t.coeff_count > fs_scene.fourier_floats.size() ||
+                t.series + 2 * pairs > fs_scene.fourier_uints.size()) {
+                fprintf(stderr, "fourier table out of range\n");
+                return 1;
+            }
+            Pbrt3_Fourier_Material m;
+            m.max_order = t.max_order;
+            m.channel_count = t.channel_count;
+            m.eta = t.eta;
+            const float* ff = fs_scene.fourier_floats.data();
+            m.zenith_angle_discretization.assign(ff + t.nodes, ff + t.nodes + t.node_count);
+            m.coeffs.assign(ff + t.coeffs, ff + t.coeffs + t.coeff_count);
+            m.coeff_offset.resize(pairs);
+            m.coeff_count.resize(pairs);
+            m.first_coeffs.resize(pairs);
+            for (uint64_t k = 0; k < pairs; k++) {
+                m.coeff_offset[k] = fs_scene.fourier_uints[t.series + 2 * k];
+                m.coeff_count[k] = fs_scene.fourier_uints[t.series + 2 * k + 1];
+                m.first_coeffs[k] = m.coeff_count[k] > 0 ? m.coeffs[m.coeff_offset[k]] : 0.f;
+            }
+            scene.materials.pbrt3_fourier.push_back(m);
+            handles.push_back({Material_Type::pbrt3_fourier, (int)scene.materials.pbrt3_fourier.size() - 1});
         } else if (d.type == YAR_MATERIAL_MIX) {
             scene.materials.mix.push_back(Mix_Material{});  // sub-materials below, once every handle exists
             handles.push_back({Material_Type::mix, (int)scene.materials.mix.size() - 1});

@@ -754,6 +754,10 @@ typedef struct bsdf_t {
     const struct bsdf_t* sub[2];    /* mix: the two BSDFs; scaled: sub[0] */
     col mix_coeff;                  /* mix: White - amount */
     float p_coeff, scale;           /* mix: 1 - luminance(mix_coeff); scaled: the factor */
+    /* pbrt3 fourier: zenith cosines, coefficients, (offset, length) per node pair */
+    const float *fourier_nodes, *fourier_coeffs;
+    const uint32_t* fourier_series;
+    uint32_t fourier_node_count, fourier_channels;
 } bsdf_t;
 
 #define ORACLE_BSDF_SCALED 0x100u   /* Scaled_BSDF: a mix whose other material is pure delta */
@@ -857,6 +861,15 @@ static int make_leaf_bsdf(const yar_flat_scene* s, const shading_ctx* sc, uint32
         f->eta_i = enter ? 1.5f : 1.f;
         f->reflection = !blackc(f->reflectance);
         f->transmission = !blackc(f->transmittance);
+    } else if (f->type == YAR_MATERIAL_PBRT3_FOURIER) {
+        /* Pbrt3_Fourier_BSDF, src/ref/bsdf_pbrt.cpp:297-303: reflection only */
+        const yar_fourier_desc* t = &s->fourier_tables[m->fourier_table - 1];
+        f->reflection = 1;
+        f->fourier_nodes = s->fourier_floats + t->nodes;
+        f->fourier_coeffs = s->fourier_floats + t->coeffs;
+        f->fourier_series = s->fourier_uints + t->series;
+        f->fourier_node_count = t->node_count;
+        f->fourier_channels = t->channel_count;
     } else {
         return YAR_ERR_UNSUPPORTED;
     }
@@ -1262,8 +1275,66 @@ static v3 refraction_half(float eta_o, v3 wo, float eta_i, v3 wi, v3 n) {
 
 static float pow5(float v) { return (v * v) * (v * v) * v; }
 
+/* cos_delta_phi (src/lib/math.h:87-104): the cosine of the azimuth between a
+ * and b in the tangent plane (1 for a direction along the normal). */
+static float cos_delta_phi(v3 a, v3 b, v3 t1, v3 t2) {
+    const float ax = dot3(a, t1), ay = dot3(a, t2), bx = dot3(b, t1), by = dot3(b, t2);
+    const float a_len_sq = ax * ax + ay * ay, b_len_sq = bx * bx + by * by;
+    if (a_len_sq == 0.f || b_len_sq == 0.f) return 1.f;
+    const float cosine = (ax * bx + ay * by) / sqrtf(a_len_sq * b_len_sq);
+    return cosine < -1.f ? -1.f : (1.f < cosine ? 1.f : cosine);
+}
+
+/* The first zenith node not below c (std::lower_bound over increasing nodes). */
+static uint32_t fourier_node(const bsdf_t* f, float c) {
+    uint32_t lo = 0, n = f->fourier_node_count;
+    while (n > 0) {
+        const uint32_t half = n / 2;
+        if (f->fourier_nodes[lo + half] < c) {
+            lo += half + 1;
+            n -= half + 1;
+        } else {
+            n = half;
+        }
+    }
+    return lo;
+}
+
+/* Pbrt3_Fourier_BSDF::evaluate (src/ref/bsdf_pbrt.cpp:305-358): the nearest
+ * node pair's Fourier series in the azimuth (no interpolation), divided by
+ * |cos_i|; three channels store Y, R, B. */
+static col fourier_evaluate(const bsdf_t* f, v3 wo, v3 wi) {
+    const v3 nwi = neg3(wi);
+    float cos_i = dot3(f->n, nwi);
+    cos_i = cos_i < -1.f ? -1.f : (1.f < cos_i ? 1.f : cos_i);
+    float cos_o = dot3(f->n, wo);
+    cos_o = cos_o < -1.f ? -1.f : (1.f < cos_o ? 1.f : cos_o);
+    const uint32_t index = fourier_node(f, cos_o) * f->fourier_node_count + fourier_node(f, cos_i);
+    const uint32_t offset = f->fourier_series[2 * index], count = f->fourier_series[2 * index + 1];
+    const float* coeffs = f->fourier_coeffs + offset;
+    const float cos_phi = cos_delta_phi(wo, nwi, f->t, f->bt);
+    const float phi = acos_sample(cos_phi);
+    const float scale = cos_i != 0.f ? 1.f / fabsf(cos_i) : 0.f;
+    if (f->fourier_channels == 1) {
+        float y = 0.f;
+        for (uint32_t i = 0; i < count; i++) y += coeffs[i] * cos_sample((float)i * phi);
+        const float v = y * scale;
+        return mkc(v, v, v);
+    }
+    float y = 0.f, r = 0.f, b = 0.f;
+    for (uint32_t i = 0; i < count; i++) {
+        const float c = cos_sample((float)i * phi);
+        y += coeffs[i + 0 * count] * c;
+        r += coeffs[i + 1 * count] * c;
+        b += coeffs[i + 2 * count] * c;
+    }
+    const float g = 1.398304f * y - 0.297381f * r - 0.100923f * b; /* get_green_from_YRB, src/lib/color.cpp:26-29 */
+    return mkc(r * scale, g * scale, b * scale);
+}
+
 static col leaf_evaluate(const bsdf_t* f, v3 wo, v3 wi) {
     if (f->type == YAR_MATERIAL_DIFFUSE) return mulcs(f->reflectance, PI_INV_F);
+    if (f->type == YAR_MATERIAL_PBRT3_FOURIER) return fourier_evaluate(f, wo, wi);
     if (f->type == YAR_MATERIAL_PBRT3_UBER) { /* src/ref/bsdf_pbrt.cpp:34-52; diffuse_coeff holds the opacity */
         col diffuse = mulc(mulcs(f->reflectance, PI_INV_F), f->diffuse_coeff);
         v3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
@@ -1385,7 +1456,8 @@ static float glass_reflection_probability(const bsdf_t* f, float fresnel) {
 }
 
 static float leaf_pdf(const bsdf_t* f, v3 wo, v3 wi) {
-    if (f->type == YAR_MATERIAL_DIFFUSE) return dot3(f->n, wi) / PI_F;
+    /* Pbrt3_Fourier_BSDF::pdf (src/ref/bsdf_pbrt.cpp:368-372): cosine-weighted */
+    if (f->type == YAR_MATERIAL_DIFFUSE || f->type == YAR_MATERIAL_PBRT3_FOURIER) return dot3(f->n, wi) / PI_F;
     if (f->type == YAR_MATERIAL_PBRT3_UBER) { /* src/ref/bsdf_pbrt.cpp:74-87 */
         float diffuse_pdf = dot3(f->n, wi) / PI_F;
         v3 wo_l = world_to_local(f, wo), wi_l = world_to_local(f, wi);
@@ -1489,7 +1561,8 @@ static col leaf_sample(const bsdf_t* f, float u0, float u1, float u_scatter, v3 
         if (*pdf == 0.f) return mkc(0, 0, 0);
         return leaf_evaluate(f, wo, *wi);
     }
-    if (f->type == YAR_MATERIAL_DIFFUSE) {
+    if (f->type == YAR_MATERIAL_DIFFUSE || f->type == YAR_MATERIAL_PBRT3_FOURIER) {
+        /* Pbrt3_Fourier_BSDF::sample (src/ref/bsdf_pbrt.cpp:360-366) samples as Diffuse_BRDF */
         v3 l = sample_hemisphere_cosine(u0, u1);
         *wi = local_to_world(f, l);
         *pdf = leaf_pdf(f, wo, *wi);
@@ -2764,8 +2837,30 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
         if (t != YAR_MATERIAL_DIFFUSE && t != YAR_MATERIAL_METAL && t != YAR_MATERIAL_GLASS &&
             t != YAR_MATERIAL_PLASTIC && t != YAR_MATERIAL_COATED_DIFFUSE && t != YAR_MATERIAL_PERFECT_REFLECTOR &&
             t != YAR_MATERIAL_PERFECT_REFRACTOR && t != YAR_MATERIAL_DIFFUSE_TRANSMISSION &&
-            t != YAR_MATERIAL_PBRT3_TRANSLUCENT && t != YAR_MATERIAL_PBRT3_UBER && t != YAR_MATERIAL_MIX)
+            t != YAR_MATERIAL_PBRT3_TRANSLUCENT && t != YAR_MATERIAL_PBRT3_UBER && t != YAR_MATERIAL_MIX &&
+            t != YAR_MATERIAL_PBRT3_FOURIER)
             return YAR_ERR_UNSUPPORTED;
+        if (t == YAR_MATERIAL_PBRT3_FOURIER) {
+            /* the tables the reference's evaluation accepts: one or three channels,
+             * reflection only (eta 1), increasing nodes ending at or above 1 (so
+             * lower_bound finds every clamped cosine), series inside the coefficients */
+            const uint32_t ti = s->materials[i].fourier_table;
+            if (ti == 0 || ti > s->fourier_count) return YAR_ERR_INVALID;
+            const yar_fourier_desc* ft = &s->fourier_tables[ti - 1];
+            const uint64_t pairs = (uint64_t)ft->node_count * ft->node_count;
+            if (ft->node_count == 0 || ft->nodes + ft->node_count > s->fourier_float_count ||
+                ft->coeffs + ft->coeff_count > s->fourier_float_count || ft->series + 2 * pairs > s->fourier_uint_count)
+                return YAR_ERR_INVALID;
+            if ((ft->channel_count != 1 && ft->channel_count != 3) || ft->eta != 1.f) return YAR_ERR_UNSUPPORTED;
+            const float* nodes = s->fourier_floats + ft->nodes;
+            for (uint32_t k = 1; k < ft->node_count; k++)
+                if (!(nodes[k - 1] <= nodes[k])) return YAR_ERR_INVALID;
+            if (!(nodes[ft->node_count - 1] >= 1.f)) return YAR_ERR_UNSUPPORTED;
+            for (uint64_t k = 0; k < pairs; k++) {
+                const uint64_t off = s->fourier_uints[ft->series + 2 * k], cnt = s->fourier_uints[ft->series + 2 * k + 1];
+                if (off + cnt * ft->channel_count > ft->coeff_count) return YAR_ERR_INVALID;
+            }
+        }
     }
     if (s->other_light_count) return YAR_ERR_UNSUPPORTED;
     /* image textures: the reflectance of diffuse, plastic, coated diffuse, glass
@@ -2809,7 +2904,8 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
                 if (si < 0 || (uint32_t)si >= s->material_count) return YAR_ERR_INVALID;
                 const yar_material_desc* sm = &s->materials[si];
                 if (sm->type == YAR_MATERIAL_MIX || sm->type == YAR_MATERIAL_PBRT3_UBER ||
-                    (sm->type == YAR_MATERIAL_GLASS && !(sm->u_roughness > 0.f)) || sm->bump)
+                    (sm->type == YAR_MATERIAL_GLASS && !(sm->u_roughness > 0.f)) || sm->bump ||
+                    sm->type == YAR_MATERIAL_PBRT3_FOURIER)
                     return YAR_ERR_UNSUPPORTED;
                 delta_subs += is_pure_delta(sm->type);
             }

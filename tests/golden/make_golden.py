@@ -76,6 +76,11 @@ Fixtures
                              checker reflectance and transmittance, GGX boxes;
                              rendered by the reference from the edited flat
                              scene, seed 21.
+  cornell_fourier_64.yfs / .npz  pbrt "fourier" boxes: a one-channel and a
+                             three-channel layerlab table written by
+                             write_fourier_bsdf (15 zenith nodes, glossy lobes
+                             of up to 8 azimuthal terms, series lengths that
+                             vary per node pair), seed 23.
   cornell_direct_64.yfs / .npz  the reference's direct-lighting algorithm
                              (pbrt "directlighting"): GGX boxes, the quad light
                              with 4 samples (2 x 2 arrays), point, spot and
@@ -457,6 +462,66 @@ def cornell_bump_64():
     np.savez_compressed(os.path.join(HERE, "cornell_bump_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def write_fourier_bsdf(path, channels, nodes=15, order=8, gloss=6.0, albedo=(0.7, 0.5, 0.3)):
+    """A layerlab "SCATFUN" v1 file (the subset Pbrt3_Fourier_Material::load_bsdf_file
+    reads, src/lib/material_pbrt.cpp:24-102): increasing zenith cosines from -1
+    to 1, an unused CDF table, (offset, length) per node pair (outgoing-major)
+    and the coefficients.  The tabulated function |mu_i| f(mu_o, mu_i, phi) is
+    a diffuse term plus a lobe around phi = pi, reflection pairs only (mu_o > 0,
+    mu_i < 0); each pair keeps the terms above a threshold, so series lengths
+    differ.  Three channels store Y, R and B."""
+    import struct
+    mu = np.linspace(-1.0, 1.0, nodes).astype(np.float32)
+    phi = (np.arange(256) + 0.5) * (np.pi / 256)
+    lum = np.array([0.2126729, 0.7151522, 0.0721750])
+    offsets, counts, coeffs = [], [], []
+    for o in range(nodes):
+        for i in range(nodes):
+            if not (mu[o] > 0 and mu[i] < 0):
+                offsets.append(len(coeffs))
+                counts.append(0)
+                continue
+            spread = gloss * (0.5 + 0.5 * float(mu[o]))
+            f = abs(float(mu[i])) * (0.15 + np.exp(spread * (np.cos(phi - np.pi) - 1.0)) * (0.3 + 0.4 * float(mu[o])))
+            a = np.array([np.mean(f * np.cos(k * phi)) * (1.0 if k == 0 else 2.0) for k in range(order)])
+            keep = int(np.max(np.nonzero(np.abs(a) > 1e-3)[0])) + 1
+            offsets.append(len(coeffs))
+            counts.append(keep)
+            if channels == 1:
+                coeffs.extend(a[:keep])
+            else:
+                rgb = [a[:keep] * c for c in albedo]
+                y = lum[0] * rgb[0] + lum[1] * rgb[1] + lum[2] * rgb[2]
+                coeffs.extend(y)
+                coeffs.extend(rgb[0])
+                coeffs.extend(rgb[2])
+    header = b"SCATFUN" + bytes([1]) + struct.pack("<9I", 1, nodes, len(coeffs), order, channels, 1, 0, 0, 0) + \
+        struct.pack("<5f", 1.0, 0.1, 0.1, 0.0, 0.0)
+    assert len(header) == 64
+    table = np.stack([np.array(offsets, np.uint32), np.array(counts, np.uint32)], axis=1).reshape(-1)
+    with open(path, "wb") as f:
+        f.write(header)
+        f.write(mu.tobytes())
+        f.write(np.zeros(nodes * nodes, np.float32).tobytes())
+        f.write(table.astype(np.uint32).tobytes())
+        f.write(np.array(coeffs, np.float32).tobytes())
+
+
+FOURIER_BOXES = ('Material "fourier" "string bsdffile" "mono.bsdf"', 'Material "fourier" "string bsdffile" "rgb.bsdf"')
+
+
+def cornell_fourier_64():
+    with tempfile.TemporaryDirectory() as d:
+        write_fourier_bsdf(os.path.join(d, "mono.bsdf"), 1)
+        write_fourier_bsdf(os.path.join(d, "rgb.bsdf"), 3, gloss=12.0)
+        pbrt = os.path.join(d, "cornell_fourier.pbrt")
+        open(pbrt, "w").write(scenes.cornell_pbrt(seed=23, width=64, height=64, spp=16, maxdepth=8,
+                                                  box_materials=FOURIER_BOXES))
+        oracle.ref_flatten(pbrt, os.path.join(HERE, "cornell_fourier_64.yfs"), seed_offset=1)
+        img, info = oracle.ref_render(pbrt, seed_offset=1, threads=8)
+    np.savez_compressed(os.path.join(HERE, "cornell_fourier_64.npz"), image=img, variance=np.float64(info["variance"]))
+
+
 def cornell_direct_64():
     _pbrt_golden("cornell_direct_64", 15, box_materials=scenes.GGX_BOXES, light_sources=scenes.DELTA_LIGHTS,
                  light_samples=4, integrator="directlighting")
@@ -546,7 +611,7 @@ if __name__ == "__main__":
                              "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64",
                              "cornell_direct_64", "cornell_direct_env_64", "cornell_texture_64", "checkpoint_c1",
                              "cornell_gaussian_64", "cornell_triangle_64", "cornell_c1_256", "cornell_alpha_64",
-                             "cornell_bump_64",
+                             "cornell_bump_64", "cornell_fourier_64",
                              "exr_files",
                              "kdtree_cache_files"]
     for name in which:

@@ -46,7 +46,7 @@ def test_struct_sizes_match_the_header():
     from yar_gb300 import native
     assert ctypes.sizeof(native.KdNode) == 8
     assert ctypes.sizeof(native.ObjectDesc) == 164
-    assert ctypes.sizeof(native.MaterialDesc) == 212
+    assert ctypes.sizeof(native.MaterialDesc) == 216
     assert ctypes.sizeof(native.RectLightDesc) == 72
 
 
@@ -64,7 +64,7 @@ def test_struct_layouts_match_the_c_compiler(tmp_path):
                "yar_camera_desc": native.CameraDesc, "yar_render_config": native.RenderConfig,
                "yar_flat_scene": native.FlatSceneDesc, "yar_texture_desc": native.TextureDesc,
                "yar_texture_mip_desc": native.TextureMipDesc, "yar_gpu_options": native.GpuOptions,
-               "yar_hit_soa": native.HitSoa}
+               "yar_hit_soa": native.HitSoa, "yar_fourier_desc": native.FourierDesc}
     lines = ['#include <stdio.h>', '#include <stddef.h>', '#include "yar_gpu.h"', "int main(void) {"]
     for name, cls in mirrors.items():
         lines.append('  printf("%s %%zu\\n", sizeof(%s));' % (name, name))

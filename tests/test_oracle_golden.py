@@ -126,7 +126,7 @@ def test_builder_against_live_reference_large_mesh():
                                   "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64",
                                   "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64",
                                   "cornell_texture_64", "cornell_gaussian_64", "cornell_triangle_64",
-                                  "cornell_alpha_64", "cornell_bump_64"])
+                                  "cornell_alpha_64", "cornell_bump_64", "cornell_fourier_64"])
 def test_oracle_render_matches_reference_golden(name):
     """The oracle's path loop, sampler, shading, BSDFs (diffuse, GGX metal, rough
     glass, plastic in both of the reference's forms, coated diffuse), delta

@@ -4,7 +4,8 @@
 // kd-trees (node words bit for bit as KdTree::save writes them,
 // src/ref/kdtree.cpp:137-160), scene objects, the scene kd-tree, constant
 // materials, rectangular lights, point/spot/directional, triangle-mesh,
-// sphere and environment lights and image textures (optional chunks), camera
+// sphere and environment lights, image textures and pbrt3 fourier BSDF
+// tables (optional chunks), camera
 // and Raytracer_Config.  It is produced
 // by the host scene loader of this library and by the reference-side adapter
 // that flattens a reference Scene_Context, so both sides can be compared on
@@ -54,6 +55,9 @@ struct Scene {
     std::vector<yar_texture_desc> textures;
     std::vector<yar_texture_mip_desc> texture_mips;
     std::vector<float> texels;           // RGB triples
+    std::vector<yar_fourier_desc> fourier_tables;
+    std::vector<float> fourier_floats;
+    std::vector<uint32_t> fourier_uints;
     uint32_t other_light_count = 0;
     yar_camera_desc camera{};
     yar_render_config config{};
@@ -109,6 +113,12 @@ struct Scene {
         s.texture_mips = texture_mips.empty() ? nullptr : texture_mips.data();
         s.texels = texels.empty() ? nullptr : texels.data();
         s.texel_count = texels.size() / 3;
+        s.fourier_count = (uint32_t)fourier_tables.size();
+        s.fourier_tables = fourier_tables.empty() ? nullptr : fourier_tables.data();
+        s.fourier_float_count = fourier_floats.size();
+        s.fourier_floats = fourier_floats.empty() ? nullptr : fourier_floats.data();
+        s.fourier_uint_count = fourier_uints.size();
+        s.fourier_uints = fourier_uints.empty() ? nullptr : fourier_uints.data();
         return s;
     }
 };
@@ -249,6 +259,18 @@ inline bool write(const std::string& path, const Scene& s) {
         b.raw(s.texels.data(), s.texels.size() * sizeof(float));
         w.chunk("TEXS", b.b);
     }
+    if (!s.fourier_tables.empty()) {  // FOUR: counts, table records, floats, uints
+        detail::Buf b;
+        const uint32_t nt = (uint32_t)s.fourier_tables.size();
+        const uint64_t nf = s.fourier_floats.size(), nu = s.fourier_uints.size();
+        b.pod(nt);
+        b.pod(nf);
+        b.pod(nu);
+        b.raw(s.fourier_tables.data(), nt * sizeof(yar_fourier_desc));
+        b.raw(s.fourier_floats.data(), nf * sizeof(float));
+        b.raw(s.fourier_uints.data(), nu * sizeof(uint32_t));
+        w.chunk("FOUR", b.b);
+    }
     bool ok = w.ok;
     if (fclose(f) != 0) ok = false;
     return ok;
@@ -362,6 +384,18 @@ inline bool read(const std::string& path, Scene& s, std::string* err = nullptr) 
             c.raw(s.texture_mips.data(), nm * sizeof(yar_texture_mip_desc));
             s.texels.resize(nx * 3);
             c.raw(s.texels.data(), s.texels.size() * sizeof(float));
+        } else if (!memcmp(tag, "FOUR", 4)) {
+            const uint32_t nt = c.pod<uint32_t>();
+            const uint64_t nf = c.pod<uint64_t>(), nu = c.pod<uint64_t>();
+            if (!c.ok || nt > size / sizeof(yar_fourier_desc) || nf > size / 4 || nu > size / 4 ||
+                (uint64_t)nt * sizeof(yar_fourier_desc) + (nf + nu) * 4 > size)
+                return fail("bad fourier chunk");
+            s.fourier_tables.resize(nt);
+            c.raw(s.fourier_tables.data(), nt * sizeof(yar_fourier_desc));
+            s.fourier_floats.resize(nf);
+            c.raw(s.fourier_floats.data(), nf * sizeof(float));
+            s.fourier_uints.resize(nu);
+            c.raw(s.fourier_uints.data(), nu * sizeof(uint32_t));
         } else if (!memcmp(tag, "ENVM", 4)) {
             s.environment = c.pod<yar_environment_desc>();
             const uint64_t count = 3ull * s.environment.width * s.environment.height;

@@ -79,7 +79,7 @@ class MaterialDesc(C.Structure):
                 ("other_textured_parameters", C.c_uint32),
                 ("transmittance_texture", C.c_uint32), ("transmittance_uv_scale", C.c_float * 2),
                 ("bump", C.c_uint32), ("bump_height", C.c_float), ("bump_texture", C.c_uint32),
-                ("bump_uv_scale", C.c_float * 2)]
+                ("bump_uv_scale", C.c_float * 2), ("fourier_table", C.c_uint32)]
 
 
 class RectLightDesc(C.Structure):
@@ -131,6 +131,12 @@ class TextureMipDesc(C.Structure):
     _fields_ = [("width", C.c_uint32), ("height", C.c_uint32), ("texel_offset", C.c_uint64)]
 
 
+class FourierDesc(C.Structure):
+    _fields_ = [("node_count", C.c_uint32), ("channel_count", C.c_uint32), ("max_order", C.c_uint32),
+                ("eta", C.c_float), ("nodes", C.c_uint64), ("coeffs", C.c_uint64), ("coeff_count", C.c_uint64),
+                ("series", C.c_uint64)]
+
+
 class FlatSceneDesc(C.Structure):
     _fields_ = [("mesh_count", C.c_uint32), ("meshes", C.POINTER(MeshDesc)),
                 ("object_count", C.c_uint32), ("objects", C.POINTER(ObjectDesc)),
@@ -144,7 +150,10 @@ class FlatSceneDesc(C.Structure):
                 ("environment", C.POINTER(EnvironmentDesc)),
                 ("texture_count", C.c_uint32), ("textures", C.POINTER(TextureDesc)),
                 ("texture_mip_count", C.c_uint32), ("texture_mips", C.POINTER(TextureMipDesc)),
-                ("texels", C.c_void_p), ("texel_count", C.c_uint64)]
+                ("texels", C.c_void_p), ("texel_count", C.c_uint64),
+                ("fourier_count", C.c_uint32), ("fourier_tables", C.POINTER(FourierDesc)),
+                ("fourier_float_count", C.c_uint64), ("fourier_floats", C.c_void_p),
+                ("fourier_uint_count", C.c_uint64), ("fourier_uints", C.c_void_p)]
 
 
 class HitSoa(C.Structure):

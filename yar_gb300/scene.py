@@ -27,7 +27,7 @@ MATERIAL_DTYPE = np.dtype([("type", "<u4"), ("reflectance", "<f4", 3), ("transmi
                            ("other_textured_parameters", "<u4"),
                            ("transmittance_texture", "<u4"), ("transmittance_uv_scale", "<f4", 2),
                            ("bump", "<u4"), ("bump_height", "<f4"), ("bump_texture", "<u4"),
-                           ("bump_uv_scale", "<f4", 2)])
+                           ("bump_uv_scale", "<f4", 2), ("fourier_table", "<u4")])
 MATERIAL_RECORD_V1 = 72  # the MATS chunk's records: the fields up to roughness_is_alpha
 LIGHT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("emitted_radiance", "<f4", 3), ("size", "<f4", 2),
                         ("sample_count", "<i4")])
@@ -41,6 +41,8 @@ ENVIRONMENT_DTYPE = np.dtype([("light_to_world", "<f4", 12), ("world_to_light", 
                               ("sample_count", "<i4"), ("width", "<u4"), ("height", "<u4"), ("radiance", "<u8")])
 TEXTURE_DTYPE = np.dtype([("first_mip", "<u4"), ("mip_count", "<u4")])
 TEXTURE_MIP_DTYPE = np.dtype([("width", "<u4"), ("height", "<u4"), ("texel_offset", "<u8")])
+FOURIER_DTYPE = np.dtype([("node_count", "<u4"), ("channel_count", "<u4"), ("max_order", "<u4"), ("eta", "<f4"),
+                          ("nodes", "<u8"), ("coeffs", "<u8"), ("coeff_count", "<u8"), ("series", "<u8")])
 CAMERA_DTYPE = np.dtype([("camera_to_world", "<f4", 12), ("image_extent", "<f4", 2), ("horz_half_dist", "<f4"),
                          ("vert_half_dist", "<f4"), ("z_is_up", "<i4")])
 CONFIG_DTYPE = np.dtype([("render_region", "<i4", 4), ("rendering_algorithm", "<i4"), ("max_light_bounces", "<i4"),
@@ -61,6 +63,7 @@ assert SPHERE_LIGHT_DTYPE.itemsize == C.sizeof(native.SphereLightDesc)
 assert CAMERA_DTYPE.itemsize == C.sizeof(native.CameraDesc)
 assert TEXTURE_DTYPE.itemsize == C.sizeof(native.TextureDesc)
 assert TEXTURE_MIP_DTYPE.itemsize == C.sizeof(native.TextureMipDesc)
+assert FOURIER_DTYPE.itemsize == C.sizeof(native.FourierDesc)
 assert CONFIG_DTYPE.itemsize == C.sizeof(native.RenderConfig)
 
 IDENTITY = np.array([1, 0, 0, 0, 0, 1, 0, 0, 0, 0, 1, 0], np.float32)
@@ -121,6 +124,10 @@ class FlatScene:
         self.textures = np.zeros(0, TEXTURE_DTYPE)
         self.texture_mips = np.zeros(0, TEXTURE_MIP_DTYPE)
         self.texels = np.zeros((0, 3), np.float32)
+        # pbrt3 fourier BSDF tables: records and the floats / uints they index
+        self.fourier_tables = np.zeros(0, FOURIER_DTYPE)
+        self.fourier_floats = np.zeros(0, np.float32)
+        self.fourier_uints = np.zeros(0, np.uint32)
         self.other_light_count = 0
         self.camera = np.zeros((), CAMERA_DTYPE)
         self.config = default_config()
@@ -245,6 +252,17 @@ class FlatScene:
             s.texture_mips = C.cast(mips.ctypes.data, C.POINTER(native.TextureMipDesc))
             s.texels = texels.ctypes.data
             s.texel_count = texels.shape[0]
+        if self.fourier_tables.shape[0]:
+            ft = np.ascontiguousarray(self.fourier_tables, FOURIER_DTYPE)
+            ff = np.ascontiguousarray(self.fourier_floats, np.float32)
+            fu = np.ascontiguousarray(self.fourier_uints, np.uint32)
+            keep += [ft, ff, fu]
+            s.fourier_count = ft.shape[0]
+            s.fourier_tables = C.cast(ft.ctypes.data, C.POINTER(native.FourierDesc))
+            s.fourier_float_count = ff.shape[0]
+            s.fourier_floats = ff.ctypes.data
+            s.fourier_uint_count = fu.shape[0]
+            s.fourier_uints = fu.ctypes.data
         C.memmove(C.byref(s.camera), np.ascontiguousarray(self.camera).ctypes.data, CAMERA_DTYPE.itemsize)
         C.memmove(C.byref(s.config), np.ascontiguousarray(self.config).ctypes.data, CONFIG_DTYPE.itemsize)
         return s, keep
@@ -295,6 +313,12 @@ class FlatScene:
                                np.ascontiguousarray(self.textures, TEXTURE_DTYPE).tobytes() +
                                np.ascontiguousarray(self.texture_mips, TEXTURE_MIP_DTYPE).tobytes() +
                                np.ascontiguousarray(self.texels, np.float32).tobytes()))
+        if self.fourier_tables.shape[0]:
+            parts.append(chunk(b"FOUR", struct.pack("<IQQ", self.fourier_tables.shape[0], self.fourier_floats.shape[0],
+                                                    self.fourier_uints.shape[0]) +
+                               np.ascontiguousarray(self.fourier_tables, FOURIER_DTYPE).tobytes() +
+                               np.ascontiguousarray(self.fourier_floats, np.float32).tobytes() +
+                               np.ascontiguousarray(self.fourier_uints, np.uint32).tobytes()))
         with open(path, "wb") as f:
             f.write(b"".join(parts))
 
@@ -375,6 +399,14 @@ class FlatScene:
                 s.texture_mips = np.frombuffer(p[q:q + nm * TEXTURE_MIP_DTYPE.itemsize], TEXTURE_MIP_DTYPE).copy()
                 q += nm * TEXTURE_MIP_DTYPE.itemsize
                 s.texels = np.frombuffer(p[q:q + 12 * nx], np.float32).reshape(-1, 3).copy()
+            elif tag == b"FOUR":
+                nt, nf, nu = struct.unpack_from("<IQQ", p, 0)
+                q = 20
+                s.fourier_tables = np.frombuffer(p[q:q + nt * FOURIER_DTYPE.itemsize], FOURIER_DTYPE).copy()
+                q += nt * FOURIER_DTYPE.itemsize
+                s.fourier_floats = np.frombuffer(p[q:q + 4 * nf], np.float32).copy()
+                q += 4 * nf
+                s.fourier_uints = np.frombuffer(p[q:q + 4 * nu], np.uint32).copy()
             elif tag == b"SPHL":
                 n = struct.unpack_from("<I", p, 0)[0]
                 s.sphere_lights = np.frombuffer(p[4:4 + n * SPHERE_LIGHT_DTYPE.itemsize], SPHERE_LIGHT_DTYPE).copy()
