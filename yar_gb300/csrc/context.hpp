@@ -37,10 +37,13 @@ struct Render_Scene {
     Device_Buffer texture_mips;  // uint4 per mip: width, height, texel offset, -
     Device_Buffer textures;      // uint2 per texture: first mip, mip count
     Device_Buffer ewa_weights;   // the EWA filter's 256 weights
+    Device_Buffer fourier_floats;  // pbrt3 fourier tables: zenith cosines and coefficients
+    Device_Buffer fourier_uints;   // and (offset, length) per node pair
     Device_Buffer object_info;  // int4 per object: material type, material index, light type, light index
     Device_Buffer object_to_world;         // float[12] per object
     Device_Buffer object_to_world_normal;  // float[12] per object
     std::vector<yar_material_desc> host_materials;
+    std::vector<yar_fourier_desc> host_fourier_tables;
     std::vector<yar_rect_light_desc> host_rect_lights;
     std::vector<yar_delta_light_desc> host_delta_lights;
     uint32_t mesh_light_count = 0;

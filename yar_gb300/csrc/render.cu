@@ -69,6 +69,12 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
         d.bump_height = m.bump_height;
         d.bump_texture = m.bump == 2 ? m.bump_texture : 0u;
         d.bump_scale = make_float2(m.bump_uv_scale[0], m.bump_uv_scale[1]);
+        if (m.type == YAR_MATERIAL_PBRT3_FOURIER && m.fourier_table >= 1 && m.fourier_table <= scene->fourier_count &&
+            scene->fourier_tables) {  // the table's device addresses are set after its upload
+            const yar_fourier_desc& t = scene->fourier_tables[m.fourier_table - 1];
+            d.fourier_node_count = t.node_count;
+            d.fourier_channels = t.channel_count;
+        }
         d.transmittance = Col{m.transmittance[0], m.transmittance[1], m.transmittance[2]};
         d.eta_t = Col{m.eta[0], m.eta[1], m.eta[2]};
         d.k_t = Col{m.k[0], m.k[1], m.k[2]};
@@ -265,6 +271,9 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
         }
     }
     R.host_materials.assign(scene->materials, scene->materials + scene->material_count);
+    R.host_fourier_tables.clear();
+    if (scene->fourier_tables)
+        R.host_fourier_tables.assign(scene->fourier_tables, scene->fourier_tables + scene->fourier_count);
     R.host_rect_lights.assign(scene->rect_lights, scene->rect_lights + scene->rect_light_count);
     R.host_object_info.resize(4 * (size_t)scene->object_count);
     for (uint32_t i = 0; i < scene->object_count; i++) {
@@ -283,6 +292,43 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
     };
     if ((rc = up(R.shading, shading.data(), shading.size() * sizeof(float4))) != YAR_OK) return rc;
     if ((rc = up(R.object_info, obj.data(), obj.size() * sizeof(float4))) != YAR_OK) return rc;
+    // pbrt3 fourier tables: every read the evaluation makes stays inside them
+    // (one or three channels, series inside the coefficients, the last node at
+    // least 1 so that the node search of a clamped cosine ends inside)
+    if (scene->fourier_count) {
+        if (!scene->fourier_tables || !scene->fourier_floats || !scene->fourier_uints)
+            return fail(ctx, YAR_ERR_INVALID, "fourier tables without data");
+        for (uint32_t i = 0; i < scene->fourier_count; i++) {
+            const yar_fourier_desc& t = scene->fourier_tables[i];
+            const uint64_t pairs = (uint64_t)t.node_count * t.node_count;
+            bool ok = t.node_count > 0 && t.node_count <= 65536 && (t.channel_count == 1 || t.channel_count == 3) &&
+                      t.nodes + t.node_count <= scene->fourier_float_count &&
+                      t.coeffs + t.coeff_count <= scene->fourier_float_count &&
+                      t.series + 2 * pairs <= scene->fourier_uint_count;
+            if (ok) ok = scene->fourier_floats[t.nodes + t.node_count - 1] >= 1.f;
+            for (uint64_t k = 0; ok && k < pairs; k++) {
+                const uint64_t off = scene->fourier_uints[t.series + 2 * k];
+                const uint64_t cnt = scene->fourier_uints[t.series + 2 * k + 1];
+                ok = off + cnt * t.channel_count <= t.coeff_count;
+            }
+            if (!ok) return fail(ctx, YAR_ERR_INVALID, "fourier table " + std::to_string(i) + " is malformed");
+        }
+        if ((rc = up(R.fourier_floats, scene->fourier_floats, scene->fourier_float_count * sizeof(float))) != YAR_OK)
+            return rc;
+        if ((rc = up(R.fourier_uints, scene->fourier_uints, scene->fourier_uint_count * sizeof(uint32_t))) != YAR_OK)
+            return rc;
+        const float* ff = reinterpret_cast<const float*>(R.fourier_floats.ptr);
+        const uint32_t* fu = reinterpret_cast<const uint32_t*>(R.fourier_uints.ptr);
+        for (uint32_t i = 0; i < scene->material_count; i++) {
+            const yar_material_desc& m = scene->materials[i];
+            if (m.type != YAR_MATERIAL_PBRT3_FOURIER || m.fourier_table == 0 || m.fourier_table > scene->fourier_count)
+                continue;
+            const yar_fourier_desc& t = scene->fourier_tables[m.fourier_table - 1];
+            mats[i].fourier_nodes = ff + t.nodes;
+            mats[i].fourier_coeffs = ff + t.coeffs;
+            mats[i].fourier_series = fu + t.series;
+        }
+    }
     if ((rc = up(R.materials, mats.data(), mats.size() * sizeof(Material_Dev))) != YAR_OK) return rc;
     if ((rc = up(R.rect_lights, lights.data(), lights.size() * sizeof(Rect_Light_Dev))) != YAR_OK) return rc;
     if ((rc = up(R.delta_lights, dlights.data(), dlights.size() * sizeof(Delta_Light_Dev))) != YAR_OK) return rc;
@@ -374,7 +420,7 @@ void render_release(yar_gpu_ctx* ctx) {
     Render_Scene& R = ctx->render;
     for (Device_Buffer* b : {&R.shading, &R.materials, &R.rect_lights, &R.delta_lights, &R.mesh_lights, &R.mesh_cdf,
                              &R.sphere_lights, &R.env_map, &R.env_marginal, &R.env_cdfs, &R.texels,
-                             &R.texture_mips, &R.textures, &R.ewa_weights, &R.object_info,
+                             &R.texture_mips, &R.textures, &R.ewa_weights, &R.fourier_floats, &R.fourier_uints, &R.object_info,
                              &R.object_to_world, &R.object_to_world_normal})
         device_free(*b);
     for (Device_Buffer& b : ctx->render_scratch) device_free(b);

@@ -145,6 +145,7 @@ enum : uint32_t {
     kMix = 8,
     kUber = 9,
     kTranslucent = 10,
+    kFourier = 11,
     kPbrt3Plastic = 0x105,
     kScaled = 0x108  // a mix with a pure delta material: the other one's BSDF, scaled
 };
@@ -185,6 +186,11 @@ struct Material_Dev {
     float bump_height;      // bump 1: the height
     uint32_t bump_texture;  // bump 2: 1 + the texture
     float2 bump_scale;      // bump 2: its uv scale
+    // pbrt3 fourier: the table (device pointers), its node count and channels
+    const float* fourier_nodes;
+    const float* fourier_coeffs;
+    const uint32_t* fourier_series;  // (offset, length) per node pair
+    uint32_t fourier_node_count, fourier_channels;
 };
 
 struct Bsdf {
@@ -230,6 +236,8 @@ __device__ __forceinline__ void set_material(Bsdf& f, const Material_Dev& m) {
         f.eta_i = enter ? 1.5f : 1.f;
     } else if (m.type == kUber) {  // Pbrt3_Uber_BRDF's relative IOR (bsdf_pbrt.cpp:14-32)
         f.eta_i = enter ? m.ior : 1.f / m.ior;
+    } else if (m.type == kFourier) {  // the table, read through the material
+        f.sub[0] = &m;
     }
 }
 
@@ -512,9 +520,69 @@ __device__ __forceinline__ Col leaf_sample(const Bsdf& f, float u0, float u1, fl
 
 // FULL = false compiles out the plastic and coated-diffuse branches, for
 // scenes that only use the diffuse, metal and rough-glass BSDFs.
+// cos_delta_phi (src/lib/math.h:87-104): the cosine of the azimuth between a
+// and b in the tangent plane (1 for a direction along the normal).
+__device__ __forceinline__ float cos_delta_phi(V3 a, V3 b, V3 t1, V3 t2) {
+    const float ax = dot(a, t1), ay = dot(a, t2), bx = dot(b, t1), by = dot(b, t2);
+    const float a_len_sq = ax * ax + ay * ay, b_len_sq = bx * bx + by * by;
+    if (a_len_sq == 0.f || b_len_sq == 0.f) return 1.f;
+    const float cosine = (ax * bx + ay * by) / sqrtf(a_len_sq * b_len_sq);
+    return cosine < -1.f ? -1.f : (1.f < cosine ? 1.f : cosine);
+}
+
+// The first zenith node not below c (std::lower_bound over increasing nodes;
+// the last node is at least 1, so a clamped cosine always finds one).
+__device__ __forceinline__ uint32_t fourier_node(const float* nodes, uint32_t count, float c) {
+    uint32_t lo = 0, n = count;
+    while (n > 0) {
+        const uint32_t half = n / 2;
+        if (__ldg(nodes + lo + half) < c) {
+            lo += half + 1;
+            n -= half + 1;
+        } else {
+            n = half;
+        }
+    }
+    return lo;
+}
+
+// Pbrt3_Fourier_BSDF::evaluate (src/ref/bsdf_pbrt.cpp:305-358): the nearest
+// node pair's Fourier series in the azimuth (no interpolation), divided by
+// |cos_i|; three channels store Y, R, B.  acos and cos rounded correctly.
+static __device__ __noinline__ Col fourier_evaluate(const Bsdf& f, V3 wo, V3 wi) {
+    const Material_Dev& m = *f.sub[0];
+    const V3 nwi = -wi;
+    float cos_i = dot(f.n, nwi);
+    cos_i = cos_i < -1.f ? -1.f : (1.f < cos_i ? 1.f : cos_i);
+    float cos_o = dot(f.n, wo);
+    cos_o = cos_o < -1.f ? -1.f : (1.f < cos_o ? 1.f : cos_o);
+    const uint32_t nc = m.fourier_node_count;
+    const uint32_t index = fourier_node(m.fourier_nodes, nc, cos_o) * nc + fourier_node(m.fourier_nodes, nc, cos_i);
+    const float* coeffs = m.fourier_coeffs + __ldg(m.fourier_series + 2 * (size_t)index);
+    const uint32_t count = __ldg(m.fourier_series + 2 * (size_t)index + 1);
+    const float phi = (float)acos((double)cos_delta_phi(wo, nwi, f.t, f.bt));
+    const float scale = cos_i != 0.f ? 1.f / fabsf(cos_i) : 0.f;
+    if (m.fourier_channels == 1) {
+        float y = 0.f;
+        for (uint32_t i = 0; i < count; i++) y += __ldg(coeffs + i) * cos_f((float)i * phi);
+        const float v = y * scale;
+        return col(v, v, v);
+    }
+    float y = 0.f, r = 0.f, b = 0.f;
+    for (uint32_t i = 0; i < count; i++) {
+        const float c = cos_f((float)i * phi);
+        y += __ldg(coeffs + i) * c;
+        r += __ldg(coeffs + i + count) * c;
+        b += __ldg(coeffs + i + 2 * count) * c;
+    }
+    const float g = 1.398304f * y - 0.297381f * r - 0.100923f * b;  // get_green_from_YRB, src/lib/color.cpp:26-29
+    return col(r * scale, g * scale, b * scale);
+}
+
 template <bool FULL>
 __device__ __forceinline__ Col leaf_evaluate_body(const Bsdf& f, V3 wo, V3 wi) {
     if (f.type == kDiffuse) return mul(f.reflectance, 1.f / kPi);
+    if (FULL && f.type == kFourier) return fourier_evaluate(f, wo, wi);
     if (FULL && (f.type == kPlastic || f.type == kPbrt3Plastic)) {
         // Plastic_BRDF::evaluate (src/ref/bsdf.cpp:215-234); Pbrt3_Plastic_BRDF::evaluate
         // (src/ref/bsdf_pbrt.cpp:264-290) with pbrt-v3's swapped 1.0 / 1.5 IOR pair
@@ -624,7 +692,8 @@ __device__ __forceinline__ Col leaf_evaluate_body(const Bsdf& f, V3 wo, V3 wi) {
 
 template <bool FULL>
 __device__ __forceinline__ float leaf_pdf_body(const Bsdf& f, V3 wo, V3 wi) {
-    if (f.type == kDiffuse) return dot(f.n, wi) / kPi;
+    // Pbrt3_Fourier_BSDF::pdf (src/ref/bsdf_pbrt.cpp:368-372): cosine-weighted as diffuse
+    if (f.type == kDiffuse || (FULL && f.type == kFourier)) return dot(f.n, wi) / kPi;
     if (FULL && (f.type == kPlastic || f.type == kPbrt3Plastic)) {  // Plastic_BRDF::pdf (src/ref/bsdf.cpp:253-263)
         const float diffuse_pdf = dot(f.n, wi) / kPi;
         const V3 wh = normalized(wo + wi);
@@ -750,7 +819,7 @@ __device__ __forceinline__ Col leaf_sample_body(const Bsdf& f, float u0, float u
         pdf = leaf_pdf<FULL>(f, wo, wi);
         return leaf_evaluate<FULL>(f, wo, wi);
     }
-    if (f.type == kDiffuse) {
+    if (f.type == kDiffuse || (FULL && f.type == kFourier)) {  // Pbrt3_Fourier_BSDF::sample: as diffuse
         wi = local_to_world(f, sample_hemisphere_cosine(u0, u1));
         pdf = leaf_pdf<FULL>(f, wo, wi);
         return leaf_evaluate<FULL>(f, wo, wi);

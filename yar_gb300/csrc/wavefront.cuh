@@ -1182,16 +1182,18 @@ __device__ __forceinline__ V3 sphere_sampler_sample(const Sphere_Sampler& ss, fl
 // light kind but the quad light.  A scene without them runs the FULL = false
 // instantiation, which has none of that code (launch_shade picks it from
 // Render_Params::full_shading).
-// Launch bounds: 4 blocks of 128 threads per SM (128 registers), where the
-// plain and the FULL instantiations spill nothing: the shadow, probe and next
-// extend rays wait for the warp's appends in shared memory, and the path's
-// radiance is read and written only where emission adds to it.  The guided
-// FULL instantiation keeps 3 blocks (164 registers, no spills); the guided
-// plain one spills 10 B at 4.  Before those changes the plain kernel ran at 5
+// Launch bounds: the plain instantiation (diffuse, metal, rough glass, quad
+// lights: the C1, C3 and batch renders) at 4 blocks of 128 threads per SM
+// (128 registers) spills nothing: the shadow, probe and next extend rays wait
+// for the warp's appends in shared memory, and the path's radiance is read and
+// written only where emission adds to it; its guided form spills 18 B.  The
+// FULL instantiations keep 3 blocks (160-162 registers, no spills; at 4 the
+// out-of-line BSDF routines, the fourier series among them, push the kernel
+// to 36-60 B of spills).  Before those changes the plain kernel ran at 5
 // blocks (96 registers, 202 B of spill stores), which measured 1.726 s on the
 // C3 render against 1.732 s at 4 blocks and 1.764 s at 3.
 template <bool GUIDED, bool FULL>
-__global__ void __launch_bounds__(kBlock, GUIDED && FULL ? 3 : 4)
+__global__ void __launch_bounds__(kBlock, FULL ? 3 : 4)
 shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float* __restrict__ s1d,
              const float2* __restrict__ s2d, Path_State ps, Queues q, Guide_Shade g) {
     // this thread's shadow, probe and next extend rays (origin + tmax,
@@ -2187,8 +2189,14 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
             m.type != YAR_MATERIAL_PLASTIC && m.type != YAR_MATERIAL_COATED_DIFFUSE &&
             m.type != YAR_MATERIAL_PERFECT_REFLECTOR && m.type != YAR_MATERIAL_PERFECT_REFRACTOR &&
             m.type != YAR_MATERIAL_DIFFUSE_TRANSMISSION && m.type != YAR_MATERIAL_PBRT3_TRANSLUCENT &&
-            m.type != YAR_MATERIAL_PBRT3_UBER && m.type != YAR_MATERIAL_MIX)
+            m.type != YAR_MATERIAL_PBRT3_UBER && m.type != YAR_MATERIAL_MIX && m.type != YAR_MATERIAL_PBRT3_FOURIER)
             return fail(ctx, YAR_ERR_UNSUPPORTED, "material type " + std::to_string(m.type) + " is not implemented");
+        if (m.type == YAR_MATERIAL_PBRT3_FOURIER) {
+            if (m.fourier_table == 0 || m.fourier_table > R.host_fourier_tables.size())
+                return fail(ctx, YAR_ERR_INVALID, "a fourier material without a table");
+            if (R.host_fourier_tables[m.fourier_table - 1].eta != 1.f)  // the reference asserts eta == 1
+                return fail(ctx, YAR_ERR_UNSUPPORTED, "fourier tables with refraction (eta != 1)");
+        }
         if (m.type == YAR_MATERIAL_MIX) {
             // one level: sub-materials that are pure delta or have no delta event, not both delta
             int delta_subs = 0;
@@ -2198,8 +2206,8 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
                     return fail(ctx, YAR_ERR_INVALID, "mix material with an invalid sub-material");
                 const yar_material_desc& sm = R.host_materials[si];
                 if (sm.type == YAR_MATERIAL_MIX || sm.type == YAR_MATERIAL_PBRT3_UBER ||
-                    (sm.type == YAR_MATERIAL_GLASS && !(sm.u_roughness > 0.f)))
-                    return fail(ctx, YAR_ERR_UNSUPPORTED, "mix of a mix, an uber or a smooth glass material");
+                    (sm.type == YAR_MATERIAL_GLASS && !(sm.u_roughness > 0.f)) || sm.type == YAR_MATERIAL_PBRT3_FOURIER)
+                    return fail(ctx, YAR_ERR_UNSUPPORTED, "mix of a mix, an uber, a smooth glass or a fourier material");
                 if (sm.bump)
                     return fail(ctx, YAR_ERR_UNSUPPORTED, "a mix of a bump-mapped material");
                 delta_subs += sm.type == YAR_MATERIAL_PERFECT_REFLECTOR || sm.type == YAR_MATERIAL_PERFECT_REFRACTOR;
