@@ -115,8 +115,12 @@ struct yar_gpu_ctx {
 
     cudaEvent_t ev_start = nullptr, ev_stop = nullptr;
 
-    // render scratch (path state, queues, per-pixel sample tables)
+    // render scratch (path state, queues, per-pixel sample tables); the guided
+    // render's training passes and its network inputs and lobes keep their own.
+    // Buffers stay allocated between calls and grow when a call needs more.
     std::vector<yar::Device_Buffer> render_scratch;
+    std::vector<yar::Device_Buffer> guided_scratch;
+    yar::Device_Buffer guide_queries, guide_lobes;
 
     // learned proposal (allocated on first use)
     yar::Guide guide;

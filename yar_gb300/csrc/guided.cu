@@ -173,11 +173,13 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
         if (!gp->keep_guide && (rc = guide_reset(ctx, 0x5eed0000ull + gp->stream_offset)) != YAR_OK) return rc;
     }
 
-    std::vector<Device_Buffer>& B = ctx->render_scratch;
-    for (Device_Buffer& b : B) device_free(b);
-    B.assign(40, Device_Buffer{});
-    auto alloc = [&](int i, size_t bytes) {
-        if (rc == YAR_OK && bytes) rc = device_alloc(ctx, B[i], bytes);
+    std::vector<Device_Buffer>& B = ctx->guided_scratch;
+    if (B.size() != 40) {
+        for (Device_Buffer& b : B) device_free(b);
+        B.assign(40, Device_Buffer{});
+    }
+    auto alloc = [&](int i, size_t bytes) {  // kept from an earlier call when large enough
+        if (rc == YAR_OK && bytes && !(B[i].ptr && B[i].bytes >= bytes)) rc = device_alloc(ctx, B[i], bytes);
     };
     const size_t cap = paths;
     alloc(1, cap * sizeof(float2));                        // image-plane samples
@@ -330,21 +332,19 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
     if (spp_side && e == cudaSuccess) {
         // the image: the scene's pixel sampler at spp_side^2 samples per pixel,
         // continuations from the trained proposal
-        for (Device_Buffer& b : B) device_free(b);  // the stratified render allocates its own working set
-        Device_Buffer qbuf, lbuf;
+        Device_Buffer& qbuf = ctx->guide_queries;
+        Device_Buffer& lbuf = ctx->guide_lobes;
         Guide_Hook_State hs{ctx, S, nullptr, nullptr, {box[0], box[1], box[2], box[3], box[4], box[5]}};
         Guide_Render_Hook hook;
         hook.alpha = guided ? gp->guide_fraction : 0.f;
         hook.max_bounce = (int)std::min<uint32_t>(gp->guide_bounces, 1u << 20);
         hook.chunk_paths = std::max<uint64_t>(kGuidedChunkPaths, (uint64_t)spp_side * spp_side);
         if (guided) {
-            rc = device_alloc(ctx, qbuf, hook.chunk_paths * 3 * sizeof(float4));
-            if (rc == YAR_OK) rc = device_alloc(ctx, lbuf, hook.chunk_paths * kGuideLobeFloats * sizeof(float));
-            if (rc != YAR_OK) {
-                device_free(qbuf);
-                device_free(lbuf);
-                return rc;
-            }
+            const size_t qbytes = hook.chunk_paths * 3 * sizeof(float4);
+            const size_t lbytes = hook.chunk_paths * kGuideLobeFloats * sizeof(float);
+            if (!(qbuf.ptr && qbuf.bytes >= qbytes)) rc = device_alloc(ctx, qbuf, qbytes);
+            if (rc == YAR_OK && !(lbuf.ptr && lbuf.bytes >= lbytes)) rc = device_alloc(ctx, lbuf, lbytes);
+            if (rc != YAR_OK) return rc;
             hs.queries = dp<float4>(qbuf);
             hs.lobes = dp<float>(lbuf);
             hook.queries = hs.queries;
@@ -356,8 +356,6 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
         yar_render_stats rs{};
         if (!guided) hook.chunk_paths = std::max<uint64_t>(kChunkSampleBudget, (uint64_t)spp_side * spp_side);
         rc = render_guided_stratified(ctx, spp_side, (gp->stream_offset << 20) | 0xfffffu, hook, img.data(), &rs);
-        device_free(qbuf);
-        device_free(lbuf);
         if (rc != YAR_OK) return rc;
         int h_err = 0;
         e = cudaMemcpy(&h_err, ctx->d_error, sizeof(int), cudaMemcpyDeviceToHost);

@@ -425,6 +425,10 @@ void render_release(yar_gpu_ctx* ctx) {
         device_free(*b);
     for (Device_Buffer& b : ctx->render_scratch) device_free(b);
     ctx->render_scratch.clear();
+    for (Device_Buffer& b : ctx->guided_scratch) device_free(b);
+    ctx->guided_scratch.clear();
+    device_free(ctx->guide_queries);
+    device_free(ctx->guide_lobes);
 }
 
 // Per-tile film data of a render (checkpoint bands): each tile's variance
