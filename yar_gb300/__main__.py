@@ -43,6 +43,9 @@ def main(argv=None):
             q.add_argument("--spp", type=int, default=0, help="samples per pixel (rounded up to k*k)")
             q.add_argument("--seedoffset", type=int, default=None)
             q.add_argument("--traversal", choices=["auto", "p64", "p128", "per-ray", "per-ray-vote"], default="auto")
+            q.add_argument("--repeat", type=int, default=1,
+                           help="render this many times (the first render of a scene times the traversal "
+                                "kernels; later ones drive their bounces from the device); the last is written")
         else:
             q.add_argument("--passes", type=int, default=256)
             q.add_argument("--guide-fraction", type=float, default=0.7)
@@ -74,7 +77,8 @@ def main(argv=None):
         if a.seedoffset is not None:
             s.config["rng_seed_offset"] = a.seedoffset
         ctx.upload_scene(s)
-        img, st = ctx.render(w, h)
+        for _ in range(max(1, a.repeat)):
+            img, st = ctx.render(w, h)
         spp = int(s.config["x_pixel_sample_count"] * s.config["y_pixel_sample_count"])
         attrs = exr.yar_attributes(spp=spp, variance=st.variance, input_file=a.scene, device="gpu")
         print("rendered %dx%d at %d spp in %.3f s (%.1f M paths/s), variance %.6g" % (
