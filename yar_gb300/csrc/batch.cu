@@ -122,13 +122,14 @@ int alloc_branches(Batch& bt, int nb, uint64_t chunk_cap, bool one_spp) {
         cudaError_t e = cudaStreamCreateWithFlags(&br.stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "batch streams");
         if (br.cap == 0) continue;
-        br.B.assign(27, Device_Buffer{});
+        br.B.assign(30, Device_Buffer{});
         const size_t cap = br.cap;
-        const size_t sizes[27] = {0, 0, cap * br.n1d * sizeof(float), cap * br.n2d * sizeof(float2),
+        const size_t sizes[30] = {0, 0, cap * br.n1d * sizeof(float), cap * br.n2d * sizeof(float2),
                                   cap * 16, cap * 16, cap * 4, cap * 16, cap * 16, cap * 16, cap * 16, cap * 16,
                                   cap * 16, cap, cap * 16, cap * 8, cap * 32, cap * 32, cap * 4, cap * 4, cap * 16,
-                                  cap * 8, cap * 32, cap * 4, cap * 32, cap * 4, 16 * sizeof(uint32_t)};
-        for (int i = 2; i < 27 && rc == YAR_OK; i++) rc = device_alloc(ctx, br.B[i], sizes[i]);
+                                  cap * 8, cap * 32, cap * 4, cap * 32, cap * 4, 16 * sizeof(uint32_t),
+                                  cap, cap * 4, 2 * kShadeClasses * sizeof(uint32_t)};  // shading order
+        for (int i = 2; i < 30 && rc == YAR_OK; i++) rc = device_alloc(ctx, br.B[i], sizes[i]);
         if (rc != YAR_OK) return rc;
         std::vector<Device_Buffer>& B = br.B;
         br.ps = Path_State{dp<float4>(B[4]), dp<float4>(B[5]), dp<uint32_t>(B[6]), dp<uint4>(B[7]),
@@ -165,6 +166,18 @@ cudaError_t enqueue_scene(Batch& bt, int si, bool one_spp, unsigned long long* s
     Queues q = br.q;
     Path_State ps = br.ps;
     uint32_t* ctr = q.counters;
+    // the shading order of each extend queue when the scene mixes BSDF classes
+    // (as render_run_params decides it)
+    uint32_t seen = 0;
+    const std::vector<int32_t>& oi = sub->render.host_object_info;
+    for (size_t o = 0; o + 3 < oi.size(); o += 4) {
+        if ((uint32_t)oi[o + 2] != YAR_LIGHT_NULL || (uint32_t)oi[o] == YAR_MATERIAL_NULL) continue;
+        const uint32_t m = (uint32_t)oi[o];
+        seen |= m == YAR_MATERIAL_DIFFUSE ? 1u : (m == YAR_MATERIAL_METAL ? 2u : 4u);
+    }
+    const bool mixed = (seen & (seen - 1)) != 0;
+    Queues qs = q;  // q with the order, for the shade kernel
+    qs.order = mixed ? dp<uint32_t>(br.B[28]) : nullptr;
     cudaError_t e = cudaSuccess;
     for (uint64_t first = 0; first < sc.pixels && e == cudaSuccess; first += chunk_pixels) {
         const uint32_t cp = (uint32_t)std::min<uint64_t>(chunk_pixels, sc.pixels - first);
@@ -186,7 +199,14 @@ cudaError_t enqueue_scene(Batch& bt, int si, bool one_spp, unsigned long long* s
             a.hit2 = q.ext_hit2;
             e = launch_extend(sub->ds, a, sc.kernel[0], st);
             if (e != cudaSuccess) break;
-            launch_shade<false>(p, kFixedGrid, st, S, cur, paths, dp<float>(br.B[2]), dp<float2>(br.B[3]), ps, q,
+            if (mixed) {
+                uint32_t* bins = dp<uint32_t>(br.B[29]);
+                cudaMemsetAsync(bins, 0, 2 * kShadeClasses * sizeof(uint32_t), st);
+                shade_bin_kernel<<<kFixedGrid, kBlock, 0, st>>>(S, q, paths, dp<uint8_t>(br.B[27]), bins);
+                shade_order_kernel<<<kFixedGrid, kBlock, 0, st>>>(q, paths, dp<uint8_t>(br.B[27]), bins,
+                                                                  dp<uint32_t>(br.B[28]));
+            }
+            launch_shade<false>(p, kFixedGrid, st, S, cur, paths, dp<float>(br.B[2]), dp<float2>(br.B[3]), ps, qs,
                                 Guide_Shade{});
             Cast_Args sh;
             sh.rays = q.shd_rays;

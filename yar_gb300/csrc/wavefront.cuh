@@ -194,6 +194,7 @@ struct Queues {
     uint32_t* prb_slot;
     uint32_t* counters;  // [0] next ext, [1] shadow, [2] probe, [3] error, [4..6] ray hand-out
     const uint32_t* ext_count = nullptr;  // device count of the extend queue (graph-captured renders)
+    const uint32_t* order = nullptr;      // the shade kernel's visiting order of the extend queue, or none
 };
 
 struct Scene_Dev {
@@ -1202,10 +1203,11 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
     __shared__ float4 stash[6][kBlock];
     if (q.ext_count) count = *q.ext_count;
     for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
-        const uint32_t i = base + threadIdx.x;
+        const uint32_t k = base + threadIdx.x;
+        const uint32_t i = (q.order && k < count) ? q.order[k] : k;  // queue entry this thread shades
         bool want_shadow = false, want_probe = false, want_next = false;
         uint32_t slot = 0;
-        if (i < count) {
+        if (k < count) {
             slot = q.ext_slot[cur][i];
             const float4 rb = q.ext_rays[cur][2 * (size_t)i + 1];
             const float4 h4 = q.ext_hit4[i];
@@ -1787,6 +1789,73 @@ connect_kernel(Render_Params p, Scene_Dev S, const uint32_t* __restrict__ slots,
             const uint32_t r = ps.rec[slot];
             if (r != 0xffffffffu) records[(size_t)r * kGuideRecordF4 + 5] = make_float4(L.r, L.g, L.b, 0.f);
         }
+    }
+}
+
+// ---------------------------------------------------------------- shading order
+// The shade kernel visits the extend queue grouped by what the hit needs:
+// misses and emitters, diffuse, metal, then every other material, so that a
+// warp mostly runs one BSDF's code (the kernel's stalls are mostly
+// instruction fetch, and mixed warps run every material's branch).  Each
+// path's result does not depend on the order; the appends to the next
+// queues, already in atomic order, only change places.
+constexpr uint32_t kShadeClasses = 4;
+
+__device__ __forceinline__ uint32_t shade_class(const Scene_Dev& S, uint2 h2) {
+    if (h2.y == 0xffffffffu) return 0u;  // a miss
+    const float4 inf4 = __ldg(S.obj_render + 7 * (size_t)h2.y + 6);
+    if ((uint32_t)__float_as_int(inf4.z) != 0xffffffffu) return 0u;  // an emitter: emission only
+    const uint32_t m = (uint32_t)__float_as_int(inf4.x);
+    return m == YAR_MATERIAL_DIFFUSE ? 1u : (m == YAR_MATERIAL_METAL ? 2u : 3u);
+}
+
+// Lane's rank among the warp's lanes with the same key, and that group's
+// leader lane (the lowest); every lane of the warp takes part.
+__device__ __forceinline__ void key_group(uint32_t key, uint32_t& rank, int& leader, uint32_t& size) {
+    const uint32_t group = __match_any_sync(0xffffffffu, key);
+    const uint32_t lane = threadIdx.x & 31u;
+    rank = __popc(group & ((1u << lane) - 1u));
+    leader = __ffs(group) - 1;
+    size = __popc(group);
+}
+
+// bins[0..3]: the queue's entries per class (bins zeroed by the caller).
+__global__ void __launch_bounds__(kBlock)
+shade_bin_kernel(Scene_Dev S, Queues q, uint32_t count, uint8_t* __restrict__ keys, uint32_t* __restrict__ bins) {
+    if (q.ext_count) count = *q.ext_count;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t key = i < count ? shade_class(S, q.ext_hit2[i]) : kShadeClasses;
+        if (i < count) keys[i] = (uint8_t)key;
+        uint32_t rank, size;
+        int leader;
+        key_group(key, rank, leader, size);
+        if (i < count && rank == 0) atomicAdd(&bins[key], size);
+    }
+}
+
+// order[]: the queue's entries class after class (bins[4..7] hand out the
+// places within a class).
+__global__ void __launch_bounds__(kBlock)
+shade_order_kernel(Queues q, uint32_t count, const uint8_t* __restrict__ keys, uint32_t* __restrict__ bins,
+                   uint32_t* __restrict__ order) {
+    if (q.ext_count) count = *q.ext_count;
+    uint32_t first[kShadeClasses];
+    uint32_t acc = 0;
+    for (uint32_t c = 0; c < kShadeClasses; c++) {
+        first[c] = acc;
+        acc += bins[c];
+    }
+    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const uint32_t key = i < count ? keys[i] : kShadeClasses;
+        uint32_t rank, size;
+        int leader;
+        key_group(key, rank, leader, size);
+        uint32_t at = 0;
+        if (i < count && rank == 0) at = atomicAdd(&bins[kShadeClasses + key], size);
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (i < count) order[first[key] + at + rank] = i;
     }
 }
 
