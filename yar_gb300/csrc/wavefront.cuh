@@ -1859,6 +1859,100 @@ shade_order_kernel(Queues q, uint32_t count, const uint8_t* __restrict__ keys, u
     }
 }
 
+// ---------------------------------------------------------------- extend-queue order
+// The rays of a bounce can be traced grouped by direction octant and origin
+// cell (an 8 x 8 x 8 grid over the scene box in Morton order): neighbours in
+// the queue then walk much of the same kd-tree.  A counting sort: per-ray
+// keys and a histogram, an exclusive scan, then a scatter of each ray and its
+// path slot into the other extend buffer.  Results do not depend on the
+// order (every per-ray quantity travels with the ray).
+constexpr uint32_t kRayBins = 8u * 512u;
+
+struct Ray_Grid {
+    float lo[3], scale[3];  // cell = (origin - lo) * scale, 8 cells per axis
+};
+
+__device__ __forceinline__ uint32_t spread3(uint32_t v) {
+    return (v & 1u) | ((v & 2u) << 2) | ((v & 4u) << 4);
+}
+
+__device__ __forceinline__ uint32_t ray_bin(const Ray_Grid& g, float4 a, float4 b) {
+    const float o[3] = {a.x, a.y, a.z};
+    uint32_t c[3];
+    for (int k = 0; k < 3; k++) {
+        const float f = (o[k] - g.lo[k]) * g.scale[k];
+        c[k] = f >= 1.f ? (f < 7.f ? (uint32_t)f : 7u) : 0u;  // NaN and below the box: cell 0
+    }
+    const uint32_t oct = (b.x < 0.f ? 1u : 0u) | (b.y < 0.f ? 2u : 0u) | (b.z < 0.f ? 4u : 0u);
+    return (oct << 9) | spread3(c[0]) | (spread3(c[1]) << 1) | (spread3(c[2]) << 2);
+}
+
+__global__ void __launch_bounds__(256)
+ray_hist_kernel(Ray_Grid g, const float4* __restrict__ rays, const uint32_t* __restrict__ count_dev, uint32_t count,
+                uint16_t* __restrict__ keys, uint32_t* __restrict__ hist) {
+    __shared__ uint32_t sh[kRayBins];
+    for (uint32_t j = threadIdx.x; j < kRayBins; j += blockDim.x) sh[j] = 0u;
+    __syncthreads();
+    if (count_dev) count = *count_dev;
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < count; i += gridDim.x * blockDim.x) {
+        const uint32_t key = ray_bin(g, rays[2 * (size_t)i], rays[2 * (size_t)i + 1]);
+        keys[i] = (uint16_t)key;
+        atomicAdd(&sh[key], 1u);
+    }
+    __syncthreads();
+    for (uint32_t j = threadIdx.x; j < kRayBins; j += blockDim.x)
+        if (sh[j]) atomicAdd(&hist[j], sh[j]);
+}
+
+// hist[] becomes each bin's first place (exclusive prefix), one block of 1024 threads.
+__global__ void __launch_bounds__(1024) ray_scan_kernel(uint32_t* __restrict__ hist) {
+    constexpr uint32_t kPer = kRayBins / 1024u;
+    __shared__ uint32_t part[1024];
+    uint32_t v[kPer], sum = 0;
+    for (uint32_t k = 0; k < kPer; k++) {
+        v[k] = hist[threadIdx.x * kPer + k];
+        sum += v[k];
+    }
+    part[threadIdx.x] = sum;
+    __syncthreads();
+    for (uint32_t off = 1; off < 1024u; off <<= 1) {  // inclusive scan of the thread sums
+        const uint32_t add = threadIdx.x >= off ? part[threadIdx.x - off] : 0u;
+        __syncthreads();
+        part[threadIdx.x] += add;
+        __syncthreads();
+    }
+    uint32_t run = part[threadIdx.x] - sum;
+    for (uint32_t k = 0; k < kPer; k++) {
+        hist[threadIdx.x * kPer + k] = run;
+        run += v[k];
+    }
+}
+
+__global__ void __launch_bounds__(kBlock)
+ray_scatter_kernel(const float4* __restrict__ src_rays, const uint32_t* __restrict__ src_slot,
+                   float4* __restrict__ dst_rays, uint32_t* __restrict__ dst_slot,
+                   const uint16_t* __restrict__ keys, uint32_t* __restrict__ cursor,
+                   const uint32_t* __restrict__ count_dev, uint32_t count) {
+    if (count_dev) count = *count_dev;
+    for (uint32_t base = blockIdx.x * blockDim.x; base < count; base += gridDim.x * blockDim.x) {
+        const uint32_t i = base + threadIdx.x;
+        const bool valid = i < count;
+        const uint32_t key = valid ? keys[i] : 0xffffffffu;
+        uint32_t rank, size;
+        int leader;
+        key_group(key, rank, leader, size);
+        uint32_t at = 0;
+        if (valid && rank == 0) at = atomicAdd(&cursor[key], size);
+        at = __shfl_sync(0xffffffffu, at, leader);
+        if (valid) {
+            const uint32_t pos = at + rank;
+            dst_rays[2 * (size_t)pos] = src_rays[2 * (size_t)i];
+            dst_rays[2 * (size_t)pos + 1] = src_rays[2 * (size_t)i + 1];
+            dst_slot[pos] = src_slot[i];
+        }
+    }
+}
+
 // Device-driven bounces.  Queue counters: [0] next extend, [1] shadow, [2]
 // probe, [3] error, [4..6] ray hand-out, [7] this bounce's extend count; rays:
 // [0] closest, [1] any.  Turns the last bounce's appends into this bounce's
