@@ -9,8 +9,9 @@
 // kernel reads its queue length from device memory and exits early on an
 // empty queue), so a scene's whole chunk/bounce sequence can be captured.
 // The graph forks into `branches` streams; scenes are assigned to branches
-// longest-first, so small scenes overlap with each other and with the tails
-// of large ones.  A one-thread kernel stamps the GPU clock when each scene's
+// longest-first (balancing their loads) and each branch runs its scenes
+// shortest-first, so small scenes overlap with each other and with the tails
+// of large ones and finish early.  A one-thread kernel stamps the GPU clock when each scene's
 // film is resolved: per-scene completion times come from the device.
 //
 // Autotuner: before capture, (1) each scene's traversal kernel is chosen by
@@ -122,14 +123,15 @@ int alloc_branches(Batch& bt, int nb, uint64_t chunk_cap, bool one_spp) {
         cudaError_t e = cudaStreamCreateWithFlags(&br.stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "batch streams");
         if (br.cap == 0) continue;
-        br.B.assign(30, Device_Buffer{});
+        br.B.assign(32, Device_Buffer{});
         const size_t cap = br.cap;
-        const size_t sizes[30] = {0, 0, cap * br.n1d * sizeof(float), cap * br.n2d * sizeof(float2),
+        const size_t sizes[32] = {0, 0, cap * br.n1d * sizeof(float), cap * br.n2d * sizeof(float2),
                                   cap * 16, cap * 16, cap * 4, cap * 16, cap * 16, cap * 16, cap * 16, cap * 16,
                                   cap * 16, cap, cap * 16, cap * 8, cap * 32, cap * 32, cap * 4, cap * 4, cap * 16,
                                   cap * 8, cap * 32, cap * 4, cap * 32, cap * 4, 16 * sizeof(uint32_t),
-                                  cap, cap * 4, 2 * kShadeClasses * sizeof(uint32_t)};  // shading order
-        for (int i = 2; i < 30 && rc == YAR_OK; i++) rc = device_alloc(ctx, br.B[i], sizes[i]);
+                                  cap, cap * 4, 2 * kShadeClasses * sizeof(uint32_t),  // shading order
+                                  cap * 2, kRayBins * sizeof(uint32_t)};              // extend-queue sort
+        for (int i = 2; i < 32 && rc == YAR_OK; i++) rc = device_alloc(ctx, br.B[i], sizes[i]);
         if (rc != YAR_OK) return rc;
         std::vector<Device_Buffer>& B = br.B;
         br.ps = Path_State{dp<float4>(B[4]), dp<float4>(B[5]), dp<uint32_t>(B[6]), dp<uint4>(B[7]),
@@ -176,6 +178,15 @@ cudaError_t enqueue_scene(Batch& bt, int si, bool one_spp, unsigned long long* s
         seen |= m == YAR_MATERIAL_DIFFUSE ? 1u : (m == YAR_MATERIAL_METAL ? 2u : 4u);
     }
     const bool mixed = (seen & (seen - 1)) != 0;
+    // the extend queues after the camera bounce sorted by direction octant and
+    // origin cell, in scenes up to 1M triangles (as render_run_params does)
+    const bool sort_rays = sub->tris.bytes / (3 * sizeof(float4)) <= (1u << 20);
+    Ray_Grid grid_box;
+    for (int k = 0; k < 3; k++) {
+        const float lo = sub->ds.scene_bounds[k], ext = sub->ds.scene_bounds[3 + k] - lo;
+        grid_box.lo[k] = lo;
+        grid_box.scale[k] = ext > 0.f ? 8.f / ext : 0.f;
+    }
     Queues qs = q;  // q with the order, for the shade kernel
     qs.order = mixed ? dp<uint32_t>(br.B[28]) : nullptr;
     cudaError_t e = cudaSuccess;
@@ -189,6 +200,16 @@ cudaError_t enqueue_scene(Batch& bt, int si, bool one_spp, unsigned long long* s
         int cur = 0;
         for (int bounce = 0; bounce <= p.max_bounces + 1 && e == cudaSuccess; bounce++) {
             bounce_begin_kernel<<<1, 1, 0, st>>>(ctr, bounce == 0 ? paths : 0u, rays);
+            if (sort_rays && bounce > 0) {
+                uint16_t* keys = dp<uint16_t>(br.B[30]);
+                uint32_t* hist = dp<uint32_t>(br.B[31]);
+                cudaMemsetAsync(hist, 0, kRayBins * sizeof(uint32_t), st);
+                ray_hist_kernel<<<152 * 2, 256, 0, st>>>(grid_box, q.ext_rays[cur], ctr + 7, 0u, keys, hist);
+                ray_scan_kernel<<<1, 1024, 0, st>>>(hist);
+                ray_scatter_kernel<<<kFixedGrid, kBlock, 0, st>>>(q.ext_rays[cur], q.ext_slot[cur], q.ext_rays[cur ^ 1],
+                                                                  q.ext_slot[cur ^ 1], keys, hist, ctr + 7, 0u);
+                cur ^= 1;
+            }
             Cast_Args a;
             a.rays = q.ext_rays[cur];
             a.count = ctr + 7;
@@ -265,8 +286,18 @@ cudaError_t capture(Batch& bt, bool one_spp, cudaGraphExec_t* exec) {
     if (e == cudaSuccess) e = cudaEventRecord(fork, main);
     for (size_t b = 0; b < bt.branches.size() && e == cudaSuccess; b++)
         e = cudaStreamWaitEvent(bt.branches[b].stream, fork, 0);
-    for (size_t i = 0; i < bt.scenes.size() && e == cudaSuccess; i++)
-        e = enqueue_scene(bt, (int)i, one_spp, stamps + 1 + i, rays + 2 * bt.scenes[i].branch);
+    // scenes went longest-first onto the least-loaded branch; within a branch
+    // they run shortest-first, which leaves the makespan and brings most
+    // completions forward
+    std::vector<int> run_order(bt.scenes.size());
+    for (size_t i = 0; i < run_order.size(); i++) run_order[i] = (int)i;
+    std::stable_sort(run_order.begin(), run_order.end(), [&](int a, int b) {
+        return bt.scenes[a].pixels * bt.scenes[a].p.spp < bt.scenes[b].pixels * bt.scenes[b].p.spp;
+    });
+    for (size_t k = 0; k < run_order.size() && e == cudaSuccess; k++) {
+        const int i = run_order[k];
+        e = enqueue_scene(bt, i, one_spp, stamps + 1 + i, rays + 2 * bt.scenes[i].branch);
+    }
     for (size_t b = 0; b < bt.branches.size() && e == cudaSuccess; b++) {
         e = cudaEventCreateWithFlags(&join[b], cudaEventDisableTiming);
         if (e == cudaSuccess) e = cudaEventRecord(join[b], bt.branches[b].stream);
