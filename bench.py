@@ -404,6 +404,20 @@ def run_gb300(args, rank, world, local, pg):
     hits = native.HitSoa(h_t.data_ptr(), h_prim.data_ptr(), h_obj.data_ptr(), h_bary.data_ptr())
     import ctypes as C
 
+    # the box's pinned host <-> device copy bandwidth (512 MiB each way, best of 3):
+    # the end-to-end figure overlaps these copies with the traversal
+    def copy_gbs(dst, src):
+        best = None
+        for _ in range(3):
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            dst.copy_(src, non_blocking=True)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+            best = dt if best is None else min(best, dt)
+        return round(src.numel() * src.element_size() / best / 1e9, 1)
+    host_copy = {"h2d": copy_gbs(d_rays, h_rays), "d2h": copy_gbs(h_rays, d_rays)}
+
     def e2e_step():
         rc = native.lib().yar_gpu_cast_closest(ctx._h, h_rays.data_ptr(), n, C.byref(hits), native.YAR_BUFFERS_HOST)
         ctx._check(rc, "cast_closest")
@@ -448,7 +462,8 @@ def run_gb300(args, rank, world, local, pg):
         "vs_baseline": None, "dtype": "f32",
         "data": "synthetic (seeded fBm terrain + icospheres, seed %d)" % SEED,
         "config": raycast_config(s.triangle_count, n, world, args.grid),
-        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
+                "pipeline_chunk_rays": 4 << 20, "host_copy_gbs": host_copy},
         "gpu_launches": 2 * args.steps,
         "kernels": {"extend_ms": round(ext_ms, 3), "shadow_ms": round(shd_ms, 3),
                     "extend_mrays_s": round(n / ext_ms / 1e3, 1), "shadow_mrays_s": round(n / shd_ms / 1e3, 1)},

@@ -449,8 +449,8 @@ int yar_gpu_render_checkpoint(yar_gpu_ctx* ctx, const char* checkpoint_directory
 
 /* ---- render without allocation ----
  * No counterpart in the reference.  yar_gpu_render allocates its working
- * memory (path state, ray queues, per-sample film data) with cudaMalloc on
- * every call.  Callers that must not allocate device memory at render time -
+ * memory (path state, ray queues, per-sample film data) with cudaMalloc,
+ * on its first call and whenever a call needs more.  Callers that must not allocate device memory at render time -
  * an application running under a fixed, pre-reserved memory budget, a host
  * that forbids allocation after start-up for latency reasons, or code whose
  * device allocator is owned by someone else - use this entry point instead:
