@@ -340,8 +340,10 @@ __global__ void sample_tables_kernel(Render_Params p, uint32_t chunk_first, uint
     const uint32_t rows = 1u + (uint32_t)p.n1d + (uint32_t)p.n2d;
     const uint64_t g = (uint64_t)blockIdx.x * blockDim.x + threadIdx.x;
     if (g >= (uint64_t)chunk_pixels * rows) return;
-    const uint32_t lp = (uint32_t)(g / rows);
-    const uint32_t row = (uint32_t)(g % rows);
+    // row-major over the pixels: a warp builds the same row (the same kind,
+    // jump-ahead distance and loop lengths) for 32 pixels
+    const uint32_t lp = (uint32_t)(g % chunk_pixels);
+    const uint32_t row = (uint32_t)(g / chunk_pixels);
     int x, y;
     Pcg rng = pixel_pcg(p, pixel_stream(p, chunk_first + lp, x, y));
     const int spp = p.spp;
