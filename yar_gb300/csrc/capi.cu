@@ -170,8 +170,10 @@ extern "C" void yar_gpu_destroy(yar_gpu_ctx* ctx) {
     if (ctx->d_counter) cudaFree(ctx->d_counter);
     if (ctx->ev_start) cudaEventDestroy(ctx->ev_start);
     if (ctx->ev_stop) cudaEventDestroy(ctx->ev_stop);
-    for (cudaStream_t s : {ctx->pipe_in, ctx->pipe_compute, ctx->pipe_out})
+    for (cudaStream_t s : {ctx->pipe_in, ctx->pipe_compute, ctx->pipe_out, ctx->aux_stream})
         if (s) cudaStreamDestroy(s);
+    for (cudaEvent_t ev : {ctx->aux_fork, ctx->aux_join})
+        if (ev) cudaEventDestroy(ev);
     if (ctx->pipe_start) cudaEventDestroy(ctx->pipe_start);
     for (int c = 0; c < yar_gpu_ctx::kPipeChunks; c++) {
         if (ctx->pipe_in_done[c]) cudaEventDestroy(ctx->pipe_in_done[c]);

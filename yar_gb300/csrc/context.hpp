@@ -97,6 +97,9 @@ struct yar_gpu_ctx {
     // where the persistent traversal's tail per launch outweighs the overlap)
     uint32_t pipe_chunk = 4u << 20;
     cudaStream_t pipe_in = nullptr, pipe_compute = nullptr, pipe_out = nullptr;
+    // renders: the per-tile variance sums run beside the film resolve
+    cudaStream_t aux_stream = nullptr;
+    cudaEvent_t aux_fork = nullptr, aux_join = nullptr;
     cudaEvent_t pipe_start = nullptr, pipe_in_done[kPipeChunks] = {}, pipe_cast_done[kPipeChunks] = {};
     // traversal kernel per ray kind (0 closest, 1 any) for C-ABI casts and for
     // renders; -1 until tuned on the current scene (or fixed by the options)

@@ -760,15 +760,25 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
     }
     if (e == cudaSuccess) {
         samples_kernel<<<(uint32_t)((pixels + kBlock - 1) / kBlock), kBlock, 0, st>>>(p, radiance, dptr<double>(B[27]));
-        tile_variance_kernel<<<p.tiles_x * p.tiles_y, kTileVarThreads, 0, st>>>(p, dptr<double>(B[27]),
-                                                                                dptr<double>(B[28]));
+        // the tile sums (one sequential FP64 chain per 64 x 64 tile, the
+        // reference's order) run on a second stream beside the film
+        if (!ctx->aux_stream) e = cudaStreamCreateWithFlags(&ctx->aux_stream, cudaStreamNonBlocking);
+        if (e == cudaSuccess && !ctx->aux_fork) e = cudaEventCreateWithFlags(&ctx->aux_fork, cudaEventDisableTiming);
+        if (e == cudaSuccess && !ctx->aux_join) e = cudaEventCreateWithFlags(&ctx->aux_join, cudaEventDisableTiming);
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->aux_fork, st);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->aux_stream, ctx->aux_fork, 0);
+        if (e == cudaSuccess)
+            tile_variance_kernel<<<p.tiles_x * p.tiles_y, kTileVarThreads, 0, ctx->aux_stream>>>(
+                p, dptr<double>(B[27]), dptr<double>(B[28]));
         launches += 2;
-        if (!tiles_out) {
+        if (e == cudaSuccess && !tiles_out) {
             film_kernel<<<(uint32_t)(((uint64_t)p.rw * p.rh + kBlock - 1) / kBlock), kBlock, 0, st>>>(
                 p, radiance, image_samples, dptr<float>(B[29]));
             launches++;
         }
-        e = cudaGetLastError();
+        if (e == cudaSuccess) e = cudaEventRecord(ctx->aux_join, ctx->aux_stream);
+        if (e == cudaSuccess) e = cudaStreamWaitEvent(st, ctx->aux_join, 0);
+        if (e == cudaSuccess) e = cudaGetLastError();
     }
     std::vector<double> tile_var((size_t)p.tiles_x * p.tiles_y);
     if (e == cudaSuccess && tiles_out) {

@@ -2189,7 +2189,9 @@ __device__ __forceinline__ float film_filter_weight(const Render_Params& p, floa
 __device__ __forceinline__ float4 tile_pixel_sum(const Render_Params& p, const float4* __restrict__ radiance,
                                                  const float2* __restrict__ image_samples, int t, int px, int py) {
     const float r = p.filter_radius;
-    const int R = (int)ceilf(r) + 1;
+    // a sample in pixel q reaches pixels p with |p - q| <= ceil(r + 1/2)
+    // (Film_Tile::add_sample's ceil(x - r - 1/2) .. floor(x + r - 1/2))
+    const int R = (int)ceilf(r + 0.5f);
     const int qx0 = max(px - R, p.sx0), qx1 = min(px + R, p.sx0 + p.sw - 1);
     const int qy0 = max(py - R, p.sy0), qy1 = min(py + R, p.sy0 + p.sh - 1);
     int bx0, by0, bx1, by1;
@@ -2230,7 +2232,7 @@ film_kernel(Render_Params p, const float4* __restrict__ radiance, const float2* 
     const int px = p.rx0 + (int)(idx % (uint32_t)p.rw);
     const int py = p.ry0 + (int)(idx / (uint32_t)p.rw);
     const float r = p.filter_radius;
-    const int R = (int)ceilf(r) + 1;
+    const int R = (int)ceilf(r + 0.5f);  // the samples' reach, as in tile_pixel_sum
     // candidate sample pixels: [px - R, px + R] x [py - R, py + R] inside the sample region
     const int qx0 = max(px - R, p.sx0), qx1 = min(px + R, p.sx0 + p.sw - 1);
     const int qy0 = max(py - R, p.sy0), qy1 = min(py + R, p.sy0 + p.sh - 1);
