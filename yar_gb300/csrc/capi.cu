@@ -358,7 +358,7 @@ int check_error_word(yar_gpu_ctx* ctx) {
 uint32_t pipeline_chunks(const yar_gpu_ctx* ctx, uint32_t n) {
     if (ctx->pipe_chunk == 0xffffffffu) return 1;
     const uint64_t c = ((uint64_t)n + ctx->pipe_chunk - 1) / ctx->pipe_chunk;
-    return (uint32_t)std::min<uint64_t>(c, yar_gpu_ctx::kPipeChunks);
+    return (uint32_t)std::min<uint64_t>(c, yar_gpu_ctx::kPipeChunks - 2);  // room for the two short chunks
 }
 
 int ensure_pipeline(yar_gpu_ctx* ctx) {
@@ -379,8 +379,25 @@ int cast_pipelined(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t n, const yar_
     const bool closest = hits != nullptr;
     int rc = ensure_pipeline(ctx);
     if (rc != YAR_OK) return rc;
-    const uint32_t chunks = pipeline_chunks(ctx, n);
-    const uint32_t per = (uint32_t)((((uint64_t)n + chunks - 1) / chunks + 31u) & ~31ull);
+    // chunk boundaries: a short first chunk (the traversal starts after a
+    // quarter of a chunk's copy) and a short last one (its results come down
+    // sooner), equal chunks between
+    std::vector<uint32_t> bounds{0u};
+    {
+        const uint32_t mid_chunks = pipeline_chunks(ctx, n);
+        const uint32_t ramp = std::min<uint32_t>(ctx->pipe_chunk / 4u, n / 8u) & ~31u;
+        const uint32_t head = ramp, tail = ramp;
+        const uint32_t middle = n - head - tail;
+        const uint32_t per = (uint32_t)((((uint64_t)middle + mid_chunks - 1) / mid_chunks + 31u) & ~31ull);
+        if (head) bounds.push_back(head);
+        for (uint32_t c = 0; c < mid_chunks; c++) {
+            const uint64_t b = std::min<uint64_t>((uint64_t)head + (uint64_t)(c + 1) * per, (uint64_t)n - tail);
+            if (b > bounds.back()) bounds.push_back((uint32_t)b);
+        }
+        if (n > bounds.back()) bounds.push_back(n);
+    }
+    const uint32_t chunks = (uint32_t)bounds.size() - 1u;
+    if (chunks > (uint32_t)yar_gpu_ctx::kPipeChunks) return fail(ctx, YAR_ERR_INVALID, "pipeline chunks");
     cudaStream_t compute[2] = {ctx->stream, ctx->pipe_compute};
     cudaError_t e = cudaEventRecord(ctx->pipe_start, ctx->stream);  // after the context's earlier work
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->pipe_in, ctx->pipe_start, 0);
@@ -388,9 +405,8 @@ int cast_pipelined(yar_gpu_ctx* ctx, const yar_ray* rays, uint32_t n, const yar_
     if (e == cudaSuccess) e = cudaStreamWaitEvent(ctx->pipe_out, ctx->pipe_start, 0);
     float4* d_rays = (float4*)ctx->d_rays.ptr;
     for (uint32_t c = 0; c < chunks && e == cudaSuccess; c++) {
-        const uint32_t first = c * per;
-        if (first >= n) break;
-        const uint32_t m = std::min(per, n - first);
+        const uint32_t first = bounds[c];
+        const uint32_t m = bounds[c + 1] - first;
         e = cudaMemcpyAsync(d_rays + 2 * (size_t)first, rays + first, (size_t)m * 32, cudaMemcpyHostToDevice,
                             ctx->pipe_in);
         if (e == cudaSuccess) e = cudaEventRecord(ctx->pipe_in_done[c], ctx->pipe_in);
