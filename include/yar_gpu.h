@@ -526,7 +526,8 @@ typedef struct yar_guided_params {
     /* 0: the image is the mean of `passes` one-sample passes.  > 0: the
      * stratified form - the train_passes training passes (guided only), then
      * the image rendered with the scene's stratified pixel sampler at this
-     * many samples per pixel (rounded up to a perfect square, as RAY's --spp),
+     * many samples per pixel (rounded up to nx x ny strata, nx = ceil(sqrt(n)),
+     * ny = ceil(n / nx): a perfect square stays one, as RAY's --spp makes it),
      * continuations drawn from the trained proposal; `passes` and
      * `time_budget` are not used, radiance_sum receives image x spp. */
     uint32_t samples_per_pixel;

@@ -89,7 +89,8 @@ def test_stratified_guided_is_unbiased(gpu_ctx, small_room):
     c.config["x_pixel_sample_count"] = c.config["y_pixel_sample_count"] = 15
     gpu_ctx.upload_scene(c)
     plain, _ = gpu_ctx.render(64, 64)
-    unguided, _, st0 = gpu_ctx.guided_render(64, 64, samples_per_pixel=200, stream_offset=4)  # rounds up to 15 x 15
+    unguided, sums0, st0 = gpu_ctx.guided_render(64, 64, samples_per_pixel=200, stream_offset=4)  # 15 x 14 strata
     assert st0.passes == 0
+    assert np.array_equal(sums0, unguided.astype(np.float64).reshape(sums0.shape) * 210.0)
     assert not np.array_equal(unguided, plain)
     assert abs(unguided.mean() - plain.mean()) < 0.01 * plain.mean(), (unguided.mean(), plain.mean())

@@ -88,7 +88,11 @@ def main(argv=None):
         img, _, st = ctx.guided_render(w, h, passes=a.passes, guide_fraction=a.guide_fraction,
                                        train_passes=a.train_passes, time_budget=a.time_budget,
                                        samples_per_pixel=a.spp)
-        spp = int(math.ceil(math.sqrt(a.spp))) ** 2 if a.spp else st.passes
+        if a.spp:  # nx x ny strata, nx = ceil(sqrt(spp)), ny = ceil(spp / nx)
+            nx = int(math.ceil(math.sqrt(a.spp)))
+            spp = nx * ((a.spp + nx - 1) // nx)
+        else:
+            spp = st.passes
         attrs = exr.yar_attributes(spp=spp, input_file=a.scene, device="gpu")
         print("rendered %dx%d, %s in %.3f s (training %.3f s)" % (
             w, h, ("%d guided samples per pixel after %d training passes" % (spp, st.passes)) if a.spp

@@ -223,10 +223,10 @@ struct Guide_Render_Hook {
                                 uint32_t count, cudaStream_t st) = nullptr;
     void* user = nullptr;
 };
-// The path tracer with the scene's pixel sampler at spp_side x spp_side
-// samples per pixel, pixel streams offset by stream_hi (non-zero: streams
-// independent of the reference's), continuations guided through `hook`.
-int render_guided_stratified(yar_gpu_ctx* ctx, int spp_side, uint32_t stream_hi, const Guide_Render_Hook& hook,
+// The path tracer with the scene's pixel sampler at nx x ny samples per
+// pixel, pixel streams offset by stream_hi (non-zero: streams independent of
+// the reference's), continuations guided through `hook`.
+int render_guided_stratified(yar_gpu_ctx* ctx, int nx, int ny, uint32_t stream_hi, const Guide_Render_Hook& hook,
                              float* rgb_out, yar_render_stats* stats);
 
 } // namespace yar

@@ -146,8 +146,10 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
     if (!gp || (gp->passes == 0 && gp->samples_per_pixel == 0))
         return fail(ctx, YAR_ERR_INVALID, "guided render: no passes");
     // stratified: the training passes, then one render with the pixel sampler
+    // stratified: nx x ny strata, nx = ceil(sqrt(n)), ny = ceil(n / nx)
     const int spp_side = gp->samples_per_pixel ? (int)std::ceil(std::sqrt((double)gp->samples_per_pixel)) : 0;
     if (spp_side > 256) return fail(ctx, YAR_ERR_INVALID, "guided render: at most 65536 samples per pixel");
+    const int spp_rows = spp_side ? (int)((gp->samples_per_pixel + (uint32_t)spp_side - 1) / (uint32_t)spp_side) : 0;
     const uint32_t pass_count = spp_side ? (gp->guide_fraction > 0.f ? gp->train_passes : 0u) : gp->passes;
     if (!(gp->guide_fraction >= 0.f && gp->guide_fraction < 1.f))
         return fail(ctx, YAR_ERR_INVALID, "guide fraction must be in [0, 1)");
@@ -330,7 +332,7 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
         if (!spp_side && gp->time_budget > 0.f && elapsed >= gp->time_budget) break;
     }
     if (spp_side && e == cudaSuccess) {
-        // the image: the scene's pixel sampler at spp_side^2 samples per pixel,
+        // the image: the scene's pixel sampler at spp_side x spp_rows samples per pixel,
         // continuations from the trained proposal
         Device_Buffer& qbuf = ctx->guide_queries;
         Device_Buffer& lbuf = ctx->guide_lobes;
@@ -338,7 +340,7 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
         Guide_Render_Hook hook;
         hook.alpha = guided ? gp->guide_fraction : 0.f;
         hook.max_bounce = (int)std::min<uint32_t>(gp->guide_bounces, 1u << 20);
-        hook.chunk_paths = std::max<uint64_t>(kGuidedChunkPaths, (uint64_t)spp_side * spp_side);
+        hook.chunk_paths = std::max<uint64_t>(kGuidedChunkPaths, (uint64_t)spp_side * spp_rows);
         if (guided) {
             const size_t qbytes = hook.chunk_paths * 3 * sizeof(float4);
             const size_t lbytes = hook.chunk_paths * kGuideLobeFloats * sizeof(float);
@@ -354,8 +356,9 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
         }
         std::vector<float> img((size_t)p.rw * p.rh * 3);
         yar_render_stats rs{};
-        if (!guided) hook.chunk_paths = std::max<uint64_t>(kChunkSampleBudget, (uint64_t)spp_side * spp_side);
-        rc = render_guided_stratified(ctx, spp_side, (gp->stream_offset << 20) | 0xfffffu, hook, img.data(), &rs);
+        if (!guided) hook.chunk_paths = std::max<uint64_t>(kChunkSampleBudget, (uint64_t)spp_side * spp_rows);
+        rc = render_guided_stratified(ctx, spp_side, spp_rows, (gp->stream_offset << 20) | 0xfffffu, hook, img.data(),
+                                      &rs);
         if (rc != YAR_OK) return rc;
         int h_err = 0;
         e = cudaMemcpy(&h_err, ctx->d_error, sizeof(int), cudaMemcpyDeviceToHost);
@@ -365,7 +368,7 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
             return fail(ctx, YAR_ERR_TIMEOUT, "tensor-core wait gave up");
         }
         const double seconds = std::chrono::duration<double>(std::chrono::steady_clock::now() - t0).count();
-        const double n = (double)spp_side * spp_side;
+        const double n = (double)spp_side * spp_rows;
         for (size_t k = 0; k < img.size(); k++) {
             if (rgb_out) rgb_out[k] = img[k];
             if (sum_out) sum_out[k] = (double)img[k] * n;

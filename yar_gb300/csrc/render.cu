@@ -857,14 +857,15 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
     return YAR_OK;
 }
 
-int render_guided_stratified(yar_gpu_ctx* ctx, int spp_side, uint32_t stream_hi, const Guide_Render_Hook& hook,
+int render_guided_stratified(yar_gpu_ctx* ctx, int nx, int ny, uint32_t stream_hi, const Guide_Render_Hook& hook,
                              float* rgb_out, yar_render_stats* stats) {
-    if (!rgb_out || spp_side < 1 || spp_side > 256 || stream_hi == 0)
+    if (!rgb_out || nx < 1 || nx > 256 || ny < 1 || ny > 256 || stream_hi == 0)
         return fail(ctx, YAR_ERR_INVALID, "guided stratified render: arguments");
     Render_Params p;
     if (int rc0 = prepare_render_params(ctx, p)) return rc0;
-    p.nx = p.ny = spp_side;
-    p.spp = spp_side * spp_side;
+    p.nx = nx;
+    p.ny = ny;
+    p.spp = nx * ny;
     p.stream_hi = stream_hi;  // own pixel streams: draws past the budget from one pcg stream per sample
     if (hook.chunk_paths < (uint64_t)p.spp) return fail(ctx, YAR_ERR_CAPACITY, "guided stratified render: chunk");
     return render_run_params(ctx, p, rgb_out, stats, nullptr, &hook);
