@@ -373,6 +373,30 @@ def test_constant_bump_with_delta_materials_bit_identical_to_oracle(gpu_ctx):
     assert stats.variance == ref_var
 
 
+@pytest.mark.parametrize("scale", [1.6, 0.5])
+def test_probe_culling_follows_the_light_geometry(gpu_ctx, scale):
+    """MIS probes that cannot reach the sampled quad light are not traced, but
+    only for lights whose own triangles lie on their rectangle.  The light's
+    quad scaled about its centre: grown (the check fails, every probe is
+    traced, and the geometry beyond the rectangle is hit) or shrunk (probes are
+    culled against the rectangle, which still holds the triangles): both
+    bit-identical to the oracle, which traces every probe."""
+    from yar_gb300 import native
+    s = FlatScene.read(golden("cornell_c1_64.yfs"))
+    k = int(np.nonzero(s.objects["area_light_type"] == native.LIGHT_RECT)[0][0])
+    mesh = s.meshes[int(s.objects["mesh_index"][k])]
+    v = mesh.vertices.reshape(-1, 3)
+    c = v.mean(axis=0)
+    mesh.vertices = (c + (v - c) * np.float32(scale)).astype(np.float32).reshape(mesh.vertices.shape)
+    s.build_kdtrees()
+    s.config["rng_seed_offset"] = 7
+    ref, ref_var = oracle.render(s, threads=8, correctly_rounded_trig=True)
+    gpu_ctx.upload_scene(s)
+    img, stats = gpu_ctx.render(64, 64)
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    assert stats.variance == ref_var
+
+
 def test_fourier_direct_lighting_bit_identical_to_oracle(gpu_ctx):
     """The fourier boxes under the direct-lighting algorithm: the light
     samples evaluate the series, bit-identical to the oracle."""

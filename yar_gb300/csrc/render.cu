@@ -164,6 +164,45 @@ int render_upload(yar_gpu_ctx* ctx, const yar_flat_scene* scene) {
         lights[i].le = make_float4(l.emitted_radiance[0], l.emitted_radiance[1], l.emitted_radiance[2], l.size[0]);
         lights[i].sz = make_float4(l.size[1], 0.f, 0.f, 0.f);
     }
+    // Probe culling per rectangular light (probe_may_reach): only when the
+    // light frame is orthogonal with a unit normal and every vertex of the
+    // light's objects lies on its plane and inside its rectangle (within 1e-3
+    // of its larger side), so that a ray missing the widened rectangle misses
+    // the light's triangles.
+    for (uint32_t i = 0; i < scene->rect_light_count; i++) {
+        const float* m = scene->rect_lights[i].light_to_world;
+        const double X[3] = {m[0], m[4], m[8]}, Y[3] = {m[1], m[5], m[9]}, N[3] = {m[2], m[6], m[10]};
+        const double C[3] = {m[3], m[7], m[11]};
+        auto dot3d = [](const double* a, const double* b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; };
+        const double xx = dot3d(X, X), yy = dot3d(Y, Y), nn = dot3d(N, N);
+        const double sx = scene->rect_lights[i].size[0], sy = scene->rect_lights[i].size[1];
+        bool ok = xx > 0 && yy > 0 && std::fabs(nn - 1.0) <= 1e-3 && sx > 0 && sy > 0 &&
+                  std::fabs(dot3d(X, Y)) <= 1e-6 * std::sqrt(xx * yy) &&
+                  std::fabs(dot3d(X, N)) <= 1e-6 * std::sqrt(xx * nn) && std::fabs(dot3d(Y, N)) <= 1e-6 * std::sqrt(yy * nn);
+        const double tol = 1e-3 * std::max(sx, sy);
+        uint32_t objects_found = 0;
+        for (uint32_t o = 0; ok && o < scene->object_count; o++) {
+            const yar_object_desc& ob = scene->objects[o];
+            if (ob.area_light_type != YAR_LIGHT_DIFFUSE_RECTANGULAR || ob.area_light_index != (int32_t)i) continue;
+            if (ob.mesh_index < 0 || (uint32_t)ob.mesh_index >= scene->mesh_count) {
+                ok = false;
+                break;
+            }
+            objects_found++;
+            const yar_mesh_desc& mesh = scene->meshes[ob.mesh_index];
+            const float* w = ob.object_to_world;
+            for (uint32_t v = 0; ok && v < mesh.vertex_count; v++) {
+                const float* pv = mesh.vertices + 3 * (size_t)v;
+                double P[3];
+                for (int r = 0; r < 3; r++)
+                    P[r] = w[4 * r] * pv[0] + w[4 * r + 1] * pv[1] + w[4 * r + 2] * pv[2] + w[4 * r + 3] - C[r];
+                const double a = dot3d(P, X) / xx, b = dot3d(P, Y) / yy, h = dot3d(P, N) / std::sqrt(nn);
+                ok = std::fabs(h) <= tol && std::fabs(a) <= 0.5 * sx + tol && std::fabs(b) <= 0.5 * sy + tol;
+            }
+        }
+        if (ok && objects_found > 0)
+            lights[i].sz = make_float4((float)sy, (float)(1.0 / xx), (float)(1.0 / yy), 1.f);
+    }
     std::vector<Delta_Light_Dev> dlights(std::max<uint32_t>(1, scene->delta_light_count));
     for (uint32_t i = 0; i < scene->delta_light_count; i++) {
         const yar_delta_light_desc& l = scene->delta_lights[i];

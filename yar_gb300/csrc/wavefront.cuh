@@ -63,8 +63,31 @@ enum : uint32_t {
 struct Rect_Light_Dev {
     float4 r0, r1, r2;  // light_to_world rows
     float4 le;          // emitted radiance rgb, size.x
-    float4 sz;          // size.y, -, -, -
+    float4 sz;          // size.y, then (probe culling, set when the light's own triangles lie on its
+                        // rectangle) 1 / |x axis|^2, 1 / |y axis|^2, 0 = off
 };
+
+// Whether the MIS probe from o along d can reach rectangular light L: false
+// only when the ray's crossing of the light's plane lies behind o or outside
+// the rectangle widened by 10%, by 2e-3 of its larger side and by 2e-3 of that
+// side per unit of 1/cos (the light's triangles lie within 1e-3 of its larger
+// side of the rectangle, in the plane and across it, checked on upload, so such
+// a ray cannot hit them and the probe would add nothing).
+__device__ __forceinline__ bool probe_may_reach(const Rect_Light_Dev& L, V3 o, V3 d, float lndw) {
+    const float4 r0 = __ldg(&L.r0), r1 = __ldg(&L.r1), r2 = __ldg(&L.r2), sz = __ldg(&L.sz);
+    if (sz.w == 0.f) return true;
+    const V3 c = v3(r0.w, r1.w, r2.w), n = v3(r0.z, r1.z, r2.z);
+    const float den = dot(d, n);
+    if (!(fabsf(den) > 0.f)) return true;
+    const float t = dot(c - o, n) / den;
+    if (t < 0.f) return false;
+    const V3 q = (o + mul(d, t)) - c;
+    const float sx = __ldg(&L.le).w, sy = sz.x;
+    const float big = fmaxf(sx, sy);
+    const float slack = 2e-3f * big + 2e-3f * big / lndw;
+    const float a = dot(q, v3(r0.x, r1.x, r2.x)) * sz.y, b = dot(q, v3(r0.y, r1.y, r2.y)) * sz.z;
+    return fabsf(a) <= 0.55f * sx + slack && fabsf(b) <= 0.55f * sy + slack;
+}
 
 // Point, spot and directional lights (direct_lighting.cpp:26-107):
 //   a = position xyz, type bits | b = direction xyz, cos(cone angle)
@@ -1562,8 +1585,8 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                             const Col fv = bsdf_sample<FULL>(f, ub.x, ub.y, u_sc, sc.wo, wi, bpdf);
                             if (!black(fv)) {
                                 const float lndw = dot(light_n, -wi);
-                                if (lndw > 1e-4f) {
-                                    const V3 position = origin_for_direction(sc, wi);
+                                const V3 position = origin_for_direction(sc, wi);
+                                if (lndw > 1e-4f && probe_may_reach(Ld, position, wi, lndw)) {
                                     const Col lef = Le * fv;
                                     ps.pend_probe0[slot] = make_float4(lef.r, lef.g, lef.b, bpdf);
                                     ps.pend_probe1[slot] = make_float4(position.x, position.y, position.z, lndw);
