@@ -597,6 +597,10 @@ typedef struct shading_ctx {
     /* for bump mapping: the normal's uv derivatives (world space, flipped
      * with the normal) and the shading frame's second tangent */
     v3 dndu, dndv, dpdv_shading;
+    /* has_dxdy_derivatives and the position and direction derivatives along
+     * the differential rays (the specular differential rays start from them) */
+    int has_dxdy;
+    v3 dpdx, dpdy, dwo_dx, dwo_dy;
 } shading_ctx;
 
 /* adjust_shading_normal, src/ref/shading_context.cpp:17-63 */
@@ -1111,16 +1115,22 @@ static float ray_plane_t(v3 o, v3 d, v3 n, float plane_d) {
 }
 
 /* Shading_Context::calculate_dxdy_derivatives + calculate_uv_derivates
- * (src/ref/shading_context.cpp:242-333) for differential rays from origin o */
-static void uv_derivatives(shading_ctx* sc, v3 o, v3 dx_dir, v3 dy_dir) {
+ * (src/ref/shading_context.cpp:242-333) for the differential rays (ox, dx_dir)
+ * and (oy, dy_dir) */
+static void uv_derivatives(shading_ctx* sc, v3 ox, v3 dx_dir, v3 oy, v3 dy_dir) {
     if (!sc->has_uv) return;
+    sc->has_dxdy = 1;
     const v3 gn = sc->geometric_normal;
     const float plane_d = -dot3(gn, sc->position);
     v3 dpdx = mk3(0, 0, 0), dpdy = mk3(0, 0, 0);
-    const float tx = ray_plane_t(o, dx_dir, gn, plane_d);
-    if (fabsf(tx) != INFINITY) dpdx = sub3(add3(o, mul3s(dx_dir, tx)), sc->position);
-    const float ty = ray_plane_t(o, dy_dir, gn, plane_d);
-    if (fabsf(ty) != INFINITY) dpdy = sub3(add3(o, mul3s(dy_dir, ty)), sc->position);
+    const float tx = ray_plane_t(ox, dx_dir, gn, plane_d);
+    if (fabsf(tx) != INFINITY) dpdx = sub3(add3(ox, mul3s(dx_dir, tx)), sc->position);
+    const float ty = ray_plane_t(oy, dy_dir, gn, plane_d);
+    if (fabsf(ty) != INFINITY) dpdy = sub3(add3(oy, mul3s(dy_dir, ty)), sc->position);
+    sc->dpdx = dpdx;
+    sc->dpdy = dpdy;
+    sc->dwo_dx = sub3(neg3(dx_dir), sc->wo);
+    sc->dwo_dy = sub3(neg3(dy_dir), sc->wo);
     int dim0, dim1;
     {
         const float ax = fabsf(gn.x), ay = fabsf(gn.y), az = fabsf(gn.z);
@@ -1140,8 +1150,45 @@ static void uv_derivatives(shading_ctx* sc, v3 o, v3 dx_dir, v3 dy_dir) {
         sc->dudy = (a11 * py[dim0] - a01 * py[dim1]) * inv_det;
         sc->dvdy = (-a10 * py[dim0] + a00 * py[dim1]) * inv_det;
     }
-    if (fabsf(sc->dudx) > 1e9f || fabsf(sc->dvdx) > 1e9f || fabsf(sc->dudy) > 1e9f || fabsf(sc->dvdy) > 1e9f)
+    if (fabsf(sc->dudx) > 1e9f || fabsf(sc->dvdx) > 1e9f || fabsf(sc->dudy) > 1e9f || fabsf(sc->dvdy) > 1e9f) {
+        sc->has_dxdy = 0;
+        sc->dpdx = sc->dpdy = sc->dwo_dx = sc->dwo_dy = mk3(0, 0, 0);
         sc->dudx = sc->dvdx = sc->dudy = sc->dvdy = 0.f;
+    }
+}
+
+/* Raytracer_Config::max_differential_ray_specular_bounces (src/lib/raytracer_config.h:33);
+ * no scene format sets it */
+#define MAX_DIFFERENTIAL_RAY_SPECULAR_BOUNCES 4
+
+/* Shading_Context::compute_differential_rays_for_specular_reflection (eta 0)
+ * and _for_specular_transmission (eta = etaI / etaT), src/ref/shading_context.cpp:357-403:
+ * the differential rays of the delta ray from the hit position in direction
+ * dir; ray[0], ray[1] the dx ray's origin and direction, ray[2], ray[3] the dy ray's. */
+static void specular_differentials(const shading_ctx* sc, v3 dir, float eta, v3 ray[4]) {
+    const v3 n = sc->normal, wo = sc->wo;
+    const v3 dndx = add3(mul3s(sc->dndu, sc->dudx), mul3s(sc->dndv, sc->dvdx));
+    const v3 dndy = add3(mul3s(sc->dndu, sc->dudy), mul3s(sc->dndv, sc->dvdy));
+    const float d_wo_dot_n_dx = dot3(sc->dwo_dx, n) + dot3(wo, dndx);
+    const float d_wo_dot_n_dy = dot3(sc->dwo_dy, n) + dot3(wo, dndy);
+    v3 dwi_dx, dwi_dy;
+    if (eta == 0.f) {
+        const float dot_wo_n = dot3(wo, n);
+        dwi_dx = sub3(mul3s(add3(mul3s(n, d_wo_dot_n_dx), mul3s(dndx, dot_wo_n)), 2.f), sc->dwo_dx);
+        dwi_dy = sub3(mul3s(add3(mul3s(n, d_wo_dot_n_dy), mul3s(dndy, dot_wo_n)), 2.f), sc->dwo_dy);
+    } else {
+        const float cos_o = dot3(wo, n);
+        const float cos_t = -dot3(dir, n);
+        const float k1 = eta * eta * cos_o / cos_t;
+        const float k2 = eta * cos_o - cos_t;
+        const float d_cos_t_dx = k1 * d_wo_dot_n_dx, d_cos_t_dy = k1 * d_wo_dot_n_dy;
+        dwi_dx = add3(add3(mul3s(sc->dwo_dx, -eta), mul3s(dndx, k2)), mul3s(n, eta * d_wo_dot_n_dx - d_cos_t_dx));
+        dwi_dy = add3(add3(mul3s(sc->dwo_dy, -eta), mul3s(dndy, k2)), mul3s(n, eta * d_wo_dot_n_dy - d_cos_t_dy));
+    }
+    ray[0] = add3(sc->position, sc->dpdx);
+    ray[1] = norm3(add3(dir, dwi_dx));
+    ray[2] = add3(sc->position, sc->dpdy);
+    ray[3] = norm3(add3(dir, dwi_dy));
 }
 
 static v3 sample_hemisphere_cosine(float u0, float u1) {
@@ -2271,23 +2318,26 @@ static void apply_material_bump(const yar_flat_scene* s, shading_ctx* sc) {
 
 /* check_for_delta_scattering_event / get_*_info, src/ref/delta_scattering.cpp:27-97, :252-324
  * (perfect reflector, perfect refractor, smooth glass; no nested dielectrics).  Returns 1 and the delta direction and attenuation for a delta
- * material, 2 for a delta material without a direction, 0 otherwise. */
+ * material, 2 for a delta material without a direction, 0 otherwise.  *kind: the
+ * Delta_Scattering_Type of the event, 0 reflection, etaI_over_etaT (> 0)
+ * transmission, -1 passthrough. */
 static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, float* u_ptr, v3* dir, col* atten,
-                            float* bsdf_prob) {
+                            float* bsdf_prob, float* kind) {
     const yar_material_desc* m = &s->materials[sc->material_index];
     *atten = mkc(1, 1, 1);
+    *kind = 0.f;
     if (sc->material_type == YAR_MATERIAL_PBRT3_UBER) {
         /* get_pbrt_uber_info, src/ref/delta_scattering.cpp:102-150 */
         const float fp = *u_ptr * (float)m->component_count;
         const int k = (int)fp;
-        const uint32_t kind = m->components[k];
+        const uint32_t comp = m->components[k];
         const float r = fp - (float)k;
         *u_ptr = r < 0.f ? 0.f : (ONE_MINUS_EPSILON < r ? ONE_MINUS_EPSILON : r);
         float delta_terms = 0.f;
         for (uint32_t c = 0; c < m->component_count; c++)
             if (m->components[c] >= YAR_UBER_DELTA_REFLECTION) delta_terms += 1.f;
         *bsdf_prob = 1.f - delta_terms / (float)m->component_count;
-        if (kind == YAR_UBER_DELTA_REFLECTION) {
+        if (comp == YAR_UBER_DELTA_REFLECTION) {
             const int enter = !sc->flipped;
             float fresnel = dielectric_fresnel(dot3(sc->normal, sc->wo),
                                                enter ? m->index_of_refraction : 1.f / m->index_of_refraction);
@@ -2295,9 +2345,10 @@ static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, floa
             *dir = reflect3(sc->wo, sc->normal);
             return 1;
         }
-        if (kind == YAR_UBER_OPACITY) {
+        if (comp == YAR_UBER_OPACITY) {
             *atten = mulcs(subc(mkc(1, 1, 1), ldc(m->opacity)), (float)m->component_count);
             *dir = neg3(sc->wo);
+            *kind = -1.f;
             return 1;
         }
         return 0;
@@ -2327,6 +2378,7 @@ static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, floa
         } else if (pick->type == YAR_MATERIAL_PERFECT_REFRACTOR) {
             const float eta = !sc->flipped ? 1.f / pick->index_of_refraction : pick->index_of_refraction;
             event = refract3(sc->wo, sc->normal, eta, dir) ? 1 : 2;
+            *kind = eta;
             prob = 1.f;
         }
         if (has1 && has2) prob *= pick == m1 ? amount : 1.f - amount;
@@ -2348,6 +2400,7 @@ static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, floa
     const int enter = !sc->flipped;
     if (sc->material_type == YAR_MATERIAL_PERFECT_REFRACTOR) {
         const float eta = enter ? 1.f / m->index_of_refraction : m->index_of_refraction;
+        *kind = eta;
         /* Total internal reflection leaves the reference's direction at its
          * zero default (an ASSERT in debug builds); the zero-length ray finds
          * nothing and the path ends.  Reported here as 2: no delta ray. */
@@ -2367,6 +2420,7 @@ static int delta_scattering(const yar_flat_scene* s, const shading_ctx* sc, floa
         const float eta = 1.f / eta_t_over_i;
         *atten = mulcs(m->transmittance_texture ? texture_transmittance(s, sc, m) : ldc(m->transmittance), eta * eta);
         refract3(sc->wo, sc->normal, eta, dir);
+        *kind = eta;
     }
     return 1;
 }
@@ -2408,7 +2462,7 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
             if (hit < 0) return YAR_ERR_CAPACITY;
             if (hit) init_shading(s, rd, h.object, h.prim, h.b, &sc);
             /* the camera ray's differential rays (trace_ray at bounce 0, path_tracing.cpp:25) */
-            if (hit && bounce == 0) uv_derivatives(&sc, ro, differential_dirs[0], differential_dirs[1]);
+            if (hit && bounce == 0) uv_derivatives(&sc, ro, differential_dirs[0], ro, differential_dirs[1]);
             if (bounce == 0) {
                 if (hit && emitted_radiance(s, &sc, &le)) L = addc(L, mulc(coeff, le));
                 else if (!hit && env->e) L = addc(L, mulc(coeff, env_radiance(env, rd, 1)));
@@ -2431,8 +2485,9 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
         v3 ddir;
         col datten;
         float bsdf_prob = 1.f; /* 1 - delta_layer_selection_probability */
+        float delta_kind;
         apply_material_bump(s, &sc);
-        const int delta = delta_scattering(s, &sc, &u_scatter, &ddir, &datten, &bsdf_prob);
+        const int delta = delta_scattering(s, &sc, &u_scatter, &ddir, &datten, &bsdf_prob, &delta_kind);
         if (delta == 2) break; /* perfect refractor at total internal reflection */
         bsdf_t f, f_sub[2];
         if (!delta || bsdf_prob != 0.f) {
@@ -2467,12 +2522,19 @@ static int trace_path(const yar_flat_scene* s, const mesh_light_sampler* mesh_sa
             ro = origin_for_direction(&sc, wi);
             rd = wi;
         } else {
-            /* the delta ray is traced at once; light it reaches counts (path_tracing.cpp:76-107) */
+            /* the delta ray is traced at once; light it reaches counts (path_tracing.cpp:76-107);
+             * reflected and transmitted delta rays carry differential rays while the vertex
+             * has dxdy derivatives, for max_differential_ray_specular_bounces bounces
+             * (delta_scattering.cpp:283-322) */
+            v3 diff[4];
+            const int has_diff = delta_kind >= 0.f && sc.has_dxdy && bounce < MAX_DIFFERENTIAL_RAY_SPECULAR_BOUNCES;
+            if (has_diff) specular_differentials(&sc, ddir, delta_kind, diff);
             ro = origin_for_direction(&sc, ddir);
             rd = ddir;
             hit = trace_closest(s, ro, rd, &h);
             if (hit < 0) return YAR_ERR_CAPACITY;
             if (hit) init_shading(s, rd, h.object, h.prim, h.b, &sc);
+            if (hit && has_diff) uv_derivatives(&sc, diff[0], diff[1], diff[2], diff[3]);
             coeff = mulc(coeff, datten);
             if (hit && emitted_radiance(s, &sc, &le)) L = addc(L, mulc(coeff, le));
             else if (!hit && env->e) L = addc(L, mulc(coeff, env_radiance(env, rd, 1)));
@@ -2531,7 +2593,9 @@ static int trace_direct(const yar_flat_scene* s, const env_sampler* env, v3 ro, 
     float bsdf_prob = 1.f;
     int delta = 0;
     if (sc.light_type == YAR_LIGHT_NULL) apply_material_bump(s, &sc);
-    if (sc.material_type != YAR_MATERIAL_NULL) delta = delta_scattering(s, &sc, &u_scatter, &ddir, &datten, &bsdf_prob);
+    float delta_kind;
+    if (sc.material_type != YAR_MATERIAL_NULL)
+        delta = delta_scattering(s, &sc, &u_scatter, &ddir, &datten, &bsdf_prob, &delta_kind);
     if (sc.light_type != YAR_LIGHT_NULL) {
         if (emitted_radiance(s, &sc, &le)) L = le;
     } else if (sc.material_type != YAR_MATERIAL_NULL && (!delta || bsdf_prob != 0.f)) {
@@ -2865,10 +2929,11 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
     if (s->other_light_count) return YAR_ERR_UNSUPPORTED;
     /* image textures: the reflectance of diffuse, plastic, coated diffuse, glass
      * and diffuse transmission, the transmittance of glass and diffuse
-     * transmission, and bump maps, with camera-ray differentials in the path
-     * tracer; no delta materials in a textured scene (their differential rays
-     * are not restated).  A constant bump height needs no differentials. */
-    int textured = 0, delta_materials = 0;
+     * transmission, and bump maps, with camera-ray differentials and the
+     * specular differential rays of delta bounces in the path tracer; not with
+     * the direct-lighting algorithm.  A constant bump height needs no
+     * differentials. */
+    int textured = 0;
     for (uint32_t i = 0; i < s->material_count; i++) {
         const yar_material_desc* m = &s->materials[i];
         if (m->other_textured_parameters) return YAR_ERR_UNSUPPORTED;
@@ -2888,11 +2953,8 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
             textured = 1;
         }
         if (m->bump == 2 && !used[2]) return YAR_ERR_INVALID;
-        delta_materials |= m->type == YAR_MATERIAL_PERFECT_REFLECTOR || m->type == YAR_MATERIAL_PERFECT_REFRACTOR ||
-                           (m->type == YAR_MATERIAL_GLASS && !(m->u_roughness > 0.f)) ||
-                           m->type == YAR_MATERIAL_PBRT3_UBER || m->type == YAR_MATERIAL_MIX;
     }
-    if (textured && (cfg->rendering_algorithm == 0 || delta_materials)) return YAR_ERR_UNSUPPORTED;
+    if (textured && cfg->rendering_algorithm == 0) return YAR_ERR_UNSUPPORTED;
     init_ewa_weights();
     for (uint32_t i = 0; i < s->material_count; i++) {
         const yar_material_desc* m = &s->materials[i];

@@ -76,6 +76,17 @@ Fixtures
                              checker reflectance and transmittance, GGX boxes;
                              rendered by the reference from the edited flat
                              scene, seed 21.
+  cornell_spectex_64.yfs / .npz  textures seen through delta bounces: the
+                             floor, back and left walls checker-textured, the
+                             right wall a mirror with uvs and splayed vertex
+                             normals, a smooth glass panel with uvs and
+                             splayed normals in front of the room (checker Kr
+                             2 x 3 and Kt set on the flattened scene), a
+                             mirror box and a glass box without uvs; the
+                             texture lookups behind the panel and in the
+                             mirror use the specular differential rays;
+                             rendered by the reference from the edited flat
+                             scene, seed 23.
   cornell_fourier_64.yfs / .npz  pbrt "fourier" boxes: a one-channel and a
                              three-channel layerlab table written by
                              write_fourier_bsdf (15 zenith nodes, glossy lobes
@@ -462,6 +473,20 @@ def cornell_bump_64():
     np.savez_compressed(os.path.join(HERE, "cornell_bump_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def cornell_spectex_64():
+    from yar_gb300 import exr
+    with tempfile.TemporaryDirectory() as d:
+        exr.write_exr(os.path.join(d, "checks.exr"), scenes.texture_image(), False, {})
+        pbrt = os.path.join(d, "cornell_spectex.pbrt")
+        open(pbrt, "w").write(scenes.specular_texture_pbrt("checks.exr"))
+        yfs = os.path.join(d, "cornell_spectex.yfs")
+        oracle.ref_flatten(pbrt, yfs, seed_offset=1)
+        s = scenes.texture_glass_panel(FlatScene.read(yfs))
+        s.write(os.path.join(HERE, "cornell_spectex_64.yfs"))
+        img, info = oracle.ref_render_flat(s, threads=8, textures_from=pbrt)
+    np.savez_compressed(os.path.join(HERE, "cornell_spectex_64.npz"), image=img, variance=np.float64(info["variance"]))
+
+
 def write_fourier_bsdf(path, channels, nodes=15, order=8, gloss=6.0, albedo=(0.7, 0.5, 0.3)):
     """A layerlab "SCATFUN" v1 file (the subset Pbrt3_Fourier_Material::load_bsdf_file
     reads, src/lib/material_pbrt.cpp:24-102): increasing zenith cosines from -1
@@ -611,7 +636,7 @@ if __name__ == "__main__":
                              "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64",
                              "cornell_direct_64", "cornell_direct_env_64", "cornell_texture_64", "checkpoint_c1",
                              "cornell_gaussian_64", "cornell_triangle_64", "cornell_c1_256", "cornell_alpha_64",
-                             "cornell_bump_64", "cornell_fourier_64",
+                             "cornell_bump_64", "cornell_fourier_64", "cornell_spectex_64",
                              "exr_files",
                              "kdtree_cache_files"]
     for name in which:

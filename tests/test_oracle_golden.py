@@ -126,7 +126,8 @@ def test_builder_against_live_reference_large_mesh():
                                   "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64",
                                   "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64",
                                   "cornell_texture_64", "cornell_gaussian_64", "cornell_triangle_64",
-                                  "cornell_alpha_64", "cornell_bump_64", "cornell_fourier_64"])
+                                  "cornell_alpha_64", "cornell_bump_64", "cornell_fourier_64",
+                                  "cornell_spectex_64"])
 def test_oracle_render_matches_reference_golden(name):
     """The oracle's path loop, sampler, shading, BSDFs (diffuse, GGX metal, rough
     glass, plastic in both of the reference's forms, coated diffuse), delta
@@ -216,16 +217,14 @@ def test_alpha_texture_file_round_trip(tmp_path):
 
 def test_textured_scenes_outside_the_restated_part_are_refused():
     """Image textures are restated for the reflectance and transmittance slots
-    and bump maps in the path tracer with camera-ray differentials; with the
-    direct-lighting algorithm, next to delta materials, on other parameters,
-    in a slot the material does not read, or as the bump map of a mix's
+    and bump maps in the path tracer with camera-ray and specular
+    differentials; with the direct-lighting algorithm, on other parameters, in
+    a slot the material does not read, or as the bump map of a mix's
     sub-material the oracle refuses the scene."""
-    for change in ("direct", "mirror", "other", "slot", "mix_bump"):
+    for change in ("direct", "other", "slot", "mix_bump"):
         s = FlatScene.read(golden("cornell_texture_64.yfs"))
         if change == "direct":
             s.config["rendering_algorithm"] = 0
-        elif change == "mirror":
-            s.materials["type"][-1] = 0  # perfect reflector
         elif change == "other":
             s.materials["other_textured_parameters"][-1] = 1
         elif change == "slot":
@@ -248,6 +247,25 @@ def test_oracle_constant_bump_on_delta_materials_against_live_reference():
     s = constant_bumps_with_delta_materials()
     s.config["max_light_bounces"] = 5
     ref, info = oracle.ref_render_flat(s, threads=8)
+    img, var = oracle.render(s, threads=8)
+    assert np.array_equal(bits(img), bits(ref))
+    assert var == info["variance"]
+
+
+@pytest.mark.skipif(not oracle.have_reference(), reason="reference not built here")
+def test_oracle_specular_differentials_against_live_reference(tmp_path):
+    """Textures behind chains of delta bounces, past the reference's 4
+    specular bounces with differential rays and past the sampler's dimension
+    budget (maxdepth 12, another seed): the oracle against the reference's
+    render of the same flat scene, bit for bit."""
+    from yar_gb300 import exr
+    exr.write_exr(str(tmp_path / "checks.exr"), scenes.texture_image(), False, {})
+    pbrt = tmp_path / "spectex.pbrt"
+    pbrt.write_text(scenes.specular_texture_pbrt("checks.exr", seed=29, width=32, height=32, spp=4, maxdepth=12))
+    yfs = tmp_path / "spectex.yfs"
+    oracle.ref_flatten(str(pbrt), str(yfs), seed_offset=3)
+    s = scenes.texture_glass_panel(FlatScene.read(str(yfs)))
+    ref, info = oracle.ref_render_flat(s, threads=8, textures_from=str(pbrt))
     img, var = oracle.render(s, threads=8)
     assert np.array_equal(bits(img), bits(ref))
     assert var == info["variance"]

@@ -70,7 +70,8 @@ def compare(img, ref):
                                   "cornell_meshlight_64", "cornell_spherelight_64", "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
                   "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64",
                                   "cornell_texture_64", "cornell_gaussian_64", "cornell_triangle_64",
-                                  "cornell_alpha_64", "cornell_bump_64", "cornell_fourier_64"])
+                                  "cornell_alpha_64", "cornell_bump_64", "cornell_fourier_64",
+                                  "cornell_spectex_64"])
 def test_render_matches_reference_golden(gpu_ctx, name):
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
@@ -96,7 +97,7 @@ RENDER_GOLDENS = ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornel
                   "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
                   "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64", "cornell_texture_64",
                   "cornell_gaussian_64", "cornell_triangle_64", "cornell_alpha_64", "cornell_bump_64",
-                  "cornell_fourier_64"]
+                  "cornell_fourier_64", "cornell_spectex_64"]
 
 
 @pytest.mark.parametrize("name", RENDER_GOLDENS)
@@ -141,7 +142,7 @@ def _past_budget_scene(name):
 @pytest.mark.parametrize("name,maxb,rr,seed_offset", [
     ("cornell_c1_64", 16, 3, 1), ("cornell_ggx_64", 14, 1, 4), ("cornell_delta_64", 12, 1, 2),
     ("cornell_delta_64", 9, 1, 6), ("cornell_delta_64", 16, 1, 11), ("cornell_mix_64", 12, 2, 3), ("cornell_uber_64", 12, 1, 5),
-    ("cornell_envmap_64", 13, 3, 8), ("cornell_meshlight_64", 12, 2, 9)])
+    ("cornell_envmap_64", 13, 3, 8), ("cornell_meshlight_64", 12, 2, 9), ("cornell_spectex_64", 12, 1, 3)])
 def test_render_past_the_dimension_budget_bit_identical(gpu_ctx, name, maxb, rr, seed_offset):
     """Paths that run past the sampler's dimension budget (deep paths, and
     delta chains whose Russian roulette takes extra dimensions, so even
@@ -433,14 +434,12 @@ def test_fourier_tables_checked_on_upload(gpu_ctx):
 
 
 def test_bump_maps_refused_where_they_are_not_evaluated(gpu_ctx):
-    """The static, batched and guided renders and the direct-lighting algorithm
-    refuse bump maps; a mix's sub-material may not have one; a texture in a
-    slot the material does not read is refused."""
+    """The guided render and the direct-lighting algorithm refuse bump maps; a
+    mix's sub-material may not have one; a texture in a slot the material does
+    not read is refused."""
     from yar_gb300 import native
     s = constant_bumps_with_delta_materials()
     gpu_ctx.upload_scene(s)
-    with pytest.raises(native.YarError):
-        gpu_ctx.render_batch([s])
     with pytest.raises(native.YarError):
         gpu_ctx.guided_render(64, 64, passes=1)
     d = constant_bumps_with_delta_materials()
@@ -463,17 +462,33 @@ def test_bump_maps_refused_where_they_are_not_evaluated(gpu_ctx):
 
 
 def test_textured_scene_refused_where_textures_are_not_evaluated(gpu_ctx):
-    """The static and batched renders and scenes with delta materials refuse
-    image textures instead of rendering them as constants."""
+    """The direct-lighting algorithm and the guided render refuse image
+    textures instead of rendering them as constants."""
     from yar_gb300 import native
-    s = FlatScene.read(golden("cornell_texture_64.yfs"))
+    s = FlatScene.read(golden("cornell_spectex_64.yfs"))
     gpu_ctx.upload_scene(s)
-    with pytest.raises(native.YarError):
-        gpu_ctx.render_batch([s])
-    s.materials["type"][-1] = native.MATERIAL_PERFECT_REFLECTOR
+    with pytest.raises(native.YarError) as e:
+        gpu_ctx.guided_render(64, 64, passes=1)
+    assert e.value.code == native.YAR_ERR_UNSUPPORTED
+    s.config["rendering_algorithm"] = 0
     gpu_ctx.upload_scene(s)
-    with pytest.raises(native.YarError):
+    with pytest.raises(native.YarError) as e:
         gpu_ctx.render(64, 64)
+    assert e.value.code == native.YAR_ERR_UNSUPPORTED
+
+
+def test_specular_differentials_reach_textures_behind_delta_bounces(gpu_ctx):
+    """Textures seen through the glass panel and in the mirror wall are looked
+    up with the differential rays the delta bounces carry (up to the
+    reference's 4 specular bounces): bit for bit the oracle's image, with the
+    chains of delta bounces cut at several depths."""
+    s = FlatScene.read(golden("cornell_spectex_64.yfs"))
+    for maxb in (2, 5, 9):
+        s.config["max_light_bounces"] = maxb
+        gpu_ctx.upload_scene(s)
+        img, _ = gpu_ctx.render(64, 64)
+        ref, _ = oracle.render(s, threads=8, correctly_rounded_trig=True)
+        assert np.array_equal(img.view(np.uint32), ref.view(np.uint32)), maxb
 
 
 def test_direct_lighting_scene_refused_by_path_tracer_only_entry_points(gpu_ctx, tmp_path):

@@ -64,6 +64,7 @@ struct Branch {
     cudaStream_t stream = nullptr;
     uint64_t cap = 0;  // paths per chunk
     int n1d = 1, n2d = 1;
+    bool diffs = false;  // a scene of the branch carries specular differential rays
     std::vector<Device_Buffer> B;
     Path_State ps{};
     Queues q{};
@@ -117,13 +118,14 @@ int alloc_branches(Batch& bt, int nb, uint64_t chunk_cap, bool one_spp) {
         br.cap = std::max(br.cap, cp);
         br.n1d = std::max(br.n1d, s.p.n1d);
         br.n2d = std::max(br.n2d, s.p.n2d);
+        br.diffs = br.diffs || s.p.spec_diffs;
     }
     int rc = YAR_OK;
     for (Branch& br : bt.branches) {
         cudaError_t e = cudaStreamCreateWithFlags(&br.stream, cudaStreamNonBlocking);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "batch streams");
         if (br.cap == 0) continue;
-        br.B.assign(32, Device_Buffer{});
+        br.B.assign(33, Device_Buffer{});
         const size_t cap = br.cap;
         const size_t sizes[32] = {0, 0, cap * br.n1d * sizeof(float), cap * br.n2d * sizeof(float2),
                                   cap * 16, cap * 16, cap * 4, cap * 16, cap * 16, cap * 16, cap * 16, cap * 16,
@@ -132,11 +134,13 @@ int alloc_branches(Batch& bt, int nb, uint64_t chunk_cap, bool one_spp) {
                                   cap, cap * 4, 2 * kShadeClasses * sizeof(uint32_t),  // shading order
                                   cap * 2, kRayBins * sizeof(uint32_t)};              // extend-queue sort
         for (int i = 2; i < 32 && rc == YAR_OK; i++) rc = device_alloc(ctx, br.B[i], sizes[i]);
+        if (br.diffs && rc == YAR_OK) rc = device_alloc(ctx, br.B[32], cap * 3 * sizeof(float4));
         if (rc != YAR_OK) return rc;
         std::vector<Device_Buffer>& B = br.B;
         br.ps = Path_State{dp<float4>(B[4]), dp<float4>(B[5]), dp<uint32_t>(B[6]), dp<uint4>(B[7]),
                            dp<float4>(B[8]), dp<float4>(B[9]), dp<float4>(B[10]), dp<float4>(B[11]),
                            dp<float4>(B[12]), dp<uint8_t>(B[13]), dp<float4>(B[14]), dp<uint2>(B[15]), nullptr};
+        br.ps.diff = dp<float4>(B[32]);
         br.q = Queues{};
         br.q.ext_rays[0] = dp<float4>(B[16]);
         br.q.ext_rays[1] = dp<float4>(B[17]);
@@ -189,10 +193,12 @@ cudaError_t enqueue_scene(Batch& bt, int si, bool one_spp, unsigned long long* s
     }
     Queues qs = q;  // q with the order, for the shade kernel
     qs.order = mixed ? dp<uint32_t>(br.B[28]) : nullptr;
+    ps.image_samples = dp<float2>(sc.image_samples);  // textured hits' camera differentials
     cudaError_t e = cudaSuccess;
     for (uint64_t first = 0; first < sc.pixels && e == cudaSuccess; first += chunk_pixels) {
         const uint32_t cp = (uint32_t)std::min<uint64_t>(chunk_pixels, sc.pixels - first);
         const uint32_t paths = cp * (uint32_t)p.spp;
+        ps.chunk_first = (uint32_t)first;
         e = cudaMemsetAsync(ctr, 0, 8 * sizeof(uint32_t), st);
         if (e == cudaSuccess)
             e = launch_generate(p, (uint32_t)first, cp, dp<float>(br.B[2]), dp<float>(br.B[3]),
@@ -350,8 +356,6 @@ int render_batch(yar_gpu_ctx* ctx, const yar_flat_scene* const* scenes, uint32_t
             return fail(ctx, rc, "scene " + std::to_string(i) + ": " + yar_gpu_last_error(s.sub));
         if ((rc = prepare_render_params(s.sub, s.p)) != YAR_OK)
             return fail(ctx, rc, "scene " + std::to_string(i) + ": " + yar_gpu_last_error(s.sub));
-        if (s.p.textured)
-            return fail(ctx, YAR_ERR_UNSUPPORTED, "scene " + std::to_string(i) + ": batched renders do not evaluate image textures or bump maps");
         if (s.sub->render.config.rendering_algorithm == 0)
             return fail(ctx, YAR_ERR_UNSUPPORTED, "scene " + std::to_string(i) +
                                                       ": batched renders run the path tracer only (rendering_algorithm 1)");

@@ -312,8 +312,9 @@ direct_shade_kernel(Render_Params p, Scene_Dev S, uint32_t chunk_first, uint32_t
         int delta = 0;
         const bool is_light = (uint32_t)oinfo.z != YAR_LIGHT_NULL;
         const Material_Dev* mat = (uint32_t)oinfo.x != YAR_MATERIAL_NULL ? &S.materials[oinfo.y] : nullptr;
+        float delta_kind;
         if (mat && mat->delta != kDeltaNone)
-            delta = delta_scattering(sc, *mat, S.materials, u_sc, delta_wi, delta_atten, bsdf_prob);
+            delta = delta_scattering(sc, *mat, S.materials, u_sc, delta_wi, delta_atten, bsdf_prob, delta_kind);
         if (is_light) {
             L = emitted(S, oinfo, sc.flipped);
         } else if (mat && (delta == 0 || bsdf_prob != 0.f)) {

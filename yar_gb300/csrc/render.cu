@@ -510,9 +510,9 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
     // scratch: everything sized by the largest chunk; a buffer of the last
     // call is kept when it is large enough (cudaMalloc and cudaFree synchronise)
     std::vector<Device_Buffer>& B = ctx->render_scratch;
-    if (B.size() != 42) {
+    if (B.size() != 43) {
         for (Device_Buffer& b : B) device_free(b);
-        B.assign(42, Device_Buffer{});
+        B.assign(43, Device_Buffer{});
     }
     int rc = YAR_OK;
     auto alloc = [&](int i, size_t bytes) {
@@ -562,6 +562,7 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
     alloc(39, 2 * kShadeClasses * sizeof(uint32_t));       // class sizes and cursors
     alloc(40, cap * sizeof(uint16_t));                     // extend-queue sort keys
     alloc(41, kRayBins * sizeof(uint32_t));                // their histogram, then the bins' cursors
+    if (p.spec_diffs) alloc(42, cap * 3 * sizeof(float4));  // delta rays' specular differential rays
     if (rc != YAR_OK) return rc;
 
     Path_State ps{dptr<float4>(B[4]), dptr<float4>(B[5]), dptr<uint32_t>(B[6]), dptr<uint4>(B[7]),
@@ -570,6 +571,7 @@ int render_run_params(yar_gpu_ctx* ctx, const Render_Params& p_in, float* rgb_ou
     ps.rng_draws = dptr<uint32_t>(B[30]);
     ps.deferred = dptr<float4>(B[31]);
     ps.image_samples = dptr<float2>(B[1]);
+    ps.diff = dptr<float4>(B[42]);
     Queues q{};
     q.ext_rays[0] = dptr<float4>(B[16]);
     q.ext_rays[1] = dptr<float4>(B[17]);

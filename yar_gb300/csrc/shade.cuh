@@ -286,15 +286,18 @@ __device__ __forceinline__ float dielectric_fresnel(float cos_i, float eta) {
 
 // check_for_delta_scattering_event with get_perfect_reflector_info,
 // get_perfect_refractor_info and get_glass_info (src/ref/delta_scattering.cpp:27-97,
-// :252-324) and get_pbrt_uber_info (:102-150), constant parameters, no bump
-// map, no nested dielectrics.  Returns 0 (no delta event), 1 (dir and atten
-// set) or 2: a perfect refractor at total internal reflection, where the
-// reference has no direction (an assertion) and the path ends.  bsdf_prob is
-// 1 - the delta layers' selection probability.
+// :252-324) and get_pbrt_uber_info (:102-150), constant parameters, no
+// nested dielectrics.  Returns 0 (no delta event), 1 (dir and atten set) or
+// 2: a perfect refractor at total internal reflection, where the reference
+// has no direction (an assertion) and the path ends.  bsdf_prob is 1 - the
+// delta layers' selection probability; kind the event's
+// Delta_Scattering_Type: 0 reflection, etaI_over_etaT (> 0) transmission, -1
+// passthrough.
 __device__ __forceinline__ int delta_scattering(const Shading& sc, const Material_Dev& m,
                                                 const Material_Dev* materials, float& u, V3& dir, Col& atten,
-                                                float& bsdf_prob) {
+                                                float& bsdf_prob, float& kind) {
     atten = col(1.f, 1.f, 1.f);
+    kind = 0.f;
     const bool enter = !sc.flipped;
     if (m.delta == kDeltaMix) {
         // get_mix_info (delta_scattering.cpp:154-189) for sub-materials that are pure
@@ -314,7 +317,8 @@ __device__ __forceinline__ int delta_scattering(const Shading& sc, const Materia
             event = 1;
             prob = 1.f;
         } else if (pick.type == kPerfectRefractor) {
-            event = refract(sc.wo, sc.n, enter ? 1.f / pick.ior : pick.ior, dir) ? 1 : 2;
+            kind = enter ? 1.f / pick.ior : pick.ior;
+            event = refract(sc.wo, sc.n, kind, dir) ? 1 : 2;
             prob = 1.f;
         }
         if (has1 && has2) prob *= first ? m.mix_amount : 1.f - m.mix_amount;
@@ -328,22 +332,23 @@ __device__ __forceinline__ int delta_scattering(const Shading& sc, const Materia
         const uint32_t count = (m.uber_components >> 24) & 0xfu;
         const float fp = u * (float)count;
         const int k = (int)fp;
-        const uint32_t kind = (m.uber_components >> (3 * k)) & 7u;
+        const uint32_t comp = (m.uber_components >> (3 * k)) & 7u;
         const float r = fp - (float)k;
         u = r < 0.f ? 0.f : (__uint_as_float(0x3f7fffffu) < r ? __uint_as_float(0x3f7fffffu) : r);
         float delta_terms = 0.f;
         for (uint32_t c = 0; c < count; c++)
             if (((m.uber_components >> (3 * c)) & 7u) >= YAR_UBER_DELTA_REFLECTION) delta_terms += 1.f;
         bsdf_prob = 1.f - delta_terms / (float)count;
-        if (kind == YAR_UBER_DELTA_REFLECTION) {
+        if (comp == YAR_UBER_DELTA_REFLECTION) {
             const float fresnel = dielectric_fresnel(dot(sc.n, sc.wo), enter ? m.ior : 1.f / m.ior);
             atten = mul(m.delta_reflectance, (float)count * fresnel);
             dir = reflect(sc.wo, sc.n);
             return 1;
         }
-        if (kind == YAR_UBER_OPACITY) {
+        if (comp == YAR_UBER_OPACITY) {
             atten = mul(col(1.f, 1.f, 1.f) - m.extra, (float)count);
             dir = -sc.wo;
+            kind = -1.f;
             return 1;
         }
         return 0;
@@ -354,7 +359,10 @@ __device__ __forceinline__ int delta_scattering(const Shading& sc, const Materia
         atten = m.reflectance;
         return 1;
     }
-    if (m.delta == kDeltaRefractor) return refract(sc.wo, sc.n, enter ? 1.f / m.ior : m.ior, dir) ? 1 : 2;
+    if (m.delta == kDeltaRefractor) {
+        kind = enter ? 1.f / m.ior : m.ior;
+        return refract(sc.wo, sc.n, kind, dir) ? 1 : 2;
+    }
     const float eta_t_over_i = enter ? m.ior : 1.f / m.ior;
     const float fresnel = dielectric_fresnel(dot(sc.n, sc.wo), eta_t_over_i);
     if (u < fresnel) {
@@ -364,6 +372,7 @@ __device__ __forceinline__ int delta_scattering(const Shading& sc, const Materia
     }
     const float eta = 1.f / eta_t_over_i;
     atten = mul(m.transmittance, eta * eta);
+    kind = eta;
     return refract(sc.wo, sc.n, eta, dir) ? 1 : 2;
 }
 

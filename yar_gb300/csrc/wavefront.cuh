@@ -57,8 +57,13 @@ enum : uint32_t {
     kPendDirect = 1u << 26,
     kDeltaArrival = 1u << 27,
     kDeltaFinal = 1u << 28,
-    kDeferred = 1u << 29  // exact tail: the path's next extend ray waits in Path_State::deferred
+    kDeferred = 1u << 29,  // exact tail: the path's next extend ray waits in Path_State::deferred
+    kDiffRays = 1u << 30   // the delta ray carries specular differential rays (Path_State::diff)
 };
+
+// Raytracer_Config::max_differential_ray_specular_bounces (src/lib/raytracer_config.h:33);
+// no scene format sets it.
+constexpr int kMaxDifferentialRaySpecularBounces = 4;
 
 struct Rect_Light_Dev {
     float4 r0, r1, r2;  // light_to_world rows
@@ -134,6 +139,7 @@ struct Render_Params {
     // vertex is deferred); 2 = exact tail, waves (draws are counted per path).
     int32_t exact_tail;
     int32_t textured;  // some material has an image texture or a bump map
+    int32_t spec_diffs;  // image textures with delta materials: delta rays carry differential rays
 };
 
 struct Path_State {
@@ -154,6 +160,8 @@ struct Path_State {
     float4* deferred;      // exact tail: the deferred extend ray, 2 float4 per slot
     const float2* image_samples;  // image-plane samples of the render (textured scenes' ray differentials)
     uint32_t chunk_first;         // the chunk's first pixel
+    float4* diff;  // specular differential rays of the slot's delta ray: dx origin, dx direction, dy origin,
+                   // dy direction packed in 3 float4 (Render_Params::spec_diffs)
 };
 
 // Learned-proposal hooks of the shade kernel (guided render only).
@@ -960,21 +968,23 @@ __device__ bool texture_geometry(const Scene_Dev& S, uint32_t object, uint32_t p
 }
 
 // Shading_Context::calculate_dxdy_derivatives + calculate_uv_derivates
-// (shading_context.cpp:242-333): the uv derivatives along the differential
-// rays (origin o, directions dx, dy) through the hit plane.
-__device__ void uv_derivatives(const Shading& sc, V3 o, V3 dx, V3 dy, V3 dpdu, V3 dpdv, float2& duvdx,
-                               float2& duvdy) {
+// (shading_context.cpp:242-333): where the differential rays (ox, dx) and
+// (oy, dy) cross the hit's plane, and the uv derivatives there.  False when
+// the sanity check drops them (has_dxdy_derivatives false: all zero).
+__device__ bool dxdy_derivatives(const Shading& sc, V3 ox, V3 dx, V3 oy, V3 dy, V3 dpdu, V3 dpdv, V3& dpdx, V3& dpdy,
+                                 float2& duvdx, float2& duvdy) {
     const V3 gn = sc.ng;
     const float plane_d = -dot(gn, sc.position);
-    V3 dpdx = v3(0.f, 0.f, 0.f), dpdy = v3(0.f, 0.f, 0.f);
-    auto plane_t = [&](V3 d) {  // ray_plane_intersection, src/lib/math.cpp:27-31
+    dpdx = v3(0.f, 0.f, 0.f);
+    dpdy = v3(0.f, 0.f, 0.f);
+    auto plane_t = [&](V3 o, V3 d) {  // ray_plane_intersection, src/lib/math.cpp:27-31
         const float k = -dot(o, gn) - plane_d;
         return k == 0 ? 0.f : k / dot(d, gn);
     };
-    const float tx = plane_t(dx);
-    if (fabsf(tx) != __int_as_float(0x7f800000)) dpdx = (o + mul(dx, tx)) - sc.position;
-    const float ty = plane_t(dy);
-    if (fabsf(ty) != __int_as_float(0x7f800000)) dpdy = (o + mul(dy, ty)) - sc.position;
+    const float tx = plane_t(ox, dx);
+    if (fabsf(tx) != __int_as_float(0x7f800000)) dpdx = (ox + mul(dx, tx)) - sc.position;
+    const float ty = plane_t(oy, dy);
+    if (fabsf(ty) != __int_as_float(0x7f800000)) dpdy = (oy + mul(dy, ty)) - sc.position;
     const float ax = fabsf(gn.x), ay = fabsf(gn.y), az = fabsf(gn.z);
     const int dim0 = (ax > ay && ax > az) ? 1 : 0;
     const int dim1 = (ax > ay && ax > az) ? 2 : (ay > az ? 2 : 1);
@@ -993,7 +1003,45 @@ __device__ void uv_derivatives(const Shading& sc, V3 o, V3 dx, V3 dy, V3 dpdu, V
     if (fabsf(duvdx.x) > 1e9f || fabsf(duvdx.y) > 1e9f || fabsf(duvdy.x) > 1e9f || fabsf(duvdy.y) > 1e9f) {
         duvdx = make_float2(0.f, 0.f);
         duvdy = make_float2(0.f, 0.f);
+        dpdx = v3(0.f, 0.f, 0.f);
+        dpdy = v3(0.f, 0.f, 0.f);
+        return false;
     }
+    return true;
+}
+
+// The differential rays a hit's derivatives come from (trace_ray's
+// differential_rays argument, src/ref/path_tracing.cpp:25, :86-87): at bounce
+// 0 the camera ray's, one pixel over and scaled to the sample's footprint
+// (src/ref/reference_renderer.cpp:367-378); where a delta ray arrives, the
+// specular differential rays it carries (kDiffRays); else none.
+__device__ __noinline__ bool incoming_differentials(const Render_Params& p, const Path_State& ps, uint32_t slot,
+                                                   int bounce, uint32_t info, V3& ox, V3& dx, V3& oy, V3& dy) {
+    if (bounce == 0) {
+        const uint32_t lp = slot / (uint32_t)p.spp, k = slot - lp * (uint32_t)p.spp;
+        int x, y;
+        pixel_stream(p, ps.chunk_first + lp, x, y);
+        const float2 fs = ps.image_samples[((size_t)ps.chunk_first + lp) * (uint32_t)p.spp + k];
+        const float fx = (float)x + fs.x, fy = (float)y + fs.y;
+        V3 d, o1;
+        camera_ray(p.camera, fx, fy, ox, d);
+        camera_ray(p.camera, fx + 1.f, fy, o1, dx);
+        camera_ray(p.camera, fx, fy + 1.f, o1, dy);
+        const float scale = 1.f / sqrtf((float)p.spp);
+        dx = d + mul(dx - d, scale);
+        dx = divs(dx, len(dx));
+        dy = d + mul(dy - d, scale);
+        dy = divs(dy, len(dy));
+        oy = ox;
+        return true;
+    }
+    if (!(info & kDiffRays)) return false;
+    const float4 a = ps.diff[3 * (size_t)slot], b = ps.diff[3 * (size_t)slot + 1], c = ps.diff[3 * (size_t)slot + 2];
+    ox = v3(a.x, a.y, a.z);
+    dx = v3(a.w, b.x, b.y);
+    oy = v3(b.z, b.w, c.x);
+    dy = v3(c.y, c.z, c.w);
+    return true;
 }
 
 // Where a hit looks its textures up: the shading context's uv, world-space
@@ -1005,31 +1053,18 @@ struct Tex_Site {
 };
 
 // The texture site of a hit (init_from_triangle_mesh_intersection and
-// calculate_dxdy_derivatives): the camera ray's differential rays, one pixel
-// over and scaled to the sample's footprint (src/ref/reference_renderer.cpp:367-378),
-// give the derivatives at bounce 0; later vertices have none.
+// calculate_dxdy_derivatives): the uv derivatives come from the hit's
+// incoming differential rays, if it has any.
 __device__ __noinline__ void texture_site(const Render_Params& p, const Scene_Dev& S, const Path_State& ps,
-                                          uint32_t slot, int bounce, const Shading& sc, float4 h4, uint2 h2,
-                                          Tex_Site& t) {
+                                          uint32_t slot, int bounce, uint32_t info, const Shading& sc, float4 h4,
+                                          uint2 h2, Tex_Site& t) {
     float2 uv = make_float2(0.f, 0.f), duvdx = make_float2(0.f, 0.f), duvdy = make_float2(0.f, 0.f);
     V3 dpdu = v3(0.f, 0.f, 0.f), dpdv = v3(0.f, 0.f, 0.f);
     t.has_uv = texture_geometry(S, h2.y, h2.x, h4.y, h4.z, h4.w, uv, dpdu, dpdv);
-    if (t.has_uv && bounce == 0) {
-        const uint32_t lp = slot / (uint32_t)p.spp, k = slot - lp * (uint32_t)p.spp;
-        int x, y;
-        pixel_stream(p, ps.chunk_first + lp, x, y);
-        const float2 fs = ps.image_samples[((size_t)ps.chunk_first + lp) * (uint32_t)p.spp + k];
-        const float fx = (float)x + fs.x, fy = (float)y + fs.y;
-        V3 o, d, o1, dx, dy;
-        camera_ray(p.camera, fx, fy, o, d);
-        camera_ray(p.camera, fx + 1.f, fy, o1, dx);
-        camera_ray(p.camera, fx, fy + 1.f, o1, dy);
-        const float scale = 1.f / sqrtf((float)p.spp);
-        dx = d + mul(dx - d, scale);
-        dx = divs(dx, len(dx));
-        dy = d + mul(dy - d, scale);
-        dy = divs(dy, len(dy));
-        uv_derivatives(sc, o, dx, dy, dpdu, dpdv, duvdx, duvdy);
+    V3 ox, dx, oy, dy;
+    if (t.has_uv && incoming_differentials(p, ps, slot, bounce, info, ox, dx, oy, dy)) {
+        V3 dpdx, dpdy;
+        dxdy_derivatives(sc, ox, dx, oy, dy, dpdu, dpdv, dpdx, dpdy, duvdx, duvdy);
     }
     t.uv = uv;
     t.duvdx = duvdx;
@@ -1057,14 +1092,12 @@ __device__ __forceinline__ float bump_height_at(const Scene_Dev& S, const Tex_Si
     return 0.2126729f * c.r + 0.7151522f * c.g + 0.0721750f * c.b;
 }
 
-// Shading_Context::apply_bump_map (src/ref/shading_context.cpp:419-462) with the
-// geometry it reads: the normal's uv derivatives (init_from_triangle_mesh_intersection,
-// :225-238; to world space and flipped with the normal, :102-109, :128-133) and
-// the shading frame's second tangent (:150-167).  Heights at the uv and one
-// footprint step along u and v perturb the tangents; the normal is rebuilt
-// from them, turned into the geometric normal's hemisphere and adjusted.
-__device__ __noinline__ void apply_bump(const Scene_Dev& S, const Material_Dev& m, const Tex_Site& t,
-                                        uint32_t object, uint32_t prim, float b0, float b1, float b2, Shading& sc) {
+// The normal's uv derivatives of a hit (init_from_triangle_mesh_intersection,
+// src/ref/shading_context.cpp:225-238; to world space, scaled with the
+// normal and flipped with it, :102-109, :128-133); zero without uvs.
+__device__ __noinline__ void normal_derivatives(const Scene_Dev& S, uint32_t object, uint32_t prim, float b0,
+                                                float b1, float b2, bool has_uv, bool flipped, V3& dndu_out,
+                                                V3& dndv_out) {
     const float4* orec = S.ds.objects + 6 * (size_t)object;
     const uint32_t tri_offset = __float_as_uint(__ldg(orec + 4).w);
     const size_t g = (size_t)tri_offset + prim;
@@ -1084,7 +1117,7 @@ __device__ __noinline__ void apply_bump(const Scene_Dev& S, const Material_Dev& 
         if (len2(in) != 0.f) normal = normalized(in);
     }
     V3 dndu = v3(0.f, 0.f, 0.f), dndv = v3(0.f, 0.f, 0.f);
-    if (t.has_uv) {
+    if (has_uv) {
         // uvs: u0 = h0.w, v0 = h1.w, u1 = h2.w, v1 = h3.x, u2 = h3.y, v2 = h3.z
         const float a00 = h2.w - h0.w, a01 = h3.x - h1.w, a10 = h3.y - h0.w, a11 = h3.z - h1.w;
         const V3 bn0 = vn1 - vn0, bn1 = vn2 - vn0;
@@ -1110,10 +1143,23 @@ __device__ __noinline__ void apply_bump(const Scene_Dev& S, const Material_Dev& 
     const float inv_length = 1 / len(xform_vector(n0, n1, n2, normal));
     dndu = mul(xform_vector(n0, n1, n2, dndu), inv_length);
     dndv = mul(xform_vector(n0, n1, n2, dndv), inv_length);
-    if (sc.flipped) {
+    if (flipped) {
         dndu = -dndu;
         dndv = -dndv;
     }
+    dndu_out = dndu;
+    dndv_out = dndv;
+}
+
+// Shading_Context::apply_bump_map (src/ref/shading_context.cpp:419-462) with the
+// geometry it reads: the normal's uv derivatives and the shading frame's second
+// tangent (:150-167).  Heights at the uv and one footprint step along u and v
+// perturb the tangents; the normal is rebuilt from them, turned into the
+// geometric normal's hemisphere and adjusted.
+__device__ __noinline__ void apply_bump(const Scene_Dev& S, const Material_Dev& m, const Tex_Site& t,
+                                        uint32_t object, uint32_t prim, float b0, float b1, float b2, Shading& sc) {
+    V3 dndu, dndv;
+    normal_derivatives(S, object, prim, b0, b1, b2, t.has_uv, sc.flipped, dndu, dndv);
     // the shading frame's second tangent before the bump
     V3 dpdv_shading;
     if (!t.has_uv) {
@@ -1161,6 +1207,64 @@ __device__ __noinline__ void textured_bsdf_params(const Scene_Dev& S, const Tex_
         const Col r = texture_lookup(S, t, m.texture2, m.texture2_scale, t.uv.x, t.uv.y);
         f.transmittance = m.type == YAR_MATERIAL_DIFFUSE_TRANSMISSION ? clamp_unit(m.extra * r) : r;
     }
+}
+
+// get_glass_info's textured Kr and Kt (src/ref/delta_scattering.cpp:53-97): the
+// attenuation of a smooth-glass delta event of the given kind (0 reflection,
+// else etaI_over_etaT of the transmission).
+__device__ __noinline__ Col textured_glass_attenuation(const Scene_Dev& S, const Tex_Site& t, const Material_Dev& m,
+                                                       float kind, Col atten) {
+    if (kind == 0.f) return m.texture ? texture_lookup(S, t, m.texture, m.texture_scale, t.uv.x, t.uv.y) : atten;
+    if (!m.texture2) return atten;
+    return mul(texture_lookup(S, t, m.texture2, m.texture2_scale, t.uv.x, t.uv.y), kind * kind);
+}
+
+// Shading_Context::compute_differential_rays_for_specular_reflection (kind 0)
+// and _for_specular_transmission (kind = etaI_over_etaT), src/ref/shading_context.cpp:357-403:
+// the differential rays of a delta ray in direction dir from a vertex that
+// has dxdy derivatives (check_for_delta_scattering_event,
+// src/ref/delta_scattering.cpp:283-322), written to Path_State::diff for the
+// ray's arrival.  False when the vertex has none: no incoming differential
+// rays, no uvs, or derivatives dropped as implausible.
+__device__ __noinline__ bool specular_differentials(const Render_Params& p, const Scene_Dev& S, const Path_State& ps,
+                                                    uint32_t slot, int bounce, uint32_t info, const Shading& sc,
+                                                    float4 h4, uint2 h2, V3 dir, float kind) {
+    float2 uv;
+    V3 dpdu, dpdv;
+    if (!texture_geometry(S, h2.y, h2.x, h4.y, h4.z, h4.w, uv, dpdu, dpdv)) return false;
+    V3 ox, dx, oy, dy;
+    if (!incoming_differentials(p, ps, slot, bounce, info, ox, dx, oy, dy)) return false;
+    V3 dpdx, dpdy;
+    float2 duvdx, duvdy;
+    if (!dxdy_derivatives(sc, ox, dx, oy, dy, dpdu, dpdv, dpdx, dpdy, duvdx, duvdy)) return false;
+    V3 dndu, dndv;
+    normal_derivatives(S, h2.y, h2.x, h4.y, h4.z, h4.w, true, sc.flipped, dndu, dndv);
+    const V3 n = sc.n, wo = sc.wo;
+    const V3 dwo_dx = -dx - wo, dwo_dy = -dy - wo;
+    const V3 dndx = mul(dndu, duvdx.x) + mul(dndv, duvdx.y);
+    const V3 dndy = mul(dndu, duvdy.x) + mul(dndv, duvdy.y);
+    const float d_wo_dot_n_dx = dot(dwo_dx, n) + dot(wo, dndx);
+    const float d_wo_dot_n_dy = dot(dwo_dy, n) + dot(wo, dndy);
+    V3 dwi_dx, dwi_dy;
+    if (kind == 0.f) {
+        const float dot_wo_n = dot(wo, n);
+        dwi_dx = mul(mul(n, d_wo_dot_n_dx) + mul(dndx, dot_wo_n), 2.f) - dwo_dx;
+        dwi_dy = mul(mul(n, d_wo_dot_n_dy) + mul(dndy, dot_wo_n), 2.f) - dwo_dy;
+    } else {
+        const float cos_o = dot(wo, n);
+        const float cos_t = -dot(dir, n);
+        const float k1 = kind * kind * cos_o / cos_t;
+        const float k2 = kind * cos_o - cos_t;
+        const float d_cos_t_dx = k1 * d_wo_dot_n_dx, d_cos_t_dy = k1 * d_wo_dot_n_dy;
+        dwi_dx = (mul(dwo_dx, -kind) + mul(dndx, k2)) + mul(n, kind * d_wo_dot_n_dx - d_cos_t_dx);
+        dwi_dy = (mul(dwo_dy, -kind) + mul(dndy, k2)) + mul(n, kind * d_wo_dot_n_dy - d_cos_t_dy);
+    }
+    const V3 o_x = sc.position + dpdx, d_x = normalized(dir + dwi_dx);
+    const V3 o_y = sc.position + dpdy, d_y = normalized(dir + dwi_dy);
+    ps.diff[3 * (size_t)slot] = make_float4(o_x.x, o_x.y, o_x.z, d_x.x);
+    ps.diff[3 * (size_t)slot + 1] = make_float4(d_x.y, d_x.z, o_y.x, o_y.y);
+    ps.diff[3 * (size_t)slot + 2] = make_float4(o_y.z, d_y.x, d_y.y, d_y.z);
+    return true;
 }
 
 // ---------------------------------------------------------------- sphere lights
@@ -1329,7 +1433,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 Tex_Site site;
                 const bool textured = FULL && !GUIDED && (mat.texture | mat.texture2 | mat.bump) != 0u;
                 if (textured) {
-                    texture_site(p, S, ps, slot, bounce, sc, h4, h2, site);
+                    texture_site(p, S, ps, slot, bounce, info, sc, h4, h2, site);
                     if (mat.bump) apply_bump(S, mat, site, h2.y, h2.x, h4.y, h4.z, h4.w, sc);
                 }
                 // Shading_Context::initialize_scattering (shading_context.cpp:174-186): a
@@ -1339,9 +1443,13 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 float bsdf_prob = 1.f;  // 1 - delta_layer_selection_probability
                 V3 delta_wi = v3(0.f, 0.f, 0.f);
                 Col delta_atten = col(1.f, 1.f, 1.f);
+                float delta_kind = 0.f;
                 int delta = 0;
-                if (FULL && mat.delta != kDeltaNone)
-                    delta = delta_scattering(sc, mat, S.materials, u_sc, delta_wi, delta_atten, bsdf_prob);
+                if (FULL && mat.delta != kDeltaNone) {
+                    delta = delta_scattering(sc, mat, S.materials, u_sc, delta_wi, delta_atten, bsdf_prob, delta_kind);
+                    if (textured && delta == 1 && mat.delta == kDeltaGlass && (mat.texture | mat.texture2) != 0u)
+                        delta_atten = textured_glass_attenuation(S, site, mat, delta_kind, delta_atten);
+                }
                 Bsdf f;
                 uint32_t pend = 0;
                 if (delta == 0 || bsdf_prob != 0.f) {
@@ -1605,6 +1713,13 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                     // The delta branch of trace_path (path_tracing.cpp:76-112): the delta
                     // ray is the next extend ray, whose hit adds the light it reaches.
                     // A perfect refractor at total internal reflection ends the path.
+                    // Reflected and transmitted delta rays carry differential rays for
+                    // the first max_differential_ray_specular_bounces bounces.
+                    uint32_t diff_flag = 0u;
+                    if (FULL && !GUIDED && p.spec_diffs && delta == 1 && delta_kind >= 0.f &&
+                        bounce < kMaxDifferentialRaySpecularBounces &&
+                        specular_differentials(p, S, ps, slot, bounce, info, sc, h4, h2, delta_wi, delta_kind))
+                        diff_flag = kDiffRays;
                     bounce++;
                     if (delta == 1) {
                         coeff = coeff * delta_atten;
@@ -1615,7 +1730,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                     }
                     if (GUIDED && g.records) ps.rec[slot] = 0xffffffffu;
                     info = (uint32_t)bounce | ((uint32_t)dm.i1d << 8) | ((uint32_t)dm.i2d << 16) | kDeltaArrival |
-                           (bounce == p.max_bounces ? kDeltaFinal : 0u) | pend;
+                           (bounce == p.max_bounces ? kDeltaFinal : 0u) | pend | diff_flag;
                 } else {
                     bounce++;
                     bool cont = bounce != p.max_bounces;
@@ -2494,10 +2609,10 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
         if (m.type != YAR_MATERIAL_DIFFUSE && m.type != YAR_MATERIAL_METAL &&
             !(m.type == YAR_MATERIAL_GLASS && m.u_roughness > 0.f))
             p.full_shading = 1;
-    // Image textures and bump maps: FULL shading.  The differential rays of
-    // delta bounces are not restated, so image textures (which read them) and
-    // delta materials are not mixed; a constant bump height reads none.  The
-    // direct-lighting algorithm evaluates neither.
+    // Image textures and bump maps: FULL shading.  Image textures read the ray
+    // differentials, which delta bounces carry on in scenes with delta
+    // materials; a constant bump height reads none.  The direct-lighting
+    // algorithm evaluates neither.
     bool delta_materials = false, image_textures = false;
     for (const yar_material_desc& m : R.host_materials) {
         if (m.reflectance_texture || m.transmittance_texture || m.bump == 2) image_textures = true;
@@ -2507,10 +2622,11 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
                           (m.type == YAR_MATERIAL_GLASS && !(m.u_roughness > 0.f)) ||
                           m.type == YAR_MATERIAL_PBRT3_UBER || m.type == YAR_MATERIAL_MIX;
     }
-    if ((image_textures && delta_materials) || (p.textured && c.rendering_algorithm == 0))
-        return fail(ctx, YAR_ERR_UNSUPPORTED,
-                    "image textures with delta materials, or textures or bump maps with the direct-lighting algorithm");
+    if (p.textured && c.rendering_algorithm == 0)
+        return fail(ctx, YAR_ERR_UNSUPPORTED, "textures or bump maps with the direct-lighting algorithm");
     if (p.textured) p.full_shading = 1;
+    // delta rays carry specular differential rays where image textures read them
+    p.spec_diffs = image_textures && delta_materials ? 1 : 0;
     p.seed_offset = (uint32_t)c.rng_seed_offset;
     return YAR_OK;
 }

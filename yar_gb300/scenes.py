@@ -390,6 +390,42 @@ def texture_statements(filename, name="checks", uscale=1.0, vscale=1.0):
             % (name, filename, uscale, vscale),)
 
 
+def specular_texture_pbrt(texture_file, seed=23, width=64, height=64, spp=16, maxdepth=8):
+    """pbrt-v3 text of a Cornell box whose textures are also seen through
+    delta bounces: the floor, back and left walls textured with
+    `texture_file` (uv scale 1 and 2 x 3), the right wall a mirror with uvs
+    and splayed vertex normals, a smooth glass panel with uvs and splayed
+    normals in front of the room, a mirror box and a glass box without uvs."""
+    texs = texture_statements(texture_file) + texture_statements(texture_file, "fine", 2.0, 3.0)
+    mirror_normals = ' "normal N" [-1 -0.12 -0.1 -1 0.1 -0.12 -1 0.12 0.1 -1 -0.1 0.12]'
+    walls = {4: ('Material "mirror" "rgb Kr" [0.9 0.85 0.8]', mirror_normals)}
+    v = [-0.65, 0.05, 0.6, 0.25, 0.05, 0.6, 0.25, 1.45, 0.6, -0.65, 1.45, 0.6]
+    n = [-0.12, -0.1, 1, 0.12, -0.1, 1, 0.12, 0.1, 1, -0.12, 0.1, 1]
+    panel = ("AttributeBegin",
+             '  Material "glass" "float index" [1.5] "rgb Kr" [1 1 1] "rgb Kt" [1 1 1]',
+             '  Shape "trianglemesh" "integer indices" [0 1 2 0 2 3] "point P" [%s] "float uv" [0 0 2 0 2 2 0 2]'
+             ' "normal N" [%s]' % (" ".join("%g" % x for x in v), " ".join("%g" % x for x in n)),
+             "AttributeEnd")
+    return cornell_pbrt(seed=seed, width=width, height=height, spp=spp, maxdepth=maxdepth, box_materials=DELTA_BOXES,
+                        textures=texs, wall_textures={0: "fine", 2: "checks", 3: "fine"}, wall_materials=walls,
+                        extra_shapes=panel)
+
+
+def texture_glass_panel(s):
+    """Gives the flattened scene of specular_texture_pbrt's glass panel (its
+    last object) the back wall's texture as Kr (uv scale 2 x 3) and Kt: the
+    pbrt loader reads constant Kr and Kt only."""
+    mats = s.materials
+    checks = int(mats["reflectance_texture"][s.objects["material_index"][2]])
+    g = int(s.objects["material_index"][-1])
+    assert checks > 0 and int(mats["type"][g]) == 7 and not float(mats["u_roughness"][g]) > 0  # smooth glass
+    mats["reflectance_texture"][g] = checks
+    mats["reflectance_uv_scale"][g] = (2.0, 3.0)
+    mats["transmittance_texture"][g] = checks
+    mats["transmittance_uv_scale"][g] = (1.0, 1.0)
+    return s
+
+
 def environment_statements(mapname, scale=(1, 1, 1), samples=1):
     """pbrt statements of an infinite light with the given map, turned so that
     the map's pole points along +y."""
