@@ -140,8 +140,11 @@ typedef struct yar_object_desc {
  * Plastic/Coated_Diffuse/Glass_Material, src/lib/material.h:48-150).  Glass with
  * roughness 0 scatters as the reference's smooth (delta) glass; plastic in a scene
  * with pbrt3_scene set is shaded as pbrt-v3's plastic, as the reference does.
- * Textured parameters and bump maps are outside the implemented path
- * (YAR_ERR_UNSUPPORTED). */
+ * Image textures on the reflectance and transmittance slots and bump maps are
+ * evaluated by the path tracer (yar_gpu_render, yar_gpu_render_checkpoint and
+ * yar_gpu_render_batch), behind delta bounces too; the direct-lighting
+ * algorithm, the guided and the static renders, and textures on any other
+ * parameter, return YAR_ERR_UNSUPPORTED. */
 typedef struct yar_material_desc {
     uint32_t type;              /* YAR_MATERIAL_PERFECT_REFLECTOR / PERFECT_REFRACTOR / DIFFUSE / METAL /
                                    PLASTIC / COATED_DIFFUSE / GLASS */

@@ -2574,9 +2574,10 @@ typedef struct direct_arrays {
     const size_t* offset[2];  /* per light, its first element in the arrays above */
 } direct_arrays;
 
-/* estimate_direct_lighting, src/ref/direct_lighting.cpp:415-520 */
-static int trace_direct(const yar_flat_scene* s, const env_sampler* env, v3 ro, v3 rd, const direct_arrays* da,
-                        oracle_pcg32* rng, col* radiance) {
+/* estimate_direct_lighting, src/ref/direct_lighting.cpp:415-520 (the delta ray's
+ * hit adds its emission only, so only the camera hit reads derivatives) */
+static int trace_direct(const yar_flat_scene* s, const env_sampler* env, v3 ro, v3 rd, const v3 differential_dirs[2],
+                        const direct_arrays* da, oracle_pcg32* rng, col* radiance) {
     hit_state h;
     int hit = trace_closest(s, ro, rd, &h);
     if (hit < 0) return YAR_ERR_CAPACITY;
@@ -2586,6 +2587,7 @@ static int trace_direct(const yar_flat_scene* s, const env_sampler* env, v3 ro, 
     }
     shading_ctx sc;
     init_shading(s, rd, h.object, h.prim, h.b, &sc);
+    uv_derivatives(&sc, ro, differential_dirs[0], ro, differential_dirs[1]);
     float u_scatter = oracle_pcg32_float(rng); /* past the (empty) 1D budget */
     col L = mkc(0, 0, 0), le;
     v3 ddir;
@@ -2800,6 +2802,16 @@ static int render_tile(render_job* J, int t) {
                 camera_ray(&s->camera, fx, fy, &o, &d);
                 sampler_view sv = {s1d + (size_t)k * n1d, s2d + 2 * (size_t)k * n2d, n1d, n2d, 0, 0, &rng};
                 col radiance;
+                /* differential rays one pixel over, scaled to the sample's footprint
+                 * (src/ref/reference_renderer.cpp:367-378) */
+                v3 dd[2], ox;
+                camera_ray(&s->camera, fx + 1.f, fy, &ox, &dd[0]);
+                camera_ray(&s->camera, fx, fy + 1.f, &ox, &dd[1]);
+                const float dscale = 1.f / sqrtf((float)spp);
+                for (int q = 0; q < 2; q++) {
+                    dd[q] = add3(d, mul3s(sub3(dd[q], d), dscale));
+                    dd[q] = div3s(dd[q], len3(dd[q]));
+                }
                 if (direct) {
                     direct_arrays da;
                     for (int kind = 0; kind < 2; kind++) {
@@ -2809,18 +2821,8 @@ static int render_tile(render_job* J, int t) {
                         da.k[kind] = dk[kind];
                         da.offset[kind] = doff[kind];
                     }
-                    rc = trace_direct(s, &J->env, o, d, &da, &rng, &radiance);
+                    rc = trace_direct(s, &J->env, o, d, dd, &da, &rng, &radiance);
                 } else {
-                    /* differential rays one pixel over, scaled to the sample's footprint
-                     * (src/ref/reference_renderer.cpp:367-378) */
-                    v3 dd[2], ox;
-                    camera_ray(&s->camera, fx + 1.f, fy, &ox, &dd[0]);
-                    camera_ray(&s->camera, fx, fy + 1.f, &ox, &dd[1]);
-                    const float dscale = 1.f / sqrtf((float)spp);
-                    for (int q = 0; q < 2; q++) {
-                        dd[q] = add3(d, mul3s(sub3(dd[q], d), dscale));
-                        dd[q] = div3s(dd[q], len3(dd[q]));
-                    }
                     rc = trace_path(s, J->mesh_samplers, &J->env, o, d, dd, &sv, &radiance);
                 }
                 if (rc != YAR_OK) break;
@@ -2930,10 +2932,8 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
     /* image textures: the reflectance of diffuse, plastic, coated diffuse, glass
      * and diffuse transmission, the transmittance of glass and diffuse
      * transmission, and bump maps, with camera-ray differentials and the
-     * specular differential rays of delta bounces in the path tracer; not with
-     * the direct-lighting algorithm.  A constant bump height needs no
-     * differentials. */
-    int textured = 0;
+     * specular differential rays of delta bounces.  A constant bump height
+     * needs no differentials. */
     for (uint32_t i = 0; i < s->material_count; i++) {
         const yar_material_desc* m = &s->materials[i];
         if (m->other_textured_parameters) return YAR_ERR_UNSUPPORTED;
@@ -2950,11 +2950,9 @@ int oracle_render(const yar_flat_scene* s, float* rgb, double* variance, int32_t
             if (used[k] > s->texture_count) return YAR_ERR_INVALID;
             const yar_texture_desc* t = &s->textures[used[k] - 1];
             if (t->mip_count == 0 || t->first_mip + t->mip_count > s->texture_mip_count) return YAR_ERR_INVALID;
-            textured = 1;
         }
         if (m->bump == 2 && !used[2]) return YAR_ERR_INVALID;
     }
-    if (textured && cfg->rendering_algorithm == 0) return YAR_ERR_UNSUPPORTED;
     init_ewa_weights();
     for (uint32_t i = 0; i < s->material_count; i++) {
         const yar_material_desc* m = &s->materials[i];

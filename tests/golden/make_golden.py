@@ -87,6 +87,11 @@ Fixtures
                              mirror use the specular differential rays;
                              rendered by the reference from the edited flat
                              scene, seed 23.
+  cornell_direct_tex_64.yfs / .npz  the cornell_spectex_64 scene with an image
+                             bump map on the back wall, rendered by the
+                             direct-lighting algorithm (2 quad-light samples;
+                             textures and the bump read the camera-ray
+                             differentials), seed 31.
   cornell_fourier_64.yfs / .npz  pbrt "fourier" boxes: a one-channel and a
                              three-channel layerlab table written by
                              write_fourier_bsdf (15 zenith nodes, glossy lobes
@@ -487,6 +492,23 @@ def cornell_spectex_64():
     np.savez_compressed(os.path.join(HERE, "cornell_spectex_64.npz"), image=img, variance=np.float64(info["variance"]))
 
 
+def cornell_direct_tex_64():
+    from yar_gb300 import exr
+    with tempfile.TemporaryDirectory() as d:
+        exr.write_exr(os.path.join(d, "checks.exr"), scenes.texture_image(), False, {})
+        exr.write_exr(os.path.join(d, "bumps.exr"), scenes.bump_image(), False, {})
+        pbrt = os.path.join(d, "cornell_direct_tex.pbrt")
+        open(pbrt, "w").write(scenes.specular_texture_pbrt("checks.exr", seed=31, bump_file="bumps.exr",
+                                                           integrator="directlighting", light_samples=2))
+        yfs = os.path.join(d, "cornell_direct_tex.yfs")
+        oracle.ref_flatten(pbrt, yfs, seed_offset=1)
+        s = scenes.texture_glass_panel(FlatScene.read(yfs))
+        assert int(s.config["rendering_algorithm"]) == 0
+        s.write(os.path.join(HERE, "cornell_direct_tex_64.yfs"))
+        img, info = oracle.ref_render_flat(s, threads=8, textures_from=pbrt)
+    np.savez_compressed(os.path.join(HERE, "cornell_direct_tex_64.npz"), image=img, variance=np.float64(info["variance"]))
+
+
 def write_fourier_bsdf(path, channels, nodes=15, order=8, gloss=6.0, albedo=(0.7, 0.5, 0.3)):
     """A layerlab "SCATFUN" v1 file (the subset Pbrt3_Fourier_Material::load_bsdf_file
     reads, src/lib/material_pbrt.cpp:24-102): increasing zenith cosines from -1
@@ -636,7 +658,7 @@ if __name__ == "__main__":
                              "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64",
                              "cornell_direct_64", "cornell_direct_env_64", "cornell_texture_64", "checkpoint_c1",
                              "cornell_gaussian_64", "cornell_triangle_64", "cornell_c1_256", "cornell_alpha_64",
-                             "cornell_bump_64", "cornell_fourier_64", "cornell_spectex_64",
+                             "cornell_bump_64", "cornell_fourier_64", "cornell_spectex_64", "cornell_direct_tex_64",
                              "exr_files",
                              "kdtree_cache_files"]
     for name in which:

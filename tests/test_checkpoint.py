@@ -119,6 +119,22 @@ def test_gpu_checkpoint_from_scratch_equals_the_plain_render(tmp_path):
 
 
 @pytest.mark.gpu
+def test_gpu_checkpoint_of_a_textured_scene_equals_the_plain_render(tmp_path, gpu_ctx):
+    """Tiles rendered row by row as their own sample regions keep the camera
+    differentials and the specular differential rays of textured scenes: the
+    merged image is the plain render's, bit for bit."""
+    from yar_gb300.scene import FlatScene
+    s = FlatScene.read(golden("cornell_spectex_64.yfs"))
+    s.config["render_region"] = (0, 0, 130, 72)
+    s.camera["image_extent"] = (130, 72)
+    gpu_ctx.upload_scene(s)
+    plain, pst = gpu_ctx.render(130, 72)
+    img, st = gpu_ctx.render_checkpoint(130, 72, tmp_path / "tex", "spectex.pbrt")
+    assert np.array_equal(img.view(np.uint32), plain.view(np.uint32))
+    assert st.variance == pst.variance
+
+
+@pytest.mark.gpu
 def test_gpu_checkpoint_refuses_another_project(tmp_path):
     from yar_gb300 import native
     d = tmp_path / "ckpt"

@@ -127,7 +127,7 @@ def test_builder_against_live_reference_large_mesh():
                                   "cornell_mix_64", "cornell_envconst_64", "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64",
                                   "cornell_texture_64", "cornell_gaussian_64", "cornell_triangle_64",
                                   "cornell_alpha_64", "cornell_bump_64", "cornell_fourier_64",
-                                  "cornell_spectex_64"])
+                                  "cornell_spectex_64", "cornell_direct_tex_64"])
 def test_oracle_render_matches_reference_golden(name):
     """The oracle's path loop, sampler, shading, BSDFs (diffuse, GGX metal, rough
     glass, plastic in both of the reference's forms, coated diffuse), delta
@@ -217,15 +217,12 @@ def test_alpha_texture_file_round_trip(tmp_path):
 
 def test_textured_scenes_outside_the_restated_part_are_refused():
     """Image textures are restated for the reflectance and transmittance slots
-    and bump maps in the path tracer with camera-ray and specular
-    differentials; with the direct-lighting algorithm, on other parameters, in
-    a slot the material does not read, or as the bump map of a mix's
-    sub-material the oracle refuses the scene."""
-    for change in ("direct", "other", "slot", "mix_bump"):
+    and bump maps, with camera-ray and specular differentials; on other
+    parameters, in a slot the material does not read, or as the bump map of a
+    mix's sub-material the oracle refuses the scene."""
+    for change in ("other", "slot", "mix_bump"):
         s = FlatScene.read(golden("cornell_texture_64.yfs"))
-        if change == "direct":
-            s.config["rendering_algorithm"] = 0
-        elif change == "other":
+        if change == "other":
             s.materials["other_textured_parameters"][-1] = 1
         elif change == "slot":
             k = int(np.nonzero(s.materials["reflectance_texture"])[0][0])

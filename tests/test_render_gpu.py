@@ -71,7 +71,7 @@ def compare(img, ref):
                   "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64",
                                   "cornell_texture_64", "cornell_gaussian_64", "cornell_triangle_64",
                                   "cornell_alpha_64", "cornell_bump_64", "cornell_fourier_64",
-                                  "cornell_spectex_64"])
+                                  "cornell_spectex_64", "cornell_direct_tex_64"])
 def test_render_matches_reference_golden(gpu_ctx, name):
     s = FlatScene.read(golden(name + ".yfs"))
     g = np.load(golden(name + ".npz"))
@@ -97,7 +97,7 @@ RENDER_GOLDENS = ["cornell_c1_64", "cornell_ggx_64", "cornell_delta_64", "cornel
                   "cornell_translucent_64", "cornell_transmission_64", "cornell_uber_64", "cornell_mix_64", "cornell_envconst_64",
                   "cornell_envmap_64", "cornell_direct_64", "cornell_direct_env_64", "cornell_texture_64",
                   "cornell_gaussian_64", "cornell_triangle_64", "cornell_alpha_64", "cornell_bump_64",
-                  "cornell_fourier_64", "cornell_spectex_64"]
+                  "cornell_fourier_64", "cornell_spectex_64", "cornell_direct_tex_64"]
 
 
 @pytest.mark.parametrize("name", RENDER_GOLDENS)
@@ -434,19 +434,13 @@ def test_fourier_tables_checked_on_upload(gpu_ctx):
 
 
 def test_bump_maps_refused_where_they_are_not_evaluated(gpu_ctx):
-    """The guided render and the direct-lighting algorithm refuse bump maps; a
-    mix's sub-material may not have one; a texture in a slot the material does
-    not read is refused."""
+    """The guided render refuses bump maps; a mix's sub-material may not have
+    one; a texture in a slot the material does not read is refused."""
     from yar_gb300 import native
     s = constant_bumps_with_delta_materials()
     gpu_ctx.upload_scene(s)
     with pytest.raises(native.YarError):
         gpu_ctx.guided_render(64, 64, passes=1)
-    d = constant_bumps_with_delta_materials()
-    d.config["rendering_algorithm"] = 0
-    gpu_ctx.upload_scene(d)
-    with pytest.raises(native.YarError):
-        gpu_ctx.render(64, 64)
     t = FlatScene.read(golden("cornell_texture_64.yfs"))
     k = int(np.nonzero(t.materials["reflectance_texture"])[0][0])
     t.materials["transmittance_texture"][k] = t.materials["reflectance_texture"][k]  # diffuse has no such slot
@@ -462,19 +456,27 @@ def test_bump_maps_refused_where_they_are_not_evaluated(gpu_ctx):
 
 
 def test_textured_scene_refused_where_textures_are_not_evaluated(gpu_ctx):
-    """The direct-lighting algorithm and the guided render refuse image
-    textures instead of rendering them as constants."""
+    """The guided render refuses image textures instead of rendering them as
+    constants."""
     from yar_gb300 import native
     s = FlatScene.read(golden("cornell_spectex_64.yfs"))
     gpu_ctx.upload_scene(s)
     with pytest.raises(native.YarError) as e:
         gpu_ctx.guided_render(64, 64, passes=1)
     assert e.value.code == native.YAR_ERR_UNSUPPORTED
+
+
+def test_direct_lighting_with_constant_bumps_on_delta_materials(gpu_ctx):
+    """The direct-lighting algorithm with constant bump heights on a mirror,
+    smooth glass and a floor with splayed normals: bit for bit the oracle's
+    image with correctly rounded trigonometry."""
+    s = constant_bumps_with_delta_materials()
     s.config["rendering_algorithm"] = 0
     gpu_ctx.upload_scene(s)
-    with pytest.raises(native.YarError) as e:
-        gpu_ctx.render(64, 64)
-    assert e.value.code == native.YAR_ERR_UNSUPPORTED
+    img, st = gpu_ctx.render(64, 64)
+    ref, ref_var = oracle.render(s, threads=8, correctly_rounded_trig=True)
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    assert st.variance == ref_var
 
 
 def test_specular_differentials_reach_textures_behind_delta_bounces(gpu_ctx):

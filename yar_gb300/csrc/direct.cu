@@ -282,12 +282,16 @@ __global__ void direct_prefix_kernel(uint32_t pixels, int spp, uint32_t* draws) 
 }
 
 // Pass 3: estimate_direct_lighting of every sample.
+// TEXTURED: image textures or bump maps in the scene (a separate
+// instantiation: their calls take the plain kernel from 228 registers without
+// spills to 168 with 768 B of spill stores).
+template <bool TEXTURED>
 __global__ void __launch_bounds__(kBlock)
 direct_shade_kernel(Render_Params p, Scene_Dev S, uint32_t chunk_first, uint32_t paths, const Queues q, float4* rec,
                     const float4* __restrict__ hit4, const uint2* __restrict__ hit2,
                     const uint32_t* __restrict__ draw_offset, uint32_t stream_base, const float* __restrict__ s1d,
                     const float2* __restrict__ s2d, const int* __restrict__ array_sides, int env_samples,
-                    float4* __restrict__ radiance, int* err) {
+                    const float2* __restrict__ image_samples, float4* __restrict__ radiance, int* err) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= paths) return;
     const uint32_t lp = i / (uint32_t)p.spp, sample = i - lp * (uint32_t)p.spp;
@@ -312,14 +316,29 @@ direct_shade_kernel(Render_Params p, Scene_Dev S, uint32_t chunk_first, uint32_t
         int delta = 0;
         const bool is_light = (uint32_t)oinfo.z != YAR_LIGHT_NULL;
         const Material_Dev* mat = (uint32_t)oinfo.x != YAR_MATERIAL_NULL ? &S.materials[oinfo.y] : nullptr;
-        float delta_kind;
-        if (mat && mat->delta != kDeltaNone)
+        // Image textures and bump maps at the camera hit, with the camera ray's
+        // differentials (the delta ray's hit adds its emission only)
+        Tex_Site site;
+        const bool textured = TEXTURED && mat && !is_light && (mat->texture | mat->texture2 | mat->bump) != 0u;
+        if (textured) {
+            Path_State ps{};
+            ps.image_samples = image_samples;
+            ps.chunk_first = chunk_first;
+            texture_site(p, S, ps, i, 0, 0u, sc, h4, h2, site);
+            if (mat->bump) apply_bump(S, *mat, site, h2.y, h2.x, h4.y, h4.z, h4.w, sc);
+        }
+        float delta_kind = 0.f;
+        if (mat && mat->delta != kDeltaNone) {
             delta = delta_scattering(sc, *mat, S.materials, u_sc, delta_wi, delta_atten, bsdf_prob, delta_kind);
+            if (textured && delta == 1 && mat->delta == kDeltaGlass && (mat->texture | mat->texture2) != 0u)
+                delta_atten = textured_glass_attenuation(S, site, *mat, delta_kind, delta_atten);
+        }
         if (is_light) {
             L = emitted(S, oinfo, sc.flipped);
         } else if (mat && (delta == 0 || bsdf_prob != 0.f)) {
             Bsdf f;
             make_bsdf(sc, *mat, S.materials, f);
+            if (textured && (mat->texture | mat->texture2) != 0u) textured_bsdf_params(S, site, *mat, f);
             for (int l = 0; l < p.delta_lights; l++)  // point lights, then directional lights
                 if (__float_as_uint(__ldg(&S.delta_lights[l].a).w) == YAR_LIGHT_POINT)
                     L = L + direct_point_or_directional(S, sc, f, l, rec, i, err);
@@ -461,10 +480,11 @@ int render_direct(yar_gpu_ctx* ctx, float* rgb_out, yar_render_stats* stats) {
             p, S, paths, q, dptr<float4>(B[10]), dptr<float4>(B[11]), dptr<uint2>(B[12]), dptr<uint32_t>(B[13]),
             env_samples, err);
         direct_prefix_kernel<<<(cp + kBlock - 1) / kBlock, kBlock, 0, st>>>(cp, p.spp, dptr<uint32_t>(B[13]));
-        direct_shade_kernel<<<(paths + kBlock - 1) / kBlock, kBlock, 0, st>>>(
+        (p.textured ? direct_shade_kernel<true> : direct_shade_kernel<false>)<<<(paths + kBlock - 1) / kBlock,
+                                                                              kBlock, 0, st>>>(
             p, S, (uint32_t)first, paths, q, dptr<float4>(B[10]), dptr<float4>(B[11]), dptr<uint2>(B[12]),
             dptr<uint32_t>(B[13]), (uint32_t)base, dptr<float>(B[2]), dptr<float2>(B[3]), dptr<int>(B[18]),
-            env_samples, dptr<float4>(B[0]), err);
+            env_samples, dptr<float2>(B[1]), dptr<float4>(B[0]), err);
         launches += 5;
         e = cudaGetLastError();
     }

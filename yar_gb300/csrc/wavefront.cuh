@@ -2610,9 +2610,10 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
             !(m.type == YAR_MATERIAL_GLASS && m.u_roughness > 0.f))
             p.full_shading = 1;
     // Image textures and bump maps: FULL shading.  Image textures read the ray
-    // differentials, which delta bounces carry on in scenes with delta
-    // materials; a constant bump height reads none.  The direct-lighting
-    // algorithm evaluates neither.
+    // differentials, which the path tracer's delta bounces carry on in scenes
+    // with delta materials; a constant bump height reads none.  The
+    // direct-lighting algorithm reads them at the camera hit only (its delta
+    // ray's hit adds emission).
     bool delta_materials = false, image_textures = false;
     for (const yar_material_desc& m : R.host_materials) {
         if (m.reflectance_texture || m.transmittance_texture || m.bump == 2) image_textures = true;
@@ -2622,11 +2623,9 @@ int prepare_render_params(yar_gpu_ctx* ctx, Render_Params& p) {
                           (m.type == YAR_MATERIAL_GLASS && !(m.u_roughness > 0.f)) ||
                           m.type == YAR_MATERIAL_PBRT3_UBER || m.type == YAR_MATERIAL_MIX;
     }
-    if (p.textured && c.rendering_algorithm == 0)
-        return fail(ctx, YAR_ERR_UNSUPPORTED, "textures or bump maps with the direct-lighting algorithm");
     if (p.textured) p.full_shading = 1;
-    // delta rays carry specular differential rays where image textures read them
-    p.spec_diffs = image_textures && delta_materials ? 1 : 0;
+    // the path tracer's delta rays carry specular differential rays where image textures read them
+    p.spec_diffs = image_textures && delta_materials && c.rendering_algorithm != 0 ? 1 : 0;
     p.seed_offset = (uint32_t)c.rng_seed_offset;
     return YAR_OK;
 }

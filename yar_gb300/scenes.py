@@ -390,15 +390,22 @@ def texture_statements(filename, name="checks", uscale=1.0, vscale=1.0):
             % (name, filename, uscale, vscale),)
 
 
-def specular_texture_pbrt(texture_file, seed=23, width=64, height=64, spp=16, maxdepth=8):
+def specular_texture_pbrt(texture_file, seed=23, width=64, height=64, spp=16, maxdepth=8, bump_file=None, **kw):
     """pbrt-v3 text of a Cornell box whose textures are also seen through
     delta bounces: the floor, back and left walls textured with
     `texture_file` (uv scale 1 and 2 x 3), the right wall a mirror with uvs
     and splayed vertex normals, a smooth glass panel with uvs and splayed
-    normals in front of the room, a mirror box and a glass box without uvs."""
+    normals in front of the room, a mirror box and a glass box without uvs.
+    bump_file: an image bump map on the back wall too; kw: more cornell_pbrt
+    arguments (the integrator)."""
     texs = texture_statements(texture_file) + texture_statements(texture_file, "fine", 2.0, 3.0)
     mirror_normals = ' "normal N" [-1 -0.12 -0.1 -1 0.1 -0.12 -1 0.12 0.1 -1 -0.1 0.12]'
     walls = {4: ('Material "mirror" "rgb Kr" [0.9 0.85 0.8]', mirror_normals)}
+    wall_textures = {0: "fine", 2: "checks", 3: "fine"}
+    if bump_file:
+        texs += ('Texture "bumps" "float" "imagemap" "string filename" "%s"' % bump_file,)
+        walls[2] = ('Material "matte" "texture Kd" "checks" "texture bumpmap" "bumps"', "")
+        del wall_textures[2]
     v = [-0.65, 0.05, 0.6, 0.25, 0.05, 0.6, 0.25, 1.45, 0.6, -0.65, 1.45, 0.6]
     n = [-0.12, -0.1, 1, 0.12, -0.1, 1, 0.12, 0.1, 1, -0.12, 0.1, 1]
     panel = ("AttributeBegin",
@@ -407,8 +414,7 @@ def specular_texture_pbrt(texture_file, seed=23, width=64, height=64, spp=16, ma
              ' "normal N" [%s]' % (" ".join("%g" % x for x in v), " ".join("%g" % x for x in n)),
              "AttributeEnd")
     return cornell_pbrt(seed=seed, width=width, height=height, spp=spp, maxdepth=maxdepth, box_materials=DELTA_BOXES,
-                        textures=texs, wall_textures={0: "fine", 2: "checks", 3: "fine"}, wall_materials=walls,
-                        extra_shapes=panel)
+                        textures=texs, wall_textures=wall_textures, wall_materials=walls, extra_shapes=panel, **kw)
 
 
 def texture_glass_panel(s):
