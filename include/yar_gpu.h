@@ -141,10 +141,10 @@ typedef struct yar_object_desc {
  * roughness 0 scatters as the reference's smooth (delta) glass; plastic in a scene
  * with pbrt3_scene set is shaded as pbrt-v3's plastic, as the reference does.
  * Image textures on the reflectance and transmittance slots and bump maps are
- * evaluated by the path tracer (yar_gpu_render, yar_gpu_render_checkpoint and
- * yar_gpu_render_batch), behind delta bounces too; the direct-lighting
- * algorithm, the guided and the static renders, and textures on any other
- * parameter, return YAR_ERR_UNSUPPORTED. */
+ * evaluated by yar_gpu_render (both rendering algorithms),
+ * yar_gpu_render_checkpoint and yar_gpu_render_batch, behind delta bounces
+ * too; the guided and static renders, and textures on any other parameter,
+ * return YAR_ERR_UNSUPPORTED. */
 typedef struct yar_material_desc {
     uint32_t type;              /* YAR_MATERIAL_PERFECT_REFLECTOR / PERFECT_REFRACTOR / DIFFUSE / METAL /
                                    PLASTIC / COATED_DIFFUSE / GLASS */
