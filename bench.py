@@ -596,7 +596,20 @@ def render_bench(kind, with_cpu=True, reps=3):
 GUIDE = dict(guide_fraction=0.7, train_passes=32, train_steps=32, learning_rate=5e-3)  # one-sample passes
 # stratified form: settings from a sweep on the room (guide fraction 0.5-0.8, guided bounces 1-3 or all,
 # 4-16 training passes, 32-128 Adam steps, learning rate 3e-3-1e-2)
-GUIDE_STRATIFIED = dict(guide_fraction=0.6, train_passes=8, train_steps=64, learning_rate=5e-3, guide_bounces=2)
+GUIDE_STRATIFIED = dict(guide_fraction=0.6, train_passes=4, train_steps=64, learning_rate=5e-3, guide_bounces=2)
+
+
+def strata_grids(k):
+    """(columns, rows) grids between (k - 1)^2 and k^2 samples (exclusive),
+    columns >= rows, aspect at most 4:3, the squarest of each sample count,
+    by increasing count; then k x k."""
+    best = {}
+    for nx in range(k - 4, k + 5):
+        for ny in range(max(1, k - 5), nx + 1):
+            n = nx * ny
+            if (k - 1) ** 2 < n < k * k and 3 * nx <= 4 * ny and (n not in best or nx - ny < best[n][0] - best[n][1]):
+                best[n] = (nx, ny)
+    return [best[n] for n in sorted(best)] + [(k, k)]
 
 
 def guided_bench(plain_spp_side=32, offsets=(2, 3, 4), with_cpu=True):
@@ -608,11 +621,12 @@ def guided_bench(plain_spp_side=32, offsets=(2, 3, 4), with_cpu=True):
       - plain passes: yar_gpu_guided_render at guide fraction 0, 1024 one-sample
         passes;
       - guided (stratified form of yar_gpu_guided_render: the training passes,
-        then the pixel sampler at k x k samples per pixel with continuations
+        then the pixel sampler at nx x ny samples per pixel with continuations
         from the trained proposal): for each stream offset, k is raised until
-        the RMSE is at or below the better plain form's, then the k x (k - 1)
-        grid is tried; the wall time of the smallest grid that reaches it
-        (training included) is the measured time to that RMSE.
+        the k x k render's RMSE is at or below the better plain form's; then
+        every near-square grid between (k - 1)^2 and k^2 samples is rendered,
+        and the wall time (training included) of the smallest grid from which
+        on every larger grid reaches that RMSE is the measured time to it.
     oracle_vs_reference: the oracle's 64 x 64 tile means against the reference
     CPU renderer's at 16 spp (z-scores from the noise of two reference renders
     with different seed offsets)."""
@@ -658,15 +672,22 @@ def guided_bench(plain_spp_side=32, offsets=(2, 3, 4), with_cpu=True):
             if r_g <= target:
                 break
             side += 1
-        spp = side * side
-        if r_g <= target and side > 1:  # the rectangular grid one row short, if it reaches too
-            img_2, _, st_2 = ctx.guided_render(w, h, samples_per_pixel=side * (side - 1), stream_offset=off,
-                                               **GUIDE_STRATIFIED)
-            r_2 = rmse(img_2)
-            if r_2 <= target:
-                img_g, st_g, r_g, spp = img_2, st_2, r_2, side * (side - 1)
-        runs.append({"stream_offset": off, "spp": spp, "seconds": round(st_g.seconds, 3), "rmse": r_g,
-                     "reached": bool(r_g <= target), "train_passes": int(st_g.passes),
+        spp, grid = side * side, (side, side)
+        if r_g <= target and side > 2:
+            # the grids below k x k: the smallest from which on all reach the target
+            tried = []
+            for nx, ny in strata_grids(side)[:-1]:
+                img_2, _, st_2 = ctx.guided_render(w, h, samples_per_pixel=nx * ny, strata_x=nx, stream_offset=off,
+                                                   **GUIDE_STRATIFIED)
+                tried.append(((nx, ny), st_2, rmse(img_2)))
+            tried.append(((side, side), st_g, r_g))
+            i = len(tried) - 1
+            while i > 0 and tried[i - 1][2] <= target:
+                i -= 1
+            grid, st_g, r_g = tried[i]
+            spp = grid[0] * grid[1]
+        runs.append({"stream_offset": off, "spp": spp, "strata": list(grid), "seconds": round(st_g.seconds, 3),
+                     "rmse": r_g, "reached": bool(r_g <= target), "train_passes": int(st_g.passes),
                      "train_seconds": round(st_g.train_seconds, 3)})
     ctx.close()
     times = [r["seconds"] for r in runs if r["reached"]]

@@ -538,6 +538,9 @@ typedef struct yar_guided_params {
      * guide_bounces vertices of each path (0: every vertex); deeper vertices
      * sample the BSDF alone */
     uint32_t guide_bounces;
+    /* stratified form: > 0 sets the strata columns nx (ny = ceil(n / nx))
+     * instead of ceil(sqrt(n)); at most 4 x ny and at least ny / 4 */
+    uint32_t strata_x;
 } yar_guided_params;
 
 typedef struct yar_guided_stats {

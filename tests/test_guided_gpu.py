@@ -94,3 +94,19 @@ def test_stratified_guided_is_unbiased(gpu_ctx, small_room):
     assert np.array_equal(sums0, unguided.astype(np.float64).reshape(sums0.shape) * 210.0)
     assert not np.array_equal(unguided, plain)
     assert abs(unguided.mean() - plain.mean()) < 0.01 * plain.mean(), (unguided.mean(), plain.mean())
+
+
+def test_stratified_form_takes_the_strata_columns(gpu_ctx):
+    """strata_x sets the columns of the pixel sampler's grid (rows ceil(n /
+    nx)): 16 x 12 strata hold 192 samples per pixel; grids beyond 4:1 are
+    refused."""
+    from yar_gb300 import native
+    c = FlatScene.read(golden("cornell_c1_64.yfs"))
+    c.config["x_pixel_sample_count"] = c.config["y_pixel_sample_count"] = 14
+    gpu_ctx.upload_scene(c)
+    img, sums, st = gpu_ctx.guided_render(64, 64, samples_per_pixel=190, strata_x=16, stream_offset=5)
+    assert np.array_equal(sums, img.astype(np.float64).reshape(sums.shape) * 192.0)
+    plain, _ = gpu_ctx.render(64, 64)
+    assert abs(img.mean() - plain.mean()) < 0.01 * plain.mean(), (img.mean(), plain.mean())
+    with pytest.raises(native.YarError):
+        gpu_ctx.guided_render(64, 64, samples_per_pixel=200, strata_x=100, stream_offset=5)

@@ -146,10 +146,16 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
     if (!gp || (gp->passes == 0 && gp->samples_per_pixel == 0))
         return fail(ctx, YAR_ERR_INVALID, "guided render: no passes");
     // stratified: the training passes, then one render with the pixel sampler
-    // stratified: nx x ny strata, nx = ceil(sqrt(n)), ny = ceil(n / nx)
-    const int spp_side = gp->samples_per_pixel ? (int)std::ceil(std::sqrt((double)gp->samples_per_pixel)) : 0;
+    // at nx x ny strata, nx = strata_x or ceil(sqrt(n)), ny = ceil(n / nx)
+    int spp_side = gp->samples_per_pixel ? (int)std::ceil(std::sqrt((double)gp->samples_per_pixel)) : 0;
+    if (spp_side && gp->strata_x) {
+        if (gp->strata_x > gp->samples_per_pixel) return fail(ctx, YAR_ERR_INVALID, "guided render: strata_x > spp");
+        spp_side = (int)gp->strata_x;
+    }
     if (spp_side > 256) return fail(ctx, YAR_ERR_INVALID, "guided render: at most 65536 samples per pixel");
     const int spp_rows = spp_side ? (int)((gp->samples_per_pixel + (uint32_t)spp_side - 1) / (uint32_t)spp_side) : 0;
+    if (spp_rows > 256 || spp_side > 4 * spp_rows || 4 * spp_side < spp_rows)
+        return fail(ctx, YAR_ERR_INVALID, "guided render: strata columns and rows at most 256 and 4:1");
     const uint32_t pass_count = spp_side ? (gp->guide_fraction > 0.f ? gp->train_passes : 0u) : gp->passes;
     if (!(gp->guide_fraction >= 0.f && gp->guide_fraction < 1.f))
         return fail(ctx, YAR_ERR_INVALID, "guide fraction must be in [0, 1)");

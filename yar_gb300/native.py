@@ -175,7 +175,7 @@ class GuidedParams(C.Structure):
     _fields_ = [("passes", C.c_uint32), ("train_passes", C.c_uint32), ("guide_fraction", C.c_float),
                 ("learning_rate", C.c_float), ("train_steps", C.c_uint32), ("stream_offset", C.c_uint32),
                 ("time_budget", C.c_float), ("keep_guide", C.c_uint32), ("samples_per_pixel", C.c_uint32),
-                ("guide_bounces", C.c_uint32)]
+                ("guide_bounces", C.c_uint32), ("strata_x", C.c_uint32)]
 
 
 class GuidedStats(C.Structure):
@@ -449,13 +449,14 @@ class Context:
 
     def guided_render(self, width, height, passes=0, guide_fraction=0.0, train_passes=0, learning_rate=2e-3,
                       train_steps=8, stream_offset=0, time_budget=0.0, keep_guide=False, samples_per_pixel=0,
-                      guide_bounces=0):
+                      guide_bounces=0, strata_x=0):
         """yar_gpu_guided_render: returns (mean image, per-pixel FP64 radiance
         sums, GuidedStats).  samples_per_pixel > 0: the stratified form (the
-        training passes, then the pixel sampler at that many samples)."""
+        training passes, then the pixel sampler at that many samples, in
+        strata_x columns of strata when given)."""
         prm = GuidedParams(int(passes), int(train_passes), float(guide_fraction), float(learning_rate),
                            int(train_steps), int(stream_offset), float(time_budget), int(bool(keep_guide)),
-                           int(samples_per_pixel), int(guide_bounces))
+                           int(samples_per_pixel), int(guide_bounces), int(strata_x))
         sums = np.zeros((height, width, 3), np.float64)
         rgb = np.zeros((height, width, 3), np.float32)
         st = GuidedStats()
