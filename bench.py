@@ -624,9 +624,10 @@ def guided_bench(plain_spp_side=32, offsets=(2, 3, 4), with_cpu=True):
         then the pixel sampler at nx x ny samples per pixel with continuations
         from the trained proposal): for each stream offset, k is raised until
         the k x k render's RMSE is at or below the better plain form's; then
-        every near-square grid between (k - 1)^2 and k^2 samples is rendered,
-        and the wall time (training included) of the smallest grid from which
-        on every larger grid reaches that RMSE is the measured time to it.
+        every near-square grid between (k - 1)^2 and k^2 samples is rendered;
+        the smallest grid from which on every larger grid reaches that RMSE is
+        rendered once more, and that render's wall time (training included),
+        like the plain render's second run, is the measured time to it.
     oracle_vs_reference: the oracle's 64 x 64 tile means against the reference
     CPU renderer's at 16 spp (z-scores from the noise of two reference renders
     with different seed offsets)."""
@@ -686,6 +687,10 @@ def guided_bench(plain_spp_side=32, offsets=(2, 3, 4), with_cpu=True):
                 i -= 1
             grid, st_g, r_g = tried[i]
             spp = grid[0] * grid[1]
+        # timed as the plain render is: a second render of the same grid (warm buffers)
+        img_g, _, st_g = ctx.guided_render(w, h, samples_per_pixel=spp, strata_x=grid[0], stream_offset=off,
+                                           **GUIDE_STRATIFIED)
+        r_g = rmse(img_g)
         runs.append({"stream_offset": off, "spp": spp, "strata": list(grid), "seconds": round(st_g.seconds, 3),
                      "rmse": r_g, "reached": bool(r_g <= target), "train_passes": int(st_g.passes),
                      "train_seconds": round(st_g.train_seconds, 3)})
