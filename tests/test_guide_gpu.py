@@ -69,8 +69,8 @@ def features(rows):
     hi = torch.tensor(BOX[3:], dtype=torch.float64)
     p = (r[:, 0:3] - lo) / (hi - lo)
     cols = []
-    for k in range(16):
-        s = float(np.exp2(np.float32(k) * np.float32(1.0 / 3.0)))
+    for k in range(16):  # f_k = (2^((k mod 3)/3) in float32) 2^(k div 3)
+        s = float(np.float32(np.exp2(np.float64(k % 3) / 3.0))) * 2.0 ** (k // 3)
         for c in range(3):
             x = p[:, c].float().double() * s
             cols += [torch.sin(math.pi * x), torch.cos(math.pi * x)]

@@ -3,7 +3,8 @@
 // tensor memory), with hand-written inference and training kernels.
 //
 // Network: 128 inputs (16-frequency sin/cos encoding of the normalised
-// position, frequencies pi 2^(k/3), k = 0..15: 96; shading normal 3,
+// position, frequencies pi f_k, f_k = (2^((k mod 3)/3) in float32) 2^(k div 3),
+// k = 0..15: 96; shading normal 3,
 // outgoing direction 3, zeros, input 127 = constant 1) -> 3 hidden layers of 64 ReLU units (unit 63 of each is the
 // constant 1, so every bias is an ordinary weight column) -> 64 outputs, of
 // which 40 parameterise a mixture of 8 von Mises-Fisher lobes in world space:
@@ -90,26 +91,38 @@ __device__ __forceinline__ uint32_t pack_bf16(float a, float b) {
     return *reinterpret_cast<const uint32_t*>(&h);
 }
 
-// Encoding frequencies 2^(k/3), k = 0..15 (1 to 32 half-periods across the
-// scene box), as float32 values of exp2(k * (1/3)).
-__constant__ float kFreq[16] = {1.000000000e+00f, 1.259921074e+00f, 1.587401032e+00f, 2.000000000e+00f,
-                                2.519842148e+00f, 3.174802303e+00f, 4.000000000e+00f, 5.039684772e+00f,
-                                6.349604607e+00f, 8.000000000e+00f, 1.007936954e+01f, 1.269920921e+01f,
-                                1.600000000e+01f, 2.015873909e+01f, 2.539842224e+01f, 3.200000000e+01f};
+// Encoding frequencies f_k = f_(k mod 3) 2^(k div 3), k = 0..15 (1 to 32
+// half-periods across the scene box), from the float32 values of 2^(b/3),
+// b = 0, 1, 2: three chains of doublings.
+__constant__ float kFreq[3] = {1.000000000e+00f, 1.259921074e+00f, 1.587401032e+00f};
 
-// Input features j and j + 1 (j even).  j < 96: sin and cos of
-// pi 2^(k/3) p_axis, k = j / 6, axis = (j % 6) / 2 (one sincospif per pair);
-// then the normal, wo, zeros and the constant 1 at 127.
-__device__ __forceinline__ void feature_pair(int j, float3 p, float3 nrm, float3 wo, bool valid, float& f0,
-                                             float& f1) {
-    if (!valid) {
-        f0 = f1 = 0.f;
+// Input features j and j + 1 (j even), visited in increasing j.  j < 96: sin
+// and cos of pi f_k p_axis, k = j / 6, axis = (j % 6) / 2: a sincospif for
+// k < 3, then each chain (axis, k mod 3) doubles its angle (sin 2x =
+// 2 sin x cos x, cos 2x = (cos x - sin x)(cos x + sin x)), which leaves the
+// features within 1e-6 of sincospif's, far below their BF16 rounding.  Then
+// the normal, wo, zeros and the constant 1 at 127.
+struct Encoding {
+    float s[3][3], c[3][3];  // running sin and cos per (axis, chain)
+};
+__device__ __forceinline__ void feature_pair(int j, float3 p, float3 nrm, float3 wo, bool valid, Encoding& e,
+                                             float& f0, float& f1) {
+    if (j < 96) {
+        const int k = j / 6, a = (j % 6) / 2, b = k % 3;
+        if (k < 3) {
+            const float x = (a == 0) ? p.x : (a == 1 ? p.y : p.z);
+            sincospif(x * kFreq[b], &e.s[a][b], &e.c[a][b]);
+        } else {
+            const float sn = e.s[a][b], cs = e.c[a][b];
+            e.s[a][b] = 2.f * sn * cs;
+            e.c[a][b] = (cs - sn) * (cs + sn);
+        }
+        f0 = valid ? e.s[a][b] : 0.f;
+        f1 = valid ? e.c[a][b] : 0.f;
         return;
     }
-    if (j < 96) {
-        const int k = j / 6, m = j % 6;
-        const float c = (m < 2) ? p.x : (m < 4 ? p.y : p.z);
-        sincospif(c * kFreq[k], &f0, &f1);
+    if (!valid) {
+        f0 = f1 = 0.f;
         return;
     }
     auto fixed = [&](int i) -> float {
@@ -281,11 +294,12 @@ __global__ void __launch_bounds__(kRows, 1) mlp_kernel(Mlp_Args a) {
             }
         }
         // ---- input features: X rows (and X^T for the weight gradient of layer 1)
+        Encoding enc;
 #pragma unroll
         for (int c = 0; c < 16; c++) {
             float v[8];
 #pragma unroll
-            for (int i = 0; i < 8; i += 2) feature_pair(8 * c + i, p, nrm, wo, valid, v[i], v[i + 1]);
+            for (int i = 0; i < 8; i += 2) feature_pair(8 * c + i, p, nrm, wo, valid, enc, v[i], v[i + 1]);
             store_row8(R0, tid, 8 * c, kIn, v);
             if (TRAIN) {
 #pragma unroll
