@@ -2,6 +2,7 @@
 
     python -m yar_gb300 render SCENE --out image.exr [--spp N] [--seedoffset K] [--compress] [--resolution WxH]
     python -m yar_gb300 guided SCENE --out image.exr --passes N [--guide-fraction A] [--train-passes T] [--spp N]
+        [--strata-x NX] [--train-steps S] [--learning-rate R] [--guide-bounces B]
     python -m yar_gb300 info SCENE
 
 SCENE is a .yfs flat scene (the reference's pbrt-v3 loader and kd-tree
@@ -53,6 +54,12 @@ def main(argv=None):
             q.add_argument("--time-budget", type=float, default=0.0)
             q.add_argument("--spp", type=int, default=0,
                            help="stratified form: after the training passes, this many samples per pixel")
+            q.add_argument("--strata-x", type=int, default=0,
+                           help="stratified form: columns of the strata grid (default ceil(sqrt(spp)))")
+            q.add_argument("--train-steps", type=int, default=8, help="optimizer steps per training pass")
+            q.add_argument("--learning-rate", type=float, default=2e-3)
+            q.add_argument("--guide-bounces", type=int, default=0,
+                           help="stratified form: guide the first this many vertices of each path (0: all)")
     a = p.parse_args(argv)
     s = load(a.scene)
     if getattr(a, "resolution", None):
@@ -87,9 +94,10 @@ def main(argv=None):
         ctx.upload_scene(s)
         img, _, st = ctx.guided_render(w, h, passes=a.passes, guide_fraction=a.guide_fraction,
                                        train_passes=a.train_passes, time_budget=a.time_budget,
-                                       samples_per_pixel=a.spp)
-        if a.spp:  # nx x ny strata, nx = ceil(sqrt(spp)), ny = ceil(spp / nx)
-            nx = int(math.ceil(math.sqrt(a.spp)))
+                                       samples_per_pixel=a.spp, strata_x=a.strata_x, train_steps=a.train_steps,
+                                       learning_rate=a.learning_rate, guide_bounces=a.guide_bounces)
+        if a.spp:  # nx x ny strata, nx = strata_x or ceil(sqrt(spp)), ny = ceil(spp / nx)
+            nx = a.strata_x or int(math.ceil(math.sqrt(a.spp)))
             spp = nx * ((a.spp + nx - 1) // nx)
         else:
             spp = st.passes
