@@ -134,6 +134,25 @@ def test_render_matches_oracle_other_configs(gpu_ctx, seed_offset, spp_xy, maxb)
     assert stats.variance == ref_var
 
 
+@pytest.mark.parametrize("name,nx,ny,size", [("cornell_ggx_64", 11, 10, 64), ("cornell_delta_64", 26, 20, 16),
+                                              ("cornell_direct_64", 13, 8, 32)])
+def test_many_samples_per_pixel_bit_identical_to_oracle(gpu_ctx, name, nx, ny, size):
+    """Above 96 samples per pixel the sample tables are built one warp per
+    table row (the lanes draw the stratified values with jump-aheads, lane 0
+    replays the shuffle): images and variance bit-identical to the oracle with
+    correctly rounded trigonometry, in both rendering algorithms."""
+    s = FlatScene.read(golden(name + ".yfs"))
+    s.config["x_pixel_sample_count"], s.config["y_pixel_sample_count"] = nx, ny
+    s.config["render_region"] = (0, 0, size, size)
+    s.camera["image_extent"] = (size, size)
+    ref, ref_var = oracle.render(s, threads=8, correctly_rounded_trig=True)
+    gpu_ctx.upload_scene(s)
+    img, stats = gpu_ctx.render(size, size)
+    assert np.array_equal(img.view(np.uint32), ref.view(np.uint32))
+    assert stats.variance == ref_var
+    assert stats.paths == size * size * nx * ny
+
+
 def _past_budget_scene(name):
     s = FlatScene.read(golden(name + ".yfs"))
     return scenes.make_ceiling_refractor(s) if name == "cornell_delta_64" else s
