@@ -137,10 +137,10 @@ def test_render_matches_oracle_other_configs(gpu_ctx, seed_offset, spp_xy, maxb)
 @pytest.mark.parametrize("name,nx,ny,size", [("cornell_ggx_64", 11, 10, 64), ("cornell_delta_64", 26, 20, 16),
                                               ("cornell_direct_64", 13, 8, 32)])
 def test_many_samples_per_pixel_bit_identical_to_oracle(gpu_ctx, name, nx, ny, size):
-    """Above 96 samples per pixel the sample tables are built one warp per
-    table row (the lanes draw the stratified values with jump-aheads, lane 0
-    replays the shuffle): images and variance bit-identical to the oracle with
-    correctly rounded trigonometry, in both rendering algorithms."""
+    """Above 96 samples per pixel the sample-table kernel runs smaller blocks
+    (each thread shuffles its row's spp values in shared memory), and 26 x 20
+    strata are not square: images and variance bit-identical to the oracle
+    with correctly rounded trigonometry, in both rendering algorithms."""
     s = FlatScene.read(golden(name + ".yfs"))
     s.config["x_pixel_sample_count"], s.config["y_pixel_sample_count"] = nx, ny
     s.config["render_region"] = (0, 0, size, size)

@@ -341,12 +341,6 @@ __device__ __forceinline__ void pcg_advance(Pcg& r, uint32_t n) {
     pcg_jump(n, acc_mult, acc_plus);
     r.state = acc_mult * r.state + acc_plus * r.inc;
 }
-// pcg32's output of a state (the draw pcg_next returns from it)
-__device__ __forceinline__ uint32_t pcg_output(uint64_t old) {
-    const uint32_t xs = (uint32_t)(((old >> 18u) ^ old) >> 27u);
-    const uint32_t rot = (uint32_t)(old >> 59u);
-    return (xs >> rot) | (xs << ((-rot) & 31));
-}
 
 // SplitMix64's output function (Steele, Lea, Flood, "Fast splittable
 // pseudorandom number generators", 2014): a bijective 64-bit mix.
@@ -451,87 +445,6 @@ __global__ void sample_tables_kernel(Render_Params p, uint32_t chunk_first, uint
         }
     } else {
         for (int k = 0; k < spp; k++) out[k] = sm[k * stride];
-    }
-}
-
-// sample_tables_kernel for many samples per pixel: one warp per (table row,
-// pixel), so a row's spp values need one warp's shared memory instead of each
-// thread's (the per-thread kernel runs fewer than 128 threads per block above
-// 96 samples per pixel).  The lanes draw the stratified values together, each
-// jumping the row's stream 32 draws (64 for 2D rows) per step; lane 0 then
-// replays the shuffle's bounded draws and swaps in order; the lanes write the
-// row out coalesced.  The same draws land in the same places: the tables are
-// the per-thread kernel's bit for bit.
-__global__ void __launch_bounds__(128)
-sample_tables_wide_kernel(Render_Params p, uint32_t chunk_first, uint32_t chunk_pixels, float* __restrict__ s1d,
-                          float* __restrict__ s2d, float2* __restrict__ image_samples) {
-    extern __shared__ float2 gen_smem[];
-    const uint32_t rows = 1u + (uint32_t)p.n1d + (uint32_t)p.n2d;
-    const uint32_t warps = blockDim.x >> 5, lane = threadIdx.x & 31u;
-    const uint64_t item = (uint64_t)blockIdx.x * warps + (threadIdx.x >> 5);
-    if (item >= (uint64_t)chunk_pixels * rows) return;  // uniform per warp
-    const uint32_t lp = (uint32_t)(item % chunk_pixels);
-    const uint32_t row = (uint32_t)(item / chunk_pixels);
-    const int spp = p.spp;
-    float2* vals = gen_smem + (size_t)(threadIdx.x >> 5) * (uint32_t)spp;
-    int x, y;
-    const Pcg rng0 = pixel_pcg(p, pixel_stream(p, chunk_first + lp, x, y));
-    const uint32_t n1d = (uint32_t)p.n1d;
-    const float dx = 1.f / (float)p.nx, dy = 1.f / (float)p.ny;
-    const bool one_d = row >= 1u && row <= n1d;
-    uint32_t off;
-    if (row == 0)
-        off = 0u;
-    else if (one_d)
-        off = (uint32_t)(2 * spp) + (p.arrays_2d_first ? (uint32_t)p.n2d * (uint32_t)(3 * spp - 1) : 0u) +
-              (row - 1u) * (uint32_t)(2 * spp - 1);
-    else
-        off = (uint32_t)(2 * spp) + (p.arrays_2d_first ? 0u : n1d * (uint32_t)(2 * spp - 1)) +
-              (row - 1u - n1d) * (uint32_t)(3 * spp - 1);
-    // the values: draw k (1D) or draws 2k, 2k + 1 (2D) of the row
-    const uint32_t per = one_d ? 1u : 2u;
-    uint64_t jm, jp;
-    pcg_jump(32u * per, jm, jp);
-    const uint64_t inc = rng0.inc;
-    Pcg r = rng0;
-    pcg_advance(r, off + per * lane);
-    uint64_t st = r.state;
-    float2* img = image_samples + ((size_t)chunk_first + lp) * (uint32_t)spp;
-    for (uint32_t k = lane; k < (uint32_t)spp; k += 32u) {
-        const float a = __uint_as_float((pcg_output(st) >> 9) | 0x3f800000u) - 1.0f;
-        if (one_d) {
-            vals[k].x = one_minus_eps_min(((float)k + a) * (1.f / (float)spp));
-        } else {
-            const uint64_t st1 = st * 6364136223846793005ULL + inc;
-            const float b = __uint_as_float((pcg_output(st1) >> 9) | 0x3f800000u) - 1.0f;
-            const uint32_t i = k % (uint32_t)p.nx, j = k / (uint32_t)p.nx;
-            const float2 v = make_float2(one_minus_eps_min(((float)i + a) * dx), one_minus_eps_min(((float)j + b) * dy));
-            if (row == 0)
-                img[k] = v;  // image samples: stratified, not shuffled
-            else
-                vals[k] = v;
-        }
-        st = jm * st + jp * inc;
-    }
-    if (row == 0) return;
-    __syncwarp();
-    if (lane == 0) {  // the shuffle, src/lib/math.h:138-145: its draws follow the values'
-        Pcg q = rng0;
-        pcg_advance(q, off + per * (uint32_t)spp);
-        for (int m = spp; m > 1; m--) {
-            const uint32_t rr = pcg_bounded_fast(q, (uint32_t)m);
-            const float2 t = vals[m - 1];
-            vals[m - 1] = vals[rr];
-            vals[rr] = t;
-        }
-    }
-    __syncwarp();
-    if (one_d) {
-        float* out = s1d + ((size_t)lp * n1d + (row - 1u)) * (uint32_t)spp;
-        for (uint32_t k = lane; k < (uint32_t)spp; k += 32u) out[k] = vals[k].x;
-    } else {
-        float2* out = reinterpret_cast<float2*>(s2d) + ((size_t)lp * (uint32_t)p.n2d + (row - 1u - n1d)) * (uint32_t)spp;
-        for (uint32_t k = lane; k < (uint32_t)spp; k += 32u) out[k] = vals[k];
     }
 }
 
@@ -2375,7 +2288,7 @@ constexpr size_t kTablesSmemLimit = 96 * 1024;
 // One-time kernel attribute (also called before a stream capture, so that
 // no attribute change happens inside one).
 cudaError_t generate_prepare() {
-    // the dynamic shared-memory limit of both table kernels, once per device
+    // the table kernel's dynamic shared-memory limit, once per device
     static bool attr_set[64] = {};
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
@@ -2384,9 +2297,6 @@ cudaError_t generate_prepare() {
     if (!attr_set[dev]) {
         e = cudaFuncSetAttribute(sample_tables_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                  (int)kTablesSmemLimit);
-        if (e == cudaSuccess)
-            e = cudaFuncSetAttribute(sample_tables_wide_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                                     (int)kTablesSmemLimit);
         if (e != cudaSuccess) return e;
         attr_set[dev] = true;
     }
@@ -2398,18 +2308,18 @@ cudaError_t launch_generate(const Render_Params& p, uint32_t first, uint32_t cp,
     constexpr size_t kSmemLimit = kTablesSmemLimit;
     cudaError_t pe = generate_prepare();
     if (pe != cudaSuccess) return pe;
-    const size_t per_row = (size_t)p.spp * sizeof(float2);
-    if (per_row > kSmemLimit) return cudaErrorInvalidValue;
+    // One thread per table row, its spp values shuffled in shared memory: above
+    // 96 samples per pixel fewer threads fit a block.  (One warp per row, the
+    // lanes drawing the values and lane 0 replaying the shuffle, measured
+    // slower at 256-1024 samples per pixel: the shuffle's serial chain then
+    // runs on one lane per warp instead of in lockstep across the threads.)
+    const size_t per_thread = (size_t)p.spp * sizeof(float2);
+    int threads = 128;
+    while (threads > 1 && (size_t)threads * per_thread > kSmemLimit) threads /= 2;
+    if ((size_t)threads * per_thread > kSmemLimit) return cudaErrorInvalidValue;
     const uint64_t rows = (uint64_t)cp * (1u + (uint32_t)p.n1d + (uint32_t)p.n2d);
-    if (128 * per_row <= kSmemLimit) {  // up to 96 samples per pixel: one thread per row
-        sample_tables_kernel<<<(uint32_t)((rows + 127) / 128), 128, 128 * per_row, st>>>(p, first, cp, s1d, s2d,
-                                                                                         image_samples);
-    } else {  // one warp per row, up to 4 warps per block
-        uint32_t warps = 4;
-        while (warps > 1 && warps * per_row > kSmemLimit) warps /= 2;
-        sample_tables_wide_kernel<<<(uint32_t)((rows + warps - 1) / warps), 32 * warps, warps * per_row, st>>>(
-            p, first, cp, s1d, s2d, image_samples);
-    }
+    sample_tables_kernel<<<(uint32_t)((rows + threads - 1) / threads), threads, threads * per_thread, st>>>(
+        p, first, cp, s1d, s2d, image_samples);
     const uint32_t paths = cp * (uint32_t)p.spp;
     camera_kernel<<<(paths + kBlock - 1) / kBlock, kBlock, 0, st>>>(p, first, paths, image_samples, ps, q);
     return cudaGetLastError();
