@@ -513,14 +513,14 @@ __global__ void adam_kernel(const float* __restrict__ partials, int parts, float
     params[i] -= lr * (mi * c1) / (sqrtf(vi * c2) + eps);
 }
 
+// The current device's SM count (the partial-gradient slots and the grids),
+// cached per device.
 int sm_count() {
-    static int sms = 0;
-    if (sms == 0) {
-        int dev = 0;
-        cudaGetDevice(&dev);
-        cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
-    }
-    return sms;
+    static int sms[64] = {};
+    int dev = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) return 0;
+    if (sms[dev] == 0) cudaDeviceGetAttribute(&sms[dev], cudaDevAttrMultiProcessorCount, dev);
+    return sms[dev];
 }
 
 } // namespace
@@ -530,6 +530,8 @@ int guide_ensure(yar_gpu_ctx* ctx) {
     if (g.params.ptr) return YAR_OK;
     int rc = YAR_OK;
     const size_t pb = kGuideParams * sizeof(float);
+    cudaSetDevice(ctx->device);
+    if (sm_count() <= 0) return fail(ctx, YAR_ERR_INVALID, "guide: no SM count for the device");
     if ((rc = device_alloc(ctx, g.params, pb)) != YAR_OK) return rc;
     if ((rc = device_alloc(ctx, g.adam_m, pb)) != YAR_OK) return rc;
     if ((rc = device_alloc(ctx, g.adam_v, pb)) != YAR_OK) return rc;
@@ -538,14 +540,15 @@ int guide_ensure(yar_gpu_ctx* ctx) {
     if ((rc = device_alloc(ctx, g.scalars, 64)) != YAR_OK) return rc;
     cudaError_t e = cudaMemsetAsync(g.images.ptr, 0, kImgBytes, ctx->stream);
     if (e != cudaSuccess) return cuda_fail(ctx, e, "guide init");
-    static bool attr = false;
-    if (!attr) {
+    static bool attr[64] = {};  // per device
+    if (ctx->device < 0 || ctx->device >= 64) return fail(ctx, YAR_ERR_INVALID, "guide: device index");
+    if (!attr[ctx->device]) {
         e = cudaFuncSetAttribute(mlp_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kTrMisc + 64);
         if (e == cudaSuccess)
             e = cudaFuncSetAttribute(mlp_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                      (int)kInMisc + 64);
         if (e != cudaSuccess) return cuda_fail(ctx, e, "guide kernel attributes");
-        attr = true;
+        attr[ctx->device] = true;
     }
     return guide_reset(ctx, 1);
 }
