@@ -51,6 +51,25 @@ def test_guided_is_unbiased_and_trains(gpu_ctx, small_room):
         assert abs(guided[sl].mean() - plain[sl].mean()) < 2 * MEAN_REL_TOL * plain[sl].mean()
 
 
+@pytest.mark.parametrize("name", ["cornell_texture_64", "cornell_spectex_64", "cornell_bump_64"])
+def test_guided_renders_of_textured_scenes_are_unbiased(gpu_ctx, name):
+    """Image textures, bump maps and textures behind delta bounces in the
+    guided render: the stratified form and the one-sample passes, guided,
+    have the plain render's image mean."""
+    s = FlatScene.read(golden(name + ".yfs"))
+    s.config["x_pixel_sample_count"] = s.config["y_pixel_sample_count"] = 16
+    gpu_ctx.upload_scene(s)
+    plain, _ = gpu_ctx.render(64, 64)
+    strat, _, st = gpu_ctx.guided_render(64, 64, samples_per_pixel=256, guide_fraction=0.5, train_passes=8,
+                                         train_steps=16, learning_rate=5e-3, stream_offset=6)
+    assert st.train_samples > 0
+    passes, _, _ = gpu_ctx.guided_render(64, 64, passes=256, guide_fraction=0.5, train_passes=8, train_steps=16,
+                                         learning_rate=5e-3, stream_offset=7)
+    for img in (strat, passes):
+        assert np.isfinite(img).all()
+        assert abs(img.mean() - plain.mean()) < MEAN_REL_TOL * plain.mean(), (name, img.mean(), plain.mean())
+
+
 def test_time_budget_stops_early(gpu_ctx, small_room):
     gpu_ctx.upload_scene(small_room)
     _, _, st = gpu_ctx.guided_render(64, 64, passes=100000, time_budget=0.5)

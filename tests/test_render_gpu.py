@@ -452,14 +452,10 @@ def test_fourier_tables_checked_on_upload(gpu_ctx):
             gpu_ctx.render(64, 64)
 
 
-def test_bump_maps_refused_where_they_are_not_evaluated(gpu_ctx):
-    """The guided render refuses bump maps; a mix's sub-material may not have
-    one; a texture in a slot the material does not read is refused."""
+def test_bump_maps_and_textures_refused_where_the_material_does_not_read_them(gpu_ctx):
+    """A mix's sub-material may not have a bump map; a texture in a slot the
+    material does not read is refused."""
     from yar_gb300 import native
-    s = constant_bumps_with_delta_materials()
-    gpu_ctx.upload_scene(s)
-    with pytest.raises(native.YarError):
-        gpu_ctx.guided_render(64, 64, passes=1)
     t = FlatScene.read(golden("cornell_texture_64.yfs"))
     k = int(np.nonzero(t.materials["reflectance_texture"])[0][0])
     t.materials["transmittance_texture"][k] = t.materials["reflectance_texture"][k]  # diffuse has no such slot
@@ -472,17 +468,6 @@ def test_bump_maps_refused_where_they_are_not_evaluated(gpu_ctx):
     gpu_ctx.upload_scene(x)
     with pytest.raises(native.YarError):
         gpu_ctx.render(64, 64)
-
-
-def test_textured_scene_refused_where_textures_are_not_evaluated(gpu_ctx):
-    """The guided render refuses image textures instead of rendering them as
-    constants."""
-    from yar_gb300 import native
-    s = FlatScene.read(golden("cornell_spectex_64.yfs"))
-    gpu_ctx.upload_scene(s)
-    with pytest.raises(native.YarError) as e:
-        gpu_ctx.guided_render(64, 64, passes=1)
-    assert e.value.code == native.YAR_ERR_UNSUPPORTED
 
 
 def test_direct_lighting_with_constant_bumps_on_delta_materials(gpu_ctx):

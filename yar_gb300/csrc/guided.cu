@@ -163,7 +163,6 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
         return fail(ctx, YAR_ERR_UNSUPPORTED, "the guided render runs the path tracer only (rendering_algorithm 1)");
     Render_Params p;
     if (int rc0 = prepare_render_params(ctx, p)) return rc0;
-    if (p.textured) return fail(ctx, YAR_ERR_UNSUPPORTED, "the guided render does not evaluate image textures or bump maps");
     if (!spp_side && (p.filter_radius > 0.5f || p.filter_type != 0))
         return fail(ctx, YAR_ERR_UNSUPPORTED, "guided passes: box filter of radius <= 0.5 only (one pixel per sample)");
     p.nx = p.ny = p.spp = 1;
@@ -225,12 +224,16 @@ int guided_render(yar_gpu_ctx* ctx, const yar_guided_params* gp, double* sum_out
         alloc(34, (size_t)rec_cap * 4 * sizeof(float4));   // training samples
         alloc(35, 4 * sizeof(float));                      // weight scale
     }
+    if (p.spec_diffs) alloc(36, cap * 3 * sizeof(float4));  // delta rays' specular differential rays
     if (rc != YAR_OK) return rc;
 
     Path_State ps{dp<float4>(B[4]), dp<float4>(B[5]), dp<uint32_t>(B[6]), dp<uint4>(B[7]),
                   dp<float4>(B[8]), dp<float4>(B[9]), dp<float4>(B[10]), dp<float4>(B[11]),
                   dp<float4>(B[12]), dp<uint8_t>(B[13]), dp<float4>(B[14]), dp<uint2>(B[15]),
                   guided ? dp<uint32_t>(B[32]) : nullptr};
+    ps.image_samples = dp<float2>(B[1]);  // textured hits' camera differentials (one chunk per pass)
+    ps.chunk_first = 0;
+    ps.diff = dp<float4>(B[36]);
     Queues q{};
     q.ext_rays[0] = dp<float4>(B[16]);
     q.ext_rays[1] = dp<float4>(B[17]);

@@ -1437,7 +1437,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                 // src/ref/delta_scattering.cpp:252-257; create_bsdf again, which
                 // gives the same frame).
                 Tex_Site site;
-                const bool textured = FULL && !GUIDED && (mat.texture | mat.texture2 | mat.bump) != 0u;
+                const bool textured = FULL && (mat.texture | mat.texture2 | mat.bump) != 0u;
                 if (textured) {
                     texture_site(p, S, ps, slot, bounce, info, sc, h4, h2, site);
                     if (mat.bump) apply_bump(S, mat, site, h2.y, h2.x, h4.y, h4.z, h4.w, sc);
@@ -1722,7 +1722,7 @@ shade_kernel(Render_Params p, Scene_Dev S, int cur, uint32_t count, const float*
                     // Reflected and transmitted delta rays carry differential rays for
                     // the first max_differential_ray_specular_bounces bounces.
                     uint32_t diff_flag = 0u;
-                    if (FULL && !GUIDED && p.spec_diffs && delta == 1 && delta_kind >= 0.f &&
+                    if (FULL && p.spec_diffs && delta == 1 && delta_kind >= 0.f &&
                         bounce < kMaxDifferentialRaySpecularBounces &&
                         specular_differentials(p, S, ps, slot, bounce, info, sc, h4, h2, delta_wi, delta_kind))
                         diff_flag = kDiffRays;
