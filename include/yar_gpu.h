@@ -142,9 +142,9 @@ typedef struct yar_object_desc {
  * with pbrt3_scene set is shaded as pbrt-v3's plastic, as the reference does.
  * Image textures on the reflectance and transmittance slots and bump maps are
  * evaluated by yar_gpu_render (both rendering algorithms),
- * yar_gpu_render_checkpoint and yar_gpu_render_batch, behind delta bounces
- * too; the guided and static renders, and textures on any other parameter,
- * return YAR_ERR_UNSUPPORTED. */
+ * yar_gpu_render_checkpoint, yar_gpu_render_batch and yar_gpu_guided_render,
+ * behind delta bounces too; the static render, and textures on any other
+ * parameter, return YAR_ERR_UNSUPPORTED. */
 typedef struct yar_material_desc {
     uint32_t type;              /* YAR_MATERIAL_PERFECT_REFLECTOR / PERFECT_REFRACTOR / DIFFUSE / METAL /
                                    PLASTIC / COATED_DIFFUSE / GLASS */
