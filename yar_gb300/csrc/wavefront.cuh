@@ -1325,7 +1325,9 @@ __device__ __forceinline__ V3 sphere_sampler_sample(const Sphere_Sampler& ss, fl
 // written only where emission adds to it; its guided form spills 18 B.  The
 // FULL instantiations keep 3 blocks (160-162 registers, no spills; at 4 the
 // out-of-line BSDF routines, the fourier series among them, push the kernel
-// to 36-60 B of spills).  Before those changes the plain kernel ran at 5
+// to 36-60 B of spills).  The guided plain-material form at 3 blocks (152
+// registers, no spills) rendered the guided room no faster than at 4 (38 B
+// of spills).  Before those changes the plain kernel ran at 5
 // blocks (96 registers, 202 B of spill stores), which measured 1.726 s on the
 // C3 render against 1.732 s at 4 blocks and 1.764 s at 3.
 template <bool GUIDED, bool FULL>
